@@ -1,0 +1,197 @@
+"""Seeded synthetic scenes for the MPM transfer path.
+
+A scene holds exactly what the reference reads from its input decks for one
+rank: the grid header of ``InputParaGriddata`` (module/data_io.cpp:31-125),
+the particle table of ``SolidMaterialPointBase::InputPointData``
+(module/solid/solid_data_io.cpp:13-36: coord, matid, mass, vol0, F = I,
+vol = vol0), the material table of ``datain_para``
+(work/src_solid/explicit/datain_para.cpp:63-82: iprop, E, nu) and the
+``BoundaryCondition`` node lists (module/bc.h:7-21).
+
+Particles are seeded at the ``GaussianDistribution`` offsets
+(module/mesh.cpp:12-54) inside each cell of a block, plus a seeded uniform
+jitter, as ``MaterialPoint::BuildGaussianPoint`` (module/material_point.cpp:16)
+places them.  Every generator takes a seed; ``seed = 12345 + config_id`` by
+default.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+PIC, FLIP = 0, 1
+BC_U, BC_V, BC_W = 0, 1, 2
+
+
+@dataclass
+class Scene:
+    xyelem: tuple            # cells per direction
+    xymin: tuple             # grid origin
+    dxy: tuple               # cell size per direction
+    idimc: tuple             # shape-function order per direction (1 linear, 2 quadratic B-spline)
+    npxye: tuple             # particles per cell per direction used by MakNodalVol
+    dt: float
+    mtol: float
+    gravity: tuple
+    iprop: np.ndarray        # (nmat,) int32: -1 rigid, 0 linear elastic, 1 Neo-Hookean
+    mat_prop: np.ndarray     # (nmat, 3) float64: E, nu, spare
+    coord: np.ndarray        # (n, 3) float64
+    vel: np.ndarray          # (n, 3) float64
+    mass: np.ndarray         # (n,) float64
+    vol0: np.ndarray         # (n,) float64
+    matid: np.ndarray        # (n,) int32
+    scheme: int = PIC
+    bcs: list = field(default_factory=list)   # [(comp, nodes int32, values float64)]
+    name: str = "scene"
+
+    @property
+    def num(self) -> int:
+        return int(self.mass.shape[0])
+
+    @property
+    def xynodec(self) -> tuple:
+        return tuple(int(self.xyelem[i] + self.idimc[i]) for i in range(3))
+
+    @property
+    def nodec(self) -> int:
+        nx, ny, nz = self.xynodec
+        return nx * ny * nz
+
+    def node_id(self, i, j, k):
+        nx, ny, _ = self.xynodec
+        return i + nx * j + nx * ny * k
+
+
+def gaussian_offsets(npc: int, d: float) -> np.ndarray:
+    """Particle offsets from the cell centre, module/mesh.cpp:16-51."""
+    table = {
+        1: [0.0],
+        2: [-0.25, 0.25],
+        3: [-1.0 / 3.0, 0.0, 1.0 / 3.0],
+        4: [-0.375, -0.125, 0.125, 0.375],
+        5: [-0.4, -0.2, 0.0, 0.2, 0.4],
+        6: [-5.0 / 12.0, -3.0 / 12.0, -1.0 / 12.0, 1.0 / 12.0, 3.0 / 12.0, 5.0 / 12.0],
+    }
+    return np.asarray(table[npc], dtype=np.float64) * d
+
+
+def block_particles(cell_lo, cell_hi, xymin, dxy, npc, jitter, rng):
+    """Particles of a block of cells [cell_lo, cell_hi) at npc^3 per cell."""
+    offs = [gaussian_offsets(npc[i], dxy[i]) for i in range(3)]
+    ci = [np.arange(cell_lo[i], cell_hi[i]) for i in range(3)]
+    # cell-major ordering like BuildGaussianPoint: cell loop outside, z/y/x offsets inside
+    kz, jy, ix = np.meshgrid(ci[2], ci[1], ci[0], indexing="ij")
+    centres = np.stack([xymin[d] + dxy[d] * ((ix, jy, kz)[d].ravel() + 0.5) for d in range(3)], axis=1)
+    oz, oy, ox = np.meshgrid(offs[2], offs[1], offs[0], indexing="ij")
+    local = np.stack([ox.ravel(), oy.ravel(), oz.ravel()], axis=1)
+    pts = (centres[:, None, :] + local[None, :, :]).reshape(-1, 3)
+    if jitter > 0.0:
+        pts = pts + rng.uniform(-jitter, jitter, size=pts.shape) * np.asarray(dxy)[None, :]
+    return pts
+
+
+def face_nodes(xynodec, axis, index):
+    nx, ny, nz = xynodec
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    ijk = (i, j, k)
+    mask = ijk[axis] == index
+    return (i[mask] + nx * j[mask] + nx * ny * k[mask]).astype(np.int32)
+
+
+def elastic_block(grid=(32, 32, 32), dx=1.0e-2, cell_lo=(6, 6, 0), cell_hi=(26, 26, 20), npc=2,
+                  jitter=0.1, E=1.0e6, nu=0.3, rho=1000.0, dt=1.0e-5, gravity=(0.0, 0.0, -9.81),
+                  fix_bottom=True, scheme=PIC, idimc=(1, 1, 1), iprop=0, seed=12346, mtol=1.0e-12,
+                  name="elastic_block"):
+    """Linear-elastic block under gravity with a fixed bottom face.
+
+    The defaults are the 64,000-particle FP64 CPU case: 32^3 cells,
+    dx = 1e-2 m, a 20^3-cell block at 2x2x2 particles per cell, +-0.1 dx jitter,
+    E = 1e6 Pa, nu = 0.3, rho = 1000 kg/m^3, dt = 1e-5 s, fixed bottom face.
+    """
+    rng = np.random.default_rng(seed)
+    xymin = (0.0, 0.0, 0.0)
+    dxy = (dx, dx, dx)
+    pts = block_particles(cell_lo, cell_hi, xymin, dxy, (npc, npc, npc), jitter, rng)
+    n = pts.shape[0]
+    vp = dx ** 3 / npc ** 3
+    scene = Scene(
+        xyelem=tuple(grid), xymin=xymin, dxy=dxy, idimc=tuple(idimc), npxye=(npc, npc, npc),
+        dt=dt, mtol=mtol, gravity=tuple(gravity),
+        iprop=np.array([iprop], dtype=np.int32), mat_prop=np.array([[E, nu, 0.0]]),
+        coord=pts, vel=np.zeros((n, 3)), mass=np.full(n, rho * vp), vol0=np.full(n, vp),
+        matid=np.zeros(n, dtype=np.int32), scheme=scheme, name=name)
+    if fix_bottom:
+        nodes = face_nodes(scene.xynodec, 2, 0)
+        for comp in (BC_U, BC_V, BC_W):
+            scene.bcs.append((comp, nodes, np.zeros(nodes.shape[0])))
+    return scene
+
+
+def spinning_block(grid=(128, 128, 128), dx=4.0e-3, cell_lo=(24, 24, 24), cells=(80, 80, 80), npc=2,
+                   compress_quarter=True, jitter=0.1, E=1.0e6, nu=0.3, rho=1000.0, dt=2.0e-6,
+                   gravity=(0.0, 0.0, -9.81), vel_sigma=0.5, omega=10.0, scheme=PIC, seed=12347,
+                   mtol=1.0e-12, name="spinning_block"):
+    """The 4,096,000-particle FP32 explicit case (defaults).
+
+    80^3 cells at 2x2x2 particles per cell on a 128^3 grid, dx = 4e-3 m.
+    Velocities are N(0, vel_sigma^2) per component plus a rigid rotation
+    omega about z through the block centre.  With ``compress_quarter`` the
+    top quarter of the block (its upper cells[2]/4 layers) is squeezed along
+    z by 8/27 into a slab at 27 particles per cell with vol0 = dx^3/27 and
+    mass = rho * vol0, so that the P2G scatter sees 3.4x the particle density
+    there; the particle count is unchanged.
+    """
+    rng = np.random.default_rng(seed)
+    xymin = (0.0, 0.0, 0.0)
+    dxy = (dx, dx, dx)
+    cell_hi = tuple(cell_lo[i] + cells[i] for i in range(3))
+    pts = block_particles(cell_lo, cell_hi, xymin, dxy, (npc, npc, npc), jitter, rng)
+    n = pts.shape[0]
+    vp = np.full(n, dx ** 3 / npc ** 3)
+    if compress_quarter:
+        z_lo = xymin[2] + dx * cell_lo[2]
+        z0 = z_lo + dx * (cells[2] - cells[2] // 4)
+        top = pts[:, 2] >= z0
+        factor = float(npc ** 3) / 27.0
+        pts[top, 2] = z0 + (pts[top, 2] - z0) * factor
+        vp[top] = dx ** 3 / 27.0
+    centre = np.array([xymin[d] + dx * (cell_lo[d] + 0.5 * cells[d]) for d in range(3)])
+    vel = rng.normal(0.0, vel_sigma, size=(n, 3))
+    rel = pts - centre[None, :]
+    vel[:, 0] += -omega * rel[:, 1]
+    vel[:, 1] += omega * rel[:, 0]
+    return Scene(
+        xyelem=tuple(grid), xymin=xymin, dxy=dxy, idimc=(1, 1, 1), npxye=(npc, npc, npc),
+        dt=dt, mtol=mtol, gravity=tuple(gravity),
+        iprop=np.array([0], dtype=np.int32), mat_prop=np.array([[E, nu, 0.0]]),
+        coord=pts, vel=vel, mass=rho * vp, vol0=vp.copy(),
+        matid=np.zeros(n, dtype=np.int32), scheme=scheme, name=name)
+
+
+def cantilever(grid=(64, 64, 64), dx=1.0e-2, cell_lo=(0, 2, 2), cells=(60, 60, 60), npc=2, jitter=0.0,
+               E=1.0e7, nu=0.3, rho=1000.0, dt=1.0e-3, gravity=(0.0, 0.0, -9.81), iprop=0,
+               scheme=PIC, seed=12348, mtol=1.0e-12, name="cantilever"):
+    """Implicit-solid cantilever: cells[0] x cells[1] x cells[2] block clamped at x = 0.
+
+    Defaults: 64^3 grid, 60^3 cells at 2x2x2 particles per cell = 1,728,000
+    particles, E = 1e7 Pa, nu = 0.3, dt = 1e-3 s.  All three displacement
+    components are fixed on the nodes of the x = 0 face.
+    """
+    rng = np.random.default_rng(seed)
+    xymin = (0.0, 0.0, 0.0)
+    dxy = (dx, dx, dx)
+    cell_hi = tuple(cell_lo[i] + cells[i] for i in range(3))
+    pts = block_particles(cell_lo, cell_hi, xymin, dxy, (npc, npc, npc), jitter, rng)
+    n = pts.shape[0]
+    vp = dx ** 3 / npc ** 3
+    scene = Scene(
+        xyelem=tuple(grid), xymin=xymin, dxy=dxy, idimc=(1, 1, 1), npxye=(npc, npc, npc),
+        dt=dt, mtol=mtol, gravity=tuple(gravity),
+        iprop=np.array([iprop], dtype=np.int32), mat_prop=np.array([[E, nu, 0.0]]),
+        coord=pts, vel=np.zeros((n, 3)), mass=np.full(n, rho * vp), vol0=np.full(n, vp),
+        matid=np.zeros(n, dtype=np.int32), scheme=scheme, name=name)
+    nodes = face_nodes(scene.xynodec, 0, cell_lo[0])
+    for comp in (BC_U, BC_V, BC_W):
+        scene.bcs.append((comp, nodes, np.zeros(nodes.shape[0])))
+    return scene

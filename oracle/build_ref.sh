@@ -1,0 +1,35 @@
+#!/usr/bin/env bash
+# ORACLE build recipe (test infrastructure).  Compiles the reference's own,
+# unmodified C++ translation units for the solid transfer path plus
+# oracle/ref_harness.cpp into oracle/_ref/libmpmref.so, against the
+# single-rank stubs in oracle/ref_stubs/.  Reads the reference sources where
+# they lie; copies nothing.  Exits 0 without building when the reference
+# checkout is absent (it is only present in the development container).
+set -euo pipefail
+HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${MPM_REFERENCE_DIR:-/root/reference}"
+OUT="$HERE/_ref"
+if [ ! -d "$REF/module" ]; then
+    echo "build_ref: reference checkout not found at $REF; skipping oracle/_ref" >&2
+    exit 0
+fi
+mkdir -p "$OUT/obj"
+TUS="shape_function mesh material_point map_and_interpolate nonlinear_time_integration bc data_io mpi_data
+     solid/constitutive_model solid/solid_material_point solid/solid_data_io
+     solid/implicit/var_trans_solid_implicit solid/implicit/solve_solid_implicit
+     solver/crsmat solver/solver"
+CXX="${CXX:-g++}"
+FLAGS="-std=c++17 -O3 -fPIC -w -I$HERE/ref_stubs -I$REF/module"
+pids=()
+objs=()
+for tu in $TUS; do
+    o="$OUT/obj/$(echo "$tu" | tr / _).o"
+    objs+=("$o")
+    $CXX $FLAGS -c "$REF/module/$tu.cpp" -o "$o" &
+    pids+=($!)
+done
+$CXX $FLAGS -c "$HERE/ref_harness.cpp" -o "$OUT/obj/ref_harness.o" &
+pids+=($!)
+for p in "${pids[@]}"; do wait "$p"; done
+$CXX -shared -o "$OUT/libmpmref.so" "${objs[@]}" "$OUT/obj/ref_harness.o"
+echo "build_ref: wrote $OUT/libmpmref.so"

@@ -1,0 +1,112 @@
+"""ORACLE (test infrastructure only): ctypes driver for oracle/_ref/libmpmref.so.
+
+libmpmref.so is the reference's own compiled C++ (module/*.cpp of
+HPC-MPM-Code) plus oracle/ref_harness.cpp, built by oracle/build_ref.sh in
+the development container only (the reference checkout is not present
+anywhere else).  It is used to generate the committed golden fixtures
+(tests/golden/make_golden.py) and, where present, as the CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_ref", "libmpmref.so")
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def available() -> bool:
+    return os.path.exists(LIB_PATH)
+
+
+def _lib():
+    lib = C.CDLL(LIB_PATH)
+    lib.ref_setup.argtypes = [_ip, _dp, _dp, _ip, _ip, C.c_double, C.c_double, _dp, C.c_int, _ip, _dp]
+    lib.ref_explicit_init.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _ip, C.c_int, C.c_int]
+    lib.ref_set_bc.argtypes = [C.c_int, C.c_int, _ip, _dp]
+    lib.ref_explicit_steps.argtypes = [C.c_int, C.c_double]
+    lib.ref_explicit_p2g.argtypes = [C.c_double]
+    lib.ref_get_nodal.argtypes = [C.c_int, _dp]
+    lib.ref_get_particles.argtypes = [_dp, _dp, _dp, _dp, _dp]
+    lib.ref_implicit_init.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _ip, C.c_int, C.c_int, C.c_double]
+    lib.ref_implicit_steps.argtypes = [C.c_int, C.c_double]
+    lib.ref_implicit_assemble.argtypes = [C.c_double]
+    lib.ref_implicit_get_matrix.argtypes = [_ip, _ip, _dp, _dp, _dp]
+    lib.ref_implicit_matvec.argtypes = [_dp, _dp]
+    lib.ref_implicit_solve.argtypes = [_dp]
+    return lib
+
+
+NODAL_FIELDS = {"nmass": (0, 1), "nvof": (1, 1), "nmome": (2, 3), "nforce": (3, 3), "nvel": (4, 3),
+                "naccel": (5, 3), "nvol": (6, 1), "ndispl": (7, 3)}
+
+
+class RefSolid:
+    """One reference solid (explicit restated driver or implicit as-is)."""
+
+    def __init__(self, scene, implicit=False, shifting=True, nr_flag=False, spec_rad=1.0):
+        self.lib = _lib()
+        self.scene = s = scene
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        self.nodec = self.lib.ref_setup(i32(s.xyelem), f64(s.xymin), f64(s.dxy), i32(s.idimc), i32(s.npxye),
+                                        s.dt, s.mtol, f64(s.gravity), len(s.iprop), i32(s.iprop),
+                                        f64(s.mat_prop).ravel())
+        args = (s.num, f64(s.coord).ravel(), f64(s.vel).ravel(), f64(s.mass), f64(s.vol0), i32(s.matid), s.scheme)
+        if implicit:
+            self.nmat = self.lib.ref_implicit_init(*args, int(nr_flag), float(spec_rad))
+        else:
+            self.lib.ref_explicit_init(*args, int(shifting))
+        for comp, nodes, vals in s.bcs:
+            self.lib.ref_set_bc(comp, len(nodes), i32(nodes), f64(vals))
+
+    def steps(self, n, facl=1.0):
+        assert self.lib.ref_explicit_steps(n, facl) == 0
+
+    def p2g(self, facl=1.0):
+        assert self.lib.ref_explicit_p2g(facl) == 0
+
+    def implicit_steps(self, n, facl=1.0):
+        assert self.lib.ref_implicit_steps(n, facl) == 0
+
+    def nodal(self, name):
+        fid, ncomp = NODAL_FIELDS[name]
+        out = np.zeros(self.nodec * ncomp)
+        self.lib.ref_get_nodal(fid, out)
+        return out.reshape(ncomp, self.nodec) if ncomp == 3 else out
+
+    def particles(self):
+        n = self.scene.num
+        x, v, F, sig, vol = (np.zeros(n * 3), np.zeros(n * 3), np.zeros(n * 9), np.zeros(n * 6), np.zeros(n))
+        self.lib.ref_get_particles(x, v, F, sig, vol)
+        return {"x": x.reshape(n, 3), "v": v.reshape(n, 3), "F": F.reshape(n, 3, 3), "sigma": sig.reshape(n, 6),
+                "vol": vol}
+
+    # --- implicit solid hooks -------------------------------------------------
+    def assemble(self, facl=1.0):
+        return self.lib.ref_implicit_assemble(facl)
+
+    def matrix(self):
+        nodec, nmat = self.nodec, self.nmat
+        matrow = np.zeros(nodec + 1, dtype=np.int32)
+        matcol = np.zeros(nmat, dtype=np.int32)
+        amat = np.zeros(nmat * 9)
+        adiag = np.zeros(nodec * 3)
+        b = np.zeros(nodec * 3)
+        self.lib.ref_implicit_get_matrix(matrow, matcol, amat, adiag, b)
+        return matrow, matcol, amat.reshape(9, nmat), adiag, b
+
+    def matvec(self, x):
+        y = np.zeros(self.nodec * 3)
+        self.lib.ref_implicit_matvec(np.ascontiguousarray(x, dtype=np.float64), y)
+        return y
+
+    def solve(self):
+        x = np.zeros(self.nodec * 3)
+        it = self.lib.ref_implicit_solve(x)
+        return x, it

@@ -1,0 +1,494 @@
+/*
+ * ORACLE (test infrastructure only) -- drives the reference's own compiled
+ * translation units (module/*.cpp of HPC-MPM-Code, built unchanged by
+ * oracle/build_ref.sh against the single-rank stubs in oracle/ref_stubs/).
+ *
+ * Only tests/golden/make_golden.py and the CPU-baseline leg of bench.py may
+ * load the resulting oracle/_ref/libmpmref.so.  The product never does.
+ *
+ * What is reference code and what is restated here:
+ *   - Grid set-up, MakSf, the particle container, StandardVarP2G, VelP2G,
+ *     ComputeInternalForce/ComputeExternalForce, PIC/FLIP VarG2P,
+ *     UpdateConstitutiveModel, DeltaCorrectionParticleShifting, DetMat3,
+ *     BoundaryCondition::BCSet*, and the whole implicit solid
+ *     (implicitmpm::SolidMaterialPoint, CrsMat, GPBiCGSafe) are the
+ *     reference's compiled code, called as-is.
+ *   - The explicit solid driver functions in module/solid/explicit/ and
+ *     work/src_solid/ do not compile (they include a missing header and use
+ *     undeclared globals), so ExplicitSolid below restates
+ *       Particle2NodeS          module/solid/explicit/var_trans_solid_explicit.cpp:20-99
+ *       SolveSolid              module/solid/explicit/solve_solid_explicit.cpp:8-31
+ *       Node2ParticleS + MUSL   module/solid/explicit/var_trans_solid_explicit.cpp:101-148,187-311
+ *       update_point_coord_and_stress  ...var_trans_solid_explicit.cpp:150-185
+ *     on top of the compiled primitives, replacing the dead names
+ *     (sp -> this object, usbc/vsbc/wsbc -> ubc/vbc/wbc, the
+ *     vector-of-vector delta_def_grad -> one 3x3 per particle).
+ *   - The grid globals are set the way datain_para + InputParaGriddata set
+ *     them for one rank (work/src_fsi/datain_para.cpp:90-110,
+ *     module/data_io.cpp:31-125 with isb == 0).
+ */
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "bc.h"
+#include "cal_mat.h"
+#include "dataset.h"
+#include "material_point.h"
+#include "mesh.h"
+#include "mpi_data.h"
+#include "shape_function.h"
+#include "solid/implicit/implicit_mpm_solid.h"
+#include "solid/solid_material_point.h"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Explicit solid: restated driver functions on the compiled primitives.
+// ---------------------------------------------------------------------------
+class ExplicitSolid : public SolidMaterialPointBase {
+  public:
+    // Particle2NodeS, var_trans_solid_explicit.cpp:20-99
+    void Particle2Node() override {
+        int nenode;
+        std::vector<int> ncm;
+        std::vector<double> sf;
+        std::vector<std::array<double, 3>> dsf;
+        VectorAssign(nodec, this->nmass);
+        VectorAssign(nodec, this->nvof);
+        VectorAssign(nodec * 3, this->nmome);
+        VectorAssign(nodec * 3, this->nforce);
+        for (int m = 0; m < nelem; m++) {
+            int pid = this->idepf[m];
+            while (pid != -1) {
+                std::array<double, 3> xyp = this->coord[pid];
+                std::array<double, 6> sts = this->stress[pid];
+                MakSf(m, xyp, idimc, xynodec, ncm, nenode, sf, dsf);
+                for (int ni = 0; ni < nenode; ni++) {
+                    int nid = ncm[ni];
+                    double sfi = sf[ni];
+                    this->StandardVarP2G(pid, nid, sfi, this->mass, this->nmass);
+                    this->StandardVarP2G(pid, nid, sfi, this->vol, this->nvof);
+                    this->VelP2G(pid, nid, sfi);
+                    std::array<double, 3> fi = this->ComputeInternalForce(ni, pid, dsf, sts);
+                    std::array<double, 3> fe = this->ComputeExternalForce(pid, sfi);
+                    this->nforce[nid + nuc] += fi[0] + fe[0];
+                    this->nforce[nid + nvc] += fi[1] + fe[1];
+                    this->nforce[nid + nwc] += fi[2] + fe[2];
+                }
+                pid = this->idp2p[pid];
+            }
+        }
+        NodeVarComm(this->nmass, 0);
+        NodeVarComm(this->nvof, 0);
+        NodeVarComm(this->nmome, {nuc, nvc, nwc});
+        NodeVarComm(this->nforce, {nuc, nvc, nwc});
+        VectorAssign(nodec * 3, this->nvel);
+        for (int n = 0; n < nodec; n++) {
+            if (this->nmass[n] > mtol) {
+                this->nvel[n + nuc] = this->nmome[n + nuc] / this->nmass[n];
+                this->nvel[n + nvc] = this->nmome[n + nvc] / this->nmass[n];
+                this->nvel[n + nwc] = this->nmome[n + nwc] / this->nmass[n];
+            }
+            if (this->nvof[n] < mtol) this->nvof[n] = 0.0e0;
+        }
+        SetVelBC();
+    }
+
+    // SolveSolid, solve_solid_explicit.cpp:8-31
+    void SolveSolid() override {
+        VectorAssign(nodec * 3, this->naccel);
+        for (int n = 0; n < nodec; n++) {
+            if (this->nmass[n] > mtol) {
+                this->naccel[n + nuc] = this->nforce[n + nuc] / this->nmass[n];
+                this->naccel[n + nvc] = this->nforce[n + nvc] / this->nmass[n];
+                this->naccel[n + nwc] = this->nforce[n + nwc] / this->nmass[n];
+            }
+        }
+        this->ubc.BCSetZero(nuc, this->naccel);
+        this->vbc.BCSetZero(nvc, this->naccel);
+        this->wbc.BCSetZero(nwc, this->naccel);
+        this->rigid_bc.BCSetZero(nuc, this->naccel);
+        this->rigid_bc.BCSetZero(nvc, this->naccel);
+        this->rigid_bc.BCSetZero(nwc, this->naccel);
+    }
+
+    // Node2ParticleS, var_trans_solid_explicit.cpp:187-311 (PIC / FLIP, no F-bar)
+    void Node2Particle() override {
+        int nenode;
+        std::vector<int> ncm;
+        std::vector<double> sf;
+        std::vector<std::array<double, 3>> dsf;
+        const bool flip = (this->solswitch == MapScheme::FLIP);
+        if (!flip) {
+            for (int n = 0; n < nodec; n++) {
+                this->nvel[n + nuc] += dt * this->naccel[n + nuc];
+                this->nvel[n + nvc] += dt * this->naccel[n + nvc];
+                this->nvel[n + nwc] += dt * this->naccel[n + nwc];
+            }
+            VectorAssign(this->num, this->vel);
+        }
+        for (int m = 0; m < nelem; m++) {
+            int pid = this->idepf[m];
+            while (pid != -1) {
+                std::array<double, 3> xyp = this->coord[pid];
+                MakSf(m, xyp, idimc, xynodec, ncm, nenode, sf, dsf);
+                for (int ni = 0; ni < nenode; ni++) {
+                    if (!flip)
+                        this->pic.VarG2P(pid, ncm[ni], sf[ni], this->vel, this->nvel);
+                    else
+                        this->flip.VarG2P(pid, ncm[ni], sf[ni], this->vel, this->naccel);
+                }
+                pid = this->idp2p[pid];
+            }
+        }
+
+        MUSL();
+
+        std::vector<std::array<std::array<double, 3>, 3>> ddg(this->num);
+        for (int m = 0; m < nelem; m++) {
+            int pid = this->idepf[m];
+            while (pid != -1) {
+                std::array<double, 3> xyp = this->coord[pid];
+                MakSf(m, xyp, idimc, xynodec, ncm, nenode, sf, dsf);
+                std::array<std::array<double, 3>, 3> d{};
+                for (int ni = 0; ni < nenode; ni++) {
+                    int nid = ncm[ni];
+                    for (int j = 0; j < 3; j++) {
+                        d[0][j] += dsf[ni][j] * this->nvel[nid + nuc] * dt;
+                        d[1][j] += dsf[ni][j] * this->nvel[nid + nvc] * dt;
+                        d[2][j] += dsf[ni][j] * this->nvel[nid + nwc] * dt;
+                    }
+                }
+                for (int i = 0; i < 3; i++) d[i][i] += 1.0e0;
+                std::array<std::array<double, 3>, 3> F{};
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++)
+                        for (int k = 0; k < 3; k++) F[i][j] += d[i][k] * this->def_grad[pid][k][j];
+                this->def_grad[pid] = F;
+                this->det_def_grad[pid] = DetMat3(F);
+                ddg[pid] = d;
+                pid = this->idp2p[pid];
+            }
+        }
+
+        // update_point_coord_and_stress, var_trans_solid_explicit.cpp:150-185
+        std::vector<std::array<double, 3>> delta_corr = this->DeltaCorrectionParticleShifting();
+        for (int m = 0; m < nelem; m++) {
+            int pid = this->idepf[m];
+            while (pid != -1) {
+                std::array<double, 3> xyp = this->coord[pid];
+                MakSf(m, xyp, idimc, xynodec, ncm, nenode, sf, dsf);
+                for (int ni = 0; ni < nenode; ni++) this->flip.VarG2P(pid, ncm[ni], sf[ni], this->coord, this->nvel);
+                if (shifting_)
+                    for (int i = 0; i < 3; i++) this->coord[pid][i] += delta_corr[pid][i];
+                this->vol[pid] = this->det_def_grad[pid] * this->vol0[pid];
+                this->UpdateConstitutiveModel(pid, this->stress, this->det_def_grad, this->def_grad, ddg);
+                pid = this->idp2p[pid];
+            }
+        }
+    }
+
+    // MUSL, var_trans_solid_explicit.cpp:101-148
+    void MUSL() {
+        int nenode;
+        std::vector<int> ncm;
+        std::vector<double> sf;
+        std::vector<std::array<double, 3>> dsf;
+        VectorAssign(nodec * 3, this->nmome);
+        for (int m = 0; m < nelem; m++) {
+            int pid = this->idepf[m];
+            while (pid != -1) {
+                std::array<double, 3> xyp = this->coord[pid];
+                MakSf(m, xyp, idimc, xynodec, ncm, nenode, sf, dsf);
+                for (int ni = 0; ni < nenode; ni++) this->VelP2G(pid, ncm[ni], sf[ni]);
+                pid = this->idp2p[pid];
+            }
+        }
+        NodeVarComm(this->nmome, {nuc, nvc, nwc});
+        VectorAssign(nodec * 3, this->nvel);
+        for (int n = 0; n < nodec; n++) {
+            if (this->nmass[n] > mtol) {
+                this->nvel[n + nuc] = this->nmome[n + nuc] / this->nmass[n];
+                this->nvel[n + nvc] = this->nmome[n + nvc] / this->nmass[n];
+                this->nvel[n + nwc] = this->nmome[n + nwc] / this->nmass[n];
+            }
+        }
+        SetVelBC();
+    }
+
+    void SetVelBC() {
+        this->ubc.BCSetVal(nuc, this->nvel);
+        this->vbc.BCSetVal(nvc, this->nvel);
+        this->wbc.BCSetVal(nwc, this->nvel);
+        this->rigid_bc.BCSetVal(nuc, this->nvel);
+        this->rigid_bc.BCSetVal(nvc, this->nvel);
+        this->rigid_bc.BCSetVal(nwc, this->nvel);
+    }
+
+    bool shifting_ = true;
+};
+
+std::unique_ptr<ExplicitSolid> g_exp;
+std::unique_ptr<implicitmpm::SolidMaterialPoint> g_imp;
+int g_last_krylov = 0;
+
+MaterialPoint *active() {
+    if (g_exp) return g_exp.get();
+    if (g_imp) return g_imp.get();
+    return nullptr;
+}
+
+void load_particles(SolidMaterialPointBase &sp, int num, const double *coord, const double *vel, const double *mass,
+                    const double *vol0, const int *matid, int scheme) {
+    sp.num = num;
+    sp.solswitch = (scheme == 1) ? MapScheme::FLIP : MapScheme::PIC;
+    sp.InitializePointData();
+    for (int p = 0; p < num; p++) {
+        sp.id[p] = p;
+        sp.matid[p] = matid ? matid[p] : 0;
+        sp.mass[p] = mass[p];
+        sp.vol0[p] = vol0[p];
+        sp.vol[p] = vol0[p];  // solid_data_io.cpp:32
+        for (int i = 0; i < 3; i++) {
+            sp.coord[p][i] = coord[3 * p + i];
+            sp.vel[p][i] = vel ? vel[3 * p + i] : 0.0;
+            for (int j = 0; j < 3; j++) sp.def_grad[p][i][j] = eye_mat[i][j];  // solid_data_io.cpp:28
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+/* Grid + material globals for one rank. mat_prop is nmat x 3 (E, nu, spare). */
+int ref_setup(const int *xyelem_in, const double *xymin_in, const double *dxy_in, const int *idimc_in,
+              const int *npxye_in, double dt_in, double mtol_in, const double *bb_in, int nmat_in, const int *iprop_in,
+              const double *mat_prop_in) {
+    g_exp.reset();
+    g_imp.reset();
+    nprocs = 1;
+    myrank = 0;
+    dt = dt_in;
+    dti = 1.0 / dt_in;
+    mtol = mtol_in;
+    facl = 1.0;
+    for (int i = 0; i < 3; i++) {
+        xyelem[i] = xyelem_in[i];
+        xyelemw[i] = xyelem_in[i];
+        dxy[i] = dxy_in[i];
+        xymin[i] = xymin_in[i];
+        xyminw[i] = xymin_in[i];
+        xymax[i] = xymin_in[i] + dxy_in[i] * xyelem_in[i];
+        xymaxw[i] = xymax[i];
+        idimc[i] = idimc_in[i];
+        npxye[i] = npxye_in[i];
+        bb[i] = bb_in[i];
+        xynode[i] = xyelem[i] + 1;
+        xynodew[i] = xynode[i];
+        xynodec[i] = xyelem[i] + idimc[i];
+        xynodecw[i] = xynodec[i];
+        aelemmin[i] = 0;
+        aelemmax[i] = xyelem[i] - 1;
+        nxyr[i] = 1;
+    }
+    nelem = xyelem[0] * xyelem[1] * xyelem[2];
+    node = xynode[0] * xynode[1] * xynode[2];
+    nodec = xynodec[0] * xynodec[1] * xynodec[2];
+    // module/data_io.cpp:48-56
+    nu = 0; nv = nu + node; nw = nv + node; np = nw + node;
+    nuc = 0; nvc = nuc + nodec; nwc = nvc + nodec; npc = nwc + nodec;
+    // module/data_io.cpp:114-123 (isb == 0)
+    isb = 0;
+    naid.resize(0); nsbc.resize(0); nsubc.resize(0); nsbl.resize(0); nsubl.resize(0);
+    dbc.assign(nodec * 4, 1.0);
+    dbl.assign(node * 4, 1.0);
+    nmat = nmat_in;
+    npropmax = 3;
+    iprop.assign(nmat, 0.0);
+    nprop.assign(nmat, 2.0);
+    mat_prop.assign(nmat, std::vector<double>(3, 0.0));
+    for (int n = 0; n < nmat; n++) {
+        iprop[n] = iprop_in[n];
+        for (int k = 0; k < 3; k++) mat_prop[n][k] = mat_prop_in[3 * n + k];
+    }
+    BuildMesh();
+    BuildControlPoint();
+    MakNodalVol();
+    return nodec;
+}
+
+int ref_explicit_init(int num, const double *coord, const double *vel, const double *mass, const double *vol0,
+                      const int *matid, int scheme, int shifting) {
+    g_imp.reset();
+    g_exp = std::make_unique<ExplicitSolid>();
+    g_exp->shifting_ = shifting != 0;
+    load_particles(*g_exp, num, coord, vel, mass, vol0, matid, scheme);
+    g_exp->MeshPointLinklist();
+    g_exp->DetermineRigidBC();
+    return 0;
+}
+
+/* which: 0 u, 1 v, 2 w (BoundaryCondition ubc/vbc/wbc) */
+int ref_set_bc(int which, int n, const int *nodes, const double *vals) {
+    MaterialPoint *mp = active();
+    if (!mp) return -1;
+    BoundaryCondition *bc = which == 0 ? &mp->ubc : which == 1 ? &mp->vbc : &mp->wbc;
+    bc->ibc = n;
+    bc->nbc.assign(nodes, nodes + n);
+    bc->fbc.assign(vals, vals + n);
+    return 0;
+}
+
+/* One explicit step = MeshPointLinklist, Particle2NodeS, SolveSolid, Node2ParticleS
+ * (work/src_solid/explicit/main.cpp:39-73). */
+int ref_explicit_steps(int nsteps, double facl_in) {
+    if (!g_exp) return -1;
+    facl = facl_in;
+    for (int s = 0; s < nsteps; s++) {
+        g_exp->MeshPointLinklist();
+        g_exp->Particle2Node();
+        g_exp->SolveSolid();
+        g_exp->Node2Particle();
+    }
+    return 0;
+}
+
+/* P2G only (binning + Particle2NodeS + SolveSolid): the first-kernel parity point. */
+int ref_explicit_p2g(double facl_in) {
+    if (!g_exp) return -1;
+    facl = facl_in;
+    g_exp->MeshPointLinklist();
+    g_exp->Particle2Node();
+    g_exp->SolveSolid();
+    return 0;
+}
+
+/* field: 0 nmass, 1 nvof, 2 nmome, 3 nforce, 4 nvel, 5 naccel, 6 nvol, 7 ndispl */
+int ref_get_nodal(int field, double *out) {
+    MaterialPoint *mp = active();
+    const std::vector<double> *v = nullptr;
+    switch (field) {
+    case 0: v = &mp->nmass; break;
+    case 1: v = &mp->nvof; break;
+    case 2: v = &mp->nmome; break;
+    case 3: v = &mp->nforce; break;
+    case 4: v = &mp->nvel; break;
+    case 5: v = &mp->naccel; break;
+    case 6: v = &nvol; break;
+    case 7: v = &mp->ndispl; break;
+    default: return -1;
+    }
+    std::memcpy(out, v->data(), v->size() * sizeof(double));
+    return (int)v->size();
+}
+
+int ref_get_particles(double *coord, double *vel, double *F, double *stress, double *vol) {
+    MaterialPoint *mp = active();
+    for (int p = 0; p < mp->num; p++) {
+        for (int i = 0; i < 3; i++) {
+            coord[3 * p + i] = mp->coord[p][i];
+            vel[3 * p + i] = mp->vel[p][i];
+            for (int j = 0; j < 3; j++) F[9 * p + 3 * i + j] = mp->def_grad[p][i][j];
+        }
+        for (int k = 0; k < 6; k++) stress[6 * p + k] = mp->stress[p][k];
+        vol[p] = mp->vol[p];
+    }
+    return mp->num;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Implicit solid: the reference's implicitmpm::SolidMaterialPoint as-is.      */
+/* ------------------------------------------------------------------------- */
+int ref_implicit_init(int num, const double *coord, const double *vel, const double *mass, const double *vol0,
+                      const int *matid, int scheme, int nr_flag, double spec_rad) {
+    g_exp.reset();
+    g_imp = std::make_unique<implicitmpm::SolidMaterialPoint>();
+    auto &sp = *g_imp;
+    sp.SM_.use_petsc = false;  // native GPBiCGSafe + diagonal scaling
+    sp.NR_flag = nr_flag != 0;
+    sp.spec_rad = spec_rad;
+    load_particles(sp, num, coord, vel, mass, vol0, matid, scheme);
+    sp.GeneralizedAlphaParaSet();  // work/src_fsi/datain_para.cpp:103-105
+    sp.NewmarkBetaParaSet();
+    sp.SM_.BuildCrsMat(9);  // work/src_fsi/main.cpp:47
+    sp.MeshPointLinklist();
+    sp.DetermineRigidBC();
+    VectorAssign(nodec * 3, sp.ndispl);
+    return sp.SM_.nmat;
+}
+
+/* Steps of work/src_fsi/main.cpp:80-88 without the fluid. */
+int ref_implicit_steps(int nsteps, double facl_in) {
+    if (!g_imp) return -1;
+    facl = facl_in;
+    for (int s = 0; s < nsteps; s++) {
+        g_imp->MeshPointLinklist();
+        g_imp->Particle2Node();
+        g_imp->SolveSolid();
+        g_imp->Node2Particle();
+    }
+    return 0;
+}
+
+/* Assemble the first Newton system of a step (ndispl = 0) exactly as
+ * SolveSolid does before its first linear solve, and leave it in SM_:
+ * amat/adiag are the diagonally scaled matrix and its D^{-1/2}. */
+int ref_implicit_assemble(double facl_in) {
+    if (!g_imp) return -1;
+    auto &sp = *g_imp;
+    facl = facl_in;
+    sp.MeshPointLinklist();
+    sp.Particle2Node();
+    std::vector<double> nvel_k(nodec * 3), naccel_k(nodec * 3);
+    std::vector<std::array<double, 6>> stress_k = sp.InitializeNRStress();
+    VectorAssign(nodec * 3, sp.ndispl);
+    VectorAssign(nodec * 3, sp.SM_.x_lhs);
+    sp.BCNRSet();
+    sp.PredictNewmarkBetaVelAndAccel(nvel_k, naccel_k);
+    sp.AssembleSystem(naccel_k, nvel_k, stress_k);
+    return sp.SM_.nmat;
+}
+
+/* CSR graph + block-major values of the assembled (scaled) matrix. */
+int ref_implicit_get_matrix(int *matrow, int *matcolid, double *amat, double *adiag, double *b_rhs) {
+    auto &M = g_imp->SM_;
+    std::memcpy(matrow, M.matrow.data(), M.matrow.size() * sizeof(int));
+    std::memcpy(matcolid, M.matcolid.data(), M.matcolid.size() * sizeof(int));
+    std::memcpy(amat, M.amat.data(), M.amat.size() * sizeof(double));
+    std::memcpy(adiag, M.adiag.data(), M.adiag.size() * sizeof(double));
+    std::memcpy(b_rhs, M.b_rhs.data(), M.b_rhs.size() * sizeof(double));
+    return M.nmat;
+}
+
+/* y = CrsMat::MatVecMult(x) on the assembled, scaled matrix (solver.cpp:405-433). */
+int ref_implicit_matvec(const double *x, double *y) {
+    auto &M = g_imp->SM_;
+    std::vector<double> xx(x, x + (size_t)nodec * 3);
+    M.x_lhs.assign((size_t)nodec * 3, 0.0);
+    std::vector<double> yy = M.MatVecMult(xx);
+    std::memcpy(y, yy.data(), yy.size() * sizeof(double));
+    return 0;
+}
+
+/* GPBiCGSafe (solver.cpp:19-141) on the assembled system from x = 0;
+ * returns the iteration count and leaves the physical solution in x_out. */
+int ref_implicit_solve(double *x_out) {
+    auto &M = g_imp->SM_;
+    M.x_lhs.assign((size_t)nodec * 3, 0.0);
+    int it = GPBiCGSafe(M);
+    std::memcpy(x_out, M.x_lhs.data(), M.x_lhs.size() * sizeof(double));
+    g_last_krylov = it;
+    return it;
+}
+
+int ref_nodec(void) { return nodec; }
+int ref_num(void) {
+    MaterialPoint *mp = active();
+    return mp ? mp->num : 0;
+}
+
+}  // extern "C"

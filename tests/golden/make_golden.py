@@ -1,0 +1,103 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Runs the reference's own compiled translation units (oracle/_ref/libmpmref.so,
+built by oracle/build_ref.sh from the reference checkout) on small seeded
+scenes and stores inputs and outputs as compressed .npz files.  The reference
+checkout exists only in the development container, so the fixtures are
+committed and this script is re-run only when a case is added:
+
+    oracle/build_ref.sh && python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "hpc-mpm-code_gb300"))
+
+from mpm_gb300 import scenes  # noqa: E402
+from oracle import ref  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def scene_arrays(s):
+    d = {"xyelem": np.array(s.xyelem), "xymin": np.array(s.xymin), "dxy": np.array(s.dxy),
+         "idimc": np.array(s.idimc), "npxye": np.array(s.npxye), "dt": np.array(s.dt), "mtol": np.array(s.mtol),
+         "gravity": np.array(s.gravity), "iprop": s.iprop, "mat_prop": s.mat_prop, "coord": s.coord, "vel": s.vel,
+         "mass": s.mass, "vol0": s.vol0, "matid": s.matid, "scheme": np.array(s.scheme)}
+    for i, (comp, nodes, vals) in enumerate(s.bcs):
+        d[f"bc{i}_comp"] = np.array(comp)
+        d[f"bc{i}_nodes"] = nodes
+        d[f"bc{i}_vals"] = vals
+    d["nbc"] = np.array(len(s.bcs))
+    return d
+
+
+def explicit_case(name, scene, nsteps, facl=1.0):
+    r = ref.RefSolid(scene)
+    r.p2g(facl)
+    out = {f"p2g_{k}": r.nodal(k) for k in ("nmass", "nvof", "nmome", "nforce", "nvel", "naccel", "nvol")}
+    r = ref.RefSolid(scene)
+    r.steps(1, facl)
+    out.update({f"step1_{k}": v for k, v in r.particles().items()})
+    r.steps(nsteps - 1, facl)
+    out.update({f"stepN_{k}": v for k, v in r.particles().items()})
+    out["nsteps"] = np.array(nsteps)
+    out["facl"] = np.array(facl)
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **scene_arrays(scene), **out)
+    print("wrote", name, scene.num, "particles")
+
+
+def implicit_case(name, scene, nr_flag, nsteps):
+    r = ref.RefSolid(scene, implicit=True, nr_flag=nr_flag)
+    r.assemble()
+    matrow, matcol, amat, adiag, b = r.matrix()
+    rng = np.random.default_rng(7)
+    x = rng.normal(size=r.nodec * 3)
+    y = r.matvec(x)
+    xs, it = r.solve()
+    out = {"matrow": matrow, "matcolid": matcol, "amat": amat, "adiag": adiag, "b_rhs": b, "mv_x": x, "mv_y": y,
+           "solve_x": xs, "solve_iters": np.array(it)}
+    r = ref.RefSolid(scene, implicit=True, nr_flag=nr_flag)
+    r.implicit_steps(nsteps)
+    out.update({f"stepN_{k}": v for k, v in r.particles().items()})
+    out["nsteps"] = np.array(nsteps)
+    out["nr_flag"] = np.array(int(nr_flag))
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **scene_arrays(scene), **out)
+    print("wrote", name, scene.num, "particles", r.nmat, "blocks")
+
+
+def main():
+    if not ref.available():
+        raise SystemExit("oracle/_ref/libmpmref.so missing: run oracle/build_ref.sh first")
+    rng = np.random.default_rng(20261203)
+    # small elastic block, fixed bottom, PIC and FLIP, random initial velocity
+    for scheme, nm in ((scenes.PIC, "explicit_pic"), (scenes.FLIP, "explicit_flip")):
+        s = scenes.elastic_block(grid=(10, 10, 8), cell_lo=(2, 2, 0), cell_hi=(7, 7, 5), scheme=scheme,
+                                 dt=1.0e-5, seed=101 + scheme)
+        s.vel[:] = rng.normal(0.0, 0.3, size=s.vel.shape)
+        explicit_case(nm, s, nsteps=25)
+    # quadratic B-spline shape functions in x and z (idimc 2 1 2, like the reference's beam deck)
+    s = scenes.elastic_block(grid=(10, 6, 10), cell_lo=(2, 1, 0), cell_hi=(8, 5, 5), idimc=(2, 1, 2), seed=103,
+                             scheme=scenes.FLIP)
+    s.vel[:] = rng.normal(0.0, 0.2, size=s.vel.shape)
+    explicit_case("explicit_quadratic", s, nsteps=10)
+    # load ramp factor below one and a Neo-Hookean block
+    s = scenes.elastic_block(grid=(10, 10, 10), cell_lo=(2, 2, 0), cell_hi=(8, 8, 6), iprop=1, seed=104,
+                             E=5.0e5)
+    s.vel[:] = rng.normal(0.0, 0.2, size=s.vel.shape)
+    explicit_case("explicit_neohookean", s, nsteps=10, facl=0.5)
+    # implicit solid: linear elastic single solve per step, and Neo-Hookean Newton
+    s = scenes.cantilever(grid=(10, 8, 8), cells=(6, 4, 4), cell_lo=(0, 2, 2), iprop=0)
+    implicit_case("implicit_linear", s, nr_flag=False, nsteps=3)
+    s = scenes.cantilever(grid=(10, 8, 8), cells=(6, 4, 4), cell_lo=(0, 2, 2), iprop=1)
+    implicit_case("implicit_neohookean", s, nr_flag=True, nsteps=3)
+
+
+if __name__ == "__main__":
+    main()
