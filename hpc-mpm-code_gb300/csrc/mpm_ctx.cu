@@ -1,0 +1,545 @@
+// C ABI of the GB300 MPM transfer path: context lifetime, particle load,
+// boundary conditions, the explicit step and result downloads.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "mpm_device.cuh"
+
+using namespace mpm;
+
+namespace mpm {
+
+static const char *kClassNames[NKCLASS] = {"bin",  "scan", "scatter", "permute", "p2g",    "grid1",
+                                           "g2p_musl", "grid2", "g2p_update", "misc", "matvec", "krylov"};
+
+void timer_begin(mpm_ctx *c, int cls) {
+    if (!c->timer.on) return;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, c->stream);
+    c->timer.ev.push_back(e0);
+    c->timer.ev.push_back(e1);
+    c->timer.cls.push_back(cls);
+}
+
+void timer_end(mpm_ctx *c, int) {
+    if (!c->timer.on) return;
+    cudaEventRecord(c->timer.ev.back(), c->stream);
+}
+
+mpm_status check_launch(mpm_ctx *c) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        fprintf(stderr, "mpm_gb300: CUDA error %s\n", cudaGetErrorString(e));
+        c->latched = MPM_ERR_CUDA;
+        return MPM_ERR_CUDA;
+    }
+    return MPM_OK;
+}
+
+}  // namespace mpm
+
+#define CK(call)                                                                                                       \
+    do {                                                                                                               \
+        cudaError_t _e = (call);                                                                                       \
+        if (_e != cudaSuccess) {                                                                                       \
+            fprintf(stderr, "mpm_gb300: %s failed: %s\n", #call, cudaGetErrorString(_e));                              \
+            return _e == cudaErrorMemoryAllocation ? MPM_ERR_OOM : MPM_ERR_CUDA;                                       \
+        }                                                                                                              \
+    } while (0)
+
+static void free_dev(void *p) {
+    if (p) cudaFree(p);
+}
+
+static void free_particles(mpm_ctx *c) {
+    free_dev(c->pbuf[0]);
+    free_dev(c->pbuf[1]);
+    free_dev(c->d_key);
+    free_dev(c->d_perm);
+    free_dev(c->d_work);
+    c->pbuf[0] = c->pbuf[1] = nullptr;
+    c->d_key = c->d_perm = nullptr;
+    c->d_work = nullptr;
+    c->num = 0;
+}
+
+// The exported functions take C linkage from their declarations in mpm_gpu.h.
+
+const char *mpm_gpu_status_string(mpm_status s) {
+    switch (s) {
+    case MPM_OK: return "ok";
+    case MPM_ERR_BAD_ARG: return "bad argument";
+    case MPM_ERR_OOM: return "out of device memory";
+    case MPM_ERR_NONFINITE: return "non-finite particle state";
+    case MPM_ERR_PARTICLE_OUT_OF_BOX: return "particle outside the grid";
+    case MPM_ERR_KRYLOV_MAXIT: return "Krylov solver reached its iteration limit";
+    case MPM_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+    case MPM_ERR_CUDA: return "CUDA error";
+    case MPM_ERR_STATE: return "call out of order";
+    case MPM_ERR_UNSUPPORTED: return "unsupported configuration";
+    }
+    return "unknown";
+}
+
+mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *mat, const mpm_config *cfg,
+                          mpm_ctx **out) {
+    if (!grid || !mat || !cfg || !out) return MPM_ERR_BAD_ARG;
+    *out = nullptr;
+    if (cfg->precision != 32 && cfg->precision != 64) return MPM_ERR_BAD_ARG;
+    if (cfg->scheme != MPM_PIC && cfg->scheme != MPM_FLIP) return MPM_ERR_UNSUPPORTED;
+    if (!(cfg->dt > 0.0) || mat->nmat <= 0 || !mat->iprop || !mat->mat_prop) return MPM_ERR_BAD_ARG;
+    for (int d = 0; d < 3; d++) {
+        if (grid->xyelem[d] <= 0 || !(grid->dxy[d] > 0.0)) return MPM_ERR_BAD_ARG;
+        if (grid->idimc[d] != 1 && grid->idimc[d] != 2) return MPM_ERR_UNSUPPORTED;
+        if (grid->npxye[d] < 1 || grid->npxye[d] > 6) return MPM_ERR_BAD_ARG;
+    }
+    {
+        const int *o = grid->idimc;
+        bool ok = (o[0] == 1 && o[1] == 1 && o[2] == 1) || (o[0] == 2 && o[1] == 2 && o[2] == 2) ||
+                  (o[0] == 2 && o[1] == 1 && o[2] == 2);
+        if (!ok) return MPM_ERR_UNSUPPORTED;
+    }
+    for (int k = 0; k < mat->nmat; k++)
+        if (mat->iprop[k] < -1 || mat->iprop[k] > 1) return MPM_ERR_UNSUPPORTED;
+    mpm_ctx *c = new (std::nothrow) mpm_ctx();
+    if (!c) return MPM_ERR_OOM;
+    Geom &g = c->g;
+    long long nodec = 1;
+    for (int d = 0; d < 3; d++) {
+        g.nel[d] = grid->xyelem[d];
+        g.order[d] = grid->idimc[d];
+        g.nnc[d] = grid->xyelem[d] + grid->idimc[d];
+        g.ntile[d] = (g.nnc[d] + TILE - 1) / TILE;
+        g.xmin[d] = grid->xymin[d];
+        g.dx[d] = grid->dxy[d];
+        c->npxye[d] = grid->npxye[d];
+        c->gravity[d] = cfg->gravity[d];
+        nodec *= g.nnc[d];
+    }
+    if (nodec > (1LL << 30)) {
+        delete c;
+        return MPM_ERR_BAD_ARG;
+    }
+    g.nodec = (int)nodec;
+    g.nelem = g.nel[0] * g.nel[1] * g.nel[2];
+    g.ntiles = g.ntile[0] * g.ntile[1] * g.ntile[2];
+    c->precision = cfg->precision;
+    c->rsize = cfg->precision == 64 ? 8 : 4;
+    c->scheme = cfg->scheme;
+    c->shifting = cfg->shifting ? 1 : 0;
+    c->resort_period = cfg->resort_period > 0 ? cfg->resort_period : 8;
+    c->dt = cfg->dt;
+    c->mtol = cfg->mtol;
+    c->nmat = mat->nmat;
+    size_t N = (size_t)g.nodec;
+    mpm_status st = MPM_OK;
+    auto alloc = [&](void **p, size_t bytes) {
+        if (st != MPM_OK) return;
+        cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+        if (e != cudaSuccess) st = MPM_ERR_OOM;
+    };
+    alloc((void **)&c->d_iprop, sizeof(int) * c->nmat);
+    alloc((void **)&c->d_matprop, sizeof(double) * 3 * c->nmat);
+    alloc((void **)&c->d_acc, sizeof(unsigned long long) * NACC * N);
+    alloc((void **)&c->d_acc2, sizeof(unsigned long long) * 3 * N);
+    alloc(&c->d_nodal, c->rsize * 13 * N);
+    alloc((void **)&c->d_nvol, sizeof(double) * N);
+    alloc((void **)&c->d_bcflag, N);
+    alloc(&c->d_bcval, c->rsize * 3 * N);
+    alloc((void **)&c->d_tileflag, g.ntiles);
+    alloc((void **)&c->d_eu_part, sizeof(double) * g.ntiles);
+    alloc((void **)&c->d_tcount, sizeof(int) * g.ntiles);
+    alloc((void **)&c->d_tstart, sizeof(int) * g.ntiles);
+    alloc((void **)&c->d_tcursor, sizeof(int) * g.ntiles);
+    alloc((void **)&c->d_nwork, sizeof(int));
+    alloc((void **)&c->d_ctl, sizeof(DevCtl));
+    if (st == MPM_OK && cudaMallocHost((void **)&c->h_ctl, sizeof(DevCtl)) != cudaSuccess) st = MPM_ERR_OOM;
+    if (st != MPM_OK) {
+        mpm_gpu_destroy(c);
+        return st;
+    }
+    cudaMemcpy(c->d_iprop, mat->iprop, sizeof(int) * c->nmat, cudaMemcpyHostToDevice);
+    cudaMemcpy(c->d_matprop, mat->mat_prop, sizeof(double) * 3 * c->nmat, cudaMemcpyHostToDevice);
+    cudaMemset(c->d_acc, 0, sizeof(unsigned long long) * NACC * N);
+    cudaMemset(c->d_acc2, 0, sizeof(unsigned long long) * 3 * N);
+    cudaMemset(c->d_nodal, 0, c->rsize * 13 * N);
+    cudaMemset(c->d_bcflag, 0, N);
+    cudaMemset(c->d_bcval, 0, c->rsize * 3 * N);
+    cudaMemset(c->d_tileflag, 0, g.ntiles);
+    cudaMemset(c->d_eu_part, 0, sizeof(double) * g.ntiles);
+    cudaMemset(c->d_tcount, 0, sizeof(int) * g.ntiles);
+    cudaMemset(c->d_tcursor, 0, sizeof(int) * g.ntiles);
+    cudaMemset(c->d_nwork, 0, sizeof(int));
+    cudaMemset(c->d_ctl, 0, sizeof(DevCtl));
+    memset(c->h_ctl, 0, sizeof(DevCtl));
+    compute_nodal_volume(c);
+    if (cudaDeviceSynchronize() != cudaSuccess || check_launch(c) != MPM_OK) {
+        mpm_gpu_destroy(c);
+        return MPM_ERR_CUDA;
+    }
+    *out = c;
+    return MPM_OK;
+}
+
+void mpm_gpu_destroy(mpm_ctx *c) {
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_particles(c);
+    free_dev(c->d_iprop);
+    free_dev(c->d_matprop);
+    free_dev(c->d_acc);
+    free_dev(c->d_acc2);
+    free_dev(c->d_nodal);
+    free_dev(c->d_nvol);
+    free_dev(c->d_bcflag);
+    free_dev(c->d_bcval);
+    free_dev(c->d_tileflag);
+    free_dev(c->d_eu_part);
+    free_dev(c->d_tcount);
+    free_dev(c->d_tstart);
+    free_dev(c->d_tcursor);
+    free_dev(c->d_nwork);
+    free_dev(c->d_ctl);
+    if (c->h_ctl) cudaFreeHost(c->h_ctl);
+    for (auto e : c->timer.ev) cudaEventDestroy(e);
+    delete c;
+}
+
+mpm_status mpm_gpu_set_stream(mpm_ctx *c, void *stream) {
+    if (!c) return MPM_ERR_BAD_ARG;
+    c->stream = (cudaStream_t)stream;
+    return MPM_OK;
+}
+
+template <typename R>
+static mpm_status upload_particles(mpm_ctx *c, int64_t n, const double *coord, const double *vel, const double *mass,
+                                   const double *vol0, const double *F, const double *stress, const int *matid) {
+    size_t N = (size_t)n;
+    size_t bytes = N * (24 * sizeof(R) + 2 * sizeof(int));
+    std::vector<char> host(bytes);
+    R *f = (R *)host.data();
+    double vmax = 0.0, volmax = 0.0, vsmax = 0.0, mmax = 0.0;
+    for (size_t p = 0; p < N; p++) {
+        for (int k = 0; k < 3; k++) {
+            f[k * N + p] = (R)coord[3 * p + k];
+            double v = vel ? vel[3 * p + k] : 0.0;
+            f[(3 + k) * N + p] = (R)v;
+            vmax = fmax(vmax, fabs(v));
+        }
+        for (int k = 0; k < 9; k++) f[(6 + k) * N + p] = (R)(F ? F[9 * p + k] : ((k % 4) == 0 ? 1.0 : 0.0));
+        double s[6];
+        for (int k = 0; k < 6; k++) {
+            s[k] = stress ? stress[6 * p + k] : 0.0;
+            f[(15 + k) * N + p] = (R)s[k];
+        }
+        f[21 * N + p] = (R)mass[p];
+        f[22 * N + p] = (R)vol0[p];
+        f[23 * N + p] = (R)vol0[p];   // vol = vol0 (solid_data_io.cpp:32)
+        mmax = fmax(mmax, fabs(mass[p]));
+        volmax = fmax(volmax, fabs(vol0[p]));
+        double rs = fmax(fabs(s[0]) + fabs(s[5]) + fabs(s[4]),
+                         fmax(fabs(s[5]) + fabs(s[1]) + fabs(s[3]), fabs(s[4]) + fabs(s[3]) + fabs(s[2])));
+        vsmax = fmax(vsmax, fabs(vol0[p]) * rs);
+    }
+    int *ip = (int *)(f + 24 * N);
+    for (size_t p = 0; p < N; p++) {
+        int mid = matid ? matid[p] : 0;
+        if (mid < 0 || mid >= c->nmat) return MPM_ERR_BAD_ARG;
+        ip[p] = mid;
+        ip[N + p] = (int)p;
+    }
+    CK(cudaMemcpy(c->pbuf[c->cur], host.data(), bytes, cudaMemcpyHostToDevice));
+    c->mmax = mmax * 1.000001;
+    // bounds for the first step's fixed-point scales (slot of the current parity)
+    DevCtl h;
+    memset(&h, 0, sizeof(h));
+    int par = (int)(c->step & 1);
+    auto fb = [](double v) {
+        float f = (float)(v * 1.000001);
+        unsigned u;
+        memcpy(&u, &f, 4);
+        return u;
+    };
+    h.nxt[par][B_VMAX] = fb(vmax);
+    h.nxt[par][B_VOLMAX] = fb(volmax);
+    h.nxt[par][B_VOLSMAX] = fb(vsmax);
+    CK(cudaMemcpy(c->d_ctl, &h, sizeof(DevCtl), cudaMemcpyHostToDevice));
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_load_particles(mpm_ctx *c, int64_t n, const double *coord, const double *vel, const double *mass,
+                                  const double *vol0, const double *F, const double *stress, const int *matid) {
+    if (!c || n < 0 || n > (1LL << 30) || (n > 0 && (!coord || !mass || !vol0))) return MPM_ERR_BAD_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    free_particles(c);
+    c->num = n;
+    size_t N = (size_t)(n > 0 ? n : 1);
+    size_t bytes = N * (24 * c->rsize + 2 * sizeof(int));
+    CK(cudaMalloc(&c->pbuf[0], bytes));
+    CK(cudaMalloc(&c->pbuf[1], bytes));
+    CK(cudaMalloc((void **)&c->d_key, sizeof(int) * N));
+    CK(cudaMalloc((void **)&c->d_perm, sizeof(int) * N));
+    c->nwork_cap = c->g.ntiles + (int)(N / CHUNK) + 1;
+    CK(cudaMalloc((void **)&c->d_work, sizeof(WorkItem) * c->nwork_cap));
+    c->cur = 0;
+    mpm_status s = c->precision == 64 ? upload_particles<double>(c, n, coord, vel, mass, vol0, F, stress, matid)
+                                      : upload_particles<float>(c, n, coord, vel, mass, vol0, F, stress, matid);
+    if (s != MPM_OK) return s;
+    CK(cudaMemset(c->d_acc, 0, sizeof(unsigned long long) * NACC * c->g.nodec));
+    CK(cudaMemset(c->d_acc2, 0, sizeof(unsigned long long) * 3 * c->g.nodec));
+    CK(cudaMemset(c->d_tileflag, 0, c->g.ntiles));
+    c->accum_dirty = false;
+    c->stage = 0;
+    if (n > 0) {
+        s = sort_particles(c);
+        if (s != MPM_OK) return s;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_set_bc(mpm_ctx *c, int comp, int n, const int *nodes, const double *vals) {
+    if (!c || comp < 0 || comp > 2 || n < 0 || (n > 0 && (!nodes || !vals))) return MPM_ERR_BAD_ARG;
+    for (int i = 0; i < n; i++)
+        if (nodes[i] < 0 || nodes[i] >= c->g.nodec) return MPM_ERR_BAD_ARG;
+    c->bc_nodes[comp].assign(nodes, nodes + n);
+    c->bc_vals[comp].assign(vals, vals + n);
+    size_t N = (size_t)c->g.nodec;
+    std::vector<unsigned char> flag(N, 0);
+    std::vector<double> val(3 * N, 0.0);
+    for (int k = 0; k < 3; k++)
+        for (size_t i = 0; i < c->bc_nodes[k].size(); i++) {   // later entries win, as BCSetVal's loop
+            int nd = c->bc_nodes[k][i];
+            flag[nd] |= (unsigned char)(1 << k);
+            val[k * N + nd] = c->bc_vals[k][i];
+        }
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(c->d_bcflag, flag.data(), N, cudaMemcpyHostToDevice));
+    if (c->precision == 64) {
+        CK(cudaMemcpy(c->d_bcval, val.data(), sizeof(double) * 3 * N, cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> vf(3 * N);
+        for (size_t i = 0; i < 3 * N; i++) vf[i] = (float)val[i];
+        CK(cudaMemcpy(c->d_bcval, vf.data(), sizeof(float) * 3 * N, cudaMemcpyHostToDevice));
+    }
+    return MPM_OK;
+}
+
+static mpm_status begin_step(mpm_ctx *c, double facl) {
+    if (c->accum_dirty) {
+        CK(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * NACC * c->g.nodec, c->stream));
+        CK(cudaMemsetAsync(c->d_acc2, 0, sizeof(unsigned long long) * 3 * c->g.nodec, c->stream));
+        CK(cudaMemsetAsync(c->d_tileflag, 0, c->g.ntiles, c->stream));
+        c->accum_dirty = false;
+    }
+    if (c->steps_since_sort >= c->resort_period) {
+        mpm_status s = sort_particles(c);
+        if (s != MPM_OK) return s;
+    }
+    mpm_status s = run_p2g(c, facl);
+    if (s != MPM_OK) return s;
+    return run_grid1(c, 0);
+}
+
+mpm_status mpm_gpu_p2g(mpm_ctx *c, double facl) {
+    if (!c) return MPM_ERR_BAD_ARG;
+    if (c->num == 0) return MPM_ERR_STATE;
+    c->write_nodal_dl = true;
+    if (c->stage != 0) c->accum_dirty = true;
+    mpm_status s = begin_step(c, facl);
+    c->stage = 1;
+    return s;
+}
+
+mpm_status mpm_gpu_grid_update(mpm_ctx *c) {
+    // SolveSolid's a = f/m with the BC zeroing is evaluated in the same grid
+    // pass as Particle2NodeS's nvel; this call only checks the ordering.
+    if (!c) return MPM_ERR_BAD_ARG;
+    if (c->stage != 1) return MPM_ERR_STATE;
+    c->stage = 2;
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_g2p(mpm_ctx *c) {
+    if (!c) return MPM_ERR_BAD_ARG;
+    if (c->stage != 2) return MPM_ERR_STATE;
+    c->write_nodal_dl = true;
+    mpm_status s = run_g2p(c);
+    c->accum_dirty = true;   // accumulators kept for downloads; cleared by the next P2G
+    c->stage = 0;
+    c->step++;
+    c->steps_since_sort++;
+    return s;
+}
+
+mpm_status mpm_gpu_step_explicit(mpm_ctx *c, int nsteps, double facl) {
+    if (!c || nsteps < 0) return MPM_ERR_BAD_ARG;
+    if (c->num == 0) return MPM_ERR_STATE;
+    if (c->stage != 0) return MPM_ERR_STATE;
+    c->write_nodal_dl = false;
+    for (int s = 0; s < nsteps; s++) {
+        mpm_status st = begin_step(c, facl);
+        if (st != MPM_OK) return st;
+        st = run_g2p(c);
+        if (st != MPM_OK) return st;
+        c->step++;
+        c->steps_since_sort++;
+    }
+    return MPM_OK;
+}
+
+static mpm_status read_errors(mpm_ctx *c) {
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(c->h_ctl, c->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost));
+    if (c->latched != MPM_OK) return c->latched;
+    if (c->h_ctl->err_nonfinite) return MPM_ERR_NONFINITE;
+    if (c->h_ctl->err_oob) return MPM_ERR_PARTICLE_OUT_OF_BOX;
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_sync(mpm_ctx *c) {
+    if (!c) return MPM_ERR_BAD_ARG;
+    mpm_status s = read_errors(c);
+    if (s != MPM_OK && s != MPM_ERR_CUDA) {
+        // clear latched device error counters
+        unsigned z[2] = {0, 0};
+        cudaMemcpy(&c->d_ctl->err_oob, z, sizeof(unsigned) * 2, cudaMemcpyHostToDevice);
+        c->latched = MPM_OK;
+    }
+    return s;
+}
+
+template <typename R>
+static void to_host(const void *dev, size_t count, double *host) {
+    std::vector<R> t(count);
+    cudaMemcpy(t.data(), dev, sizeof(R) * count, cudaMemcpyDeviceToHost);
+    for (size_t i = 0; i < count; i++) host[i] = (double)t[i];
+}
+
+mpm_status mpm_gpu_download_nodal(mpm_ctx *c, int field, double *host) {
+    if (!c || !host || field < 0 || field > 6) return MPM_ERR_BAD_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    size_t N = (size_t)c->g.nodec;
+    if (field == 6) {
+        CK(cudaMemcpy(host, c->d_nvol, sizeof(double) * N, cudaMemcpyDeviceToHost));
+        return MPM_OK;
+    }
+    if (field == 4 || field == 5) {
+        // nvel: after g2p the MUSL velocity, before it the P2G velocity; naccel from the grid update
+        size_t off = (field == 5) ? 10 * N : (c->stage == 0 && c->step > 0 ? 4 * N : 7 * N);
+        const char *base = (const char *)c->d_nodal + off * c->rsize;
+        if (c->precision == 64) to_host<double>(base, 3 * N, host);
+        else to_host<float>(base, 3 * N, host);
+        return MPM_OK;
+    }
+    // accumulated sums, with the scales the last P2G used
+    std::vector<long long> q;
+    DevCtl h;
+    CK(cudaMemcpy(&h, c->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost));
+    int f0 = field == 0 ? 0 : field == 1 ? 1 : field == 2 ? 2 : 5;
+    int nf = (field <= 1) ? 1 : 3;
+    const double inv = h.p2g_inv[field == 0 ? 0 : field == 1 ? 1 : field == 2 ? 2 : 3];
+    q.resize(nf * N);
+    CK(cudaMemcpy(q.data(), c->d_acc + (size_t)f0 * N, sizeof(long long) * nf * N, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < nf * N; i++) {
+        double v = (double)q[i] * inv;
+        if (c->precision == 32) v = (double)(float)v;
+        host[i] = v;
+    }
+    if (field == 1)
+        for (size_t i = 0; i < N; i++)
+            if (host[i] < c->mtol) host[i] = 0.0;   // Particle2NodeS:88
+    return MPM_OK;
+}
+
+template <typename R>
+static mpm_status dl_particles(mpm_ctx *c, double *coord, double *vel, double *F, double *stress, double *vol) {
+    size_t N = (size_t)c->num;
+    size_t bytes = N * (24 * sizeof(R) + 2 * sizeof(int));
+    std::vector<char> host(bytes);
+    CK(cudaMemcpy(host.data(), c->pbuf[c->cur], bytes, cudaMemcpyDeviceToHost));
+    const R *f = (const R *)host.data();
+    const int *pid = (const int *)(f + 24 * N) + N;
+    for (size_t j = 0; j < N; j++) {
+        size_t p = (size_t)pid[j];
+        for (int k = 0; k < 3; k++) {
+            if (coord) coord[3 * p + k] = (double)f[k * N + j];
+            if (vel) vel[3 * p + k] = (double)f[(3 + k) * N + j];
+        }
+        if (F)
+            for (int k = 0; k < 9; k++) F[9 * p + k] = (double)f[(6 + k) * N + j];
+        if (stress)
+            for (int k = 0; k < 6; k++) stress[6 * p + k] = (double)f[(15 + k) * N + j];
+        if (vol) vol[p] = (double)f[23 * N + j];
+    }
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_download_particles(mpm_ctx *c, double *coord, double *vel, double *F, double *stress, double *vol) {
+    if (!c) return MPM_ERR_BAD_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->num == 0) return MPM_OK;
+    return c->precision == 64 ? dl_particles<double>(c, coord, vel, F, stress, vol)
+                              : dl_particles<float>(c, coord, vel, F, stress, vol);
+}
+
+mpm_status mpm_gpu_get_stats(mpm_ctx *c, mpm_stats *out) {
+    if (!c || !out) return MPM_ERR_BAD_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    DevCtl h;
+    CK(cudaMemcpy(&h, c->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost));
+    int nw = 0;
+    CK(cudaMemcpy(&nw, c->d_nwork, sizeof(int), cudaMemcpyDeviceToHost));
+    out->num = c->num;
+    out->nodec = c->g.nodec;
+    out->steps = c->step;
+    out->resorts = c->resorts;
+    out->kernel_launches = c->launches;
+    out->out_of_box = h.err_oob;
+    out->tile_misses = h.tile_misses;
+    out->ntiles = c->g.ntiles;
+    out->nwork = nw;
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_enable_kernel_timing(mpm_ctx *c, int on) {
+    if (!c) return MPM_ERR_BAD_ARG;
+    c->timer.on = on != 0;
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_kernel_times(mpm_ctx *c, int *count, const char **names, double *ms, int64_t *launches) {
+    if (!c || !count) return MPM_ERR_BAD_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    auto &t = c->timer;
+    for (size_t i = 0; i < t.cls.size(); i++) {
+        float e = 0.0f;
+        cudaEventElapsedTime(&e, t.ev[2 * i], t.ev[2 * i + 1]);
+        t.ms[t.cls[i]] += e;
+        t.launches[t.cls[i]]++;
+        cudaEventDestroy(t.ev[2 * i]);
+        cudaEventDestroy(t.ev[2 * i + 1]);
+    }
+    t.ev.clear();
+    t.cls.clear();
+    int cap = *count, k = 0;
+    for (int i = 0; i < NKCLASS && k < cap; i++) {
+        if (names) names[k] = kClassNames[i];
+        if (ms) ms[k] = t.ms[i];
+        if (launches) launches[k] = t.launches[i];
+        k++;
+    }
+    *count = k;
+    for (int i = 0; i < NKCLASS; i++) {
+        t.ms[i] = 0.0;
+        t.launches[i] = 0;
+    }
+    return MPM_OK;
+}
+
+

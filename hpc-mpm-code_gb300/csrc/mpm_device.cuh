@@ -1,0 +1,195 @@
+// Device-side building blocks: shape functions, fixed-point accumulation,
+// small 3x3 algebra and the constitutive updates.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "mpm_internal.cuh"
+
+namespace mpm {
+
+// ---------------------------------------------------------------------------
+// Shape functions.  Per direction the same closed forms as MakSf
+// (module/shape_function.cpp:39-105): the linear hat 1 - |x - x_i|/dx with
+// gradient +-1/dx, and the open-knot quadratic B-spline with its boundary
+// pieces.  Tensor product ordering: x fastest, then y, then z
+// (module/shape_function.cpp:107-110).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float rdiv(float a, float b, float inv_b) { return a * inv_b; }
+__device__ __forceinline__ double rdiv(double a, double b, double) { return a / b; }
+
+template <typename R, int O>
+struct Axis {
+    R w[O + 1];
+    R dw[O + 1];
+};
+
+template <typename R>
+__device__ __forceinline__ void axis_linear(R x, R xmin, R dx, R inv_dx, int ie, Axis<R, 1> &a) {
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        R xy = xmin + dx * (R)(ie + k);
+        R r = x - xy;
+        a.w[k] = (R)1 - rdiv(fabs(r), dx, inv_dx);
+        a.dw[k] = (r < (R)0) ? inv_dx : -inv_dx;
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ void axis_quadratic(R x, R xmin, R dx, R inv_dx, int ie, int nnc, Axis<R, 2> &a) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        int ncxy = ie + k;
+        R xy = xmin + dx * (R)(ncxy - 2);
+        R h = rdiv(x - xy, dx, inv_dx);
+        R s1, s2, s3, d1, d2;
+        if (ncxy == 0) {
+            h -= (R)2;
+            s1 = 1; s2 = -2; s3 = 1; d1 = 2; d2 = -2;
+        } else if (ncxy == 1) {
+            h -= (R)1;
+            if (h <= (R)1) { s1 = -1.5; s2 = 2; s3 = 0; d1 = -3; d2 = 2; }
+            else { s1 = 0.5; s2 = -2; s3 = 2; d1 = 1; d2 = -2; }
+        } else if (ncxy == nnc - 1) {
+            s1 = 1; s2 = 0; s3 = 0; d1 = 2; d2 = 0;
+        } else if (ncxy == nnc - 2) {
+            if (h <= (R)1) { s1 = 0.5; s2 = 0; s3 = 0; d1 = 1; d2 = 0; }
+            else { s1 = -1.5; s2 = 4; s3 = -2; d1 = -3; d2 = 4; }
+        } else {
+            if (h <= (R)1) { s1 = 0.5; s2 = 0; s3 = 0; d1 = 1; d2 = 0; }
+            else if (h <= (R)2) { s1 = -1; s2 = 3; s3 = -1.5; d1 = -2; d2 = 3; }
+            else { s1 = 0.5; s2 = -3; s3 = 4.5; d1 = 1; d2 = -3; }
+        }
+        a.w[k] = (s1 * h + s2) * h + s3;
+        a.dw[k] = rdiv(d1 * h + d2, dx, inv_dx);
+    }
+}
+
+// Geometry as seen by a kernel, in the kernel's precision.
+template <typename R>
+struct KGeom {
+    R xmin[3], dx[3], inv_dx[3];
+    int nel[3], nnc[3], ntile[3];
+    int nodec;
+};
+
+template <typename R, int O>
+__device__ __forceinline__ void axis_eval(R x, const KGeom<R> &g, int d, int ie, Axis<R, O> &a);
+
+template <>
+__device__ __forceinline__ void axis_eval<float, 1>(float x, const KGeom<float> &g, int d, int ie, Axis<float, 1> &a) {
+    axis_linear<float>(x, g.xmin[d], g.dx[d], g.inv_dx[d], ie, a);
+}
+template <>
+__device__ __forceinline__ void axis_eval<double, 1>(double x, const KGeom<double> &g, int d, int ie,
+                                                     Axis<double, 1> &a) {
+    axis_linear<double>(x, g.xmin[d], g.dx[d], g.inv_dx[d], ie, a);
+}
+template <>
+__device__ __forceinline__ void axis_eval<float, 2>(float x, const KGeom<float> &g, int d, int ie, Axis<float, 2> &a) {
+    axis_quadratic<float>(x, g.xmin[d], g.dx[d], g.inv_dx[d], ie, g.nnc[d], a);
+}
+template <>
+__device__ __forceinline__ void axis_eval<double, 2>(double x, const KGeom<double> &g, int d, int ie,
+                                                     Axis<double, 2> &a) {
+    axis_quadratic<double>(x, g.xmin[d], g.dx[d], g.inv_dx[d], ie, g.nnc[d], a);
+}
+
+// Element index of a point (MeshPointLinklist, module/material_point.cpp:59-65).
+// Out-of-grid points are clamped and reported through *oob.
+template <typename R>
+__device__ __forceinline__ int cell_of(R x, const KGeom<R> &g, int d, bool &oob) {
+    R t = (x - g.xmin[d]) / g.dx[d];
+    int c = (int)floor(t);
+    if (!(t >= (R)0) || c >= g.nel[d]) {   // also catches NaN
+        oob = true;
+        c = c < 0 || !(t >= (R)0) ? 0 : g.nel[d] - 1;
+    }
+    return c;
+}
+
+// ---------------------------------------------------------------------------
+// Fixed-point accumulation.  Every contribution c is scaled by 2^e and
+// rounded to an int64; the sums are exact integers, so the result does not
+// depend on the order in which particles are visited.
+// ---------------------------------------------------------------------------
+__host__ __device__ inline Fix make_fix(double bound) {
+    int e = 0;
+    if (bound > 0.0 && bound < 1.0e300) {
+        int k;
+        frexp(bound, &k);   // bound < 2^k
+        e = 62 - k;         // |sum| <= bound * 2^e < 2^62
+    }
+    if (e > 240) e = 240;
+    if (e < -240) e = -240;
+    Fix f;
+    f.sd = ldexp(1.0, e);
+    f.inv = ldexp(1.0, -e);
+    f.s1 = (float)ldexp(1.0, e / 2);
+    f.s2 = (float)ldexp(1.0, e - e / 2);
+    return f;
+}
+
+__device__ __forceinline__ long long fx(float c, const Fix &f) { return __float2ll_rn((c * f.s1) * f.s2); }
+__device__ __forceinline__ long long fx(double c, const Fix &f) { return __double2ll_rn(c * f.sd); }
+
+__device__ __forceinline__ void atomic_add_i64(unsigned long long *p, long long v) {
+    atomicAdd(p, (unsigned long long)v);
+}
+
+__device__ __forceinline__ float bits_f(unsigned int u) { return __uint_as_float(u); }
+__device__ __forceinline__ void atomic_max_pos(unsigned int *slot, float v) {
+    // v >= 0 (or NaN, mapped to +inf so that the caller's bounds stay safe)
+    if (!(v >= 0.0f)) v = INFINITY;
+    atomicMax(slot, __float_as_uint(v));
+}
+
+// ---------------------------------------------------------------------------
+// Constitutive updates (module/solid/constitutive_model.cpp).
+// D = dt * sum(dN (x) v) is the velocity-gradient increment, i.e. the
+// reference's delta_def_grad minus the identity.
+// ---------------------------------------------------------------------------
+// MatLinElast (constitutive_model.cpp:16-60): incremental, engineering shear.
+template <typename R>
+__device__ __forceinline__ void lin_elast_update(R *s, const R D[3][3], R E, R nu) {
+    R C0 = E * ((R)1 - nu) / (((R)1 - (R)2 * nu) * ((R)1 + nu));
+    R C1 = E * nu / (((R)1 - (R)2 * nu) * ((R)1 + nu));
+    R C2 = E / ((R)2 * ((R)1 + nu));
+    R e0 = D[0][0], e1 = D[1][1], e2 = D[2][2];
+    R e3 = D[1][2] + D[2][1], e4 = D[2][0] + D[0][2], e5 = D[0][1] + D[1][0];
+    s[0] += C0 * e0 + C1 * e1 + C1 * e2;
+    s[1] += C1 * e0 + C0 * e1 + C1 * e2;
+    s[2] += C1 * e0 + C1 * e1 + C0 * e2;
+    s[3] += C2 * e3;
+    s[4] += C2 * e4;
+    s[5] += C2 * e5;
+}
+
+// MatNeoHookean (constitutive_model.cpp:62-125), stress part.
+template <typename R>
+__device__ __forceinline__ void neo_hookean_stress(R *s, const R F[3][3], R jac, R E, R nu) {
+    R lmd = nu * E / (((R)1 + nu) * ((R)1 - (R)2 * nu));
+    R mu = E / ((R)2 * ((R)1 + nu));
+    R lnj = log(jac);
+    R be[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) be[i][j] = F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2];
+    s[0] = (mu * (be[0][0] - (R)1) + lmd * lnj) / jac;
+    s[1] = (mu * (be[1][1] - (R)1) + lmd * lnj) / jac;
+    s[2] = (mu * (be[2][2] - (R)1) + lmd * lnj) / jac;
+    s[3] = (mu * be[1][2]) / jac;
+    s[4] = (mu * be[0][2]) / jac;
+    s[5] = (mu * be[0][1]) / jac;
+}
+
+template <typename R>
+__device__ __forceinline__ R det3(const R a[3][3]) {
+    return a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) + a[0][1] * (a[1][2] * a[2][0] - a[1][0] * a[2][2]) +
+           a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+}
+
+}  // namespace mpm

@@ -1,0 +1,158 @@
+// Internal declarations of the GB300 MPM transfer path.
+//
+// Data layout in HBM
+//   particles: structure of arrays, one array per scalar component, in the
+//     context's precision R (float or double): x[3], v[3], F[9] (row major),
+//     sigma[6] (Voigt xx,yy,zz,yz,xz,xy), m, vol0, vol; plus matid and the
+//     particle's load index (pid).  Two copies exist; a re-sort permutes A
+//     into B and swaps.
+//   grid: node n = i + nx*(j + ny*k) exactly as MakSf numbers control points
+//     (module/shape_function.cpp:28); vector fields component-major.
+//     P2G sums are int64 fixed point, field-major: acc[f*nodec + n].
+//   tiles: 8x8x8 blocks of cells/nodes.  Particles are kept grouped by the
+//     tile of their cell; a "work item" is a chunk of one tile's particles
+//     and is the unit one CTA processes.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "mpm_gpu.h"
+
+namespace mpm {
+
+constexpr int TILE = 8;              // cells per tile edge
+constexpr int CHUNK = 2048;          // max particles per work item
+constexpr int NACC = 8;              // P2G fields: mass, vof, mome xyz, force xyz
+constexpr int NKCLASS = 12;          // kernel classes for timing
+
+enum KernelClass {
+    K_BIN = 0, K_SCAN, K_SCATTER, K_PERMUTE, K_P2G, K_GRID1, K_G2P_MUSL, K_GRID2, K_G2P_UPDATE, K_MISC,
+    K_MATVEC, K_KRYLOV
+};
+
+struct Geom {
+    int nel[3];      // cells
+    int nnc[3];      // control points per direction (nel + order)
+    int order[3];    // 1 or 2
+    int ntile[3];    // tiles per direction (over control points)
+    int ntiles;
+    int nodec;
+    int nelem;
+    double xmin[3], dx[3];
+};
+
+// Bounds that set the fixed-point scales.  Values are non-negative floats
+// stored as their bit patterns so that atomicMax on unsigned int orders them.
+enum BoundSlot { B_VMAX = 0, B_VOLMAX, B_VOLSMAX, B_NB };      // produced for the next step
+enum CurSlot { C_GMAX = 0, C_NEIMAX, C_NC };                    // produced and used within a step
+
+struct DevCtl {
+    unsigned int nxt[2][B_NB];
+    unsigned int cur[C_NC];
+    unsigned long long geup_acc;     // fixed-point sum of |geup|^2
+    double eu_norm;                  // sum nei^2 (deterministic per-tile reduction)
+    unsigned int tile_counter;
+    unsigned int err_oob;
+    unsigned int err_nonfinite;
+    unsigned int tile_misses;
+    double p2g_inv[4];               // 2^-e of the P2G scales (mass, vof, momentum, force) of the last P2G
+};
+
+template <typename R>
+struct Particles {
+    R *x[3], *v[3], *F[9], *s[6], *m, *vol0, *vol;
+    int *matid, *pid;
+};
+
+struct WorkItem {
+    int tile;
+    int begin;
+    int end;
+};
+
+// Fixed-point scale 2^e, applied as two float factors so that e up to +-250
+// never overflows an intermediate.
+struct Fix {
+    float s1, s2;
+    double sd;    // 2^e
+    double inv;   // 2^-e
+};
+
+struct KernelTimer {
+    bool on = false;
+    std::vector<cudaEvent_t> ev;      // pairs
+    std::vector<int> cls;
+    double ms[NKCLASS] = {0};
+    int64_t launches[NKCLASS] = {0};
+};
+
+}  // namespace mpm
+
+struct mpm_ctx {
+    mpm::Geom g;
+    int precision = 32;
+    int scheme = 0;
+    int shifting = 1;
+    int resort_period = 8;
+    double dt = 0, mtol = 0, gravity[3] = {0, 0, 0};
+    double facl = 1.0;
+    int nmat = 0;
+    int npxye[3] = {1, 1, 1};
+    cudaStream_t stream = nullptr;
+    // materials on device
+    int *d_iprop = nullptr;
+    double *d_matprop = nullptr;
+    // particles
+    int64_t num = 0;
+    size_t rsize = 4;
+    void *pbuf[2] = {nullptr, nullptr};   // two SoA copies
+    int cur = 0;
+    double mmax = 0.0;
+    // grid
+    unsigned long long *d_acc = nullptr;   // NACC * nodec int64 P2G sums
+    unsigned long long *d_acc2 = nullptr;  // 3 * nodec int64 MUSL momentum
+    void *d_nodal = nullptr;               // R: gather field G (3), nei (1), nvel2 (3), nvel (3), naccel (3)
+    double *d_nvol = nullptr;              // nodal reference volume (FP64)
+    unsigned char *d_bcflag = nullptr;     // bit c: component c constrained
+    void *d_bcval = nullptr;               // R[3*nodec] prescribed values
+    unsigned char *d_tileflag = nullptr;
+    double *d_eu_part = nullptr;
+    // sorting
+    int *d_key = nullptr, *d_perm = nullptr, *d_tcount = nullptr, *d_tstart = nullptr, *d_tcursor = nullptr;
+    mpm::WorkItem *d_work = nullptr;
+    int *d_nwork = nullptr;
+    int nwork_cap = 0;
+    int nwork = 0;
+    mpm::DevCtl *d_ctl = nullptr;
+    mpm::DevCtl *h_ctl = nullptr;          // pinned mirror
+    // state
+    int64_t step = 0;
+    int64_t resorts = 0;
+    int64_t launches = 0;
+    int64_t steps_since_sort = 1 << 30;
+    int stage = 0;   // 0 idle, 1 after p2g, 2 after grid update
+    bool accum_dirty = false;
+    bool write_nodal_dl = false;
+    mpm_status latched = MPM_OK;
+    mpm::KernelTimer timer;
+    std::vector<int> bc_nodes[3];
+    std::vector<double> bc_vals[3];
+};
+
+namespace mpm {
+// mpm_sort.cu
+mpm_status sort_particles(mpm_ctx *c);
+// mpm_explicit.cu
+mpm_status run_p2g(mpm_ctx *c, double facl);
+mpm_status run_grid1(mpm_ctx *c, int mode);
+mpm_status run_g2p(mpm_ctx *c);
+mpm_status compute_nodal_volume(mpm_ctx *c);
+// timing helpers (mpm_ctx.cu)
+void timer_begin(mpm_ctx *c, int cls);
+void timer_end(mpm_ctx *c, int cls);
+mpm_status check_launch(mpm_ctx *c);
+}  // namespace mpm

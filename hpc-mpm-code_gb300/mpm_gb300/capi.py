@@ -1,0 +1,218 @@
+"""ctypes binding of the C ABI in include/mpm_gpu.h (libmpm_gb300.so).
+
+This is the binding a Python caller of the reference-facing API uses; the
+tests and bench.py call the CUDA path through it.  There is no CPU fallback:
+if the library is missing or a call fails, an exception is raised.
+
+``GpuSolid`` keeps the reference's operator names (module/material_point.h,
+module/solid/solid_material_point.h): ``MeshPointLinklist`` +
+``Particle2Node`` -> ``p2g``, ``SolveSolid`` -> ``grid_update``,
+``Node2Particle`` -> ``g2p``; ``steps`` runs the fused explicit step.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+MPM_PIC, MPM_FLIP = 0, 1
+STATUS = {0: "ok", 1: "bad argument", 2: "out of device memory", 3: "non-finite particle state",
+          4: "particle outside the grid", 5: "Krylov iteration limit", 6: "device wait timed out", 7: "CUDA error",
+          8: "call out of order", 9: "unsupported configuration"}
+
+
+class MpmError(RuntimeError):
+    def __init__(self, code, where):
+        super().__init__(f"{where}: {STATUS.get(code, code)} (status {code})")
+        self.code = code
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("xyelem", C.c_int * 3), ("xymin", C.c_double * 3), ("dxy", C.c_double * 3),
+                ("idimc", C.c_int * 3), ("npxye", C.c_int * 3)]
+
+
+class MaterialDesc(C.Structure):
+    _fields_ = [("nmat", C.c_int), ("iprop", C.POINTER(C.c_int)), ("mat_prop", C.POINTER(C.c_double))]
+
+
+class Config(C.Structure):
+    _fields_ = [("dt", C.c_double), ("mtol", C.c_double), ("gravity", C.c_double * 3), ("scheme", C.c_int),
+                ("precision", C.c_int), ("shifting", C.c_int), ("resort_period", C.c_int),
+                ("reserved", C.c_int * 8)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("num", C.c_int64), ("nodec", C.c_int64), ("steps", C.c_int64), ("resorts", C.c_int64),
+                ("kernel_launches", C.c_int64), ("out_of_box", C.c_int64), ("tile_misses", C.c_int64),
+                ("ntiles", C.c_int32), ("nwork", C.c_int32)]
+
+
+_lib = None
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_status_string",
+           "mpm_gpu_load_particles", "mpm_gpu_set_bc", "mpm_gpu_p2g", "mpm_gpu_grid_update", "mpm_gpu_g2p",
+           "mpm_gpu_step_explicit", "mpm_gpu_download_nodal", "mpm_gpu_download_particles", "mpm_gpu_sync",
+           "mpm_gpu_get_stats", "mpm_gpu_enable_kernel_timing", "mpm_gpu_kernel_times"]
+
+
+def load(path: str | None = None):
+    """Load libmpm_gb300.so (building it in-tree first if absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        _build.build()
+    lib = C.CDLL(path)
+    lib.mpm_gpu_create.argtypes = [C.POINTER(GridDesc), C.POINTER(MaterialDesc), C.POINTER(Config),
+                                   C.POINTER(C.c_void_p)]
+    lib.mpm_gpu_destroy.argtypes = [C.c_void_p]
+    lib.mpm_gpu_destroy.restype = None
+    lib.mpm_gpu_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+    lib.mpm_gpu_status_string.restype = C.c_char_p
+    lib.mpm_gpu_status_string.argtypes = [C.c_int]
+    lib.mpm_gpu_load_particles.argtypes = [C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
+    lib.mpm_gpu_set_bc.argtypes = [C.c_void_p, C.c_int, C.c_int, _ip, _dp]
+    lib.mpm_gpu_p2g.argtypes = [C.c_void_p, C.c_double]
+    lib.mpm_gpu_grid_update.argtypes = [C.c_void_p]
+    lib.mpm_gpu_g2p.argtypes = [C.c_void_p]
+    lib.mpm_gpu_step_explicit.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    lib.mpm_gpu_download_nodal.argtypes = [C.c_void_p, C.c_int, _dp]
+    lib.mpm_gpu_download_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
+    lib.mpm_gpu_sync.argtypes = [C.c_void_p]
+    lib.mpm_gpu_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
+    lib.mpm_gpu_enable_kernel_timing.argtypes = [C.c_void_p, C.c_int]
+    lib.mpm_gpu_kernel_times.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_char_p), _dp,
+                                         C.POINTER(C.c_int64)]
+    _lib = lib
+    return lib
+
+
+def _chk(code, where):
+    if code != 0:
+        raise MpmError(code, where)
+
+
+def _d(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a, ty=_dp):
+    return None if a is None else a.ctypes.data_as(ty)
+
+
+NODAL = {"nmass": (0, 1), "nvof": (1, 1), "nmome": (2, 3), "nforce": (3, 3), "nvel": (4, 3), "naccel": (5, 3),
+         "nvol": (6, 1)}
+
+
+class GpuSolid:
+    """One explicit solid on the GPU, built from a scene (mpm_gb300.scenes.Scene)."""
+
+    def __init__(self, scene, precision=32, shifting=True, resort_period=0, stream=None):
+        self.lib = lib = load()
+        self.scene = s = scene
+        g = GridDesc((C.c_int * 3)(*s.xyelem), (C.c_double * 3)(*s.xymin), (C.c_double * 3)(*s.dxy),
+                     (C.c_int * 3)(*s.idimc), (C.c_int * 3)(*s.npxye))
+        self._iprop = np.ascontiguousarray(s.iprop, dtype=np.int32)
+        self._mat = np.ascontiguousarray(s.mat_prop, dtype=np.float64).ravel()
+        m = MaterialDesc(len(self._iprop), self._iprop.ctypes.data_as(_ip), self._mat.ctypes.data_as(_dp))
+        cfg = Config(s.dt, s.mtol, (C.c_double * 3)(*s.gravity), s.scheme, precision, int(shifting),
+                     int(resort_period), (C.c_int * 8)())
+        h = C.c_void_p()
+        _chk(lib.mpm_gpu_create(C.byref(g), C.byref(m), C.byref(cfg), C.byref(h)), "mpm_gpu_create")
+        self.ctx = h
+        self.nodec = s.nodec
+        self.precision = precision
+        if stream is not None:
+            _chk(lib.mpm_gpu_set_stream(self.ctx, C.c_void_p(stream)), "mpm_gpu_set_stream")
+        self.load(s.coord, s.vel, s.mass, s.vol0, matid=s.matid)
+        for comp, nodes, vals in s.bcs:
+            self.set_bc(comp, nodes, vals)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.mpm_gpu_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- set-up ---------------------------------------------------------------
+    def load(self, coord, vel, mass, vol0, F=None, stress=None, matid=None):
+        coord, vel, mass, vol0, F, stress = map(_d, (coord, vel, mass, vol0, F, stress))
+        matid = None if matid is None else np.ascontiguousarray(matid, dtype=np.int32)
+        n = mass.shape[0]
+        self.num = n
+        _chk(self.lib.mpm_gpu_load_particles(self.ctx, n, _ptr(coord), _ptr(vel), _ptr(mass), _ptr(vol0), _ptr(F),
+                                             _ptr(stress), _ptr(matid, _ip)), "mpm_gpu_load_particles")
+
+    def set_bc(self, comp, nodes, vals):
+        nodes = np.ascontiguousarray(nodes, dtype=np.int32)
+        vals = _d(vals)
+        _chk(self.lib.mpm_gpu_set_bc(self.ctx, comp, len(nodes), _ptr(nodes, _ip), _ptr(vals)), "mpm_gpu_set_bc")
+
+    def set_stream(self, stream_handle):
+        _chk(self.lib.mpm_gpu_set_stream(self.ctx, C.c_void_p(stream_handle)), "mpm_gpu_set_stream")
+
+    # -- reference operator names -------------------------------------------
+    def p2g(self, facl=1.0):
+        _chk(self.lib.mpm_gpu_p2g(self.ctx, facl), "mpm_gpu_p2g")
+
+    def grid_update(self):
+        _chk(self.lib.mpm_gpu_grid_update(self.ctx), "mpm_gpu_grid_update")
+
+    def g2p(self):
+        _chk(self.lib.mpm_gpu_g2p(self.ctx), "mpm_gpu_g2p")
+
+    Particle2Node = p2g
+    SolveSolid = grid_update
+    Node2Particle = g2p
+
+    def steps(self, n, facl=1.0):
+        _chk(self.lib.mpm_gpu_step_explicit(self.ctx, n, facl), "mpm_gpu_step_explicit")
+
+    def sync(self):
+        _chk(self.lib.mpm_gpu_sync(self.ctx), "mpm_gpu_sync")
+
+    # -- results ----------------------------------------------------------------
+    def nodal(self, name):
+        fid, ncomp = NODAL[name]
+        out = np.zeros(self.nodec * ncomp)
+        _chk(self.lib.mpm_gpu_download_nodal(self.ctx, fid, _ptr(out)), "mpm_gpu_download_nodal")
+        return out.reshape(ncomp, self.nodec) if ncomp == 3 else out
+
+    def particles(self):
+        n = self.num
+        x, v, F, sig, vol = (np.zeros(n * 3), np.zeros(n * 3), np.zeros(n * 9), np.zeros(n * 6), np.zeros(n))
+        _chk(self.lib.mpm_gpu_download_particles(self.ctx, _ptr(x), _ptr(v), _ptr(F), _ptr(sig), _ptr(vol)),
+             "mpm_gpu_download_particles")
+        return {"x": x.reshape(n, 3), "v": v.reshape(n, 3), "F": F.reshape(n, 3, 3), "sigma": sig.reshape(n, 6),
+                "vol": vol}
+
+    def stats(self):
+        st = Stats()
+        _chk(self.lib.mpm_gpu_get_stats(self.ctx, C.byref(st)), "mpm_gpu_get_stats")
+        return {k: getattr(st, k) for k, _ in Stats._fields_}
+
+    def enable_kernel_timing(self, on=True):
+        _chk(self.lib.mpm_gpu_enable_kernel_timing(self.ctx, int(on)), "mpm_gpu_enable_kernel_timing")
+
+    def kernel_times(self):
+        cap = 16
+        cnt = C.c_int(cap)
+        names = (C.c_char_p * cap)()
+        ms = (C.c_double * cap)()
+        launches = (C.c_int64 * cap)()
+        _chk(self.lib.mpm_gpu_kernel_times(self.ctx, C.byref(cnt), names, ms, launches), "mpm_gpu_kernel_times")
+        return {names[i].decode(): (ms[i], launches[i]) for i in range(cnt.value)}

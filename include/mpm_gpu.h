@@ -1,0 +1,147 @@
+/*
+ * mpm_gpu.h -- C ABI of the GB300 MPM transfer path (libmpm_gb300.so).
+ *
+ * The reference (HPC-MPM-Code) has no FFI layer: its operator surface is the
+ * C++ member functions of MaterialPoint / SolidMaterialPointBase and the
+ * module globals.  Each entry point below replaces one of those calls; the
+ * C++ shim in hpc-mpm-code_gb300/host/ re-exposes them with the reference's
+ * own names (Particle2Node / SolveSolid / Node2Particle).
+ *
+ * Conventions
+ *   - Plain pointers and sizes only.  Host arrays are FP64 and laid out like
+ *     the reference: particle vectors AoS (coord[3*p+i]), F row-major
+ *     (F[9*p+3*i+j]), Voigt stress [xx,yy,zz,yz,xz,xy] (stress[6*p+k]),
+ *     nodal vectors component-major with the u/v/w blocks at offsets
+ *     0, nodec, 2*nodec (module/data_io.cpp:53-56).
+ *   - Every call returns an mpm_status; nothing aborts the process or traps
+ *     the GPU.  Device-side problems (non-finite values, particles leaving
+ *     the grid, solver limits) are latched in the context and returned by the
+ *     next synchronising call.
+ *   - One context per host thread; calls are ordered on the context's CUDA
+ *     stream (mpm_gpu_set_stream).  The caller owns host memory; the context
+ *     owns all device memory.
+ */
+#ifndef MPM_GPU_H
+#define MPM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MPM_OK = 0,
+    MPM_ERR_BAD_ARG = 1,
+    MPM_ERR_OOM = 2,
+    MPM_ERR_NONFINITE = 3,
+    MPM_ERR_PARTICLE_OUT_OF_BOX = 4,
+    MPM_ERR_KRYLOV_MAXIT = 5,
+    MPM_ERR_DEVICE_TIMEOUT = 6,
+    MPM_ERR_CUDA = 7,
+    MPM_ERR_STATE = 8,
+    MPM_ERR_UNSUPPORTED = 9
+} mpm_status;
+
+typedef enum { MPM_PIC = 0, MPM_FLIP = 1 } mpm_scheme;  /* MapScheme, module/dataset.h:19 */
+
+typedef struct mpm_ctx mpm_ctx;
+
+/* Grid header of one rank: InputParaGriddata (module/data_io.cpp:31-125) and
+ * datain_para (work/src_solid/explicit/datain_para.cpp:43-90). */
+typedef struct {
+    int xyelem[3];    /* cells per direction (xyelem) */
+    double xymin[3];  /* grid origin (xymin) */
+    double dxy[3];    /* cell size (dxy) */
+    int idimc[3];     /* shape order per direction: 1 linear, 2 quadratic B-spline (idimc) */
+    int npxye[3];     /* particles per cell per direction, for the nodal volume (npxye) */
+} mpm_grid_desc;
+
+/* Material table: iprop[nmat] (-1 rigid, 0 linear elastic, 1 Neo-Hookean)
+ * and mat_prop[3*nmat] = {E, nu, spare} (module/dataset.h:13-14). */
+typedef struct {
+    int nmat;
+    const int *iprop;
+    const double *mat_prop;
+} mpm_material_desc;
+
+typedef struct {
+    double dt;          /* time step (dt) */
+    double mtol;        /* mass tolerance (mtol) */
+    double gravity[3];  /* body force per unit mass (bb) */
+    int scheme;         /* MPM_PIC or MPM_FLIP (solswitch) */
+    int precision;      /* 32: FP32 particle/grid arithmetic; 64: FP64 */
+    int shifting;       /* 1: DeltaCorrectionParticleShifting as the reference; 0: off */
+    int resort_period;  /* physical re-sort of particles by tile every N steps (>= 1); 0 = default */
+    int reserved[8];
+} mpm_config;
+
+/* ---- lifetime ------------------------------------------------------------
+ * Replaces the grid set-up of the drivers: BuildMesh / BuildControlPoint /
+ * MakNodalVol (module/mesh.cpp:56,105,160) and the globals in dataset.h /
+ * mesh.h. */
+mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *mat, const mpm_config *cfg,
+                          mpm_ctx **out);
+void mpm_gpu_destroy(mpm_ctx *ctx);
+/* stream: a cudaStream_t (as void*); NULL selects the legacy default stream. */
+mpm_status mpm_gpu_set_stream(mpm_ctx *ctx, void *stream);
+const char *mpm_gpu_status_string(mpm_status s);
+
+/* ---- particles and boundary conditions ------------------------------------
+ * Replaces SolidMaterialPointBase::InputPointData (module/solid/solid_data_io.cpp:13-36):
+ * vel, F, stress and matid may be NULL (zero, identity, zero, material 0). */
+mpm_status mpm_gpu_load_particles(mpm_ctx *ctx, int64_t n, const double *coord, const double *vel,
+                                  const double *mass, const double *vol0, const double *F, const double *stress,
+                                  const int *matid);
+/* Replaces BoundaryCondition::BCInput for ubc/vbc/wbc (module/bc.cpp:9-27):
+ * comp 0/1/2 = u/v/w, node ids and prescribed values (applied x facl). */
+mpm_status mpm_gpu_set_bc(mpm_ctx *ctx, int comp, int n, const int *nodes, const double *vals);
+
+/* ---- the explicit transfer path -------------------------------------------
+ * mpm_gpu_p2g          MeshPointLinklist + Particle2NodeS
+ *                      (module/material_point.cpp:52, module/solid/explicit/var_trans_solid_explicit.cpp:20-99)
+ * mpm_gpu_grid_update  SolveSolid (module/solid/explicit/solve_solid_explicit.cpp:8-31)
+ * mpm_gpu_g2p          Node2ParticleS + MUSL + update_point_coord_and_stress
+ *                      (module/solid/explicit/var_trans_solid_explicit.cpp:101-311)
+ * mpm_gpu_step_explicit  nsteps x (p2g, grid_update, g2p), fused: the hot path
+ *                      (work/src_solid/explicit/main.cpp:39-73). */
+mpm_status mpm_gpu_p2g(mpm_ctx *ctx, double facl);
+mpm_status mpm_gpu_grid_update(mpm_ctx *ctx);
+mpm_status mpm_gpu_g2p(mpm_ctx *ctx);
+mpm_status mpm_gpu_step_explicit(mpm_ctx *ctx, int nsteps, double facl);
+
+/* ---- results ----------------------------------------------------------------
+ * field: 0 nmass, 1 nvof, 2 nmome, 3 nforce, 4 nvel, 5 naccel, 6 nvol
+ * (MaterialPoint members, module/material_point.h:151-153; nvol from mesh.h).
+ * Vectors are written component-major (3*nodec). Synchronises the stream. */
+mpm_status mpm_gpu_download_nodal(mpm_ctx *ctx, int field, double *host);
+/* Particles in the order they were loaded; any pointer may be NULL. */
+mpm_status mpm_gpu_download_particles(mpm_ctx *ctx, double *coord, double *vel, double *F, double *stress,
+                                      double *vol);
+/* Wait for the stream and return (and clear) any latched device error. */
+mpm_status mpm_gpu_sync(mpm_ctx *ctx);
+
+typedef struct {
+    int64_t num;            /* particles */
+    int64_t nodec;          /* control points */
+    int64_t steps;          /* explicit steps taken */
+    int64_t resorts;        /* physical re-sorts done */
+    int64_t kernel_launches;/* kernels launched by this context */
+    int64_t out_of_box;     /* particles found outside the grid (clamped) */
+    int64_t tile_misses;    /* particles scattered outside their tile's staging box, last step */
+    int32_t ntiles;
+    int32_t nwork;
+} mpm_stats;
+mpm_status mpm_gpu_get_stats(mpm_ctx *ctx, mpm_stats *out);
+
+/* Per-kernel device time, accumulated between calls of this function with
+ * CUDA events recorded on the context's stream around each kernel class
+ * (enabled by mpm_gpu_enable_kernel_timing).  names[i] / ms[i] / launches[i]
+ * for i < *count (count in: capacity).  Synchronises the stream. */
+mpm_status mpm_gpu_enable_kernel_timing(mpm_ctx *ctx, int on);
+mpm_status mpm_gpu_kernel_times(mpm_ctx *ctx, int *count, const char **names, double *ms, int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

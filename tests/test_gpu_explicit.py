@@ -1,0 +1,140 @@
+"""Parity of the CUDA explicit path (through the C ABI) with the reference.
+
+Tolerances (relative L2 over the whole field):
+  FP64 mode vs the reference's own outputs / the C oracle: 1e-10
+  FP32 mode vs the FP64 oracle: 1e-5 on P2G sums, 1e-4 on particle state
+The P2G sums are int64 fixed point, so FP32 results are bitwise independent
+of particle order and of the re-sort schedule.
+"""
+import numpy as np
+import pytest
+
+from helpers import load_golden, rel_l2, scene_from_golden
+from mpm_gb300 import capi, scenes
+from oracle import port
+
+pytestmark = pytest.mark.gpu
+
+EXPLICIT = ["explicit_pic", "explicit_flip", "explicit_quadratic", "explicit_neohookean"]
+P2G_FIELDS = ("nmass", "nvof", "nmome", "nforce", "nvel", "naccel", "nvol")
+PARTICLE_FIELDS = ("x", "v", "F", "sigma", "vol")
+
+
+def particle_err(p, ref, prefix=""):
+    return {k: rel_l2(p[k], ref[prefix + k]) for k in PARTICLE_FIELDS}
+
+
+@pytest.mark.parametrize("name", EXPLICIT)
+def test_p2g_fp64_matches_reference(name):
+    g = load_golden(name)
+    gpu = capi.GpuSolid(scene_from_golden(g), precision=64)
+    gpu.p2g(float(g["facl"]))
+    gpu.grid_update()
+    for f in P2G_FIELDS:
+        assert rel_l2(gpu.nodal(f), g[f"p2g_{f}"]) <= 1e-12, f
+    gpu.sync()
+
+
+@pytest.mark.parametrize("name", EXPLICIT)
+def test_steps_fp64_match_reference(name):
+    g = load_golden(name)
+    gpu = capi.GpuSolid(scene_from_golden(g), precision=64)
+    gpu.steps(1, float(g["facl"]))
+    e1 = particle_err(gpu.particles(), g, "step1_")
+    gpu.steps(int(g["nsteps"]) - 1, float(g["facl"]))
+    eN = particle_err(gpu.particles(), g, "stepN_")
+    gpu.sync()
+    assert max(e1.values()) <= 1e-12, e1
+    assert max(eN.values()) <= 1e-10, eN
+
+
+@pytest.mark.parametrize("name", EXPLICIT)
+def test_steps_fp32_within_tolerance(name):
+    g = load_golden(name)
+    gpu = capi.GpuSolid(scene_from_golden(g), precision=32)
+    gpu.p2g(float(g["facl"]))
+    gpu.grid_update()
+    for f in ("nmass", "nvof", "nmome", "nforce"):
+        assert rel_l2(gpu.nodal(f), g[f"p2g_{f}"]) <= 1e-5, f
+    gpu.g2p()
+    gpu.steps(int(g["nsteps"]) - 1, float(g["facl"]))
+    e = particle_err(gpu.particles(), g, "stepN_")
+    gpu.sync()
+    assert e["x"] <= 1e-6 and e["v"] <= 1e-4 and e["F"] <= 1e-5 and e["vol"] <= 1e-5, e
+    assert e["sigma"] <= 1e-3, e
+
+
+def test_fine_grained_calls_equal_fused_step():
+    g = load_golden("explicit_pic")
+    a = capi.GpuSolid(scene_from_golden(g), precision=32)
+    b = capi.GpuSolid(scene_from_golden(g), precision=32)
+    for _ in range(3):
+        a.Particle2Node(1.0)
+        a.SolveSolid()
+        a.Node2Particle()
+    b.steps(3, 1.0)
+    pa, pb = a.particles(), b.particles()
+    for k in PARTICLE_FIELDS:
+        assert np.array_equal(pa[k], pb[k]), k
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_results_independent_of_sort_schedule(precision):
+    s = scenes.spinning_block(grid=(40, 40, 40), cell_lo=(8, 8, 8), cells=(24, 24, 24), dt=2e-5)
+    runs = []
+    for period in (1, 3, 1000):
+        gpu = capi.GpuSolid(s, precision=precision, resort_period=period)
+        gpu.steps(12)
+        runs.append(gpu.particles())
+        gpu.sync()
+    for k in PARTICLE_FIELDS:
+        assert np.array_equal(runs[0][k], runs[1][k]), k
+        assert np.array_equal(runs[0][k], runs[2][k]), k
+
+
+def test_elastic_block_64k_fp64_vs_oracle():
+    """The 64,000-particle elastic block (32^3 grid, gravity, fixed bottom)."""
+    s = scenes.elastic_block()
+    o = port.PortSolid(s)
+    gpu = capi.GpuSolid(s, precision=64)
+    o.steps(20)
+    gpu.steps(20)
+    e = particle_err(gpu.particles(), o.particles())
+    gpu.sync()
+    assert max(e.values()) <= 1e-10, e
+
+
+def test_spinning_block_fp32_vs_fp64_oracle():
+    """A 262k-particle version of the 4.1M-particle case (same dx, dt, density, rotation, compressed quarter)."""
+    s = scenes.spinning_block(grid=(48, 48, 48), cell_lo=(8, 8, 8), cells=(32, 32, 32))
+    o = port.PortSolid(s)
+    gpu = capi.GpuSolid(s, precision=32)
+    o.steps(50)
+    gpu.steps(50)
+    e = particle_err(gpu.particles(), o.particles())
+    gpu.sync()
+    assert e["v"] <= 1e-4 and e["x"] <= 1e-6, e
+
+
+def test_full_size_conservation_and_determinism():
+    """4,096,000 particles: P2G conserves mass exactly and momentum to rounding; two runs agree bitwise."""
+    s = scenes.spinning_block()
+    gpu = capi.GpuSolid(s, precision=32)
+    gpu.p2g()
+    gpu.grid_update()
+    m = gpu.nodal("nmass").sum()
+    assert abs(m - s.mass.astype(np.float32).astype(np.float64).sum()) <= 1e-6 * m
+    p = gpu.nodal("nmome").sum(axis=1)
+    pm = (s.mass[:, None] * s.vel).sum(axis=0)
+    assert np.abs(p - pm).max() <= 1e-5 * np.abs(s.mass[:, None] * s.vel).sum()
+    gpu.g2p()
+    gpu.steps(5)
+    a = gpu.particles()
+    gpu2 = capi.GpuSolid(s, precision=32, resort_period=2)
+    gpu2.steps(6)
+    b = gpu2.particles()
+    for k in PARTICLE_FIELDS:
+        assert np.array_equal(a[k], b[k]), k
+    st = gpu.stats()
+    assert st["out_of_box"] == 0
+    gpu.sync()
