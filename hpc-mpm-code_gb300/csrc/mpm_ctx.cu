@@ -61,9 +61,11 @@ static void free_particles(mpm_ctx *c) {
     free_dev(c->pbuf[1]);
     free_dev(c->d_key);
     free_dev(c->d_perm);
+    free_dev(c->d_tmp);
+    free_dev(c->d_perm2);
     free_dev(c->d_work);
     c->pbuf[0] = c->pbuf[1] = nullptr;
-    c->d_key = c->d_perm = nullptr;
+    c->d_key = c->d_perm = c->d_tmp = c->d_perm2 = nullptr;
     c->d_work = nullptr;
     c->num = 0;
 }
@@ -128,11 +130,16 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     g.nodec = (int)nodec;
     g.nelem = g.nel[0] * g.nel[1] * g.nel[2];
     g.ntiles = g.ntile[0] * g.ntile[1] * g.ntile[2];
+    g.nbrick[0] = (g.nel[0] + BRX - 1) / BRX;
+    g.nbrick[1] = (g.nel[1] + BRY - 1) / BRY;
+    g.nbrick[2] = (g.nel[2] + BRZ - 1) / BRZ;
+    g.nbricks = g.nbrick[0] * g.nbrick[1] * g.nbrick[2];
     c->precision = cfg->precision;
     c->rsize = cfg->precision == 64 ? 8 : 4;
     c->scheme = cfg->scheme;
     c->shifting = cfg->shifting ? 1 : 0;
     c->resort_period = cfg->resort_period > 0 ? cfg->resort_period : 8;
+    c->cell_scatter = cfg->scatter == 1 ? 0 : 1;
     c->dt = cfg->dt;
     c->mtol = cfg->mtol;
     c->nmat = mat->nmat;
@@ -153,9 +160,10 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     alloc(&c->d_bcval, c->rsize * 3 * N);
     alloc((void **)&c->d_tileflag, g.ntiles);
     alloc((void **)&c->d_eu_part, sizeof(double) * g.ntiles);
-    alloc((void **)&c->d_tcount, sizeof(int) * g.ntiles);
-    alloc((void **)&c->d_tstart, sizeof(int) * g.ntiles);
-    alloc((void **)&c->d_tcursor, sizeof(int) * g.ntiles);
+    alloc((void **)&c->d_tcount, sizeof(int) * g.nbricks);
+    alloc((void **)&c->d_tstart, sizeof(int) * (g.nbricks + 1));
+    alloc((void **)&c->d_tcursor, sizeof(int) * g.nbricks);
+    alloc((void **)&c->d_cstart, sizeof(int) * (size_t)g.nbricks * (BRC + 1));
     alloc((void **)&c->d_nwork, sizeof(int));
     alloc((void **)&c->d_ctl, sizeof(DevCtl));
     if (st == MPM_OK && cudaMallocHost((void **)&c->h_ctl, sizeof(DevCtl)) != cudaSuccess) st = MPM_ERR_OOM;
@@ -172,8 +180,9 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     cudaMemset(c->d_bcval, 0, c->rsize * 3 * N);
     cudaMemset(c->d_tileflag, 0, g.ntiles);
     cudaMemset(c->d_eu_part, 0, sizeof(double) * g.ntiles);
-    cudaMemset(c->d_tcount, 0, sizeof(int) * g.ntiles);
-    cudaMemset(c->d_tcursor, 0, sizeof(int) * g.ntiles);
+    cudaMemset(c->d_tcount, 0, sizeof(int) * g.nbricks);
+    cudaMemset(c->d_tcursor, 0, sizeof(int) * g.nbricks);
+    cudaMemset(c->d_cstart, 0, sizeof(int) * (size_t)g.nbricks * (BRC + 1));
     cudaMemset(c->d_nwork, 0, sizeof(int));
     cudaMemset(c->d_ctl, 0, sizeof(DevCtl));
     memset(c->h_ctl, 0, sizeof(DevCtl));
@@ -203,6 +212,7 @@ void mpm_gpu_destroy(mpm_ctx *c) {
     free_dev(c->d_tcount);
     free_dev(c->d_tstart);
     free_dev(c->d_tcursor);
+    free_dev(c->d_cstart);
     free_dev(c->d_nwork);
     free_dev(c->d_ctl);
     if (c->h_ctl) cudaFreeHost(c->h_ctl);
@@ -284,7 +294,9 @@ mpm_status mpm_gpu_load_particles(mpm_ctx *c, int64_t n, const double *coord, co
     CK(cudaMalloc(&c->pbuf[1], bytes));
     CK(cudaMalloc((void **)&c->d_key, sizeof(int) * N));
     CK(cudaMalloc((void **)&c->d_perm, sizeof(int) * N));
-    c->nwork_cap = c->g.ntiles + (int)(N / CHUNK) + 1;
+    CK(cudaMalloc((void **)&c->d_tmp, sizeof(int) * N));
+    CK(cudaMalloc((void **)&c->d_perm2, sizeof(int) * N));
+    c->nwork_cap = c->g.nbricks + (int)(N / CHUNK) + 1;
     CK(cudaMalloc((void **)&c->d_work, sizeof(WorkItem) * c->nwork_cap));
     c->cur = 0;
     mpm_status s = c->precision == 64 ? upload_particles<double>(c, n, coord, vel, mass, vol0, F, stress, matid)
@@ -502,7 +514,7 @@ mpm_status mpm_gpu_get_stats(mpm_ctx *c, mpm_stats *out) {
     out->kernel_launches = c->launches;
     out->out_of_box = h.err_oob;
     out->tile_misses = h.tile_misses;
-    out->ntiles = c->g.ntiles;
+    out->ntiles = c->g.nbricks;
     out->nwork = nw;
     return MPM_OK;
 }

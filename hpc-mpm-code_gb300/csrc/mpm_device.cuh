@@ -129,11 +129,16 @@ __host__ __device__ inline Fix make_fix(double bound) {
     f.inv = ldexp(1.0, -e);
     f.s1 = (float)ldexp(1.0, e / 2);
     f.s2 = (float)ldexp(1.0, e - e / 2);
+    f.i1 = (float)ldexp(1.0, -(e / 2));
+    f.i2 = (float)ldexp(1.0, -(e - e / 2));
     return f;
 }
 
 __device__ __forceinline__ long long fx(float c, const Fix &f) { return __float2ll_rn((c * f.s1) * f.s2); }
 __device__ __forceinline__ long long fx(double c, const Fix &f) { return __double2ll_rn(c * f.sd); }
+// fixed point back to the working precision
+__device__ __forceinline__ float unfx(long long q, const Fix &f, float) { return (__ll2float_rn(q) * f.i1) * f.i2; }
+__device__ __forceinline__ double unfx(long long q, const Fix &f, double) { return (double)q * f.inv; }
 
 __device__ __forceinline__ void atomic_add_i64(unsigned long long *p, long long v) {
     atomicAdd(p, (unsigned long long)v);

@@ -2,16 +2,30 @@
 // the MUSL re-projection, and the position / deformation / stress update.
 //
 // One explicit step (the sequence of work/src_solid/explicit/main.cpp:39-73):
-//   k_p2g         Particle2NodeS scatter  (var_trans_solid_explicit.cpp:35-70)
+//   p2g           Particle2NodeS scatter  (module/solid/explicit/var_trans_solid_explicit.cpp:35-70)
 //   k_grid1       nvel = p/m + BC, SolveSolid a = f/m + BC, PIC v* = v + dt a,
-//                 shifting nei and sum nei^2       (..:77-96, solve_solid_explicit.cpp:8-31,
-//                 var_trans_solid_explicit.cpp:194-200, material_point.cpp:179-185)
-//   k_g2p_musl    particle velocity gather, MUSL momentum re-scatter, |geup|^2
+//                 shifting nei and sum nei^2   (var_trans_solid_explicit.cpp:77-96,
+//                 solve_solid_explicit.cpp:8-31, var_trans_solid_explicit.cpp:194-200,
+//                 module/material_point.cpp:179-185)
+//   g2p_musl      particle velocity gather, MUSL momentum re-scatter, |geup|^2
 //                 (var_trans_solid_explicit.cpp:211-240,101-129, material_point.cpp:192-217)
-//   k_grid2       MUSL nvel = p/m + BC, clears the accumulators (..:131-146)
+//   k_grid2       MUSL nvel = p/m + BC, shifting b0, clears the accumulators
+//                 (var_trans_solid_explicit.cpp:131-146, material_point.cpp:219)
 //   k_g2p_update  F update, position update + shift, vol = J vol0, stress
-//                 (..:247-296,150-185)
+//                 (var_trans_solid_explicit.cpp:247-296,150-185)
+//
+// Two scatter formulations:
+//   * FP32 with linear shape functions (8 nodes per particle): one thread per
+//     cell of a 4x4x8-cell brick.  Particles are sorted by (brick, cell, load
+//     index), so a thread sums its cell's particles into FP32 registers in a
+//     fixed order, writes them to shared memory as cell corners, and a node
+//     pass adds the 8 corners of each node in a fixed order before one int64
+//     fixed-point RED per node and field.  Runs are bitwise reproducible.
+//   * FP64, and quadratic B-splines: particles of a brick chunk convert every
+//     contribution to int64 fixed point and scatter into a shared staging box
+//     with atomics; the sums are exact and independent of particle order.
 #include <cstdio>
+#include <cstring>
 
 #include "mpm_device.cuh"
 
@@ -21,8 +35,11 @@ template <typename R>
 struct StepArgs {
     KGeom<R> g;
     Particles<R> P;
+    int64_t num;
     const WorkItem *work;
     const int *nwork;
+    const int *cstart;          // nbricks * (BRC + 1)
+    int nbrick[3];
     unsigned long long *acc;    // NACC * nodec
     unsigned long long *acc2;   // 3 * nodec
     R *G;                       // gather field for the velocity gather (3 * nodec)
@@ -63,38 +80,42 @@ __device__ __forceinline__ int tile_of_node(const KGeom<R> &g, int gx, int gy, i
     return gx / TILE + g.ntile[0] * (gy / TILE + g.ntile[1] * (gz / TILE));
 }
 
-// Scales shared by the P2G kernel (producer) and the first grid pass (consumer).
 template <typename R>
-struct P2GScales {
-    Fix m, v, p, f;
+__device__ __forceinline__ size_t node_id(const KGeom<R> &g, int gx, int gy, int gz) {
+    return (size_t)gx + (size_t)g.nnc[0] * ((size_t)gy + (size_t)g.nnc[1] * (size_t)gz);
+}
+
+// Fixed-point scales.  Computed by one thread of a CTA (FP64 scalar work)
+// and shared; producer and consumer kernels derive them from the same
+// device-resident bounds, so they agree exactly.
+struct Scales {
+    Fix m, v, p, f;   // P2G: mass, vof, momentum, force
+    Fix q;            // MUSL momentum
+    Fix gd;           // |geup|^2
 };
 
 template <typename R>
-__device__ __forceinline__ P2GScales<R> p2g_scales(const StepArgs<R> &a) {
+__device__ void compute_scales(const StepArgs<R> &a, Scales &s) {
     const unsigned *nb = a.ctl->nxt[a.parity];
-    P2GScales<R> s;
     double gabs = fmax(fabs((double)a.grav[0]), fmax(fabs((double)a.grav[1]), fabs((double)a.grav[2])));
     s.m = make_fix(a.nump * a.mmax);
     s.v = make_fix(a.nump * (double)bits_f(nb[B_VOLMAX]));
     s.p = make_fix(a.nump * a.mmax * (double)bits_f(nb[B_VMAX]));
     s.f = make_fix(a.nump * ((double)bits_f(nb[B_VOLSMAX]) * 3.0 * a.gshape + a.mmax * gabs * fabs((double)a.facl)));
-    return s;
-}
-
-template <typename R>
-__device__ __forceinline__ Fix musl_scale(const StepArgs<R> &a) {
     double vb = (double)bits_f(a.ctl->cur[C_GMAX]);
-    if (a.scheme == MPM_FLIP) vb = (double)bits_f(a.ctl->nxt[a.parity][B_VMAX]) + fabs((double)a.dt) * vb;
-    return make_fix(a.nump * a.mmax * vb * 1.0000001);
+    if (a.scheme == MPM_FLIP) vb = (double)bits_f(nb[B_VMAX]) + fabs((double)a.dt) * vb;
+    s.q = make_fix(a.nump * a.mmax * vb * 1.0000001);
+    double gb = 2.0 * (double)bits_f(nb[B_VOLMAX]) * a.gsum * (double)bits_f(a.ctl->cur[C_NEIMAX]);
+    s.gd = make_fix(a.nump * 3.0 * gb * gb * 1.0000001);
 }
 
 template <typename R>
-__device__ __forceinline__ Fix geup_scale(const StepArgs<R> &a) {
-    double gb = 2.0 * (double)bits_f(a.ctl->nxt[a.parity][B_VOLMAX]) * a.gsum * (double)bits_f(a.ctl->cur[C_NEIMAX]);
-    return make_fix(a.nump * 3.0 * gb * gb * 1.0000001);
+__device__ __forceinline__ void load_scales(const StepArgs<R> &a, Scales &sh) {
+    if (threadIdx.x == 0) compute_scales(a, sh);
+    __syncthreads();
 }
 
-// Block-wide reductions over 256 threads (fixed order: deterministic).
+// Block-wide reduction (fixed order: deterministic); result valid in thread 0.
 template <typename T, typename Op>
 __device__ __forceinline__ T block_reduce(T v, Op op, T *sh) {
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -106,7 +127,7 @@ __device__ __forceinline__ T block_reduce(T v, Op op, T *sh) {
     T r = sh[0];
     if (threadIdx.x == 0)
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) r = op(r, sh[w]);
-    return r;  // valid in thread 0
+    return r;
 }
 
 struct OpAddD { __device__ double operator()(double a, double b) const { return a + b; } };
@@ -114,39 +135,337 @@ struct OpAddL { __device__ long long operator()(long long a, long long b) const 
 struct OpAddI { __device__ int operator()(int a, int b) const { return a + b; } };
 struct OpMaxF { __device__ float operator()(float a, float b) const { return fmaxf(a, b); } };
 
-// -------------------------------------------------------------------- P2G
+// The eight P2G contributions of one particle to one node
+// (StandardVarP2G x3, ComputeInternalForce + ComputeExternalForce,
+// material_point.h:223-247, solid_material_point.h:48-73).
+template <typename R>
+__device__ __forceinline__ void p2g_terms(R N, R d0, R d1, R d2, R m, R vol, const R *v, const R *s, R mfx, R mfy,
+                                          R mfz, R *q) {
+    const R Nm = N * m;
+    q[0] = Nm;
+    q[1] = N * vol;
+    q[2] = Nm * v[0];
+    q[3] = Nm * v[1];
+    q[4] = Nm * v[2];
+    q[5] = -vol * (s[0] * d0 + s[5] * d1 + s[4] * d2) + N * mfx;
+    q[6] = -vol * (s[5] * d0 + s[1] * d1 + s[3] * d2) + N * mfy;
+    q[7] = -vol * (s[4] * d0 + s[3] * d1 + s[2] * d2) + N * mfz;
+}
+
+template <typename R>
+__device__ __forceinline__ void fx_terms(const R *q, const Scales &S, long long *o) {
+    o[0] = fx(q[0], S.m);
+    o[1] = fx(q[1], S.v);
+    o[2] = fx(q[2], S.p);
+    o[3] = fx(q[3], S.p);
+    o[4] = fx(q[4], S.p);
+    o[5] = fx(q[5], S.f);
+    o[6] = fx(q[6], S.f);
+    o[7] = fx(q[7], S.f);
+}
+
+__device__ __forceinline__ void brick_origin(int b, const int *nb, int &ox, int &oy, int &oz) {
+    ox = (b % nb[0]) * BRX;
+    oy = ((b / nb[0]) % nb[1]) * BRY;
+    oz = (b / (nb[0] * nb[1])) * BRZ;
+}
+
+// ================================================ FP32 linear, per cell
+// One CTA per brick, one thread per cell.  Cell corner c = i + 2 (j + 2 k).
+__global__ void __launch_bounds__(BRC) k_p2g_cell(StepArgs<float> a) {
+    __shared__ float corner[NACC * 8][BRC];       // 32 KB
+    __shared__ Scales S;
+    __shared__ int sh_red[32];
+    const int b = blockIdx.x;
+    const int lc = threadIdx.x;
+    const int *cs = a.cstart + (size_t)b * (BRC + 1);
+    if (cs[0] == cs[BRC]) return;   // empty brick (uniform across the CTA)
+    int ox, oy, oz;
+    brick_origin(b, a.nbrick, ox, oy, oz);
+    const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
+    const int p0 = cs[lc], p1 = cs[lc + 1];
+    load_scales(a, S);
+    const float fxg = a.grav[0] * a.facl, fyg = a.grav[1] * a.facl, fzg = a.grav[2] * a.facl;
+    const Particles<float> &P = a.P;
+    float acc[NACC][8];
+#pragma unroll
+    for (int f = 0; f < NACC; f++)
+#pragma unroll
+        for (int c = 0; c < 8; c++) acc[f][c] = 0.0f;
+    int misses = 0, oobs = 0;
+    for (int p = p0; p < p1; p++) {
+        const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+        bool oob = false;
+        const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
+        oobs += oob;
+        Axis<float, 1> ax, ay, az;
+        axis_eval<float, 1>(x0, a.g, 0, px, ax);
+        axis_eval<float, 1>(x1, a.g, 1, py, ay);
+        axis_eval<float, 1>(x2, a.g, 2, pz, az);
+        const float m = ld(P.m + p), vol = ld(P.vol + p);
+        const float v[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
+        const float s[6] = {ld(P.s[0] + p), ld(P.s[1] + p), ld(P.s[2] + p),
+                            ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
+        const float mfx = m * fxg, mfy = m * fyg, mfz = m * fzg;
+        const bool mine = (px == cx) && (py == cy) && (pz == cz);
+        misses += !mine;
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+#pragma unroll
+            for (int j = 0; j < 2; j++)
+#pragma unroll
+                for (int i = 0; i < 2; i++) {
+                    const float wxy = ax.w[i] * ay.w[j];
+                    float q[NACC];
+                    p2g_terms(wxy * az.w[k], ax.dw[i] * ay.w[j] * az.w[k], ax.w[i] * ay.dw[j] * az.w[k],
+                              wxy * az.dw[k], m, vol, v, s, mfx, mfy, mfz, q);
+                    const int c = i + 2 * (j + 2 * k);
+                    if (mine) {
+#pragma unroll
+                        for (int f = 0; f < NACC; f++) acc[f][c] += q[f];
+                    } else {
+                        // a particle that left its sorted cell scatters on its own
+                        long long o[NACC];
+                        fx_terms(q, S, o);
+                        const size_t gn = node_id(a.g, px + i, py + j, pz + k);
+#pragma unroll
+                        for (int f = 0; f < NACC; f++)
+                            if (o[f]) atomic_add_i64(&a.acc[(size_t)f * a.g.nodec + gn], o[f]);
+                        a.tileflag[tile_of_node(a.g, px + i, py + j, pz + k)] = 1;
+                    }
+                }
+    }
+#pragma unroll
+    for (int f = 0; f < NACC; f++)
+#pragma unroll
+        for (int c = 0; c < 8; c++) corner[f * 8 + c][lc] = acc[f][c];
+    int tot = block_reduce(misses + (oobs << 16), OpAddI(), sh_red);
+    if (lc == 0 && tot) {
+        if (tot & 0xffff) atomicAdd(&a.ctl->tile_misses, (unsigned)(tot & 0xffff));
+        if (tot >> 16) atomicAdd(&a.ctl->err_oob, (unsigned)(tot >> 16));
+    }
+    __syncthreads();
+    // node pass: each node of the (BRX+1)(BRY+1)(BRZ+1) box adds the corners of
+    // its adjacent cells in a fixed order
+    constexpr int NX = BRX + 1, NY = BRY + 1, NZ = BRZ + 1, NB = NX * NY * NZ;
+    for (int it = lc; it < NB * NACC; it += BRC) {
+        const int f = it / NB, n = it % NB;
+        const int nx = n % NX, ny = (n / NX) % NY, nz = n / (NX * NY);
+        const int gx = ox + nx, gy = oy + ny, gz = oz + nz;
+        if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
+        float sum = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+#pragma unroll
+            for (int j = 0; j < 2; j++)
+#pragma unroll
+                for (int i = 0; i < 2; i++) {
+                    const int ex = nx - i, ey = ny - j, ez = nz - k;
+                    if (ex >= 0 && ex < BRX && ey >= 0 && ey < BRY && ez >= 0 && ez < BRZ)
+                        sum += corner[f * 8 + i + 2 * (j + 2 * k)][ex + BRX * (ey + BRY * ez)];
+                }
+        // every node of a non-empty brick's box is marked active, so that the
+        // grid passes also refresh nodes a particle touches with zero weight
+        if (f == 0) a.tileflag[tile_of_node(a.g, gx, gy, gz)] = 1;
+        if (sum != 0.0f) {
+            const Fix &F = f == 0 ? S.m : f == 1 ? S.v : f <= 4 ? S.p : S.f;
+            atomic_add_i64(&a.acc[(size_t)f * a.g.nodec + node_id(a.g, gx, gy, gz)], fx(sum, F));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(BRC) k_g2p_musl_cell(StepArgs<float> a) {
+    __shared__ float corner[3 * 8][BRC];
+    __shared__ Scales S;
+    __shared__ long long sh_l[32];
+    __shared__ float sh_f[32];
+    const int b = blockIdx.x;
+    const int lc = threadIdx.x;
+    const int *cs = a.cstart + (size_t)b * (BRC + 1);
+    if (cs[0] == cs[BRC]) return;
+    int ox, oy, oz;
+    brick_origin(b, a.nbrick, ox, oy, oz);
+    const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
+    const int p0 = cs[lc], p1 = cs[lc + 1];
+    load_scales(a, S);
+    const size_t N = (size_t)a.g.nodec;
+    const Particles<float> &P = a.P;
+    const bool flip = (a.scheme == MPM_FLIP);
+    // the gather fields of this cell's 8 nodes, loaded once
+    float Gc[3][8], Ec[8];
+#pragma unroll
+    for (int k = 0; k < 2; k++)
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const int c = i + 2 * (j + 2 * k);
+                if (p1 > p0) {
+                    const int gx = min(cx + i, a.g.nnc[0] - 1), gy = min(cy + j, a.g.nnc[1] - 1),
+                              gz = min(cz + k, a.g.nnc[2] - 1);
+                    const size_t gn = node_id(a.g, gx, gy, gz);
+#pragma unroll
+                    for (int d = 0; d < 3; d++) Gc[d][c] = ld(a.G + d * N + gn);
+                    Ec[c] = ld(a.nei + gn);
+                } else {
+                    Gc[0][c] = Gc[1][c] = Gc[2][c] = Ec[c] = 0.0f;
+                }
+            }
+    float acc[3][8];
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int c = 0; c < 8; c++) acc[d][c] = 0.0f;
+    long long gacc = 0;
+    float vmax = 0.0f;
+    for (int p = p0; p < p1; p++) {
+        const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+        bool oob = false;
+        const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
+        Axis<float, 1> ax, ay, az;
+        axis_eval<float, 1>(x0, a.g, 0, px, ax);
+        axis_eval<float, 1>(x1, a.g, 1, py, ay);
+        axis_eval<float, 1>(x2, a.g, 2, pz, az);
+        const float m = ld(P.m + p), vol = ld(P.vol + p);
+        const bool mine = (px == cx) && (py == cy) && (pz == cz);
+        float v[3];
+        if (flip) {
+            v[0] = ld(P.v[0] + p); v[1] = ld(P.v[1] + p); v[2] = ld(P.v[2] + p);
+        } else {
+            v[0] = v[1] = v[2] = 0.0f;
+        }
+        float gu[3] = {0.0f, 0.0f, 0.0f};
+        // PIC v = sum N v*, FLIP v += sum N dt a (PIC/FLIP::VarG2P, map_and_interpolate.h:12-55)
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+#pragma unroll
+            for (int j = 0; j < 2; j++)
+#pragma unroll
+                for (int i = 0; i < 2; i++) {
+                    const int c = i + 2 * (j + 2 * k);
+                    const float wxy = ax.w[i] * ay.w[j];
+                    const float N_ = wxy * az.w[k];
+                    float gv[3], e;
+                    if (mine) {
+                        gv[0] = Gc[0][c]; gv[1] = Gc[1][c]; gv[2] = Gc[2][c];
+                        e = Ec[c];
+                    } else {
+                        const size_t gn = node_id(a.g, px + i, py + j, pz + k);
+                        gv[0] = ld(a.G + gn); gv[1] = ld(a.G + N + gn); gv[2] = ld(a.G + 2 * N + gn);
+                        e = ld(a.nei + gn);
+                    }
+                    if (flip) {
+                        const float Nd = N_ * a.dt;
+#pragma unroll
+                        for (int d = 0; d < 3; d++) v[d] += Nd * gv[d];
+                    } else {
+#pragma unroll
+                        for (int d = 0; d < 3; d++) v[d] += N_ * gv[d];
+                    }
+                    gu[0] += ax.dw[i] * ay.w[j] * az.w[k] * e;
+                    gu[1] += ax.w[i] * ay.dw[j] * az.w[k] * e;
+                    gu[2] += wxy * az.dw[k] * e;
+                }
+        P.v[0][p] = v[0];
+        P.v[1][p] = v[1];
+        P.v[2][p] = v[2];
+        vmax = fmaxf(vmax, fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2]))));
+        const float tv = 2.0f * vol;
+        const float g0 = gu[0] * tv, g1 = gu[1] * tv, g2 = gu[2] * tv;
+        gacc += fx(g0 * g0 + g1 * g1 + g2 * g2, S.gd);
+        // MUSL re-projection of momentum (var_trans_solid_explicit.cpp:108-129)
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+#pragma unroll
+            for (int j = 0; j < 2; j++)
+#pragma unroll
+                for (int i = 0; i < 2; i++) {
+                    const int c = i + 2 * (j + 2 * k);
+                    const float Nm = ax.w[i] * ay.w[j] * az.w[k] * m;
+                    if (mine) {
+#pragma unroll
+                        for (int d = 0; d < 3; d++) acc[d][c] += Nm * v[d];
+                    } else {
+                        const size_t gn = node_id(a.g, px + i, py + j, pz + k);
+#pragma unroll
+                        for (int d = 0; d < 3; d++) {
+                            long long q = fx(Nm * v[d], S.q);
+                            if (q) atomic_add_i64(&a.acc2[d * N + gn], q);
+                        }
+                    }
+                }
+    }
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int c = 0; c < 8; c++) corner[d * 8 + c][lc] = acc[d][c];
+    long long gsum = block_reduce(gacc, OpAddL(), sh_l);
+    float vm = block_reduce(vmax, OpMaxF(), sh_f);
+    if (lc == 0) {
+        if (gsum) atomicAdd(&a.ctl->geup_acc, (unsigned long long)gsum);
+        if (vm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VMAX], vm * 1.000001f);
+    }
+    __syncthreads();
+    constexpr int NX = BRX + 1, NY = BRY + 1, NZ = BRZ + 1, NB = NX * NY * NZ;
+    for (int it = lc; it < NB * 3; it += BRC) {
+        const int d = it / NB, n = it % NB;
+        const int nx = n % NX, ny = (n / NX) % NY, nz = n / (NX * NY);
+        const int gx = ox + nx, gy = oy + ny, gz = oz + nz;
+        if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
+        float sum = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+#pragma unroll
+            for (int j = 0; j < 2; j++)
+#pragma unroll
+                for (int i = 0; i < 2; i++) {
+                    const int ex = nx - i, ey = ny - j, ez = nz - k;
+                    if (ex >= 0 && ex < BRX && ey >= 0 && ey < BRY && ez >= 0 && ez < BRZ)
+                        sum += corner[d * 8 + i + 2 * (j + 2 * k)][ex + BRX * (ey + BRY * ez)];
+                }
+        if (sum != 0.0f) atomic_add_i64(&a.acc2[d * N + node_id(a.g, gx, gy, gz)], fx(sum, S.q));
+    }
+}
+
+// Launched before the P2G of every step: records the P2G scales (for result
+// downloads) and resets the per-step device counters.
+template <typename R>
+__global__ void k_step_reset(StepArgs<R> a) {
+    Scales s;
+    compute_scales(a, s);
+    DevCtl *ctl = a.ctl;
+    ctl->p2g_inv[0] = s.m.inv;
+    ctl->p2g_inv[1] = s.v.inv;
+    ctl->p2g_inv[2] = s.p.inv;
+    ctl->p2g_inv[3] = s.f.inv;
+    for (int k = 0; k < B_NB; k++) ctl->nxt[a.parity ^ 1][k] = 0u;
+    for (int k = 0; k < C_NC; k++) ctl->cur[k] = 0u;
+    ctl->geup_acc = 0ull;
+}
+
+// ================================================= any order, staging box
+// One CTA per work item (a chunk of one brick's particles); every
+// contribution is converted to int64 and added into a shared box of the
+// brick's nodes (exact, order independent).
 template <typename R, int OX, int OY, int OZ>
-__global__ void __launch_bounds__(256) k_p2g(StepArgs<R> a) {
-    constexpr int BX = TILE + OX, BY = TILE + OY, BZ = TILE + OZ, BOX = BX * BY * BZ;
+__global__ void __launch_bounds__(256) k_p2g_box(StepArgs<R> a) {
+    constexpr int BX = BRX + OX, BY = BRY + OY, BZ = BRZ + OZ, BOX = BX * BY * BZ;
     extern __shared__ unsigned long long sacc[];   // NACC * BOX
+    __shared__ Scales S;
     __shared__ int sh_red[32];
     if ((int)blockIdx.x >= *a.nwork) return;
     const WorkItem w = a.work[blockIdx.x];
-    int tx, ty, tz;
-    tile_coords(w.tile, a.g.ntile, tx, ty, tz);
-    const int ox = tx * TILE, oy = ty * TILE, oz = tz * TILE;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        // per-step resets for the passes that follow
-        for (int k = 0; k < B_NB; k++) a.ctl->nxt[a.parity ^ 1][k] = 0u;
-        for (int k = 0; k < C_NC; k++) a.ctl->cur[k] = 0u;
-        a.ctl->geup_acc = 0ull;
-    }
+    int ox, oy, oz;
+    brick_origin(w.tile, a.nbrick, ox, oy, oz);
     for (int i = threadIdx.x; i < NACC * BOX; i += blockDim.x) sacc[i] = 0ull;
-    __syncthreads();
-    const P2GScales<R> S = p2g_scales(a);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        a.ctl->p2g_inv[0] = S.m.inv;
-        a.ctl->p2g_inv[1] = S.v.inv;
-        a.ctl->p2g_inv[2] = S.p.inv;
-        a.ctl->p2g_inv[3] = S.f.inv;
-    }
+    load_scales(a, S);
     const R fxg = a.grav[0] * a.facl, fyg = a.grav[1] * a.facl, fzg = a.grav[2] * a.facl;
     const Particles<R> &P = a.P;
     int misses = 0, oobs = 0;
     for (int p = w.begin + threadIdx.x; p < w.end; p += blockDim.x) {
-        R x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+        const R x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
         bool oob = false;
-        int cx = cell_of(x0, a.g, 0, oob), cy = cell_of(x1, a.g, 1, oob), cz = cell_of(x2, a.g, 2, oob);
+        const int cx = cell_of(x0, a.g, 0, oob), cy = cell_of(x1, a.g, 1, oob), cz = cell_of(x2, a.g, 2, oob);
         oobs += oob;
         Axis<R, OX> ax;
         Axis<R, OY> ay;
@@ -155,12 +474,12 @@ __global__ void __launch_bounds__(256) k_p2g(StepArgs<R> a) {
         axis_eval<R, OY>(x1, a.g, 1, cy, ay);
         axis_eval<R, OZ>(x2, a.g, 2, cz, az);
         const R m = ld(P.m + p), vol = ld(P.vol + p);
-        const R v0 = ld(P.v[0] + p), v1 = ld(P.v[1] + p), v2 = ld(P.v[2] + p);
-        const R s0 = ld(P.s[0] + p), s1 = ld(P.s[1] + p), s2 = ld(P.s[2] + p);
-        const R s3 = ld(P.s[3] + p), s4 = ld(P.s[4] + p), s5 = ld(P.s[5] + p);
+        const R v[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
+        const R s[6] = {ld(P.s[0] + p), ld(P.s[1] + p), ld(P.s[2] + p),
+                        ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
         const R mfx = m * fxg, mfy = m * fyg, mfz = m * fzg;
         const int lx = cx - ox, ly = cy - oy, lz = cz - oz;
-        const bool in = (unsigned)lx < (unsigned)TILE && (unsigned)ly < (unsigned)TILE && (unsigned)lz < (unsigned)TILE;
+        const bool in = (unsigned)lx < (unsigned)BRX && (unsigned)ly < (unsigned)BRY && (unsigned)lz < (unsigned)BRZ;
         misses += !in;
 #pragma unroll
         for (int k = 0; k <= OZ; k++)
@@ -169,30 +488,20 @@ __global__ void __launch_bounds__(256) k_p2g(StepArgs<R> a) {
 #pragma unroll
                 for (int i = 0; i <= OX; i++) {
                     const R wxy = ax.w[i] * ay.w[j];
-                    const R N = wxy * az.w[k];
-                    const R d0 = ax.dw[i] * ay.w[j] * az.w[k];
-                    const R d1 = ax.w[i] * ay.dw[j] * az.w[k];
-                    const R d2 = wxy * az.dw[k];
-                    const R Nm = N * m;
-                    long long q[NACC];
-                    q[0] = fx(Nm, S.m);
-                    q[1] = fx(N * vol, S.v);
-                    q[2] = fx(Nm * v0, S.p);
-                    q[3] = fx(Nm * v1, S.p);
-                    q[4] = fx(Nm * v2, S.p);
-                    q[5] = fx(-vol * (s0 * d0 + s5 * d1 + s4 * d2) + N * mfx, S.f);
-                    q[6] = fx(-vol * (s5 * d0 + s1 * d1 + s3 * d2) + N * mfy, S.f);
-                    q[7] = fx(-vol * (s4 * d0 + s3 * d1 + s2 * d2) + N * mfz, S.f);
+                    R q[NACC];
+                    p2g_terms(wxy * az.w[k], ax.dw[i] * ay.w[j] * az.w[k], ax.w[i] * ay.dw[j] * az.w[k],
+                              wxy * az.dw[k], m, vol, v, s, mfx, mfy, mfz, q);
+                    long long o[NACC];
+                    fx_terms(q, S, o);
                     if (in) {
                         const int li = (lx + i) + BX * ((ly + j) + BY * (lz + k));
 #pragma unroll
-                        for (int f = 0; f < NACC; f++) atomic_add_i64(&sacc[f * BOX + li], q[f]);
+                        for (int f = 0; f < NACC; f++) atomic_add_i64(&sacc[f * BOX + li], o[f]);
                     } else {
-                        const int gx = cx + i, gy = cy + j, gz = cz + k;
-                        const int gn = gx + a.g.nnc[0] * (gy + a.g.nnc[1] * gz);
+                        const size_t gn = node_id(a.g, cx + i, cy + j, cz + k);
 #pragma unroll
-                        for (int f = 0; f < NACC; f++) atomic_add_i64(&a.acc[(size_t)f * a.g.nodec + gn], q[f]);
-                        a.tileflag[tile_of_node(a.g, gx, gy, gz)] = 1;
+                        for (int f = 0; f < NACC; f++) atomic_add_i64(&a.acc[(size_t)f * a.g.nodec + gn], o[f]);
+                        a.tileflag[tile_of_node(a.g, cx + i, cy + j, cz + k)] = 1;
                     }
                 }
     }
@@ -202,22 +511,125 @@ __global__ void __launch_bounds__(256) k_p2g(StepArgs<R> a) {
         if (tot >> 16) atomicAdd(&a.ctl->err_oob, (unsigned)(tot >> 16));
     }
     __syncthreads();
-    // flush the tile box to the global accumulators
     for (int li = threadIdx.x; li < BOX; li += blockDim.x) {
         const int lx = li % BX, ly = (li / BX) % BY, lz = li / (BX * BY);
         const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
         if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
-        const int gn = gx + a.g.nnc[0] * (gy + a.g.nnc[1] * gz);
-        bool any = false;
+        const size_t gn = node_id(a.g, gx, gy, gz);
 #pragma unroll
         for (int f = 0; f < NACC; f++) {
             unsigned long long v = sacc[f * BOX + li];
-            if (v) {
-                atomicAdd(&a.acc[(size_t)f * a.g.nodec + gn], v);
-                any = true;
-            }
+            if (v) atomicAdd(&a.acc[(size_t)f * a.g.nodec + gn], v);
         }
-        if (any) a.tileflag[tile_of_node(a.g, gx, gy, gz)] = 1;
+        a.tileflag[tile_of_node(a.g, gx, gy, gz)] = 1;
+    }
+}
+
+template <typename R, int OX, int OY, int OZ>
+__global__ void __launch_bounds__(256) k_g2p_musl_box(StepArgs<R> a) {
+    constexpr int BX = BRX + OX, BY = BRY + OY, BZ = BRZ + OZ, BOX = BX * BY * BZ;
+    extern __shared__ unsigned long long sacc[];   // 3 * BOX
+    __shared__ Scales S;
+    __shared__ long long sh_l[32];
+    __shared__ float sh_f[32];
+    if ((int)blockIdx.x >= *a.nwork) return;
+    const WorkItem w = a.work[blockIdx.x];
+    int ox, oy, oz;
+    brick_origin(w.tile, a.nbrick, ox, oy, oz);
+    for (int i = threadIdx.x; i < 3 * BOX; i += blockDim.x) sacc[i] = 0ull;
+    load_scales(a, S);
+    const size_t N = (size_t)a.g.nodec;
+    const Particles<R> &P = a.P;
+    const bool flip = (a.scheme == MPM_FLIP);
+    long long gacc = 0;
+    float vmax = 0.0f;
+    for (int p = w.begin + threadIdx.x; p < w.end; p += blockDim.x) {
+        const R x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+        bool oob = false;
+        const int cx = cell_of(x0, a.g, 0, oob), cy = cell_of(x1, a.g, 1, oob), cz = cell_of(x2, a.g, 2, oob);
+        Axis<R, OX> ax;
+        Axis<R, OY> ay;
+        Axis<R, OZ> az;
+        axis_eval<R, OX>(x0, a.g, 0, cx, ax);
+        axis_eval<R, OY>(x1, a.g, 1, cy, ay);
+        axis_eval<R, OZ>(x2, a.g, 2, cz, az);
+        const R m = ld(P.m + p), vol = ld(P.vol + p);
+        R v[3];
+        if (flip) {
+            v[0] = ld(P.v[0] + p); v[1] = ld(P.v[1] + p); v[2] = ld(P.v[2] + p);
+        } else {
+            v[0] = v[1] = v[2] = (R)0;
+        }
+        R gu[3] = {(R)0, (R)0, (R)0};
+#pragma unroll
+        for (int k = 0; k <= OZ; k++)
+#pragma unroll
+            for (int j = 0; j <= OY; j++)
+#pragma unroll
+                for (int i = 0; i <= OX; i++) {
+                    const R wxy = ax.w[i] * ay.w[j];
+                    const R N_ = wxy * az.w[k];
+                    const size_t gn = node_id(a.g, cx + i, cy + j, cz + k);
+                    if (flip) {
+                        const R Nd = N_ * a.dt;
+#pragma unroll
+                        for (int d = 0; d < 3; d++) v[d] += Nd * ld(a.G + d * N + gn);
+                    } else {
+#pragma unroll
+                        for (int d = 0; d < 3; d++) v[d] += N_ * ld(a.G + d * N + gn);
+                    }
+                    const R e = ld(a.nei + gn);
+                    gu[0] += ax.dw[i] * ay.w[j] * az.w[k] * e;
+                    gu[1] += ax.w[i] * ay.dw[j] * az.w[k] * e;
+                    gu[2] += wxy * az.dw[k] * e;
+                }
+        P.v[0][p] = v[0];
+        P.v[1][p] = v[1];
+        P.v[2][p] = v[2];
+        vmax = fmaxf(vmax, fmaxf(fabsf((float)v[0]), fmaxf(fabsf((float)v[1]), fabsf((float)v[2]))));
+        const R tv = (R)2 * vol;
+        const R g0 = gu[0] * tv, g1 = gu[1] * tv, g2 = gu[2] * tv;
+        gacc += fx(g0 * g0 + g1 * g1 + g2 * g2, S.gd);
+        const int lx = cx - ox, ly = cy - oy, lz = cz - oz;
+        const bool in = (unsigned)lx < (unsigned)BRX && (unsigned)ly < (unsigned)BRY && (unsigned)lz < (unsigned)BRZ;
+#pragma unroll
+        for (int k = 0; k <= OZ; k++)
+#pragma unroll
+            for (int j = 0; j <= OY; j++)
+#pragma unroll
+                for (int i = 0; i <= OX; i++) {
+                    const R Nm = ax.w[i] * ay.w[j] * az.w[k] * m;
+                    const long long q0 = fx(Nm * v[0], S.q), q1 = fx(Nm * v[1], S.q), q2 = fx(Nm * v[2], S.q);
+                    if (in) {
+                        const int li = (lx + i) + BX * ((ly + j) + BY * (lz + k));
+                        atomic_add_i64(&sacc[li], q0);
+                        atomic_add_i64(&sacc[BOX + li], q1);
+                        atomic_add_i64(&sacc[2 * BOX + li], q2);
+                    } else {
+                        const size_t gn = node_id(a.g, cx + i, cy + j, cz + k);
+                        atomic_add_i64(&a.acc2[gn], q0);
+                        atomic_add_i64(&a.acc2[N + gn], q1);
+                        atomic_add_i64(&a.acc2[2 * N + gn], q2);
+                    }
+                }
+    }
+    long long gsum = block_reduce(gacc, OpAddL(), sh_l);
+    float vm = block_reduce(vmax, OpMaxF(), sh_f);
+    if (threadIdx.x == 0) {
+        if (gsum) atomicAdd(&a.ctl->geup_acc, (unsigned long long)gsum);
+        if (vm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VMAX], vm * 1.000001f);
+    }
+    __syncthreads();
+    for (int li = threadIdx.x; li < BOX; li += blockDim.x) {
+        const int lx = li % BX, ly = (li / BX) % BY, lz = li / (BX * BY);
+        const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
+        if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
+        const size_t gn = node_id(a.g, gx, gy, gz);
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            unsigned long long v = sacc[d * BOX + li];
+            if (v) atomicAdd(&a.acc2[d * N + gn], v);
+        }
     }
 }
 
@@ -227,25 +639,27 @@ __global__ void __launch_bounds__(256) k_grid1(StepArgs<R> a) {
     __shared__ double sh_d[32];
     __shared__ float sh_f[32];
     __shared__ bool s_last;
+    __shared__ Scales S;
     const int t = blockIdx.x;
-    double eu = 0.0;
+    float eu = 0.0f;
     float gmax = 0.0f, neimax = 0.0f;
-    if (a.all_tiles || a.tileflag[t]) {
-        const P2GScales<R> S = p2g_scales(a);
+    const bool active = a.all_tiles || a.tileflag[t];
+    if (active) {
+        load_scales(a, S);
         int tx, ty, tz;
         tile_coords(t, a.g.ntile, tx, ty, tz);
         const size_t N = (size_t)a.g.nodec;
         for (int li = threadIdx.x; li < TILE * TILE * TILE; li += blockDim.x) {
             const int gx = tx * TILE + (li % TILE), gy = ty * TILE + (li / TILE) % TILE, gz = tz * TILE + li / (TILE * TILE);
             if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
-            const size_t n = gx + (size_t)a.g.nnc[0] * (gy + (size_t)a.g.nnc[1] * gz);
-            const R mass = (R)((double)(long long)a.acc[n] * S.m.inv);
-            R vof = (R)((double)(long long)a.acc[N + n] * S.v.inv);
+            const size_t n = node_id(a.g, gx, gy, gz);
+            const R mass = unfx((long long)a.acc[n], S.m, (R)0);
+            R vof = unfx((long long)a.acc[N + n], S.v, (R)0);
             R nv[3], na[3];
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-                const R pc = (R)((double)(long long)a.acc[(2 + c) * N + n] * S.p.inv);
-                const R fc = (R)((double)(long long)a.acc[(5 + c) * N + n] * S.f.inv);
+                const R pc = unfx((long long)a.acc[(2 + c) * N + n], S.p, (R)0);
+                const R fc = unfx((long long)a.acc[(5 + c) * N + n], S.f, (R)0);
                 nv[c] = (mass > a.mtol) ? pc / mass : (R)0;
                 na[c] = (mass > a.mtol) ? fc / mass : (R)0;
             }
@@ -275,12 +689,12 @@ __global__ void __launch_bounds__(256) k_grid1(StepArgs<R> a) {
             R e = vof - (R)a.nvol[n];
             e = e > (R)0 ? e : (R)0;
             a.nei[n] = e;
-            eu += (double)e * (double)e;
+            eu += (float)e * (float)e;
             neimax = fmaxf(neimax, (float)e);
         }
     }
     // deterministic sum of nei^2: per-tile partials, reduced in tile order by the last CTA
-    double ebl = block_reduce(eu, OpAddD(), sh_d);
+    double ebl = block_reduce((double)eu, OpAddD(), sh_d);
     float gm = block_reduce(gmax, OpMaxF(), sh_f);
     float nm = block_reduce(neimax, OpMaxF(), sh_f);
     if (threadIdx.x == 0) {
@@ -304,139 +718,32 @@ __global__ void __launch_bounds__(256) k_grid1(StepArgs<R> a) {
     }
 }
 
-// ------------------------------------------------------ G2P 1 + MUSL scatter
-template <typename R, int OX, int OY, int OZ>
-__global__ void __launch_bounds__(256) k_g2p_musl(StepArgs<R> a) {
-    constexpr int BX = TILE + OX, BY = TILE + OY, BZ = TILE + OZ, BOX = BX * BY * BZ;
-    extern __shared__ unsigned long long sacc[];   // 3 * BOX
-    __shared__ long long sh_l[32];
-    __shared__ float sh_f[32];
-    if ((int)blockIdx.x >= *a.nwork) return;
-    const WorkItem w = a.work[blockIdx.x];
-    int tx, ty, tz;
-    tile_coords(w.tile, a.g.ntile, tx, ty, tz);
-    const int ox = tx * TILE, oy = ty * TILE, oz = tz * TILE;
-    for (int i = threadIdx.x; i < 3 * BOX; i += blockDim.x) sacc[i] = 0ull;
-    __syncthreads();
-    const Fix SQ = musl_scale(a);
-    const Fix SG = geup_scale(a);
-    const size_t N = (size_t)a.g.nodec;
-    const Particles<R> &P = a.P;
-    const bool flip = (a.scheme == MPM_FLIP);
-    long long gacc = 0;
-    float vmax = 0.0f;
-    for (int p = w.begin + threadIdx.x; p < w.end; p += blockDim.x) {
-        R x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
-        bool oob = false;
-        int cx = cell_of(x0, a.g, 0, oob), cy = cell_of(x1, a.g, 1, oob), cz = cell_of(x2, a.g, 2, oob);
-        Axis<R, OX> ax;
-        Axis<R, OY> ay;
-        Axis<R, OZ> az;
-        axis_eval<R, OX>(x0, a.g, 0, cx, ax);
-        axis_eval<R, OY>(x1, a.g, 1, cy, ay);
-        axis_eval<R, OZ>(x2, a.g, 2, cz, az);
-        const R m = ld(P.m + p), vol = ld(P.vol + p);
-        R v[3];
-        if (flip) {
-            v[0] = ld(P.v[0] + p); v[1] = ld(P.v[1] + p); v[2] = ld(P.v[2] + p);
-        } else {
-            v[0] = v[1] = v[2] = (R)0;
-        }
-        R gu[3] = {(R)0, (R)0, (R)0};
-        // gather: PIC v = sum N v*, FLIP v += sum N dt a (PIC/FLIP::VarG2P, map_and_interpolate.h:12-55)
-#pragma unroll
-        for (int k = 0; k <= OZ; k++)
-#pragma unroll
-            for (int j = 0; j <= OY; j++)
-#pragma unroll
-                for (int i = 0; i <= OX; i++) {
-                    const R wxy = ax.w[i] * ay.w[j];
-                    const R N_ = wxy * az.w[k];
-                    const size_t gn = (cx + i) + (size_t)a.g.nnc[0] * ((cy + j) + (size_t)a.g.nnc[1] * (cz + k));
-                    if (flip) {
-                        const R Nd = N_ * a.dt;
-#pragma unroll
-                        for (int c = 0; c < 3; c++) v[c] += Nd * ld(a.G + c * N + gn);
-                    } else {
-#pragma unroll
-                        for (int c = 0; c < 3; c++) v[c] += N_ * ld(a.G + c * N + gn);
-                    }
-                    const R e = ld(a.nei + gn);
-                    gu[0] += ax.dw[i] * ay.w[j] * az.w[k] * e;
-                    gu[1] += ax.w[i] * ay.dw[j] * az.w[k] * e;
-                    gu[2] += wxy * az.dw[k] * e;
-                }
-        P.v[0][p] = v[0];
-        P.v[1][p] = v[1];
-        P.v[2][p] = v[2];
-        vmax = fmaxf(vmax, fmaxf(fabsf((float)v[0]), fmaxf(fabsf((float)v[1]), fabsf((float)v[2]))));
-        // |geup|^2 with geup = 2 vol sum dN nei (material_point.cpp:192-216)
-        const R tv = (R)2 * vol;
-        const R g0 = gu[0] * tv, g1 = gu[1] * tv, g2 = gu[2] * tv;
-        gacc += fx((double)g0 * (double)g0 + (double)g1 * (double)g1 + (double)g2 * (double)g2, SG);
-        // MUSL re-projection of momentum (var_trans_solid_explicit.cpp:108-129)
-        const int lx = cx - ox, ly = cy - oy, lz = cz - oz;
-        const bool in = (unsigned)lx < (unsigned)TILE && (unsigned)ly < (unsigned)TILE && (unsigned)lz < (unsigned)TILE;
-#pragma unroll
-        for (int k = 0; k <= OZ; k++)
-#pragma unroll
-            for (int j = 0; j <= OY; j++)
-#pragma unroll
-                for (int i = 0; i <= OX; i++) {
-                    const R Nm = ax.w[i] * ay.w[j] * az.w[k] * m;
-                    long long q0 = fx(Nm * v[0], SQ), q1 = fx(Nm * v[1], SQ), q2 = fx(Nm * v[2], SQ);
-                    if (in) {
-                        const int li = (lx + i) + BX * ((ly + j) + BY * (lz + k));
-                        atomic_add_i64(&sacc[li], q0);
-                        atomic_add_i64(&sacc[BOX + li], q1);
-                        atomic_add_i64(&sacc[2 * BOX + li], q2);
-                    } else {
-                        const size_t gn = (cx + i) + (size_t)a.g.nnc[0] * ((cy + j) + (size_t)a.g.nnc[1] * (cz + k));
-                        atomic_add_i64(&a.acc2[gn], q0);
-                        atomic_add_i64(&a.acc2[N + gn], q1);
-                        atomic_add_i64(&a.acc2[2 * N + gn], q2);
-                    }
-                }
-    }
-    long long gsum = block_reduce(gacc, OpAddL(), sh_l);
-    float vm = block_reduce(vmax, OpMaxF(), sh_f);
-    if (threadIdx.x == 0) {
-        if (gsum) atomicAdd(&a.ctl->geup_acc, (unsigned long long)gsum);
-        if (vm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VMAX], vm * 1.000001f);
-    }
-    __syncthreads();
-    for (int li = threadIdx.x; li < BOX; li += blockDim.x) {
-        const int lx = li % BX, ly = (li / BX) % BY, lz = li / (BX * BY);
-        const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-        if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
-        const size_t gn = gx + (size_t)a.g.nnc[0] * (gy + (size_t)a.g.nnc[1] * gz);
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            unsigned long long v = sacc[c * BOX + li];
-            if (v) atomicAdd(&a.acc2[c * N + gn], v);
-        }
-    }
-}
-
 // ------------------------------------------------------------ grid pass 2
 template <typename R>
 __global__ void __launch_bounds__(256) k_grid2(StepArgs<R> a) {
+    __shared__ Scales S;
     const int t = blockIdx.x;
+    if (t == 0 && threadIdx.x == 0) {
+        // b0 of DeltaCorrectionParticleShifting (material_point.cpp:219)
+        Scales s;
+        compute_scales(a, s);
+        double gd = (double)(long long)a.ctl->geup_acc * s.gd.inv;
+        a.ctl->b0 = (!a.shifting || gd < (double)a.mtol) ? 0.0 : a.ctl->eu_norm / gd;
+    }
     if (!(a.all_tiles || a.tileflag[t])) return;
-    const P2GScales<R> S = p2g_scales(a);
-    const Fix SQ = musl_scale(a);
+    load_scales(a, S);
     int tx, ty, tz;
     tile_coords(t, a.g.ntile, tx, ty, tz);
     const size_t N = (size_t)a.g.nodec;
     for (int li = threadIdx.x; li < TILE * TILE * TILE; li += blockDim.x) {
         const int gx = tx * TILE + (li % TILE), gy = ty * TILE + (li / TILE) % TILE, gz = tz * TILE + li / (TILE * TILE);
         if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
-        const size_t n = gx + (size_t)a.g.nnc[0] * (gy + (size_t)a.g.nnc[1] * gz);
-        const R mass = (R)((double)(long long)a.acc[n] * S.m.inv);
+        const size_t n = node_id(a.g, gx, gy, gz);
+        const R mass = unfx((long long)a.acc[n], S.m, (R)0);
         R nv[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            const R pc = (R)((double)(long long)a.acc2[c * N + n] * SQ.inv);
+            const R pc = unfx((long long)a.acc2[c * N + n], S.q, (R)0);
             nv[c] = (mass > a.mtol) ? pc / mass : (R)0;
         }
         const unsigned char bf = a.bcflag[n];
@@ -461,28 +768,21 @@ __global__ void __launch_bounds__(256) k_grid2(StepArgs<R> a) {
 }
 
 // ----------------------------------------------- G2P 2: F, x, vol, stress
+// One thread per particle (coalesced particle I/O; node gathers hit L1/L2).
 template <typename R, int OX, int OY, int OZ>
 __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
     __shared__ float sh_f[32];
     __shared__ int sh_i[32];
-    if ((int)blockIdx.x >= *a.nwork) return;
-    const WorkItem w = a.work[blockIdx.x];
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const size_t N = (size_t)a.g.nodec;
     const Particles<R> &P = a.P;
-    // b0 of DeltaCorrectionParticleShifting (material_point.cpp:219)
-    double b0 = 0.0;
-    if (a.shifting) {
-        const Fix SG = geup_scale(a);
-        double gd = (double)(long long)a.ctl->geup_acc * SG.inv;
-        b0 = (gd < (double)a.mtol) ? 0.0 : a.ctl->eu_norm / gd;
-    }
-    const R rb0 = (R)b0;
+    const R rb0 = (R)a.ctl->b0;
     float volmax = 0.0f, vsmax = 0.0f;
     int bad = 0;
-    for (int p = w.begin + threadIdx.x; p < w.end; p += blockDim.x) {
+    if (p < a.num) {
         R x[3] = {ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p)};
         bool oob = false;
-        int cx = cell_of(x[0], a.g, 0, oob), cy = cell_of(x[1], a.g, 1, oob), cz = cell_of(x[2], a.g, 2, oob);
+        const int cx = cell_of(x[0], a.g, 0, oob), cy = cell_of(x[1], a.g, 1, oob), cz = cell_of(x[2], a.g, 2, oob);
         Axis<R, OX> ax;
         Axis<R, OY> ay;
         Axis<R, OZ> az;
@@ -501,7 +801,7 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
                     const R wxy = ax.w[i] * ay.w[j];
                     const R N_ = wxy * az.w[k];
                     const R dn[3] = {ax.dw[i] * ay.w[j] * az.w[k], ax.w[i] * ay.dw[j] * az.w[k], wxy * az.dw[k]};
-                    const size_t gn = (cx + i) + (size_t)a.g.nnc[0] * ((cy + j) + (size_t)a.g.nnc[1] * (cz + k));
+                    const size_t gn = node_id(a.g, cx + i, cy + j, cz + k);
                     const R nv[3] = {ld(a.nvel2 + gn), ld(a.nvel2 + N + gn), ld(a.nvel2 + 2 * N + gn)};
 #pragma unroll
                     for (int r = 0; r < 3; r++)
@@ -574,8 +874,8 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
 #pragma unroll
             for (int k = 0; k < 6; k++) s[k] = (R)0;
         }
-        bool fin = isfinite(xn[0]) && isfinite(xn[1]) && isfinite(xn[2]) && isfinite(J) && isfinite(s[0]) &&
-                   isfinite(s[1]) && isfinite(s[2]) && isfinite(s[3]) && isfinite(s[4]) && isfinite(s[5]);
+        const bool fin = isfinite(xn[0]) && isfinite(xn[1]) && isfinite(xn[2]) && isfinite(J) && isfinite(s[0]) &&
+                         isfinite(s[1]) && isfinite(s[2]) && isfinite(s[3]) && isfinite(s[4]) && isfinite(s[5]);
         bad += !fin;
 #pragma unroll
         for (int c = 0; c < 3; c++) P.x[c][p] = xn[c];
@@ -590,12 +890,12 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
         const float rs1 = fabsf((float)s[5]) + fabsf((float)s[1]) + fabsf((float)s[3]);
         const float rs2 = fabsf((float)s[4]) + fabsf((float)s[3]) + fabsf((float)s[2]);
         const float vf = fabsf((float)volp);
-        volmax = fmaxf(volmax, vf);
-        vsmax = fmaxf(vsmax, vf * fmaxf(rs0, fmaxf(rs1, rs2)));
+        volmax = vf;
+        vsmax = vf * fmaxf(rs0, fmaxf(rs1, rs2));
     }
-    float vm = block_reduce(volmax, OpMaxF(), sh_f);
-    float sm = block_reduce(vsmax, OpMaxF(), sh_f);
-    int nb = block_reduce(bad, OpAddI(), sh_i);
+    const float vm = block_reduce(volmax, OpMaxF(), sh_f);
+    const float sm = block_reduce(vsmax, OpMaxF(), sh_f);
+    const int nb = block_reduce(bad, OpAddI(), sh_i);
     if (threadIdx.x == 0) {
         if (vm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VOLMAX], vm * 1.000001f);
         if (sm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VOLSMAX], sm * 1.000001f);
@@ -615,9 +915,11 @@ static StepArgs<R> make_args(mpm_ctx *c) {
         a.g.nel[d] = c->g.nel[d];
         a.g.nnc[d] = c->g.nnc[d];
         a.g.ntile[d] = c->g.ntile[d];
+        a.nbrick[d] = c->g.nbrick[d];
         a.grav[d] = (R)c->gravity[d];
     }
     a.g.nodec = c->g.nodec;
+    a.num = c->num;
     char *base = (char *)c->pbuf[c->cur];
     size_t n = (size_t)c->num, rs = sizeof(R);
     R *f = (R *)base;
@@ -632,6 +934,7 @@ static StepArgs<R> make_args(mpm_ctx *c) {
     a.P.pid = a.P.matid + n;
     a.work = c->d_work;
     a.nwork = c->d_nwork;
+    a.cstart = c->d_cstart;
     a.acc = c->d_acc;
     a.acc2 = c->d_acc2;
     R *nod = (R *)c->d_nodal;
@@ -669,35 +972,50 @@ static StepArgs<R> make_args(mpm_ctx *c) {
     return a;
 }
 
+static bool use_cell_kernels(const mpm_ctx *c) {
+    return c->cell_scatter && c->precision == 32 && c->g.order[0] == 1 && c->g.order[1] == 1 && c->g.order[2] == 1;
+}
+
+// which: 0 P2G, 1 G2P + MUSL, 2 G2P update
 template <typename R, int OX, int OY, int OZ>
 static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
     StepArgs<R> a = make_args<R>(c);
-    constexpr int BOX = (TILE + OX) * (TILE + OY) * (TILE + OZ);
-    const int grid = c->nwork_cap;
-    if (grid == 0) return MPM_OK;
+    constexpr int BOX = (BRX + OX) * (BRY + OY) * (BRZ + OZ);
+    if (c->num == 0) return MPM_OK;
     if (which == 0) {
-        size_t smem = (size_t)NACC * BOX * sizeof(unsigned long long);
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_p2g<R, OX, OY, OZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            attr = true;
-        }
+        k_step_reset<R><<<1, 1, 0, c->stream>>>(a);
+        c->launches++;
         timer_begin(c, K_P2G);
-        k_p2g<R, OX, OY, OZ><<<grid, 256, smem, c->stream>>>(a);
+        if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
+            if (use_cell_kernels(c)) {
+                k_p2g_cell<<<c->g.nbricks, BRC, 0, c->stream>>>(a);
+                timer_end(c, K_P2G);
+                c->launches++;
+                return check_launch(c);
+            }
+        }
+        size_t smem = (size_t)NACC * BOX * sizeof(unsigned long long);
+        cudaFuncSetAttribute(k_p2g_box<R, OX, OY, OZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_p2g_box<R, OX, OY, OZ><<<c->nwork_cap, 256, smem, c->stream>>>(a);
         timer_end(c, K_P2G);
     } else if (which == 1) {
-        size_t smem = (size_t)3 * BOX * sizeof(unsigned long long);
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_g2p_musl<R, OX, OY, OZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            attr = true;
-        }
         timer_begin(c, K_G2P_MUSL);
-        k_g2p_musl<R, OX, OY, OZ><<<grid, 256, smem, c->stream>>>(a);
+        if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
+            if (use_cell_kernels(c)) {
+                k_g2p_musl_cell<<<c->g.nbricks, BRC, 0, c->stream>>>(a);
+                timer_end(c, K_G2P_MUSL);
+                c->launches++;
+                return check_launch(c);
+            }
+        }
+        size_t smem = (size_t)3 * BOX * sizeof(unsigned long long);
+        cudaFuncSetAttribute(k_g2p_musl_box<R, OX, OY, OZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_g2p_musl_box<R, OX, OY, OZ><<<c->nwork_cap, 256, smem, c->stream>>>(a);
         timer_end(c, K_G2P_MUSL);
     } else {
         timer_begin(c, K_G2P_UPDATE);
-        k_g2p_update<R, OX, OY, OZ><<<grid, 256, 0, c->stream>>>(a);
+        const int nb = (int)((c->num + 255) / 256);
+        k_g2p_update<R, OX, OY, OZ><<<nb, 256, 0, c->stream>>>(a);
         timer_end(c, K_G2P_UPDATE);
     }
     c->launches++;
@@ -773,7 +1091,6 @@ __global__ void k_nodal_volume(Geom g, int npx, int npy, int npz, double *nvol) 
     int np[3] = {npx, npy, npz};
     int idx[3] = {i, j, k};
     double volp = g.dx[0] * g.dx[1] * g.dx[2] / (double)(npx * npy * npz);
-    // per direction: sum over adjacent cells e (ie - order .. ie) of the weights at the Gaussian points
     double wsum[3];
     for (int d = 0; d < 3; d++) {
         double s = 0.0;

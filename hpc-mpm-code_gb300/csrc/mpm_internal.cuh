@@ -24,8 +24,10 @@
 
 namespace mpm {
 
-constexpr int TILE = 8;              // cells per tile edge
-constexpr int CHUNK = 2048;          // max particles per work item
+constexpr int TILE = 8;              // node tile edge for the grid passes and activity flags
+constexpr int BRX = 4, BRY = 4, BRZ = 8;   // particle brick: cells per brick edge
+constexpr int BRC = BRX * BRY * BRZ;       // cells per brick (one CTA thread per cell)
+constexpr int CHUNK = 1024;          // max particles per work item
 constexpr int NACC = 8;              // P2G fields: mass, vof, mome xyz, force xyz
 constexpr int NKCLASS = 12;          // kernel classes for timing
 
@@ -38,8 +40,10 @@ struct Geom {
     int nel[3];      // cells
     int nnc[3];      // control points per direction (nel + order)
     int order[3];    // 1 or 2
-    int ntile[3];    // tiles per direction (over control points)
+    int ntile[3];    // node tiles per direction (over control points)
     int ntiles;
+    int nbrick[3];   // particle bricks per direction (over cells)
+    int nbricks;
     int nodec;
     int nelem;
     double xmin[3], dx[3];
@@ -60,6 +64,7 @@ struct DevCtl {
     unsigned int err_nonfinite;
     unsigned int tile_misses;
     double p2g_inv[4];               // 2^-e of the P2G scales (mass, vof, momentum, force) of the last P2G
+    double b0;                       // shifting coefficient of this step
 };
 
 template <typename R>
@@ -77,9 +82,10 @@ struct WorkItem {
 // Fixed-point scale 2^e, applied as two float factors so that e up to +-250
 // never overflows an intermediate.
 struct Fix {
-    float s1, s2;
-    double sd;    // 2^e
-    double inv;   // 2^-e
+    float s1, s2;   // s1 * s2 = 2^e
+    float i1, i2;   // i1 * i2 = 2^-e
+    double sd;      // 2^e
+    double inv;     // 2^-e
 };
 
 struct KernelTimer {
@@ -123,6 +129,8 @@ struct mpm_ctx {
     double *d_eu_part = nullptr;
     // sorting
     int *d_key = nullptr, *d_perm = nullptr, *d_tcount = nullptr, *d_tstart = nullptr, *d_tcursor = nullptr;
+    int *d_tmp = nullptr, *d_perm2 = nullptr;   // per-brick cell sort
+    int *d_cstart = nullptr;                    // nbricks * (BRC + 1) cell start offsets
     mpm::WorkItem *d_work = nullptr;
     int *d_nwork = nullptr;
     int nwork_cap = 0;
@@ -137,6 +145,7 @@ struct mpm_ctx {
     int stage = 0;   // 0 idle, 1 after p2g, 2 after grid update
     bool accum_dirty = false;
     bool write_nodal_dl = false;
+    int cell_scatter = 1;   // FP32 linear: per-cell register scatter (else staging-box atomics)
     mpm_status latched = MPM_OK;
     mpm::KernelTimer timer;
     std::vector<int> bc_nodes[3];

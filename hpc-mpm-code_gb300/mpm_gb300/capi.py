@@ -43,8 +43,8 @@ class MaterialDesc(C.Structure):
 
 class Config(C.Structure):
     _fields_ = [("dt", C.c_double), ("mtol", C.c_double), ("gravity", C.c_double * 3), ("scheme", C.c_int),
-                ("precision", C.c_int), ("shifting", C.c_int), ("resort_period", C.c_int),
-                ("reserved", C.c_int * 8)]
+                ("precision", C.c_int), ("shifting", C.c_int), ("resort_period", C.c_int), ("scatter", C.c_int),
+                ("reserved", C.c_int * 7)]
 
 
 class Stats(C.Structure):
@@ -116,7 +116,7 @@ NODAL = {"nmass": (0, 1), "nvof": (1, 1), "nmome": (2, 3), "nforce": (3, 3), "nv
 class GpuSolid:
     """One explicit solid on the GPU, built from a scene (mpm_gb300.scenes.Scene)."""
 
-    def __init__(self, scene, precision=32, shifting=True, resort_period=0, stream=None):
+    def __init__(self, scene, precision=32, shifting=True, resort_period=0, scatter=0, stream=None):
         self.lib = lib = load()
         self.scene = s = scene
         g = GridDesc((C.c_int * 3)(*s.xyelem), (C.c_double * 3)(*s.xymin), (C.c_double * 3)(*s.dxy),
@@ -125,7 +125,7 @@ class GpuSolid:
         self._mat = np.ascontiguousarray(s.mat_prop, dtype=np.float64).ravel()
         m = MaterialDesc(len(self._iprop), self._iprop.ctypes.data_as(_ip), self._mat.ctypes.data_as(_dp))
         cfg = Config(s.dt, s.mtol, (C.c_double * 3)(*s.gravity), s.scheme, precision, int(shifting),
-                     int(resort_period), (C.c_int * 8)())
+                     int(resort_period), int(scatter), (C.c_int * 7)())
         h = C.c_void_p()
         _chk(lib.mpm_gpu_create(C.byref(g), C.byref(m), C.byref(cfg), C.byref(h)), "mpm_gpu_create")
         self.ctx = h

@@ -72,8 +72,9 @@ typedef struct {
     int scheme;         /* MPM_PIC or MPM_FLIP (solswitch) */
     int precision;      /* 32: FP32 particle/grid arithmetic; 64: FP64 */
     int shifting;       /* 1: DeltaCorrectionParticleShifting as the reference; 0: off */
-    int resort_period;  /* physical re-sort of particles by tile every N steps (>= 1); 0 = default */
-    int reserved[8];
+    int resort_period;  /* physical re-sort of particles by brick every N steps (>= 1); 0 = default (8) */
+    int scatter;        /* 0: per-cell register scatter for FP32 linear grids (default); 1: staging-box atomics */
+    int reserved[7];
 } mpm_config;
 
 /* ---- lifetime ------------------------------------------------------------
