@@ -1,0 +1,301 @@
+"""Benchmark of the GB300 MPM transfer path: explicit solid MPM, particle-steps/s.
+
+Workload (default): the 4,096,000-particle spinning elastic block on a 128^3
+grid (dx = 4e-3 m, 80^3 cells at 8 particles per cell, the top quarter
+squeezed to 27 per cell, Gaussian + rigid-rotation velocities), FP32, PIC,
+dt = 2e-6 s.  Seeded synthetic data; the reference publishes no dataset.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+* value      K fused explicit steps (mpm_gpu_step_explicit) with the particle
+             state resident in HBM, timed with CUDA events on the library's
+             stream between a barrier + synchronize on both sides; the
+             particle state (393 MB) is larger than L2.
+* e2e        the same steps through the reference-facing C ABI with host
+             buffers: per step the FP64 particle state is uploaded from
+             pinned host memory (mpm_gpu_upload_particles), one step runs,
+             and the state is downloaded (mpm_gpu_download_particles).
+* roofline   the whole explicit step against the measured HBM copy
+             bandwidth, with the algorithmic bytes N_p*176 + N_n*56 per step.
+* cpu_baseline / --impl reference: the CPU restatement of the reference's
+             algorithm (oracle/mpm_oracle.c, pinned bit-exact to the
+             reference's own compiled code) on a bounded sample.
+N > 1: independent replicas, one per GPU (the path does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "hpc-mpm-code_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s"
+WORKLOAD = "explicit solid MPM, spinning elastic block, 4,096,000 particles, 128^3 grid, FP32, PIC"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def algorithmic_bytes(num, nodec):
+    # per explicit step, FP32: 23 words read + 21 written per particle, 7 nodal words written + read
+    return num * 176 + nodec * 56
+
+
+def cpu_baseline(scene, steps):
+    """The oracle restatement on this host, one core, a bounded sample of the same workload."""
+    from oracle import port
+
+    o = port.PortSolid(scene)
+    o.steps(1)   # warm-up (page-in, first linked list)
+    t0 = time.perf_counter()
+    o.steps(steps)
+    dt = time.perf_counter() - t0
+    value = scene.num * steps / dt
+    return {"value": value, "unit": METRIC, "cores": 1, "kind": "port",
+            "sample": f"{steps} FP64 steps of the full {scene.num}-particle workload ({dt:.1f} s)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from mpm_gb300 import scenes
+
+    s = scenes.spinning_block()
+    base = cpu_baseline(s, 1)   # warm-up leg, discarded
+    vals = []
+    for _ in range(max(1, args.steps)):
+        vals.append(cpu_baseline(s, max(1, args.cpu_steps))["value"])
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD.replace("FP32", "FP64 CPU"), "particles": s.num, "grid": list(s.xyelem)},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": 1, "kind": "port",
+                             "sample": f"{args.steps} x {args.cpu_steps} FP64 steps of the full workload; the "
+                                       "reference MPI+PETSc build cannot be produced on this host and its code "
+                                       "is single-threaded per rank"},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    del base
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from mpm_gb300 import build, capi, scenes
+
+    build.build()
+    s = scenes.spinning_block()
+    stream = torch.cuda.Stream()
+    gpu = capi.GpuSolid(s, precision=32, stream=stream.cuda_stream)
+    hbm_peak, peak_kind = measured_peaks()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up
+    gpu.steps(args.warmup)
+    gpu.sync()
+    launches0 = gpu.stats()["kernel_launches"]
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        gpu.steps(args.steps)
+        ev1.record(stream)
+        ev1.synchronize()
+    barrier()
+    gpu.sync()
+    ms = ev0.elapsed_time(ev1)
+    launches = gpu.stats()["kernel_launches"] - launches0
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * s.num * args.steps / (ms * 1e-3)
+
+    # per-kernel device time over a second timed window (events around every kernel)
+    gpu.enable_kernel_timing(True)
+    ksteps = min(args.steps, 100)
+    gpu.steps(ksteps)
+    kt = gpu.kernel_times()
+    gpu.enable_kernel_timing(False)
+    gpu.sync()
+    kernels = {k: {"ms_per_step": v[0] / ksteps, "launches": v[1]} for k, v in kt.items() if v[1]}
+    ktot = sum(k["ms_per_step"] for k in kernels.values())
+    for k in kernels.values():
+        k["share"] = k["ms_per_step"] / ktot if ktot else None
+
+    alg = algorithmic_bytes(s.num, s.nodec)
+    achieved = alg / (ms_step * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "explicit_step_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get("dram_bytes_per_step")
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": traffic,
+                "kernel": "one explicit step (p2g, grid1, g2p_musl, grid2, g2p_update, amortised re-sort)",
+                "algorithmic_bytes_per_step": alg, "peak_source": peak_kind}
+
+    # end to end through the C ABI with host buffers
+    n = s.num
+    pin = lambda *shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    hx, hv, hF, hs, hvol = pin(n, 3), pin(n, 3), pin(n, 9), pin(n, 6), pin(n)
+    gpu.download_into(hx, hv, hF, hs, hvol)
+    e_steps = max(1, args.e2e_steps)
+    gpu.upload_state(hx, hv, hF, hs, hvol)
+    gpu.steps(1)
+    gpu.download_into(hx, hv, hF, hs, hvol)
+    barrier()
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    for _ in range(e_steps):
+        gpu.upload_state(hx, hv, hF, hs, hvol)
+        gpu.steps(1)
+        gpu.download_into(hx, hv, hF, hs, hvol)
+    ev1.record(stream)
+    ev1.synchronize()
+    e_ms = max(ev0.elapsed_time(ev1), (time.perf_counter() - t0) * 1e3)
+    barrier()
+    if world > 1:
+        t = torch.tensor([e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e_ms = float(t.item())
+    state_bytes = n * 8 * (3 + 3 + 9 + 6 + 1)
+    e2e = {"value": world * n * e_steps / (e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": state_bytes,
+           "d2h_bytes_per_step": state_bytes, "steps": e_steps,
+           "call": "mpm_gpu_upload_particles + mpm_gpu_step_explicit(1) + mpm_gpu_download_particles, FP64 host "
+                   "arrays in pinned memory"}
+    gpu.sync()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline(s, args.cpu_steps)
+        except Exception as exc:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": METRIC, "cores": 1, "kind": "port", "sample": f"failed: {exc}"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "particles": s.num, "grid": list(s.xyelem), "nodes": s.nodec,
+                           "dt": s.dt, "scheme": "PIC", "parallelism": f"replicas x{world}",
+                           "l2": "inputs larger than L2: 393 MB particle state per step, no flush"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(),
+                "gpu_launches": int(launches), "kernels": kernels}
+        print(json.dumps(line), flush=True)
+    gpu.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

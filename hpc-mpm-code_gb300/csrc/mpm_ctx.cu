@@ -63,9 +63,11 @@ static void free_particles(mpm_ctx *c) {
     free_dev(c->d_perm);
     free_dev(c->d_tmp);
     free_dev(c->d_perm2);
+    free_dev(c->d_stage);
     free_dev(c->d_work);
     c->pbuf[0] = c->pbuf[1] = nullptr;
     c->d_key = c->d_perm = c->d_tmp = c->d_perm2 = nullptr;
+    c->d_stage = nullptr;
     c->d_work = nullptr;
     c->num = 0;
 }
@@ -241,7 +243,12 @@ static mpm_status upload_particles(mpm_ctx *c, int64_t n, const double *coord, c
             f[(3 + k) * N + p] = (R)v;
             vmax = fmax(vmax, fabs(v));
         }
-        for (int k = 0; k < 9; k++) f[(6 + k) * N + p] = (R)(F ? F[9 * p + k] : ((k % 4) == 0 ? 1.0 : 0.0));
+        for (int k = 0; k < 9; k++) {
+            // FP32 stores the displacement gradient H = F - I; FP64 stores F
+            const double eye = (k % 4) == 0 ? 1.0 : 0.0;
+            const double Fk = F ? F[9 * p + k] : eye;
+            f[(6 + k) * N + p] = sizeof(R) == 4 ? (R)(Fk - eye) : (R)Fk;
+        }
         double s[6];
         for (int k = 0; k < 6; k++) {
             s[k] = stress ? stress[6 * p + k] : 0.0;
@@ -469,35 +476,97 @@ mpm_status mpm_gpu_download_nodal(mpm_ctx *c, int field, double *host) {
     return MPM_OK;
 }
 
+// Host <-> device particle state in the reference's FP64 AoS layout.  The
+// copies go through a device staging buffer in load order; a kernel moves the
+// fields between it and the sorted SoA arrays (pid maps sorted -> load index).
+// Staging layout (per particle, load order): coord 3 | vel 3 | F 9 | stress 6 | vol 1.
+namespace mpm {
+constexpr int ST_X = 0, ST_V = 3, ST_F = 6, ST_S = 15, ST_VOL = 21, ST_W = 22;
+
 template <typename R>
-static mpm_status dl_particles(mpm_ctx *c, double *coord, double *vel, double *F, double *stress, double *vol) {
-    size_t N = (size_t)c->num;
-    size_t bytes = N * (24 * sizeof(R) + 2 * sizeof(int));
-    std::vector<char> host(bytes);
-    CK(cudaMemcpy(host.data(), c->pbuf[c->cur], bytes, cudaMemcpyDeviceToHost));
-    const R *f = (const R *)host.data();
+__global__ void k_state_gather(const R *f, size_t N, double *st, unsigned mask) {
+    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N) return;
     const int *pid = (const int *)(f + 24 * N) + N;
-    for (size_t j = 0; j < N; j++) {
-        size_t p = (size_t)pid[j];
-        for (int k = 0; k < 3; k++) {
-            if (coord) coord[3 * p + k] = (double)f[k * N + j];
-            if (vel) vel[3 * p + k] = (double)f[(3 + k) * N + j];
-        }
-        if (F)
-            for (int k = 0; k < 9; k++) F[9 * p + k] = (double)f[(6 + k) * N + j];
-        if (stress)
-            for (int k = 0; k < 6; k++) stress[6 * p + k] = (double)f[(15 + k) * N + j];
-        if (vol) vol[p] = (double)f[23 * N + j];
-    }
+    const size_t p = (size_t)pid[j];
+    if (mask & 1)
+        for (int k = 0; k < 3; k++) st[ST_X * N + 3 * p + k] = (double)f[k * N + j];
+    if (mask & 2)
+        for (int k = 0; k < 3; k++) st[ST_V * N + 3 * p + k] = (double)f[(3 + k) * N + j];
+    if (mask & 4)
+        for (int k = 0; k < 9; k++)
+            st[ST_F * N + 9 * p + k] = (double)f[(6 + k) * N + j] + (sizeof(R) == 4 && (k % 4) == 0 ? 1.0 : 0.0);
+    if (mask & 8)
+        for (int k = 0; k < 6; k++) st[ST_S * N + 6 * p + k] = (double)f[(15 + k) * N + j];
+    if (mask & 16) st[ST_VOL * N + p] = (double)f[23 * N + j];
+}
+
+template <typename R>
+__global__ void k_state_scatter(R *f, size_t N, const double *st, unsigned mask) {
+    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N) return;
+    const int *pid = (const int *)(f + 24 * N) + N;
+    const size_t p = (size_t)pid[j];
+    if (mask & 1)
+        for (int k = 0; k < 3; k++) f[k * N + j] = (R)st[ST_X * N + 3 * p + k];
+    if (mask & 2)
+        for (int k = 0; k < 3; k++) f[(3 + k) * N + j] = (R)st[ST_V * N + 3 * p + k];
+    if (mask & 4)
+        for (int k = 0; k < 9; k++)
+            f[(6 + k) * N + j] = (R)(st[ST_F * N + 9 * p + k] - (sizeof(R) == 4 && (k % 4) == 0 ? 1.0 : 0.0));
+    if (mask & 8)
+        for (int k = 0; k < 6; k++) f[(15 + k) * N + j] = (R)st[ST_S * N + 6 * p + k];
+    if (mask & 16) f[23 * N + j] = (R)st[ST_VOL * N + p];
+}
+}  // namespace mpm
+
+static mpm_status ensure_staging(mpm_ctx *c) {
+    if (c->d_stage) return MPM_OK;
+    CK(cudaMalloc((void **)&c->d_stage, sizeof(double) * ST_W * (size_t)c->num));
     return MPM_OK;
 }
 
 mpm_status mpm_gpu_download_particles(mpm_ctx *c, double *coord, double *vel, double *F, double *stress, double *vol) {
     if (!c) return MPM_ERR_BAD_ARG;
-    CK(cudaStreamSynchronize(c->stream));
     if (c->num == 0) return MPM_OK;
-    return c->precision == 64 ? dl_particles<double>(c, coord, vel, F, stress, vol)
-                              : dl_particles<float>(c, coord, vel, F, stress, vol);
+    mpm_status s = ensure_staging(c);
+    if (s != MPM_OK) return s;
+    const size_t N = (size_t)c->num;
+    unsigned mask = (coord ? 1u : 0u) | (vel ? 2u : 0u) | (F ? 4u : 0u) | (stress ? 8u : 0u) | (vol ? 16u : 0u);
+    const int nb = (int)((N + 255) / 256);
+    if (c->precision == 64) k_state_gather<double><<<nb, 256, 0, c->stream>>>((const double *)c->pbuf[c->cur], N, c->d_stage, mask);
+    else k_state_gather<float><<<nb, 256, 0, c->stream>>>((const float *)c->pbuf[c->cur], N, c->d_stage, mask);
+    c->launches++;
+    if (check_launch(c) != MPM_OK) return MPM_ERR_CUDA;
+    const double *st = c->d_stage;
+    if (coord) CK(cudaMemcpyAsync(coord, st + ST_X * N, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, c->stream));
+    if (vel) CK(cudaMemcpyAsync(vel, st + ST_V * N, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, c->stream));
+    if (F) CK(cudaMemcpyAsync(F, st + ST_F * N, sizeof(double) * 9 * N, cudaMemcpyDeviceToHost, c->stream));
+    if (stress) CK(cudaMemcpyAsync(stress, st + ST_S * N, sizeof(double) * 6 * N, cudaMemcpyDeviceToHost, c->stream));
+    if (vol) CK(cudaMemcpyAsync(vol, st + ST_VOL * N, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_upload_particles(mpm_ctx *c, const double *coord, const double *vel, const double *F,
+                                    const double *stress, const double *vol) {
+    if (!c) return MPM_ERR_BAD_ARG;
+    if (c->num == 0) return MPM_OK;
+    mpm_status s = ensure_staging(c);
+    if (s != MPM_OK) return s;
+    const size_t N = (size_t)c->num;
+    double *st = c->d_stage;
+    if (coord) CK(cudaMemcpyAsync(st + ST_X * N, coord, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->stream));
+    if (vel) CK(cudaMemcpyAsync(st + ST_V * N, vel, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->stream));
+    if (F) CK(cudaMemcpyAsync(st + ST_F * N, F, sizeof(double) * 9 * N, cudaMemcpyHostToDevice, c->stream));
+    if (stress) CK(cudaMemcpyAsync(st + ST_S * N, stress, sizeof(double) * 6 * N, cudaMemcpyHostToDevice, c->stream));
+    if (vol) CK(cudaMemcpyAsync(st + ST_VOL * N, vol, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+    unsigned mask = (coord ? 1u : 0u) | (vel ? 2u : 0u) | (F ? 4u : 0u) | (stress ? 8u : 0u) | (vol ? 16u : 0u);
+    const int nb = (int)((N + 255) / 256);
+    if (c->precision == 64) k_state_scatter<double><<<nb, 256, 0, c->stream>>>((double *)c->pbuf[c->cur], N, st, mask);
+    else k_state_scatter<float><<<nb, 256, 0, c->stream>>>((float *)c->pbuf[c->cur], N, st, mask);
+    c->launches++;
+    return check_launch(c);
 }
 
 mpm_status mpm_gpu_get_stats(mpm_ctx *c, mpm_stats *out) {

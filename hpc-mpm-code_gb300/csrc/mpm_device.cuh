@@ -191,6 +191,38 @@ __device__ __forceinline__ void neo_hookean_stress(R *s, const R F[3][3], R jac,
     s[5] = (mu * be[0][1]) / jac;
 }
 
+// The same stress from the displacement gradient H = F - I and jm1 = J - 1,
+// used by the FP32 path, which stores H: be - I = H + H^T + H H^T keeps the
+// small strain out of the rounding of F F^T.
+__device__ __forceinline__ void neo_hookean_stress_h(float *s, const float H[3][3], float jm1, float E, float nu) {
+    const float lmd = nu * E / ((1.0f + nu) * (1.0f - 2.0f * nu));
+    const float mu = E / (2.0f * (1.0f + nu));
+    const float lnj = log1pf(jm1);
+    const float J = 1.0f + jm1;
+    float bm[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+            bm[i][j] = H[i][j] + H[j][i] + H[i][0] * H[j][0] + H[i][1] * H[j][1] + H[i][2] * H[j][2];
+    s[0] = (mu * bm[0][0] + lmd * lnj) / J;
+    s[1] = (mu * bm[1][1] + lmd * lnj) / J;
+    s[2] = (mu * bm[2][2] + lmd * lnj) / J;
+    s[3] = (mu * bm[1][2]) / J;
+    s[4] = (mu * bm[0][2]) / J;
+    s[5] = (mu * bm[0][1]) / J;
+}
+
+// det(I + H) - 1 without forming I + H
+__device__ __forceinline__ float det_ipm1(const float H[3][3]) {
+    const float tr = H[0][0] + H[1][1] + H[2][2];
+    const float m2 = H[0][0] * H[1][1] + H[0][0] * H[2][2] + H[1][1] * H[2][2] - H[0][1] * H[1][0] -
+                     H[0][2] * H[2][0] - H[1][2] * H[2][1];
+    const float d = H[0][0] * (H[1][1] * H[2][2] - H[1][2] * H[2][1]) + H[0][1] * (H[1][2] * H[2][0] - H[1][0] * H[2][2]) +
+                    H[0][2] * (H[1][0] * H[2][1] - H[1][1] * H[2][0]);
+    return tr + m2 + d;
+}
+
 template <typename R>
 __device__ __forceinline__ R det3(const R a[3][3]) {
     return a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) + a[0][1] * (a[1][2] * a[2][0] - a[1][0] * a[2][2]) +

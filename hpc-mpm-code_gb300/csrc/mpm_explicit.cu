@@ -791,7 +791,9 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
         axis_eval<R, OZ>(x[2], a.g, 2, cz, az);
         R D[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
         R xn[3] = {x[0], x[1], x[2]};
+        R du[3] = {(R)0, (R)0, (R)0};
         R gu[3] = {(R)0, (R)0, (R)0};
+        constexpr bool FP64 = sizeof(R) == 8;
 #pragma unroll
         for (int k = 0; k <= OZ; k++)
 #pragma unroll
@@ -807,15 +809,26 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
                     for (int r = 0; r < 3; r++)
 #pragma unroll
                         for (int c = 0; c < 3; c++) D[r][c] += dn[c] * nv[r] * a.dt;
-                    const R Nd = N_ * a.dt;
+                    if (FP64) {
+                        // FLIP::VarG2P on coord, term by term as the reference adds them
+                        const R Nd = N_ * a.dt;
 #pragma unroll
-                    for (int c = 0; c < 3; c++) xn[c] += Nd * nv[c];   // FLIP::VarG2P on coord
+                        for (int c = 0; c < 3; c++) xn[c] += Nd * nv[c];
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < 3; c++) du[c] += N_ * nv[c];
+                    }
                     if (rb0 != (R)0) {
                         const R e = ld(a.nei + gn);
 #pragma unroll
                         for (int c = 0; c < 3; c++) gu[c] += dn[c] * e;
                     }
                 }
+        if (!FP64) {
+            // FP32: one rounding of the position per step
+#pragma unroll
+            for (int c = 0; c < 3; c++) xn[c] += du[c] * a.dt;
+        }
         if (rb0 != (R)0) {
             const R tv = (R)2 * ld(P.vol + p);
 #pragma unroll
@@ -828,7 +841,8 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
 #pragma unroll
             for (int c = 0; c < 3; c++) F[r][c] = ld(P.F[3 * r + c] + p);
         R Dm[3][3];   // delta_def_grad - I as the stress update sees it
-        if (sizeof(R) == 8) {
+        R J;
+        if constexpr (FP64) {
             // FP64 keeps the reference's arithmetic: ddg = D + I, F = ddg F, deps = ddg_ii - 1
             R ddg[3][3];
 #pragma unroll
@@ -845,20 +859,22 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
                     Fn[r][c] = acc;
                     Dm[r][c] = (r == c) ? ddg[r][c] - (R)1 : ddg[r][c];
                 }
+            J = det3(Fn);
         } else {
-            // FP32: F + D F keeps the small increment out of the rounding of I + D
+            // FP32 stores H = F - I: H <- H + D + D H keeps the small strain exact to
+            // FP32 rounding instead of to the rounding of numbers near 1
 #pragma unroll
             for (int r = 0; r < 3; r++)
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
-                    R acc = F[r][c];
+                    R acc = F[r][c] + D[r][c];
 #pragma unroll
                     for (int k2 = 0; k2 < 3; k2++) acc += D[r][k2] * F[k2][c];
                     Fn[r][c] = acc;
                     Dm[r][c] = D[r][c];
                 }
+            J = (R)1 + (R)det_ipm1((const float(*)[3])Fn);
         }
-        const R J = det3(Fn);
         const R volp = J * ld(P.vol0 + p);
         R s[6];
 #pragma unroll
@@ -869,7 +885,8 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
         if (model == 0) {
             lin_elast_update(s, Dm, E, nu);
         } else if (model == 1) {
-            neo_hookean_stress(s, Fn, J, E, nu);
+            if constexpr (sizeof(R) == 8) neo_hookean_stress(s, Fn, J, E, nu);
+            else neo_hookean_stress_h(s, Fn, det_ipm1(Fn), E, nu);
         } else if (model == -1) {
 #pragma unroll
             for (int k = 0; k < 6; k++) s[k] = (R)0;

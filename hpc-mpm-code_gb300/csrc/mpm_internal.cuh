@@ -2,7 +2,8 @@
 //
 // Data layout in HBM
 //   particles: structure of arrays, one array per scalar component, in the
-//     context's precision R (float or double): x[3], v[3], F[9] (row major),
+//     context's precision R (float or double): x[3], v[3], F[9] (row major;
+//     FP32 stores the displacement gradient F - I in these arrays),
 //     sigma[6] (Voigt xx,yy,zz,yz,xz,xy), m, vol0, vol; plus matid and the
 //     particle's load index (pid).  Two copies exist; a re-sort permutes A
 //     into B and swaps.
@@ -131,6 +132,7 @@ struct mpm_ctx {
     int *d_key = nullptr, *d_perm = nullptr, *d_tcount = nullptr, *d_tstart = nullptr, *d_tcursor = nullptr;
     int *d_tmp = nullptr, *d_perm2 = nullptr;   // per-brick cell sort
     int *d_cstart = nullptr;                    // nbricks * (BRC + 1) cell start offsets
+    double *d_stage = nullptr;                  // FP64 AoS staging for host <-> device particle state
     mpm::WorkItem *d_work = nullptr;
     int *d_nwork = nullptr;
     int nwork_cap = 0;

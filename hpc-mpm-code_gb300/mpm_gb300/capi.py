@@ -59,7 +59,8 @@ _ip = C.POINTER(C.c_int)
 
 EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_status_string",
            "mpm_gpu_load_particles", "mpm_gpu_set_bc", "mpm_gpu_p2g", "mpm_gpu_grid_update", "mpm_gpu_g2p",
-           "mpm_gpu_step_explicit", "mpm_gpu_download_nodal", "mpm_gpu_download_particles", "mpm_gpu_sync",
+           "mpm_gpu_step_explicit", "mpm_gpu_download_nodal", "mpm_gpu_download_particles",
+           "mpm_gpu_upload_particles", "mpm_gpu_sync",
            "mpm_gpu_get_stats", "mpm_gpu_enable_kernel_timing", "mpm_gpu_kernel_times"]
 
 
@@ -87,6 +88,7 @@ def load(path: str | None = None):
     lib.mpm_gpu_step_explicit.argtypes = [C.c_void_p, C.c_int, C.c_double]
     lib.mpm_gpu_download_nodal.argtypes = [C.c_void_p, C.c_int, _dp]
     lib.mpm_gpu_download_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
+    lib.mpm_gpu_upload_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
     lib.mpm_gpu_sync.argtypes = [C.c_void_p]
     lib.mpm_gpu_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     lib.mpm_gpu_enable_kernel_timing.argtypes = [C.c_void_p, C.c_int]
@@ -199,6 +201,16 @@ class GpuSolid:
              "mpm_gpu_download_particles")
         return {"x": x.reshape(n, 3), "v": v.reshape(n, 3), "F": F.reshape(n, 3, 3), "sigma": sig.reshape(n, 6),
                 "vol": vol}
+
+    def download_into(self, coord=None, vel=None, F=None, stress=None, vol=None):
+        """Download into caller-provided C-contiguous float64 arrays (pinned for full speed)."""
+        _chk(self.lib.mpm_gpu_download_particles(self.ctx, _ptr(coord), _ptr(vel), _ptr(F), _ptr(stress), _ptr(vol)),
+             "mpm_gpu_download_particles")
+
+    def upload_state(self, coord=None, vel=None, F=None, stress=None, vol=None):
+        """Overwrite particle state from float64 host arrays in load order."""
+        _chk(self.lib.mpm_gpu_upload_particles(self.ctx, _ptr(coord), _ptr(vel), _ptr(F), _ptr(stress), _ptr(vol)),
+             "mpm_gpu_upload_particles")
 
     def stats(self):
         st = Stats()

@@ -116,9 +116,18 @@ mpm_status mpm_gpu_step_explicit(mpm_ctx *ctx, int nsteps, double facl);
  * (MaterialPoint members, module/material_point.h:151-153; nvol from mesh.h).
  * Vectors are written component-major (3*nodec). Synchronises the stream. */
 mpm_status mpm_gpu_download_nodal(mpm_ctx *ctx, int field, double *host);
-/* Particles in the order they were loaded; any pointer may be NULL. */
+/* Particles in the order they were loaded; any pointer may be NULL.  The
+ * state of the particle vectors (coord, vel, def_grad, stress, vol) that the
+ * reference's drivers read after Node2Particle (module/material_point.h:186-198).
+ * Host buffers in pinned memory transfer at full link speed. */
 mpm_status mpm_gpu_download_particles(mpm_ctx *ctx, double *coord, double *vel, double *F, double *stress,
                                       double *vol);
+/* Overwrites the state of the loaded particles (same count, load order) from
+ * host arrays; NULL leaves a field unchanged.  Replaces writing the particle
+ * vectors between steps (e.g. SolidMaterialPointBase::RestartInput,
+ * module/solid/solid_data_io.cpp:61-100). */
+mpm_status mpm_gpu_upload_particles(mpm_ctx *ctx, const double *coord, const double *vel, const double *F,
+                                    const double *stress, const double *vol);
 /* Wait for the stream and return (and clear) any latched device error. */
 mpm_status mpm_gpu_sync(mpm_ctx *ctx);
 
