@@ -53,7 +53,17 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cells", type=int, default=80,
+                    help="block edge in cells (80 = the 4,096,000-particle workload; smaller for profiling)")
     return ap.parse_args()
+
+
+def workload(cells):
+    from mpm_gb300 import scenes
+
+    if cells == 80:
+        return scenes.spinning_block()
+    return scenes.spinning_block(grid=(cells + 48,) * 3, cell_lo=(24, 24, 24), cells=(cells,) * 3)
 
 
 def dist_env():
@@ -144,27 +154,45 @@ def cpu_baseline(scene, steps):
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's algorithm on this host.
+
+    Each of the K timed steps is one FP64 explicit step of a block of the same
+    workload (same dx, dt, particle density, velocity field and compressed
+    quarter), with the block edge chosen so that W + K steps take about two
+    minutes on one core; the reference's solid path is single-threaded per
+    MPI rank and its MPI+PETSc build cannot be produced on this host.
+    """
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from mpm_gb300 import scenes
+    from oracle import port
 
-    s = scenes.spinning_block()
-    base = cpu_baseline(s, 1)   # warm-up leg, discarded
-    vals = []
-    for _ in range(max(1, args.steps)):
-        vals.append(cpu_baseline(s, max(1, args.cpu_steps))["value"])
-    v = statistics.median(vals)
+    K, W = max(1, args.steps), max(0, args.warmup)
+    probe = workload(24)
+    o = port.PortSolid(probe)
+    o.steps(1)
+    t0 = time.perf_counter()
+    o.steps(2)
+    rate = probe.num * 2 / (time.perf_counter() - t0)
+    del o
+    budget = 120.0
+    cells = int(((budget * rate) / (8.0 * (K + W))) ** (1.0 / 3.0))
+    cells = max(8, min(args.cells, cells - cells % 4))
+    s = workload(cells)
+    o = port.PortSolid(s)
+    o.steps(W)
+    t0 = time.perf_counter()
+    o.steps(K)
+    dt = time.perf_counter() - t0
+    v = s.num * K / dt
+    sample = (f"{K} FP64 explicit steps of a {cells}^3-cell block ({s.num} particles) of the workload "
+              f"({dt:.1f} s on 1 core)")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "steps": K, "warmup": W, "ms_per_step": dt / K * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD.replace("FP32", "FP64 CPU"), "particles": s.num, "grid": list(s.xyelem)},
-            "cpu_baseline": {"value": v, "unit": METRIC, "cores": 1, "kind": "port",
-                             "sample": f"{args.steps} x {args.cpu_steps} FP64 steps of the full workload; the "
-                                       "reference MPI+PETSc build cannot be produced on this host and its code "
-                                       "is single-threaded per rank"},
+            "config": {"workload": WORKLOAD, "particles_per_step_sample": s.num, "grid": list(s.xyelem)},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": 1, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    del base
     print(json.dumps(line), flush=True)
 
 
@@ -177,10 +205,10 @@ def run_gb300(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    from mpm_gb300 import build, capi, scenes
+    from mpm_gb300 import build, capi
 
     build.build()
-    s = scenes.spinning_block()
+    s = workload(args.cells)
     stream = torch.cuda.Stream()
     gpu = capi.GpuSolid(s, precision=32, stream=stream.cuda_stream)
     hbm_peak, peak_kind = measured_peaks()
@@ -278,7 +306,8 @@ def run_gb300(args):
         line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": WORKLOAD, "particles": s.num, "grid": list(s.xyelem), "nodes": s.nodec,
+                "config": {"workload": WORKLOAD if args.cells == 80 else f"{WORKLOAD} (block of {args.cells}^3 cells)",
+                           "particles": s.num, "grid": list(s.xyelem), "nodes": s.nodec,
                            "dt": s.dt, "scheme": "PIC", "parallelism": f"replicas x{world}",
                            "l2": "inputs larger than L2: 393 MB particle state per step, no flush"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(),

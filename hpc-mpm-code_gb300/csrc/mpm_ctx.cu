@@ -232,8 +232,9 @@ template <typename R>
 static mpm_status upload_particles(mpm_ctx *c, int64_t n, const double *coord, const double *vel, const double *mass,
                                    const double *vol0, const double *F, const double *stress, const int *matid) {
     size_t N = (size_t)n;
-    size_t bytes = N * (24 * sizeof(R) + 2 * sizeof(int));
-    std::vector<char> host(bytes);
+    const int nr = c->nreal;
+    size_t bytes = N * (nr * sizeof(R) + 2 * sizeof(int));
+    std::vector<char> host(bytes, 0);
     R *f = (R *)host.data();
     double vmax = 0.0, volmax = 0.0, vsmax = 0.0, mmax = 0.0;
     for (size_t p = 0; p < N; p++) {
@@ -263,7 +264,7 @@ static mpm_status upload_particles(mpm_ctx *c, int64_t n, const double *coord, c
                          fmax(fabs(s[5]) + fabs(s[1]) + fabs(s[3]), fabs(s[4]) + fabs(s[3]) + fabs(s[2])));
         vsmax = fmax(vsmax, fabs(vol0[p]) * rs);
     }
-    int *ip = (int *)(f + 24 * N);
+    int *ip = (int *)(f + nr * N);
     for (size_t p = 0; p < N; p++) {
         int mid = matid ? matid[p] : 0;
         if (mid < 0 || mid >= c->nmat) return MPM_ERR_BAD_ARG;
@@ -296,7 +297,7 @@ mpm_status mpm_gpu_load_particles(mpm_ctx *c, int64_t n, const double *coord, co
     free_particles(c);
     c->num = n;
     size_t N = (size_t)(n > 0 ? n : 1);
-    size_t bytes = N * (24 * c->rsize + 2 * sizeof(int));
+    size_t bytes = N * (c->nreal * c->rsize + 2 * sizeof(int));
     CK(cudaMalloc(&c->pbuf[0], bytes));
     CK(cudaMalloc(&c->pbuf[1], bytes));
     CK(cudaMalloc((void **)&c->d_key, sizeof(int) * N));
@@ -484,10 +485,10 @@ namespace mpm {
 constexpr int ST_X = 0, ST_V = 3, ST_F = 6, ST_S = 15, ST_VOL = 21, ST_W = 22;
 
 template <typename R>
-__global__ void k_state_gather(const R *f, size_t N, double *st, unsigned mask) {
+__global__ void k_state_gather(const R *f, size_t N, int nreal, double *st, unsigned mask) {
     const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= N) return;
-    const int *pid = (const int *)(f + 24 * N) + N;
+    const int *pid = (const int *)(f + nreal * N) + N;
     const size_t p = (size_t)pid[j];
     if (mask & 1)
         for (int k = 0; k < 3; k++) st[ST_X * N + 3 * p + k] = (double)f[k * N + j];
@@ -501,11 +502,29 @@ __global__ void k_state_gather(const R *f, size_t N, double *st, unsigned mask) 
     if (mask & 16) st[ST_VOL * N + p] = (double)f[23 * N + j];
 }
 
+// Also raises the fixed-point bounds of the next P2G to cover the new state.
 template <typename R>
-__global__ void k_state_scatter(R *f, size_t N, const double *st, unsigned mask) {
+__global__ void k_state_scatter(R *f, size_t N, int nreal, const double *st, unsigned mask, DevCtl *ctl,
+                                int parity) {
     const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= N) return;
-    const int *pid = (const int *)(f + 24 * N) + N;
+    {
+        const size_t p = (size_t)((const int *)(f + nreal * N) + N)[j];
+        if (mask & 2) {
+            float vm = 0.0f;
+            for (int k = 0; k < 3; k++) vm = fmaxf(vm, fabsf((float)st[ST_V * N + 3 * p + k]));
+            atomic_max_pos(&ctl->nxt[parity][B_VMAX], vm * 1.000001f);
+        }
+        const float vol = (mask & 16) ? fabsf((float)st[ST_VOL * N + p]) : fabsf((float)f[23 * N + j]);
+        if (mask & 16) atomic_max_pos(&ctl->nxt[parity][B_VOLMAX], vol * 1.000001f);
+        if (mask & 8) {
+            const double *s6 = st + ST_S * N + 6 * p;
+            const double rs = fmax(fabs(s6[0]) + fabs(s6[5]) + fabs(s6[4]),
+                                   fmax(fabs(s6[5]) + fabs(s6[1]) + fabs(s6[3]), fabs(s6[4]) + fabs(s6[3]) + fabs(s6[2])));
+            atomic_max_pos(&ctl->nxt[parity][B_VOLSMAX], (float)(vol * rs) * 1.000001f);
+        }
+    }
+    const int *pid = (const int *)(f + nreal * N) + N;
     const size_t p = (size_t)pid[j];
     if (mask & 1)
         for (int k = 0; k < 3; k++) f[k * N + j] = (R)st[ST_X * N + 3 * p + k];
@@ -534,8 +553,8 @@ mpm_status mpm_gpu_download_particles(mpm_ctx *c, double *coord, double *vel, do
     const size_t N = (size_t)c->num;
     unsigned mask = (coord ? 1u : 0u) | (vel ? 2u : 0u) | (F ? 4u : 0u) | (stress ? 8u : 0u) | (vol ? 16u : 0u);
     const int nb = (int)((N + 255) / 256);
-    if (c->precision == 64) k_state_gather<double><<<nb, 256, 0, c->stream>>>((const double *)c->pbuf[c->cur], N, c->d_stage, mask);
-    else k_state_gather<float><<<nb, 256, 0, c->stream>>>((const float *)c->pbuf[c->cur], N, c->d_stage, mask);
+    if (c->precision == 64) k_state_gather<double><<<nb, 256, 0, c->stream>>>((const double *)c->pbuf[c->cur], N, c->nreal, c->d_stage, mask);
+    else k_state_gather<float><<<nb, 256, 0, c->stream>>>((const float *)c->pbuf[c->cur], N, c->nreal, c->d_stage, mask);
     c->launches++;
     if (check_launch(c) != MPM_OK) return MPM_ERR_CUDA;
     const double *st = c->d_stage;
@@ -563,8 +582,11 @@ mpm_status mpm_gpu_upload_particles(mpm_ctx *c, const double *coord, const doubl
     if (vol) CK(cudaMemcpyAsync(st + ST_VOL * N, vol, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
     unsigned mask = (coord ? 1u : 0u) | (vel ? 2u : 0u) | (F ? 4u : 0u) | (stress ? 8u : 0u) | (vol ? 16u : 0u);
     const int nb = (int)((N + 255) / 256);
-    if (c->precision == 64) k_state_scatter<double><<<nb, 256, 0, c->stream>>>((double *)c->pbuf[c->cur], N, st, mask);
-    else k_state_scatter<float><<<nb, 256, 0, c->stream>>>((float *)c->pbuf[c->cur], N, st, mask);
+    const int par = (int)(c->step & 1);
+    if (c->precision == 64)
+        k_state_scatter<double><<<nb, 256, 0, c->stream>>>((double *)c->pbuf[c->cur], N, c->nreal, st, mask, c->d_ctl, par);
+    else
+        k_state_scatter<float><<<nb, 256, 0, c->stream>>>((float *)c->pbuf[c->cur], N, c->nreal, st, mask, c->d_ctl, par);
     c->launches++;
     return check_launch(c);
 }

@@ -947,7 +947,8 @@ static StepArgs<R> make_args(mpm_ctx *c) {
     a.P.m = f + 21 * n;
     a.P.vol0 = f + 22 * n;
     a.P.vol = f + 23 * n;
-    a.P.matid = (int *)(base + 24 * n * rs);
+    for (int k = 0; k < 3; k++) a.P.a[k] = c->nreal == 27 ? f + (24 + k) * n : nullptr;
+    a.P.matid = (int *)(base + (size_t)c->nreal * n * rs);
     a.P.pid = a.P.matid + n;
     a.work = c->d_work;
     a.nwork = c->d_nwork;

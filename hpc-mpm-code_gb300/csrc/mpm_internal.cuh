@@ -71,6 +71,7 @@ struct DevCtl {
 template <typename R>
 struct Particles {
     R *x[3], *v[3], *F[9], *s[6], *m, *vol0, *vol;
+    R *a[3];          // particle acceleration (implicit contexts only, else null)
     int *matid, *pid;
 };
 
@@ -116,6 +117,7 @@ struct mpm_ctx {
     // particles
     int64_t num = 0;
     size_t rsize = 4;
+    int nreal = 24;                        // real fields per particle: 24, or 27 with acceleration (implicit)
     void *pbuf[2] = {nullptr, nullptr};   // two SoA copies
     int cur = 0;
     double mmax = 0.0;

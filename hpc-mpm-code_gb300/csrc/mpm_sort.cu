@@ -154,17 +154,17 @@ __global__ void __launch_bounds__(BRC) k_cell_sort(const int *bstart, const int 
     }
 }
 
-// dst[j] = src[perm[j]] for all 24 real fields and the two int fields.
+// dst[j] = src[perm[j]] for all real fields and the two int fields.
 template <typename R>
-__global__ void k_permute(const R *src, R *dst, const int *perm, int n) {
+__global__ void k_permute(const R *src, R *dst, const int *perm, int n, int nreal) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     int i = perm[j];
     size_t N = (size_t)n;
 #pragma unroll 4
-    for (int f = 0; f < 24; f++) dst[f * N + j] = src[f * N + i];
-    const int *si = (const int *)(src + 24 * N);
-    int *di = (int *)(dst + 24 * N);
+    for (int f = 0; f < nreal; f++) dst[f * N + j] = src[f * N + i];
+    const int *si = (const int *)(src + nreal * N);
+    int *di = (int *)(dst + nreal * N);
     di[j] = si[i];
     di[N + j] = si[N + i];
 }
@@ -186,7 +186,7 @@ static mpm_status sort_impl(mpm_ctx *c) {
     const R *src = (const R *)c->pbuf[c->cur];
     R *dst = (R *)c->pbuf[c->cur ^ 1];
     size_t N = (size_t)n;
-    const int *pid = (const int *)(src + 24 * N) + N;
+    const int *pid = (const int *)(src + c->nreal * N) + N;
     int nb = (n + 255) / 256;
     timer_begin(c, K_BIN);
     k_bin<R><<<nb, 256, 0, c->stream>>>(g, c->g.nbrick[0], c->g.nbrick[1], src, src + N, src + 2 * N, n, c->d_key,
@@ -202,7 +202,7 @@ static mpm_status sort_impl(mpm_ctx *c) {
                                                       c->d_cstart);
     timer_end(c, K_SCATTER);
     timer_begin(c, K_PERMUTE);
-    k_permute<R><<<nb, 256, 0, c->stream>>>(src, dst, c->d_perm, n);
+    k_permute<R><<<nb, 256, 0, c->stream>>>(src, dst, c->d_perm, n, c->nreal);
     timer_end(c, K_PERMUTE);
     c->launches += 5;
     c->cur ^= 1;
