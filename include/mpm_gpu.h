@@ -151,6 +151,27 @@ mpm_status mpm_gpu_get_stats(mpm_ctx *ctx, mpm_stats *out);
 mpm_status mpm_gpu_enable_kernel_timing(mpm_ctx *ctx, int on);
 mpm_status mpm_gpu_kernel_times(mpm_ctx *ctx, int *count, const char **names, double *ms, int64_t *launches);
 
+/* ---- allocation-free P2G -----------------------------------------------------
+ * No counterpart in the reference: an extra entry point for callers that
+ * cannot let a library allocate device memory (a host program that owns
+ * every allocation through its own pool, or a time loop that must not hit
+ * the device-wide synchronisation of cudaMalloc/cudaFree).  It runs the P2G
+ * scatter of Particle2NodeS for linear shape functions and writes nmass,
+ * nvof (zeroed below mtol), nmome and nforce (component-major, 3*nodec) into
+ * caller-owned device arrays.  Inputs are caller-owned device arrays in
+ * structure-of-arrays FP32 layout: x and v as three blocks of n, stress as
+ * six Voigt blocks of n, mass and vol of n.  Launches on `stream`
+ * (a cudaStream_t, NULL = default stream) and returns without waiting.
+ * Scratch: one static device array sized for at most 262,144 control points
+ * (64^3); larger grids return MPM_ERR_BAD_ARG.  Every call shares that array
+ * and clears it first, so calls that overlap on the GPU race.  The first call
+ * on a device looks up the array's address (cudaGetSymbolAddress) and should
+ * come before any stream capture.  Nothing is allocated or freed. */
+mpm_status mpm_gpu_p2g_noalloc(const mpm_grid_desc *grid, const double *gravity, double facl, double mtol, int64_t n,
+                               const float *x, const float *v, const float *stress, const float *mass,
+                               const float *vol, float *nmass, float *nvof, float *nmome, float *nforce,
+                               void *stream);
+
 #ifdef __cplusplus
 }
 #endif
