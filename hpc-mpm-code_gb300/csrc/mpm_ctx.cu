@@ -86,6 +86,7 @@ const char *mpm_gpu_status_string(mpm_status s) {
     case MPM_ERR_CUDA: return "CUDA error";
     case MPM_ERR_STATE: return "call out of order";
     case MPM_ERR_UNSUPPORTED: return "unsupported configuration";
+    case MPM_ERR_NEWTON_MAXIT: return "Newton iteration did not converge";
     }
     return "unknown";
 }
@@ -142,6 +143,7 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     c->shifting = cfg->shifting ? 1 : 0;
     c->resort_period = cfg->resort_period > 0 ? cfg->resort_period : 8;
     c->cell_scatter = cfg->scatter == 1 ? 0 : 1;
+    c->nreal = cfg->implicit ? 27 : 24;
     c->dt = cfg->dt;
     c->mtol = cfg->mtol;
     c->nmat = mat->nmat;
@@ -200,6 +202,7 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
 void mpm_gpu_destroy(mpm_ctx *c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    implicit_free(c);
     free_particles(c);
     free_dev(c->d_iprop);
     free_dev(c->d_matprop);

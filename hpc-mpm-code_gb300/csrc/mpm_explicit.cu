@@ -59,6 +59,7 @@ struct StepArgs {
     int scheme;
     int shifting;
     int all_tiles;              // process every tile in the grid passes (download mode)
+    int implicit;               // implicit solid: the force fields carry sum N m a (AccelP2G)
     double nump;                // particle count as a bound factor
     double mmax;                // max particle mass
     double gshape;              // bound on |dN/dx|
@@ -101,7 +102,9 @@ __device__ void compute_scales(const StepArgs<R> &a, Scales &s) {
     s.m = make_fix(a.nump * a.mmax);
     s.v = make_fix(a.nump * (double)bits_f(nb[B_VOLMAX]));
     s.p = make_fix(a.nump * a.mmax * (double)bits_f(nb[B_VMAX]));
-    s.f = make_fix(a.nump * ((double)bits_f(nb[B_VOLSMAX]) * 3.0 * a.gshape + a.mmax * gabs * fabs((double)a.facl)));
+    s.f = a.implicit ? make_fix(a.nump * a.mmax * (double)bits_f(nb[B_AMAX]) * 1.0000001)
+                     : make_fix(a.nump * ((double)bits_f(nb[B_VOLSMAX]) * 3.0 * a.gshape +
+                                          a.mmax * gabs * fabs((double)a.facl)));
     double vb = (double)bits_f(a.ctl->cur[C_GMAX]);
     if (a.scheme == MPM_FLIP) vb = (double)bits_f(nb[B_VMAX]) + fabs((double)a.dt) * vb;
     s.q = make_fix(a.nump * a.mmax * vb * 1.0000001);
@@ -481,6 +484,10 @@ __global__ void __launch_bounds__(256) k_p2g_box(StepArgs<R> a) {
         const int lx = cx - ox, ly = cy - oy, lz = cz - oz;
         const bool in = (unsigned)lx < (unsigned)BRX && (unsigned)ly < (unsigned)BRY && (unsigned)lz < (unsigned)BRZ;
         misses += !in;
+        R pa[3] = {(R)0, (R)0, (R)0};
+        if (a.implicit) {
+            pa[0] = ld(P.a[0] + p); pa[1] = ld(P.a[1] + p); pa[2] = ld(P.a[2] + p);
+        }
 #pragma unroll
         for (int k = 0; k <= OZ; k++)
 #pragma unroll
@@ -491,6 +498,13 @@ __global__ void __launch_bounds__(256) k_p2g_box(StepArgs<R> a) {
                     R q[NACC];
                     p2g_terms(wxy * az.w[k], ax.dw[i] * ay.w[j] * az.w[k], ax.w[i] * ay.dw[j] * az.w[k],
                               wxy * az.dw[k], m, vol, v, s, mfx, mfy, mfz, q);
+                    if (a.implicit) {
+                        // AccelP2G (map_and_interpolate.cpp:42-53): nforce += N m a
+                        const R Nm = wxy * az.w[k] * m;
+                        q[5] = Nm * pa[0];
+                        q[6] = Nm * pa[1];
+                        q[7] = Nm * pa[2];
+                    }
                     long long o[NACC];
                     fx_terms(q, S, o);
                     if (in) {
@@ -977,6 +991,7 @@ static StepArgs<R> make_args(mpm_ctx *c) {
     a.scheme = c->scheme;
     a.shifting = c->shifting;
     a.all_tiles = c->write_nodal_dl ? 1 : 0;
+    a.implicit = c->nreal == 27 ? 1 : 0;
     a.nump = (double)c->num;
     a.mmax = c->mmax;
     double gs = 0.0, gsum = 0.0;

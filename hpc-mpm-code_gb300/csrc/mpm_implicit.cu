@@ -1,0 +1,1004 @@
+// Implicit solid MPM on the GPU (FP64): generalized-alpha / Newmark time
+// integration, Newton iteration, assembly of the stiffness operator into a
+// 27-point block stencil, symmetric diagonal scaling, and a preconditioned
+// conjugate-gradient solve with FP64 reductions.
+//
+// Reference (module/solid/implicit/, module/solver/, module/nonlinear_time_integration.cpp):
+//   Particle2Node            var_trans_solid_implicit.cpp:20-80      -> run_p2g (AccelP2G mode) + k_imp_grid
+//   SolveSolid (Newton)      solve_solid_implicit.cpp:65-103         -> implicit_newton
+//   BCNRSet / Predict        implicit_mpm_solid.h:55-64,
+//                            nonlinear_time_integration.cpp:59-71    -> k_imp_bcnr, k_imp_predict
+//   AssembleSystem           solve_solid_implicit.cpp:105-204        -> k_imp_assemble, k_imp_rhs_diag
+//   ComputeTangentModulus    solve_solid_implicit.cpp:34-63          -> tangent() below
+//   BuildDiagonalPreconditioner crsmat.cpp:87-184                     -> k_imp_rhs_diag, k_imp_scale
+//   MatVecMult               solver.cpp:405-433                      -> k_imp_matvec
+//   GPBiCGSafe               solver.cpp:19-141                       -> conjugate gradients (the scaled
+//                            system is symmetric), stopped on the same squared-norm ratio
+//   CheckNRConvergence       solver.cpp:484-593                      -> newton_residuals
+//   Node2Particle            var_trans_solid_implicit.cpp:106-167,
+//                            nonlinear_time_integration.cpp:73-96    -> k_imp_g2p, k_imp_shift
+//
+// Matrix storage: for control point n and stencil slot s (the 27 neighbours
+// n + (dx, dy, dz), dx,dy,dz in {-1,0,1}, s = (dx+1) + 3 (dy+1) + 9 (dz+1)),
+// the 3x3 block entry (a, b) lives at A[(s * 9 + 3 a + b) * nodec + n]:
+// coalesced over n, no column indices (the grid is structured).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "mpm_device.cuh"
+
+namespace mpm {
+mpm_status run_p2g(mpm_ctx *c, double facl);
+}
+
+struct ImpState {
+    int nr_flag = 0;
+    double alpha_f = 1, alpha_m = 1, gamma = 0.5, beta = 0.25, nb[6] = {0};
+    double *A = nullptr;                   // 27 * 9 * nodec
+    double *adiag = nullptr, *b = nullptr;  // 3 * nodec
+    double *x = nullptr, *r = nullptr, *p = nullptr, *Ap = nullptr, *xs = nullptr;
+    double *ndispl = nullptr, *nvel = nullptr, *naccel = nullptr, *naccel_k = nullptr;
+    double *nmass = nullptr, *nvof = nullptr, *nei = nullptr;
+    double *stress_k = nullptr;            // 6 * num, Newton stress of the step
+    double *geup = nullptr;                // 3 * num
+    double *part = nullptr;                // reduction partials
+    double *scal = nullptr;                // device scalars
+    double *h_scal = nullptr;              // pinned mirror
+    int nblk = 0;
+    int64_t num_alloc = 0;
+    int64_t krylov_total = 0, newton_total = 0;
+    double last_rel = 0.0;
+};
+
+namespace mpm {
+
+enum Scal { S_RR0 = 0, S_RR1, S_PAP, S_RR_INIT, S_RES, S_IDOF, S_EU, S_GD, S_NSCAL };
+
+struct ImpArgs {
+    int nnc[3];
+    int nel[3];
+    int nodec;
+    double xmin[3], dx[3];
+    double dt, facl, mtol, grav[3];
+    double af, am, gamma, nb[6];
+    int nr_flag;
+    int shifting;
+    int scheme;
+    int64_t num;
+    const unsigned char *bcflag;
+    const double *bcval;
+    const double *nvol;
+    const int *iprop;
+    const double *matprop;
+};
+
+static ImpArgs imp_args(mpm_ctx *c) {
+    ImpArgs a;
+    memset(&a, 0, sizeof(a));
+    for (int d = 0; d < 3; d++) {
+        a.nnc[d] = c->g.nnc[d];
+        a.nel[d] = c->g.nel[d];
+        a.xmin[d] = c->g.xmin[d];
+        a.dx[d] = c->g.dx[d];
+        a.grav[d] = c->gravity[d];
+    }
+    a.nodec = c->g.nodec;
+    a.dt = c->dt;
+    a.facl = c->facl;
+    a.mtol = c->mtol;
+    ImpState *s = c->imp;
+    a.af = s->alpha_f;
+    a.am = s->alpha_m;
+    a.gamma = s->gamma;
+    for (int k = 0; k < 6; k++) a.nb[k] = s->nb[k];
+    a.nr_flag = s->nr_flag;
+    a.shifting = c->shifting;
+    a.scheme = c->scheme;
+    a.num = c->num;
+    a.bcflag = c->d_bcflag;
+    a.bcval = (const double *)c->d_bcval;
+    a.nvol = c->d_nvol;
+    a.iprop = c->d_iprop;
+    a.matprop = c->d_matprop;
+    return a;
+}
+
+struct PView {
+    double *x[3], *v[3], *F[9], *s[6], *m, *vol0, *vol, *acc[3];
+    int *matid;
+};
+
+static PView pview(mpm_ctx *c) {
+    PView v;
+    size_t n = (size_t)c->num;
+    double *f = (double *)c->pbuf[c->cur];
+    for (int k = 0; k < 3; k++) v.x[k] = f + k * n;
+    for (int k = 0; k < 3; k++) v.v[k] = f + (3 + k) * n;
+    for (int k = 0; k < 9; k++) v.F[k] = f + (6 + k) * n;
+    for (int k = 0; k < 6; k++) v.s[k] = f + (15 + k) * n;
+    v.m = f + 21 * n;
+    v.vol0 = f + 22 * n;
+    v.vol = f + 23 * n;
+    for (int k = 0; k < 3; k++) v.acc[k] = f + (24 + k) * n;
+    v.matid = (int *)(f + 27 * n);
+    return v;
+}
+
+__device__ __forceinline__ void node_ijk(int n, const int *nnc, int &i, int &j, int &k) {
+    i = n % nnc[0];
+    j = (n / nnc[0]) % nnc[1];
+    k = n / (nnc[0] * nnc[1]);
+}
+
+// Linear shape functions at x in element (cx, cy, cz): weights and gradients
+// of the 8 nodes in MakSf order (module/shape_function.cpp:28-110).
+__device__ __forceinline__ void shape8(const ImpArgs &a, const double *x, int &cx, int &cy, int &cz, double *N,
+                                       double (*dN)[3], int *nid, bool &oob) {
+    KGeom<double> g;
+    for (int d = 0; d < 3; d++) {
+        g.xmin[d] = a.xmin[d];
+        g.dx[d] = a.dx[d];
+        g.inv_dx[d] = 1.0 / a.dx[d];
+        g.nel[d] = a.nel[d];
+        g.nnc[d] = a.nnc[d];
+    }
+    cx = cell_of(x[0], g, 0, oob);
+    cy = cell_of(x[1], g, 1, oob);
+    cz = cell_of(x[2], g, 2, oob);
+    Axis<double, 1> ax, ay, az;
+    axis_linear<double>(x[0], g.xmin[0], g.dx[0], g.inv_dx[0], cx, ax);
+    axis_linear<double>(x[1], g.xmin[1], g.dx[1], g.inv_dx[1], cy, ay);
+    axis_linear<double>(x[2], g.xmin[2], g.dx[2], g.inv_dx[2], cz, az);
+    int id = 0;
+    for (int k = 0; k < 2; k++)
+        for (int j = 0; j < 2; j++)
+            for (int i = 0; i < 2; i++) {
+                N[id] = ax.w[i] * ay.w[j] * az.w[k];
+                dN[id][0] = ax.dw[i] * ay.w[j] * az.w[k];
+                dN[id][1] = ax.w[i] * ay.dw[j] * az.w[k];
+                dN[id][2] = ax.w[i] * ay.w[j] * az.dw[k];
+                nid[id] = (cx + i) + a.nnc[0] * ((cy + j) + a.nnc[1] * (cz + k));
+                id++;
+            }
+}
+
+// ------------------------------------------------------------ node kernels
+// Particle2Node's grid part: nvel = p/m, naccel = f/m, BCs (var_trans_solid_implicit.cpp:47-75)
+__global__ void k_imp_grid(ImpArgs a, const unsigned long long *acc, const double *inv, double *nmass, double *nvof,
+                           double *nvel, double *naccel) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.nodec) return;
+    const size_t N = (size_t)a.nodec;
+    const double m = (double)(long long)acc[n] * inv[0];
+    nmass[n] = m;
+    nvof[n] = (double)(long long)acc[N + n] * inv[1];
+    const unsigned char bf = a.bcflag[n];
+    for (int c = 0; c < 3; c++) {
+        double v = 0.0, ac = 0.0;
+        if (m > a.mtol) {
+            v = (double)(long long)acc[(2 + c) * N + n] * inv[2] / m;
+            ac = (double)(long long)acc[(5 + c) * N + n] * inv[3] / m;
+        }
+        if (bf & (1 << c)) {
+            v = a.bcval[c * N + n] * a.facl;
+            ac = 0.0;
+        }
+        nvel[c * N + n] = v;
+        naccel[c * N + n] = ac;
+    }
+}
+
+// BCNRSet (BCSetDt on ndispl) then PredictNewmarkBetaVelAndAccel's acceleration
+__global__ void k_imp_predict(ImpArgs a, double *ndispl, const double *nvel, const double *naccel, double *naccel_k,
+                              double *nvel_k, int set_bc) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.nodec) return;
+    const size_t N = (size_t)a.nodec;
+    const unsigned char bf = a.bcflag[n];
+    for (int c = 0; c < 3; c++) {
+        const size_t i = c * N + n;
+        if (set_bc && (bf & (1 << c))) ndispl[i] = a.bcval[i] * a.dt * a.facl;
+        const double d = ndispl[i];
+        naccel_k[i] = a.nb[3] * d - a.nb[4] * nvel[i] - a.nb[5] * naccel[i];
+        if (nvel_k) nvel_k[i] = a.nb[0] * d - a.nb[1] * nvel[i] - a.nb[2] * naccel[i];
+    }
+}
+
+// Tangent block K_ij = dNa . ce . dNb with ce[i][k][j][l] = lambda' d_ik d_jl
+// + mu' (d_ij d_kl + d_il d_kj) + (NR) sigma_kl d_ij -- the isotropic
+// stif_mat of models 0 and 1 contracted as ComputeTangentModulus does.
+__device__ __forceinline__ void tangent(const double *da, const double *db, double lam, double mu,
+                                       const double sg[3][3], int nr, double K[3][3]) {
+    const double ab = da[0] * db[0] + da[1] * db[1] + da[2] * db[2];
+    double asb = 0.0;
+    if (nr)
+        for (int k = 0; k < 3; k++) asb += da[k] * (sg[k][0] * db[0] + sg[k][1] * db[1] + sg[k][2] * db[2]);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) K[i][j] = lam * da[i] * db[j] + mu * da[j] * db[i] + (i == j ? mu * ab + asb : 0.0);
+}
+
+// ------------------------------------------------------------- assembly
+// One thread per particle (AssembleSystem, solve_solid_implicit.cpp:123-189):
+// UpdateDefGrad with alpha_f, the stress of the Newton iterate, the gradient
+// correction dN <- dN dF^-1, then 8x8 tangent blocks + lumped mass and the
+// internal/external force into the RHS, with FP64 atomics.
+__global__ void __launch_bounds__(128) k_imp_assemble(ImpArgs a, PView P, const double *ndispl, double *stress_k,
+                                                      double *A, double *b) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.num) return;
+    const size_t N = (size_t)a.nodec, NP = (size_t)a.num;
+    double x[3] = {P.x[0][p], P.x[1][p], P.x[2][p]};
+    int cx, cy, cz, nid[8];
+    double Nw[8], dN[8][3];
+    bool oob = false;
+    shape8(a, x, cx, cy, cz, Nw, dN, nid, oob);
+    // ComputeDeltaDefGrad with alpha_f (material_point.cpp:127-151)
+    double d[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int q = 0; q < 8; q++)
+        for (int r = 0; r < 3; r++) {
+            const double u = ndispl[r * N + nid[q]];
+            for (int c = 0; c < 3; c++) d[r][c] += dN[q][c] * a.af * u;
+        }
+    for (int r = 0; r < 3; r++) d[r][r] += 1.0;
+    double F[3][3], Fn[3][3];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) F[r][c] = P.F[3 * r + c][p];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            double s = 0.0;
+            for (int k = 0; k < 3; k++) s += d[r][k] * F[k][c];
+            Fn[r][c] = s;
+        }
+    const double J = det3(Fn);
+    const double vol = J * P.vol0[p];
+    // UpdateConstitutiveModel on the Newton stress (constitutive_model.cpp:16-120)
+    double sk[6];
+    for (int k = 0; k < 6; k++) sk[k] = stress_k[k * NP + p];
+    const int mid = P.matid[p];
+    const int model = a.iprop[mid];
+    const double E = a.matprop[3 * mid], nu = a.matprop[3 * mid + 1];
+    double lam = 0.0, mu = 0.0;
+    if (model == 0) {
+        double Dm[3][3];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) Dm[r][c] = (r == c) ? d[r][c] - 1.0 : d[r][c];
+        lin_elast_update(sk, Dm, E, nu);
+        lam = E * nu / ((1.0 - 2.0 * nu) * (1.0 + nu));
+        mu = E / (2.0 * (1.0 + nu));
+    } else if (model == 1) {
+        neo_hookean_stress(sk, Fn, J, E, nu);
+        const double lmd = nu * E / ((1.0 + nu) * (1.0 - 2.0 * nu));
+        const double mu0 = E / (2.0 * (1.0 + nu));
+        lam = lmd / J;
+        mu = (mu0 - lmd * log(J)) / J;
+    } else {
+        for (int k = 0; k < 6; k++) sk[k] = 0.0;
+    }
+    for (int k = 0; k < 6; k++) stress_k[k * NP + p] = sk[k];
+    // ImplicitDsfCorr: dN <- dN dF^-1 (material_point.cpp:153-172)
+    double di[3][3];
+    {
+        const double det = 1.0 / det3(d);
+        di[0][0] = (d[1][1] * d[2][2] - d[1][2] * d[2][1]) * det;
+        di[0][1] = (d[0][2] * d[2][1] - d[0][1] * d[2][2]) * det;
+        di[0][2] = (d[0][1] * d[1][2] - d[0][2] * d[1][1]) * det;
+        di[1][0] = (d[1][2] * d[2][0] - d[1][0] * d[2][2]) * det;
+        di[1][1] = (d[0][0] * d[2][2] - d[0][2] * d[2][0]) * det;
+        di[1][2] = (d[0][2] * d[1][0] - d[0][0] * d[1][2]) * det;
+        di[2][0] = (d[1][0] * d[2][1] - d[1][1] * d[2][0]) * det;
+        di[2][1] = (d[0][1] * d[2][0] - d[0][0] * d[2][1]) * det;
+        di[2][2] = (d[0][0] * d[1][1] - d[0][1] * d[1][0]) * det;
+    }
+    for (int q = 0; q < 8; q++) {
+        double t[3];
+        for (int c = 0; c < 3; c++) t[c] = dN[q][0] * di[0][c] + dN[q][1] * di[1][c] + dN[q][2] * di[2][c];
+        for (int c = 0; c < 3; c++) dN[q][c] = t[c];
+    }
+    const double sg[3][3] = {{sk[0], sk[5], sk[4]}, {sk[5], sk[1], sk[3]}, {sk[4], sk[3], sk[2]}};
+    const double m = P.m[p];
+    const double fx = a.grav[0] * a.facl, fy = a.grav[1] * a.facl, fz = a.grav[2] * a.facl;
+    const double afv = a.af * vol;
+    for (int qa = 0; qa < 8; qa++) {
+        const int na = nid[qa];
+        int ia, ja, ka;
+        node_ijk(na, a.nnc, ia, ja, ka);
+        const double emd = a.nb[3] * Nw[qa] * m;   // ComputeNRLumpedMat (material_point.h:144)
+        for (int qb = 0; qb < 8; qb++) {
+            const int nbn = nid[qb];
+            int ib, jb, kb;
+            node_ijk(nbn, a.nnc, ib, jb, kb);
+            const int s = (ib - ia + 1) + 3 * (jb - ja + 1) + 9 * (kb - ka + 1);
+            double K[3][3];
+            tangent(dN[qa], dN[qb], lam, mu, sg, a.nr_flag, K);
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) {
+                    double v = afv * K[i][j];
+                    if (qa == qb && i == j) v += a.am * emd;
+                    atomicAdd(&A[(size_t)(s * 9 + 3 * i + j) * N + na], v);
+                }
+        }
+        const double f0 = -vol * (sk[0] * dN[qa][0] + sk[5] * dN[qa][1] + sk[4] * dN[qa][2]) + Nw[qa] * (m * fx);
+        const double f1 = -vol * (sk[5] * dN[qa][0] + sk[1] * dN[qa][1] + sk[3] * dN[qa][2]) + Nw[qa] * (m * fy);
+        const double f2 = -vol * (sk[4] * dN[qa][0] + sk[3] * dN[qa][1] + sk[2] * dN[qa][2]) + Nw[qa] * (m * fz);
+        atomicAdd(&b[na], f0);
+        atomicAdd(&b[N + na], f1);
+        atomicAdd(&b[2 * N + na], f2);
+    }
+}
+
+// AddInertialForceToRHS (material_point.h:151-161) and the diagonal of the
+// scaling D^-1/2 (crsmat.cpp:87-146, FEM_flag false)
+__global__ void k_imp_rhs_diag(ImpArgs a, const double *A, const double *nmass, const double *naccel_k,
+                               const double *naccel, double *b, double *adiag) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.nodec) return;
+    const size_t N = (size_t)a.nodec;
+    for (int c = 0; c < 3; c++) {
+        const double aam = a.am * naccel_k[c * N + n] + (1.0 - a.am) * naccel[c * N + n];
+        b[c * N + n] -= nmass[n] * aam;
+        const double dg = fabs(A[(size_t)(13 * 9 + 4 * c) * N + n]);
+        adiag[c * N + n] = dg < a.mtol ? 0.0 : 1.0 / sqrt(dg);
+    }
+}
+
+// ApplyDiagonalScaling (crsmat.cpp:152-172)
+__global__ void k_imp_scale(ImpArgs a, double *A, const double *adiag) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.nodec) return;
+    const size_t N = (size_t)a.nodec;
+    int i, j, k;
+    node_ijk(n, a.nnc, i, j, k);
+    for (int s = 0; s < 27; s++) {
+        const int ii = i + s % 3 - 1, jj = j + (s / 3) % 3 - 1, kk = k + s / 9 - 1;
+        if (ii < 0 || jj < 0 || kk < 0 || ii >= a.nnc[0] || jj >= a.nnc[1] || kk >= a.nnc[2]) continue;
+        const size_t col = ii + (size_t)a.nnc[0] * (jj + (size_t)a.nnc[1] * kk);
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) A[(size_t)(s * 9 + 3 * r + c) * N + n] *= adiag[r * N + n] * adiag[c * N + col];
+    }
+}
+
+// ----------------------------------------------------------- reductions
+// Per-block partial sums in fixed order; k_finish adds the partials in index order.
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) r += sh[w];
+    return r;
+}
+
+__global__ void k_finish(const double *part, int nblk, double *out, int slot) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < nblk; i += blockDim.x) acc += part[i];
+    const double t = block_sum(acc, sh);
+    if (threadIdx.x == 0) out[slot] = t;
+}
+
+// y = A x with BC rows zeroed (MatVecMult + BCResidualSet), optional dot(x, y)
+__global__ void __launch_bounds__(256) k_imp_matvec(ImpArgs a, const double *A, const double *x, double *y,
+                                                    double *part) {
+    __shared__ double sh[32];
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    double dot = 0.0;
+    if (n < a.nodec) {
+        const size_t N = (size_t)a.nodec;
+        int i, j, k;
+        node_ijk(n, a.nnc, i, j, k);
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int s = 0; s < 27; s++) {
+            const int ii = i + s % 3 - 1, jj = j + (s / 3) % 3 - 1, kk = k + s / 9 - 1;
+            if (ii < 0 || jj < 0 || kk < 0 || ii >= a.nnc[0] || jj >= a.nnc[1] || kk >= a.nnc[2]) continue;
+            const size_t col = ii + (size_t)a.nnc[0] * (jj + (size_t)a.nnc[1] * kk);
+            const double x0 = x[col], x1 = x[N + col], x2 = x[2 * N + col];
+            const double *As = A + (size_t)s * 9 * N + n;
+            acc[0] += As[0 * N] * x0 + As[1 * N] * x1 + As[2 * N] * x2;
+            acc[1] += As[3 * N] * x0 + As[4 * N] * x1 + As[5 * N] * x2;
+            acc[2] += As[6 * N] * x0 + As[7 * N] * x1 + As[8 * N] * x2;
+        }
+        const unsigned char bf = a.bcflag[n];
+        for (int c = 0; c < 3; c++) {
+            if (bf & (1 << c)) acc[c] = 0.0;
+            y[c * N + n] = acc[c];
+            dot += x[c * N + n] * acc[c];
+        }
+    }
+    if (part) {
+        const double t = block_sum(dot, sh);
+        if (threadIdx.x == 0) part[blockIdx.x] = t;
+    }
+}
+
+// ScaleSolution + BCResidualSet: xs = x / D, r = b D (crsmat.cpp:190-209)
+__global__ void k_cg_scale_in(ImpArgs a, const double *x, const double *b, const double *adiag, double *xs,
+                              double *rr) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.nodec) return;
+    const size_t N = (size_t)a.nodec;
+    const unsigned char bf = a.bcflag[n];
+    for (int c = 0; c < 3; c++) {
+        const size_t i = c * N + n;
+        const double dg = adiag[i];
+        if (dg < a.mtol) {
+            xs[i] = 0.0;
+            rr[i] = 0.0;
+        } else {
+            xs[i] = x[i] / dg;
+            rr[i] = b[i] * dg;
+        }
+        if (bf & (1 << c)) rr[i] = 0.0;
+    }
+}
+
+// r = rr - Ax, p = r, partial r.r
+__global__ void k_cg_init(ImpArgs a, const double *Ax, double *r, double *p, double *part) {
+    __shared__ double sh[32];
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    double dot = 0.0;
+    if (n < a.nodec) {
+        const size_t N = (size_t)a.nodec;
+        for (int c = 0; c < 3; c++) {
+            const size_t i = c * N + n;
+            const double v = r[i] - Ax[i];
+            r[i] = v;
+            p[i] = v;
+            dot += v * v;
+        }
+    }
+    const double t = block_sum(dot, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// x += alpha p, r -= alpha Ap, partial r.r;  alpha = rr_cur / pAp
+__global__ void k_cg_update(ImpArgs a, const double *scal, int cur, double *x, double *r, const double *p,
+                            const double *Ap, double *part) {
+    __shared__ double sh[32];
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const double pap = scal[S_PAP];
+    const double alpha = pap != 0.0 ? scal[cur] / pap : 0.0;
+    double dot = 0.0;
+    if (n < a.nodec) {
+        const size_t N = (size_t)a.nodec;
+        for (int c = 0; c < 3; c++) {
+            const size_t i = c * N + n;
+            x[i] += alpha * p[i];
+            const double v = r[i] - alpha * Ap[i];
+            r[i] = v;
+            dot += v * v;
+        }
+    }
+    const double t = block_sum(dot, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// p = r + beta p;  beta = rr_new / rr_cur
+__global__ void k_cg_dir(ImpArgs a, const double *scal, int cur, const double *r, double *p) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.nodec) return;
+    const double rc = scal[cur];
+    const double beta = rc != 0.0 ? scal[cur ^ 1] / rc : 0.0;
+    const size_t N = (size_t)a.nodec;
+    for (int c = 0; c < 3; c++) {
+        const size_t i = c * N + n;
+        p[i] = r[i] + beta * p[i];
+    }
+}
+
+// RestorSolution: x = xs D (crsmat.cpp:214-230)
+__global__ void k_cg_scale_out(ImpArgs a, const double *xs, const double *adiag, double *x) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= 3 * a.nodec) return;
+    x[n] = adiag[n] > a.mtol ? xs[n] * adiag[n] : 0.0;
+}
+
+// Newton residual of the linear system (ComputeRefResidual / ComputeAbsResidual,
+// solver.cpp:484-555): b with BC rows zeroed, r = b - (A (x / D)) / D
+__global__ void k_imp_prepare_residual(ImpArgs a, const double *x, const double *adiag, double *b, double *xs) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.nodec) return;
+    const size_t N = (size_t)a.nodec;
+    const unsigned char bf = a.bcflag[n];
+    for (int c = 0; c < 3; c++) {
+        const size_t i = c * N + n;
+        if (bf & (1 << c)) b[i] = 0.0;
+        xs[i] = adiag[i] > a.mtol ? x[i] / adiag[i] : 0.0;
+    }
+}
+
+__global__ void k_imp_residual(ImpArgs a, const double *Ax, const double *adiag, const double *b, double *part) {
+    __shared__ double sh[32];
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0, cnt = 0.0;
+    if (n < a.nodec) {
+        const size_t N = (size_t)a.nodec;
+        for (int c = 0; c < 3; c++) {
+            const size_t i = c * N + n;
+            const double axp = adiag[i] > a.mtol ? Ax[i] / adiag[i] : 0.0;
+            const double r = b[i] - axp;
+            rr += r * r;
+            if (adiag[i] > a.mtol) cnt += 1.0;
+        }
+    }
+    const double t = block_sum(rr, sh);
+    const double u = block_sum(cnt, sh);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = t;
+        part[gridDim.x + blockIdx.x] = u;
+    }
+}
+
+// ---------------------------------------------------------------- G2P
+// nei = max(0, nvof - nvol) and sum nei^2 (material_point.cpp:175-185)
+__global__ void k_imp_nei(ImpArgs a, const double *nvof, double *nei, double *part) {
+    __shared__ double sh[32];
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    double e2 = 0.0;
+    if (n < a.nodec) {
+        const double e = fmax(0.0, -a.nvol[n] + nvof[n]);
+        nei[n] = e;
+        e2 = e * e;
+    }
+    const double t = block_sum(e2, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// Node2Particle (var_trans_solid_implicit.cpp:202-255) with the nodal kinematics
+// already committed: F, J, vol, stress, displacement/acceleration/velocity
+// gathers and the shifting gradient; CommitParticleKinematics without the shift.
+__global__ void __launch_bounds__(128) k_imp_g2p(ImpArgs a, PView P, const double *ndispl, const double *nvel,
+                                                 const double *naccel, const double *nei, double *geup,
+                                                 double *part, DevCtl *ctl, int parity) {
+    __shared__ double sh[32];
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    double gd = 0.0;
+    if (p < a.num) {
+        const size_t N = (size_t)a.nodec, NP = (size_t)a.num;
+        double x[3] = {P.x[0][p], P.x[1][p], P.x[2][p]};
+        int cx, cy, cz, nid[8];
+        double Nw[8], dN[8][3];
+        bool oob = false;
+        shape8(a, x, cx, cy, cz, Nw, dN, nid, oob);
+        double d[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int q = 0; q < 8; q++)
+            for (int r = 0; r < 3; r++) {
+                const double u = ndispl[r * N + nid[q]];
+                for (int c = 0; c < 3; c++) d[r][c] += dN[q][c] * 1.0 * u;
+            }
+        for (int r = 0; r < 3; r++) d[r][r] += 1.0;
+        double F[3][3], Fn[3][3];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) F[r][c] = P.F[3 * r + c][p];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) {
+                double s = 0.0;
+                for (int k = 0; k < 3; k++) s += d[r][k] * F[k][c];
+                Fn[r][c] = s;
+            }
+        const double J = det3(Fn);
+        const double vol = J * P.vol0[p];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) P.F[3 * r + c][p] = Fn[r][c];
+        P.vol[p] = vol;
+        double sk[6];
+        for (int k = 0; k < 6; k++) sk[k] = P.s[k][p];
+        const int mid = P.matid[p];
+        const int model = a.iprop[mid];
+        const double E = a.matprop[3 * mid], nu = a.matprop[3 * mid + 1];
+        if (model == 0) {
+            double Dm[3][3];
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) Dm[r][c] = (r == c) ? d[r][c] - 1.0 : d[r][c];
+            lin_elast_update(sk, Dm, E, nu);
+        } else if (model == 1) {
+            neo_hookean_stress(sk, Fn, J, E, nu);
+        } else {
+            for (int k = 0; k < 6; k++) sk[k] = 0.0;
+        }
+        for (int k = 0; k < 6; k++) P.s[k][p] = sk[k];
+        const bool flip = (a.scheme == MPM_FLIP);
+        double disp[3] = {0, 0, 0}, acc[3] = {0, 0, 0}, vel[3] = {0, 0, 0};
+        const double aold[3] = {P.acc[0][p], P.acc[1][p], P.acc[2][p]};
+        if (model != -1) {
+            for (int q = 0; q < 8; q++)
+                for (int c = 0; c < 3; c++) {
+                    disp[c] += Nw[q] * ndispl[c * N + nid[q]];
+                    acc[c] += Nw[q] * naccel[c * N + nid[q]];
+                    vel[c] += Nw[q] * nvel[c * N + nid[q]];
+                }
+        }
+        // shifting gradient at the old position with the new volume (material_point.cpp:192-216)
+        double g[3] = {0, 0, 0};
+        for (int q = 0; q < 8; q++)
+            for (int c = 0; c < 3; c++) g[c] += dN[q][c] * nei[nid[q]];
+        for (int c = 0; c < 3; c++) {
+            g[c] *= 2.0 * vol;
+            geup[c * NP + p] = g[c];
+            gd += g[c] * g[c];
+        }
+        // CommitParticleKinematics (nonlinear_time_integration.cpp:83-96), shift added by k_imp_shift
+        float amax = 0.0f, vmax = 0.0f;
+        for (int c = 0; c < 3; c++) {
+            double vc = flip ? P.v[c][p] + a.dt * ((1.0 - a.gamma) * aold[c] + a.gamma * acc[c]) : vel[c];
+            P.v[c][p] = vc;
+            P.acc[c][p] = acc[c];
+            P.x[c][p] = x[c] + disp[c];
+            amax = fmaxf(amax, (float)fabs(acc[c]));
+            vmax = fmaxf(vmax, (float)fabs(vc));
+        }
+        const float rs = (float)fmax(fabs(sk[0]) + fabs(sk[5]) + fabs(sk[4]),
+                                     fmax(fabs(sk[5]) + fabs(sk[1]) + fabs(sk[3]), fabs(sk[4]) + fabs(sk[3]) + fabs(sk[2])));
+        atomic_max_pos(&ctl->nxt[parity ^ 1][B_AMAX], amax * 1.000001f);
+        atomic_max_pos(&ctl->nxt[parity ^ 1][B_VMAX], vmax * 1.000001f);
+        atomic_max_pos(&ctl->nxt[parity ^ 1][B_VOLMAX], (float)fabs(vol) * 1.000001f);
+        atomic_max_pos(&ctl->nxt[parity ^ 1][B_VOLSMAX], (float)fabs(vol) * rs * 1.000001f);
+    }
+    const double t = block_sum(gd, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// x += -b0 geup, b0 = eu / gd unless gd < mtol (material_point.cpp:219-225)
+__global__ void k_imp_shift(ImpArgs a, PView P, const double *geup, const double *scal) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.num || !a.shifting) return;
+    const double gd = scal[S_GD];
+    const double b0 = gd < a.mtol ? 0.0 : scal[S_EU] / gd;
+    if (b0 == 0.0) return;
+    const size_t NP = (size_t)a.num;
+    for (int c = 0; c < 3; c++) P.x[c][p] += -b0 * geup[c * NP + p];
+}
+
+__global__ void k_imp_reset_next(DevCtl *ctl, int parity) {
+    for (int k = 0; k < B_NB; k++) ctl->nxt[parity ^ 1][k] = 0u;
+}
+
+}  // namespace mpm
+
+using namespace mpm;
+
+#define CKI(call)                                                                                                      \
+    do {                                                                                                               \
+        cudaError_t _e = (call);                                                                                       \
+        if (_e != cudaSuccess) {                                                                                       \
+            fprintf(stderr, "mpm_gb300: %s failed: %s\n", #call, cudaGetErrorString(_e));                              \
+            return _e == cudaErrorMemoryAllocation ? MPM_ERR_OOM : MPM_ERR_CUDA;                                       \
+        }                                                                                                              \
+    } while (0)
+
+namespace mpm {
+void implicit_free(mpm_ctx *c) {
+    ImpState *s = c->imp;
+    if (!s) return;
+    double *bufs[] = {s->A, s->adiag, s->b, s->x, s->r, s->p, s->Ap, s->xs, s->ndispl, s->nvel, s->naccel,
+                      s->naccel_k, s->nmass, s->nvof, s->nei, s->stress_k, s->geup, s->part, s->scal};
+    for (double *b : bufs)
+        if (b) cudaFree(b);
+    if (s->h_scal) cudaFreeHost(s->h_scal);
+    delete s;
+    c->imp = nullptr;
+}
+}  // namespace mpm
+
+static mpm_status ensure_particle_scratch(mpm_ctx *c) {
+    ImpState *s = c->imp;
+    if (s->num_alloc == c->num && s->stress_k) return MPM_OK;
+    if (s->stress_k) cudaFree(s->stress_k);
+    if (s->geup) cudaFree(s->geup);
+    s->stress_k = s->geup = nullptr;
+    size_t n = (size_t)(c->num > 0 ? c->num : 1);
+    CKI(cudaMalloc((void **)&s->stress_k, sizeof(double) * 6 * n));
+    CKI(cudaMalloc((void **)&s->geup, sizeof(double) * 3 * n));
+    s->num_alloc = c->num;
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
+    if (!c) return MPM_ERR_BAD_ARG;
+    if (c->nreal != 27 || c->precision != 64) return MPM_ERR_UNSUPPORTED;
+    if (c->g.order[0] != 1 || c->g.order[1] != 1 || c->g.order[2] != 1) return MPM_ERR_UNSUPPORTED;
+    implicit_free(c);
+    ImpState *s = new ImpState();
+    c->imp = s;
+    s->nr_flag = nr_flag ? 1 : 0;
+    // GeneralizedAlphaParaSet + NewmarkBetaParaSet (nonlinear_time_integration.cpp:10-56), second order
+    double t = 1.0 + spec_rad;
+    s->alpha_f = 1.0 / t;
+    s->alpha_m = (2.0 - spec_rad) / t;
+    t = 1.0 - s->alpha_f + s->alpha_m;
+    s->gamma = t - 0.5;
+    s->beta = 0.25 * t * t;
+    const double g = s->gamma, b = s->beta, dt = c->dt;
+    s->nb[0] = g / (b * dt);
+    s->nb[1] = g / b - 1.0;
+    s->nb[2] = dt / 2.0 * (g / b - 2.0);
+    s->nb[3] = 1.0 / (b * dt * dt);
+    s->nb[4] = 1.0 / (b * dt);
+    s->nb[5] = 1.0 / (2.0 * b) - 1.0;
+    const size_t N = (size_t)c->g.nodec;
+    CKI(cudaMalloc((void **)&s->A, sizeof(double) * 27 * 9 * N));
+    double **vec3[] = {&s->adiag, &s->b, &s->x, &s->r, &s->p, &s->Ap, &s->xs, &s->ndispl, &s->nvel, &s->naccel,
+                       &s->naccel_k};
+    for (double **v : vec3) CKI(cudaMalloc((void **)v, sizeof(double) * 3 * N));
+    CKI(cudaMalloc((void **)&s->nmass, sizeof(double) * N));
+    CKI(cudaMalloc((void **)&s->nvof, sizeof(double) * N));
+    CKI(cudaMalloc((void **)&s->nei, sizeof(double) * N));
+    s->nblk = (int)((N + 255) / 256);
+    int pblk = (int)((c->num + 127) / 128);
+    int nparts = 2 * (s->nblk > pblk ? s->nblk : pblk) + 2 * ((3 * (int)N + 255) / 256) + 64;
+    CKI(cudaMalloc((void **)&s->part, sizeof(double) * (size_t)nparts));
+    CKI(cudaMalloc((void **)&s->scal, sizeof(double) * S_NSCAL));
+    CKI(cudaMallocHost((void **)&s->h_scal, sizeof(double) * S_NSCAL));
+    CKI(cudaMemset(s->ndispl, 0, sizeof(double) * 3 * N));
+    CKI(cudaMemset(s->x, 0, sizeof(double) * 3 * N));
+    CKI(cudaMemset(s->scal, 0, sizeof(double) * S_NSCAL));
+    return ensure_particle_scratch(c);
+}
+
+static int nb_nodes(mpm_ctx *c) { return (c->g.nodec + 255) / 256; }
+
+// P2G of the implicit solid: AccelP2G mode of the scatter + k_imp_grid
+static mpm_status imp_p2g(mpm_ctx *c, double facl) {
+    ImpState *s = c->imp;
+    c->facl = facl;
+    const size_t N = (size_t)c->g.nodec;
+    if (c->steps_since_sort >= c->resort_period) {
+        mpm_status st = sort_particles(c);
+        if (st != MPM_OK) return st;
+    }
+    CKI(cudaMemsetAsync(c->d_acc, 0, sizeof(unsigned long long) * NACC * N, c->stream));
+    c->write_nodal_dl = false;
+    mpm_status st = run_p2g(c, facl);
+    if (st != MPM_OK) return st;
+    ImpArgs a = imp_args(c);
+    k_imp_grid<<<nb_nodes(c), 256, 0, c->stream>>>(a, c->d_acc, c->d_ctl->p2g_inv, s->nmass, s->nvof, s->nvel,
+                                                   s->naccel);
+    c->launches++;
+    return check_launch(c);
+}
+
+// one linear solve of the assembled, scaled system; s->x holds the initial
+// guess (physical) and receives the physical solution.  Returns iterations.
+static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
+    ImpState *s = c->imp;
+    ImpArgs a = imp_args(c);
+    const int nb = nb_nodes(c);
+    k_cg_scale_in<<<nb, 256, 0, c->stream>>>(a, s->x, s->b, s->adiag, s->xs, s->r);
+    k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->xs, s->Ap, nullptr);
+    k_cg_init<<<nb, 256, 0, c->stream>>>(a, s->Ap, s->r, s->p, s->part);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RR0);
+    c->launches += 4;
+    CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, c->stream));
+    CKI(cudaStreamSynchronize(c->stream));
+    const double rr0 = s->h_scal[S_RR0];
+    int it = 0;
+    bool done = !(rr0 > 1.0e-300);
+    const int check = 8;
+    while (!done && it < kmax) {
+        const int cur = (it & 1) ? S_RR1 : S_RR0;
+        k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->p, s->Ap, s->part);
+        k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_PAP);
+        k_cg_update<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->xs, s->r, s->p, s->Ap, s->part);
+        k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, cur ^ 1);
+        k_cg_dir<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->r, s->p);
+        c->launches += 5;
+        it++;
+        if (it % check == 0 || it == kmax) {
+            CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream));
+            CKI(cudaStreamSynchronize(c->stream));
+            const double rr = s->h_scal[(it & 1) ? S_RR1 : S_RR0];
+            if (rr != rr) {
+                *iters = it;
+                return MPM_ERR_NONFINITE;
+            }
+            if (rr < eps * rr0) done = true;
+            s->last_rel = sqrt(rr / rr0);
+        }
+    }
+    k_cg_scale_out<<<(3 * c->g.nodec + 255) / 256, 256, 0, c->stream>>>(a, s->xs, s->adiag, s->x);
+    c->launches++;
+    *iters = it;
+    if (!done) return MPM_ERR_KRYLOV_MAXIT;
+    return check_launch(c);
+}
+
+static mpm_status imp_assemble(mpm_ctx *c) {
+    ImpState *s = c->imp;
+    ImpArgs a = imp_args(c);
+    const size_t N = (size_t)c->g.nodec;
+    CKI(cudaMemsetAsync(s->A, 0, sizeof(double) * 27 * 9 * N, c->stream));
+    CKI(cudaMemsetAsync(s->b, 0, sizeof(double) * 3 * N, c->stream));
+    PView P = pview(c);
+    const int pb = (int)((c->num + 127) / 128);
+    k_imp_assemble<<<pb, 128, 0, c->stream>>>(a, P, s->ndispl, s->stress_k, s->A, s->b);
+    k_imp_rhs_diag<<<nb_nodes(c), 256, 0, c->stream>>>(a, s->A, s->nmass, s->naccel_k, s->naccel, s->b, s->adiag);
+    k_imp_scale<<<nb_nodes(c), 256, 0, c->stream>>>(a, s->A, s->adiag);
+    c->launches += 3;
+    return check_launch(c);
+}
+
+// CheckNRConvergence's two residual measures of the last linear solve
+static mpm_status imp_residuals(mpm_ctx *c, double *ref, double *absr) {
+    ImpState *s = c->imp;
+    ImpArgs a = imp_args(c);
+    const int nb = nb_nodes(c);
+    k_imp_prepare_residual<<<nb, 256, 0, c->stream>>>(a, s->x, s->adiag, s->b, s->xs);
+    k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->xs, s->Ap, nullptr);
+    k_imp_residual<<<nb, 256, 0, c->stream>>>(a, s->Ap, s->adiag, s->b, s->part);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RES);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part + nb, nb, s->scal, S_IDOF);
+    c->launches += 5;
+    CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, c->stream));
+    CKI(cudaStreamSynchronize(c->stream));
+    const double rtr = s->h_scal[S_RES], idof = s->h_scal[S_IDOF];
+    *ref = sqrt(rtr);
+    *absr = idof <= 1.0e-30 ? 0.0 : sqrt(rtr / idof);
+    return MPM_OK;
+}
+
+__global__ void k_add(double *y, const double *x, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] += x[i];
+}
+
+// SolidMaterialPoint::SolveSolid (solve_solid_implicit.cpp:65-103)
+static mpm_status imp_newton(mpm_ctx *c, double eps, int kmax, int *krylov, int *newton) {
+    ImpState *s = c->imp;
+    ImpArgs a = imp_args(c);
+    const size_t N = (size_t)c->g.nodec;
+    PView P = pview(c);
+    for (int k = 0; k < 6; k++)
+        CKI(cudaMemcpyAsync(s->stress_k + k * (size_t)c->num, P.s[k], sizeof(double) * c->num,
+                            cudaMemcpyDeviceToDevice, c->stream));
+    CKI(cudaMemsetAsync(s->ndispl, 0, sizeof(double) * 3 * N, c->stream));
+    CKI(cudaMemsetAsync(s->x, 0, sizeof(double) * 3 * N, c->stream));
+    const int iter_max = s->nr_flag ? 1000 : 0;
+    double r0r = 0.0;
+    int ktot = 0, it;
+    mpm_status st = MPM_OK;
+    for (it = 0; it <= iter_max; it++) {
+        k_imp_predict<<<nb_nodes(c), 256, 0, c->stream>>>(a, s->ndispl, s->nvel, s->naccel, s->naccel_k, nullptr, 1);
+        c->launches++;
+        st = imp_assemble(c);
+        if (st != MPM_OK) return st;
+        int k = 0;
+        st = imp_cg(c, eps, kmax, &k);
+        ktot += k;
+        if (st != MPM_OK) break;
+        k_add<<<(3 * c->g.nodec + 255) / 256, 256, 0, c->stream>>>(s->ndispl, s->x, 3 * c->g.nodec);
+        c->launches++;
+        if (s->nr_flag) {
+            double rkr, ra;
+            st = imp_residuals(c, &rkr, &ra);
+            if (st != MPM_OK) break;
+            if (it == 0) r0r = rkr;
+            const double rref = r0r > 1.0e-30 ? rkr / r0r : 0.0;
+            if (rref < 1.0e-6 || r0r < 1.0e-6 || ra < 1.0e-8) break;
+        }
+    }
+    *krylov = ktot;
+    *newton = (it > iter_max ? iter_max : it) + 1;
+    if (st == MPM_OK && s->nr_flag && it > iter_max) st = MPM_ERR_NEWTON_MAXIT;
+    return st;
+}
+
+// Node2Particle (var_trans_solid_implicit.cpp:106-167)
+static mpm_status imp_g2p(mpm_ctx *c) {
+    ImpState *s = c->imp;
+    ImpArgs a = imp_args(c);
+    const int nb = nb_nodes(c);
+    const int parity = (int)(c->step & 1);
+    // PredictNewmarkBetaVelAndAccel + CommitNodalKinematics: nvel, naccel <- predicted
+    k_imp_predict<<<nb, 256, 0, c->stream>>>(a, s->ndispl, s->nvel, s->naccel, s->naccel_k, s->Ap, 0);
+    CKI(cudaMemcpyAsync(s->nvel, s->Ap, sizeof(double) * 3 * c->g.nodec, cudaMemcpyDeviceToDevice, c->stream));
+    CKI(cudaMemcpyAsync(s->naccel, s->naccel_k, sizeof(double) * 3 * c->g.nodec, cudaMemcpyDeviceToDevice,
+                        c->stream));
+    k_imp_nei<<<nb, 256, 0, c->stream>>>(a, s->nvof, s->nei, s->part);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_EU);
+    k_imp_reset_next<<<1, 1, 0, c->stream>>>(c->d_ctl, parity);
+    PView P = pview(c);
+    const int pb = (int)((c->num + 127) / 128);
+    k_imp_g2p<<<pb, 128, 0, c->stream>>>(a, P, s->ndispl, s->nvel, s->naccel, s->nei, s->geup, s->part, c->d_ctl,
+                                         parity);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part, pb, s->scal, S_GD);
+    k_imp_shift<<<pb, 128, 0, c->stream>>>(a, P, s->geup, s->scal);
+    c->launches += 7;
+    return check_launch(c);
+}
+
+mpm_status mpm_gpu_implicit_step(mpm_ctx *c, int nsteps, double facl, double eps, int kmax, mpm_solve_stats *stats) {
+    if (!c || !c->imp || nsteps < 0 || !(eps > 0.0) || kmax <= 0) return MPM_ERR_BAD_ARG;
+    if (c->num == 0) return MPM_ERR_STATE;
+    mpm_status st = ensure_particle_scratch(c);
+    if (st != MPM_OK) return st;
+    int kt = 0, nt = 0;
+    for (int i = 0; i < nsteps; i++) {
+        st = imp_p2g(c, facl);
+        if (st != MPM_OK) break;
+        int k = 0, n = 0;
+        st = imp_newton(c, eps, kmax, &k, &n);
+        kt += k;
+        nt += n;
+        if (st != MPM_OK) break;
+        st = imp_g2p(c);
+        if (st != MPM_OK) break;
+        c->step++;
+        c->steps_since_sort++;
+    }
+    c->imp->krylov_total += kt;
+    c->imp->newton_total += nt;
+    if (stats) {
+        stats->krylov_iters = kt;
+        stats->newton_iters = nt;
+        stats->last_rel_residual = c->imp->last_rel;
+    }
+    if (st != MPM_OK) return st;
+    CKI(cudaStreamSynchronize(c->stream));
+    return check_launch(c);
+}
+
+// ------------------------------------------------------------- test hooks
+mpm_status mpm_gpu_implicit_assemble(mpm_ctx *c, double facl) {
+    if (!c || !c->imp) return MPM_ERR_BAD_ARG;
+    if (c->num == 0) return MPM_ERR_STATE;
+    mpm_status st = ensure_particle_scratch(c);
+    if (st != MPM_OK) return st;
+    st = imp_p2g(c, facl);
+    if (st != MPM_OK) return st;
+    ImpState *s = c->imp;
+    ImpArgs a = imp_args(c);
+    PView P = pview(c);
+    for (int k = 0; k < 6; k++)
+        CKI(cudaMemcpyAsync(s->stress_k + k * (size_t)c->num, P.s[k], sizeof(double) * c->num,
+                            cudaMemcpyDeviceToDevice, c->stream));
+    CKI(cudaMemsetAsync(s->ndispl, 0, sizeof(double) * 3 * c->g.nodec, c->stream));
+    CKI(cudaMemsetAsync(s->x, 0, sizeof(double) * 3 * c->g.nodec, c->stream));
+    k_imp_predict<<<nb_nodes(c), 256, 0, c->stream>>>(a, s->ndispl, s->nvel, s->naccel, s->naccel_k, nullptr, 1);
+    c->launches++;
+    st = imp_assemble(c);
+    if (st != MPM_OK) return st;
+    CKI(cudaStreamSynchronize(c->stream));
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_implicit_get_system(mpm_ctx *c, double *stencil, double *adiag, double *b_rhs) {
+    if (!c || !c->imp) return MPM_ERR_BAD_ARG;
+    ImpState *s = c->imp;
+    const size_t N = (size_t)c->g.nodec;
+    CKI(cudaStreamSynchronize(c->stream));
+    if (stencil) CKI(cudaMemcpy(stencil, s->A, sizeof(double) * 27 * 9 * N, cudaMemcpyDeviceToHost));
+    if (adiag) CKI(cudaMemcpy(adiag, s->adiag, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost));
+    if (b_rhs) CKI(cudaMemcpy(b_rhs, s->b, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost));
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_implicit_matvec(mpm_ctx *c, const double *x, double *y) {
+    if (!c || !c->imp || !x || !y) return MPM_ERR_BAD_ARG;
+    ImpState *s = c->imp;
+    const size_t N = (size_t)c->g.nodec;
+    CKI(cudaMemcpyAsync(s->xs, x, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->stream));
+    ImpArgs a = imp_args(c);
+    timer_begin(c, K_MATVEC);
+    k_imp_matvec<<<nb_nodes(c), 256, 0, c->stream>>>(a, s->A, s->xs, s->Ap, nullptr);
+    timer_end(c, K_MATVEC);
+    c->launches++;
+    CKI(cudaMemcpyAsync(y, s->Ap, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, c->stream));
+    CKI(cudaStreamSynchronize(c->stream));
+    return check_launch(c);
+}
+
+mpm_status mpm_gpu_implicit_solve(mpm_ctx *c, double eps, int kmax, double *x, int *iters) {
+    if (!c || !c->imp || !(eps > 0.0) || kmax <= 0) return MPM_ERR_BAD_ARG;
+    ImpState *s = c->imp;
+    const size_t N = (size_t)c->g.nodec;
+    CKI(cudaMemsetAsync(s->x, 0, sizeof(double) * 3 * N, c->stream));
+    int it = 0;
+    mpm_status st = imp_cg(c, eps, kmax, &it);
+    if (iters) *iters = it;
+    if (x) CKI(cudaMemcpy(x, s->x, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost));
+    return st;
+}

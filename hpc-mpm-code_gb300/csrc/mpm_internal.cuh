@@ -52,7 +52,7 @@ struct Geom {
 
 // Bounds that set the fixed-point scales.  Values are non-negative floats
 // stored as their bit patterns so that atomicMax on unsigned int orders them.
-enum BoundSlot { B_VMAX = 0, B_VOLMAX, B_VOLSMAX, B_NB };      // produced for the next step
+enum BoundSlot { B_VMAX = 0, B_VOLMAX, B_VOLSMAX, B_AMAX, B_NB };   // produced for the next step
 enum CurSlot { C_GMAX = 0, C_NEIMAX, C_NC };                    // produced and used within a step
 
 struct DevCtl {
@@ -152,6 +152,7 @@ struct mpm_ctx {
     int cell_scatter = 1;   // FP32 linear: per-cell register scatter (else staging-box atomics)
     mpm_status latched = MPM_OK;
     mpm::KernelTimer timer;
+    struct ImpState *imp = nullptr;   // implicit solid state (mpm_implicit.cu)
     std::vector<int> bc_nodes[3];
     std::vector<double> bc_vals[3];
 };
@@ -159,6 +160,8 @@ struct mpm_ctx {
 namespace mpm {
 // mpm_sort.cu
 mpm_status sort_particles(mpm_ctx *c);
+// mpm_implicit.cu
+void implicit_free(mpm_ctx *c);
 // mpm_explicit.cu
 mpm_status run_p2g(mpm_ctx *c, double facl);
 mpm_status run_grid1(mpm_ctx *c, int mode);

@@ -23,7 +23,7 @@ LIB_PATH = _build.LIB
 MPM_PIC, MPM_FLIP = 0, 1
 STATUS = {0: "ok", 1: "bad argument", 2: "out of device memory", 3: "non-finite particle state",
           4: "particle outside the grid", 5: "Krylov iteration limit", 6: "device wait timed out", 7: "CUDA error",
-          8: "call out of order", 9: "unsupported configuration"}
+          8: "call out of order", 9: "unsupported configuration", 10: "Newton iteration did not converge"}
 
 
 class MpmError(RuntimeError):
@@ -44,7 +44,11 @@ class MaterialDesc(C.Structure):
 class Config(C.Structure):
     _fields_ = [("dt", C.c_double), ("mtol", C.c_double), ("gravity", C.c_double * 3), ("scheme", C.c_int),
                 ("precision", C.c_int), ("shifting", C.c_int), ("resort_period", C.c_int), ("scatter", C.c_int),
-                ("reserved", C.c_int * 7)]
+                ("implicit", C.c_int), ("reserved", C.c_int * 6)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("newton_iters", C.c_int), ("krylov_iters", C.c_int), ("last_rel_residual", C.c_double)]
 
 
 class Stats(C.Structure):
@@ -61,7 +65,9 @@ EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_s
            "mpm_gpu_load_particles", "mpm_gpu_set_bc", "mpm_gpu_p2g", "mpm_gpu_grid_update", "mpm_gpu_g2p",
            "mpm_gpu_step_explicit", "mpm_gpu_download_nodal", "mpm_gpu_download_particles",
            "mpm_gpu_upload_particles", "mpm_gpu_sync",
-           "mpm_gpu_get_stats", "mpm_gpu_enable_kernel_timing", "mpm_gpu_kernel_times"]
+           "mpm_gpu_get_stats", "mpm_gpu_enable_kernel_timing", "mpm_gpu_kernel_times", "mpm_gpu_implicit_setup",
+           "mpm_gpu_implicit_step", "mpm_gpu_implicit_assemble", "mpm_gpu_implicit_get_system",
+           "mpm_gpu_implicit_matvec", "mpm_gpu_implicit_solve", "mpm_gpu_p2g_noalloc"]
 
 
 def load(path: str | None = None):
@@ -92,6 +98,13 @@ def load(path: str | None = None):
     lib.mpm_gpu_sync.argtypes = [C.c_void_p]
     lib.mpm_gpu_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     lib.mpm_gpu_enable_kernel_timing.argtypes = [C.c_void_p, C.c_int]
+    lib.mpm_gpu_implicit_setup.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    lib.mpm_gpu_implicit_step.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int,
+                                          C.POINTER(SolveStats)]
+    lib.mpm_gpu_implicit_assemble.argtypes = [C.c_void_p, C.c_double]
+    lib.mpm_gpu_implicit_get_system.argtypes = [C.c_void_p, _dp, _dp, _dp]
+    lib.mpm_gpu_implicit_matvec.argtypes = [C.c_void_p, _dp, _dp]
+    lib.mpm_gpu_implicit_solve.argtypes = [C.c_void_p, C.c_double, C.c_int, _dp, C.POINTER(C.c_int)]
     lib.mpm_gpu_kernel_times.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_char_p), _dp,
                                          C.POINTER(C.c_int64)]
     _lib = lib
@@ -118,7 +131,7 @@ NODAL = {"nmass": (0, 1), "nvof": (1, 1), "nmome": (2, 3), "nforce": (3, 3), "nv
 class GpuSolid:
     """One explicit solid on the GPU, built from a scene (mpm_gb300.scenes.Scene)."""
 
-    def __init__(self, scene, precision=32, shifting=True, resort_period=0, scatter=0, stream=None):
+    def __init__(self, scene, precision=32, shifting=True, resort_period=0, scatter=0, stream=None, implicit=False):
         self.lib = lib = load()
         self.scene = s = scene
         g = GridDesc((C.c_int * 3)(*s.xyelem), (C.c_double * 3)(*s.xymin), (C.c_double * 3)(*s.dxy),
@@ -127,7 +140,7 @@ class GpuSolid:
         self._mat = np.ascontiguousarray(s.mat_prop, dtype=np.float64).ravel()
         m = MaterialDesc(len(self._iprop), self._iprop.ctypes.data_as(_ip), self._mat.ctypes.data_as(_dp))
         cfg = Config(s.dt, s.mtol, (C.c_double * 3)(*s.gravity), s.scheme, precision, int(shifting),
-                     int(resort_period), int(scatter), (C.c_int * 7)())
+                     int(resort_period), int(scatter), int(implicit), (C.c_int * 6)())
         h = C.c_void_p()
         _chk(lib.mpm_gpu_create(C.byref(g), C.byref(m), C.byref(cfg), C.byref(h)), "mpm_gpu_create")
         self.ctx = h
@@ -228,3 +241,55 @@ class GpuSolid:
         launches = (C.c_int64 * cap)()
         _chk(self.lib.mpm_gpu_kernel_times(self.ctx, C.byref(cnt), names, ms, launches), "mpm_gpu_kernel_times")
         return {names[i].decode(): (ms[i], launches[i]) for i in range(cnt.value)}
+
+
+class GpuImplicitSolid(GpuSolid):
+    """The implicit solid (FP64) on the GPU; operator names of implicitmpm::SolidMaterialPoint."""
+
+    def __init__(self, scene, nr_flag=False, spec_rad=1.0, shifting=True, stream=None):
+        super().__init__(scene, precision=64, shifting=shifting, stream=stream, implicit=True)
+        _chk(self.lib.mpm_gpu_implicit_setup(self.ctx, int(nr_flag), float(spec_rad)), "mpm_gpu_implicit_setup")
+
+    def implicit_steps(self, n, facl=1.0, eps=1.0e-8, kmax=10000):
+        st = SolveStats()
+        _chk(self.lib.mpm_gpu_implicit_step(self.ctx, n, facl, eps, kmax, C.byref(st)), "mpm_gpu_implicit_step")
+        return st.krylov_iters, st.newton_iters, st.last_rel_residual
+
+    def assemble(self, facl=1.0):
+        _chk(self.lib.mpm_gpu_implicit_assemble(self.ctx, facl), "mpm_gpu_implicit_assemble")
+
+    def system(self):
+        n = self.nodec
+        A = np.zeros(27 * 9 * n)
+        d = np.zeros(3 * n)
+        b = np.zeros(3 * n)
+        _chk(self.lib.mpm_gpu_implicit_get_system(self.ctx, _ptr(A), _ptr(d), _ptr(b)), "mpm_gpu_implicit_get_system")
+        return A.reshape(27, 9, n), d, b
+
+    def matvec(self, x):
+        x = _d(x)
+        y = np.zeros(3 * self.nodec)
+        _chk(self.lib.mpm_gpu_implicit_matvec(self.ctx, _ptr(x), _ptr(y)), "mpm_gpu_implicit_matvec")
+        return y
+
+    def solve(self, eps=1.0e-8, kmax=10000):
+        x = np.zeros(3 * self.nodec)
+        it = C.c_int(0)
+        _chk(self.lib.mpm_gpu_implicit_solve(self.ctx, eps, kmax, _ptr(x), C.byref(it)), "mpm_gpu_implicit_solve")
+        return x, it.value
+
+
+def stencil_to_csr(stencil, xynodec, matrow, matcolid):
+    """Reorder [27][9][nodec] stencil values into the reference's CSR block-major
+    layout amat[e][j] for the graph (matrow, matcolid) of CrsMat::BuildCrsMat."""
+    nx, ny, nz = xynodec
+    nodec = nx * ny * nz
+    amat = np.zeros((9, len(matcolid)))
+    rows = np.repeat(np.arange(nodec), np.diff(matrow))
+    cols = np.asarray(matcolid)
+    ri, rj, rk = rows % nx, (rows // nx) % ny, rows // (nx * ny)
+    ci, cj, ck = cols % nx, (cols // nx) % ny, cols // (nx * ny)
+    slot = (ci - ri + 1) + 3 * (cj - rj + 1) + 9 * (ck - rk + 1)
+    for e in range(9):
+        amat[e] = stencil[slot, e, rows]
+    return amat

@@ -40,7 +40,8 @@ typedef enum {
     MPM_ERR_DEVICE_TIMEOUT = 6,
     MPM_ERR_CUDA = 7,
     MPM_ERR_STATE = 8,
-    MPM_ERR_UNSUPPORTED = 9
+    MPM_ERR_UNSUPPORTED = 9,
+    MPM_ERR_NEWTON_MAXIT = 10
 } mpm_status;
 
 typedef enum { MPM_PIC = 0, MPM_FLIP = 1 } mpm_scheme;  /* MapScheme, module/dataset.h:19 */
@@ -74,7 +75,8 @@ typedef struct {
     int shifting;       /* 1: DeltaCorrectionParticleShifting as the reference; 0: off */
     int resort_period;  /* physical re-sort of particles by brick every N steps (>= 1); 0 = default (8) */
     int scatter;        /* 0: per-cell register scatter for FP32 linear grids (default); 1: staging-box atomics */
-    int reserved[7];
+    int implicit;       /* 1: implicit solid context (particles carry acceleration; mpm_gpu_implicit_*) */
+    int reserved[6];
 } mpm_config;
 
 /* ---- lifetime ------------------------------------------------------------
@@ -150,6 +152,39 @@ mpm_status mpm_gpu_get_stats(mpm_ctx *ctx, mpm_stats *out);
  * for i < *count (count in: capacity).  Synchronises the stream. */
 mpm_status mpm_gpu_enable_kernel_timing(mpm_ctx *ctx, int on);
 mpm_status mpm_gpu_kernel_times(mpm_ctx *ctx, int *count, const char **names, double *ms, int64_t *launches);
+
+/* ---- the implicit solid (module/solid/implicit/, module/solver/) ----------------
+ * A context created with cfg->implicit = 1 and precision 64 (linear shape
+ * functions).  mpm_gpu_implicit_setup replaces the solid set-up of the FSI
+ * driver: GeneralizedAlphaParaSet + NewmarkBetaParaSet
+ * (module/nonlinear_time_integration.cpp:10-56, spec_rad = 1 gives
+ * alpha_f = alpha_m = 0.5, Newmark beta = 1/4, gamma = 1/2) and
+ * CrsMat::BuildCrsMat (module/solver/crsmat.cpp:21-81; here a 27-point block
+ * stencil).  nr_flag as MaterialPoint::NR_flag (module/material_point.h:134). */
+typedef struct {
+    int newton_iters;          /* linear solves (Newton iterations) over the call */
+    int krylov_iters;          /* CG iterations over the call */
+    double last_rel_residual;  /* ||r|| / ||r0|| of the last solve (scaled system) */
+} mpm_solve_stats;
+mpm_status mpm_gpu_implicit_setup(mpm_ctx *ctx, int nr_flag, double spec_rad);
+/* nsteps x (MeshPointLinklist, Particle2Node, SolveSolid, Node2Particle) of the
+ * implicit solid (module/solid/implicit/var_trans_solid_implicit.cpp:20-167,
+ * solve_solid_implicit.cpp:65-204).  Each linear system is solved by
+ * diagonally scaled conjugate gradients until ||r||^2 < eps ||r0||^2 (the
+ * reference's GPBiCGSafe stops at eps = 1e-8, module/solver/solver.cpp:64,128),
+ * at most kmax iterations per solve. */
+mpm_status mpm_gpu_implicit_step(mpm_ctx *ctx, int nsteps, double facl, double eps, int kmax,
+                                 mpm_solve_stats *stats);
+/* Test hooks.  assemble: Particle2Node + the first Newton system of a step
+ * (ndispl = 0), scaled as BuildDiagonalPreconditioner leaves it.
+ * get_system: stencil values [27][9][nodec] (slot s = (dx+1)+3(dy+1)+9(dz+1),
+ * entry 3a+b), D^-1/2 and the RHS (3*nodec each).  matvec: y = A x with BC
+ * rows zeroed, CrsMat::MatVecMult (module/solver/solver.cpp:405-433), host
+ * arrays of 3*nodec.  solve: the assembled system from x = 0, physical x. */
+mpm_status mpm_gpu_implicit_assemble(mpm_ctx *ctx, double facl);
+mpm_status mpm_gpu_implicit_get_system(mpm_ctx *ctx, double *stencil, double *adiag, double *b_rhs);
+mpm_status mpm_gpu_implicit_matvec(mpm_ctx *ctx, const double *x, double *y);
+mpm_status mpm_gpu_implicit_solve(mpm_ctx *ctx, double eps, int kmax, double *x, int *iters);
 
 /* ---- allocation-free P2G -----------------------------------------------------
  * No counterpart in the reference: an extra entry point for callers that
