@@ -235,44 +235,45 @@ template <typename R>
 static mpm_status upload_particles(mpm_ctx *c, int64_t n, const double *coord, const double *vel, const double *mass,
                                    const double *vol0, const double *F, const double *stress, const int *matid) {
     size_t N = (size_t)n;
+    const size_t S = c->pstride;
     const int nr = c->nreal;
-    size_t bytes = N * (nr * sizeof(R) + 2 * sizeof(int));
+    size_t bytes = S * (nr * sizeof(R) + 2 * sizeof(int));
     std::vector<char> host(bytes, 0);
     R *f = (R *)host.data();
     double vmax = 0.0, volmax = 0.0, vsmax = 0.0, mmax = 0.0;
     for (size_t p = 0; p < N; p++) {
         for (int k = 0; k < 3; k++) {
-            f[k * N + p] = (R)coord[3 * p + k];
+            f[k * S + p] = (R)coord[3 * p + k];
             double v = vel ? vel[3 * p + k] : 0.0;
-            f[(3 + k) * N + p] = (R)v;
+            f[(3 + k) * S + p] = (R)v;
             vmax = fmax(vmax, fabs(v));
         }
         for (int k = 0; k < 9; k++) {
             // FP32 stores the displacement gradient H = F - I; FP64 stores F
             const double eye = (k % 4) == 0 ? 1.0 : 0.0;
             const double Fk = F ? F[9 * p + k] : eye;
-            f[(6 + k) * N + p] = sizeof(R) == 4 ? (R)(Fk - eye) : (R)Fk;
+            f[(6 + k) * S + p] = sizeof(R) == 4 ? (R)(Fk - eye) : (R)Fk;
         }
         double s[6];
         for (int k = 0; k < 6; k++) {
             s[k] = stress ? stress[6 * p + k] : 0.0;
-            f[(15 + k) * N + p] = (R)s[k];
+            f[(15 + k) * S + p] = (R)s[k];
         }
-        f[21 * N + p] = (R)mass[p];
-        f[22 * N + p] = (R)vol0[p];
-        f[23 * N + p] = (R)vol0[p];   // vol = vol0 (solid_data_io.cpp:32)
+        f[21 * S + p] = (R)mass[p];
+        f[22 * S + p] = (R)vol0[p];
+        f[23 * S + p] = (R)vol0[p];   // vol = vol0 (solid_data_io.cpp:32)
         mmax = fmax(mmax, fabs(mass[p]));
         volmax = fmax(volmax, fabs(vol0[p]));
         double rs = fmax(fabs(s[0]) + fabs(s[5]) + fabs(s[4]),
                          fmax(fabs(s[5]) + fabs(s[1]) + fabs(s[3]), fabs(s[4]) + fabs(s[3]) + fabs(s[2])));
         vsmax = fmax(vsmax, fabs(vol0[p]) * rs);
     }
-    int *ip = (int *)(f + nr * N);
+    int *ip = (int *)(f + nr * S);
     for (size_t p = 0; p < N; p++) {
         int mid = matid ? matid[p] : 0;
         if (mid < 0 || mid >= c->nmat) return MPM_ERR_BAD_ARG;
         ip[p] = mid;
-        ip[N + p] = (int)p;
+        ip[S + p] = (int)p;
     }
     CK(cudaMemcpy(c->pbuf[c->cur], host.data(), bytes, cudaMemcpyHostToDevice));
     c->mmax = mmax * 1.000001;
@@ -300,7 +301,8 @@ mpm_status mpm_gpu_load_particles(mpm_ctx *c, int64_t n, const double *coord, co
     free_particles(c);
     c->num = n;
     size_t N = (size_t)(n > 0 ? n : 1);
-    size_t bytes = N * (c->nreal * c->rsize + 2 * sizeof(int));
+    c->pstride = (N + 63) / 64 * 64;
+    size_t bytes = c->pstride * (c->nreal * c->rsize + 2 * sizeof(int));
     CK(cudaMalloc(&c->pbuf[0], bytes));
     CK(cudaMalloc(&c->pbuf[1], bytes));
     CK(cudaMalloc((void **)&c->d_key, sizeof(int) * N));
@@ -488,37 +490,37 @@ namespace mpm {
 constexpr int ST_X = 0, ST_V = 3, ST_F = 6, ST_S = 15, ST_VOL = 21, ST_W = 22;
 
 template <typename R>
-__global__ void k_state_gather(const R *f, size_t N, int nreal, double *st, unsigned mask) {
+__global__ void k_state_gather(const R *f, size_t N, size_t S, int nreal, double *st, unsigned mask) {
     const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= N) return;
-    const int *pid = (const int *)(f + nreal * N) + N;
+    const int *pid = (const int *)(f + nreal * S) + S;
     const size_t p = (size_t)pid[j];
     if (mask & 1)
-        for (int k = 0; k < 3; k++) st[ST_X * N + 3 * p + k] = (double)f[k * N + j];
+        for (int k = 0; k < 3; k++) st[ST_X * N + 3 * p + k] = (double)f[k * S + j];
     if (mask & 2)
-        for (int k = 0; k < 3; k++) st[ST_V * N + 3 * p + k] = (double)f[(3 + k) * N + j];
+        for (int k = 0; k < 3; k++) st[ST_V * N + 3 * p + k] = (double)f[(3 + k) * S + j];
     if (mask & 4)
         for (int k = 0; k < 9; k++)
-            st[ST_F * N + 9 * p + k] = (double)f[(6 + k) * N + j] + (sizeof(R) == 4 && (k % 4) == 0 ? 1.0 : 0.0);
+            st[ST_F * N + 9 * p + k] = (double)f[(6 + k) * S + j] + (sizeof(R) == 4 && (k % 4) == 0 ? 1.0 : 0.0);
     if (mask & 8)
-        for (int k = 0; k < 6; k++) st[ST_S * N + 6 * p + k] = (double)f[(15 + k) * N + j];
-    if (mask & 16) st[ST_VOL * N + p] = (double)f[23 * N + j];
+        for (int k = 0; k < 6; k++) st[ST_S * N + 6 * p + k] = (double)f[(15 + k) * S + j];
+    if (mask & 16) st[ST_VOL * N + p] = (double)f[23 * S + j];
 }
 
 // Also raises the fixed-point bounds of the next P2G to cover the new state.
 template <typename R>
-__global__ void k_state_scatter(R *f, size_t N, int nreal, const double *st, unsigned mask, DevCtl *ctl,
+__global__ void k_state_scatter(R *f, size_t N, size_t S, int nreal, const double *st, unsigned mask, DevCtl *ctl,
                                 int parity) {
     const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= N) return;
     {
-        const size_t p = (size_t)((const int *)(f + nreal * N) + N)[j];
+        const size_t p = (size_t)((const int *)(f + nreal * S) + S)[j];
         if (mask & 2) {
             float vm = 0.0f;
             for (int k = 0; k < 3; k++) vm = fmaxf(vm, fabsf((float)st[ST_V * N + 3 * p + k]));
             atomic_max_pos(&ctl->nxt[parity][B_VMAX], vm * 1.000001f);
         }
-        const float vol = (mask & 16) ? fabsf((float)st[ST_VOL * N + p]) : fabsf((float)f[23 * N + j]);
+        const float vol = (mask & 16) ? fabsf((float)st[ST_VOL * N + p]) : fabsf((float)f[23 * S + j]);
         if (mask & 16) atomic_max_pos(&ctl->nxt[parity][B_VOLMAX], vol * 1.000001f);
         if (mask & 8) {
             const double *s6 = st + ST_S * N + 6 * p;
@@ -527,18 +529,18 @@ __global__ void k_state_scatter(R *f, size_t N, int nreal, const double *st, uns
             atomic_max_pos(&ctl->nxt[parity][B_VOLSMAX], (float)(vol * rs) * 1.000001f);
         }
     }
-    const int *pid = (const int *)(f + nreal * N) + N;
+    const int *pid = (const int *)(f + nreal * S) + S;
     const size_t p = (size_t)pid[j];
     if (mask & 1)
-        for (int k = 0; k < 3; k++) f[k * N + j] = (R)st[ST_X * N + 3 * p + k];
+        for (int k = 0; k < 3; k++) f[k * S + j] = (R)st[ST_X * N + 3 * p + k];
     if (mask & 2)
-        for (int k = 0; k < 3; k++) f[(3 + k) * N + j] = (R)st[ST_V * N + 3 * p + k];
+        for (int k = 0; k < 3; k++) f[(3 + k) * S + j] = (R)st[ST_V * N + 3 * p + k];
     if (mask & 4)
         for (int k = 0; k < 9; k++)
-            f[(6 + k) * N + j] = (R)(st[ST_F * N + 9 * p + k] - (sizeof(R) == 4 && (k % 4) == 0 ? 1.0 : 0.0));
+            f[(6 + k) * S + j] = (R)(st[ST_F * N + 9 * p + k] - (sizeof(R) == 4 && (k % 4) == 0 ? 1.0 : 0.0));
     if (mask & 8)
-        for (int k = 0; k < 6; k++) f[(15 + k) * N + j] = (R)st[ST_S * N + 6 * p + k];
-    if (mask & 16) f[23 * N + j] = (R)st[ST_VOL * N + p];
+        for (int k = 0; k < 6; k++) f[(15 + k) * S + j] = (R)st[ST_S * N + 6 * p + k];
+    if (mask & 16) f[23 * S + j] = (R)st[ST_VOL * N + p];
 }
 }  // namespace mpm
 
@@ -556,8 +558,8 @@ mpm_status mpm_gpu_download_particles(mpm_ctx *c, double *coord, double *vel, do
     const size_t N = (size_t)c->num;
     unsigned mask = (coord ? 1u : 0u) | (vel ? 2u : 0u) | (F ? 4u : 0u) | (stress ? 8u : 0u) | (vol ? 16u : 0u);
     const int nb = (int)((N + 255) / 256);
-    if (c->precision == 64) k_state_gather<double><<<nb, 256, 0, c->stream>>>((const double *)c->pbuf[c->cur], N, c->nreal, c->d_stage, mask);
-    else k_state_gather<float><<<nb, 256, 0, c->stream>>>((const float *)c->pbuf[c->cur], N, c->nreal, c->d_stage, mask);
+    if (c->precision == 64) k_state_gather<double><<<nb, 256, 0, c->stream>>>((const double *)c->pbuf[c->cur], N, c->pstride, c->nreal, c->d_stage, mask);
+    else k_state_gather<float><<<nb, 256, 0, c->stream>>>((const float *)c->pbuf[c->cur], N, c->pstride, c->nreal, c->d_stage, mask);
     c->launches++;
     if (check_launch(c) != MPM_OK) return MPM_ERR_CUDA;
     const double *st = c->d_stage;
@@ -587,9 +589,9 @@ mpm_status mpm_gpu_upload_particles(mpm_ctx *c, const double *coord, const doubl
     const int nb = (int)((N + 255) / 256);
     const int par = (int)(c->step & 1);
     if (c->precision == 64)
-        k_state_scatter<double><<<nb, 256, 0, c->stream>>>((double *)c->pbuf[c->cur], N, c->nreal, st, mask, c->d_ctl, par);
+        k_state_scatter<double><<<nb, 256, 0, c->stream>>>((double *)c->pbuf[c->cur], N, c->pstride, c->nreal, st, mask, c->d_ctl, par);
     else
-        k_state_scatter<float><<<nb, 256, 0, c->stream>>>((float *)c->pbuf[c->cur], N, c->nreal, st, mask, c->d_ctl, par);
+        k_state_scatter<float><<<nb, 256, 0, c->stream>>>((float *)c->pbuf[c->cur], N, c->pstride, c->nreal, st, mask, c->d_ctl, par);
     c->launches++;
     return check_launch(c);
 }

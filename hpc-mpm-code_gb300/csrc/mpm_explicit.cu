@@ -174,13 +174,19 @@ __device__ __forceinline__ void brick_origin(int b, const int *nb, int &ox, int 
 }
 
 // ================================================ FP32 linear, per cell
-// One CTA per brick, one thread per cell.  Cell corner c = i + 2 (j + 2 k).
-__global__ void __launch_bounds__(BRC) k_p2g_cell(StepArgs<float> a) {
+// One CTA per brick, two threads per cell: thread h of cell lc owns the four
+// corners of z-layer h (corner c = i + 2 (j + 2 k), k = h), so each thread
+// holds 32 FP32 accumulators.  Both threads of a cell read the same
+// particles (adjacent lanes, one memory transaction).
+constexpr int CELL_SPLIT = 2;
+constexpr int CELL_THREADS = BRC * CELL_SPLIT;
+
+__global__ void __launch_bounds__(CELL_THREADS, 3) k_p2g_cell(StepArgs<float> a) {
     __shared__ float corner[NACC * 8][BRC];       // 32 KB
     __shared__ Scales S;
     __shared__ int sh_red[32];
     const int b = blockIdx.x;
-    const int lc = threadIdx.x;
+    const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
     const int *cs = a.cstart + (size_t)b * (BRC + 1);
     if (cs[0] == cs[BRC]) return;   // empty brick (uniform across the CTA)
     int ox, oy, oz;
@@ -190,17 +196,17 @@ __global__ void __launch_bounds__(BRC) k_p2g_cell(StepArgs<float> a) {
     load_scales(a, S);
     const float fxg = a.grav[0] * a.facl, fyg = a.grav[1] * a.facl, fzg = a.grav[2] * a.facl;
     const Particles<float> &P = a.P;
-    float acc[NACC][8];
+    float acc[NACC][4];
 #pragma unroll
     for (int f = 0; f < NACC; f++)
 #pragma unroll
-        for (int c = 0; c < 8; c++) acc[f][c] = 0.0f;
+        for (int c = 0; c < 4; c++) acc[f][c] = 0.0f;
     int misses = 0, oobs = 0;
     for (int p = p0; p < p1; p++) {
         const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
         bool oob = false;
         const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
-        oobs += oob;
+        oobs += oob && h == 0;
         Axis<float, 1> ax, ay, az;
         axis_eval<float, 1>(x0, a.g, 0, px, ax);
         axis_eval<float, 1>(x1, a.g, 1, py, ay);
@@ -211,39 +217,38 @@ __global__ void __launch_bounds__(BRC) k_p2g_cell(StepArgs<float> a) {
                             ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
         const float mfx = m * fxg, mfy = m * fyg, mfz = m * fzg;
         const bool mine = (px == cx) && (py == cy) && (pz == cz);
-        misses += !mine;
+        misses += !mine && h == 0;
+        const float wz = h ? az.w[1] : az.w[0], dwz = h ? az.dw[1] : az.dw[0];
 #pragma unroll
-        for (int k = 0; k < 2; k++)
+        for (int j = 0; j < 2; j++)
 #pragma unroll
-            for (int j = 0; j < 2; j++)
+            for (int i = 0; i < 2; i++) {
+                const float wxy = ax.w[i] * ay.w[j];
+                float q[NACC];
+                p2g_terms(wxy * wz, ax.dw[i] * ay.w[j] * wz, ax.w[i] * ay.dw[j] * wz, wxy * dwz, m, vol, v, s, mfx,
+                          mfy, mfz, q);
+                const int c = i + 2 * j;
+                if (mine) {
 #pragma unroll
-                for (int i = 0; i < 2; i++) {
-                    const float wxy = ax.w[i] * ay.w[j];
-                    float q[NACC];
-                    p2g_terms(wxy * az.w[k], ax.dw[i] * ay.w[j] * az.w[k], ax.w[i] * ay.dw[j] * az.w[k],
-                              wxy * az.dw[k], m, vol, v, s, mfx, mfy, mfz, q);
-                    const int c = i + 2 * (j + 2 * k);
-                    if (mine) {
+                    for (int f = 0; f < NACC; f++) acc[f][c] += q[f];
+                } else {
+                    // a particle that left its sorted cell scatters on its own
+                    long long o[NACC];
+                    fx_terms(q, S, o);
+                    const size_t gn = node_id(a.g, px + i, py + j, pz + h);
 #pragma unroll
-                        for (int f = 0; f < NACC; f++) acc[f][c] += q[f];
-                    } else {
-                        // a particle that left its sorted cell scatters on its own
-                        long long o[NACC];
-                        fx_terms(q, S, o);
-                        const size_t gn = node_id(a.g, px + i, py + j, pz + k);
-#pragma unroll
-                        for (int f = 0; f < NACC; f++)
-                            if (o[f]) atomic_add_i64(&a.acc[(size_t)f * a.g.nodec + gn], o[f]);
-                        a.tileflag[tile_of_node(a.g, px + i, py + j, pz + k)] = 1;
-                    }
+                    for (int f = 0; f < NACC; f++)
+                        if (o[f]) atomic_add_i64(&a.acc[(size_t)f * a.g.nodec + gn], o[f]);
+                    a.tileflag[tile_of_node(a.g, px + i, py + j, pz + h)] = 1;
                 }
+            }
     }
 #pragma unroll
     for (int f = 0; f < NACC; f++)
 #pragma unroll
-        for (int c = 0; c < 8; c++) corner[f * 8 + c][lc] = acc[f][c];
+        for (int c = 0; c < 4; c++) corner[f * 8 + c + 4 * h][lc] = acc[f][c];
     int tot = block_reduce(misses + (oobs << 16), OpAddI(), sh_red);
-    if (lc == 0 && tot) {
+    if (threadIdx.x == 0 && tot) {
         if (tot & 0xffff) atomicAdd(&a.ctl->tile_misses, (unsigned)(tot & 0xffff));
         if (tot >> 16) atomicAdd(&a.ctl->err_oob, (unsigned)(tot >> 16));
     }
@@ -251,7 +256,7 @@ __global__ void __launch_bounds__(BRC) k_p2g_cell(StepArgs<float> a) {
     // node pass: each node of the (BRX+1)(BRY+1)(BRZ+1) box adds the corners of
     // its adjacent cells in a fixed order
     constexpr int NX = BRX + 1, NY = BRY + 1, NZ = BRZ + 1, NB = NX * NY * NZ;
-    for (int it = lc; it < NB * NACC; it += BRC) {
+    for (int it = threadIdx.x; it < NB * NACC; it += CELL_THREADS) {
         const int f = it / NB, n = it % NB;
         const int nx = n % NX, ny = (n / NX) % NY, nz = n / (NX * NY);
         const int gx = ox + nx, gy = oy + ny, gz = oz + nz;
@@ -277,13 +282,13 @@ __global__ void __launch_bounds__(BRC) k_p2g_cell(StepArgs<float> a) {
     }
 }
 
-__global__ void __launch_bounds__(BRC) k_g2p_musl_cell(StepArgs<float> a) {
+__global__ void __launch_bounds__(CELL_THREADS, 3) k_g2p_musl_cell(StepArgs<float> a) {
     __shared__ float corner[3 * 8][BRC];
     __shared__ Scales S;
     __shared__ long long sh_l[32];
     __shared__ float sh_f[32];
     const int b = blockIdx.x;
-    const int lc = threadIdx.x;
+    const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
     const int *cs = a.cstart + (size_t)b * (BRC + 1);
     if (cs[0] == cs[BRC]) return;
     int ox, oy, oz;
@@ -294,31 +299,29 @@ __global__ void __launch_bounds__(BRC) k_g2p_musl_cell(StepArgs<float> a) {
     const size_t N = (size_t)a.g.nodec;
     const Particles<float> &P = a.P;
     const bool flip = (a.scheme == MPM_FLIP);
-    // the gather fields of this cell's 8 nodes, loaded once
-    float Gc[3][8], Ec[8];
+    // the gather fields of this cell's four nodes of z-layer h, loaded once
+    float Gc[3][4], Ec[4];
 #pragma unroll
-    for (int k = 0; k < 2; k++)
+    for (int j = 0; j < 2; j++)
 #pragma unroll
-        for (int j = 0; j < 2; j++)
+        for (int i = 0; i < 2; i++) {
+            const int c = i + 2 * j;
+            if (p1 > p0) {
+                const int gx = min(cx + i, a.g.nnc[0] - 1), gy = min(cy + j, a.g.nnc[1] - 1),
+                          gz = min(cz + h, a.g.nnc[2] - 1);
+                const size_t gn = node_id(a.g, gx, gy, gz);
 #pragma unroll
-            for (int i = 0; i < 2; i++) {
-                const int c = i + 2 * (j + 2 * k);
-                if (p1 > p0) {
-                    const int gx = min(cx + i, a.g.nnc[0] - 1), gy = min(cy + j, a.g.nnc[1] - 1),
-                              gz = min(cz + k, a.g.nnc[2] - 1);
-                    const size_t gn = node_id(a.g, gx, gy, gz);
-#pragma unroll
-                    for (int d = 0; d < 3; d++) Gc[d][c] = ld(a.G + d * N + gn);
-                    Ec[c] = ld(a.nei + gn);
-                } else {
-                    Gc[0][c] = Gc[1][c] = Gc[2][c] = Ec[c] = 0.0f;
-                }
+                for (int d = 0; d < 3; d++) Gc[d][c] = ld(a.G + d * N + gn);
+                Ec[c] = ld(a.nei + gn);
+            } else {
+                Gc[0][c] = Gc[1][c] = Gc[2][c] = Ec[c] = 0.0f;
             }
-    float acc[3][8];
+        }
+    float acc[3][4];
 #pragma unroll
     for (int d = 0; d < 3; d++)
 #pragma unroll
-        for (int c = 0; c < 8; c++) acc[d][c] = 0.0f;
+        for (int c = 0; c < 4; c++) acc[d][c] = 0.0f;
     long long gacc = 0;
     float vmax = 0.0f;
     for (int p = p0; p < p1; p++) {
@@ -331,86 +334,86 @@ __global__ void __launch_bounds__(BRC) k_g2p_musl_cell(StepArgs<float> a) {
         axis_eval<float, 1>(x2, a.g, 2, pz, az);
         const float m = ld(P.m + p), vol = ld(P.vol + p);
         const bool mine = (px == cx) && (py == cy) && (pz == cz);
-        float v[3];
-        if (flip) {
-            v[0] = ld(P.v[0] + p); v[1] = ld(P.v[1] + p); v[2] = ld(P.v[2] + p);
-        } else {
-            v[0] = v[1] = v[2] = 0.0f;
-        }
-        float gu[3] = {0.0f, 0.0f, 0.0f};
-        // PIC v = sum N v*, FLIP v += sum N dt a (PIC/FLIP::VarG2P, map_and_interpolate.h:12-55)
+        const float wz = h ? az.w[1] : az.w[0], dwz = h ? az.dw[1] : az.dw[0];
+        // partial gathers over this thread's four nodes
+        float vs[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
-        for (int k = 0; k < 2; k++)
+        for (int j = 0; j < 2; j++)
 #pragma unroll
-            for (int j = 0; j < 2; j++)
-#pragma unroll
-                for (int i = 0; i < 2; i++) {
-                    const int c = i + 2 * (j + 2 * k);
-                    const float wxy = ax.w[i] * ay.w[j];
-                    const float N_ = wxy * az.w[k];
-                    float gv[3], e;
-                    if (mine) {
-                        gv[0] = Gc[0][c]; gv[1] = Gc[1][c]; gv[2] = Gc[2][c];
-                        e = Ec[c];
-                    } else {
-                        const size_t gn = node_id(a.g, px + i, py + j, pz + k);
-                        gv[0] = ld(a.G + gn); gv[1] = ld(a.G + N + gn); gv[2] = ld(a.G + 2 * N + gn);
-                        e = ld(a.nei + gn);
-                    }
-                    if (flip) {
-                        const float Nd = N_ * a.dt;
-#pragma unroll
-                        for (int d = 0; d < 3; d++) v[d] += Nd * gv[d];
-                    } else {
-#pragma unroll
-                        for (int d = 0; d < 3; d++) v[d] += N_ * gv[d];
-                    }
-                    gu[0] += ax.dw[i] * ay.w[j] * az.w[k] * e;
-                    gu[1] += ax.w[i] * ay.dw[j] * az.w[k] * e;
-                    gu[2] += wxy * az.dw[k] * e;
+            for (int i = 0; i < 2; i++) {
+                const int c = i + 2 * j;
+                const float wxy = ax.w[i] * ay.w[j];
+                const float N_ = wxy * wz;
+                float gv[3], e;
+                if (mine) {
+                    gv[0] = Gc[0][c]; gv[1] = Gc[1][c]; gv[2] = Gc[2][c];
+                    e = Ec[c];
+                } else {
+                    const size_t gn = node_id(a.g, px + i, py + j, pz + h);
+                    gv[0] = ld(a.G + gn); gv[1] = ld(a.G + N + gn); gv[2] = ld(a.G + 2 * N + gn);
+                    e = ld(a.nei + gn);
                 }
-        P.v[0][p] = v[0];
-        P.v[1][p] = v[1];
-        P.v[2][p] = v[2];
-        vmax = fmaxf(vmax, fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2]))));
-        const float tv = 2.0f * vol;
-        const float g0 = gu[0] * tv, g1 = gu[1] * tv, g2 = gu[2] * tv;
-        gacc += fx(g0 * g0 + g1 * g1 + g2 * g2, S.gd);
+                const float wv = flip ? N_ * a.dt : N_;
+#pragma unroll
+                for (int d = 0; d < 3; d++) vs[d] += wv * gv[d];
+                gu[0] += ax.dw[i] * ay.w[j] * wz * e;
+                gu[1] += ax.w[i] * ay.dw[j] * wz * e;
+                gu[2] += wxy * dwz * e;
+            }
+        // combine the two halves of the cell (a + b == b + a: both threads agree)
+        float v[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const float other = __shfl_xor_sync(0xffffffffu, vs[d], 1);
+            v[d] = vs[d] + other;
+            gu[d] += __shfl_xor_sync(0xffffffffu, gu[d], 1);
+        }
+        if (flip) {
+#pragma unroll
+            for (int d = 0; d < 3; d++) v[d] += ld(P.v[d] + p);
+        }
+        if (h == 0) {
+            P.v[0][p] = v[0];
+            P.v[1][p] = v[1];
+            P.v[2][p] = v[2];
+            vmax = fmaxf(vmax, fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2]))));
+            const float tv = 2.0f * vol;
+            const float g0 = gu[0] * tv, g1 = gu[1] * tv, g2 = gu[2] * tv;
+            gacc += fx(g0 * g0 + g1 * g1 + g2 * g2, S.gd);
+        }
         // MUSL re-projection of momentum (var_trans_solid_explicit.cpp:108-129)
 #pragma unroll
-        for (int k = 0; k < 2; k++)
+        for (int j = 0; j < 2; j++)
 #pragma unroll
-            for (int j = 0; j < 2; j++)
+            for (int i = 0; i < 2; i++) {
+                const int c = i + 2 * j;
+                const float Nm = ax.w[i] * ay.w[j] * wz * m;
+                if (mine) {
 #pragma unroll
-                for (int i = 0; i < 2; i++) {
-                    const int c = i + 2 * (j + 2 * k);
-                    const float Nm = ax.w[i] * ay.w[j] * az.w[k] * m;
-                    if (mine) {
+                    for (int d = 0; d < 3; d++) acc[d][c] += Nm * v[d];
+                } else {
+                    const size_t gn = node_id(a.g, px + i, py + j, pz + h);
 #pragma unroll
-                        for (int d = 0; d < 3; d++) acc[d][c] += Nm * v[d];
-                    } else {
-                        const size_t gn = node_id(a.g, px + i, py + j, pz + k);
-#pragma unroll
-                        for (int d = 0; d < 3; d++) {
-                            long long q = fx(Nm * v[d], S.q);
-                            if (q) atomic_add_i64(&a.acc2[d * N + gn], q);
-                        }
+                    for (int d = 0; d < 3; d++) {
+                        long long q = fx(Nm * v[d], S.q);
+                        if (q) atomic_add_i64(&a.acc2[d * N + gn], q);
                     }
                 }
+            }
     }
 #pragma unroll
     for (int d = 0; d < 3; d++)
 #pragma unroll
-        for (int c = 0; c < 8; c++) corner[d * 8 + c][lc] = acc[d][c];
+        for (int c = 0; c < 4; c++) corner[d * 8 + c + 4 * h][lc] = acc[d][c];
     long long gsum = block_reduce(gacc, OpAddL(), sh_l);
     float vm = block_reduce(vmax, OpMaxF(), sh_f);
-    if (lc == 0) {
+    if (threadIdx.x == 0) {
         if (gsum) atomicAdd(&a.ctl->geup_acc, (unsigned long long)gsum);
         if (vm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VMAX], vm * 1.000001f);
     }
     __syncthreads();
     constexpr int NX = BRX + 1, NY = BRY + 1, NZ = BRZ + 1, NB = NX * NY * NZ;
-    for (int it = lc; it < NB * 3; it += BRC) {
+    for (int it = threadIdx.x; it < NB * 3; it += CELL_THREADS) {
         const int d = it / NB, n = it % NB;
         const int nx = n % NX, ny = (n / NX) % NY, nz = n / (NX * NY);
         const int gx = ox + nx, gy = oy + ny, gz = oz + nz;
@@ -952,7 +955,7 @@ static StepArgs<R> make_args(mpm_ctx *c) {
     a.g.nodec = c->g.nodec;
     a.num = c->num;
     char *base = (char *)c->pbuf[c->cur];
-    size_t n = (size_t)c->num, rs = sizeof(R);
+    size_t n = c->pstride, rs = sizeof(R);
     R *f = (R *)base;
     for (int k = 0; k < 3; k++) a.P.x[k] = f + (0 + k) * n;
     for (int k = 0; k < 3; k++) a.P.v[k] = f + (3 + k) * n;
@@ -1021,7 +1024,7 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
         timer_begin(c, K_P2G);
         if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
             if (use_cell_kernels(c)) {
-                k_p2g_cell<<<c->g.nbricks, BRC, 0, c->stream>>>(a);
+                k_p2g_cell<<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
                 timer_end(c, K_P2G);
                 c->launches++;
                 return check_launch(c);
@@ -1035,7 +1038,7 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
         timer_begin(c, K_G2P_MUSL);
         if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
             if (use_cell_kernels(c)) {
-                k_g2p_musl_cell<<<c->g.nbricks, BRC, 0, c->stream>>>(a);
+                k_g2p_musl_cell<<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
                 timer_end(c, K_G2P_MUSL);
                 c->launches++;
                 return check_launch(c);

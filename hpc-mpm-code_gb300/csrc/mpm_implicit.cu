@@ -112,7 +112,7 @@ struct PView {
 
 static PView pview(mpm_ctx *c) {
     PView v;
-    size_t n = (size_t)c->num;
+    size_t n = c->pstride;
     double *f = (double *)c->pbuf[c->cur];
     for (int k = 0; k < 3; k++) v.x[k] = f + k * n;
     for (int k = 0; k < 3; k++) v.v[k] = f + (3 + k) * n;

@@ -3,7 +3,9 @@
 // Data layout in HBM
 //   particles: structure of arrays, one array per scalar component, in the
 //     context's precision R (float or double): x[3], v[3], F[9] (row major;
-//     FP32 stores the displacement gradient F - I in these arrays),
+//     FP32 stores the displacement gradient F - I in these arrays), each
+//     array pstride (num rounded up to 64) elements long so that every
+//     array starts 256-byte aligned for bulk asynchronous copies,
 //     sigma[6] (Voigt xx,yy,zz,yz,xz,xy), m, vol0, vol; plus matid and the
 //     particle's load index (pid).  Two copies exist; a re-sort permutes A
 //     into B and swaps.
@@ -118,6 +120,7 @@ struct mpm_ctx {
     int64_t num = 0;
     size_t rsize = 4;
     int nreal = 24;                        // real fields per particle: 24, or 27 with acceleration (implicit)
+    size_t pstride = 64;                   // elements between particle field arrays: num rounded up to 64
     void *pbuf[2] = {nullptr, nullptr};   // two SoA copies
     int cur = 0;
     double mmax = 0.0;

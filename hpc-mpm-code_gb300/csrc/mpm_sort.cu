@@ -156,11 +156,10 @@ __global__ void __launch_bounds__(BRC) k_cell_sort(const int *bstart, const int 
 
 // dst[j] = src[perm[j]] for all real fields and the two int fields.
 template <typename R>
-__global__ void k_permute(const R *src, R *dst, const int *perm, int n, int nreal) {
+__global__ void k_permute(const R *src, R *dst, const int *perm, int n, int nreal, size_t N) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     int i = perm[j];
-    size_t N = (size_t)n;
 #pragma unroll 4
     for (int f = 0; f < nreal; f++) dst[f * N + j] = src[f * N + i];
     const int *si = (const int *)(src + nreal * N);
@@ -185,7 +184,7 @@ static mpm_status sort_impl(mpm_ctx *c) {
     g.nodec = c->g.nodec;
     const R *src = (const R *)c->pbuf[c->cur];
     R *dst = (R *)c->pbuf[c->cur ^ 1];
-    size_t N = (size_t)n;
+    size_t N = c->pstride;
     const int *pid = (const int *)(src + c->nreal * N) + N;
     int nb = (n + 255) / 256;
     timer_begin(c, K_BIN);
@@ -202,7 +201,7 @@ static mpm_status sort_impl(mpm_ctx *c) {
                                                       c->d_cstart);
     timer_end(c, K_SCATTER);
     timer_begin(c, K_PERMUTE);
-    k_permute<R><<<nb, 256, 0, c->stream>>>(src, dst, c->d_perm, n, c->nreal);
+    k_permute<R><<<nb, 256, 0, c->stream>>>(src, dst, c->d_perm, n, c->nreal, N);
     timer_end(c, K_PERMUTE);
     c->launches += 5;
     c->cur ^= 1;
