@@ -422,6 +422,7 @@ static mpm_status read_errors(mpm_ctx *c) {
     CK(cudaStreamSynchronize(c->stream));
     CK(cudaMemcpy(c->h_ctl, c->d_ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost));
     if (c->latched != MPM_OK) return c->latched;
+    if (c->h_ctl->err_timeout) return MPM_ERR_DEVICE_TIMEOUT;
     if (c->h_ctl->err_nonfinite) return MPM_ERR_NONFINITE;
     if (c->h_ctl->err_oob) return MPM_ERR_PARTICLE_OUT_OF_BOX;
     return MPM_OK;

@@ -24,6 +24,7 @@
 //   * FP64, and quadratic B-splines: particles of a brick chunk convert every
 //     contribution to int64 fixed point and scatter into a shared staging box
 //     with atomics; the sums are exact and independent of particle order.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 
@@ -937,6 +938,174 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
     }
 }
 
+// ------------------------------------- G2P 2, FP32 linear, TMA-staged input
+// The same update as k_g2p_update for FP32 and linear shape functions, with
+// the particle fields it reads (x 3, H 9, sigma 6, vol0, vol, matid) brought
+// into shared memory by bulk asynchronous copies, two chunks of UCH particles
+// in flight per CTA, so that memory parallelism does not depend on how many
+// warps are resident.  Persistent CTAs walk the chunks with a grid stride.
+constexpr int UCH = 256;                          // particles per chunk (= threads per CTA)
+constexpr int UNF = 20;                           // staged real fields
+constexpr size_t USTAGE = (size_t)UNF * UCH * 4 + UCH * 4;   // bytes per stage
+constexpr unsigned UWAIT = 1u << 22;              // bounded mbarrier wait (try_wait iterations)
+
+__global__ void __launch_bounds__(UCH) k_g2p_update_tma(StepArgs<float> a, int nchunks) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) unsigned long long bar[2];
+    __shared__ float sh_f[32];
+    __shared__ int sh_i[32];
+    const size_t N = (size_t)a.g.nodec;
+    const Particles<float> &P = a.P;
+    const float *src[UNF] = {P.x[0], P.x[1], P.x[2], P.F[0], P.F[1], P.F[2], P.F[3], P.F[4], P.F[5], P.F[6],
+                             P.F[7], P.F[8], P.s[0], P.s[1], P.s[2], P.s[3], P.s[4], P.s[5], P.vol0, P.vol};
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](int chunk, int stage) {
+        const int p0 = chunk * UCH;
+        const int cnt = min(UCH, (int)a.num - p0);
+        const unsigned bytes = (unsigned)((cnt + 3) & ~3) * 4u;   // whole 16-byte units (arrays are padded)
+        float *dst = (float *)(smem + stage * USTAGE);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&bar[stage], bytes * (UNF + 1));
+        for (int f = 0; f < UNF; f++) bulk_g2s(dst + f * UCH, src[f] + p0, bytes, &bar[stage]);
+        bulk_g2s(dst + UNF * UCH, P.matid + p0, bytes, &bar[stage]);
+    };
+    const float rb0 = (float)a.ctl->b0;
+    float volmax = 0.0f, vsmax = 0.0f;
+    int bad = 0;
+    bool failed = false;
+    int it = 0;
+    if (threadIdx.x == 0 && (int)blockIdx.x < nchunks) issue(blockIdx.x, 0);
+    for (int chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x, it++) {
+        const int stage = it & 1;
+        if (threadIdx.x == 0 && chunk + (int)gridDim.x < nchunks) issue(chunk + gridDim.x, stage ^ 1);
+        const bool ok = mbar_wait_bounded(&bar[stage], (unsigned)((it >> 1) & 1), UWAIT);
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        const float *sf = (const float *)(smem + stage * USTAGE);
+        const int *smid = (const int *)(sf + UNF * UCH);
+        const int t = threadIdx.x;
+        const int p = chunk * UCH + t;
+        if (p < a.num) {
+            float x[3] = {sf[0 * UCH + t], sf[1 * UCH + t], sf[2 * UCH + t]};
+            bool oob = false;
+            const int cx = cell_of(x[0], a.g, 0, oob), cy = cell_of(x[1], a.g, 1, oob), cz = cell_of(x[2], a.g, 2, oob);
+            Axis<float, 1> ax, ay, az;
+            axis_eval<float, 1>(x[0], a.g, 0, cx, ax);
+            axis_eval<float, 1>(x[1], a.g, 1, cy, ay);
+            axis_eval<float, 1>(x[2], a.g, 2, cz, az);
+            float D[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            float du[3] = {0, 0, 0}, gu[3] = {0, 0, 0};
+#pragma unroll
+            for (int k = 0; k < 2; k++)
+#pragma unroll
+                for (int j = 0; j < 2; j++)
+#pragma unroll
+                    for (int i = 0; i < 2; i++) {
+                        const float wxy = ax.w[i] * ay.w[j];
+                        const float N_ = wxy * az.w[k];
+                        const float dn[3] = {ax.dw[i] * ay.w[j] * az.w[k], ax.w[i] * ay.dw[j] * az.w[k], wxy * az.dw[k]};
+                        const size_t gn = node_id(a.g, cx + i, cy + j, cz + k);
+                        const float nv[3] = {ld(a.nvel2 + gn), ld(a.nvel2 + N + gn), ld(a.nvel2 + 2 * N + gn)};
+#pragma unroll
+                        for (int r = 0; r < 3; r++)
+#pragma unroll
+                            for (int c = 0; c < 3; c++) D[r][c] += dn[c] * nv[r] * a.dt;
+#pragma unroll
+                        for (int c = 0; c < 3; c++) du[c] += N_ * nv[c];
+                        if (rb0 != 0.0f) {
+                            const float e = ld(a.nei + gn);
+#pragma unroll
+                            for (int c = 0; c < 3; c++) gu[c] += dn[c] * e;
+                        }
+                    }
+            float xn[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) xn[c] = x[c] + du[c] * a.dt;
+            if (rb0 != 0.0f) {
+                const float tv = 2.0f * sf[19 * UCH + t];
+#pragma unroll
+                for (int c = 0; c < 3; c++) xn[c] += -rb0 * (gu[c] * tv);
+            }
+            // H <- H + D + D H (the FP32 path stores H = F - I)
+            float H[3][3], Hn[3][3];
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) H[r][c] = sf[(3 + 3 * r + c) * UCH + t];
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    float acc = H[r][c] + D[r][c];
+#pragma unroll
+                    for (int k2 = 0; k2 < 3; k2++) acc += D[r][k2] * H[k2][c];
+                    Hn[r][c] = acc;
+                }
+            const float jm1 = det_ipm1(Hn);
+            const float J = 1.0f + jm1;
+            const float volp = J * sf[18 * UCH + t];
+            float s[6];
+#pragma unroll
+            for (int k = 0; k < 6; k++) s[k] = sf[(12 + k) * UCH + t];
+            const int mid = smid[t];
+            const int model = a.iprop[mid];
+            const float E = (float)a.matprop[3 * mid], nu = (float)a.matprop[3 * mid + 1];
+            if (model == 0) lin_elast_update(s, D, E, nu);
+            else if (model == 1) neo_hookean_stress_h(s, Hn, jm1, E, nu);
+            else if (model == -1)
+#pragma unroll
+                for (int k = 0; k < 6; k++) s[k] = 0.0f;
+            const bool fin = isfinite(xn[0]) && isfinite(xn[1]) && isfinite(xn[2]) && isfinite(J) &&
+                             isfinite(s[0]) && isfinite(s[1]) && isfinite(s[2]) && isfinite(s[3]) && isfinite(s[4]) &&
+                             isfinite(s[5]);
+            bad += !fin;
+#pragma unroll
+            for (int c = 0; c < 3; c++) P.x[c][p] = xn[c];
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) P.F[3 * r + c][p] = Hn[r][c];
+#pragma unroll
+            for (int k = 0; k < 6; k++) P.s[k][p] = s[k];
+            P.vol[p] = volp;
+            const float rs0 = fabsf(s[0]) + fabsf(s[5]) + fabsf(s[4]);
+            const float rs1 = fabsf(s[5]) + fabsf(s[1]) + fabsf(s[3]);
+            const float rs2 = fabsf(s[4]) + fabsf(s[3]) + fabsf(s[2]);
+            const float vf = fabsf(volp);
+            volmax = fmaxf(volmax, vf);
+            vsmax = fmaxf(vsmax, vf * fmaxf(rs0, fmaxf(rs1, rs2)));
+        }
+        __syncthreads();   // the stage is refilled only after every thread has read it
+    }
+    if (failed) {
+        // let the copies this CTA started land before the CTA exits
+        if (threadIdx.x == 0) {
+            atomicAdd(&a.ctl->err_timeout, 1u);
+            const int stage = it & 1;
+            mbar_wait_bounded(&bar[stage], (unsigned)((it >> 1) & 1), UWAIT);
+            if (blockIdx.x + (it + 1) * gridDim.x < (unsigned)nchunks)
+                mbar_wait_bounded(&bar[stage ^ 1], (unsigned)(((it + 1) >> 1) & 1), UWAIT);
+        }
+        __syncthreads();
+        return;
+    }
+    const float vm = block_reduce(volmax, OpMaxF(), sh_f);
+    const float sm = block_reduce(vsmax, OpMaxF(), sh_f);
+    const int nb = block_reduce(bad, OpAddI(), sh_i);
+    if (threadIdx.x == 0) {
+        if (vm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VOLMAX], vm * 1.000001f);
+        if (sm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VOLSMAX], sm * 1.000001f);
+        if (nb) atomicAdd(&a.ctl->err_nonfinite, (unsigned)nb);
+    }
+}
+
 // ------------------------------------------------------------- host side
 template <typename R>
 static StepArgs<R> make_args(mpm_ctx *c) {
@@ -1050,8 +1219,28 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
         timer_end(c, K_G2P_MUSL);
     } else {
         timer_begin(c, K_G2P_UPDATE);
-        const int nb = (int)((c->num + 255) / 256);
-        k_g2p_update<R, OX, OY, OZ><<<nb, 256, 0, c->stream>>>(a);
+        bool staged = false;
+        if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
+            if (c->tma_update) {
+                const int nchunks = (int)((c->num + UCH - 1) / UCH);
+                static bool attr = false;
+                if (!attr) {
+                    cudaFuncSetAttribute(k_g2p_update_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(2 * USTAGE));
+                    attr = true;
+                }
+                int dev = 0, nsm = 148;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+                const int grid = std::min(nchunks, nsm * 4);
+                k_g2p_update_tma<<<grid, UCH, 2 * USTAGE, c->stream>>>(a, nchunks);
+                staged = true;
+            }
+        }
+        if (!staged) {
+            const int nb = (int)((c->num + 255) / 256);
+            k_g2p_update<R, OX, OY, OZ><<<nb, 256, 0, c->stream>>>(a);
+        }
         timer_end(c, K_G2P_UPDATE);
     }
     c->launches++;

@@ -68,6 +68,7 @@ struct DevCtl {
     unsigned int tile_misses;
     double p2g_inv[4];               // 2^-e of the P2G scales (mass, vof, momentum, force) of the last P2G
     double b0;                       // shifting coefficient of this step
+    unsigned int err_timeout;        // bounded device waits that gave up
 };
 
 template <typename R>
@@ -153,6 +154,7 @@ struct mpm_ctx {
     bool accum_dirty = false;
     bool write_nodal_dl = false;
     int cell_scatter = 1;   // FP32 linear: per-cell register scatter (else staging-box atomics)
+    int tma_update = 1;     // FP32 linear: particle update with bulk-copy staged input
     mpm_status latched = MPM_OK;
     mpm::KernelTimer timer;
     struct ImpState *imp = nullptr;   // implicit solid state (mpm_implicit.cu)
