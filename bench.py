@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--implicit-steps", type=int, default=3,
+                    help="implicit cantilever steps timed after the explicit run (0 skips)")
     ap.add_argument("--cells", type=int, default=80,
                     help="block edge in cells (80 = the 4,096,000-particle workload; smaller for profiling)")
     return ap.parse_args()
@@ -134,6 +136,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
+def max_over_ranks(value, world, device="cpu"):
+    """Largest value over the ranks (the slowest replica's time); identity at N = 1."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(num, steps, ms_max, world):
+    """Whole-job particle-steps/s of `world` independent replicas timed by the slowest one."""
+    return world * num * steps / (ms_max * 1e-3)
+
+
 def algorithmic_bytes(num, nodec):
     # per explicit step, FP32: 23 words read + 21 written per particle, 7 nodal words written + read
     return num * 176 + nodec * 56
@@ -196,6 +215,31 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_implicit(args, torch, stream):
+    """The implicit solid: 1,728,000-particle Neo-Hookean cantilever on a 64^3 grid,
+    E = 1e7 Pa, nu = 0.3, dt = 1e-3 s, Newton + diagonally scaled CG solved to a
+    relative residual of 1e-8 (eps = 1e-16 on squared norms), FP64."""
+    from mpm_gb300 import capi, scenes
+
+    s = scenes.cantilever(iprop=1)
+    gpu = capi.GpuImplicitSolid(s, nr_flag=True, stream=stream.cuda_stream)
+    gpu.implicit_steps(1, eps=1.0e-16)           # warm-up step
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    t0 = time.perf_counter()
+    kry, newton, rel = gpu.implicit_steps(args.implicit_steps, eps=1.0e-16)
+    ev1.record(stream)
+    ev1.synchronize()
+    ms = max(ev0.elapsed_time(ev1), (time.perf_counter() - t0) * 1e3) / args.implicit_steps
+    gpu.close()
+    return {"metric": "implicit step time", "value": ms, "unit": "ms/step", "higher_is_better": False,
+            "steps": args.implicit_steps, "particles": s.num, "grid": list(s.xyelem), "dtype": "f64",
+            "solver": "Newton + Jacobi (symmetric diagonal scaling) CG to ||r||/||r0|| <= 1e-8",
+            "krylov_iters_per_step": kry / args.implicit_steps, "newton_iters_per_step": newton / args.implicit_steps,
+            "learned_preconditioner": "not built"}
+
+
 def run_gb300(args):
     import torch
 
@@ -233,12 +277,9 @@ def run_gb300(args):
     gpu.sync()
     ms = ev0.elapsed_time(ev1)
     launches = gpu.stats()["kernel_launches"] - launches0
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, "cuda")
     ms_step = ms / args.steps
-    value = world * s.num * args.steps / (ms * 1e-3)
+    value = replica_throughput(s.num, args.steps, ms, world)
 
     # per-kernel device time over a second timed window (events around every kernel)
     gpu.enable_kernel_timing(True)
@@ -284,16 +325,20 @@ def run_gb300(args):
     ev1.synchronize()
     e_ms = max(ev0.elapsed_time(ev1), (time.perf_counter() - t0) * 1e3)
     barrier()
-    if world > 1:
-        t = torch.tensor([e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e_ms = float(t.item())
+    e_ms = max_over_ranks(e_ms, world, "cuda")
     state_bytes = n * 8 * (3 + 3 + 9 + 6 + 1)
-    e2e = {"value": world * n * e_steps / (e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": state_bytes,
+    e2e = {"value": replica_throughput(n, e_steps, e_ms, world), "unit": METRIC, "h2d_bytes_per_step": state_bytes,
            "d2h_bytes_per_step": state_bytes, "steps": e_steps,
            "call": "mpm_gpu_upload_particles + mpm_gpu_step_explicit(1) + mpm_gpu_download_particles, FP64 host "
                    "arrays in pinned memory"}
     gpu.sync()
+
+    implicit = None
+    if args.implicit_steps > 0:
+        try:
+            implicit = run_implicit(args, torch, stream)
+        except Exception as exc:   # reported, never required
+            implicit = {"metric": "implicit step time", "value": None, "error": str(exc)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -311,7 +356,7 @@ def run_gb300(args):
                            "dt": s.dt, "scheme": "PIC", "parallelism": f"replicas x{world}",
                            "l2": "inputs larger than L2: 393 MB particle state per step, no flush"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(),
-                "gpu_launches": int(launches), "kernels": kernels}
+                "gpu_launches": int(launches), "kernels": kernels, "implicit": implicit}
         print(json.dumps(line), flush=True)
     gpu.close()
     if world > 1:

@@ -56,6 +56,26 @@ def _compile(src, verbose=False, ptxas_info=False):
     return obj, r.stderr
 
 
+DRIVER = os.path.join(LIBDIR, "explicit_driver")
+
+
+def build_host(verbose: bool = False) -> str:
+    """The C++ host layer (host/gpu_solid.cpp) and its explicit driver, linked
+    against libmpm_gb300.so."""
+    lib = build(verbose)
+    srcs = [os.path.join(HOST, "gpu_solid.cpp"), os.path.join(HOST, "explicit_driver.cpp")]
+    deps = srcs + [os.path.join(HOST, "gpu_solid.h"), lib]
+    if _stale(DRIVER, deps):
+        cmd = ["g++", "-O2", "-std=c++17", "-I" + INCLUDE, "-I" + HOST] + srcs + [
+            "-L" + LIBDIR, "-lmpm_gb300", "-Wl,-rpath," + LIBDIR, "-o", DRIVER]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"host build failed:\n{r.stdout}\n{r.stderr}")
+    return DRIVER
+
+
 def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
