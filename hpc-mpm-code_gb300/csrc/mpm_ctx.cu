@@ -616,6 +616,48 @@ mpm_status mpm_gpu_get_stats(mpm_ctx *c, mpm_stats *out) {
     return MPM_OK;
 }
 
+mpm_status mpm_gpu_autotune(mpm_ctx *c, int steps_per_trial, double facl) {
+    if (!c || steps_per_trial <= 0) return MPM_ERR_BAD_ARG;
+    if (c->num == 0 || c->stage != 0) return MPM_ERR_STATE;
+    // every candidate computes bitwise the same step, so the trial steps are
+    // ordinary simulation steps; each kernel class is timed on its own
+    const int p2g_opts[3] = {2, 3, 2}, musl_opts[3] = {3, 2, 3}, upd_opts[3] = {4, 3, 6};
+    double best[3] = {1e300, 1e300, 1e300};
+    Tune pick = c->tune;
+    const bool was_on = c->timer.on;
+    for (int t = 0; t < 3; t++) {
+        c->tune.p2g_minb = p2g_opts[t];
+        c->tune.musl_minb = musl_opts[t];
+        c->tune.update_ctas_per_sm = upd_opts[t];
+        int cnt = NKCLASS;
+        const char *names[NKCLASS];
+        double ms[NKCLASS];
+        int64_t nl[NKCLASS];
+        mpm_gpu_kernel_times(c, &cnt, nullptr, nullptr, nullptr);   // discard earlier records
+        c->timer.on = true;
+        mpm_status st = mpm_gpu_step_explicit(c, steps_per_trial, facl);
+        c->timer.on = was_on;
+        if (st != MPM_OK) return st;
+        cnt = NKCLASS;
+        st = mpm_gpu_kernel_times(c, &cnt, names, ms, nl);
+        if (st != MPM_OK) return st;
+        if (ms[K_P2G] < best[0]) { best[0] = ms[K_P2G]; pick.p2g_minb = p2g_opts[t]; }
+        if (ms[K_G2P_MUSL] < best[1]) { best[1] = ms[K_G2P_MUSL]; pick.musl_minb = musl_opts[t]; }
+        if (ms[K_G2P_UPDATE] < best[2]) { best[2] = ms[K_G2P_UPDATE]; pick.update_ctas_per_sm = upd_opts[t]; }
+    }
+    pick.done = true;
+    c->tune = pick;
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_get_tuning(mpm_ctx *c, int *p2g_minb, int *musl_minb, int *update_ctas_per_sm) {
+    if (!c) return MPM_ERR_BAD_ARG;
+    if (p2g_minb) *p2g_minb = c->tune.p2g_minb;
+    if (musl_minb) *musl_minb = c->tune.musl_minb;
+    if (update_ctas_per_sm) *update_ctas_per_sm = c->tune.update_ctas_per_sm;
+    return MPM_OK;
+}
+
 mpm_status mpm_gpu_enable_kernel_timing(mpm_ctx *c, int on) {
     if (!c) return MPM_ERR_BAD_ARG;
     c->timer.on = on != 0;

@@ -99,9 +99,16 @@ __device__ __forceinline__ void axis_eval<double, 2>(double x, const KGeom<doubl
 
 // Element index of a point (MeshPointLinklist, module/material_point.cpp:59-65).
 // Out-of-grid points are clamped and reported through *oob.
+__device__ __forceinline__ float cell_coord(float x, const KGeom<float> &g, int d) {
+    return (x - g.xmin[d]) * g.inv_dx[d];
+}
+__device__ __forceinline__ double cell_coord(double x, const KGeom<double> &g, int d) {
+    return (x - g.xmin[d]) / g.dx[d];   // the reference's floor((x - xmin) / dx) in FP64
+}
+
 template <typename R>
 __device__ __forceinline__ int cell_of(R x, const KGeom<R> &g, int d, bool &oob) {
-    R t = (x - g.xmin[d]) / g.dx[d];
+    R t = cell_coord(x, g, d);
     int c = (int)floor(t);
     if (!(t >= (R)0) || c >= g.nel[d]) {   // also catches NaN
         oob = true;

@@ -182,7 +182,8 @@ __device__ __forceinline__ void brick_origin(int b, const int *nb, int &ox, int 
 constexpr int CELL_SPLIT = 2;
 constexpr int CELL_THREADS = BRC * CELL_SPLIT;
 
-__global__ void __launch_bounds__(CELL_THREADS, 3) k_p2g_cell(StepArgs<float> a) {
+template <int MINB>
+__global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell(StepArgs<float> a) {
     __shared__ float corner[NACC * 8][BRC];       // 32 KB
     __shared__ Scales S;
     __shared__ int sh_red[32];
@@ -218,8 +219,26 @@ __global__ void __launch_bounds__(CELL_THREADS, 3) k_p2g_cell(StepArgs<float> a)
                             ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
         const float mfx = m * fxg, mfy = m * fyg, mfz = m * fzg;
         const bool mine = (px == cx) && (py == cy) && (pz == cz);
-        misses += !mine && h == 0;
         const float wz = h ? az.w[1] : az.w[0], dwz = h ? az.dw[1] : az.dw[0];
+        if (!mine) {
+            // a particle that left its sorted cell scatters on its own
+            misses += h == 0;
+#pragma unroll 1
+            for (int c = 0; c < 4; c++) {
+                const int i = c & 1, j = c >> 1;
+                const float wxy = ax.w[i] * ay.w[j];
+                float q[NACC];
+                p2g_terms(wxy * wz, ax.dw[i] * ay.w[j] * wz, ax.w[i] * ay.dw[j] * wz, wxy * dwz, m, vol, v, s, mfx,
+                          mfy, mfz, q);
+                long long o[NACC];
+                fx_terms(q, S, o);
+                const size_t gn = node_id(a.g, px + i, py + j, pz + h);
+                for (int f = 0; f < NACC; f++)
+                    if (o[f]) atomic_add_i64(&a.acc[(size_t)f * a.g.nodec + gn], o[f]);
+                a.tileflag[tile_of_node(a.g, px + i, py + j, pz + h)] = 1;
+            }
+            continue;
+        }
 #pragma unroll
         for (int j = 0; j < 2; j++)
 #pragma unroll
@@ -229,19 +248,8 @@ __global__ void __launch_bounds__(CELL_THREADS, 3) k_p2g_cell(StepArgs<float> a)
                 p2g_terms(wxy * wz, ax.dw[i] * ay.w[j] * wz, ax.w[i] * ay.dw[j] * wz, wxy * dwz, m, vol, v, s, mfx,
                           mfy, mfz, q);
                 const int c = i + 2 * j;
-                if (mine) {
 #pragma unroll
-                    for (int f = 0; f < NACC; f++) acc[f][c] += q[f];
-                } else {
-                    // a particle that left its sorted cell scatters on its own
-                    long long o[NACC];
-                    fx_terms(q, S, o);
-                    const size_t gn = node_id(a.g, px + i, py + j, pz + h);
-#pragma unroll
-                    for (int f = 0; f < NACC; f++)
-                        if (o[f]) atomic_add_i64(&a.acc[(size_t)f * a.g.nodec + gn], o[f]);
-                    a.tileflag[tile_of_node(a.g, px + i, py + j, pz + h)] = 1;
-                }
+                for (int f = 0; f < NACC; f++) acc[f][c] += q[f];
             }
     }
 #pragma unroll
@@ -283,7 +291,8 @@ __global__ void __launch_bounds__(CELL_THREADS, 3) k_p2g_cell(StepArgs<float> a)
     }
 }
 
-__global__ void __launch_bounds__(CELL_THREADS, 3) k_g2p_musl_cell(StepArgs<float> a) {
+template <int MINB>
+__global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell(StepArgs<float> a) {
     __shared__ float corner[3 * 8][BRC];
     __shared__ Scales S;
     __shared__ long long sh_l[32];
@@ -1193,7 +1202,8 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
         timer_begin(c, K_P2G);
         if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
             if (use_cell_kernels(c)) {
-                k_p2g_cell<<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                if (c->tune.p2g_minb == 3) k_p2g_cell<3><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                else k_p2g_cell<2><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
                 timer_end(c, K_P2G);
                 c->launches++;
                 return check_launch(c);
@@ -1207,7 +1217,8 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
         timer_begin(c, K_G2P_MUSL);
         if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
             if (use_cell_kernels(c)) {
-                k_g2p_musl_cell<<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                if (c->tune.musl_minb == 2) k_g2p_musl_cell<2><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                else k_g2p_musl_cell<3><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
                 timer_end(c, K_G2P_MUSL);
                 c->launches++;
                 return check_launch(c);
@@ -1232,7 +1243,7 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                 int dev = 0, nsm = 148;
                 cudaGetDevice(&dev);
                 cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-                const int grid = std::min(nchunks, nsm * 4);
+                const int grid = std::min(nchunks, nsm * c->tune.update_ctas_per_sm);
                 k_g2p_update_tma<<<grid, UCH, 2 * USTAGE, c->stream>>>(a, nchunks);
                 staged = true;
             }

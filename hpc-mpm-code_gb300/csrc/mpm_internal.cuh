@@ -93,6 +93,15 @@ struct Fix {
     double inv;     // 2^-e
 };
 
+// Launch variants that give bitwise identical results; chosen by
+// mpm_gpu_autotune from measured times (defaults otherwise).
+struct Tune {
+    int p2g_minb = 2;               // resident CTAs the per-cell P2G is compiled for (2 or 3)
+    int musl_minb = 3;              // same for the gather + MUSL kernel
+    int update_ctas_per_sm = 4;     // persistent CTAs per SM of the staged particle update
+    bool done = false;
+};
+
 struct KernelTimer {
     bool on = false;
     std::vector<cudaEvent_t> ev;      // pairs
@@ -157,6 +166,7 @@ struct mpm_ctx {
     int tma_update = 1;     // FP32 linear: particle update with bulk-copy staged input
     mpm_status latched = MPM_OK;
     mpm::KernelTimer timer;
+    mpm::Tune tune;
     struct ImpState *imp = nullptr;   // implicit solid state (mpm_implicit.cu)
     std::vector<int> bc_nodes[3];
     std::vector<double> bc_vals[3];

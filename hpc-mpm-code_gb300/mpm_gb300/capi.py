@@ -67,7 +67,8 @@ EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_s
            "mpm_gpu_upload_particles", "mpm_gpu_sync",
            "mpm_gpu_get_stats", "mpm_gpu_enable_kernel_timing", "mpm_gpu_kernel_times", "mpm_gpu_implicit_setup",
            "mpm_gpu_implicit_step", "mpm_gpu_implicit_assemble", "mpm_gpu_implicit_get_system",
-           "mpm_gpu_implicit_matvec", "mpm_gpu_implicit_solve", "mpm_gpu_p2g_noalloc"]
+           "mpm_gpu_implicit_matvec", "mpm_gpu_implicit_solve", "mpm_gpu_p2g_noalloc", "mpm_gpu_autotune",
+           "mpm_gpu_get_tuning"]
 
 
 def load(path: str | None = None):
@@ -98,6 +99,8 @@ def load(path: str | None = None):
     lib.mpm_gpu_sync.argtypes = [C.c_void_p]
     lib.mpm_gpu_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     lib.mpm_gpu_enable_kernel_timing.argtypes = [C.c_void_p, C.c_int]
+    lib.mpm_gpu_autotune.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    lib.mpm_gpu_get_tuning.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.mpm_gpu_implicit_setup.argtypes = [C.c_void_p, C.c_int, C.c_double]
     lib.mpm_gpu_implicit_step.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int,
                                           C.POINTER(SolveStats)]
@@ -229,6 +232,13 @@ class GpuSolid:
         st = Stats()
         _chk(self.lib.mpm_gpu_get_stats(self.ctx, C.byref(st)), "mpm_gpu_get_stats")
         return {k: getattr(st, k) for k, _ in Stats._fields_}
+
+    def autotune(self, steps_per_trial=5, facl=1.0):
+        """Runs 3 x steps_per_trial explicit steps and keeps the fastest launch variants."""
+        _chk(self.lib.mpm_gpu_autotune(self.ctx, steps_per_trial, facl), "mpm_gpu_autotune")
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        _chk(self.lib.mpm_gpu_get_tuning(self.ctx, C.byref(a), C.byref(b), C.byref(c)), "mpm_gpu_get_tuning")
+        return {"p2g_minb": a.value, "musl_minb": b.value, "update_ctas_per_sm": c.value}
 
     def enable_kernel_timing(self, on=True):
         _chk(self.lib.mpm_gpu_enable_kernel_timing(self.ctx, int(on)), "mpm_gpu_enable_kernel_timing")
