@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "mpm_device.cuh"
+#include "mpm_nn.cuh"
 
 namespace mpm {
 mpm_status run_p2g(mpm_ctx *c, double facl);
@@ -50,11 +51,17 @@ struct ImpState {
     int64_t num_alloc = 0;
     int64_t krylov_total = 0, newton_total = 0;
     double last_rel = 0.0;
+    // flexible CG with the learned preconditioner
+    mpm_nn *net = nullptr;
+    double *z = nullptr, *bs = nullptr;    // preconditioned residual, scaled RHS (3 * nodec)
+    double *xstar = nullptr, *ev = nullptr; // training-pair harvest: converged solution, error
+    int fallbacks = 0;                      // solves that switched from the network to Jacobi
+    int nn_applications = 0;
 };
 
 namespace mpm {
 
-enum Scal { S_RR0 = 0, S_RR1, S_PAP, S_RR_INIT, S_RES, S_IDOF, S_EU, S_GD, S_NSCAL };
+enum Scal { S_RR0 = 0, S_RR1, S_PAP, S_RR_INIT, S_RES, S_IDOF, S_EU, S_GD, S_ZQ, S_PR, S_RRC, S_NSCAL };
 
 struct ImpArgs {
     int nnc[3];
@@ -653,6 +660,130 @@ __global__ void k_imp_shift(ImpArgs a, PView P, const double *geup, const double
     for (int c = 0; c < 3; c++) P.x[c][p] += -b0 * geup[c * NP + p];
 }
 
+// ------------------------------------------------ flexible CG (Notay's FCG(1))
+// partial dot u.w over the 3 * nodec vector (node-blocked like the matvec)
+__global__ void k_dot3(ImpArgs a, const double *u, const double *w, double *part) {
+    __shared__ double sh[32];
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    double d = 0.0;
+    if (n < a.nodec) {
+        const size_t N = (size_t)a.nodec;
+        for (int c = 0; c < 3; c++) d += u[c * N + n] * w[c * N + n];
+    }
+    const double t = block_sum(d, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// p = z - (z.q_prev / p_prev.q_prev) p_prev (p = z on a restart); partial p.r
+__global__ void k_fcg_dir(ImpArgs a, const double *scal, int restart, const double *z, const double *r, double *p,
+                          double *part) {
+    __shared__ double sh[32];
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const double pq = scal[S_PAP];
+    const double beta = (restart || pq == 0.0) ? 0.0 : -scal[S_ZQ] / pq;
+    double d = 0.0;
+    if (n < a.nodec) {
+        const size_t N = (size_t)a.nodec;
+        for (int c = 0; c < 3; c++) {
+            const size_t i = c * N + n;
+            const double v = z[i] + beta * p[i];
+            p[i] = v;
+            d += v * r[i];
+        }
+    }
+    const double t = block_sum(d, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// alpha = p.r / p.q; x += alpha p; r -= alpha q; partial r.r
+__global__ void k_fcg_update(ImpArgs a, const double *scal, double *x, double *r, const double *p, const double *q,
+                             double *part) {
+    __shared__ double sh[32];
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const double pq = scal[S_PAP];
+    const double alpha = pq != 0.0 ? scal[S_PR] / pq : 0.0;
+    double d = 0.0;
+    if (n < a.nodec) {
+        const size_t N = (size_t)a.nodec;
+        for (int c = 0; c < 3; c++) {
+            const size_t i = c * N + n;
+            x[i] += alpha * p[i];
+            const double v = r[i] - alpha * q[i];
+            r[i] = v;
+            d += v * v;
+        }
+    }
+    const double t = block_sum(d, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// true residual r = bs - Ax (scaled system, BC rows already zero in Ax and bs); partial r.r
+__global__ void k_true_residual(ImpArgs a, const double *bs, const double *Ax, double *r, double *part) {
+    __shared__ double sh[32];
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    double d = 0.0;
+    if (n < a.nodec) {
+        const size_t N = (size_t)a.nodec;
+        for (int c = 0; c < 3; c++) {
+            const size_t i = c * N + n;
+            const double v = bs[i] - Ax[i];
+            r[i] = v;
+            d += v * v;
+        }
+    }
+    const double t = block_sum(d, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// e = xstar - x
+__global__ void k_sub3(const double *xstar, const double *x, double *e, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) e[i] = xstar[i] - x[i];
+}
+
+// seeded random right-hand side of the scaled system for training-pair
+// harvesting: a few random low-wavenumber cosine modes per component plus
+// white noise, zero on inactive and boundary rows
+__device__ __forceinline__ uint64_t hash64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double hash_unit(uint64_t k) { return ((hash64(k) >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+
+__global__ void k_random_rhs(ImpArgs a, const double *adiag, uint64_t seed, double smooth_amp, double noise_amp,
+                             double *bs) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.nodec) return;
+    int i, j, k;
+    node_ijk(n, a.nnc, i, j, k);
+    const size_t N = (size_t)a.nodec;
+    const unsigned char bf = a.bcflag[n];
+    for (int c = 0; c < 3; c++) {
+        double v = 0.0;
+        for (int m = 0; m < 4; m++) {
+            const uint64_t key = seed * 1315423911ull + (uint64_t)(c * 4 + m) * 97;
+            const double kx = 1.0 + floor(4.0 * hash_unit(key + 1)), ky = 1.0 + floor(4.0 * hash_unit(key + 2));
+            const double kz = 1.0 + floor(4.0 * hash_unit(key + 3));
+            const double ph = 6.283185307179586 * hash_unit(key + 4);
+            const double amp = 2.0 * hash_unit(key + 5) - 1.0;
+            v += amp * cos(3.141592653589793 * (kx * i / a.nnc[0] + ky * j / a.nnc[1] + kz * k / a.nnc[2]) + ph);
+        }
+        const uint64_t nk = seed * 2654435761ull + (uint64_t)n * 3 + c;
+        const double u1 = hash_unit(nk * 2 + 11), u2 = hash_unit(nk * 2 + 12);
+        const double g = sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+        const size_t idx = c * N + n;
+        const bool off = (bf & (1 << c)) || !(adiag[idx] >= a.mtol);
+        bs[idx] = off ? 0.0 : smooth_amp * v + noise_amp * g;
+    }
+}
+
+__global__ void k_set_modulus(double *matprop, int nmat, double E) {
+    const int m = threadIdx.x;
+    if (m < nmat) matprop[3 * m] = E;
+}
+
 __global__ void k_imp_reset_next(DevCtl *ctl, int parity) {
     for (int k = 0; k < B_NB; k++) ctl->nxt[parity ^ 1][k] = 0u;
 }
@@ -675,7 +806,8 @@ void implicit_free(mpm_ctx *c) {
     ImpState *s = c->imp;
     if (!s) return;
     double *bufs[] = {s->A, s->adiag, s->b, s->x, s->r, s->p, s->Ap, s->xs, s->ndispl, s->nvel, s->naccel,
-                      s->naccel_k, s->nmass, s->nvof, s->nei, s->stress_k, s->geup, s->part, s->scal};
+                      s->naccel_k, s->nmass, s->nvof, s->nei, s->stress_k, s->geup, s->part, s->scal,
+                      s->z, s->bs, s->xstar, s->ev};
     for (double *b : bufs)
         if (b) cudaFree(b);
     if (s->h_scal) cudaFreeHost(s->h_scal);
@@ -721,8 +853,8 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
     s->nb[5] = 1.0 / (2.0 * b) - 1.0;
     const size_t N = (size_t)c->g.nodec;
     CKI(cudaMalloc((void **)&s->A, sizeof(double) * 27 * 9 * N));
-    double **vec3[] = {&s->adiag, &s->b, &s->x, &s->r, &s->p, &s->Ap, &s->xs, &s->ndispl, &s->nvel, &s->naccel,
-                       &s->naccel_k};
+    double **vec3[] = {&s->adiag, &s->b,    &s->x,       &s->r, &s->p,  &s->Ap,    &s->xs, &s->ndispl,
+                       &s->nvel,  &s->naccel, &s->naccel_k, &s->z, &s->bs, &s->xstar, &s->ev};
     for (double **v : vec3) CKI(cudaMalloc((void **)v, sizeof(double) * 3 * N));
     CKI(cudaMalloc((void **)&s->nmass, sizeof(double) * N));
     CKI(cudaMalloc((void **)&s->nvof, sizeof(double) * N));
@@ -806,6 +938,93 @@ static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
     return check_launch(c);
 }
 
+// One solve of the assembled, scaled system by flexible CG with the learned
+// preconditioner z = net(r) (Notay's FCG(1): p = z - (z.q'/p'.q') p',
+// alpha = p.r / p.q).  The residual is checked every 8 iterations; when it
+// did not drop over a window the solve continues with the Jacobi
+// preconditioner (z = r in the scaled system).  Convergence is accepted only
+// on the true residual bs - A x, recomputed in FP64.
+static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
+    ImpState *s = c->imp;
+    ImpArgs a = imp_args(c);
+    const int nb = nb_nodes(c);
+    const size_t N = (size_t)c->g.nodec;
+    k_cg_scale_in<<<nb, 256, 0, c->stream>>>(a, s->x, s->b, s->adiag, s->xs, s->r);
+    CKI(cudaMemcpyAsync(s->bs, s->r, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, c->stream));
+    k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->xs, s->Ap, nullptr);
+    k_true_residual<<<nb, 256, 0, c->stream>>>(a, s->bs, s->Ap, s->r, s->part);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RR0);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
+    c->launches += 5;
+    CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, c->stream));
+    CKI(cudaStreamSynchronize(c->stream));
+    const double rr0 = s->h_scal[S_RR0];
+    int it = 0;
+    bool done = !(rr0 > 1.0e-300);
+    bool use_nn = s->net != nullptr;
+    int restart = 1;
+    double rr_window = rr0;
+    const int check = 8;
+    while (!done && it < kmax) {
+        if (use_nn) {
+            mpm_status st = mpm_nn_apply_precond(s->net, c->stream, s->r, s->scal + S_RRC, s->adiag, a.bcflag, a.mtol,
+                                                 s->z);
+            if (st != MPM_OK) return st;
+            s->nn_applications++;
+            c->launches += 9;
+        } else {
+            CKI(cudaMemcpyAsync(s->z, s->r, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, c->stream));
+        }
+        if (!restart) {
+            k_dot3<<<nb, 256, 0, c->stream>>>(a, s->z, s->Ap, s->part);
+            k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_ZQ);
+            c->launches += 2;
+        }
+        k_fcg_dir<<<nb, 256, 0, c->stream>>>(a, s->scal, restart, s->z, s->r, s->p, s->part);
+        k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_PR);
+        k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->p, s->Ap, s->part);
+        k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_PAP);
+        k_fcg_update<<<nb, 256, 0, c->stream>>>(a, s->scal, s->xs, s->r, s->p, s->Ap, s->part);
+        k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
+        c->launches += 6;
+        restart = 0;
+        it++;
+        if (it % check == 0 || it == kmax) {
+            CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, c->stream));
+            CKI(cudaStreamSynchronize(c->stream));
+            double rr = s->h_scal[S_RRC];
+            if (rr != rr) {
+                *iters = it;
+                return MPM_ERR_NONFINITE;
+            }
+            if (rr < eps * rr0) {
+                // confirm on the true residual
+                k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->xs, s->z, nullptr);
+                k_true_residual<<<nb, 256, 0, c->stream>>>(a, s->bs, s->z, s->r, s->part);
+                k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
+                c->launches += 3;
+                CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, c->stream));
+                CKI(cudaStreamSynchronize(c->stream));
+                rr = s->h_scal[S_RRC];
+                if (rr < eps * rr0) done = true;
+                else restart = 1;
+            }
+            if (!done && use_nn && !(rr < rr_window)) {
+                use_nn = false;   // the network stopped reducing the residual
+                restart = 1;
+                s->fallbacks++;
+            }
+            rr_window = rr;
+            s->last_rel = sqrt(rr / rr0);
+        }
+    }
+    k_cg_scale_out<<<(3 * c->g.nodec + 255) / 256, 256, 0, c->stream>>>(a, s->xs, s->adiag, s->x);
+    c->launches++;
+    *iters = it;
+    if (!done) return MPM_ERR_KRYLOV_MAXIT;
+    return check_launch(c);
+}
+
 static mpm_status imp_assemble(mpm_ctx *c) {
     ImpState *s = c->imp;
     ImpArgs a = imp_args(c);
@@ -866,7 +1085,7 @@ static mpm_status imp_newton(mpm_ctx *c, double eps, int kmax, int *krylov, int 
         st = imp_assemble(c);
         if (st != MPM_OK) return st;
         int k = 0;
-        st = imp_cg(c, eps, kmax, &k);
+        st = s->net ? imp_fcg(c, eps, kmax, &k) : imp_cg(c, eps, kmax, &k);
         ktot += k;
         if (st != MPM_OK) break;
         k_add<<<(3 * c->g.nodec + 255) / 256, 256, 0, c->stream>>>(s->ndispl, s->x, 3 * c->g.nodec);
@@ -916,6 +1135,7 @@ mpm_status mpm_gpu_implicit_step(mpm_ctx *c, int nsteps, double facl, double eps
     mpm_status st = ensure_particle_scratch(c);
     if (st != MPM_OK) return st;
     int kt = 0, nt = 0;
+    const int fb0 = c->imp->fallbacks, na0 = c->imp->nn_applications;
     for (int i = 0; i < nsteps; i++) {
         st = imp_p2g(c, facl);
         if (st != MPM_OK) break;
@@ -935,6 +1155,8 @@ mpm_status mpm_gpu_implicit_step(mpm_ctx *c, int nsteps, double facl, double eps
         stats->krylov_iters = kt;
         stats->newton_iters = nt;
         stats->last_rel_residual = c->imp->last_rel;
+        stats->precond_fallbacks = c->imp->fallbacks - fb0;
+        stats->nn_applications = c->imp->nn_applications - na0;
     }
     if (st != MPM_OK) return st;
     CKI(cudaStreamSynchronize(c->stream));
@@ -997,8 +1219,106 @@ mpm_status mpm_gpu_implicit_solve(mpm_ctx *c, double eps, int kmax, double *x, i
     const size_t N = (size_t)c->g.nodec;
     CKI(cudaMemsetAsync(s->x, 0, sizeof(double) * 3 * N, c->stream));
     int it = 0;
-    mpm_status st = imp_cg(c, eps, kmax, &it);
+    mpm_status st = s->net ? imp_fcg(c, eps, kmax, &it) : imp_cg(c, eps, kmax, &it);
     if (iters) *iters = it;
     if (x) CKI(cudaMemcpy(x, s->x, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost));
     return st;
+}
+
+// ------------------------------------------------ learned preconditioner hooks
+mpm_status mpm_gpu_implicit_set_precond(mpm_ctx *c, mpm_nn *net) {
+    if (!c || !c->imp) return MPM_ERR_BAD_ARG;
+    if (net && !mpm_nn_grid_matches(net, c->g.nnc)) return MPM_ERR_BAD_ARG;
+    c->imp->net = net;
+    return MPM_OK;
+}
+
+// CG on the scaled system from x = 0 with right-hand side s->bs.  With a
+// network, every `stride`-th iterate appends the pair (r_k, xstar - x_k).
+static mpm_status cg_scaled(mpm_ctx *c, double eps, int kmax, mpm_nn *net, int stride, int max_pairs, int *iters) {
+    ImpState *s = c->imp;
+    ImpArgs a = imp_args(c);
+    const int nb = nb_nodes(c);
+    const size_t N = (size_t)c->g.nodec;
+    CKI(cudaMemsetAsync(s->xs, 0, sizeof(double) * 3 * N, c->stream));
+    CKI(cudaMemsetAsync(s->Ap, 0, sizeof(double) * 3 * N, c->stream));
+    CKI(cudaMemcpyAsync(s->r, s->bs, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, c->stream));
+    k_cg_init<<<nb, 256, 0, c->stream>>>(a, s->Ap, s->r, s->p, s->part);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RR0);
+    CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, c->stream));
+    CKI(cudaStreamSynchronize(c->stream));
+    const double rr0 = s->h_scal[S_RR0];
+    int it = 0, pairs = 0;
+    bool done = !(rr0 > 1.0e-300);
+    while (!done && it < kmax) {
+        const int cur = (it & 1) ? S_RR1 : S_RR0;
+        if (net && it % stride == 0 && pairs < max_pairs) {
+            k_sub3<<<(3 * c->g.nodec + 255) / 256, 256, 0, c->stream>>>(s->xstar, s->xs, s->ev, 3 * c->g.nodec);
+            mpm_status st = mpm_nn_append_pair(net, c->stream, s->r, s->scal + cur, s->ev);
+            if (st != MPM_OK) return st;
+            pairs++;
+        }
+        k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->p, s->Ap, s->part);
+        k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_PAP);
+        k_cg_update<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->xs, s->r, s->p, s->Ap, s->part);
+        k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, cur ^ 1);
+        k_cg_dir<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->r, s->p);
+        it++;
+        if (it % 8 == 0 || it == kmax) {
+            CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream));
+            CKI(cudaStreamSynchronize(c->stream));
+            const double rr = s->h_scal[(it & 1) ? S_RR1 : S_RR0];
+            if (rr != rr) return MPM_ERR_NONFINITE;
+            if (rr < eps * rr0) done = true;
+        }
+    }
+    *iters = it;
+    return check_launch(c);
+}
+
+mpm_status mpm_gpu_implicit_harvest(mpm_ctx *c, mpm_nn *net, int nsystems, int loads_per_system, int pairs_per_load,
+                                    double e_min, double e_max, uint64_t seed, double eps, int kmax) {
+    if (!c || !c->imp || !net || nsystems < 1 || loads_per_system < 1 || pairs_per_load < 1 || !(e_min > 0.0) ||
+        !(e_max >= e_min) || !(eps > 0.0) || kmax < 1)
+        return MPM_ERR_BAD_ARG;
+    if (!mpm_nn_grid_matches(net, c->g.nnc)) return MPM_ERR_BAD_ARG;
+    if (c->num == 0) return MPM_ERR_STATE;
+    ImpState *s = c->imp;
+    ImpArgs a = imp_args(c);
+    const int nb = nb_nodes(c);
+    const size_t N = (size_t)c->g.nodec;
+    std::vector<double> saved(3 * (size_t)c->nmat);
+    CKI(cudaMemcpy(saved.data(), c->d_matprop, sizeof(double) * saved.size(), cudaMemcpyDeviceToHost));
+    mpm_status st = MPM_OK;
+    uint64_t z = seed;
+    auto next_unit = [&z]() {
+        z += 0x9E3779B97F4A7C15ull;
+        uint64_t t = z;
+        t = (t ^ (t >> 30)) * 0xBF58476D1CE4E5B9ull;
+        t = (t ^ (t >> 27)) * 0x94D049BB133111EBull;
+        t ^= t >> 31;
+        return ((t >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    };
+    for (int sys = 0; sys < nsystems && st == MPM_OK; sys++) {
+        const double E = exp(log(e_min) + next_unit() * (log(e_max) - log(e_min)));
+        k_set_modulus<<<1, 32, 0, c->stream>>>(c->d_matprop, c->nmat, E);
+        st = mpm_gpu_implicit_assemble(c, 1.0);
+        for (int ld = 0; ld < loads_per_system && st == MPM_OK; ld++) {
+            const uint64_t key = seed * 1000003ull + (uint64_t)sys * 1009ull + (uint64_t)ld;
+            // alternate smooth-dominated and noise-dominated loads
+            const double smooth = (ld & 1) ? 0.2 : 1.0, noise = (ld & 1) ? 1.0 : 0.2;
+            k_random_rhs<<<nb, 256, 0, c->stream>>>(a, s->adiag, key, smooth, noise, s->bs);
+            int K = 0;
+            st = cg_scaled(c, eps, kmax, nullptr, 1, 0, &K);
+            if (st != MPM_OK) break;
+            CKI(cudaMemcpyAsync(s->xstar, s->xs, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, c->stream));
+            const int stride = K / pairs_per_load > 1 ? K / pairs_per_load : 1;
+            int K2 = 0;
+            st = cg_scaled(c, eps, K, net, stride, pairs_per_load, &K2);
+        }
+    }
+    cudaMemcpy(c->d_matprop, saved.data(), sizeof(double) * saved.size(), cudaMemcpyHostToDevice);
+    if (st != MPM_OK) return st;
+    CKI(cudaStreamSynchronize(c->stream));
+    return check_launch(c);
 }

@@ -1,0 +1,1179 @@
+// Learned preconditioner network: forward, backward (data and weight
+// gradients) and Adam training, with the 3x3x3 convolutions on tcgen05
+// tensor cores (BF16 operands, FP32 accumulators in tensor memory).
+//
+// No counterpart in the reference: HPC-MPM-Code solves its linear systems
+// with GPBiCGSafe or PETSc (module/solver/solver.cpp:19-141,
+// module/solver/crsmat.cpp:338-686).  The network is the right
+// preconditioner of the flexible conjugate gradient solver in
+// mpm_implicit.cu.
+//
+// Convolution as implicit GEMM: a CTA owns 128 output nodes (one TMEM lane
+// each); for every one of the 27 taps its 128 threads gather the tap's input
+// rows (channels-last, 16-byte vectors) into a K-major shared-memory tile
+// while the tensor core multiplies the previous tap's tile by that tap's
+// weights (all 27 weight tiles stay in shared memory).  Two tile buffers, an
+// mbarrier per buffer completed by tcgen05.commit.  The weight gradient
+// dW[t][ci][co] = sum_v x[gather(v, t)][ci] g[v][co] runs as a GEMM with the
+// (tap, ci) pairs as M (128 per MMA), the output channels as N and the nodes
+// as K: the gathered input is written transposed into shared memory.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "mpm_nn.cuh"
+#include "mpm_tc.cuh"
+
+typedef __nv_bfloat16 bf16;
+
+using namespace mpm;
+using namespace mpm::nn;
+
+#define CKN(call)                                                                                                      \
+    do {                                                                                                               \
+        cudaError_t _e = (call);                                                                                       \
+        if (_e != cudaSuccess) {                                                                                       \
+            fprintf(stderr, "mpm_gb300 (nn): %s failed: %s\n", #call, cudaGetErrorString(_e));                         \
+            return _e == cudaErrorMemoryAllocation ? MPM_ERR_OOM : MPM_ERR_CUDA;                                       \
+        }                                                                                                              \
+    } while (0)
+
+namespace mpm {
+namespace nn {
+
+int64_t w_offset(int l) {
+    int64_t o = 0;
+    for (int i = 0; i < l; i++) o += 27LL * CIN[i] * COUT[i] + COUT[i];
+    return o;
+}
+int64_t b_offset(int l) { return w_offset(l) + 27LL * CIN[l] * COUT[l]; }
+int64_t w5_offset() { return w_offset(NCONV); }
+int64_t b5_offset() { return w5_offset() + 48; }
+int64_t param_count() { return b5_offset() + 3; }
+
+enum Mode { S1 = 0, S2 = 1, S1T = 2, S2T = 3 };
+constexpr unsigned TC_WAIT = 1u << 22;   // try_wait polls before a wait gives up
+
+struct Lvl {
+    int n[3];
+    int64_t v;
+};
+
+// Source row of output node (b, o) for tap t, or -1 (zero padding).
+template <int MODE>
+__device__ __forceinline__ int64_t gather_src(int b, int ox, int oy, int oz, int t, const Lvl &in) {
+    const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
+    int ix, iy, iz;
+    if (MODE == S1) {
+        ix = ox + dx;
+        iy = oy + dy;
+        iz = oz + dz;
+    } else if (MODE == S2) {
+        ix = 2 * ox + dx;
+        iy = 2 * oy + dy;
+        iz = 2 * oz + dz;
+    } else if (MODE == S1T) {
+        ix = ox - dx;
+        iy = oy - dy;
+        iz = oz - dz;
+    } else {
+        const int tx = ox - dx, ty = oy - dy, tz = oz - dz;
+        if ((tx | ty | tz) & 1) return -1;
+        ix = tx >> 1;
+        iy = ty >> 1;
+        iz = tz >> 1;
+    }
+    if (ix < 0 || iy < 0 || iz < 0 || ix >= in.n[0] || iy >= in.n[1] || iz >= in.n[2]) return -1;
+    return (int64_t)b * in.v + ix + (int64_t)in.n[0] * (iy + (int64_t)in.n[1] * iz);
+}
+
+__device__ __forceinline__ void row_coords(int64_t row, const Lvl &L, int &b, int &x, int &y, int &z) {
+    b = (int)(row / L.v);
+    const int64_t v = row - (int64_t)b * L.v;
+    x = (int)(v % L.n[0]);
+    const int64_t q = v / L.n[0];
+    y = (int)(q % L.n[1]);
+    z = (int)(q / L.n[1]);
+}
+
+__device__ __forceinline__ void unpack8(const uint4 &u, float *f) {
+    const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float2 t = __bfloat1622float2(h[i]);
+        f[2 * i] = t.x;
+        f[2 * i + 1] = t.y;
+    }
+}
+
+__device__ __forceinline__ uint4 pack8(const float *f) {
+    uint4 u;
+    __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&u);
+#pragma unroll
+    for (int i = 0; i < 4; i++) h[i] = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+    return u;
+}
+
+// ------------------------------------------------------------------ conv
+struct ConvArgs {
+    const bf16 *in;     // [rows_in][K]
+    bf16 *out;          // [rows][N]
+    const bf16 *w;      // 27 canonical N x K tiles
+    const float *bias;  // [N] or null
+    const bf16 *add;    // [rows][N] or null: added before the activation
+    const bf16 *mask;   // [rows][N] or null: output zeroed where mask <= 0
+    int relu;
+    Lvl lin, lout;
+    int64_t rows;       // batch * lout.v
+    int *err;
+};
+
+template <int K, int N>
+constexpr size_t conv_smem() {
+    return 27u * N * K * 2 + 2u * 128 * K * 2;
+}
+
+template <int K, int N, int MODE>
+__global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a) {
+    constexpr uint32_t WT = (uint32_t)N * K * 2;        // one tap's weight tile
+    constexpr uint32_t WB = 27u * WT;
+    constexpr uint32_t AB = 128u * K * 2;               // one A stage
+    constexpr uint32_t TCOLS = N < 32 ? 32 : N;
+    constexpr uint32_t IDESC = tc::idesc_bf16(128, N);
+    constexpr uint32_t SBO = K * 16;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ unsigned long long bar[2];
+    __shared__ uint32_t tslot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) tc::tmem_alloc(&tslot, TCOLS);
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    {
+        const uint4 *src = reinterpret_cast<const uint4 *>(a.w);
+        uint4 *dst = reinterpret_cast<uint4 *>(smem);
+        for (uint32_t i = tid; i < WB / 16; i += 128) dst[i] = __ldg(src + i);
+    }
+    tc::fence_async_smem();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t taddr = tslot;
+    const uint32_t sw = smem_addr(smem), sa = sw + WB;
+    unsigned char *pa = smem + WB;
+    const int64_t ntile = (a.rows + 127) / 128;
+    uint32_t it = 0;
+    bool ok = true;
+    for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+        const int64_t row = tile * 128 + tid;
+        const bool valid = row < a.rows;
+        int b = 0, ox = 0, oy = 0, oz = 0;
+        if (valid) row_coords(row, a.lout, b, ox, oy, oz);
+        for (int t = 0; t < 27; t++) {
+            const uint32_t s = it & 1;
+            bool mine = true;
+            if (it >= 2) mine = mbar_wait_bounded(&bar[s], ((it >> 1) - 1) & 1, TC_WAIT);
+            const int64_t src = valid ? gather_src<MODE>(b, ox, oy, oz, t, a.lin) : -1;
+            uint4 *dst = reinterpret_cast<uint4 *>(pa + s * AB + (tid >> 3) * SBO + (tid & 7) * 16);
+            const uint4 *in = reinterpret_cast<const uint4 *>(a.in + (src >= 0 ? src : 0) * K);
+#pragma unroll
+            for (int kc = 0; kc < K / 8; kc++) {
+                uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                if (src >= 0) v = __ldg(in + kc);
+                dst[kc * 8] = v;
+            }
+            tc::fence_async_smem();
+            tc::fence_before();
+            if (!__syncthreads_and(mine)) {
+                ok = false;
+                break;
+            }
+            if (tid == 0) {
+                tc::fence_after();
+#pragma unroll
+                for (int kk = 0; kk < K / 16; kk++) {
+                    const uint64_t ad = tc::sdesc(sa + s * AB + kk * 256, 128, SBO);
+                    const uint64_t bd = tc::sdesc(sw + t * WT + kk * 256, 128, SBO);
+                    tc::mma_bf16(taddr, ad, bd, IDESC, (t | kk) != 0);
+                }
+                tc::mma_commit(&bar[s]);
+            }
+            it++;
+        }
+        if (!ok) break;
+        const bool done = mbar_wait_bounded(&bar[(it - 1) & 1], ((it - 1) >> 1) & 1, TC_WAIT);
+        if (!__syncthreads_and(done)) {
+            ok = false;
+            break;
+        }
+        tc::fence_after();
+        float acc[N];
+#pragma unroll
+        for (int c = 0; c < N / 16; c++) tc::tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + c * 16, acc + c * 16);
+        if (valid) {
+            if (a.bias) {
+#pragma unroll
+                for (int c = 0; c < N; c++) acc[c] += __ldg(a.bias + c);
+            }
+            if (a.add) {
+                const uint4 *ap = reinterpret_cast<const uint4 *>(a.add + row * N);
+#pragma unroll
+                for (int c = 0; c < N / 8; c++) {
+                    float f[8];
+                    unpack8(__ldg(ap + c), f);
+#pragma unroll
+                    for (int i = 0; i < 8; i++) acc[c * 8 + i] += f[i];
+                }
+            }
+            if (a.relu) {
+#pragma unroll
+                for (int c = 0; c < N; c++) acc[c] = fmaxf(acc[c], 0.0f);
+            }
+            if (a.mask) {
+                const uint4 *mp = reinterpret_cast<const uint4 *>(a.mask + row * N);
+#pragma unroll
+                for (int c = 0; c < N / 8; c++) {
+                    float f[8];
+                    unpack8(__ldg(mp + c), f);
+#pragma unroll
+                    for (int i = 0; i < 8; i++)
+                        if (!(f[i] > 0.0f)) acc[c * 8 + i] = 0.0f;
+                }
+            }
+            uint4 *op = reinterpret_cast<uint4 *>(a.out + row * N);
+#pragma unroll
+            for (int c = 0; c < N / 8; c++) op[c] = pack8(acc + c * 8);
+        }
+        tc::fence_before();
+        __syncthreads();
+    }
+    if (!ok) {
+        if (tid == 0) atomicAdd(a.err, 1);
+        if (it > 0) mbar_wait_bounded(&bar[(it - 1) & 1], ((it - 1) >> 1) & 1, TC_WAIT);
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 0) tc::tmem_dealloc(taddr, TCOLS);
+}
+
+// --------------------------------------------------------- weight gradient
+struct DwArgs {
+    const bf16 *in;   // [rows_in][CIN]
+    const bf16 *g;    // [rows][COUT], gradient of the conv's pre-activation output
+    float *part;      // [gridDim.x][27 * CIN * COUT]
+    Lvl lin, lout;
+    int64_t rows;
+    int *err;
+};
+
+constexpr int DW_KV = 32;   // nodes per MMA chunk (GEMM K)
+
+__host__ __device__ constexpr uint32_t pow2_cols(uint32_t c) {
+    return c <= 32 ? 32 : c <= 64 ? 64 : c <= 128 ? 128 : c <= 256 ? 256 : 512;
+}
+
+template <int CIN_, int COUT_>
+constexpr size_t dw_smem() {
+    return (size_t)((27 + 128 / CIN_ - 1) / (128 / CIN_)) * 128 * DW_KV * 2 + (size_t)COUT_ * DW_KV * 2;
+}
+
+template <int CI, int CO, int MODE>
+__global__ void __launch_bounds__(128) k_conv_dw_tc(DwArgs a) {
+    constexpr int KV = DW_KV;
+    constexpr int TPM = 128 / CI;                    // taps per M tile
+    constexpr int NMT = (27 + TPM - 1) / TPM;        // M tiles
+    constexpr uint32_t MTB = 128u * KV * 2;          // bytes of one M tile
+    constexpr uint32_t AB = NMT * MTB;
+    constexpr uint32_t BB = (uint32_t)CO * KV * 2;
+    constexpr uint32_t TCOLS = pow2_cols(NMT * CO);
+    constexpr uint32_t SBO = KV * 16;
+    constexpr uint32_t IDESC = tc::idesc_bf16(128, CO);
+    static_assert(NMT * CO <= 512, "tensor memory");
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ unsigned long long bar;
+    __shared__ uint32_t tslot;
+    __shared__ int rb[KV], rx[KV], ry[KV], rz[KV];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) tc::tmem_alloc(&tslot, TCOLS);
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    for (uint32_t i = tid; i < (AB + BB) / 16; i += 128) reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t taddr = tslot;
+    const uint32_t sa = smem_addr(smem), sb = sa + AB;
+    unsigned char *pb = smem + AB;
+    const int64_t nchunk = (a.rows + KV - 1) / KV;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int64_t ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
+        bool mine = true;
+        if (phase > 0) mine = mbar_wait_bounded(&bar, (phase - 1) & 1, TC_WAIT);
+        if (!__syncthreads_and(mine)) {
+            ok = false;
+            break;
+        }
+        if (tid < KV) {
+            const int64_t row = ch * KV + tid;
+            if (row < a.rows) {
+                int b, x, y, z;
+                row_coords(row, a.lout, b, x, y, z);
+                rb[tid] = b;
+                rx[tid] = x;
+                ry[tid] = y;
+                rz[tid] = z;
+            } else {
+                rb[tid] = -1;
+            }
+        }
+        __syncthreads();
+        // B = g^T: CO rows x KV nodes
+        for (int item = tid; item < KV * (CO / 8); item += 128) {
+            const int j = item / (CO / 8), cc = item % (CO / 8);
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (rb[j] >= 0) v = __ldg(reinterpret_cast<const uint4 *>(a.g + (ch * KV + j) * CO) + cc);
+            const unsigned short *h = reinterpret_cast<const unsigned short *>(&v);
+#pragma unroll
+            for (int e = 0; e < 8; e++)
+                *reinterpret_cast<unsigned short *>(pb + tc::kmaj_off(cc * 8 + e, j, KV)) = h[e];
+        }
+        // A = gathered input^T: (tap, ci) rows x KV nodes, NMT tiles of 128 rows
+        for (int item = tid; item < 27 * KV * (CI / 8); item += 128) {
+            const int cc = item % (CI / 8);
+            const int rest = item / (CI / 8);
+            const int j = rest % KV, t = rest / KV;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (rb[j] >= 0) {
+                const int64_t src = gather_src<MODE>(rb[j], rx[j], ry[j], rz[j], t, a.lin);
+                if (src >= 0) v = __ldg(reinterpret_cast<const uint4 *>(a.in + src * CI) + cc);
+            }
+            const int m = t / TPM, r0 = (t % TPM) * CI + cc * 8;
+            unsigned char *tileb = smem + m * MTB;
+            const unsigned short *h = reinterpret_cast<const unsigned short *>(&v);
+#pragma unroll
+            for (int e = 0; e < 8; e++)
+                *reinterpret_cast<unsigned short *>(tileb + tc::kmaj_off(r0 + e, j, KV)) = h[e];
+        }
+        tc::fence_async_smem();
+        tc::fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after();
+            for (int m = 0; m < NMT; m++) {
+#pragma unroll
+                for (int kk = 0; kk < KV / 16; kk++) {
+                    const uint64_t ad = tc::sdesc(sa + m * MTB + kk * 256, 128, SBO);
+                    const uint64_t bd = tc::sdesc(sb + kk * 256, 128, SBO);
+                    tc::mma_bf16(taddr + m * CO, ad, bd, IDESC, (phase > 0 || kk > 0) ? 1u : 0u);
+                }
+            }
+            tc::mma_commit(&bar);
+        }
+        phase++;
+    }
+    bool done = true;
+    if (phase > 0) done = mbar_wait_bounded(&bar, (phase - 1) & 1, TC_WAIT);
+    if (!__syncthreads_and(done)) ok = false;
+    tc::fence_after();
+    float *dst = a.part + (size_t)blockIdx.x * (27 * CI * CO);
+    for (int m = 0; m < NMT; m++) {
+        float v[CO];
+#pragma unroll
+        for (int c = 0; c < CO / 16; c++)
+            tc::tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + m * CO + c * 16, v + c * 16);
+        const int t = m * TPM + tid / CI, ci = tid % CI;
+        if (t < 27) {
+#pragma unroll
+            for (int c = 0; c < CO; c++) dst[(t * CI + ci) * CO + c] = (phase > 0 && ok) ? v[c] : 0.0f;
+        }
+    }
+    if (!ok && tid == 0) atomicAdd(a.err, 1);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 0) tc::tmem_dealloc(taddr, TCOLS);
+}
+
+// sum of per-CTA partials (fixed order) into the FP32 gradient, dropping padded input channels
+__global__ void k_dw_reduce(const float *part, int nblk, int ci_pad, int ci, int co, float *grad) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 27 * ci * co) return;
+    const int c = idx % co, rest = idx / co;
+    const int i = rest % ci, t = rest / ci;
+    const size_t src = ((size_t)t * ci_pad + i) * co + c;
+    const size_t stride = (size_t)27 * ci_pad * co;
+    float s = 0.0f;
+    for (int b = 0; b < nblk; b++) s += part[b * stride + src];
+    grad[idx] = s;
+}
+
+// ----------------------------------------------------- CUDA-core layers
+// x0 = [in(3), 0 x 13] (host-style FP32 input [rows][3])
+__global__ void k_input_f32(const float *in, bf16 *x0, int64_t rows) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    float f[8] = {in[3 * r], in[3 * r + 1], in[3 * r + 2], 0, 0, 0, 0, 0};
+    uint4 *o = reinterpret_cast<uint4 *>(x0 + r * 16);
+    o[0] = pack8(f);
+    o[1] = make_uint4(0, 0, 0, 0);
+}
+
+// x0 from an FP64 component-major residual, scaled by 1 / sqrt(rr / (3 nodec))
+__global__ void k_input_r(const double *r, const double *rr, int64_t nodec, bf16 *x0) {
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nodec) return;
+    const double ms = rr[0] / (3.0 * (double)nodec);
+    const double inv = ms > 0.0 ? 1.0 / sqrt(ms) : 0.0;
+    float f[8] = {(float)(r[n] * inv), (float)(r[nodec + n] * inv), (float)(r[2 * nodec + n] * inv), 0, 0, 0, 0, 0};
+    uint4 *o = reinterpret_cast<uint4 *>(x0 + n * 16);
+    o[0] = pack8(f);
+    o[1] = make_uint4(0, 0, 0, 0);
+}
+
+// out = relu(up(coarse) + skip), C channels, one thread per (fine row, 8 channels)
+template <int C>
+__global__ void k_up_add_relu(const bf16 *coarse, const bf16 *skip, bf16 *out, Lvl lf, Lvl lc, int64_t rows) {
+    const int64_t item = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (item >= rows * (C / 8)) return;
+    const int64_t row = item / (C / 8);
+    const int cc = (int)(item % (C / 8));
+    int b, x, y, z;
+    row_coords(row, lf, b, x, y, z);
+    float acc[8];
+    unpack8(__ldg(reinterpret_cast<const uint4 *>(skip + row * C) + cc), acc);
+    const int p[3] = {x, y, z};
+    int lo[3], nn[3];
+    for (int d = 0; d < 3; d++) {
+        lo[d] = p[d] >> 1;
+        nn[d] = (p[d] & 1) ? 2 : 1;
+    }
+    for (int k = 0; k < nn[2]; k++)
+        for (int j = 0; j < nn[1]; j++)
+            for (int i = 0; i < nn[0]; i++) {
+                const float w = (nn[0] == 2 ? 0.5f : 1.0f) * (nn[1] == 2 ? 0.5f : 1.0f) * (nn[2] == 2 ? 0.5f : 1.0f);
+                const int64_t src =
+                    (int64_t)b * lc.v + (lo[0] + i) + (int64_t)lc.n[0] * ((lo[1] + j) + (int64_t)lc.n[1] * (lo[2] + k));
+                float f[8];
+                unpack8(__ldg(reinterpret_cast<const uint4 *>(coarse + src * C) + cc), f);
+#pragma unroll
+                for (int e = 0; e < 8; e++) acc[e] += w * f[e];
+            }
+#pragma unroll
+    for (int e = 0; e < 8; e++) acc[e] = fmaxf(acc[e], 0.0f);
+    reinterpret_cast<uint4 *>(out + row * C)[cc] = pack8(acc);
+}
+
+// gc = up^T(gf): coarse node I collects fine nodes 2I + d, d in {-1,0,1}^3,
+// weight 1 (d = 0) or 1/2 per axis
+template <int C>
+__global__ void k_restrict(const bf16 *gf, bf16 *gc, Lvl lf, Lvl lc, int64_t rows_c) {
+    const int64_t item = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (item >= rows_c * (C / 8)) return;
+    const int64_t row = item / (C / 8);
+    const int cc = (int)(item % (C / 8));
+    int b, x, y, z;
+    row_coords(row, lc, b, x, y, z);
+    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int dz = -1; dz <= 1; dz++) {
+        const int fz = 2 * z + dz;
+        if (fz < 0 || fz >= lf.n[2]) continue;
+        for (int dy = -1; dy <= 1; dy++) {
+            const int fy = 2 * y + dy;
+            if (fy < 0 || fy >= lf.n[1]) continue;
+            for (int dx = -1; dx <= 1; dx++) {
+                const int fx = 2 * x + dx;
+                if (fx < 0 || fx >= lf.n[0]) continue;
+                const float w = (dx ? 0.5f : 1.0f) * (dy ? 0.5f : 1.0f) * (dz ? 0.5f : 1.0f);
+                const int64_t src = (int64_t)b * lf.v + fx + (int64_t)lf.n[0] * (fy + (int64_t)lf.n[1] * fz);
+                float f[8];
+                unpack8(__ldg(reinterpret_cast<const uint4 *>(gf + src * C) + cc), f);
+#pragma unroll
+                for (int e = 0; e < 8; e++) acc[e] += w * f[e];
+            }
+        }
+    }
+    reinterpret_cast<uint4 *>(gc + row * C)[cc] = pack8(acc);
+}
+
+// z = d0 W5 + b5 (FP32 [rows][3])
+__global__ void k_output(const bf16 *d0, const float *w5, const float *b5, float *z, int64_t rows) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    float f[16];
+    const uint4 *p = reinterpret_cast<const uint4 *>(d0 + r * 16);
+    unpack8(p[0], f);
+    unpack8(p[1], f + 8);
+    for (int c = 0; c < 3; c++) {
+        float s = b5[c];
+#pragma unroll
+        for (int k = 0; k < 16; k++) s += f[k] * w5[k * 3 + c];
+        z[3 * r + c] = s;
+    }
+}
+
+// preconditioner output: z (FP64 component-major) = s * (d0 W5 + b5), zero on
+// inactive and boundary rows
+__global__ void k_output_precond(const bf16 *d0, const float *w5, const float *b5, const double *rr, int64_t nodec,
+                                 const double *adiag, const unsigned char *bcflag, double mtol, double *z) {
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nodec) return;
+    const double ms = rr[0] / (3.0 * (double)nodec);
+    const double s = ms > 0.0 ? sqrt(ms) : 0.0;
+    float f[16];
+    const uint4 *p = reinterpret_cast<const uint4 *>(d0 + n * 16);
+    unpack8(p[0], f);
+    unpack8(p[1], f + 8);
+    const unsigned char bf = bcflag[n];
+    for (int c = 0; c < 3; c++) {
+        float o = b5[c];
+#pragma unroll
+        for (int k = 0; k < 16; k++) o += f[k] * w5[k * 3 + c];
+        const int64_t i = c * nodec + n;
+        const bool off = (bf & (1 << c)) || !(adiag[i] >= mtol);
+        z[i] = off ? 0.0 : s * (double)o;
+    }
+}
+
+constexpr int RED_THREADS = 256;
+
+// gd0 = (gz W5^T) masked by d0 > 0; per-block partials of dW5 (48) and db5 (3)
+__global__ void __launch_bounds__(RED_THREADS) k_output_bwd(const float *gz, const bf16 *d0, const float *w5,
+                                                            bf16 *gd0, float *part, int64_t rows) {
+    __shared__ float sh[RED_THREADS / 32][51];
+    float acc[51];
+    for (int i = 0; i < 51; i++) acc[i] = 0.0f;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
+        float f[16];
+        const uint4 *p = reinterpret_cast<const uint4 *>(d0 + r * 16);
+        unpack8(p[0], f);
+        unpack8(p[1], f + 8);
+        const float g0 = gz[3 * r], g1 = gz[3 * r + 1], g2 = gz[3 * r + 2];
+        float o[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            const float v = g0 * w5[k * 3] + g1 * w5[k * 3 + 1] + g2 * w5[k * 3 + 2];
+            o[k] = f[k] > 0.0f ? v : 0.0f;
+            acc[k * 3] += f[k] * g0;
+            acc[k * 3 + 1] += f[k] * g1;
+            acc[k * 3 + 2] += f[k] * g2;
+        }
+        acc[48] += g0;
+        acc[49] += g1;
+        acc[50] += g2;
+        uint4 *q = reinterpret_cast<uint4 *>(gd0 + r * 16);
+        q[0] = pack8(o);
+        q[1] = pack8(o + 8);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int i = 0; i < 51; i++) {
+        float v = acc[i];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[wid][i] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 51) {
+        float s = 0.0f;
+        for (int w = 0; w < RED_THREADS / 32; w++) s += sh[w][threadIdx.x];
+        part[(size_t)blockIdx.x * 51 + threadIdx.x] = s;
+    }
+}
+
+// per-block channel sums of g [rows][C] (bias gradients)
+template <int C>
+__global__ void __launch_bounds__(RED_THREADS) k_chan_sum(const bf16 *g, float *part, int64_t rows) {
+    __shared__ float sh[RED_THREADS / 32][C];
+    float acc[C];
+    for (int i = 0; i < C; i++) acc[i] = 0.0f;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(g + r * C);
+#pragma unroll
+        for (int c = 0; c < C / 8; c++) {
+            float f[8];
+            unpack8(p[c], f);
+#pragma unroll
+            for (int e = 0; e < 8; e++) acc[c * 8 + e] += f[e];
+        }
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int i = 0; i < C; i++) {
+        float v = acc[i];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[wid][i] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < C) {
+        float s = 0.0f;
+        for (int w = 0; w < RED_THREADS / 32; w++) s += sh[w][threadIdx.x];
+        part[(size_t)blockIdx.x * C + threadIdx.x] = s;
+    }
+}
+
+__global__ void k_part_reduce(const float *part, int nblk, int n, float *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s = 0.0f;
+    for (int b = 0; b < nblk; b++) s += part[(size_t)b * n + i];
+    out[i] = s;
+}
+
+// canonical BF16 weight tiles of conv l from the FP32 parameters:
+// forward: per tap an N = cout x K = kpad tile of W[t][ci][co];
+// transposed (data gradient): per tap an N = cin x K = cout tile.
+__global__ void k_wprep(const float *w, int cin, int cout, int kpad, bf16 *fwd, bf16 *trn) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < 27 * cout * kpad) {
+        const int k = idx % kpad, rest = idx / kpad;
+        const int n = rest % cout, t = rest / cout;
+        const float v = k < cin ? w[((size_t)t * cin + k) * cout + n] : 0.0f;
+        const uint32_t off = t * (uint32_t)(cout * kpad * 2) + tc::kmaj_off(n, k, kpad);
+        *reinterpret_cast<bf16 *>(reinterpret_cast<unsigned char *>(fwd) + off) = __float2bfloat16_rn(v);
+    }
+    if (trn && idx < 27 * cin * cout) {
+        const int k = idx % cout, rest = idx / cout;
+        const int n = rest % cin, t = rest / cin;
+        const float v = w[((size_t)t * cin + n) * cout + k];
+        const uint32_t off = t * (uint32_t)(cin * cout * 2) + tc::kmaj_off(n, k, cout);
+        *reinterpret_cast<bf16 *>(reinterpret_cast<unsigned char *>(trn) + off) = __float2bfloat16_rn(v);
+    }
+}
+
+__global__ void k_adam(float *p, const float *g, float *m, float *v, int64_t n, float lr, float b1, float b2,
+                       float eps, float c1, float c2) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// training batch: x0 from stored residuals, FP32 targets, per-sample |e|^2
+__global__ void k_gather_batch(const bf16 *dr, const bf16 *de, const int *idx, int64_t v0, int batch, bf16 *x0,
+                               float *tgt) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= v0 * batch) return;
+    const int b = (int)(r / v0);
+    const int64_t n = r - (int64_t)b * v0;
+    const int64_t src = (int64_t)idx[b] * v0 + n;
+    float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int c = 0; c < 3; c++) {
+        f[c] = __bfloat162float(dr[3 * src + c]);
+        tgt[3 * r + c] = __bfloat162float(de[3 * src + c]);
+    }
+    uint4 *o = reinterpret_cast<uint4 *>(x0 + r * 16);
+    o[0] = pack8(f);
+    o[1] = make_uint4(0, 0, 0, 0);
+}
+
+// loss = mean_b |z - t|^2 / |t|^2 ; gz = d loss / d z.  One block per sample.
+__global__ void __launch_bounds__(RED_THREADS) k_mse(const float *z, const float *t, float *gz, int64_t v0, int batch,
+                                                     float *loss_part) {
+    __shared__ float sh[RED_THREADS / 32];
+    __shared__ float tot;
+    const int b = blockIdx.x;
+    const float *zb = z + (size_t)b * v0 * 3, *tb = t + (size_t)b * v0 * 3;
+    float *gb = gz + (size_t)b * v0 * 3;
+    float s = 0.0f;
+    for (int64_t i = threadIdx.x; i < 3 * v0; i += blockDim.x) s += tb[i] * tb[i];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) sh[wid] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = 0.0f;
+        for (int w = 0; w < RED_THREADS / 32; w++) a += sh[w];
+        tot = a > 0.0f ? a : 1.0f;
+    }
+    __syncthreads();
+    const float inv = 1.0f / (tot * (float)batch);
+    float l = 0.0f;
+    for (int64_t i = threadIdx.x; i < 3 * v0; i += blockDim.x) {
+        const float d = zb[i] - tb[i];
+        l += d * d;
+        gb[i] = 2.0f * d * inv;
+    }
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
+    __syncthreads();
+    if (lane == 0) sh[wid] = l;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = 0.0f;
+        for (int w = 0; w < RED_THREADS / 32; w++) a += sh[w];
+        loss_part[b] = a * inv;
+    }
+}
+
+// training pair: residual and error, both divided by the residual's RMS
+__global__ void k_append_pair(const double *r, const double *rr, const double *e, int64_t nodec, bf16 *dr, bf16 *de) {
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nodec) return;
+    const double ms = rr[0] / (3.0 * (double)nodec);
+    const double inv = ms > 0.0 ? 1.0 / sqrt(ms) : 0.0;
+    for (int c = 0; c < 3; c++) {
+        dr[3 * n + c] = __float2bfloat16_rn((float)(r[c * nodec + n] * inv));
+        de[3 * n + c] = __float2bfloat16_rn((float)(e[c * nodec + n] * inv));
+    }
+}
+
+}  // namespace nn
+}  // namespace mpm
+
+// ------------------------------------------------------------- network object
+struct mpm_nn {
+    nn::Lvl L[3];
+    int max_batch = 1;
+    int nsm = 148;
+    float *p = nullptr, *g = nullptr, *am = nullptr, *av = nullptr;
+    bf16 *wf[NCONV] = {}, *wt[NCONV] = {};
+    bf16 *x0 = nullptr, *e0 = nullptr, *e1 = nullptr, *e2 = nullptr, *c2 = nullptr, *d1 = nullptr, *c1 = nullptr,
+         *d0 = nullptr;
+    bf16 *gd0 = nullptr, *ge0 = nullptr, *gc1 = nullptr, *gd1 = nullptr, *ge1 = nullptr, *gc2 = nullptr,
+         *ge2 = nullptr;
+    float *z = nullptr, *gz = nullptr, *tgt = nullptr;
+    float *part = nullptr;
+    size_t part_cap = 0;
+    float *loss = nullptr;
+    int *idx = nullptr;
+    int *err = nullptr;
+    bool weights_dirty = true;
+    int64_t adam_step = 0;
+    bf16 *data_r = nullptr, *data_e = nullptr;
+    int64_t ndata = 0, data_cap = 0;
+    int64_t *d_ndata = nullptr;
+    cudaStream_t stream = nullptr;
+};
+
+namespace {
+
+using namespace mpm::nn;
+
+template <int K, int N, int MODE>
+cudaError_t launch_conv(mpm_nn *net, cudaStream_t st, const bf16 *in, bf16 *out, const bf16 *w, const float *bias,
+                        const bf16 *add, const bf16 *mask, int relu, const Lvl &lin, const Lvl &lout, int batch) {
+    constexpr size_t smem = conv_smem<K, N>();
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_conv_tc<K, N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    ConvArgs a;
+    a.in = in;
+    a.out = out;
+    a.w = w;
+    a.bias = bias;
+    a.add = add;
+    a.mask = mask;
+    a.relu = relu;
+    a.lin = lin;
+    a.lout = lout;
+    a.rows = (int64_t)batch * lout.v;
+    a.err = net->err;
+    const int64_t ntile = (a.rows + 127) / 128;
+    const int per_sm = smem <= 50000 ? 4 : smem <= 70000 ? 3 : smem <= 110000 ? 2 : 1;
+    const int grid = (int)std::min<int64_t>(ntile, (int64_t)net->nsm * per_sm);
+    k_conv_tc<K, N, MODE><<<grid, 128, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int CI, int CO, int MODE>
+cudaError_t launch_dw(mpm_nn *net, cudaStream_t st, const bf16 *in, const bf16 *g, const Lvl &lin, const Lvl &lout,
+                      int batch, int ci_real, float *grad) {
+    constexpr size_t smem = dw_smem<CI, CO>();
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_conv_dw_tc<CI, CO, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    DwArgs a;
+    a.in = in;
+    a.g = g;
+    a.lin = lin;
+    a.lout = lout;
+    a.rows = (int64_t)batch * lout.v;
+    a.err = net->err;
+    const int64_t nchunk = (a.rows + DW_KV - 1) / DW_KV;
+    int grid = (int)std::min<int64_t>(nchunk, (int64_t)net->nsm);
+    const size_t per = (size_t)27 * CI * CO;
+    if ((size_t)grid * per > net->part_cap) grid = (int)(net->part_cap / per);
+    a.part = net->part;
+    k_conv_dw_tc<CI, CO, MODE><<<grid, 128, smem, st>>>(a);
+    const int n = 27 * ci_real * CO;
+    k_dw_reduce<<<(n + 255) / 256, 256, 0, st>>>(net->part, grid, CI, ci_real, CO, grad);
+    return cudaGetLastError();
+}
+
+template <int C>
+void launch_chan_sum(mpm_nn *net, cudaStream_t st, const bf16 *g, int64_t rows, float *out) {
+    const int nblk = (int)std::min<int64_t>((rows + RED_THREADS - 1) / RED_THREADS, 2 * (int64_t)net->nsm);
+    k_chan_sum<C><<<nblk, RED_THREADS, 0, st>>>(g, net->part, rows);
+    k_part_reduce<<<1, 64, 0, st>>>(net->part, nblk, C, out);
+}
+
+int blocks(int64_t n, int t = 256) { return (int)((n + t - 1) / t); }
+
+cudaError_t prep_weights(mpm_nn *net, cudaStream_t st) {
+    if (!net->weights_dirty) return cudaSuccess;
+    for (int l = 0; l < NCONV; l++) {
+        const int n = 27 * COUT[l] * std::max(KPAD[l], CIN[l]);
+        k_wprep<<<blocks(n), 256, 0, st>>>(net->p + w_offset(l), CIN[l], COUT[l], KPAD[l], net->wf[l],
+                                           l == 0 ? nullptr : net->wt[l]);
+    }
+    net->weights_dirty = false;
+    return cudaGetLastError();
+}
+
+// forward of `batch` samples whose x0 is already in place
+cudaError_t forward(mpm_nn *net, cudaStream_t st, int batch) {
+    cudaError_t e = prep_weights(net, st);
+    if (e != cudaSuccess) return e;
+    const Lvl &L0 = net->L[0], &L1 = net->L[1], &L2 = net->L[2];
+    const float *P = net->p;
+    if ((e = launch_conv<16, 16, S1>(net, st, net->x0, net->e0, net->wf[0], P + b_offset(0), nullptr, nullptr, 1, L0,
+                                     L0, batch)) != cudaSuccess)
+        return e;
+    if ((e = launch_conv<16, 32, S2>(net, st, net->e0, net->e1, net->wf[1], P + b_offset(1), nullptr, nullptr, 1, L0,
+                                     L1, batch)) != cudaSuccess)
+        return e;
+    if ((e = launch_conv<32, 64, S2>(net, st, net->e1, net->e2, net->wf[2], P + b_offset(2), nullptr, nullptr, 1, L1,
+                                     L2, batch)) != cudaSuccess)
+        return e;
+    if ((e = launch_conv<64, 32, S1>(net, st, net->e2, net->c2, net->wf[3], P + b_offset(3), nullptr, nullptr, 0, L2,
+                                     L2, batch)) != cudaSuccess)
+        return e;
+    const int64_t r1 = (int64_t)batch * L1.v, r0 = (int64_t)batch * L0.v;
+    k_up_add_relu<32><<<blocks(r1 * 4), 256, 0, st>>>(net->c2, net->e1, net->d1, L1, L2, r1);
+    if ((e = launch_conv<32, 16, S1>(net, st, net->d1, net->c1, net->wf[4], P + b_offset(4), nullptr, nullptr, 0, L1,
+                                     L1, batch)) != cudaSuccess)
+        return e;
+    k_up_add_relu<16><<<blocks(r0 * 2), 256, 0, st>>>(net->c1, net->e0, net->d0, L0, L1, r0);
+    return cudaGetLastError();
+}
+
+// backward from gz (FP32 [rows0][3]) into net->g
+cudaError_t backward(mpm_nn *net, cudaStream_t st, int batch) {
+    const Lvl &L0 = net->L[0], &L1 = net->L[1], &L2 = net->L[2];
+    const int64_t r0 = (int64_t)batch * L0.v, r1 = (int64_t)batch * L1.v, r2 = (int64_t)batch * L2.v;
+    float *G = net->g;
+    cudaError_t e;
+    {
+        const int nblk = (int)std::min<int64_t>(blocks(r0, RED_THREADS), 2 * (int64_t)net->nsm);
+        k_output_bwd<<<nblk, RED_THREADS, 0, st>>>(net->gz, net->d0, net->p + w5_offset(), net->gd0, net->part, r0);
+        k_part_reduce<<<1, 64, 0, st>>>(net->part, nblk, 51, G + w5_offset());
+    }
+    // c1 -> d0 through up: gc1 = up^T(gd0)
+    k_restrict<16><<<blocks(r1 * 2), 256, 0, st>>>(net->gd0, net->gc1, L0, L1, r1);
+    launch_chan_sum<16>(net, st, net->gc1, r1, G + b_offset(4));
+    if ((e = launch_dw<32, 16, S1>(net, st, net->d1, net->gc1, L1, L1, batch, 32, G + w_offset(4))) != cudaSuccess)
+        return e;
+    // gd1 = conv4^T(gc1) masked by d1
+    if ((e = launch_conv<16, 32, S1T>(net, st, net->gc1, net->gd1, net->wt[4], nullptr, nullptr, net->d1, 0, L1, L1,
+                                      batch)) != cudaSuccess)
+        return e;
+    k_restrict<32><<<blocks(r2 * 4), 256, 0, st>>>(net->gd1, net->gc2, L1, L2, r2);
+    launch_chan_sum<32>(net, st, net->gc2, r2, G + b_offset(3));
+    if ((e = launch_dw<64, 32, S1>(net, st, net->e2, net->gc2, L2, L2, batch, 64, G + w_offset(3))) != cudaSuccess)
+        return e;
+    // ge2 = conv3^T(gc2) masked by e2
+    if ((e = launch_conv<32, 64, S1T>(net, st, net->gc2, net->ge2, net->wt[3], nullptr, nullptr, net->e2, 0, L2, L2,
+                                      batch)) != cudaSuccess)
+        return e;
+    launch_chan_sum<64>(net, st, net->ge2, r2, G + b_offset(2));
+    if ((e = launch_dw<32, 64, S2>(net, st, net->e1, net->ge2, L1, L2, batch, 32, G + w_offset(2))) != cudaSuccess)
+        return e;
+    // ge1 = (conv2^T(ge2) + gd1) masked by e1
+    if ((e = launch_conv<64, 32, S2T>(net, st, net->ge2, net->ge1, net->wt[2], nullptr, net->gd1, net->e1, 0, L2, L1,
+                                      batch)) != cudaSuccess)
+        return e;
+    launch_chan_sum<32>(net, st, net->ge1, r1, G + b_offset(1));
+    if ((e = launch_dw<16, 32, S2>(net, st, net->e0, net->ge1, L0, L1, batch, 16, G + w_offset(1))) != cudaSuccess)
+        return e;
+    // ge0 = (conv1^T(ge1) + gd0) masked by e0
+    if ((e = launch_conv<32, 16, S2T>(net, st, net->ge1, net->ge0, net->wt[1], nullptr, net->gd0, net->e0, 0, L1, L0,
+                                      batch)) != cudaSuccess)
+        return e;
+    launch_chan_sum<16>(net, st, net->ge0, r0, G + b_offset(0));
+    if ((e = launch_dw<16, 16, S1>(net, st, net->x0, net->ge0, L0, L0, batch, 3, G + w_offset(0))) != cudaSuccess)
+        return e;
+    return cudaGetLastError();
+}
+
+mpm_status read_err(mpm_nn *net) {
+    int h = 0;
+    CKN(cudaMemcpy(&h, net->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) {
+        CKN(cudaMemset(net->err, 0, sizeof(int)));
+        return MPM_ERR_DEVICE_TIMEOUT;
+    }
+    return MPM_OK;
+}
+
+void net_free(mpm_nn *n) {
+    void *ptrs[] = {n->p,   n->g,   n->am,  n->av,  n->x0,  n->e0,  n->e1,  n->e2,     n->c2,     n->d1,
+                    n->c1,  n->d0,  n->gd0, n->ge0, n->gc1, n->gd1, n->ge1, n->gc2,    n->ge2,    n->z,
+                    n->gz,  n->tgt, n->part, n->loss, n->idx, n->err, n->data_r, n->data_e, n->d_ndata};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (int l = 0; l < NCONV; l++) {
+        if (n->wf[l]) cudaFree(n->wf[l]);
+        if (n->wt[l]) cudaFree(n->wt[l]);
+    }
+}
+
+// splitmix64 + Box-Muller: deterministic parameter initialisation
+struct Rng {
+    uint64_t s;
+    uint64_t next() {
+        uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    double uniform() { return ((next() >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+    double normal() {
+        const double u1 = uniform(), u2 = uniform();
+        return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+    }
+};
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+int64_t mpm_nn_num_params(void) { return param_count(); }
+
+mpm_status mpm_nn_create(const int nodes[3], int max_batch, int64_t max_pairs, mpm_nn **out) {
+    if (!nodes || !out || max_batch < 1 || max_pairs < 0) return MPM_ERR_BAD_ARG;
+    for (int d = 0; d < 3; d++)
+        if (nodes[d] < 3) return MPM_ERR_BAD_ARG;
+    mpm_nn *n = new (std::nothrow) mpm_nn();
+    if (!n) return MPM_ERR_OOM;
+    for (int d = 0; d < 3; d++) {
+        n->L[0].n[d] = nodes[d];
+        n->L[1].n[d] = nodes[d] / 2 + 1;
+        n->L[2].n[d] = n->L[1].n[d] / 2 + 1;
+    }
+    for (int l = 0; l < 3; l++) n->L[l].v = (int64_t)n->L[l].n[0] * n->L[l].n[1] * n->L[l].n[2];
+    n->max_batch = max_batch;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n->nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t P = param_count();
+    const int64_t B = max_batch, v0 = n->L[0].v, v1 = n->L[1].v, v2 = n->L[2].v;
+    auto fail = [&](cudaError_t e) {
+        fprintf(stderr, "mpm_gb300 (nn): allocation failed: %s\n", cudaGetErrorString(e));
+        net_free(n);
+        delete n;
+        return e == cudaErrorMemoryAllocation ? MPM_ERR_OOM : MPM_ERR_CUDA;
+    };
+    cudaError_t e;
+#define NN_ALLOC(ptr, bytes)                                       \
+    do {                                                           \
+        if ((e = cudaMalloc((void **)&(ptr), (bytes))) != cudaSuccess) return fail(e); \
+    } while (0)
+    NN_ALLOC(n->p, P * 4);
+    NN_ALLOC(n->g, P * 4);
+    NN_ALLOC(n->am, P * 4);
+    NN_ALLOC(n->av, P * 4);
+    for (int l = 0; l < NCONV; l++) {
+        NN_ALLOC(n->wf[l], (size_t)27 * COUT[l] * KPAD[l] * 2);
+        NN_ALLOC(n->wt[l], (size_t)27 * CIN[l] * COUT[l] * 2);
+    }
+    NN_ALLOC(n->x0, B * v0 * 16 * 2);
+    NN_ALLOC(n->e0, B * v0 * 16 * 2);
+    NN_ALLOC(n->d0, B * v0 * 16 * 2);
+    NN_ALLOC(n->gd0, B * v0 * 16 * 2);
+    NN_ALLOC(n->ge0, B * v0 * 16 * 2);
+    NN_ALLOC(n->e1, B * v1 * 32 * 2);
+    NN_ALLOC(n->d1, B * v1 * 32 * 2);
+    NN_ALLOC(n->c1, B * v1 * 16 * 2);
+    NN_ALLOC(n->gc1, B * v1 * 16 * 2);
+    NN_ALLOC(n->gd1, B * v1 * 32 * 2);
+    NN_ALLOC(n->ge1, B * v1 * 32 * 2);
+    NN_ALLOC(n->e2, B * v2 * 64 * 2);
+    NN_ALLOC(n->c2, B * v2 * 32 * 2);
+    NN_ALLOC(n->gc2, B * v2 * 32 * 2);
+    NN_ALLOC(n->ge2, B * v2 * 64 * 2);
+    NN_ALLOC(n->z, B * v0 * 3 * 4);
+    NN_ALLOC(n->gz, B * v0 * 3 * 4);
+    NN_ALLOC(n->tgt, B * v0 * 3 * 4);
+    n->part_cap = (size_t)n->nsm * 27 * 64 * 32;   // largest weight-gradient partials
+    NN_ALLOC(n->part, n->part_cap * 4);
+    NN_ALLOC(n->loss, (size_t)B * 4);
+    NN_ALLOC(n->idx, (size_t)B * 4);
+    NN_ALLOC(n->err, sizeof(int));
+    NN_ALLOC(n->d_ndata, sizeof(int64_t));
+    if (max_pairs > 0) {
+        NN_ALLOC(n->data_r, (size_t)max_pairs * v0 * 3 * 2);
+        NN_ALLOC(n->data_e, (size_t)max_pairs * v0 * 3 * 2);
+    }
+#undef NN_ALLOC
+    n->data_cap = max_pairs;
+    cudaMemset(n->p, 0, P * 4);
+    cudaMemset(n->am, 0, P * 4);
+    cudaMemset(n->av, 0, P * 4);
+    cudaMemset(n->err, 0, sizeof(int));
+    *out = n;
+    return MPM_OK;
+}
+
+mpm_status mpm_nn_destroy(mpm_nn *net) {
+    if (!net) return MPM_ERR_BAD_ARG;
+    cudaDeviceSynchronize();
+    net_free(net);
+    delete net;
+    return MPM_OK;
+}
+
+mpm_status mpm_nn_set_stream(mpm_nn *net, void *stream) {
+    if (!net) return MPM_ERR_BAD_ARG;
+    net->stream = (cudaStream_t)stream;
+    return MPM_OK;
+}
+
+mpm_status mpm_nn_init_params(mpm_nn *net, uint64_t seed) {
+    if (!net) return MPM_ERR_BAD_ARG;
+    std::vector<float> h(param_count(), 0.0f);
+    Rng rng{seed};
+    for (int l = 0; l < NCONV; l++) {
+        const double sd = sqrt(2.0 / (27.0 * CIN[l]));
+        float *w = h.data() + w_offset(l);
+        for (int64_t i = 0; i < 27LL * CIN[l] * COUT[l]; i++) w[i] = (float)(sd * rng.normal());
+    }
+    const double sd5 = sqrt(1.0 / 16.0);
+    for (int i = 0; i < 48; i++) h[w5_offset() + i] = (float)(sd5 * rng.normal());
+    CKN(cudaMemcpy(net->p, h.data(), h.size() * 4, cudaMemcpyHostToDevice));
+    CKN(cudaMemset(net->am, 0, h.size() * 4));
+    CKN(cudaMemset(net->av, 0, h.size() * 4));
+    net->adam_step = 0;
+    net->weights_dirty = true;
+    return MPM_OK;
+}
+
+mpm_status mpm_nn_set_params(mpm_nn *net, const float *params) {
+    if (!net || !params) return MPM_ERR_BAD_ARG;
+    CKN(cudaMemcpy(net->p, params, param_count() * 4, cudaMemcpyHostToDevice));
+    net->weights_dirty = true;
+    return MPM_OK;
+}
+
+mpm_status mpm_nn_get_params(mpm_nn *net, float *params) {
+    if (!net || !params) return MPM_ERR_BAD_ARG;
+    CKN(cudaStreamSynchronize(net->stream));
+    CKN(cudaMemcpy(params, net->p, param_count() * 4, cudaMemcpyDeviceToHost));
+    return MPM_OK;
+}
+
+mpm_status mpm_nn_forward(mpm_nn *net, int batch, const float *in, float *out) {
+    if (!net || !in || !out || batch < 1 || batch > net->max_batch) return MPM_ERR_BAD_ARG;
+    cudaStream_t st = net->stream;
+    const int64_t r0 = (int64_t)batch * net->L[0].v;
+    CKN(cudaMemcpyAsync(net->z, in, r0 * 3 * 4, cudaMemcpyHostToDevice, st));
+    k_input_f32<<<blocks(r0), 256, 0, st>>>(net->z, net->x0, r0);
+    CKN(forward(net, st, batch));
+    k_output<<<blocks(r0), 256, 0, st>>>(net->d0, net->p + w5_offset(), net->p + b5_offset(), net->z, r0);
+    CKN(cudaGetLastError());
+    CKN(cudaMemcpyAsync(out, net->z, r0 * 3 * 4, cudaMemcpyDeviceToHost, st));
+    CKN(cudaStreamSynchronize(st));
+    return read_err(net);
+}
+
+mpm_status mpm_nn_backward(mpm_nn *net, int batch, const float *in, const float *gout, float *grad) {
+    if (!net || !in || !gout || !grad || batch < 1 || batch > net->max_batch) return MPM_ERR_BAD_ARG;
+    cudaStream_t st = net->stream;
+    const int64_t r0 = (int64_t)batch * net->L[0].v;
+    CKN(cudaMemcpyAsync(net->z, in, r0 * 3 * 4, cudaMemcpyHostToDevice, st));
+    CKN(cudaMemcpyAsync(net->gz, gout, r0 * 3 * 4, cudaMemcpyHostToDevice, st));
+    k_input_f32<<<blocks(r0), 256, 0, st>>>(net->z, net->x0, r0);
+    CKN(forward(net, st, batch));
+    CKN(backward(net, st, batch));
+    CKN(cudaMemcpyAsync(grad, net->g, param_count() * 4, cudaMemcpyDeviceToHost, st));
+    CKN(cudaStreamSynchronize(st));
+    return read_err(net);
+}
+
+mpm_status mpm_nn_num_pairs(mpm_nn *net, int64_t *n) {
+    if (!net || !n) return MPM_ERR_BAD_ARG;
+    *n = net->ndata;
+    return MPM_OK;
+}
+
+mpm_status mpm_nn_train(mpm_nn *net, int epochs, int batch, double lr, uint64_t seed, float *epoch_loss) {
+    if (!net || epochs < 1 || batch < 1 || batch > net->max_batch || !(lr > 0.0)) return MPM_ERR_BAD_ARG;
+    if (net->ndata < batch) return MPM_ERR_STATE;
+    cudaStream_t st = net->stream;
+    const int64_t v0 = net->L[0].v, r0 = (int64_t)batch * v0;
+    const int64_t P = param_count();
+    const int64_t nb = net->ndata / batch;
+    std::vector<int> perm(net->ndata);
+    std::vector<float> lbuf(batch);
+    Rng rng{seed};
+    const float b1 = 0.9f, b2 = 0.999f;
+    for (int ep = 0; ep < epochs; ep++) {
+        for (int64_t i = 0; i < net->ndata; i++) perm[i] = (int)i;
+        for (int64_t i = net->ndata - 1; i > 0; i--) std::swap(perm[i], perm[rng.next() % (uint64_t)(i + 1)]);
+        double lsum = 0.0;
+        for (int64_t bi = 0; bi < nb; bi++) {
+            CKN(cudaMemcpyAsync(net->idx, perm.data() + bi * batch, batch * 4, cudaMemcpyHostToDevice, st));
+            k_gather_batch<<<blocks(r0), 256, 0, st>>>(net->data_r, net->data_e, net->idx, v0, batch, net->x0,
+                                                       net->tgt);
+            CKN(forward(net, st, batch));
+            k_output<<<blocks(r0), 256, 0, st>>>(net->d0, net->p + w5_offset(), net->p + b5_offset(), net->z, r0);
+            k_mse<<<batch, RED_THREADS, 0, st>>>(net->z, net->tgt, net->gz, v0, batch, net->loss);
+            CKN(backward(net, st, batch));
+            net->adam_step++;
+            const float c1 = 1.0f - powf(b1, (float)net->adam_step), c2 = 1.0f - powf(b2, (float)net->adam_step);
+            k_adam<<<blocks(P), 256, 0, st>>>(net->p, net->g, net->am, net->av, P, (float)lr, b1, b2, 1e-8f, c1, c2);
+            net->weights_dirty = true;
+            CKN(cudaMemcpyAsync(lbuf.data(), net->loss, batch * 4, cudaMemcpyDeviceToHost, st));
+            CKN(cudaStreamSynchronize(st));
+            for (int b = 0; b < batch; b++) lsum += lbuf[b];
+        }
+        if (epoch_loss) epoch_loss[ep] = (float)(lsum / (double)nb);
+    }
+    CKN(cudaStreamSynchronize(st));
+    return read_err(net);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------- solver-side hooks
+int mpm_nn_grid_matches(const mpm_nn *net, const int nodes[3]) {
+    return net && net->L[0].n[0] == nodes[0] && net->L[0].n[1] == nodes[1] && net->L[0].n[2] == nodes[2];
+}
+
+mpm_status mpm_nn_apply_precond(mpm_nn *net, cudaStream_t st, const double *r, const double *rr, const double *adiag,
+                                const unsigned char *bcflag, double mtol, double *z) {
+    const int64_t nodec = net->L[0].v;
+    k_input_r<<<blocks(nodec), 256, 0, st>>>(r, rr, nodec, net->x0);
+    CKN(forward(net, st, 1));
+    k_output_precond<<<blocks(nodec), 256, 0, st>>>(net->d0, net->p + w5_offset(), net->p + b5_offset(), rr, nodec,
+                                                   adiag, bcflag, mtol, z);
+    CKN(cudaGetLastError());
+    return MPM_OK;
+}
+
+mpm_status mpm_nn_append_pair(mpm_nn *net, cudaStream_t st, const double *r, const double *rr, const double *e) {
+    if (net->ndata >= net->data_cap) return MPM_OK;
+    const int64_t nodec = net->L[0].v;
+    k_append_pair<<<blocks(nodec), 256, 0, st>>>(r, rr, e, nodec, net->data_r + net->ndata * nodec * 3,
+                                                net->data_e + net->ndata * nodec * 3);
+    net->ndata++;
+    CKN(cudaGetLastError());
+    return MPM_OK;
+}

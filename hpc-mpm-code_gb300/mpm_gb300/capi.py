@@ -48,7 +48,8 @@ class Config(C.Structure):
 
 
 class SolveStats(C.Structure):
-    _fields_ = [("newton_iters", C.c_int), ("krylov_iters", C.c_int), ("last_rel_residual", C.c_double)]
+    _fields_ = [("newton_iters", C.c_int), ("krylov_iters", C.c_int), ("last_rel_residual", C.c_double),
+                ("precond_fallbacks", C.c_int), ("nn_applications", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -68,7 +69,9 @@ EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_s
            "mpm_gpu_get_stats", "mpm_gpu_enable_kernel_timing", "mpm_gpu_kernel_times", "mpm_gpu_implicit_setup",
            "mpm_gpu_implicit_step", "mpm_gpu_implicit_assemble", "mpm_gpu_implicit_get_system",
            "mpm_gpu_implicit_matvec", "mpm_gpu_implicit_solve", "mpm_gpu_p2g_noalloc", "mpm_gpu_autotune",
-           "mpm_gpu_get_tuning"]
+           "mpm_gpu_get_tuning", "mpm_nn_num_params", "mpm_nn_create", "mpm_nn_destroy", "mpm_nn_set_stream",
+           "mpm_nn_init_params", "mpm_nn_set_params", "mpm_nn_get_params", "mpm_nn_forward", "mpm_nn_backward",
+           "mpm_nn_num_pairs", "mpm_nn_train", "mpm_gpu_implicit_set_precond", "mpm_gpu_implicit_harvest"]
 
 
 def load(path: str | None = None):
@@ -110,6 +113,22 @@ def load(path: str | None = None):
     lib.mpm_gpu_implicit_solve.argtypes = [C.c_void_p, C.c_double, C.c_int, _dp, C.POINTER(C.c_int)]
     lib.mpm_gpu_kernel_times.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_char_p), _dp,
                                          C.POINTER(C.c_int64)]
+    _fp = C.POINTER(C.c_float)
+    lib.mpm_nn_num_params.restype = C.c_int64
+    lib.mpm_nn_num_params.argtypes = []
+    lib.mpm_nn_create.argtypes = [_ip, C.c_int, C.c_int64, C.POINTER(C.c_void_p)]
+    lib.mpm_nn_destroy.argtypes = [C.c_void_p]
+    lib.mpm_nn_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+    lib.mpm_nn_init_params.argtypes = [C.c_void_p, C.c_uint64]
+    lib.mpm_nn_set_params.argtypes = [C.c_void_p, _fp]
+    lib.mpm_nn_get_params.argtypes = [C.c_void_p, _fp]
+    lib.mpm_nn_forward.argtypes = [C.c_void_p, C.c_int, _fp, _fp]
+    lib.mpm_nn_backward.argtypes = [C.c_void_p, C.c_int, _fp, _fp, _fp]
+    lib.mpm_nn_num_pairs.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+    lib.mpm_nn_train.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_uint64, _fp]
+    lib.mpm_gpu_implicit_set_precond.argtypes = [C.c_void_p, C.c_void_p]
+    lib.mpm_gpu_implicit_harvest.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
+                                             C.c_double, C.c_uint64, C.c_double, C.c_int]
     _lib = lib
     return lib
 
@@ -260,10 +279,24 @@ class GpuImplicitSolid(GpuSolid):
         super().__init__(scene, precision=64, shifting=shifting, stream=stream, implicit=True)
         _chk(self.lib.mpm_gpu_implicit_setup(self.ctx, int(nr_flag), float(spec_rad)), "mpm_gpu_implicit_setup")
 
-    def implicit_steps(self, n, facl=1.0, eps=1.0e-8, kmax=10000):
+    def implicit_steps(self, n, facl=1.0, eps=1.0e-8, kmax=10000, full=False):
         st = SolveStats()
         _chk(self.lib.mpm_gpu_implicit_step(self.ctx, n, facl, eps, kmax, C.byref(st)), "mpm_gpu_implicit_step")
+        if full:
+            return {k: getattr(st, k) for k, _ in SolveStats._fields_}
         return st.krylov_iters, st.newton_iters, st.last_rel_residual
+
+    def set_precond(self, net):
+        """Use a PrecondNet (or None: Jacobi) for the linear solves."""
+        _chk(self.lib.mpm_gpu_implicit_set_precond(self.ctx, net.net if net is not None else None),
+             "mpm_gpu_implicit_set_precond")
+        self._net = net
+
+    def harvest(self, net, nsystems, loads_per_system, pairs_per_load, e_min, e_max, seed=0, eps=1.0e-16,
+                kmax=20000):
+        """Training pairs for `net` from this solid's own Jacobi-PCG solves."""
+        _chk(self.lib.mpm_gpu_implicit_harvest(self.ctx, net.net, nsystems, loads_per_system, pairs_per_load,
+                                                 e_min, e_max, seed, eps, kmax), "mpm_gpu_implicit_harvest")
 
     def assemble(self, facl=1.0):
         _chk(self.lib.mpm_gpu_implicit_assemble(self.ctx, facl), "mpm_gpu_implicit_assemble")
@@ -303,3 +336,69 @@ def stencil_to_csr(stencil, xynodec, matrow, matcolid):
     for e in range(9):
         amat[e] = stencil[slot, e, rows]
     return amat
+
+
+_fp32 = C.POINTER(C.c_float)
+
+
+class PrecondNet:
+    """The learned preconditioner network (mpm_nn_*) on a grid of `nodes` control points."""
+
+    def __init__(self, nodes, max_batch=1, max_pairs=0, seed=None):
+        self.lib = load()
+        self.nodes = tuple(int(n) for n in nodes)
+        n3 = (C.c_int * 3)(*self.nodes)
+        h = C.c_void_p()
+        _chk(self.lib.mpm_nn_create(n3, int(max_batch), int(max_pairs), C.byref(h)), "mpm_nn_create")
+        self.net = h
+        self.nvox = self.nodes[0] * self.nodes[1] * self.nodes[2]
+        self.nparams = int(self.lib.mpm_nn_num_params())
+        if seed is not None:
+            _chk(self.lib.mpm_nn_init_params(self.net, int(seed)), "mpm_nn_init_params")
+
+    def close(self):
+        if getattr(self, "net", None):
+            self.lib.mpm_nn_destroy(self.net)
+            self.net = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.nparams
+        _chk(self.lib.mpm_nn_set_params(self.net, p.ctypes.data_as(_fp32)), "mpm_nn_set_params")
+
+    def params(self):
+        p = np.zeros(self.nparams, dtype=np.float32)
+        _chk(self.lib.mpm_nn_get_params(self.net, p.ctypes.data_as(_fp32)), "mpm_nn_get_params")
+        return p
+
+    def forward(self, x):
+        """x: [batch][nodes][3] float32 -> same shape."""
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.nvox, 3)
+        out = np.zeros_like(x)
+        _chk(self.lib.mpm_nn_forward(self.net, x.shape[0], x.ctypes.data_as(_fp32), out.ctypes.data_as(_fp32)),
+             "mpm_nn_forward")
+        return out
+
+    def backward(self, x, gout):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.nvox, 3)
+        g = np.ascontiguousarray(gout, dtype=np.float32).reshape(x.shape)
+        grad = np.zeros(self.nparams, dtype=np.float32)
+        _chk(self.lib.mpm_nn_backward(self.net, x.shape[0], x.ctypes.data_as(_fp32), g.ctypes.data_as(_fp32),
+                                      grad.ctypes.data_as(_fp32)), "mpm_nn_backward")
+        return grad
+
+    def num_pairs(self):
+        n = C.c_int64(0)
+        _chk(self.lib.mpm_nn_num_pairs(self.net, C.byref(n)), "mpm_nn_num_pairs")
+        return n.value
+
+    def train(self, epochs, batch, lr=1.0e-3, seed=0):
+        losses = np.zeros(epochs, dtype=np.float32)
+        _chk(self.lib.mpm_nn_train(self.net, epochs, batch, lr, seed, losses.ctypes.data_as(_fp32)), "mpm_nn_train")
+        return losses

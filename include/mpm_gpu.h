@@ -174,6 +174,8 @@ typedef struct {
     int newton_iters;          /* linear solves (Newton iterations) over the call */
     int krylov_iters;          /* CG iterations over the call */
     double last_rel_residual;  /* ||r|| / ||r0|| of the last solve (scaled system) */
+    int precond_fallbacks;     /* solves that left the learned preconditioner for Jacobi */
+    int nn_applications;       /* learned-preconditioner applications over the call */
 } mpm_solve_stats;
 mpm_status mpm_gpu_implicit_setup(mpm_ctx *ctx, int nr_flag, double spec_rad);
 /* nsteps x (MeshPointLinklist, Particle2Node, SolveSolid, Node2Particle) of the
@@ -194,6 +196,52 @@ mpm_status mpm_gpu_implicit_assemble(mpm_ctx *ctx, double facl);
 mpm_status mpm_gpu_implicit_get_system(mpm_ctx *ctx, double *stencil, double *adiag, double *b_rhs);
 mpm_status mpm_gpu_implicit_matvec(mpm_ctx *ctx, const double *x, double *y);
 mpm_status mpm_gpu_implicit_solve(mpm_ctx *ctx, double eps, int kmax, double *x, int *iters);
+
+/* ---- learned preconditioner ------------------------------------------------
+ * No counterpart in the reference, whose solid solves use GPBiCGSafe with
+ * diagonal scaling or PETSc (module/solver/solver.cpp:19-141,
+ * module/solver/crsmat.cpp:338-686).  A 3-level convolutional
+ * encoder-decoder over the control-point grid (3 input and 3 output
+ * channels, 16/32/64 hidden channels, BF16 weights and activations, FP32
+ * accumulation on tcgen05 tensor cores) serves as the right preconditioner
+ * of a flexible conjugate gradient solver.  Convergence is always judged on
+ * the true FP64 residual, and a solve falls back to the Jacobi preconditioner
+ * when the network stops reducing the residual, so the accuracy of the
+ * solution does not depend on the network.
+ *
+ * Parameters (FP32, mpm_nn_num_params() values): for the five 3x3x3
+ * convolutions l = 0..4 with (cin, cout) = (3,16), (16,32), (32,64),
+ * (64,32), (32,16): W_l[27][cin][cout] (tap t = (dx+1) + 3(dy+1) + 9(dz+1))
+ * then b_l[cout]; then the 1x1 output layer W5[16][3], b5[3].
+ * Host tensors of forward/backward are FP32 [batch][nodes][3] with nodes in
+ * control-point order i + nx (j + ny k). */
+typedef struct mpm_nn mpm_nn;
+int64_t mpm_nn_num_params(void);
+/* nodes: control points per direction of the grid the network runs on;
+ * max_pairs: capacity of the on-device training set (0: none). */
+mpm_status mpm_nn_create(const int nodes[3], int max_batch, int64_t max_pairs, mpm_nn **out);
+mpm_status mpm_nn_destroy(mpm_nn *net);
+mpm_status mpm_nn_set_stream(mpm_nn *net, void *stream);
+mpm_status mpm_nn_init_params(mpm_nn *net, uint64_t seed);
+mpm_status mpm_nn_set_params(mpm_nn *net, const float *params);
+mpm_status mpm_nn_get_params(mpm_nn *net, float *params);
+mpm_status mpm_nn_forward(mpm_nn *net, int batch, const float *in, float *out);
+/* gradient of sum(out * gout) with respect to the parameters */
+mpm_status mpm_nn_backward(mpm_nn *net, int batch, const float *in, const float *gout, float *grad);
+mpm_status mpm_nn_num_pairs(mpm_nn *net, int64_t *n);
+/* Adam on the stored (residual, error) pairs, loss = mean |net(r) - e|^2 / |e|^2;
+ * epoch_loss[epochs] receives the mean loss of each epoch (may be NULL). */
+mpm_status mpm_nn_train(mpm_nn *net, int epochs, int batch, double lr, uint64_t seed, float *epoch_loss);
+/* Use `net` (NULL: none) as the preconditioner of the implicit solves of ctx. */
+mpm_status mpm_gpu_implicit_set_precond(mpm_ctx *ctx, mpm_nn *net);
+/* Training pairs from the solver's own solves: for each of nsystems moduli
+ * E drawn log-uniformly from [e_min, e_max] the system of the current state
+ * is assembled; for each of loads_per_system seeded random right-hand sides
+ * it is solved twice by Jacobi-PCG to ||r||^2 < eps ||r0||^2, the second
+ * time storing pairs_per_load (residual, error) pairs spread over the
+ * iterations.  The materials' moduli are restored afterwards. */
+mpm_status mpm_gpu_implicit_harvest(mpm_ctx *ctx, mpm_nn *net, int nsystems, int loads_per_system, int pairs_per_load,
+                                    double e_min, double e_max, uint64_t seed, double eps, int kmax);
 
 /* ---- allocation-free P2G -----------------------------------------------------
  * No counterpart in the reference: an extra entry point for callers that
