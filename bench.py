@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--train-pairs", type=int, default=2000,
+                    help="training pairs when no committed preconditioner parameters exist")
     ap.add_argument("--implicit-steps", type=int, default=3,
                     help="implicit cantilever steps timed after the explicit run (0 skips)")
     ap.add_argument("--cells", type=int, default=80,
@@ -217,27 +219,57 @@ def run_reference(args):
 
 def run_implicit(args, torch, stream):
     """The implicit solid: 1,728,000-particle Neo-Hookean cantilever on a 64^3 grid,
-    E = 1e7 Pa, nu = 0.3, dt = 1e-3 s, Newton + diagonally scaled CG solved to a
-    relative residual of 1e-8 (eps = 1e-16 on squared norms), FP64."""
-    from mpm_gb300 import capi, scenes
+    E = 1e7 Pa, nu = 0.3, dt = 1e-3 s, Newton + Krylov solved to a relative
+    residual of 1e-8 (eps = 1e-16 on squared norms), FP64.  Two solids from the
+    same initial state: Jacobi-PCG, and flexible CG with the learned
+    preconditioner (committed parameters trained by mpm_gb300.train_precond,
+    else a short on-the-spot training run, stated in the record)."""
+    from mpm_gb300 import capi, scenes, train_precond
 
     s = scenes.cantilever(iprop=1)
+
+    def timed(gpu):
+        gpu.implicit_steps(1, eps=1.0e-16)           # warm-up step
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        t0 = time.perf_counter()
+        st = gpu.implicit_steps(args.implicit_steps, eps=1.0e-16, full=True)
+        ev1.record(stream)
+        ev1.synchronize()
+        ms = max(ev0.elapsed_time(ev1), (time.perf_counter() - t0) * 1e3) / args.implicit_steps
+        return ms, st
+
     gpu = capi.GpuImplicitSolid(s, nr_flag=True, stream=stream.cuda_stream)
-    gpu.implicit_steps(1, eps=1.0e-16)           # warm-up step
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    t0 = time.perf_counter()
-    kry, newton, rel = gpu.implicit_steps(args.implicit_steps, eps=1.0e-16)
-    ev1.record(stream)
-    ev1.synchronize()
-    ms = max(ev0.elapsed_time(ev1), (time.perf_counter() - t0) * 1e3) / args.implicit_steps
+    jac_ms, jac = timed(gpu)
     gpu.close()
-    return {"metric": "implicit step time", "value": ms, "unit": "ms/step", "higher_is_better": False,
-            "steps": args.implicit_steps, "particles": s.num, "grid": list(s.xyelem), "dtype": "f64",
-            "solver": "Newton + Jacobi (symmetric diagonal scaling) CG to ||r||/||r0|| <= 1e-8",
-            "krylov_iters_per_step": kry / args.implicit_steps, "newton_iters_per_step": newton / args.implicit_steps,
-            "learned_preconditioner": "not built"}
+    out = {"metric": "implicit step time", "value": jac_ms, "unit": "ms/step", "higher_is_better": False,
+           "steps": args.implicit_steps, "particles": s.num, "grid": list(s.xyelem), "dtype": "f64",
+           "solver": "Newton + Jacobi (symmetric diagonal scaling) CG to ||r||/||r0|| <= 1e-8",
+           "krylov_iters_per_step": jac["krylov_iters"] / args.implicit_steps,
+           "newton_iters_per_step": jac["newton_iters"] / args.implicit_steps}
+    params = train_precond.load_weights()
+    training = "committed parameters (" + os.path.basename(train_precond.WEIGHTS) + ")"
+    if params is None:
+        params, rec = train_precond.train(pairs=args.train_pairs, epochs=2, out=None, log=lambda *_: None)
+        training = (f"trained in this run: {rec['pairs']} pairs, {rec['epochs']} epochs, "
+                    f"{rec['harvest_s'] + rec['train_s']:.0f} s")
+    net = capi.PrecondNet(s.xynodec)
+    net.set_params(params)
+    gpu = capi.GpuImplicitSolid(s, nr_flag=True, stream=stream.cuda_stream)
+    gpu.set_precond(net)
+    nn_ms, nn = timed(gpu)
+    gpu.close()
+    net.close()
+    out["learned"] = {"value": nn_ms, "unit": "ms/step",
+                      "solver": "Newton + flexible CG, learned right preconditioner (BF16 tcgen05 conv "
+                                "encoder-decoder), Jacobi fallback, true FP64 residual <= 1e-8",
+                      "krylov_iters_per_step": nn["krylov_iters"] / args.implicit_steps,
+                      "newton_iters_per_step": nn["newton_iters"] / args.implicit_steps,
+                      "fallbacks": nn["precond_fallbacks"], "network_applications": nn["nn_applications"],
+                      "training": training,
+                      "speedup_vs_jacobi": jac_ms / nn_ms if nn_ms > 0 else None}
+    return out
 
 
 def run_gb300(args):

@@ -220,6 +220,27 @@ __device__ __forceinline__ void neo_hookean_stress_h(float *s, const float H[3][
     s[5] = (mu * bm[0][1]) / J;
 }
 
+// Weakly compressible Newtonian fluid (material model 2, no counterpart in the
+// reference): Tait equation of state p = (rho0 c0^2 / gamma) ((rho / rho0)^gamma - 1)
+// with rho = rho0 / J, and sigma = -p I + 2 mu dev(D), D = sym(grad v).
+// `inc` is the step increment dF - I = dt grad v; mat_prop = {c0, gamma, mu}.
+// (rho/rho0)^gamma - 1 = expm1(-gamma log1p(J - 1)) keeps the small volume
+// change out of the rounding of numbers near 1.
+template <typename R>
+__device__ __forceinline__ void tait_stress(R *s, const R inc[3][3], R jm1, R rho0, R c0, R gam, R mu, R inv_dt) {
+    R pr;
+    if constexpr (sizeof(R) == 8) pr = rho0 * c0 * c0 / gam * expm1(-gam * log1p(jm1));
+    else pr = rho0 * c0 * c0 / gam * expm1f(-gam * log1pf(jm1));
+    const R d0 = inc[0][0] * inv_dt, d1 = inc[1][1] * inv_dt, d2 = inc[2][2] * inv_dt;
+    const R tr3 = (d0 + d1 + d2) / (R)3;
+    s[0] = -pr + (R)2 * mu * (d0 - tr3);
+    s[1] = -pr + (R)2 * mu * (d1 - tr3);
+    s[2] = -pr + (R)2 * mu * (d2 - tr3);
+    s[3] = mu * (inc[1][2] + inc[2][1]) * inv_dt;
+    s[4] = mu * (inc[0][2] + inc[2][0]) * inv_dt;
+    s[5] = mu * (inc[0][1] + inc[1][0]) * inv_dt;
+}
+
 // det(I + H) - 1 without forming I + H
 __device__ __forceinline__ float det_ipm1(const float H[3][3]) {
     const float tr = H[0][0] + H[1][1] + H[2][2];

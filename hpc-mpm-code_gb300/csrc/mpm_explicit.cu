@@ -914,6 +914,11 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
         } else if (model == 1) {
             if constexpr (sizeof(R) == 8) neo_hookean_stress(s, Fn, J, E, nu);
             else neo_hookean_stress_h(s, Fn, det_ipm1(Fn), E, nu);
+        } else if (model == 2) {
+            R jm1;
+            if constexpr (sizeof(R) == 8) jm1 = J - (R)1;
+            else jm1 = det_ipm1(Fn);
+            tait_stress<R>(s, Dm, jm1, ld(P.m + p) / ld(P.vol0 + p), E, nu, (R)a.matprop[3 * mid + 2], (R)1 / a.dt);
         } else if (model == -1) {
 #pragma unroll
             for (int k = 0; k < 6; k++) s[k] = (R)0;
@@ -1068,6 +1073,9 @@ __global__ void __launch_bounds__(UCH) k_g2p_update_tma(StepArgs<float> a, int n
             const float E = (float)a.matprop[3 * mid], nu = (float)a.matprop[3 * mid + 1];
             if (model == 0) lin_elast_update(s, D, E, nu);
             else if (model == 1) neo_hookean_stress_h(s, Hn, jm1, E, nu);
+            else if (model == 2)
+                tait_stress<float>(s, D, jm1, P.m[p] / sf[18 * UCH + t], E, nu, (float)a.matprop[3 * mid + 2],
+                                   1.0f / a.dt);
             else if (model == -1)
 #pragma unroll
                 for (int k = 0; k < 6; k++) s[k] = 0.0f;

@@ -195,3 +195,34 @@ def cantilever(grid=(64, 64, 64), dx=1.0e-2, cell_lo=(0, 2, 2), cells=(60, 60, 6
     for comp in (BC_U, BC_V, BC_W):
         scene.bcs.append((comp, nodes, np.zeros(nodes.shape[0])))
     return scene
+
+
+def dam_break(grid=(256, 128, 128), dx=4.0e-3, cells=(128, 128, 96), npc=2, jitter=0.0, c0=30.0, gamma=7.0,
+              mu=1.0e-3, rho=1000.0, dt=5.0e-6, gravity=(0.0, 0.0, -9.81), scheme=PIC, seed=12350,
+              mtol=1.0e-12, name="dam_break"):
+    """Weakly compressible water column (Tait fluid, material model 2).
+
+    Defaults: 256 x 128 x 128-cell grid, dx = 4e-3 m, a 128 x 128 x 96-cell
+    column in the x = 0 corner at 2x2x2 particles per cell = 12,582,912
+    particles, c0 = 30 m/s, gamma = 7, rho0 = 1000 kg/m^3, mu = 1e-3 Pa s,
+    dt = 5e-6 s.  Slip walls on every face of the box: the normal velocity
+    component is fixed to zero on the boundary nodes.  mat_prop holds
+    {c0, gamma, mu}.
+    """
+    rng = np.random.default_rng(seed)
+    xymin = (0.0, 0.0, 0.0)
+    dxy = (dx, dx, dx)
+    pts = block_particles((0, 0, 0), tuple(cells), xymin, dxy, (npc, npc, npc), jitter, rng)
+    n = pts.shape[0]
+    vp = dx ** 3 / npc ** 3
+    scene = Scene(
+        xyelem=tuple(grid), xymin=xymin, dxy=dxy, idimc=(1, 1, 1), npxye=(npc, npc, npc),
+        dt=dt, mtol=mtol, gravity=tuple(gravity),
+        iprop=np.array([2], dtype=np.int32), mat_prop=np.array([[c0, gamma, mu]]),
+        coord=pts, vel=np.zeros((n, 3)), mass=np.full(n, rho * vp), vol0=np.full(n, vp),
+        matid=np.zeros(n, dtype=np.int32), scheme=scheme, name=name)
+    nn = scene.xynodec
+    for axis, comp in ((0, BC_U), (1, BC_V), (2, BC_W)):
+        nodes = np.concatenate([face_nodes(nn, axis, 0), face_nodes(nn, axis, nn[axis] - 1)])
+        scene.bcs.append((comp, nodes, np.zeros(nodes.shape[0])))
+    return scene

@@ -1,0 +1,83 @@
+"""Train the learned preconditioner for the implicit cantilever on the GPU.
+
+Training pairs come from the implicit solver's own Jacobi-PCG solves on the
+1,728,000-particle cantilever (64^3-cell grid, 65^3 control points): for
+moduli E drawn log-uniformly from [1e6, 1e8] and seeded random loads, each
+system is solved twice and (residual, error) pairs are stored along the
+second solve (mpm_gpu_implicit_harvest).  The network is then trained with
+Adam by the library's own tensor-core forward and backward kernels
+(mpm_nn_train).  The result is written as raw FP32 parameters plus a JSON
+record of the run; bench.py and the tests load them through
+``load_weights``.
+
+    python -m mpm_gb300.train_precond            # 20,000 pairs, default schedule
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import time
+
+import numpy as np
+
+from . import capi, scenes
+
+WEIGHTS_DIR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "weights")
+WEIGHTS = os.path.join(WEIGHTS_DIR, "precond_cantilever64.f32")
+
+
+def load_weights(path=WEIGHTS):
+    """The committed parameters (FP32) or None."""
+    if not os.path.exists(path):
+        return None
+    p = np.fromfile(path, dtype=np.float32)
+    return p if p.size == capi.load().mpm_nn_num_params() else None
+
+
+def train(pairs=20000, loads_per_system=8, pairs_per_load=25, epochs=4, batch=8, lr=1.0e-3, seed=0,
+          harvest_eps=1.0e-20, scene=None, out=WEIGHTS, log=print):
+    s = scene if scene is not None else scenes.cantilever(iprop=1)
+    gpu = capi.GpuImplicitSolid(s, nr_flag=True)
+    per_system = loads_per_system * pairs_per_load
+    nsystems = max(1, math.ceil(pairs / per_system))
+    net = capi.PrecondNet(s.xynodec, max_batch=batch, max_pairs=pairs, seed=seed)
+    t0 = time.perf_counter()
+    gpu.harvest(net, nsystems, loads_per_system, pairs_per_load, 1.0e6, 1.0e8, seed=seed, eps=harvest_eps)
+    t1 = time.perf_counter()
+    n = net.num_pairs()
+    log(f"harvested {n} pairs from {nsystems} systems in {t1 - t0:.1f} s")
+    losses = net.train(epochs, batch, lr=lr, seed=seed)
+    t2 = time.perf_counter()
+    log(f"trained {epochs} epochs in {t2 - t1:.1f} s, loss per epoch {[round(float(x), 4) for x in losses]}")
+    params = net.params()
+    rec = {"scene": s.name, "particles": int(s.num), "nodes": list(s.xynodec), "pairs": int(n),
+           "systems": nsystems, "loads_per_system": loads_per_system, "pairs_per_load": pairs_per_load,
+           "moduli": [1.0e6, 1.0e8], "epochs": epochs, "batch": batch, "lr": lr, "seed": seed,
+           "harvest_eps": harvest_eps, "loss_per_epoch": [float(x) for x in losses],
+           "harvest_s": t1 - t0, "train_s": t2 - t1}
+    if out:
+        os.makedirs(os.path.dirname(out), exist_ok=True)
+        params.astype(np.float32).tofile(out)
+        with open(out + ".json", "w") as f:
+            json.dump(rec, f, indent=1)
+    net.close()
+    gpu.close()
+    return params, rec
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--pairs", type=int, default=20000)
+    ap.add_argument("--epochs", type=int, default=4)
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--lr", type=float, default=1.0e-3)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--out", default=WEIGHTS)
+    a = ap.parse_args()
+    train(pairs=a.pairs, epochs=a.epochs, batch=a.batch, lr=a.lr, seed=a.seed, out=a.out)
+
+
+if __name__ == "__main__":
+    main()

@@ -356,6 +356,26 @@ static void mat_neo_hookean(mo_ctx *c, double *sts, const double FF[3][3], const
     }
 }
 
+/* Weakly compressible Newtonian fluid (material model 2, no counterpart in
+ * the reference): Tait equation of state p = (rho0 c0^2 / gamma)((rho/rho0)^gamma - 1),
+ * rho = rho0 / J, rho0 = m / V0, and sigma = -p I + 2 mu dev(D) with
+ * D = sym(dF - I) / dt; mat_prop = {c0, gamma, mu}.  (rho/rho0)^gamma - 1 is
+ * evaluated as expm1(-gamma log1p(J - 1)). */
+static void mat_tait(mo_ctx *c, int p, double *sts, const double d[3][3], const double *mp) {
+    double c0 = mp[0], gam = mp[1], mu = mp[2];
+    double rho0 = c->mass[p] / c->vol0[p];
+    double pr = rho0 * c0 * c0 / gam * expm1(-gam * log1p(c->jac[p] - 1.0));
+    double inv_dt = 1.0 / c->dt;
+    double d0 = (d[0][0] - 1.0) * inv_dt, d1 = (d[1][1] - 1.0) * inv_dt, d2 = (d[2][2] - 1.0) * inv_dt;
+    double tr3 = (d0 + d1 + d2) / 3.0;
+    sts[0] = -pr + 2.0 * mu * (d0 - tr3);
+    sts[1] = -pr + 2.0 * mu * (d1 - tr3);
+    sts[2] = -pr + 2.0 * mu * (d2 - tr3);
+    sts[3] = mu * (d[1][2] + d[2][1]) * inv_dt;
+    sts[4] = mu * (d[0][2] + d[2][0]) * inv_dt;
+    sts[5] = mu * (d[0][1] + d[1][0]) * inv_dt;
+}
+
 /* ConstitutiveModel::UpdateStress dispatch, module/solid/constitutive_model.cpp:287-305 */
 static void update_stress(mo_ctx *c, int p, double *sts, const double FF[3][3], const double d[3][3], int implicit) {
     int mid = c->matid[p];
@@ -368,6 +388,8 @@ static void update_stress(mo_ctx *c, int p, double *sts, const double FF[3][3], 
         mat_lin_elast(c, sts, d, mp, implicit);
     } else if (model == 1) {
         mat_neo_hookean(c, sts, FF, mp, c->jac[p], c->jac[p], implicit);
+    } else if (model == 2 && !implicit) {
+        mat_tait(c, p, sts, d, mp);
     }
 }
 

@@ -86,3 +86,18 @@ def test_shape_functions_partition_of_unity():
         assert len(nc) == 18  # 3 x 2 x 3 nodes for idimc (2, 1, 2)
         assert abs(sf.sum() - 1.0) < 1e-13
         assert np.abs(dsf.sum(axis=0)).max() < 1e-9
+
+
+def test_tait_fluid_at_rest_without_gravity():
+    """Oracle known answer: a fluid column at rest with no body force keeps
+    J = 1, zero velocity and zero stress (shifting off: a uniform lattice)."""
+    from mpm_gb300 import scenes
+    from oracle import port
+
+    s = scenes.dam_break(grid=(8, 8, 8), cells=(4, 4, 4), npc=2, gravity=(0.0, 0.0, 0.0))
+    o = port.PortSolid(s, shifting=False)
+    o.steps(5)
+    q = o.particles()
+    assert np.abs(q["v"]).max() == 0.0
+    assert np.abs(q["sigma"]).max() == 0.0
+    assert np.allclose(q["vol"], s.vol0, rtol=0, atol=0)
