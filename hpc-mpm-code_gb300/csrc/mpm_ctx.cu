@@ -52,6 +52,8 @@ mpm_status check_launch(mpm_ctx *c) {
         }                                                                                                              \
     } while (0)
 
+void drop_graph(mpm_ctx *c);
+
 static void free_dev(void *p) {
     if (p) cudaFree(p);
 }
@@ -202,6 +204,7 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
 void mpm_gpu_destroy(mpm_ctx *c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    drop_graph(c);
     implicit_free(c);
     free_particles(c);
     free_dev(c->d_iprop);
@@ -402,11 +405,7 @@ mpm_status mpm_gpu_g2p(mpm_ctx *c) {
     return s;
 }
 
-mpm_status mpm_gpu_step_explicit(mpm_ctx *c, int nsteps, double facl) {
-    if (!c || nsteps < 0) return MPM_ERR_BAD_ARG;
-    if (c->num == 0) return MPM_ERR_STATE;
-    if (c->stage != 0) return MPM_ERR_STATE;
-    c->write_nodal_dl = false;
+static mpm_status eager_steps(mpm_ctx *c, int nsteps, double facl) {
     for (int s = 0; s < nsteps; s++) {
         mpm_status st = begin_step(c, facl);
         if (st != MPM_OK) return st;
@@ -415,6 +414,92 @@ mpm_status mpm_gpu_step_explicit(mpm_ctx *c, int nsteps, double facl) {
         c->step++;
         c->steps_since_sort++;
     }
+    return MPM_OK;
+}
+
+void drop_graph(mpm_ctx *c) {
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    c->graph_exec = nullptr;
+}
+
+// Captures G = 2 * resort_period fused steps, starting at a step with a
+// re-sort due and even step parity, into one executable graph.  Two re-sorts
+// per block leave the particle buffers where they were and an even step
+// count leaves the bound-slot parity unchanged, so the same graph replays
+// every block.  Launch configurations never depend on device data, so the
+// host-side bookkeeping of a replay is the same as that of the captured steps.
+static mpm_status capture_block(mpm_ctx *c, int G, double facl) {
+    drop_graph(c);
+    const int64_t l0 = c->launches;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    mpm_status st = eager_steps(c, G, facl);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (st != MPM_OK || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return st != MPM_OK ? st : MPM_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&c->graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        c->graph_exec = nullptr;
+        return MPM_ERR_CUDA;
+    }
+    c->graph_launches = c->launches - l0;
+    c->graph_facl = facl;
+    c->graph_stream = c->stream;
+    c->graph_tune[0] = c->tune.p2g_minb;
+    c->graph_tune[1] = c->tune.musl_minb;
+    c->graph_tune[2] = c->tune.update_ctas_per_sm;
+    c->graph_cur = c->cur;
+    c->graph_pbuf[0] = c->pbuf[0];
+    c->graph_pbuf[1] = c->pbuf[1];
+    // the captured steps have not run yet: the first launch runs them
+    CK(cudaGraphLaunch(c->graph_exec, c->stream));
+    c->graph_replays++;
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_step_explicit(mpm_ctx *c, int nsteps, double facl) {
+    if (!c || nsteps < 0) return MPM_ERR_BAD_ARG;
+    if (c->num == 0) return MPM_ERR_STATE;
+    if (c->stage != 0) return MPM_ERR_STATE;
+    c->write_nodal_dl = false;
+    const int G = 2 * c->resort_period;
+    if (!c->use_graph || c->stream == nullptr || c->timer.on || nsteps < 3 * G) return eager_steps(c, nsteps, facl);
+    int done = 0;
+    while (done < nsteps && !(c->steps_since_sort >= c->resort_period && (c->step & 1) == 0)) {
+        mpm_status st = eager_steps(c, 1, facl);
+        if (st != MPM_OK) return st;
+        done++;
+    }
+    if (c->graph_exec && (c->graph_facl != facl || c->graph_stream != c->stream ||
+                          c->graph_tune[0] != c->tune.p2g_minb || c->graph_tune[1] != c->tune.musl_minb ||
+                          c->graph_tune[2] != c->tune.update_ctas_per_sm || c->graph_cur != c->cur ||
+                          c->graph_pbuf[0] != c->pbuf[0] || c->graph_pbuf[1] != c->pbuf[1]))
+        drop_graph(c);
+    if (!c->graph_exec && nsteps - done >= G) {
+        mpm_status st = capture_block(c, G, facl);
+        if (st != MPM_OK) return st;
+        done += G;
+    }
+    while (c->graph_exec && nsteps - done >= G) {
+        CK(cudaGraphLaunch(c->graph_exec, c->stream));
+        c->step += G;
+        c->resorts += 2;
+        c->steps_since_sort = c->resort_period;
+        c->launches += c->graph_launches;
+        c->graph_replays++;
+        done += G;
+    }
+    return eager_steps(c, nsteps - done, facl);
+}
+
+mpm_status mpm_gpu_set_graph(mpm_ctx *c, int on) {
+    if (!c) return MPM_ERR_BAD_ARG;
+    c->use_graph = on != 0;
+    if (!c->use_graph) drop_graph(c);
     return MPM_OK;
 }
 

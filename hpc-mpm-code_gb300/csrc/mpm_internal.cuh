@@ -167,6 +167,16 @@ struct mpm_ctx {
     mpm_status latched = MPM_OK;
     mpm::KernelTimer timer;
     mpm::Tune tune;
+    // CUDA graph of 2 x resort_period fused explicit steps (mpm_gpu_step_explicit)
+    int use_graph = 1;
+    cudaGraphExec_t graph_exec = nullptr;
+    double graph_facl = 0.0;
+    cudaStream_t graph_stream = nullptr;
+    int graph_tune[3] = {0, 0, 0};
+    int graph_cur = 0;
+    void *graph_pbuf[2] = {nullptr, nullptr};
+    int64_t graph_launches = 0;
+    int64_t graph_replays = 0;
     struct ImpState *imp = nullptr;   // implicit solid state (mpm_implicit.cu)
     std::vector<int> bc_nodes[3];
     std::vector<double> bc_vals[3];

@@ -71,7 +71,8 @@ EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_s
            "mpm_gpu_implicit_matvec", "mpm_gpu_implicit_solve", "mpm_gpu_p2g_noalloc", "mpm_gpu_autotune",
            "mpm_gpu_get_tuning", "mpm_nn_num_params", "mpm_nn_create", "mpm_nn_destroy", "mpm_nn_set_stream",
            "mpm_nn_init_params", "mpm_nn_set_params", "mpm_nn_get_params", "mpm_nn_forward", "mpm_nn_backward",
-           "mpm_nn_num_pairs", "mpm_nn_train", "mpm_gpu_implicit_set_precond", "mpm_gpu_implicit_harvest"]
+           "mpm_nn_num_pairs", "mpm_nn_train", "mpm_gpu_implicit_set_precond", "mpm_gpu_implicit_harvest",
+           "mpm_gpu_set_graph"]
 
 
 def load(path: str | None = None):
@@ -103,6 +104,7 @@ def load(path: str | None = None):
     lib.mpm_gpu_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     lib.mpm_gpu_enable_kernel_timing.argtypes = [C.c_void_p, C.c_int]
     lib.mpm_gpu_autotune.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    lib.mpm_gpu_set_graph.argtypes = [C.c_void_p, C.c_int]
     lib.mpm_gpu_get_tuning.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.mpm_gpu_implicit_setup.argtypes = [C.c_void_p, C.c_int, C.c_double]
     lib.mpm_gpu_implicit_step.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int,
@@ -251,6 +253,10 @@ class GpuSolid:
         st = Stats()
         _chk(self.lib.mpm_gpu_get_stats(self.ctx, C.byref(st)), "mpm_gpu_get_stats")
         return {k: getattr(st, k) for k, _ in Stats._fields_}
+
+    def set_graph(self, on=True):
+        """Replay blocks of fused steps from a captured CUDA graph (default on)."""
+        _chk(self.lib.mpm_gpu_set_graph(self.ctx, int(on)), "mpm_gpu_set_graph")
 
     def autotune(self, steps_per_trial=5, facl=1.0):
         """Runs 3 x steps_per_trial explicit steps and keeps the fastest launch variants."""

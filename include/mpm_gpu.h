@@ -112,6 +112,11 @@ mpm_status mpm_gpu_p2g(mpm_ctx *ctx, double facl);
 mpm_status mpm_gpu_grid_update(mpm_ctx *ctx);
 mpm_status mpm_gpu_g2p(mpm_ctx *ctx);
 mpm_status mpm_gpu_step_explicit(mpm_ctx *ctx, int nsteps, double facl);
+/* No counterpart in the reference.  on (default): mpm_gpu_step_explicit on a
+ * non-default stream with at least 6 x resort_period steps replays blocks of
+ * 2 x resort_period steps from one captured CUDA graph (results are identical
+ * to launching the steps one by one); off: always launches kernel by kernel. */
+mpm_status mpm_gpu_set_graph(mpm_ctx *ctx, int on);
 
 /* ---- results ----------------------------------------------------------------
  * field: 0 nmass, 1 nvof, 2 nmome, 3 nforce, 4 nvel, 5 naccel, 6 nvol
