@@ -370,13 +370,16 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell(StepArgs<f
                 gu[1] += ax.w[i] * ay.dw[j] * wz * e;
                 gu[2] += wxy * dwz * e;
             }
-        // combine the two halves of the cell (a + b == b + a: both threads agree)
+        // combine the two halves of the cell (a + b == b + a: both threads agree).
+        // Only the cell's own two lanes take part: the other cells of the warp
+        // run different particle counts, so a full-warp mask would not converge.
+        const unsigned pair = 3u << ((threadIdx.x & 31) & ~1u);
         float v[3];
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-            const float other = __shfl_xor_sync(0xffffffffu, vs[d], 1);
+            const float other = __shfl_xor_sync(pair, vs[d], 1);
             v[d] = vs[d] + other;
-            gu[d] += __shfl_xor_sync(0xffffffffu, gu[d], 1);
+            gu[d] += __shfl_xor_sync(pair, gu[d], 1);
         }
         if (flip) {
 #pragma unroll

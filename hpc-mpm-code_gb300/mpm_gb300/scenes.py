@@ -226,3 +226,128 @@ def dam_break(grid=(256, 128, 128), dx=4.0e-3, cells=(128, 128, 96), npc=2, jitt
         nodes = np.concatenate([face_nodes(nn, axis, 0), face_nodes(nn, axis, nn[axis] - 1)])
         scene.bcs.append((comp, nodes, np.zeros(nodes.shape[0])))
     return scene
+
+
+@dataclass
+class Batch:
+    """Independent scenes packed into one grid (see ``pack_scenes``)."""
+    scene: Scene             # the packed scene run by one context
+    scenes: list             # the individual scenes, in their own coordinates
+    cell_offset: np.ndarray  # (n_scenes, 3) int: cell offset of each scene inside the packed grid
+    begin: np.ndarray        # (n_scenes,) first particle of each scene in the packed arrays
+    end: np.ndarray          # (n_scenes,) one past the last particle
+
+    def local(self, i, coord):
+        """Packed coordinates of scene i's particles -> the scene's own coordinates."""
+        s = self.scenes[i]
+        return coord - (np.asarray(self.cell_offset[i], dtype=np.float64) * np.asarray(s.dxy))[None, :]
+
+
+def batch_scenes(n_scenes=256, n_min=1.0e3, n_max=1.0e5, sizes=(32, 40, 48, 56, 64), dx=1.0e-2, npc=2,
+                 e_min=1.0e5, e_max=1.0e7, nu_min=0.2, nu_max=0.45, rho=1000.0, dt=1.0e-5, vel_sigma=0.5,
+                 gravity=(0.0, 0.0, -9.81), scheme=PIC, seed=12349):
+    """The batched workload: independent elastic blocks resting on a fixed floor.
+
+    Scene i: a grid of g^3 cells (g drawn from ``sizes``), a block of about
+    N_i particles at npc^3 per cell with N_i log-uniform in [n_min, n_max],
+    E log-uniform in [e_min, e_max], nu uniform in [nu_min, nu_max], seeded
+    N(0, vel_sigma^2) velocities, the bottom face (k = 0) fixed.  The block
+    sits on the floor at a random (x, y) position at least 2 cells from the
+    scene's sides.
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_scenes):
+        g = int(rng.choice(sizes))
+        n_target = float(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        cells = max(1.0, n_target / npc ** 3)
+        side = max(1, int(round(cells ** (1.0 / 3.0))))
+        bz = max(1, int(round(cells / (side * side))))
+        b = (min(side, g - 4), min(side, g - 4), min(bz, g - 4))
+        lo = (int(rng.integers(2, g - 2 - b[0] + 1)), int(rng.integers(2, g - 2 - b[1] + 1)), 0)
+        hi = tuple(lo[d] + b[d] for d in range(3))
+        dxy = (dx, dx, dx)
+        pts = block_particles(lo, hi, (0.0, 0.0, 0.0), dxy, (npc, npc, npc), 0.1, rng)
+        n = pts.shape[0]
+        vp = dx ** 3 / npc ** 3
+        E = float(np.exp(rng.uniform(np.log(e_min), np.log(e_max))))
+        nu = float(rng.uniform(nu_min, nu_max))
+        s = Scene(xyelem=(g, g, g), xymin=(0.0, 0.0, 0.0), dxy=dxy, idimc=(1, 1, 1), npxye=(npc, npc, npc),
+                  dt=dt, mtol=1.0e-12, gravity=tuple(gravity), iprop=np.array([0], dtype=np.int32),
+                  mat_prop=np.array([[E, nu, 0.0]]), coord=pts, vel=rng.normal(0.0, vel_sigma, size=(n, 3)),
+                  mass=np.full(n, rho * vp), vol0=np.full(n, vp), matid=np.zeros(n, dtype=np.int32),
+                  scheme=scheme, name=f"batch_scene_{i}")
+        nodes = face_nodes(s.xynodec, 2, 0)
+        for comp in (BC_U, BC_V, BC_W):
+            s.bcs.append((comp, nodes, np.zeros(nodes.shape[0])))
+        out.append(s)
+    return out
+
+
+def pack_scenes(scenes, gap=2):
+    """Pack independent scenes (same dx, dt, gravity, scheme, linear shape
+    functions) into one grid so that one context advances all of them with
+    one launch per kernel.  Scenes are placed by shelf packing (rows along x,
+    rows of rows along y, layers along z) with ``gap`` empty cells between
+    neighbours, so no control point is shared and no scene's particles can
+    reach another's nodes.  Each scene gets its own material (matid = scene
+    index).  Particle-shifting sums are global in a context, so batched runs
+    use shifting off."""
+    s0 = scenes[0]
+    for s in scenes:
+        assert s.dxy == s0.dxy and s.dt == s0.dt and s.gravity == s0.gravity and s.scheme == s0.scheme
+        assert tuple(s.idimc) == (1, 1, 1)
+    ext = np.array([s.xyelem for s in scenes], dtype=np.int64) + gap
+    order = np.argsort(-ext.max(axis=1), kind="stable")
+    side = int(np.ceil(1.15 * float((ext.prod(axis=1)).sum()) ** (1.0 / 3.0)))
+    offs = np.zeros((len(scenes), 3), dtype=np.int64)
+    x = y = z = 0
+    row_h = layer_h = 0
+    width = depth = 0
+    for i in order:
+        ex, ey, ez = ext[i]
+        if x + ex > side and x > 0:            # next row
+            x, y = 0, y + row_h
+            row_h = 0
+        if y + ey > side and y > 0:            # next layer
+            x, y, z = 0, 0, z + layer_h
+            row_h = layer_h = 0
+        offs[i] = (x, y, z)
+        x += ex
+        row_h = max(row_h, ey)
+        layer_h = max(layer_h, ez)
+        width, depth = max(width, x), max(depth, y + row_h)
+    height = z + layer_h
+    grid = (int(width), int(depth), int(height))
+    nn = (grid[0] + 1, grid[1] + 1, grid[2] + 1)
+    coords, vels, mass, vol0, matid = [], [], [], [], []
+    begin, end = [], []
+    bcs = {BC_U: [], BC_V: [], BC_W: []}
+    n0 = 0
+    for i, s in enumerate(scenes):
+        shift = offs[i] * np.asarray(s.dxy)
+        coords.append(s.coord + shift[None, :])
+        vels.append(s.vel)
+        mass.append(s.mass)
+        vol0.append(s.vol0)
+        matid.append(np.full(s.num, i, dtype=np.int32))
+        begin.append(n0)
+        n0 += s.num
+        end.append(n0)
+        snx, sny, _ = s.xynodec
+        for comp, nodes, vals in s.bcs:
+            i_, j_, k_ = nodes % snx, (nodes // snx) % sny, nodes // (snx * sny)
+            g = (i_ + offs[i][0]) + nn[0] * ((j_ + offs[i][1]) + nn[1] * (k_ + offs[i][2]))
+            bcs[comp].append((g.astype(np.int32), vals))
+    packed = Scene(xyelem=grid, xymin=s0.xymin, dxy=s0.dxy, idimc=(1, 1, 1), npxye=s0.npxye, dt=s0.dt,
+                   mtol=s0.mtol, gravity=s0.gravity,
+                   iprop=np.concatenate([s.iprop[:1] for s in scenes]).astype(np.int32),
+                   mat_prop=np.concatenate([s.mat_prop[:1] for s in scenes]),
+                   coord=np.concatenate(coords), vel=np.concatenate(vels), mass=np.concatenate(mass),
+                   vol0=np.concatenate(vol0), matid=np.concatenate(matid), scheme=s0.scheme,
+                   name=f"batch_of_{len(scenes)}")
+    for comp in (BC_U, BC_V, BC_W):
+        if bcs[comp]:
+            packed.bcs.append((comp, np.concatenate([b[0] for b in bcs[comp]]),
+                               np.concatenate([b[1] for b in bcs[comp]])))
+    return Batch(scene=packed, scenes=list(scenes), cell_offset=offs, begin=np.array(begin), end=np.array(end))
