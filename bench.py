@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batched-steps", type=int, default=100,
+                    help="steps of the 256-scene batched workload (0 skips)")
+    ap.add_argument("--fluid-steps", type=int, default=100,
+                    help="steps of the 12.6M-particle Tait dam break (0 skips)")
     ap.add_argument("--train-pairs", type=int, default=2000,
                     help="training pairs when no committed preconditioner parameters exist")
     ap.add_argument("--implicit-steps", type=int, default=3,
@@ -272,6 +276,66 @@ def run_implicit(args, torch, stream):
     return out
 
 
+def timed_steps(torch, stream, gpu, steps):
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    gpu.steps(steps)
+    ev1.record(stream)
+    ev1.synchronize()
+    return ev0.elapsed_time(ev1)
+
+
+def run_batched(args, torch, stream, hbm_peak):
+    """256 independent elastic scenes (log-uniform 1e3..1e5 particles, grids 32^3..64^3,
+    E log-uniform 1e5..1e7) packed into one grid and advanced by one context: one
+    launch per kernel and step for all scenes, blocks of steps replayed from a CUDA
+    graph, launch variants picked by the autotuner.  FP32, shifting off."""
+    from mpm_gb300 import capi, scenes
+
+    b = scenes.pack_scenes(scenes.batch_scenes())
+    s = b.scene
+    gpu = capi.GpuSolid(s, precision=32, shifting=False, stream=stream.cuda_stream)
+    tune = gpu.autotune(3)
+    gpu.steps(args.warmup)
+    gpu.sync()
+    ms = timed_steps(torch, stream, gpu, args.batched_steps)
+    gpu.sync()
+    gpu.close()
+    ms_step = ms / args.batched_steps
+    nodes = int(sum(sc.nodec for sc in b.scenes))
+    alg = algorithmic_bytes(s.num, nodes)
+    return {"metric": METRIC, "value": s.num * args.batched_steps / (ms * 1e-3), "unit": METRIC,
+            "ms_per_step": ms_step, "steps": args.batched_steps, "scenes": len(b.scenes), "particles": s.num,
+            "scene_nodes": nodes, "packed_grid": list(s.xyelem), "dtype": "f32", "tuning": tune,
+            "roofline": {"bound": "hbm", "achieved": alg / (ms_step * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": alg / (ms_step * 1e-3) / 1e9 / hbm_peak,
+                         "algorithmic_bytes_per_step": alg}}
+
+
+def run_fluid(args, torch, stream, hbm_peak):
+    """Tait-fluid dam break: 12,582,912 particles (128x128x96-cell column at 8 per cell)
+    in a 256x128x128-cell box, dx = 4e-3 m, c0 = 30 m/s, gamma = 7, mu = 1e-3 Pa s,
+    slip walls, dt = 5e-6 s, FP32."""
+    from mpm_gb300 import capi, scenes
+
+    s = scenes.dam_break()
+    gpu = capi.GpuSolid(s, precision=32, stream=stream.cuda_stream)
+    gpu.steps(args.warmup)
+    gpu.sync()
+    ms = timed_steps(torch, stream, gpu, args.fluid_steps)
+    gpu.sync()
+    gpu.close()
+    ms_step = ms / args.fluid_steps
+    alg = s.num * 64 + s.nodec * 56    # read x3 v3 m V0 J, write x3 v3 J; 7 nodal words written + read
+    return {"metric": METRIC, "value": s.num * args.fluid_steps / (ms * 1e-3), "unit": METRIC,
+            "ms_per_step": ms_step, "steps": args.fluid_steps, "particles": s.num, "grid": list(s.xyelem),
+            "dtype": "f32",
+            "roofline": {"bound": "hbm", "achieved": alg / (ms_step * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": alg / (ms_step * 1e-3) / 1e9 / hbm_peak, "algorithmic_bytes_per_step": alg,
+                         "note": "fluid formula N_p*64 + N_n*56; the generic solid kernels also move F and stress"}}
+
+
 def run_gb300(args):
     import torch
 
@@ -372,6 +436,18 @@ def run_gb300(args):
         except Exception as exc:   # reported, never required
             implicit = {"metric": "implicit step time", "value": None, "error": str(exc)}
 
+    batched = fluid = None
+    if args.batched_steps > 0:
+        try:
+            batched = run_batched(args, torch, stream, hbm_peak)
+        except Exception as exc:
+            batched = {"metric": METRIC, "value": None, "error": str(exc)}
+    if args.fluid_steps > 0:
+        try:
+            fluid = run_fluid(args, torch, stream, hbm_peak)
+        except Exception as exc:
+            fluid = {"metric": METRIC, "value": None, "error": str(exc)}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -388,7 +464,8 @@ def run_gb300(args):
                            "dt": s.dt, "scheme": "PIC", "parallelism": f"replicas x{world}",
                            "l2": "inputs larger than L2: 393 MB particle state per step, no flush"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(),
-                "gpu_launches": int(launches), "kernels": kernels, "implicit": implicit}
+                "gpu_launches": int(launches), "kernels": kernels, "implicit": implicit,
+                "batched": batched, "fluid": fluid}
         print(json.dumps(line), flush=True)
     gpu.close()
     if world > 1:

@@ -833,6 +833,12 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
     if (!c) return MPM_ERR_BAD_ARG;
     if (c->nreal != 27 || c->precision != 64) return MPM_ERR_UNSUPPORTED;
     if (c->g.order[0] != 1 || c->g.order[1] != 1 || c->g.order[2] != 1) return MPM_ERR_UNSUPPORTED;
+    {
+        std::vector<int> ip(c->nmat);
+        CKI(cudaMemcpy(ip.data(), c->d_iprop, sizeof(int) * c->nmat, cudaMemcpyDeviceToHost));
+        for (int m : ip)
+            if (m > 1) return MPM_ERR_UNSUPPORTED;   // no tangent for the fluid model
+    }
     implicit_free(c);
     ImpState *s = new ImpState();
     c->imp = s;

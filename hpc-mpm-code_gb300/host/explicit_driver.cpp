@@ -63,7 +63,7 @@ int main(int argc, char **argv) {
             vz += sp.vel[q][2];
             z += sp.coord[q][2];
         }
-        std::printf("particles %d steps %d mean_vz %.9e mean_z %.9e\n", n, nsteps, vz / n, z / n);
+        std::printf("particles %d steps %d mean_vz %.17e mean_z %.17e\n", n, nsteps, vz / n, z / n);
     } catch (const mpmgpu::Error &e) {
         std::fprintf(stderr, "explicit_driver: %s\n", e.what());
         return 2;

@@ -59,7 +59,11 @@ typedef struct {
 } mpm_grid_desc;
 
 /* Material table: iprop[nmat] (-1 rigid, 0 linear elastic, 1 Neo-Hookean)
- * and mat_prop[3*nmat] = {E, nu, spare} (module/dataset.h:13-14). */
+ * and mat_prop[3*nmat] = {E, nu, spare} (module/dataset.h:13-14).
+ * iprop 2 (no counterpart in the reference, explicit contexts only): a weakly
+ * compressible Newtonian fluid with the Tait equation of state,
+ * mat_prop = {c0 (speed of sound), gamma, mu (dynamic viscosity)}; the rest
+ * density is each particle's mass / vol0. */
 typedef struct {
     int nmat;
     const int *iprop;

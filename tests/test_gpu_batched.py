@@ -4,7 +4,9 @@ the oracle run of that scene alone (shifting off, as batched runs use it).
 
 * FP64: relative L2 <= 1e-10 per scene on x, v, sigma after 30 steps -- the
   packing introduces no coupling between scenes.
-* FP32: per scene x <= 1e-6, v <= 1e-4, sigma <= 2e-3.
+* FP32: per scene x <= 3e-6, v <= 1e-4, sigma <= 2e-3.  Positions live in
+  the packed grid's coordinates, whose FP32 spacing is coarser than in a
+  scene's own coordinates, hence the looser x bound than for single scenes.
 """
 import numpy as np
 import pytest
@@ -24,7 +26,7 @@ def _batch():
 
 
 @pytest.mark.parametrize("prec,tol", [(64, {"x": 1e-10, "v": 1e-10, "sigma": 1e-10}),
-                                      (32, {"x": 1e-6, "v": 1e-4, "sigma": 2e-3})])
+                                      (32, {"x": 3e-6, "v": 1e-4, "sigma": 2e-3})])
 def test_packed_scenes_match_single_runs(prec, tol):
     b = _batch()
     gpu = capi.GpuSolid(b.scene, precision=prec, shifting=False)
