@@ -13,7 +13,8 @@ using namespace mpm;
 namespace mpm {
 
 static const char *kClassNames[NKCLASS] = {"bin",  "scan", "scatter", "permute", "p2g",    "grid1",
-                                           "g2p_musl", "grid2", "g2p_update", "misc", "matvec", "krylov"};
+                                           "g2p_musl", "grid2", "g2p_update", "misc", "matvec", "krylov",
+                                           "assemble", "precond_nn"};
 
 void timer_begin(mpm_ctx *c, int cls) {
     if (!c->timer.on) return;
@@ -452,6 +453,8 @@ static mpm_status capture_block(mpm_ctx *c, int G, double facl) {
     c->graph_tune[0] = c->tune.p2g_minb;
     c->graph_tune[1] = c->tune.musl_minb;
     c->graph_tune[2] = c->tune.update_ctas_per_sm;
+    c->graph_tune[3] = c->tune.p2g_staged;
+    c->graph_tune[4] = c->tune.musl_staged;
     c->graph_cur = c->cur;
     c->graph_pbuf[0] = c->pbuf[0];
     c->graph_pbuf[1] = c->pbuf[1];
@@ -476,7 +479,9 @@ mpm_status mpm_gpu_step_explicit(mpm_ctx *c, int nsteps, double facl) {
     }
     if (c->graph_exec && (c->graph_facl != facl || c->graph_stream != c->stream ||
                           c->graph_tune[0] != c->tune.p2g_minb || c->graph_tune[1] != c->tune.musl_minb ||
-                          c->graph_tune[2] != c->tune.update_ctas_per_sm || c->graph_cur != c->cur ||
+                          c->graph_tune[2] != c->tune.update_ctas_per_sm || c->graph_tune[3] != c->tune.p2g_staged ||
+                          c->graph_tune[4] != c->tune.musl_staged ||
+                          c->graph_cur != c->cur ||
                           c->graph_pbuf[0] != c->pbuf[0] || c->graph_pbuf[1] != c->pbuf[1]))
         drop_graph(c);
     if (!c->graph_exec && nsteps - done >= G) {
@@ -706,13 +711,16 @@ mpm_status mpm_gpu_autotune(mpm_ctx *c, int steps_per_trial, double facl) {
     if (c->num == 0 || c->stage != 0) return MPM_ERR_STATE;
     // every candidate computes bitwise the same step, so the trial steps are
     // ordinary simulation steps; each kernel class is timed on its own
-    const int p2g_opts[3] = {2, 3, 2}, musl_opts[3] = {3, 2, 3}, upd_opts[3] = {4, 3, 6};
+    const int p2g_opts[3] = {2, 3, 2}, stg_opts[3] = {1, 0, 0}, musl_opts[3] = {3, 2, 3}, mstg_opts[3] = {1, 0, 0};
+    const int upd_opts[3] = {4, 3, 6};
     double best[3] = {1e300, 1e300, 1e300};
     Tune pick = c->tune;
     const bool was_on = c->timer.on;
     for (int t = 0; t < 3; t++) {
         c->tune.p2g_minb = p2g_opts[t];
+        c->tune.p2g_staged = stg_opts[t];
         c->tune.musl_minb = musl_opts[t];
+        c->tune.musl_staged = mstg_opts[t];
         c->tune.update_ctas_per_sm = upd_opts[t];
         int cnt = NKCLASS;
         const char *names[NKCLASS];
@@ -726,8 +734,16 @@ mpm_status mpm_gpu_autotune(mpm_ctx *c, int steps_per_trial, double facl) {
         cnt = NKCLASS;
         st = mpm_gpu_kernel_times(c, &cnt, names, ms, nl);
         if (st != MPM_OK) return st;
-        if (ms[K_P2G] < best[0]) { best[0] = ms[K_P2G]; pick.p2g_minb = p2g_opts[t]; }
-        if (ms[K_G2P_MUSL] < best[1]) { best[1] = ms[K_G2P_MUSL]; pick.musl_minb = musl_opts[t]; }
+        if (ms[K_P2G] < best[0]) {
+            best[0] = ms[K_P2G];
+            pick.p2g_minb = p2g_opts[t];
+            pick.p2g_staged = stg_opts[t];
+        }
+        if (ms[K_G2P_MUSL] < best[1]) {
+            best[1] = ms[K_G2P_MUSL];
+            pick.musl_minb = musl_opts[t];
+            pick.musl_staged = mstg_opts[t];
+        }
         if (ms[K_G2P_UPDATE] < best[2]) { best[2] = ms[K_G2P_UPDATE]; pick.update_ctas_per_sm = upd_opts[t]; }
     }
     pick.done = true;
@@ -735,10 +751,23 @@ mpm_status mpm_gpu_autotune(mpm_ctx *c, int steps_per_trial, double facl) {
     return MPM_OK;
 }
 
+mpm_status mpm_gpu_set_tuning(mpm_ctx *c, int p2g_minb, int musl_minb, int update_ctas_per_sm) {
+    if (!c) return MPM_ERR_BAD_ARG;
+    if ((p2g_minb != 0 && p2g_minb != 2 && p2g_minb != 3) || (musl_minb != 0 && musl_minb != 2 && musl_minb != 3) ||
+        update_ctas_per_sm < 1 || update_ctas_per_sm > 8)
+        return MPM_ERR_BAD_ARG;
+    c->tune.p2g_staged = p2g_minb == 0;
+    if (p2g_minb) c->tune.p2g_minb = p2g_minb;
+    c->tune.musl_staged = musl_minb == 0;
+    if (musl_minb) c->tune.musl_minb = musl_minb;
+    c->tune.update_ctas_per_sm = update_ctas_per_sm;
+    return MPM_OK;
+}
+
 mpm_status mpm_gpu_get_tuning(mpm_ctx *c, int *p2g_minb, int *musl_minb, int *update_ctas_per_sm) {
     if (!c) return MPM_ERR_BAD_ARG;
-    if (p2g_minb) *p2g_minb = c->tune.p2g_minb;
-    if (musl_minb) *musl_minb = c->tune.musl_minb;
+    if (p2g_minb) *p2g_minb = c->tune.p2g_staged ? 0 : c->tune.p2g_minb;
+    if (musl_minb) *musl_minb = c->tune.musl_staged ? 0 : c->tune.musl_minb;
     if (update_ctas_per_sm) *update_ctas_per_sm = c->tune.update_ctas_per_sm;
     return MPM_OK;
 }

@@ -182,76 +182,62 @@ __device__ __forceinline__ void brick_origin(int b, const int *nb, int &ox, int 
 constexpr int CELL_SPLIT = 2;
 constexpr int CELL_THREADS = BRC * CELL_SPLIT;
 
-template <int MINB>
-__global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell(StepArgs<float> a) {
-    __shared__ float corner[NACC * 8][BRC];       // 32 KB
-    __shared__ Scales S;
-    __shared__ int sh_red[32];
-    const int b = blockIdx.x;
-    const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
-    const int *cs = a.cstart + (size_t)b * (BRC + 1);
-    if (cs[0] == cs[BRC]) return;   // empty brick (uniform across the CTA)
-    int ox, oy, oz;
-    brick_origin(b, a.nbrick, ox, oy, oz);
-    const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
-    const int p0 = cs[lc], p1 = cs[lc + 1];
-    load_scales(a, S);
-    const float fxg = a.grav[0] * a.facl, fyg = a.grav[1] * a.facl, fzg = a.grav[2] * a.facl;
-    const Particles<float> &P = a.P;
-    float acc[NACC][4];
-#pragma unroll
-    for (int f = 0; f < NACC; f++)
-#pragma unroll
-        for (int c = 0; c < 4; c++) acc[f][c] = 0.0f;
-    int misses = 0, oobs = 0;
-    for (int p = p0; p < p1; p++) {
-        const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
-        bool oob = false;
-        const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
-        oobs += oob && h == 0;
-        Axis<float, 1> ax, ay, az;
-        axis_eval<float, 1>(x0, a.g, 0, px, ax);
-        axis_eval<float, 1>(x1, a.g, 1, py, ay);
-        axis_eval<float, 1>(x2, a.g, 2, pz, az);
-        const float m = ld(P.m + p), vol = ld(P.vol + p);
-        const float v[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
-        const float s[6] = {ld(P.s[0] + p), ld(P.s[1] + p), ld(P.s[2] + p),
-                            ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
-        const float mfx = m * fxg, mfy = m * fyg, mfz = m * fzg;
-        const bool mine = (px == cx) && (py == cy) && (pz == cz);
-        const float wz = h ? az.w[1] : az.w[0], dwz = h ? az.dw[1] : az.dw[0];
-        if (!mine) {
-            // a particle that left its sorted cell scatters on its own
-            misses += h == 0;
+// One particle of a cell's P2G: FP32 register sums of the four corners of
+// z-layer h, or (a particle that left its sorted cell) its own fixed-point
+// atomics.
+__device__ __forceinline__ void p2g_particle(const StepArgs<float> &a, const Scales &S, int cx, int cy, int cz, int h,
+                                             float x0, float x1, float x2, float m, float vol, const float *v,
+                                             const float *s, float fxg, float fyg, float fzg, float (*acc)[4],
+                                             int &misses, int &oobs) {
+    bool oob = false;
+    const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
+    oobs += oob && h == 0;
+    Axis<float, 1> ax, ay, az;
+    axis_eval<float, 1>(x0, a.g, 0, px, ax);
+    axis_eval<float, 1>(x1, a.g, 1, py, ay);
+    axis_eval<float, 1>(x2, a.g, 2, pz, az);
+    const float mfx = m * fxg, mfy = m * fyg, mfz = m * fzg;
+    const bool mine = (px == cx) && (py == cy) && (pz == cz);
+    const float wz = h ? az.w[1] : az.w[0], dwz = h ? az.dw[1] : az.dw[0];
+    if (!mine) {
+        // a particle that left its sorted cell scatters on its own
+        misses += h == 0;
 #pragma unroll 1
-            for (int c = 0; c < 4; c++) {
-                const int i = c & 1, j = c >> 1;
-                const float wxy = ax.w[i] * ay.w[j];
-                float q[NACC];
-                p2g_terms(wxy * wz, ax.dw[i] * ay.w[j] * wz, ax.w[i] * ay.dw[j] * wz, wxy * dwz, m, vol, v, s, mfx,
-                          mfy, mfz, q);
-                long long o[NACC];
-                fx_terms(q, S, o);
-                const size_t gn = node_id(a.g, px + i, py + j, pz + h);
-                for (int f = 0; f < NACC; f++)
-                    if (o[f]) atomic_add_i64(&a.acc[(size_t)f * a.g.nodec + gn], o[f]);
-                a.tileflag[tile_of_node(a.g, px + i, py + j, pz + h)] = 1;
-            }
-            continue;
+        for (int c = 0; c < 4; c++) {
+            const int i = c & 1, j = c >> 1;
+            const float wxy = ax.w[i] * ay.w[j];
+            float q[NACC];
+            p2g_terms(wxy * wz, ax.dw[i] * ay.w[j] * wz, ax.w[i] * ay.dw[j] * wz, wxy * dwz, m, vol, v, s, mfx, mfy,
+                      mfz, q);
+            long long o[NACC];
+            fx_terms(q, S, o);
+            const size_t gn = node_id(a.g, px + i, py + j, pz + h);
+            for (int f = 0; f < NACC; f++)
+                if (o[f]) atomic_add_i64(&a.acc[(size_t)f * a.g.nodec + gn], o[f]);
+            a.tileflag[tile_of_node(a.g, px + i, py + j, pz + h)] = 1;
         }
-#pragma unroll
-        for (int j = 0; j < 2; j++)
-#pragma unroll
-            for (int i = 0; i < 2; i++) {
-                const float wxy = ax.w[i] * ay.w[j];
-                float q[NACC];
-                p2g_terms(wxy * wz, ax.dw[i] * ay.w[j] * wz, ax.w[i] * ay.dw[j] * wz, wxy * dwz, m, vol, v, s, mfx,
-                          mfy, mfz, q);
-                const int c = i + 2 * j;
-#pragma unroll
-                for (int f = 0; f < NACC; f++) acc[f][c] += q[f];
-            }
+        return;
     }
+#pragma unroll
+    for (int j = 0; j < 2; j++)
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const float wxy = ax.w[i] * ay.w[j];
+            float q[NACC];
+            p2g_terms(wxy * wz, ax.dw[i] * ay.w[j] * wz, ax.w[i] * ay.dw[j] * wz, wxy * dwz, m, vol, v, s, mfx, mfy,
+                      mfz, q);
+            const int c = i + 2 * j;
+#pragma unroll
+            for (int f = 0; f < NACC; f++) acc[f][c] += q[f];
+        }
+}
+
+// The end of a cell-P2G CTA: corners to shared memory, counters, and the
+// node pass: each node of the (BRX+1)(BRY+1)(BRZ+1) box adds the corners of
+// its adjacent cells in a fixed order and issues one int64 RED per field.
+__device__ __forceinline__ void p2g_node_pass(const StepArgs<float> &a, const Scales &S, float (*corner)[BRC],
+                                              int *sh_red, int lc, int h, int ox, int oy, int oz,
+                                              const float (*acc)[4], int misses, int oobs) {
 #pragma unroll
     for (int f = 0; f < NACC; f++)
 #pragma unroll
@@ -262,8 +248,6 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell(StepArgs<float>
         if (tot >> 16) atomicAdd(&a.ctl->err_oob, (unsigned)(tot >> 16));
     }
     __syncthreads();
-    // node pass: each node of the (BRX+1)(BRY+1)(BRZ+1) box adds the corners of
-    // its adjacent cells in a fixed order
     constexpr int NX = BRX + 1, NY = BRY + 1, NZ = BRZ + 1, NB = NX * NY * NZ;
     for (int it = threadIdx.x; it < NB * NACC; it += CELL_THREADS) {
         const int f = it / NB, n = it % NB;
@@ -292,128 +276,242 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell(StepArgs<float>
 }
 
 template <int MINB>
-__global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell(StepArgs<float> a) {
-    __shared__ float corner[3 * 8][BRC];
+__global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell(StepArgs<float> a) {
+    __shared__ float corner[NACC * 8][BRC];       // 32 KB
     __shared__ Scales S;
-    __shared__ long long sh_l[32];
-    __shared__ float sh_f[32];
+    __shared__ int sh_red[32];
     const int b = blockIdx.x;
     const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
     const int *cs = a.cstart + (size_t)b * (BRC + 1);
-    if (cs[0] == cs[BRC]) return;
+    if (cs[0] == cs[BRC]) return;   // empty brick (uniform across the CTA)
     int ox, oy, oz;
     brick_origin(b, a.nbrick, ox, oy, oz);
     const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
     const int p0 = cs[lc], p1 = cs[lc + 1];
     load_scales(a, S);
-    const size_t N = (size_t)a.g.nodec;
+    const float fxg = a.grav[0] * a.facl, fyg = a.grav[1] * a.facl, fzg = a.grav[2] * a.facl;
     const Particles<float> &P = a.P;
-    const bool flip = (a.scheme == MPM_FLIP);
-    // the gather fields of this cell's four nodes of z-layer h, loaded once
-    float Gc[3][4], Ec[4];
+    float acc[NACC][4];
+#pragma unroll
+    for (int f = 0; f < NACC; f++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[f][c] = 0.0f;
+    int misses = 0, oobs = 0;
+    for (int p = p0; p < p1; p++) {
+        const float v[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
+        const float s[6] = {ld(P.s[0] + p), ld(P.s[1] + p), ld(P.s[2] + p),
+                            ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
+        p2g_particle(a, S, cx, cy, cz, h, ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p), ld(P.m + p),
+                     ld(P.vol + p), v, s, fxg, fyg, fzg, acc, misses, oobs);
+    }
+    p2g_node_pass(a, S, corner, sh_red, lc, h, ox, oy, oz, acc, misses, oobs);
+}
+
+// The same P2G with the brick's particles brought into shared memory by
+// bulk asynchronous copies (TMA, 1-D): the brick's particles are one
+// contiguous range (sorted by brick, then cell), copied in chunks of PCH
+// particles per field, two chunks in flight.  Each thread then reads its
+// cell's particles from shared memory in the same order as k_p2g_cell, so
+// both kernels give bitwise the same sums.
+constexpr int PCH = 512;                     // particles per staged chunk
+constexpr int PNF = 14;                      // x 3, v 3, sigma 6, m, vol
+constexpr int PST = PCH + 8;                 // floats per field in a stage (16-byte alignment slack)
+constexpr size_t PSTAGE = (size_t)PNF * PST * 4;
+
+template <int MINB>
+__global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_staged(StepArgs<float> a) {
+    extern __shared__ __align__(128) unsigned char dsm[];
+    __shared__ float corner[NACC * 8][BRC];       // 32 KB
+    __shared__ Scales S;
+    __shared__ int sh_red[32];
+    __shared__ __align__(8) unsigned long long bar[2];
+    const int b = blockIdx.x;
+    const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
+    const int *cs = a.cstart + (size_t)b * (BRC + 1);
+    const int P0 = cs[0], P1 = cs[BRC];
+    if (P0 == P1) return;   // empty brick (uniform across the CTA)
+    const Particles<float> &P = a.P;
+    const float *src[PNF] = {P.x[0], P.x[1], P.x[2], P.v[0], P.v[1], P.v[2], P.s[0],
+                             P.s[1], P.s[2], P.s[3], P.s[4], P.s[5], P.m,    P.vol};
+    const int nch = (P1 - P0 + PCH - 1) / PCH;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](int k) {
+        const int st = k & 1;
+        const int c0 = P0 + k * PCH, c1 = min(c0 + PCH, P1);
+        const int a0 = c0 & ~3, a1 = (c1 + 3) & ~3;
+        const unsigned bytes = (unsigned)(a1 - a0) * 4u;
+        float *dst = reinterpret_cast<float *>(dsm + st * PSTAGE);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&bar[st], bytes * PNF);
+        for (int f = 0; f < PNF; f++) bulk_g2s(dst + f * PST, src[f] + a0, bytes, &bar[st]);
+    };
+    if (threadIdx.x == 0) issue(0);
+    int ox, oy, oz;
+    brick_origin(b, a.nbrick, ox, oy, oz);
+    const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
+    const int p0 = cs[lc], p1 = cs[lc + 1];
+    load_scales(a, S);
+    const float fxg = a.grav[0] * a.facl, fyg = a.grav[1] * a.facl, fzg = a.grav[2] * a.facl;
+    float acc[NACC][4];
+#pragma unroll
+    for (int f = 0; f < NACC; f++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[f][c] = 0.0f;
+    int misses = 0, oobs = 0;
+    for (int k = 0; k < nch; k++) {
+        const int st = k & 1;
+        if (threadIdx.x == 0 && k + 1 < nch) issue(k + 1);
+        const bool ok = mbar_wait_bounded(&bar[st], (unsigned)((k >> 1) & 1), 1u << 22);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                atomicAdd(&a.ctl->err_timeout, 1u);
+                if (k + 1 < nch) mbar_wait_bounded(&bar[st ^ 1], (unsigned)(((k + 1) >> 1) & 1), 1u << 22);
+            }
+            __syncthreads();
+            return;
+        }
+        const int c0 = P0 + k * PCH, c1 = min(c0 + PCH, P1);
+        const int a0 = c0 & ~3;
+        const float *sf = reinterpret_cast<const float *>(dsm + st * PSTAGE);
+        const int q0 = max(p0, c0), q1 = min(p1, c1);
+        for (int p = q0; p < q1; p++) {
+            const int l = p - a0;
+            const float v[3] = {sf[3 * PST + l], sf[4 * PST + l], sf[5 * PST + l]};
+            const float s[6] = {sf[6 * PST + l], sf[7 * PST + l], sf[8 * PST + l],
+                                sf[9 * PST + l], sf[10 * PST + l], sf[11 * PST + l]};
+            p2g_particle(a, S, cx, cy, cz, h, sf[l], sf[PST + l], sf[2 * PST + l], sf[12 * PST + l],
+                         sf[13 * PST + l], v, s, fxg, fyg, fzg, acc, misses, oobs);
+        }
+        __syncthreads();   // the stage is refilled only after every thread has read it
+    }
+    p2g_node_pass(a, S, corner, sh_red, lc, h, ox, oy, oz, acc, misses, oobs);
+}
+// Per-thread gather fields of the cell's four nodes of z-layer h, loaded once.
+struct MuslCell {
+    float G[3][4], E[4];
+};
+
+__device__ __forceinline__ void musl_load_cell(const StepArgs<float> &a, int cx, int cy, int cz, int h, bool any,
+                                               MuslCell &C) {
+    const size_t N = (size_t)a.g.nodec;
 #pragma unroll
     for (int j = 0; j < 2; j++)
 #pragma unroll
         for (int i = 0; i < 2; i++) {
             const int c = i + 2 * j;
-            if (p1 > p0) {
+            if (any) {
                 const int gx = min(cx + i, a.g.nnc[0] - 1), gy = min(cy + j, a.g.nnc[1] - 1),
                           gz = min(cz + h, a.g.nnc[2] - 1);
                 const size_t gn = node_id(a.g, gx, gy, gz);
 #pragma unroll
-                for (int d = 0; d < 3; d++) Gc[d][c] = ld(a.G + d * N + gn);
-                Ec[c] = ld(a.nei + gn);
+                for (int d = 0; d < 3; d++) C.G[d][c] = ld(a.G + d * N + gn);
+                C.E[c] = ld(a.nei + gn);
             } else {
-                Gc[0][c] = Gc[1][c] = Gc[2][c] = Ec[c] = 0.0f;
+                C.G[0][c] = C.G[1][c] = C.G[2][c] = C.E[c] = 0.0f;
             }
         }
-    float acc[3][4];
+}
+
+// One particle of the gather + MUSL re-projection: velocity from the four
+// nodes of this thread's z-layer plus the partner lane's four, the particle
+// velocity write, |geup|^2 and the momentum re-projection sums.
+__device__ __forceinline__ void musl_particle(const StepArgs<float> &a, const Scales &S, const MuslCell &C, int cx,
+                                              int cy, int cz, int h, int p, float x0, float x1, float x2, float m,
+                                              float vol, const float *vold, float (*acc)[4], long long &gacc,
+                                              float &vmax) {
+    const size_t N = (size_t)a.g.nodec;
+    const bool flip = (a.scheme == MPM_FLIP);
+    bool oob = false;
+    const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
+    Axis<float, 1> ax, ay, az;
+    axis_eval<float, 1>(x0, a.g, 0, px, ax);
+    axis_eval<float, 1>(x1, a.g, 1, py, ay);
+    axis_eval<float, 1>(x2, a.g, 2, pz, az);
+    const bool mine = (px == cx) && (py == cy) && (pz == cz);
+    const float wz = h ? az.w[1] : az.w[0], dwz = h ? az.dw[1] : az.dw[0];
+    // partial gathers over this thread's four nodes
+    float vs[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
-    for (int d = 0; d < 3; d++)
+    for (int j = 0; j < 2; j++)
 #pragma unroll
-        for (int c = 0; c < 4; c++) acc[d][c] = 0.0f;
-    long long gacc = 0;
-    float vmax = 0.0f;
-    for (int p = p0; p < p1; p++) {
-        const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
-        bool oob = false;
-        const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
-        Axis<float, 1> ax, ay, az;
-        axis_eval<float, 1>(x0, a.g, 0, px, ax);
-        axis_eval<float, 1>(x1, a.g, 1, py, ay);
-        axis_eval<float, 1>(x2, a.g, 2, pz, az);
-        const float m = ld(P.m + p), vol = ld(P.vol + p);
-        const bool mine = (px == cx) && (py == cy) && (pz == cz);
-        const float wz = h ? az.w[1] : az.w[0], dwz = h ? az.dw[1] : az.dw[0];
-        // partial gathers over this thread's four nodes
-        float vs[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-        for (int j = 0; j < 2; j++)
-#pragma unroll
-            for (int i = 0; i < 2; i++) {
-                const int c = i + 2 * j;
-                const float wxy = ax.w[i] * ay.w[j];
-                const float N_ = wxy * wz;
-                float gv[3], e;
-                if (mine) {
-                    gv[0] = Gc[0][c]; gv[1] = Gc[1][c]; gv[2] = Gc[2][c];
-                    e = Ec[c];
-                } else {
-                    const size_t gn = node_id(a.g, px + i, py + j, pz + h);
-                    gv[0] = ld(a.G + gn); gv[1] = ld(a.G + N + gn); gv[2] = ld(a.G + 2 * N + gn);
-                    e = ld(a.nei + gn);
-                }
-                const float wv = flip ? N_ * a.dt : N_;
-#pragma unroll
-                for (int d = 0; d < 3; d++) vs[d] += wv * gv[d];
-                gu[0] += ax.dw[i] * ay.w[j] * wz * e;
-                gu[1] += ax.w[i] * ay.dw[j] * wz * e;
-                gu[2] += wxy * dwz * e;
+        for (int i = 0; i < 2; i++) {
+            const int c = i + 2 * j;
+            const float wxy = ax.w[i] * ay.w[j];
+            const float N_ = wxy * wz;
+            float gv[3], e;
+            if (mine) {
+                gv[0] = C.G[0][c];
+                gv[1] = C.G[1][c];
+                gv[2] = C.G[2][c];
+                e = C.E[c];
+            } else {
+                const size_t gn = node_id(a.g, px + i, py + j, pz + h);
+                gv[0] = ld(a.G + gn);
+                gv[1] = ld(a.G + N + gn);
+                gv[2] = ld(a.G + 2 * N + gn);
+                e = ld(a.nei + gn);
             }
-        // combine the two halves of the cell (a + b == b + a: both threads agree).
-        // Only the cell's own two lanes take part: the other cells of the warp
-        // run different particle counts, so a full-warp mask would not converge.
-        const unsigned pair = 3u << ((threadIdx.x & 31) & ~1u);
-        float v[3];
+            const float wv = flip ? N_ * a.dt : N_;
 #pragma unroll
-        for (int d = 0; d < 3; d++) {
-            const float other = __shfl_xor_sync(pair, vs[d], 1);
-            v[d] = vs[d] + other;
-            gu[d] += __shfl_xor_sync(pair, gu[d], 1);
+            for (int d = 0; d < 3; d++) vs[d] += wv * gv[d];
+            gu[0] += ax.dw[i] * ay.w[j] * wz * e;
+            gu[1] += ax.w[i] * ay.dw[j] * wz * e;
+            gu[2] += wxy * dwz * e;
         }
-        if (flip) {
+    // combine the two halves of the cell (a + b == b + a: both threads agree).
+    // Only the cell's own two lanes take part: the other cells of the warp
+    // run different particle counts, so a full-warp mask would not converge.
+    const unsigned pair = 3u << ((threadIdx.x & 31) & ~1u);
+    float v[3];
 #pragma unroll
-            for (int d = 0; d < 3; d++) v[d] += ld(P.v[d] + p);
-        }
-        if (h == 0) {
-            P.v[0][p] = v[0];
-            P.v[1][p] = v[1];
-            P.v[2][p] = v[2];
-            vmax = fmaxf(vmax, fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2]))));
-            const float tv = 2.0f * vol;
-            const float g0 = gu[0] * tv, g1 = gu[1] * tv, g2 = gu[2] * tv;
-            gacc += fx(g0 * g0 + g1 * g1 + g2 * g2, S.gd);
-        }
-        // MUSL re-projection of momentum (var_trans_solid_explicit.cpp:108-129)
-#pragma unroll
-        for (int j = 0; j < 2; j++)
-#pragma unroll
-            for (int i = 0; i < 2; i++) {
-                const int c = i + 2 * j;
-                const float Nm = ax.w[i] * ay.w[j] * wz * m;
-                if (mine) {
-#pragma unroll
-                    for (int d = 0; d < 3; d++) acc[d][c] += Nm * v[d];
-                } else {
-                    const size_t gn = node_id(a.g, px + i, py + j, pz + h);
-#pragma unroll
-                    for (int d = 0; d < 3; d++) {
-                        long long q = fx(Nm * v[d], S.q);
-                        if (q) atomic_add_i64(&a.acc2[d * N + gn], q);
-                    }
-                }
-            }
+    for (int d = 0; d < 3; d++) {
+        const float other = __shfl_xor_sync(pair, vs[d], 1);
+        v[d] = vs[d] + other;
+        gu[d] += __shfl_xor_sync(pair, gu[d], 1);
     }
+    if (flip) {
+#pragma unroll
+        for (int d = 0; d < 3; d++) v[d] += vold[d];
+    }
+    if (h == 0) {
+        a.P.v[0][p] = v[0];
+        a.P.v[1][p] = v[1];
+        a.P.v[2][p] = v[2];
+        vmax = fmaxf(vmax, fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2]))));
+        const float tv = 2.0f * vol;
+        const float g0 = gu[0] * tv, g1 = gu[1] * tv, g2 = gu[2] * tv;
+        gacc += fx(g0 * g0 + g1 * g1 + g2 * g2, S.gd);
+    }
+    // MUSL re-projection of momentum (var_trans_solid_explicit.cpp:108-129)
+#pragma unroll
+    for (int j = 0; j < 2; j++)
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const int c = i + 2 * j;
+            const float Nm = ax.w[i] * ay.w[j] * wz * m;
+            if (mine) {
+#pragma unroll
+                for (int d = 0; d < 3; d++) acc[d][c] += Nm * v[d];
+            } else {
+                const size_t gn = node_id(a.g, px + i, py + j, pz + h);
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    long long q = fx(Nm * v[d], S.q);
+                    if (q) atomic_add_i64(&a.acc2[d * N + gn], q);
+                }
+            }
+        }
+}
+
+__device__ __forceinline__ void musl_node_pass(const StepArgs<float> &a, const Scales &S, float (*corner)[BRC],
+                                               long long *sh_l, float *sh_f, int lc, int h, int ox, int oy, int oz,
+                                               const float (*acc)[4], long long gacc, float vmax) {
+    const size_t N = (size_t)a.g.nodec;
 #pragma unroll
     for (int d = 0; d < 3; d++)
 #pragma unroll
@@ -444,6 +542,132 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell(StepArgs<f
                 }
         if (sum != 0.0f) atomic_add_i64(&a.acc2[d * N + node_id(a.g, gx, gy, gz)], fx(sum, S.q));
     }
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell(StepArgs<float> a) {
+    __shared__ float corner[3 * 8][BRC];
+    __shared__ Scales S;
+    __shared__ long long sh_l[32];
+    __shared__ float sh_f[32];
+    const int b = blockIdx.x;
+    const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
+    const int *cs = a.cstart + (size_t)b * (BRC + 1);
+    if (cs[0] == cs[BRC]) return;
+    int ox, oy, oz;
+    brick_origin(b, a.nbrick, ox, oy, oz);
+    const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
+    const int p0 = cs[lc], p1 = cs[lc + 1];
+    load_scales(a, S);
+    const Particles<float> &P = a.P;
+    MuslCell C;
+    musl_load_cell(a, cx, cy, cz, h, p1 > p0, C);
+    float acc[3][4];
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[d][c] = 0.0f;
+    long long gacc = 0;
+    float vmax = 0.0f;
+    const bool flip = (a.scheme == MPM_FLIP);
+    for (int p = p0; p < p1; p++) {
+        float vold[3] = {0.0f, 0.0f, 0.0f};
+        if (flip) {
+            vold[0] = ld(P.v[0] + p);
+            vold[1] = ld(P.v[1] + p);
+            vold[2] = ld(P.v[2] + p);
+        }
+        musl_particle(a, S, C, cx, cy, cz, h, p, ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p), ld(P.m + p),
+                      ld(P.vol + p), vold, acc, gacc, vmax);
+    }
+    musl_node_pass(a, S, corner, sh_l, sh_f, lc, h, ox, oy, oz, acc, gacc, vmax);
+}
+
+// The gather + MUSL with the brick's x, m, vol and (FLIP) v staged in shared
+// memory by bulk asynchronous copies, as k_p2g_cell_staged; same order of
+// operations as k_g2p_musl_cell, so the same results bit for bit.
+constexpr int MNF = 8;                       // x 3, m, vol, v 3
+constexpr size_t MSTAGE = (size_t)MNF * PST * 4;
+
+template <int MINB>
+__global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell_staged(StepArgs<float> a) {
+    extern __shared__ __align__(128) unsigned char dsm[];
+    __shared__ float corner[3 * 8][BRC];
+    __shared__ Scales S;
+    __shared__ long long sh_l[32];
+    __shared__ float sh_f[32];
+    __shared__ __align__(8) unsigned long long bar[2];
+    const int b = blockIdx.x;
+    const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
+    const int *cs = a.cstart + (size_t)b * (BRC + 1);
+    const int P0 = cs[0], P1 = cs[BRC];
+    if (P0 == P1) return;
+    const Particles<float> &P = a.P;
+    const bool flip = (a.scheme == MPM_FLIP);
+    const int nf = flip ? MNF : 5;
+    const float *src[MNF] = {P.x[0], P.x[1], P.x[2], P.m, P.vol, P.v[0], P.v[1], P.v[2]};
+    const int nch = (P1 - P0 + PCH - 1) / PCH;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](int k) {
+        const int st = k & 1;
+        const int c0 = P0 + k * PCH, c1 = min(c0 + PCH, P1);
+        const int a0 = c0 & ~3, a1 = (c1 + 3) & ~3;
+        const unsigned bytes = (unsigned)(a1 - a0) * 4u;
+        float *dst = reinterpret_cast<float *>(dsm + st * MSTAGE);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&bar[st], bytes * nf);
+        for (int f = 0; f < nf; f++) bulk_g2s(dst + f * PST, src[f] + a0, bytes, &bar[st]);
+    };
+    if (threadIdx.x == 0) issue(0);
+    int ox, oy, oz;
+    brick_origin(b, a.nbrick, ox, oy, oz);
+    const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
+    const int p0 = cs[lc], p1 = cs[lc + 1];
+    load_scales(a, S);
+    MuslCell C;
+    musl_load_cell(a, cx, cy, cz, h, p1 > p0, C);
+    float acc[3][4];
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[d][c] = 0.0f;
+    long long gacc = 0;
+    float vmax = 0.0f;
+    for (int k = 0; k < nch; k++) {
+        const int st = k & 1;
+        if (threadIdx.x == 0 && k + 1 < nch) issue(k + 1);
+        const bool ok = mbar_wait_bounded(&bar[st], (unsigned)((k >> 1) & 1), 1u << 22);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                atomicAdd(&a.ctl->err_timeout, 1u);
+                if (k + 1 < nch) mbar_wait_bounded(&bar[st ^ 1], (unsigned)(((k + 1) >> 1) & 1), 1u << 22);
+            }
+            __syncthreads();
+            return;
+        }
+        const int c0 = P0 + k * PCH, c1 = min(c0 + PCH, P1);
+        const int a0 = c0 & ~3;
+        const float *sf = reinterpret_cast<const float *>(dsm + st * MSTAGE);
+        const int q0 = max(p0, c0), q1 = min(p1, c1);
+        for (int p = q0; p < q1; p++) {
+            const int l = p - a0;
+            float vold[3] = {0.0f, 0.0f, 0.0f};
+            if (flip) {
+                vold[0] = sf[5 * PST + l];
+                vold[1] = sf[6 * PST + l];
+                vold[2] = sf[7 * PST + l];
+            }
+            musl_particle(a, S, C, cx, cy, cz, h, p, sf[l], sf[PST + l], sf[2 * PST + l], sf[3 * PST + l],
+                          sf[4 * PST + l], vold, acc, gacc, vmax);
+        }
+        __syncthreads();
+    }
+    musl_node_pass(a, S, corner, sh_l, sh_f, lc, h, ox, oy, oz, acc, gacc, vmax);
 }
 
 // Launched before the P2G of every step: records the P2G scales (for result
@@ -1213,8 +1437,19 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
         timer_begin(c, K_P2G);
         if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
             if (use_cell_kernels(c)) {
-                if (c->tune.p2g_minb == 3) k_p2g_cell<3><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
-                else k_p2g_cell<2><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                if (c->tune.p2g_staged) {
+                    static bool attr = false;
+                    if (!attr) {
+                        cudaFuncSetAttribute(k_p2g_cell_staged<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(2 * PSTAGE));
+                        attr = true;
+                    }
+                    k_p2g_cell_staged<2><<<c->g.nbricks, CELL_THREADS, 2 * PSTAGE, c->stream>>>(a);
+                } else if (c->tune.p2g_minb == 3) {
+                    k_p2g_cell<3><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                } else {
+                    k_p2g_cell<2><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                }
                 timer_end(c, K_P2G);
                 c->launches++;
                 return check_launch(c);
@@ -1228,8 +1463,19 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
         timer_begin(c, K_G2P_MUSL);
         if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
             if (use_cell_kernels(c)) {
-                if (c->tune.musl_minb == 2) k_g2p_musl_cell<2><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
-                else k_g2p_musl_cell<3><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                if (c->tune.musl_staged) {
+                    static bool attr = false;
+                    if (!attr) {
+                        cudaFuncSetAttribute(k_g2p_musl_cell_staged<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(2 * MSTAGE));
+                        attr = true;
+                    }
+                    k_g2p_musl_cell_staged<3><<<c->g.nbricks, CELL_THREADS, 2 * MSTAGE, c->stream>>>(a);
+                } else if (c->tune.musl_minb == 2) {
+                    k_g2p_musl_cell<2><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                } else {
+                    k_g2p_musl_cell<3><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                }
                 timer_end(c, K_G2P_MUSL);
                 c->launches++;
                 return check_launch(c);

@@ -918,11 +918,15 @@ static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
     const int check = 8;
     while (!done && it < kmax) {
         const int cur = (it & 1) ? S_RR1 : S_RR0;
+        timer_begin(c, K_MATVEC);
         k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->p, s->Ap, s->part);
+        timer_end(c, K_MATVEC);
+        timer_begin(c, K_KRYLOV);
         k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_PAP);
         k_cg_update<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->xs, s->r, s->p, s->Ap, s->part);
         k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, cur ^ 1);
         k_cg_dir<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->r, s->p);
+        timer_end(c, K_KRYLOV);
         c->launches += 5;
         it++;
         if (it % check == 0 || it == kmax) {
@@ -973,8 +977,10 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
     const int check = 8;
     while (!done && it < kmax) {
         if (use_nn) {
+            timer_begin(c, K_PRECOND);
             mpm_status st = mpm_nn_apply_precond(s->net, c->stream, s->r, s->scal + S_RRC, s->adiag, a.bcflag, a.mtol,
                                                  s->z);
+            timer_end(c, K_PRECOND);
             if (st != MPM_OK) return st;
             s->nn_applications++;
             c->launches += 9;
@@ -986,12 +992,18 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
             k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_ZQ);
             c->launches += 2;
         }
+        timer_begin(c, K_KRYLOV);
         k_fcg_dir<<<nb, 256, 0, c->stream>>>(a, s->scal, restart, s->z, s->r, s->p, s->part);
         k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_PR);
+        timer_end(c, K_KRYLOV);
+        timer_begin(c, K_MATVEC);
         k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->p, s->Ap, s->part);
+        timer_end(c, K_MATVEC);
+        timer_begin(c, K_KRYLOV);
         k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_PAP);
         k_fcg_update<<<nb, 256, 0, c->stream>>>(a, s->scal, s->xs, s->r, s->p, s->Ap, s->part);
         k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
+        timer_end(c, K_KRYLOV);
         c->launches += 6;
         restart = 0;
         it++;
@@ -1039,9 +1051,11 @@ static mpm_status imp_assemble(mpm_ctx *c) {
     CKI(cudaMemsetAsync(s->b, 0, sizeof(double) * 3 * N, c->stream));
     PView P = pview(c);
     const int pb = (int)((c->num + 127) / 128);
+    timer_begin(c, K_ASSEMBLE);
     k_imp_assemble<<<pb, 128, 0, c->stream>>>(a, P, s->ndispl, s->stress_k, s->A, s->b);
     k_imp_rhs_diag<<<nb_nodes(c), 256, 0, c->stream>>>(a, s->A, s->nmass, s->naccel_k, s->naccel, s->b, s->adiag);
     k_imp_scale<<<nb_nodes(c), 256, 0, c->stream>>>(a, s->A, s->adiag);
+    timer_end(c, K_ASSEMBLE);
     c->launches += 3;
     return check_launch(c);
 }

@@ -32,11 +32,11 @@ constexpr int BRX = 4, BRY = 4, BRZ = 8;   // particle brick: cells per brick ed
 constexpr int BRC = BRX * BRY * BRZ;       // cells per brick (one CTA thread per cell)
 constexpr int CHUNK = 1024;          // max particles per work item
 constexpr int NACC = 8;              // P2G fields: mass, vof, mome xyz, force xyz
-constexpr int NKCLASS = 12;          // kernel classes for timing
+constexpr int NKCLASS = 14;          // kernel classes for timing
 
 enum KernelClass {
     K_BIN = 0, K_SCAN, K_SCATTER, K_PERMUTE, K_P2G, K_GRID1, K_G2P_MUSL, K_GRID2, K_G2P_UPDATE, K_MISC,
-    K_MATVEC, K_KRYLOV
+    K_MATVEC, K_KRYLOV, K_ASSEMBLE, K_PRECOND
 };
 
 struct Geom {
@@ -96,8 +96,10 @@ struct Fix {
 // Launch variants that give bitwise identical results; chosen by
 // mpm_gpu_autotune from measured times (defaults otherwise).
 struct Tune {
-    int p2g_minb = 2;               // resident CTAs the per-cell P2G is compiled for (2 or 3)
-    int musl_minb = 3;              // same for the gather + MUSL kernel
+    int p2g_staged = 1;             // per-cell P2G reads the brick's particles from bulk-copied shared memory
+    int p2g_minb = 2;               // resident CTAs the direct per-cell P2G is compiled for (2 or 3)
+    int musl_staged = 1;            // gather + MUSL reads the brick's particles from staged shared memory
+    int musl_minb = 3;              // resident CTAs the direct gather + MUSL kernel is compiled for
     int update_ctas_per_sm = 4;     // persistent CTAs per SM of the staged particle update
     bool done = false;
 };
@@ -172,7 +174,7 @@ struct mpm_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     double graph_facl = 0.0;
     cudaStream_t graph_stream = nullptr;
-    int graph_tune[3] = {0, 0, 0};
+    int graph_tune[5] = {0, 0, 0, 0, 0};
     int graph_cur = 0;
     void *graph_pbuf[2] = {nullptr, nullptr};
     int64_t graph_launches = 0;

@@ -72,7 +72,7 @@ EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_s
            "mpm_gpu_get_tuning", "mpm_nn_num_params", "mpm_nn_create", "mpm_nn_destroy", "mpm_nn_set_stream",
            "mpm_nn_init_params", "mpm_nn_set_params", "mpm_nn_get_params", "mpm_nn_forward", "mpm_nn_backward",
            "mpm_nn_num_pairs", "mpm_nn_train", "mpm_gpu_implicit_set_precond", "mpm_gpu_implicit_harvest",
-           "mpm_gpu_set_graph"]
+           "mpm_gpu_set_graph", "mpm_gpu_set_tuning"]
 
 
 def load(path: str | None = None):
@@ -105,6 +105,7 @@ def load(path: str | None = None):
     lib.mpm_gpu_enable_kernel_timing.argtypes = [C.c_void_p, C.c_int]
     lib.mpm_gpu_autotune.argtypes = [C.c_void_p, C.c_int, C.c_double]
     lib.mpm_gpu_set_graph.argtypes = [C.c_void_p, C.c_int]
+    lib.mpm_gpu_set_tuning.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
     lib.mpm_gpu_get_tuning.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.mpm_gpu_implicit_setup.argtypes = [C.c_void_p, C.c_int, C.c_double]
     lib.mpm_gpu_implicit_step.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int,
@@ -253,6 +254,10 @@ class GpuSolid:
         st = Stats()
         _chk(self.lib.mpm_gpu_get_stats(self.ctx, C.byref(st)), "mpm_gpu_get_stats")
         return {k: getattr(st, k) for k, _ in Stats._fields_}
+
+    def set_tuning(self, p2g_minb, musl_minb, update_ctas_per_sm):
+        """Launch variants (0 = shared-memory staged kernel); see mpm_gpu_set_tuning."""
+        _chk(self.lib.mpm_gpu_set_tuning(self.ctx, p2g_minb, musl_minb, update_ctas_per_sm), "mpm_gpu_set_tuning")
 
     def set_graph(self, on=True):
         """Replay blocks of fused steps from a captured CUDA graph (default on)."""

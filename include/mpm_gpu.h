@@ -161,14 +161,19 @@ mpm_status mpm_gpu_get_stats(mpm_ctx *ctx, mpm_stats *out);
  * for i < *count (count in: capacity).  Synchronises the stream. */
 mpm_status mpm_gpu_enable_kernel_timing(mpm_ctx *ctx, int on);
 /* No counterpart in the reference (which has no tuning): picks, per kernel,
- * the launch variant with the lowest measured time (resident CTAs per SM of
- * the per-cell scatter and gather kernels, persistent CTAs per SM of the
- * staged particle update) by running 3 x steps_per_trial explicit steps.
+ * the launch variant with the lowest measured time (shared-memory staged or
+ * direct per-cell P2G and the resident CTAs per SM of the per-cell scatter and
+ * gather kernels, persistent CTAs per SM of the staged particle update) by
+ * running 3 x steps_per_trial explicit steps.
  * All variants compute bitwise the same results, so the trial steps are
  * ordinary steps of the simulation.  The re-sort period is not tuned: it
  * changes FP32 rounding. */
 mpm_status mpm_gpu_autotune(mpm_ctx *ctx, int steps_per_trial, double facl);
+/* p2g_minb / musl_minb: 0 = the shared-memory staged kernel, 2 or 3 = the
+ * direct per-cell kernel compiled for that many resident CTAs per SM;
+ * update_ctas_per_sm: 1..8. */
 mpm_status mpm_gpu_get_tuning(mpm_ctx *ctx, int *p2g_minb, int *musl_minb, int *update_ctas_per_sm);
+mpm_status mpm_gpu_set_tuning(mpm_ctx *ctx, int p2g_minb, int musl_minb, int update_ctas_per_sm);
 mpm_status mpm_gpu_kernel_times(mpm_ctx *ctx, int *count, const char **names, double *ms, int64_t *launches);
 
 /* ---- the implicit solid (module/solid/implicit/, module/solver/) ----------------
