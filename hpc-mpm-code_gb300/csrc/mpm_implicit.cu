@@ -735,6 +735,19 @@ __global__ void k_true_residual(ImpArgs a, const double *bs, const double *Ax, d
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
+// network feature channels: the mass term's share of each diagonal entry,
+// phi = alpha_m nb3 nmass / diag (diag = 1 / adiag^2), clamped to [0, 1]
+__global__ void k_phi(ImpArgs a, const double *nmass, const double *adiag, double *phi) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.nodec) return;
+    const size_t N = (size_t)a.nodec;
+    for (int c = 0; c < 3; c++) {
+        const double d = adiag[c * N + n];
+        const double v = a.am * a.nb[3] * nmass[n] * d * d;
+        phi[c * N + n] = v < 0.0 ? 0.0 : (v > 1.0 ? 1.0 : v);
+    }
+}
+
 // e = xstar - x
 __global__ void k_sub3(const double *xstar, const double *x, double *e, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -972,6 +985,11 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
     int it = 0;
     bool done = !(rr0 > 1.0e-300);
     bool use_nn = s->net != nullptr;
+    if (use_nn) {
+        k_phi<<<nb, 256, 0, c->stream>>>(a, s->nmass, s->adiag, s->ev);
+        mpm_status st = mpm_nn_set_feature(s->net, c->stream, s->ev);
+        if (st != MPM_OK) return st;
+    }
     int restart = 1;
     double rr_window = rr0;
     const int check = 8;
@@ -1323,6 +1341,10 @@ mpm_status mpm_gpu_implicit_harvest(mpm_ctx *c, mpm_nn *net, int nsystems, int l
         const double E = exp(log(e_min) + next_unit() * (log(e_max) - log(e_min)));
         k_set_modulus<<<1, 32, 0, c->stream>>>(c->d_matprop, c->nmat, E);
         st = mpm_gpu_implicit_assemble(c, 1.0);
+        if (st == MPM_OK) {
+            k_phi<<<nb, 256, 0, c->stream>>>(a, s->nmass, s->adiag, s->ev);
+            st = mpm_nn_begin_system(net, c->stream, s->ev);
+        }
         for (int ld = 0; ld < loads_per_system && st == MPM_OK; ld++) {
             const uint64_t key = seed * 1000003ull + (uint64_t)sys * 1009ull + (uint64_t)ld;
             // alternate smooth-dominated and noise-dominated loads

@@ -417,23 +417,27 @@ __global__ void k_dw_reduce(const float *part, int nblk, int ci_pad, int ci, int
 }
 
 // ----------------------------------------------------- CUDA-core layers
-// x0 = [in(3), 0 x 13] (host-style FP32 input [rows][3])
+// x0 = [in(6), 0 x 10] (host-style FP32 input [rows][6])
 __global__ void k_input_f32(const float *in, bf16 *x0, int64_t rows) {
     const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (r >= rows) return;
-    float f[8] = {in[3 * r], in[3 * r + 1], in[3 * r + 2], 0, 0, 0, 0, 0};
+    const float *q = in + NIN * r;
+    float f[8] = {q[0], q[1], q[2], q[3], q[4], q[5], 0, 0};
     uint4 *o = reinterpret_cast<uint4 *>(x0 + r * 16);
     o[0] = pack8(f);
     o[1] = make_uint4(0, 0, 0, 0);
 }
 
-// x0 from an FP64 component-major residual, scaled by 1 / sqrt(rr / (3 nodec))
-__global__ void k_input_r(const double *r, const double *rr, int64_t nodec, bf16 *x0) {
+// x0 from an FP64 component-major residual, scaled by 1 / sqrt(rr / (3 nodec)),
+// and the system's feature channels
+__global__ void k_input_r(const double *r, const double *rr, const bf16 *feat, int64_t nodec, bf16 *x0) {
     const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (n >= nodec) return;
     const double ms = rr[0] / (3.0 * (double)nodec);
     const double inv = ms > 0.0 ? 1.0 / sqrt(ms) : 0.0;
-    float f[8] = {(float)(r[n] * inv), (float)(r[nodec + n] * inv), (float)(r[2 * nodec + n] * inv), 0, 0, 0, 0, 0};
+    float f[8] = {(float)(r[n] * inv), (float)(r[nodec + n] * inv), (float)(r[2 * nodec + n] * inv),
+                  __bfloat162float(feat[3 * n]), __bfloat162float(feat[3 * n + 1]), __bfloat162float(feat[3 * n + 2]),
+                  0, 0};
     uint4 *o = reinterpret_cast<uint4 *>(x0 + n * 16);
     o[0] = pack8(f);
     o[1] = make_uint4(0, 0, 0, 0);
@@ -658,17 +662,19 @@ __global__ void k_adam(float *p, const float *g, float *m, float *v, int64_t n, 
     p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
-// training batch: x0 from stored residuals, FP32 targets, per-sample |e|^2
-__global__ void k_gather_batch(const bf16 *dr, const bf16 *de, const int *idx, int64_t v0, int batch, bf16 *x0,
-                               float *tgt) {
+// training batch: x0 from stored residuals and their system's features, FP32 targets
+__global__ void k_gather_batch(const bf16 *dr, const bf16 *de, const bf16 *df, const int *dsys, const int *idx,
+                               int64_t v0, int batch, bf16 *x0, float *tgt) {
     const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (r >= v0 * batch) return;
     const int b = (int)(r / v0);
     const int64_t n = r - (int64_t)b * v0;
     const int64_t src = (int64_t)idx[b] * v0 + n;
+    const int64_t fs = (int64_t)dsys[idx[b]] * v0 + n;
     float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int c = 0; c < 3; c++) {
         f[c] = __bfloat162float(dr[3 * src + c]);
+        f[3 + c] = __bfloat162float(df[3 * fs + c]);
         tgt[3 * r + c] = __bfloat162float(de[3 * src + c]);
     }
     uint4 *o = reinterpret_cast<uint4 *>(x0 + r * 16);
@@ -726,6 +732,15 @@ __global__ void k_append_pair(const double *r, const double *rr, const double *e
     }
 }
 
+__global__ void k_set_int(int *p, int v) { *p = v; }
+
+// feature channels of a system: phi (FP64 component-major) -> bf16 [nodec][3]
+__global__ void k_feature(const double *phi, int64_t nodec, bf16 *feat) {
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nodec) return;
+    for (int c = 0; c < 3; c++) feat[3 * n + c] = __float2bfloat16_rn((float)phi[c * nodec + n]);
+}
+
 }  // namespace nn
 }  // namespace mpm
 
@@ -750,6 +765,10 @@ struct mpm_nn {
     int64_t adam_step = 0;
     bf16 *data_r = nullptr, *data_e = nullptr;
     int64_t ndata = 0, data_cap = 0;
+    bf16 *feat = nullptr;        // feature channels of the system being solved [v0][3]
+    bf16 *data_f = nullptr;      // feature channels of each harvested system [max_systems][v0][3]
+    int *data_sys = nullptr;     // system of each stored pair
+    int nsys = 0, sys_cap = 0;
     int64_t *d_ndata = nullptr;
     cudaStream_t stream = nullptr;
 };
@@ -907,7 +926,7 @@ cudaError_t backward(mpm_nn *net, cudaStream_t st, int batch) {
                                       batch)) != cudaSuccess)
         return e;
     launch_chan_sum<16>(net, st, net->ge0, r0, G + b_offset(0));
-    if ((e = launch_dw<16, 16, S1>(net, st, net->x0, net->ge0, L0, L0, batch, 3, G + w_offset(0))) != cudaSuccess)
+    if ((e = launch_dw<16, 16, S1>(net, st, net->x0, net->ge0, L0, L0, batch, NIN, G + w_offset(0))) != cudaSuccess)
         return e;
     return cudaGetLastError();
 }
@@ -925,7 +944,8 @@ mpm_status read_err(mpm_nn *net) {
 void net_free(mpm_nn *n) {
     void *ptrs[] = {n->p,   n->g,   n->am,  n->av,  n->x0,  n->e0,  n->e1,  n->e2,     n->c2,     n->d1,
                     n->c1,  n->d0,  n->gd0, n->ge0, n->gc1, n->gd1, n->ge1, n->gc2,    n->ge2,    n->z,
-                    n->gz,  n->tgt, n->part, n->loss, n->idx, n->err, n->data_r, n->data_e, n->d_ndata};
+                    n->gz,  n->tgt, n->part, n->loss, n->idx, n->err, n->data_r, n->data_e, n->d_ndata,
+                    n->feat, n->data_f, n->data_sys};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int l = 0; l < NCONV; l++) {
@@ -1011,16 +1031,20 @@ mpm_status mpm_nn_create(const int nodes[3], int max_batch, int64_t max_pairs, m
     NN_ALLOC(n->ge2, B * v2 * 64 * 2);
     NN_ALLOC(n->z, B * v0 * 3 * 4);
     NN_ALLOC(n->gz, B * v0 * 3 * 4);
-    NN_ALLOC(n->tgt, B * v0 * 3 * 4);
+    NN_ALLOC(n->tgt, B * v0 * NIN * 4);
     n->part_cap = (size_t)n->nsm * 27 * 64 * 32;   // largest weight-gradient partials
     NN_ALLOC(n->part, n->part_cap * 4);
     NN_ALLOC(n->loss, (size_t)B * 4);
     NN_ALLOC(n->idx, (size_t)B * 4);
     NN_ALLOC(n->err, sizeof(int));
     NN_ALLOC(n->d_ndata, sizeof(int64_t));
+    NN_ALLOC(n->feat, (size_t)v0 * 3 * 2);
     if (max_pairs > 0) {
         NN_ALLOC(n->data_r, (size_t)max_pairs * v0 * 3 * 2);
         NN_ALLOC(n->data_e, (size_t)max_pairs * v0 * 3 * 2);
+        NN_ALLOC(n->data_sys, (size_t)max_pairs * sizeof(int));
+        n->sys_cap = (int)std::min<int64_t>(max_pairs, 512);
+        NN_ALLOC(n->data_f, (size_t)n->sys_cap * v0 * 3 * 2);
     }
 #undef NN_ALLOC
     n->data_cap = max_pairs;
@@ -1028,6 +1052,7 @@ mpm_status mpm_nn_create(const int nodes[3], int max_batch, int64_t max_pairs, m
     cudaMemset(n->am, 0, P * 4);
     cudaMemset(n->av, 0, P * 4);
     cudaMemset(n->err, 0, sizeof(int));
+    cudaMemset(n->feat, 0, (size_t)v0 * 3 * 2);
     *out = n;
     return MPM_OK;
 }
@@ -1083,8 +1108,8 @@ mpm_status mpm_nn_forward(mpm_nn *net, int batch, const float *in, float *out) {
     if (!net || !in || !out || batch < 1 || batch > net->max_batch) return MPM_ERR_BAD_ARG;
     cudaStream_t st = net->stream;
     const int64_t r0 = (int64_t)batch * net->L[0].v;
-    CKN(cudaMemcpyAsync(net->z, in, r0 * 3 * 4, cudaMemcpyHostToDevice, st));
-    k_input_f32<<<blocks(r0), 256, 0, st>>>(net->z, net->x0, r0);
+    CKN(cudaMemcpyAsync(net->tgt, in, r0 * NIN * 4, cudaMemcpyHostToDevice, st));
+    k_input_f32<<<blocks(r0), 256, 0, st>>>(net->tgt, net->x0, r0);
     CKN(forward(net, st, batch));
     k_output<<<blocks(r0), 256, 0, st>>>(net->d0, net->p + w5_offset(), net->p + b5_offset(), net->z, r0);
     CKN(cudaGetLastError());
@@ -1097,9 +1122,9 @@ mpm_status mpm_nn_backward(mpm_nn *net, int batch, const float *in, const float 
     if (!net || !in || !gout || !grad || batch < 1 || batch > net->max_batch) return MPM_ERR_BAD_ARG;
     cudaStream_t st = net->stream;
     const int64_t r0 = (int64_t)batch * net->L[0].v;
-    CKN(cudaMemcpyAsync(net->z, in, r0 * 3 * 4, cudaMemcpyHostToDevice, st));
+    CKN(cudaMemcpyAsync(net->tgt, in, r0 * NIN * 4, cudaMemcpyHostToDevice, st));
     CKN(cudaMemcpyAsync(net->gz, gout, r0 * 3 * 4, cudaMemcpyHostToDevice, st));
-    k_input_f32<<<blocks(r0), 256, 0, st>>>(net->z, net->x0, r0);
+    k_input_f32<<<blocks(r0), 256, 0, st>>>(net->tgt, net->x0, r0);
     CKN(forward(net, st, batch));
     CKN(backward(net, st, batch));
     CKN(cudaMemcpyAsync(grad, net->g, param_count() * 4, cudaMemcpyDeviceToHost, st));
@@ -1130,15 +1155,18 @@ mpm_status mpm_nn_train(mpm_nn *net, int epochs, int batch, double lr, uint64_t 
         double lsum = 0.0;
         for (int64_t bi = 0; bi < nb; bi++) {
             CKN(cudaMemcpyAsync(net->idx, perm.data() + bi * batch, batch * 4, cudaMemcpyHostToDevice, st));
-            k_gather_batch<<<blocks(r0), 256, 0, st>>>(net->data_r, net->data_e, net->idx, v0, batch, net->x0,
-                                                       net->tgt);
+            k_gather_batch<<<blocks(r0), 256, 0, st>>>(net->data_r, net->data_e, net->data_f, net->data_sys,
+                                                       net->idx, v0, batch, net->x0, net->tgt);
             CKN(forward(net, st, batch));
             k_output<<<blocks(r0), 256, 0, st>>>(net->d0, net->p + w5_offset(), net->p + b5_offset(), net->z, r0);
             k_mse<<<batch, RED_THREADS, 0, st>>>(net->z, net->tgt, net->gz, v0, batch, net->loss);
             CKN(backward(net, st, batch));
             net->adam_step++;
             const float c1 = 1.0f - powf(b1, (float)net->adam_step), c2 = 1.0f - powf(b2, (float)net->adam_step);
-            k_adam<<<blocks(P), 256, 0, st>>>(net->p, net->g, net->am, net->av, P, (float)lr, b1, b2, 1e-8f, c1, c2);
+            // cosine decay of the step size over the whole call
+            const double prog = (double)(ep * nb + bi) / (double)(epochs * nb);
+            const float lr_t = (float)(lr * 0.5 * (1.0 + cos(3.141592653589793 * prog)));
+            k_adam<<<blocks(P), 256, 0, st>>>(net->p, net->g, net->am, net->av, P, lr_t, b1, b2, 1e-8f, c1, c2);
             net->weights_dirty = true;
             CKN(cudaMemcpyAsync(lbuf.data(), net->loss, batch * 4, cudaMemcpyDeviceToHost, st));
             CKN(cudaStreamSynchronize(st));
@@ -1160,7 +1188,7 @@ int mpm_nn_grid_matches(const mpm_nn *net, const int nodes[3]) {
 mpm_status mpm_nn_apply_precond(mpm_nn *net, cudaStream_t st, const double *r, const double *rr, const double *adiag,
                                 const unsigned char *bcflag, double mtol, double *z) {
     const int64_t nodec = net->L[0].v;
-    k_input_r<<<blocks(nodec), 256, 0, st>>>(r, rr, nodec, net->x0);
+    k_input_r<<<blocks(nodec), 256, 0, st>>>(r, rr, net->feat, nodec, net->x0);
     CKN(forward(net, st, 1));
     k_output_precond<<<blocks(nodec), 256, 0, st>>>(net->d0, net->p + w5_offset(), net->p + b5_offset(), rr, nodec,
                                                    adiag, bcflag, mtol, z);
@@ -1168,8 +1196,25 @@ mpm_status mpm_nn_apply_precond(mpm_nn *net, cudaStream_t st, const double *r, c
     return MPM_OK;
 }
 
+mpm_status mpm_nn_set_feature(mpm_nn *net, cudaStream_t st, const double *phi) {
+    const int64_t nodec = net->L[0].v;
+    k_feature<<<blocks(nodec), 256, 0, st>>>(phi, nodec, net->feat);
+    CKN(cudaGetLastError());
+    return MPM_OK;
+}
+
+mpm_status mpm_nn_begin_system(mpm_nn *net, cudaStream_t st, const double *phi) {
+    if (net->nsys >= net->sys_cap) return MPM_ERR_BAD_ARG;
+    const int64_t nodec = net->L[0].v;
+    k_feature<<<blocks(nodec), 256, 0, st>>>(phi, nodec, net->data_f + (size_t)net->nsys * nodec * 3);
+    net->nsys++;
+    CKN(cudaGetLastError());
+    return MPM_OK;
+}
+
 mpm_status mpm_nn_append_pair(mpm_nn *net, cudaStream_t st, const double *r, const double *rr, const double *e) {
-    if (net->ndata >= net->data_cap) return MPM_OK;
+    if (net->ndata >= net->data_cap || net->nsys == 0) return MPM_OK;
+    k_set_int<<<1, 1, 0, st>>>(net->data_sys + net->ndata, net->nsys - 1);
     const int64_t nodec = net->L[0].v;
     k_append_pair<<<blocks(nodec), 256, 0, st>>>(r, rr, e, nodec, net->data_r + net->ndata * nodec * 3,
                                                 net->data_e + net->ndata * nodec * 3);

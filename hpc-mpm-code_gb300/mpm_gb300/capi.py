@@ -389,16 +389,16 @@ class PrecondNet:
         return p
 
     def forward(self, x):
-        """x: [batch][nodes][3] float32 -> same shape."""
-        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.nvox, 3)
-        out = np.zeros_like(x)
+        """x: [batch][nodes][6] float32 (residual, features) -> [batch][nodes][3]."""
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.nvox, 6)
+        out = np.zeros(x.shape[:2] + (3,), dtype=np.float32)
         _chk(self.lib.mpm_nn_forward(self.net, x.shape[0], x.ctypes.data_as(_fp32), out.ctypes.data_as(_fp32)),
              "mpm_nn_forward")
         return out
 
     def backward(self, x, gout):
-        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.nvox, 3)
-        g = np.ascontiguousarray(gout, dtype=np.float32).reshape(x.shape)
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, self.nvox, 6)
+        g = np.ascontiguousarray(gout, dtype=np.float32).reshape(x.shape[:2] + (3,))
         grad = np.zeros(self.nparams, dtype=np.float32)
         _chk(self.lib.mpm_nn_backward(self.net, x.shape[0], x.ctypes.data_as(_fp32), g.ctypes.data_as(_fp32),
                                       grad.ctypes.data_as(_fp32)), "mpm_nn_backward")

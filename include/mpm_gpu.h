@@ -223,12 +223,17 @@ mpm_status mpm_gpu_implicit_solve(mpm_ctx *ctx, double eps, int kmax, double *x,
  * when the network stops reducing the residual, so the accuracy of the
  * solution does not depend on the network.
  *
+ * Input channels: the residual (3) and, per degree of freedom, the share of
+ * the diagonal entry that comes from the mass term (3; 1 for a mass-dominated
+ * row, small for a stiffness-dominated one), so that one network serves
+ * systems of different stiffness.  Output: 3 channels.
  * Parameters (FP32, mpm_nn_num_params() values): for the five 3x3x3
- * convolutions l = 0..4 with (cin, cout) = (3,16), (16,32), (32,64),
+ * convolutions l = 0..4 with (cin, cout) = (6,16), (16,32), (32,64),
  * (64,32), (32,16): W_l[27][cin][cout] (tap t = (dx+1) + 3(dy+1) + 9(dz+1))
  * then b_l[cout]; then the 1x1 output layer W5[16][3], b5[3].
- * Host tensors of forward/backward are FP32 [batch][nodes][3] with nodes in
- * control-point order i + nx (j + ny k). */
+ * Host tensors of forward/backward are FP32, input [batch][nodes][6],
+ * output and its gradient [batch][nodes][3], nodes in control-point order
+ * i + nx (j + ny k). */
 typedef struct mpm_nn mpm_nn;
 int64_t mpm_nn_num_params(void);
 /* nodes: control points per direction of the grid the network runs on;
@@ -243,7 +248,8 @@ mpm_status mpm_nn_forward(mpm_nn *net, int batch, const float *in, float *out);
 /* gradient of sum(out * gout) with respect to the parameters */
 mpm_status mpm_nn_backward(mpm_nn *net, int batch, const float *in, const float *gout, float *grad);
 mpm_status mpm_nn_num_pairs(mpm_nn *net, int64_t *n);
-/* Adam on the stored (residual, error) pairs, loss = mean |net(r) - e|^2 / |e|^2;
+/* Adam on the stored (residual, error) pairs, loss = mean |net(r) - e|^2 / |e|^2,
+ * step size lr with a cosine decay to 0 over the call;
  * epoch_loss[epochs] receives the mean loss of each epoch (may be NULL). */
 mpm_status mpm_nn_train(mpm_nn *net, int epochs, int batch, double lr, uint64_t seed, float *epoch_loss);
 /* Use `net` (NULL: none) as the preconditioner of the implicit solves of ctx. */

@@ -6,8 +6,8 @@ The network has no counterpart in the reference (its solid solves use
 GPBiCGSafe, module/solver/solver.cpp:19-141); the definition followed here is
 the one documented in include/mpm_gpu.h and csrc/mpm_nn.cuh:
 
-    x0 = r (3 channels)
-    e0 = relu(conv3(x0; 3->16))          e1 = relu(conv3/2(e0; 16->32))
+    x0 = [r (3 channels), phi (3 channels)]
+    e0 = relu(conv3(x0; 6->16))          e1 = relu(conv3/2(e0; 16->32))
     e2 = relu(conv3/2(e1; 32->64))       c2 = conv3(e2; 64->32)
     d1 = relu(up(c2) + e1)               c1 = conv3(d1; 32->16)
     d0 = relu(up(c1) + e0)               z  = d0 W5 + b5
@@ -22,7 +22,7 @@ from __future__ import annotations
 
 import numpy as np
 
-CIN = (3, 16, 32, 64, 32)
+CIN = (6, 16, 32, 64, 32)
 COUT = (16, 32, 64, 32, 16)
 TAPS = [((t % 3) - 1, ((t // 3) % 3) - 1, (t // 9) - 1) for t in range(27)]   # (dx, dy, dz)
 
@@ -160,7 +160,7 @@ def relu(a):
 
 
 def forward(params, r, bf16=False):
-    """r (B, nz, ny, nx, 3) -> (z, cache)."""
+    """r (B, nz, ny, nx, 6): residual and feature channels -> (z (..., 3), cache)."""
     P = unpack(params)
     q = bf16_round if bf16 else (lambda a: np.asarray(a, dtype=np.float64))
     W = [q(P[f"W{l}"]) for l in range(5)]

@@ -24,8 +24,9 @@ NODES = (17, 12, 10)   # x, y, z control points
 
 def _inputs(seed, batch=2):
     rng = np.random.default_rng(seed)
-    shape = (batch, NODES[2], NODES[1], NODES[0], 3)
-    return rng.normal(size=shape).astype(np.float32), rng.normal(size=shape).astype(np.float32)
+    shape = (batch, NODES[2], NODES[1], NODES[0])
+    x = np.concatenate([rng.normal(size=shape + (3,)), rng.uniform(0.0, 1.0, size=shape + (3,))], axis=-1)
+    return x.astype(np.float32), rng.normal(size=shape + (3,)).astype(np.float32)
 
 
 def test_forward_matches_oracle():
@@ -33,7 +34,7 @@ def test_forward_matches_oracle():
     net = capi.PrecondNet(NODES, max_batch=2)
     net.set_params(p)
     x, _ = _inputs(1)
-    z = net.forward(x.reshape(2, -1, 3)).reshape(x.shape)
+    z = net.forward(x.reshape(2, -1, 6)).reshape(x.shape[:-1] + (3,))
     zq, _ = O.forward(p.astype(np.float64), x.astype(np.float64), bf16=True)
     ze, _ = O.forward(p.astype(np.float64), x.astype(np.float64), bf16=False)
     net.close()
@@ -46,7 +47,7 @@ def test_backward_matches_oracle():
     net = capi.PrecondNet(NODES, max_batch=2)
     net.set_params(p)
     x, g = _inputs(2)
-    grad = net.backward(x.reshape(2, -1, 3), g.reshape(2, -1, 3))
+    grad = net.backward(x.reshape(2, -1, 6), g.reshape(2, -1, 3))
     _, go = O.backward(p.astype(np.float64), x.astype(np.float64), g.astype(np.float64), bf16=True)
     net.close()
     gb, ob = O.unpack(grad), O.unpack(go)
@@ -59,7 +60,7 @@ def test_single_sample_equals_batch():
     net = capi.PrecondNet(NODES, max_batch=2)
     net.set_params(p)
     x, _ = _inputs(3)
-    zb = net.forward(x.reshape(2, -1, 3))
-    z1 = net.forward(x[1].reshape(1, -1, 3))
+    zb = net.forward(x.reshape(2, -1, 6))
+    z1 = net.forward(x[1].reshape(1, -1, 6))
     net.close()
     assert np.array_equal(zb[1], z1[0])

@@ -12,7 +12,7 @@ from oracle import nn_oracle as O
 
 
 def test_parameter_layout():
-    assert O.num_params() == 139747
+    assert O.num_params() == 139747 + 27 * 3 * 16
     p = O.init_params(0)
     assert np.array_equal(O.pack(O.unpack(p)).astype(np.float32), p)
 
@@ -20,8 +20,8 @@ def test_parameter_layout():
 def test_gradients_match_finite_differences():
     rng = np.random.default_rng(7)
     p = O.init_params(3).astype(np.float64)
-    r = rng.normal(size=(1, 6, 7, 9, 3))
-    gz = rng.normal(size=r.shape)
+    r = np.concatenate([rng.normal(size=(1, 6, 7, 9, 3)), rng.uniform(size=(1, 6, 7, 9, 3))], axis=-1)
+    gz = rng.normal(size=(1, 6, 7, 9, 3))
     _, g = O.backward(p, r, gz)
 
     def loss(pp):
