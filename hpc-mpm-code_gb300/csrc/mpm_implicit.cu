@@ -57,6 +57,10 @@ struct ImpState {
     double *xstar = nullptr, *ev = nullptr; // training-pair harvest: converged solution, error
     int fallbacks = 0;                      // solves that switched from the network to Jacobi
     int nn_applications = 0;
+    // CUDA graphs of 8 Krylov iterations (CG; FCG with the network; FCG with Jacobi)
+    cudaGraphExec_t g_cg = nullptr, g_fcg_nn = nullptr, g_fcg_jac = nullptr;
+    mpm_nn *g_net = nullptr;
+    bool no_graph = false;
 };
 
 namespace mpm {
@@ -234,6 +238,7 @@ __device__ __forceinline__ void tangent(const double *da, const double *db, doub
 __global__ void __launch_bounds__(128) k_imp_assemble(ImpArgs a, PView P, const double *ndispl, double *stress_k,
                                                       double *A, double *b) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned live = __ballot_sync(0xffffffffu, p < a.num);
     if (p >= a.num) return;
     const size_t N = (size_t)a.nodec, NP = (size_t)a.num;
     double x[3] = {P.x[0][p], P.x[1][p], P.x[2][p]};
@@ -307,6 +312,24 @@ __global__ void __launch_bounds__(128) k_imp_assemble(ImpArgs a, PView P, const 
     const double m = P.m[p];
     const double fx = a.grav[0] * a.facl, fy = a.grav[1] * a.facl, fz = a.grav[2] * a.facl;
     const double afv = a.af * vol;
+    // Particles are sorted by cell, so aligned groups of 8 lanes often hold the
+    // particles of one cell: such a group adds its 600 values with butterfly
+    // shuffles and only its first lane issues the atomics (8x fewer atomics).
+    // Other lanes add their own values.  (The sum order of FP64 atomics is not
+    // fixed in either case.)
+    const int lane = threadIdx.x & 31;
+    const unsigned gmask = 0xffu << (lane & ~7);
+    const long long key = ((long long)cz * a.nnc[1] + cy) * a.nnc[0] + cx;
+    const bool grouped = (live & gmask) == gmask && (__match_any_sync(live, key) & gmask) == gmask;
+    const bool writer = !grouped || (lane & 7) == 0;
+    auto gsum = [&](double v) {
+        if (grouped) {
+            v += __shfl_xor_sync(gmask, v, 1);
+            v += __shfl_xor_sync(gmask, v, 2);
+            v += __shfl_xor_sync(gmask, v, 4);
+        }
+        return v;
+    };
     for (int qa = 0; qa < 8; qa++) {
         const int na = nid[qa];
         int ia, ja, ka;
@@ -323,15 +346,19 @@ __global__ void __launch_bounds__(128) k_imp_assemble(ImpArgs a, PView P, const 
                 for (int j = 0; j < 3; j++) {
                     double v = afv * K[i][j];
                     if (qa == qb && i == j) v += a.am * emd;
-                    atomicAdd(&A[(size_t)(s * 9 + 3 * i + j) * N + na], v);
+                    v = gsum(v);
+                    if (writer) atomicAdd(&A[(size_t)(s * 9 + 3 * i + j) * N + na], v);
                 }
         }
         const double f0 = -vol * (sk[0] * dN[qa][0] + sk[5] * dN[qa][1] + sk[4] * dN[qa][2]) + Nw[qa] * (m * fx);
         const double f1 = -vol * (sk[5] * dN[qa][0] + sk[1] * dN[qa][1] + sk[3] * dN[qa][2]) + Nw[qa] * (m * fy);
         const double f2 = -vol * (sk[4] * dN[qa][0] + sk[3] * dN[qa][1] + sk[2] * dN[qa][2]) + Nw[qa] * (m * fz);
-        atomicAdd(&b[na], f0);
-        atomicAdd(&b[N + na], f1);
-        atomicAdd(&b[2 * N + na], f2);
+        const double g0 = gsum(f0), g1 = gsum(f1), g2 = gsum(f2);
+        if (writer) {
+            atomicAdd(&b[na], g0);
+            atomicAdd(&b[N + na], g1);
+            atomicAdd(&b[2 * N + na], g2);
+        }
     }
 }
 
@@ -824,6 +851,8 @@ void implicit_free(mpm_ctx *c) {
     for (double *b : bufs)
         if (b) cudaFree(b);
     if (s->h_scal) cudaFreeHost(s->h_scal);
+    for (cudaGraphExec_t g : {s->g_cg, s->g_fcg_nn, s->g_fcg_jac})
+        if (g) cudaGraphExecDestroy(g);
     delete s;
     c->imp = nullptr;
 }
@@ -914,6 +943,47 @@ static mpm_status imp_p2g(mpm_ctx *c, double facl) {
 
 // one linear solve of the assembled, scaled system; s->x holds the initial
 // guess (physical) and receives the physical solution.  Returns iterations.
+static constexpr int KCHECK = 8;   // Krylov iterations between residual checks (and per graph)
+
+static bool graphs_on(mpm_ctx *c) { return c->use_graph && c->stream != nullptr && !c->timer.on && !c->imp->no_graph; }
+
+template <typename F>
+static mpm_status capture_iters(mpm_ctx *c, cudaGraphExec_t *exec, F body) {
+    CKI(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    body();
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return MPM_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        *exec = nullptr;
+        cudaGetLastError();
+        return MPM_ERR_CUDA;
+    }
+    return MPM_OK;
+}
+
+// one CG iteration on the scaled system; `it` fixes the residual-norm slot parity
+static void cg_iteration(mpm_ctx *c, const ImpArgs &a, int nb, int it) {
+    ImpState *s = c->imp;
+    const int cur = (it & 1) ? S_RR1 : S_RR0;
+    timer_begin(c, K_MATVEC);
+    k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->p, s->Ap, s->part);
+    timer_end(c, K_MATVEC);
+    timer_begin(c, K_KRYLOV);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_PAP);
+    k_cg_update<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->xs, s->r, s->p, s->Ap, s->part);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, cur ^ 1);
+    k_cg_dir<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->r, s->p);
+    timer_end(c, K_KRYLOV);
+    c->launches += 5;
+}
+
 static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
     ImpState *s = c->imp;
     ImpArgs a = imp_args(c);
@@ -928,21 +998,24 @@ static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
     const double rr0 = s->h_scal[S_RR0];
     int it = 0;
     bool done = !(rr0 > 1.0e-300);
-    const int check = 8;
     while (!done && it < kmax) {
-        const int cur = (it & 1) ? S_RR1 : S_RR0;
-        timer_begin(c, K_MATVEC);
-        k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->p, s->Ap, s->part);
-        timer_end(c, K_MATVEC);
-        timer_begin(c, K_KRYLOV);
-        k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_PAP);
-        k_cg_update<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->xs, s->r, s->p, s->Ap, s->part);
-        k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, cur ^ 1);
-        k_cg_dir<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->r, s->p);
-        timer_end(c, K_KRYLOV);
-        c->launches += 5;
-        it++;
-        if (it % check == 0 || it == kmax) {
+        if (graphs_on(c) && it % KCHECK == 0 && it + KCHECK <= kmax) {
+            if (!s->g_cg && capture_iters(c, &s->g_cg, [&] {
+                    for (int k = 0; k < KCHECK; k++) cg_iteration(c, a, nb, k);
+                }) != MPM_OK)
+                s->no_graph = true;
+            if (s->g_cg) {
+                CKI(cudaGraphLaunch(s->g_cg, c->stream));
+                it += KCHECK;
+                if (it > KCHECK) c->launches += 5 * KCHECK;   // the capture counted the first block
+            } else {
+                continue;
+            }
+        } else {
+            cg_iteration(c, a, nb, it);
+            it++;
+        }
+        if (it % KCHECK == 0 || it == kmax) {
             CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream));
             CKI(cudaStreamSynchronize(c->stream));
             const double rr = s->h_scal[(it & 1) ? S_RR1 : S_RR0];
@@ -992,26 +1065,26 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
     }
     int restart = 1;
     double rr_window = rr0;
-    const int check = 8;
-    while (!done && it < kmax) {
-        if (use_nn) {
+    const int check = KCHECK;
+    // one FCG iteration: z = M(r), p = z - (z.q'/p'.q') p', q = A p, x, r update
+    auto iteration = [&](bool nn, int rs) -> mpm_status {
+        if (nn) {
             timer_begin(c, K_PRECOND);
             mpm_status st = mpm_nn_apply_precond(s->net, c->stream, s->r, s->scal + S_RRC, s->adiag, a.bcflag, a.mtol,
                                                  s->z);
             timer_end(c, K_PRECOND);
             if (st != MPM_OK) return st;
-            s->nn_applications++;
             c->launches += 9;
         } else {
             CKI(cudaMemcpyAsync(s->z, s->r, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, c->stream));
         }
-        if (!restart) {
+        if (!rs) {
             k_dot3<<<nb, 256, 0, c->stream>>>(a, s->z, s->Ap, s->part);
             k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_ZQ);
             c->launches += 2;
         }
         timer_begin(c, K_KRYLOV);
-        k_fcg_dir<<<nb, 256, 0, c->stream>>>(a, s->scal, restart, s->z, s->r, s->p, s->part);
+        k_fcg_dir<<<nb, 256, 0, c->stream>>>(a, s->scal, rs, s->z, s->r, s->p, s->part);
         k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_PR);
         timer_end(c, K_KRYLOV);
         timer_begin(c, K_MATVEC);
@@ -1023,8 +1096,36 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
         k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
         timer_end(c, K_KRYLOV);
         c->launches += 6;
-        restart = 0;
-        it++;
+        return MPM_OK;
+    };
+    if (s->g_fcg_nn && s->g_net != s->net) {
+        cudaGraphExecDestroy(s->g_fcg_nn);
+        s->g_fcg_nn = nullptr;
+    }
+    while (!done && it < kmax) {
+        cudaGraphExec_t *gx = use_nn ? &s->g_fcg_nn : &s->g_fcg_jac;
+        if (graphs_on(c) && !restart && it % check == 0 && it + check <= kmax) {
+            const int64_t l0 = c->launches;
+            if (!*gx && capture_iters(c, gx, [&] {
+                    for (int k = 0; k < check; k++) iteration(use_nn, 0);
+                }) != MPM_OK)
+                s->no_graph = true;
+            if (*gx) {
+                if (use_nn) s->g_net = s->net;
+                CKI(cudaGraphLaunch(*gx, c->stream));
+                if (c->launches == l0) c->launches += (use_nn ? 17 : 8) * check;
+                if (use_nn) s->nn_applications += check;
+                it += check;
+            } else {
+                continue;
+            }
+        } else {
+            mpm_status st = iteration(use_nn, restart);
+            if (st != MPM_OK) return st;
+            if (use_nn) s->nn_applications++;
+            restart = 0;
+            it++;
+        }
         if (it % check == 0 || it == kmax) {
             CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, c->stream));
             CKI(cudaStreamSynchronize(c->stream));
