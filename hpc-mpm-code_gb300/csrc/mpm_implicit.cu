@@ -1036,8 +1036,8 @@ static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
 
 // One solve of the assembled, scaled system by flexible CG with the learned
 // preconditioner z = net(r) (Notay's FCG(1): p = z - (z.q'/p'.q') p',
-// alpha = p.r / p.q).  The residual is checked every 8 iterations; when it
-// did not drop over a window the solve continues with the Jacobi
+// alpha = p.r / p.q).  The residual is checked every 8 iterations; when two
+// checks in a row find no new minimum the solve continues with the Jacobi
 // preconditioner (z = r in the scaled system).  Convergence is accepted only
 // on the true residual bs - A x, recomputed in FP64.
 static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
@@ -1064,7 +1064,8 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
         if (st != MPM_OK) return st;
     }
     int restart = 1;
-    double rr_window = rr0;
+    double rr_window = rr0;   // smallest residual norm seen at a check
+    int stall = 0;
     const int check = KCHECK;
     // one FCG iteration: z = M(r), p = z - (z.q'/p'.q') p', q = A p, x, r update
     auto iteration = [&](bool nn, int rs) -> mpm_status {
@@ -1146,12 +1147,19 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
                 if (rr < eps * rr0) done = true;
                 else restart = 1;
             }
-            if (!done && use_nn && !(rr < rr_window)) {
+            // the residual norm of a preconditioned solve need not fall at every
+            // check: fall back only after two windows without a new minimum
+            if (rr < rr_window) {
+                rr_window = rr;
+                stall = 0;
+            } else {
+                stall++;
+            }
+            if (!done && use_nn && stall >= 2) {
                 use_nn = false;   // the network stopped reducing the residual
                 restart = 1;
                 s->fallbacks++;
             }
-            rr_window = rr;
             s->last_rel = sqrt(rr / rr0);
         }
     }

@@ -96,9 +96,9 @@ struct Fix {
 // Launch variants that give bitwise identical results; chosen by
 // mpm_gpu_autotune from measured times (defaults otherwise).
 struct Tune {
-    int p2g_staged = 1;             // per-cell P2G reads the brick's particles from bulk-copied shared memory
+    int p2g_staged = 0;             // per-cell P2G reads the brick's particles from bulk-copied shared memory
     int p2g_minb = 2;               // resident CTAs the direct per-cell P2G is compiled for (2 or 3)
-    int musl_staged = 1;            // gather + MUSL reads the brick's particles from staged shared memory
+    int musl_staged = 0;            // gather + MUSL reads the brick's particles from staged shared memory
     int musl_minb = 3;              // resident CTAs the direct gather + MUSL kernel is compiled for
     int update_ctas_per_sm = 4;     // persistent CTAs per SM of the staged particle update
     bool done = false;
