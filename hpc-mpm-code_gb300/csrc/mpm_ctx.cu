@@ -712,7 +712,7 @@ mpm_status mpm_gpu_autotune(mpm_ctx *c, int steps_per_trial, double facl) {
     // every candidate computes bitwise the same step, so the trial steps are
     // ordinary simulation steps; each kernel class is timed on its own
     const int p2g_opts[3] = {2, 3, 2}, stg_opts[3] = {1, 0, 0}, musl_opts[3] = {3, 2, 3}, mstg_opts[3] = {1, 0, 0};
-    const int upd_opts[3] = {4, 3, 6};
+    const int upd_opts[3] = {4, 0, 6};
     double best[3] = {1e300, 1e300, 1e300};
     Tune pick = c->tune;
     const bool was_on = c->timer.on;
@@ -754,7 +754,7 @@ mpm_status mpm_gpu_autotune(mpm_ctx *c, int steps_per_trial, double facl) {
 mpm_status mpm_gpu_set_tuning(mpm_ctx *c, int p2g_minb, int musl_minb, int update_ctas_per_sm) {
     if (!c) return MPM_ERR_BAD_ARG;
     if ((p2g_minb != 0 && p2g_minb != 2 && p2g_minb != 3) || (musl_minb != 0 && musl_minb != 2 && musl_minb != 3) ||
-        update_ctas_per_sm < 1 || update_ctas_per_sm > 8)
+        update_ctas_per_sm < 0 || update_ctas_per_sm > 8)
         return MPM_ERR_BAD_ARG;
     c->tune.p2g_staged = p2g_minb == 0;
     if (p2g_minb) c->tune.p2g_minb = p2g_minb;

@@ -1185,6 +1185,194 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
 // into shared memory by bulk asynchronous copies, two chunks of UCH particles
 // in flight per CTA, so that memory parallelism does not depend on how many
 // warps are resident.  Persistent CTAs walk the chunks with a grid stride.
+// Node values for the particle update: nvel2 (3 components) and nei.
+struct GlobalNodes {
+    const float *nvel2, *nei;
+    size_t N;
+    KGeom<float> g;
+    __device__ __forceinline__ void get(int gx, int gy, int gz, bool shift, float *nv, float &e) const {
+        const size_t gn = node_id(g, gx, gy, gz);
+        nv[0] = ld(nvel2 + gn);
+        nv[1] = ld(nvel2 + N + gn);
+        nv[2] = ld(nvel2 + 2 * N + gn);
+        if (shift) e = ld(nei + gn);
+    }
+};
+
+// The same values from a brick's node box in shared memory, or from global
+// memory for a particle whose cell lies outside the brick.
+struct BoxNodes {
+    const float *box;   // [4][NBX] : nvel2 x, y, z, nei
+    int ox, oy, oz;
+    GlobalNodes gl;
+    static constexpr int NX = BRX + 1, NY = BRY + 1, NZ = BRZ + 1, NBX = NX * NY * NZ;
+    __device__ __forceinline__ bool inside(int cx, int cy, int cz) const {
+        return (unsigned)(cx - ox) < (unsigned)BRX && (unsigned)(cy - oy) < (unsigned)BRY &&
+               (unsigned)(cz - oz) < (unsigned)BRZ;
+    }
+    __device__ __forceinline__ void get(int gx, int gy, int gz, bool shift, float *nv, float &e) const {
+        const int l = (gx - ox) + NX * ((gy - oy) + NY * (gz - oz));
+        nv[0] = box[l];
+        nv[1] = box[NBX + l];
+        nv[2] = box[2 * NBX + l];
+        if (shift) e = box[3 * NBX + l];
+    }
+};
+
+// Second G2P pass of one FP32 particle on linear shape functions
+// (var_trans_solid_explicit.cpp:150-185, 247-296): F from the MUSL nodal
+// velocities, position with shifting, volume and stress, written back.
+template <typename Nodes>
+__device__ __forceinline__ void update_particle(const StepArgs<float> &a, const Particles<float> &P, int p,
+                                                const float *x, const float (*H)[3], const float *s_in, float vol0,
+                                                float volc, int mid, float rb0, const Nodes &nodes, float &volmax,
+                                                float &vsmax, int &bad) {
+    bool oob = false;
+    const int cx = cell_of(x[0], a.g, 0, oob), cy = cell_of(x[1], a.g, 1, oob), cz = cell_of(x[2], a.g, 2, oob);
+    Axis<float, 1> ax, ay, az;
+    axis_eval<float, 1>(x[0], a.g, 0, cx, ax);
+    axis_eval<float, 1>(x[1], a.g, 1, cy, ay);
+    axis_eval<float, 1>(x[2], a.g, 2, cz, az);
+    float D[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    float du[3] = {0, 0, 0}, gu[3] = {0, 0, 0};
+    const bool shift = rb0 != 0.0f;
+#pragma unroll
+    for (int k = 0; k < 2; k++)
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const float wxy = ax.w[i] * ay.w[j];
+                const float N_ = wxy * az.w[k];
+                const float dn[3] = {ax.dw[i] * ay.w[j] * az.w[k], ax.w[i] * ay.dw[j] * az.w[k], wxy * az.dw[k]};
+                float nv[3], e = 0.0f;
+                nodes.get(cx + i, cy + j, cz + k, shift, nv, e);
+#pragma unroll
+                for (int r = 0; r < 3; r++)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) D[r][c] += dn[c] * nv[r] * a.dt;
+#pragma unroll
+                for (int c = 0; c < 3; c++) du[c] += N_ * nv[c];
+                if (shift) {
+#pragma unroll
+                    for (int c = 0; c < 3; c++) gu[c] += dn[c] * e;
+                }
+            }
+    float xn[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) xn[c] = x[c] + du[c] * a.dt;
+    if (shift) {
+        const float tv = 2.0f * volc;
+#pragma unroll
+        for (int c = 0; c < 3; c++) xn[c] += -rb0 * (gu[c] * tv);
+    }
+    // H <- H + D + D H (the FP32 path stores H = F - I)
+    float Hn[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            float acc = H[r][c] + D[r][c];
+#pragma unroll
+            for (int k2 = 0; k2 < 3; k2++) acc += D[r][k2] * H[k2][c];
+            Hn[r][c] = acc;
+        }
+    const float jm1 = det_ipm1(Hn);
+    const float J = 1.0f + jm1;
+    const float volp = J * vol0;
+    float s[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) s[k] = s_in[k];
+    const int model = a.iprop[mid];
+    const float E = (float)a.matprop[3 * mid], nu = (float)a.matprop[3 * mid + 1];
+    if (model == 0) lin_elast_update(s, D, E, nu);
+    else if (model == 1) neo_hookean_stress_h(s, Hn, jm1, E, nu);
+    else if (model == 2)
+        tait_stress<float>(s, D, jm1, P.m[p] / vol0, E, nu, (float)a.matprop[3 * mid + 2], 1.0f / a.dt);
+    else if (model == -1)
+#pragma unroll
+        for (int k = 0; k < 6; k++) s[k] = 0.0f;
+    const bool fin = isfinite(xn[0]) && isfinite(xn[1]) && isfinite(xn[2]) && isfinite(J) && isfinite(s[0]) &&
+                     isfinite(s[1]) && isfinite(s[2]) && isfinite(s[3]) && isfinite(s[4]) && isfinite(s[5]);
+    bad += !fin;
+#pragma unroll
+    for (int c = 0; c < 3; c++) P.x[c][p] = xn[c];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) P.F[3 * r + c][p] = Hn[r][c];
+#pragma unroll
+    for (int k = 0; k < 6; k++) P.s[k][p] = s[k];
+    P.vol[p] = volp;
+    const float rs0 = fabsf(s[0]) + fabsf(s[5]) + fabsf(s[4]);
+    const float rs1 = fabsf(s[5]) + fabsf(s[1]) + fabsf(s[3]);
+    const float rs2 = fabsf(s[4]) + fabsf(s[3]) + fabsf(s[2]);
+    const float vf = fabsf(volp);
+    volmax = fmaxf(volmax, vf);
+    vsmax = fmaxf(vsmax, vf * fmaxf(rs0, fmaxf(rs1, rs2)));
+}
+
+// Particle update, one CTA per brick: the brick's node box (nvel2, nei) is
+// loaded into shared memory once, then the brick's particles (a contiguous
+// range) are updated one per thread with coalesced loads and stores.
+__global__ void __launch_bounds__(256) k_g2p_update_brick(StepArgs<float> a) {
+    constexpr int NBX = BoxNodes::NBX;
+    __shared__ float box[4 * NBX];
+    __shared__ float sh_f[32];
+    __shared__ int sh_i[32];
+    const int b = blockIdx.x;
+    const int *cs = a.cstart + (size_t)b * (BRC + 1);
+    const int P0 = cs[0], P1 = cs[BRC];
+    if (P0 == P1) return;
+    const size_t N = (size_t)a.g.nodec;
+    BoxNodes nodes;
+    brick_origin(b, a.nbrick, nodes.ox, nodes.oy, nodes.oz);
+    nodes.box = box;
+    nodes.gl = GlobalNodes{a.nvel2, a.nei, N, a.g};
+    const float rb0 = (float)a.ctl->b0;
+    for (int l = threadIdx.x; l < NBX; l += blockDim.x) {
+        const int nx = l % BoxNodes::NX, ny = (l / BoxNodes::NX) % BoxNodes::NY, nz = l / (BoxNodes::NX * BoxNodes::NY);
+        const int gx = min(nodes.ox + nx, a.g.nnc[0] - 1), gy = min(nodes.oy + ny, a.g.nnc[1] - 1),
+                  gz = min(nodes.oz + nz, a.g.nnc[2] - 1);
+        const size_t gn = node_id(a.g, gx, gy, gz);
+        box[l] = ld(a.nvel2 + gn);
+        box[NBX + l] = ld(a.nvel2 + N + gn);
+        box[2 * NBX + l] = ld(a.nvel2 + 2 * N + gn);
+        box[3 * NBX + l] = rb0 != 0.0f ? ld(a.nei + gn) : 0.0f;
+    }
+    __syncthreads();
+    const Particles<float> &P = a.P;
+    float volmax = 0.0f, vsmax = 0.0f;
+    int bad = 0;
+    for (int p = P0 + threadIdx.x; p < P1; p += blockDim.x) {
+        float x[3] = {ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p)};
+        float H[3][3];
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) H[r][c] = ld(P.F[3 * r + c] + p);
+        float s6[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) s6[k] = ld(P.s[k] + p);
+        bool oob = false;
+        const int cx = cell_of(x[0], a.g, 0, oob), cy = cell_of(x[1], a.g, 1, oob), cz = cell_of(x[2], a.g, 2, oob);
+        if (nodes.inside(cx, cy, cz))
+            update_particle(a, P, p, x, H, s6, ld(P.vol0 + p), ld(P.vol + p), P.matid[p], rb0, nodes, volmax, vsmax,
+                            bad);
+        else
+            update_particle(a, P, p, x, H, s6, ld(P.vol0 + p), ld(P.vol + p), P.matid[p], rb0, nodes.gl, volmax,
+                            vsmax, bad);
+    }
+    const float vm = block_reduce(volmax, OpMaxF(), sh_f);
+    const float sm = block_reduce(vsmax, OpMaxF(), sh_f);
+    const int nb = block_reduce(bad, OpAddI(), sh_i);
+    if (threadIdx.x == 0) {
+        if (vm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VOLMAX], vm * 1.000001f);
+        if (sm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VOLSMAX], sm * 1.000001f);
+        if (nb) atomicAdd(&a.ctl->err_nonfinite, (unsigned)nb);
+    }
+}
+
 constexpr int UCH = 256;                          // particles per chunk (= threads per CTA)
 constexpr int UNF = 20;                           // staged real fields
 constexpr size_t USTAGE = (size_t)UNF * UCH * 4 + UCH * 4;   // bytes per stage
@@ -1235,96 +1423,17 @@ __global__ void __launch_bounds__(UCH) k_g2p_update_tma(StepArgs<float> a, int n
         const int p = chunk * UCH + t;
         if (p < a.num) {
             float x[3] = {sf[0 * UCH + t], sf[1 * UCH + t], sf[2 * UCH + t]};
-            bool oob = false;
-            const int cx = cell_of(x[0], a.g, 0, oob), cy = cell_of(x[1], a.g, 1, oob), cz = cell_of(x[2], a.g, 2, oob);
-            Axis<float, 1> ax, ay, az;
-            axis_eval<float, 1>(x[0], a.g, 0, cx, ax);
-            axis_eval<float, 1>(x[1], a.g, 1, cy, ay);
-            axis_eval<float, 1>(x[2], a.g, 2, cz, az);
-            float D[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-            float du[3] = {0, 0, 0}, gu[3] = {0, 0, 0};
-#pragma unroll
-            for (int k = 0; k < 2; k++)
-#pragma unroll
-                for (int j = 0; j < 2; j++)
-#pragma unroll
-                    for (int i = 0; i < 2; i++) {
-                        const float wxy = ax.w[i] * ay.w[j];
-                        const float N_ = wxy * az.w[k];
-                        const float dn[3] = {ax.dw[i] * ay.w[j] * az.w[k], ax.w[i] * ay.dw[j] * az.w[k], wxy * az.dw[k]};
-                        const size_t gn = node_id(a.g, cx + i, cy + j, cz + k);
-                        const float nv[3] = {ld(a.nvel2 + gn), ld(a.nvel2 + N + gn), ld(a.nvel2 + 2 * N + gn)};
-#pragma unroll
-                        for (int r = 0; r < 3; r++)
-#pragma unroll
-                            for (int c = 0; c < 3; c++) D[r][c] += dn[c] * nv[r] * a.dt;
-#pragma unroll
-                        for (int c = 0; c < 3; c++) du[c] += N_ * nv[c];
-                        if (rb0 != 0.0f) {
-                            const float e = ld(a.nei + gn);
-#pragma unroll
-                            for (int c = 0; c < 3; c++) gu[c] += dn[c] * e;
-                        }
-                    }
-            float xn[3];
-#pragma unroll
-            for (int c = 0; c < 3; c++) xn[c] = x[c] + du[c] * a.dt;
-            if (rb0 != 0.0f) {
-                const float tv = 2.0f * sf[19 * UCH + t];
-#pragma unroll
-                for (int c = 0; c < 3; c++) xn[c] += -rb0 * (gu[c] * tv);
-            }
-            // H <- H + D + D H (the FP32 path stores H = F - I)
-            float H[3][3], Hn[3][3];
+            float H[3][3];
 #pragma unroll
             for (int r = 0; r < 3; r++)
 #pragma unroll
                 for (int c = 0; c < 3; c++) H[r][c] = sf[(3 + 3 * r + c) * UCH + t];
+            float s6[6];
 #pragma unroll
-            for (int r = 0; r < 3; r++)
-#pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    float acc = H[r][c] + D[r][c];
-#pragma unroll
-                    for (int k2 = 0; k2 < 3; k2++) acc += D[r][k2] * H[k2][c];
-                    Hn[r][c] = acc;
-                }
-            const float jm1 = det_ipm1(Hn);
-            const float J = 1.0f + jm1;
-            const float volp = J * sf[18 * UCH + t];
-            float s[6];
-#pragma unroll
-            for (int k = 0; k < 6; k++) s[k] = sf[(12 + k) * UCH + t];
-            const int mid = smid[t];
-            const int model = a.iprop[mid];
-            const float E = (float)a.matprop[3 * mid], nu = (float)a.matprop[3 * mid + 1];
-            if (model == 0) lin_elast_update(s, D, E, nu);
-            else if (model == 1) neo_hookean_stress_h(s, Hn, jm1, E, nu);
-            else if (model == 2)
-                tait_stress<float>(s, D, jm1, P.m[p] / sf[18 * UCH + t], E, nu, (float)a.matprop[3 * mid + 2],
-                                   1.0f / a.dt);
-            else if (model == -1)
-#pragma unroll
-                for (int k = 0; k < 6; k++) s[k] = 0.0f;
-            const bool fin = isfinite(xn[0]) && isfinite(xn[1]) && isfinite(xn[2]) && isfinite(J) &&
-                             isfinite(s[0]) && isfinite(s[1]) && isfinite(s[2]) && isfinite(s[3]) && isfinite(s[4]) &&
-                             isfinite(s[5]);
-            bad += !fin;
-#pragma unroll
-            for (int c = 0; c < 3; c++) P.x[c][p] = xn[c];
-#pragma unroll
-            for (int r = 0; r < 3; r++)
-#pragma unroll
-                for (int c = 0; c < 3; c++) P.F[3 * r + c][p] = Hn[r][c];
-#pragma unroll
-            for (int k = 0; k < 6; k++) P.s[k][p] = s[k];
-            P.vol[p] = volp;
-            const float rs0 = fabsf(s[0]) + fabsf(s[5]) + fabsf(s[4]);
-            const float rs1 = fabsf(s[5]) + fabsf(s[1]) + fabsf(s[3]);
-            const float rs2 = fabsf(s[4]) + fabsf(s[3]) + fabsf(s[2]);
-            const float vf = fabsf(volp);
-            volmax = fmaxf(volmax, vf);
-            vsmax = fmaxf(vsmax, vf * fmaxf(rs0, fmaxf(rs1, rs2)));
+            for (int k = 0; k < 6; k++) s6[k] = sf[(12 + k) * UCH + t];
+            GlobalNodes gnodes{a.nvel2, a.nei, N, a.g};
+            update_particle(a, P, p, x, H, s6, sf[18 * UCH + t], sf[19 * UCH + t], smid[t], rb0, gnodes, volmax,
+                            vsmax, bad);
         }
         __syncthreads();   // the stage is refilled only after every thread has read it
     }
@@ -1489,7 +1598,10 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
         timer_begin(c, K_G2P_UPDATE);
         bool staged = false;
         if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
-            if (c->tma_update) {
+            if (c->tma_update && c->tune.update_ctas_per_sm == 0) {
+                k_g2p_update_brick<<<c->g.nbricks, 256, 0, c->stream>>>(a);
+                staged = true;
+            } else if (c->tma_update) {
                 const int nchunks = (int)((c->num + UCH - 1) / UCH);
                 static bool attr = false;
                 if (!attr) {

@@ -20,8 +20,10 @@
 //
 // Matrix storage: for control point n and stencil slot s (the 27 neighbours
 // n + (dx, dy, dz), dx,dy,dz in {-1,0,1}, s = (dx+1) + 3 (dy+1) + 9 (dz+1)),
-// the 3x3 block entry (a, b) lives at A[(s * 9 + 3 a + b) * nodec + n]:
-// coalesced over n, no column indices (the grid is structured).
+// the 3x3 block entry q = s * 9 + 3 a + b lives at A[aidx(q, n)], tiled by
+// 32 control points: ((n / 32) * 243 + q) * 32 + n % 32.  A warp reading
+// its 32 nodes' 243 values walks one contiguous 62 KB range (coalesced and
+// DRAM-page friendly); no column indices (the grid is structured).
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -37,7 +39,7 @@ mpm_status run_p2g(mpm_ctx *c, double facl);
 struct ImpState {
     int nr_flag = 0;
     double alpha_f = 1, alpha_m = 1, gamma = 0.5, beta = 0.25, nb[6] = {0};
-    double *A = nullptr;                   // 27 * 9 * nodec
+    double *A = nullptr;                   // 243 values per node, tiled by 32 nodes (aidx)
     double *adiag = nullptr, *b = nullptr;  // 3 * nodec
     double *x = nullptr, *r = nullptr, *p = nullptr, *Ap = nullptr, *xs = nullptr;
     double *ndispl = nullptr, *nvel = nullptr, *naccel = nullptr, *naccel_k = nullptr;
@@ -84,6 +86,11 @@ struct ImpArgs {
     const int *iprop;
     const double *matprop;
 };
+
+__host__ __device__ __forceinline__ size_t aidx(int q, int n) {
+    return (((size_t)(n >> 5) * 243 + (size_t)q) << 5) + (size_t)(n & 31);
+}
+static size_t a_size(int nodec) { return (size_t)((nodec + 31) / 32) * 32 * 243; }
 
 static ImpArgs imp_args(mpm_ctx *c) {
     ImpArgs a;
@@ -238,7 +245,6 @@ __device__ __forceinline__ void tangent(const double *da, const double *db, doub
 __global__ void __launch_bounds__(128) k_imp_assemble(ImpArgs a, PView P, const double *ndispl, double *stress_k,
                                                       double *A, double *b) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned live = __ballot_sync(0xffffffffu, p < a.num);
     if (p >= a.num) return;
     const size_t N = (size_t)a.nodec, NP = (size_t)a.num;
     double x[3] = {P.x[0][p], P.x[1][p], P.x[2][p]};
@@ -312,24 +318,6 @@ __global__ void __launch_bounds__(128) k_imp_assemble(ImpArgs a, PView P, const 
     const double m = P.m[p];
     const double fx = a.grav[0] * a.facl, fy = a.grav[1] * a.facl, fz = a.grav[2] * a.facl;
     const double afv = a.af * vol;
-    // Particles are sorted by cell, so aligned groups of 8 lanes often hold the
-    // particles of one cell: such a group adds its 600 values with butterfly
-    // shuffles and only its first lane issues the atomics (8x fewer atomics).
-    // Other lanes add their own values.  (The sum order of FP64 atomics is not
-    // fixed in either case.)
-    const int lane = threadIdx.x & 31;
-    const unsigned gmask = 0xffu << (lane & ~7);
-    const long long key = ((long long)cz * a.nnc[1] + cy) * a.nnc[0] + cx;
-    const bool grouped = (live & gmask) == gmask && (__match_any_sync(live, key) & gmask) == gmask;
-    const bool writer = !grouped || (lane & 7) == 0;
-    auto gsum = [&](double v) {
-        if (grouped) {
-            v += __shfl_xor_sync(gmask, v, 1);
-            v += __shfl_xor_sync(gmask, v, 2);
-            v += __shfl_xor_sync(gmask, v, 4);
-        }
-        return v;
-    };
     for (int qa = 0; qa < 8; qa++) {
         const int na = nid[qa];
         int ia, ja, ka;
@@ -346,19 +334,15 @@ __global__ void __launch_bounds__(128) k_imp_assemble(ImpArgs a, PView P, const 
                 for (int j = 0; j < 3; j++) {
                     double v = afv * K[i][j];
                     if (qa == qb && i == j) v += a.am * emd;
-                    v = gsum(v);
-                    if (writer) atomicAdd(&A[(size_t)(s * 9 + 3 * i + j) * N + na], v);
+                    atomicAdd(&A[aidx(s * 9 + 3 * i + j, na)], v);
                 }
         }
         const double f0 = -vol * (sk[0] * dN[qa][0] + sk[5] * dN[qa][1] + sk[4] * dN[qa][2]) + Nw[qa] * (m * fx);
         const double f1 = -vol * (sk[5] * dN[qa][0] + sk[1] * dN[qa][1] + sk[3] * dN[qa][2]) + Nw[qa] * (m * fy);
         const double f2 = -vol * (sk[4] * dN[qa][0] + sk[3] * dN[qa][1] + sk[2] * dN[qa][2]) + Nw[qa] * (m * fz);
-        const double g0 = gsum(f0), g1 = gsum(f1), g2 = gsum(f2);
-        if (writer) {
-            atomicAdd(&b[na], g0);
-            atomicAdd(&b[N + na], g1);
-            atomicAdd(&b[2 * N + na], g2);
-        }
+        atomicAdd(&b[na], f0);
+        atomicAdd(&b[N + na], f1);
+        atomicAdd(&b[2 * N + na], f2);
     }
 }
 
@@ -372,7 +356,7 @@ __global__ void k_imp_rhs_diag(ImpArgs a, const double *A, const double *nmass, 
     for (int c = 0; c < 3; c++) {
         const double aam = a.am * naccel_k[c * N + n] + (1.0 - a.am) * naccel[c * N + n];
         b[c * N + n] -= nmass[n] * aam;
-        const double dg = fabs(A[(size_t)(13 * 9 + 4 * c) * N + n]);
+        const double dg = fabs(A[aidx(13 * 9 + 4 * c, n)]);
         adiag[c * N + n] = dg < a.mtol ? 0.0 : 1.0 / sqrt(dg);
     }
 }
@@ -389,7 +373,7 @@ __global__ void k_imp_scale(ImpArgs a, double *A, const double *adiag) {
         if (ii < 0 || jj < 0 || kk < 0 || ii >= a.nnc[0] || jj >= a.nnc[1] || kk >= a.nnc[2]) continue;
         const size_t col = ii + (size_t)a.nnc[0] * (jj + (size_t)a.nnc[1] * kk);
         for (int r = 0; r < 3; r++)
-            for (int c = 0; c < 3; c++) A[(size_t)(s * 9 + 3 * r + c) * N + n] *= adiag[r * N + n] * adiag[c * N + col];
+            for (int c = 0; c < 3; c++) A[aidx(s * 9 + 3 * r + c, n)] *= adiag[r * N + n] * adiag[c * N + col];
     }
 }
 
@@ -431,10 +415,10 @@ __global__ void __launch_bounds__(256) k_imp_matvec(ImpArgs a, const double *A, 
             if (ii < 0 || jj < 0 || kk < 0 || ii >= a.nnc[0] || jj >= a.nnc[1] || kk >= a.nnc[2]) continue;
             const size_t col = ii + (size_t)a.nnc[0] * (jj + (size_t)a.nnc[1] * kk);
             const double x0 = x[col], x1 = x[N + col], x2 = x[2 * N + col];
-            const double *As = A + (size_t)s * 9 * N + n;
-            acc[0] += As[0 * N] * x0 + As[1 * N] * x1 + As[2 * N] * x2;
-            acc[1] += As[3 * N] * x0 + As[4 * N] * x1 + As[5 * N] * x2;
-            acc[2] += As[6 * N] * x0 + As[7 * N] * x1 + As[8 * N] * x2;
+            const double *As = A + aidx(s * 9, n);   // entry e of the block at As[32 e]
+            acc[0] += As[0 * 32] * x0 + As[1 * 32] * x1 + As[2 * 32] * x2;
+            acc[1] += As[3 * 32] * x0 + As[4 * 32] * x1 + As[5 * 32] * x2;
+            acc[2] += As[6 * 32] * x0 + As[7 * 32] * x1 + As[8 * 32] * x2;
         }
         const unsigned char bf = a.bcflag[n];
         for (int c = 0; c < 3; c++) {
@@ -782,8 +766,9 @@ __global__ void k_sub3(const double *xstar, const double *x, double *e, int n) {
 }
 
 // seeded random right-hand side of the scaled system for training-pair
-// harvesting: a few random low-wavenumber cosine modes per component plus
-// white noise, zero on inactive and boundary rows
+// harvesting: a few random low-wavenumber cosine modes per component
+// (wavenumber 0, a uniform load, included) plus white noise, zero on
+// inactive and boundary rows
 __device__ __forceinline__ uint64_t hash64(uint64_t z) {
     z += 0x9E3779B97F4A7C15ull;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -804,8 +789,8 @@ __global__ void k_random_rhs(ImpArgs a, const double *adiag, uint64_t seed, doub
         double v = 0.0;
         for (int m = 0; m < 4; m++) {
             const uint64_t key = seed * 1315423911ull + (uint64_t)(c * 4 + m) * 97;
-            const double kx = 1.0 + floor(4.0 * hash_unit(key + 1)), ky = 1.0 + floor(4.0 * hash_unit(key + 2));
-            const double kz = 1.0 + floor(4.0 * hash_unit(key + 3));
+            const double kx = floor(4.0 * hash_unit(key + 1)), ky = floor(4.0 * hash_unit(key + 2));
+            const double kz = floor(4.0 * hash_unit(key + 3));
             const double ph = 6.283185307179586 * hash_unit(key + 4);
             const double amp = 2.0 * hash_unit(key + 5) - 1.0;
             v += amp * cos(3.141592653589793 * (kx * i / a.nnc[0] + ky * j / a.nnc[1] + kz * k / a.nnc[2]) + ph);
@@ -900,7 +885,7 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
     s->nb[4] = 1.0 / (b * dt);
     s->nb[5] = 1.0 / (2.0 * b) - 1.0;
     const size_t N = (size_t)c->g.nodec;
-    CKI(cudaMalloc((void **)&s->A, sizeof(double) * 27 * 9 * N));
+    CKI(cudaMalloc((void **)&s->A, sizeof(double) * a_size((int)N)));
     double **vec3[] = {&s->adiag, &s->b,    &s->x,       &s->r, &s->p,  &s->Ap,    &s->xs, &s->ndispl,
                        &s->nvel,  &s->naccel, &s->naccel_k, &s->z, &s->bs, &s->xstar, &s->ev};
     for (double **v : vec3) CKI(cudaMalloc((void **)v, sizeof(double) * 3 * N));
@@ -1174,7 +1159,7 @@ static mpm_status imp_assemble(mpm_ctx *c) {
     ImpState *s = c->imp;
     ImpArgs a = imp_args(c);
     const size_t N = (size_t)c->g.nodec;
-    CKI(cudaMemsetAsync(s->A, 0, sizeof(double) * 27 * 9 * N, c->stream));
+    CKI(cudaMemsetAsync(s->A, 0, sizeof(double) * a_size((int)N), c->stream));
     CKI(cudaMemsetAsync(s->b, 0, sizeof(double) * 3 * N, c->stream));
     PView P = pview(c);
     const int pb = (int)((c->num + 127) / 128);
@@ -1339,7 +1324,12 @@ mpm_status mpm_gpu_implicit_get_system(mpm_ctx *c, double *stencil, double *adia
     ImpState *s = c->imp;
     const size_t N = (size_t)c->g.nodec;
     CKI(cudaStreamSynchronize(c->stream));
-    if (stencil) CKI(cudaMemcpy(stencil, s->A, sizeof(double) * 27 * 9 * N, cudaMemcpyDeviceToHost));
+    if (stencil) {
+        std::vector<double> t(a_size((int)N));
+        CKI(cudaMemcpy(t.data(), s->A, sizeof(double) * t.size(), cudaMemcpyDeviceToHost));
+        for (int q = 0; q < 243; q++)
+            for (size_t n = 0; n < N; n++) stencil[(size_t)q * N + n] = t[aidx(q, (int)n)];
+    }
     if (adiag) CKI(cudaMemcpy(adiag, s->adiag, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost));
     if (b_rhs) CKI(cudaMemcpy(b_rhs, s->b, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost));
     return MPM_OK;
@@ -1456,9 +1446,14 @@ mpm_status mpm_gpu_implicit_harvest(mpm_ctx *c, mpm_nn *net, int nsystems, int l
         }
         for (int ld = 0; ld < loads_per_system && st == MPM_OK; ld++) {
             const uint64_t key = seed * 1000003ull + (uint64_t)sys * 1009ull + (uint64_t)ld;
-            // alternate smooth-dominated and noise-dominated loads
-            const double smooth = (ld & 1) ? 0.2 : 1.0, noise = (ld & 1) ? 1.0 : 0.2;
-            k_random_rhs<<<nb, 256, 0, c->stream>>>(a, s->adiag, key, smooth, noise, s->bs);
+            if (ld == 0) {
+                // the assembled system's own right-hand side (body force and inertia)
+                k_cg_scale_in<<<nb, 256, 0, c->stream>>>(a, s->x, s->b, s->adiag, s->xs, s->bs);
+            } else {
+                // alternate smooth-dominated and noise-dominated loads
+                const double smooth = (ld & 1) ? 0.2 : 1.0, noise = (ld & 1) ? 1.0 : 0.2;
+                k_random_rhs<<<nb, 256, 0, c->stream>>>(a, s->adiag, key, smooth, noise, s->bs);
+            }
             int K = 0;
             st = cg_scaled(c, eps, kmax, nullptr, 1, 0, &K);
             if (st != MPM_OK) break;

@@ -131,16 +131,41 @@ struct ConvArgs {
     int *err;
 };
 
+// Taps gathered per pipeline stage: a whole 3x3 plane (9) when the stage
+// fits, else a row of 3.
 template <int K, int N>
-constexpr size_t conv_smem() {
-    return 27u * N * K * 2 + 2u * 128 * K * 2;
+__host__ __device__ constexpr int conv_tg() {
+    return (27u * N * K * 2 + 2u * 9 * 128 * K * 2 <= 200u * 1024) ? 9 : 3;
 }
 
+template <int K, int N>
+__host__ __device__ constexpr size_t conv_smem() {
+    return 27u * N * K * 2 + 2u * conv_tg<K, N>() * 128 * K * 2;
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_wait() {
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+// Per tile of 128 output nodes the 27 taps are processed in groups of TG:
+// every thread gathers its row of the group's TG input tiles with 16-byte
+// cp.async copies (zero-filled for padding, no registers held), so TG taps'
+// loads are in flight at once; then one thread issues the group's MMAs and
+// commits them to the stage's mbarrier.  Two stages: a stage is refilled
+// only after the MMAs that read it completed.
 template <int K, int N, int MODE>
 __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a) {
+    constexpr int TG = conv_tg<K, N>();
+    constexpr int NG = 27 / TG;
     constexpr uint32_t WT = (uint32_t)N * K * 2;        // one tap's weight tile
     constexpr uint32_t WB = 27u * WT;
-    constexpr uint32_t AB = 128u * K * 2;               // one A stage
+    constexpr uint32_t AB = 128u * K * 2;               // one tap's A tile
+    constexpr uint32_t SB = TG * AB;                    // one stage
     constexpr uint32_t TCOLS = N < 32 ? 32 : N;
     constexpr uint32_t IDESC = tc::idesc_bf16(128, N);
     constexpr uint32_t SBO = K * 16;
@@ -165,41 +190,48 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a) {
     tc::fence_after();
     const uint32_t taddr = tslot;
     const uint32_t sw = smem_addr(smem), sa = sw + WB;
-    unsigned char *pa = smem + WB;
+    // this thread's row inside a tap tile: (row / 8) * SBO + (row % 8) * 16
+    const uint32_t rowoff = (uint32_t)(tid >> 3) * SBO + (uint32_t)(tid & 7) * 16;
     const int64_t ntile = (a.rows + 127) / 128;
-    uint32_t it = 0;
+    uint32_t it = 0;   // stage uses so far
     bool ok = true;
     for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
         const int64_t row = tile * 128 + tid;
         const bool valid = row < a.rows;
         int b = 0, ox = 0, oy = 0, oz = 0;
         if (valid) row_coords(row, a.lout, b, ox, oy, oz);
-        for (int t = 0; t < 27; t++) {
+        for (int g = 0; g < NG; g++) {
             const uint32_t s = it & 1;
             bool mine = true;
             if (it >= 2) mine = mbar_wait_bounded(&bar[s], ((it >> 1) - 1) & 1, TC_WAIT);
-            const int64_t src = valid ? gather_src<MODE>(b, ox, oy, oz, t, a.lin) : -1;
-            uint4 *dst = reinterpret_cast<uint4 *>(pa + s * AB + (tid >> 3) * SBO + (tid & 7) * 16);
-            const uint4 *in = reinterpret_cast<const uint4 *>(a.in + (src >= 0 ? src : 0) * K);
-#pragma unroll
-            for (int kc = 0; kc < K / 8; kc++) {
-                uint4 v = make_uint4(0u, 0u, 0u, 0u);
-                if (src >= 0) v = __ldg(in + kc);
-                dst[kc * 8] = v;
-            }
-            tc::fence_async_smem();
-            tc::fence_before();
             if (!__syncthreads_and(mine)) {
                 ok = false;
                 break;
             }
+#pragma unroll
+            for (int tl = 0; tl < TG; tl++) {
+                const int t = g * TG + tl;
+                const int64_t src = valid ? gather_src<MODE>(b, ox, oy, oz, t, a.lin) : -1;
+                const bf16 *in = a.in + (src >= 0 ? src : 0) * K;
+                const uint32_t dst = sa + s * SB + tl * AB + rowoff;
+#pragma unroll
+                for (int kc = 0; kc < K / 8; kc++) cp_async16(dst + kc * 128, in + kc * 8, src >= 0);
+            }
+            cp_async_commit_wait();
+            tc::fence_async_smem();
+            tc::fence_before();
+            __syncthreads();
             if (tid == 0) {
                 tc::fence_after();
 #pragma unroll
-                for (int kk = 0; kk < K / 16; kk++) {
-                    const uint64_t ad = tc::sdesc(sa + s * AB + kk * 256, 128, SBO);
-                    const uint64_t bd = tc::sdesc(sw + t * WT + kk * 256, 128, SBO);
-                    tc::mma_bf16(taddr, ad, bd, IDESC, (t | kk) != 0);
+                for (int tl = 0; tl < TG; tl++) {
+                    const int t = g * TG + tl;
+#pragma unroll
+                    for (int kk = 0; kk < K / 16; kk++) {
+                        const uint64_t ad = tc::sdesc(sa + s * SB + tl * AB + kk * 256, 128, SBO);
+                        const uint64_t bd = tc::sdesc(sw + t * WT + kk * 256, 128, SBO);
+                        tc::mma_bf16(taddr, ad, bd, IDESC, (t | kk) != 0);
+                    }
                 }
                 tc::mma_commit(&bar[s]);
             }
@@ -801,7 +833,7 @@ cudaError_t launch_conv(mpm_nn *net, cudaStream_t st, const bf16 *in, bf16 *out,
     a.rows = (int64_t)batch * lout.v;
     a.err = net->err;
     const int64_t ntile = (a.rows + 127) / 128;
-    const int per_sm = smem <= 50000 ? 4 : smem <= 70000 ? 3 : smem <= 110000 ? 2 : 1;
+    const int per_sm = std::max<int>(1, std::min<int>(4, (int)(220000 / smem)));
     const int grid = (int)std::min<int64_t>(ntile, (int64_t)net->nsm * per_sm);
     k_conv_tc<K, N, MODE><<<grid, 128, smem, st>>>(a);
     return cudaGetLastError();

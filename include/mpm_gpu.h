@@ -171,7 +171,9 @@ mpm_status mpm_gpu_enable_kernel_timing(mpm_ctx *ctx, int on);
 mpm_status mpm_gpu_autotune(mpm_ctx *ctx, int steps_per_trial, double facl);
 /* p2g_minb / musl_minb: 0 = the shared-memory staged kernel, 2 or 3 = the
  * direct per-cell kernel compiled for that many resident CTAs per SM;
- * update_ctas_per_sm: 1..8. */
+ * update_ctas_per_sm: 1..8 persistent CTAs per SM of the bulk-copy staged
+ * particle update, 0 = the update with one CTA per brick and the brick's
+ * nodal values in shared memory. */
 mpm_status mpm_gpu_get_tuning(mpm_ctx *ctx, int *p2g_minb, int *musl_minb, int *update_ctas_per_sm);
 mpm_status mpm_gpu_set_tuning(mpm_ctx *ctx, int p2g_minb, int musl_minb, int update_ctas_per_sm);
 mpm_status mpm_gpu_kernel_times(mpm_ctx *ctx, int *count, const char **names, double *ms, int64_t *launches);
@@ -256,8 +258,8 @@ mpm_status mpm_nn_train(mpm_nn *net, int epochs, int batch, double lr, uint64_t 
 mpm_status mpm_gpu_implicit_set_precond(mpm_ctx *ctx, mpm_nn *net);
 /* Training pairs from the solver's own solves: for each of nsystems moduli
  * E drawn log-uniformly from [e_min, e_max] the system of the current state
- * is assembled; for each of loads_per_system seeded random right-hand sides
- * it is solved twice by Jacobi-PCG to ||r||^2 < eps ||r0||^2, the second
+ * is assembled; for its own right-hand side and loads_per_system - 1 seeded
+ * random ones it is solved twice by Jacobi-PCG to ||r||^2 < eps ||r0||^2, the second
  * time storing pairs_per_load (residual, error) pairs spread over the
  * iterations.  The materials' moduli are restored afterwards. */
 mpm_status mpm_gpu_implicit_harvest(mpm_ctx *ctx, mpm_nn *net, int nsystems, int loads_per_system, int pairs_per_load,
