@@ -25,6 +25,7 @@
 // its 32 nodes' 243 values walks one contiguous 62 KB range (coalesced and
 // DRAM-page friendly); no column indices (the grid is structured).
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -63,6 +64,7 @@ struct ImpState {
     cudaGraphExec_t g_cg = nullptr, g_fcg_nn = nullptr, g_fcg_jac = nullptr;
     mpm_nn *g_net = nullptr;
     bool no_graph = false;
+    bool debug = false;   // MPM_GB300_KRYLOV_TRACE set: residual history to stderr
 };
 
 namespace mpm {
@@ -869,6 +871,7 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
     implicit_free(c);
     ImpState *s = new ImpState();
     c->imp = s;
+    s->debug = getenv("MPM_GB300_KRYLOV_TRACE") != nullptr;
     s->nr_flag = nr_flag ? 1 : 0;
     // GeneralizedAlphaParaSet + NewmarkBetaParaSet (nonlinear_time_integration.cpp:10-56), second order
     double t = 1.0 + spec_rad;
@@ -1008,6 +1011,7 @@ static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
                 *iters = it;
                 return MPM_ERR_NONFINITE;
             }
+            if (s->debug) fprintf(stderr, "mpm_gb300 cg: it %d |r|/|r0| %.3e\n", it, sqrt(rr / rr0));
             if (rr < eps * rr0) done = true;
             s->last_rel = sqrt(rr / rr0);
         }
@@ -1120,6 +1124,9 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
                 *iters = it;
                 return MPM_ERR_NONFINITE;
             }
+            if (s->debug)
+                fprintf(stderr, "mpm_gb300 fcg: it %d |r|/|r0| %.3e (%s)\n", it, sqrt(rr / rr0),
+                        use_nn ? "network" : "jacobi");
             if (rr < eps * rr0) {
                 // confirm on the true residual
                 k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->xs, s->z, nullptr);
