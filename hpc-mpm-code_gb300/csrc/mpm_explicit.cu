@@ -307,6 +307,131 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell(StepArgs<float>
     p2g_node_pass(a, S, corner, sh_red, lc, h, ox, oy, oz, acc, misses, oobs);
 }
 
+// P2G in moment form.  Within a cell the linear weights are products of
+// (1/2 - u) and (1/2 + u) per axis, u in [-1/2, 1/2] the particle's offset
+// from the cell centre.  Each thread sums, over its share of the cell's
+// particles (the two threads of a cell take alternate particles), the
+// moments of q = (m, vol, m v) against {1, u, v, w, uv, uw, vw, uvw} and of
+// vol * sigma_ab against the bilinear monomials of the two axes other than
+// b: 76 FMAs per particle instead of evaluating eight corner weights and
+// gradients.  The pair adds its moments (a + b == b + a, so both threads
+// agree), each thread expands them into the four corners of its z-layer,
+// and the node pass is the one of k_p2g_cell.  Deterministic: every sum is
+// in a fixed order.
+__device__ __forceinline__ float cell_offset_u(float x, const KGeom<float> &g, int d, int c) {
+    const float xy = g.xmin[d] + g.dx[d] * (float)c;   // as axis_linear forms x - x_i
+    return (x - xy) * g.inv_dx[d] - 0.5f;
+}
+
+// both z-layers of a particle that left its sorted cell, by fixed-point atomics
+__device__ __noinline__ void p2g_miss(const StepArgs<float> &a, const Scales &S, int cx, int cy, int cz, float x0,
+                                      float x1, float x2, float m, float vol, const float *vel, const float *sg,
+                                      float fxg, float fyg, float fzg, int &misses, int &oobs) {
+    float dummy[NACC][4];
+    p2g_particle(a, S, cx, cy, cz, 0, x0, x1, x2, m, vol, vel, sg, fxg, fyg, fzg, dummy, misses, oobs);
+    p2g_particle(a, S, cx, cy, cz, 1, x0, x1, x2, m, vol, vel, sg, fxg, fyg, fzg, dummy, misses, oobs);
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_mom(StepArgs<float> a) {
+    __shared__ float corner[NACC * 8][BRC];       // 32 KB
+    __shared__ Scales S;
+    __shared__ int sh_red[32];
+    const int b = blockIdx.x;
+    const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
+    const int *cs = a.cstart + (size_t)b * (BRC + 1);
+    if (cs[0] == cs[BRC]) return;   // empty brick (uniform across the CTA)
+    int ox, oy, oz;
+    brick_origin(b, a.nbrick, ox, oy, oz);
+    const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
+    const int p0 = cs[lc], p1 = cs[lc + 1];
+    load_scales(a, S);
+    const float fxg = a.grav[0] * a.facl, fyg = a.grav[1] * a.facl, fzg = a.grav[2] * a.facl;
+    const Particles<float> &P = a.P;
+    float M[5][8], Fm[9][4];
+#pragma unroll
+    for (int f = 0; f < 5; f++)
+#pragma unroll
+        for (int k = 0; k < 8; k++) M[f][k] = 0.0f;
+#pragma unroll
+    for (int f = 0; f < 9; f++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) Fm[f][k] = 0.0f;
+    int misses = 0, oobs = 0;
+    for (int p = p0 + h; p < p1; p += 2) {
+        const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+        const float m = ld(P.m + p), vol = ld(P.vol + p);
+        const float vel[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
+        const float sg[6] = {ld(P.s[0] + p), ld(P.s[1] + p), ld(P.s[2] + p),
+                             ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
+        bool oob = false;
+        const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
+        if (px != cx || py != cy || pz != cz) {
+            // a particle that left its sorted cell scatters on its own (both z-layers)
+            p2g_miss(a, S, cx, cy, cz, x0, x1, x2, m, vol, vel, sg, fxg, fyg, fzg, misses, oobs);
+            continue;
+        }
+        oobs += oob;
+        const float u = cell_offset_u(x0, a.g, 0, px), v = cell_offset_u(x1, a.g, 1, py),
+                    w = cell_offset_u(x2, a.g, 2, pz);
+        const float uv = u * v, uw = u * w, vw = v * w;
+        const float mono[8] = {1.0f, u, v, w, uv, uw, vw, uv * w};
+        const float q[5] = {m, vol, m * vel[0], m * vel[1], m * vel[2]};
+#pragma unroll
+        for (int f = 0; f < 5; f++)
+#pragma unroll
+            for (int k = 0; k < 8; k++) M[f][k] += q[f] * mono[k];
+        // vol * sigma_ab, Voigt xx yy zz yz xz xy
+        const float vs[9] = {vol * sg[0], vol * sg[5], vol * sg[4], vol * sg[5], vol * sg[1],
+                             vol * sg[3], vol * sg[4], vol * sg[3], vol * sg[2]};
+        const float mb[3][4] = {{1.0f, v, w, vw}, {1.0f, u, w, uw}, {1.0f, u, v, uv}};
+#pragma unroll
+        for (int ab = 0; ab < 9; ab++)
+#pragma unroll
+            for (int k = 0; k < 4; k++) Fm[ab][k] += vs[ab] * mb[ab % 3][k];
+    }
+    const unsigned pair = 3u << ((threadIdx.x & 31) & ~1u);
+#pragma unroll
+    for (int f = 0; f < 5; f++)
+#pragma unroll
+        for (int k = 0; k < 8; k++) M[f][k] += __shfl_xor_sync(pair, M[f][k], 1);
+#pragma unroll
+    for (int f = 0; f < 9; f++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) Fm[f][k] += __shfl_xor_sync(pair, Fm[f][k], 1);
+    // corners (i, j, h) of this thread's z-layer
+    float acc[NACC][4];
+    const float sz = h ? 1.0f : -1.0f;
+    const float gv[3] = {fxg, fyg, fzg};
+#pragma unroll
+    for (int j = 0; j < 2; j++)
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            const int c = i + 2 * j;
+            const float sx = i ? 1.0f : -1.0f, sy = j ? 1.0f : -1.0f;
+#pragma unroll
+            for (int f = 0; f < 5; f++)
+                acc[f][c] = M[f][0] * 0.125f + (sx * M[f][1] + sy * M[f][2] + sz * M[f][3]) * 0.25f +
+                            (sx * sy * M[f][4] + sx * sz * M[f][5] + sy * sz * M[f][6]) * 0.5f +
+                            sx * sy * sz * M[f][7];
+            // the signs of the two bilinear axes of each derivative direction b
+            const float sb[3] = {sx, sy, sz};
+            const float sc[3] = {sy, sx, sx}, sd[3] = {sz, sz, sy};
+#pragma unroll
+            for (int ax = 0; ax < 3; ax++) {
+                float fi = 0.0f;
+#pragma unroll
+                for (int bb = 0; bb < 3; bb++) {
+                    const float *F = Fm[3 * ax + bb];
+                    fi += a.g.inv_dx[bb] * sb[bb] *
+                          (F[0] * 0.25f + (sc[bb] * F[1] + sd[bb] * F[2]) * 0.5f + sc[bb] * sd[bb] * F[3]);
+                }
+                acc[5 + ax][c] = -fi + acc[0][c] * gv[ax];
+            }
+        }
+    p2g_node_pass(a, S, corner, sh_red, lc, h, ox, oy, oz, acc, misses, oobs);
+}
+
 // The same P2G with the brick's particles brought into shared memory by
 // bulk asynchronous copies (TMA, 1-D): the brick's particles are one
 // contiguous range (sorted by brick, then cell), copied in chunks of PCH
@@ -1546,7 +1671,11 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
         timer_begin(c, K_P2G);
         if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
             if (use_cell_kernels(c)) {
-                if (c->tune.p2g_staged) {
+                if (c->tune.p2g_moments == 2) {
+                    k_p2g_cell_mom<1><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                } else if (c->tune.p2g_moments) {
+                    k_p2g_cell_mom<2><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                } else if (c->tune.p2g_staged) {
                     static bool attr = false;
                     if (!attr) {
                         cudaFuncSetAttribute(k_p2g_cell_staged<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -69,7 +69,7 @@ struct ImpState {
 
 namespace mpm {
 
-enum Scal { S_RR0 = 0, S_RR1, S_PAP, S_RR_INIT, S_RES, S_IDOF, S_EU, S_GD, S_ZQ, S_PR, S_RRC, S_NSCAL };
+enum Scal { S_RR0 = 0, S_RR1, S_PAP, S_RR_INIT, S_RES, S_IDOF, S_EU, S_GD, S_ZQ, S_PR, S_RRC, S_DZZ, S_DZR, S_NSCAL };
 
 struct ImpArgs {
     int nnc[3];
@@ -1094,6 +1094,19 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
     }
     while (!done && it < kmax) {
         cudaGraphExec_t *gx = use_nn ? &s->g_fcg_nn : &s->g_fcg_jac;
+        if (s->debug && use_nn) {
+            // diagnostics: |z| / |r| and cos(z, r) of the preconditioned residual
+            mpm_nn_apply_precond(s->net, c->stream, s->r, s->scal + S_RRC, s->adiag, a.bcflag, a.mtol, s->z);
+            k_dot3<<<nb, 256, 0, c->stream>>>(a, s->z, s->z, s->part);
+            k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_DZZ);
+            k_dot3<<<nb, 256, 0, c->stream>>>(a, s->z, s->r, s->part);
+            k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_DZR);
+            CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, c->stream));
+            CKI(cudaStreamSynchronize(c->stream));
+            const double zz = s->h_scal[S_DZZ], zr = s->h_scal[S_DZR], rr = s->h_scal[S_RRC];
+            fprintf(stderr, "mpm_gb300 fcg: it %d |z|/|r| %.3e cos(z,r) %.3e\n", it, sqrt(zz / rr),
+                    zr / sqrt(zz * rr + 1e-300));
+        }
         if (graphs_on(c) && !restart && it % check == 0 && it + check <= kmax) {
             const int64_t l0 = c->launches;
             if (!*gx && capture_iters(c, gx, [&] {

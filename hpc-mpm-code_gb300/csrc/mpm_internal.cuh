@@ -96,6 +96,7 @@ struct Fix {
 // Launch variants that give bitwise identical results; chosen by
 // mpm_gpu_autotune from measured times (defaults otherwise).
 struct Tune {
+    int p2g_moments = 1;            // FP32 P2G in moment form (k_p2g_cell_mom); 0: corner sums
     int p2g_staged = 0;             // per-cell P2G reads the brick's particles from bulk-copied shared memory
     int p2g_minb = 2;               // resident CTAs the direct per-cell P2G is compiled for (2 or 3)
     int musl_staged = 0;            // gather + MUSL reads the brick's particles from staged shared memory
