@@ -21,9 +21,11 @@
 // Matrix storage: for control point n and stencil slot s (the 27 neighbours
 // n + (dx, dy, dz), dx,dy,dz in {-1,0,1}, s = (dx+1) + 3 (dy+1) + 9 (dz+1)),
 // the 3x3 block entry q = s * 9 + 3 a + b lives at A[aidx(q, n)], tiled by
-// 32 control points: ((n / 32) * 243 + q) * 32 + n % 32.  A warp reading
-// its 32 nodes' 243 values walks one contiguous 62 KB range (coalesced and
-// DRAM-page friendly); no column indices (the grid is structured).
+// 32 control points and by pairs of entries:
+// ((n / 32) * 122 + q / 2) * 64 + (n % 32) * 2 + q % 2.  A thread reads
+// entry pairs as 16-byte loads and a warp reading its 32 nodes' 243 values
+// walks one contiguous 62 KB range (coalesced and DRAM-page friendly); no
+// column indices (the grid is structured).
 #include <cmath>
 #include <cstdlib>
 #include <cstdio>
@@ -90,9 +92,9 @@ struct ImpArgs {
 };
 
 __host__ __device__ __forceinline__ size_t aidx(int q, int n) {
-    return (((size_t)(n >> 5) * 243 + (size_t)q) << 5) + (size_t)(n & 31);
+    return (((size_t)(n >> 5) * 122 + (size_t)(q >> 1)) << 6) + (size_t)((n & 31) << 1) + (size_t)(q & 1);
 }
-static size_t a_size(int nodec) { return (size_t)((nodec + 31) / 32) * 32 * 243; }
+static size_t a_size(int nodec) { return (size_t)((nodec + 31) / 32) * 32 * 244; }
 
 static ImpArgs imp_args(mpm_ctx *c) {
     ImpArgs a;
@@ -412,15 +414,34 @@ __global__ void __launch_bounds__(256) k_imp_matvec(ImpArgs a, const double *A, 
         int i, j, k;
         node_ijk(n, a.nnc, i, j, k);
         double acc[3] = {0.0, 0.0, 0.0};
+#pragma unroll
         for (int s = 0; s < 27; s++) {
             const int ii = i + s % 3 - 1, jj = j + (s / 3) % 3 - 1, kk = k + s / 9 - 1;
             if (ii < 0 || jj < 0 || kk < 0 || ii >= a.nnc[0] || jj >= a.nnc[1] || kk >= a.nnc[2]) continue;
             const size_t col = ii + (size_t)a.nnc[0] * (jj + (size_t)a.nnc[1] * kk);
             const double x0 = x[col], x1 = x[N + col], x2 = x[2 * N + col];
-            const double *As = A + aidx(s * 9, n);   // entry e of the block at As[32 e]
-            acc[0] += As[0 * 32] * x0 + As[1 * 32] * x1 + As[2 * 32] * x2;
-            acc[1] += As[3 * 32] * x0 + As[4 * 32] * x1 + As[5 * 32] * x2;
-            acc[2] += As[6 * 32] * x0 + As[7 * 32] * x1 + As[8 * 32] * x2;
+            // the block's 9 entries: 4 aligned pairs and 1 single (which end depends on the parity of 9 s)
+            double e[9];
+            if ((s & 1) == 0) {
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    const double2 v = __ldg(reinterpret_cast<const double2 *>(A + aidx(s * 9 + 2 * t, n)));
+                    e[2 * t] = v.x;
+                    e[2 * t + 1] = v.y;
+                }
+                e[8] = __ldg(A + aidx(s * 9 + 8, n));
+            } else {
+                e[0] = __ldg(A + aidx(s * 9, n));
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    const double2 v = __ldg(reinterpret_cast<const double2 *>(A + aidx(s * 9 + 1 + 2 * t, n)));
+                    e[1 + 2 * t] = v.x;
+                    e[2 + 2 * t] = v.y;
+                }
+            }
+            acc[0] += e[0] * x0 + e[1] * x1 + e[2] * x2;
+            acc[1] += e[3] * x0 + e[4] * x1 + e[5] * x2;
+            acc[2] += e[6] * x0 + e[7] * x1 + e[8] * x2;
         }
         const unsigned char bf = a.bcflag[n];
         for (int c = 0; c < 3; c++) {
