@@ -462,7 +462,7 @@ __global__ void k_input_f32(const float *in, bf16 *x0, int64_t rows) {
 
 // x0 from an FP64 component-major residual, scaled by 1 / sqrt(rr / (3 nodec)),
 // and the system's feature channels
-__global__ void k_input_r(const double *r, const double *rr, const bf16 *feat, int64_t nodec, bf16 *x0) {
+__global__ void k_input_r(const double *r, const double *rr, const bf16 *feat, int64_t nodec, int linear, bf16 *x0) {
     const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (n >= nodec) return;
     const double ms = rr[0] / (3.0 * (double)nodec);
@@ -470,6 +470,8 @@ __global__ void k_input_r(const double *r, const double *rr, const bf16 *feat, i
     float f[8] = {(float)(r[n] * inv), (float)(r[nodec + n] * inv), (float)(r[2 * nodec + n] * inv),
                   __bfloat162float(feat[3 * n]), __bfloat162float(feat[3 * n + 1]), __bfloat162float(feat[3 * n + 2]),
                   0, 0};
+    if (linear)
+        for (int c = 0; c < 3; c++) f[3 + c] *= f[c];   // r * phi keeps the map linear in r
     uint4 *o = reinterpret_cast<uint4 *>(x0 + n * 16);
     o[0] = pack8(f);
     o[1] = make_uint4(0, 0, 0, 0);
@@ -477,7 +479,7 @@ __global__ void k_input_r(const double *r, const double *rr, const bf16 *feat, i
 
 // out = relu(up(coarse) + skip), C channels, one thread per (fine row, 8 channels)
 template <int C>
-__global__ void k_up_add_relu(const bf16 *coarse, const bf16 *skip, bf16 *out, Lvl lf, Lvl lc, int64_t rows) {
+__global__ void k_up_add_relu(const bf16 *coarse, const bf16 *skip, bf16 *out, Lvl lf, Lvl lc, int64_t rows, int act) {
     const int64_t item = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (item >= rows * (C / 8)) return;
     const int64_t row = item / (C / 8);
@@ -503,8 +505,10 @@ __global__ void k_up_add_relu(const bf16 *coarse, const bf16 *skip, bf16 *out, L
 #pragma unroll
                 for (int e = 0; e < 8; e++) acc[e] += w * f[e];
             }
+    if (act) {
 #pragma unroll
-    for (int e = 0; e < 8; e++) acc[e] = fmaxf(acc[e], 0.0f);
+        for (int e = 0; e < 8; e++) acc[e] = fmaxf(acc[e], 0.0f);
+    }
     reinterpret_cast<uint4 *>(out + row * C)[cc] = pack8(acc);
 }
 
@@ -549,7 +553,7 @@ __global__ void k_output(const bf16 *d0, const float *w5, const float *b5, float
     unpack8(p[0], f);
     unpack8(p[1], f + 8);
     for (int c = 0; c < 3; c++) {
-        float s = b5[c];
+        float s = b5 ? b5[c] : 0.0f;
 #pragma unroll
         for (int k = 0; k < 16; k++) s += f[k] * w5[k * 3 + c];
         z[3 * r + c] = s;
@@ -570,7 +574,7 @@ __global__ void k_output_precond(const bf16 *d0, const float *w5, const float *b
     unpack8(p[1], f + 8);
     const unsigned char bf = bcflag[n];
     for (int c = 0; c < 3; c++) {
-        float o = b5[c];
+        float o = b5 ? b5[c] : 0.0f;
 #pragma unroll
         for (int k = 0; k < 16; k++) o += f[k] * w5[k * 3 + c];
         const int64_t i = c * nodec + n;
@@ -583,7 +587,7 @@ constexpr int RED_THREADS = 256;
 
 // gd0 = (gz W5^T) masked by d0 > 0; per-block partials of dW5 (48) and db5 (3)
 __global__ void __launch_bounds__(RED_THREADS) k_output_bwd(const float *gz, const bf16 *d0, const float *w5,
-                                                            bf16 *gd0, float *part, int64_t rows) {
+                                                            bf16 *gd0, float *part, int64_t rows, int act) {
     __shared__ float sh[RED_THREADS / 32][51];
     float acc[51];
     for (int i = 0; i < 51; i++) acc[i] = 0.0f;
@@ -597,7 +601,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_output_bwd(const float *gz, con
 #pragma unroll
         for (int k = 0; k < 16; k++) {
             const float v = g0 * w5[k * 3] + g1 * w5[k * 3 + 1] + g2 * w5[k * 3 + 2];
-            o[k] = f[k] > 0.0f ? v : 0.0f;
+            o[k] = (!act || f[k] > 0.0f) ? v : 0.0f;
             acc[k * 3] += f[k] * g0;
             acc[k * 3 + 1] += f[k] * g1;
             acc[k * 3 + 2] += f[k] * g2;
@@ -696,7 +700,7 @@ __global__ void k_adam(float *p, const float *g, float *m, float *v, int64_t n, 
 
 // training batch: x0 from stored residuals and their system's features, FP32 targets
 __global__ void k_gather_batch(const bf16 *dr, const bf16 *de, const bf16 *df, const int *dsys, const int *idx,
-                               int64_t v0, int batch, bf16 *x0, float *tgt) {
+                               int64_t v0, int batch, int linear, bf16 *x0, float *tgt) {
     const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (r >= v0 * batch) return;
     const int b = (int)(r / v0);
@@ -706,7 +710,7 @@ __global__ void k_gather_batch(const bf16 *dr, const bf16 *de, const bf16 *df, c
     float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int c = 0; c < 3; c++) {
         f[c] = __bfloat162float(dr[3 * src + c]);
-        f[3 + c] = __bfloat162float(df[3 * fs + c]);
+        f[3 + c] = __bfloat162float(df[3 * fs + c]) * (linear ? f[c] : 1.0f);
         tgt[3 * r + c] = __bfloat162float(de[3 * src + c]);
     }
     uint4 *o = reinterpret_cast<uint4 *>(x0 + r * 16);
@@ -794,6 +798,7 @@ struct mpm_nn {
     int *idx = nullptr;
     int *err = nullptr;
     bool weights_dirty = true;
+    int linear = 1;   // 1: no activations and no biases (a linear operator of the input)
     int64_t adam_step = 0;
     bf16 *data_r = nullptr, *data_e = nullptr;
     int64_t ndata = 0, data_cap = 0;
@@ -894,24 +899,26 @@ cudaError_t forward(mpm_nn *net, cudaStream_t st, int batch) {
     if (e != cudaSuccess) return e;
     const Lvl &L0 = net->L[0], &L1 = net->L[1], &L2 = net->L[2];
     const float *P = net->p;
-    if ((e = launch_conv<16, 16, S1>(net, st, net->x0, net->e0, net->wf[0], P + b_offset(0), nullptr, nullptr, 1, L0,
-                                     L0, batch)) != cudaSuccess)
+    const int act = net->linear ? 0 : 1;
+    auto bias = [&](int l) -> const float * { return net->linear ? nullptr : P + b_offset(l); };
+    if ((e = launch_conv<16, 16, S1>(net, st, net->x0, net->e0, net->wf[0], bias(0), nullptr, nullptr, act, L0, L0,
+                                     batch)) != cudaSuccess)
         return e;
-    if ((e = launch_conv<16, 32, S2>(net, st, net->e0, net->e1, net->wf[1], P + b_offset(1), nullptr, nullptr, 1, L0,
-                                     L1, batch)) != cudaSuccess)
+    if ((e = launch_conv<16, 32, S2>(net, st, net->e0, net->e1, net->wf[1], bias(1), nullptr, nullptr, act, L0, L1,
+                                     batch)) != cudaSuccess)
         return e;
-    if ((e = launch_conv<32, 64, S2>(net, st, net->e1, net->e2, net->wf[2], P + b_offset(2), nullptr, nullptr, 1, L1,
-                                     L2, batch)) != cudaSuccess)
+    if ((e = launch_conv<32, 64, S2>(net, st, net->e1, net->e2, net->wf[2], bias(2), nullptr, nullptr, act, L1, L2,
+                                     batch)) != cudaSuccess)
         return e;
-    if ((e = launch_conv<64, 32, S1>(net, st, net->e2, net->c2, net->wf[3], P + b_offset(3), nullptr, nullptr, 0, L2,
-                                     L2, batch)) != cudaSuccess)
+    if ((e = launch_conv<64, 32, S1>(net, st, net->e2, net->c2, net->wf[3], bias(3), nullptr, nullptr, 0, L2, L2,
+                                     batch)) != cudaSuccess)
         return e;
     const int64_t r1 = (int64_t)batch * L1.v, r0 = (int64_t)batch * L0.v;
-    k_up_add_relu<32><<<blocks(r1 * 4), 256, 0, st>>>(net->c2, net->e1, net->d1, L1, L2, r1);
-    if ((e = launch_conv<32, 16, S1>(net, st, net->d1, net->c1, net->wf[4], P + b_offset(4), nullptr, nullptr, 0, L1,
-                                     L1, batch)) != cudaSuccess)
+    k_up_add_relu<32><<<blocks(r1 * 4), 256, 0, st>>>(net->c2, net->e1, net->d1, L1, L2, r1, act);
+    if ((e = launch_conv<32, 16, S1>(net, st, net->d1, net->c1, net->wf[4], bias(4), nullptr, nullptr, 0, L1, L1,
+                                     batch)) != cudaSuccess)
         return e;
-    k_up_add_relu<16><<<blocks(r0 * 2), 256, 0, st>>>(net->c1, net->e0, net->d0, L0, L1, r0);
+    k_up_add_relu<16><<<blocks(r0 * 2), 256, 0, st>>>(net->c1, net->e0, net->d0, L0, L1, r0, act);
     return cudaGetLastError();
 }
 
@@ -923,41 +930,45 @@ cudaError_t backward(mpm_nn *net, cudaStream_t st, int batch) {
     cudaError_t e;
     {
         const int nblk = (int)std::min<int64_t>(blocks(r0, RED_THREADS), 2 * (int64_t)net->nsm);
-        k_output_bwd<<<nblk, RED_THREADS, 0, st>>>(net->gz, net->d0, net->p + w5_offset(), net->gd0, net->part, r0);
+        k_output_bwd<<<nblk, RED_THREADS, 0, st>>>(net->gz, net->d0, net->p + w5_offset(), net->gd0, net->part, r0,
+                                                   net->linear ? 0 : 1);
         k_part_reduce<<<1, 64, 0, st>>>(net->part, nblk, 51, G + w5_offset());
     }
     // c1 -> d0 through up: gc1 = up^T(gd0)
     k_restrict<16><<<blocks(r1 * 2), 256, 0, st>>>(net->gd0, net->gc1, L0, L1, r1);
-    launch_chan_sum<16>(net, st, net->gc1, r1, G + b_offset(4));
+    const bool lin = net->linear != 0;
+    if (!lin) launch_chan_sum<16>(net, st, net->gc1, r1, G + b_offset(4));
     if ((e = launch_dw<32, 16, S1>(net, st, net->d1, net->gc1, L1, L1, batch, 32, G + w_offset(4))) != cudaSuccess)
         return e;
     // gd1 = conv4^T(gc1) masked by d1
-    if ((e = launch_conv<16, 32, S1T>(net, st, net->gc1, net->gd1, net->wt[4], nullptr, nullptr, net->d1, 0, L1, L1,
+    if ((e = launch_conv<16, 32, S1T>(net, st, net->gc1, net->gd1, net->wt[4], nullptr, nullptr, lin ? nullptr : net->d1, 0, L1, L1,
                                       batch)) != cudaSuccess)
         return e;
     k_restrict<32><<<blocks(r2 * 4), 256, 0, st>>>(net->gd1, net->gc2, L1, L2, r2);
-    launch_chan_sum<32>(net, st, net->gc2, r2, G + b_offset(3));
+    if (!lin) launch_chan_sum<32>(net, st, net->gc2, r2, G + b_offset(3));
     if ((e = launch_dw<64, 32, S1>(net, st, net->e2, net->gc2, L2, L2, batch, 64, G + w_offset(3))) != cudaSuccess)
         return e;
     // ge2 = conv3^T(gc2) masked by e2
-    if ((e = launch_conv<32, 64, S1T>(net, st, net->gc2, net->ge2, net->wt[3], nullptr, nullptr, net->e2, 0, L2, L2,
+    if ((e = launch_conv<32, 64, S1T>(net, st, net->gc2, net->ge2, net->wt[3], nullptr, nullptr, lin ? nullptr : net->e2, 0, L2, L2,
                                       batch)) != cudaSuccess)
         return e;
-    launch_chan_sum<64>(net, st, net->ge2, r2, G + b_offset(2));
+    if (!lin) launch_chan_sum<64>(net, st, net->ge2, r2, G + b_offset(2));
     if ((e = launch_dw<32, 64, S2>(net, st, net->e1, net->ge2, L1, L2, batch, 32, G + w_offset(2))) != cudaSuccess)
         return e;
     // ge1 = (conv2^T(ge2) + gd1) masked by e1
-    if ((e = launch_conv<64, 32, S2T>(net, st, net->ge2, net->ge1, net->wt[2], nullptr, net->gd1, net->e1, 0, L2, L1,
+    if ((e = launch_conv<64, 32, S2T>(net, st, net->ge2, net->ge1, net->wt[2], nullptr, net->gd1, lin ? nullptr : net->e1, 0, L2, L1,
                                       batch)) != cudaSuccess)
         return e;
-    launch_chan_sum<32>(net, st, net->ge1, r1, G + b_offset(1));
+    if (!lin) launch_chan_sum<32>(net, st, net->ge1, r1, G + b_offset(1));
     if ((e = launch_dw<16, 32, S2>(net, st, net->e0, net->ge1, L0, L1, batch, 16, G + w_offset(1))) != cudaSuccess)
         return e;
     // ge0 = (conv1^T(ge1) + gd0) masked by e0
-    if ((e = launch_conv<32, 16, S2T>(net, st, net->ge1, net->ge0, net->wt[1], nullptr, net->gd0, net->e0, 0, L1, L0,
+    if ((e = launch_conv<32, 16, S2T>(net, st, net->ge1, net->ge0, net->wt[1], nullptr, net->gd0, lin ? nullptr : net->e0, 0, L1, L0,
                                       batch)) != cudaSuccess)
         return e;
-    launch_chan_sum<16>(net, st, net->ge0, r0, G + b_offset(0));
+    if (!lin) launch_chan_sum<16>(net, st, net->ge0, r0, G + b_offset(0));
+    if (lin)   // biases are not used: their gradients are zero
+        for (int l = 0; l < NCONV; l++) cudaMemsetAsync(G + b_offset(l), 0, sizeof(float) * COUT[l], st);
     if ((e = launch_dw<16, 16, S1>(net, st, net->x0, net->ge0, L0, L0, batch, NIN, G + w_offset(0))) != cudaSuccess)
         return e;
     return cudaGetLastError();
@@ -1097,6 +1108,12 @@ mpm_status mpm_nn_destroy(mpm_nn *net) {
     return MPM_OK;
 }
 
+mpm_status mpm_nn_set_linear(mpm_nn *net, int linear) {
+    if (!net) return MPM_ERR_BAD_ARG;
+    net->linear = linear ? 1 : 0;
+    return MPM_OK;
+}
+
 mpm_status mpm_nn_set_stream(mpm_nn *net, void *stream) {
     if (!net) return MPM_ERR_BAD_ARG;
     net->stream = (cudaStream_t)stream;
@@ -1143,7 +1160,7 @@ mpm_status mpm_nn_forward(mpm_nn *net, int batch, const float *in, float *out) {
     CKN(cudaMemcpyAsync(net->tgt, in, r0 * NIN * 4, cudaMemcpyHostToDevice, st));
     k_input_f32<<<blocks(r0), 256, 0, st>>>(net->tgt, net->x0, r0);
     CKN(forward(net, st, batch));
-    k_output<<<blocks(r0), 256, 0, st>>>(net->d0, net->p + w5_offset(), net->p + b5_offset(), net->z, r0);
+    k_output<<<blocks(r0), 256, 0, st>>>(net->d0, net->p + w5_offset(), net->linear ? nullptr : net->p + b5_offset(), net->z, r0);
     CKN(cudaGetLastError());
     CKN(cudaMemcpyAsync(out, net->z, r0 * 3 * 4, cudaMemcpyDeviceToHost, st));
     CKN(cudaStreamSynchronize(st));
@@ -1188,9 +1205,9 @@ mpm_status mpm_nn_train(mpm_nn *net, int epochs, int batch, double lr, uint64_t 
         for (int64_t bi = 0; bi < nb; bi++) {
             CKN(cudaMemcpyAsync(net->idx, perm.data() + bi * batch, batch * 4, cudaMemcpyHostToDevice, st));
             k_gather_batch<<<blocks(r0), 256, 0, st>>>(net->data_r, net->data_e, net->data_f, net->data_sys,
-                                                       net->idx, v0, batch, net->x0, net->tgt);
+                                                       net->idx, v0, batch, net->linear, net->x0, net->tgt);
             CKN(forward(net, st, batch));
-            k_output<<<blocks(r0), 256, 0, st>>>(net->d0, net->p + w5_offset(), net->p + b5_offset(), net->z, r0);
+            k_output<<<blocks(r0), 256, 0, st>>>(net->d0, net->p + w5_offset(), net->linear ? nullptr : net->p + b5_offset(), net->z, r0);
             k_mse<<<batch, RED_THREADS, 0, st>>>(net->z, net->tgt, net->gz, v0, batch, net->loss);
             CKN(backward(net, st, batch));
             net->adam_step++;
@@ -1220,9 +1237,10 @@ int mpm_nn_grid_matches(const mpm_nn *net, const int nodes[3]) {
 mpm_status mpm_nn_apply_precond(mpm_nn *net, cudaStream_t st, const double *r, const double *rr, const double *adiag,
                                 const unsigned char *bcflag, double mtol, double *z) {
     const int64_t nodec = net->L[0].v;
-    k_input_r<<<blocks(nodec), 256, 0, st>>>(r, rr, net->feat, nodec, net->x0);
+    k_input_r<<<blocks(nodec), 256, 0, st>>>(r, rr, net->feat, nodec, net->linear, net->x0);
     CKN(forward(net, st, 1));
-    k_output_precond<<<blocks(nodec), 256, 0, st>>>(net->d0, net->p + w5_offset(), net->p + b5_offset(), rr, nodec,
+    k_output_precond<<<blocks(nodec), 256, 0, st>>>(net->d0, net->p + w5_offset(),
+                                                   net->linear ? nullptr : net->p + b5_offset(), rr, nodec,
                                                    adiag, bcflag, mtol, z);
     CKN(cudaGetLastError());
     return MPM_OK;

@@ -243,6 +243,11 @@ int64_t mpm_nn_num_params(void);
 mpm_status mpm_nn_create(const int nodes[3], int max_batch, int64_t max_pairs, mpm_nn **out);
 mpm_status mpm_nn_destroy(mpm_nn *net);
 mpm_status mpm_nn_set_stream(mpm_nn *net, void *stream);
+/* linear = 1 (default): no activations and no biases, and the stiffness
+ * channels enter as residual x mass share, so the network is a linear
+ * operator of the residual (a preconditioner must not change with the
+ * residual's scale or sign); 0: ReLU activations with biases. */
+mpm_status mpm_nn_set_linear(mpm_nn *net, int linear);
 mpm_status mpm_nn_init_params(mpm_nn *net, uint64_t seed);
 mpm_status mpm_nn_set_params(mpm_nn *net, const float *params);
 mpm_status mpm_nn_get_params(mpm_nn *net, float *params);

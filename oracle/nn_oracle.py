@@ -159,12 +159,14 @@ def relu(a):
     return np.maximum(a, 0.0)
 
 
-def forward(params, r, bf16=False):
-    """r (B, nz, ny, nx, 6): residual and feature channels -> (z (..., 3), cache)."""
+def forward(params, r, bf16=False, linear=False):
+    """r (B, nz, ny, nx, 6): input channels -> (z (..., 3), cache).  linear:
+    no activations and no biases (the network's default mode on the GPU)."""
     P = unpack(params)
     q = bf16_round if bf16 else (lambda a: np.asarray(a, dtype=np.float64))
     W = [q(P[f"W{l}"]) for l in range(5)]
-    b = [P[f"b{l}"] for l in range(5)]
+    b = [0.0 * P[f"b{l}"] if linear else P[f"b{l}"] for l in range(5)]
+    relu = (lambda a: a) if linear else globals()["relu"]
     x0 = q(r)
     n0 = x0.shape[1:4]
     n1 = coarse_dims(n0)
@@ -175,37 +177,42 @@ def forward(params, r, bf16=False):
     d1 = q(relu(up(c2, n1) + e1))
     c1 = q(conv(d1, W[4], b[4], 1))
     d0 = q(relu(up(c1, n0) + e0))
-    z = d0 @ P["W5"] + P["b5"]
-    cache = dict(x0=x0, e0=e0, e1=e1, e2=e2, c2=c2, d1=d1, c1=c1, d0=d0, W=W, P=P, q=q)
+    z = d0 @ P["W5"] + (0.0 if linear else P["b5"])
+    cache = dict(x0=x0, e0=e0, e1=e1, e2=e2, c2=c2, d1=d1, c1=c1, d0=d0, W=W, P=P, q=q, linear=linear)
     return z, cache
 
 
-def backward(params, r, gz, bf16=False):
+def backward(params, r, gz, bf16=False, linear=False):
     """Gradient of sum(z * gz) with respect to the parameters (packed like params)."""
-    z, C = forward(params, r, bf16)
+    z, C = forward(params, r, bf16, linear)
     q, W, P = C["q"], C["W"], C["P"]
+    act = (lambda a: np.ones_like(a)) if linear else (lambda a: a > 0)
     x0, e0, e1, e2, c2, d1, c1, d0 = (C[k] for k in ("x0", "e0", "e1", "e2", "c2", "d1", "c1", "d0"))
     n0, n1, n2 = x0.shape[1:4], e1.shape[1:4], e2.shape[1:4]
     G = {}
     G["W5"] = d0.reshape(-1, 16).T @ gz.reshape(-1, 3)
     G["b5"] = gz.reshape(-1, 3).sum(0)
-    gd0 = q((gz @ P["W5"].T) * (d0 > 0))
+    gd0 = q((gz @ P["W5"].T) * act(d0))
     gc1 = q(restrict(gd0, n1))
     G["b4"] = gc1.reshape(-1, 16).sum(0)
     G["W4"] = conv_dw(d1, gc1, 1)
-    gd1 = q(conv_t(gc1, W[4], 1, n1) * (d1 > 0))
+    gd1 = q(conv_t(gc1, W[4], 1, n1) * act(d1))
     gc2 = q(restrict(gd1, n2))
     G["b3"] = gc2.reshape(-1, 32).sum(0)
     G["W3"] = conv_dw(e2, gc2, 1)
-    ge2 = q(conv_t(gc2, W[3], 1, n2) * (e2 > 0))
+    ge2 = q(conv_t(gc2, W[3], 1, n2) * act(e2))
     G["b2"] = ge2.reshape(-1, 64).sum(0)
     G["W2"] = conv_dw(e1, ge2, 2)
-    ge1 = q((conv_t(ge2, W[2], 2, n1) + gd1) * (e1 > 0))
+    ge1 = q((conv_t(ge2, W[2], 2, n1) + gd1) * act(e1))
     G["b1"] = ge1.reshape(-1, 32).sum(0)
     G["W1"] = conv_dw(e0, ge1, 2)
-    ge0 = q((conv_t(ge1, W[1], 2, n0) + gd0) * (e0 > 0))
+    ge0 = q((conv_t(ge1, W[1], 2, n0) + gd0) * act(e0))
     G["b0"] = ge0.reshape(-1, 16).sum(0)
     G["W0"] = conv_dw(x0, ge0, 1)
+    if linear:
+        for l in range(5):
+            G[f"b{l}"] = 0.0 * G[f"b{l}"]
+        G["b5"] = 0.0 * G["b5"]
     return z, pack(G)
 
 

@@ -29,29 +29,34 @@ def _inputs(seed, batch=2):
     return x.astype(np.float32), rng.normal(size=shape + (3,)).astype(np.float32)
 
 
-def test_forward_matches_oracle():
+@pytest.mark.parametrize("linear", [True, False])
+def test_forward_matches_oracle(linear):
     p = O.init_params(11)
-    net = capi.PrecondNet(NODES, max_batch=2)
+    net = capi.PrecondNet(NODES, max_batch=2, linear=linear)
     net.set_params(p)
     x, _ = _inputs(1)
     z = net.forward(x.reshape(2, -1, 6)).reshape(x.shape[:-1] + (3,))
-    zq, _ = O.forward(p.astype(np.float64), x.astype(np.float64), bf16=True)
-    ze, _ = O.forward(p.astype(np.float64), x.astype(np.float64), bf16=False)
+    zq, _ = O.forward(p.astype(np.float64), x.astype(np.float64), bf16=True, linear=linear)
+    ze, _ = O.forward(p.astype(np.float64), x.astype(np.float64), bf16=False, linear=linear)
     net.close()
     assert rel_l2(z, zq) <= 1e-2, rel_l2(z, zq)
     assert rel_l2(z, ze) <= 5e-2, rel_l2(z, ze)
 
 
-def test_backward_matches_oracle():
+@pytest.mark.parametrize("linear", [True, False])
+def test_backward_matches_oracle(linear):
     p = O.init_params(12)
-    net = capi.PrecondNet(NODES, max_batch=2)
+    net = capi.PrecondNet(NODES, max_batch=2, linear=linear)
     net.set_params(p)
     x, g = _inputs(2)
     grad = net.backward(x.reshape(2, -1, 6), g.reshape(2, -1, 3))
-    _, go = O.backward(p.astype(np.float64), x.astype(np.float64), g.astype(np.float64), bf16=True)
+    _, go = O.backward(p.astype(np.float64), x.astype(np.float64), g.astype(np.float64), bf16=True, linear=linear)
     net.close()
     gb, ob = O.unpack(grad), O.unpack(go)
     for k in gb:
+        if linear and k.startswith("b"):
+            assert np.all(gb[k] == 0.0), k
+            continue
         assert rel_l2(gb[k], ob[k]) <= 3e-2, (k, rel_l2(gb[k], ob[k]))
 
 

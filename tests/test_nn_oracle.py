@@ -7,6 +7,7 @@ must match a central difference to 1e-3.  The step is small (1e-8) so that
 no ReLU kink falls inside the difference interval.
 """
 import numpy as np
+import pytest
 
 from oracle import nn_oracle as O
 
@@ -17,15 +18,16 @@ def test_parameter_layout():
     assert np.array_equal(O.pack(O.unpack(p)).astype(np.float32), p)
 
 
-def test_gradients_match_finite_differences():
+@pytest.mark.parametrize("linear", [False, True])
+def test_gradients_match_finite_differences(linear):
     rng = np.random.default_rng(7)
     p = O.init_params(3).astype(np.float64)
     r = np.concatenate([rng.normal(size=(1, 6, 7, 9, 3)), rng.uniform(size=(1, 6, 7, 9, 3))], axis=-1)
     gz = rng.normal(size=(1, 6, 7, 9, 3))
-    _, g = O.backward(p, r, gz)
+    _, g = O.backward(p, r, gz, linear=linear)
 
     def loss(pp):
-        return float((O.forward(pp, r)[0] * gz).sum())
+        return float((O.forward(pp, r, linear=linear)[0] * gz).sum())
 
     eps = 1e-8
     base = O.unpack(np.zeros_like(p))
@@ -35,6 +37,9 @@ def test_gradients_match_finite_differences():
         v = O.pack(d)
         fd = (loss(p + eps * v) - loss(p - eps * v)) / (2 * eps)
         an = float(g @ v)
+        if linear and name.startswith("b"):
+            assert an == 0.0
+            continue
         assert abs(fd - an) <= 1e-3 * max(abs(fd), 1e-6), (name, fd, an)
 
 
