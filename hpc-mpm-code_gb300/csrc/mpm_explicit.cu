@@ -432,6 +432,156 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_mom(StepArgs<fl
     p2g_node_pass(a, S, corner, sh_red, lc, h, ox, oy, oz, acc, misses, oobs);
 }
 
+// P2G, one CTA of 128 threads per brick, in two phases per chunk of 128 of
+// the brick's particles (a contiguous, coalesced range): (1) thread t takes
+// particle t of the chunk and writes its 76 moment terms (see
+// k_p2g_cell_mom) to shared memory, or scatters it with atomics if it left
+// its sorted cell; (2) thread c adds the terms of its cell's particles in
+// particle order into 76 register sums.  Every memory access of the particle
+// data is coalesced and the loads of a whole chunk are in flight at once;
+// the sums keep a fixed order (deterministic).
+constexpr int BCH = 128;                        // particles per chunk
+constexpr int NMOM = 76;                        // 40 mass/vol/momentum + 36 stress moments
+
+__global__ void __launch_bounds__(BCH) k_p2g_brick(StepArgs<float> a) {
+    __shared__ float T[NMOM][BCH];                 // 38 KB; reused for the corner sums
+    __shared__ Scales S;
+    __shared__ int sh_red[32];
+    __shared__ int scs[BRC + 1];
+    const int b = blockIdx.x;
+    const int *cs = a.cstart + (size_t)b * (BRC + 1);
+    const int P0 = cs[0], P1 = cs[BRC];
+    if (P0 == P1) return;
+    const int tid = threadIdx.x;
+    for (int i = tid; i <= BRC; i += BCH) scs[i] = cs[i];
+    int ox, oy, oz;
+    brick_origin(b, a.nbrick, ox, oy, oz);
+    load_scales(a, S);   // also publishes scs
+    const float fxg = a.grav[0] * a.facl, fyg = a.grav[1] * a.facl, fzg = a.grav[2] * a.facl;
+    const Particles<float> &P = a.P;
+    // this thread's cell (phase 2)
+    const int lc = tid;
+    const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
+    const int p0 = scs[lc], p1 = scs[lc + 1];
+    float M[NMOM];
+#pragma unroll
+    for (int k = 0; k < NMOM; k++) M[k] = 0.0f;
+    int misses = 0, oobs = 0;
+    for (int c0 = P0; c0 < P1; c0 += BCH) {
+        // phase 1: one particle per thread
+        const int p = c0 + tid;
+        if (p < P1) {
+            const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+            const float m = ld(P.m + p), vol = ld(P.vol + p);
+            const float vel[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
+            const float sg[6] = {ld(P.s[0] + p), ld(P.s[1] + p), ld(P.s[2] + p),
+                                 ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
+            bool oob = false;
+            const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
+            // mine: the particle sits in the cell whose sorted range holds it
+            const int qx = px - ox, qy = py - oy, qz = pz - oz;
+            bool mine = (unsigned)qx < (unsigned)BRX && (unsigned)qy < (unsigned)BRY && (unsigned)qz < (unsigned)BRZ;
+            if (mine) {
+                const int q = qx + BRX * (qy + BRY * qz);
+                mine = p >= scs[q] && p < scs[q + 1];
+            }
+            if (!mine) {
+                p2g_miss(a, S, -1, -1, -1, x0, x1, x2, m, vol, vel, sg, fxg, fyg, fzg, misses, oobs);
+#pragma unroll
+                for (int k = 0; k < NMOM; k++) T[k][tid] = 0.0f;
+            } else {
+                oobs += oob;
+                const float u = cell_offset_u(x0, a.g, 0, px), v = cell_offset_u(x1, a.g, 1, py),
+                            w = cell_offset_u(x2, a.g, 2, pz);
+                const float uv = u * v, uw = u * w, vw = v * w;
+                const float mono[8] = {1.0f, u, v, w, uv, uw, vw, uv * w};
+                const float qv[5] = {m, vol, m * vel[0], m * vel[1], m * vel[2]};
+#pragma unroll
+                for (int f = 0; f < 5; f++)
+#pragma unroll
+                    for (int k = 0; k < 8; k++) T[8 * f + k][tid] = qv[f] * mono[k];
+                const float vs[9] = {vol * sg[0], vol * sg[5], vol * sg[4], vol * sg[5], vol * sg[1],
+                                     vol * sg[3], vol * sg[4], vol * sg[3], vol * sg[2]};
+                const float mb[3][4] = {{1.0f, v, w, vw}, {1.0f, u, w, uw}, {1.0f, u, v, uv}};
+#pragma unroll
+                for (int ab = 0; ab < 9; ab++)
+#pragma unroll
+                    for (int k = 0; k < 4; k++) T[40 + 4 * ab + k][tid] = vs[ab] * mb[ab % 3][k];
+            }
+        }
+        __syncthreads();
+        // phase 2: this thread's cell adds its particles of the chunk in order
+        const int q0 = max(p0, c0), q1 = min(p1, c0 + BCH);
+        for (int q = q0; q < q1; q++) {
+            const int j = q - c0;
+#pragma unroll
+            for (int k = 0; k < NMOM; k++) M[k] += T[k][j];
+        }
+        __syncthreads();
+    }
+    // corners: moments -> the 8 corners of this cell, 8 fields each, into T[f * 8 + corner][cell]
+    const float gv[3] = {fxg, fyg, fzg};
+#pragma unroll
+    for (int kk = 0; kk < 2; kk++)
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const int corner = i + 2 * (j + 2 * kk);
+                const float sx = i ? 1.0f : -1.0f, sy = j ? 1.0f : -1.0f, sz = kk ? 1.0f : -1.0f;
+                float cm[5];
+#pragma unroll
+                for (int f = 0; f < 5; f++) {
+                    const float *Mf = M + 8 * f;
+                    cm[f] = Mf[0] * 0.125f + (sx * Mf[1] + sy * Mf[2] + sz * Mf[3]) * 0.25f +
+                            (sx * sy * Mf[4] + sx * sz * Mf[5] + sy * sz * Mf[6]) * 0.5f + sx * sy * sz * Mf[7];
+                    T[f * 8 + corner][lc] = cm[f];
+                }
+                const float sb[3] = {sx, sy, sz};
+                const float sc[3] = {sy, sx, sx}, sd[3] = {sz, sz, sy};
+#pragma unroll
+                for (int ax = 0; ax < 3; ax++) {
+                    float fi = 0.0f;
+#pragma unroll
+                    for (int bb = 0; bb < 3; bb++) {
+                        const float *F = M + 40 + 4 * (3 * ax + bb);
+                        fi += a.g.inv_dx[bb] * sb[bb] *
+                              (F[0] * 0.25f + (sc[bb] * F[1] + sd[bb] * F[2]) * 0.5f + sc[bb] * sd[bb] * F[3]);
+                    }
+                    T[(5 + ax) * 8 + corner][lc] = -fi + cm[0] * gv[ax];
+                }
+            }
+    int tot = block_reduce(misses + (oobs << 16), OpAddI(), sh_red);
+    if (threadIdx.x == 0 && tot) {
+        if (tot & 0xffff) atomicAdd(&a.ctl->tile_misses, (unsigned)(tot & 0xffff));
+        if (tot >> 16) atomicAdd(&a.ctl->err_oob, (unsigned)(tot >> 16));
+    }
+    __syncthreads();
+    constexpr int NX = BRX + 1, NY = BRY + 1, NZ = BRZ + 1, NB = NX * NY * NZ;
+    for (int it = threadIdx.x; it < NB * NACC; it += BCH) {
+        const int f = it / NB, n = it % NB;
+        const int nx = n % NX, ny = (n / NX) % NY, nz = n / (NX * NY);
+        const int gx = ox + nx, gy = oy + ny, gz = oz + nz;
+        if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
+        float sum = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+#pragma unroll
+            for (int j = 0; j < 2; j++)
+#pragma unroll
+                for (int i = 0; i < 2; i++) {
+                    const int ex = nx - i, ey = ny - j, ez = nz - k;
+                    if (ex >= 0 && ex < BRX && ey >= 0 && ey < BRY && ez >= 0 && ez < BRZ)
+                        sum += T[f * 8 + i + 2 * (j + 2 * k)][ex + BRX * (ey + BRY * ez)];
+                }
+        if (f == 0) a.tileflag[tile_of_node(a.g, gx, gy, gz)] = 1;
+        if (sum != 0.0f) {
+            const Fix &F = f == 0 ? S.m : f == 1 ? S.v : f <= 4 ? S.p : S.f;
+            atomic_add_i64(&a.acc[(size_t)f * a.g.nodec + node_id(a.g, gx, gy, gz)], fx(sum, F));
+        }
+    }
+}
+
 // The same P2G with the brick's particles brought into shared memory by
 // bulk asynchronous copies (TMA, 1-D): the brick's particles are one
 // contiguous range (sorted by brick, then cell), copied in chunks of PCH
@@ -1671,7 +1821,9 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
         timer_begin(c, K_P2G);
         if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
             if (use_cell_kernels(c)) {
-                if (c->tune.p2g_moments == 2) {
+                if (c->tune.p2g_moments == 3) {
+                    k_p2g_brick<<<c->g.nbricks, BCH, 0, c->stream>>>(a);
+                } else if (c->tune.p2g_moments == 2) {
                     k_p2g_cell_mom<1><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
                 } else if (c->tune.p2g_moments) {
                     k_p2g_cell_mom<2><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
