@@ -563,7 +563,8 @@ __global__ void k_output(const bf16 *d0, const float *w5, const float *b5, float
 // preconditioner output: z (FP64 component-major) = s * (d0 W5 + b5), zero on
 // inactive and boundary rows
 __global__ void k_output_precond(const bf16 *d0, const float *w5, const float *b5, const double *rr, int64_t nodec,
-                                 const double *adiag, const unsigned char *bcflag, double mtol, double *z) {
+                                 const double *adiag, const unsigned char *bcflag, double mtol, const double *r,
+                                 double *z) {
     const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (n >= nodec) return;
     const double ms = rr[0] / (3.0 * (double)nodec);
@@ -579,7 +580,7 @@ __global__ void k_output_precond(const bf16 *d0, const float *w5, const float *b
         for (int k = 0; k < 16; k++) o += f[k] * w5[k * 3 + c];
         const int64_t i = c * nodec + n;
         const bool off = (bf & (1 << c)) || !(adiag[i] >= mtol);
-        z[i] = off ? 0.0 : s * (double)o;
+        z[i] = off ? 0.0 : (r ? r[i] : 0.0) + s * (double)o;
     }
 }
 
@@ -700,7 +701,7 @@ __global__ void k_adam(float *p, const float *g, float *m, float *v, int64_t n, 
 
 // training batch: x0 from stored residuals and their system's features, FP32 targets
 __global__ void k_gather_batch(const bf16 *dr, const bf16 *de, const bf16 *df, const int *dsys, const int *idx,
-                               int64_t v0, int batch, int linear, bf16 *x0, float *tgt) {
+                               int64_t v0, int batch, int linear, int additive, bf16 *x0, float *tgt) {
     const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (r >= v0 * batch) return;
     const int b = (int)(r / v0);
@@ -711,7 +712,7 @@ __global__ void k_gather_batch(const bf16 *dr, const bf16 *de, const bf16 *df, c
     for (int c = 0; c < 3; c++) {
         f[c] = __bfloat162float(dr[3 * src + c]);
         f[3 + c] = __bfloat162float(df[3 * fs + c]) * (linear ? f[c] : 1.0f);
-        tgt[3 * r + c] = __bfloat162float(de[3 * src + c]);
+        tgt[3 * r + c] = __bfloat162float(de[3 * src + c]) - (additive ? f[c] : 0.0f);
     }
     uint4 *o = reinterpret_cast<uint4 *>(x0 + r * 16);
     o[0] = pack8(f);
@@ -798,7 +799,8 @@ struct mpm_nn {
     int *idx = nullptr;
     int *err = nullptr;
     bool weights_dirty = true;
-    int linear = 1;   // 1: no activations and no biases (a linear operator of the input)
+    int linear = 1;     // 1: no activations and no biases (a linear operator of the input)
+    int additive = 1;   // 1: preconditioner r + net(r), the network trained on (error - residual)
     int64_t adam_step = 0;
     bf16 *data_r = nullptr, *data_e = nullptr;
     int64_t ndata = 0, data_cap = 0;
@@ -967,8 +969,10 @@ cudaError_t backward(mpm_nn *net, cudaStream_t st, int batch) {
                                       batch)) != cudaSuccess)
         return e;
     if (!lin) launch_chan_sum<16>(net, st, net->ge0, r0, G + b_offset(0));
-    if (lin)   // biases are not used: their gradients are zero
+    if (lin) {   // biases are not used: their gradients are zero
         for (int l = 0; l < NCONV; l++) cudaMemsetAsync(G + b_offset(l), 0, sizeof(float) * COUT[l], st);
+        cudaMemsetAsync(G + b5_offset(), 0, sizeof(float) * 3, st);
+    }
     if ((e = launch_dw<16, 16, S1>(net, st, net->x0, net->ge0, L0, L0, batch, NIN, G + w_offset(0))) != cudaSuccess)
         return e;
     return cudaGetLastError();
@@ -1114,6 +1118,12 @@ mpm_status mpm_nn_set_linear(mpm_nn *net, int linear) {
     return MPM_OK;
 }
 
+mpm_status mpm_nn_set_additive(mpm_nn *net, int additive) {
+    if (!net) return MPM_ERR_BAD_ARG;
+    net->additive = additive ? 1 : 0;
+    return MPM_OK;
+}
+
 mpm_status mpm_nn_set_stream(mpm_nn *net, void *stream) {
     if (!net) return MPM_ERR_BAD_ARG;
     net->stream = (cudaStream_t)stream;
@@ -1205,7 +1215,8 @@ mpm_status mpm_nn_train(mpm_nn *net, int epochs, int batch, double lr, uint64_t 
         for (int64_t bi = 0; bi < nb; bi++) {
             CKN(cudaMemcpyAsync(net->idx, perm.data() + bi * batch, batch * 4, cudaMemcpyHostToDevice, st));
             k_gather_batch<<<blocks(r0), 256, 0, st>>>(net->data_r, net->data_e, net->data_f, net->data_sys,
-                                                       net->idx, v0, batch, net->linear, net->x0, net->tgt);
+                                                       net->idx, v0, batch, net->linear, net->additive, net->x0,
+                                                       net->tgt);
             CKN(forward(net, st, batch));
             k_output<<<blocks(r0), 256, 0, st>>>(net->d0, net->p + w5_offset(), net->linear ? nullptr : net->p + b5_offset(), net->z, r0);
             k_mse<<<batch, RED_THREADS, 0, st>>>(net->z, net->tgt, net->gz, v0, batch, net->loss);
@@ -1241,7 +1252,7 @@ mpm_status mpm_nn_apply_precond(mpm_nn *net, cudaStream_t st, const double *r, c
     CKN(forward(net, st, 1));
     k_output_precond<<<blocks(nodec), 256, 0, st>>>(net->d0, net->p + w5_offset(),
                                                    net->linear ? nullptr : net->p + b5_offset(), rr, nodec,
-                                                   adiag, bcflag, mtol, z);
+                                                   adiag, bcflag, mtol, net->additive ? r : nullptr, z);
     CKN(cudaGetLastError());
     return MPM_OK;
 }

@@ -70,7 +70,7 @@ EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_s
            "mpm_gpu_implicit_step", "mpm_gpu_implicit_assemble", "mpm_gpu_implicit_get_system",
            "mpm_gpu_implicit_matvec", "mpm_gpu_implicit_solve", "mpm_gpu_p2g_noalloc", "mpm_gpu_autotune",
            "mpm_gpu_get_tuning", "mpm_nn_num_params", "mpm_nn_create", "mpm_nn_destroy", "mpm_nn_set_stream",
-           "mpm_nn_init_params", "mpm_nn_set_linear", "mpm_nn_set_params", "mpm_nn_get_params", "mpm_nn_forward", "mpm_nn_backward",
+           "mpm_nn_init_params", "mpm_nn_set_linear", "mpm_nn_set_additive", "mpm_nn_set_params", "mpm_nn_get_params", "mpm_nn_forward", "mpm_nn_backward",
            "mpm_nn_num_pairs", "mpm_nn_train", "mpm_gpu_implicit_set_precond", "mpm_gpu_implicit_harvest",
            "mpm_gpu_set_graph", "mpm_gpu_set_tuning"]
 
@@ -123,6 +123,7 @@ def load(path: str | None = None):
     lib.mpm_nn_destroy.argtypes = [C.c_void_p]
     lib.mpm_nn_set_stream.argtypes = [C.c_void_p, C.c_void_p]
     lib.mpm_nn_set_linear.argtypes = [C.c_void_p, C.c_int]
+    lib.mpm_nn_set_additive.argtypes = [C.c_void_p, C.c_int]
     lib.mpm_nn_init_params.argtypes = [C.c_void_p, C.c_uint64]
     lib.mpm_nn_set_params.argtypes = [C.c_void_p, _fp]
     lib.mpm_nn_get_params.argtypes = [C.c_void_p, _fp]
@@ -356,7 +357,7 @@ _fp32 = C.POINTER(C.c_float)
 class PrecondNet:
     """The learned preconditioner network (mpm_nn_*) on a grid of `nodes` control points."""
 
-    def __init__(self, nodes, max_batch=1, max_pairs=0, seed=None, linear=True):
+    def __init__(self, nodes, max_batch=1, max_pairs=0, seed=None, linear=True, additive=True):
         self.lib = load()
         self.nodes = tuple(int(n) for n in nodes)
         n3 = (C.c_int * 3)(*self.nodes)
@@ -364,6 +365,7 @@ class PrecondNet:
         _chk(self.lib.mpm_nn_create(n3, int(max_batch), int(max_pairs), C.byref(h)), "mpm_nn_create")
         self.net = h
         _chk(self.lib.mpm_nn_set_linear(self.net, int(linear)), "mpm_nn_set_linear")
+        _chk(self.lib.mpm_nn_set_additive(self.net, int(additive)), "mpm_nn_set_additive")
         self.nvox = self.nodes[0] * self.nodes[1] * self.nodes[2]
         self.nparams = int(self.lib.mpm_nn_num_params())
         if seed is not None:

@@ -36,7 +36,7 @@ def load_weights(path=WEIGHTS):
     return p if p.size == capi.load().mpm_nn_num_params() else None
 
 
-def train(pairs=20000, loads_per_system=8, pairs_per_load=25, epochs=4, batch=8, lr=1.0e-3, seed=0,
+def train(pairs=20000, loads_per_system=8, pairs_per_load=25, epochs=8, batch=8, lr=1.0e-3, seed=0,
           harvest_eps=1.0e-20, scene=None, out=WEIGHTS, log=print):
     s = scene if scene is not None else scenes.cantilever(iprop=1)
     gpu = capi.GpuImplicitSolid(s, nr_flag=True)
@@ -70,7 +70,7 @@ def train(pairs=20000, loads_per_system=8, pairs_per_load=25, epochs=4, batch=8,
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--pairs", type=int, default=20000)
-    ap.add_argument("--epochs", type=int, default=4)
+    ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--lr", type=float, default=1.0e-3)
     ap.add_argument("--seed", type=int, default=0)

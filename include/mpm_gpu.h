@@ -248,6 +248,10 @@ mpm_status mpm_nn_set_stream(mpm_nn *net, void *stream);
  * operator of the residual (a preconditioner must not change with the
  * residual's scale or sign); 0: ReLU activations with biases. */
 mpm_status mpm_nn_set_linear(mpm_nn *net, int linear);
+/* additive = 1 (default): the preconditioner is z = r + net(r) (Jacobi in the
+ * scaled system plus a learned correction) and training fits net(r) to
+ * e - r; 0: z = net(r), trained on e. */
+mpm_status mpm_nn_set_additive(mpm_nn *net, int additive);
 mpm_status mpm_nn_init_params(mpm_nn *net, uint64_t seed);
 mpm_status mpm_nn_set_params(mpm_nn *net, const float *params);
 mpm_status mpm_nn_get_params(mpm_nn *net, float *params);
