@@ -753,14 +753,14 @@ mpm_status mpm_gpu_autotune(mpm_ctx *c, int steps_per_trial, double facl) {
 
 mpm_status mpm_gpu_set_tuning(mpm_ctx *c, int p2g_minb, int musl_minb, int update_ctas_per_sm) {
     if (!c) return MPM_ERR_BAD_ARG;
-    if ((p2g_minb < 0 || p2g_minb == 1 || p2g_minb > 6) || (musl_minb != 0 && musl_minb != 2 && musl_minb != 3) ||
+    if ((p2g_minb < 0 || p2g_minb == 1 || p2g_minb > 6) || (musl_minb < 0 || musl_minb == 1 || musl_minb > 4) ||
         update_ctas_per_sm < 0 || update_ctas_per_sm > 8)
         return MPM_ERR_BAD_ARG;
     c->tune.p2g_staged = p2g_minb == 0;
     c->tune.p2g_moments = p2g_minb == 4 ? 1 : p2g_minb == 5 ? 2 : p2g_minb == 6 ? 3 : 0;
     if (p2g_minb == 2 || p2g_minb == 3) c->tune.p2g_minb = p2g_minb;
-    c->tune.musl_staged = musl_minb == 0;
-    if (musl_minb) c->tune.musl_minb = musl_minb;
+    c->tune.musl_staged = musl_minb == 0 ? 1 : musl_minb == 4 ? 2 : 0;
+    if (musl_minb == 2 || musl_minb == 3) c->tune.musl_minb = musl_minb;
     c->tune.update_ctas_per_sm = update_ctas_per_sm;
     return MPM_OK;
 }
@@ -769,7 +769,7 @@ mpm_status mpm_gpu_get_tuning(mpm_ctx *c, int *p2g_minb, int *musl_minb, int *up
     if (!c) return MPM_ERR_BAD_ARG;
     if (p2g_minb)
         *p2g_minb = c->tune.p2g_moments ? 3 + c->tune.p2g_moments : c->tune.p2g_staged ? 0 : c->tune.p2g_minb;
-    if (musl_minb) *musl_minb = c->tune.musl_staged ? 0 : c->tune.musl_minb;
+    if (musl_minb) *musl_minb = c->tune.musl_staged == 2 ? 4 : c->tune.musl_staged ? 0 : c->tune.musl_minb;
     if (update_ctas_per_sm) *update_ctas_per_sm = c->tune.update_ctas_per_sm;
     return MPM_OK;
 }

@@ -858,6 +858,193 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell(StepArgs<f
     musl_node_pass(a, S, corner, sh_l, sh_f, lc, h, ox, oy, oz, acc, gacc, vmax);
 }
 
+// Gather + MUSL, one CTA of 128 threads per brick, two phases per chunk of
+// 128 of the brick's particles as in k_p2g_brick: (1) thread t gathers its
+// particle's velocity and shifting gradient from the brick's node box in
+// shared memory, writes the velocity (coalesced) and puts the 24 moment
+// terms m v x {1, u, v, w, uv, uw, vw, uvw} in shared memory; (2) thread c
+// adds its cell's terms in particle order.  Particles that left their
+// sorted cell gather from global memory and re-project with atomics.
+constexpr int MMOM = 24;
+
+__global__ void __launch_bounds__(BCH) k_musl_brick(StepArgs<float> a) {
+    constexpr int NX = BRX + 1, NY = BRY + 1, NZ = BRZ + 1, NBX = NX * NY * NZ;
+    __shared__ float T[MMOM][BCH];            // 12 KB; reused for the corner sums
+    __shared__ float box[4][NBX];             // G x, y, z and nei of the brick's nodes
+    __shared__ Scales S;
+    __shared__ long long sh_l[32];
+    __shared__ float sh_f[32];
+    __shared__ int scs[BRC + 1];
+    const int b = blockIdx.x;
+    const int *cs = a.cstart + (size_t)b * (BRC + 1);
+    const int P0 = cs[0], P1 = cs[BRC];
+    if (P0 == P1) return;
+    const int tid = threadIdx.x;
+    const size_t N = (size_t)a.g.nodec;
+    for (int i = tid; i <= BRC; i += BCH) scs[i] = cs[i];
+    int ox, oy, oz;
+    brick_origin(b, a.nbrick, ox, oy, oz);
+    for (int l = tid; l < NBX; l += BCH) {
+        const int nx = l % NX, ny = (l / NX) % NY, nz = l / (NX * NY);
+        const int gx = min(ox + nx, a.g.nnc[0] - 1), gy = min(oy + ny, a.g.nnc[1] - 1),
+                  gz = min(oz + nz, a.g.nnc[2] - 1);
+        const size_t gn = node_id(a.g, gx, gy, gz);
+        box[0][l] = ld(a.G + gn);
+        box[1][l] = ld(a.G + N + gn);
+        box[2][l] = ld(a.G + 2 * N + gn);
+        box[3][l] = ld(a.nei + gn);
+    }
+    load_scales(a, S);   // also publishes scs and box
+    const Particles<float> &P = a.P;
+    const bool flip = (a.scheme == MPM_FLIP);
+    const int lc = tid;
+    const int p0 = scs[lc], p1 = scs[lc + 1];
+    float M[MMOM];
+#pragma unroll
+    for (int k = 0; k < MMOM; k++) M[k] = 0.0f;
+    long long gacc = 0;
+    float vmax = 0.0f;
+    for (int c0 = P0; c0 < P1; c0 += BCH) {
+        const int p = c0 + tid;
+        if (p < P1) {
+            const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+            const float m = ld(P.m + p), vol = ld(P.vol + p);
+            bool oob = false;
+            const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
+            const int qx = px - ox, qy = py - oy, qz = pz - oz;
+            const bool inbox =
+                (unsigned)qx < (unsigned)BRX && (unsigned)qy < (unsigned)BRY && (unsigned)qz < (unsigned)BRZ;
+            bool mine = inbox;
+            if (mine) {
+                const int q = qx + BRX * (qy + BRY * qz);
+                mine = p >= scs[q] && p < scs[q + 1];
+            }
+            const float u = cell_offset_u(x0, a.g, 0, px), v = cell_offset_u(x1, a.g, 1, py),
+                        w = cell_offset_u(x2, a.g, 2, pz);
+            const float wx[2] = {0.5f - u, 0.5f + u}, wy[2] = {0.5f - v, 0.5f + v}, wz[2] = {0.5f - w, 0.5f + w};
+            const float dx[2] = {-a.g.inv_dx[0], a.g.inv_dx[0]}, dy[2] = {-a.g.inv_dx[1], a.g.inv_dx[1]},
+                        dz[2] = {-a.g.inv_dx[2], a.g.inv_dx[2]};
+            float vs[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+            for (int k = 0; k < 2; k++)
+#pragma unroll
+                for (int j = 0; j < 2; j++)
+#pragma unroll
+                    for (int i = 0; i < 2; i++) {
+                        float gv[3], e;
+                        if (inbox) {
+                            const int l = (qx + i) + NX * ((qy + j) + NY * (qz + k));
+                            gv[0] = box[0][l];
+                            gv[1] = box[1][l];
+                            gv[2] = box[2][l];
+                            e = box[3][l];
+                        } else {
+                            const size_t gn = node_id(a.g, px + i, py + j, pz + k);
+                            gv[0] = ld(a.G + gn);
+                            gv[1] = ld(a.G + N + gn);
+                            gv[2] = ld(a.G + 2 * N + gn);
+                            e = ld(a.nei + gn);
+                        }
+                        const float wxy = wx[i] * wy[j];
+                        const float Nn = wxy * wz[k];
+                        const float wv = flip ? Nn * a.dt : Nn;
+#pragma unroll
+                        for (int d = 0; d < 3; d++) vs[d] += wv * gv[d];
+                        gu[0] += dx[i] * wy[j] * wz[k] * e;
+                        gu[1] += wx[i] * dy[j] * wz[k] * e;
+                        gu[2] += wxy * dz[k] * e;
+                    }
+            float vel[3] = {vs[0], vs[1], vs[2]};
+            if (flip) {
+                vel[0] += ld(P.v[0] + p);
+                vel[1] += ld(P.v[1] + p);
+                vel[2] += ld(P.v[2] + p);
+            }
+            P.v[0][p] = vel[0];
+            P.v[1][p] = vel[1];
+            P.v[2][p] = vel[2];
+            vmax = fmaxf(vmax, fmaxf(fabsf(vel[0]), fmaxf(fabsf(vel[1]), fabsf(vel[2]))));
+            const float tv = 2.0f * vol;
+            const float g0 = gu[0] * tv, g1 = gu[1] * tv, g2 = gu[2] * tv;
+            gacc += fx(g0 * g0 + g1 * g1 + g2 * g2, S.gd);
+            if (mine) {
+                const float uv = u * v;
+                const float mono[8] = {1.0f, u, v, w, uv, u * w, v * w, uv * w};
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    const float q = m * vel[d];
+#pragma unroll
+                    for (int k = 0; k < 8; k++) T[8 * d + k][tid] = q * mono[k];
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < MMOM; k++) T[k][tid] = 0.0f;
+#pragma unroll 1
+                for (int k = 0; k < 2; k++)
+                    for (int j = 0; j < 2; j++)
+                        for (int i = 0; i < 2; i++) {
+                            const float Nm = wx[i] * wy[j] * wz[k] * m;
+                            const size_t gn = node_id(a.g, px + i, py + j, pz + k);
+                            for (int d = 0; d < 3; d++) {
+                                long long q = fx(Nm * vel[d], S.q);
+                                if (q) atomic_add_i64(&a.acc2[d * N + gn], q);
+                            }
+                        }
+            }
+        }
+        __syncthreads();
+        const int q0 = max(p0, c0), q1 = min(p1, c0 + BCH);
+        for (int q = q0; q < q1; q++) {
+            const int j = q - c0;
+#pragma unroll
+            for (int k = 0; k < MMOM; k++) M[k] += T[k][j];
+        }
+        __syncthreads();
+    }
+    // corners of this cell: T[d * 8 + corner][cell]
+#pragma unroll
+    for (int kk = 0; kk < 2; kk++)
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const int corner = i + 2 * (j + 2 * kk);
+                const float sx = i ? 1.0f : -1.0f, sy = j ? 1.0f : -1.0f, sz = kk ? 1.0f : -1.0f;
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    const float *Md = M + 8 * d;
+                    T[d * 8 + corner][lc] = Md[0] * 0.125f + (sx * Md[1] + sy * Md[2] + sz * Md[3]) * 0.25f +
+                                            (sx * sy * Md[4] + sx * sz * Md[5] + sy * sz * Md[6]) * 0.5f +
+                                            sx * sy * sz * Md[7];
+                }
+            }
+    long long gsum = block_reduce(gacc, OpAddL(), sh_l);
+    float vm = block_reduce(vmax, OpMaxF(), sh_f);
+    if (threadIdx.x == 0) {
+        if (gsum) atomicAdd(&a.ctl->geup_acc, (unsigned long long)gsum);
+        if (vm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VMAX], vm * 1.000001f);
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < NBX * 3; it += BCH) {
+        const int d = it / NBX, n = it % NBX;
+        const int nx = n % NX, ny = (n / NX) % NY, nz = n / (NX * NY);
+        const int gx = ox + nx, gy = oy + ny, gz = oz + nz;
+        if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
+        float sum = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+#pragma unroll
+            for (int j = 0; j < 2; j++)
+#pragma unroll
+                for (int i = 0; i < 2; i++) {
+                    const int ex = nx - i, ey = ny - j, ez = nz - k;
+                    if (ex >= 0 && ex < BRX && ey >= 0 && ey < BRY && ez >= 0 && ez < BRZ)
+                        sum += T[d * 8 + i + 2 * (j + 2 * k)][ex + BRX * (ey + BRY * ez)];
+                }
+        if (sum != 0.0f) atomic_add_i64(&a.acc2[d * N + node_id(a.g, gx, gy, gz)], fx(sum, S.q));
+    }
+}
+
 // The gather + MUSL with the brick's x, m, vol and (FLIP) v staged in shared
 // memory by bulk asynchronous copies, as k_p2g_cell_staged; same order of
 // operations as k_g2p_musl_cell, so the same results bit for bit.
@@ -1853,7 +2040,9 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
         timer_begin(c, K_G2P_MUSL);
         if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
             if (use_cell_kernels(c)) {
-                if (c->tune.musl_staged) {
+                if (c->tune.musl_staged == 2) {
+                    k_musl_brick<<<c->g.nbricks, BCH, 0, c->stream>>>(a);
+                } else if (c->tune.musl_staged) {
                     static bool attr = false;
                     if (!attr) {
                         cudaFuncSetAttribute(k_g2p_musl_cell_staged<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
