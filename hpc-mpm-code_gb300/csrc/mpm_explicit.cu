@@ -90,11 +90,6 @@ __device__ __forceinline__ size_t node_id(const KGeom<R> &g, int gx, int gy, int
 // Fixed-point scales.  Computed by one thread of a CTA (FP64 scalar work)
 // and shared; producer and consumer kernels derive them from the same
 // device-resident bounds, so they agree exactly.
-struct Scales {
-    Fix m, v, p, f;   // P2G: mass, vof, momentum, force
-    Fix q;            // MUSL momentum
-    Fix gd;           // |geup|^2
-};
 
 template <typename R>
 __device__ void compute_scales(const StepArgs<R> &a, Scales &s) {
@@ -113,10 +108,22 @@ __device__ void compute_scales(const StepArgs<R> &a, Scales &s) {
     s.gd = make_fix(a.nump * 3.0 * gb * gb * 1.0000001);
 }
 
+// The scales of a step are computed once: the P2G ones by k_step_reset, the
+// gather/MUSL ones by the last CTA of k_grid1 (they depend on the grid
+// maxima it records).  Kernels copy them into shared memory.
+template <typename R>
+__device__ __forceinline__ void load_scales_from(const Scales *src, Scales &sh) {
+    constexpr int W = (int)(sizeof(Scales) / 4);
+    if ((int)threadIdx.x < W) reinterpret_cast<unsigned *>(&sh)[threadIdx.x] = reinterpret_cast<const unsigned *>(src)[threadIdx.x];
+    __syncthreads();
+}
 template <typename R>
 __device__ __forceinline__ void load_scales(const StepArgs<R> &a, Scales &sh) {
-    if (threadIdx.x == 0) compute_scales(a, sh);
-    __syncthreads();
+    load_scales_from<R>(&a.ctl->sc_p2g, sh);
+}
+template <typename R>
+__device__ __forceinline__ void load_scales_musl(const StepArgs<R> &a, Scales &sh) {
+    load_scales_from<R>(&a.ctl->sc_musl, sh);
 }
 
 // Block-wide reduction (fixed order: deterministic); result valid in thread 0.
@@ -833,7 +840,7 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell(StepArgs<f
     brick_origin(b, a.nbrick, ox, oy, oz);
     const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
     const int p0 = cs[lc], p1 = cs[lc + 1];
-    load_scales(a, S);
+    load_scales_musl(a, S);
     const Particles<float> &P = a.P;
     MuslCell C;
     musl_load_cell(a, cx, cy, cz, h, p1 > p0, C);
@@ -894,7 +901,7 @@ __global__ void __launch_bounds__(BCH) k_musl_brick(StepArgs<float> a) {
         box[2][l] = ld(a.G + 2 * N + gn);
         box[3][l] = ld(a.nei + gn);
     }
-    load_scales(a, S);   // also publishes scs and box
+    load_scales_musl(a, S);   // also publishes scs and box
     const Particles<float> &P = a.P;
     const bool flip = (a.scheme == MPM_FLIP);
     const int lc = tid;
@@ -1090,7 +1097,7 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell_staged(Ste
     brick_origin(b, a.nbrick, ox, oy, oz);
     const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
     const int p0 = cs[lc], p1 = cs[lc + 1];
-    load_scales(a, S);
+    load_scales_musl(a, S);
     MuslCell C;
     musl_load_cell(a, cx, cy, cz, h, p1 > p0, C);
     float acc[3][4];
@@ -1143,6 +1150,7 @@ __global__ void k_step_reset(StepArgs<R> a) {
     ctl->p2g_inv[1] = s.v.inv;
     ctl->p2g_inv[2] = s.p.inv;
     ctl->p2g_inv[3] = s.f.inv;
+    ctl->sc_p2g = s;
     for (int k = 0; k < B_NB; k++) ctl->nxt[a.parity ^ 1][k] = 0u;
     for (int k = 0; k < C_NC; k++) ctl->cur[k] = 0u;
     ctl->geup_acc = 0ull;
@@ -1253,7 +1261,7 @@ __global__ void __launch_bounds__(256) k_g2p_musl_box(StepArgs<R> a) {
     int ox, oy, oz;
     brick_origin(w.tile, a.nbrick, ox, oy, oz);
     for (int i = threadIdx.x; i < 3 * BOX; i += blockDim.x) sacc[i] = 0ull;
-    load_scales(a, S);
+    load_scales_musl(a, S);
     const size_t N = (size_t)a.g.nodec;
     const Particles<R> &P = a.P;
     const bool flip = (a.scheme == MPM_FLIP);
@@ -1430,6 +1438,9 @@ __global__ void __launch_bounds__(256) k_grid1(StepArgs<R> a) {
         if (threadIdx.x == 0) {
             a.ctl->eu_norm = tot;
             a.ctl->tile_counter = 0u;
+            Scales sm;
+            compute_scales(a, sm);
+            a.ctl->sc_musl = sm;
         }
     }
 }
@@ -1441,13 +1452,11 @@ __global__ void __launch_bounds__(256) k_grid2(StepArgs<R> a) {
     const int t = blockIdx.x;
     if (t == 0 && threadIdx.x == 0) {
         // b0 of DeltaCorrectionParticleShifting (material_point.cpp:219)
-        Scales s;
-        compute_scales(a, s);
-        double gd = (double)(long long)a.ctl->geup_acc * s.gd.inv;
+        double gd = (double)(long long)a.ctl->geup_acc * a.ctl->sc_musl.gd.inv;
         a.ctl->b0 = (!a.shifting || gd < (double)a.mtol) ? 0.0 : a.ctl->eu_norm / gd;
     }
     if (!(a.all_tiles || a.tileflag[t])) return;
-    load_scales(a, S);
+    load_scales_musl(a, S);
     int tx, ty, tz;
     tile_coords(t, a.g.ntile, tx, ty, tz);
     const size_t N = (size_t)a.g.nodec;

@@ -57,6 +57,22 @@ struct Geom {
 enum BoundSlot { B_VMAX = 0, B_VOLMAX, B_VOLSMAX, B_AMAX, B_NB };   // produced for the next step
 enum CurSlot { C_GMAX = 0, C_NEIMAX, C_NC };                    // produced and used within a step
 
+// Fixed-point scale 2^e, applied as two float factors so that e up to +-250
+// never overflows an intermediate.
+struct Fix {
+    float s1, s2;   // s1 * s2 = 2^e
+    float i1, i2;   // i1 * i2 = 2^-e
+    double sd;      // 2^e
+    double inv;     // 2^-e
+};
+
+// Fixed-point scales of one step (see make_fix).
+struct Scales {
+    Fix m, v, p, f;   // P2G: mass, vof, momentum, force
+    Fix q;            // MUSL momentum
+    Fix gd;           // |geup|^2
+};
+
 struct DevCtl {
     unsigned int nxt[2][B_NB];
     unsigned int cur[C_NC];
@@ -69,6 +85,8 @@ struct DevCtl {
     double p2g_inv[4];               // 2^-e of the P2G scales (mass, vof, momentum, force) of the last P2G
     double b0;                       // shifting coefficient of this step
     unsigned int err_timeout;        // bounded device waits that gave up
+    Scales sc_p2g;                   // this step's P2G scales (k_step_reset)
+    Scales sc_musl;                  // this step's gather/MUSL scales (last CTA of k_grid1)
 };
 
 template <typename R>
@@ -84,14 +102,6 @@ struct WorkItem {
     int end;
 };
 
-// Fixed-point scale 2^e, applied as two float factors so that e up to +-250
-// never overflows an intermediate.
-struct Fix {
-    float s1, s2;   // s1 * s2 = 2^e
-    float i1, i2;   // i1 * i2 = 2^-e
-    double sd;      // 2^e
-    double inv;     // 2^-e
-};
 
 // Launch variants that give bitwise identical results; chosen by
 // mpm_gpu_autotune from measured times (defaults otherwise).

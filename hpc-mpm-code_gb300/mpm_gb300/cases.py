@@ -1,0 +1,85 @@
+"""Focused runs of one workload each, for profiling with ncu.
+
+    python -m mpm_gb300.cases explicit [--cells 64] [--steps 20]
+    python -m mpm_gb300.cases implicit [--steps 1]       # Jacobi-PCG Newton steps, 1.728M-particle cantilever
+    python -m mpm_gb300.cases precond  [--steps 1]       # the same with the learned preconditioner
+    python -m mpm_gb300.cases network  [--reps 10]       # network forward passes on the 65^3 grid
+    python -m mpm_gb300.cases batched  [--steps 20]      # 256 packed scenes
+    python -m mpm_gb300.cases fluid    [--steps 20]      # 12.6M-particle Tait dam break
+
+Each case builds its scene, runs a few warm-up steps, then the requested
+steps on a non-default stream, and exits 0.  Nothing is timed here: the
+numbers come from the profiler or from bench.py.
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+
+import numpy as np
+
+from . import capi, scenes
+
+
+def _stream():
+    import torch
+
+    return torch.cuda.Stream()
+
+
+def run(case, steps, cells, reps):
+    st = _stream()
+    if case == "explicit":
+        s = scenes.spinning_block(cells=(cells, cells, cells),
+                                  grid=(cells + 48, cells + 48, cells + 48))
+        g = capi.GpuSolid(s, precision=32, stream=st.cuda_stream)
+        g.steps(3)
+        g.steps(steps)
+        g.sync()
+    elif case in ("implicit", "precond"):
+        s = scenes.cantilever(iprop=1)
+        g = capi.GpuImplicitSolid(s, nr_flag=True, stream=st.cuda_stream)
+        if case == "precond":
+            from . import train_precond
+
+            p = train_precond.load_weights()
+            if p is None:
+                sys.exit("no committed preconditioner parameters")
+            net = capi.PrecondNet(s.xynodec)
+            net.set_params(p)
+            g.set_precond(net)
+        g.implicit_steps(1, eps=1.0e-16)
+        g.implicit_steps(steps, eps=1.0e-16)
+        g.sync()
+    elif case == "network":
+        net = capi.PrecondNet((65, 65, 65), seed=1)
+        x = np.random.default_rng(0).normal(size=(1, 65 ** 3, 6)).astype(np.float32)
+        for _ in range(reps):
+            net.forward(x)
+    elif case == "batched":
+        b = scenes.pack_scenes(scenes.batch_scenes())
+        g = capi.GpuSolid(b.scene, precision=32, shifting=False, stream=st.cuda_stream)
+        g.steps(3)
+        g.steps(steps)
+        g.sync()
+    elif case == "fluid":
+        g = capi.GpuSolid(scenes.dam_break(), precision=32, stream=st.cuda_stream)
+        g.steps(3)
+        g.steps(steps)
+        g.sync()
+    else:
+        sys.exit(f"unknown case {case}")
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("case")
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--cells", type=int, default=64)
+    ap.add_argument("--reps", type=int, default=10)
+    a = ap.parse_args()
+    run(a.case, a.steps, a.cells, a.reps)
+
+
+if __name__ == "__main__":
+    main()
