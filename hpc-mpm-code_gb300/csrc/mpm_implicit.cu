@@ -1509,3 +1509,24 @@ mpm_status mpm_gpu_implicit_harvest(mpm_ctx *c, mpm_nn *net, int nsystems, int l
     CKI(cudaStreamSynchronize(c->stream));
     return check_launch(c);
 }
+
+// Test hook: z = M(r) for host arrays r, z (3 * nodec, scaled system) with the
+// preconditioner set on ctx and the features of the assembled system.
+mpm_status mpm_gpu_implicit_apply_precond(mpm_ctx *c, const double *r, double *z) {
+    if (!c || !c->imp || !c->imp->net || !r || !z) return MPM_ERR_BAD_ARG;
+    ImpState *s = c->imp;
+    ImpArgs a = imp_args(c);
+    const int nb = nb_nodes(c);
+    const size_t N = (size_t)c->g.nodec;
+    CKI(cudaMemcpyAsync(s->r, r, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->stream));
+    k_phi<<<nb, 256, 0, c->stream>>>(a, s->nmass, s->adiag, s->ev);
+    mpm_status st = mpm_nn_set_feature(s->net, c->stream, s->ev);
+    if (st != MPM_OK) return st;
+    k_dot3<<<nb, 256, 0, c->stream>>>(a, s->r, s->r, s->part);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
+    st = mpm_nn_apply_precond(s->net, c->stream, s->r, s->scal + S_RRC, s->adiag, a.bcflag, a.mtol, s->z);
+    if (st != MPM_OK) return st;
+    CKI(cudaMemcpyAsync(z, s->z, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, c->stream));
+    CKI(cudaStreamSynchronize(c->stream));
+    return check_launch(c);
+}

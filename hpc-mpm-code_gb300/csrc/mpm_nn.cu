@@ -584,6 +584,58 @@ __global__ void k_output_precond(const bf16 *d0, const float *w5, const float *b
     }
 }
 
+// adjoint input: gz = the normalized residual (the vector the symmetric
+// part is applied to), FP32 [nodec][3]
+__global__ void k_adj_seed(const bf16 *x0, float *gz, int64_t nodec) {
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nodec) return;
+    float f[8];
+    unpack8(reinterpret_cast<const uint4 *>(x0 + n * 16)[0], f);
+    gz[3 * n] = f[0];
+    gz[3 * n + 1] = f[1];
+    gz[3 * n + 2] = f[2];
+}
+
+// gd0 = gz W5^T (linear network: no activation mask)
+__global__ void k_output_adj(const float *gz, const float *w5, bf16 *gd0, int64_t rows) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const float g0 = gz[3 * r], g1 = gz[3 * r + 1], g2 = gz[3 * r + 2];
+    float o[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) o[k] = g0 * w5[k * 3] + g1 * w5[k * 3 + 1] + g2 * w5[k * 3 + 2];
+    uint4 *q = reinterpret_cast<uint4 *>(gd0 + r * 16);
+    q[0] = pack8(o);
+    q[1] = pack8(o + 8);
+}
+
+// symmetric preconditioner output: z = r + s/2 (N x + B^T N^T x), x = r / s,
+// with N x = d0 W5 and B^T v = v[0:3] + phi * v[3:6] (the input map of the
+// linear network); zero on inactive and boundary rows
+__global__ void k_output_sym(const bf16 *d0, const bf16 *gx0, const bf16 *feat, const float *w5, const double *rr,
+                             int64_t nodec, const double *adiag, const unsigned char *bcflag, double mtol,
+                             const double *r, double *z) {
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nodec) return;
+    const double ms = rr[0] / (3.0 * (double)nodec);
+    const double s = ms > 0.0 ? sqrt(ms) : 0.0;
+    float f[16], g[8];
+    const uint4 *p = reinterpret_cast<const uint4 *>(d0 + n * 16);
+    unpack8(p[0], f);
+    unpack8(p[1], f + 8);
+    unpack8(reinterpret_cast<const uint4 *>(gx0 + n * 16)[0], g);
+    const unsigned char bf = bcflag[n];
+    for (int c = 0; c < 3; c++) {
+        float o = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 16; k++) o += f[k] * w5[k * 3 + c];
+        const float adj = g[c] + __bfloat162float(feat[3 * n + c]) * g[3 + c];
+        const int64_t i = c * nodec + n;
+        const bool off = (bf & (1 << c)) || !(adiag[i] >= mtol);
+        z[i] = off ? 0.0 : r[i] + 0.5 * s * ((double)o + (double)adj);
+    }
+}
+
 constexpr int RED_THREADS = 256;
 
 // gd0 = (gz W5^T) masked by d0 > 0; per-block partials of dW5 (48) and db5 (3)
@@ -670,6 +722,7 @@ __global__ void k_part_reduce(const float *part, int nblk, int n, float *out) {
 // forward: per tap an N = cout x K = kpad tile of W[t][ci][co];
 // transposed (data gradient): per tap an N = cin x K = cout tile.
 __global__ void k_wprep(const float *w, int cin, int cout, int kpad, bf16 *fwd, bf16 *trn) {
+    const int npad = (cin + 15) / 16 * 16;   // rows of a transposed tile (MMA N, a multiple of 16)
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx < 27 * cout * kpad) {
         const int k = idx % kpad, rest = idx / kpad;
@@ -678,11 +731,11 @@ __global__ void k_wprep(const float *w, int cin, int cout, int kpad, bf16 *fwd, 
         const uint32_t off = t * (uint32_t)(cout * kpad * 2) + tc::kmaj_off(n, k, kpad);
         *reinterpret_cast<bf16 *>(reinterpret_cast<unsigned char *>(fwd) + off) = __float2bfloat16_rn(v);
     }
-    if (trn && idx < 27 * cin * cout) {
+    if (trn && idx < 27 * npad * cout) {
         const int k = idx % cout, rest = idx / cout;
-        const int n = rest % cin, t = rest / cin;
-        const float v = w[((size_t)t * cin + n) * cout + k];
-        const uint32_t off = t * (uint32_t)(cin * cout * 2) + tc::kmaj_off(n, k, cout);
+        const int n = rest % npad, t = rest / npad;
+        const float v = n < cin ? w[((size_t)t * cin + n) * cout + k] : 0.0f;
+        const uint32_t off = t * (uint32_t)(npad * cout * 2) + tc::kmaj_off(n, k, cout);
         *reinterpret_cast<bf16 *>(reinterpret_cast<unsigned char *>(trn) + off) = __float2bfloat16_rn(v);
     }
 }
@@ -801,6 +854,8 @@ struct mpm_nn {
     bool weights_dirty = true;
     int linear = 1;     // 1: no activations and no biases (a linear operator of the input)
     int additive = 1;   // 1: preconditioner r + net(r), the network trained on (error - residual)
+    int symmetric = 1;  // 1 (linear, additive): apply r + (N + N^T) r / 2
+    bf16 *gx0 = nullptr;   // adjoint result at the input [v0][16]
     int64_t adam_step = 0;
     bf16 *data_r = nullptr, *data_e = nullptr;
     int64_t ndata = 0, data_cap = 0;
@@ -888,8 +943,7 @@ cudaError_t prep_weights(mpm_nn *net, cudaStream_t st) {
     if (!net->weights_dirty) return cudaSuccess;
     for (int l = 0; l < NCONV; l++) {
         const int n = 27 * COUT[l] * std::max(KPAD[l], CIN[l]);
-        k_wprep<<<blocks(n), 256, 0, st>>>(net->p + w_offset(l), CIN[l], COUT[l], KPAD[l], net->wf[l],
-                                           l == 0 ? nullptr : net->wt[l]);
+        k_wprep<<<blocks(n), 256, 0, st>>>(net->p + w_offset(l), CIN[l], COUT[l], KPAD[l], net->wf[l], net->wt[l]);
     }
     net->weights_dirty = false;
     return cudaGetLastError();
@@ -978,6 +1032,33 @@ cudaError_t backward(mpm_nn *net, cudaStream_t st, int batch) {
     return cudaGetLastError();
 }
 
+// N^T applied to net->gz (linear network): the data-gradient chain of
+// backward() without weight gradients, down to the input x0 (net->gx0)
+cudaError_t adjoint(mpm_nn *net, cudaStream_t st) {
+    const Lvl &L0 = net->L[0], &L1 = net->L[1], &L2 = net->L[2];
+    const int64_t r0 = L0.v, r1 = L1.v, r2 = L2.v;
+    cudaError_t e;
+    k_output_adj<<<blocks(r0), 256, 0, st>>>(net->gz, net->p + w5_offset(), net->gd0, r0);
+    k_restrict<16><<<blocks(r1 * 2), 256, 0, st>>>(net->gd0, net->gc1, L0, L1, r1);
+    if ((e = launch_conv<16, 32, S1T>(net, st, net->gc1, net->gd1, net->wt[4], nullptr, nullptr, nullptr, 0, L1, L1,
+                                      1)) != cudaSuccess)
+        return e;
+    k_restrict<32><<<blocks(r2 * 4), 256, 0, st>>>(net->gd1, net->gc2, L1, L2, r2);
+    if ((e = launch_conv<32, 64, S1T>(net, st, net->gc2, net->ge2, net->wt[3], nullptr, nullptr, nullptr, 0, L2, L2,
+                                      1)) != cudaSuccess)
+        return e;
+    if ((e = launch_conv<64, 32, S2T>(net, st, net->ge2, net->ge1, net->wt[2], nullptr, net->gd1, nullptr, 0, L2, L1,
+                                      1)) != cudaSuccess)
+        return e;
+    if ((e = launch_conv<32, 16, S2T>(net, st, net->ge1, net->ge0, net->wt[1], nullptr, net->gd0, nullptr, 0, L1, L0,
+                                      1)) != cudaSuccess)
+        return e;
+    if ((e = launch_conv<16, 16, S1T>(net, st, net->ge0, net->gx0, net->wt[0], nullptr, nullptr, nullptr, 0, L0, L0,
+                                      1)) != cudaSuccess)
+        return e;
+    return cudaGetLastError();
+}
+
 mpm_status read_err(mpm_nn *net) {
     int h = 0;
     CKN(cudaMemcpy(&h, net->err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -992,7 +1073,7 @@ void net_free(mpm_nn *n) {
     void *ptrs[] = {n->p,   n->g,   n->am,  n->av,  n->x0,  n->e0,  n->e1,  n->e2,     n->c2,     n->d1,
                     n->c1,  n->d0,  n->gd0, n->ge0, n->gc1, n->gd1, n->ge1, n->gc2,    n->ge2,    n->z,
                     n->gz,  n->tgt, n->part, n->loss, n->idx, n->err, n->data_r, n->data_e, n->d_ndata,
-                    n->feat, n->data_f, n->data_sys};
+                    n->feat, n->data_f, n->data_sys, n->gx0};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int l = 0; l < NCONV; l++) {
@@ -1059,7 +1140,7 @@ mpm_status mpm_nn_create(const int nodes[3], int max_batch, int64_t max_pairs, m
     NN_ALLOC(n->av, P * 4);
     for (int l = 0; l < NCONV; l++) {
         NN_ALLOC(n->wf[l], (size_t)27 * COUT[l] * KPAD[l] * 2);
-        NN_ALLOC(n->wt[l], (size_t)27 * CIN[l] * COUT[l] * 2);
+        NN_ALLOC(n->wt[l], (size_t)27 * ((CIN[l] + 15) / 16 * 16) * COUT[l] * 2);
     }
     NN_ALLOC(n->x0, B * v0 * 16 * 2);
     NN_ALLOC(n->e0, B * v0 * 16 * 2);
@@ -1086,6 +1167,7 @@ mpm_status mpm_nn_create(const int nodes[3], int max_batch, int64_t max_pairs, m
     NN_ALLOC(n->err, sizeof(int));
     NN_ALLOC(n->d_ndata, sizeof(int64_t));
     NN_ALLOC(n->feat, (size_t)v0 * 3 * 2);
+    NN_ALLOC(n->gx0, (size_t)v0 * 16 * 2);
     if (max_pairs > 0) {
         NN_ALLOC(n->data_r, (size_t)max_pairs * v0 * 3 * 2);
         NN_ALLOC(n->data_e, (size_t)max_pairs * v0 * 3 * 2);
@@ -1115,6 +1197,12 @@ mpm_status mpm_nn_destroy(mpm_nn *net) {
 mpm_status mpm_nn_set_linear(mpm_nn *net, int linear) {
     if (!net) return MPM_ERR_BAD_ARG;
     net->linear = linear ? 1 : 0;
+    return MPM_OK;
+}
+
+mpm_status mpm_nn_set_symmetric(mpm_nn *net, int symmetric) {
+    if (!net) return MPM_ERR_BAD_ARG;
+    net->symmetric = symmetric ? 1 : 0;
     return MPM_OK;
 }
 
@@ -1250,6 +1338,14 @@ mpm_status mpm_nn_apply_precond(mpm_nn *net, cudaStream_t st, const double *r, c
     const int64_t nodec = net->L[0].v;
     k_input_r<<<blocks(nodec), 256, 0, st>>>(r, rr, net->feat, nodec, net->linear, net->x0);
     CKN(forward(net, st, 1));
+    if (net->symmetric && net->linear && net->additive) {
+        k_adj_seed<<<blocks(nodec), 256, 0, st>>>(net->x0, net->gz, nodec);
+        CKN(adjoint(net, st));
+        k_output_sym<<<blocks(nodec), 256, 0, st>>>(net->d0, net->gx0, net->feat, net->p + w5_offset(), rr, nodec,
+                                                   adiag, bcflag, mtol, r, z);
+        CKN(cudaGetLastError());
+        return MPM_OK;
+    }
     k_output_precond<<<blocks(nodec), 256, 0, st>>>(net->d0, net->p + w5_offset(),
                                                    net->linear ? nullptr : net->p + b5_offset(), rr, nodec,
                                                    adiag, bcflag, mtol, net->additive ? r : nullptr, z);

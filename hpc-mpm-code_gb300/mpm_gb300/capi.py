@@ -70,8 +70,8 @@ EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_s
            "mpm_gpu_implicit_step", "mpm_gpu_implicit_assemble", "mpm_gpu_implicit_get_system",
            "mpm_gpu_implicit_matvec", "mpm_gpu_implicit_solve", "mpm_gpu_p2g_noalloc", "mpm_gpu_autotune",
            "mpm_gpu_get_tuning", "mpm_nn_num_params", "mpm_nn_create", "mpm_nn_destroy", "mpm_nn_set_stream",
-           "mpm_nn_init_params", "mpm_nn_set_linear", "mpm_nn_set_additive", "mpm_nn_set_params", "mpm_nn_get_params", "mpm_nn_forward", "mpm_nn_backward",
-           "mpm_nn_num_pairs", "mpm_nn_train", "mpm_gpu_implicit_set_precond", "mpm_gpu_implicit_harvest",
+           "mpm_nn_init_params", "mpm_nn_set_linear", "mpm_nn_set_additive", "mpm_nn_set_symmetric", "mpm_nn_set_params", "mpm_nn_get_params", "mpm_nn_forward", "mpm_nn_backward",
+           "mpm_nn_num_pairs", "mpm_nn_train", "mpm_gpu_implicit_set_precond", "mpm_gpu_implicit_harvest", "mpm_gpu_implicit_apply_precond",
            "mpm_gpu_set_graph", "mpm_gpu_set_tuning"]
 
 
@@ -124,6 +124,7 @@ def load(path: str | None = None):
     lib.mpm_nn_set_stream.argtypes = [C.c_void_p, C.c_void_p]
     lib.mpm_nn_set_linear.argtypes = [C.c_void_p, C.c_int]
     lib.mpm_nn_set_additive.argtypes = [C.c_void_p, C.c_int]
+    lib.mpm_nn_set_symmetric.argtypes = [C.c_void_p, C.c_int]
     lib.mpm_nn_init_params.argtypes = [C.c_void_p, C.c_uint64]
     lib.mpm_nn_set_params.argtypes = [C.c_void_p, _fp]
     lib.mpm_nn_get_params.argtypes = [C.c_void_p, _fp]
@@ -132,6 +133,7 @@ def load(path: str | None = None):
     lib.mpm_nn_num_pairs.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
     lib.mpm_nn_train.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_uint64, _fp]
     lib.mpm_gpu_implicit_set_precond.argtypes = [C.c_void_p, C.c_void_p]
+    lib.mpm_gpu_implicit_apply_precond.argtypes = [C.c_void_p, _dp, _dp]
     lib.mpm_gpu_implicit_harvest.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
                                              C.c_double, C.c_uint64, C.c_double, C.c_int]
     _lib = lib
@@ -305,6 +307,13 @@ class GpuImplicitSolid(GpuSolid):
              "mpm_gpu_implicit_set_precond")
         self._net = net
 
+    def apply_precond(self, r):
+        """z = M(r) with the preconditioner set by set_precond (scaled system)."""
+        r = _d(r)
+        z = np.zeros(3 * self.nodec)
+        _chk(self.lib.mpm_gpu_implicit_apply_precond(self.ctx, _ptr(r), _ptr(z)), "mpm_gpu_implicit_apply_precond")
+        return z
+
     def harvest(self, net, nsystems, loads_per_system, pairs_per_load, e_min, e_max, seed=0, eps=1.0e-16,
                 kmax=20000):
         """Training pairs for `net` from this solid's own Jacobi-PCG solves."""
@@ -357,7 +366,7 @@ _fp32 = C.POINTER(C.c_float)
 class PrecondNet:
     """The learned preconditioner network (mpm_nn_*) on a grid of `nodes` control points."""
 
-    def __init__(self, nodes, max_batch=1, max_pairs=0, seed=None, linear=True, additive=True):
+    def __init__(self, nodes, max_batch=1, max_pairs=0, seed=None, linear=True, additive=True, symmetric=True):
         self.lib = load()
         self.nodes = tuple(int(n) for n in nodes)
         n3 = (C.c_int * 3)(*self.nodes)
@@ -366,6 +375,7 @@ class PrecondNet:
         self.net = h
         _chk(self.lib.mpm_nn_set_linear(self.net, int(linear)), "mpm_nn_set_linear")
         _chk(self.lib.mpm_nn_set_additive(self.net, int(additive)), "mpm_nn_set_additive")
+        _chk(self.lib.mpm_nn_set_symmetric(self.net, int(symmetric)), "mpm_nn_set_symmetric")
         self.nvox = self.nodes[0] * self.nodes[1] * self.nodes[2]
         self.nparams = int(self.lib.mpm_nn_num_params())
         if seed is not None:

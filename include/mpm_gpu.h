@@ -252,6 +252,11 @@ mpm_status mpm_nn_set_linear(mpm_nn *net, int linear);
  * scaled system plus a learned correction) and training fits net(r) to
  * e - r; 0: z = net(r), trained on e. */
 mpm_status mpm_nn_set_additive(mpm_nn *net, int additive);
+/* symmetric = 1 (default; linear additive networks): the solver applies the
+ * symmetric part z = r + (N r + N^T r) / 2, N^T by the network's transposed
+ * (data-gradient) convolutions, so that conjugate gradients see a symmetric
+ * preconditioner; 0: z = r + N r. */
+mpm_status mpm_nn_set_symmetric(mpm_nn *net, int symmetric);
 mpm_status mpm_nn_init_params(mpm_nn *net, uint64_t seed);
 mpm_status mpm_nn_set_params(mpm_nn *net, const float *params);
 mpm_status mpm_nn_get_params(mpm_nn *net, float *params);
@@ -265,6 +270,9 @@ mpm_status mpm_nn_num_pairs(mpm_nn *net, int64_t *n);
 mpm_status mpm_nn_train(mpm_nn *net, int epochs, int batch, double lr, uint64_t seed, float *epoch_loss);
 /* Use `net` (NULL: none) as the preconditioner of the implicit solves of ctx. */
 mpm_status mpm_gpu_implicit_set_precond(mpm_ctx *ctx, mpm_nn *net);
+/* Test hook: z = M(r) for host arrays (3 * nodec, diagonally scaled system)
+ * with the preconditioner set on ctx, after mpm_gpu_implicit_assemble. */
+mpm_status mpm_gpu_implicit_apply_precond(mpm_ctx *ctx, const double *r, double *z);
 /* Training pairs from the solver's own solves: for each of nsystems moduli
  * E drawn log-uniformly from [e_min, e_max] the system of the current state
  * is assembled; for its own right-hand side and loads_per_system - 1 seeded

@@ -65,3 +65,29 @@ def test_untrained_network_falls_back_and_converges():
     gpu.sync()
     assert rel_l2(xn, xj) <= 1e-5
     assert itn > 0
+
+
+def test_symmetric_preconditioner_is_symmetric():
+    """The applied preconditioner r + (N r + N^T r) / 2 is symmetric:
+    <M a, b> = <a, M b> up to BF16 rounding (the transposed convolutions are
+    the exact adjoints of the forward ones)."""
+    s = _cantilever()
+    gpu = capi.GpuImplicitSolid(s, nr_flag=False)
+    gpu.assemble()
+    _, d, _ = gpu.system()
+    act = np.abs(d) > 0
+    rng = np.random.default_rng(4)
+    net = capi.PrecondNet(s.xynodec, seed=21)
+    gpu.set_precond(net)
+    bcmask = np.ones(3 * s.nodec, dtype=bool)
+    for comp, nodes, _v in s.bcs:
+        bcmask[comp * s.nodec + nodes] = False
+    a = rng.normal(size=3 * s.nodec) * act * bcmask
+    b = rng.normal(size=3 * s.nodec) * act * bcmask
+    scale = np.linalg.norm(a) / np.linalg.norm(b)
+    b *= scale   # same RMS, so both applications use the same input scaling
+    ma, mb = gpu.apply_precond(a), gpu.apply_precond(b)
+    lhs, rhs = float(ma @ b), float(a @ mb)
+    gpu.set_precond(None)
+    gpu.sync()
+    assert abs(lhs - rhs) <= 3e-2 * max(abs(lhs), abs(rhs)), (lhs, rhs)
