@@ -40,6 +40,7 @@ struct StepArgs {
     const WorkItem *work;
     const int *nwork;
     const int *cstart;          // nbricks * (BRC + 1)
+    int *miss;                  // particles that left their sorted cell, processed by a deferred pass
     int nbrick[3];
     unsigned long long *acc;    // NACC * nodec
     unsigned long long *acc2;   // 3 * nodec
@@ -195,7 +196,7 @@ constexpr int CELL_THREADS = BRC * CELL_SPLIT;
 __device__ __forceinline__ void p2g_particle(const StepArgs<float> &a, const Scales &S, int cx, int cy, int cz, int h,
                                              float x0, float x1, float x2, float m, float vol, const float *v,
                                              const float *s, float fxg, float fyg, float fzg, float (*acc)[4],
-                                             int &misses, int &oobs) {
+                                             int &misses, int &oobs, int defer_p = -1) {
     bool oob = false;
     const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
     oobs += oob && h == 0;
@@ -207,8 +208,13 @@ __device__ __forceinline__ void p2g_particle(const StepArgs<float> &a, const Sca
     const bool mine = (px == cx) && (py == cy) && (pz == cz);
     const float wz = h ? az.w[1] : az.w[0], dwz = h ? az.dw[1] : az.dw[0];
     if (!mine) {
-        // a particle that left its sorted cell scatters on its own
+        // a particle that left its sorted cell scatters on its own, in the
+        // deferred pass (k_p2g_misses) when defer_p names it
         misses += h == 0;
+        if (defer_p >= 0) {
+            if (h == 0) a.miss[atomicAdd(&a.ctl->n_miss_p2g, 1u)] = defer_p;
+            return;
+        }
 #pragma unroll 1
         for (int c = 0; c < 4; c++) {
             const int i = c & 1, j = c >> 1;
@@ -309,7 +315,7 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell(StepArgs<float>
         const float s[6] = {ld(P.s[0] + p), ld(P.s[1] + p), ld(P.s[2] + p),
                             ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
         p2g_particle(a, S, cx, cy, cz, h, ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p), ld(P.m + p),
-                     ld(P.vol + p), v, s, fxg, fyg, fzg, acc, misses, oobs);
+                     ld(P.vol + p), v, s, fxg, fyg, fzg, acc, misses, oobs, p);
     }
     p2g_node_pass(a, S, corner, sh_red, lc, h, ox, oy, oz, acc, misses, oobs);
 }
@@ -374,8 +380,9 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_mom(StepArgs<fl
         bool oob = false;
         const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
         if (px != cx || py != cy || pz != cz) {
-            // a particle that left its sorted cell scatters on its own (both z-layers)
-            p2g_miss(a, S, cx, cy, cz, x0, x1, x2, m, vol, vel, sg, fxg, fyg, fzg, misses, oobs);
+            // a particle that left its sorted cell scatters in the deferred pass
+            misses++;
+            a.miss[atomicAdd(&a.ctl->n_miss_p2g, 1u)] = p;
             continue;
         }
         oobs += oob;
@@ -493,7 +500,8 @@ __global__ void __launch_bounds__(BCH) k_p2g_brick(StepArgs<float> a) {
                 mine = p >= scs[q] && p < scs[q + 1];
             }
             if (!mine) {
-                p2g_miss(a, S, -1, -1, -1, x0, x1, x2, m, vol, vel, sg, fxg, fyg, fzg, misses, oobs);
+                misses++;
+                a.miss[atomicAdd(&a.ctl->n_miss_p2g, 1u)] = p;
 #pragma unroll
                 for (int k = 0; k < NMOM; k++) T[k][tid] = 0.0f;
             } else {
@@ -667,7 +675,7 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_staged(StepArgs
             const float s[6] = {sf[6 * PST + l], sf[7 * PST + l], sf[8 * PST + l],
                                 sf[9 * PST + l], sf[10 * PST + l], sf[11 * PST + l]};
             p2g_particle(a, S, cx, cy, cz, h, sf[l], sf[PST + l], sf[2 * PST + l], sf[12 * PST + l],
-                         sf[13 * PST + l], v, s, fxg, fyg, fzg, acc, misses, oobs);
+                         sf[13 * PST + l], v, s, fxg, fyg, fzg, acc, misses, oobs, p);
         }
         __syncthreads();   // the stage is refilled only after every thread has read it
     }
@@ -715,6 +723,12 @@ __device__ __forceinline__ void musl_particle(const StepArgs<float> &a, const Sc
     axis_eval<float, 1>(x1, a.g, 1, py, ay);
     axis_eval<float, 1>(x2, a.g, 2, pz, az);
     const bool mine = (px == cx) && (py == cy) && (pz == cz);
+    if (!mine) {
+        // a particle that left its sorted cell: gathered and re-projected by
+        // the deferred pass (k_musl_misses); both lanes of the pair skip it
+        if (h == 0) a.miss[atomicAdd(&a.ctl->n_miss_musl, 1u)] = p;
+        return;
+    }
     const float wz = h ? az.w[1] : az.w[0], dwz = h ? az.dw[1] : az.dw[0];
     // partial gathers over this thread's four nodes
     float vs[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f};
@@ -1139,6 +1153,92 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell_staged(Ste
     musl_node_pass(a, S, corner, sh_l, sh_f, lc, h, ox, oy, oz, acc, gacc, vmax);
 }
 
+// Deferred passes for the particles that left their sorted cell since the
+// last re-sort: one thread per queued particle, fixed-point atomics (order
+// independent, so the results do not depend on the queue order).
+__global__ void __launch_bounds__(256) k_p2g_misses(StepArgs<float> a) {
+    __shared__ Scales S;
+    load_scales(a, S);
+    const unsigned n = a.ctl->n_miss_p2g;
+    const float fxg = a.grav[0] * a.facl, fyg = a.grav[1] * a.facl, fzg = a.grav[2] * a.facl;
+    const Particles<float> &P = a.P;
+    int misses = 0, oobs = 0;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int p = a.miss[i];
+        const float vel[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
+        const float sg[6] = {ld(P.s[0] + p), ld(P.s[1] + p), ld(P.s[2] + p),
+                             ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
+        p2g_miss(a, S, -1, -1, -1, ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p), ld(P.m + p), ld(P.vol + p), vel,
+                 sg, fxg, fyg, fzg, misses, oobs);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_musl_misses(StepArgs<float> a) {
+    __shared__ Scales S;
+    __shared__ long long sh_l[32];
+    __shared__ float sh_f[32];
+    load_scales_musl(a, S);
+    const unsigned n = a.ctl->n_miss_musl;
+    const size_t N = (size_t)a.g.nodec;
+    const bool flip = (a.scheme == MPM_FLIP);
+    const Particles<float> &P = a.P;
+    long long gacc = 0;
+    float vmax = 0.0f;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int p = a.miss[i];
+        const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+        const float m = ld(P.m + p), vol = ld(P.vol + p);
+        bool oob = false;
+        const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
+        Axis<float, 1> ax, ay, az;
+        axis_eval<float, 1>(x0, a.g, 0, px, ax);
+        axis_eval<float, 1>(x1, a.g, 1, py, ay);
+        axis_eval<float, 1>(x2, a.g, 2, pz, az);
+        float v[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f};
+        for (int k = 0; k < 2; k++)
+            for (int j = 0; j < 2; j++)
+                for (int ii = 0; ii < 2; ii++) {
+                    const size_t gn = node_id(a.g, px + ii, py + j, pz + k);
+                    const float wxy = ax.w[ii] * ay.w[j];
+                    const float N_ = wxy * az.w[k];
+                    const float wv = flip ? N_ * a.dt : N_;
+                    const float e = ld(a.nei + gn);
+#pragma unroll
+                    for (int d = 0; d < 3; d++) v[d] += wv * ld(a.G + d * N + gn);
+                    gu[0] += ax.dw[ii] * ay.w[j] * az.w[k] * e;
+                    gu[1] += ax.w[ii] * ay.dw[j] * az.w[k] * e;
+                    gu[2] += wxy * az.dw[k] * e;
+                }
+        if (flip) {
+#pragma unroll
+            for (int d = 0; d < 3; d++) v[d] += ld(P.v[d] + p);
+        }
+        P.v[0][p] = v[0];
+        P.v[1][p] = v[1];
+        P.v[2][p] = v[2];
+        vmax = fmaxf(vmax, fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2]))));
+        const float tv = 2.0f * vol;
+        const float g0 = gu[0] * tv, g1 = gu[1] * tv, g2 = gu[2] * tv;
+        gacc += fx(g0 * g0 + g1 * g1 + g2 * g2, S.gd);
+        for (int k = 0; k < 2; k++)
+            for (int j = 0; j < 2; j++)
+                for (int ii = 0; ii < 2; ii++) {
+                    const float Nm = ax.w[ii] * ay.w[j] * az.w[k] * m;
+                    const size_t gn = node_id(a.g, px + ii, py + j, pz + k);
+                    for (int d = 0; d < 3; d++) {
+                        const long long q = fx(Nm * v[d], S.q);
+                        if (q) atomic_add_i64(&a.acc2[d * N + gn], q);
+                    }
+                }
+    }
+    const long long gsum = block_reduce(gacc, OpAddL(), sh_l);
+    const float vm = block_reduce(vmax, OpMaxF(), sh_f);
+    if (threadIdx.x == 0) {
+        if (gsum) atomicAdd(&a.ctl->geup_acc, (unsigned long long)gsum);
+        if (vm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VMAX], vm * 1.000001f);
+    }
+}
+
 // Launched before the P2G of every step: records the P2G scales (for result
 // downloads) and resets the per-step device counters.
 template <typename R>
@@ -1151,6 +1251,8 @@ __global__ void k_step_reset(StepArgs<R> a) {
     ctl->p2g_inv[2] = s.p.inv;
     ctl->p2g_inv[3] = s.f.inv;
     ctl->sc_p2g = s;
+    ctl->n_miss_p2g = 0u;
+    ctl->n_miss_musl = 0u;
     for (int k = 0; k < B_NB; k++) ctl->nxt[a.parity ^ 1][k] = 0u;
     for (int k = 0; k < C_NC; k++) ctl->cur[k] = 0u;
     ctl->geup_acc = 0ull;
@@ -1963,6 +2065,7 @@ static StepArgs<R> make_args(mpm_ctx *c) {
     a.work = c->d_work;
     a.nwork = c->d_nwork;
     a.cstart = c->d_cstart;
+    a.miss = c->d_tmp;
     a.acc = c->d_acc;
     a.acc2 = c->d_acc2;
     R *nod = (R *)c->d_nodal;
@@ -2005,6 +2108,17 @@ static bool use_cell_kernels(const mpm_ctx *c) {
     return c->cell_scatter && c->precision == 32 && c->g.order[0] == 1 && c->g.order[1] == 1 && c->g.order[2] == 1;
 }
 
+static int num_sms() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 148;
+    }
+    return n;
+}
+
 // which: 0 P2G, 1 G2P + MUSL, 2 G2P update
 template <typename R, int OX, int OY, int OZ>
 static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
@@ -2036,8 +2150,9 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                 } else {
                     k_p2g_cell<2><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
                 }
+                k_p2g_misses<<<2 * num_sms(), 256, 0, c->stream>>>(a);
                 timer_end(c, K_P2G);
-                c->launches++;
+                c->launches += 2;
                 return check_launch(c);
             }
         }
@@ -2064,8 +2179,9 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                 } else {
                     k_g2p_musl_cell<3><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
                 }
+                k_musl_misses<<<2 * num_sms(), 256, 0, c->stream>>>(a);
                 timer_end(c, K_G2P_MUSL);
-                c->launches++;
+                c->launches += 2;
                 return check_launch(c);
             }
         }

@@ -85,6 +85,8 @@ struct DevCtl {
     double p2g_inv[4];               // 2^-e of the P2G scales (mass, vof, momentum, force) of the last P2G
     double b0;                       // shifting coefficient of this step
     unsigned int err_timeout;        // bounded device waits that gave up
+    unsigned int n_miss_p2g;         // particles queued for the deferred P2G pass this step
+    unsigned int n_miss_musl;        // particles queued for the deferred gather/MUSL pass this step
     Scales sc_p2g;                   // this step's P2G scales (k_step_reset)
     Scales sc_musl;                  // this step's gather/MUSL scales (last CTA of k_grid1)
 };
