@@ -60,18 +60,23 @@ struct ImpState {
     mpm_nn *net = nullptr;
     double *z = nullptr, *bs = nullptr;    // preconditioned residual, scaled RHS (3 * nodec)
     double *xstar = nullptr, *ev = nullptr; // training-pair harvest: converged solution, error
+    double *gp = nullptr, *gq = nullptr;    // flexible GCR: GM directions and their images (GM * 3 * nodec)
+    double *gqq = nullptr, *gbeta = nullptr;  // |A p|^2 of each kept direction, projection coefficients
     int fallbacks = 0;                      // solves that switched from the network to Jacobi
     int nn_applications = 0;
     // CUDA graphs of 8 Krylov iterations (CG; FCG with the network; FCG with Jacobi)
-    cudaGraphExec_t g_cg = nullptr, g_fcg_nn = nullptr, g_fcg_jac = nullptr;
+    cudaGraphExec_t g_cg = nullptr, g_fcg_nn = nullptr, g_fcg_jac = nullptr, g_gcr = nullptr;
     mpm_nn *g_net = nullptr;
     bool no_graph = false;
+    bool gcr = true;      // learned preconditioner: flexible GCR first (else flexible CG only)
     bool debug = false;   // MPM_GB300_KRYLOV_TRACE set: residual history to stderr
 };
 
 namespace mpm {
 
-enum Scal { S_RR0 = 0, S_RR1, S_PAP, S_RR_INIT, S_RES, S_IDOF, S_EU, S_GD, S_ZQ, S_PR, S_RRC, S_DZZ, S_DZR, S_NSCAL };
+constexpr int GM = 8;   // directions kept by the flexible GCR solver
+
+enum Scal { S_RR0 = 0, S_RR1, S_PAP, S_RR_INIT, S_RES, S_IDOF, S_EU, S_GD, S_ZQ, S_PR, S_RRC, S_DZZ, S_DZR, S_QR, S_QQ, S_NSCAL };
 
 struct ImpArgs {
     int nnc[3];
@@ -832,6 +837,91 @@ __global__ void k_set_modulus(double *matprop, int nmat, double E) {
     if (m < nmat) matprop[3 * m] = E;
 }
 
+// ------------------------------------------------ flexible GCR(GM)
+__device__ __forceinline__ int gcr_prev(int slot, int j) { return (slot - 1 - j + 2 * GM) % GM; }
+
+// partial dots q . Q_j with the `used` previous images (j = 0 the newest)
+__global__ void k_gcr_dots(ImpArgs a, const double *Q, int slot, int used, double *part) {
+    __shared__ double sh[32];
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t N = (size_t)a.nodec, st = 3 * N;
+    const double *q = Q + (size_t)slot * st;
+    for (int j = 0; j < used; j++) {
+        const double *qj = Q + (size_t)gcr_prev(slot, j) * st;
+        double d = 0.0;
+        if (n < a.nodec)
+            for (int c = 0; c < 3; c++) d += q[c * N + n] * qj[c * N + n];
+        const double t = block_sum(d, sh);
+        if (threadIdx.x == 0) part[j * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+// beta_j = (q . Q_j) / (Q_j . Q_j), one block per j
+__global__ void k_gcr_beta(const double *part, int nb, int slot, const double *qq, double *beta) {
+    __shared__ double sh[32];
+    const int j = blockIdx.x;
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) acc += part[j * nb + i];
+    const double t = block_sum(acc, sh);
+    if (threadIdx.x == 0) {
+        const double d = qq[gcr_prev(slot, j)];
+        beta[j] = d > 0.0 ? t / d : 0.0;
+    }
+}
+
+// p -= sum beta_j P_j, q -= sum beta_j Q_j; partial q.r and q.q
+__global__ void k_gcr_axpy(ImpArgs a, double *P, double *Q, int slot, int used, const double *beta, const double *r,
+                           double *part) {
+    __shared__ double sh[32];
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t N = (size_t)a.nodec, st = 3 * N;
+    double dqr = 0.0, dqq = 0.0;
+    if (n < a.nodec) {
+        double *p = P + (size_t)slot * st, *q = Q + (size_t)slot * st;
+        for (int c = 0; c < 3; c++) {
+            const size_t i = c * N + n;
+            double pv = p[i], qv = q[i];
+            for (int j = 0; j < used; j++) {
+                const size_t o = (size_t)gcr_prev(slot, j) * st + i;
+                pv -= beta[j] * P[o];
+                qv -= beta[j] * Q[o];
+            }
+            p[i] = pv;
+            q[i] = qv;
+            dqr += qv * r[i];
+            dqq += qv * qv;
+        }
+    }
+    const double t1 = block_sum(dqr, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t1;
+    const double t2 = block_sum(dqq, sh);
+    if (threadIdx.x == 0) part[gridDim.x + blockIdx.x] = t2;
+}
+
+// alpha = q.r / q.q; x += alpha p; r -= alpha q; partial r.r; keeps q.q of the slot
+__global__ void k_gcr_update(ImpArgs a, const double *scal, double *x, double *r, const double *P, const double *Q,
+                             int slot, double *qq, double *part) {
+    __shared__ double sh[32];
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t N = (size_t)a.nodec, st = 3 * N;
+    const double dqq = scal[S_QQ];
+    const double alpha = dqq > 0.0 ? scal[S_QR] / dqq : 0.0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) qq[slot] = dqq;
+    double d = 0.0;
+    if (n < a.nodec) {
+        const double *p = P + (size_t)slot * st, *q = Q + (size_t)slot * st;
+        for (int c = 0; c < 3; c++) {
+            const size_t i = c * N + n;
+            x[i] += alpha * p[i];
+            const double v = r[i] - alpha * q[i];
+            r[i] = v;
+            d += v * v;
+        }
+    }
+    const double t = block_sum(d, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
 __global__ void k_imp_reset_next(DevCtl *ctl, int parity) {
     for (int k = 0; k < B_NB; k++) ctl->nxt[parity ^ 1][k] = 0u;
 }
@@ -855,11 +945,11 @@ void implicit_free(mpm_ctx *c) {
     if (!s) return;
     double *bufs[] = {s->A, s->adiag, s->b, s->x, s->r, s->p, s->Ap, s->xs, s->ndispl, s->nvel, s->naccel,
                       s->naccel_k, s->nmass, s->nvof, s->nei, s->stress_k, s->geup, s->part, s->scal,
-                      s->z, s->bs, s->xstar, s->ev};
+                      s->z, s->bs, s->xstar, s->ev, s->gp, s->gq, s->gqq, s->gbeta};
     for (double *b : bufs)
         if (b) cudaFree(b);
     if (s->h_scal) cudaFreeHost(s->h_scal);
-    for (cudaGraphExec_t g : {s->g_cg, s->g_fcg_nn, s->g_fcg_jac})
+    for (cudaGraphExec_t g : {s->g_cg, s->g_fcg_nn, s->g_fcg_jac, s->g_gcr})
         if (g) cudaGraphExecDestroy(g);
     delete s;
     c->imp = nullptr;
@@ -893,6 +983,7 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
     ImpState *s = new ImpState();
     c->imp = s;
     s->debug = getenv("MPM_GB300_KRYLOV_TRACE") != nullptr;
+    s->gcr = getenv("MPM_GB300_FCG_ONLY") == nullptr;
     s->nr_flag = nr_flag ? 1 : 0;
     // GeneralizedAlphaParaSet + NewmarkBetaParaSet (nonlinear_time_integration.cpp:10-56), second order
     double t = 1.0 + spec_rad;
@@ -913,12 +1004,16 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
     double **vec3[] = {&s->adiag, &s->b,    &s->x,       &s->r, &s->p,  &s->Ap,    &s->xs, &s->ndispl,
                        &s->nvel,  &s->naccel, &s->naccel_k, &s->z, &s->bs, &s->xstar, &s->ev};
     for (double **v : vec3) CKI(cudaMalloc((void **)v, sizeof(double) * 3 * N));
+    CKI(cudaMalloc((void **)&s->gp, sizeof(double) * GM * 3 * N));
+    CKI(cudaMalloc((void **)&s->gq, sizeof(double) * GM * 3 * N));
+    CKI(cudaMalloc((void **)&s->gqq, sizeof(double) * GM));
+    CKI(cudaMalloc((void **)&s->gbeta, sizeof(double) * GM));
     CKI(cudaMalloc((void **)&s->nmass, sizeof(double) * N));
     CKI(cudaMalloc((void **)&s->nvof, sizeof(double) * N));
     CKI(cudaMalloc((void **)&s->nei, sizeof(double) * N));
     s->nblk = (int)((N + 255) / 256);
     int pblk = (int)((c->num + 127) / 128);
-    int nparts = 2 * (s->nblk > pblk ? s->nblk : pblk) + 2 * ((3 * (int)N + 255) / 256) + 64;
+    int nparts = 2 * (s->nblk > pblk ? s->nblk : pblk) + 2 * ((3 * (int)N + 255) / 256) + (GM + 2) * s->nblk + 64;
     CKI(cudaMalloc((void **)&s->part, sizeof(double) * (size_t)nparts));
     CKI(cudaMalloc((void **)&s->scal, sizeof(double) * S_NSCAL));
     CKI(cudaMallocHost((void **)&s->h_scal, sizeof(double) * S_NSCAL));
@@ -1112,6 +1207,95 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
     if (s->g_fcg_nn && s->g_net != s->net) {
         cudaGraphExecDestroy(s->g_fcg_nn);
         s->g_fcg_nn = nullptr;
+    }
+    if (s->g_gcr && s->g_net != s->net) {
+        cudaGraphExecDestroy(s->g_gcr);
+        s->g_gcr = nullptr;
+    }
+    // Phase 1: flexible GCR(GM) with the network as right preconditioner.  It
+    // minimises the residual over the kept directions, so it needs no
+    // symmetry of the (learned, non-symmetric) preconditioner.  It runs while
+    // every window of `check` iterations at least halves the residual norm.
+    if (use_nn && s->gcr) {
+        const size_t st3 = 3 * N;
+        int used = 0, slot = 0;
+        double rr_win = rr0;
+        auto gcr_iteration = [&](int u, int sl) -> mpm_status {
+            timer_begin(c, K_PRECOND);
+            mpm_status st = mpm_nn_apply_precond(s->net, c->stream, s->r, s->scal + S_RRC, s->adiag, a.bcflag, a.mtol,
+                                                 s->gp + (size_t)sl * st3);
+            timer_end(c, K_PRECOND);
+            if (st != MPM_OK) return st;
+            timer_begin(c, K_MATVEC);
+            k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->gp + (size_t)sl * st3, s->gq + (size_t)sl * st3,
+                                                    nullptr);
+            timer_end(c, K_MATVEC);
+            timer_begin(c, K_KRYLOV);
+            if (u > 0) {
+                k_gcr_dots<<<nb, 256, 0, c->stream>>>(a, s->gq, sl, u, s->part);
+                k_gcr_beta<<<u, 256, 0, c->stream>>>(s->part, nb, sl, s->gqq, s->gbeta);
+            }
+            k_gcr_axpy<<<nb, 256, 0, c->stream>>>(a, s->gp, s->gq, sl, u, s->gbeta, s->r, s->part);
+            k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_QR);
+            k_finish<<<1, 256, 0, c->stream>>>(s->part + nb, nb, s->scal, S_QQ);
+            k_gcr_update<<<nb, 256, 0, c->stream>>>(a, s->scal, s->xs, s->r, s->gp, s->gq, sl, s->gqq, s->part);
+            k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
+            timer_end(c, K_KRYLOV);
+            c->launches += 9 + 7 + (u > 0 ? 2 : 0);
+            return MPM_OK;
+        };
+        while (!done && use_nn && it < kmax) {
+            if (graphs_on(c) && used == GM && slot == 0 && it % check == 0 && it + check <= kmax) {
+                const int64_t l0 = c->launches;
+                if (!s->g_gcr && capture_iters(c, &s->g_gcr, [&] {
+                        for (int k = 0; k < check; k++) gcr_iteration(GM, k % GM);
+                    }) != MPM_OK)
+                    s->no_graph = true;
+                if (!s->g_gcr) continue;
+                s->g_net = s->net;
+                CKI(cudaGraphLaunch(s->g_gcr, c->stream));
+                if (c->launches == l0) c->launches += 18 * check;
+                s->nn_applications += check;
+                it += check;
+            } else {
+                mpm_status st = gcr_iteration(used, slot);
+                if (st != MPM_OK) return st;
+                s->nn_applications++;
+                used = used < GM ? used + 1 : GM;
+                slot = (slot + 1) % GM;
+                it++;
+            }
+            if (it % check == 0 || it == kmax) {
+                CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, c->stream));
+                CKI(cudaStreamSynchronize(c->stream));
+                double rr = s->h_scal[S_RRC];
+                if (rr != rr) {
+                    *iters = it;
+                    return MPM_ERR_NONFINITE;
+                }
+                if (s->debug) fprintf(stderr, "mpm_gb300 gcr: it %d |r|/|r0| %.3e\n", it, sqrt(rr / rr0));
+                if (rr < eps * rr0) {
+                    k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->xs, s->z, nullptr);
+                    k_true_residual<<<nb, 256, 0, c->stream>>>(a, s->bs, s->z, s->r, s->part);
+                    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
+                    c->launches += 3;
+                    CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost,
+                                        c->stream));
+                    CKI(cudaStreamSynchronize(c->stream));
+                    rr = s->h_scal[S_RRC];
+                    if (rr < eps * rr0) done = true;
+                    used = 0;   // the residual was replaced: the kept directions no longer apply
+                    slot = 0;
+                }
+                if (!done && !(rr < 0.25 * rr_win)) {
+                    use_nn = false;   // less than a halving of |r| per window: Jacobi does better
+                    s->fallbacks++;
+                }
+                rr_win = rr;
+                s->last_rel = sqrt(rr / rr0);
+            }
+        }
+        restart = 1;
     }
     while (!done && it < kmax) {
         cudaGraphExec_t *gx = use_nn ? &s->g_fcg_nn : &s->g_fcg_jac;
