@@ -854,7 +854,7 @@ struct mpm_nn {
     bool weights_dirty = true;
     int linear = 1;     // 1: no activations and no biases (a linear operator of the input)
     int additive = 1;   // 1: preconditioner r + net(r), the network trained on (error - residual)
-    int symmetric = 1;  // 1 (linear, additive): apply r + (N + N^T) r / 2
+    int symmetric = 0;  // 1 (linear, additive): apply r + (N + N^T) r / 2
     bf16 *gx0 = nullptr;   // adjoint result at the input [v0][16]
     int64_t adam_step = 0;
     bf16 *data_r = nullptr, *data_e = nullptr;

@@ -366,7 +366,7 @@ _fp32 = C.POINTER(C.c_float)
 class PrecondNet:
     """The learned preconditioner network (mpm_nn_*) on a grid of `nodes` control points."""
 
-    def __init__(self, nodes, max_batch=1, max_pairs=0, seed=None, linear=True, additive=True, symmetric=True):
+    def __init__(self, nodes, max_batch=1, max_pairs=0, seed=None, linear=True, additive=True, symmetric=False):
         self.lib = load()
         self.nodes = tuple(int(n) for n in nodes)
         n3 = (C.c_int * 3)(*self.nodes)

@@ -252,10 +252,11 @@ mpm_status mpm_nn_set_linear(mpm_nn *net, int linear);
  * scaled system plus a learned correction) and training fits net(r) to
  * e - r; 0: z = net(r), trained on e. */
 mpm_status mpm_nn_set_additive(mpm_nn *net, int additive);
-/* symmetric = 1 (default; linear additive networks): the solver applies the
+/* symmetric = 1 (linear additive networks): the solver applies the
  * symmetric part z = r + (N r + N^T r) / 2, N^T by the network's transposed
  * (data-gradient) convolutions, so that conjugate gradients see a symmetric
- * preconditioner; 0: z = r + N r. */
+ * preconditioner; 0 (default): z = r + N r, for the residual-minimising
+ * flexible GCR phase of the solve. */
 mpm_status mpm_nn_set_symmetric(mpm_nn *net, int symmetric);
 mpm_status mpm_nn_init_params(mpm_nn *net, uint64_t seed);
 mpm_status mpm_nn_set_params(mpm_nn *net, const float *params);

@@ -77,7 +77,7 @@ def test_symmetric_preconditioner_is_symmetric():
     _, d, _ = gpu.system()
     act = np.abs(d) > 0
     rng = np.random.default_rng(4)
-    net = capi.PrecondNet(s.xynodec, seed=21)
+    net = capi.PrecondNet(s.xynodec, seed=21, symmetric=True)
     gpu.set_precond(net)
     bcmask = np.ones(3 * s.nodec, dtype=bool)
     for comp, nodes, _v in s.bcs:
