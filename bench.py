@@ -266,8 +266,9 @@ def run_implicit(args, torch, stream):
     gpu.close()
     net.close()
     out["learned"] = {"value": nn_ms, "unit": "ms/step",
-                      "solver": "Newton + flexible CG, learned right preconditioner (BF16 tcgen05 conv "
-                                "encoder-decoder), Jacobi fallback, true FP64 residual <= 1e-8",
+                      "solver": "Newton + flexible GCR(8) with the learned right preconditioner (linear BF16 "
+                                "tcgen05 conv encoder-decoder, z = r + N r) while each 8-iteration window halves "
+                                "the residual, then CG with Jacobi; true FP64 residual <= 1e-8",
                       "krylov_iters_per_step": nn["krylov_iters"] / args.implicit_steps,
                       "newton_iters_per_step": nn["newton_iters"] / args.implicit_steps,
                       "fallbacks": nn["precond_fallbacks"], "network_applications": nn["nn_applications"],
