@@ -1139,6 +1139,35 @@ static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
     return check_launch(c);
 }
 
+// One flexible GCR iteration on the scaled system: z = M(r) into direction
+// slot `sl`, q = A z, orthogonalised against the `u` previous images, then
+// x += alpha z, r -= alpha q with alpha = q.r / q.q.
+static mpm_status gcr_iter(mpm_ctx *c, const ImpArgs &a, int nb, int u, int sl) {
+    ImpState *s = c->imp;
+    const size_t st3 = 3 * (size_t)c->g.nodec;
+    timer_begin(c, K_PRECOND);
+    mpm_status st = mpm_nn_apply_precond(s->net, c->stream, s->r, s->scal + S_RRC, s->adiag, a.bcflag, a.mtol,
+                                         s->gp + (size_t)sl * st3);
+    timer_end(c, K_PRECOND);
+    if (st != MPM_OK) return st;
+    timer_begin(c, K_MATVEC);
+    k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->gp + (size_t)sl * st3, s->gq + (size_t)sl * st3, nullptr);
+    timer_end(c, K_MATVEC);
+    timer_begin(c, K_KRYLOV);
+    if (u > 0) {
+        k_gcr_dots<<<nb, 256, 0, c->stream>>>(a, s->gq, sl, u, s->part);
+        k_gcr_beta<<<u, 256, 0, c->stream>>>(s->part, nb, sl, s->gqq, s->gbeta);
+    }
+    k_gcr_axpy<<<nb, 256, 0, c->stream>>>(a, s->gp, s->gq, sl, u, s->gbeta, s->r, s->part);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_QR);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part + nb, nb, s->scal, S_QQ);
+    k_gcr_update<<<nb, 256, 0, c->stream>>>(a, s->scal, s->xs, s->r, s->gp, s->gq, sl, s->gqq, s->part);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
+    timer_end(c, K_KRYLOV);
+    c->launches += 9 + 7 + (u > 0 ? 2 : 0);
+    return MPM_OK;
+}
+
 // One solve of the assembled, scaled system by flexible CG with the learned
 // preconditioner z = net(r) (Notay's FCG(1): p = z - (z.q'/p'.q') p',
 // alpha = p.r / p.q).  The residual is checked every 8 iterations; when two
@@ -1220,30 +1249,7 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
         const size_t st3 = 3 * N;
         int used = 0, slot = 0;
         double rr_win = rr0;
-        auto gcr_iteration = [&](int u, int sl) -> mpm_status {
-            timer_begin(c, K_PRECOND);
-            mpm_status st = mpm_nn_apply_precond(s->net, c->stream, s->r, s->scal + S_RRC, s->adiag, a.bcflag, a.mtol,
-                                                 s->gp + (size_t)sl * st3);
-            timer_end(c, K_PRECOND);
-            if (st != MPM_OK) return st;
-            timer_begin(c, K_MATVEC);
-            k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->gp + (size_t)sl * st3, s->gq + (size_t)sl * st3,
-                                                    nullptr);
-            timer_end(c, K_MATVEC);
-            timer_begin(c, K_KRYLOV);
-            if (u > 0) {
-                k_gcr_dots<<<nb, 256, 0, c->stream>>>(a, s->gq, sl, u, s->part);
-                k_gcr_beta<<<u, 256, 0, c->stream>>>(s->part, nb, sl, s->gqq, s->gbeta);
-            }
-            k_gcr_axpy<<<nb, 256, 0, c->stream>>>(a, s->gp, s->gq, sl, u, s->gbeta, s->r, s->part);
-            k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_QR);
-            k_finish<<<1, 256, 0, c->stream>>>(s->part + nb, nb, s->scal, S_QQ);
-            k_gcr_update<<<nb, 256, 0, c->stream>>>(a, s->scal, s->xs, s->r, s->gp, s->gq, sl, s->gqq, s->part);
-            k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
-            timer_end(c, K_KRYLOV);
-            c->launches += 9 + 7 + (u > 0 ? 2 : 0);
-            return MPM_OK;
-        };
+        auto gcr_iteration = [&](int u, int sl) -> mpm_status { return gcr_iter(c, a, nb, u, sl); };
         while (!done && use_nn && it < kmax) {
             if (graphs_on(c) && used == GM && slot == 0 && it % check == 0 && it + check <= kmax) {
                 const int64_t l0 = c->launches;
@@ -1638,6 +1644,30 @@ static mpm_status cg_scaled(mpm_ctx *c, double eps, int kmax, mpm_nn *net, int s
     return check_launch(c);
 }
 
+// Flexible GCR with the context's preconditioner from x = 0 for the RHS s->bs,
+// storing (r_k, xstar - x_k) before each of its first `npairs` iterations.
+static mpm_status gcr_record(mpm_ctx *c, mpm_nn *rec, int npairs) {
+    ImpState *s = c->imp;
+    ImpArgs a = imp_args(c);
+    const int nb = nb_nodes(c);
+    const size_t N = (size_t)c->g.nodec;
+    CKI(cudaMemsetAsync(s->xs, 0, sizeof(double) * 3 * N, c->stream));
+    CKI(cudaMemcpyAsync(s->r, s->bs, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, c->stream));
+    k_dot3<<<nb, 256, 0, c->stream>>>(a, s->r, s->r, s->part);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
+    int used = 0, slot = 0;
+    for (int k = 0; k < npairs; k++) {
+        k_sub3<<<(3 * c->g.nodec + 255) / 256, 256, 0, c->stream>>>(s->xstar, s->xs, s->ev, 3 * c->g.nodec);
+        mpm_status st = mpm_nn_append_pair(rec, c->stream, s->r, s->scal + S_RRC, s->ev);
+        if (st != MPM_OK) return st;
+        st = gcr_iter(c, a, nb, used, slot);
+        if (st != MPM_OK) return st;
+        used = used < GM ? used + 1 : GM;
+        slot = (slot + 1) % GM;
+    }
+    return check_launch(c);
+}
+
 mpm_status mpm_gpu_implicit_harvest(mpm_ctx *c, mpm_nn *net, int nsystems, int loads_per_system, int pairs_per_load,
                                     double e_min, double e_max, uint64_t seed, double eps, int kmax) {
     if (!c || !c->imp || !net || nsystems < 1 || loads_per_system < 1 || pairs_per_load < 1 || !(e_min > 0.0) ||
@@ -1668,6 +1698,7 @@ mpm_status mpm_gpu_implicit_harvest(mpm_ctx *c, mpm_nn *net, int nsystems, int l
         if (st == MPM_OK) {
             k_phi<<<nb, 256, 0, c->stream>>>(a, s->nmass, s->adiag, s->ev);
             st = mpm_nn_begin_system(net, c->stream, s->ev);
+            if (st == MPM_OK && s->net) st = mpm_nn_set_feature(s->net, c->stream, s->ev);
         }
         for (int ld = 0; ld < loads_per_system && st == MPM_OK; ld++) {
             const uint64_t key = seed * 1000003ull + (uint64_t)sys * 1009ull + (uint64_t)ld;
@@ -1683,9 +1714,15 @@ mpm_status mpm_gpu_implicit_harvest(mpm_ctx *c, mpm_nn *net, int nsystems, int l
             st = cg_scaled(c, eps, kmax, nullptr, 1, 0, &K);
             if (st != MPM_OK) break;
             CKI(cudaMemcpyAsync(s->xstar, s->xs, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, c->stream));
-            const int stride = K / pairs_per_load > 1 ? K / pairs_per_load : 1;
-            int K2 = 0;
-            st = cg_scaled(c, eps, K, net, stride, pairs_per_load, &K2);
+            if (s->net) {
+                // pairs along the learned solve itself: the residuals the
+                // preconditioner meets once it has removed what it can
+                st = gcr_record(c, net, pairs_per_load);
+            } else {
+                const int stride = K / pairs_per_load > 1 ? K / pairs_per_load : 1;
+                int K2 = 0;
+                st = cg_scaled(c, eps, K, net, stride, pairs_per_load, &K2);
+            }
         }
     }
     cudaMemcpy(c->d_matprop, saved.data(), sizeof(double) * saved.size(), cudaMemcpyHostToDevice);

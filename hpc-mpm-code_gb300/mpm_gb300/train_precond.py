@@ -1,10 +1,11 @@
 """Train the learned preconditioner for the implicit cantilever on the GPU.
 
-Training pairs come from the implicit solver's own Jacobi-PCG solves on the
+Training pairs come from the implicit solver's own solves on the
 1,728,000-particle cantilever (64^3-cell grid, 65^3 control points): for
-moduli E drawn log-uniformly from [1e6, 1e8] and seeded random loads, each
-system is solved twice and (residual, error) pairs are stored along the
-second solve (mpm_gpu_implicit_harvest).  The network is then trained with
+moduli E drawn log-uniformly from [1e6, 1e8] and the system's own plus
+seeded random loads, each system is solved twice and (residual, error)
+pairs are stored along the second solve (mpm_gpu_implicit_harvest); a
+second round stores pairs along the learned solver's own iterations.  The network is then trained with
 Adam by the library's own tensor-core forward and backward kernels
 (mpm_nn_train).  The result is written as raw FP32 parameters plus a JSON
 record of the run; bench.py and the tests load them through
@@ -37,12 +38,16 @@ def load_weights(path=WEIGHTS):
 
 
 def train(pairs=20000, loads_per_system=8, pairs_per_load=25, epochs=8, batch=8, lr=1.0e-3, seed=0,
-          harvest_eps=1.0e-20, scene=None, out=WEIGHTS, log=print):
+          harvest_eps=1.0e-20, learned_pairs=8000, learned_pairs_per_load=16, epochs2=4, scene=None, out=WEIGHTS,
+          log=print):
+    """Two rounds: pairs along Jacobi-PCG solves, training; then (if
+    learned_pairs > 0) pairs along the learned solver's own iterations with
+    the round-one network, and training on all pairs."""
     s = scene if scene is not None else scenes.cantilever(iprop=1)
     gpu = capi.GpuImplicitSolid(s, nr_flag=True)
     per_system = loads_per_system * pairs_per_load
     nsystems = max(1, math.ceil(pairs / per_system))
-    net = capi.PrecondNet(s.xynodec, max_batch=batch, max_pairs=pairs, seed=seed)
+    net = capi.PrecondNet(s.xynodec, max_batch=batch, max_pairs=pairs + learned_pairs, seed=seed)
     t0 = time.perf_counter()
     gpu.harvest(net, nsystems, loads_per_system, pairs_per_load, 1.0e6, 1.0e8, seed=seed, eps=harvest_eps)
     t1 = time.perf_counter()
@@ -51,12 +56,26 @@ def train(pairs=20000, loads_per_system=8, pairs_per_load=25, epochs=8, batch=8,
     losses = net.train(epochs, batch, lr=lr, seed=seed)
     t2 = time.perf_counter()
     log(f"trained {epochs} epochs in {t2 - t1:.1f} s, loss per epoch {[round(float(x), 4) for x in losses]}")
+    losses2, nsys2 = [], 0
+    if learned_pairs > 0:
+        nsys2 = max(1, math.ceil(learned_pairs / (loads_per_system * learned_pairs_per_load)))
+        gpu.set_precond(net)
+        gpu.harvest(net, nsys2, loads_per_system, learned_pairs_per_load, 1.0e6, 1.0e8, seed=seed + 1,
+                    eps=harvest_eps)
+        gpu.set_precond(None)
+        losses2 = net.train(epochs2, batch, lr=lr * 0.5, seed=seed + 1)
+        log(f"round 2: {net.num_pairs()} pairs, {epochs2} epochs, loss per epoch "
+            f"{[round(float(x), 4) for x in losses2]}")
+    t3 = time.perf_counter()
     params = net.params()
+    n = net.num_pairs()
     rec = {"scene": s.name, "particles": int(s.num), "nodes": list(s.xynodec), "pairs": int(n),
            "systems": nsystems, "loads_per_system": loads_per_system, "pairs_per_load": pairs_per_load,
-           "moduli": [1.0e6, 1.0e8], "epochs": epochs, "batch": batch, "lr": lr, "seed": seed,
+           "learned_systems": nsys2, "learned_pairs_per_load": learned_pairs_per_load,
+           "moduli": [1.0e6, 1.0e8], "epochs": epochs, "epochs2": epochs2, "batch": batch, "lr": lr, "seed": seed,
            "harvest_eps": harvest_eps, "loss_per_epoch": [float(x) for x in losses],
-           "harvest_s": t1 - t0, "train_s": t2 - t1}
+           "loss_per_epoch2": [float(x) for x in losses2],
+           "harvest_s": t1 - t0, "train_s": t3 - t1}
     if out:
         os.makedirs(os.path.dirname(out), exist_ok=True)
         params.astype(np.float32).tofile(out)

@@ -277,9 +277,12 @@ mpm_status mpm_gpu_implicit_apply_precond(mpm_ctx *ctx, const double *r, double 
 /* Training pairs from the solver's own solves: for each of nsystems moduli
  * E drawn log-uniformly from [e_min, e_max] the system of the current state
  * is assembled; for its own right-hand side and loads_per_system - 1 seeded
- * random ones it is solved twice by Jacobi-PCG to ||r||^2 < eps ||r0||^2, the second
- * time storing pairs_per_load (residual, error) pairs spread over the
- * iterations.  The materials' moduli are restored afterwards. */
+ * random ones it is solved twice by Jacobi-PCG to ||r||^2 < eps ||r0||^2, the
+ * second time storing pairs_per_load (residual, error) pairs spread over the
+ * iterations.  When ctx already has a preconditioner (set_precond), the pairs
+ * come instead from the first pairs_per_load iterations of the learned
+ * flexible GCR solve: the residuals that preconditioner leaves behind.
+ * The materials' moduli are restored afterwards. */
 mpm_status mpm_gpu_implicit_harvest(mpm_ctx *ctx, mpm_nn *net, int nsystems, int loads_per_system, int pairs_per_load,
                                     double e_min, double e_max, uint64_t seed, double eps, int kmax);
 
