@@ -41,6 +41,8 @@ struct StepArgs {
     const int *nwork;
     const int *cstart;          // nbricks * (BRC + 1)
     int *miss;                  // particles that left their sorted cell, processed by a deferred pass
+    const int *blist;           // bricks holding particles (brick order) and their count
+    const int *nblist;
     int nbrick[3];
     unsigned long long *acc;    // NACC * nodec
     unsigned long long *acc2;   // 3 * nodec
@@ -345,105 +347,109 @@ __device__ __noinline__ void p2g_miss(const StepArgs<float> &a, const Scales &S,
     p2g_particle(a, S, cx, cy, cz, 1, x0, x1, x2, m, vol, vel, sg, fxg, fyg, fzg, dummy, misses, oobs);
 }
 
-template <int MINB>
+template <int MINB, bool LIST>
 __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_mom(StepArgs<float> a) {
     __shared__ float corner[NACC * 8][BRC];       // 32 KB
     __shared__ Scales S;
     __shared__ int sh_red[32];
-    const int b = blockIdx.x;
-    const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
-    const int *cs = a.cstart + (size_t)b * (BRC + 1);
-    if (cs[0] == cs[BRC]) return;   // empty brick (uniform across the CTA)
-    int ox, oy, oz;
-    brick_origin(b, a.nbrick, ox, oy, oz);
-    const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
-    const int p0 = cs[lc], p1 = cs[lc + 1];
     load_scales(a, S);
-    const float fxg = a.grav[0] * a.facl, fyg = a.grav[1] * a.facl, fzg = a.grav[2] * a.facl;
-    const Particles<float> &P = a.P;
-    float M[5][8], Fm[9][4];
-#pragma unroll
-    for (int f = 0; f < 5; f++)
-#pragma unroll
-        for (int k = 0; k < 8; k++) M[f][k] = 0.0f;
-#pragma unroll
-    for (int f = 0; f < 9; f++)
-#pragma unroll
-        for (int k = 0; k < 4; k++) Fm[f][k] = 0.0f;
-    int misses = 0, oobs = 0;
-    for (int p = p0 + h; p < p1; p += 2) {
-        const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
-        const float m = ld(P.m + p), vol = ld(P.vol + p);
-        const float vel[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
-        const float sg[6] = {ld(P.s[0] + p), ld(P.s[1] + p), ld(P.s[2] + p),
-                             ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
-        bool oob = false;
-        const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
-        if (px != cx || py != cy || pz != cz) {
-            // a particle that left its sorted cell scatters in the deferred pass
-            misses++;
-            a.miss[atomicAdd(&a.ctl->n_miss_p2g, 1u)] = p;
-            continue;
-        }
-        oobs += oob;
-        const float u = cell_offset_u(x0, a.g, 0, px), v = cell_offset_u(x1, a.g, 1, py),
-                    w = cell_offset_u(x2, a.g, 2, pz);
-        const float uv = u * v, uw = u * w, vw = v * w;
-        const float mono[8] = {1.0f, u, v, w, uv, uw, vw, uv * w};
-        const float q[5] = {m, vol, m * vel[0], m * vel[1], m * vel[2]};
+    const int nbl = LIST ? *a.nblist : 1;
+    for (int li = LIST ? (int)blockIdx.x : 0; li < nbl; li += LIST ? (int)gridDim.x : 1) {
+        const int b = LIST ? a.blist[li] : (int)blockIdx.x;
+        const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
+        const int *cs = a.cstart + (size_t)b * (BRC + 1);
+        if (cs[0] == cs[BRC]) continue;   // empty brick (uniform across the CTA)
+        int ox, oy, oz;
+        brick_origin(b, a.nbrick, ox, oy, oz);
+        const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
+        const int p0 = cs[lc], p1 = cs[lc + 1];
+        const float fxg = a.grav[0] * a.facl, fyg = a.grav[1] * a.facl, fzg = a.grav[2] * a.facl;
+        const Particles<float> &P = a.P;
+        float M[5][8], Fm[9][4];
 #pragma unroll
         for (int f = 0; f < 5; f++)
 #pragma unroll
-            for (int k = 0; k < 8; k++) M[f][k] += q[f] * mono[k];
-        // vol * sigma_ab, Voigt xx yy zz yz xz xy
-        const float vs[9] = {vol * sg[0], vol * sg[5], vol * sg[4], vol * sg[5], vol * sg[1],
-                             vol * sg[3], vol * sg[4], vol * sg[3], vol * sg[2]};
-        const float mb[3][4] = {{1.0f, v, w, vw}, {1.0f, u, w, uw}, {1.0f, u, v, uv}};
+            for (int k = 0; k < 8; k++) M[f][k] = 0.0f;
 #pragma unroll
-        for (int ab = 0; ab < 9; ab++)
+        for (int f = 0; f < 9; f++)
 #pragma unroll
-            for (int k = 0; k < 4; k++) Fm[ab][k] += vs[ab] * mb[ab % 3][k];
-    }
-    const unsigned pair = 3u << ((threadIdx.x & 31) & ~1u);
-#pragma unroll
-    for (int f = 0; f < 5; f++)
-#pragma unroll
-        for (int k = 0; k < 8; k++) M[f][k] += __shfl_xor_sync(pair, M[f][k], 1);
-#pragma unroll
-    for (int f = 0; f < 9; f++)
-#pragma unroll
-        for (int k = 0; k < 4; k++) Fm[f][k] += __shfl_xor_sync(pair, Fm[f][k], 1);
-    // corners (i, j, h) of this thread's z-layer
-    float acc[NACC][4];
-    const float sz = h ? 1.0f : -1.0f;
-    const float gv[3] = {fxg, fyg, fzg};
-#pragma unroll
-    for (int j = 0; j < 2; j++)
-#pragma unroll
-        for (int i = 0; i < 2; i++) {
-            const int c = i + 2 * j;
-            const float sx = i ? 1.0f : -1.0f, sy = j ? 1.0f : -1.0f;
+            for (int k = 0; k < 4; k++) Fm[f][k] = 0.0f;
+        int misses = 0, oobs = 0;
+        for (int p = p0 + h; p < p1; p += 2) {
+            const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+            const float m = ld(P.m + p), vol = ld(P.vol + p);
+            const float vel[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
+            const float sg[6] = {ld(P.s[0] + p), ld(P.s[1] + p), ld(P.s[2] + p),
+                                 ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
+            bool oob = false;
+            const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
+            if (px != cx || py != cy || pz != cz) {
+                // a particle that left its sorted cell scatters in the deferred pass
+                misses++;
+                a.miss[atomicAdd(&a.ctl->n_miss_p2g, 1u)] = p;
+                continue;
+            }
+            oobs += oob;
+            const float u = cell_offset_u(x0, a.g, 0, px), v = cell_offset_u(x1, a.g, 1, py),
+                        w = cell_offset_u(x2, a.g, 2, pz);
+            const float uv = u * v, uw = u * w, vw = v * w;
+            const float mono[8] = {1.0f, u, v, w, uv, uw, vw, uv * w};
+            const float q[5] = {m, vol, m * vel[0], m * vel[1], m * vel[2]};
 #pragma unroll
             for (int f = 0; f < 5; f++)
-                acc[f][c] = M[f][0] * 0.125f + (sx * M[f][1] + sy * M[f][2] + sz * M[f][3]) * 0.25f +
-                            (sx * sy * M[f][4] + sx * sz * M[f][5] + sy * sz * M[f][6]) * 0.5f +
-                            sx * sy * sz * M[f][7];
-            // the signs of the two bilinear axes of each derivative direction b
-            const float sb[3] = {sx, sy, sz};
-            const float sc[3] = {sy, sx, sx}, sd[3] = {sz, sz, sy};
 #pragma unroll
-            for (int ax = 0; ax < 3; ax++) {
-                float fi = 0.0f;
+                for (int k = 0; k < 8; k++) M[f][k] += q[f] * mono[k];
+            // vol * sigma_ab, Voigt xx yy zz yz xz xy
+            const float vs[9] = {vol * sg[0], vol * sg[5], vol * sg[4], vol * sg[5], vol * sg[1],
+                                 vol * sg[3], vol * sg[4], vol * sg[3], vol * sg[2]};
+            const float mb[3][4] = {{1.0f, v, w, vw}, {1.0f, u, w, uw}, {1.0f, u, v, uv}};
 #pragma unroll
-                for (int bb = 0; bb < 3; bb++) {
-                    const float *F = Fm[3 * ax + bb];
-                    fi += a.g.inv_dx[bb] * sb[bb] *
-                          (F[0] * 0.25f + (sc[bb] * F[1] + sd[bb] * F[2]) * 0.5f + sc[bb] * sd[bb] * F[3]);
-                }
-                acc[5 + ax][c] = -fi + acc[0][c] * gv[ax];
-            }
+            for (int ab = 0; ab < 9; ab++)
+#pragma unroll
+                for (int k = 0; k < 4; k++) Fm[ab][k] += vs[ab] * mb[ab % 3][k];
         }
-    p2g_node_pass(a, S, corner, sh_red, lc, h, ox, oy, oz, acc, misses, oobs);
+        const unsigned pair = 3u << ((threadIdx.x & 31) & ~1u);
+#pragma unroll
+        for (int f = 0; f < 5; f++)
+#pragma unroll
+            for (int k = 0; k < 8; k++) M[f][k] += __shfl_xor_sync(pair, M[f][k], 1);
+#pragma unroll
+        for (int f = 0; f < 9; f++)
+#pragma unroll
+            for (int k = 0; k < 4; k++) Fm[f][k] += __shfl_xor_sync(pair, Fm[f][k], 1);
+        // corners (i, j, h) of this thread's z-layer
+        float acc[NACC][4];
+        const float sz = h ? 1.0f : -1.0f;
+        const float gv[3] = {fxg, fyg, fzg};
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const int c = i + 2 * j;
+                const float sx = i ? 1.0f : -1.0f, sy = j ? 1.0f : -1.0f;
+#pragma unroll
+                for (int f = 0; f < 5; f++)
+                    acc[f][c] = M[f][0] * 0.125f + (sx * M[f][1] + sy * M[f][2] + sz * M[f][3]) * 0.25f +
+                                (sx * sy * M[f][4] + sx * sz * M[f][5] + sy * sz * M[f][6]) * 0.5f +
+                                sx * sy * sz * M[f][7];
+                // the signs of the two bilinear axes of each derivative direction b
+                const float sb[3] = {sx, sy, sz};
+                const float sc[3] = {sy, sx, sx}, sd[3] = {sz, sz, sy};
+#pragma unroll
+                for (int ax = 0; ax < 3; ax++) {
+                    float fi = 0.0f;
+#pragma unroll
+                    for (int bb = 0; bb < 3; bb++) {
+                        const float *F = Fm[3 * ax + bb];
+                        fi += a.g.inv_dx[bb] * sb[bb] *
+                              (F[0] * 0.25f + (sc[bb] * F[1] + sd[bb] * F[2]) * 0.5f + sc[bb] * sd[bb] * F[3]);
+                    }
+                    acc[5 + ax][c] = -fi + acc[0][c] * gv[ax];
+                }
+            }
+        p2g_node_pass(a, S, corner, sh_red, lc, h, ox, oy, oz, acc, misses, oobs);
+        __syncthreads();   // shared memory is reused by the next brick
+    }
 }
 
 // P2G, one CTA of 128 threads per brick, in two phases per chunk of 128 of
@@ -840,43 +846,47 @@ __device__ __forceinline__ void musl_node_pass(const StepArgs<float> &a, const S
     }
 }
 
-template <int MINB>
+template <int MINB, bool LIST>
 __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell(StepArgs<float> a) {
     __shared__ float corner[3 * 8][BRC];
     __shared__ Scales S;
     __shared__ long long sh_l[32];
     __shared__ float sh_f[32];
-    const int b = blockIdx.x;
-    const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
-    const int *cs = a.cstart + (size_t)b * (BRC + 1);
-    if (cs[0] == cs[BRC]) return;
-    int ox, oy, oz;
-    brick_origin(b, a.nbrick, ox, oy, oz);
-    const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
-    const int p0 = cs[lc], p1 = cs[lc + 1];
     load_scales_musl(a, S);
-    const Particles<float> &P = a.P;
-    MuslCell C;
-    musl_load_cell(a, cx, cy, cz, h, p1 > p0, C);
-    float acc[3][4];
+    const int nbl = LIST ? *a.nblist : 1;
+    for (int li = LIST ? (int)blockIdx.x : 0; li < nbl; li += LIST ? (int)gridDim.x : 1) {
+        const int b = LIST ? a.blist[li] : (int)blockIdx.x;
+        const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
+        const int *cs = a.cstart + (size_t)b * (BRC + 1);
+        if (cs[0] == cs[BRC]) continue;   // empty brick (uniform across the CTA)
+        int ox, oy, oz;
+        brick_origin(b, a.nbrick, ox, oy, oz);
+        const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
+        const int p0 = cs[lc], p1 = cs[lc + 1];
+        const Particles<float> &P = a.P;
+        MuslCell C;
+        musl_load_cell(a, cx, cy, cz, h, p1 > p0, C);
+        float acc[3][4];
 #pragma unroll
-    for (int d = 0; d < 3; d++)
+        for (int d = 0; d < 3; d++)
 #pragma unroll
-        for (int c = 0; c < 4; c++) acc[d][c] = 0.0f;
-    long long gacc = 0;
-    float vmax = 0.0f;
-    const bool flip = (a.scheme == MPM_FLIP);
-    for (int p = p0; p < p1; p++) {
-        float vold[3] = {0.0f, 0.0f, 0.0f};
-        if (flip) {
-            vold[0] = ld(P.v[0] + p);
-            vold[1] = ld(P.v[1] + p);
-            vold[2] = ld(P.v[2] + p);
+            for (int c = 0; c < 4; c++) acc[d][c] = 0.0f;
+        long long gacc = 0;
+        float vmax = 0.0f;
+        const bool flip = (a.scheme == MPM_FLIP);
+        for (int p = p0; p < p1; p++) {
+            float vold[3] = {0.0f, 0.0f, 0.0f};
+            if (flip) {
+                vold[0] = ld(P.v[0] + p);
+                vold[1] = ld(P.v[1] + p);
+                vold[2] = ld(P.v[2] + p);
+            }
+            musl_particle(a, S, C, cx, cy, cz, h, p, ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p), ld(P.m + p),
+                          ld(P.vol + p), vold, acc, gacc, vmax);
         }
-        musl_particle(a, S, C, cx, cy, cz, h, p, ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p), ld(P.m + p),
-                      ld(P.vol + p), vold, acc, gacc, vmax);
+        musl_node_pass(a, S, corner, sh_l, sh_f, lc, h, ox, oy, oz, acc, gacc, vmax);
+        __syncthreads();   // shared memory is reused by the next brick
     }
-    musl_node_pass(a, S, corner, sh_l, sh_f, lc, h, ox, oy, oz, acc, gacc, vmax);
 }
 
 // Gather + MUSL, one CTA of 128 threads per brick, two phases per chunk of
@@ -2066,6 +2076,8 @@ static StepArgs<R> make_args(mpm_ctx *c) {
     a.nwork = c->d_nwork;
     a.cstart = c->d_cstart;
     a.miss = c->d_tmp;
+    a.blist = c->d_blist;
+    a.nblist = c->d_nblist;
     a.acc = c->d_acc;
     a.acc2 = c->d_acc2;
     R *nod = (R *)c->d_nodal;
@@ -2119,6 +2131,11 @@ static int num_sms() {
     return n;
 }
 
+// persistent grid over the active-brick list: never more CTAs than bricks
+static int list_grid(const mpm_ctx *c, int per_sm) {
+    return std::min(c->g.nbricks, per_sm * num_sms());
+}
+
 // which: 0 P2G, 1 G2P + MUSL, 2 G2P update
 template <typename R, int OX, int OY, int OZ>
 static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
@@ -2134,9 +2151,12 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                 if (c->tune.p2g_moments == 3) {
                     k_p2g_brick<<<c->g.nbricks, BCH, 0, c->stream>>>(a);
                 } else if (c->tune.p2g_moments == 2) {
-                    k_p2g_cell_mom<1><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                    k_p2g_cell_mom<1, false><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
                 } else if (c->tune.p2g_moments) {
-                    k_p2g_cell_mom<2><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                    if (c->tune.brick_list)
+                        k_p2g_cell_mom<2, true><<<list_grid(c, 2), CELL_THREADS, 0, c->stream>>>(a);
+                    else
+                        k_p2g_cell_mom<2, false><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
                 } else if (c->tune.p2g_staged) {
                     static bool attr = false;
                     if (!attr) {
@@ -2175,9 +2195,11 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                     }
                     k_g2p_musl_cell_staged<3><<<c->g.nbricks, CELL_THREADS, 2 * MSTAGE, c->stream>>>(a);
                 } else if (c->tune.musl_minb == 2) {
-                    k_g2p_musl_cell<2><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                    k_g2p_musl_cell<2, false><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                } else if (c->tune.brick_list) {
+                    k_g2p_musl_cell<3, true><<<list_grid(c, 3), CELL_THREADS, 0, c->stream>>>(a);
                 } else {
-                    k_g2p_musl_cell<3><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                    k_g2p_musl_cell<3, false><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
                 }
                 k_musl_misses<<<2 * num_sms(), 256, 0, c->stream>>>(a);
                 timer_end(c, K_G2P_MUSL);

@@ -109,6 +109,7 @@ struct WorkItem {
 // mpm_gpu_autotune from measured times (defaults otherwise).
 struct Tune {
     int p2g_moments = 1;            // FP32 P2G in moment form (k_p2g_cell_mom); 0: corner sums
+    int brick_list = 1;             // moment P2G and gather + MUSL walk the list of bricks holding particles
     int p2g_staged = 0;             // per-cell P2G reads the brick's particles from bulk-copied shared memory
     int p2g_minb = 2;               // resident CTAs the direct per-cell P2G is compiled for (2 or 3)
     int musl_staged = 0;            // gather + MUSL reads the brick's particles from staged shared memory
@@ -165,6 +166,8 @@ struct mpm_ctx {
     double *d_stage = nullptr;                  // FP64 AoS staging for host <-> device particle state
     mpm::WorkItem *d_work = nullptr;
     int *d_nwork = nullptr;
+    int *d_blist = nullptr;       // bricks holding particles, in brick order (rebuilt by every sort)
+    int *d_nblist = nullptr;
     int nwork_cap = 0;
     int nwork = 0;
     mpm::DevCtl *d_ctl = nullptr;

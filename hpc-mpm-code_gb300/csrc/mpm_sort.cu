@@ -45,33 +45,40 @@ __global__ void k_bin(KGeom<R> g, int nbx, int nby, const R *x0, const R *x1, co
 // One CTA: exclusive scan of the brick counts, the work list of <= CHUNK
 // particle chunks per brick, and the reset of the counters for the next sort.
 __global__ void __launch_bounds__(1024) k_scan(int nb, int *bcount, int *bstart, int *bcursor, WorkItem *work,
-                                               int *nwork, int cap) {
+                                               int *nwork, int cap, int *blist, int *nblist) {
     __shared__ int s_cnt[1024];
     __shared__ int s_chk[1024];
+    __shared__ int s_act[1024];
     const int T = blockDim.x;
     const int per = (nb + T - 1) / T;
     const int lo = threadIdx.x * per, hi = min(lo + per, nb);
-    int csum = 0, ksum = 0;
+    int csum = 0, ksum = 0, asum = 0;
     for (int t = lo; t < hi; t++) {
         int c = bcount[t];
         csum += c;
         ksum += (c + CHUNK - 1) / CHUNK;
+        asum += c > 0;
     }
     s_cnt[threadIdx.x] = csum;
     s_chk[threadIdx.x] = ksum;
+    s_act[threadIdx.x] = asum;
     __syncthreads();
     for (int off = 1; off < T; off <<= 1) {
         int a = threadIdx.x >= off ? s_cnt[threadIdx.x - off] : 0;
         int b = threadIdx.x >= off ? s_chk[threadIdx.x - off] : 0;
+        int d = threadIdx.x >= off ? s_act[threadIdx.x - off] : 0;
         __syncthreads();
         s_cnt[threadIdx.x] += a;
         s_chk[threadIdx.x] += b;
+        s_act[threadIdx.x] += d;
         __syncthreads();
     }
     int pbase = s_cnt[threadIdx.x] - csum;
     int wbase = s_chk[threadIdx.x] - ksum;
+    int abase = s_act[threadIdx.x] - asum;
     for (int t = lo; t < hi; t++) {
         int c = bcount[t];
+        if (c > 0) blist[abase++] = t;
         bstart[t] = pbase;
         bcursor[t] = 0;
         bcount[t] = 0;
@@ -89,6 +96,7 @@ __global__ void __launch_bounds__(1024) k_scan(int nb, int *bcount, int *bstart,
     }
     if (threadIdx.x == T - 1) {
         *nwork = min(s_chk[T - 1], cap);
+        *nblist = s_act[T - 1];
         bstart[nb] = s_cnt[T - 1];
     }
 }
@@ -193,7 +201,7 @@ static mpm_status sort_impl(mpm_ctx *c) {
     timer_end(c, K_BIN);
     timer_begin(c, K_SCAN);
     k_scan<<<1, 1024, 0, c->stream>>>(c->g.nbricks, c->d_tcount, c->d_tstart, c->d_tcursor, c->d_work, c->d_nwork,
-                                      c->nwork_cap);
+                                      c->nwork_cap, c->d_blist, c->d_nblist);
     timer_end(c, K_SCAN);
     timer_begin(c, K_SCATTER);
     k_scatter<<<nb, 256, 0, c->stream>>>(c->d_key, n, c->d_tstart, c->d_tcursor, c->d_tmp);
