@@ -174,6 +174,8 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     alloc((void **)&c->d_nwork, sizeof(int));
     alloc((void **)&c->d_blist, sizeof(int) * g.nbricks);
     alloc((void **)&c->d_nblist, sizeof(int));
+    alloc((void **)&c->d_tlist, sizeof(int) * g.ntiles);
+    alloc((void **)&c->d_ntlist, sizeof(int));
     alloc((void **)&c->d_ctl, sizeof(DevCtl));
     if (st == MPM_OK && cudaMallocHost((void **)&c->h_ctl, sizeof(DevCtl)) != cudaSuccess) st = MPM_ERR_OOM;
     if (st != MPM_OK) {
@@ -194,6 +196,7 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     cudaMemset(c->d_cstart, 0, sizeof(int) * (size_t)g.nbricks * (BRC + 1));
     cudaMemset(c->d_nwork, 0, sizeof(int));
     cudaMemset(c->d_nblist, 0, sizeof(int));
+    cudaMemset(c->d_ntlist, 0, sizeof(int));
     cudaMemset(c->d_ctl, 0, sizeof(DevCtl));
     memset(c->h_ctl, 0, sizeof(DevCtl));
     compute_nodal_volume(c);
@@ -228,6 +231,8 @@ void mpm_gpu_destroy(mpm_ctx *c) {
     free_dev(c->d_nwork);
     free_dev(c->d_blist);
     free_dev(c->d_nblist);
+    free_dev(c->d_tlist);
+    free_dev(c->d_ntlist);
     free_dev(c->d_ctl);
     if (c->h_ctl) cudaFreeHost(c->h_ctl);
     for (auto e : c->timer.ev) cudaEventDestroy(e);

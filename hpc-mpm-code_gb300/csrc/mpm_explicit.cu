@@ -43,6 +43,8 @@ struct StepArgs {
     int *miss;                  // particles that left their sorted cell, processed by a deferred pass
     const int *blist;           // bricks holding particles (brick order) and their count
     const int *nblist;
+    const int *tlist;           // active node tiles of this step (tile order) and their count
+    const int *ntlist;
     int nbrick[3];
     unsigned long long *acc;    // NACC * nodec
     unsigned long long *acc2;   // 3 * nodec
@@ -1470,18 +1472,20 @@ __global__ void __launch_bounds__(256) k_g2p_musl_box(StepArgs<R> a) {
 }
 
 // ------------------------------------------------------------ grid pass 1
-template <typename R>
+template <typename R, bool LIST>
 __global__ void __launch_bounds__(256) k_grid1(StepArgs<R> a) {
     __shared__ double sh_d[32];
     __shared__ float sh_f[32];
     __shared__ bool s_last;
     __shared__ Scales S;
-    const int t = blockIdx.x;
-    float eu = 0.0f;
     float gmax = 0.0f, neimax = 0.0f;
-    const bool active = a.all_tiles || a.tileflag[t];
+    load_scales(a, S);
+    const int ntl = LIST ? *a.ntlist : 1;
+    for (int lt = LIST ? (int)blockIdx.x : 0; lt < ntl; lt += LIST ? (int)gridDim.x : 1) {
+    const int t = LIST ? a.tlist[lt] : (int)blockIdx.x;
+    float eu = 0.0f;
+    const bool active = LIST || a.all_tiles || a.tileflag[t];
     if (active) {
-        load_scales(a, S);
         int tx, ty, tz;
         tile_coords(t, a.g.ntile, tx, ty, tz);
         const size_t N = (size_t)a.g.nodec;
@@ -1529,12 +1533,15 @@ __global__ void __launch_bounds__(256) k_grid1(StepArgs<R> a) {
             neimax = fmaxf(neimax, (float)e);
         }
     }
-    // deterministic sum of nei^2: per-tile partials, reduced in tile order by the last CTA
+    // deterministic sum of nei^2: per-tile partials (by list position in list
+    // mode), reduced in order by the last CTA
     double ebl = block_reduce((double)eu, OpAddD(), sh_d);
+    if (threadIdx.x == 0) a.eu_part[LIST ? lt : t] = ebl;
+    __syncthreads();
+    }
     float gm = block_reduce(gmax, OpMaxF(), sh_f);
     float nm = block_reduce(neimax, OpMaxF(), sh_f);
     if (threadIdx.x == 0) {
-        a.eu_part[t] = ebl;
         if (gm > 0.0f) atomic_max_pos(&a.ctl->cur[C_GMAX], gm * 1.000001f);
         if (nm > 0.0f) atomic_max_pos(&a.ctl->cur[C_NEIMAX], nm * 1.000001f);
         __threadfence();
@@ -1545,7 +1552,8 @@ __global__ void __launch_bounds__(256) k_grid1(StepArgs<R> a) {
     if (s_last) {
         __threadfence();
         double acc = 0.0;
-        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) acc += ((volatile double *)a.eu_part)[i];
+        const int npart = LIST ? *a.ntlist : (int)gridDim.x;
+        for (int i = threadIdx.x; i < npart; i += blockDim.x) acc += ((volatile double *)a.eu_part)[i];
         double tot = block_reduce(acc, OpAddD(), sh_d);
         if (threadIdx.x == 0) {
             a.ctl->eu_norm = tot;
@@ -1558,17 +1566,19 @@ __global__ void __launch_bounds__(256) k_grid1(StepArgs<R> a) {
 }
 
 // ------------------------------------------------------------ grid pass 2
-template <typename R>
+template <typename R, bool LIST>
 __global__ void __launch_bounds__(256) k_grid2(StepArgs<R> a) {
     __shared__ Scales S;
-    const int t = blockIdx.x;
-    if (t == 0 && threadIdx.x == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         // b0 of DeltaCorrectionParticleShifting (material_point.cpp:219)
         double gd = (double)(long long)a.ctl->geup_acc * a.ctl->sc_musl.gd.inv;
         a.ctl->b0 = (!a.shifting || gd < (double)a.mtol) ? 0.0 : a.ctl->eu_norm / gd;
     }
-    if (!(a.all_tiles || a.tileflag[t])) return;
     load_scales_musl(a, S);
+    const int ntl = LIST ? *a.ntlist : 1;
+    for (int lt = LIST ? (int)blockIdx.x : 0; lt < ntl; lt += LIST ? (int)gridDim.x : 1) {
+    const int t = LIST ? a.tlist[lt] : (int)blockIdx.x;
+    if (!(LIST || a.all_tiles || a.tileflag[t])) return;
     int tx, ty, tz;
     tile_coords(t, a.g.ntile, tx, ty, tz);
     const size_t N = (size_t)a.g.nodec;
@@ -1602,6 +1612,29 @@ __global__ void __launch_bounds__(256) k_grid2(StepArgs<R> a) {
         __syncthreads();
         if (threadIdx.x == 0) a.tileflag[t] = 0;
     }
+    }
+}
+
+// Compaction of the active-tile flags into a list in tile order (one CTA).
+__global__ void __launch_bounds__(1024) k_tile_list(const unsigned char *flag, int ntiles, int *list, int *nlist) {
+    __shared__ int s_cnt[1024];
+    const int T = blockDim.x;
+    const int per = (ntiles + T - 1) / T;
+    const int lo = threadIdx.x * per, hi = min(lo + per, ntiles);
+    int cnt = 0;
+    for (int t = lo; t < hi; t++) cnt += flag[t] != 0;
+    s_cnt[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int off = 1; off < T; off <<= 1) {
+        const int v = threadIdx.x >= off ? s_cnt[threadIdx.x - off] : 0;
+        __syncthreads();
+        s_cnt[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int base = s_cnt[threadIdx.x] - cnt;
+    for (int t = lo; t < hi; t++)
+        if (flag[t]) list[base++] = t;
+    if (threadIdx.x == T - 1) *nlist = s_cnt[T - 1];
 }
 
 // ----------------------------------------------- G2P 2: F, x, vol, stress
@@ -2078,6 +2111,8 @@ static StepArgs<R> make_args(mpm_ctx *c) {
     a.miss = c->d_tmp;
     a.blist = c->d_blist;
     a.nblist = c->d_nblist;
+    a.tlist = c->d_tlist;
+    a.ntlist = c->d_ntlist;
     a.acc = c->d_acc;
     a.acc2 = c->d_acc2;
     R *nod = (R *)c->d_nodal;
@@ -2260,13 +2295,22 @@ static mpm_status particle_kernel(mpm_ctx *c, int which) {
 template <typename R>
 static mpm_status grid_kernel(mpm_ctx *c, int which) {
     StepArgs<R> a = make_args<R>(c);
+    const bool list = !a.all_tiles;
+    const int lgrid = std::min(c->g.ntiles, 4 * num_sms());
     if (which == 0) {
         timer_begin(c, K_GRID1);
-        k_grid1<R><<<c->g.ntiles, 256, 0, c->stream>>>(a);
+        if (list) {
+            k_tile_list<<<1, 1024, 0, c->stream>>>(c->d_tileflag, c->g.ntiles, c->d_tlist, c->d_ntlist);
+            k_grid1<R, true><<<lgrid, 256, 0, c->stream>>>(a);
+            c->launches++;
+        } else {
+            k_grid1<R, false><<<c->g.ntiles, 256, 0, c->stream>>>(a);
+        }
         timer_end(c, K_GRID1);
     } else {
         timer_begin(c, K_GRID2);
-        k_grid2<R><<<c->g.ntiles, 256, 0, c->stream>>>(a);
+        if (list) k_grid2<R, true><<<lgrid, 256, 0, c->stream>>>(a);
+        else k_grid2<R, false><<<c->g.ntiles, 256, 0, c->stream>>>(a);
         timer_end(c, K_GRID2);
     }
     c->launches++;

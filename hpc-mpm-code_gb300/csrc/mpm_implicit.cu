@@ -9,7 +9,7 @@
 //   BCNRSet / Predict        implicit_mpm_solid.h:55-64,
 //                            nonlinear_time_integration.cpp:59-71    -> k_imp_bcnr, k_imp_predict
 //   AssembleSystem           solve_solid_implicit.cpp:105-204        -> k_imp_assemble, k_imp_rhs_diag
-//   ComputeTangentModulus    solve_solid_implicit.cpp:34-63          -> tangent() below
+//   ComputeTangentModulus    solve_solid_implicit.cpp:34-63          -> pair loop of k_imp_assemble
 //   BuildDiagonalPreconditioner crsmat.cpp:87-184                     -> k_imp_rhs_diag, k_imp_scale
 //   MatVecMult               solver.cpp:405-433                      -> k_imp_matvec
 //   GPBiCGSafe               solver.cpp:19-141                       -> conjugate gradients (the scaled
@@ -62,6 +62,7 @@ struct ImpState {
     double *xstar = nullptr, *ev = nullptr; // training-pair harvest: converged solution, error
     double *gp = nullptr, *gq = nullptr;    // flexible GCR: GM directions and their images (GM * 3 * nodec)
     double *gqq = nullptr, *gbeta = nullptr;  // |A p|^2 of each kept direction, projection coefficients
+    unsigned *cnt = nullptr;                // block counters of the single-launch reductions (zero between launches)
     int fallbacks = 0;                      // solves that switched from the network to Jacobi
     int nn_applications = 0;
     // CUDA graphs of 8 Krylov iterations (CG; FCG with the network; FCG with Jacobi)
@@ -233,19 +234,6 @@ __global__ void k_imp_predict(ImpArgs a, double *ndispl, const double *nvel, con
     }
 }
 
-// Tangent block K_ij = dNa . ce . dNb with ce[i][k][j][l] = lambda' d_ik d_jl
-// + mu' (d_ij d_kl + d_il d_kj) + (NR) sigma_kl d_ij -- the isotropic
-// stif_mat of models 0 and 1 contracted as ComputeTangentModulus does.
-__device__ __forceinline__ void tangent(const double *da, const double *db, double lam, double mu,
-                                       const double sg[3][3], int nr, double K[3][3]) {
-    const double ab = da[0] * db[0] + da[1] * db[1] + da[2] * db[2];
-    double asb = 0.0;
-    if (nr)
-        for (int k = 0; k < 3; k++) asb += da[k] * (sg[k][0] * db[0] + sg[k][1] * db[1] + sg[k][2] * db[2]);
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) K[i][j] = lam * da[i] * db[j] + mu * da[j] * db[i] + (i == j ? mu * ab + asb : 0.0);
-}
-
 // ------------------------------------------------------------- assembly
 // One thread per particle (AssembleSystem, solve_solid_implicit.cpp:123-189):
 // UpdateDefGrad with alpha_f, the stress of the Newton iterate, the gradient
@@ -327,23 +315,44 @@ __global__ void __launch_bounds__(128) k_imp_assemble(ImpArgs a, PView P, const 
     const double m = P.m[p];
     const double fx = a.grav[0] * a.facl, fy = a.grav[1] * a.facl, fz = a.grav[2] * a.facl;
     const double afv = a.af * vol;
+    // Tangent blocks with the factors of the particle folded into three
+    // vectors per node (L = af vol lambda' dN_a, M = af vol mu' dN_a,
+    // S = af vol sigma dN_a):  K_ab = L_a db^T + db M_a^T + I (M_a + S_a).db,
+    // and K_ba = K_ab^T, so each unordered pair is computed once.
     for (int qa = 0; qa < 8; qa++) {
         const int na = nid[qa];
-        int ia, ja, ka;
-        node_ijk(na, a.nnc, ia, ja, ka);
         const double emd = a.nb[3] * Nw[qa] * m;   // ComputeNRLumpedMat (material_point.h:144)
-        for (int qb = 0; qb < 8; qb++) {
+        double L[3], M[3], T[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            L[k] = afv * lam * dN[qa][k];
+            M[k] = afv * mu * dN[qa][k];
+            const double sk_ = a.nr_flag ? afv * (sg[k][0] * dN[qa][0] + sg[k][1] * dN[qa][1] + sg[k][2] * dN[qa][2]) : 0.0;
+            T[k] = M[k] + sk_;
+        }
+#pragma unroll 1
+        for (int qb = qa; qb < 8; qb++) {
             const int nbn = nid[qb];
-            int ib, jb, kb;
-            node_ijk(nbn, a.nnc, ib, jb, kb);
-            const int s = (ib - ia + 1) + 3 * (jb - ja + 1) + 9 * (kb - ka + 1);
+            const int dxo = (qb & 1) - (qa & 1), dyo = ((qb >> 1) & 1) - ((qa >> 1) & 1), dzo = (qb >> 2) - (qa >> 2);
+            const int s = (dxo + 1) + 3 * (dyo + 1) + 9 * (dzo + 1);
+            const double db0 = dN[qb][0], db1 = dN[qb][1], db2 = dN[qb][2];
+            const double db[3] = {db0, db1, db2};
+            const double dg = T[0] * db0 + T[1] * db1 + T[2] * db2;
             double K[3][3];
-            tangent(dN[qa], dN[qb], lam, mu, sg, a.nr_flag, K);
+#pragma unroll
             for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) K[i][j] = L[i] * db[j] + M[j] * db[i] + (i == j ? dg : 0.0);
+            if (qa == qb) {
+#pragma unroll
+                for (int i = 0; i < 3; i++) K[i][i] += a.am * emd;
+            }
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
                 for (int j = 0; j < 3; j++) {
-                    double v = afv * K[i][j];
-                    if (qa == qb && i == j) v += a.am * emd;
-                    atomicAdd(&A[aidx(s * 9 + 3 * i + j, na)], v);
+                    atomicAdd(&A[aidx(s * 9 + 3 * i + j, na)], K[i][j]);
+                    if (qb != qa) atomicAdd(&A[aidx((26 - s) * 9 + 3 * j + i, nbn)], K[i][j]);
                 }
         }
         const double f0 = -vol * (sk[0] * dN[qa][0] + sk[5] * dN[qa][1] + sk[4] * dN[qa][2]) + Nw[qa] * (m * fx);
@@ -444,9 +453,10 @@ __global__ void __launch_bounds__(256) k_imp_matvec(ImpArgs a, const double *A, 
                     e[2 + 2 * t] = v.y;
                 }
             }
-            acc[0] += e[0] * x0 + e[1] * x1 + e[2] * x2;
-            acc[1] += e[3] * x0 + e[4] * x1 + e[5] * x2;
-            acc[2] += e[6] * x0 + e[7] * x1 + e[8] * x2;
+            // chained FMAs: the FP64 pipe is this kernel's limit, and a
+            // separate product and add per entry would cost a third more
+#pragma unroll
+            for (int r = 0; r < 3; r++) acc[r] = fma(e[3 * r + 2], x2, fma(e[3 * r + 1], x1, fma(e[3 * r], x0, acc[r])));
         }
         const unsigned char bf = a.bcflag[n];
         for (int c = 0; c < 3; c++) {
@@ -841,85 +851,142 @@ __global__ void k_set_modulus(double *matprop, int nmat, double E) {
 __device__ __forceinline__ int gcr_prev(int slot, int j) { return (slot - 1 - j + 2 * GM) % GM; }
 
 // partial dots q . Q_j with the `used` previous images (j = 0 the newest)
-__global__ void k_gcr_dots(ImpArgs a, const double *Q, int slot, int used, double *part) {
-    __shared__ double sh[32];
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    const size_t N = (size_t)a.nodec, st = 3 * N;
-    const double *q = Q + (size_t)slot * st;
-    for (int j = 0; j < used; j++) {
-        const double *qj = Q + (size_t)gcr_prev(slot, j) * st;
-        double d = 0.0;
-        if (n < a.nodec)
-            for (int c = 0; c < 3; c++) d += q[c * N + n] * qj[c * N + n];
-        const double t = block_sum(d, sh);
-        if (threadIdx.x == 0) part[j * gridDim.x + blockIdx.x] = t;
+// Per-block partial sums of nv (<= V) values into part[j * gridDim.x + b];
+// true in the last block to finish (the blocks count themselves on *cnt),
+// which then reduces the partials in block order (last_sum), so the sums
+// are reproducible without a separate reduction launch.
+template <int V>
+__device__ __forceinline__ bool partials_last(const double (&v)[V], int nv, double *part, unsigned *cnt) {
+    __shared__ double sh[V][8];
+    __shared__ bool s_last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < V; j++) {
+        if (j < nv) {
+            double x = v[j];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) sh[j][wid] = x;
+        }
     }
+    __syncthreads();
+    if ((int)threadIdx.x < nv) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[threadIdx.x][w];
+        part[threadIdx.x * gridDim.x + blockIdx.x] = t;
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (s_last) __threadfence();
+    return s_last;
 }
 
-// beta_j = (q . Q_j) / (Q_j . Q_j), one block per j
-__global__ void k_gcr_beta(const double *part, int nb, int slot, const double *qq, double *beta) {
-    __shared__ double sh[32];
-    const int j = blockIdx.x;
+// in the last block: the total of value j over all blocks (thread 0)
+__device__ __forceinline__ double last_sum(const double *part, int j, double *sh32) {
     double acc = 0.0;
-    for (int i = threadIdx.x; i < nb; i += blockDim.x) acc += part[j * nb + i];
-    const double t = block_sum(acc, sh);
-    if (threadIdx.x == 0) {
-        const double d = qq[gcr_prev(slot, j)];
-        beta[j] = d > 0.0 ? t / d : 0.0;
-    }
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) acc += __ldcg(part + (size_t)j * gridDim.x + i);
+    return block_sum(acc, sh32);
 }
 
-// p -= sum beta_j P_j, q -= sum beta_j Q_j; partial q.r and q.q
-__global__ void k_gcr_axpy(ImpArgs a, double *P, double *Q, int slot, int used, const double *beta, const double *r,
-                           double *part) {
+// flexible GCR: the dots q . Q_j of the new image with the kept ones, then
+// (last block) beta_j = (q . Q_j) / (Q_j . Q_j)
+__global__ void __launch_bounds__(256) k_gcr_dots(ImpArgs a, const double *Q, int slot, int used, double *part,
+                                                  unsigned *cnt, const double *qq, double *beta) {
     __shared__ double sh[32];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const size_t N = (size_t)a.nodec, st = 3 * N;
-    double dqr = 0.0, dqq = 0.0;
+    double d[GM];
+#pragma unroll
+    for (int j = 0; j < GM; j++) d[j] = 0.0;
+    if (n < a.nodec) {
+        const double *q = Q + (size_t)slot * st;
+        const double q0 = q[n], q1 = q[N + n], q2 = q[2 * N + n];
+#pragma unroll
+        for (int j = 0; j < GM; j++)
+            if (j < used) {
+                const double *qj = Q + (size_t)gcr_prev(slot, j) * st;
+                d[j] = q0 * qj[n] + q1 * qj[N + n] + q2 * qj[2 * N + n];
+            }
+    }
+    if (!partials_last<GM>(d, used, part, cnt)) return;
+    for (int j = 0; j < used; j++) {
+        const double t = last_sum(part, j, sh);
+        if (threadIdx.x == 0) {
+            const double dq = qq[gcr_prev(slot, j)];
+            beta[j] = dq > 0.0 ? t / dq : 0.0;
+        }
+    }
+    if (threadIdx.x == 0) *cnt = 0u;
+}
+
+// p -= sum beta_j P_j, q -= sum beta_j Q_j; then (last block) q.r and q.q
+__global__ void __launch_bounds__(256) k_gcr_axpy(ImpArgs a, double *P, double *Q, int slot, int used,
+                                                  const double *beta, const double *r, double *part, unsigned *cnt,
+                                                  double *scal) {
+    __shared__ double sh[32];
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t N = (size_t)a.nodec, st = 3 * N;
+    double v[2] = {0.0, 0.0};
     if (n < a.nodec) {
         double *p = P + (size_t)slot * st, *q = Q + (size_t)slot * st;
+        double bj[GM];
+#pragma unroll
+        for (int j = 0; j < GM; j++) bj[j] = j < used ? beta[j] : 0.0;
         for (int c = 0; c < 3; c++) {
             const size_t i = c * N + n;
             double pv = p[i], qv = q[i];
-            for (int j = 0; j < used; j++) {
-                const size_t o = (size_t)gcr_prev(slot, j) * st + i;
-                pv -= beta[j] * P[o];
-                qv -= beta[j] * Q[o];
-            }
+#pragma unroll
+            for (int j = 0; j < GM; j++)
+                if (j < used) {
+                    const size_t o = (size_t)gcr_prev(slot, j) * st + i;
+                    pv -= bj[j] * P[o];
+                    qv -= bj[j] * Q[o];
+                }
             p[i] = pv;
             q[i] = qv;
-            dqr += qv * r[i];
-            dqq += qv * qv;
+            v[0] += qv * r[i];
+            v[1] += qv * qv;
         }
     }
-    const double t1 = block_sum(dqr, sh);
-    if (threadIdx.x == 0) part[blockIdx.x] = t1;
-    const double t2 = block_sum(dqq, sh);
-    if (threadIdx.x == 0) part[gridDim.x + blockIdx.x] = t2;
+    if (!partials_last<2>(v, 2, part, cnt)) return;
+    const double qr = last_sum(part, 0, sh);
+    const double qq = last_sum(part, 1, sh);
+    if (threadIdx.x == 0) {
+        scal[S_QR] = qr;
+        scal[S_QQ] = qq;
+        *cnt = 0u;
+    }
 }
 
-// alpha = q.r / q.q; x += alpha p; r -= alpha q; partial r.r; keeps q.q of the slot
-__global__ void k_gcr_update(ImpArgs a, const double *scal, double *x, double *r, const double *P, const double *Q,
-                             int slot, double *qq, double *part) {
+// alpha = q.r / q.q; x += alpha p; r -= alpha q; keeps q.q of the slot; then
+// (last block) r.r
+__global__ void __launch_bounds__(256) k_gcr_update(ImpArgs a, double *scal, double *x, double *r, const double *P,
+                                                    const double *Q, int slot, double *qq, double *part,
+                                                    unsigned *cnt) {
     __shared__ double sh[32];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const size_t N = (size_t)a.nodec, st = 3 * N;
     const double dqq = scal[S_QQ];
     const double alpha = dqq > 0.0 ? scal[S_QR] / dqq : 0.0;
     if (blockIdx.x == 0 && threadIdx.x == 0) qq[slot] = dqq;
-    double d = 0.0;
+    double v[1] = {0.0};
     if (n < a.nodec) {
         const double *p = P + (size_t)slot * st, *q = Q + (size_t)slot * st;
         for (int c = 0; c < 3; c++) {
             const size_t i = c * N + n;
             x[i] += alpha * p[i];
-            const double v = r[i] - alpha * q[i];
-            r[i] = v;
-            d += v * v;
+            const double w = r[i] - alpha * q[i];
+            r[i] = w;
+            v[0] += w * w;
         }
     }
-    const double t = block_sum(d, sh);
-    if (threadIdx.x == 0) part[blockIdx.x] = t;
+    if (!partials_last<1>(v, 1, part, cnt)) return;
+    const double rr = last_sum(part, 0, sh);
+    if (threadIdx.x == 0) {
+        scal[S_RRC] = rr;
+        *cnt = 0u;
+    }
 }
 
 __global__ void k_imp_reset_next(DevCtl *ctl, int parity) {
@@ -948,6 +1015,7 @@ void implicit_free(mpm_ctx *c) {
                       s->z, s->bs, s->xstar, s->ev, s->gp, s->gq, s->gqq, s->gbeta};
     for (double *b : bufs)
         if (b) cudaFree(b);
+    if (s->cnt) cudaFree(s->cnt);
     if (s->h_scal) cudaFreeHost(s->h_scal);
     for (cudaGraphExec_t g : {s->g_cg, s->g_fcg_nn, s->g_fcg_jac, s->g_gcr})
         if (g) cudaGraphExecDestroy(g);
@@ -1008,6 +1076,8 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
     CKI(cudaMalloc((void **)&s->gq, sizeof(double) * GM * 3 * N));
     CKI(cudaMalloc((void **)&s->gqq, sizeof(double) * GM));
     CKI(cudaMalloc((void **)&s->gbeta, sizeof(double) * GM));
+    CKI(cudaMalloc((void **)&s->cnt, sizeof(unsigned) * 8));
+    CKI(cudaMemset(s->cnt, 0, sizeof(unsigned) * 8));
     CKI(cudaMalloc((void **)&s->nmass, sizeof(double) * N));
     CKI(cudaMalloc((void **)&s->nvof, sizeof(double) * N));
     CKI(cudaMalloc((void **)&s->nei, sizeof(double) * N));
@@ -1154,17 +1224,13 @@ static mpm_status gcr_iter(mpm_ctx *c, const ImpArgs &a, int nb, int u, int sl) 
     k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->gp + (size_t)sl * st3, s->gq + (size_t)sl * st3, nullptr);
     timer_end(c, K_MATVEC);
     timer_begin(c, K_KRYLOV);
-    if (u > 0) {
-        k_gcr_dots<<<nb, 256, 0, c->stream>>>(a, s->gq, sl, u, s->part);
-        k_gcr_beta<<<u, 256, 0, c->stream>>>(s->part, nb, sl, s->gqq, s->gbeta);
-    }
-    k_gcr_axpy<<<nb, 256, 0, c->stream>>>(a, s->gp, s->gq, sl, u, s->gbeta, s->r, s->part);
-    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_QR);
-    k_finish<<<1, 256, 0, c->stream>>>(s->part + nb, nb, s->scal, S_QQ);
-    k_gcr_update<<<nb, 256, 0, c->stream>>>(a, s->scal, s->xs, s->r, s->gp, s->gq, sl, s->gqq, s->part);
-    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
+    if (u > 0)
+        k_gcr_dots<<<nb, 256, 0, c->stream>>>(a, s->gq, sl, u, s->part, s->cnt, s->gqq, s->gbeta);
+    k_gcr_axpy<<<nb, 256, 0, c->stream>>>(a, s->gp, s->gq, sl, u, s->gbeta, s->r, s->part, s->cnt + 1, s->scal);
+    k_gcr_update<<<nb, 256, 0, c->stream>>>(a, s->scal, s->xs, s->r, s->gp, s->gq, sl, s->gqq, s->part,
+                                            s->cnt + 2);
     timer_end(c, K_KRYLOV);
-    c->launches += 9 + 7 + (u > 0 ? 2 : 0);
+    c->launches += 9 + 3 + (u > 0 ? 1 : 0);
     return MPM_OK;
 }
 

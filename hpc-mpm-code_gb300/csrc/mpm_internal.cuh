@@ -168,6 +168,8 @@ struct mpm_ctx {
     int *d_nwork = nullptr;
     int *d_blist = nullptr;       // bricks holding particles, in brick order (rebuilt by every sort)
     int *d_nblist = nullptr;
+    int *d_tlist = nullptr;       // active node tiles of the current step (tile order)
+    int *d_ntlist = nullptr;
     int nwork_cap = 0;
     int nwork = 0;
     mpm::DevCtl *d_ctl = nullptr;

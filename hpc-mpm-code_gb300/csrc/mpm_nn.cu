@@ -20,9 +20,12 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
+
+#include <cuda.h>
 
 #include "mpm_nn.cuh"
 #include "mpm_tc.cuh"
@@ -294,6 +297,243 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a) {
     if (warp == 0) tc::tmem_dealloc(taddr, TCOLS);
 }
 
+// ------------------------------------------------- halo-tiled convolution
+// Forward convolutions (S1, S2) as an implicit GEMM over a shared-memory halo
+// tile loaded by TMA.  An output tile is 8 (x) x 16 (y) x 1 (z) nodes = the
+// 128 rows of one MMA, row m = x + 8 y.  Its input halo (S1: 10 x 18 x 3
+// nodes; S2: 17 x 33 x 3) is brought in by one tensor copy per 8-channel
+// chunk (a 5-D tensor map per chunk: 8 channels, x, y, z, sample; zero fill
+// outside the grid), which lands as [z][y][x] 16-byte entries.  For every tap
+// the A operand is then the same canonical K-major no-swizzle matrix at a
+// shifted start address: 8 consecutive x entries form a core matrix, the
+// chunk stride is the leading byte offset and the y stride (2 y strides for
+// S2) the stride byte offset.  For S2 the even and odd x positions are two
+// copies with a traversal stride of 2, so that the stride-2 rows of a tap are
+// again consecutive entries.  Each input node is read about 4 times per tile
+// instead of 27 times, one thread issues all copies, and with two halo
+// buffers the copy of the next tile overlaps the MMAs and the epilogue of the
+// current one.
+template <int MODE>
+struct Halo {
+    static constexpr int TX = 8, TY = 16;
+    static constexpr int XE = MODE == S1 ? 10 : 9;     // x entries per row and copy
+    static constexpr int HY = MODE == S1 ? 18 : 33;
+    static constexpr int HZ = 3;
+    static constexpr uint32_t COPY = 16u * XE * HY * HZ;            // bytes of one tensor copy
+    static constexpr uint32_t BLK = (COPY + 127u) / 128u * 128u;   // its 128-byte aligned slot
+    static constexpr uint32_t CHUNK = (MODE == S1 ? 1u : 2u) * BLK; // one 8-channel chunk (S2: even, odd)
+    static constexpr uint32_t RS = 16u * XE;                        // y stride
+    static constexpr uint32_t PS = RS * HY;                         // z stride
+};
+
+template <int K, int MODE>
+__host__ __device__ constexpr uint32_t halo_bytes() {
+    return (uint32_t)(K / 8) * Halo<MODE>::CHUNK;
+}
+
+template <int K, int N, int MODE>
+__host__ __device__ constexpr int halo_nbuf() {
+    return 27u * N * K * 2 + 2u * halo_bytes<K, MODE>() <= 200u * 1024 ? 2 : 1;
+}
+
+template <int K, int N, int MODE>
+__host__ __device__ constexpr size_t halo_smem() {
+    return 27u * N * K * 2 + (size_t)halo_nbuf<K, N, MODE>() * halo_bytes<K, MODE>() + 128;
+}
+
+struct HaloMaps {
+    CUtensorMap m[8];   // one per 8-channel chunk of the input
+};
+
+__device__ __forceinline__ void tma_load5(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3, int c4,
+                                          unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5, %6}], [%7];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_addr(bar))
+        : "memory");
+}
+
+template <int K, int N, int MODE>
+__global__ void __launch_bounds__(128) k_conv_halo(ConvArgs a, const __grid_constant__ HaloMaps maps) {
+    using H = Halo<MODE>;
+    constexpr int KC = K / 8;
+    constexpr int NBUF = halo_nbuf<K, N, MODE>();
+    constexpr uint32_t WT = (uint32_t)N * K * 2;
+    constexpr uint32_t WB = 27u * WT;
+    constexpr uint32_t HB = halo_bytes<K, MODE>();
+    constexpr uint32_t LBO = H::CHUNK;
+    constexpr uint32_t SBO_A = MODE == S1 ? H::RS : 2 * H::RS;
+    constexpr uint32_t SBO_W = K * 16;
+    constexpr uint32_t TX_BYTES = (uint32_t)KC * (MODE == S1 ? 1u : 2u) * H::COPY;
+    constexpr uint32_t TCOLS = N < 32 ? 32 : N;
+    constexpr uint32_t IDESC = tc::idesc_bf16(128, N);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ unsigned long long bar, full[2];
+    __shared__ uint32_t tslot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // halo buffers first, 128-byte aligned (tensor copy destinations), then the weights
+    const uint32_t sbase = (smem_addr(smem_raw) + 127u) & ~127u;
+    unsigned char *smem = smem_raw + (sbase - smem_addr(smem_raw));
+    const uint32_t sh = sbase, sw = sbase + NBUF * HB;
+    if (warp == 0) tc::tmem_alloc(&tslot, TCOLS);
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        fence_mbar_init();
+    }
+    {
+        const uint4 *src = reinterpret_cast<const uint4 *>(a.w);
+        uint4 *dst = reinterpret_cast<uint4 *>(smem + NBUF * HB);
+        for (uint32_t i = tid; i < WB / 16; i += 128) dst[i] = __ldg(src + i);
+    }
+    tc::fence_async_smem();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t taddr = tslot;
+    const int ntx = (a.lout.n[0] + H::TX - 1) / H::TX, nty = (a.lout.n[1] + H::TY - 1) / H::TY;
+    const int64_t per_b = (int64_t)ntx * nty * a.lout.n[2];
+    const int64_t ntile = (a.rows / a.lout.v) * per_b;
+    auto coords = [&](int64_t tile, int &b, int &x0, int &y0, int &z0) {
+        b = (int)(tile / per_b);
+        int64_t r = tile - (int64_t)b * per_b;
+        x0 = (int)(r % ntx) * H::TX;
+        r /= ntx;
+        y0 = (int)(r % nty) * H::TY;
+        z0 = (int)(r / nty);
+    };
+    // thread 0 only: the halo of `tile` into buffer `buf`
+    auto issue = [&](int64_t tile, int buf) {
+        int b, x0, y0, z0;
+        coords(tile, b, x0, y0, z0);
+        const uint32_t dst = sh + (uint32_t)buf * HB;
+        mbar_expect_tx(&full[buf], TX_BYTES);
+#pragma unroll
+        for (int kc = 0; kc < KC; kc++) {
+            if (MODE == S1) {
+                tma_load5(dst + kc * LBO, &maps.m[kc], 0, x0 - 1, y0 - 1, z0 - 1, b, &full[buf]);
+            } else {
+                tma_load5(dst + kc * LBO, &maps.m[kc], 0, 2 * x0 - 1, 2 * y0 - 1, 2 * z0 - 1, b, &full[buf]);
+                tma_load5(dst + kc * LBO + H::BLK, &maps.m[kc], 0, 2 * x0, 2 * y0 - 1, 2 * z0 - 1, b, &full[buf]);
+            }
+        }
+    };
+    uint32_t iss0 = 0u, iss1 = 0u, con0 = 0u, con1 = 0u;   // copies issued into / consumed from each buffer
+    uint32_t i = 0;
+    bool ok = true, mma_pending = false;
+    int64_t tile = blockIdx.x;
+    if (tile < ntile) {
+        if (tid == 0) issue(tile, 0);
+        iss0++;
+    }
+    for (; tile < ntile; tile += gridDim.x, i++) {
+        const int buf = NBUF == 2 ? (int)(i & 1) : 0;
+        const int64_t next = tile + gridDim.x;
+        // the other buffer was last read by the MMAs of the previous tile,
+        // which completed before that tile's epilogue
+        if (NBUF == 2 && next < ntile) {
+            if (tid == 0) issue(next, buf ^ 1);
+            if (buf) iss0++;
+            else iss1++;
+        }
+        const bool landed = mbar_wait_bounded(&full[buf], (buf ? con1 : con0) & 1u, TC_WAIT);
+        if (buf) con1++;
+        else con0++;
+        if (!__syncthreads_and(landed)) {
+            ok = false;
+            break;
+        }
+        if (tid == 0) {
+            tc::fence_after();
+            const uint32_t cur = sh + (uint32_t)buf * HB;
+#pragma unroll
+            for (int t = 0; t < 27; t++) {
+                const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
+                uint32_t base = cur + (uint32_t)(dz + 1) * H::PS + (uint32_t)(dy + 1) * H::RS;
+                if (MODE == S1) base += (uint32_t)(dx + 1) * 16u;
+                else base += dx == 0 ? H::BLK : (dx > 0 ? 16u : 0u);
+#pragma unroll
+                for (int kk = 0; kk < K / 16; kk++) {
+                    const uint64_t ad = tc::sdesc(base + kk * 2 * LBO, LBO, SBO_A);
+                    const uint64_t bd = tc::sdesc(sw + t * WT + kk * 256, 128, SBO_W);
+                    tc::mma_bf16(taddr, ad, bd, IDESC, (t | kk) != 0);
+                }
+            }
+            tc::mma_commit(&bar);
+        }
+        mma_pending = true;
+        const bool done = mbar_wait_bounded(&bar, i & 1, TC_WAIT);
+        if (!__syncthreads_and(done)) {
+            ok = false;
+            break;
+        }
+        mma_pending = false;
+        if (NBUF == 1 && next < ntile) {   // the MMAs are done with the only buffer
+            if (tid == 0) issue(next, 0);
+            iss0++;
+        }
+        tc::fence_after();
+        float acc[N];
+#pragma unroll
+        for (int c = 0; c < N / 16; c++) tc::tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + c * 16, acc + c * 16);
+        int b, x0, y0, z0;
+        coords(tile, b, x0, y0, z0);
+        const int ox = x0 + (tid & 7), oy = y0 + (tid >> 3);
+        if (ox < a.lout.n[0] && oy < a.lout.n[1]) {
+            const int64_t row = (int64_t)b * a.lout.v + ox + (int64_t)a.lout.n[0] * (oy + (int64_t)a.lout.n[1] * z0);
+            if (a.bias) {
+#pragma unroll
+                for (int c = 0; c < N; c++) acc[c] += __ldg(a.bias + c);
+            }
+            if (a.add) {
+                const uint4 *ap = reinterpret_cast<const uint4 *>(a.add + row * N);
+#pragma unroll
+                for (int c = 0; c < N / 8; c++) {
+                    float f[8];
+                    unpack8(__ldg(ap + c), f);
+#pragma unroll
+                    for (int e = 0; e < 8; e++) acc[c * 8 + e] += f[e];
+                }
+            }
+            if (a.relu) {
+#pragma unroll
+                for (int c = 0; c < N; c++) acc[c] = fmaxf(acc[c], 0.0f);
+            }
+            if (a.mask) {
+                const uint4 *mp = reinterpret_cast<const uint4 *>(a.mask + row * N);
+#pragma unroll
+                for (int c = 0; c < N / 8; c++) {
+                    float f[8];
+                    unpack8(__ldg(mp + c), f);
+#pragma unroll
+                    for (int e = 0; e < 8; e++)
+                        if (!(f[e] > 0.0f)) acc[c * 8 + e] = 0.0f;
+                }
+            }
+            uint4 *op = reinterpret_cast<uint4 *>(a.out + row * N);
+#pragma unroll
+            for (int c = 0; c < N / 8; c++) op[c] = pack8(acc + c * 8);
+        }
+        tc::fence_before();
+        __syncthreads();
+    }
+    if (!ok) {
+        if (tid == 0) {
+            atomicAdd(a.err, 1);
+            // let every copy still in flight land before the block exits
+            if (iss0 > con0) mbar_wait_bounded(&full[0], (iss0 - 1u) & 1u, TC_WAIT);
+            if (iss1 > con1) mbar_wait_bounded(&full[1], (iss1 - 1u) & 1u, TC_WAIT);
+        }
+        if (mma_pending) mbar_wait_bounded(&bar, i & 1, TC_WAIT);
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    if (warp == 0) tc::tmem_dealloc(taddr, TCOLS);
+}
+
 // --------------------------------------------------------- weight gradient
 struct DwArgs {
     const bf16 *in;   // [rows_in][CIN]
@@ -460,13 +700,25 @@ __global__ void k_input_f32(const float *in, bf16 *x0, int64_t rows) {
     o[1] = make_uint4(0, 0, 0, 0);
 }
 
+// The residual's RMS sqrt(rr / (3 nodec)) (or its inverse), evaluated once
+// per block: FP64 division and square root are slow on this part, so no
+// thread but the first does them.  Called by every thread before any return.
+__device__ __forceinline__ double block_rms(const double *rr, int64_t nodec, bool inverse) {
+    __shared__ double s_rms;
+    if (threadIdx.x == 0) {
+        const double ms = rr[0] / (3.0 * (double)nodec);
+        s_rms = ms > 0.0 ? (inverse ? 1.0 / sqrt(ms) : sqrt(ms)) : 0.0;
+    }
+    __syncthreads();
+    return s_rms;
+}
+
 // x0 from an FP64 component-major residual, scaled by 1 / sqrt(rr / (3 nodec)),
 // and the system's feature channels
 __global__ void k_input_r(const double *r, const double *rr, const bf16 *feat, int64_t nodec, int linear, bf16 *x0) {
     const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const double inv = block_rms(rr, nodec, true);
     if (n >= nodec) return;
-    const double ms = rr[0] / (3.0 * (double)nodec);
-    const double inv = ms > 0.0 ? 1.0 / sqrt(ms) : 0.0;
     float f[8] = {(float)(r[n] * inv), (float)(r[nodec + n] * inv), (float)(r[2 * nodec + n] * inv),
                   __bfloat162float(feat[3 * n]), __bfloat162float(feat[3 * n + 1]), __bfloat162float(feat[3 * n + 2]),
                   0, 0};
@@ -566,9 +818,8 @@ __global__ void k_output_precond(const bf16 *d0, const float *w5, const float *b
                                  const double *adiag, const unsigned char *bcflag, double mtol, const double *r,
                                  double *z) {
     const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const double s = block_rms(rr, nodec, false);
     if (n >= nodec) return;
-    const double ms = rr[0] / (3.0 * (double)nodec);
-    const double s = ms > 0.0 ? sqrt(ms) : 0.0;
     float f[16];
     const uint4 *p = reinterpret_cast<const uint4 *>(d0 + n * 16);
     unpack8(p[0], f);
@@ -616,9 +867,8 @@ __global__ void k_output_sym(const bf16 *d0, const bf16 *gx0, const bf16 *feat, 
                              int64_t nodec, const double *adiag, const unsigned char *bcflag, double mtol,
                              const double *r, double *z) {
     const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const double s = block_rms(rr, nodec, false);
     if (n >= nodec) return;
-    const double ms = rr[0] / (3.0 * (double)nodec);
-    const double s = ms > 0.0 ? sqrt(ms) : 0.0;
     float f[16], g[8];
     const uint4 *p = reinterpret_cast<const uint4 *>(d0 + n * 16);
     unpack8(p[0], f);
@@ -813,9 +1063,8 @@ __global__ void __launch_bounds__(RED_THREADS) k_mse(const float *z, const float
 // training pair: residual and error, both divided by the residual's RMS
 __global__ void k_append_pair(const double *r, const double *rr, const double *e, int64_t nodec, bf16 *dr, bf16 *de) {
     const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const double inv = block_rms(rr, nodec, true);
     if (n >= nodec) return;
-    const double ms = rr[0] / (3.0 * (double)nodec);
-    const double inv = ms > 0.0 ? 1.0 / sqrt(ms) : 0.0;
     for (int c = 0; c < 3; c++) {
         dr[3 * n + c] = __float2bfloat16_rn((float)(r[c * nodec + n] * inv));
         de[3 * n + c] = __float2bfloat16_rn((float)(e[c * nodec + n] * inv));
@@ -855,6 +1104,7 @@ struct mpm_nn {
     int linear = 1;     // 1: no activations and no biases (a linear operator of the input)
     int additive = 1;   // 1: preconditioner r + net(r), the network trained on (error - residual)
     int symmetric = 0;  // 1 (linear, additive): apply r + (N + N^T) r / 2
+    int halo = 1;       // forward convolutions on halo tiles (k_conv_halo); 0: per-tap gathers (k_conv_tc)
     bf16 *gx0 = nullptr;   // adjoint result at the input [v0][16]
     int64_t adam_step = 0;
     bf16 *data_r = nullptr, *data_e = nullptr;
@@ -870,6 +1120,72 @@ struct mpm_nn {
 namespace {
 
 using namespace mpm::nn;
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled from the driver (no link-time dependency on libcuda)
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        cudaGetLastError();
+    }
+    return fn;
+}
+
+// The per-chunk tensor maps of a channels-last BF16 activation [batch][z][y][x][K]
+// for the halo copies of k_conv_halo: dims (8 channels, x, y, z, sample),
+// box (8, S1 ? 10 : 18, S1 ? 18 : 33, 3, 1), x traversal stride 1 (S1) or 2 (S2).
+template <int K, int MODE>
+bool make_halo_maps(const bf16 *in, const Lvl &L, int batch, HaloMaps &m) {
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) return false;
+    const cuuint64_t dims[5] = {8, (cuuint64_t)L.n[0], (cuuint64_t)L.n[1], (cuuint64_t)L.n[2], (cuuint64_t)batch};
+    const cuuint64_t es = (cuuint64_t)K * 2;
+    const cuuint64_t strides[4] = {es, es * L.n[0], es * L.n[0] * L.n[1], es * (cuuint64_t)L.v};
+    // S2: 9 elements at stride 2 (the driver loads ceil(box / stride) elements)
+    const cuuint32_t box[5] = {8, MODE == S1 ? 10u : 18u, (cuuint32_t)Halo<MODE>::HY, 3, 1};
+    const cuuint32_t estr[5] = {1, MODE == S1 ? 1u : 2u, 1, 1, 1};
+    for (int kc = 0; kc < K / 8; kc++) {
+        CUresult r = enc(&m.m[kc], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(in) + kc * 8, dims, strides,
+                         box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return false;
+    }
+    return true;
+}
+
+template <int K, int N, int MODE>
+cudaError_t launch_conv_halo(mpm_nn *net, cudaStream_t st, const ConvArgs &a) {
+    constexpr size_t smem = halo_smem<K, N, MODE>();
+    static_assert(smem <= 227u * 1024, "shared memory");
+    HaloMaps maps;
+    memset(&maps, 0, sizeof(maps));
+    if (!make_halo_maps<K, MODE>(a.in, a.lin, (int)(a.rows / a.lout.v), maps)) return cudaErrorNotSupported;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_conv_halo<K, N, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    const int64_t ntile = (int64_t)(a.rows / a.lout.v) * ((a.lout.n[0] + 7) / 8) * ((a.lout.n[1] + 15) / 16) *
+                          a.lout.n[2];
+    const int per_sm = std::max<int>(1, std::min<int>(4, (int)(225000 / (smem + 1024))));
+    const int grid = (int)std::min<int64_t>(ntile, (int64_t)net->nsm * per_sm);
+    if (grid <= 0) return cudaSuccess;
+    k_conv_halo<K, N, MODE><<<grid, 128, smem, st>>>(a, maps);
+    return cudaGetLastError();
+}
 
 template <int K, int N, int MODE>
 cudaError_t launch_conv(mpm_nn *net, cudaStream_t st, const bf16 *in, bf16 *out, const bf16 *w, const float *bias,
@@ -894,6 +1210,9 @@ cudaError_t launch_conv(mpm_nn *net, cudaStream_t st, const bf16 *in, bf16 *out,
     a.lout = lout;
     a.rows = (int64_t)batch * lout.v;
     a.err = net->err;
+    if constexpr (MODE == S1 || MODE == S2) {
+        if (net->halo) return launch_conv_halo<K, N, MODE>(net, st, a);
+    }
     const int64_t ntile = (a.rows + 127) / 128;
     const int per_sm = std::max<int>(1, std::min<int>(4, (int)(220000 / smem)));
     const int grid = (int)std::min<int64_t>(ntile, (int64_t)net->nsm * per_sm);
@@ -1121,6 +1440,7 @@ mpm_status mpm_nn_create(const int nodes[3], int max_batch, int64_t max_pairs, m
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&n->nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (const char *g = getenv("MPM_GB300_CONV_GATHER")) n->halo = atoi(g) ? 0 : 1;
     const int64_t P = param_count();
     const int64_t B = max_batch, v0 = n->L[0].v, v1 = n->L[1].v, v2 = n->L[2].v;
     auto fail = [&](cudaError_t e) {
