@@ -244,8 +244,23 @@ def run_implicit(args, torch, stream):
         ms = max(ev0.elapsed_time(ev1), (time.perf_counter() - t0) * 1e3) / args.implicit_steps
         return ms, st
 
+    def timed_solve(gpu, reps=3):
+        """The linear solve alone: the system of the solid's current state, assembled
+        once, solved from x = 0 to the same tolerance `reps` times."""
+        gpu.assemble()
+        gpu.solve(eps=1.0e-16, download=False)       # warm-up (graphs captured)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        t0 = time.perf_counter()
+        its = [gpu.solve(eps=1.0e-16, download=False)[1] for _ in range(reps)]
+        ev1.record(stream)
+        ev1.synchronize()
+        return max(ev0.elapsed_time(ev1), (time.perf_counter() - t0) * 1e3) / reps, its[-1]
+
     gpu = capi.GpuImplicitSolid(s, nr_flag=True, stream=stream.cuda_stream)
     jac_ms, jac = timed(gpu)
+    jac_solve_ms, jac_solve_it = timed_solve(gpu)
     gpu.close()
     out = {"metric": "implicit step time", "value": jac_ms, "unit": "ms/step", "higher_is_better": False,
            "steps": args.implicit_steps, "particles": s.num, "grid": list(s.xyelem), "dtype": "f64",
@@ -263,6 +278,7 @@ def run_implicit(args, torch, stream):
     gpu = capi.GpuImplicitSolid(s, nr_flag=True, stream=stream.cuda_stream)
     gpu.set_precond(net)
     nn_ms, nn = timed(gpu)
+    nn_solve_ms, nn_solve_it = timed_solve(gpu)
     gpu.close()
     net.close()
     out["learned"] = {"value": nn_ms, "unit": "ms/step",
@@ -274,6 +290,11 @@ def run_implicit(args, torch, stream):
                       "fallbacks": nn["precond_fallbacks"], "network_applications": nn["nn_applications"],
                       "training": training,
                       "speedup_vs_jacobi": jac_ms / nn_ms if nn_ms > 0 else None}
+    out["solve"] = {"what": "one linear solve of the assembled system after the timed steps, from x = 0 to "
+                            "||r||/||r0|| <= 1e-8, solution left on the device",
+                    "jacobi_ms": jac_solve_ms, "jacobi_iters": jac_solve_it,
+                    "learned_ms": nn_solve_ms, "learned_iters": nn_solve_it,
+                    "speedup": jac_solve_ms / nn_solve_ms if nn_solve_ms > 0 else None}
     return out
 
 

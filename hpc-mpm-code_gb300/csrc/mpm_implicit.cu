@@ -855,19 +855,41 @@ __device__ __forceinline__ int gcr_prev(int slot, int j) { return (slot - 1 - j 
 // true in the last block to finish (the blocks count themselves on *cnt),
 // which then reduces the partials in block order (last_sum), so the sums
 // are reproducible without a separate reduction launch.
+// Warp sums of V values (V a power of two <= 32) with the values spread over
+// the lanes as the butterfly goes: at each of the first log2(V) steps a lane
+// keeps half of its values and adds its partner's copy of that half, so a
+// lane adds 2V - 1 + log2(32 / V) numbers instead of 5 V.  FP64 adds are the
+// scarce resource on this part.  Returns the value index whose warp total the
+// lane holds in v[0] (every lane of a group of 32 / V lanes holds it).
 template <int V>
-__device__ __forceinline__ bool partials_last(const double (&v)[V], int nv, double *part, unsigned *cnt) {
+__device__ __forceinline__ int warp_sums(double (&v)[V]) {
+    const int lane = threadIdx.x & 31;
+    int j = 0, o = 16;
+#pragma unroll
+    for (int h = V / 2; h >= 1; h /= 2, o >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < h; i++) {
+            const double send = up ? v[i] : v[i + h];
+            const double keep = up ? v[i + h] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+        if (up) j += h;
+    }
+    for (; o >= 1; o >>= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
+    return j;
+}
+
+template <int V>
+__device__ __forceinline__ bool partials_last(const double (&vin)[V], int nv, double *part, unsigned *cnt) {
     __shared__ double sh[V][8];
     __shared__ bool s_last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double v[V];
 #pragma unroll
-    for (int j = 0; j < V; j++) {
-        if (j < nv) {
-            double x = v[j];
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-            if (lane == 0) sh[j][wid] = x;
-        }
-    }
+    for (int j = 0; j < V; j++) v[j] = vin[j];
+    const int j = warp_sums<V>(v);
+    if ((lane & (32 / V - 1)) == 0) sh[j][wid] = v[0];
     __syncthreads();
     if ((int)threadIdx.x < nv) {
         double t = 0.0;

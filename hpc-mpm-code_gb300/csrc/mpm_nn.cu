@@ -93,13 +93,16 @@ __device__ __forceinline__ int64_t gather_src(int b, int ox, int oy, int oz, int
     return (int64_t)b * in.v + ix + (int64_t)in.n[0] * (iy + (int64_t)in.n[1] * iz);
 }
 
+// (sample, x, y, z) of a row; rows are below 2^31 (checked when the network
+// is created), so 32-bit divisions do
 __device__ __forceinline__ void row_coords(int64_t row, const Lvl &L, int &b, int &x, int &y, int &z) {
-    b = (int)(row / L.v);
-    const int64_t v = row - (int64_t)b * L.v;
-    x = (int)(v % L.n[0]);
-    const int64_t q = v / L.n[0];
-    y = (int)(q % L.n[1]);
-    z = (int)(q / L.n[1]);
+    const int r = (int)row, lv = (int)L.v;
+    b = r / lv;
+    const int v = r - b * lv;
+    const int q = v / L.n[0];
+    x = v - q * L.n[0];
+    z = q / L.n[1];
+    y = q - z * L.n[1];
 }
 
 __device__ __forceinline__ void unpack8(const uint4 &u, float *f) {
@@ -173,24 +176,27 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a) {
     constexpr uint32_t IDESC = tc::idesc_bf16(128, N);
     constexpr uint32_t SBO = K * 16;
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ unsigned long long bar[2];
+    __shared__ unsigned long long bar[2], wbar;
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, warp = tid >> 5;
     if (warp == 0) tc::tmem_alloc(&tslot, TCOLS);
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
+        mbar_init(&wbar, 1);
         fence_mbar_init();
     }
-    {
-        const uint4 *src = reinterpret_cast<const uint4 *>(a.w);
-        uint4 *dst = reinterpret_cast<uint4 *>(smem);
-        for (uint32_t i = tid; i < WB / 16; i += 128) dst[i] = __ldg(src + i);
-    }
-    tc::fence_async_smem();
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
+    // the 27 weight tiles by bulk copies, waited for before the first MMA
+    if (tid == 0) {
+        mbar_expect_tx(&wbar, WB);
+        constexpr uint32_t WCH = 32768;
+        for (uint32_t o = 0; o < WB; o += WCH)
+            bulk_g2s(smem + o, reinterpret_cast<const unsigned char *>(a.w) + o, WB - o < WCH ? WB - o : WCH, &wbar);
+    }
+    bool wready = false;
     const uint32_t taddr = tslot;
     const uint32_t sw = smem_addr(smem), sa = sw + WB;
     // this thread's row inside a tap tile: (row / 8) * SBO + (row % 8) * 16
@@ -223,6 +229,13 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a) {
             cp_async_commit_wait();
             tc::fence_async_smem();
             tc::fence_before();
+            if (!wready) {
+                wready = true;
+                if (!__syncthreads_and(mbar_wait_bounded(&wbar, 0, TC_WAIT))) {
+                    ok = false;
+                    break;
+                }
+            }
             __syncthreads();
             if (tid == 0) {
                 tc::fence_after();
@@ -290,7 +303,9 @@ __global__ void __launch_bounds__(128) k_conv_tc(ConvArgs a) {
     if (!ok) {
         if (tid == 0) atomicAdd(a.err, 1);
         if (it > 0) mbar_wait_bounded(&bar[(it - 1) & 1], ((it - 1) >> 1) & 1, TC_WAIT);
+        mbar_wait_bounded(&wbar, 0, TC_WAIT);
     }
+    if (!wready) mbar_wait_bounded(&wbar, 0, TC_WAIT);   // a block without tiles still lets its copy land
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
@@ -369,7 +384,7 @@ __global__ void __launch_bounds__(128) k_conv_halo(ConvArgs a, const __grid_cons
     constexpr uint32_t TCOLS = N < 32 ? 32 : N;
     constexpr uint32_t IDESC = tc::idesc_bf16(128, N);
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ unsigned long long bar, full[2];
+    __shared__ unsigned long long bar, full[2], wbar;
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, warp = tid >> 5;
     // halo buffers first, 128-byte aligned (tensor copy destinations), then the weights
@@ -381,17 +396,21 @@ __global__ void __launch_bounds__(128) k_conv_halo(ConvArgs a, const __grid_cons
         mbar_init(&bar, 1);
         mbar_init(&full[0], 1);
         mbar_init(&full[1], 1);
+        mbar_init(&wbar, 1);
         fence_mbar_init();
     }
-    {
-        const uint4 *src = reinterpret_cast<const uint4 *>(a.w);
-        uint4 *dst = reinterpret_cast<uint4 *>(smem + NBUF * HB);
-        for (uint32_t i = tid; i < WB / 16; i += 128) dst[i] = __ldg(src + i);
-    }
-    tc::fence_async_smem();
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
+    // the 27 weight tiles by bulk copies (one thread, in flight with the
+    // first halo copy; waited for before the first MMA)
+    if (tid == 0) {
+        mbar_expect_tx(&wbar, WB);
+        constexpr uint32_t WCH = 32768;
+        for (uint32_t o = 0; o < WB; o += WCH)
+            bulk_g2s(smem + NBUF * HB + o, reinterpret_cast<const unsigned char *>(a.w) + o, WB - o < WCH ? WB - o : WCH,
+                     &wbar);
+    }
     const uint32_t taddr = tslot;
     const int ntx = (a.lout.n[0] + H::TX - 1) / H::TX, nty = (a.lout.n[1] + H::TY - 1) / H::TY;
     const int64_t per_b = (int64_t)ntx * nty * a.lout.n[2];
@@ -428,6 +447,8 @@ __global__ void __launch_bounds__(128) k_conv_halo(ConvArgs a, const __grid_cons
         if (tid == 0) issue(tile, 0);
         iss0++;
     }
+    ok = __syncthreads_and(mbar_wait_bounded(&wbar, 0, TC_WAIT));
+    if (!ok) tile = ntile;
     for (; tile < ntile; tile += gridDim.x, i++) {
         const int buf = NBUF == 2 ? (int)(i & 1) : 0;
         const int64_t next = tile + gridDim.x;
@@ -525,6 +546,7 @@ __global__ void __launch_bounds__(128) k_conv_halo(ConvArgs a, const __grid_cons
             // let every copy still in flight land before the block exits
             if (iss0 > con0) mbar_wait_bounded(&full[0], (iss0 - 1u) & 1u, TC_WAIT);
             if (iss1 > con1) mbar_wait_bounded(&full[1], (iss1 - 1u) & 1u, TC_WAIT);
+            mbar_wait_bounded(&wbar, 0, TC_WAIT);
         }
         if (mma_pending) mbar_wait_bounded(&bar, i & 1, TC_WAIT);
     }
@@ -829,6 +851,50 @@ __global__ void k_output_precond(const bf16 *d0, const float *w5, const float *b
         float o = b5 ? b5[c] : 0.0f;
 #pragma unroll
         for (int k = 0; k < 16; k++) o += f[k] * w5[k * 3 + c];
+        const int64_t i = c * nodec + n;
+        const bool off = (bf & (1 << c)) || !(adiag[i] >= mtol);
+        z[i] = off ? 0.0 : (r ? r[i] : 0.0) + s * (double)o;
+    }
+}
+
+// Linear network: the last prolongation, skip addition and output layer in
+// one pass, z = r + s * W5^T (e0 + up(c1)), without storing d0; zero on
+// inactive and boundary rows.
+__global__ void k_output_up(const bf16 *c1, const bf16 *e0, const float *w5, const double *rr, Lvl lf, Lvl lc,
+                            const double *adiag, const unsigned char *bcflag, double mtol, const double *r, double *z) {
+    __shared__ float sw5[48];
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (threadIdx.x < 48) sw5[threadIdx.x] = w5[threadIdx.x];
+    const double s = block_rms(rr, lf.v, false);
+    if (n >= lf.v) return;
+    const int64_t nodec = lf.v;
+    float f[16];
+    {
+        const uint4 *p = reinterpret_cast<const uint4 *>(e0 + n * 16);
+        unpack8(__ldg(p), f);
+        unpack8(__ldg(p + 1), f + 8);
+    }
+    int b_, x, y, zz;
+    row_coords(n, lf, b_, x, y, zz);
+    const int lo[3] = {x >> 1, y >> 1, zz >> 1}, nn[3] = {(x & 1) ? 2 : 1, (y & 1) ? 2 : 1, (zz & 1) ? 2 : 1};
+    const float w = (nn[0] == 2 ? 0.5f : 1.0f) * (nn[1] == 2 ? 0.5f : 1.0f) * (nn[2] == 2 ? 0.5f : 1.0f);
+    for (int k = 0; k < nn[2]; k++)
+        for (int j = 0; j < nn[1]; j++)
+            for (int i = 0; i < nn[0]; i++) {
+                const int64_t src = (lo[0] + i) + (int64_t)lc.n[0] * ((lo[1] + j) + (int64_t)lc.n[1] * (lo[2] + k));
+                const uint4 *p = reinterpret_cast<const uint4 *>(c1 + src * 16);
+                float g[16];
+                unpack8(__ldg(p), g);
+                unpack8(__ldg(p + 1), g + 8);
+#pragma unroll
+                for (int e = 0; e < 16; e++) f[e] += w * g[e];
+            }
+    const unsigned char bf = bcflag[n];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        float o = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 16; k++) o += f[k] * sw5[k * 3 + c];
         const int64_t i = c * nodec + n;
         const bool off = (bf & (1 << c)) || !(adiag[i] >= mtol);
         z[i] = off ? 0.0 : (r ? r[i] : 0.0) + s * (double)o;
@@ -1269,7 +1335,7 @@ cudaError_t prep_weights(mpm_nn *net, cudaStream_t st) {
 }
 
 // forward of `batch` samples whose x0 is already in place
-cudaError_t forward(mpm_nn *net, cudaStream_t st, int batch) {
+cudaError_t forward(mpm_nn *net, cudaStream_t st, int batch, bool make_d0 = true) {
     cudaError_t e = prep_weights(net, st);
     if (e != cudaSuccess) return e;
     const Lvl &L0 = net->L[0], &L1 = net->L[1], &L2 = net->L[2];
@@ -1293,7 +1359,7 @@ cudaError_t forward(mpm_nn *net, cudaStream_t st, int batch) {
     if ((e = launch_conv<32, 16, S1>(net, st, net->d1, net->c1, net->wf[4], bias(4), nullptr, nullptr, 0, L1, L1,
                                      batch)) != cudaSuccess)
         return e;
-    k_up_add_relu<16><<<blocks(r0 * 2), 256, 0, st>>>(net->c1, net->e0, net->d0, L0, L1, r0, act);
+    if (make_d0) k_up_add_relu<16><<<blocks(r0 * 2), 256, 0, st>>>(net->c1, net->e0, net->d0, L0, L1, r0, act);
     return cudaGetLastError();
 }
 
@@ -1428,6 +1494,8 @@ mpm_status mpm_nn_create(const int nodes[3], int max_batch, int64_t max_pairs, m
     if (!nodes || !out || max_batch < 1 || max_pairs < 0) return MPM_ERR_BAD_ARG;
     for (int d = 0; d < 3; d++)
         if (nodes[d] < 3) return MPM_ERR_BAD_ARG;
+    // row indices of a batch are 32-bit on the device
+    if ((int64_t)nodes[0] * nodes[1] * nodes[2] * (int64_t)max_batch >= ((int64_t)1 << 31)) return MPM_ERR_BAD_ARG;
     mpm_nn *n = new (std::nothrow) mpm_nn();
     if (!n) return MPM_ERR_OOM;
     for (int d = 0; d < 3; d++) {
@@ -1657,6 +1725,13 @@ mpm_status mpm_nn_apply_precond(mpm_nn *net, cudaStream_t st, const double *r, c
                                 const unsigned char *bcflag, double mtol, double *z) {
     const int64_t nodec = net->L[0].v;
     k_input_r<<<blocks(nodec), 256, 0, st>>>(r, rr, net->feat, nodec, net->linear, net->x0);
+    if (net->linear && !net->symmetric) {
+        CKN(forward(net, st, 1, false));
+        k_output_up<<<blocks(nodec), 256, 0, st>>>(net->c1, net->e0, net->p + w5_offset(), rr, net->L[0], net->L[1],
+                                                   adiag, bcflag, mtol, net->additive ? r : nullptr, z);
+        CKN(cudaGetLastError());
+        return MPM_OK;
+    }
     CKN(forward(net, st, 1));
     if (net->symmetric && net->linear && net->additive) {
         k_adj_seed<<<blocks(nodec), 256, 0, st>>>(net->x0, net->gz, nodec);

@@ -337,10 +337,13 @@ class GpuImplicitSolid(GpuSolid):
         _chk(self.lib.mpm_gpu_implicit_matvec(self.ctx, _ptr(x), _ptr(y)), "mpm_gpu_implicit_matvec")
         return y
 
-    def solve(self, eps=1.0e-8, kmax=10000):
-        x = np.zeros(3 * self.nodec)
+    def solve(self, eps=1.0e-8, kmax=10000, download=True):
+        """One linear solve of the assembled system from x = 0; returns (x, iterations),
+        x None with download=False (the solution stays on the device)."""
+        x = np.zeros(3 * self.nodec) if download else None
         it = C.c_int(0)
-        _chk(self.lib.mpm_gpu_implicit_solve(self.ctx, eps, kmax, _ptr(x), C.byref(it)), "mpm_gpu_implicit_solve")
+        _chk(self.lib.mpm_gpu_implicit_solve(self.ctx, eps, kmax, _ptr(x) if download else None, C.byref(it)),
+             "mpm_gpu_implicit_solve")
         return x, it.value
 
 
