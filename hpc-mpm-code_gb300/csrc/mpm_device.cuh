@@ -166,9 +166,10 @@ __device__ __forceinline__ void atomic_max_pos(unsigned int *slot, float v) {
 // MatLinElast (constitutive_model.cpp:16-60): incremental, engineering shear.
 template <typename R>
 __device__ __forceinline__ void lin_elast_update(R *s, const R D[3][3], R E, R nu) {
-    R C0 = E * ((R)1 - nu) / (((R)1 - (R)2 * nu) * ((R)1 + nu));
-    R C1 = E * nu / (((R)1 - (R)2 * nu) * ((R)1 + nu));
-    R C2 = E / ((R)2 * ((R)1 + nu));
+    const R rd = (R)1 / (((R)1 - (R)2 * nu) * ((R)1 + nu));   // one division (FP64 divisions are slow here)
+    const R C0 = E * ((R)1 - nu) * rd;
+    const R C1 = E * nu * rd;
+    const R C2 = (R)0.5 * E * ((R)1 - (R)2 * nu) * rd;
     R e0 = D[0][0], e1 = D[1][1], e2 = D[2][2];
     R e3 = D[1][2] + D[2][1], e4 = D[2][0] + D[0][2], e5 = D[0][1] + D[1][0];
     s[0] += C0 * e0 + C1 * e1 + C1 * e2;
@@ -180,22 +181,28 @@ __device__ __forceinline__ void lin_elast_update(R *s, const R D[3][3], R E, R n
 }
 
 // MatNeoHookean (constitutive_model.cpp:62-125), stress part.
+// One division for the Lame constants and one for 1/J: FP64 divisions are
+// expensive on this part (tens of FP64-pipe operations each).  Returns
+// log(J) for callers that need it again (the tangent of the implicit solid).
 template <typename R>
-__device__ __forceinline__ void neo_hookean_stress(R *s, const R F[3][3], R jac, R E, R nu) {
-    R lmd = nu * E / (((R)1 + nu) * ((R)1 - (R)2 * nu));
-    R mu = E / ((R)2 * ((R)1 + nu));
-    R lnj = log(jac);
+__device__ __forceinline__ R neo_hookean_stress(R *s, const R F[3][3], R jac, R E, R nu) {
+    const R rd = (R)1 / (((R)1 + nu) * ((R)1 - (R)2 * nu));
+    const R lmd = nu * E * rd;
+    const R mu = (R)0.5 * E * ((R)1 - (R)2 * nu) * rd;
+    const R lnj = log(jac);
+    const R ij = (R)1 / jac;
     R be[3][3];
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int j = 0; j < 3; j++) be[i][j] = F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2];
-    s[0] = (mu * (be[0][0] - (R)1) + lmd * lnj) / jac;
-    s[1] = (mu * (be[1][1] - (R)1) + lmd * lnj) / jac;
-    s[2] = (mu * (be[2][2] - (R)1) + lmd * lnj) / jac;
-    s[3] = (mu * be[1][2]) / jac;
-    s[4] = (mu * be[0][2]) / jac;
-    s[5] = (mu * be[0][1]) / jac;
+    s[0] = (mu * (be[0][0] - (R)1) + lmd * lnj) * ij;
+    s[1] = (mu * (be[1][1] - (R)1) + lmd * lnj) * ij;
+    s[2] = (mu * (be[2][2] - (R)1) + lmd * lnj) * ij;
+    s[3] = (mu * be[1][2]) * ij;
+    s[4] = (mu * be[0][2]) * ij;
+    s[5] = (mu * be[0][1]) * ij;
+    return lnj;
 }
 
 // The same stress from the displacement gradient H = F - I and jm1 = J - 1,

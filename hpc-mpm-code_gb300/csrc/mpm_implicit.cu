@@ -70,6 +70,7 @@ struct ImpState {
     mpm_nn *g_net = nullptr;
     bool no_graph = false;
     bool gcr = true;      // learned preconditioner: flexible GCR first (else flexible CG only)
+    int gm = 8;           // GCR window in use (1, 2, 4 or 8 <= GM directions)
     bool debug = false;   // MPM_GB300_KRYLOV_TRACE set: residual history to stderr
 };
 
@@ -83,7 +84,7 @@ struct ImpArgs {
     int nnc[3];
     int nel[3];
     int nodec;
-    double xmin[3], dx[3];
+    double xmin[3], dx[3], inv_dx[3];
     double dt, facl, mtol, grav[3];
     double af, am, gamma, nb[6];
     int nr_flag;
@@ -110,6 +111,7 @@ static ImpArgs imp_args(mpm_ctx *c) {
         a.nel[d] = c->g.nel[d];
         a.xmin[d] = c->g.xmin[d];
         a.dx[d] = c->g.dx[d];
+        a.inv_dx[d] = 1.0 / c->g.dx[d];
         a.grav[d] = c->gravity[d];
     }
     a.nodec = c->g.nodec;
@@ -168,7 +170,7 @@ __device__ __forceinline__ void shape8(const ImpArgs &a, const double *x, int &c
     for (int d = 0; d < 3; d++) {
         g.xmin[d] = a.xmin[d];
         g.dx[d] = a.dx[d];
-        g.inv_dx[d] = 1.0 / a.dx[d];
+        g.inv_dx[d] = a.inv_dx[d];
         g.nel[d] = a.nel[d];
         g.nnc[d] = a.nnc[d];
     }
@@ -254,9 +256,12 @@ __global__ void __launch_bounds__(128) k_imp_assemble(ImpArgs a, PView P, const 
     for (int q = 0; q < 8; q++)
         for (int r = 0; r < 3; r++) {
             const double u = ndispl[r * N + nid[q]];
-            for (int c = 0; c < 3; c++) d[r][c] += dN[q][c] * a.af * u;
+            for (int c = 0; c < 3; c++) d[r][c] += dN[q][c] * u;
         }
-    for (int r = 0; r < 3; r++) d[r][r] += 1.0;
+    for (int r = 0; r < 3; r++) {
+        for (int c = 0; c < 3; c++) d[r][c] *= a.af;
+        d[r][r] += 1.0;
+    }
     double F[3][3], Fn[3][3];
     for (int r = 0; r < 3; r++)
         for (int c = 0; c < 3; c++) F[r][c] = P.F[3 * r + c][p];
@@ -283,11 +288,13 @@ __global__ void __launch_bounds__(128) k_imp_assemble(ImpArgs a, PView P, const 
         lam = E * nu / ((1.0 - 2.0 * nu) * (1.0 + nu));
         mu = E / (2.0 * (1.0 + nu));
     } else if (model == 1) {
-        neo_hookean_stress(sk, Fn, J, E, nu);
-        const double lmd = nu * E / ((1.0 + nu) * (1.0 - 2.0 * nu));
-        const double mu0 = E / (2.0 * (1.0 + nu));
-        lam = lmd / J;
-        mu = (mu0 - lmd * log(J)) / J;
+        const double lnj = neo_hookean_stress(sk, Fn, J, E, nu);
+        const double rd = 1.0 / ((1.0 + nu) * (1.0 - 2.0 * nu));
+        const double lmd = nu * E * rd;
+        const double mu0 = 0.5 * E * (1.0 - 2.0 * nu) * rd;
+        const double ij = 1.0 / J;
+        lam = lmd * ij;
+        mu = (mu0 - lmd * lnj) * ij;
     } else {
         for (int k = 0; k < 6; k++) sk[k] = 0.0;
     }
@@ -511,13 +518,23 @@ __global__ void k_cg_init(ImpArgs a, const double *Ax, double *r, double *p, dou
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
+// num / den (0 when den is 0 or `zero`) evaluated by one thread of the block
+// and shared: an FP64 division costs tens of FP64-pipe operations on this
+// part, too many to repeat in every thread.  Every thread of the block must
+// call it (it synchronises the block), at most once per kernel.
+__device__ __forceinline__ double block_div(double num, double den, bool zero = false) {
+    __shared__ double s_q;
+    if (threadIdx.x == 0) s_q = (zero || den == 0.0) ? 0.0 : num / den;
+    __syncthreads();
+    return s_q;
+}
+
 // x += alpha p, r -= alpha Ap, partial r.r;  alpha = rr_cur / pAp
 __global__ void k_cg_update(ImpArgs a, const double *scal, int cur, double *x, double *r, const double *p,
                             const double *Ap, double *part) {
     __shared__ double sh[32];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    const double pap = scal[S_PAP];
-    const double alpha = pap != 0.0 ? scal[cur] / pap : 0.0;
+    const double alpha = block_div(scal[cur], scal[S_PAP]);
     double dot = 0.0;
     if (n < a.nodec) {
         const size_t N = (size_t)a.nodec;
@@ -536,9 +553,8 @@ __global__ void k_cg_update(ImpArgs a, const double *scal, int cur, double *x, d
 // p = r + beta p;  beta = rr_new / rr_cur
 __global__ void k_cg_dir(ImpArgs a, const double *scal, int cur, const double *r, double *p) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const double beta = block_div(scal[cur ^ 1], scal[cur]);
     if (n >= a.nodec) return;
-    const double rc = scal[cur];
-    const double beta = rc != 0.0 ? scal[cur ^ 1] / rc : 0.0;
     const size_t N = (size_t)a.nodec;
     for (int c = 0; c < 3; c++) {
         const size_t i = c * N + n;
@@ -701,10 +717,9 @@ __global__ void __launch_bounds__(128) k_imp_g2p(ImpArgs a, PView P, const doubl
 // x += -b0 geup, b0 = eu / gd unless gd < mtol (material_point.cpp:219-225)
 __global__ void k_imp_shift(ImpArgs a, PView P, const double *geup, const double *scal) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.num || !a.shifting) return;
     const double gd = scal[S_GD];
-    const double b0 = gd < a.mtol ? 0.0 : scal[S_EU] / gd;
-    if (b0 == 0.0) return;
+    const double b0 = block_div(scal[S_EU], gd, gd < a.mtol);
+    if (p >= a.num || !a.shifting || b0 == 0.0) return;
     const size_t NP = (size_t)a.num;
     for (int c = 0; c < 3; c++) P.x[c][p] += -b0 * geup[c * NP + p];
 }
@@ -728,8 +743,7 @@ __global__ void k_fcg_dir(ImpArgs a, const double *scal, int restart, const doub
                           double *part) {
     __shared__ double sh[32];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    const double pq = scal[S_PAP];
-    const double beta = (restart || pq == 0.0) ? 0.0 : -scal[S_ZQ] / pq;
+    const double beta = block_div(-scal[S_ZQ], scal[S_PAP], restart != 0);
     double d = 0.0;
     if (n < a.nodec) {
         const size_t N = (size_t)a.nodec;
@@ -749,8 +763,7 @@ __global__ void k_fcg_update(ImpArgs a, const double *scal, double *x, double *r
                              double *part) {
     __shared__ double sh[32];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    const double pq = scal[S_PAP];
-    const double alpha = pq != 0.0 ? scal[S_PR] / pq : 0.0;
+    const double alpha = block_div(scal[S_PR], scal[S_PAP]);
     double d = 0.0;
     if (n < a.nodec) {
         const size_t N = (size_t)a.nodec;
@@ -848,7 +861,8 @@ __global__ void k_set_modulus(double *matprop, int nmat, double E) {
 }
 
 // ------------------------------------------------ flexible GCR(GM)
-__device__ __forceinline__ int gcr_prev(int slot, int j) { return (slot - 1 - j + 2 * GM) % GM; }
+// slot of the direction kept j + 1 iterations before the one in `slot` (ring of w)
+__device__ __forceinline__ int gcr_prev(int slot, int j, int w) { return (slot - 1 - j + 2 * w) % w; }
 
 // partial dots q . Q_j with the `used` previous images (j = 0 the newest)
 // Per-block partial sums of nv (<= V) values into part[j * gridDim.x + b];
@@ -913,7 +927,7 @@ __device__ __forceinline__ double last_sum(const double *part, int j, double *sh
 
 // flexible GCR: the dots q . Q_j of the new image with the kept ones, then
 // (last block) beta_j = (q . Q_j) / (Q_j . Q_j)
-__global__ void __launch_bounds__(256) k_gcr_dots(ImpArgs a, const double *Q, int slot, int used, double *part,
+__global__ void __launch_bounds__(256) k_gcr_dots(ImpArgs a, const double *Q, int slot, int used, int w, double *part,
                                                   unsigned *cnt, const double *qq, double *beta) {
     __shared__ double sh[32];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -927,7 +941,7 @@ __global__ void __launch_bounds__(256) k_gcr_dots(ImpArgs a, const double *Q, in
 #pragma unroll
         for (int j = 0; j < GM; j++)
             if (j < used) {
-                const double *qj = Q + (size_t)gcr_prev(slot, j) * st;
+                const double *qj = Q + (size_t)gcr_prev(slot, j, w) * st;
                 d[j] = q0 * qj[n] + q1 * qj[N + n] + q2 * qj[2 * N + n];
             }
     }
@@ -935,7 +949,7 @@ __global__ void __launch_bounds__(256) k_gcr_dots(ImpArgs a, const double *Q, in
     for (int j = 0; j < used; j++) {
         const double t = last_sum(part, j, sh);
         if (threadIdx.x == 0) {
-            const double dq = qq[gcr_prev(slot, j)];
+            const double dq = qq[gcr_prev(slot, j, w)];
             beta[j] = dq > 0.0 ? t / dq : 0.0;
         }
     }
@@ -943,7 +957,7 @@ __global__ void __launch_bounds__(256) k_gcr_dots(ImpArgs a, const double *Q, in
 }
 
 // p -= sum beta_j P_j, q -= sum beta_j Q_j; then (last block) q.r and q.q
-__global__ void __launch_bounds__(256) k_gcr_axpy(ImpArgs a, double *P, double *Q, int slot, int used,
+__global__ void __launch_bounds__(256) k_gcr_axpy(ImpArgs a, double *P, double *Q, int slot, int used, int w,
                                                   const double *beta, const double *r, double *part, unsigned *cnt,
                                                   double *scal) {
     __shared__ double sh[32];
@@ -961,7 +975,7 @@ __global__ void __launch_bounds__(256) k_gcr_axpy(ImpArgs a, double *P, double *
 #pragma unroll
             for (int j = 0; j < GM; j++)
                 if (j < used) {
-                    const size_t o = (size_t)gcr_prev(slot, j) * st + i;
+                    const size_t o = (size_t)gcr_prev(slot, j, w) * st + i;
                     pv -= bj[j] * P[o];
                     qv -= bj[j] * Q[o];
                 }
@@ -990,7 +1004,7 @@ __global__ void __launch_bounds__(256) k_gcr_update(ImpArgs a, double *scal, dou
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const size_t N = (size_t)a.nodec, st = 3 * N;
     const double dqq = scal[S_QQ];
-    const double alpha = dqq > 0.0 ? scal[S_QR] / dqq : 0.0;
+    const double alpha = block_div(scal[S_QR], dqq, !(dqq > 0.0));
     if (blockIdx.x == 0 && threadIdx.x == 0) qq[slot] = dqq;
     double v[1] = {0.0};
     if (n < a.nodec) {
@@ -1074,6 +1088,10 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
     c->imp = s;
     s->debug = getenv("MPM_GB300_KRYLOV_TRACE") != nullptr;
     s->gcr = getenv("MPM_GB300_FCG_ONLY") == nullptr;
+    if (const char *w = getenv("MPM_GB300_GCR_WINDOW")) {
+        const int v = atoi(w);
+        if (v == 1 || v == 2 || v == 4 || v == 8) s->gm = v;   // divides the 8 iterations of a graph launch
+    }
     s->nr_flag = nr_flag ? 1 : 0;
     // GeneralizedAlphaParaSet + NewmarkBetaParaSet (nonlinear_time_integration.cpp:10-56), second order
     double t = 1.0 + spec_rad;
@@ -1247,8 +1265,9 @@ static mpm_status gcr_iter(mpm_ctx *c, const ImpArgs &a, int nb, int u, int sl) 
     timer_end(c, K_MATVEC);
     timer_begin(c, K_KRYLOV);
     if (u > 0)
-        k_gcr_dots<<<nb, 256, 0, c->stream>>>(a, s->gq, sl, u, s->part, s->cnt, s->gqq, s->gbeta);
-    k_gcr_axpy<<<nb, 256, 0, c->stream>>>(a, s->gp, s->gq, sl, u, s->gbeta, s->r, s->part, s->cnt + 1, s->scal);
+        k_gcr_dots<<<nb, 256, 0, c->stream>>>(a, s->gq, sl, u, s->gm, s->part, s->cnt, s->gqq, s->gbeta);
+    k_gcr_axpy<<<nb, 256, 0, c->stream>>>(a, s->gp, s->gq, sl, u, s->gm, s->gbeta, s->r, s->part, s->cnt + 1,
+                                          s->scal);
     k_gcr_update<<<nb, 256, 0, c->stream>>>(a, s->scal, s->xs, s->r, s->gp, s->gq, sl, s->gqq, s->part,
                                             s->cnt + 2);
     timer_end(c, K_KRYLOV);
@@ -1339,10 +1358,10 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
         double rr_win = rr0;
         auto gcr_iteration = [&](int u, int sl) -> mpm_status { return gcr_iter(c, a, nb, u, sl); };
         while (!done && use_nn && it < kmax) {
-            if (graphs_on(c) && used == GM && slot == 0 && it % check == 0 && it + check <= kmax) {
+            if (graphs_on(c) && used == s->gm && slot == 0 && it % check == 0 && it + check <= kmax) {
                 const int64_t l0 = c->launches;
                 if (!s->g_gcr && capture_iters(c, &s->g_gcr, [&] {
-                        for (int k = 0; k < check; k++) gcr_iteration(GM, k % GM);
+                        for (int k = 0; k < check; k++) gcr_iteration(s->gm, k % s->gm);
                     }) != MPM_OK)
                     s->no_graph = true;
                 if (!s->g_gcr) continue;
@@ -1355,8 +1374,8 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
                 mpm_status st = gcr_iteration(used, slot);
                 if (st != MPM_OK) return st;
                 s->nn_applications++;
-                used = used < GM ? used + 1 : GM;
-                slot = (slot + 1) % GM;
+                used = used < s->gm ? used + 1 : s->gm;
+                slot = (slot + 1) % s->gm;
                 it++;
             }
             if (it % check == 0 || it == kmax) {
@@ -1750,8 +1769,8 @@ static mpm_status gcr_record(mpm_ctx *c, mpm_nn *rec, int npairs) {
         if (st != MPM_OK) return st;
         st = gcr_iter(c, a, nb, used, slot);
         if (st != MPM_OK) return st;
-        used = used < GM ? used + 1 : GM;
-        slot = (slot + 1) % GM;
+        used = used < s->gm ? used + 1 : s->gm;
+        slot = (slot + 1) % s->gm;
     }
     return check_launch(c);
 }

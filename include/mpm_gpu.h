@@ -207,7 +207,8 @@ mpm_status mpm_gpu_implicit_step(mpm_ctx *ctx, int nsteps, double facl, double e
  * get_system: stencil values [27][9][nodec] (slot s = (dx+1)+3(dy+1)+9(dz+1),
  * entry 3a+b), D^-1/2 and the RHS (3*nodec each).  matvec: y = A x with BC
  * rows zeroed, CrsMat::MatVecMult (module/solver/solver.cpp:405-433), host
- * arrays of 3*nodec.  solve: the assembled system from x = 0, physical x. */
+ * arrays of 3*nodec.  solve: the assembled system from x = 0, physical x
+ * (x may be NULL: the solution then stays on the device, no copy back). */
 mpm_status mpm_gpu_implicit_assemble(mpm_ctx *ctx, double facl);
 mpm_status mpm_gpu_implicit_get_system(mpm_ctx *ctx, double *stencil, double *adiag, double *b_rhs);
 mpm_status mpm_gpu_implicit_matvec(mpm_ctx *ctx, const double *x, double *y);
