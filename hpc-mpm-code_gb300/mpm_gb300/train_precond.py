@@ -5,7 +5,7 @@ Training pairs come from the implicit solver's own solves on the
 moduli E drawn log-uniformly from [1e6, 1e8] and the system's own plus
 seeded random loads, each system is solved twice and (residual, error)
 pairs are stored along the second solve (mpm_gpu_implicit_harvest); a
-second round stores pairs along the learned solver's own iterations.  The network is then trained with
+second pass stores pairs along the learned solver's own iterations.  The network is then trained with
 Adam by the library's own tensor-core forward and backward kernels
 (mpm_nn_train).  The result is written as raw FP32 parameters plus a JSON
 record of the run; bench.py and the tests load them through
@@ -40,9 +40,9 @@ def load_weights(path=WEIGHTS):
 def train(pairs=20000, loads_per_system=8, pairs_per_load=25, epochs=8, batch=8, lr=1.0e-3, seed=0,
           harvest_eps=1.0e-20, learned_pairs=8000, learned_pairs_per_load=16, epochs2=4, scene=None, out=WEIGHTS,
           log=print):
-    """Two rounds: pairs along Jacobi-PCG solves, training; then (if
+    """Two passes: pairs along Jacobi-PCG solves, training; then (if
     learned_pairs > 0) pairs along the learned solver's own iterations with
-    the round-one network, and training on all pairs."""
+    the first-pass network, and training on all pairs."""
     s = scene if scene is not None else scenes.cantilever(iprop=1)
     gpu = capi.GpuImplicitSolid(s, nr_flag=True)
     per_system = loads_per_system * pairs_per_load
@@ -64,7 +64,7 @@ def train(pairs=20000, loads_per_system=8, pairs_per_load=25, epochs=8, batch=8,
                     eps=harvest_eps)
         gpu.set_precond(None)
         losses2 = net.train(epochs2, batch, lr=lr * 0.5, seed=seed + 1)
-        log(f"round 2: {net.num_pairs()} pairs, {epochs2} epochs, loss per epoch "
+        log(f"second pass: {net.num_pairs()} pairs, {epochs2} epochs, loss per epoch "
             f"{[round(float(x), 4) for x in losses2]}")
     t3 = time.perf_counter()
     params = net.params()
