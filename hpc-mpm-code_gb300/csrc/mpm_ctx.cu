@@ -113,7 +113,7 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
         if (!ok) return MPM_ERR_UNSUPPORTED;
     }
     for (int k = 0; k < mat->nmat; k++)
-        if (mat->iprop[k] < -1 || mat->iprop[k] > 2) return MPM_ERR_UNSUPPORTED;
+        if (mat->iprop[k] < -1 || mat->iprop[k] > 4) return MPM_ERR_UNSUPPORTED;
     mpm_ctx *c = new (std::nothrow) mpm_ctx();
     if (!c) return MPM_ERR_OOM;
     Geom &g = c->g;

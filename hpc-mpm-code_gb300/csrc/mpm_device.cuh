@@ -227,7 +227,127 @@ __device__ __forceinline__ void neo_hookean_stress_h(float *s, const float H[3][
     s[5] = (mu * bm[0][1]) / J;
 }
 
-// Weakly compressible Newtonian fluid (material model 2, no counterpart in the
+// MatStVk (constitutive_model.cpp:122-185), stress part: with b = F F^T and
+// tr E = (tr b - 3) / 2, sigma = (mu b^2 + (lambda tr E - mu) b) / J.
+template <typename R>
+__device__ __forceinline__ void stvk_stress(R *s, const R F[3][3], R jac, R E, R nu) {
+    const R rd = (R)1 / (((R)1 + nu) * ((R)1 - (R)2 * nu));
+    const R lmd = nu * E * rd;
+    const R mu = (R)0.5 * E * ((R)1 - (R)2 * nu) * rd;
+    R be[3][3], b2[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) be[i][j] = F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) b2[i][j] = be[i][0] * be[0][j] + be[i][1] * be[1][j] + be[i][2] * be[2][j];
+    const R tre = (R)0.5 * (be[0][0] + be[1][1] + be[2][2] - (R)3);
+    const R ij = (R)1 / jac;
+    const R cb = lmd * tre - mu;
+    s[0] = (mu * b2[0][0] + cb * be[0][0]) * ij;
+    s[1] = (mu * b2[1][1] + cb * be[1][1]) * ij;
+    s[2] = (mu * b2[2][2] + cb * be[2][2]) * ij;
+    s[3] = (mu * b2[1][2] + cb * be[1][2]) * ij;
+    s[4] = (mu * b2[0][2] + cb * be[0][2]) * ij;
+    s[5] = (mu * b2[0][1] + cb * be[0][1]) * ij;
+}
+
+// The same from H = F - I (FP32 path): with m = b - I = H + H^T + H H^T,
+// mu b^2 + (lambda trE - mu) b = lambda trE (I + m) + mu (m + m^2), trE = tr m / 2,
+// free of the cancellation of numbers near 1.
+__device__ __forceinline__ void stvk_stress_h(float *s, const float H[3][3], float jm1, float E, float nu) {
+    const float rd = 1.0f / ((1.0f + nu) * (1.0f - 2.0f * nu));
+    const float lmd = nu * E * rd;
+    const float mu = 0.5f * E * (1.0f - 2.0f * nu) * rd;
+    float m[3][3], m2[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) m[i][j] = H[i][j] + H[j][i] + H[i][0] * H[j][0] + H[i][1] * H[j][1] + H[i][2] * H[j][2];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) m2[i][j] = m[i][0] * m[0][j] + m[i][1] * m[1][j] + m[i][2] * m[2][j];
+    const float lt = lmd * 0.5f * (m[0][0] + m[1][1] + m[2][2]);
+    const float ij = 1.0f / (1.0f + jm1);
+    s[0] = (lt * (1.0f + m[0][0]) + mu * (m[0][0] + m2[0][0])) * ij;
+    s[1] = (lt * (1.0f + m[1][1]) + mu * (m[1][1] + m2[1][1])) * ij;
+    s[2] = (lt * (1.0f + m[2][2]) + mu * (m[2][2] + m2[2][2])) * ij;
+    s[3] = (lt * m[1][2] + mu * (m[1][2] + m2[1][2])) * ij;
+    s[4] = (lt * m[0][2] + mu * (m[0][2] + m2[0][2])) * ij;
+    s[5] = (lt * m[0][1] + mu * (m[0][1] + m2[0][1])) * ij;
+}
+
+// MatMooneyRivlin (constitutive_model.cpp:187-285), stress part; mat_prop =
+// {c1, c2, bulk}.  With b = J^(-2/3) F F^T, I1 = tr b, I2 = (I1^2 - tr b^2) / 2:
+// sigma = 2 ((c1 + c2 I1) b - c2 b^2) / J + (bulk ln J / J - 2 (c1 I1 + 2 c2 I2) / (3 J)) I.
+template <typename R>
+__device__ __forceinline__ void mooney_rivlin_stress(R *s, const R F[3][3], R jac, R c1, R c2, R bulk) {
+    const R k = (R)1 / cbrt(jac);
+    R be[3][3], b2[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+            be[i][j] = (k * F[i][0]) * (k * F[j][0]) + (k * F[i][1]) * (k * F[j][1]) + (k * F[i][2]) * (k * F[j][2]);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) b2[i][j] = be[i][0] * be[0][j] + be[i][1] * be[1][j] + be[i][2] * be[2][j];
+    const R i1 = be[0][0] + be[1][1] + be[2][2];
+    const R i2 = (R)0.5 * (i1 * i1 - (b2[0][0] + b2[1][1] + b2[2][2]));
+    const R ij = (R)1 / jac;
+    const R hp = bulk * log(jac) * ij;
+    const R dg = hp - (R)2 / (R)3 * ij * (c1 * i1 + (R)2 * c2 * i2);
+    const R ca = (R)2 * (c1 + c2 * i1) * ij, cb = (R)2 * c2 * ij;
+    s[0] = ca * be[0][0] - cb * b2[0][0] + dg;
+    s[1] = ca * be[1][1] - cb * b2[1][1] + dg;
+    s[2] = ca * be[2][2] - cb * b2[2][2] + dg;
+    s[3] = ca * be[1][2] - cb * b2[1][2];
+    s[4] = ca * be[0][2] - cb * b2[0][2];
+    s[5] = ca * be[0][1] - cb * b2[0][1];
+}
+
+// The same from H = F - I (FP32 path).  With B = b - I = (J^(-2/3) - 1) I +
+// J^(-2/3) m, m = H + H^T + H H^T, the stress is
+//   2/J [ (c2 trB - (c1 trB + 4 c2 trB + c2 (trB)^2 - c2 tr B^2) / 3) I
+//         + (c1 + c2 + c2 trB) B - c2 B^2 ] + bulk ln(J) / J I,
+// which is the expression above with the parts that cancel at small strain
+// taken out exactly.
+__device__ __forceinline__ void mooney_rivlin_stress_h(float *s, const float H[3][3], float jm1, float c1, float c2,
+                                                       float bulk) {
+    const float lj = log1pf(jm1);
+    const float km1 = expm1f(-(2.0f / 3.0f) * lj);   // J^(-2/3) - 1
+    const float k = 1.0f + km1;
+    float B[3][3], B2[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const float m = H[i][j] + H[j][i] + H[i][0] * H[j][0] + H[i][1] * H[j][1] + H[i][2] * H[j][2];
+            B[i][j] = k * m + (i == j ? km1 : 0.0f);
+        }
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) B2[i][j] = B[i][0] * B[0][j] + B[i][1] * B[1][j] + B[i][2] * B[2][j];
+    const float tb = B[0][0] + B[1][1] + B[2][2];
+    const float tb2 = B2[0][0] + B2[1][1] + B2[2][2];
+    const float ij = 1.0f / (1.0f + jm1);
+    const float dg = 2.0f * ij * (c2 * tb - (c1 * tb + 4.0f * c2 * tb + c2 * tb * tb - c2 * tb2) / 3.0f) +
+                     bulk * lj * ij;
+    const float ca = 2.0f * ij * (c1 + c2 + c2 * tb), cb = 2.0f * ij * c2;
+    s[0] = ca * B[0][0] - cb * B2[0][0] + dg;
+    s[1] = ca * B[1][1] - cb * B2[1][1] + dg;
+    s[2] = ca * B[2][2] - cb * B2[2][2] + dg;
+    s[3] = ca * B[1][2] - cb * B2[1][2];
+    s[4] = ca * B[0][2] - cb * B2[0][2];
+    s[5] = ca * B[0][1] - cb * B2[0][1];
+}
+
+// Weakly compressible Newtonian fluid (material model 4, no counterpart in the
 // reference): Tait equation of state p = (rho0 c0^2 / gamma) ((rho / rho0)^gamma - 1)
 // with rho = rho0 / J, and sigma = -p I + 2 mu dev(D), D = sym(grad v).
 // `inc` is the step increment dF - I = dt grad v; mat_prop = {c0, gamma, mu}.

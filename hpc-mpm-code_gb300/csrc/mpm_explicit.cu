@@ -738,8 +738,11 @@ __device__ __forceinline__ void musl_particle(const StepArgs<float> &a, const Sc
         return;
     }
     const float wz = h ? az.w[1] : az.w[0], dwz = h ? az.dw[1] : az.dw[0];
-    // partial gathers over this thread's four nodes
-    float vs[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f};
+    // partial gathers over this thread's four nodes; ws sums the weights the
+    // gather used, which in FP32 add up to 1 only within a few ulps: dividing
+    // by it keeps that per-particle bias (the same sign step after step for a
+    // particle that stays near its place in the cell) out of the velocity
+    float vs[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f}, ws = 0.0f;
 #pragma unroll
     for (int j = 0; j < 2; j++)
 #pragma unroll
@@ -761,6 +764,7 @@ __device__ __forceinline__ void musl_particle(const StepArgs<float> &a, const Sc
                 e = ld(a.nei + gn);
             }
             const float wv = flip ? N_ * a.dt : N_;
+            ws += N_;
 #pragma unroll
             for (int d = 0; d < 3; d++) vs[d] += wv * gv[d];
             gu[0] += ax.dw[i] * ay.w[j] * wz * e;
@@ -771,11 +775,12 @@ __device__ __forceinline__ void musl_particle(const StepArgs<float> &a, const Sc
     // Only the cell's own two lanes take part: the other cells of the warp
     // run different particle counts, so a full-warp mask would not converge.
     const unsigned pair = 3u << ((threadIdx.x & 31) & ~1u);
+    const float rw = __frcp_rn(ws + __shfl_xor_sync(pair, ws, 1));
     float v[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         const float other = __shfl_xor_sync(pair, vs[d], 1);
-        v[d] = vs[d] + other;
+        v[d] = (vs[d] + other) * rw;
         gu[d] += __shfl_xor_sync(pair, gu[d], 1);
     }
     if (flip) {
@@ -957,7 +962,7 @@ __global__ void __launch_bounds__(BCH) k_musl_brick(StepArgs<float> a) {
             const float wx[2] = {0.5f - u, 0.5f + u}, wy[2] = {0.5f - v, 0.5f + v}, wz[2] = {0.5f - w, 0.5f + w};
             const float dx[2] = {-a.g.inv_dx[0], a.g.inv_dx[0]}, dy[2] = {-a.g.inv_dx[1], a.g.inv_dx[1]},
                         dz[2] = {-a.g.inv_dx[2], a.g.inv_dx[2]};
-            float vs[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f};
+            float vs[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f}, ws = 0.0f;
 #pragma unroll
             for (int k = 0; k < 2; k++)
 #pragma unroll
@@ -981,13 +986,15 @@ __global__ void __launch_bounds__(BCH) k_musl_brick(StepArgs<float> a) {
                         const float wxy = wx[i] * wy[j];
                         const float Nn = wxy * wz[k];
                         const float wv = flip ? Nn * a.dt : Nn;
+                        ws += Nn;
 #pragma unroll
                         for (int d = 0; d < 3; d++) vs[d] += wv * gv[d];
                         gu[0] += dx[i] * wy[j] * wz[k] * e;
                         gu[1] += wx[i] * dy[j] * wz[k] * e;
                         gu[2] += wxy * dz[k] * e;
                     }
-            float vel[3] = {vs[0], vs[1], vs[2]};
+            const float rw = __frcp_rn(ws);   // weights summed as gathered (musl_particle)
+            float vel[3] = {vs[0] * rw, vs[1] * rw, vs[2] * rw};
             if (flip) {
                 vel[0] += ld(P.v[0] + p);
                 vel[1] += ld(P.v[1] + p);
@@ -1206,8 +1213,12 @@ __global__ void __launch_bounds__(256) k_musl_misses(StepArgs<float> a) {
         axis_eval<float, 1>(x0, a.g, 0, px, ax);
         axis_eval<float, 1>(x1, a.g, 1, py, ay);
         axis_eval<float, 1>(x2, a.g, 2, pz, az);
-        float v[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f};
-        for (int k = 0; k < 2; k++)
+        // the two z-layers summed separately and then added, in the order of
+        // musl_particle's two lanes, so that a particle gets the same bits
+        // on either path
+        float v[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f}, wsum = 0.0f;
+        for (int k = 0; k < 2; k++) {
+            float vk[3] = {0.0f, 0.0f, 0.0f}, wk = 0.0f;
             for (int j = 0; j < 2; j++)
                 for (int ii = 0; ii < 2; ii++) {
                     const size_t gn = node_id(a.g, px + ii, py + j, pz + k);
@@ -1215,12 +1226,20 @@ __global__ void __launch_bounds__(256) k_musl_misses(StepArgs<float> a) {
                     const float N_ = wxy * az.w[k];
                     const float wv = flip ? N_ * a.dt : N_;
                     const float e = ld(a.nei + gn);
+                    wk += N_;
 #pragma unroll
-                    for (int d = 0; d < 3; d++) v[d] += wv * ld(a.G + d * N + gn);
+                    for (int d = 0; d < 3; d++) vk[d] += wv * ld(a.G + d * N + gn);
                     gu[0] += ax.dw[ii] * ay.w[j] * az.w[k] * e;
                     gu[1] += ax.w[ii] * ay.dw[j] * az.w[k] * e;
                     gu[2] += wxy * az.dw[k] * e;
                 }
+            wsum += wk;
+#pragma unroll
+            for (int d = 0; d < 3; d++) v[d] += vk[d];
+        }
+        const float rw = __frcp_rn(wsum);
+#pragma unroll
+        for (int d = 0; d < 3; d++) v[d] *= rw;
         if (flip) {
 #pragma unroll
             for (int d = 0; d < 3; d++) v[d] += ld(P.v[d] + p);
@@ -1758,6 +1777,12 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
             if constexpr (sizeof(R) == 8) neo_hookean_stress(s, Fn, J, E, nu);
             else neo_hookean_stress_h(s, Fn, det_ipm1(Fn), E, nu);
         } else if (model == 2) {
+            if constexpr (sizeof(R) == 8) stvk_stress(s, Fn, J, E, nu);
+            else stvk_stress_h(s, Fn, det_ipm1(Fn), E, nu);
+        } else if (model == 3) {   // mat_prop = {c1, c2, bulk}
+            if constexpr (sizeof(R) == 8) mooney_rivlin_stress(s, Fn, J, E, nu, (R)a.matprop[3 * mid + 2]);
+            else mooney_rivlin_stress_h(s, Fn, det_ipm1(Fn), E, nu, (R)a.matprop[3 * mid + 2]);
+        } else if (model == 4) {
             R jm1;
             if constexpr (sizeof(R) == 8) jm1 = J - (R)1;
             else jm1 = det_ipm1(Fn);
@@ -1903,7 +1928,9 @@ __device__ __forceinline__ void update_particle(const StepArgs<float> &a, const 
     const float E = (float)a.matprop[3 * mid], nu = (float)a.matprop[3 * mid + 1];
     if (model == 0) lin_elast_update(s, D, E, nu);
     else if (model == 1) neo_hookean_stress_h(s, Hn, jm1, E, nu);
-    else if (model == 2)
+    else if (model == 2) stvk_stress_h(s, Hn, jm1, E, nu);
+    else if (model == 3) mooney_rivlin_stress_h(s, Hn, jm1, E, nu, (float)a.matprop[3 * mid + 2]);
+    else if (model == 4)
         tait_stress<float>(s, D, jm1, P.m[p] / vol0, E, nu, (float)a.matprop[3 * mid + 2], 1.0f / a.dt);
     else if (model == -1)
 #pragma unroll

@@ -416,6 +416,62 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
     return r;
 }
 
+// Warp sums of V values (V a power of two <= 32) with the values spread over
+// the lanes as the butterfly goes: at each of the first log2(V) steps a lane
+// keeps half of its values and adds its partner's copy of that half, so a
+// lane adds 2V - 1 + log2(32 / V) numbers instead of 5 V.  FP64 adds are the
+// scarce resource on this part.  Returns the value index whose warp total the
+// lane holds in v[0] (every lane of a group of 32 / V lanes holds it).
+template <int V>
+__device__ __forceinline__ int warp_sums(double (&v)[V]) {
+    const int lane = threadIdx.x & 31;
+    int j = 0, o = 16;
+#pragma unroll
+    for (int h = V / 2; h >= 1; h /= 2, o >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < h; i++) {
+            const double send = up ? v[i] : v[i + h];
+            const double keep = up ? v[i + h] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+        if (up) j += h;
+    }
+    for (; o >= 1; o >>= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
+    return j;
+}
+
+template <int V>
+__device__ __forceinline__ bool partials_last(const double (&vin)[V], int nv, double *part, unsigned *cnt) {
+    __shared__ double sh[V][8];
+    __shared__ bool s_last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double v[V];
+#pragma unroll
+    for (int j = 0; j < V; j++) v[j] = vin[j];
+    const int j = warp_sums<V>(v);
+    if ((lane & (32 / V - 1)) == 0) sh[j][wid] = v[0];
+    __syncthreads();
+    if ((int)threadIdx.x < nv) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[threadIdx.x][w];
+        part[threadIdx.x * gridDim.x + blockIdx.x] = t;
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (s_last) __threadfence();
+    return s_last;
+}
+
+// in the last block: the total of value j over all blocks (thread 0)
+__device__ __forceinline__ double last_sum(const double *part, int j, double *sh32) {
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) acc += __ldcg(part + (size_t)j * gridDim.x + i);
+    return block_sum(acc, sh32);
+}
+
 __global__ void k_finish(const double *part, int nblk, double *out, int slot) {
     __shared__ double sh[32];
     double acc = 0.0;
@@ -426,7 +482,8 @@ __global__ void k_finish(const double *part, int nblk, double *out, int slot) {
 
 // y = A x with BC rows zeroed (MatVecMult + BCResidualSet), optional dot(x, y)
 __global__ void __launch_bounds__(256) k_imp_matvec(ImpArgs a, const double *A, const double *x, double *y,
-                                                    double *part) {
+                                                    double *part, unsigned *cnt = nullptr, double *scal = nullptr,
+                                                    int slot = 0) {
     __shared__ double sh[32];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     double dot = 0.0;
@@ -472,7 +529,15 @@ __global__ void __launch_bounds__(256) k_imp_matvec(ImpArgs a, const double *A, 
             dot += x[c * N + n] * acc[c];
         }
     }
-    if (part) {
+    if (part && cnt) {   // dot(x, y) reduced by the last block into scal[slot]
+        const double v[1] = {dot};
+        if (!partials_last<1>(v, 1, part, cnt)) return;
+        const double t = last_sum(part, 0, sh);
+        if (threadIdx.x == 0) {
+            scal[slot] = t;
+            *cnt = 0u;
+        }
+    } else if (part) {
         const double t = block_sum(dot, sh);
         if (threadIdx.x == 0) part[blockIdx.x] = t;
     }
@@ -529,9 +594,9 @@ __device__ __forceinline__ double block_div(double num, double den, bool zero = 
     return s_q;
 }
 
-// x += alpha p, r -= alpha Ap, partial r.r;  alpha = rr_cur / pAp
-__global__ void k_cg_update(ImpArgs a, const double *scal, int cur, double *x, double *r, const double *p,
-                            const double *Ap, double *part) {
+// x += alpha p, r -= alpha Ap, then (last block) r.r;  alpha = rr_cur / pAp
+__global__ void k_cg_update(ImpArgs a, double *scal, int cur, double *x, double *r, const double *p,
+                            const double *Ap, double *part, unsigned *cnt) {
     __shared__ double sh[32];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const double alpha = block_div(scal[cur], scal[S_PAP]);
@@ -546,8 +611,13 @@ __global__ void k_cg_update(ImpArgs a, const double *scal, int cur, double *x, d
             dot += v * v;
         }
     }
-    const double t = block_sum(dot, sh);
-    if (threadIdx.x == 0) part[blockIdx.x] = t;
+    const double v[1] = {dot};
+    if (!partials_last<1>(v, 1, part, cnt)) return;
+    const double t = last_sum(part, 0, sh);
+    if (threadIdx.x == 0) {
+        scal[cur ^ 1] = t;
+        *cnt = 0u;
+    }
 }
 
 // p = r + beta p;  beta = rr_new / rr_cur
@@ -869,62 +939,6 @@ __device__ __forceinline__ int gcr_prev(int slot, int j, int w) { return (slot -
 // true in the last block to finish (the blocks count themselves on *cnt),
 // which then reduces the partials in block order (last_sum), so the sums
 // are reproducible without a separate reduction launch.
-// Warp sums of V values (V a power of two <= 32) with the values spread over
-// the lanes as the butterfly goes: at each of the first log2(V) steps a lane
-// keeps half of its values and adds its partner's copy of that half, so a
-// lane adds 2V - 1 + log2(32 / V) numbers instead of 5 V.  FP64 adds are the
-// scarce resource on this part.  Returns the value index whose warp total the
-// lane holds in v[0] (every lane of a group of 32 / V lanes holds it).
-template <int V>
-__device__ __forceinline__ int warp_sums(double (&v)[V]) {
-    const int lane = threadIdx.x & 31;
-    int j = 0, o = 16;
-#pragma unroll
-    for (int h = V / 2; h >= 1; h /= 2, o >>= 1) {
-        const bool up = (lane & o) != 0;
-#pragma unroll
-        for (int i = 0; i < h; i++) {
-            const double send = up ? v[i] : v[i + h];
-            const double keep = up ? v[i + h] : v[i];
-            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-        }
-        if (up) j += h;
-    }
-    for (; o >= 1; o >>= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
-    return j;
-}
-
-template <int V>
-__device__ __forceinline__ bool partials_last(const double (&vin)[V], int nv, double *part, unsigned *cnt) {
-    __shared__ double sh[V][8];
-    __shared__ bool s_last;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    double v[V];
-#pragma unroll
-    for (int j = 0; j < V; j++) v[j] = vin[j];
-    const int j = warp_sums<V>(v);
-    if ((lane & (32 / V - 1)) == 0) sh[j][wid] = v[0];
-    __syncthreads();
-    if ((int)threadIdx.x < nv) {
-        double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[threadIdx.x][w];
-        part[threadIdx.x * gridDim.x + blockIdx.x] = t;
-        __threadfence();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(cnt, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (s_last) __threadfence();
-    return s_last;
-}
-
-// in the last block: the total of value j over all blocks (thread 0)
-__device__ __forceinline__ double last_sum(const double *part, int j, double *sh32) {
-    double acc = 0.0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) acc += __ldcg(part + (size_t)j * gridDim.x + i);
-    return block_sum(acc, sh32);
-}
-
 // flexible GCR: the dots q . Q_j of the new image with the kept ones, then
 // (last block) beta_j = (q . Q_j) / (Q_j . Q_j)
 __global__ void __launch_bounds__(256) k_gcr_dots(ImpArgs a, const double *Q, int slot, int used, int w, double *part,
@@ -1187,15 +1201,13 @@ static void cg_iteration(mpm_ctx *c, const ImpArgs &a, int nb, int it) {
     ImpState *s = c->imp;
     const int cur = (it & 1) ? S_RR1 : S_RR0;
     timer_begin(c, K_MATVEC);
-    k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->p, s->Ap, s->part);
+    k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->p, s->Ap, s->part, s->cnt + 3, s->scal, S_PAP);
     timer_end(c, K_MATVEC);
     timer_begin(c, K_KRYLOV);
-    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_PAP);
-    k_cg_update<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->xs, s->r, s->p, s->Ap, s->part);
-    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, cur ^ 1);
+    k_cg_update<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->xs, s->r, s->p, s->Ap, s->part, s->cnt + 4);
     k_cg_dir<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->r, s->p);
     timer_end(c, K_KRYLOV);
-    c->launches += 5;
+    c->launches += 3;
 }
 
 static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
@@ -1733,10 +1745,8 @@ static mpm_status cg_scaled(mpm_ctx *c, double eps, int kmax, mpm_nn *net, int s
             if (st != MPM_OK) return st;
             pairs++;
         }
-        k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->p, s->Ap, s->part);
-        k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_PAP);
-        k_cg_update<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->xs, s->r, s->p, s->Ap, s->part);
-        k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, cur ^ 1);
+        k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->p, s->Ap, s->part, s->cnt + 3, s->scal, S_PAP);
+        k_cg_update<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->xs, s->r, s->p, s->Ap, s->part, s->cnt + 4);
         k_cg_dir<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->r, s->p);
         it++;
         if (it % 8 == 0 || it == kmax) {

@@ -200,7 +200,7 @@ def cantilever(grid=(64, 64, 64), dx=1.0e-2, cell_lo=(0, 2, 2), cells=(60, 60, 6
 def dam_break(grid=(256, 128, 128), dx=4.0e-3, cells=(128, 128, 96), npc=2, jitter=0.0, c0=30.0, gamma=7.0,
               mu=1.0e-3, rho=1000.0, dt=5.0e-6, gravity=(0.0, 0.0, -9.81), scheme=PIC, seed=12350,
               mtol=1.0e-12, name="dam_break"):
-    """Weakly compressible water column (Tait fluid, material model 2).
+    """Weakly compressible water column (Tait fluid, material model 4).
 
     Defaults: 256 x 128 x 128-cell grid, dx = 4e-3 m, a 128 x 128 x 96-cell
     column in the x = 0 corner at 2x2x2 particles per cell = 12,582,912
@@ -218,7 +218,7 @@ def dam_break(grid=(256, 128, 128), dx=4.0e-3, cells=(128, 128, 96), npc=2, jitt
     scene = Scene(
         xyelem=tuple(grid), xymin=xymin, dxy=dxy, idimc=(1, 1, 1), npxye=(npc, npc, npc),
         dt=dt, mtol=mtol, gravity=tuple(gravity),
-        iprop=np.array([2], dtype=np.int32), mat_prop=np.array([[c0, gamma, mu]]),
+        iprop=np.array([4], dtype=np.int32), mat_prop=np.array([[c0, gamma, mu]]),
         coord=pts, vel=np.zeros((n, 3)), mass=np.full(n, rho * vp), vol0=np.full(n, vp),
         matid=np.zeros(n, dtype=np.int32), scheme=scheme, name=name)
     nn = scene.xynodec

@@ -58,12 +58,16 @@ typedef struct {
     int npxye[3];     /* particles per cell per direction, for the nodal volume (npxye) */
 } mpm_grid_desc;
 
-/* Material table: iprop[nmat] (-1 rigid, 0 linear elastic, 1 Neo-Hookean)
- * and mat_prop[3*nmat] = {E, nu, spare} (module/dataset.h:13-14).
- * iprop 2 (no counterpart in the reference, explicit contexts only): a weakly
- * compressible Newtonian fluid with the Tait equation of state,
- * mat_prop = {c0 (speed of sound), gamma, mu (dynamic viscosity)}; the rest
- * density is each particle's mass / vol0. */
+/* Material table: iprop[nmat] and mat_prop[3*nmat] (module/dataset.h:13-14),
+ * the model numbers of ConstitutiveModel::UpdateStress
+ * (module/solid/constitutive_model.cpp:287-305): -1 rigid, 0 linear elastic,
+ * 1 Neo-Hookean, 2 St.Venant-Kirchhoff ({E, nu, -}), 3 Mooney-Rivlin
+ * ({c1, c2, bulk modulus}).  Implicit contexts take -1, 0 and 1 (the models
+ * with a GPU tangent); explicit contexts all of them and
+ * iprop 4 (no counterpart in the reference): a weakly compressible Newtonian
+ * fluid with the Tait equation of state, mat_prop = {c0 (speed of sound),
+ * gamma, mu (dynamic viscosity)}; the rest density is each particle's
+ * mass / vol0. */
 typedef struct {
     int nmat;
     const int *iprop;

@@ -10,7 +10,7 @@
  *   explicit G2P + MUSL        module/solid/explicit/var_trans_solid_explicit.cpp:101-148,187-311
  *   position/stress update     module/solid/explicit/var_trans_solid_explicit.cpp:150-185
  *   particle shifting          module/material_point.cpp:174-228
- *   constitutive models        module/solid/constitutive_model.cpp:7-120,287-305
+ *   constitutive models        module/solid/constitutive_model.cpp:7-285,287-305
  *   implicit P2G/G2P           module/solid/implicit/var_trans_solid_implicit.cpp:20-167
  *   implicit Newton + assembly module/solid/implicit/solve_solid_implicit.cpp:26-204
  *   Newmark / gen.-alpha       module/nonlinear_time_integration.cpp:10-96
@@ -356,7 +356,46 @@ static void mat_neo_hookean(mo_ctx *c, double *sts, const double FF[3][3], const
     }
 }
 
-/* Weakly compressible Newtonian fluid (material model 2, no counterpart in
+/* MatStVk, module/solid/constitutive_model.cpp:122-185 (stress part) */
+static void mat_stvk(double *sts, const double FF[3][3], const double *mp, double jac) {
+    double yng = mp[0], nu = mp[1];
+    double lmd = nu * yng / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    double mu = yng / (2.0 * (1.0 + nu));
+    double be[3][3], be2[3][3], sig[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) be[i][j] = FF[i][0] * FF[j][0] + FF[i][1] * FF[j][1] + FF[i][2] * FF[j][2];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) be2[i][j] = be[i][0] * be[0][j] + be[i][1] * be[1][j] + be[i][2] * be[2][j];
+    double tr_gls = 0.5 * (be[0][0] + be[1][1] + be[2][2] - 3.0);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) sig[i][j] = (mu * be2[i][j] + (lmd * tr_gls - mu) * be[i][j]) / jac;
+    sts[0] = sig[0][0]; sts[1] = sig[1][1]; sts[2] = sig[2][2];
+    sts[3] = sig[1][2]; sts[4] = sig[0][2]; sts[5] = sig[0][1];
+}
+
+/* MatMooneyRivlin, module/solid/constitutive_model.cpp:187-285 (stress part);
+ * mat_prop = {c1, c2, bulk} */
+static void mat_mooney_rivlin(double *sts, const double FF[3][3], const double *mp, double jac) {
+    double c1 = mp[0], c2 = mp[1], bulk = mp[2];
+    double fi[3][3], be[3][3], be2[3][3], sig[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) fi[i][j] = 1.0 / cbrt(jac) * FF[i][j];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) be[i][j] = fi[i][0] * fi[j][0] + fi[i][1] * fi[j][1] + fi[i][2] * fi[j][2];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) be2[i][j] = be[i][0] * be[0][j] + be[i][1] * be[1][j] + be[i][2] * be[2][j];
+    double i1 = be[0][0] + be[1][1] + be[2][2];
+    double i2 = 0.5 * (i1 * i1 - (be2[0][0] + be2[1][1] + be2[2][2]));
+    double hp = bulk * log(jac) / jac;
+    for (int i = 0; i < 3; i++) {
+        for (int j = 0; j < 3; j++) sig[i][j] = 2.0 * ((c1 + c2 * i1) * be[i][j] - c2 * be2[i][j]) / jac;
+        sig[i][i] += hp - 2.0 / (3.0 * jac) * (c1 * i1 + 2.0 * c2 * i2);
+    }
+    sts[0] = sig[0][0]; sts[1] = sig[1][1]; sts[2] = sig[2][2];
+    sts[3] = sig[1][2]; sts[4] = sig[0][2]; sts[5] = sig[0][1];
+}
+
+/* Weakly compressible Newtonian fluid (material model 4, no counterpart in
  * the reference): Tait equation of state p = (rho0 c0^2 / gamma)((rho/rho0)^gamma - 1),
  * rho = rho0 / J, rho0 = m / V0, and sigma = -p I + 2 mu dev(D) with
  * D = sym(dF - I) / dt; mat_prop = {c0, gamma, mu}.  (rho/rho0)^gamma - 1 is
@@ -389,6 +428,10 @@ static void update_stress(mo_ctx *c, int p, double *sts, const double FF[3][3], 
     } else if (model == 1) {
         mat_neo_hookean(c, sts, FF, mp, c->jac[p], c->jac[p], implicit);
     } else if (model == 2 && !implicit) {
+        mat_stvk(sts, FF, mp, c->jac[p]);
+    } else if (model == 3 && !implicit) {
+        mat_mooney_rivlin(sts, FF, mp, c->jac[p]);
+    } else if (model == 4 && !implicit) {
         mat_tait(c, p, sts, d, mp);
     }
 }

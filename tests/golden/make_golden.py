@@ -7,6 +7,7 @@ checkout exists only in the development container, so the fixtures are
 committed and this script is re-run only when a case is added:
 
     oracle/build_ref.sh && python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --hyperelastic     # only models 2 and 3
 """
 from __future__ import annotations
 
@@ -72,9 +73,28 @@ def implicit_case(name, scene, nr_flag, nsteps):
     print("wrote", name, scene.num, "particles", r.nmat, "blocks")
 
 
+def hyperelastic_cases():
+    """St.Venant-Kirchhoff (model 2) and Mooney-Rivlin (model 3) blocks with a
+    random initial velocity; their own generator so that adding them leaves
+    the earlier fixtures untouched."""
+    rng = np.random.default_rng(20261204)
+    s = scenes.elastic_block(grid=(10, 10, 10), cell_lo=(2, 2, 0), cell_hi=(8, 8, 6), iprop=2, seed=105,
+                             E=5.0e5, scheme=scenes.FLIP)
+    s.vel[:] = rng.normal(0.0, 0.3, size=s.vel.shape)
+    explicit_case("explicit_stvk", s, nsteps=10)
+    # Mooney-Rivlin: c1 + c2 = mu / 2 and the bulk modulus of E = 1e6, nu = 0.3
+    s = scenes.elastic_block(grid=(10, 10, 10), cell_lo=(2, 2, 0), cell_hi=(8, 8, 6), iprop=3, seed=106)
+    s.mat_prop[:] = [[1.5e5, 0.42e5, 8.33e5]]
+    s.vel[:] = rng.normal(0.0, 0.3, size=s.vel.shape)
+    explicit_case("explicit_mooney_rivlin", s, nsteps=10)
+
+
 def main():
     if not ref.available():
         raise SystemExit("oracle/_ref/libmpmref.so missing: run oracle/build_ref.sh first")
+    if "--hyperelastic" in sys.argv[1:]:
+        hyperelastic_cases()
+        return
     rng = np.random.default_rng(20261203)
     # small elastic block, fixed bottom, PIC and FLIP, random initial velocity
     for scheme, nm in ((scenes.PIC, "explicit_pic"), (scenes.FLIP, "explicit_flip")):
@@ -97,6 +117,7 @@ def main():
     implicit_case("implicit_linear", s, nr_flag=False, nsteps=3)
     s = scenes.cantilever(grid=(10, 8, 8), cells=(6, 4, 4), cell_lo=(0, 2, 2), iprop=1)
     implicit_case("implicit_neohookean", s, nr_flag=True, nsteps=3)
+    hyperelastic_cases()
 
 
 if __name__ == "__main__":

@@ -15,7 +15,8 @@ from oracle import port
 
 pytestmark = pytest.mark.gpu
 
-EXPLICIT = ["explicit_pic", "explicit_flip", "explicit_quadratic", "explicit_neohookean"]
+EXPLICIT = ["explicit_pic", "explicit_flip", "explicit_quadratic", "explicit_neohookean", "explicit_stvk",
+            "explicit_mooney_rivlin"]
 P2G_FIELDS = ("nmass", "nvof", "nmome", "nforce", "nvel", "naccel", "nvol")
 PARTICLE_FIELDS = ("x", "v", "F", "sigma", "vol")
 

@@ -1,4 +1,4 @@
-"""Weakly compressible Tait fluid (material model 2; the dam-break
+"""Weakly compressible Tait fluid (material model 4; the dam-break
 workload) on the GPU against the oracle restatement.
 
 The reference has no explicit fluid MPM, so parity here is unpinned by the

@@ -12,7 +12,8 @@ from helpers import load_golden, rel_l2, scene_from_golden
 from oracle import port
 
 TOL = 1.0e-12
-EXPLICIT = ["explicit_pic", "explicit_flip", "explicit_quadratic", "explicit_neohookean"]
+EXPLICIT = ["explicit_pic", "explicit_flip", "explicit_quadratic", "explicit_neohookean", "explicit_stvk",
+            "explicit_mooney_rivlin"]
 IMPLICIT = ["implicit_linear", "implicit_neohookean"]
 
 
