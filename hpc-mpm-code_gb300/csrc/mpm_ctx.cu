@@ -2,6 +2,7 @@
 // boundary conditions, the explicit step and result downloads.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -116,6 +117,7 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
         if (mat->iprop[k] < -1 || mat->iprop[k] > 4) return MPM_ERR_UNSUPPORTED;
     mpm_ctx *c = new (std::nothrow) mpm_ctx();
     if (!c) return MPM_ERR_OOM;
+    if (const char *gn = getenv("MPM_GB300_GATHER_NORM")) c->gather_norm = atoi(gn) != 0;
     Geom &g = c->g;
     long long nodec = 1;
     for (int d = 0; d < 3; d++) {

@@ -65,6 +65,7 @@ struct StepArgs {
     int scheme;
     int shifting;
     int all_tiles;              // process every tile in the grid passes (download mode)
+    int gnorm;                  // FP32 gathers divide by their weight sum
     int implicit;               // implicit solid: the force fields carry sum N m a (AccelP2G)
     double nump;                // particle count as a bound factor
     double mmax;                // max particle mass
@@ -129,6 +130,15 @@ __device__ __forceinline__ void load_scales(const StepArgs<R> &a, Scales &sh) {
 template <typename R>
 __device__ __forceinline__ void load_scales_musl(const StepArgs<R> &a, Scales &sh) {
     load_scales_from<R>(&a.ctl->sc_musl, sh);
+}
+
+// Hardware reciprocal (rcp.approx: one MUFU operation, deterministic, within
+// about an ulp); used to normalise gathers by their weight sum, which is 1
+// to within a few ulps, so the approximation error does not matter.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
 }
 
 // Block-wide reduction (fixed order: deterministic); result valid in thread 0.
@@ -738,10 +748,10 @@ __device__ __forceinline__ void musl_particle(const StepArgs<float> &a, const Sc
         return;
     }
     const float wz = h ? az.w[1] : az.w[0], dwz = h ? az.dw[1] : az.dw[0];
-    // partial gathers over this thread's four nodes; ws sums the weights the
-    // gather used, which in FP32 add up to 1 only within a few ulps: dividing
-    // by it keeps that per-particle bias (the same sign step after step for a
-    // particle that stays near its place in the cell) out of the velocity
+    // partial gathers over this thread's four nodes; the velocity is divided
+    // by the sum of the weights, which in FP32 add up to 1 only within a few
+    // ulps: that keeps the per-particle bias (the same sign step after step
+    // for a particle that stays near its place in the cell) out of it
     float vs[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f}, ws = 0.0f;
 #pragma unroll
     for (int j = 0; j < 2; j++)
@@ -764,7 +774,7 @@ __device__ __forceinline__ void musl_particle(const StepArgs<float> &a, const Sc
                 e = ld(a.nei + gn);
             }
             const float wv = flip ? N_ * a.dt : N_;
-            ws += N_;
+            ws += wxy;
 #pragma unroll
             for (int d = 0; d < 3; d++) vs[d] += wv * gv[d];
             gu[0] += ax.dw[i] * ay.w[j] * wz * e;
@@ -775,7 +785,9 @@ __device__ __forceinline__ void musl_particle(const StepArgs<float> &a, const Sc
     // Only the cell's own two lanes take part: the other cells of the warp
     // run different particle counts, so a full-warp mask would not converge.
     const unsigned pair = 3u << ((threadIdx.x & 31) & ~1u);
-    const float rw = __frcp_rn(ws + __shfl_xor_sync(pair, ws, 1));
+    // sum of the eight weights: the four xy products (the same in both lanes)
+    // times each z weight, with no exchange between the lanes
+    const float rw = a.gnorm ? rcp_approx(ws * az.w[0] + ws * az.w[1]) : 1.0f;
     float v[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
@@ -993,7 +1005,7 @@ __global__ void __launch_bounds__(BCH) k_musl_brick(StepArgs<float> a) {
                         gu[1] += wx[i] * dy[j] * wz[k] * e;
                         gu[2] += wxy * dz[k] * e;
                     }
-            const float rw = __frcp_rn(ws);   // weights summed as gathered (musl_particle)
+            const float rw = a.gnorm ? rcp_approx(ws) : 1.0f;   // weights summed as gathered (musl_particle)
             float vel[3] = {vs[0] * rw, vs[1] * rw, vs[2] * rw};
             if (flip) {
                 vel[0] += ld(P.v[0] + p);
@@ -1213,12 +1225,8 @@ __global__ void __launch_bounds__(256) k_musl_misses(StepArgs<float> a) {
         axis_eval<float, 1>(x0, a.g, 0, px, ax);
         axis_eval<float, 1>(x1, a.g, 1, py, ay);
         axis_eval<float, 1>(x2, a.g, 2, pz, az);
-        // the two z-layers summed separately and then added, in the order of
-        // musl_particle's two lanes, so that a particle gets the same bits
-        // on either path
-        float v[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f}, wsum = 0.0f;
-        for (int k = 0; k < 2; k++) {
-            float vk[3] = {0.0f, 0.0f, 0.0f}, wk = 0.0f;
+        float v[3] = {0.0f, 0.0f, 0.0f}, gu[3] = {0.0f, 0.0f, 0.0f}, ws = 0.0f;
+        for (int k = 0; k < 2; k++)
             for (int j = 0; j < 2; j++)
                 for (int ii = 0; ii < 2; ii++) {
                     const size_t gn = node_id(a.g, px + ii, py + j, pz + k);
@@ -1226,18 +1234,14 @@ __global__ void __launch_bounds__(256) k_musl_misses(StepArgs<float> a) {
                     const float N_ = wxy * az.w[k];
                     const float wv = flip ? N_ * a.dt : N_;
                     const float e = ld(a.nei + gn);
-                    wk += N_;
+                    ws += N_;
 #pragma unroll
-                    for (int d = 0; d < 3; d++) vk[d] += wv * ld(a.G + d * N + gn);
+                    for (int d = 0; d < 3; d++) v[d] += wv * ld(a.G + d * N + gn);
                     gu[0] += ax.dw[ii] * ay.w[j] * az.w[k] * e;
                     gu[1] += ax.w[ii] * ay.dw[j] * az.w[k] * e;
                     gu[2] += wxy * az.dw[k] * e;
                 }
-            wsum += wk;
-#pragma unroll
-            for (int d = 0; d < 3; d++) v[d] += vk[d];
-        }
-        const float rw = __frcp_rn(wsum);
+        const float rw = a.gnorm ? rcp_approx(ws) : 1.0f;   // divided by the weights it used, as musl_particle
 #pragma unroll
         for (int d = 0; d < 3; d++) v[d] *= rw;
         if (flip) {
@@ -2164,6 +2168,7 @@ static StepArgs<R> make_args(mpm_ctx *c) {
     a.scheme = c->scheme;
     a.shifting = c->shifting;
     a.all_tiles = c->write_nodal_dl ? 1 : 0;
+    a.gnorm = c->gather_norm;
     a.implicit = c->nreal == 27 ? 1 : 0;
     a.nump = (double)c->num;
     a.mmax = c->mmax;

@@ -189,6 +189,7 @@ struct mpm_ctx {
     mpm::Tune tune;
     // CUDA graph of 2 x resort_period fused explicit steps (mpm_gpu_step_explicit)
     int use_graph = 1;
+    int gather_norm = 1;   // FP32 gathers divide by their weight sum (MPM_GB300_GATHER_NORM=0: off)
     cudaGraphExec_t graph_exec = nullptr;
     double graph_facl = 0.0;
     cudaStream_t graph_stream = nullptr;

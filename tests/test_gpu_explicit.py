@@ -133,6 +133,24 @@ def test_spinning_block_fp32_vs_fp64_oracle():
     assert e["v"] <= 1e-4 and e["x"] <= 5e-6, e
 
 
+def test_full_size_fp32_velocity_after_1000_steps():
+    """The accuracy target at full size: the 4,096,000-particle spinning block
+    after 1000 FP32 steps stays within 1e-4 relative L2 in velocity of the
+    same run in the GPU's FP64 mode (the FP64 mode is pinned to the oracle at
+    <= 1e-10 on the cases above; the single-core oracle itself would need
+    about 40 minutes for this run).  Positions within 1e-5."""
+    s = scenes.spinning_block()
+    res = {}
+    for prec in (64, 32):
+        gpu = capi.GpuSolid(s, precision=prec)
+        gpu.steps(1000)
+        res[prec] = gpu.particles()
+        gpu.sync()
+        gpu.close()
+    assert rel_l2(res[32]["v"], res[64]["v"]) <= 1e-4
+    assert rel_l2(res[32]["x"], res[64]["x"]) <= 1e-5
+
+
 def test_state_upload_download_round_trip():
     """mpm_gpu_upload_particles / mpm_gpu_download_particles keep the load order."""
     g = load_golden("explicit_flip")
