@@ -2,6 +2,8 @@
 // small 3x3 algebra and the constitutive updates.
 #pragma once
 
+#include <cstring>
+
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -122,22 +124,43 @@ __device__ __forceinline__ int cell_of(R x, const KGeom<R> &g, int d, bool &oob)
 // rounded to an int64; the sums are exact integers, so the result does not
 // depend on the order in which particles are visited.
 // ---------------------------------------------------------------------------
+// 2^e for |e| <= 240 (double) and |e| <= 120 (float), built from the
+// exponent bits: exact, and cheap on a part whose FP64 library calls are slow
+__host__ __device__ inline double pow2d(int e) {
+    const unsigned long long b = (unsigned long long)(e + 1023) << 52;
+    double d;
+    memcpy(&d, &b, sizeof(d));
+    return d;
+}
+__host__ __device__ inline float pow2f(int e) {
+    const unsigned b = (unsigned)(e + 127) << 23;
+    float f;
+    memcpy(&f, &b, sizeof(f));
+    return f;
+}
+
 __host__ __device__ inline Fix make_fix(double bound) {
     int e = 0;
     if (bound > 0.0 && bound < 1.0e300) {
+        // k with bound < 2^k <= 2 bound (frexp's exponent), from the exponent
+        // bits of a normal number; subnormal bounds take frexp
+        unsigned long long bits;
+        memcpy(&bits, &bound, sizeof(bits));
+        const int ex = (int)((bits >> 52) & 0x7FF);
         int k;
-        frexp(bound, &k);   // bound < 2^k
+        if (ex != 0) k = ex - 1022;
+        else frexp(bound, &k);
         e = 62 - k;         // |sum| <= bound * 2^e < 2^62
     }
     if (e > 240) e = 240;
     if (e < -240) e = -240;
     Fix f;
-    f.sd = ldexp(1.0, e);
-    f.inv = ldexp(1.0, -e);
-    f.s1 = (float)ldexp(1.0, e / 2);
-    f.s2 = (float)ldexp(1.0, e - e / 2);
-    f.i1 = (float)ldexp(1.0, -(e / 2));
-    f.i2 = (float)ldexp(1.0, -(e - e / 2));
+    f.sd = pow2d(e);
+    f.inv = pow2d(-e);
+    f.s1 = pow2f(e / 2);
+    f.s2 = pow2f(e - e / 2);
+    f.i1 = pow2f(-(e / 2));
+    f.i2 = pow2f(-(e - e / 2));
     return f;
 }
 
@@ -164,9 +187,24 @@ __device__ __forceinline__ void atomic_max_pos(unsigned int *slot, float v) {
 // reference's delta_def_grad minus the identity.
 // ---------------------------------------------------------------------------
 // MatLinElast (constitutive_model.cpp:16-60): incremental, engineering shear.
+// Hardware reciprocal (rcp.approx: one MUFU operation, deterministic, within
+// about an ulp of 1/x).  The FP32 path uses it where an IEEE division would
+// cost a slow-path sequence per particle: the normalisation of gathers by
+// their weight sum and the material constants; FP64 keeps 1.0 / x.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+template <typename R>
+__device__ __forceinline__ R recip(R x) {
+    if constexpr (sizeof(R) == 4) return rcp_approx(x);
+    else return (R)1 / x;
+}
+
 template <typename R>
 __device__ __forceinline__ void lin_elast_update(R *s, const R D[3][3], R E, R nu) {
-    const R rd = (R)1 / (((R)1 - (R)2 * nu) * ((R)1 + nu));   // one division (FP64 divisions are slow here)
+    const R rd = recip<R>(((R)1 - (R)2 * nu) * ((R)1 + nu));   // one division
     const R C0 = E * ((R)1 - nu) * rd;
     const R C1 = E * nu * rd;
     const R C2 = (R)0.5 * E * ((R)1 - (R)2 * nu) * rd;
@@ -209,22 +247,24 @@ __device__ __forceinline__ R neo_hookean_stress(R *s, const R F[3][3], R jac, R 
 // used by the FP32 path, which stores H: be - I = H + H^T + H H^T keeps the
 // small strain out of the rounding of F F^T.
 __device__ __forceinline__ void neo_hookean_stress_h(float *s, const float H[3][3], float jm1, float E, float nu) {
-    const float lmd = nu * E / ((1.0f + nu) * (1.0f - 2.0f * nu));
-    const float mu = E / (2.0f * (1.0f + nu));
+    const float rd = rcp_approx((1.0f + nu) * (1.0f - 2.0f * nu));
+    const float lmd = nu * E * rd;
+    const float mu = 0.5f * E * (1.0f - 2.0f * nu) * rd;
     const float lnj = log1pf(jm1);
     const float J = 1.0f + jm1;
+    const float ij = rcp_approx(J);
     float bm[3][3];
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int j = 0; j < 3; j++)
             bm[i][j] = H[i][j] + H[j][i] + H[i][0] * H[j][0] + H[i][1] * H[j][1] + H[i][2] * H[j][2];
-    s[0] = (mu * bm[0][0] + lmd * lnj) / J;
-    s[1] = (mu * bm[1][1] + lmd * lnj) / J;
-    s[2] = (mu * bm[2][2] + lmd * lnj) / J;
-    s[3] = (mu * bm[1][2]) / J;
-    s[4] = (mu * bm[0][2]) / J;
-    s[5] = (mu * bm[0][1]) / J;
+    s[0] = (mu * bm[0][0] + lmd * lnj) * ij;
+    s[1] = (mu * bm[1][1] + lmd * lnj) * ij;
+    s[2] = (mu * bm[2][2] + lmd * lnj) * ij;
+    s[3] = (mu * bm[1][2]) * ij;
+    s[4] = (mu * bm[0][2]) * ij;
+    s[5] = (mu * bm[0][1]) * ij;
 }
 
 // MatStVk (constitutive_model.cpp:122-185), stress part: with b = F F^T and
@@ -258,7 +298,7 @@ __device__ __forceinline__ void stvk_stress(R *s, const R F[3][3], R jac, R E, R
 // mu b^2 + (lambda trE - mu) b = lambda trE (I + m) + mu (m + m^2), trE = tr m / 2,
 // free of the cancellation of numbers near 1.
 __device__ __forceinline__ void stvk_stress_h(float *s, const float H[3][3], float jm1, float E, float nu) {
-    const float rd = 1.0f / ((1.0f + nu) * (1.0f - 2.0f * nu));
+    const float rd = rcp_approx((1.0f + nu) * (1.0f - 2.0f * nu));
     const float lmd = nu * E * rd;
     const float mu = 0.5f * E * (1.0f - 2.0f * nu) * rd;
     float m[3][3], m2[3][3];
@@ -271,7 +311,7 @@ __device__ __forceinline__ void stvk_stress_h(float *s, const float H[3][3], flo
 #pragma unroll
         for (int j = 0; j < 3; j++) m2[i][j] = m[i][0] * m[0][j] + m[i][1] * m[1][j] + m[i][2] * m[2][j];
     const float lt = lmd * 0.5f * (m[0][0] + m[1][1] + m[2][2]);
-    const float ij = 1.0f / (1.0f + jm1);
+    const float ij = rcp_approx(1.0f + jm1);
     s[0] = (lt * (1.0f + m[0][0]) + mu * (m[0][0] + m2[0][0])) * ij;
     s[1] = (lt * (1.0f + m[1][1]) + mu * (m[1][1] + m2[1][1])) * ij;
     s[2] = (lt * (1.0f + m[2][2]) + mu * (m[2][2] + m2[2][2])) * ij;
@@ -335,7 +375,7 @@ __device__ __forceinline__ void mooney_rivlin_stress_h(float *s, const float H[3
         for (int j = 0; j < 3; j++) B2[i][j] = B[i][0] * B[0][j] + B[i][1] * B[1][j] + B[i][2] * B[2][j];
     const float tb = B[0][0] + B[1][1] + B[2][2];
     const float tb2 = B2[0][0] + B2[1][1] + B2[2][2];
-    const float ij = 1.0f / (1.0f + jm1);
+    const float ij = rcp_approx(1.0f + jm1);
     const float dg = 2.0f * ij * (c2 * tb - (c1 * tb + 4.0f * c2 * tb + c2 * tb * tb - c2 * tb2) / 3.0f) +
                      bulk * lj * ij;
     const float ca = 2.0f * ij * (c1 + c2 + c2 * tb), cb = 2.0f * ij * c2;
@@ -357,9 +397,9 @@ template <typename R>
 __device__ __forceinline__ void tait_stress(R *s, const R inc[3][3], R jm1, R rho0, R c0, R gam, R mu, R inv_dt) {
     R pr;
     if constexpr (sizeof(R) == 8) pr = rho0 * c0 * c0 / gam * expm1(-gam * log1p(jm1));
-    else pr = rho0 * c0 * c0 / gam * expm1f(-gam * log1pf(jm1));
+    else pr = rho0 * c0 * c0 * rcp_approx(gam) * expm1f(-gam * log1pf(jm1));
     const R d0 = inc[0][0] * inv_dt, d1 = inc[1][1] * inv_dt, d2 = inc[2][2] * inv_dt;
-    const R tr3 = (d0 + d1 + d2) / (R)3;
+    const R tr3 = (d0 + d1 + d2) * ((R)1 / (R)3);
     s[0] = -pr + (R)2 * mu * (d0 - tr3);
     s[1] = -pr + (R)2 * mu * (d1 - tr3);
     s[2] = -pr + (R)2 * mu * (d2 - tr3);

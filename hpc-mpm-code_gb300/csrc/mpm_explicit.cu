@@ -132,15 +132,6 @@ __device__ __forceinline__ void load_scales_musl(const StepArgs<R> &a, Scales &s
     load_scales_from<R>(&a.ctl->sc_musl, sh);
 }
 
-// Hardware reciprocal (rcp.approx: one MUFU operation, deterministic, within
-// about an ulp); used to normalise gathers by their weight sum, which is 1
-// to within a few ulps, so the approximation error does not matter.
-__device__ __forceinline__ float rcp_approx(float x) {
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
 // Block-wide reduction (fixed order: deterministic); result valid in thread 0.
 template <typename T, typename Op>
 __device__ __forceinline__ T block_reduce(T v, Op op, T *sh) {
@@ -1520,11 +1511,12 @@ __global__ void __launch_bounds__(256) k_grid1(StepArgs<R> a) {
             R vof = unfx((long long)a.acc[N + n], S.v, (R)0);
             R nv[3], na[3];
 #pragma unroll
+            const R im = (mass > a.mtol) ? recip<R>(mass) : (R)0;   // one reciprocal per node
             for (int c = 0; c < 3; c++) {
                 const R pc = unfx((long long)a.acc[(2 + c) * N + n], S.p, (R)0);
                 const R fc = unfx((long long)a.acc[(5 + c) * N + n], S.f, (R)0);
-                nv[c] = (mass > a.mtol) ? pc / mass : (R)0;
-                na[c] = (mass > a.mtol) ? fc / mass : (R)0;
+                nv[c] = pc * im;
+                na[c] = fc * im;
             }
             if (vof < a.mtol) vof = (R)0;
             const unsigned char bf = a.bcflag[n];
@@ -1612,9 +1604,10 @@ __global__ void __launch_bounds__(256) k_grid2(StepArgs<R> a) {
         const R mass = unfx((long long)a.acc[n], S.m, (R)0);
         R nv[3];
 #pragma unroll
+        const R im = (mass > a.mtol) ? recip<R>(mass) : (R)0;
         for (int c = 0; c < 3; c++) {
             const R pc = unfx((long long)a.acc2[c * N + n], S.q, (R)0);
-            nv[c] = (mass > a.mtol) ? pc / mass : (R)0;
+            nv[c] = pc * im;
         }
         const unsigned char bf = a.bcflag[n];
         if (bf) {
@@ -1790,7 +1783,8 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
             R jm1;
             if constexpr (sizeof(R) == 8) jm1 = J - (R)1;
             else jm1 = det_ipm1(Fn);
-            tait_stress<R>(s, Dm, jm1, ld(P.m + p) / ld(P.vol0 + p), E, nu, (R)a.matprop[3 * mid + 2], (R)1 / a.dt);
+            tait_stress<R>(s, Dm, jm1, ld(P.m + p) * recip<R>(ld(P.vol0 + p)), E, nu, (R)a.matprop[3 * mid + 2],
+                           recip<R>(a.dt));
         } else if (model == -1) {
 #pragma unroll
             for (int k = 0; k < 6; k++) s[k] = (R)0;
@@ -1935,7 +1929,8 @@ __device__ __forceinline__ void update_particle(const StepArgs<float> &a, const 
     else if (model == 2) stvk_stress_h(s, Hn, jm1, E, nu);
     else if (model == 3) mooney_rivlin_stress_h(s, Hn, jm1, E, nu, (float)a.matprop[3 * mid + 2]);
     else if (model == 4)
-        tait_stress<float>(s, D, jm1, P.m[p] / vol0, E, nu, (float)a.matprop[3 * mid + 2], 1.0f / a.dt);
+        tait_stress<float>(s, D, jm1, P.m[p] * rcp_approx(vol0), E, nu, (float)a.matprop[3 * mid + 2],
+                           rcp_approx(a.dt));
     else if (model == -1)
 #pragma unroll
         for (int k = 0; k < 6; k++) s[k] = 0.0f;
