@@ -62,6 +62,7 @@ struct ImpState {
     double *xstar = nullptr, *ev = nullptr; // training-pair harvest: converged solution, error
     double *gp = nullptr, *gq = nullptr;    // flexible GCR: GM directions and their images (GM * 3 * nodec)
     double *gqq = nullptr, *gbeta = nullptr;  // |A p|^2 of each kept direction, projection coefficients
+    float *gqf = nullptr;                   // FP32 copies of the kept images (GM * 3 * nodec), for the dots
     unsigned *cnt = nullptr;                // block counters of the single-launch reductions (zero between launches)
     int fallbacks = 0;                      // solves that switched from the network to Jacobi
     int nn_applications = 0;
@@ -422,8 +423,8 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 // lane adds 2V - 1 + log2(32 / V) numbers instead of 5 V.  FP64 adds are the
 // scarce resource on this part.  Returns the value index whose warp total the
 // lane holds in v[0] (every lane of a group of 32 / V lanes holds it).
-template <int V>
-__device__ __forceinline__ int warp_sums(double (&v)[V]) {
+template <int V, typename T>
+__device__ __forceinline__ int warp_sums(T (&v)[V]) {
     const int lane = threadIdx.x & 31;
     int j = 0, o = 16;
 #pragma unroll
@@ -431,8 +432,8 @@ __device__ __forceinline__ int warp_sums(double (&v)[V]) {
         const bool up = (lane & o) != 0;
 #pragma unroll
         for (int i = 0; i < h; i++) {
-            const double send = up ? v[i] : v[i + h];
-            const double keep = up ? v[i + h] : v[i];
+            const T send = up ? v[i] : v[i + h];
+            const T keep = up ? v[i + h] : v[i];
             v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
         }
         if (up) j += h;
@@ -940,26 +941,48 @@ __device__ __forceinline__ int gcr_prev(int slot, int j, int w) { return (slot -
 // which then reduces the partials in block order (last_sum), so the sums
 // are reproducible without a separate reduction launch.
 // flexible GCR: the dots q . Q_j of the new image with the kept ones, then
-// (last block) beta_j = (q . Q_j) / (Q_j . Q_j)
-__global__ void __launch_bounds__(256) k_gcr_dots(ImpArgs a, const double *Q, int slot, int used, int w, double *part,
-                                                  unsigned *cnt, const double *qq, double *beta) {
+// (last block) beta_j = (q . Q_j) / (Q_j . Q_j).  beta only has to be close:
+// the same beta_j update both the direction and its image (k_gcr_axpy, in
+// FP64), so A p = q holds whatever their accuracy and only the
+// orthogonality of the kept images is at FP32 level.  So the dots run in
+// FP32 on FP32 copies of the kept images (the FP64 pipe is this part's
+// scarce resource), and the block partials are summed in FP64.
+__global__ void __launch_bounds__(256) k_gcr_dots(ImpArgs a, const double *Q, const float *Qf, int slot, int used,
+                                                  int w, double *part, unsigned *cnt, const double *qq,
+                                                  double *beta) {
     __shared__ double sh[32];
+    __shared__ double shw[GM][8];
+    __shared__ bool s_last;
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const size_t N = (size_t)a.nodec, st = 3 * N;
-    double d[GM];
+    float d[GM];
 #pragma unroll
-    for (int j = 0; j < GM; j++) d[j] = 0.0;
+    for (int j = 0; j < GM; j++) d[j] = 0.0f;
     if (n < a.nodec) {
         const double *q = Q + (size_t)slot * st;
-        const double q0 = q[n], q1 = q[N + n], q2 = q[2 * N + n];
+        const float q0 = (float)q[n], q1 = (float)q[N + n], q2 = (float)q[2 * N + n];
 #pragma unroll
         for (int j = 0; j < GM; j++)
             if (j < used) {
-                const double *qj = Q + (size_t)gcr_prev(slot, j, w) * st;
+                const float *qj = Qf + (size_t)gcr_prev(slot, j, w) * st;
                 d[j] = q0 * qj[n] + q1 * qj[N + n] + q2 * qj[2 * N + n];
             }
     }
-    if (!partials_last<GM>(d, used, part, cnt)) return;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int jv = warp_sums<GM>(d);
+    if ((lane & (32 / GM - 1)) == 0) shw[jv][wid] = (double)d[0];
+    __syncthreads();
+    if ((int)threadIdx.x < used) {
+        double t = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += shw[threadIdx.x][q];
+        part[threadIdx.x * gridDim.x + blockIdx.x] = t;
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
     for (int j = 0; j < used; j++) {
         const double t = last_sum(part, j, sh);
         if (threadIdx.x == 0) {
@@ -970,10 +993,11 @@ __global__ void __launch_bounds__(256) k_gcr_dots(ImpArgs a, const double *Q, in
     if (threadIdx.x == 0) *cnt = 0u;
 }
 
-// p -= sum beta_j P_j, q -= sum beta_j Q_j; then (last block) q.r and q.q
-__global__ void __launch_bounds__(256) k_gcr_axpy(ImpArgs a, double *P, double *Q, int slot, int used, int w,
-                                                  const double *beta, const double *r, double *part, unsigned *cnt,
-                                                  double *scal) {
+// p -= sum beta_j P_j, q -= sum beta_j Q_j (FP64; an FP32 copy of q is kept
+// for the dots); then (last block) q.r and q.q
+__global__ void __launch_bounds__(256) k_gcr_axpy(ImpArgs a, double *P, double *Q, float *Qf, int slot, int used,
+                                                  int w, const double *beta, const double *r, double *part,
+                                                  unsigned *cnt, double *scal) {
     __shared__ double sh[32];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     const size_t N = (size_t)a.nodec, st = 3 * N;
@@ -995,6 +1019,7 @@ __global__ void __launch_bounds__(256) k_gcr_axpy(ImpArgs a, double *P, double *
                 }
             p[i] = pv;
             q[i] = qv;
+            Qf[(size_t)slot * st + i] = (float)qv;   // the copy k_gcr_dots reads
             v[0] += qv * r[i];
             v[1] += qv * qv;
         }
@@ -1066,6 +1091,7 @@ void implicit_free(mpm_ctx *c) {
     for (double *b : bufs)
         if (b) cudaFree(b);
     if (s->cnt) cudaFree(s->cnt);
+    if (s->gqf) cudaFree(s->gqf);
     if (s->h_scal) cudaFreeHost(s->h_scal);
     for (cudaGraphExec_t g : {s->g_cg, s->g_fcg_nn, s->g_fcg_jac, s->g_gcr})
         if (g) cudaGraphExecDestroy(g);
@@ -1130,6 +1156,7 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
     CKI(cudaMalloc((void **)&s->gq, sizeof(double) * GM * 3 * N));
     CKI(cudaMalloc((void **)&s->gqq, sizeof(double) * GM));
     CKI(cudaMalloc((void **)&s->gbeta, sizeof(double) * GM));
+    CKI(cudaMalloc((void **)&s->gqf, sizeof(float) * GM * 3 * N));
     CKI(cudaMalloc((void **)&s->cnt, sizeof(unsigned) * 8));
     CKI(cudaMemset(s->cnt, 0, sizeof(unsigned) * 8));
     CKI(cudaMalloc((void **)&s->nmass, sizeof(double) * N));
@@ -1277,8 +1304,8 @@ static mpm_status gcr_iter(mpm_ctx *c, const ImpArgs &a, int nb, int u, int sl) 
     timer_end(c, K_MATVEC);
     timer_begin(c, K_KRYLOV);
     if (u > 0)
-        k_gcr_dots<<<nb, 256, 0, c->stream>>>(a, s->gq, sl, u, s->gm, s->part, s->cnt, s->gqq, s->gbeta);
-    k_gcr_axpy<<<nb, 256, 0, c->stream>>>(a, s->gp, s->gq, sl, u, s->gm, s->gbeta, s->r, s->part, s->cnt + 1,
+        k_gcr_dots<<<nb, 256, 0, c->stream>>>(a, s->gq, s->gqf, sl, u, s->gm, s->part, s->cnt, s->gqq, s->gbeta);
+    k_gcr_axpy<<<nb, 256, 0, c->stream>>>(a, s->gp, s->gq, s->gqf, sl, u, s->gm, s->gbeta, s->r, s->part, s->cnt + 1,
                                           s->scal);
     k_gcr_update<<<nb, 256, 0, c->stream>>>(a, s->scal, s->xs, s->r, s->gp, s->gq, sl, s->gqq, s->part,
                                             s->cnt + 2);
