@@ -91,3 +91,34 @@ def test_symmetric_preconditioner_is_symmetric():
     gpu.set_precond(None)
     gpu.sync()
     assert abs(lhs - rhs) <= 3e-2 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+
+
+def test_committed_network_on_the_full_cantilever():
+    """The committed parameters (weights/precond_cantilever64.f32, trained by
+    mpm_gb300.train_precond) on the 1,728,000-particle cantilever they were
+    trained for: the system after one implicit step is solved to
+    ||r|| / ||r0|| <= 1e-8 on the true FP64 residual by both solvers; the
+    learned solver needs at most a third of Jacobi-PCG's iterations and the
+    two solutions agree to 1e-5; a following implicit step with the network
+    falls back to Jacobi nowhere."""
+    from mpm_gb300 import train_precond
+
+    params = train_precond.load_weights()
+    if params is None:
+        pytest.skip("no committed preconditioner parameters")
+    s = scenes.cantilever(iprop=1)
+    gpu = capi.GpuImplicitSolid(s, nr_flag=True)
+    gpu.implicit_steps(1, eps=EPS)
+    gpu.assemble()
+    xj, itj = gpu.solve(eps=EPS)
+    net = capi.PrecondNet(s.xynodec)
+    net.set_params(params)
+    gpu.set_precond(net)
+    xn, itn = gpu.solve(eps=EPS)
+    st = gpu.implicit_steps(1, eps=EPS, full=True)   # a whole step with the network: its statistics
+    gpu.set_precond(None)
+    gpu.sync()
+    print(f"\nfull cantilever: Jacobi-PCG {itj} iterations, learned GCR {itn} iterations; next step {st}")
+    assert rel_l2(xn, xj) <= 1e-5
+    assert 3 * itn <= itj, (itn, itj)
+    assert st["precond_fallbacks"] == 0 and st["nn_applications"] > 0, st
