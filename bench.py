@@ -59,8 +59,8 @@ def parse():
                     help="steps of the 12.6M-particle Tait dam break (0 skips)")
     ap.add_argument("--train-pairs", type=int, default=2000,
                     help="training pairs when no committed preconditioner parameters exist")
-    ap.add_argument("--implicit-steps", type=int, default=3,
-                    help="implicit cantilever steps timed after the explicit run (0 skips)")
+    ap.add_argument("--implicit-steps", type=int, default=50,
+                    help="implicit cantilever steps timed per solver after the explicit run (50: the mean over 50 steps; 0 skips)")
     ap.add_argument("--cells", type=int, default=80,
                     help="block edge in cells (80 = the 4,096,000-particle workload; smaller for profiling)")
     return ap.parse_args()
@@ -279,6 +279,15 @@ def run_implicit(args, torch, stream):
     gpu.set_precond(net)
     nn_ms, nn = timed(gpu)
     nn_solve_ms, nn_solve_it = timed_solve(gpu)
+    # one application of the network: CUDA-event kernel timers over one more
+    # solve (timers run the solve without graphs; the per-class time is the
+    # network's kernels, from the input scaling to the output layer)
+    gpu.enable_kernel_timing(True)
+    gpu.solve(eps=1.0e-16, download=False)
+    kt = gpu.kernel_times()
+    gpu.enable_kernel_timing(False)
+    gpu.sync()
+    nn_app_ms = kt["precond_nn"][0] / max(kt["precond_nn"][1], 1) if "precond_nn" in kt else None
     gpu.close()
     net.close()
     out["learned"] = {"value": nn_ms, "unit": "ms/step",
@@ -290,6 +299,27 @@ def run_implicit(args, torch, stream):
                       "fallbacks": nn["precond_fallbacks"], "network_applications": nn["nn_applications"],
                       "training": training,
                       "speedup_vs_jacobi": jac_ms / nn_ms if nn_ms > 0 else None}
+    # algorithmic FLOPs of one application: sum over the five 3x3x3
+    # convolutions of output nodes x 2 x 27 x C_in x C_out (real channels)
+    n0 = list(s.xynodec)
+    n1 = [m // 2 + 1 for m in n0]
+    n2 = [m // 2 + 1 for m in n1]
+    v0, v1, v2 = (int(np.prod(v)) for v in (n0, n1, n2))
+    flops = 2 * 27 * (v0 * 6 * 16 + v1 * 16 * 32 + v2 * 32 * 64 + v2 * 64 * 32 + v1 * 32 * 16)
+    tc_peak = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            tc_peak = json.load(f).get("bf16_tflops")
+    except (OSError, ValueError):
+        pass
+    if nn_app_ms:
+        ach = flops / (nn_app_ms * 1e-3) / 1e12
+        out["learned"]["network"] = {
+            "us_per_application": nn_app_ms * 1e3, "flops_per_application": flops,
+            "roofline": {"bound": "tensor", "achieved": ach, "peak": tc_peak, "unit": "TFLOP/s",
+                         "frac": ach / tc_peak if tc_peak else None,
+                         "note": "latency-bound: the five convolutions run on 65^3, 33^3 and 17^3 grids "
+                                 "out of L2; the tensor pipe is 7-13 % busy (ncu)"}}
     out["solve"] = {"what": "one linear solve of the assembled system after the timed steps, from x = 0 to "
                             "||r||/||r0|| <= 1e-8, solution left on the device",
                     "jacobi_ms": jac_solve_ms, "jacobi_iters": jac_solve_it,

@@ -1199,6 +1199,11 @@ static mpm_status imp_p2g(mpm_ctx *c, double facl) {
 // one linear solve of the assembled, scaled system; s->x holds the initial
 // guess (physical) and receives the physical solution.  Returns iterations.
 static constexpr int KCHECK = 8;   // Krylov iterations between residual checks (and per graph)
+// Within this factor of the tolerance (squared norms, 100x in the norm) the
+// solvers leave the 8-iteration graphs and check after every iteration, so
+// that a solve stops at the iteration that reaches the tolerance instead of
+// at the end of the next block of 8.
+static constexpr double FINE_FACTOR = 1.0e4;
 
 static bool graphs_on(mpm_ctx *c) { return c->use_graph && c->stream != nullptr && !c->timer.on && !c->imp->no_graph; }
 
@@ -1251,8 +1256,9 @@ static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
     const double rr0 = s->h_scal[S_RR0];
     int it = 0;
     bool done = !(rr0 > 1.0e-300);
+    bool fine = false;   // close to the tolerance: one iteration at a time, checked after each
     while (!done && it < kmax) {
-        if (graphs_on(c) && it % KCHECK == 0 && it + KCHECK <= kmax) {
+        if (graphs_on(c) && !fine && it % KCHECK == 0 && it + KCHECK <= kmax) {
             if (!s->g_cg && capture_iters(c, &s->g_cg, [&] {
                     for (int k = 0; k < KCHECK; k++) cg_iteration(c, a, nb, k);
                 }) != MPM_OK)
@@ -1268,7 +1274,7 @@ static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
             cg_iteration(c, a, nb, it);
             it++;
         }
-        if (it % KCHECK == 0 || it == kmax) {
+        if (it % KCHECK == 0 || it == kmax || fine) {
             CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream));
             CKI(cudaStreamSynchronize(c->stream));
             const double rr = s->h_scal[(it & 1) ? S_RR1 : S_RR0];
@@ -1278,6 +1284,7 @@ static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
             }
             if (s->debug) fprintf(stderr, "mpm_gb300 cg: it %d |r|/|r0| %.3e\n", it, sqrt(rr / rr0));
             if (rr < eps * rr0) done = true;
+            else if (rr < FINE_FACTOR * eps * rr0) fine = true;
             s->last_rel = sqrt(rr / rr0);
         }
     }
@@ -1395,9 +1402,10 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
         const size_t st3 = 3 * N;
         int used = 0, slot = 0;
         double rr_win = rr0;
+        bool fine = false;   // close to the tolerance: one iteration at a time, checked after each
         auto gcr_iteration = [&](int u, int sl) -> mpm_status { return gcr_iter(c, a, nb, u, sl); };
         while (!done && use_nn && it < kmax) {
-            if (graphs_on(c) && used == s->gm && slot == 0 && it % check == 0 && it + check <= kmax) {
+            if (graphs_on(c) && !fine && used == s->gm && slot == 0 && it % check == 0 && it + check <= kmax) {
                 const int64_t l0 = c->launches;
                 if (!s->g_gcr && capture_iters(c, &s->g_gcr, [&] {
                         for (int k = 0; k < check; k++) gcr_iteration(s->gm, k % s->gm);
@@ -1417,7 +1425,7 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
                 slot = (slot + 1) % s->gm;
                 it++;
             }
-            if (it % check == 0 || it == kmax) {
+            if (it % check == 0 || it == kmax || fine) {
                 CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, c->stream));
                 CKI(cudaStreamSynchronize(c->stream));
                 double rr = s->h_scal[S_RRC];
@@ -1439,11 +1447,14 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
                     used = 0;   // the residual was replaced: the kept directions no longer apply
                     slot = 0;
                 }
-                if (!done && !(rr < 0.25 * rr_win)) {
-                    use_nn = false;   // less than a halving of |r| per window: Jacobi does better
-                    s->fallbacks++;
+                if (!done && rr < FINE_FACTOR * eps * rr0) fine = true;
+                if (it % check == 0 || it == kmax) {   // the window test, at window ends only
+                    if (!done && !(rr < 0.25 * rr_win)) {
+                        use_nn = false;   // less than a halving of |r| per window: Jacobi does better
+                        s->fallbacks++;
+                    }
+                    rr_win = rr;
                 }
-                rr_win = rr;
                 s->last_rel = sqrt(rr / rr0);
             }
         }
