@@ -724,7 +724,7 @@ mpm_status mpm_gpu_autotune(mpm_ctx *c, int steps_per_trial, double facl) {
     // every candidate computes bitwise the same step, so the trial steps are
     // ordinary simulation steps; each kernel class is timed on its own
     const int p2g_opts[3] = {2, 3, 2}, stg_opts[3] = {1, 0, 0}, musl_opts[3] = {3, 2, 3}, mstg_opts[3] = {1, 0, 0};
-    const int upd_opts[3] = {4, 0, 6};
+    const int upd_opts[3] = {3, 0, 2};
     double best[3] = {1e300, 1e300, 1e300};
     Tune pick = c->tune;
     const bool was_on = c->timer.on;
@@ -765,14 +765,14 @@ mpm_status mpm_gpu_autotune(mpm_ctx *c, int steps_per_trial, double facl) {
 
 mpm_status mpm_gpu_set_tuning(mpm_ctx *c, int p2g_minb, int musl_minb, int update_ctas_per_sm) {
     if (!c) return MPM_ERR_BAD_ARG;
-    if ((p2g_minb < 0 || p2g_minb == 1 || p2g_minb > 6) || (musl_minb < 0 || musl_minb == 1 || musl_minb > 4) ||
+    if ((p2g_minb < 0 || p2g_minb == 1 || p2g_minb > 7) || (musl_minb < 0 || musl_minb == 1 || musl_minb > 5) ||
         update_ctas_per_sm < 0 || update_ctas_per_sm > 8)
         return MPM_ERR_BAD_ARG;
     c->tune.p2g_staged = p2g_minb == 0;
-    c->tune.p2g_moments = p2g_minb == 4 ? 1 : p2g_minb == 5 ? 2 : p2g_minb == 6 ? 3 : 0;
+    c->tune.p2g_moments = p2g_minb == 4 ? 1 : p2g_minb == 5 ? 2 : p2g_minb == 6 ? 3 : p2g_minb == 7 ? 4 : 0;
     if (p2g_minb == 2 || p2g_minb == 3) c->tune.p2g_minb = p2g_minb;
     c->tune.musl_staged = musl_minb == 0 ? 1 : musl_minb == 4 ? 2 : 0;
-    if (musl_minb == 2 || musl_minb == 3) c->tune.musl_minb = musl_minb;
+    if (musl_minb == 2 || musl_minb == 3 || musl_minb == 5) c->tune.musl_minb = musl_minb;
     c->tune.update_ctas_per_sm = update_ctas_per_sm;
     return MPM_OK;
 }

@@ -2020,7 +2020,8 @@ constexpr int UNF = 20;                           // staged real fields
 constexpr size_t USTAGE = (size_t)UNF * UCH * 4 + UCH * 4;   // bytes per stage
 constexpr unsigned UWAIT = 1u << 22;              // bounded mbarrier wait (try_wait iterations)
 
-__global__ void __launch_bounds__(UCH) k_g2p_update_tma(StepArgs<float> a, int nchunks) {
+// At most 80 registers, so that three CTAs (24 warps) are resident per SM.
+__global__ void __launch_bounds__(UCH, 3) k_g2p_update_tma(StepArgs<float> a, int nchunks) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) unsigned long long bar[2];
     __shared__ float sh_f[32];
@@ -2214,6 +2215,8 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                     k_p2g_brick<<<c->g.nbricks, BCH, 0, c->stream>>>(a);
                 } else if (c->tune.p2g_moments == 2) {
                     k_p2g_cell_mom<1, false><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                } else if (c->tune.p2g_moments == 4) {
+                    k_p2g_cell_mom<3, true><<<list_grid(c, 3), CELL_THREADS, 0, c->stream>>>(a);
                 } else if (c->tune.p2g_moments) {
                     if (c->tune.brick_list)
                         k_p2g_cell_mom<2, true><<<list_grid(c, 2), CELL_THREADS, 0, c->stream>>>(a);
@@ -2258,6 +2261,8 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                     k_g2p_musl_cell_staged<3><<<c->g.nbricks, CELL_THREADS, 2 * MSTAGE, c->stream>>>(a);
                 } else if (c->tune.musl_minb == 2) {
                     k_g2p_musl_cell<2, false><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                } else if (c->tune.musl_minb == 5) {
+                    k_g2p_musl_cell<4, true><<<list_grid(c, 4), CELL_THREADS, 0, c->stream>>>(a);
                 } else if (c->tune.brick_list) {
                     k_g2p_musl_cell<3, true><<<list_grid(c, 3), CELL_THREADS, 0, c->stream>>>(a);
                 } else {

@@ -114,7 +114,7 @@ struct Tune {
     int p2g_minb = 2;               // resident CTAs the direct per-cell P2G is compiled for (2 or 3)
     int musl_staged = 0;            // gather + MUSL reads the brick's particles from staged shared memory
     int musl_minb = 3;              // resident CTAs the direct gather + MUSL kernel is compiled for
-    int update_ctas_per_sm = 4;     // persistent CTAs per SM of the staged particle update (0: per-brick update)
+    int update_ctas_per_sm = 3;     // persistent CTAs per SM of the staged particle update (0: per-brick update)
     bool done = false;
 };
 

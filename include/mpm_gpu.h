@@ -175,9 +175,13 @@ mpm_status mpm_gpu_enable_kernel_timing(mpm_ctx *ctx, int on);
 mpm_status mpm_gpu_autotune(mpm_ctx *ctx, int steps_per_trial, double facl);
 /* p2g_minb / musl_minb: 0 = the shared-memory staged kernel, 2 or 3 = the
  * direct per-cell kernel compiled for that many resident CTAs per SM;
- * update_ctas_per_sm: 1..8 persistent CTAs per SM of the bulk-copy staged
- * particle update, 0 = the update with one CTA per brick and the brick's
- * nodal values in shared memory. */
+ * p2g_minb 4 (default) / 5 / 7 = the moment-form P2G over the active-brick
+ * list for 2 / 1 / 3 resident CTAs per SM, 6 = chunked bricks; musl_minb 4 =
+ * one CTA per brick, 5 = the gather over the brick list for 4 resident CTAs
+ * per SM (3 is the default); update_ctas_per_sm: 1..8 persistent CTAs per SM
+ * of the bulk-copy staged particle update (3, the default, is what its 80
+ * registers let reside), 0 = the update with one CTA per brick and the
+ * brick's nodal values in shared memory. */
 mpm_status mpm_gpu_get_tuning(mpm_ctx *ctx, int *p2g_minb, int *musl_minb, int *update_ctas_per_sm);
 mpm_status mpm_gpu_set_tuning(mpm_ctx *ctx, int p2g_minb, int musl_minb, int update_ctas_per_sm);
 mpm_status mpm_gpu_kernel_times(mpm_ctx *ctx, int *count, const char **names, double *ms, int64_t *launches);
