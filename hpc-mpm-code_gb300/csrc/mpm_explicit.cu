@@ -2328,7 +2328,7 @@ template <typename R>
 static mpm_status grid_kernel(mpm_ctx *c, int which) {
     StepArgs<R> a = make_args<R>(c);
     const bool list = !a.all_tiles;
-    const int lgrid = std::min(c->g.ntiles, 4 * num_sms());
+    const int lgrid = std::min(c->g.ntiles, 6 * num_sms());   // 40 registers: 6 CTAs of 256 reside per SM
     if (which == 0) {
         timer_begin(c, K_GRID1);
         if (list) {
