@@ -77,3 +77,18 @@ def test_uniform_translation(precision):
     x0 = s.coord.copy()
     p = _run(s, precision)
     _check(p, s, v0, x0 + NSTEPS * DT * v0[None, :], precision)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_p_wave_speed(precision):
+    """The compression front of the driven bar (tests/kat_pwave.py) travels
+    at sqrt((lambda + 2 mu) / rho) within 3 %, FP64 and FP32."""
+    import kat_pwave as kp
+
+    s = kp.bar()
+    x0 = s.coord.copy()
+    gpu = capi.GpuSolid(s, precision=precision, shifting=False)
+    c = kp.measured_speed(gpu.steps, lambda: gpu.particles()["v"], x0)
+    gpu.sync()
+    gpu.close()
+    assert abs(c / kp.C_P - 1.0) <= 0.03, (c, kp.C_P)

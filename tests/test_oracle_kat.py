@@ -35,3 +35,15 @@ def test_oracle_known_answers(gravity, scheme):
     assert np.max(np.abs(p["x"] - x_want)) <= 1e-13
     assert np.max(np.abs(p["F"] - np.eye(3)[None, :, :])) <= 1e-13
     assert np.max(np.abs(p["sigma"])) <= 1e-15 * E
+
+
+def test_oracle_p_wave_speed():
+    """The oracle's compression front travels at sqrt((lambda + 2 mu) / rho)
+    within 3 % (tests/kat_pwave.py)."""
+    import kat_pwave as kp
+
+    s = kp.bar()
+    x0 = s.coord.copy()
+    o = port.PortSolid(s, shifting=False)
+    c = kp.measured_speed(o.steps, lambda: o.particles()["v"], x0)
+    assert abs(c / kp.C_P - 1.0) <= 0.03, (c, kp.C_P)
