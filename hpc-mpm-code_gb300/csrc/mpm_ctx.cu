@@ -213,6 +213,13 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
 void mpm_gpu_destroy(mpm_ctx *c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    for (cudaStream_t st : {c->io_h2d, c->io_d2h})
+        if (st) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
+    for (cudaEvent_t e : c->io_ev)
+        if (e) cudaEventDestroy(e);
     drop_graph(c);
     implicit_free(c);
     free_particles(c);
@@ -697,6 +704,76 @@ mpm_status mpm_gpu_upload_particles(mpm_ctx *c, const double *coord, const doubl
         k_state_scatter<float><<<nb, 256, 0, c->stream>>>((float *)c->pbuf[c->cur], N, c->pstride, c->nreal, st, mask, c->d_ctl, par);
     c->launches++;
     return check_launch(c);
+}
+
+// Explicit steps with the particle state read from and written back to host
+// arrays every step.  Uploads run on one copy stream, downloads on another,
+// per field: the upload of a field for step n + 1 waits only for the download
+// of the same field from step n, so it overlaps the downloads of the other
+// fields and both directions of the host link carry data at once.
+mpm_status mpm_gpu_steps_host(mpm_ctx *c, int nsteps, double facl, double *coord, double *vel, double *F,
+                              double *stress, double *vol) {
+    if (!c || nsteps < 0) return MPM_ERR_BAD_ARG;
+    if (c->num == 0 || nsteps == 0) return MPM_OK;
+    if (c->imp) return MPM_ERR_STATE;
+    mpm_status s = ensure_staging(c);
+    if (s != MPM_OK) return s;
+    if (!c->io_h2d) {
+        CK(cudaStreamCreateWithFlags(&c->io_h2d, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&c->io_d2h, cudaStreamNonBlocking));
+        for (cudaEvent_t &e : c->io_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    const size_t N = (size_t)c->num;
+    double *host[5] = {coord, vel, F, stress, vol};
+    const int off[5] = {ST_X, ST_V, ST_F, ST_S, ST_VOL}, width[5] = {3, 3, 9, 6, 1};
+    unsigned mask = 0;
+    for (int f = 0; f < 5; f++)
+        if (host[f]) mask |= 1u << f;
+    double *st = c->d_stage;
+    const int nb = (int)((N + 255) / 256);
+    // the copy streams start after the work already on the context's stream
+    CK(cudaEventRecord(c->io_ev[11], c->stream));
+    CK(cudaStreamWaitEvent(c->io_h2d, c->io_ev[11], 0));
+    CK(cudaStreamWaitEvent(c->io_d2h, c->io_ev[11], 0));
+    for (int step = 0; step < nsteps; step++) {
+        for (int f = 0; f < 5; f++) {
+            if (!host[f]) continue;
+            if (step > 0) CK(cudaStreamWaitEvent(c->io_h2d, c->io_ev[5 + f], 0));
+            CK(cudaMemcpyAsync(st + (size_t)off[f] * N, host[f], sizeof(double) * width[f] * N,
+                               cudaMemcpyHostToDevice, c->io_h2d));
+            CK(cudaEventRecord(c->io_ev[f], c->io_h2d));
+            CK(cudaStreamWaitEvent(c->stream, c->io_ev[f], 0));
+        }
+        const int par = (int)(c->step & 1);
+        if (c->precision == 64)
+            k_state_scatter<double><<<nb, 256, 0, c->stream>>>((double *)c->pbuf[c->cur], N, c->pstride, c->nreal, st,
+                                                                mask, c->d_ctl, par);
+        else
+            k_state_scatter<float><<<nb, 256, 0, c->stream>>>((float *)c->pbuf[c->cur], N, c->pstride, c->nreal, st,
+                                                               mask, c->d_ctl, par);
+        c->launches++;
+        if ((s = check_launch(c)) != MPM_OK) return s;
+        if ((s = mpm_gpu_step_explicit(c, 1, facl)) != MPM_OK) return s;
+        if (c->precision == 64)
+            k_state_gather<double><<<nb, 256, 0, c->stream>>>((const double *)c->pbuf[c->cur], N, c->pstride,
+                                                               c->nreal, st, mask);
+        else
+            k_state_gather<float><<<nb, 256, 0, c->stream>>>((const float *)c->pbuf[c->cur], N, c->pstride,
+                                                              c->nreal, st, mask);
+        c->launches++;
+        if ((s = check_launch(c)) != MPM_OK) return s;
+        CK(cudaEventRecord(c->io_ev[10], c->stream));
+        CK(cudaStreamWaitEvent(c->io_d2h, c->io_ev[10], 0));
+        for (int f = 0; f < 5; f++) {
+            if (!host[f]) continue;
+            CK(cudaMemcpyAsync(host[f], st + (size_t)off[f] * N, sizeof(double) * width[f] * N,
+                               cudaMemcpyDeviceToHost, c->io_d2h));
+            CK(cudaEventRecord(c->io_ev[5 + f], c->io_d2h));
+        }
+    }
+    CK(cudaStreamSynchronize(c->io_d2h));
+    CK(cudaStreamSynchronize(c->stream));
+    return MPM_OK;
 }
 
 mpm_status mpm_gpu_get_stats(mpm_ctx *c, mpm_stats *out) {

@@ -139,6 +139,9 @@ struct mpm_ctx {
     int nmat = 0;
     int npxye[3] = {1, 1, 1};
     cudaStream_t stream = nullptr;
+    // host I/O pipeline of mpm_gpu_steps_host: copy streams and per-field events
+    cudaStream_t io_h2d = nullptr, io_d2h = nullptr;
+    cudaEvent_t io_ev[12] = {};   // [0,5) uploads done, [5,10) downloads done, 10 gather done, 11 start
     // materials on device
     int *d_iprop = nullptr;
     double *d_matprop = nullptr;

@@ -65,7 +65,7 @@ _ip = C.POINTER(C.c_int)
 EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_status_string",
            "mpm_gpu_load_particles", "mpm_gpu_set_bc", "mpm_gpu_p2g", "mpm_gpu_grid_update", "mpm_gpu_g2p",
            "mpm_gpu_step_explicit", "mpm_gpu_download_nodal", "mpm_gpu_download_particles",
-           "mpm_gpu_upload_particles", "mpm_gpu_sync",
+           "mpm_gpu_upload_particles", "mpm_gpu_steps_host", "mpm_gpu_sync",
            "mpm_gpu_get_stats", "mpm_gpu_enable_kernel_timing", "mpm_gpu_kernel_times", "mpm_gpu_implicit_setup",
            "mpm_gpu_implicit_step", "mpm_gpu_implicit_assemble", "mpm_gpu_implicit_get_system",
            "mpm_gpu_implicit_matvec", "mpm_gpu_implicit_solve", "mpm_gpu_p2g_noalloc", "mpm_gpu_autotune",
@@ -100,6 +100,7 @@ def load(path: str | None = None):
     lib.mpm_gpu_download_nodal.argtypes = [C.c_void_p, C.c_int, _dp]
     lib.mpm_gpu_download_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
     lib.mpm_gpu_upload_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
+    lib.mpm_gpu_steps_host.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, _dp, _dp, _dp, _dp]
     lib.mpm_gpu_sync.argtypes = [C.c_void_p]
     lib.mpm_gpu_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     lib.mpm_gpu_enable_kernel_timing.argtypes = [C.c_void_p, C.c_int]
@@ -248,6 +249,12 @@ class GpuSolid:
         """Download into caller-provided C-contiguous float64 arrays (pinned for full speed)."""
         _chk(self.lib.mpm_gpu_download_particles(self.ctx, _ptr(coord), _ptr(vel), _ptr(F), _ptr(stress), _ptr(vol)),
              "mpm_gpu_download_particles")
+
+    def steps_host(self, n, coord=None, vel=None, F=None, stress=None, vol=None, facl=1.0):
+        """n explicit steps, each reading the state from and writing it back to
+        the given C-contiguous float64 arrays (pinned for full speed)."""
+        _chk(self.lib.mpm_gpu_steps_host(self.ctx, int(n), float(facl), _ptr(coord), _ptr(vel), _ptr(F), _ptr(stress),
+                                         _ptr(vol)), "mpm_gpu_steps_host")
 
     def upload_state(self, coord=None, vel=None, F=None, stress=None, vol=None):
         """Overwrite particle state from float64 host arrays in load order."""

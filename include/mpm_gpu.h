@@ -143,6 +143,15 @@ mpm_status mpm_gpu_download_particles(mpm_ctx *ctx, double *coord, double *vel, 
  * module/solid/solid_data_io.cpp:61-100). */
 mpm_status mpm_gpu_upload_particles(mpm_ctx *ctx, const double *coord, const double *vel, const double *F,
                                     const double *stress, const double *vol);
+/* nsteps explicit steps, each with the particle state uploaded from the host
+ * arrays before it and downloaded into them after it (the reference's time
+ * loop with the particle vectors on the host between steps); any pointer may
+ * be NULL (that field stays on the device).  Uploads and downloads run on
+ * two internal copy streams, pipelined field by field across steps, so both
+ * directions of the host link are busy at once.  Synchronises before
+ * returning.  Explicit contexts only. */
+mpm_status mpm_gpu_steps_host(mpm_ctx *ctx, int nsteps, double facl, double *coord, double *vel, double *F,
+                              double *stress, double *vol);
 /* Wait for the stream and return (and clear) any latched device error. */
 mpm_status mpm_gpu_sync(mpm_ctx *ctx);
 

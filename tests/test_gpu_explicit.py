@@ -151,6 +151,34 @@ def test_full_size_fp32_velocity_after_1000_steps():
     assert rel_l2(res[32]["x"], res[64]["x"]) <= 1e-5
 
 
+@pytest.mark.parametrize("precision", [64, 32])
+def test_steps_host_equals_upload_step_download(precision):
+    """mpm_gpu_steps_host (uploads and downloads pipelined on copy streams)
+    gives bitwise the state of the same steps made by upload, one step and
+    download in turn."""
+    s = scenes.spinning_block(grid=(40, 40, 40), cell_lo=(8, 8, 8), cells=(24, 24, 24), dt=2e-5)
+    n = s.num
+    runs = []
+    for pipelined in (False, True):
+        gpu = capi.GpuSolid(s, precision=precision)
+        p = gpu.particles()
+        hx, hv = np.ascontiguousarray(p["x"]), np.ascontiguousarray(p["v"])
+        hF, hs = np.ascontiguousarray(p["F"]).reshape(n, 9), np.ascontiguousarray(p["sigma"])
+        hvol = np.ascontiguousarray(p["vol"])
+        if pipelined:
+            gpu.steps_host(12, hx, hv, hF, hs, hvol)
+        else:
+            for _ in range(12):
+                gpu.upload_state(hx, hv, hF, hs, hvol)
+                gpu.steps(1)
+                gpu.download_into(hx, hv, hF, hs, hvol)
+        gpu.sync()
+        gpu.close()
+        runs.append((hx, hv, hF, hs, hvol))
+    for a_, b_ in zip(*runs):
+        assert np.array_equal(a_, b_)
+
+
 def test_state_upload_download_round_trip():
     """mpm_gpu_upload_particles / mpm_gpu_download_particles keep the load order."""
     g = load_golden("explicit_flip")
