@@ -510,7 +510,7 @@ def run_gb300(args):
     e2e = {"value": replica_throughput(n, e_steps, e_ms, world), "unit": METRIC, "h2d_bytes_per_step": state_bytes,
            "d2h_bytes_per_step": state_bytes, "steps": e_steps,
            "call": "mpm_gpu_steps_host: per step the particle state uploaded from and downloaded into FP64 host "
-                   "arrays in pinned memory, the copies pipelined field by field on two copy streams"}
+                   "arrays in pinned memory, the copies pipelined piece by piece on two copy streams"}
     gpu.sync()
 
     implicit = None

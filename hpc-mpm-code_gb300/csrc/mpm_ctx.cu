@@ -1,5 +1,6 @@
 // C ABI of the GB300 MPM transfer path: context lifetime, particle load,
 // boundary conditions, the explicit step and result downloads.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -118,6 +119,8 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     mpm_ctx *c = new (std::nothrow) mpm_ctx();
     if (!c) return MPM_ERR_OOM;
     if (const char *gn = getenv("MPM_GB300_GATHER_NORM")) c->gather_norm = atoi(gn) != 0;
+    if (const char *ic = getenv("MPM_GB300_IO_CHUNKS"))
+        c->io_chunks = std::max(1, std::min(mpm_ctx::IO_MAX_CHUNKS, atoi(ic)));
     Geom &g = c->g;
     long long nodec = 1;
     for (int d = 0; d < 3; d++) {
@@ -708,9 +711,10 @@ mpm_status mpm_gpu_upload_particles(mpm_ctx *c, const double *coord, const doubl
 
 // Explicit steps with the particle state read from and written back to host
 // arrays every step.  Uploads run on one copy stream, downloads on another,
-// per field: the upload of a field for step n + 1 waits only for the download
-// of the same field from step n, so it overlaps the downloads of the other
-// fields and both directions of the host link carry data at once.
+// in pieces (io_chunks per field, the small fields first): the upload of a
+// piece for step n + 1 waits only for the download of the same piece from
+// step n, so uploads overlap the remaining downloads and both directions of
+// the host link carry data at once.
 mpm_status mpm_gpu_steps_host(mpm_ctx *c, int nsteps, double facl, double *coord, double *vel, double *F,
                               double *stress, double *vol) {
     if (!c || nsteps < 0) return MPM_ERR_BAD_ARG;
@@ -718,31 +722,47 @@ mpm_status mpm_gpu_steps_host(mpm_ctx *c, int nsteps, double facl, double *coord
     if (c->imp) return MPM_ERR_STATE;
     mpm_status s = ensure_staging(c);
     if (s != MPM_OK) return s;
+    const int NC = c->io_chunks;
+    constexpr int M = mpm_ctx::IO_MAX_CHUNKS;
+    constexpr int EV_UP = 0, EV_DOWN = 5 * M, EV_GATHER = 10 * M, EV_START = 10 * M + 1;
     if (!c->io_h2d) {
         CK(cudaStreamCreateWithFlags(&c->io_h2d, cudaStreamNonBlocking));
         CK(cudaStreamCreateWithFlags(&c->io_d2h, cudaStreamNonBlocking));
         for (cudaEvent_t &e : c->io_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
     const size_t N = (size_t)c->num;
-    double *host[5] = {coord, vel, F, stress, vol};
-    const int off[5] = {ST_X, ST_V, ST_F, ST_S, ST_VOL}, width[5] = {3, 3, 9, 6, 1};
+    // fields in copy order, smallest first: vol, coord, vel, stress, F
+    double *host[5] = {vol, coord, vel, stress, F};
+    const int off[5] = {ST_VOL, ST_X, ST_V, ST_S, ST_F}, width[5] = {1, 3, 3, 6, 9};
+    const unsigned bit[5] = {16u, 1u, 2u, 8u, 4u};
     unsigned mask = 0;
     for (int f = 0; f < 5; f++)
-        if (host[f]) mask |= 1u << f;
+        if (host[f]) mask |= bit[f];
     double *st = c->d_stage;
     const int nb = (int)((N + 255) / 256);
+    auto piece = [&](int f, int k, size_t &begin, size_t &count) {
+        const size_t total = (size_t)width[f] * N;
+        const size_t per = (total + NC - 1) / NC;
+        begin = std::min(total, (size_t)k * per);
+        count = std::min(total, begin + per) - begin;
+    };
     // the copy streams start after the work already on the context's stream
-    CK(cudaEventRecord(c->io_ev[11], c->stream));
-    CK(cudaStreamWaitEvent(c->io_h2d, c->io_ev[11], 0));
-    CK(cudaStreamWaitEvent(c->io_d2h, c->io_ev[11], 0));
+    CK(cudaEventRecord(c->io_ev[EV_START], c->stream));
+    CK(cudaStreamWaitEvent(c->io_h2d, c->io_ev[EV_START], 0));
+    CK(cudaStreamWaitEvent(c->io_d2h, c->io_ev[EV_START], 0));
     for (int step = 0; step < nsteps; step++) {
         for (int f = 0; f < 5; f++) {
             if (!host[f]) continue;
-            if (step > 0) CK(cudaStreamWaitEvent(c->io_h2d, c->io_ev[5 + f], 0));
-            CK(cudaMemcpyAsync(st + (size_t)off[f] * N, host[f], sizeof(double) * width[f] * N,
-                               cudaMemcpyHostToDevice, c->io_h2d));
-            CK(cudaEventRecord(c->io_ev[f], c->io_h2d));
-            CK(cudaStreamWaitEvent(c->stream, c->io_ev[f], 0));
+            for (int k = 0; k < NC; k++) {
+                size_t b0, cnt;
+                piece(f, k, b0, cnt);
+                if (cnt == 0) continue;
+                if (step > 0) CK(cudaStreamWaitEvent(c->io_h2d, c->io_ev[EV_DOWN + f * M + k], 0));
+                CK(cudaMemcpyAsync(st + (size_t)off[f] * N + b0, host[f] + b0, sizeof(double) * cnt,
+                                   cudaMemcpyHostToDevice, c->io_h2d));
+                CK(cudaEventRecord(c->io_ev[EV_UP + f * M + k], c->io_h2d));
+                CK(cudaStreamWaitEvent(c->stream, c->io_ev[EV_UP + f * M + k], 0));
+            }
         }
         const int par = (int)(c->step & 1);
         if (c->precision == 64)
@@ -762,13 +782,18 @@ mpm_status mpm_gpu_steps_host(mpm_ctx *c, int nsteps, double facl, double *coord
                                                               c->nreal, st, mask);
         c->launches++;
         if ((s = check_launch(c)) != MPM_OK) return s;
-        CK(cudaEventRecord(c->io_ev[10], c->stream));
-        CK(cudaStreamWaitEvent(c->io_d2h, c->io_ev[10], 0));
+        CK(cudaEventRecord(c->io_ev[EV_GATHER], c->stream));
+        CK(cudaStreamWaitEvent(c->io_d2h, c->io_ev[EV_GATHER], 0));
         for (int f = 0; f < 5; f++) {
             if (!host[f]) continue;
-            CK(cudaMemcpyAsync(host[f], st + (size_t)off[f] * N, sizeof(double) * width[f] * N,
-                               cudaMemcpyDeviceToHost, c->io_d2h));
-            CK(cudaEventRecord(c->io_ev[5 + f], c->io_d2h));
+            for (int k = 0; k < NC; k++) {
+                size_t b0, cnt;
+                piece(f, k, b0, cnt);
+                if (cnt == 0) continue;
+                CK(cudaMemcpyAsync(host[f] + b0, st + (size_t)off[f] * N + b0, sizeof(double) * cnt,
+                                   cudaMemcpyDeviceToHost, c->io_d2h));
+                CK(cudaEventRecord(c->io_ev[EV_DOWN + f * M + k], c->io_d2h));
+            }
         }
     }
     CK(cudaStreamSynchronize(c->io_d2h));

@@ -141,7 +141,10 @@ struct mpm_ctx {
     cudaStream_t stream = nullptr;
     // host I/O pipeline of mpm_gpu_steps_host: copy streams and per-field events
     cudaStream_t io_h2d = nullptr, io_d2h = nullptr;
-    cudaEvent_t io_ev[12] = {};   // [0,5) uploads done, [5,10) downloads done, 10 gather done, 11 start
+    static constexpr int IO_MAX_CHUNKS = 16;
+    int io_chunks = 4;   // pieces per field copy in the host I/O pipeline (env MPM_GB300_IO_CHUNKS)
+    // [0, 5 M) uploads done, [5 M, 10 M) downloads done, then gather done, start (M = IO_MAX_CHUNKS)
+    cudaEvent_t io_ev[10 * IO_MAX_CHUNKS + 2] = {};
     // materials on device
     int *d_iprop = nullptr;
     double *d_matprop = nullptr;

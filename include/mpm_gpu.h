@@ -147,7 +147,9 @@ mpm_status mpm_gpu_upload_particles(mpm_ctx *ctx, const double *coord, const dou
  * arrays before it and downloaded into them after it (the reference's time
  * loop with the particle vectors on the host between steps); any pointer may
  * be NULL (that field stays on the device).  Uploads and downloads run on
- * two internal copy streams, pipelined field by field across steps, so both
+ * two internal copy streams in pieces (four per field by default, environment
+ * MPM_GB300_IO_CHUNKS = 1..16), pipelined across steps: the upload of a piece
+ * waits only for the download of the same piece from the step before, so both
  * directions of the host link are busy at once.  Synchronises before
  * returning.  Explicit contexts only. */
 mpm_status mpm_gpu_steps_host(mpm_ctx *ctx, int nsteps, double facl, double *coord, double *vel, double *F,
