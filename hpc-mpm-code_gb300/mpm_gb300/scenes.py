@@ -20,7 +20,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-PIC, FLIP = 0, 1
+PIC, FLIP, TPIC, APIC = 0, 1, 2, 3   # MapScheme order, module/dataset.h:19
 BC_U, BC_V, BC_W = 0, 1, 2
 
 

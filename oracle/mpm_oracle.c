@@ -40,6 +40,8 @@ struct mo_ctx {
     /* particles (AoS like the reference: coord[3p+i], F[9p+3i+j], stress[6p+k]) */
     int num;
     double *coord, *vel, *accel, *mass, *vol0, *vol, *F, *stress, *jac;
+    /* TPIC: vel_grad; APIC: vel_Bmat and inv_Dmat (module/map_and_interpolate.h:59,105), row major */
+    double *aff, *aff_dinv;
     int *matid;
     /* nodal, component-major: comp c of node n at c*nodec + n */
     double *nmass, *nvof, *nmome, *nforce, *nvel, *naccel, *nvol, *ndispl;
@@ -103,6 +105,7 @@ mo_ctx *mo_create(const int *xyelem, const double *xymin, const double *dxy, con
 static void free_particles(mo_ctx *c) {
     free(c->coord); free(c->vel); free(c->accel); free(c->mass); free(c->vol0); free(c->vol);
     free(c->F); free(c->stress); free(c->jac); free(c->matid); free(c->idp2p);
+    free(c->aff); free(c->aff_dinv);
 }
 
 void mo_destroy(mo_ctx *c) {
@@ -136,6 +139,8 @@ int mo_load(mo_ctx *c, int num, const double *coord, const double *vel, const do
     c->stress = (double *)zalloc(sizeof(double) * 6 * n);
     c->matid = (int *)zalloc(sizeof(int) * n);
     c->idp2p = (int *)zalloc(sizeof(int) * n);
+    c->aff = (double *)zalloc(sizeof(double) * 9 * n);       /* VectorAssign: zero, solid_material_point.cpp:36-42 */
+    c->aff_dinv = (double *)zalloc(sizeof(double) * 9 * n);
     memcpy(c->coord, coord, sizeof(double) * 3 * n);
     if (vel) memcpy(c->vel, vel, sizeof(double) * 3 * n);
     memcpy(c->mass, mass, sizeof(double) * n);
@@ -456,6 +461,52 @@ static void inv3(const double a[3][3], double r[3][3]) {
 }
 
 /* --------------------------------------------------------------- explicit */
+/* Control-point coordinate xyc[nid][dir] (DefineCpPos, module/mesh.h:32-47)
+ * on one rank: xyminw = xymin, xymaxw = xymin + nel dx. */
+static double cp_coord(const mo_ctx *c, int dir, int idx) {
+    if (c->idimc[dir] == 1) return c->xmin[dir] + c->dx[dir] * (double)idx;
+    if (idx == 0) return c->xmin[dir];
+    if (idx == c->nnc[dir] - 1) return c->xmin[dir] + c->dx[dir] * (double)c->nel[dir];
+    return c->xmin[dir] + c->dx[dir] * ((double)idx - 0.5);
+}
+
+/* The particle's affine velocity matrix A of TPIC (vel_grad) or APIC
+ * (vel_Bmat . inv_Dmat, APIC::VarP2G, module/map_and_interpolate.h:108-118). */
+static void affine_matrix(const mo_ctx *c, int p, double A[3][3]) {
+    const double *B = c->aff + 9 * p, *Di = c->aff_dinv + 9 * p;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            if (c->scheme == 2) {
+                A[i][j] = B[3 * i + j];
+            } else {
+                double t = 0.0;
+                for (int k = 0; k < 3; k++) t += B[3 * i + k] * Di[3 * k + j];
+                A[i][j] = t;
+            }
+        }
+}
+
+/* Momentum of one particle at one node: TPIC::VarP2G / APIC::VarP2G
+ * (module/map_and_interpolate.h:62-77,104-130) with the node coordinate read
+ * as xyc[nid][j] (the reference writes xyc[j][nid], past the end of xyc),
+ * StandardVarP2G for PIC / FLIP. */
+static void momentum_terms(const mo_ctx *c, int p, int n, double A[3][3], double out[3]) {
+    const double *v = c->vel + 3 * p;
+    if (c->scheme < 2) {
+        out[0] = v[0]; out[1] = v[1]; out[2] = v[2];
+        return;
+    }
+    int nx = c->nnc[0], ny = c->nnc[1];
+    int idx[3] = {n % nx, (n / nx) % ny, n / (nx * ny)};
+    double d[3];
+    for (int j = 0; j < 3; j++) d[j] = cp_coord(c, j, idx[j]) - c->coord[3 * p + j];
+    for (int i = 0; i < 3; i++) {
+        double t = 0.0;
+        for (int j = 0; j < 3; j++) t += A[i][j] * d[j];
+        out[i] = v[i] + t;
+    }
+}
+
 static void p2g(mo_ctx *c) {
     size_t N = (size_t)c->nodec;
     int nc[MAXN];
@@ -469,14 +520,18 @@ static void p2g(mo_ctx *c) {
         const double *s = c->stress + 6 * p;
         int ne = maksf(c, m, c->coord + 3 * p, nc, sf, dsf);
         double mp = c->mass[p], vp = c->vol[p];
+        double A[3][3];
+        if (c->scheme >= 2) affine_matrix(c, p, A);
         for (int i = 0; i < ne; i++) {
             int n = nc[i];
             double N_ = sf[i], d1 = dsf[3 * i], d2 = dsf[3 * i + 1], d3 = dsf[3 * i + 2];
+            double vm[3];
+            momentum_terms(c, p, n, A, vm);
             c->nmass[n] += N_ * mp;
             c->nvof[n] += N_ * vp;
-            c->nmome[n] += N_ * mp * c->vel[3 * p + 0];
-            c->nmome[N + n] += N_ * mp * c->vel[3 * p + 1];
-            c->nmome[2 * N + n] += N_ * mp * c->vel[3 * p + 2];
+            c->nmome[n] += N_ * mp * vm[0];
+            c->nmome[N + n] += N_ * mp * vm[1];
+            c->nmome[2 * N + n] += N_ * mp * vm[2];
             /* ComputeInternalForce / ComputeExternalForce, solid_material_point.h:48-73 */
             double fi0 = -vp * (s[0] * d1 + s[5] * d2 + s[4] * d3);
             double fi1 = -vp * (s[5] * d1 + s[1] * d2 + s[3] * d3);
@@ -547,20 +602,55 @@ static void g2p_explicit(mo_ctx *c) {
         for (size_t i = 0; i < 3 * N; i++) c->nvel[i] += c->dt * c->naccel[i];
         memset(c->vel, 0, sizeof(double) * 3 * c->num);
     }
+    if (c->scheme >= 2) {
+        memset(c->aff, 0, sizeof(double) * 9 * (size_t)c->num);
+        memset(c->aff_dinv, 0, sizeof(double) * 9 * (size_t)c->num);
+    }
     FOR_PARTICLES(c, m, p) {
         int ne = maksf(c, m, c->coord + 3 * p, nc, sf, dsf);
-        for (int i = 0; i < ne; i++)
+        double D[3][3] = {{0}};
+        double *B = c->aff + 9 * p;
+        for (int i = 0; i < ne; i++) {
             for (int k = 0; k < 3; k++) {
                 if (!flip) c->vel[3 * p + k] += sf[i] * c->nvel[k * N + nc[i]];           /* PIC::VarG2P */
                 else c->vel[3 * p + k] += sf[i] * c->dt * c->naccel[k * N + nc[i]];       /* FLIP::VarG2P */
             }
+            if (c->scheme == 2) {
+                /* TPIC::VarGradG2P (map_and_interpolate.h:79-98): vel_grad[a][j] += dsf_j nvel_a */
+                for (int a = 0; a < 3; a++)
+                    for (int j = 0; j < 3; j++) B[3 * a + j] += dsf[3 * i + j] * c->nvel[a * N + nc[i]];
+            } else if (c->scheme == 3) {
+                /* APIC::VarBmatG2P and DmatG2P (map_and_interpolate.h:132-162) */
+                int n = nc[i], nx = c->nnc[0], ny = c->nnc[1];
+                int idx[3] = {n % nx, (n / nx) % ny, n / (nx * ny)};
+                double d[3];
+                for (int j = 0; j < 3; j++) d[j] = cp_coord(c, j, idx[j]) - c->coord[3 * p + j];
+                for (int a = 0; a < 3; a++)
+                    for (int j = 0; j < 3; j++) {
+                        B[3 * a + j] += sf[i] * c->nvel[a * N + n] * d[j];
+                        D[a][j] += sf[i] * d[a] * d[j];
+                    }
+            }
+        }
+        if (c->scheme == 3) {
+            /* APIC::InvDmatG2P (map_and_interpolate.h:164-172) */
+            double Di[3][3];
+            inv3(D, Di);
+            for (int a = 0; a < 3; a++)
+                for (int j = 0; j < 3; j++) c->aff_dinv[9 * p + 3 * a + j] = Di[a][j];
+        }
     }
     /* MUSL, var_trans_solid_explicit.cpp:101-148 */
     memset(c->nmome, 0, sizeof(double) * 3 * N);
     FOR_PARTICLES(c, m, p) {
         int ne = maksf(c, m, c->coord + 3 * p, nc, sf, dsf);
-        for (int i = 0; i < ne; i++)
-            for (int k = 0; k < 3; k++) c->nmome[k * N + nc[i]] += sf[i] * c->mass[p] * c->vel[3 * p + k];
+        double A[3][3];
+        if (c->scheme >= 2) affine_matrix(c, p, A);
+        for (int i = 0; i < ne; i++) {
+            double vm[3];
+            momentum_terms(c, p, nc[i], A, vm);
+            for (int k = 0; k < 3; k++) c->nmome[k * N + nc[i]] += sf[i] * c->mass[p] * vm[k];
+        }
     }
     for (size_t n = 0; n < N; n++)
         for (int k = 0; k < 3; k++)
@@ -640,6 +730,20 @@ int mo_get_nodal(const mo_ctx *c, int field, double *out) {
     }
     memcpy(out, src, sizeof(double) * n);
     return (int)n;
+}
+
+int mo_get_affine(const mo_ctx *c, double *out) {
+    if (c->scheme < 2) {
+        memset(out, 0, sizeof(double) * 9 * (size_t)c->num);
+        return c->num;
+    }
+    for (int p = 0; p < c->num; p++) {
+        double A[3][3];
+        affine_matrix(c, p, A);
+        for (int a = 0; a < 3; a++)
+            for (int j = 0; j < 3; j++) out[9 * p + 3 * a + j] = A[a][j];
+    }
+    return c->num;
 }
 
 int mo_get_particles(const mo_ctx *c, double *coord, double *vel, double *F, double *stress, double *vol) {

@@ -31,6 +31,9 @@ int mo_explicit_steps(mo_ctx *c, int nsteps, double facl);
 /* field: 0 nmass, 1 nvof, 2 nmome, 3 nforce, 4 nvel, 5 naccel, 6 nvol, 7 ndispl */
 int mo_get_nodal(const mo_ctx *c, int field, double *out);
 int mo_get_particles(const mo_ctx *c, double *coord, double *vel, double *F, double *stress, double *vol);
+/* scheme 2 (TPIC) / 3 (APIC): the affine velocity matrix per particle, 9
+ * row-major values (TPIC vel_grad; APIC vel_Bmat . inv_Dmat); zeros otherwise */
+int mo_get_affine(const mo_ctx *c, double *out);
 /* shape functions at one point in element m: returns nenode */
 int mo_shape(const mo_ctx *c, int m, const double *x, int *nc, double *sf, double *dsf);
 

@@ -41,6 +41,7 @@ def _lib():
     lib.mo_explicit_steps.argtypes = [C.c_void_p, C.c_int, C.c_double]
     lib.mo_get_nodal.argtypes = [C.c_void_p, C.c_int, _dp]
     lib.mo_get_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
+    lib.mo_get_affine.argtypes = [C.c_void_p, _dp]
     lib.mo_shape.argtypes = [C.c_void_p, C.c_int, _dp, _ip, _dp, _dp]
     lib.mo_implicit_setup.argtypes = [C.c_void_p, C.c_int, C.c_double]
     lib.mo_implicit_nnzb.argtypes = [C.c_void_p]
@@ -104,6 +105,13 @@ class PortSolid:
         self.lib.mo_get_particles(self.ctx, x, v, F, sig, vol)
         return {"x": x.reshape(n, 3), "v": v.reshape(n, 3), "F": F.reshape(n, 3, 3), "sigma": sig.reshape(n, 6),
                 "vol": vol}
+
+    def affine(self):
+        """TPIC / APIC: the affine velocity matrix per particle (n, 3, 3)."""
+        n = self.scene.num
+        out = np.zeros(n * 9)
+        self.lib.mo_get_affine(self.ctx, out)
+        return out.reshape(n, 3, 3)
 
     def shape(self, m, x):
         nc = np.zeros(27, dtype=np.int32)

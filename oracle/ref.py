@@ -33,6 +33,7 @@ def _lib():
     lib.ref_explicit_p2g.argtypes = [C.c_double]
     lib.ref_get_nodal.argtypes = [C.c_int, _dp]
     lib.ref_get_particles.argtypes = [_dp, _dp, _dp, _dp, _dp]
+    lib.ref_get_affine.argtypes = [_dp]
     lib.ref_implicit_init.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _ip, C.c_int, C.c_int, C.c_double]
     lib.ref_implicit_steps.argtypes = [C.c_int, C.c_double]
     lib.ref_implicit_assemble.argtypes = [C.c_double]
@@ -86,6 +87,13 @@ class RefSolid:
         self.lib.ref_get_particles(x, v, F, sig, vol)
         return {"x": x.reshape(n, 3), "v": v.reshape(n, 3), "F": F.reshape(n, 3, 3), "sigma": sig.reshape(n, 6),
                 "vol": vol}
+
+    def affine(self):
+        """TPIC / APIC: the affine velocity matrix per particle (n, 3, 3)."""
+        n = self.scene.num
+        out = np.zeros(n * 9)
+        assert self.lib.ref_get_affine(out) == n
+        return out.reshape(n, 3, 3)
 
     # --- implicit solid hooks -------------------------------------------------
     def assemble(self, facl=1.0):

@@ -71,7 +71,7 @@ class ExplicitSolid : public SolidMaterialPointBase {
                     double sfi = sf[ni];
                     this->StandardVarP2G(pid, nid, sfi, this->mass, this->nmass);
                     this->StandardVarP2G(pid, nid, sfi, this->vol, this->nvof);
-                    this->VelP2G(pid, nid, sfi);
+                    MomentumP2G(pid, nid, sfi);
                     std::array<double, 3> fi = this->ComputeInternalForce(ni, pid, dsf, sts);
                     std::array<double, 3> fe = this->ComputeExternalForce(pid, sfi);
                     this->nforce[nid + nuc] += fi[0] + fe[0];
@@ -115,7 +115,33 @@ class ExplicitSolid : public SolidMaterialPointBase {
         this->rigid_bc.BCSetZero(nwc, this->naccel);
     }
 
-    // Node2ParticleS, var_trans_solid_explicit.cpp:187-311 (PIC / FLIP, no F-bar)
+    // MaterialPoint::VelP2G (module/map_and_interpolate.cpp:12-23).  For TPIC
+    // and APIC it is restated here: TPIC::VarP2G / APIC::VarP2G
+    // (module/map_and_interpolate.h:62-77,104-130) read the node coordinate
+    // as xyc[j][nid], past the end of xyc (a vector of nodec 3-arrays); the
+    // restatement reads xyc[nid][j] and is otherwise the same arithmetic.
+    void MomentumP2G(int pid, int nid, double sfi) {
+        if (this->solswitch == MapScheme::PIC || this->solswitch == MapScheme::FLIP) {
+            this->VelP2G(pid, nid, sfi);
+            return;
+        }
+        std::array<std::array<double, 3>, 3> A{};
+        if (this->solswitch == MapScheme::TPIC) {
+            A = this->tpic.vel_grad[pid];
+        } else {
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++)
+                    for (int k = 0; k < 3; k++) A[i][j] += this->apic.vel_Bmat[pid][i][k] * this->apic.inv_Dmat[pid][k][j];
+        }
+        std::array<double, 3> t{};
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) t[i] += A[i][j] * (xyc[nid][j] - this->coord[pid][j]);
+        this->nmome[nid + nuc] += sfi * this->mass[pid] * (this->vel[pid][0] + t[0]);
+        this->nmome[nid + nvc] += sfi * this->mass[pid] * (this->vel[pid][1] + t[1]);
+        this->nmome[nid + nwc] += sfi * this->mass[pid] * (this->vel[pid][2] + t[2]);
+    }
+
+    // Node2ParticleS, var_trans_solid_explicit.cpp:187-311 (PIC / FLIP / TPIC / APIC, no F-bar)
     void Node2Particle() override {
         int nenode;
         std::vector<int> ncm;
@@ -130,17 +156,30 @@ class ExplicitSolid : public SolidMaterialPointBase {
             }
             VectorAssign(this->num, this->vel);
         }
+        const bool tpic = (this->solswitch == MapScheme::TPIC), apic = (this->solswitch == MapScheme::APIC);
+        if (tpic) VectorAssign(this->num, this->tpic.vel_grad);
+        if (apic) {
+            VectorAssign(this->num, this->apic.vel_Bmat);
+            VectorAssign(this->num, this->apic.inv_Dmat);
+        }
         for (int m = 0; m < nelem; m++) {
             int pid = this->idepf[m];
             while (pid != -1) {
                 std::array<double, 3> xyp = this->coord[pid];
                 MakSf(m, xyp, idimc, xynodec, ncm, nenode, sf, dsf);
+                std::array<std::array<double, 3>, 3> ADp{};
                 for (int ni = 0; ni < nenode; ni++) {
                     if (!flip)
                         this->pic.VarG2P(pid, ncm[ni], sf[ni], this->vel, this->nvel);
                     else
                         this->flip.VarG2P(pid, ncm[ni], sf[ni], this->vel, this->naccel);
+                    if (tpic) this->tpic.VarGradG2P(pid, ncm[ni], ni, dsf, this->tpic.vel_grad, this->nvel);
+                    if (apic) {
+                        this->apic.VarBmatG2P(pid, ncm[ni], sf[ni], this->apic.vel_Bmat, this->nvel, this->coord);
+                        this->apic.DmatG2P(pid, ncm[ni], sf[ni], this->coord, ADp);
+                    }
                 }
+                if (apic) this->apic.InvDmatG2P(pid, ADp);
                 pid = this->idp2p[pid];
             }
         }
@@ -203,7 +242,7 @@ class ExplicitSolid : public SolidMaterialPointBase {
             while (pid != -1) {
                 std::array<double, 3> xyp = this->coord[pid];
                 MakSf(m, xyp, idimc, xynodec, ncm, nenode, sf, dsf);
-                for (int ni = 0; ni < nenode; ni++) this->VelP2G(pid, ncm[ni], sf[ni]);
+                for (int ni = 0; ni < nenode; ni++) MomentumP2G(pid, ncm[ni], sf[ni]);
                 pid = this->idp2p[pid];
             }
         }
@@ -244,7 +283,8 @@ MaterialPoint *active() {
 void load_particles(SolidMaterialPointBase &sp, int num, const double *coord, const double *vel, const double *mass,
                     const double *vol0, const int *matid, int scheme) {
     sp.num = num;
-    sp.solswitch = (scheme == 1) ? MapScheme::FLIP : MapScheme::PIC;
+    const MapScheme schemes[4] = {MapScheme::PIC, MapScheme::FLIP, MapScheme::TPIC, MapScheme::APIC};
+    sp.solswitch = schemes[(scheme >= 0 && scheme < 4) ? scheme : 0];
     sp.InitializePointData();
     for (int p = 0; p < num; p++) {
         sp.id[p] = p;
@@ -384,6 +424,24 @@ int ref_get_nodal(int field, double *out) {
     }
     std::memcpy(out, v->data(), v->size() * sizeof(double));
     return (int)v->size();
+}
+
+// TPIC: vel_grad; APIC: vel_Bmat . inv_Dmat; 9 row-major values per particle
+int ref_get_affine(double *out) {
+    if (!g_exp) return -1;
+    ExplicitSolid &sp = *g_exp;
+    for (int p = 0; p < sp.num; p++)
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double a = 0.0;
+                if (sp.solswitch == MapScheme::TPIC) {
+                    a = sp.tpic.vel_grad[p][i][j];
+                } else if (sp.solswitch == MapScheme::APIC) {
+                    for (int k = 0; k < 3; k++) a += sp.apic.vel_Bmat[p][i][k] * sp.apic.inv_Dmat[p][k][j];
+                }
+                out[9 * p + 3 * i + j] = a;
+            }
+    return sp.num;
 }
 
 int ref_get_particles(double *coord, double *vel, double *F, double *stress, double *vol) {

@@ -8,6 +8,7 @@ committed and this script is re-run only when a case is added:
 
     oracle/build_ref.sh && python tests/golden/make_golden.py
     python tests/golden/make_golden.py --hyperelastic     # only models 2 and 3
+    python tests/golden/make_golden.py --affine           # only the TPIC / APIC cases
 """
 from __future__ import annotations
 
@@ -46,8 +47,12 @@ def explicit_case(name, scene, nsteps, facl=1.0):
     r = ref.RefSolid(scene)
     r.steps(1, facl)
     out.update({f"step1_{k}": v for k, v in r.particles().items()})
+    if scene.scheme >= scenes.TPIC:
+        out["step1_affine"] = r.affine()
     r.steps(nsteps - 1, facl)
     out.update({f"stepN_{k}": v for k, v in r.particles().items()})
+    if scene.scheme >= scenes.TPIC:
+        out["stepN_affine"] = r.affine()
     out["nsteps"] = np.array(nsteps)
     out["facl"] = np.array(facl)
     np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **scene_arrays(scene), **out)
@@ -89,11 +94,32 @@ def hyperelastic_cases():
     explicit_case("explicit_mooney_rivlin", s, nsteps=10)
 
 
+def affine_cases():
+    """TPIC and APIC (MapScheme 2 and 3) with linear and with quadratic
+    B-spline shape functions: a block with a random and a rotating velocity
+    field, so that the affine matrices are far from zero."""
+    rng = np.random.default_rng(20261205)
+    for scheme, nm in ((scenes.TPIC, "tpic"), (scenes.APIC, "apic")):
+        s = scenes.elastic_block(grid=(10, 10, 8), cell_lo=(2, 2, 0), cell_hi=(7, 7, 5), scheme=scheme,
+                                 dt=1.0e-5, seed=107 + scheme)
+        c = s.coord.mean(axis=0)
+        s.vel[:] = rng.normal(0.0, 0.2, size=s.vel.shape) + 20.0 * np.cross([0.0, 0.0, 1.0], s.coord - c)
+        explicit_case(f"explicit_{nm}", s, nsteps=25)
+        s = scenes.elastic_block(grid=(10, 6, 10), cell_lo=(2, 1, 0), cell_hi=(8, 5, 5), idimc=(2, 1, 2),
+                                 seed=109 + scheme, scheme=scheme)
+        c = s.coord.mean(axis=0)
+        s.vel[:] = rng.normal(0.0, 0.2, size=s.vel.shape) + 20.0 * np.cross([0.0, 1.0, 0.0], s.coord - c)
+        explicit_case(f"explicit_{nm}_quadratic", s, nsteps=10)
+
+
 def main():
     if not ref.available():
         raise SystemExit("oracle/_ref/libmpmref.so missing: run oracle/build_ref.sh first")
     if "--hyperelastic" in sys.argv[1:]:
         hyperelastic_cases()
+        return
+    if "--affine" in sys.argv[1:]:
+        affine_cases()
         return
     rng = np.random.default_rng(20261203)
     # small elastic block, fixed bottom, PIC and FLIP, random initial velocity
@@ -118,6 +144,7 @@ def main():
     s = scenes.cantilever(grid=(10, 8, 8), cells=(6, 4, 4), cell_lo=(0, 2, 2), iprop=1)
     implicit_case("implicit_neohookean", s, nr_flag=True, nsteps=3)
     hyperelastic_cases()
+    affine_cases()
 
 
 if __name__ == "__main__":

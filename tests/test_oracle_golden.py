@@ -13,7 +13,8 @@ from oracle import port
 
 TOL = 1.0e-12
 EXPLICIT = ["explicit_pic", "explicit_flip", "explicit_quadratic", "explicit_neohookean", "explicit_stvk",
-            "explicit_mooney_rivlin"]
+            "explicit_mooney_rivlin", "explicit_tpic", "explicit_apic", "explicit_tpic_quadratic",
+            "explicit_apic_quadratic"]
 IMPLICIT = ["implicit_linear", "implicit_neohookean"]
 
 
@@ -36,10 +37,14 @@ def test_explicit_steps_match_reference(name):
     p = o.particles()
     for k in ("x", "v", "F", "sigma", "vol"):
         assert rel_l2(p[k], g[f"step1_{k}"]) <= TOL, k
+    if "step1_affine" in g:   # TPIC vel_grad / APIC vel_Bmat . inv_Dmat
+        assert rel_l2(o.affine(), g["step1_affine"]) <= TOL
     o.steps(int(g["nsteps"]) - 1, float(g["facl"]))
     p = o.particles()
     for k in ("x", "v", "F", "sigma", "vol"):
         assert rel_l2(p[k], g[f"stepN_{k}"]) <= 1.0e-10, k
+    if "stepN_affine" in g:
+        assert rel_l2(o.affine(), g["stepN_affine"]) <= 1.0e-10
 
 
 @pytest.mark.parametrize("name", IMPLICIT)
