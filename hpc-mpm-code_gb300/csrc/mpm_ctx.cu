@@ -101,7 +101,8 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     if (!grid || !mat || !cfg || !out) return MPM_ERR_BAD_ARG;
     *out = nullptr;
     if (cfg->precision != 32 && cfg->precision != 64) return MPM_ERR_BAD_ARG;
-    if (cfg->scheme != MPM_PIC && cfg->scheme != MPM_FLIP) return MPM_ERR_UNSUPPORTED;
+    if (cfg->scheme < MPM_PIC || cfg->scheme > MPM_APIC) return MPM_ERR_UNSUPPORTED;
+    if (cfg->implicit && cfg->scheme > MPM_FLIP) return MPM_ERR_UNSUPPORTED;
     if (!(cfg->dt > 0.0) || mat->nmat <= 0 || !mat->iprop || !mat->mat_prop) return MPM_ERR_BAD_ARG;
     for (int d = 0; d < 3; d++) {
         if (grid->xyelem[d] <= 0 || !(grid->dxy[d] > 0.0)) return MPM_ERR_BAD_ARG;
@@ -151,7 +152,8 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     c->shifting = cfg->shifting ? 1 : 0;
     c->resort_period = cfg->resort_period > 0 ? cfg->resort_period : 8;
     c->cell_scatter = cfg->scatter == 1 ? 0 : 1;
-    c->nreal = cfg->implicit ? 27 : 24;
+    c->affine = cfg->scheme == MPM_TPIC || cfg->scheme == MPM_APIC;
+    c->nreal = cfg->implicit ? 27 : (c->affine ? 33 : 24);
     c->dt = cfg->dt;
     c->mtol = cfg->mtol;
     c->nmat = mat->nmat;
@@ -655,6 +657,14 @@ __global__ void k_state_scatter(R *f, size_t N, size_t S, int nreal, const doubl
         for (int k = 0; k < 6; k++) f[(15 + k) * S + j] = (R)st[ST_S * N + 6 * p + k];
     if (mask & 16) f[23 * S + j] = (R)st[ST_VOL * N + p];
 }
+// The affine matrices (fields 24..32) into the staging buffer in load order.
+template <typename R>
+__global__ void k_affine_gather_state(const R *f, size_t N, size_t S, int nreal, double *st) {
+    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N) return;
+    const size_t p = (size_t)((const int *)(f + nreal * S) + S)[j];
+    for (int k = 0; k < 9; k++) st[9 * p + k] = (double)f[(24 + k) * S + j];
+}
 }  // namespace mpm
 
 static mpm_status ensure_staging(mpm_ctx *c) {
@@ -681,6 +691,30 @@ mpm_status mpm_gpu_download_particles(mpm_ctx *c, double *coord, double *vel, do
     if (F) CK(cudaMemcpyAsync(F, st + ST_F * N, sizeof(double) * 9 * N, cudaMemcpyDeviceToHost, c->stream));
     if (stress) CK(cudaMemcpyAsync(stress, st + ST_S * N, sizeof(double) * 6 * N, cudaMemcpyDeviceToHost, c->stream));
     if (vol) CK(cudaMemcpyAsync(vol, st + ST_VOL * N, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_download_affine(mpm_ctx *c, double *affine) {
+    if (!c || (!affine && c->num > 0)) return MPM_ERR_BAD_ARG;
+    if (c->num == 0) return MPM_OK;
+    const size_t N = (size_t)c->num;
+    if (!c->affine) {
+        memset(affine, 0, sizeof(double) * 9 * N);
+        return MPM_OK;
+    }
+    mpm_status s = ensure_staging(c);
+    if (s != MPM_OK) return s;
+    const int nb = (int)((N + 255) / 256);
+    if (c->precision == 64)
+        k_affine_gather_state<double><<<nb, 256, 0, c->stream>>>((const double *)c->pbuf[c->cur], N, c->pstride,
+                                                                  c->nreal, c->d_stage);
+    else
+        k_affine_gather_state<float><<<nb, 256, 0, c->stream>>>((const float *)c->pbuf[c->cur], N, c->pstride,
+                                                                 c->nreal, c->d_stage);
+    c->launches++;
+    if (check_launch(c) != MPM_OK) return MPM_ERR_CUDA;
+    CK(cudaMemcpyAsync(affine, c->d_stage, sizeof(double) * 9 * N, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return MPM_OK;
 }

@@ -35,7 +35,12 @@ __device__ __forceinline__ void axis_linear(R x, R xmin, R dx, R inv_dx, int ie,
         R xy = xmin + dx * (R)(ie + k);
         R r = x - xy;
         a.w[k] = (R)1 - rdiv(fabs(r), dx, inv_dx);
-        a.dw[k] = (r < (R)0) ? inv_dx : -inv_dx;
+        // dN/dx by node: -1/dx for the lower node, +1/dx for the upper one.
+        // MakSf (module/shape_function.cpp:39-50) takes the sign of r, which is
+        // the same for a point inside the element; where rounding puts x on a
+        // node plane beyond the element's end (common in FP32) the sign test
+        // would give both nodes -1/dx.
+        a.dw[k] = k == 0 ? -inv_dx : inv_dx;
     }
 }
 

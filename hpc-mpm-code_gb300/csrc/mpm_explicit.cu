@@ -1288,7 +1288,27 @@ __global__ void k_step_reset(StepArgs<R> a) {
 // One CTA per work item (a chunk of one brick's particles); every
 // contribution is converted to int64 and added into a shared box of the
 // brick's nodes (exact, order independent).
-template <typename R, int OX, int OY, int OZ>
+// Control-point coordinate xyc[idx][d] along one axis (DefineCpPos,
+// module/mesh.h:32-47, on one rank: the open-knot end points of a quadratic
+// axis sit on the walls).
+template <typename R, int O>
+__device__ __forceinline__ R cp_coord(const KGeom<R> &g, int d, int idx) {
+    if (O == 1) return g.xmin[d] + g.dx[d] * (R)idx;
+    if (idx == 0) return g.xmin[d];
+    if (idx == g.nnc[d] - 1) return g.xmin[d] + g.dx[d] * (R)g.nel[d];
+    return g.xmin[d] + g.dx[d] * ((R)idx - (R)0.5);
+}
+
+// v + A (x_i - x_p): the velocity a TPIC / APIC particle carries to node i
+// (TPIC::VarP2G / APIC::VarP2G, module/map_and_interpolate.h:62-77,104-130,
+// with the coordinate read as xyc[nid][j]).
+template <typename R>
+__device__ __forceinline__ void affine_velocity(const R *v, const R *A, R d0, R d1, R d2, R *out) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) out[c] = v[c] + (A[3 * c] * d0 + A[3 * c + 1] * d1 + A[3 * c + 2] * d2);
+}
+
+template <typename R, int OX, int OY, int OZ, bool AFF = false>
 __global__ void __launch_bounds__(256) k_p2g_box(StepArgs<R> a) {
     constexpr int BX = BRX + OX, BY = BRY + OY, BZ = BRZ + OZ, BOX = BX * BY * BZ;
     extern __shared__ unsigned long long sacc[];   // NACC * BOX
@@ -1326,6 +1346,11 @@ __global__ void __launch_bounds__(256) k_p2g_box(StepArgs<R> a) {
         if (a.implicit) {
             pa[0] = ld(P.a[0] + p); pa[1] = ld(P.a[1] + p); pa[2] = ld(P.a[2] + p);
         }
+        R A[AFF ? 9 : 1];
+        if constexpr (AFF) {
+#pragma unroll
+            for (int e = 0; e < 9; e++) A[e] = ld(P.C[e] + p);
+        }
 #pragma unroll
         for (int k = 0; k <= OZ; k++)
 #pragma unroll
@@ -1334,8 +1359,12 @@ __global__ void __launch_bounds__(256) k_p2g_box(StepArgs<R> a) {
                 for (int i = 0; i <= OX; i++) {
                     const R wxy = ax.w[i] * ay.w[j];
                     R q[NACC];
+                    R vn[3] = {v[0], v[1], v[2]};
+                    if constexpr (AFF)
+                        affine_velocity(v, A, cp_coord<R, OX>(a.g, 0, cx + i) - x0, cp_coord<R, OY>(a.g, 1, cy + j) - x1,
+                                        cp_coord<R, OZ>(a.g, 2, cz + k) - x2, vn);
                     p2g_terms(wxy * az.w[k], ax.dw[i] * ay.w[j] * az.w[k], ax.w[i] * ay.dw[j] * az.w[k],
-                              wxy * az.dw[k], m, vol, v, s, mfx, mfy, mfz, q);
+                              wxy * az.dw[k], m, vol, vn, s, mfx, mfy, mfz, q);
                     if (a.implicit) {
                         // AccelP2G (map_and_interpolate.cpp:42-53): nforce += N m a
                         const R Nm = wxy * az.w[k] * m;
@@ -1470,6 +1499,238 @@ __global__ void __launch_bounds__(256) k_g2p_musl_box(StepArgs<R> a) {
     if (threadIdx.x == 0) {
         if (gsum) atomicAdd(&a.ctl->geup_acc, (unsigned long long)gsum);
         if (vm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VMAX], vm * 1.000001f);
+    }
+    __syncthreads();
+    for (int li = threadIdx.x; li < BOX; li += blockDim.x) {
+        const int lx = li % BX, ly = (li / BX) % BY, lz = li / (BX * BY);
+        const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
+        if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
+        const size_t gn = node_id(a.g, gx, gy, gz);
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            unsigned long long v = sacc[d * BOX + li];
+            if (v) atomicAdd(&a.acc2[d * N + gn], v);
+        }
+    }
+}
+
+// ================================================= TPIC / APIC gather + MUSL
+// Three launches replace the gather + MUSL kernel for the affine schemes:
+// the gather of the velocity (PIC) and of the affine matrix, one thread per
+// particle; a one-thread kernel that sets the MUSL fixed-point scale from the
+// bound the gather recorded (APIC's D^-1 has no a-priori bound); the MUSL
+// scatter of m (v + A (x_i - x_p)) through the brick staging box.
+//   TPIC (TPIC::VarGradG2P, map_and_interpolate.h:79-98): A[c][j] = sum_i dN_i/dx_j G_i,c
+//   APIC (APIC::VarBmatG2P / DmatG2P / InvDmatG2P, map_and_interpolate.h:132-172):
+//     B[c][j] = sum_i N_i G_i,c d_i,j, D[a][b] = sum_i N_i d_i,a d_i,b, A = B D^-1
+// with G the PIC gather field (nvel + dt naccel) and d_i = xyc_i - x_p.  The
+// recorded bound max_p,c (|v_c| + sum_j |A_cj| dmax_j), dmax_j the largest
+// node-particle distance along axis j (dx linear, 1.5 dx quadratic), covers
+// every momentum contribution of this MUSL and of the next step's P2G.
+// APIC weights and node offsets along one axis.  Linear axes take each
+// weight from its own node distance (w_i = r_{i+1} / dx, w_{i+1} = r_i / dx
+// with r_i = x - x_i, r_{i+1} = x_{i+1} - x): equal to 1 - |x - x_node| / dx
+// in exact arithmetic, but a particle close to a grid plane keeps its small
+// weight to full relative precision, so B and D (whose terms cancel to
+// O(r dx) there) stay accurate; quadratic axes, whose D is well conditioned,
+// use the B-spline weights.  On a linear axis both distances are kept at
+// least 1e-7 dx (FP32) / 1e-12 dx (FP64): a particle exactly on a grid plane
+// (common in FP32) would make D singular, and there B D^-1 has a finite
+// limit (for multilinear shape functions it equals the velocity gradient at
+// any position inside the cell), which the floored distances give.
+template <typename R, int O>
+__device__ __forceinline__ void apic_axis(const KGeom<R> &g, int d, int c, R x, const Axis<R, O> &ax, R *w, R *dd) {
+    if (O == 1) {
+        const R tiny = (sizeof(R) == 4 ? (R)1e-7 : (R)1e-12) * g.dx[d];
+        const R r0 = fmax(x - cp_coord<R, 1>(g, d, c), tiny), r1 = fmax(cp_coord<R, 1>(g, d, c + 1) - x, tiny);
+        w[0] = r1 * g.inv_dx[d];
+        w[1] = r0 * g.inv_dx[d];
+        dd[0] = -r0;
+        dd[1] = r1;
+    } else {
+#pragma unroll
+        for (int i = 0; i <= O; i++) {
+            w[i] = ax.w[i];
+            dd[i] = cp_coord<R, O>(g, d, c + i) - x;
+        }
+    }
+}
+
+template <typename R, int OX, int OY, int OZ>
+__global__ void __launch_bounds__(256) k_affine_gather(StepArgs<R> a) {
+    __shared__ Scales S;
+    __shared__ long long sh_l[32];
+    __shared__ float sh_f[32];
+    load_scales_musl(a, S);
+    const size_t N = (size_t)a.g.nodec;
+    const Particles<R> &P = a.P;
+    const bool apic = (a.scheme == MPM_APIC);
+    const R dmax[3] = {(OX == 2 ? (R)1.5 : (R)1) * a.g.dx[0], (OY == 2 ? (R)1.5 : (R)1) * a.g.dx[1],
+                       (OZ == 2 ? (R)1.5 : (R)1) * a.g.dx[2]};
+    long long gacc = 0;
+    float bmax = 0.0f;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.num; p += (int64_t)gridDim.x * blockDim.x) {
+        const R x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+        bool oob = false;
+        const int cx = cell_of(x0, a.g, 0, oob), cy = cell_of(x1, a.g, 1, oob), cz = cell_of(x2, a.g, 2, oob);
+        Axis<R, OX> ax;
+        Axis<R, OY> ay;
+        Axis<R, OZ> az;
+        axis_eval<R, OX>(x0, a.g, 0, cx, ax);
+        axis_eval<R, OY>(x1, a.g, 1, cy, ay);
+        axis_eval<R, OZ>(x2, a.g, 2, cz, az);
+        R v[3] = {(R)0, (R)0, (R)0}, gu[3] = {(R)0, (R)0, (R)0};
+        R B[9], D[6];   // D: xx yy zz xy xz yz
+        R wx[OX + 1], wy[OY + 1], wz[OZ + 1], ex[OX + 1], ey[OY + 1], ez[OZ + 1];
+        if (apic) {
+            apic_axis<R, OX>(a.g, 0, cx, x0, ax, wx, ex);
+            apic_axis<R, OY>(a.g, 1, cy, x1, ay, wy, ey);
+            apic_axis<R, OZ>(a.g, 2, cz, x2, az, wz, ez);
+        }
+#pragma unroll
+        for (int e = 0; e < 9; e++) B[e] = (R)0;
+#pragma unroll
+        for (int e = 0; e < 6; e++) D[e] = (R)0;
+#pragma unroll
+        for (int k = 0; k <= OZ; k++)
+#pragma unroll
+            for (int j = 0; j <= OY; j++)
+#pragma unroll
+                for (int i = 0; i <= OX; i++) {
+                    const R wxy = ax.w[i] * ay.w[j];
+                    const R N_ = wxy * az.w[k];
+                    const R g0 = ax.dw[i] * ay.w[j] * az.w[k], g1 = ax.w[i] * ay.dw[j] * az.w[k], g2 = wxy * az.dw[k];
+                    const size_t gn = node_id(a.g, cx + i, cy + j, cz + k);
+                    R G[3];
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        G[c] = ld(a.G + c * N + gn);
+                        v[c] += N_ * G[c];
+                    }
+                    const R e = ld(a.nei + gn);
+                    gu[0] += g0 * e;
+                    gu[1] += g1 * e;
+                    gu[2] += g2 * e;
+                    if (apic) {
+                        const R d0 = ex[i], d1 = ey[j], d2 = ez[k], Na = wx[i] * wy[j] * wz[k];
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            const R NG = Na * G[c];
+                            B[3 * c] += NG * d0;
+                            B[3 * c + 1] += NG * d1;
+                            B[3 * c + 2] += NG * d2;
+                        }
+                        D[0] += Na * d0 * d0;
+                        D[1] += Na * d1 * d1;
+                        D[2] += Na * d2 * d2;
+                        D[3] += Na * d0 * d1;
+                        D[4] += Na * d0 * d2;
+                        D[5] += Na * d1 * d2;
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            B[3 * c] += g0 * G[c];
+                            B[3 * c + 1] += g1 * G[c];
+                            B[3 * c + 2] += g2 * G[c];
+                        }
+                    }
+                }
+        if (apic) {
+            // A = B D^-1 with D^-1 = adj(D) / det(D) (D symmetric)
+            const R c00 = D[1] * D[2] - D[5] * D[5], c01 = D[4] * D[5] - D[3] * D[2], c02 = D[3] * D[5] - D[4] * D[1];
+            const R c11 = D[0] * D[2] - D[4] * D[4], c12 = D[4] * D[3] - D[0] * D[5], c22 = D[0] * D[1] - D[3] * D[3];
+            const R det = D[0] * c00 + D[3] * c01 + D[4] * c02;
+            const R id = (R)1 / det;
+            const R Di[9] = {c00 * id, c01 * id, c02 * id, c01 * id, c11 * id, c12 * id, c02 * id, c12 * id, c22 * id};
+            R Am[9];
+#pragma unroll
+            for (int c = 0; c < 3; c++)
+#pragma unroll
+                for (int jj = 0; jj < 3; jj++)
+                    Am[3 * c + jj] = B[3 * c] * Di[jj] + B[3 * c + 1] * Di[3 + jj] + B[3 * c + 2] * Di[6 + jj];
+#pragma unroll
+            for (int e = 0; e < 9; e++) B[e] = Am[e];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) P.v[c][p] = v[c];
+#pragma unroll
+        for (int e = 0; e < 9; e++) P.C[e][p] = B[e];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const float bc = (float)(fabs(v[c]) + fabs(B[3 * c]) * dmax[0] + fabs(B[3 * c + 1]) * dmax[1] +
+                                     fabs(B[3 * c + 2]) * dmax[2]);
+            bmax = fmaxf(bmax, bc);
+        }
+        const R tv = (R)2 * ld(P.vol + p);
+        const R h0 = gu[0] * tv, h1 = gu[1] * tv, h2 = gu[2] * tv;
+        gacc += fx(h0 * h0 + h1 * h1 + h2 * h2, S.gd);
+    }
+    const long long gsum = block_reduce(gacc, OpAddL(), sh_l);
+    const float bm = block_reduce(bmax, OpMaxF(), sh_f);
+    if (threadIdx.x == 0) {
+        if (gsum) atomicAdd(&a.ctl->geup_acc, (unsigned long long)gsum);
+        if (bm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VMAX], bm * 1.000001f);
+    }
+}
+
+template <typename R>
+__global__ void k_affine_scale(StepArgs<R> a) {
+    a.ctl->sc_musl.q = make_fix(a.nump * a.mmax * (double)bits_f(a.ctl->nxt[a.parity ^ 1][B_VMAX]) * 1.0000001);
+}
+
+template <typename R, int OX, int OY, int OZ>
+__global__ void __launch_bounds__(256) k_affine_musl(StepArgs<R> a) {
+    constexpr int BX = BRX + OX, BY = BRY + OY, BZ = BRZ + OZ, BOX = BX * BY * BZ;
+    extern __shared__ unsigned long long sacc[];   // 3 * BOX
+    __shared__ Scales S;
+    if ((int)blockIdx.x >= *a.nwork) return;
+    const WorkItem w = a.work[blockIdx.x];
+    int ox, oy, oz;
+    brick_origin(w.tile, a.nbrick, ox, oy, oz);
+    for (int i = threadIdx.x; i < 3 * BOX; i += blockDim.x) sacc[i] = 0ull;
+    load_scales_musl(a, S);
+    const size_t N = (size_t)a.g.nodec;
+    const Particles<R> &P = a.P;
+    for (int p = w.begin + threadIdx.x; p < w.end; p += blockDim.x) {
+        const R x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+        bool oob = false;
+        const int cx = cell_of(x0, a.g, 0, oob), cy = cell_of(x1, a.g, 1, oob), cz = cell_of(x2, a.g, 2, oob);
+        Axis<R, OX> ax;
+        Axis<R, OY> ay;
+        Axis<R, OZ> az;
+        axis_eval<R, OX>(x0, a.g, 0, cx, ax);
+        axis_eval<R, OY>(x1, a.g, 1, cy, ay);
+        axis_eval<R, OZ>(x2, a.g, 2, cz, az);
+        const R m = ld(P.m + p);
+        const R v[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
+        R A[9];
+#pragma unroll
+        for (int e = 0; e < 9; e++) A[e] = ld(P.C[e] + p);
+        const int lx = cx - ox, ly = cy - oy, lz = cz - oz;
+        const bool in = (unsigned)lx < (unsigned)BRX && (unsigned)ly < (unsigned)BRY && (unsigned)lz < (unsigned)BRZ;
+#pragma unroll
+        for (int k = 0; k <= OZ; k++)
+#pragma unroll
+            for (int j = 0; j <= OY; j++)
+#pragma unroll
+                for (int i = 0; i <= OX; i++) {
+                    const R Nm = ax.w[i] * ay.w[j] * az.w[k] * m;
+                    R vn[3];
+                    affine_velocity(v, A, cp_coord<R, OX>(a.g, 0, cx + i) - x0, cp_coord<R, OY>(a.g, 1, cy + j) - x1,
+                                    cp_coord<R, OZ>(a.g, 2, cz + k) - x2, vn);
+                    const long long q0 = fx(Nm * vn[0], S.q), q1 = fx(Nm * vn[1], S.q), q2 = fx(Nm * vn[2], S.q);
+                    if (in) {
+                        const int li = (lx + i) + BX * ((ly + j) + BY * (lz + k));
+                        atomic_add_i64(&sacc[li], q0);
+                        atomic_add_i64(&sacc[BOX + li], q1);
+                        atomic_add_i64(&sacc[2 * BOX + li], q2);
+                    } else {
+                        const size_t gn = node_id(a.g, cx + i, cy + j, cz + k);
+                        atomic_add_i64(&a.acc2[gn], q0);
+                        atomic_add_i64(&a.acc2[N + gn], q1);
+                        atomic_add_i64(&a.acc2[2 * N + gn], q2);
+                    }
+                }
     }
     __syncthreads();
     for (int li = threadIdx.x; li < BOX; li += blockDim.x) {
@@ -2130,6 +2391,7 @@ static StepArgs<R> make_args(mpm_ctx *c) {
     a.P.vol0 = f + 22 * n;
     a.P.vol = f + 23 * n;
     for (int k = 0; k < 3; k++) a.P.a[k] = c->nreal == 27 ? f + (24 + k) * n : nullptr;
+    for (int k = 0; k < 9; k++) a.P.C[k] = c->affine ? f + (24 + k) * n : nullptr;
     a.P.matid = (int *)(base + (size_t)c->nreal * n * rs);
     a.P.pid = a.P.matid + n;
     a.work = c->d_work;
@@ -2180,7 +2442,8 @@ static StepArgs<R> make_args(mpm_ctx *c) {
 }
 
 static bool use_cell_kernels(const mpm_ctx *c) {
-    return c->cell_scatter && c->precision == 32 && c->g.order[0] == 1 && c->g.order[1] == 1 && c->g.order[2] == 1;
+    return c->cell_scatter && !c->affine && c->precision == 32 && c->g.order[0] == 1 && c->g.order[1] == 1 &&
+           c->g.order[2] == 1;
 }
 
 static int num_sms() {
@@ -2242,8 +2505,14 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
             }
         }
         size_t smem = (size_t)NACC * BOX * sizeof(unsigned long long);
-        cudaFuncSetAttribute(k_p2g_box<R, OX, OY, OZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_p2g_box<R, OX, OY, OZ><<<c->nwork_cap, 256, smem, c->stream>>>(a);
+        if (c->affine) {
+            cudaFuncSetAttribute(k_p2g_box<R, OX, OY, OZ, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+            k_p2g_box<R, OX, OY, OZ, true><<<c->nwork_cap, 256, smem, c->stream>>>(a);
+        } else {
+            cudaFuncSetAttribute(k_p2g_box<R, OX, OY, OZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_p2g_box<R, OX, OY, OZ><<<c->nwork_cap, 256, smem, c->stream>>>(a);
+        }
         timer_end(c, K_P2G);
     } else if (which == 1) {
         timer_begin(c, K_G2P_MUSL);
@@ -2275,8 +2544,19 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
             }
         }
         size_t smem = (size_t)3 * BOX * sizeof(unsigned long long);
-        cudaFuncSetAttribute(k_g2p_musl_box<R, OX, OY, OZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_g2p_musl_box<R, OX, OY, OZ><<<c->nwork_cap, 256, smem, c->stream>>>(a);
+        if (c->affine) {
+            const int nb = (int)std::min<int64_t>((c->num + 255) / 256, 8 * num_sms());
+            k_affine_gather<R, OX, OY, OZ><<<nb, 256, 0, c->stream>>>(a);
+            k_affine_scale<R><<<1, 1, 0, c->stream>>>(a);
+            cudaFuncSetAttribute(k_affine_musl<R, OX, OY, OZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+            k_affine_musl<R, OX, OY, OZ><<<c->nwork_cap, 256, smem, c->stream>>>(a);
+            c->launches += 2;
+        } else {
+            cudaFuncSetAttribute(k_g2p_musl_box<R, OX, OY, OZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+            k_g2p_musl_box<R, OX, OY, OZ><<<c->nwork_cap, 256, smem, c->stream>>>(a);
+        }
         timer_end(c, K_G2P_MUSL);
     } else {
         timer_begin(c, K_G2P_UPDATE);

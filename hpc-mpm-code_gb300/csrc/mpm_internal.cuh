@@ -95,6 +95,7 @@ template <typename R>
 struct Particles {
     R *x[3], *v[3], *F[9], *s[6], *m, *vol0, *vol;
     R *a[3];          // particle acceleration (implicit contexts only, else null)
+    R *C[9];          // affine velocity matrix, row major (TPIC / APIC contexts only, else null)
     int *matid, *pid;
 };
 
@@ -151,7 +152,9 @@ struct mpm_ctx {
     // particles
     int64_t num = 0;
     size_t rsize = 4;
-    int nreal = 24;                        // real fields per particle: 24, or 27 with acceleration (implicit)
+    int nreal = 24;                        // real fields per particle: 24, 27 with acceleration (implicit),
+                                           // 33 with the affine matrix (TPIC / APIC)
+    bool affine = false;                   // TPIC or APIC: fields [24, 33) hold the affine matrix
     size_t pstride = 64;                   // elements between particle field arrays: num rounded up to 64
     void *pbuf[2] = {nullptr, nullptr};   // two SoA copies
     int cur = 0;

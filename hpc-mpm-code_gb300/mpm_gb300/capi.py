@@ -65,6 +65,7 @@ _ip = C.POINTER(C.c_int)
 EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_status_string",
            "mpm_gpu_load_particles", "mpm_gpu_set_bc", "mpm_gpu_p2g", "mpm_gpu_grid_update", "mpm_gpu_g2p",
            "mpm_gpu_step_explicit", "mpm_gpu_download_nodal", "mpm_gpu_download_particles",
+           "mpm_gpu_download_affine",
            "mpm_gpu_upload_particles", "mpm_gpu_steps_host", "mpm_gpu_sync",
            "mpm_gpu_get_stats", "mpm_gpu_enable_kernel_timing", "mpm_gpu_kernel_times", "mpm_gpu_implicit_setup",
            "mpm_gpu_implicit_step", "mpm_gpu_implicit_assemble", "mpm_gpu_implicit_get_system",
@@ -99,6 +100,7 @@ def load(path: str | None = None):
     lib.mpm_gpu_step_explicit.argtypes = [C.c_void_p, C.c_int, C.c_double]
     lib.mpm_gpu_download_nodal.argtypes = [C.c_void_p, C.c_int, _dp]
     lib.mpm_gpu_download_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
+    lib.mpm_gpu_download_affine.argtypes = [C.c_void_p, _dp]
     lib.mpm_gpu_upload_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
     lib.mpm_gpu_steps_host.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, _dp, _dp, _dp, _dp]
     lib.mpm_gpu_sync.argtypes = [C.c_void_p]
@@ -244,6 +246,12 @@ class GpuSolid:
              "mpm_gpu_download_particles")
         return {"x": x.reshape(n, 3), "v": v.reshape(n, 3), "F": F.reshape(n, 3, 3), "sigma": sig.reshape(n, 6),
                 "vol": vol}
+
+    def affine(self):
+        """TPIC / APIC: the affine velocity matrix per particle (n, 3, 3), load order."""
+        out = np.zeros(self.num * 9)
+        _chk(self.lib.mpm_gpu_download_affine(self.ctx, _ptr(out)), "mpm_gpu_download_affine")
+        return out.reshape(self.num, 3, 3)
 
     def download_into(self, coord=None, vel=None, F=None, stress=None, vol=None):
         """Download into caller-provided C-contiguous float64 arrays (pinned for full speed)."""

@@ -44,7 +44,12 @@ typedef enum {
     MPM_ERR_NEWTON_MAXIT = 10
 } mpm_status;
 
-typedef enum { MPM_PIC = 0, MPM_FLIP = 1 } mpm_scheme;  /* MapScheme, module/dataset.h:19 */
+/* MapScheme, module/dataset.h:19.  TPIC and APIC (module/map_and_interpolate.h:57-175)
+ * carry a 3x3 affine velocity matrix per particle (TPIC vel_grad; APIC
+ * vel_Bmat . inv_Dmat); their P2G reads the control-point coordinate as
+ * xyc[nid][j], where the reference's VarP2G reads xyc[j][nid] (past the end
+ * of xyc).  Explicit contexts only. */
+typedef enum { MPM_PIC = 0, MPM_FLIP = 1, MPM_TPIC = 2, MPM_APIC = 3 } mpm_scheme;
 
 typedef struct mpm_ctx mpm_ctx;
 
@@ -78,7 +83,7 @@ typedef struct {
     double dt;          /* time step (dt) */
     double mtol;        /* mass tolerance (mtol) */
     double gravity[3];  /* body force per unit mass (bb) */
-    int scheme;         /* MPM_PIC or MPM_FLIP (solswitch) */
+    int scheme;         /* mpm_scheme (solswitch) */
     int precision;      /* 32: FP32 particle/grid arithmetic; 64: FP64 */
     int shifting;       /* 1: DeltaCorrectionParticleShifting as the reference; 0: off */
     int resort_period;  /* physical re-sort of particles by brick every N steps (>= 1); 0 = default (8) */
@@ -137,6 +142,11 @@ mpm_status mpm_gpu_download_nodal(mpm_ctx *ctx, int field, double *host);
  * Host buffers in pinned memory transfer at full link speed. */
 mpm_status mpm_gpu_download_particles(mpm_ctx *ctx, double *coord, double *vel, double *F, double *stress,
                                       double *vol);
+/* TPIC / APIC contexts: the affine velocity matrix of each particle, 9
+ * row-major values per particle in load order (TPIC vel_grad, APIC
+ * vel_Bmat . inv_Dmat, module/map_and_interpolate.h:59,105); zeros for PIC
+ * and FLIP.  Synchronises the stream. */
+mpm_status mpm_gpu_download_affine(mpm_ctx *ctx, double *affine);
 /* Overwrites the state of the loaded particles (same count, load order) from
  * host arrays; NULL leaves a field unchanged.  Replaces writing the particle
  * vectors between steps (e.g. SolidMaterialPointBase::RestartInput,

@@ -47,3 +47,33 @@ def test_oracle_p_wave_speed():
     o = port.PortSolid(s, shifting=False)
     c = kp.measured_speed(o.steps, lambda: o.particles()["v"], x0)
     assert abs(c / kp.C_P - 1.0) <= 0.03, (c, kp.C_P)
+
+
+def test_oracle_affine_transfers_keep_angular_momentum():
+    """TPIC and APIC (module/map_and_interpolate.h:57-175, index fixed) keep
+    the spin of a free block after their first step (tests/kat_spin.py):
+    |L(200) / L(1) - 1| <= 1e-3, where PIC keeps less than 20 % of L(0);
+    with linear shape functions APIC equals TPIC to 1e-10 (rounding only)."""
+    import kat_spin as ks
+
+    out = {}
+    for scheme in (scenes.PIC, scenes.TPIC, scenes.APIC):
+        s = ks.block(scheme)
+        o = port.PortSolid(s, shifting=False)
+        L0 = ks.angular_momentum_z(s.mass, s.coord, s.vel)
+        o.steps(1)
+        p = o.particles()
+        L1 = ks.angular_momentum_z(s.mass, p["x"], p["v"])
+        o.steps(199)
+        p = o.particles()
+        out[scheme] = (L0, L1, ks.angular_momentum_z(s.mass, p["x"], p["v"]), o.affine(), p)
+    L0, _, Lp, _, _ = out[scenes.PIC]
+    assert Lp / L0 < 0.2
+    for scheme in (scenes.TPIC, scenes.APIC):
+        L0, L1, L, _, _ = out[scheme]
+        assert L1 / L0 > 0.9
+        assert abs(L / L1 - 1.0) <= 1.0e-3, (scheme, L / L1)
+    At, Aa = out[scenes.TPIC][3], out[scenes.APIC][3]
+    assert np.linalg.norm(At - Aa) <= 1.0e-10 * np.linalg.norm(At)
+    assert np.linalg.norm(out[scenes.TPIC][4]["v"] - out[scenes.APIC][4]["v"]) <= 1.0e-10 * np.linalg.norm(
+        out[scenes.TPIC][4]["v"])
