@@ -57,6 +57,8 @@ def parse():
                     help="steps of the 256-scene batched workload (0 skips)")
     ap.add_argument("--fluid-steps", type=int, default=100,
                     help="steps of the 12.6M-particle Tait dam break (0 skips)")
+    ap.add_argument("--apic-steps", type=int, default=100,
+                    help="steps of the headline workload with APIC transfers (0 skips)")
     ap.add_argument("--train-pairs", type=int, default=2000,
                     help="training pairs when no committed preconditioner parameters exist")
     ap.add_argument("--implicit-steps", type=int, default=50,
@@ -423,6 +425,30 @@ def run_fluid(args, torch, stream, hbm_peak):
                          "note": "fluid formula N_p*64 + N_n*56; the generic solid kernels also move F and stress"}}
 
 
+def run_apic(args, torch, stream, hbm_peak):
+    """The headline spinning block with APIC transfers (MapScheme APIC): each
+    particle also carries its 3x3 affine velocity matrix; the transfers run on
+    the generic brick kernels (affine P2G; gather, scale and MUSL launches).
+    FP32."""
+    from mpm_gb300 import capi, scenes
+
+    s = workload(args.cells)
+    s.scheme = scenes.APIC
+    gpu = capi.GpuSolid(s, precision=32, stream=stream.cuda_stream)
+    gpu.steps(args.warmup)
+    gpu.sync()
+    ms = timed_steps(torch, stream, gpu, args.apic_steps)
+    gpu.sync()
+    gpu.close()
+    ms_step = ms / args.apic_steps
+    alg = algorithmic_bytes(s.num, s.nodec) + s.num * 72   # + the affine matrix read and written (9 + 9 words)
+    return {"metric": METRIC, "value": s.num * args.apic_steps / (ms * 1e-3), "unit": METRIC,
+            "ms_per_step": ms_step, "steps": args.apic_steps, "particles": s.num, "scheme": "APIC", "dtype": "f32",
+            "roofline": {"bound": "hbm", "achieved": alg / (ms_step * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": alg / (ms_step * 1e-3) / 1e9 / hbm_peak, "algorithmic_bytes_per_step": alg,
+                         "note": "N_p*(176 + 72) + N_n*56: the solid formula plus the affine matrix"}}
+
+
 def run_gb300(args):
     import torch
 
@@ -520,7 +546,12 @@ def run_gb300(args):
         except Exception as exc:   # reported, never required
             implicit = {"metric": "implicit step time", "value": None, "error": str(exc)}
 
-    batched = fluid = None
+    batched = fluid = apic = None
+    if args.apic_steps > 0:
+        try:
+            apic = run_apic(args, torch, stream, hbm_peak)
+        except Exception as exc:
+            apic = {"metric": METRIC, "value": None, "error": str(exc)}
     if args.batched_steps > 0:
         try:
             batched = run_batched(args, torch, stream, hbm_peak)
@@ -549,7 +580,7 @@ def run_gb300(args):
                            "l2": "inputs larger than L2: 393 MB particle state per step, no flush"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(),
                 "gpu_launches": int(launches), "kernels": kernels, "implicit": implicit,
-                "batched": batched, "fluid": fluid}
+                "batched": batched, "fluid": fluid, "apic": apic}
         print(json.dumps(line), flush=True)
     gpu.close()
     if world > 1:

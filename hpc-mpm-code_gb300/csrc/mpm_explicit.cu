@@ -195,13 +195,34 @@ __device__ __forceinline__ void brick_origin(int b, const int *nb, int &ox, int 
 constexpr int CELL_SPLIT = 2;
 constexpr int CELL_THREADS = BRC * CELL_SPLIT;
 
+// Control-point coordinate xyc[idx][d] along one axis (DefineCpPos,
+// module/mesh.h:32-47, on one rank: the open-knot end points of a quadratic
+// axis sit on the walls).
+template <typename R, int O>
+__device__ __forceinline__ R cp_coord(const KGeom<R> &g, int d, int idx) {
+    if (O == 1) return g.xmin[d] + g.dx[d] * (R)idx;
+    if (idx == 0) return g.xmin[d];
+    if (idx == g.nnc[d] - 1) return g.xmin[d] + g.dx[d] * (R)g.nel[d];
+    return g.xmin[d] + g.dx[d] * ((R)idx - (R)0.5);
+}
+
+// v + A (x_i - x_p): the velocity a TPIC / APIC particle carries to node i
+// (TPIC::VarP2G / APIC::VarP2G, module/map_and_interpolate.h:62-77,104-130,
+// with the coordinate read as xyc[nid][j]).
+template <typename R>
+__device__ __forceinline__ void affine_velocity(const R *v, const R *A, R d0, R d1, R d2, R *out) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) out[c] = v[c] + (A[3 * c] * d0 + A[3 * c + 1] * d1 + A[3 * c + 2] * d2);
+}
+
 // One particle of a cell's P2G: FP32 register sums of the four corners of
 // z-layer h, or (a particle that left its sorted cell) its own fixed-point
-// atomics.
+// atomics.  AFF: TPIC / APIC, the momentum carries v + A (x_i - x_p).
+template <bool AFF = false>
 __device__ __forceinline__ void p2g_particle(const StepArgs<float> &a, const Scales &S, int cx, int cy, int cz, int h,
                                              float x0, float x1, float x2, float m, float vol, const float *v,
                                              const float *s, float fxg, float fyg, float fzg, float (*acc)[4],
-                                             int &misses, int &oobs, int defer_p = -1) {
+                                             int &misses, int &oobs, int defer_p = -1, const float *A = nullptr) {
     bool oob = false;
     const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
     oobs += oob && h == 0;
@@ -225,7 +246,11 @@ __device__ __forceinline__ void p2g_particle(const StepArgs<float> &a, const Sca
             const int i = c & 1, j = c >> 1;
             const float wxy = ax.w[i] * ay.w[j];
             float q[NACC];
-            p2g_terms(wxy * wz, ax.dw[i] * ay.w[j] * wz, ax.w[i] * ay.dw[j] * wz, wxy * dwz, m, vol, v, s, mfx, mfy,
+            float vn[3] = {v[0], v[1], v[2]};
+            if constexpr (AFF)
+                affine_velocity(v, A, cp_coord<float, 1>(a.g, 0, px + i) - x0, cp_coord<float, 1>(a.g, 1, py + j) - x1,
+                                cp_coord<float, 1>(a.g, 2, pz + h) - x2, vn);
+            p2g_terms(wxy * wz, ax.dw[i] * ay.w[j] * wz, ax.w[i] * ay.dw[j] * wz, wxy * dwz, m, vol, vn, s, mfx, mfy,
                       mfz, q);
             long long o[NACC];
             fx_terms(q, S, o);
@@ -242,7 +267,11 @@ __device__ __forceinline__ void p2g_particle(const StepArgs<float> &a, const Sca
         for (int i = 0; i < 2; i++) {
             const float wxy = ax.w[i] * ay.w[j];
             float q[NACC];
-            p2g_terms(wxy * wz, ax.dw[i] * ay.w[j] * wz, ax.w[i] * ay.dw[j] * wz, wxy * dwz, m, vol, v, s, mfx, mfy,
+            float vn[3] = {v[0], v[1], v[2]};
+            if constexpr (AFF)
+                affine_velocity(v, A, cp_coord<float, 1>(a.g, 0, px + i) - x0, cp_coord<float, 1>(a.g, 1, py + j) - x1,
+                                cp_coord<float, 1>(a.g, 2, pz + h) - x2, vn);
+            p2g_terms(wxy * wz, ax.dw[i] * ay.w[j] * wz, ax.w[i] * ay.dw[j] * wz, wxy * dwz, m, vol, vn, s, mfx, mfy,
                       mfz, q);
             const int c = i + 2 * j;
 #pragma unroll
@@ -293,7 +322,7 @@ __device__ __forceinline__ void p2g_node_pass(const StepArgs<float> &a, const Sc
     }
 }
 
-template <int MINB>
+template <int MINB, bool AFF = false>
 __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell(StepArgs<float> a) {
     __shared__ float corner[NACC * 8][BRC];       // 32 KB
     __shared__ Scales S;
@@ -319,8 +348,13 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell(StepArgs<float>
         const float v[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
         const float s[6] = {ld(P.s[0] + p), ld(P.s[1] + p), ld(P.s[2] + p),
                             ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
-        p2g_particle(a, S, cx, cy, cz, h, ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p), ld(P.m + p),
-                     ld(P.vol + p), v, s, fxg, fyg, fzg, acc, misses, oobs, p);
+        float A[AFF ? 9 : 1];
+        if constexpr (AFF) {
+#pragma unroll
+            for (int e = 0; e < 9; e++) A[e] = ld(P.C[e] + p);
+        }
+        p2g_particle<AFF>(a, S, cx, cy, cz, h, ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p), ld(P.m + p),
+                          ld(P.vol + p), v, s, fxg, fyg, fzg, acc, misses, oobs, p, A);
     }
     p2g_node_pass(a, S, corner, sh_red, lc, h, ox, oy, oz, acc, misses, oobs);
 }
@@ -342,12 +376,14 @@ __device__ __forceinline__ float cell_offset_u(float x, const KGeom<float> &g, i
 }
 
 // both z-layers of a particle that left its sorted cell, by fixed-point atomics
+template <bool AFF = false>
 __device__ __noinline__ void p2g_miss(const StepArgs<float> &a, const Scales &S, int cx, int cy, int cz, float x0,
                                       float x1, float x2, float m, float vol, const float *vel, const float *sg,
-                                      float fxg, float fyg, float fzg, int &misses, int &oobs) {
+                                      float fxg, float fyg, float fzg, int &misses, int &oobs,
+                                      const float *A = nullptr) {
     float dummy[NACC][4];
-    p2g_particle(a, S, cx, cy, cz, 0, x0, x1, x2, m, vol, vel, sg, fxg, fyg, fzg, dummy, misses, oobs);
-    p2g_particle(a, S, cx, cy, cz, 1, x0, x1, x2, m, vol, vel, sg, fxg, fyg, fzg, dummy, misses, oobs);
+    p2g_particle<AFF>(a, S, cx, cy, cz, 0, x0, x1, x2, m, vol, vel, sg, fxg, fyg, fzg, dummy, misses, oobs, -1, A);
+    p2g_particle<AFF>(a, S, cx, cy, cz, 1, x0, x1, x2, m, vol, vel, sg, fxg, fyg, fzg, dummy, misses, oobs, -1, A);
 }
 
 template <int MINB, bool LIST>
@@ -1178,6 +1214,7 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell_staged(Ste
 // Deferred passes for the particles that left their sorted cell since the
 // last re-sort: one thread per queued particle, fixed-point atomics (order
 // independent, so the results do not depend on the queue order).
+template <bool AFF = false>
 __global__ void __launch_bounds__(256) k_p2g_misses(StepArgs<float> a) {
     __shared__ Scales S;
     load_scales(a, S);
@@ -1190,8 +1227,13 @@ __global__ void __launch_bounds__(256) k_p2g_misses(StepArgs<float> a) {
         const float vel[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
         const float sg[6] = {ld(P.s[0] + p), ld(P.s[1] + p), ld(P.s[2] + p),
                              ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
-        p2g_miss(a, S, -1, -1, -1, ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p), ld(P.m + p), ld(P.vol + p), vel,
-                 sg, fxg, fyg, fzg, misses, oobs);
+        float A[AFF ? 9 : 1];
+        if constexpr (AFF) {
+#pragma unroll
+            for (int e = 0; e < 9; e++) A[e] = ld(P.C[e] + p);
+        }
+        p2g_miss<AFF>(a, S, -1, -1, -1, ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p), ld(P.m + p), ld(P.vol + p),
+                      vel, sg, fxg, fyg, fzg, misses, oobs, A);
     }
 }
 
@@ -1288,26 +1330,6 @@ __global__ void k_step_reset(StepArgs<R> a) {
 // One CTA per work item (a chunk of one brick's particles); every
 // contribution is converted to int64 and added into a shared box of the
 // brick's nodes (exact, order independent).
-// Control-point coordinate xyc[idx][d] along one axis (DefineCpPos,
-// module/mesh.h:32-47, on one rank: the open-knot end points of a quadratic
-// axis sit on the walls).
-template <typename R, int O>
-__device__ __forceinline__ R cp_coord(const KGeom<R> &g, int d, int idx) {
-    if (O == 1) return g.xmin[d] + g.dx[d] * (R)idx;
-    if (idx == 0) return g.xmin[d];
-    if (idx == g.nnc[d] - 1) return g.xmin[d] + g.dx[d] * (R)g.nel[d];
-    return g.xmin[d] + g.dx[d] * ((R)idx - (R)0.5);
-}
-
-// v + A (x_i - x_p): the velocity a TPIC / APIC particle carries to node i
-// (TPIC::VarP2G / APIC::VarP2G, module/map_and_interpolate.h:62-77,104-130,
-// with the coordinate read as xyc[nid][j]).
-template <typename R>
-__device__ __forceinline__ void affine_velocity(const R *v, const R *A, R d0, R d1, R d2, R *out) {
-#pragma unroll
-    for (int c = 0; c < 3; c++) out[c] = v[c] + (A[3 * c] * d0 + A[3 * c + 1] * d1 + A[3 * c + 2] * d2);
-}
-
 template <typename R, int OX, int OY, int OZ, bool AFF = false>
 __global__ void __launch_bounds__(256) k_p2g_box(StepArgs<R> a) {
     constexpr int BX = BRX + OX, BY = BRY + OY, BZ = BRZ + OZ, BOX = BX * BY * BZ;
@@ -1670,6 +1692,87 @@ __global__ void __launch_bounds__(256) k_affine_gather(StepArgs<R> a) {
     if (threadIdx.x == 0) {
         if (gsum) atomicAdd(&a.ctl->geup_acc, (unsigned long long)gsum);
         if (bm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VMAX], bm * 1.000001f);
+    }
+}
+
+// FP32 linear grids: the affine MUSL scatter as per-cell register sums (two
+// threads per cell, thread h owns the four corners of z-layer h), the node
+// pass of k_p2g_cell for the three momentum fields; a particle that left its
+// sorted cell adds its own fixed-point atomics.
+__global__ void __launch_bounds__(CELL_THREADS, 3) k_affine_musl_cell(StepArgs<float> a) {
+    __shared__ float corner[3 * 8][BRC];
+    __shared__ Scales S;
+    const int b = blockIdx.x;
+    const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
+    const int *cs = a.cstart + (size_t)b * (BRC + 1);
+    if (cs[0] == cs[BRC]) return;   // empty brick (uniform across the CTA)
+    int ox, oy, oz;
+    brick_origin(b, a.nbrick, ox, oy, oz);
+    const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
+    load_scales_musl(a, S);
+    const size_t N = (size_t)a.g.nodec;
+    const Particles<float> &P = a.P;
+    float acc[3][4];
+#pragma unroll
+    for (int f = 0; f < 3; f++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[f][c] = 0.0f;
+    for (int p = cs[lc]; p < cs[lc + 1]; p++) {
+        const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+        bool oob = false;
+        const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
+        Axis<float, 1> ax, ay, az;
+        axis_eval<float, 1>(x0, a.g, 0, px, ax);
+        axis_eval<float, 1>(x1, a.g, 1, py, ay);
+        axis_eval<float, 1>(x2, a.g, 2, pz, az);
+        const float m = ld(P.m + p);
+        const float v[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
+        float A[9];
+#pragma unroll
+        for (int e = 0; e < 9; e++) A[e] = ld(P.C[e] + p);
+        const bool mine = (px == cx) && (py == cy) && (pz == cz);
+        const float wz = h ? az.w[1] : az.w[0], dz = cp_coord<float, 1>(a.g, 2, pz + h) - x2;
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const float Nm = ax.w[i] * ay.w[j] * wz * m;
+                float vn[3];
+                affine_velocity(v, A, cp_coord<float, 1>(a.g, 0, px + i) - x0, cp_coord<float, 1>(a.g, 1, py + j) - x1,
+                                dz, vn);
+                if (mine) {
+#pragma unroll
+                    for (int f = 0; f < 3; f++) acc[f][i + 2 * j] += Nm * vn[f];
+                } else {
+                    const size_t gn = node_id(a.g, px + i, py + j, pz + h);
+#pragma unroll
+                    for (int f = 0; f < 3; f++) atomic_add_i64(&a.acc2[f * N + gn], fx(Nm * vn[f], S.q));
+                }
+            }
+    }
+#pragma unroll
+    for (int f = 0; f < 3; f++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) corner[f * 8 + c + 4 * h][lc] = acc[f][c];
+    __syncthreads();
+    constexpr int NX = BRX + 1, NY = BRY + 1, NZ = BRZ + 1, NB = NX * NY * NZ;
+    for (int it = threadIdx.x; it < NB * 3; it += CELL_THREADS) {
+        const int f = it / NB, n = it % NB;
+        const int nx = n % NX, ny = (n / NX) % NY, nz = n / (NX * NY);
+        const int gx = ox + nx, gy = oy + ny, gz = oz + nz;
+        if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
+        float sum = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+#pragma unroll
+            for (int j = 0; j < 2; j++)
+#pragma unroll
+                for (int i = 0; i < 2; i++) {
+                    const int ex = nx - i, ey = ny - j, ez = nz - k;
+                    if (ex >= 0 && ex < BRX && ey >= 0 && ey < BRY && ez >= 0 && ez < BRZ)
+                        sum += corner[f * 8 + i + 2 * (j + 2 * k)][ex + BRX * (ey + BRY * ez)];
+                }
+        if (sum != 0.0f) atomic_add_i64(&a.acc2[(size_t)f * N + node_id(a.g, gx, gy, gz)], fx(sum, S.q));
     }
 }
 
@@ -2504,6 +2607,16 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                 return check_launch(c);
             }
         }
+        if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
+            if (c->affine && c->cell_scatter) {
+                // TPIC / APIC: per-cell register sums with the affine momentum
+                k_p2g_cell<2, true><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                k_p2g_misses<true><<<2 * num_sms(), 256, 0, c->stream>>>(a);
+                timer_end(c, K_P2G);
+                c->launches += 2;
+                return check_launch(c);
+            }
+        }
         size_t smem = (size_t)NACC * BOX * sizeof(unsigned long long);
         if (c->affine) {
             cudaFuncSetAttribute(k_p2g_box<R, OX, OY, OZ, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2548,9 +2661,18 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
             const int nb = (int)std::min<int64_t>((c->num + 255) / 256, 8 * num_sms());
             k_affine_gather<R, OX, OY, OZ><<<nb, 256, 0, c->stream>>>(a);
             k_affine_scale<R><<<1, 1, 0, c->stream>>>(a);
-            cudaFuncSetAttribute(k_affine_musl<R, OX, OY, OZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem);
-            k_affine_musl<R, OX, OY, OZ><<<c->nwork_cap, 256, smem, c->stream>>>(a);
+            bool cell = false;
+            if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
+                if (c->cell_scatter) {
+                    k_affine_musl_cell<<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                    cell = true;
+                }
+            }
+            if (!cell) {
+                cudaFuncSetAttribute(k_affine_musl<R, OX, OY, OZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem);
+                k_affine_musl<R, OX, OY, OZ><<<c->nwork_cap, 256, smem, c->stream>>>(a);
+            }
             c->launches += 2;
         } else {
             cudaFuncSetAttribute(k_g2p_musl_box<R, OX, OY, OZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,

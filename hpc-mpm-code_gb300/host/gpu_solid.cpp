@@ -43,7 +43,7 @@ void GpuSolidMaterialPoint::Upload() {
         cfg.dt = g_.dt;
         cfg.mtol = g_.mtol;
         for (int d = 0; d < 3; d++) cfg.gravity[d] = g_.bb[d];
-        cfg.scheme = solswitch == MapScheme::FLIP ? MPM_FLIP : MPM_PIC;
+        cfg.scheme = static_cast<int>(solswitch);   // MPM_PIC .. MPM_APIC
         cfg.precision = precision_;
         cfg.shifting = 1;
         check(mpm_gpu_create(&gd, &md, &cfg, &ctx_), "mpm_gpu_create");

@@ -35,7 +35,8 @@ struct BoundaryCondition {
     std::vector<double> fbc;
 };
 
-enum class MapScheme { PIC, FLIP };
+// MapScheme (module/dataset.h:19), in the reference's order
+enum class MapScheme { PIC, FLIP, TPIC, APIC };
 
 class Error : public std::runtime_error {
   public:
