@@ -657,6 +657,28 @@ __global__ void k_state_scatter(R *f, size_t N, size_t S, int nreal, const doubl
         for (int k = 0; k < 6; k++) f[(15 + k) * S + j] = (R)st[ST_S * N + 6 * p + k];
     if (mask & 16) f[23 * S + j] = (R)st[ST_VOL * N + p];
 }
+// The affine matrices from the staging buffer (load order) into fields
+// 24..32; raises the next P2G's momentum bound to max_c (|v_c| + sum_j |A_cj| dmax_j).
+template <typename R>
+__global__ void k_affine_scatter_state(R *f, size_t N, size_t S, int nreal, const double *st, DevCtl *ctl, int parity,
+                                       double d0, double d1, double d2) {
+    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N) return;
+    const size_t p = (size_t)((const int *)(f + nreal * S) + S)[j];
+    float bm = 0.0f;
+    for (int c = 0; c < 3; c++) {
+        double b = fabs((double)f[(3 + c) * S + j]);
+        const double dm[3] = {d0, d1, d2};
+        for (int k = 0; k < 3; k++) {
+            const double v = st[9 * p + 3 * c + k];
+            f[(24 + 3 * c + k) * S + j] = (R)v;
+            b += fabs(v) * dm[k];
+        }
+        bm = fmaxf(bm, (float)b);
+    }
+    if (bm > 0.0f) atomic_max_pos(&ctl->nxt[parity][B_VMAX], bm * 1.000001f);
+}
+
 // The affine matrices (fields 24..32) into the staging buffer in load order.
 template <typename R>
 __global__ void k_affine_gather_state(const R *f, size_t N, size_t S, int nreal, double *st) {
@@ -715,6 +737,29 @@ mpm_status mpm_gpu_download_affine(mpm_ctx *c, double *affine) {
     c->launches++;
     if (check_launch(c) != MPM_OK) return MPM_ERR_CUDA;
     CK(cudaMemcpyAsync(affine, c->d_stage, sizeof(double) * 9 * N, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_upload_affine(mpm_ctx *c, const double *affine) {
+    if (!c || (!affine && c->num > 0)) return MPM_ERR_BAD_ARG;
+    if (!c->affine) return MPM_ERR_STATE;
+    if (c->num == 0) return MPM_OK;
+    mpm_status s = ensure_staging(c);
+    if (s != MPM_OK) return s;
+    const size_t N = (size_t)c->num;
+    CK(cudaMemcpyAsync(c->d_stage, affine, sizeof(double) * 9 * N, cudaMemcpyHostToDevice, c->stream));
+    double dm[3];
+    for (int d = 0; d < 3; d++) dm[d] = (c->g.order[d] == 2 ? 1.5 : 1.0) * c->g.dx[d];
+    const int nb = (int)((N + 255) / 256), par = (int)(c->step & 1);
+    if (c->precision == 64)
+        k_affine_scatter_state<double><<<nb, 256, 0, c->stream>>>((double *)c->pbuf[c->cur], N, c->pstride, c->nreal,
+                                                                   c->d_stage, c->d_ctl, par, dm[0], dm[1], dm[2]);
+    else
+        k_affine_scatter_state<float><<<nb, 256, 0, c->stream>>>((float *)c->pbuf[c->cur], N, c->pstride, c->nreal,
+                                                                  c->d_stage, c->d_ctl, par, dm[0], dm[1], dm[2]);
+    c->launches++;
+    if (check_launch(c) != MPM_OK) return MPM_ERR_CUDA;
     CK(cudaStreamSynchronize(c->stream));
     return MPM_OK;
 }

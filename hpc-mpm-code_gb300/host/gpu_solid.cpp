@@ -23,6 +23,11 @@ void GpuSolidMaterialPoint::InitializePointData(int n) {
     def_grad.assign(n, {});
     for (auto &F : def_grad)
         for (int i = 0; i < 3; i++) F[i][i] = 1.0;   // solid_data_io.cpp:28
+    id.resize(n);
+    for (int p = 0; p < n; p++) id[p] = p;
+    surf_point.assign(n, 0);
+    accel.assign(n, {});
+    affine.assign(n, {});
 }
 
 void GpuSolidMaterialPoint::Upload() {
@@ -51,6 +56,12 @@ void GpuSolidMaterialPoint::Upload() {
     check(mpm_gpu_load_particles(ctx_, num, &coord[0][0], &vel[0][0], mass.data(), vol0.data(), &def_grad[0][0][0],
                                  &stress[0][0], matid.data()),
           "mpm_gpu_load_particles");
+    // a restart carries vol (vol0 otherwise) and the affine matrix (zero otherwise)
+    if (from_restart_ && num > 0) {
+        check(mpm_gpu_upload_particles(ctx_, nullptr, nullptr, nullptr, nullptr, vol.data()), "mpm_gpu_upload_particles");
+        if (solswitch == MapScheme::TPIC || solswitch == MapScheme::APIC)
+            check(mpm_gpu_upload_affine(ctx_, &affine[0][0][0]), "mpm_gpu_upload_affine");
+    }
     const BoundaryCondition *bcs[3] = {&ubc, &vbc, &wbc};
     for (int k = 0; k < 3; k++)
         check(mpm_gpu_set_bc(ctx_, k, bcs[k]->ibc, bcs[k]->nbc.data(), bcs[k]->fbc.data()), "mpm_gpu_set_bc");
@@ -59,6 +70,10 @@ void GpuSolidMaterialPoint::Upload() {
 void GpuSolidMaterialPoint::Download() {
     check(mpm_gpu_download_particles(ctx_, &coord[0][0], &vel[0][0], &def_grad[0][0][0], &stress[0][0], vol.data()),
           "mpm_gpu_download_particles");
+    if (solswitch == MapScheme::TPIC || solswitch == MapScheme::APIC) {
+        affine.resize(num);
+        check(mpm_gpu_download_affine(ctx_, &affine[0][0][0]), "mpm_gpu_download_affine");
+    }
 }
 
 void GpuSolidMaterialPoint::Particle2Node() { check(mpm_gpu_p2g(ctx_, g_.facl), "mpm_gpu_p2g"); }

@@ -8,6 +8,8 @@
 #pragma once
 
 #include <array>
+#include <istream>
+#include <ostream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -56,6 +58,10 @@ class GpuSolidMaterialPoint {
     std::vector<std::array<double, 3>> coord, vel;
     std::vector<std::array<double, 6>> stress;
     std::vector<std::array<std::array<double, 3>, 3>> def_grad;
+    std::vector<int> id, surf_point;              // carried through the decks, not used by the transfers
+    std::vector<std::array<double, 3>> accel;     // restart field; zero on the explicit path
+    // TPIC: tpic.vel_grad; APIC: apic.vel_Bmat . apic.inv_Dmat (module/map_and_interpolate.h:59,105)
+    std::vector<std::array<std::array<double, 3>, 3>> affine;
     BoundaryCondition ubc, vbc, wbc;
 
     explicit GpuSolidMaterialPoint(const GridState &g, int precision = 32);
@@ -65,8 +71,14 @@ class GpuSolidMaterialPoint {
 
     // InputPointData (module/solid/solid_data_io.cpp:13-36) then upload
     void InitializePointData(int n);
-    void Upload();          // particles + boundary conditions to the device
+    void Upload();          // particles (with vol and the affine matrix) + boundary conditions to the device
     void Download();        // device particle state into the vectors above
+
+    // the reference's text formats (scene_io.cpp): InputPointData
+    // (module/solid/solid_data_io.cpp:13-36), RestartInput / RestartOutput (:61-142)
+    void InputPointData(std::istream &in);
+    void RestartInput(std::istream &in);
+    void RestartOutput(std::ostream &out) const;
 
     void MeshPointLinklist() {}           // the GPU bins every step inside Particle2Node
     void Particle2Node();                 // Particle2NodeS
@@ -80,6 +92,7 @@ class GpuSolidMaterialPoint {
   private:
     GridState g_;
     int precision_;
+    bool from_restart_ = false;   // set by RestartInput: Upload also sends vol and the affine matrix
     mpm_ctx *ctx_ = nullptr;
     void check(mpm_status s, const char *where) const {
         if (s != MPM_OK) throw Error(s, where);

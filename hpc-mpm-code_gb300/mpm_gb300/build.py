@@ -57,22 +57,25 @@ def _compile(src, verbose=False, ptxas_info=False):
 
 
 DRIVER = os.path.join(LIBDIR, "explicit_driver")
+SCENE_TOOL = os.path.join(LIBDIR, "scene_tool")
 
 
 def build_host(verbose: bool = False) -> str:
-    """The C++ host layer (host/gpu_solid.cpp) and its explicit driver, linked
-    against libmpm_gb300.so."""
+    """The C++ host layer (host/gpu_solid.cpp, host/scene_io.cpp), its explicit
+    driver and scene_tool, linked against libmpm_gb300.so.  Returns the driver."""
     lib = build(verbose)
-    srcs = [os.path.join(HOST, "gpu_solid.cpp"), os.path.join(HOST, "explicit_driver.cpp")]
-    deps = srcs + [os.path.join(HOST, "gpu_solid.h"), lib]
-    if _stale(DRIVER, deps):
-        cmd = ["g++", "-O2", "-std=c++17", "-I" + INCLUDE, "-I" + HOST] + srcs + [
-            "-L" + LIBDIR, "-lmpm_gb300", "-Wl,-rpath," + LIBDIR, "-o", DRIVER]
-        if verbose:
-            print(" ".join(cmd), flush=True)
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"host build failed:\n{r.stdout}\n{r.stderr}")
+    layer = [os.path.join(HOST, "gpu_solid.cpp"), os.path.join(HOST, "scene_io.cpp")]
+    headers = [os.path.join(HOST, "gpu_solid.h"), os.path.join(HOST, "scene_io.h"), os.path.join(INCLUDE, "mpm_gpu.h")]
+    for exe, main in ((DRIVER, "explicit_driver.cpp"), (SCENE_TOOL, "scene_tool.cpp")):
+        srcs = layer + [os.path.join(HOST, main)]
+        if _stale(exe, srcs + headers + [lib]):
+            cmd = ["g++", "-O2", "-std=c++17", "-I" + INCLUDE, "-I" + HOST] + srcs + [
+                "-L" + LIBDIR, "-lmpm_gb300", "-Wl,-rpath," + LIBDIR, "-o", exe]
+            if verbose:
+                print(" ".join(cmd), flush=True)
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"host build failed:\n{r.stdout}\n{r.stderr}")
     return DRIVER
 
 

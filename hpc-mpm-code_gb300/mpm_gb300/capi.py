@@ -65,7 +65,7 @@ _ip = C.POINTER(C.c_int)
 EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_status_string",
            "mpm_gpu_load_particles", "mpm_gpu_set_bc", "mpm_gpu_p2g", "mpm_gpu_grid_update", "mpm_gpu_g2p",
            "mpm_gpu_step_explicit", "mpm_gpu_download_nodal", "mpm_gpu_download_particles",
-           "mpm_gpu_download_affine",
+           "mpm_gpu_download_affine", "mpm_gpu_upload_affine",
            "mpm_gpu_upload_particles", "mpm_gpu_steps_host", "mpm_gpu_sync",
            "mpm_gpu_get_stats", "mpm_gpu_enable_kernel_timing", "mpm_gpu_kernel_times", "mpm_gpu_implicit_setup",
            "mpm_gpu_implicit_step", "mpm_gpu_implicit_assemble", "mpm_gpu_implicit_get_system",
@@ -101,6 +101,7 @@ def load(path: str | None = None):
     lib.mpm_gpu_download_nodal.argtypes = [C.c_void_p, C.c_int, _dp]
     lib.mpm_gpu_download_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
     lib.mpm_gpu_download_affine.argtypes = [C.c_void_p, _dp]
+    lib.mpm_gpu_upload_affine.argtypes = [C.c_void_p, _dp]
     lib.mpm_gpu_upload_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
     lib.mpm_gpu_steps_host.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, _dp, _dp, _dp, _dp]
     lib.mpm_gpu_sync.argtypes = [C.c_void_p]
@@ -252,6 +253,11 @@ class GpuSolid:
         out = np.zeros(self.num * 9)
         _chk(self.lib.mpm_gpu_download_affine(self.ctx, _ptr(out)), "mpm_gpu_download_affine")
         return out.reshape(self.num, 3, 3)
+
+    def upload_affine(self, affine):
+        """TPIC / APIC: overwrite the affine matrices ((n, 3, 3) float64, load order)."""
+        a = np.ascontiguousarray(affine, dtype=np.float64)
+        _chk(self.lib.mpm_gpu_upload_affine(self.ctx, _ptr(a)), "mpm_gpu_upload_affine")
 
     def download_into(self, coord=None, vel=None, F=None, stress=None, vol=None):
         """Download into caller-provided C-contiguous float64 arrays (pinned for full speed)."""

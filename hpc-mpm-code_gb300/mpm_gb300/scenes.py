@@ -351,3 +351,71 @@ def pack_scenes(scenes, gap=2):
             packed.bcs.append((comp, np.concatenate([b[0] for b in bcs[comp]]),
                                np.concatenate([b[1] for b in bcs[comp]])))
     return Batch(scene=packed, scenes=list(scenes), cell_offset=offs, begin=np.array(begin), end=np.array(end))
+
+
+# ---------------------------------------------------------------- decks
+SCHEME_NAMES = ("PIC", "FLIP", "TPIC", "APIC")
+
+
+def write_reference_decks(s: Scene, directory: str, rstflag: int = 0, nsteps: int = 100, rho: float = 1000.0):
+    """Write a scene as the reference's input decks for one rank, in the
+    formats its readers take: the parameter deck of datain_para
+    (work/src_solid/explicit/datain_para.cpp:28-84), the grid deck of
+    InputParaGriddata (module/data_io.cpp:31-125) with the u / v / w
+    boundary lists of BCInput (module/bc.cpp:9-28), and the particle deck
+    of InputPointData (module/solid/solid_data_io.cpp:13-36; it carries no
+    velocity).  Returns the three paths (para.txt, grid0.txt, point0.txt)."""
+    import os
+
+    os.makedirs(directory, exist_ok=True)
+    r = repr
+    xymax = [s.xymin[i] + s.dxy[i] * s.xyelem[i] for i in range(3)]
+    para = os.path.join(directory, "para.txt")
+    with open(para, "w") as f:
+        f.write("--- mapping scheme, restart flag, load steps ---\n")
+        f.write(f"{SCHEME_NAMES[s.scheme]} {rstflag} 1\n")
+        f.write("--- first step, last step, output interval ---\n")
+        f.write(f"0 {nsteps} {nsteps}\n")
+        f.write("--- dt, mtol ---\n")
+        f.write(f"{r(float(s.dt))} {r(float(s.mtol))}\n")
+        f.write("--- xyminw ---\n" + " ".join(r(float(v)) for v in s.xymin) + "\n")
+        f.write("--- xymaxw ---\n" + " ".join(r(float(v)) for v in xymax) + "\n")
+        f.write("--- xyelemw ---\n" + " ".join(str(int(v)) for v in s.xyelem) + "\n")
+        f.write("--- idimc ---\n" + " ".join(str(int(v)) for v in s.idimc) + "\n")
+        f.write("--- npxye ---\n" + " ".join(str(int(v)) for v in s.npxye) + "\n")
+        f.write("--- rho, nmat, npropmax ---\n")
+        f.write(f"{r(float(rho))} {len(s.iprop)} 3\n")
+        for k in range(len(s.iprop)):
+            f.write(f"--- material {k}: iprop, nprop ---\n{int(s.iprop[k])} 3\n")
+            f.write(" ".join(r(float(v)) for v in s.mat_prop[k]) + "\n")
+        f.write("--- body force ---\n" + " ".join(r(float(v)) for v in s.gravity) + "\n")
+    grid = os.path.join(directory, "grid0.txt")
+    nel, nn, nc = s.xyelem, [v + 1 for v in s.xyelem], s.xynodec
+    with open(grid, "w") as f:
+        f.write("0     --- rank ---\n")
+        f.write(f"{nel[0] * nel[1] * nel[2]} {nel[0]} {nel[1]} {nel[2]}     --- elements ---\n")
+        f.write(f"{nn[0] * nn[1] * nn[2]} {nn[0]} {nn[1]} {nn[2]}     --- nodes ---\n")
+        f.write(f"{nc[0] * nc[1] * nc[2]} {nc[0]} {nc[1]} {nc[2]}     --- control points ---\n")
+        f.write("0 0 0     --- rank position ---\n")
+        f.write(" ".join(r(float(v)) for v in s.xymin) + "     --- xymin ---\n")
+        f.write(" ".join(r(float(v)) for v in xymax) + "     --- xymax ---\n")
+        f.write("0 0 0     --- first element ---\n")
+        f.write(f"{nel[0] - 1} {nel[1] - 1} {nel[2] - 1}     --- last element ---\n")
+        f.write("0     --- overlapped ranks ---\n")
+        lists = {BC_U: ([], []), BC_V: ([], []), BC_W: ([], [])}
+        for comp, nodes, vals in s.bcs:
+            lists[comp][0].extend(int(n) for n in nodes)
+            lists[comp][1].extend(float(v) for v in vals)
+        for comp in (BC_U, BC_V, BC_W):
+            nodes, vals = lists[comp]
+            f.write(f"{len(nodes)}     --- boundary nodes, component {comp} ---\n")
+            for n, v in zip(nodes, vals):
+                f.write(f"{n} {r(v)}\n")
+    point = os.path.join(directory, "point0.txt")
+    with open(point, "w") as f:
+        f.write(f"{s.num}     --- number of solid material points ---\n")
+        for x in s.coord:
+            f.write(" ".join(r(float(v)) for v in x) + "\n")
+        for p in range(s.num):
+            f.write(f"{p} {int(s.matid[p])} 0 {r(float(s.mass[p]))} {r(float(s.vol0[p]))}\n")
+    return para, grid, point

@@ -147,6 +147,10 @@ mpm_status mpm_gpu_download_particles(mpm_ctx *ctx, double *coord, double *vel, 
  * vel_Bmat . inv_Dmat, module/map_and_interpolate.h:59,105); zeros for PIC
  * and FLIP.  Synchronises the stream. */
 mpm_status mpm_gpu_download_affine(mpm_ctx *ctx, double *affine);
+/* Overwrites the affine matrices of a TPIC / APIC context (same layout; a
+ * restart, SolidMaterialPointBase::RestartInput, module/solid/solid_data_io.cpp:61-96)
+ * and raises the next P2G's fixed-point bound to cover them. */
+mpm_status mpm_gpu_upload_affine(mpm_ctx *ctx, const double *affine);
 /* Overwrites the state of the loaded particles (same count, load order) from
  * host arrays; NULL leaves a field unchanged.  Replaces writing the particle
  * vectors between steps (e.g. SolidMaterialPointBase::RestartInput,

@@ -34,6 +34,11 @@ def _lib():
     lib.ref_get_nodal.argtypes = [C.c_int, _dp]
     lib.ref_get_particles.argtypes = [_dp, _dp, _dp, _dp, _dp]
     lib.ref_get_affine.argtypes = [_dp]
+    lib.ref_io_read.argtypes = [C.c_char_p, C.c_char_p, _ip, _dp]
+    lib.ref_io_bc.argtypes = [C.c_int, _ip, _dp]
+    lib.ref_io_particles.argtypes = [_ip, _ip, _ip, _dp, _dp]
+    lib.ref_restart_output.argtypes = [C.c_char_p]
+    lib.ref_restart_input.argtypes = [C.c_char_p]
     lib.ref_implicit_init.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _ip, C.c_int, C.c_int, C.c_double]
     lib.ref_implicit_steps.argtypes = [C.c_int, C.c_double]
     lib.ref_implicit_assemble.argtypes = [C.c_double]
@@ -45,6 +50,29 @@ def _lib():
 
 NODAL_FIELDS = {"nmass": (0, 1), "nvof": (1, 1), "nmome": (2, 3), "nforce": (3, 3), "nvel": (4, 3),
                 "naccel": (5, 3), "nvol": (6, 1), "ndispl": (7, 3)}
+
+
+def read_decks(grid_path, point_path):
+    """The reference's own readers (InputParaGriddata + BCInput x3 +
+    InputPointData) on a grid and a particle deck: what they parsed."""
+    lib = _lib()
+    ints = np.zeros(20, dtype=np.int32)
+    dbl = np.zeros(12)
+    assert lib.ref_io_read(grid_path.encode(), point_path.encode(), ints, dbl) == 0
+    out = {"ints": ints.copy(), "dbl": dbl.copy()}
+    for k in range(3):
+        n = int(ints[16 + k])
+        nodes, vals = np.zeros(max(n, 1), dtype=np.int32), np.zeros(max(n, 1))
+        lib.ref_io_bc(k, nodes, vals)
+        out[f"bc{k}_nodes"], out[f"bc{k}_vals"] = nodes[:n], vals[:n]
+    n = int(ints[19])
+    idv, mat, surf = (np.zeros(n, dtype=np.int32) for _ in range(3))
+    mass, vol0 = np.zeros(n), np.zeros(n)
+    lib.ref_io_particles(idv, mat, surf, mass, vol0)
+    x = np.zeros(3 * n)
+    lib.ref_get_particles(x, np.zeros(3 * n), np.zeros(9 * n), np.zeros(6 * n), np.zeros(n))
+    out.update({"coord": x.reshape(n, 3), "id": idv, "matid": mat, "surf": surf, "mass": mass, "vol0": vol0})
+    return out
 
 
 class RefSolid:
@@ -87,6 +115,14 @@ class RefSolid:
         self.lib.ref_get_particles(x, v, F, sig, vol)
         return {"x": x.reshape(n, 3), "v": v.reshape(n, 3), "F": F.reshape(n, 3, 3), "sigma": sig.reshape(n, 6),
                 "vol": vol}
+
+    def restart_output(self, prefix):
+        """SolidMaterialPointBase::RestartOutput to prefix + "0_re.txt"."""
+        assert self.lib.ref_restart_output(prefix.encode()) == 0
+
+    def restart_input(self, prefix):
+        """SolidMaterialPointBase::RestartInput from prefix + "0_re.txt"."""
+        assert self.lib.ref_restart_input(prefix.encode()) == self.scene.num
 
     def affine(self):
         """TPIC / APIC: the affine velocity matrix per particle (n, 3, 3)."""

@@ -30,11 +30,13 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <memory>
 #include <vector>
 
 #include "bc.h"
 #include "cal_mat.h"
+#include "data_io.h"
 #include "dataset.h"
 #include "material_point.h"
 #include "mesh.h"
@@ -442,6 +444,89 @@ int ref_get_affine(double *out) {
                 out[9 * p + 3 * i + j] = a;
             }
     return sp.num;
+}
+
+/* ---- on-disk formats, through the reference's own readers and writers ----
+ * Reads a grid deck (InputParaGriddata, module/data_io.cpp:31-125, followed by
+ * the u / v / w BoundaryCondition lists, BCInput, module/bc.cpp:9-28) and a
+ * particle deck (SolidMaterialPointBase::InputPointData,
+ * module/solid/solid_data_io.cpp:13-36) into a fresh explicit solid.
+ * ints: nelem, xyelem[3], node, xynode[3], nodec, xynodec[3], nxyr[3], isb,
+ * then ibc u, v, w, then num.  dbl: xymin[3], xymax[3], aelemmin[3],
+ * aelemmax[3].  Particle arrays are returned by ref_io_particles. */
+int ref_io_read(const char *grid_path, const char *point_path, int *ints, double *dbl) {
+    g_imp.reset();
+    g_exp = std::make_unique<ExplicitSolid>();
+    std::ifstream gin(grid_path);
+    if (!gin.is_open()) return -1;
+    InputParaGriddata(gin);
+    g_exp->ubc.BCInput(gin, true);
+    g_exp->vbc.BCInput(gin, true);
+    g_exp->wbc.BCInput(gin, true);
+    std::ifstream pin(point_path);
+    if (!pin.is_open()) return -2;
+    g_exp->InputPointData(pin);
+    int k = 0;
+    ints[k++] = nelem;
+    for (int i = 0; i < 3; i++) ints[k++] = xyelem[i];
+    ints[k++] = node;
+    for (int i = 0; i < 3; i++) ints[k++] = xynode[i];
+    ints[k++] = nodec;
+    for (int i = 0; i < 3; i++) ints[k++] = xynodec[i];
+    for (int i = 0; i < 3; i++) ints[k++] = nxyr[i];
+    ints[k++] = isb;
+    ints[k++] = g_exp->ubc.ibc;
+    ints[k++] = g_exp->vbc.ibc;
+    ints[k++] = g_exp->wbc.ibc;
+    ints[k++] = g_exp->num;
+    for (int i = 0; i < 3; i++) {
+        dbl[i] = xymin[i];
+        dbl[3 + i] = xymax[i];
+        dbl[6 + i] = aelemmin[i];
+        dbl[9 + i] = aelemmax[i];
+    }
+    return 0;
+}
+
+/* BC lists (node, value) of the last ref_io_read, which 0 u, 1 v, 2 w */
+int ref_io_bc(int which, int *nodes, double *vals) {
+    BoundaryCondition &b = which == 0 ? g_exp->ubc : which == 1 ? g_exp->vbc : g_exp->wbc;
+    for (int i = 0; i < b.ibc; i++) {
+        nodes[i] = b.nbc[i];
+        vals[i] = b.fbc[i];
+    }
+    return b.ibc;
+}
+
+/* id, matid, surf_point, mass, vol0 of the last ref_io_read (coord via ref_get_particles) */
+int ref_io_particles(int *id, int *matid, int *surf, double *mass, double *vol0) {
+    for (int p = 0; p < g_exp->num; p++) {
+        id[p] = g_exp->id[p];
+        matid[p] = g_exp->matid[p];
+        surf[p] = g_exp->surf_point[p];
+        mass[p] = g_exp->mass[p];
+        vol0[p] = g_exp->vol0[p];
+    }
+    return g_exp->num;
+}
+
+/* SolidMaterialPointBase::RestartOutput / RestartInput (solid_data_io.cpp:61-142)
+ * of the explicit solid: file = prefix + "0_re.txt" (pointfile, rank 0). */
+int ref_restart_output(const char *prefix) {
+    if (!g_exp) return -1;
+    pointfile = prefix;
+    myrank = 0;
+    g_exp->RestartOutput();
+    return 0;
+}
+
+int ref_restart_input(const char *prefix) {
+    if (!g_exp) return -1;
+    pointfile = prefix;
+    myrank = 0;
+    g_exp->RestartInput();
+    g_exp->MeshPointLinklist();
+    return g_exp->num;
 }
 
 int ref_get_particles(double *coord, double *vel, double *F, double *stress, double *vol) {

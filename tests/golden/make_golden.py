@@ -9,6 +9,7 @@ committed and this script is re-run only when a case is added:
     oracle/build_ref.sh && python tests/golden/make_golden.py
     python tests/golden/make_golden.py --hyperelastic     # only models 2 and 3
     python tests/golden/make_golden.py --affine           # only the TPIC / APIC cases
+    python tests/golden/make_golden.py --io               # only the deck / restart fixtures (tests/golden/io)
 """
 from __future__ import annotations
 
@@ -112,6 +113,40 @@ def affine_cases():
         explicit_case(f"explicit_{nm}_quadratic", s, nsteps=10)
 
 
+def io_cases():
+    """The reference's on-disk formats: decks written by
+    scenes.write_reference_decks for a small APIC block with a fixed bottom,
+    parsed by the reference's own readers (io.npz: parsed_*); a TPIC and an
+    APIC restart written by the reference's RestartOutput after 10 steps;
+    the APIC restart read back by the reference's RestartInput and run 10
+    more steps (io.npz: cont_*)."""
+    d = os.path.join(OUT, "io")
+    os.makedirs(d, exist_ok=True)
+    rng = np.random.default_rng(20261206)
+    out = {}
+    for scheme, nm in ((scenes.TPIC, "tpic"), (scenes.APIC, "apic")):
+        s = scenes.elastic_block(grid=(8, 8, 8), cell_lo=(2, 2, 0), cell_hi=(6, 6, 4), scheme=scheme, dt=1.0e-5,
+                                 seed=111 + scheme)
+        c = s.coord.mean(axis=0)
+        s.vel[:] = rng.normal(0.0, 0.2, size=s.vel.shape) + 20.0 * np.cross([0.0, 0.0, 1.0], s.coord - c)
+        if scheme == scenes.APIC:
+            para, grid, point = scenes.write_reference_decks(s, d, rstflag=1, nsteps=10)
+            parsed = ref.read_decks(grid, point)
+            out.update({f"parsed_{k}": v for k, v in parsed.items()})
+        r = ref.RefSolid(s)
+        r.steps(10)
+        r.restart_output(os.path.join(d, f"restart_{nm}"))
+        if scheme == scenes.APIC:
+            r = ref.RefSolid(s)
+            r.restart_input(os.path.join(d, f"restart_{nm}"))
+            r.steps(10)
+            out.update({f"cont_{k}": v for k, v in r.particles().items()})
+            out["cont_affine"] = r.affine()
+            out["cont_nsteps"] = np.array(10)
+    np.savez_compressed(os.path.join(d, "io.npz"), **out)
+    print("wrote", d, sorted(os.listdir(d)))
+
+
 def main():
     if not ref.available():
         raise SystemExit("oracle/_ref/libmpmref.so missing: run oracle/build_ref.sh first")
@@ -120,6 +155,9 @@ def main():
         return
     if "--affine" in sys.argv[1:]:
         affine_cases()
+        return
+    if "--io" in sys.argv[1:]:
+        io_cases()
         return
     rng = np.random.default_rng(20261203)
     # small elastic block, fixed bottom, PIC and FLIP, random initial velocity
@@ -145,6 +183,7 @@ def main():
     implicit_case("implicit_neohookean", s, nr_flag=True, nsteps=3)
     hyperelastic_cases()
     affine_cases()
+    io_cases()
 
 
 if __name__ == "__main__":
