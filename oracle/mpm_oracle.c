@@ -42,6 +42,9 @@ struct mo_ctx {
     double *coord, *vel, *accel, *mass, *vol0, *vol, *F, *stress, *jac;
     /* TPIC: vel_grad; APIC: vel_Bmat and inv_Dmat (module/map_and_interpolate.h:59,105), row major */
     double *aff, *aff_dinv;
+    /* F-bar (Fbar_flag, module/solid/solid_material_point.h:16): def_grad_bar, det_def_grad_bar */
+    int fbar;
+    double *fbarF, *jbar;
     int *matid;
     /* nodal, component-major: comp c of node n at c*nodec + n */
     double *nmass, *nvof, *nmome, *nforce, *nvel, *naccel, *nvol, *ndispl;
@@ -105,7 +108,7 @@ mo_ctx *mo_create(const int *xyelem, const double *xymin, const double *dxy, con
 static void free_particles(mo_ctx *c) {
     free(c->coord); free(c->vel); free(c->accel); free(c->mass); free(c->vol0); free(c->vol);
     free(c->F); free(c->stress); free(c->jac); free(c->matid); free(c->idp2p);
-    free(c->aff); free(c->aff_dinv);
+    free(c->aff); free(c->aff_dinv); free(c->fbarF); free(c->jbar);
 }
 
 void mo_destroy(mo_ctx *c) {
@@ -141,6 +144,8 @@ int mo_load(mo_ctx *c, int num, const double *coord, const double *vel, const do
     c->idp2p = (int *)zalloc(sizeof(int) * n);
     c->aff = (double *)zalloc(sizeof(double) * 9 * n);       /* VectorAssign: zero, solid_material_point.cpp:36-42 */
     c->aff_dinv = (double *)zalloc(sizeof(double) * 9 * n);
+    c->fbarF = (double *)zalloc(sizeof(double) * 9 * n);     /* def_grad_bar = I, det_def_grad_bar = 1 */
+    c->jbar = (double *)zalloc(sizeof(double) * n);
     memcpy(c->coord, coord, sizeof(double) * 3 * n);
     if (vel) memcpy(c->vel, vel, sizeof(double) * 3 * n);
     memcpy(c->mass, mass, sizeof(double) * n);
@@ -150,6 +155,8 @@ int mo_load(mo_ctx *c, int num, const double *coord, const double *vel, const do
         c->matid[p] = matid ? matid[p] : 0;
         c->jac[p] = 1.0; /* det_def_grad initialised to 1, solid_material_point.cpp:10 */
         c->F[9 * p + 0] = c->F[9 * p + 4] = c->F[9 * p + 8] = 1.0; /* solid_data_io.cpp:28 */
+        c->fbarF[9 * p + 0] = c->fbarF[9 * p + 4] = c->fbarF[9 * p + 8] = 1.0;
+        c->jbar[p] = 1.0;
     }
     return 0;
 }
@@ -431,7 +438,8 @@ static void update_stress(mo_ctx *c, int p, double *sts, const double FF[3][3], 
     } else if (model == 0) {
         mat_lin_elast(c, sts, d, mp, implicit);
     } else if (model == 1) {
-        mat_neo_hookean(c, sts, FF, mp, c->jac[p], c->jac[p], implicit);
+        /* UpdateStress passes det_def_grad and det_def_grad_bar (constitutive_model.cpp:287-297) */
+        mat_neo_hookean(c, sts, FF, mp, c->jac[p], c->fbar ? c->jbar[p] : c->jac[p], implicit);
     } else if (model == 2 && !implicit) {
         mat_stvk(sts, FF, mp, c->jac[p]);
     } else if (model == 3 && !implicit) {
@@ -674,6 +682,41 @@ static void g2p_explicit(mo_ctx *c) {
             for (int j = 0; j < 3; j++) { Fp[3 * a + j] = Fn[a][j]; dF[9 * p + 3 * a + j] = d[a][j]; }
         c->jac[p] = det3(Fn);
     }
+    /* cal_def_grad_bar (module/solid/explicit/fbar_projection.cpp:18-93): the trial
+     * J = det_def_grad_bar det(dF) projected to the nodes by volume (sum N J vol / nvof),
+     * gathered back as Jbar; dF scaled by cbrt(Jbar / J); def_grad_bar <- dF def_grad_bar,
+     * det_def_grad_bar <- Jbar */
+    if (c->fbar) {
+        double *nJ = (double *)zalloc(sizeof(double) * N);
+        FOR_PARTICLES(c, m, p) {
+            int ne = maksf(c, m, c->coord + 3 * p, nc, sf, dsf);
+            double d[3][3];
+            for (int a = 0; a < 3; a++)
+                for (int j = 0; j < 3; j++) d[a][j] = dF[9 * p + 3 * a + j];
+            double jt = c->jbar[p] * det3(d);
+            for (int i = 0; i < ne; i++) nJ[nc[i]] += sf[i] * jt * c->vol[p];
+        }
+        for (size_t n = 0; n < N; n++) nJ[n] = (c->nvof[n] > c->mtol) ? nJ[n] / c->nvof[n] : 0.0;
+        FOR_PARTICLES(c, m, p) {
+            int ne = maksf(c, m, c->coord + 3 * p, nc, sf, dsf);
+            double Jb = 0.0;
+            for (int i = 0; i < ne; i++) Jb += sf[i] * nJ[nc[i]];
+            double d[3][3];
+            for (int a = 0; a < 3; a++)
+                for (int j = 0; j < 3; j++) d[a][j] = dF[9 * p + 3 * a + j];
+            double J = c->jbar[p] * det3(d);
+            double sc = cbrt(Jb / J);
+            for (int a = 0; a < 9; a++) dF[9 * p + a] *= sc;
+            double Fb[3][3] = {{0}};
+            for (int a = 0; a < 3; a++)
+                for (int j = 0; j < 3; j++)
+                    for (int k = 0; k < 3; k++) Fb[a][j] += dF[9 * p + 3 * a + k] * c->fbarF[9 * p + 3 * k + j];
+            for (int a = 0; a < 3; a++)
+                for (int j = 0; j < 3; j++) c->fbarF[9 * p + 3 * a + j] = Fb[a][j];
+            c->jbar[p] = Jb;
+        }
+        free(nJ);
+    }
     /* update_point_coord_and_stress, var_trans_solid_explicit.cpp:150-185 */
     double *delta = (double *)zalloc(sizeof(double) * 3 * (size_t)c->num);
     shifting(c, delta);
@@ -686,8 +729,9 @@ static void g2p_explicit(mo_ctx *c) {
             for (int k = 0; k < 3; k++) c->coord[3 * p + k] += delta[3 * p + k];
         c->vol[p] = c->jac[p] * c->vol0[p];
         double Fm[3][3], dm[3][3];
+        const double *Fsrc = c->fbar ? c->fbarF : c->F;   /* F-bar: the stress sees def_grad_bar */
         for (int a = 0; a < 3; a++)
-            for (int j = 0; j < 3; j++) { Fm[a][j] = c->F[9 * p + 3 * a + j]; dm[a][j] = dF[9 * p + 3 * a + j]; }
+            for (int j = 0; j < 3; j++) { Fm[a][j] = Fsrc[9 * p + 3 * a + j]; dm[a][j] = dF[9 * p + 3 * a + j]; }
         update_stress(c, p, c->stress + 6 * p, Fm, dm, 0);
     }
     free(dF);
@@ -730,6 +774,17 @@ int mo_get_nodal(const mo_ctx *c, int field, double *out) {
     }
     memcpy(out, src, sizeof(double) * n);
     return (int)n;
+}
+
+int mo_set_fbar(mo_ctx *c, int on) {
+    c->fbar = on != 0;
+    return 0;
+}
+
+int mo_get_fbar(const mo_ctx *c, double *Fbar, double *Jbar) {
+    if (Fbar) memcpy(Fbar, c->fbarF, sizeof(double) * 9 * (size_t)c->num);
+    if (Jbar) memcpy(Jbar, c->jbar, sizeof(double) * (size_t)c->num);
+    return c->num;
 }
 
 int mo_get_affine(const mo_ctx *c, double *out) {

@@ -34,6 +34,10 @@ int mo_get_particles(const mo_ctx *c, double *coord, double *vel, double *F, dou
 /* scheme 2 (TPIC) / 3 (APIC): the affine velocity matrix per particle, 9
  * row-major values (TPIC vel_grad; APIC vel_Bmat . inv_Dmat); zeros otherwise */
 int mo_get_affine(const mo_ctx *c, double *out);
+/* F-bar projection (Fbar_flag; module/solid/explicit/fbar_projection.cpp): on / off
+ * after mo_load; def_grad_bar (9 per particle) and det_def_grad_bar */
+int mo_set_fbar(mo_ctx *c, int on);
+int mo_get_fbar(const mo_ctx *c, double *Fbar, double *Jbar);
 /* shape functions at one point in element m: returns nenode */
 int mo_shape(const mo_ctx *c, int m, const double *x, int *nc, double *sf, double *dsf);
 

@@ -42,6 +42,8 @@ def _lib():
     lib.mo_get_nodal.argtypes = [C.c_void_p, C.c_int, _dp]
     lib.mo_get_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
     lib.mo_get_affine.argtypes = [C.c_void_p, _dp]
+    lib.mo_set_fbar.argtypes = [C.c_void_p, C.c_int]
+    lib.mo_get_fbar.argtypes = [C.c_void_p, _dp, _dp]
     lib.mo_shape.argtypes = [C.c_void_p, C.c_int, _dp, _ip, _dp, _dp]
     lib.mo_implicit_setup.argtypes = [C.c_void_p, C.c_int, C.c_double]
     lib.mo_implicit_nnzb.argtypes = [C.c_void_p]
@@ -62,7 +64,7 @@ NODAL_FIELDS = {"nmass": (0, 1), "nvof": (1, 1), "nmome": (2, 3), "nforce": (3, 
 class PortSolid:
     """Same interface as oracle.ref.RefSolid, on the C restatement."""
 
-    def __init__(self, scene, implicit=False, shifting=True, nr_flag=False, spec_rad=1.0):
+    def __init__(self, scene, implicit=False, shifting=True, nr_flag=False, spec_rad=1.0, fbar=False):
         self.lib = lib = _lib()
         self.scene = s = scene
         i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
@@ -74,6 +76,8 @@ class PortSolid:
                     i32(s.matid), s.scheme, int(shifting))
         for comp, nodes, vals in s.bcs:
             lib.mo_set_bc(self.ctx, comp, len(nodes), i32(nodes), f64(vals))
+        if fbar:
+            lib.mo_set_fbar(self.ctx, 1)
         if implicit:
             self.nmat = lib.mo_implicit_setup(self.ctx, int(nr_flag), float(spec_rad))
 
@@ -105,6 +109,13 @@ class PortSolid:
         self.lib.mo_get_particles(self.ctx, x, v, F, sig, vol)
         return {"x": x.reshape(n, 3), "v": v.reshape(n, 3), "F": F.reshape(n, 3, 3), "sigma": sig.reshape(n, 6),
                 "vol": vol}
+
+    def fbar(self):
+        """F-bar runs: def_grad_bar (n, 3, 3) and det_def_grad_bar (n,)."""
+        n = self.scene.num
+        F, J = np.zeros(n * 9), np.zeros(n)
+        self.lib.mo_get_fbar(self.ctx, F, J)
+        return F.reshape(n, 3, 3), J
 
     def affine(self):
         """TPIC / APIC: the affine velocity matrix per particle (n, 3, 3)."""

@@ -39,6 +39,8 @@ def _lib():
     lib.ref_io_particles.argtypes = [_ip, _ip, _ip, _dp, _dp]
     lib.ref_restart_output.argtypes = [C.c_char_p]
     lib.ref_restart_input.argtypes = [C.c_char_p]
+    lib.ref_set_fbar.argtypes = [C.c_int]
+    lib.ref_get_fbar.argtypes = [_dp, _dp]
     lib.ref_implicit_init.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _ip, C.c_int, C.c_int, C.c_double]
     lib.ref_implicit_steps.argtypes = [C.c_int, C.c_double]
     lib.ref_implicit_assemble.argtypes = [C.c_double]
@@ -78,8 +80,9 @@ def read_decks(grid_path, point_path):
 class RefSolid:
     """One reference solid (explicit restated driver or implicit as-is)."""
 
-    def __init__(self, scene, implicit=False, shifting=True, nr_flag=False, spec_rad=1.0):
+    def __init__(self, scene, implicit=False, shifting=True, nr_flag=False, spec_rad=1.0, fbar=False):
         self.lib = _lib()
+        self.lib.ref_set_fbar(int(fbar))
         self.scene = s = scene
         i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
         f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
@@ -115,6 +118,13 @@ class RefSolid:
         self.lib.ref_get_particles(x, v, F, sig, vol)
         return {"x": x.reshape(n, 3), "v": v.reshape(n, 3), "F": F.reshape(n, 3, 3), "sigma": sig.reshape(n, 6),
                 "vol": vol}
+
+    def fbar(self):
+        """F-bar runs: def_grad_bar (n, 3, 3) and det_def_grad_bar (n,)."""
+        n = self.scene.num
+        F, J = np.zeros(n * 9), np.zeros(n)
+        assert self.lib.ref_get_fbar(F, J) == n
+        return F.reshape(n, 3, 3), J
 
     def restart_output(self, prefix):
         """SolidMaterialPointBase::RestartOutput to prefix + "0_re.txt"."""

@@ -215,6 +215,8 @@ class ExplicitSolid : public SolidMaterialPointBase {
             }
         }
 
+        if (this->Fbar_flag) DefGradBar(ddg);
+
         // update_point_coord_and_stress, var_trans_solid_explicit.cpp:150-185
         std::vector<std::array<double, 3>> delta_corr = this->DeltaCorrectionParticleShifting();
         for (int m = 0; m < nelem; m++) {
@@ -226,7 +228,52 @@ class ExplicitSolid : public SolidMaterialPointBase {
                 if (shifting_)
                     for (int i = 0; i < 3; i++) this->coord[pid][i] += delta_corr[pid][i];
                 this->vol[pid] = this->det_def_grad[pid] * this->vol0[pid];
-                this->UpdateConstitutiveModel(pid, this->stress, this->det_def_grad, this->def_grad, ddg);
+                if (this->Fbar_flag)   // var_trans_solid_explicit.cpp:298-304
+                    this->UpdateConstitutiveModel(pid, this->stress, this->det_def_grad_bar, this->def_grad_bar, ddg);
+                else
+                    this->UpdateConstitutiveModel(pid, this->stress, this->det_def_grad, this->def_grad, ddg);
+                pid = this->idp2p[pid];
+            }
+        }
+    }
+
+    // cal_def_grad_bar (module/solid/explicit/fbar_projection.cpp:18-93) restated
+    // on the members: that file does not compile here (it reads a global `sp`
+    // and includes the implicit solver's header).
+    void DefGradBar(std::vector<std::array<std::array<double, 3>, 3>> &ddg) {
+        int nenode;
+        std::vector<int> ncm;
+        std::vector<double> sf;
+        std::vector<std::array<double, 3>> dsf;
+        std::vector<double> det_ddg(this->num), nJbar(nodec, 0.0e0);
+        for (int p = 0; p < this->num; p++) det_ddg[p] = DetMat3(ddg[p]);
+        for (int m = 0; m < nelem; m++) {
+            int pid = this->idepf[m];
+            while (pid != -1) {
+                std::array<double, 3> xyp = this->coord[pid];
+                MakSf(m, xyp, idimc, xynodec, ncm, nenode, sf, dsf);
+                for (int ni = 0; ni < nenode; ni++)
+                    nJbar[ncm[ni]] += sf[ni] * (this->det_def_grad_bar[pid] * det_ddg[pid]) * this->vol[pid];
+                pid = this->idp2p[pid];
+            }
+        }
+        for (int n = 0; n < nodec; n++) nJbar[n] = (this->nvof[n] > mtol) ? nJbar[n] / this->nvof[n] : 0.0e0;
+        for (int m = 0; m < nelem; m++) {
+            int pid = this->idepf[m];
+            while (pid != -1) {
+                std::array<double, 3> xyp = this->coord[pid];
+                MakSf(m, xyp, idimc, xynodec, ncm, nenode, sf, dsf);
+                double Jbar = 0.0e0;
+                for (int ni = 0; ni < nenode; ni++) Jbar += sf[ni] * nJbar[ncm[ni]];
+                double J = this->det_def_grad_bar[pid] * det_ddg[pid];
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++) ddg[pid][i][j] *= cbrt((Jbar / J));
+                std::array<std::array<double, 3>, 3> Fb{};
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++)
+                        for (int k = 0; k < 3; k++) Fb[i][j] += ddg[pid][i][k] * this->def_grad_bar[pid][k][j];
+                this->def_grad_bar[pid] = Fb;
+                this->det_def_grad_bar[pid] = Jbar;
                 pid = this->idp2p[pid];
             }
         }
@@ -273,6 +320,7 @@ class ExplicitSolid : public SolidMaterialPointBase {
 };
 
 std::unique_ptr<ExplicitSolid> g_exp;
+int g_fbar = 0;   // Fbar_flag of the next explicit solid
 std::unique_ptr<implicitmpm::SolidMaterialPoint> g_imp;
 int g_last_krylov = 0;
 
@@ -287,6 +335,7 @@ void load_particles(SolidMaterialPointBase &sp, int num, const double *coord, co
     sp.num = num;
     const MapScheme schemes[4] = {MapScheme::PIC, MapScheme::FLIP, MapScheme::TPIC, MapScheme::APIC};
     sp.solswitch = schemes[(scheme >= 0 && scheme < 4) ? scheme : 0];
+    sp.Fbar_flag = g_fbar != 0;
     sp.InitializePointData();
     for (int p = 0; p < num; p++) {
         sp.id[p] = p;
@@ -297,7 +346,10 @@ void load_particles(SolidMaterialPointBase &sp, int num, const double *coord, co
         for (int i = 0; i < 3; i++) {
             sp.coord[p][i] = coord[3 * p + i];
             sp.vel[p][i] = vel ? vel[3 * p + i] : 0.0;
-            for (int j = 0; j < 3; j++) sp.def_grad[p][i][j] = eye_mat[i][j];  // solid_data_io.cpp:28
+            for (int j = 0; j < 3; j++) {
+                sp.def_grad[p][i][j] = eye_mat[i][j];  // solid_data_io.cpp:28
+                if (sp.Fbar_flag) sp.def_grad_bar[p][i][j] = eye_mat[i][j];
+            }
         }
     }
 }
@@ -526,6 +578,23 @@ int ref_restart_input(const char *prefix) {
     myrank = 0;
     g_exp->RestartInput();
     g_exp->MeshPointLinklist();
+    return g_exp->num;
+}
+
+/* Fbar_flag of the explicit solids created after this call */
+int ref_set_fbar(int on) {
+    g_fbar = on;
+    return 0;
+}
+
+/* def_grad_bar (9 per particle) and det_def_grad_bar of an F-bar run */
+int ref_get_fbar(double *Fbar, double *Jbar) {
+    if (!g_exp || !g_exp->Fbar_flag) return -1;
+    for (int p = 0; p < g_exp->num; p++) {
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) Fbar[9 * p + 3 * i + j] = g_exp->def_grad_bar[p][i][j];
+        Jbar[p] = g_exp->det_def_grad_bar[p];
+    }
     return g_exp->num;
 }
 

@@ -10,6 +10,7 @@ committed and this script is re-run only when a case is added:
     python tests/golden/make_golden.py --hyperelastic     # only models 2 and 3
     python tests/golden/make_golden.py --affine           # only the TPIC / APIC cases
     python tests/golden/make_golden.py --io               # only the deck / restart fixtures (tests/golden/io)
+    python tests/golden/make_golden.py --fbar             # only the F-bar cases
 """
 from __future__ import annotations
 
@@ -41,19 +42,24 @@ def scene_arrays(s):
     return d
 
 
-def explicit_case(name, scene, nsteps, facl=1.0):
-    r = ref.RefSolid(scene)
+def explicit_case(name, scene, nsteps, facl=1.0, fbar=False):
+    r = ref.RefSolid(scene, fbar=fbar)
     r.p2g(facl)
     out = {f"p2g_{k}": r.nodal(k) for k in ("nmass", "nvof", "nmome", "nforce", "nvel", "naccel", "nvol")}
-    r = ref.RefSolid(scene)
+    r = ref.RefSolid(scene, fbar=fbar)
     r.steps(1, facl)
     out.update({f"step1_{k}": v for k, v in r.particles().items()})
     if scene.scheme >= scenes.TPIC:
         out["step1_affine"] = r.affine()
+    if fbar:
+        out["step1_Fbar"], out["step1_Jbar"] = r.fbar()
     r.steps(nsteps - 1, facl)
     out.update({f"stepN_{k}": v for k, v in r.particles().items()})
     if scene.scheme >= scenes.TPIC:
         out["stepN_affine"] = r.affine()
+    if fbar:
+        out["stepN_Fbar"], out["stepN_Jbar"] = r.fbar()
+        out["fbar"] = np.array(1)
     out["nsteps"] = np.array(nsteps)
     out["facl"] = np.array(facl)
     np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **scene_arrays(scene), **out)
@@ -113,6 +119,21 @@ def affine_cases():
         explicit_case(f"explicit_{nm}_quadratic", s, nsteps=10)
 
 
+def fbar_cases():
+    """The F-bar projection (Fbar_flag on; fbar_projection.cpp restated in
+    the harness on the reference's members): a linear elastic PIC block and
+    a Neo-Hookean FLIP block with a random initial velocity."""
+    rng = np.random.default_rng(20261207)
+    s = scenes.elastic_block(grid=(10, 10, 8), cell_lo=(2, 2, 0), cell_hi=(7, 7, 5), iprop=0, E=5.0e5, dt=1.0e-5,
+                             seed=121)
+    s.vel[:] = rng.normal(0.0, 0.3, size=s.vel.shape)
+    explicit_case("explicit_fbar_linear", s, nsteps=20, fbar=True)
+    s = scenes.elastic_block(grid=(10, 10, 8), cell_lo=(2, 2, 0), cell_hi=(7, 7, 5), iprop=1, E=5.0e5, dt=1.0e-5,
+                             seed=122, scheme=scenes.FLIP)
+    s.vel[:] = rng.normal(0.0, 0.3, size=s.vel.shape)
+    explicit_case("explicit_fbar_neohookean", s, nsteps=20, fbar=True)
+
+
 def io_cases():
     """The reference's on-disk formats: decks written by
     scenes.write_reference_decks for a small APIC block with a fixed bottom,
@@ -159,6 +180,9 @@ def main():
     if "--io" in sys.argv[1:]:
         io_cases()
         return
+    if "--fbar" in sys.argv[1:]:
+        fbar_cases()
+        return
     rng = np.random.default_rng(20261203)
     # small elastic block, fixed bottom, PIC and FLIP, random initial velocity
     for scheme, nm in ((scenes.PIC, "explicit_pic"), (scenes.FLIP, "explicit_flip")):
@@ -184,6 +208,7 @@ def main():
     hyperelastic_cases()
     affine_cases()
     io_cases()
+    fbar_cases()
 
 
 if __name__ == "__main__":

@@ -14,7 +14,7 @@ from oracle import port
 TOL = 1.0e-12
 EXPLICIT = ["explicit_pic", "explicit_flip", "explicit_quadratic", "explicit_neohookean", "explicit_stvk",
             "explicit_mooney_rivlin", "explicit_tpic", "explicit_apic", "explicit_tpic_quadratic",
-            "explicit_apic_quadratic"]
+            "explicit_apic_quadratic", "explicit_fbar_linear", "explicit_fbar_neohookean"]
 IMPLICIT = ["implicit_linear", "implicit_neohookean"]
 
 
@@ -32,19 +32,26 @@ def test_explicit_p2g_matches_reference(name):
 def test_explicit_steps_match_reference(name):
     g = load_golden(name)
     s = scene_from_golden(g)
-    o = port.PortSolid(s)
+    fbar = "fbar" in g
+    o = port.PortSolid(s, fbar=fbar)
     o.steps(1, float(g["facl"]))
     p = o.particles()
     for k in ("x", "v", "F", "sigma", "vol"):
         assert rel_l2(p[k], g[f"step1_{k}"]) <= TOL, k
     if "step1_affine" in g:   # TPIC vel_grad / APIC vel_Bmat . inv_Dmat
         assert rel_l2(o.affine(), g["step1_affine"]) <= TOL
+    if fbar:                  # def_grad_bar, det_def_grad_bar
+        Fb, Jb = o.fbar()
+        assert rel_l2(Fb, g["step1_Fbar"]) <= TOL and rel_l2(Jb, g["step1_Jbar"]) <= TOL
     o.steps(int(g["nsteps"]) - 1, float(g["facl"]))
     p = o.particles()
     for k in ("x", "v", "F", "sigma", "vol"):
         assert rel_l2(p[k], g[f"stepN_{k}"]) <= 1.0e-10, k
     if "stepN_affine" in g:
         assert rel_l2(o.affine(), g["stepN_affine"]) <= 1.0e-10
+    if fbar:
+        Fb, Jb = o.fbar()
+        assert rel_l2(Fb, g["stepN_Fbar"]) <= 1.0e-10 and rel_l2(Jb, g["stepN_Jbar"]) <= 1.0e-10
 
 
 @pytest.mark.parametrize("name", IMPLICIT)
