@@ -103,6 +103,7 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     if (cfg->precision != 32 && cfg->precision != 64) return MPM_ERR_BAD_ARG;
     if (cfg->scheme < MPM_PIC || cfg->scheme > MPM_APIC) return MPM_ERR_UNSUPPORTED;
     if (cfg->implicit && cfg->scheme > MPM_FLIP) return MPM_ERR_UNSUPPORTED;
+    if (cfg->implicit && cfg->fbar) return MPM_ERR_UNSUPPORTED;
     if (!(cfg->dt > 0.0) || mat->nmat <= 0 || !mat->iprop || !mat->mat_prop) return MPM_ERR_BAD_ARG;
     for (int d = 0; d < 3; d++) {
         if (grid->xyelem[d] <= 0 || !(grid->dxy[d] > 0.0)) return MPM_ERR_BAD_ARG;
@@ -153,7 +154,9 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     c->resort_period = cfg->resort_period > 0 ? cfg->resort_period : 8;
     c->cell_scatter = cfg->scatter == 1 ? 0 : 1;
     c->affine = cfg->scheme == MPM_TPIC || cfg->scheme == MPM_APIC;
-    c->nreal = cfg->implicit ? 27 : (c->affine ? 33 : 24);
+    c->fbar = cfg->fbar != 0;
+    c->off_fbar = c->affine ? 33 : 24;
+    c->nreal = cfg->implicit ? 27 : c->off_fbar + (c->fbar ? 11 : 0);
     c->dt = cfg->dt;
     c->mtol = cfg->mtol;
     c->nmat = mat->nmat;
@@ -168,6 +171,7 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     alloc((void **)&c->d_matprop, sizeof(double) * 3 * c->nmat);
     alloc((void **)&c->d_acc, sizeof(unsigned long long) * NACC * N);
     alloc((void **)&c->d_acc2, sizeof(unsigned long long) * 3 * N);
+    if (c->fbar) alloc((void **)&c->d_facc, sizeof(unsigned long long) * N);
     alloc(&c->d_nodal, c->rsize * 13 * N);
     alloc((void **)&c->d_nvol, sizeof(double) * N);
     alloc((void **)&c->d_bcflag, N);
@@ -193,6 +197,7 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     cudaMemcpy(c->d_matprop, mat->mat_prop, sizeof(double) * 3 * c->nmat, cudaMemcpyHostToDevice);
     cudaMemset(c->d_acc, 0, sizeof(unsigned long long) * NACC * N);
     cudaMemset(c->d_acc2, 0, sizeof(unsigned long long) * 3 * N);
+    if (c->d_facc) cudaMemset(c->d_facc, 0, sizeof(unsigned long long) * N);
     cudaMemset(c->d_nodal, 0, c->rsize * 13 * N);
     cudaMemset(c->d_bcflag, 0, N);
     cudaMemset(c->d_bcval, 0, c->rsize * 3 * N);
@@ -232,6 +237,7 @@ void mpm_gpu_destroy(mpm_ctx *c) {
     free_dev(c->d_matprop);
     free_dev(c->d_acc);
     free_dev(c->d_acc2);
+    free_dev(c->d_facc);
     free_dev(c->d_nodal);
     free_dev(c->d_nvol);
     free_dev(c->d_bcflag);
@@ -296,6 +302,11 @@ static mpm_status upload_particles(mpm_ctx *c, int64_t n, const double *coord, c
                          fmax(fabs(s[5]) + fabs(s[1]) + fabs(s[3]), fabs(s[4]) + fabs(s[3]) + fabs(s[2])));
         vsmax = fmax(vsmax, fabs(vol0[p]) * rs);
     }
+    if (c->fbar && sizeof(R) == 8)   // def_grad_bar = I, det_def_grad_bar = 1 (FP32 stores both minus 1: zeros)
+        for (size_t p = 0; p < N; p++) {
+            f[(c->off_fbar + 0) * S + p] = f[(c->off_fbar + 4) * S + p] = f[(c->off_fbar + 8) * S + p] = (R)1;
+            f[(c->off_fbar + 9) * S + p] = (R)1;
+        }
     int *ip = (int *)(f + nr * S);
     for (size_t p = 0; p < N; p++) {
         int mid = matid ? matid[p] : 0;
@@ -679,6 +690,17 @@ __global__ void k_affine_scatter_state(R *f, size_t N, size_t S, int nreal, cons
     if (bm > 0.0f) atomic_max_pos(&ctl->nxt[parity][B_VMAX], bm * 1.000001f);
 }
 
+// def_grad_bar and det_def_grad_bar into the staging buffer in load order.
+template <typename R>
+__global__ void k_fbar_gather_state(const R *f, size_t N, size_t S, int nreal, int off, double *st) {
+    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N) return;
+    const size_t p = (size_t)((const int *)(f + nreal * S) + S)[j];
+    for (int k = 0; k < 9; k++)
+        st[9 * p + k] = (double)f[(off + k) * S + j] + (sizeof(R) == 4 && (k % 4) == 0 ? 1.0 : 0.0);
+    st[9 * N + p] = (double)f[(off + 9) * S + j] + (sizeof(R) == 4 ? 1.0 : 0.0);
+}
+
 // The affine matrices (fields 24..32) into the staging buffer in load order.
 template <typename R>
 __global__ void k_affine_gather_state(const R *f, size_t N, size_t S, int nreal, double *st) {
@@ -737,6 +759,28 @@ mpm_status mpm_gpu_download_affine(mpm_ctx *c, double *affine) {
     c->launches++;
     if (check_launch(c) != MPM_OK) return MPM_ERR_CUDA;
     CK(cudaMemcpyAsync(affine, c->d_stage, sizeof(double) * 9 * N, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return MPM_OK;
+}
+
+mpm_status mpm_gpu_download_fbar(mpm_ctx *c, double *Fbar, double *Jbar) {
+    if (!c) return MPM_ERR_BAD_ARG;
+    if (!c->fbar) return MPM_ERR_STATE;
+    if (c->num == 0) return MPM_OK;
+    mpm_status s = ensure_staging(c);
+    if (s != MPM_OK) return s;
+    const size_t N = (size_t)c->num;
+    const int nb = (int)((N + 255) / 256);
+    if (c->precision == 64)
+        k_fbar_gather_state<double><<<nb, 256, 0, c->stream>>>((const double *)c->pbuf[c->cur], N, c->pstride,
+                                                                c->nreal, c->off_fbar, c->d_stage);
+    else
+        k_fbar_gather_state<float><<<nb, 256, 0, c->stream>>>((const float *)c->pbuf[c->cur], N, c->pstride,
+                                                               c->nreal, c->off_fbar, c->d_stage);
+    c->launches++;
+    if (check_launch(c) != MPM_OK) return MPM_ERR_CUDA;
+    if (Fbar) CK(cudaMemcpyAsync(Fbar, c->d_stage, sizeof(double) * 9 * N, cudaMemcpyDeviceToHost, c->stream));
+    if (Jbar) CK(cudaMemcpyAsync(Jbar, c->d_stage + 9 * N, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return MPM_OK;
 }

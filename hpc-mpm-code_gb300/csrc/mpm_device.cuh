@@ -272,6 +272,50 @@ __device__ __forceinline__ void neo_hookean_stress_h(float *s, const float H[3][
     s[5] = (mu * bm[0][1]) * ij;
 }
 
+// F-bar form of MatNeoHookean (constitutive_model.cpp:62-120 with
+// jac_bar = det_def_grad_bar): ln of J-bar in the volumetric term, the
+// division by the plain J.  FP64 on F, FP32 on H = F - I with J - 1 values.
+template <typename R>
+__device__ __forceinline__ void neo_hookean_stress_bar(R *s, const R F[3][3], R jac, R jac_bar, R E, R nu) {
+    const R rd = (R)1 / (((R)1 + nu) * ((R)1 - (R)2 * nu));
+    const R lmd = nu * E * rd;
+    const R mu = (R)0.5 * E * ((R)1 - (R)2 * nu) * rd;
+    const R lnj = log(jac_bar);
+    const R ij = (R)1 / jac;
+    R be[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) be[i][j] = F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2];
+    s[0] = (mu * (be[0][0] - (R)1) + lmd * lnj) * ij;
+    s[1] = (mu * (be[1][1] - (R)1) + lmd * lnj) * ij;
+    s[2] = (mu * (be[2][2] - (R)1) + lmd * lnj) * ij;
+    s[3] = (mu * be[1][2]) * ij;
+    s[4] = (mu * be[0][2]) * ij;
+    s[5] = (mu * be[0][1]) * ij;
+}
+
+__device__ __forceinline__ void neo_hookean_stress_h_bar(float *s, const float H[3][3], float jm1, float jbm1, float E,
+                                                         float nu) {
+    const float rd = rcp_approx((1.0f + nu) * (1.0f - 2.0f * nu));
+    const float lmd = nu * E * rd;
+    const float mu = 0.5f * E * (1.0f - 2.0f * nu) * rd;
+    const float lnj = log1pf(jbm1);
+    const float ij = rcp_approx(1.0f + jm1);
+    float bm[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+            bm[i][j] = H[i][j] + H[j][i] + H[i][0] * H[j][0] + H[i][1] * H[j][1] + H[i][2] * H[j][2];
+    s[0] = (mu * bm[0][0] + lmd * lnj) * ij;
+    s[1] = (mu * bm[1][1] + lmd * lnj) * ij;
+    s[2] = (mu * bm[2][2] + lmd * lnj) * ij;
+    s[3] = (mu * bm[1][2]) * ij;
+    s[4] = (mu * bm[0][2]) * ij;
+    s[5] = (mu * bm[0][1]) * ij;
+}
+
 // MatStVk (constitutive_model.cpp:122-185), stress part: with b = F F^T and
 // tr E = (tr b - 3) / 2, sigma = (mu b^2 + (lambda tr E - mu) b) / J.
 template <typename R>

@@ -48,6 +48,7 @@ struct StepArgs {
     int nbrick[3];
     unsigned long long *acc;    // NACC * nodec
     unsigned long long *acc2;   // 3 * nodec
+    unsigned long long *facc;   // nodec (F-bar contexts)
     R *G;                       // gather field for the velocity gather (3 * nodec)
     R *nei;                     // nodec
     R *nvel2;                   // 3 * nodec
@@ -67,6 +68,7 @@ struct StepArgs {
     int all_tiles;              // process every tile in the grid passes (download mode)
     int gnorm;                  // FP32 gathers divide by their weight sum
     int implicit;               // implicit solid: the force fields carry sum N m a (AccelP2G)
+    int fbar;                   // F-bar projection: k_grid2 leaves the nodal volume sums to k_fbar_grid
     double nump;                // particle count as a bound factor
     double mmax;                // max particle mass
     double gshape;              // bound on |dN/dx|
@@ -1983,7 +1985,8 @@ __global__ void __launch_bounds__(256) k_grid2(StepArgs<R> a) {
         for (int c = 0; c < 3; c++) a.nvel2[c * N + n] = nv[c];
         if (!a.all_tiles) {
 #pragma unroll
-            for (int f = 0; f < NACC; f++) a.acc[f * N + n] = 0ull;
+            for (int f = 0; f < NACC; f++)
+                if (!(a.fbar && f == 1)) a.acc[f * N + n] = 0ull;   // F-bar: k_fbar_grid reads nvof first
 #pragma unroll
             for (int c = 0; c < 3; c++) a.acc2[c * N + n] = 0ull;
         }
@@ -1992,6 +1995,141 @@ __global__ void __launch_bounds__(256) k_grid2(StepArgs<R> a) {
         __syncthreads();
         if (threadIdx.x == 0) a.tileflag[t] = 0;
     }
+    }
+}
+
+// ================================================================= F-bar
+// cal_def_grad_bar (module/solid/explicit/fbar_projection.cpp:18-93), after
+// the MUSL nodal velocities (nvel2) are final:
+//   k_fbar_trial    per particle the step's dF = I + dt grad(nvel2) (the
+//                   update's own formula) and the trial J = Jbar det(dF),
+//                   stored; records max(J vol)
+//   k_fbar_scale    the fixed-point scale of the nodal sums from that bound
+//   k_fbar_scatter  sum_p N J vol into the nodes (int64 fixed point)
+//   k_fbar_grid     nJbar = sum / nvof (0 where nvof <= mtol) into the free
+//                   gather field G; clears the sums and the nvof sums
+// FP32 keeps J - 1 in place of J (trial, projected and gathered): the sums
+// are of N (J - 1) vol, a node with nvof <= mtol holds -1 (its nJbar = 0),
+// so sum_i N_i field_i = Jbar - 1 by the partition of unity.
+// and the update kernel (FBAR) gathers Jbar, scales dF by cbrt(Jbar / J),
+// advances def_grad_bar and hands (def_grad_bar, Jbar, scaled dF) to the
+// stress models, the plain J to the volume (var_trans_solid_explicit.cpp:
+// 176-180, 298-304).
+template <typename R, int OX, int OY, int OZ>
+__device__ __forceinline__ R fbar_trial_j(const StepArgs<R> &a, const Particles<R> &P, int64_t p, Axis<R, OX> &ax,
+                                          Axis<R, OY> &ay, Axis<R, OZ> &az, int &cx, int &cy, int &cz) {
+    const size_t N = (size_t)a.g.nodec;
+    const R x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+    bool oob = false;
+    cx = cell_of(x0, a.g, 0, oob);
+    cy = cell_of(x1, a.g, 1, oob);
+    cz = cell_of(x2, a.g, 2, oob);
+    axis_eval<R, OX>(x0, a.g, 0, cx, ax);
+    axis_eval<R, OY>(x1, a.g, 1, cy, ay);
+    axis_eval<R, OZ>(x2, a.g, 2, cz, az);
+    R D[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+    for (int k = 0; k <= OZ; k++)
+#pragma unroll
+        for (int j = 0; j <= OY; j++)
+#pragma unroll
+            for (int i = 0; i <= OX; i++) {
+                const R wxy = ax.w[i] * ay.w[j];
+                const R dn[3] = {ax.dw[i] * ay.w[j] * az.w[k], ax.w[i] * ay.dw[j] * az.w[k], wxy * az.dw[k]};
+                const size_t gn = node_id(a.g, cx + i, cy + j, cz + k);
+                const R nv[3] = {ld(a.nvel2 + gn), ld(a.nvel2 + N + gn), ld(a.nvel2 + 2 * N + gn)};
+#pragma unroll
+                for (int r = 0; r < 3; r++)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) D[r][c] += dn[c] * nv[r] * a.dt;
+            }
+    if constexpr (sizeof(R) == 8) {
+#pragma unroll
+        for (int r = 0; r < 3; r++) D[r][r] += (R)1;
+        return ld(P.Jb + p) * det3(D);
+    } else {
+        // FP32 carries J - 1: (1 + jb)(1 + dm) - 1 without the rounding of numbers near 1
+        const R jb = ld(P.Jb + p), dm = (R)det_ipm1((const float(*)[3])D);
+        return jb + dm + jb * dm;
+    }
+}
+
+template <typename R, int OX, int OY, int OZ>
+__global__ void __launch_bounds__(256) k_fbar_trial(StepArgs<R> a) {
+    __shared__ float sh_f[32];
+    const Particles<R> &P = a.P;
+    float jvmax = 0.0f;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.num; p += (int64_t)gridDim.x * blockDim.x) {
+        Axis<R, OX> ax;
+        Axis<R, OY> ay;
+        Axis<R, OZ> az;
+        int cx, cy, cz;
+        const R jt = fbar_trial_j<R, OX, OY, OZ>(a, P, p, ax, ay, az, cx, cy, cz);
+        P.Jt[p] = jt;
+        jvmax = fmaxf(jvmax, (float)fabs(jt * ld(P.vol + p)));
+    }
+    const float m = block_reduce(jvmax, OpMaxF(), sh_f);
+    if (threadIdx.x == 0 && m > 0.0f) atomic_max_pos(&a.ctl->cur[C_JVMAX], m * 1.000001f);
+}
+
+template <typename R>
+__global__ void k_fbar_scale(StepArgs<R> a) {
+    a.ctl->sc_fbar = make_fix(a.nump * (double)bits_f(a.ctl->cur[C_JVMAX]) * 1.0000001);
+}
+
+template <typename R, int OX, int OY, int OZ>
+__global__ void __launch_bounds__(256) k_fbar_scatter(StepArgs<R> a) {
+    __shared__ Fix F;
+    if (threadIdx.x == 0) F = a.ctl->sc_fbar;
+    __syncthreads();
+    const Particles<R> &P = a.P;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.num; p += (int64_t)gridDim.x * blockDim.x) {
+        const R x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+        bool oob = false;
+        const int cx = cell_of(x0, a.g, 0, oob), cy = cell_of(x1, a.g, 1, oob), cz = cell_of(x2, a.g, 2, oob);
+        Axis<R, OX> ax;
+        Axis<R, OY> ay;
+        Axis<R, OZ> az;
+        axis_eval<R, OX>(x0, a.g, 0, cx, ax);
+        axis_eval<R, OY>(x1, a.g, 1, cy, ay);
+        axis_eval<R, OZ>(x2, a.g, 2, cz, az);
+        const R jv = ld(P.Jt + p) * ld(P.vol + p);
+#pragma unroll
+        for (int k = 0; k <= OZ; k++)
+#pragma unroll
+            for (int j = 0; j <= OY; j++)
+#pragma unroll
+                for (int i = 0; i <= OX; i++) {
+                    const long long q = fx(ax.w[i] * ay.w[j] * az.w[k] * jv, F);
+                    if (q) atomic_add_i64(&a.facc[node_id(a.g, cx + i, cy + j, cz + k)], q);
+                }
+    }
+}
+
+template <typename R, bool LIST>
+__global__ void __launch_bounds__(256) k_fbar_grid(StepArgs<R> a) {
+    __shared__ Scales S;
+    __shared__ Fix F;
+    load_scales(a, S);
+    if (threadIdx.x == 0) F = a.ctl->sc_fbar;
+    __syncthreads();
+    const size_t N = (size_t)a.g.nodec;
+    const int ntl = LIST ? *a.ntlist : 1;
+    for (int lt = LIST ? (int)blockIdx.x : 0; lt < ntl; lt += LIST ? (int)gridDim.x : 1) {
+        const int t = LIST ? a.tlist[lt] : (int)blockIdx.x;
+        int tx, ty, tz;
+        tile_coords(t, a.g.ntile, tx, ty, tz);
+        for (int li = threadIdx.x; li < TILE * TILE * TILE; li += blockDim.x) {
+            const int gx = tx * TILE + (li % TILE), gy = ty * TILE + (li / TILE) % TILE,
+                      gz = tz * TILE + li / (TILE * TILE);
+            if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
+            const size_t n = node_id(a.g, gx, gy, gz);
+            const R nvof = unfx((long long)a.acc[N + n], S.v, (R)0);
+            const R nj = unfx((long long)a.facc[n], F, (R)0);
+            a.G[n] = (nvof > a.mtol) ? nj / nvof : (sizeof(R) == 8 ? (R)0 : (R)-1);
+            a.facc[n] = 0ull;
+            if (!a.all_tiles) a.acc[N + n] = 0ull;
+        }
     }
 }
 
@@ -2019,7 +2157,7 @@ __global__ void __launch_bounds__(1024) k_tile_list(const unsigned char *flag, i
 
 // ----------------------------------------------- G2P 2: F, x, vol, stress
 // One thread per particle (coalesced particle I/O; node gathers hit L1/L2).
-template <typename R, int OX, int OY, int OZ>
+template <typename R, int OX, int OY, int OZ, bool FBAR = false>
 __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
     __shared__ float sh_f[32];
     __shared__ int sh_i[32];
@@ -2043,6 +2181,7 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
         R xn[3] = {x[0], x[1], x[2]};
         R du[3] = {(R)0, (R)0, (R)0};
         R gu[3] = {(R)0, (R)0, (R)0};
+        R jbg = (R)0;   // F-bar: Jbar gathered from the projected nodal J
         constexpr bool FP64 = sizeof(R) == 8;
 #pragma unroll
         for (int k = 0; k <= OZ; k++)
@@ -2073,6 +2212,7 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
 #pragma unroll
                         for (int c = 0; c < 3; c++) gu[c] += dn[c] * e;
                     }
+                    if constexpr (FBAR) jbg += N_ * ld(a.G + gn);
                 }
         if (!FP64) {
             // FP32: one rounding of the position per step
@@ -2125,6 +2265,65 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
                 }
             J = (R)1 + (R)det_ipm1((const float(*)[3])Fn);
         }
+        // the F the stress models see (def_grad_bar under F-bar) and the J in
+        // the logarithm of the Neo-Hookean volumetric term (det_def_grad_bar)
+        R Fs[3][3];
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) Fs[r][c] = Fn[r][c];
+        R jl = J;
+        if constexpr (FBAR) {
+            const R jt = ld(P.Jt + p);
+            R Fb[3][3];
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) Fb[r][c] = ld(P.Fb[3 * r + c] + p);
+            if constexpr (FP64) {
+                const R sc = cbrt(jbg / jt);
+                R dd[3][3];
+#pragma unroll
+                for (int r = 0; r < 3; r++)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) dd[r][c] = (D[r][c] + (r == c ? (R)1 : (R)0)) * sc;
+#pragma unroll
+                for (int r = 0; r < 3; r++)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        R acc = (R)0;
+#pragma unroll
+                        for (int k2 = 0; k2 < 3; k2++) acc += dd[r][k2] * Fb[k2][c];
+                        Fs[r][c] = acc;
+                        Dm[r][c] = (r == c) ? dd[r][c] - (R)1 : dd[r][c];
+                    }
+            } else {
+                // FP32 (jbg, jt are J - 1): sc - 1 from log1p / expm1, H-form update of def_grad_bar
+                const R sm1 = expm1f(log1pf((jbg - jt) / (1.0f + jt)) * (1.0f / 3.0f));
+                const R sc = (R)1 + sm1;
+                R Db[3][3];
+#pragma unroll
+                for (int r = 0; r < 3; r++)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) Db[r][c] = sc * D[r][c] + (r == c ? sm1 : (R)0);
+#pragma unroll
+                for (int r = 0; r < 3; r++)
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        R acc = Fb[r][c] + Db[r][c];
+#pragma unroll
+                        for (int k2 = 0; k2 < 3; k2++) acc += Db[r][k2] * Fb[k2][c];
+                        Fs[r][c] = acc;
+                        Dm[r][c] = Db[r][c];
+                    }
+            }
+            jl = jbg;
+#pragma unroll
+            for (int r = 0; r < 3; r++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) P.Fb[3 * r + c][p] = Fs[r][c];
+            P.Jb[p] = jbg;
+        }
         const R volp = J * ld(P.vol0 + p);
         R s[6];
 #pragma unroll
@@ -2135,14 +2334,19 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
         if (model == 0) {
             lin_elast_update(s, Dm, E, nu);
         } else if (model == 1) {
-            if constexpr (sizeof(R) == 8) neo_hookean_stress(s, Fn, J, E, nu);
-            else neo_hookean_stress_h(s, Fn, det_ipm1(Fn), E, nu);
+            if constexpr (FBAR) {
+                if constexpr (sizeof(R) == 8) neo_hookean_stress_bar(s, Fs, J, jl, E, nu);
+                else neo_hookean_stress_h_bar(s, Fs, det_ipm1(Fn), jl, E, nu);   // jl = Jbar - 1
+            } else {
+                if constexpr (sizeof(R) == 8) neo_hookean_stress(s, Fn, J, E, nu);
+                else neo_hookean_stress_h(s, Fn, det_ipm1(Fn), E, nu);
+            }
         } else if (model == 2) {
-            if constexpr (sizeof(R) == 8) stvk_stress(s, Fn, J, E, nu);
-            else stvk_stress_h(s, Fn, det_ipm1(Fn), E, nu);
+            if constexpr (sizeof(R) == 8) stvk_stress(s, Fs, J, E, nu);
+            else stvk_stress_h(s, Fs, det_ipm1(Fn), E, nu);
         } else if (model == 3) {   // mat_prop = {c1, c2, bulk}
-            if constexpr (sizeof(R) == 8) mooney_rivlin_stress(s, Fn, J, E, nu, (R)a.matprop[3 * mid + 2]);
-            else mooney_rivlin_stress_h(s, Fn, det_ipm1(Fn), E, nu, (R)a.matprop[3 * mid + 2]);
+            if constexpr (sizeof(R) == 8) mooney_rivlin_stress(s, Fs, J, E, nu, (R)a.matprop[3 * mid + 2]);
+            else mooney_rivlin_stress_h(s, Fs, det_ipm1(Fn), E, nu, (R)a.matprop[3 * mid + 2]);
         } else if (model == 4) {
             R jm1;
             if constexpr (sizeof(R) == 8) jm1 = J - (R)1;
@@ -2495,6 +2699,11 @@ static StepArgs<R> make_args(mpm_ctx *c) {
     a.P.vol = f + 23 * n;
     for (int k = 0; k < 3; k++) a.P.a[k] = c->nreal == 27 ? f + (24 + k) * n : nullptr;
     for (int k = 0; k < 9; k++) a.P.C[k] = c->affine ? f + (24 + k) * n : nullptr;
+    for (int k = 0; k < 9; k++) a.P.Fb[k] = c->fbar ? f + (c->off_fbar + k) * n : nullptr;
+    a.P.Jb = c->fbar ? f + (c->off_fbar + 9) * n : nullptr;
+    a.P.Jt = c->fbar ? f + (c->off_fbar + 10) * n : nullptr;
+    a.facc = c->d_facc;
+    a.fbar = c->fbar ? 1 : 0;
     a.P.matid = (int *)(base + (size_t)c->nreal * n * rs);
     a.P.pid = a.P.matid + n;
     a.work = c->d_work;
@@ -2682,6 +2891,21 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
         timer_end(c, K_G2P_MUSL);
     } else {
         timer_begin(c, K_G2P_UPDATE);
+        if (c->fbar) {
+            const int nb = (int)((c->num + 255) / 256);
+            const int pg = (int)std::min<int64_t>(nb, 8 * num_sms());
+            k_fbar_trial<R, OX, OY, OZ><<<pg, 256, 0, c->stream>>>(a);
+            k_fbar_scale<R><<<1, 1, 0, c->stream>>>(a);
+            k_fbar_scatter<R, OX, OY, OZ><<<pg, 256, 0, c->stream>>>(a);
+            if (!a.all_tiles)
+                k_fbar_grid<R, true><<<std::min(c->g.ntiles, 6 * num_sms()), 256, 0, c->stream>>>(a);
+            else
+                k_fbar_grid<R, false><<<c->g.ntiles, 256, 0, c->stream>>>(a);
+            k_g2p_update<R, OX, OY, OZ, true><<<nb, 256, 0, c->stream>>>(a);
+            c->launches += 5;
+            timer_end(c, K_G2P_UPDATE);
+            return check_launch(c);
+        }
         bool staged = false;
         if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
             if (c->tma_update && c->tune.update_ctas_per_sm == 0) {

@@ -55,7 +55,7 @@ struct Geom {
 // Bounds that set the fixed-point scales.  Values are non-negative floats
 // stored as their bit patterns so that atomicMax on unsigned int orders them.
 enum BoundSlot { B_VMAX = 0, B_VOLMAX, B_VOLSMAX, B_AMAX, B_NB };   // produced for the next step
-enum CurSlot { C_GMAX = 0, C_NEIMAX, C_NC };                    // produced and used within a step
+enum CurSlot { C_GMAX = 0, C_NEIMAX, C_JVMAX, C_NC };                    // produced and used within a step
 
 // Fixed-point scale 2^e, applied as two float factors so that e up to +-250
 // never overflows an intermediate.
@@ -89,6 +89,7 @@ struct DevCtl {
     unsigned int n_miss_musl;        // particles queued for the deferred gather/MUSL pass this step
     Scales sc_p2g;                   // this step's P2G scales (k_step_reset)
     Scales sc_musl;                  // this step's gather/MUSL scales (last CTA of k_grid1)
+    Fix sc_fbar;                     // F-bar: scale of the projected J vol sums (k_fbar_scale)
 };
 
 template <typename R>
@@ -96,6 +97,7 @@ struct Particles {
     R *x[3], *v[3], *F[9], *s[6], *m, *vol0, *vol;
     R *a[3];          // particle acceleration (implicit contexts only, else null)
     R *C[9];          // affine velocity matrix, row major (TPIC / APIC contexts only, else null)
+    R *Fb[9], *Jb, *Jt;   // F-bar contexts: def_grad_bar, det_def_grad_bar, trial J of the step (FP32: all minus I / 1)
     int *matid, *pid;
 };
 
@@ -155,6 +157,8 @@ struct mpm_ctx {
     int nreal = 24;                        // real fields per particle: 24, 27 with acceleration (implicit),
                                            // 33 with the affine matrix (TPIC / APIC)
     bool affine = false;                   // TPIC or APIC: fields [24, 33) hold the affine matrix
+    bool fbar = false;                     // F-bar: 11 fields from off_fbar (Fbar 9, Jbar, trial J)
+    int off_fbar = 0;
     size_t pstride = 64;                   // elements between particle field arrays: num rounded up to 64
     void *pbuf[2] = {nullptr, nullptr};   // two SoA copies
     int cur = 0;
@@ -162,6 +166,7 @@ struct mpm_ctx {
     // grid
     unsigned long long *d_acc = nullptr;   // NACC * nodec int64 P2G sums
     unsigned long long *d_acc2 = nullptr;  // 3 * nodec int64 MUSL momentum
+    unsigned long long *d_facc = nullptr;  // nodec int64 F-bar sums of N J vol (F-bar contexts)
     void *d_nodal = nullptr;               // R: gather field G (3), nei (1), nvel2 (3), nvel (3), naccel (3)
     double *d_nvol = nullptr;              // nodal reference volume (FP64)
     unsigned char *d_bcflag = nullptr;     // bit c: component c constrained

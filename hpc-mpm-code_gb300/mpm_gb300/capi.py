@@ -44,7 +44,7 @@ class MaterialDesc(C.Structure):
 class Config(C.Structure):
     _fields_ = [("dt", C.c_double), ("mtol", C.c_double), ("gravity", C.c_double * 3), ("scheme", C.c_int),
                 ("precision", C.c_int), ("shifting", C.c_int), ("resort_period", C.c_int), ("scatter", C.c_int),
-                ("implicit", C.c_int), ("reserved", C.c_int * 6)]
+                ("implicit", C.c_int), ("fbar", C.c_int), ("reserved", C.c_int * 5)]
 
 
 class SolveStats(C.Structure):
@@ -65,7 +65,7 @@ _ip = C.POINTER(C.c_int)
 EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_status_string",
            "mpm_gpu_load_particles", "mpm_gpu_set_bc", "mpm_gpu_p2g", "mpm_gpu_grid_update", "mpm_gpu_g2p",
            "mpm_gpu_step_explicit", "mpm_gpu_download_nodal", "mpm_gpu_download_particles",
-           "mpm_gpu_download_affine", "mpm_gpu_upload_affine",
+           "mpm_gpu_download_affine", "mpm_gpu_upload_affine", "mpm_gpu_download_fbar",
            "mpm_gpu_upload_particles", "mpm_gpu_steps_host", "mpm_gpu_sync",
            "mpm_gpu_get_stats", "mpm_gpu_enable_kernel_timing", "mpm_gpu_kernel_times", "mpm_gpu_implicit_setup",
            "mpm_gpu_implicit_step", "mpm_gpu_implicit_assemble", "mpm_gpu_implicit_get_system",
@@ -102,6 +102,7 @@ def load(path: str | None = None):
     lib.mpm_gpu_download_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
     lib.mpm_gpu_download_affine.argtypes = [C.c_void_p, _dp]
     lib.mpm_gpu_upload_affine.argtypes = [C.c_void_p, _dp]
+    lib.mpm_gpu_download_fbar.argtypes = [C.c_void_p, _dp, _dp]
     lib.mpm_gpu_upload_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
     lib.mpm_gpu_steps_host.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, _dp, _dp, _dp, _dp]
     lib.mpm_gpu_sync.argtypes = [C.c_void_p]
@@ -164,7 +165,8 @@ NODAL = {"nmass": (0, 1), "nvof": (1, 1), "nmome": (2, 3), "nforce": (3, 3), "nv
 class GpuSolid:
     """One explicit solid on the GPU, built from a scene (mpm_gb300.scenes.Scene)."""
 
-    def __init__(self, scene, precision=32, shifting=True, resort_period=0, scatter=0, stream=None, implicit=False):
+    def __init__(self, scene, precision=32, shifting=True, resort_period=0, scatter=0, stream=None, implicit=False,
+                 fbar=False):
         self.lib = lib = load()
         self.scene = s = scene
         g = GridDesc((C.c_int * 3)(*s.xyelem), (C.c_double * 3)(*s.xymin), (C.c_double * 3)(*s.dxy),
@@ -173,7 +175,7 @@ class GpuSolid:
         self._mat = np.ascontiguousarray(s.mat_prop, dtype=np.float64).ravel()
         m = MaterialDesc(len(self._iprop), self._iprop.ctypes.data_as(_ip), self._mat.ctypes.data_as(_dp))
         cfg = Config(s.dt, s.mtol, (C.c_double * 3)(*s.gravity), s.scheme, precision, int(shifting),
-                     int(resort_period), int(scatter), int(implicit), (C.c_int * 6)())
+                     int(resort_period), int(scatter), int(implicit), int(fbar), (C.c_int * 5)())
         h = C.c_void_p()
         _chk(lib.mpm_gpu_create(C.byref(g), C.byref(m), C.byref(cfg), C.byref(h)), "mpm_gpu_create")
         self.ctx = h
@@ -253,6 +255,12 @@ class GpuSolid:
         out = np.zeros(self.num * 9)
         _chk(self.lib.mpm_gpu_download_affine(self.ctx, _ptr(out)), "mpm_gpu_download_affine")
         return out.reshape(self.num, 3, 3)
+
+    def fbar(self):
+        """F-bar contexts: def_grad_bar (n, 3, 3) and det_def_grad_bar (n,), load order."""
+        F, J = np.zeros(self.num * 9), np.zeros(self.num)
+        _chk(self.lib.mpm_gpu_download_fbar(self.ctx, _ptr(F), _ptr(J)), "mpm_gpu_download_fbar")
+        return F.reshape(self.num, 3, 3), J
 
     def upload_affine(self, affine):
         """TPIC / APIC: overwrite the affine matrices ((n, 3, 3) float64, load order)."""

@@ -89,7 +89,9 @@ typedef struct {
     int resort_period;  /* physical re-sort of particles by brick every N steps (>= 1); 0 = default (8) */
     int scatter;        /* 0: per-cell register scatter for FP32 linear grids (default); 1: staging-box atomics */
     int implicit;       /* 1: implicit solid context (particles carry acceleration; mpm_gpu_implicit_*) */
-    int reserved[6];
+    int fbar;           /* 1: F-bar projection (Fbar_flag, module/solid/explicit/fbar_projection.cpp:18-93);
+                           explicit contexts only */
+    int reserved[5];
 } mpm_config;
 
 /* ---- lifetime ------------------------------------------------------------
@@ -147,6 +149,10 @@ mpm_status mpm_gpu_download_particles(mpm_ctx *ctx, double *coord, double *vel, 
  * vel_Bmat . inv_Dmat, module/map_and_interpolate.h:59,105); zeros for PIC
  * and FLIP.  Synchronises the stream. */
 mpm_status mpm_gpu_download_affine(mpm_ctx *ctx, double *affine);
+/* F-bar contexts: def_grad_bar (9 row-major values per particle) and
+ * det_def_grad_bar in load order (module/material_point.h:116,121); either
+ * pointer may be NULL.  Synchronises the stream. */
+mpm_status mpm_gpu_download_fbar(mpm_ctx *ctx, double *Fbar, double *Jbar);
 /* Overwrites the affine matrices of a TPIC / APIC context (same layout; a
  * restart, SolidMaterialPointBase::RestartInput, module/solid/solid_data_io.cpp:61-96)
  * and raises the next P2G's fixed-point bound to cover them. */

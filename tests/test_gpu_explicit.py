@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 EXPLICIT = ["explicit_pic", "explicit_flip", "explicit_quadratic", "explicit_neohookean", "explicit_stvk",
             "explicit_mooney_rivlin", "explicit_tpic", "explicit_apic", "explicit_tpic_quadratic",
-            "explicit_apic_quadratic"]
+            "explicit_apic_quadratic", "explicit_fbar_linear", "explicit_fbar_neohookean"]
 P2G_FIELDS = ("nmass", "nvof", "nmome", "nforce", "nvel", "naccel", "nvol")
 PARTICLE_FIELDS = ("x", "v", "F", "sigma", "vol")
 
@@ -29,7 +29,7 @@ def particle_err(p, ref, prefix=""):
 @pytest.mark.parametrize("name", EXPLICIT)
 def test_p2g_fp64_matches_reference(name):
     g = load_golden(name)
-    gpu = capi.GpuSolid(scene_from_golden(g), precision=64)
+    gpu = capi.GpuSolid(scene_from_golden(g), precision=64, fbar="fbar" in g)
     gpu.p2g(float(g["facl"]))
     gpu.grid_update()
     for f in P2G_FIELDS:
@@ -40,15 +40,22 @@ def test_p2g_fp64_matches_reference(name):
 @pytest.mark.parametrize("name", EXPLICIT)
 def test_steps_fp64_match_reference(name):
     g = load_golden(name)
-    gpu = capi.GpuSolid(scene_from_golden(g), precision=64)
+    fbar = "fbar" in g
+    gpu = capi.GpuSolid(scene_from_golden(g), precision=64, fbar=fbar)
     gpu.steps(1, float(g["facl"]))
     e1 = particle_err(gpu.particles(), g, "step1_")
     if "step1_affine" in g:   # TPIC vel_grad / APIC vel_Bmat . inv_Dmat
         e1["affine"] = rel_l2(gpu.affine(), g["step1_affine"])
+    if fbar:                  # def_grad_bar, det_def_grad_bar
+        Fb, Jb = gpu.fbar()
+        e1["Fbar"], e1["Jbar"] = rel_l2(Fb, g["step1_Fbar"]), rel_l2(Jb, g["step1_Jbar"])
     gpu.steps(int(g["nsteps"]) - 1, float(g["facl"]))
     eN = particle_err(gpu.particles(), g, "stepN_")
     if "stepN_affine" in g:
         eN["affine"] = rel_l2(gpu.affine(), g["stepN_affine"])
+    if fbar:
+        Fb, Jb = gpu.fbar()
+        eN["Fbar"], eN["Jbar"] = rel_l2(Fb, g["stepN_Fbar"]), rel_l2(Jb, g["stepN_Jbar"])
     gpu.sync()
     assert max(e1.values()) <= 1e-10, e1
     assert max(eN.values()) <= 1e-10, eN
@@ -57,7 +64,7 @@ def test_steps_fp64_match_reference(name):
 @pytest.mark.parametrize("name", EXPLICIT)
 def test_steps_fp32_within_tolerance(name):
     g = load_golden(name)
-    gpu = capi.GpuSolid(scene_from_golden(g), precision=32)
+    gpu = capi.GpuSolid(scene_from_golden(g), precision=32, fbar="fbar" in g)
     gpu.p2g(float(g["facl"]))
     gpu.grid_update()
     for f in ("nmass", "nvof", "nmome", "nforce"):
@@ -67,6 +74,10 @@ def test_steps_fp32_within_tolerance(name):
     e = particle_err(gpu.particles(), g, "stepN_")
     if "stepN_affine" in g:
         e["affine"] = rel_l2(gpu.affine(), g["stepN_affine"])
+    if "fbar" in g:
+        Fb, Jb = gpu.fbar()
+        e["Fbar"], e["Jbar"] = rel_l2(Fb, g["stepN_Fbar"]), rel_l2(Jb, g["stepN_Jbar"])
+        assert e["Fbar"] <= 1e-5 and e["Jbar"] <= 1e-6, e   # Jbar: relative to J (near 1)
     gpu.sync()
     assert e["x"] <= 1e-6 and e["v"] <= 1e-4 and e["F"] <= 1e-5 and e["vol"] <= 1e-5, e
     assert e["sigma"] <= 1e-3 and e.get("affine", 0.0) <= 1e-3, e
@@ -316,3 +327,30 @@ def test_affine_full_size_keeps_angular_momentum(precision):
         assert abs(out[scheme][1] / out[scheme][0] - 1.0) <= 1e-3, (scheme, out[scheme][1] / out[scheme][0])
     d = rel_l2(out[scenes.APIC][2], out[scenes.TPIC][2])
     assert d <= (1e-9 if precision == 64 else 1e-3), d
+
+
+# ---------------------------------------------------------------- F-bar
+@pytest.mark.parametrize("precision", [64, 32])
+def test_fbar_block_matches_oracle(precision):
+    """F-bar projection (fbar_projection.cpp) on a 13,824-particle
+    Neo-Hookean block with a spinning, randomly perturbed velocity, 40 steps,
+    against the oracle: FP64 1e-10 (def_grad_bar and det_def_grad_bar
+    included); FP32 1e-6 on x, 1e-4 on v, 1e-3 on the stress, 1e-5 on Fbar."""
+    import kat_spin as ks
+
+    s = ks.block(scenes.PIC)
+    s.iprop[:] = 1
+    s.vel[:] += np.random.default_rng(5).normal(0.0, 0.2, size=s.vel.shape)
+    o = port.PortSolid(s, fbar=True)
+    o.steps(40)
+    gpu = capi.GpuSolid(s, precision=precision, fbar=True)
+    gpu.steps(40)
+    p, q = gpu.particles(), o.particles()
+    (Fb, Jb), (Fo, Jo) = gpu.fbar(), o.fbar()
+    gpu.sync()
+    e = {k: rel_l2(p[k], q[k]) for k in PARTICLE_FIELDS}
+    e["Fbar"], e["Jbar"] = rel_l2(Fb, Fo), rel_l2(Jb, Jo)
+    if precision == 64:
+        assert max(e.values()) <= 1e-10, e
+    else:
+        assert e["x"] <= 1e-6 and e["v"] <= 1e-4 and e["sigma"] <= 1e-3 and e["Fbar"] <= 1e-5, e
