@@ -59,6 +59,8 @@ def parse():
                     help="steps of the 12.6M-particle Tait dam break (0 skips)")
     ap.add_argument("--apic-steps", type=int, default=100,
                     help="steps of the headline workload with APIC transfers (0 skips)")
+    ap.add_argument("--fbar-steps", type=int, default=100,
+                    help="steps of the headline workload with the F-bar projection (0 skips)")
     ap.add_argument("--train-pairs", type=int, default=2000,
                     help="training pairs when no committed preconditioner parameters exist")
     ap.add_argument("--implicit-steps", type=int, default=50,
@@ -449,6 +451,28 @@ def run_apic(args, torch, stream, hbm_peak):
                          "note": "N_p*(176 + 72) + N_n*56: the solid formula plus the affine matrix"}}
 
 
+def run_fbar(args, torch, stream, hbm_peak):
+    """The headline spinning block with the F-bar projection on (Fbar_flag):
+    per step a trial-J pass, the nodal projection of J vol, and the generic
+    particle update with the J-bar gather.  FP32."""
+    from mpm_gb300 import capi
+
+    s = workload(args.cells)
+    gpu = capi.GpuSolid(s, precision=32, stream=stream.cuda_stream, fbar=True)
+    gpu.steps(args.warmup)
+    gpu.sync()
+    ms = timed_steps(torch, stream, gpu, args.fbar_steps)
+    gpu.sync()
+    gpu.close()
+    ms_step = ms / args.fbar_steps
+    alg = algorithmic_bytes(s.num, s.nodec) + s.num * 40   # + def_grad_bar and J-bar read and written (10 + 10 words)
+    return {"metric": METRIC, "value": s.num * args.fbar_steps / (ms * 1e-3), "unit": METRIC,
+            "ms_per_step": ms_step, "steps": args.fbar_steps, "particles": s.num, "fbar": True, "dtype": "f32",
+            "roofline": {"bound": "hbm", "achieved": alg / (ms_step * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": alg / (ms_step * 1e-3) / 1e9 / hbm_peak, "algorithmic_bytes_per_step": alg,
+                         "note": "N_p*(176 + 40) + N_n*56: the solid formula plus def_grad_bar and J-bar"}}
+
+
 def run_gb300(args):
     import torch
 
@@ -546,7 +570,12 @@ def run_gb300(args):
         except Exception as exc:   # reported, never required
             implicit = {"metric": "implicit step time", "value": None, "error": str(exc)}
 
-    batched = fluid = apic = None
+    batched = fluid = apic = fbar = None
+    if args.fbar_steps > 0:
+        try:
+            fbar = run_fbar(args, torch, stream, hbm_peak)
+        except Exception as exc:
+            fbar = {"metric": METRIC, "value": None, "error": str(exc)}
     if args.apic_steps > 0:
         try:
             apic = run_apic(args, torch, stream, hbm_peak)
@@ -580,7 +609,7 @@ def run_gb300(args):
                            "l2": "inputs larger than L2: 393 MB particle state per step, no flush"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(),
                 "gpu_launches": int(launches), "kernels": kernels, "implicit": implicit,
-                "batched": batched, "fluid": fluid, "apic": apic}
+                "batched": batched, "fluid": fluid, "apic": apic, "fbar": fbar}
         print(json.dumps(line), flush=True)
     gpu.close()
     if world > 1:
