@@ -2,7 +2,7 @@
 restatement oracle/mpm_oracle.c (built to oracle/lib/libmpmoracle.so).
 
 Only tests/, __graft_entry__.smoke() and the cpu_baseline leg of bench.py may
-use it, and only as the checker / the timed CPU baseline.
+use it, and only as the reference results are compared with / the timed CPU baseline.
 """
 from __future__ import annotations
 
