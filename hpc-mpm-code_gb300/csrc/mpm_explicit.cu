@@ -2106,6 +2106,70 @@ __global__ void __launch_bounds__(256) k_fbar_scatter(StepArgs<R> a) {
     }
 }
 
+// FP32 linear grids: the same projection as per-cell register sums (two
+// threads per cell, thread h owns the four corners of z-layer h) and one
+// fixed-point RED per node; a particle that left its sorted cell adds its own
+// atomics.
+__global__ void __launch_bounds__(CELL_THREADS, 3) k_fbar_scatter_cell(StepArgs<float> a) {
+    __shared__ float corner[8][BRC];
+    __shared__ Fix F;
+    const int b = blockIdx.x;
+    const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
+    const int *cs = a.cstart + (size_t)b * (BRC + 1);
+    if (cs[0] == cs[BRC]) return;   // empty brick (uniform across the CTA)
+    if (threadIdx.x == 0) F = a.ctl->sc_fbar;
+    int ox, oy, oz;
+    brick_origin(b, a.nbrick, ox, oy, oz);
+    const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
+    __syncthreads();
+    const Particles<float> &P = a.P;
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int p = cs[lc]; p < cs[lc + 1]; p++) {
+        const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
+        bool oob = false;
+        const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
+        Axis<float, 1> ax, ay, az;
+        axis_eval<float, 1>(x0, a.g, 0, px, ax);
+        axis_eval<float, 1>(x1, a.g, 1, py, ay);
+        axis_eval<float, 1>(x2, a.g, 2, pz, az);
+        const float jv = ld(P.Jt + p) * ld(P.vol + p) * (h ? az.w[1] : az.w[0]);
+        const bool mine = (px == cx) && (py == cy) && (pz == cz);
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const float q = ax.w[i] * ay.w[j] * jv;
+                if (mine) {
+                    acc[i + 2 * j] += q;
+                } else {
+                    const long long v = fx(q, F);
+                    if (v) atomic_add_i64(&a.facc[node_id(a.g, px + i, py + j, pz + h)], v);
+                }
+            }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) corner[c + 4 * h][lc] = acc[c];
+    __syncthreads();
+    constexpr int NX = BRX + 1, NY = BRY + 1, NZ = BRZ + 1, NB = NX * NY * NZ;
+    for (int n = threadIdx.x; n < NB; n += CELL_THREADS) {
+        const int nx = n % NX, ny = (n / NX) % NY, nz = n / (NX * NY);
+        const int gx = ox + nx, gy = oy + ny, gz = oz + nz;
+        if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
+        float sum = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+#pragma unroll
+            for (int j = 0; j < 2; j++)
+#pragma unroll
+                for (int i = 0; i < 2; i++) {
+                    const int ex = nx - i, ey = ny - j, ez = nz - k;
+                    if (ex >= 0 && ex < BRX && ey >= 0 && ey < BRY && ez >= 0 && ez < BRZ)
+                        sum += corner[i + 2 * (j + 2 * k)][ex + BRX * (ey + BRY * ez)];
+                }
+        if (sum != 0.0f) atomic_add_i64(&a.facc[node_id(a.g, gx, gy, gz)], fx(sum, F));
+    }
+}
+
 template <typename R, bool LIST>
 __global__ void __launch_bounds__(256) k_fbar_grid(StepArgs<R> a) {
     __shared__ Scales S;
@@ -2896,7 +2960,14 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
             const int pg = (int)std::min<int64_t>(nb, 8 * num_sms());
             k_fbar_trial<R, OX, OY, OZ><<<pg, 256, 0, c->stream>>>(a);
             k_fbar_scale<R><<<1, 1, 0, c->stream>>>(a);
-            k_fbar_scatter<R, OX, OY, OZ><<<pg, 256, 0, c->stream>>>(a);
+            bool cell = false;
+            if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
+                if (c->cell_scatter) {
+                    k_fbar_scatter_cell<<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
+                    cell = true;
+                }
+            }
+            if (!cell) k_fbar_scatter<R, OX, OY, OZ><<<pg, 256, 0, c->stream>>>(a);
             if (!a.all_tiles)
                 k_fbar_grid<R, true><<<std::min(c->g.ntiles, 6 * num_sms()), 256, 0, c->stream>>>(a);
             else

@@ -7,6 +7,7 @@
     python -m mpm_gb300.cases batched  [--steps 20]      # 256 packed scenes
     python -m mpm_gb300.cases fluid    [--steps 20]      # 12.6M-particle Tait dam break
     python -m mpm_gb300.cases apic     [--cells 64] [--steps 20]   # the explicit block with APIC transfers
+    python -m mpm_gb300.cases fbar     [--cells 64] [--steps 20]   # the explicit block with the F-bar projection
 
 Each case builds its scene, runs a few warm-up steps, then the requested
 steps on a non-default stream, and exits 0.  Nothing is timed here: the
@@ -30,12 +31,12 @@ def _stream():
 
 def run(case, steps, cells, reps):
     st = _stream()
-    if case in ("explicit", "apic"):
+    if case in ("explicit", "apic", "fbar"):
         s = scenes.spinning_block(cells=(cells, cells, cells),
                                   grid=(cells + 48, cells + 48, cells + 48))
         if case == "apic":
             s.scheme = scenes.APIC
-        g = capi.GpuSolid(s, precision=32, stream=st.cuda_stream)
+        g = capi.GpuSolid(s, precision=32, stream=st.cuda_stream, fbar=(case == "fbar"))
         g.steps(3)
         g.steps(steps)
         g.sync()
