@@ -354,3 +354,23 @@ def test_fbar_block_matches_oracle(precision):
         assert max(e.values()) <= 1e-10, e
     else:
         assert e["x"] <= 1e-6 and e["v"] <= 1e-4 and e["sigma"] <= 1e-3 and e["Fbar"] <= 1e-5, e
+
+
+def test_fbar_with_apic_matches_oracle():
+    """F-bar and APIC together (the F-bar fields follow the affine ones in
+    the particle layout): FP64 against the oracle after 30 steps, 1e-10."""
+    import kat_spin as ks
+
+    s = ks.block(scenes.APIC)
+    s.iprop[:] = 1
+    o = port.PortSolid(s, fbar=True)
+    o.steps(30)
+    gpu = capi.GpuSolid(s, precision=64, fbar=True)
+    gpu.steps(30)
+    p, q = gpu.particles(), o.particles()
+    e = {k: rel_l2(p[k], q[k]) for k in PARTICLE_FIELDS}
+    e["affine"] = rel_l2(gpu.affine(), o.affine())
+    (Fb, Jb), (Fo, Jo) = gpu.fbar(), o.fbar()
+    e["Fbar"], e["Jbar"] = rel_l2(Fb, Fo), rel_l2(Jb, Jo)
+    gpu.sync()
+    assert max(e.values()) <= 1e-10, e
