@@ -98,10 +98,11 @@ def test_p_wave_speed(precision):
 def test_fp32_particles_on_node_planes(scatter):
     """Particles whose x coordinate sits exactly on an FP32 grid plane
     (x = float(0.01 * i)), where FP32 rounding can put a particle on the far
-    node of the cell it is binned in: the shape gradients take their sign
-    from the node, not from the sign of x - x_node, so the FP32 path stays
-    within its tolerances against the FP64 oracle after 5 steps (per-cell
-    and staging-box scatter)."""
+    node of the cell it is binned in, in a linear velocity field: the shape
+    gradients take their sign from the node, not from the sign of
+    x - x_node, so the FP32 path stays within 1e-4 (v) and 1e-3 (F - I,
+    stress) of the FP64 oracle after 5 steps (per-cell and staging-box
+    scatter)."""
     from oracle import port
 
     s = scenes.elastic_block(grid=(32, 32, 32), cell_lo=(8, 8, 8), cell_hi=(24, 24, 24), npc=2, jitter=0.05,
@@ -111,8 +112,12 @@ def test_fp32_particles_on_node_planes(scatter):
     idx = np.argmin(np.abs(s.coord[:, 0:1] - planes[None, :]), axis=1)
     near = np.abs(s.coord[:, 0] - planes[idx]) < 0.004
     s.coord[near, 0] = planes[idx[near]]
-    rng = np.random.default_rng(11)
-    s.vel[:] = rng.normal(0.0, 0.1, size=s.vel.shape)
+    # a linear velocity field: the one-sided gradients of the two cells that
+    # meet at a plane agree (a particle on a plane may be binned on either
+    # side, in FP32 and FP64 differently), while a gradient with the wrong
+    # sign would be about -2 v / dx, 16 times the field's gradient here
+    L = np.array([[0.5, 0.2, 0.0], [-0.1, -0.3, 0.1], [0.0, 0.2, 0.4]])
+    s.vel[:] = (s.coord - s.coord.mean(axis=0)) @ L.T
     o = port.PortSolid(s, shifting=False)
     o.steps(5)
     q = o.particles()
@@ -123,5 +128,6 @@ def test_fp32_particles_on_node_planes(scatter):
     gpu.close()
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
     H, Hq = p["F"] - np.eye(3)[None], q["F"] - np.eye(3)[None]
+    e = {"v": rel(p["v"], q["v"]), "H": rel(H, Hq), "sigma": rel(p["sigma"], q["sigma"])}
     assert int(near.sum()) > 1000
-    assert rel(p["v"], q["v"]) <= 1e-4 and rel(H, Hq) <= 1e-4 and rel(p["sigma"], q["sigma"]) <= 1e-3
+    assert e["v"] <= 1e-4 and e["H"] <= 1e-3 and e["sigma"] <= 1e-3, e
