@@ -162,18 +162,29 @@ __global__ void __launch_bounds__(BRC) k_cell_sort(const int *bstart, const int 
     }
 }
 
-// dst[j] = src[perm[j]] for all real fields and the two int fields.
+// dst[j] = src[perm[j]] for all real fields and the two int fields.  The
+// two buffers never overlap; eight fields are loaded before they are stored
+// so that a thread keeps eight gathers in flight.
 template <typename R>
-__global__ void k_permute(const R *src, R *dst, const int *perm, int n, int nreal, size_t N) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_permute(const R *__restrict__ src, R *__restrict__ dst, const int *__restrict__ perm, int n,
+                          int nreal, size_t N) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    int i = perm[j];
-#pragma unroll 4
-    for (int f = 0; f < nreal; f++) dst[f * N + j] = src[f * N + i];
-    const int *si = (const int *)(src + nreal * N);
-    int *di = (int *)(dst + nreal * N);
-    di[j] = si[i];
-    di[N + j] = si[N + i];
+    const size_t i = (size_t)perm[j];
+    int f = 0;
+    for (; f + 8 <= nreal; f += 8) {
+        R v[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = __ldg(src + (size_t)(f + k) * N + i);
+#pragma unroll
+        for (int k = 0; k < 8; k++) dst[(size_t)(f + k) * N + j] = v[k];
+    }
+    for (; f < nreal; f++) dst[(size_t)f * N + j] = __ldg(src + (size_t)f * N + i);
+    const int *si = (const int *)(src + (size_t)nreal * N);
+    int *di = (int *)(dst + (size_t)nreal * N);
+    const int a0 = __ldg(si + i), a1 = __ldg(si + N + i);
+    di[j] = a0;
+    di[N + j] = a1;
 }
 
 template <typename R>
