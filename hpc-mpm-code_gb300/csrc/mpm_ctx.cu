@@ -616,7 +616,8 @@ namespace mpm {
 constexpr int ST_X = 0, ST_V = 3, ST_F = 6, ST_S = 15, ST_VOL = 21, ST_W = 22;
 
 template <typename R>
-__global__ void k_state_gather(const R *f, size_t N, size_t S, int nreal, double *st, unsigned mask) {
+__global__ void k_state_gather(const R *__restrict__ f, size_t N, size_t S, int nreal, double *__restrict__ st,
+                               unsigned mask) {
     const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= N) return;
     const int *pid = (const int *)(f + nreal * S) + S;
@@ -635,7 +636,8 @@ __global__ void k_state_gather(const R *f, size_t N, size_t S, int nreal, double
 
 // Also raises the fixed-point bounds of the next P2G to cover the new state.
 template <typename R>
-__global__ void k_state_scatter(R *f, size_t N, size_t S, int nreal, const double *st, unsigned mask, DevCtl *ctl,
+__global__ void k_state_scatter(R *__restrict__ f, size_t N, size_t S, int nreal, const double *__restrict__ st,
+                                unsigned mask, DevCtl *ctl,
                                 int parity) {
     const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= N) return;
