@@ -37,6 +37,12 @@ class GridDesc(C.Structure):
                 ("idimc", C.c_int * 3), ("npxye", C.c_int * 3)]
 
 
+class NsParams(C.Structure):
+    """mpm_ns_params: constants of the stabilized fluid (StabilizedMPM)."""
+    _fields_ = [("rho", C.c_double), ("rmu", C.c_double), ("dt", C.c_double), ("beta_nb", C.c_double),
+                ("gamma_nb", C.c_double), ("gravity", C.c_double * 3), ("facl", C.c_double), ("mtol", C.c_double)]
+
+
 class MaterialDesc(C.Structure):
     _fields_ = [("nmat", C.c_int), ("iprop", C.POINTER(C.c_int)), ("mat_prop", C.POINTER(C.c_double))]
 
@@ -69,7 +75,7 @@ EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_s
            "mpm_gpu_upload_particles", "mpm_gpu_steps_host", "mpm_gpu_sync",
            "mpm_gpu_get_stats", "mpm_gpu_enable_kernel_timing", "mpm_gpu_kernel_times", "mpm_gpu_implicit_setup",
            "mpm_gpu_implicit_step", "mpm_gpu_implicit_assemble", "mpm_gpu_implicit_get_system",
-           "mpm_gpu_implicit_matvec", "mpm_gpu_implicit_solve", "mpm_gpu_p2g_noalloc", "mpm_gpu_autotune",
+           "mpm_gpu_implicit_matvec", "mpm_gpu_implicit_solve", "mpm_gpu_p2g_noalloc", "mpm_gpu_ns_assemble", "mpm_gpu_autotune",
            "mpm_gpu_get_tuning", "mpm_nn_num_params", "mpm_nn_create", "mpm_nn_destroy", "mpm_nn_set_stream",
            "mpm_nn_init_params", "mpm_nn_set_linear", "mpm_nn_set_additive", "mpm_nn_set_symmetric", "mpm_nn_set_params", "mpm_nn_get_params", "mpm_nn_forward", "mpm_nn_backward",
            "mpm_nn_num_pairs", "mpm_nn_train", "mpm_gpu_implicit_set_precond", "mpm_gpu_implicit_harvest", "mpm_gpu_implicit_apply_precond",
@@ -377,17 +383,20 @@ class GpuImplicitSolid(GpuSolid):
 
 
 def stencil_to_csr(stencil, xynodec, matrow, matcolid):
-    """Reorder [27][9][nodec] stencil values into the reference's CSR block-major
-    layout amat[e][j] for the graph (matrow, matcolid) of CrsMat::BuildCrsMat."""
+    """Reorder [27][E][nodec] stencil values (E = 9 for the solid's 3x3
+    blocks, 16 for the fluid's 4x4 blocks) into the reference's CSR
+    block-major layout amat[e][j] for the graph (matrow, matcolid) of
+    CrsMat::BuildCrsMat."""
     nx, ny, nz = xynodec
     nodec = nx * ny * nz
-    amat = np.zeros((9, len(matcolid)))
+    ne = stencil.shape[1]
+    amat = np.zeros((ne, len(matcolid)))
     rows = np.repeat(np.arange(nodec), np.diff(matrow))
     cols = np.asarray(matcolid)
     ri, rj, rk = rows % nx, (rows // nx) % ny, rows // (nx * ny)
     ci, cj, ck = cols % nx, (cols // nx) % ny, cols // (nx * ny)
     slot = (ci - ri + 1) + 3 * (cj - rj + 1) + 9 * (ck - rk + 1)
-    for e in range(9):
+    for e in range(ne):
         amat[e] = stencil[slot, e, rows]
     return amat
 
@@ -459,3 +468,48 @@ class PrecondNet:
         losses = np.zeros(epochs, dtype=np.float32)
         _chk(self.lib.mpm_nn_train(self.net, epochs, batch, lr, seed, losses.ctypes.data_as(_fp32)), "mpm_nn_train")
         return losses
+
+
+def ns_assemble(xyelem, xymin, dxy, rho, rmu, dt, beta, gamma, gravity, facl, mtol,
+                x, mass, vol, nvel, naccel, ndispl, npres, nmass, stream=None):
+    """One Newton system of StabilizedMPM::SolveNS (module/fluid/MPM/solve_ns_mpm.cpp:28-62)
+    through mpm_gpu_ns_assemble.  Inputs are FP64 CUDA tensors: x (3, n) or
+    (3*n,), mass and vol (n), nvel / naccel / ndispl (3*nodec, component-major),
+    npres and nmass (nodec).  Returns (tau1, tau2, stencil [27][16][nodec],
+    b_rhs [4*nodec]) as CUDA tensors; raises when a particle lies outside the
+    grid or the call fails.  Waits for the stream before it returns."""
+    import torch
+
+    lib = load()
+    lib.mpm_gpu_ns_assemble.argtypes = [C.POINTER(GridDesc), C.POINTER(NsParams), C.c_int64] + \
+        [C.c_void_p] * 13 + [C.c_void_p]
+    lib.mpm_gpu_ns_assemble.restype = C.c_int
+    g = GridDesc()
+    for d in range(3):
+        g.xyelem[d] = int(xyelem[d])
+        g.xymin[d] = float(xymin[d])
+        g.dxy[d] = float(dxy[d])
+        g.idimc[d] = 1
+        g.npxye[d] = 2
+    p = NsParams(rho, rmu, dt, beta, gamma, (C.c_double * 3)(*[float(v) for v in gravity]), facl, mtol)
+    n = int(mass.numel())
+    nodec = int(np.prod(np.asarray(xyelem) + 1))
+    for t in (x, mass, vol, nvel, naccel, ndispl, npres, nmass):
+        if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+            raise ValueError("ns_assemble: inputs must be contiguous FP64 CUDA tensors")
+    dev = mass.device
+    tau1 = torch.empty(n, dtype=torch.float64, device=dev)
+    tau2 = torch.empty(n, dtype=torch.float64, device=dev)
+    st = torch.empty(27 * 16 * nodec, dtype=torch.float64, device=dev)
+    b = torch.empty(4 * nodec, dtype=torch.float64, device=dev)
+    status = torch.empty(1, dtype=torch.int32, device=dev)
+    strm = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+    rc = lib.mpm_gpu_ns_assemble(C.byref(g), C.byref(p), n, x.data_ptr(), mass.data_ptr(), vol.data_ptr(),
+                                 nvel.data_ptr(), naccel.data_ptr(), ndispl.data_ptr(), npres.data_ptr(),
+                                 nmass.data_ptr(), tau1.data_ptr(), tau2.data_ptr(), st.data_ptr(), b.data_ptr(),
+                                 status.data_ptr(), C.c_void_p(strm))
+    if rc != 0:
+        raise RuntimeError("mpm_gpu_ns_assemble failed: " + lib.mpm_gpu_status_string(rc).decode())
+    if int(status.item()) != 0:
+        raise RuntimeError("mpm_gpu_ns_assemble: a particle lies outside the grid")
+    return tau1, tau2, st.view(27, 16, nodec), b

@@ -327,6 +327,39 @@ mpm_status mpm_gpu_implicit_apply_precond(mpm_ctx *ctx, const double *r, double 
 mpm_status mpm_gpu_implicit_harvest(mpm_ctx *ctx, mpm_nn *net, int nsystems, int loads_per_system, int pairs_per_load,
                                     double e_min, double e_max, uint64_t seed, double eps, int kmax);
 
+/* ---- stabilized incompressible fluid: one Newton system ----------------
+ * Constants of StabilizedMPM (module/fluid/MPM/stabilized_mpm.h:14-100,
+ * module/material_point.h:41-112): density rho, dynamic viscosity rmu, the
+ * time step, the Newmark coefficients (beta_nb, gamma_nb), the body force bb
+ * with its load factor facl, and the mass tolerance mtol. */
+typedef struct {
+    double rho, rmu;
+    double dt;
+    double beta_nb, gamma_nb;
+    double gravity[3];
+    double facl;
+    double mtol;
+} mpm_ns_params;
+
+/* Replaces the system set-up of StabilizedMPM::SolveNS
+ * (module/fluid/MPM/solve_ns_mpm.cpp:28-62): MakNSStabCoeff (VMS, :64-135),
+ * PredictNewmarkBetaVelAndAccel (module/nonlinear_time_integration.cpp:58-70),
+ * AssembleNSSystem (:137-320, with ImplicitDsfCorr and AddInertialForceToRHS)
+ * for linear shape functions (idimc = 1 in every direction).  All pointers
+ * are caller-owned device arrays: particles x (three blocks of n), mass, vol;
+ * the Newton state nvel, naccel, ndispl (component-major, 3*nodec, after
+ * BCNRSet), npres and nmass (nodec).  Writes tau1 and tau2 (n), the unscaled
+ * matrix as 4x4 blocks of the 27-point stencil, stencil[(s*16 + k)*nodec + i]
+ * with k = row_var*4 + col_var over (u, v, w, p) and s = (dx+1) + 3(dy+1) +
+ * 9(dz+1) of column node minus row node i, and b_rhs (component-major
+ * 4*nodec); both are cleared first.  *status (device int) is set to 1 when a
+ * particle lies outside the grid (that particle is skipped), else 0.  Runs on
+ * `stream` (a cudaStream_t, NULL = default stream) without waiting. */
+mpm_status mpm_gpu_ns_assemble(const mpm_grid_desc *grid, const mpm_ns_params *prm, int64_t n, const double *x,
+                               const double *mass, const double *vol, const double *nvel, const double *naccel,
+                               const double *ndispl, const double *npres, const double *nmass, double *tau1,
+                               double *tau2, double *stencil, double *b_rhs, int *status, void *stream);
+
 /* ---- allocation-free P2G -----------------------------------------------------
  * No counterpart in the reference: an extra entry point for callers that
  * cannot let a library allocate device memory (a host program that owns

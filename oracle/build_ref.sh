@@ -1,6 +1,7 @@
 #!/usr/bin/env bash
 # ORACLE build recipe (test infrastructure).  Compiles the reference's own,
-# unmodified C++ translation units for the solid transfer path plus
+# unmodified C++ translation units for the solid transfer path and the
+# stabilized fluid assembly plus
 # oracle/ref_harness.cpp into oracle/_ref/libmpmref.so, against the
 # single-rank stubs in oracle/ref_stubs/.  Reads the reference sources where
 # they lie; copies nothing.  Exits 0 without building when the reference
@@ -17,7 +18,9 @@ mkdir -p "$OUT/obj"
 TUS="shape_function mesh material_point map_and_interpolate nonlinear_time_integration bc data_io mpi_data
      solid/constitutive_model solid/solid_material_point solid/solid_data_io
      solid/implicit/var_trans_solid_implicit solid/implicit/solve_solid_implicit
-     solver/crsmat solver/solver"
+     solver/crsmat solver/solver
+     fluid/MPM/solve_ns_mpm fluid/MPM/var_trans_fluid fluid/MPM/fluid_material_point
+     fluid/MPM/fluid_mpm_data_io fluid/MPM/fluid_point_inflow"
 CXX="${CXX:-g++}"
 FLAGS="-std=c++17 -O3 -fPIC -w -I$HERE/ref_stubs -I$REF/module"
 pids=()

@@ -1,0 +1,138 @@
+"""ORACLE (test infrastructure only): numpy restatement of one Newton system
+of the reference's stabilized incompressible fluid MPM on linear shape
+functions.  Only tests and fixture scripts import this module.
+
+Follows, step for step:
+  StabilizedMPM::MakNSStabCoeff     module/fluid/MPM/solve_ns_mpm.cpp:64-135 (VMS branch)
+  PredictNewmarkBetaVelAndAccel     module/nonlinear_time_integration.cpp:58-70
+  NewmarkBetaParaSet                module/nonlinear_time_integration.cpp:42-56
+  ImplicitDsfCorr                   module/material_point.cpp:127-172 (alpha_f = 1)
+  StabilizedMPM::AssembleNSSystem   module/fluid/MPM/solve_ns_mpm.cpp:137-320
+  ComputeNRLumpedMat                module/material_point.h:67-71
+  AddInertialForceToRHS             module/material_point.h:74-85
+The matrix is returned as a 27-point block stencil [27][16][nodec]: slot
+s = (dx+1) + 3(dy+1) + 9(dz+1) of the column node's offset from the row node,
+entry k = row_var * 4 + col_var over (u, v, w, p) -- the block_id order of
+CrsMat (module/solver/crsmat.cpp:73-75).  Pinned against the reference's own
+compiled AssembleNSSystem by tests/golden/ns_assemble.npz.
+"""
+import numpy as np
+
+
+def newmark(dt, beta, gamma):
+    """nb_para of NewmarkBetaParaSet (nonlinear_time_integration.cpp:42-56)."""
+    return np.array([gamma / (beta * dt), gamma / beta - 1.0, dt / 2.0 * (gamma / beta - 2.0),
+                     1.0 / (beta * dt * dt), 1.0 / (beta * dt), 1.0 / (2.0 * beta) - 1.0])
+
+
+def _shape(x, xmin, dx, cell, nnc):
+    """Linear MakSf (module/shape_function.cpp:28-110) of points x (n,3) in the
+    given cells: weights (n,8), gradients (n,8,3), node ids (n,8); node q =
+    i + 2j + 4k sits at cell + (i, j, k)."""
+    n = x.shape[0]
+    w = np.empty((n, 3, 2))
+    dw = np.empty((n, 3, 2))
+    for d in range(3):
+        for k in range(2):
+            xy = xmin[d] + dx[d] * (cell[:, d] + k)
+            w[:, d, k] = 1.0 - np.abs(x[:, d] - xy) / dx[d]
+            dw[:, d, k] = (-1.0 if k == 0 else 1.0) / dx[d]
+    W = np.empty((n, 8))
+    D = np.empty((n, 8, 3))
+    nid = np.empty((n, 8), dtype=np.int64)
+    for k in range(2):
+        for j in range(2):
+            for i in range(2):
+                q = i + 2 * j + 4 * k
+                W[:, q] = w[:, 0, i] * w[:, 1, j] * w[:, 2, k]
+                D[:, q, 0] = dw[:, 0, i] * w[:, 1, j] * w[:, 2, k]
+                D[:, q, 1] = w[:, 0, i] * dw[:, 1, j] * w[:, 2, k]
+                D[:, q, 2] = w[:, 0, i] * w[:, 1, j] * dw[:, 2, k]
+                nid[:, q] = (cell[:, 0] + i) + nnc[0] * ((cell[:, 1] + j) + nnc[1] * (cell[:, 2] + k))
+    return W, D, nid
+
+
+def ns_assemble(xyelem, xymin, dxy, rho, rmu, dt, beta, gamma, gravity, facl, mtol,
+                x, mass, vol, nvel, naccel, ndispl, npres, nmass):
+    """One Newton system of SolveNS on the nodal state (component-major
+    nvel/naccel/ndispl of 3*nodec; npres, nmass of nodec) and particles
+    x (n,3), mass, vol.  Returns tau1, tau2, stencil [27][16][nodec], b (4*nodec)."""
+    xyelem = np.asarray(xyelem)
+    xmin = np.asarray(xymin, dtype=np.float64)
+    dx = np.asarray(dxy, dtype=np.float64)
+    nnc = xyelem + 1
+    N = int(np.prod(nnc))
+    x = np.asarray(x, dtype=np.float64)
+    n = x.shape[0]
+    cell = np.floor((x - xmin) / dx).astype(np.int64)   # MeshPointLinklist (material_point.cpp:59-65)
+    nb = newmark(dt, beta, gamma)
+    nv = np.asarray(nvel).reshape(3, N)
+    na = np.asarray(naccel).reshape(3, N)
+    nd = np.asarray(ndispl).reshape(3, N)
+    vel_k = nb[0] * nd - nb[1] * nv - nb[2] * na
+    acc_k = nb[3] * nd - nb[4] * nv - nb[5] * na
+    # ---- MakNSStabCoeff: velocity and gradients at the element centre ----
+    xc = xmin + dx * (cell + 0.5)
+    Wc, Dc, nid = _shape(xc, xmin, dx, cell, nnc)
+    uc = np.einsum("nq,rnq->nr", Wc, nv[:, nid])
+    uvw = np.sum(uc * uc, axis=1)
+    udsf = np.sum(np.abs(np.einsum("nr,nqr->nq", uc, Dc)), axis=1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        he = np.where(udsf < mtol, dx[0] * np.cbrt(6.0 / np.pi), 2.0 * np.sqrt(uvw) / udsf)
+    t1 = rho / dt
+    t2 = 2.0 * rho * np.sqrt(uvw) / he
+    t3 = 4.0 * rmu / (he * he)
+    tau1 = 1.0 / (t1 + t2 + t3)
+    tau2 = (he * he) / (4.0 * tau1)
+    # ---- AssembleNSSystem ----
+    W, D, nid = _shape(x, xmin, dx, cell, nnc)
+    Fd = np.einsum("nqc,rnq->nrc", D, nd[:, nid]) + np.eye(3)   # ComputeDeltaDefGrad, alpha_f = 1
+    D = np.einsum("nqi,nij->nqj", D, np.linalg.inv(Fd))          # ImplicitDsfCorr
+    f = np.asarray(gravity, dtype=np.float64) * facl
+    pres_k = np.einsum("nq,nq->n", W, npres[nid])
+    accel_k = np.einsum("nq,rnq->nr", W, acc_k[:, nid])
+    gp = np.einsum("nqc,nq->nc", D, npres[nid])
+    gv = np.einsum("nqc,rnq->nrc", D, vel_k[:, nid])             # gv[r][c] = d vel_r / d x_c
+    dev = rmu * (gv + np.transpose(gv, (0, 2, 1)))
+    V = vol[:, None, None]
+    m = mass[:, None, None]
+    T1 = tau1[:, None, None]
+    T2 = tau2[:, None, None]
+    a = D[:, :, None, :]     # row node (test function)
+    b = D[:, None, :, :]     # column node (trial function)
+    Ni = W[:, :, None]
+    Nj = W[:, None, :]
+    ab = np.sum(a * b, axis=3)
+    K = np.zeros((n, 8, 8, 4, 4))
+    for r in range(3):
+        for c in range(3):
+            K[..., r, c] = nb[0] * (V * rmu * (a[..., c] * b[..., r] + (ab if r == c else 0.0))
+                                    + V * T2 * a[..., r] * b[..., c])
+        K[..., r, 3] = -V * a[..., r] * Nj
+        K[..., 3, r] = nb[0] * V * Ni * b[..., r] + nb[3] * m * a[..., r] * Nj * T1
+    K[..., 3, 3] = V * ab * T1
+    emd = nb[3] * W * mass[:, None]
+    for q in range(8):
+        for r in range(3):
+            K[:, q, q, r, r] += emd[:, q]
+    off = np.array([[i, j, k] for k in range(2) for j in range(2) for i in range(2)])
+    d = off[None, :, :] - off[:, None, :]
+    slot = (d[..., 0] + 1) + 3 * (d[..., 1] + 1) + 9 * (d[..., 2] + 1)     # [qa][qb]
+    stencil = np.zeros(27 * 16 * N)
+    idx = ((slot[None, :, :, None] * 16 + np.arange(16)[None, None, None, :]) * N
+           + nid[:, :, None, None])
+    np.add.at(stencil, np.broadcast_to(idx, (n, 8, 8, 16)).ravel(), K.reshape(n, 8, 8, 16).ravel())
+    divv = gv[:, 0, 0] + gv[:, 1, 1] + gv[:, 2, 2]
+    Vn = vol[:, None]
+    rhs = np.zeros((n, 8, 4))
+    for r in range(3):
+        rhs[..., r] = (Vn * np.einsum("nqc,nc->nq", D, dev[:, r, :]) - W * mass[:, None] * f[r]
+                       - Vn * D[..., r] * pres_k[:, None] + Vn * tau2[:, None] * D[..., r] * divv[:, None])
+    rhs[..., 3] = (Vn * W * divv[:, None]
+                   + tau1[:, None] * mass[:, None] * np.einsum("nqc,nc->nq", D, accel_k - f)
+                   + tau1[:, None] * Vn * np.einsum("nqc,nc->nq", D, gp))
+    bvec = np.zeros(4 * N)
+    for r in range(4):
+        np.add.at(bvec, r * N + nid.ravel(), -rhs[..., r].ravel())
+    bvec[:3 * N] -= (np.asarray(nmass)[None, :] * acc_k).ravel()   # AddInertialForceToRHS
+    return tau1, tau2, stencil.reshape(27, 16, N), bvec

@@ -164,3 +164,35 @@ class RefSolid:
         x = np.zeros(self.nodec * 3)
         it = self.lib.ref_implicit_solve(x)
         return x, it
+
+
+class RefFluid:
+    """The reference's stabilizedmpm::StabilizedMPM (module/fluid/MPM/) on one
+    rank, through oracle/_ref: one Newton system of SolveNS on a given nodal
+    state (MakNSStabCoeff, PredictNewmarkBetaVelAndAccel, AssembleNSSystem)."""
+
+    def __init__(self, xyelem, xymin, dxy, dt, mtol, gravity, x, mass, vol, rho, rmu, beta, gamma):
+        lib = self.lib = _lib()
+        lib.ref_ns_init.argtypes = [C.c_int, _dp, _dp, _dp, C.c_double, C.c_double, C.c_double, C.c_double]
+        lib.ref_ns_assemble.argtypes = [_dp, _dp, _dp, _dp, _dp, C.c_double, _dp, _dp]
+        lib.ref_ns_get_matrix.argtypes = [_ip, _ip, _dp, _dp]
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        self.nodec = lib.ref_setup(i32(xyelem), f64(xymin), f64(dxy), i32([1, 1, 1]), i32([2, 2, 2]), float(dt),
+                                   float(mtol), f64(gravity), 1, i32([0]), f64([0.0, 0.0, 0.0]))
+        self.num = len(mass)
+        self.nmat = lib.ref_ns_init(self.num, f64(x), f64(mass), f64(vol), rho, rmu, beta, gamma)
+
+    def assemble(self, nvel, naccel, ndispl, npres, nmass, facl):
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        tau1 = np.zeros(self.num)
+        tau2 = np.zeros(self.num)
+        assert self.lib.ref_ns_assemble(f64(nvel), f64(naccel), f64(ndispl), f64(npres), f64(nmass), facl,
+                                        tau1, tau2) == 0
+        matrow = np.zeros(self.nodec + 1, dtype=np.int32)
+        matcolid = np.zeros(self.nmat, dtype=np.int32)
+        amat = np.zeros(16 * self.nmat)
+        b = np.zeros(4 * self.nodec)
+        self.lib.ref_ns_get_matrix(matrow, matcolid, amat, b)
+        return dict(tau1=tau1, tau2=tau2, matrow=matrow, matcolid=matcolid, amat=amat.reshape(16, self.nmat),
+                    b_rhs=b)

@@ -43,6 +43,7 @@
 #include "mpi_data.h"
 #include "shape_function.h"
 #include "solid/implicit/implicit_mpm_solid.h"
+#include "fluid/MPM/stabilized_mpm.h"
 #include "solid/solid_material_point.h"
 
 namespace {
@@ -322,6 +323,7 @@ class ExplicitSolid : public SolidMaterialPointBase {
 std::unique_ptr<ExplicitSolid> g_exp;
 int g_fbar = 0;   // Fbar_flag of the next explicit solid
 std::unique_ptr<implicitmpm::SolidMaterialPoint> g_imp;
+std::unique_ptr<stabilizedmpm::StabilizedMPM> g_ns;
 int g_last_krylov = 0;
 
 MaterialPoint *active() {
@@ -363,6 +365,7 @@ int ref_setup(const int *xyelem_in, const double *xymin_in, const double *dxy_in
               const int *npxye_in, double dt_in, double mtol_in, const double *bb_in, int nmat_in, const int *iprop_in,
               const double *mat_prop_in) {
     g_exp.reset();
+    g_ns.reset();
     g_imp.reset();
     nprocs = 1;
     myrank = 0;
@@ -695,6 +698,73 @@ int ref_implicit_solve(double *x_out) {
     std::memcpy(x_out, M.x_lhs.data(), M.x_lhs.size() * sizeof(double));
     g_last_krylov = it;
     return it;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Stabilized fluid MPM: the reference's stabilizedmpm::StabilizedMPM as-is.  */
+/* ------------------------------------------------------------------------- */
+/* Particles (coord as num x 3, mass, vol), fluid constants and Newmark
+ * coefficients; builds the 4-DOF CSR graph (work/src_fluid/MPM/main.cpp:29)
+ * and the element link list.  Returns the number of CSR entries. */
+int ref_ns_init(int num, const double *coord, const double *mass, const double *vol, double rho, double rmu,
+                double beta_nb, double gamma_nb) {
+    g_exp.reset();
+    g_imp.reset();
+    g_ns = std::make_unique<stabilizedmpm::StabilizedMPM>();
+    auto &w = *g_ns;
+    w.num = num;
+    w.InitializePointData();
+    for (int p = 0; p < num; p++) {
+        w.id[p] = p;
+        w.mass[p] = mass[p];
+        w.vol[p] = vol[p];
+        for (int i = 0; i < 3; i++) w.coord[p][i] = coord[3 * p + i];
+    }
+    w.rho = rho;
+    w.rmu = rmu;
+    w.beta_nb = beta_nb;
+    w.gamma_nb = gamma_nb;
+    w.NewmarkBetaParaSet();  // work/src_fluid/MPM/datain_para.cpp:80
+    w.NS_.use_petsc = false;  // graph only: no PETSc objects behind the single-rank stubs
+    w.NS_.BuildCrsMat(16);
+    w.NS_.use_petsc = true;   // AssembleNSSystem then leaves the matrix unscaled
+    w.MeshPointLinklist();
+    return w.NS_.nmat;
+}
+
+/* One Newton system of SolveNS (solve_ns_mpm.cpp:28-62) on the given nodal
+ * state (component-major nvel/naccel/ndispl of 3*nodec, npres/nmass of
+ * nodec): MakNSStabCoeff, PredictNewmarkBetaVelAndAccel, AssembleNSSystem.
+ * The matrix stays unscaled (use_petsc is left true, so no diagonal scaling). */
+int ref_ns_assemble(const double *nvel, const double *naccel, const double *ndispl, const double *npres,
+                    const double *nmass, double facl_in, double *tau1, double *tau2) {
+    if (!g_ns) return -1;
+    auto &w = *g_ns;
+    facl = facl_in;
+    w.nvel.assign(nvel, nvel + (size_t)nodec * 3);
+    w.naccel.assign(naccel, naccel + (size_t)nodec * 3);
+    w.ndispl.assign(ndispl, ndispl + (size_t)nodec * 3);
+    w.npres.assign(npres, npres + (size_t)nodec);
+    w.nmass.assign(nmass, nmass + (size_t)nodec);
+    w.MakNSStabCoeff();
+    std::vector<double> nvel_k(nodec * 3), naccel_k(nodec * 3);
+    w.PredictNewmarkBetaVelAndAccel(nvel_k, naccel_k);
+    w.AssembleNSSystem(nvel_k, naccel_k);
+    std::memcpy(tau1, w.tau1.data(), (size_t)w.num * sizeof(double));
+    std::memcpy(tau2, w.tau2.data(), (size_t)w.num * sizeof(double));
+    return 0;
+}
+
+/* CSR graph, the 16 block-major value arrays amat[b * nmat + e]
+ * (b = row_var * 4 + col_var) and b_rhs (4 * nodec). */
+int ref_ns_get_matrix(int *matrow, int *matcolid, double *amat, double *b_rhs) {
+    if (!g_ns) return -1;
+    auto &M = g_ns->NS_;
+    std::memcpy(matrow, M.matrow.data(), M.matrow.size() * sizeof(int));
+    std::memcpy(matcolid, M.matcolid.data(), M.matcolid.size() * sizeof(int));
+    std::memcpy(amat, M.amat.data(), M.amat.size() * sizeof(double));
+    std::memcpy(b_rhs, M.b_rhs.data(), M.b_rhs.size() * sizeof(double));
+    return M.nmat;
 }
 
 int ref_nodec(void) { return nodec; }

@@ -11,6 +11,7 @@ committed and this script is re-run only when a case is added:
     python tests/golden/make_golden.py --affine           # only the TPIC / APIC cases
     python tests/golden/make_golden.py --io               # only the deck / restart fixtures (tests/golden/io)
     python tests/golden/make_golden.py --fbar             # only the F-bar cases
+    python tests/golden/make_golden.py --fluid            # only the stabilized fluid assembly
 """
 from __future__ import annotations
 
@@ -168,6 +169,47 @@ def io_cases():
     print("wrote", d, sorted(os.listdir(d)))
 
 
+def ns_inputs(seed=11, xyelem=(6, 5, 4), dx=0.1, ppd=2):
+    """Seeded particles (ppd^3 per cell, jittered, in all but the outer cell
+    layer) and a nodal Newton state for one stabilized-fluid system; the
+    velocity is zero on the lower-x third of the nodes so that the
+    zero-velocity branch of the element size (he) is taken there."""
+    rng = np.random.default_rng(seed)
+    xyelem = np.asarray(xyelem)
+    nnc = xyelem + 1
+    N = int(np.prod(nnc))
+    pts = []
+    for k in range(1, xyelem[2] - 1):
+        for j in range(1, xyelem[1] - 1):
+            for i in range(1, xyelem[0] - 1):
+                for c in np.ndindex(ppd, ppd, ppd):
+                    pts.append((np.array([i, j, k]) + (np.array(c) + 0.5 + rng.uniform(-0.3, 0.3, 3)) / ppd) * dx)
+    x = np.array(pts)
+    n = len(x)
+    vol = np.full(n, dx ** 3 / ppd ** 3) * rng.uniform(0.9, 1.1, n)
+    mass = 1000.0 * vol
+    nvel = rng.normal(0.0, 0.5, (3, N))
+    ix = np.arange(N) % nnc[0]
+    nvel[:, ix <= nnc[0] // 3] = 0.0
+    naccel = rng.normal(0.0, 2.0, (3, N))
+    ndispl = rng.normal(0.0, 1e-3 * dx, (3, N))
+    npres = rng.normal(0.0, 50.0, N)
+    nmass = rng.uniform(0.0, 0.2, N)
+    return dict(xyelem=xyelem, xymin=np.zeros(3), dxy=np.full(3, dx), x=x, mass=mass, vol=vol,
+                nvel=nvel.ravel(), naccel=naccel.ravel(), ndispl=ndispl.ravel(), npres=npres, nmass=nmass,
+                rho=1000.0, rmu=1.0e-3 * 50, dt=2.0e-3, beta=0.25, gamma=0.5, gravity=np.array([0.0, 0.0, -9.8]),
+                facl=0.8, mtol=1.0e-12)
+
+
+def fluid_case(name="ns_assemble"):
+    """One Newton system of the reference's StabilizedMPM::SolveNS."""
+    c = ns_inputs()
+    r = ref.RefFluid(c["xyelem"], c["xymin"], c["dxy"], c["dt"], c["mtol"], c["gravity"], c["x"], c["mass"],
+                     c["vol"], c["rho"], c["rmu"], c["beta"], c["gamma"])
+    out = r.assemble(c["nvel"], c["naccel"], c["ndispl"], c["npres"], c["nmass"], c["facl"])
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **c, **out)
+
+
 def main():
     if not ref.available():
         raise SystemExit("oracle/_ref/libmpmref.so missing: run oracle/build_ref.sh first")
@@ -179,6 +221,9 @@ def main():
         return
     if "--io" in sys.argv[1:]:
         io_cases()
+        return
+    if "--fluid" in sys.argv[1:]:
+        fluid_case()
         return
     if "--fbar" in sys.argv[1:]:
         fbar_cases()
@@ -209,6 +254,7 @@ def main():
     affine_cases()
     io_cases()
     fbar_cases()
+    fluid_case()
 
 
 if __name__ == "__main__":

@@ -1,0 +1,126 @@
+"""Stabilized fluid MPM assembly on the GPU (mpm_gpu_ns_assemble) against the
+reference's own compiled AssembleNSSystem (fixture), against the numpy oracle
+on a larger seeded case, and, at full size, against size-independent
+properties of the system (symmetric velocity and pressure blocks).  FP64:
+relative L2 tolerance 1e-12 (summation order differs from the reference)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from mpm_gb300 import capi
+from oracle import ns_oracle
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+import make_golden  # noqa: E402  (seeded input generator only; the reference is not touched)
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+KEYS = ("rho", "rmu", "dt", "beta", "gamma", "gravity", "facl", "mtol")
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def gpu_run(c):
+    torch = pytest.importorskip("torch")
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda:0")
+    out = capi.ns_assemble(c["xyelem"], c["xymin"], c["dxy"], *(c[k] for k in KEYS), t(c["x"].T.copy()),
+                           t(c["mass"]), t(c["vol"]), t(c["nvel"]), t(c["naccel"]), t(c["ndispl"]), t(c["npres"]),
+                           t(c["nmass"]))
+    return [o.cpu().numpy() for o in out]
+
+
+def test_gpu_ns_matches_reference_fixture():
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ns_assemble.npz")))
+    tau1, tau2, st, b = gpu_run(g)
+    assert rel(tau1, g["tau1"]) < TOL and rel(tau2, g["tau2"]) < TOL
+    amat = capi.stencil_to_csr(st, tuple(g["xyelem"] + 1), g["matrow"], g["matcolid"])
+    for k in range(16):
+        assert rel(amat[k], g["amat"][k]) < TOL, k
+    assert rel(b, g["b_rhs"]) < TOL
+    assert np.isclose(np.abs(amat).sum(), np.abs(st).sum(), rtol=1e-14)
+
+
+def test_gpu_ns_matches_oracle_ragged_grid():
+    c = make_golden.ns_inputs(seed=3, xyelem=(13, 9, 7), dx=0.05, ppd=2)
+    want = ns_oracle.ns_assemble(c["xyelem"], c["xymin"], c["dxy"], *(c[k] for k in KEYS), c["x"], c["mass"],
+                                 c["vol"], c["nvel"], c["naccel"], c["ndispl"], c["npres"], c["nmass"])
+    got = gpu_run(c)
+    for w, g_ in zip(want, got):
+        assert rel(g_.ravel(), w.ravel()) < TOL
+
+
+def test_gpu_ns_no_particles_gives_inertia_only():
+    c = make_golden.ns_inputs(seed=4, xyelem=(4, 4, 4))
+    c = {**c, "x": np.zeros((0, 3)), "mass": np.zeros(0), "vol": np.zeros(0)}
+    _, _, st, b = gpu_run(c)
+    assert not st.any()
+    nb = ns_oracle.newmark(c["dt"], c["beta"], c["gamma"])
+    N = len(c["nmass"])
+    acc = nb[3] * c["ndispl"] - nb[4] * c["nvel"] - nb[5] * c["naccel"]
+    assert np.allclose(b[:3 * N], -(np.tile(c["nmass"], 3) * acc), rtol=1e-14, atol=0)
+    assert not b[3 * N:].any()
+
+
+def test_gpu_ns_out_of_grid_particle_is_reported():
+    c = make_golden.ns_inputs(seed=5, xyelem=(4, 4, 4))
+    c["x"] = c["x"].copy()
+    c["x"][0, 0] = -1.0
+    with pytest.raises(RuntimeError, match="outside the grid"):
+        gpu_run(c)
+
+
+def test_gpu_ns_full_size_symmetry_and_timing():
+    """~4.1M particles (8 per cell in an 80^3-cell block of a 100^3 grid): the
+    velocity-velocity blocks satisfy K_ab[r][c] = K_ba[c][r] and the
+    pressure-pressure entries are symmetric; prints the mean assembly time."""
+    torch = pytest.importorskip("torch")
+    ne, blk = 100, 80
+    dx = 1.0 / ne
+    rng = np.random.default_rng(9)
+    lo = (ne - blk) // 2
+    cells = np.stack(np.meshgrid(*[np.arange(lo, lo + blk)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    sub = np.array([(i, j, k) for k in range(2) for j in range(2) for i in range(2)])
+    x = ((cells[:, None, :] + (sub[None] + 0.5) / 2.0).reshape(-1, 3) + rng.uniform(-0.2, 0.2, (len(cells) * 8, 3)) / 2) * dx
+    n = len(x)
+    N = (ne + 1) ** 3
+    dev = "cuda:0"
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=dev)
+    vol = np.full(n, dx ** 3 / 8)
+    args = [t(x.T.copy()), t(1000.0 * vol), t(vol), t(rng.normal(0, 0.5, 3 * N)), t(rng.normal(0, 2, 3 * N)),
+            t(rng.normal(0, 1e-3 * dx, 3 * N)), t(rng.normal(0, 50, N)), t(rng.uniform(0, 0.2, N))]
+    prm = (1000.0, 0.05, 1e-3, 0.25, 0.5, (0.0, 0.0, -9.8), 1.0, 1e-12)
+    geo = ((ne,) * 3, (0.0,) * 3, (dx,) * 3)
+    for _ in range(3):
+        capi.ns_assemble(*geo, *prm, *args)
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    reps = 5
+    e0.record(s)
+    for _ in range(reps):
+        out = capi.ns_assemble(*geo, *prm, *args)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    print(f"\nmpm_gpu_ns_assemble: {n} particles, {N} nodes: {ms:.3f} ms per system "
+          f"({n / ms * 1e3:.3e} particles/s, {n * 1056 / ms * 1e-6:.3e} FP64 atomics/ns)")
+    st = out[2]
+    nx = ne + 1
+    idx = torch.arange(N, device=dev)
+    ii, jj, kk = idx % nx, (idx // nx) % nx, idx // (nx * nx)
+    worst = 0.0
+    for sl in range(27):
+        dx_, dy_, dz_ = sl % 3 - 1, (sl // 3) % 3 - 1, sl // 9 - 1
+        ok = (ii + dx_ >= 0) & (ii + dx_ < nx) & (jj + dy_ >= 0) & (jj + dy_ < nx) & (kk + dz_ >= 0) & (kk + dz_ < nx)
+        rows = idx[ok]
+        cols = rows + dx_ + nx * (dy_ + nx * dz_)
+        for r, c in [(r, c) for r in range(3) for c in range(3)] + [(3, 3)]:
+            a = st[sl, 4 * r + c, rows]
+            bt = st[26 - sl, 4 * c + r, cols]
+            scale = float(a.abs().max()) + 1e-300
+            worst = max(worst, float((a - bt).abs().max()) / scale)
+    assert worst < 1e-12, worst

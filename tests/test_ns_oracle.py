@@ -1,0 +1,68 @@
+"""Stabilized fluid MPM assembly: the numpy oracle (oracle/ns_oracle.py)
+against the reference's own compiled StabilizedMPM::MakNSStabCoeff /
+AssembleNSSystem (fixture tests/golden/ns_assemble.npz, made by
+tests/golden/make_golden.py --fluid).  CPU only."""
+import os
+
+import numpy as np
+
+from mpm_gb300 import capi
+from oracle import ns_oracle
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ns_assemble.npz")
+TOL = 1e-12   # FP64, summation order differs from the reference's element-ordered loop
+
+
+def golden():
+    return dict(np.load(GOLDEN))
+
+
+def run_oracle(g):
+    return ns_oracle.ns_assemble(g["xyelem"], g["xymin"], g["dxy"], float(g["rho"]), float(g["rmu"]), float(g["dt"]),
+                                 float(g["beta"]), float(g["gamma"]), g["gravity"], float(g["facl"]),
+                                 float(g["mtol"]), g["x"], g["mass"], g["vol"], g["nvel"], g["naccel"], g["ndispl"],
+                                 g["npres"], g["nmass"])
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def test_ns_oracle_matches_reference_fixture():
+    g = golden()
+    tau1, tau2, st, b = run_oracle(g)
+    assert rel(tau1, g["tau1"]) < TOL and rel(tau2, g["tau2"]) < TOL
+    amat = capi.stencil_to_csr(st, tuple(g["xyelem"] + 1), g["matrow"], g["matcolid"])
+    for k in range(16):
+        assert rel(amat[k], g["amat"][k]) < TOL, k
+    assert rel(b, g["b_rhs"]) < TOL
+    # every stencil entry the graph does not hold is zero
+    assert np.isclose(np.abs(amat).sum(), np.abs(st).sum(), rtol=1e-14)
+
+
+def test_ns_fixture_covers_both_element_size_branches():
+    g = golden()
+    he0 = g["dxy"][0] * np.cbrt(6.0 / np.pi)
+    zero_branch = np.isclose(g["tau2"], he0 * he0 / (4.0 * g["tau1"]), rtol=1e-12)
+    assert 0 < zero_branch.sum() < len(zero_branch)
+
+
+def test_ns_velocity_blocks_are_symmetric():
+    """K_ab[r][c] = K_ba[c][r] for the velocity-velocity part (viscous and
+    shock-capturing terms), and the pressure-pressure entry is symmetric."""
+    g = golden()
+    _, _, st, _ = run_oracle(g)
+    nnc = tuple(g["xyelem"] + 1)
+    nx, ny, nz = nnc
+    N = nx * ny * nz
+    ii, jj, kk = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    for s in range(27):
+        dx, dy, dz = s % 3 - 1, (s // 3) % 3 - 1, s // 9 - 1
+        ok = ((ii + dx >= 0) & (ii + dx < nx) & (jj + dy >= 0) & (jj + dy < ny) & (kk + dz >= 0) & (kk + dz < nz))
+        rows = (ii + nx * (jj + ny * kk))[ok]
+        cols = rows + dx + nx * (dy + ny * dz)
+        for r in range(3):
+            for c in range(3):
+                assert np.allclose(st[s, 4 * r + c, rows], st[26 - s, 4 * c + r, cols], rtol=1e-12, atol=1e-9)
+        assert np.allclose(st[s, 15, rows], st[26 - s, 15, cols], rtol=1e-12, atol=1e-15)
+    assert N == st.shape[2]
