@@ -18,7 +18,13 @@
 //     and both results are then wrong.
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (once per device, with that device current); make
-//     that first call before any stream capture.
+//     that first call before any stream capture.  The address is kept for the
+//     life of the process, so the library must not be used across a
+//     cudaDeviceReset (which may move the array).
+//   * a particle outside the grid, or with a non-finite coordinate, velocity,
+//     stress, mass or volume, is skipped (it adds nothing to any node and
+//     does not enter the fixed-point bounds) and reported in the caller's
+//     device status word: bit 0 outside the grid, bit 1 non-finite.
 #include <cstdio>
 #include <mutex>
 
@@ -43,12 +49,29 @@ struct NoAllocArgs {
     float mtol;
     double gshape;
     unsigned long long *scr;
+    int *status;   // caller-owned device word: NA_OUTSIDE | NA_NONFINITE
 };
 
-__global__ void k_na_clear(unsigned long long *scr, size_t words) {
+constexpr int NA_OUTSIDE = 1;
+constexpr int NA_NONFINITE = 2;
+
+// 0 when particle p may be scattered, else the status bit that rejects it.
+__device__ __forceinline__ int na_reject(const NoAllocArgs &a, int p) {
+    const size_t N = (size_t)a.n;
+    float acc = a.m[p] + a.vol[p];
+    for (int c = 0; c < 3; c++) acc += a.x[c * N + p] + a.v[c * N + p];
+    for (int k = 0; k < 6; k++) acc += a.s[k * N + p];
+    if (!isfinite(acc)) return NA_NONFINITE;   // also rejects finite values whose sum overflows
+    bool oob = false;
+    for (int d = 0; d < 3; d++) (void)cell_of(a.x[d * N + p], a.g, d, oob);
+    return oob ? NA_OUTSIDE : 0;
+}
+
+__global__ void k_na_clear(unsigned long long *scr, size_t words, int *status) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x)
         scr[i] = 0ull;
     if (blockIdx.x == 0 && threadIdx.x < NA_BOUNDS) scr[NACC * (size_t)NOALLOC_MAX_NODES + threadIdx.x] = 0ull;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *status = 0;
 }
 
 __device__ __forceinline__ void na_max(unsigned long long *slot, float v) {
@@ -59,6 +82,11 @@ __device__ __forceinline__ void na_max(unsigned long long *slot, float v) {
 __global__ void k_na_bounds(NoAllocArgs a) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= a.n) return;
+    const int rej = na_reject(a, p);
+    if (rej) {
+        atomicOr(a.status, rej);
+        return;
+    }
     const size_t N = (size_t)a.n;
     const float m = a.m[p], vol = a.vol[p];
     const float vm = fmaxf(fabsf(a.v[p]), fmaxf(fabsf(a.v[N + p]), fabsf(a.v[2 * N + p])));
@@ -97,6 +125,7 @@ __global__ void __launch_bounds__(256) k_na_scatter(NoAllocArgs a) {
     __syncthreads();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= a.n) return;
+    if (na_reject(a, p)) return;   // reported by k_na_bounds
     const size_t N = (size_t)a.n, NN = (size_t)a.g.nodec;
     const float x0 = a.x[p], x1 = a.x[N + p], x2 = a.x[2 * N + p];
     bool oob = false;
@@ -177,10 +206,10 @@ using namespace mpm;
 mpm_status mpm_gpu_p2g_noalloc(const mpm_grid_desc *grid, const double *gravity, double facl, double mtol, int64_t n,
                                const float *x, const float *v, const float *stress, const float *mass,
                                const float *vol, float *nmass, float *nvof, float *nmome, float *nforce,
-                               void *stream) {
+                               int *status, void *stream) {
     if (!grid || !gravity || n < 0 || n > (int64_t)1 << 30) return MPM_ERR_BAD_ARG;
     if (n > 0 && (!x || !v || !stress || !mass || !vol)) return MPM_ERR_BAD_ARG;
-    if (!nmass || !nvof || !nmome || !nforce) return MPM_ERR_BAD_ARG;
+    if (!nmass || !nvof || !nmome || !nforce || !status) return MPM_ERR_BAD_ARG;
     NoAllocArgs a;
     long long nodec = 1;
     for (int d = 0; d < 3; d++) {
@@ -210,6 +239,7 @@ mpm_status mpm_gpu_p2g_noalloc(const mpm_grid_desc *grid, const double *gravity,
     a.nvof = nvof;
     a.nmome = nmome;
     a.nforce = nforce;
+    a.status = status;
     a.facl = (float)facl;
     a.mtol = (float)mtol;
     a.gshape = 0.0;
@@ -224,7 +254,7 @@ mpm_status mpm_gpu_p2g_noalloc(const mpm_grid_desc *grid, const double *gravity,
     }
     cudaStream_t st = (cudaStream_t)stream;
     const size_t words = (size_t)NACC * (size_t)nodec;
-    k_na_clear<<<(int)((words + 255) / 256 < 4096 ? (words + 255) / 256 : 4096), 256, 0, st>>>(a.scr, words);
+    k_na_clear<<<(int)((words + 255) / 256 < 4096 ? (words + 255) / 256 : 4096), 256, 0, st>>>(a.scr, words, status);
     if (n > 0) {
         const int nb = (int)((n + 255) / 256);
         k_na_bounds<<<nb, 256, 0, st>>>(a);

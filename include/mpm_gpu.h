@@ -352,7 +352,11 @@ typedef struct {
  * matrix as 4x4 blocks of the 27-point stencil, stencil[(s*16 + k)*nodec + i]
  * with k = row_var*4 + col_var over (u, v, w, p) and s = (dx+1) + 3(dy+1) +
  * 9(dz+1) of column node minus row node i, and b_rhs (component-major
- * 4*nodec); both are cleared first.  *status (device int) is set to 1 when a
+ * 4*nodec); both are cleared first.  As in the reference, where SolveNS calls
+ * MakNSStabCoeff once before its Newton loop, tau1 / tau2 are computed from
+ * nvel, which must be the nodal velocity from before the Newton loop (not
+ * the current iterate); the gradient correction uses alpha_f = 1 (the
+ * Newmark scheme StabilizedMPM sets up, no generalized-alpha weighting).  *status (device int) is set to 1 when a
  * particle lies outside the grid (that particle is skipped), else 0.  Runs on
  * `stream` (a cudaStream_t, NULL = default stream) without waiting. */
 mpm_status mpm_gpu_ns_assemble(const mpm_grid_desc *grid, const mpm_ns_params *prm, int64_t n, const double *x,
@@ -371,15 +375,22 @@ mpm_status mpm_gpu_ns_assemble(const mpm_grid_desc *grid, const mpm_ns_params *p
  * structure-of-arrays FP32 layout: x and v as three blocks of n, stress as
  * six Voigt blocks of n, mass and vol of n.  Launches on `stream`
  * (a cudaStream_t, NULL = default stream) and returns without waiting.
+ * status: a caller-owned device int, set to 0 by the call; a particle outside
+ * the grid sets bit 0 (1) and a particle with a non-finite coordinate,
+ * velocity, stress, mass or volume sets bit 1 (2), and such a particle is
+ * skipped (it adds nothing to the nodal fields), as the regular P2G counts
+ * particles out of the box instead of scattering them.
  * Scratch: one static device array sized for at most 262,144 control points
  * (64^3); larger grids return MPM_ERR_BAD_ARG.  Every call shares that array
  * and clears it first, so calls that overlap on the GPU race.  The first call
  * on a device looks up the array's address (cudaGetSymbolAddress) and should
- * come before any stream capture.  Nothing is allocated or freed. */
+ * come before any stream capture; that address is kept for the life of the
+ * process, so the library must not be used across a cudaDeviceReset.
+ * Nothing is allocated or freed. */
 mpm_status mpm_gpu_p2g_noalloc(const mpm_grid_desc *grid, const double *gravity, double facl, double mtol, int64_t n,
                                const float *x, const float *v, const float *stress, const float *mass,
                                const float *vol, float *nmass, float *nvof, float *nmome, float *nforce,
-                               void *stream);
+                               int *status, void *stream);
 
 #ifdef __cplusplus
 }

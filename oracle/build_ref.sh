@@ -4,14 +4,16 @@
 # stabilized fluid assembly plus
 # oracle/ref_harness.cpp into oracle/_ref/libmpmref.so, against the
 # single-rank stubs in oracle/ref_stubs/.  Reads the reference sources where
-# they lie; copies nothing.  Exits 0 without building when the reference
-# checkout is absent (it is only present in the development container).
+# they lie; copies nothing.  The checkout is named by the first argument or,
+# failing that, by MPM_REFERENCE_DIR; the recipe exits 0 without building when
+# neither names a checkout (it is only present in the development container):
+#     oracle/build_ref.sh <reference checkout>
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${MPM_REFERENCE_DIR:-/root/reference}"
+REF="${1:-${MPM_REFERENCE_DIR:-}}"
 OUT="$HERE/_ref"
-if [ ! -d "$REF/module" ]; then
-    echo "build_ref: reference checkout not found at $REF; skipping oracle/_ref" >&2
+if [ -z "$REF" ] || [ ! -d "$REF/module" ]; then
+    echo "build_ref: no reference checkout given (argument or MPM_REFERENCE_DIR); skipping oracle/_ref" >&2
     exit 0
 fi
 mkdir -p "$OUT/obj"

@@ -6,7 +6,7 @@ scenes and stores inputs and outputs as compressed .npz files.  The reference
 checkout exists only in the development container, so the fixtures are
 committed and this script is re-run only when a case is added:
 
-    oracle/build_ref.sh && python tests/golden/make_golden.py
+    oracle/build_ref.sh <reference checkout> && python tests/golden/make_golden.py
     python tests/golden/make_golden.py --hyperelastic     # only models 2 and 3
     python tests/golden/make_golden.py --affine           # only the TPIC / APIC cases
     python tests/golden/make_golden.py --io               # only the deck / restart fixtures (tests/golden/io)
@@ -212,7 +212,7 @@ def fluid_case(name="ns_assemble"):
 
 def main():
     if not ref.available():
-        raise SystemExit("oracle/_ref/libmpmref.so missing: run oracle/build_ref.sh first")
+        raise SystemExit("oracle/_ref/libmpmref.so missing: run oracle/build_ref.sh <reference checkout> first")
     if "--hyperelastic" in sys.argv[1:]:
         hyperelastic_cases()
         return
