@@ -560,6 +560,7 @@ mpm_status mpm_gpu_sync(mpm_ctx *c) {
         // clear latched device error counters
         unsigned z[2] = {0, 0};
         cudaMemcpy(&c->d_ctl->err_oob, z, sizeof(unsigned) * 2, cudaMemcpyHostToDevice);
+        cudaMemcpy(&c->d_ctl->err_timeout, z, sizeof(unsigned), cudaMemcpyHostToDevice);
         c->latched = MPM_OK;
     }
     return s;
@@ -942,6 +943,28 @@ mpm_status mpm_gpu_get_stats(mpm_ctx *c, mpm_stats *out) {
     out->tile_misses = h.tile_misses;
     out->ntiles = c->g.nbricks;
     out->nwork = nw;
+    return MPM_OK;
+}
+
+// One CTA waits, through the same bounded mbarrier wait the bulk-copy staged
+// kernels use, on a barrier that nothing arrives on; the wait gives up after
+// limit_ns, the kernel records the timeout as those kernels do and returns.
+__global__ void k_selftest_wait(DevCtl *ctl, unsigned long long limit_ns) {
+    __shared__ __align__(8) unsigned long long bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(&bar, 0u, 1u << 30, limit_ns);
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicAdd(&ctl->err_timeout, 1u);
+}
+
+mpm_status mpm_gpu_selftest_wait(mpm_ctx *c, double seconds) {
+    if (!c || !(seconds > 0.0) || seconds > 1.0) return MPM_ERR_BAD_ARG;
+    k_selftest_wait<<<1, 32, 0, c->stream>>>(c->d_ctl, (unsigned long long)(seconds * 1e9));
+    CK(cudaGetLastError());
+    c->launches++;
     return MPM_OK;
 }
 

@@ -511,14 +511,15 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 // Bounded wait: false when the phase did not complete within `limit` polls
-// or one second of wall time, whichever comes first (try_wait may suspend
-// the thread for a system-dependent time, so the poll count alone does not
-// bound the time).
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity, unsigned limit) {
+// or `limit_ns` of wall time (one second by default), whichever comes first
+// (try_wait may suspend the thread for a system-dependent time, so the poll
+// count alone does not bound the time).
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity, unsigned limit,
+                                                  unsigned long long limit_ns = 1000000000ull) {
     const unsigned long long t0 = global_ns();
     for (unsigned i = 0; i < limit; i++) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((i & 255u) == 255u && global_ns() - t0 > 1000000000ull) return false;
+        if ((i & 255u) == 255u && global_ns() - t0 > limit_ns) return false;
     }
     return false;
 }

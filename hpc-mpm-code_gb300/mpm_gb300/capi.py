@@ -79,7 +79,7 @@ EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_s
            "mpm_gpu_get_tuning", "mpm_nn_num_params", "mpm_nn_create", "mpm_nn_destroy", "mpm_nn_set_stream",
            "mpm_nn_init_params", "mpm_nn_set_linear", "mpm_nn_set_additive", "mpm_nn_set_symmetric", "mpm_nn_set_params", "mpm_nn_get_params", "mpm_nn_forward", "mpm_nn_backward",
            "mpm_nn_num_pairs", "mpm_nn_train", "mpm_gpu_implicit_set_precond", "mpm_gpu_implicit_harvest", "mpm_gpu_implicit_apply_precond",
-           "mpm_gpu_set_graph", "mpm_gpu_set_tuning"]
+           "mpm_gpu_set_graph", "mpm_gpu_set_tuning", "mpm_gpu_selftest_wait"]
 
 
 def load(path: str | None = None):
@@ -112,6 +112,7 @@ def load(path: str | None = None):
     lib.mpm_gpu_upload_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp]
     lib.mpm_gpu_steps_host.argtypes = [C.c_void_p, C.c_int, C.c_double, _dp, _dp, _dp, _dp, _dp]
     lib.mpm_gpu_sync.argtypes = [C.c_void_p]
+    lib.mpm_gpu_selftest_wait.argtypes = [C.c_void_p, C.c_double]
     lib.mpm_gpu_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     lib.mpm_gpu_enable_kernel_timing.argtypes = [C.c_void_p, C.c_int]
     lib.mpm_gpu_autotune.argtypes = [C.c_void_p, C.c_int, C.c_double]
@@ -240,6 +241,14 @@ class GpuSolid:
 
     def sync(self):
         _chk(self.lib.mpm_gpu_sync(self.ctx), "mpm_gpu_sync")
+
+    def sync_status(self):
+        """mpm_gpu_sync's status code (0 ok) without raising."""
+        return self.lib.mpm_gpu_sync(self.ctx)
+
+    def selftest_wait(self, seconds):
+        """Test hook: a bounded device wait that runs out after `seconds` (see mpm_gpu_selftest_wait)."""
+        _chk(self.lib.mpm_gpu_selftest_wait(self.ctx, float(seconds)), "mpm_gpu_selftest_wait")
 
     # -- results ----------------------------------------------------------------
     def nodal(self, name):

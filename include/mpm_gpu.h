@@ -176,6 +176,13 @@ mpm_status mpm_gpu_steps_host(mpm_ctx *ctx, int nsteps, double facl, double *coo
                               double *stress, double *vol);
 /* Wait for the stream and return (and clear) any latched device error. */
 mpm_status mpm_gpu_sync(mpm_ctx *ctx);
+/* Test hook with no counterpart in the reference (whose waits are blocking
+ * MPI calls): launches one CTA on the context's stream that waits, through
+ * the bounded mbarrier wait of the bulk-copy staged kernels, on a barrier
+ * that nothing completes, giving up after `seconds` (0 < seconds <= 1).  The
+ * kernel records the timeout and returns, so the next mpm_gpu_sync returns
+ * MPM_ERR_DEVICE_TIMEOUT and the context stays usable afterwards. */
+mpm_status mpm_gpu_selftest_wait(mpm_ctx *ctx, double seconds);
 
 typedef struct {
     int64_t num;            /* particles */

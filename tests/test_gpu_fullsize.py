@@ -1,0 +1,93 @@
+"""Parity at the full sizes and step counts of the explicit workloads.
+
+* The 64,000-particle elastic block (32^3 cells, dx = 1e-2 m, 2x2x2
+  particles per cell with +-0.1 dx jitter, E = 1e6 Pa, nu = 0.3, gravity,
+  fixed bottom face, dt = 1e-5 s) for its full 1000 steps, PIC and FLIP,
+  against the FP64 C oracle run alongside: the GPU's FP64 mode within
+  1e-10 relative L2 on every particle field, the FP32 mode within the
+  bounds stated in the test.
+* The 4,096,000-particle spinning block (80^3 cells on a 128^3 grid,
+  dx = 4e-3 m, Gaussian velocities plus 10 rad/s, the top quarter compressed
+  to 27 particles per cell, dt = 2e-6 s) after 1000 steps, against the
+  reference's own FP64 run stored as a fixture (a seeded subsample of 32,768
+  particles, tests/golden/fullsize_spinning_block.npz from
+  tests/golden/make_fullsize.py): the FP32 path within 1e-4 relative L2 in
+  velocity (the accuracy target), with the position and stress errors
+  stated; the FP64 mode within 1e-10.
+
+Run with -s to see the measured errors.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import GOLDEN, rel_l2
+from mpm_gb300 import capi, scenes
+from oracle import port
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("x", "v", "F", "sigma", "vol")
+# FP32 bounds after 1000 steps of the 64,000-particle block, relative L2 against the FP64 oracle
+FP32_BOUNDS_BLOCK = {"x": 1e-6, "v": 1e-4, "F": 1e-5, "sigma": 1e-3, "vol": 1e-5}
+# FP32 bounds after 1000 steps of the 4,096,000-particle spinning block (subsample), against the reference
+FP32_BOUNDS_SPIN = {"x": 1e-5, "v": 1e-4, "sigma": 1e-2}
+
+
+@pytest.mark.parametrize("scheme", [scenes.PIC, scenes.FLIP])
+def test_elastic_block_64k_1000_steps_vs_oracle(scheme):
+    s = scenes.elastic_block(scheme=scheme)
+    o = port.PortSolid(s)
+    o.steps(1000)
+    want = o.particles()
+    errs = {}
+    for prec in (64, 32):
+        gpu = capi.GpuSolid(s, precision=prec)
+        gpu.steps(1000)
+        got = gpu.particles()
+        gpu.sync()
+        gpu.close()
+        errs[prec] = {k: rel_l2(got[k], want[k]) for k in FIELDS}
+    print(f"\n64k block, scheme {scheme}, 1000 steps, relative L2 vs FP64 oracle:"
+          f"\n  FP64 {errs[64]}\n  FP32 {errs[32]}")
+    assert max(errs[64].values()) <= 1e-10, errs[64]
+    for k, b in FP32_BOUNDS_BLOCK.items():
+        assert errs[32][k] <= b, (k, errs[32])
+
+
+def _fixture():
+    path = os.path.join(GOLDEN, "fullsize_spinning_block.npz")
+    if not os.path.exists(path):
+        pytest.skip("full-size fixture not generated")
+    return dict(np.load(path))
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_spinning_block_4m_1000_steps_vs_reference(precision):
+    g = _fixture()
+    s = scenes.spinning_block()
+    ids = g["ids"]
+    # the fixture was made from the same seeded scene
+    assert s.num == int(g["num"])
+    assert np.array_equal(s.coord[ids], g["x0"]) and np.array_equal(s.vel[ids], g["v0"])
+    gpu = capi.GpuSolid(s, precision=precision)
+    gpu.steps(int(g["nsteps"]))
+    p = gpu.particles()
+    gpu.sync()
+    gpu.close()
+    errs = {k: rel_l2(p[k][ids], g[k]) for k in ("x", "v", "sigma")}
+    m = s.mass
+    mom = (m[:, None] * p["v"]).sum(axis=0)
+    mom_err = float(np.linalg.norm(mom - g["tot_momentum"]) / np.linalg.norm(g["tot_momentum"]))
+    ke = 0.5 * float((m * (p["v"] ** 2).sum(axis=1)).sum())
+    ke_err = abs(ke - float(g["tot_kinetic"])) / float(g["tot_kinetic"])
+    print(f"\n4.1M spinning block, FP{precision}, {int(g['nsteps'])} steps, relative L2 vs the reference "
+          f"(subsample of {ids.size}): {errs}; momentum {mom_err:.3e}, kinetic energy {ke_err:.3e}")
+    if precision == 64:
+        assert max(errs.values()) <= 1e-10, errs
+        assert mom_err <= 1e-10 and ke_err <= 1e-10
+    else:
+        for k, b in FP32_BOUNDS_SPIN.items():
+            assert errs[k] <= b, (k, errs)
+        assert mom_err <= 1e-4 and ke_err <= 1e-4
