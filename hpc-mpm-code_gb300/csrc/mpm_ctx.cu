@@ -301,6 +301,12 @@ static mpm_status upload_particles(mpm_ctx *c, int64_t n, const double *coord, c
         double rs = fmax(fabs(s[0]) + fabs(s[5]) + fabs(s[4]),
                          fmax(fabs(s[5]) + fabs(s[1]) + fabs(s[3]), fabs(s[4]) + fabs(s[3]) + fabs(s[2])));
         vsmax = fmax(vsmax, fabs(vol0[p]) * rs);
+        // a non-finite input value refuses the load (x * 0 is NaN exactly for inf and NaN)
+        double chk = mass[p] * 0.0 + vol0[p] * 0.0 + rs * 0.0;
+        for (int k = 0; k < 3; k++) chk += coord[3 * p + k] * 0.0 + (vel ? vel[3 * p + k] * 0.0 : 0.0);
+        if (F)
+            for (int k = 0; k < 9; k++) chk += F[9 * p + k] * 0.0;
+        if (chk != chk) return MPM_ERR_NONFINITE;
     }
     if (c->fbar && sizeof(R) == 8)   // def_grad_bar = I, det_def_grad_bar = 1 (FP32 stores both minus 1: zeros)
         for (size_t p = 0; p < N; p++) {
@@ -353,7 +359,10 @@ mpm_status mpm_gpu_load_particles(mpm_ctx *c, int64_t n, const double *coord, co
     c->cur = 0;
     mpm_status s = c->precision == 64 ? upload_particles<double>(c, n, coord, vel, mass, vol0, F, stress, matid)
                                       : upload_particles<float>(c, n, coord, vel, mass, vol0, F, stress, matid);
-    if (s != MPM_OK) return s;
+    if (s != MPM_OK) {   // a refused load leaves the context without particles
+        free_particles(c);
+        return s;
+    }
     CK(cudaMemset(c->d_acc, 0, sizeof(unsigned long long) * NACC * c->g.nodec));
     CK(cudaMemset(c->d_acc2, 0, sizeof(unsigned long long) * 3 * c->g.nodec));
     CK(cudaMemset(c->d_tileflag, 0, c->g.ntiles));
@@ -660,6 +669,19 @@ __global__ void k_state_scatter(R *__restrict__ f, size_t N, size_t S, int nreal
     }
     const int *pid = (const int *)(f + nreal * S) + S;
     const size_t p = (size_t)pid[j];
+    {   // a non-finite value from the host is reported by the next synchronising call
+        double chk = 0.0;
+        if (mask & 1)
+            for (int k = 0; k < 3; k++) chk += st[ST_X * N + 3 * p + k] * 0.0;
+        if (mask & 2)
+            for (int k = 0; k < 3; k++) chk += st[ST_V * N + 3 * p + k] * 0.0;
+        if (mask & 4)
+            for (int k = 0; k < 9; k++) chk += st[ST_F * N + 9 * p + k] * 0.0;
+        if (mask & 8)
+            for (int k = 0; k < 6; k++) chk += st[ST_S * N + 6 * p + k] * 0.0;
+        if (mask & 16) chk += st[ST_VOL * N + p] * 0.0;
+        if (chk != 0.0 || chk != chk) atomicAdd(&ctl->err_nonfinite, 1u);   // x * 0 is NaN for inf and NaN
+    }
     if (mask & 1)
         for (int k = 0; k < 3; k++) f[k * S + j] = (R)st[ST_X * N + 3 * p + k];
     if (mask & 2)
@@ -680,6 +702,7 @@ __global__ void k_affine_scatter_state(R *f, size_t N, size_t S, int nreal, cons
     if (j >= N) return;
     const size_t p = (size_t)((const int *)(f + nreal * S) + S)[j];
     float bm = 0.0f;
+    double chk = 0.0;
     for (int c = 0; c < 3; c++) {
         double b = fabs((double)f[(3 + c) * S + j]);
         const double dm[3] = {d0, d1, d2};
@@ -687,9 +710,11 @@ __global__ void k_affine_scatter_state(R *f, size_t N, size_t S, int nreal, cons
             const double v = st[9 * p + 3 * c + k];
             f[(24 + 3 * c + k) * S + j] = (R)v;
             b += fabs(v) * dm[k];
+            chk += v * 0.0;
         }
         bm = fmaxf(bm, (float)b);
     }
+    if (chk != chk) atomicAdd(&ctl->err_nonfinite, 1u);
     if (bm > 0.0f) atomic_max_pos(&ctl->nxt[parity][B_VMAX], bm * 1.000001f);
 }
 

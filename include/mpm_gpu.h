@@ -107,7 +107,10 @@ const char *mpm_gpu_status_string(mpm_status s);
 
 /* ---- particles and boundary conditions ------------------------------------
  * Replaces SolidMaterialPointBase::InputPointData (module/solid/solid_data_io.cpp:13-36):
- * vel, F, stress and matid may be NULL (zero, identity, zero, material 0). */
+ * vel, F, stress and matid may be NULL (zero, identity, zero, material 0).
+ * A non-finite input value refuses the load with MPM_ERR_NONFINITE (the
+ * context is then left without particles); mpm_gpu_upload_particles and
+ * mpm_gpu_steps_host report one through the next synchronising call. */
 mpm_status mpm_gpu_load_particles(mpm_ctx *ctx, int64_t n, const double *coord, const double *vel,
                                   const double *mass, const double *vol0, const double *F, const double *stress,
                                   const int *matid);

@@ -51,6 +51,12 @@ def test_nan_upload_reports_nonfinite_then_recovers(precision):
     gpu.upload_state(vel=v)
     gpu.steps(1)
     assert gpu.sync_status() == NONFINITE
+    # a load with a non-finite value is refused outright
+    bad = np.array(s.coord, copy=True)
+    bad[5, 1] = np.inf
+    with pytest.raises(capi.MpmError) as e:
+        gpu.load(bad, s.vel, s.mass, s.vol0, matid=s.matid)
+    assert e.value.code == NONFINITE
     # the context is still usable: a fresh load runs as a new context does
     _reload(gpu, s)
     gpu.steps(3)
