@@ -171,7 +171,7 @@ def spinning_block(grid=(128, 128, 128), dx=4.0e-3, cell_lo=(24, 24, 24), cells=
 
 def cantilever(grid=(64, 64, 64), dx=1.0e-2, cell_lo=(0, 2, 2), cells=(60, 60, 60), npc=2, jitter=0.0,
                E=1.0e7, nu=0.3, rho=1000.0, dt=1.0e-3, gravity=(0.0, 0.0, -9.81), iprop=0,
-               scheme=PIC, seed=12348, mtol=1.0e-12, name="cantilever"):
+               scheme=PIC, seed=12348, mtol=1.0e-12, idimc=(1, 1, 1), name="cantilever"):
     """Implicit-solid cantilever: cells[0] x cells[1] x cells[2] block clamped at x = 0.
 
     Defaults: 64^3 grid, 60^3 cells at 2x2x2 particles per cell = 1,728,000
@@ -186,7 +186,7 @@ def cantilever(grid=(64, 64, 64), dx=1.0e-2, cell_lo=(0, 2, 2), cells=(60, 60, 6
     n = pts.shape[0]
     vp = dx ** 3 / npc ** 3
     scene = Scene(
-        xyelem=tuple(grid), xymin=xymin, dxy=dxy, idimc=(1, 1, 1), npxye=(npc, npc, npc),
+        xyelem=tuple(grid), xymin=xymin, dxy=dxy, idimc=tuple(idimc), npxye=(npc, npc, npc),
         dt=dt, mtol=mtol, gravity=tuple(gravity),
         iprop=np.array([iprop], dtype=np.int32), mat_prop=np.array([[E, nu, 0.0]]),
         coord=pts, vel=np.zeros((n, 3)), mass=np.full(n, rho * vp), vol0=np.full(n, vp),

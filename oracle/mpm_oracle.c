@@ -368,8 +368,10 @@ static void mat_neo_hookean(mo_ctx *c, double *sts, const double FF[3][3], const
     }
 }
 
-/* MatStVk, module/solid/constitutive_model.cpp:122-185 (stress part) */
-static void mat_stvk(double *sts, const double FF[3][3], const double *mp, double jac) {
+/* MatStVk, module/solid/constitutive_model.cpp:122-185; with `implicit` also
+ * the 6x6 tangent lambda' be(x)be + mu' (be_ik be_jl + be_il be_jk), lambda' =
+ * lambda / J, mu' = mu / J, in the Voigt slots IDM (:160-183) */
+static void mat_stvk(mo_ctx *c, double *sts, const double FF[3][3], const double *mp, double jac, int implicit) {
     double yng = mp[0], nu = mp[1];
     double lmd = nu * yng / ((1.0 + nu) * (1.0 - 2.0 * nu));
     double mu = yng / (2.0 * (1.0 + nu));
@@ -383,11 +385,24 @@ static void mat_stvk(double *sts, const double FF[3][3], const double *mp, doubl
         for (int j = 0; j < 3; j++) sig[i][j] = (mu * be2[i][j] + (lmd * tr_gls - mu) * be[i][j]) / jac;
     sts[0] = sig[0][0]; sts[1] = sig[1][1]; sts[2] = sig[2][2];
     sts[3] = sig[1][2]; sts[4] = sig[0][2]; sts[5] = sig[0][1];
+    if (implicit) {
+        double c0 = lmd / jac, c1 = mu / jac;
+        memset(c->stif, 0, sizeof(c->stif));
+        for (int l = 0; l < 3; l++)
+            for (int k = 0; k < 3; k++)
+                for (int j = 0; j < 3; j++)
+                    for (int i = 0; i < 3; i++)
+                        c->stif[IDM[i][j]][IDM[k][l]] =
+                            c0 * (be[i][j] * be[k][l]) + c1 * (be[i][k] * be[j][l] + be[i][l] * be[j][k]);
+    }
 }
 
-/* MatMooneyRivlin, module/solid/constitutive_model.cpp:187-285 (stress part);
- * mat_prop = {c1, c2, bulk} */
-static void mat_mooney_rivlin(double *sts, const double FF[3][3], const double *mp, double jac) {
+/* MatMooneyRivlin, module/solid/constitutive_model.cpp:187-285; mat_prop =
+ * {c1, c2, bulk}.  With `implicit` also the 6x6 tangent of :235-283: the
+ * volumetric part (bulk / J) I(x)I - 2 hp I4sym, the deviatoric-stress part
+ * -2/3 (dev(s) (x) I + I (x) dev(s)) and the isochoric part (four terms). */
+static void mat_mooney_rivlin(mo_ctx *c, double *sts, const double FF[3][3], const double *mp, double jac,
+                              int implicit) {
     double c1 = mp[0], c2 = mp[1], bulk = mp[2];
     double fi[3][3], be[3][3], be2[3][3], sig[3][3];
     for (int i = 0; i < 3; i++)
@@ -405,6 +420,29 @@ static void mat_mooney_rivlin(double *sts, const double FF[3][3], const double *
     }
     sts[0] = sig[0][0]; sts[1] = sig[1][1]; sts[2] = sig[2][2];
     sts[3] = sig[1][2]; sts[4] = sig[0][2]; sts[5] = sig[0][1];
+    if (implicit) {
+        double trs = sig[0][0] + sig[1][1] + sig[2][2];
+        double dev[3][3];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) dev[i][j] = sig[i][j] - trs / 3.0 * (i == j);
+        memset(c->stif, 0, sizeof(c->stif));
+        for (int l = 0; l < 3; l++)
+            for (int k = 0; k < 3; k++)
+                for (int j = 0; j < 3; j++)
+                    for (int i = 0; i < 3; i++) {
+                        double dij = (i == j), dkl = (k == l), dik = (i == k), djl = (j == l), dil = (i == l),
+                               djk = (j == k);
+                        double i4 = 0.5 * (dik * djl + dil * djk);
+                        double aij = i1 * be[i][j] - be2[i][j], akl = i1 * be[k][l] - be2[k][l];
+                        double c_hp = bulk / jac * (dij * dkl) - 2.0 * hp * i4;
+                        double c_dev = -2.0 / 3.0 * (dev[i][j] * dkl + dij * dev[k][l]);
+                        double t1 = 4.0 / (3.0 * jac) * (c1 * i1 + 2.0 * c2 * i2) * (i4 - (1.0 / 3.0) * dij * dkl);
+                        double t2 = 4.0 * c2 / jac * (be[i][j] * be[k][l] - 0.5 * (be[i][k] * be[j][l] + be[i][l] * be[j][k]));
+                        double t3 = -4.0 * c2 / (3.0 * jac) * (aij * dkl + dij * akl);
+                        double t4 = 8.0 * c2 * i2 / (9.0 * jac) * dij * dkl;
+                        c->stif[IDM[i][j]][IDM[k][l]] = c_hp + c_dev + (t1 + t2 + t3 + t4);
+                    }
+    }
 }
 
 /* Weakly compressible Newtonian fluid (material model 4, no counterpart in
@@ -440,10 +478,10 @@ static void update_stress(mo_ctx *c, int p, double *sts, const double FF[3][3], 
     } else if (model == 1) {
         /* UpdateStress passes det_def_grad and det_def_grad_bar (constitutive_model.cpp:287-297) */
         mat_neo_hookean(c, sts, FF, mp, c->jac[p], c->fbar ? c->jbar[p] : c->jac[p], implicit);
-    } else if (model == 2 && !implicit) {
-        mat_stvk(sts, FF, mp, c->jac[p]);
-    } else if (model == 3 && !implicit) {
-        mat_mooney_rivlin(sts, FF, mp, c->jac[p]);
+    } else if (model == 2) {
+        mat_stvk(c, sts, FF, mp, c->jac[p], implicit);
+    } else if (model == 3) {
+        mat_mooney_rivlin(c, sts, FF, mp, c->jac[p], implicit);
     } else if (model == 4 && !implicit) {
         mat_tait(c, p, sts, d, mp);
     }

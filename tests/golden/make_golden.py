@@ -12,6 +12,7 @@ committed and this script is re-run only when a case is added:
     python tests/golden/make_golden.py --io               # only the deck / restart fixtures (tests/golden/io)
     python tests/golden/make_golden.py --fbar             # only the F-bar cases
     python tests/golden/make_golden.py --fluid            # only the stabilized fluid assembly
+    python tests/golden/make_golden.py --implicit2        # only the quadratic / StVK / Mooney-Rivlin implicit cases
 """
 from __future__ import annotations
 
@@ -100,6 +101,29 @@ def hyperelastic_cases():
     s.mat_prop[:] = [[1.5e5, 0.42e5, 8.33e5]]
     s.vel[:] = rng.normal(0.0, 0.3, size=s.vel.shape)
     explicit_case("explicit_mooney_rivlin", s, nsteps=10)
+
+
+def implicit_extra_cases():
+    """Implicit solids beyond linear shape functions and models 0 / 1: a
+    beam with the shape orders of the reference's own solid case
+    (data/generate/solid/input.txt: FLIP, Neo-Hookean, idimc 2 1 2, Newton),
+    a St.Venant-Kirchhoff cantilever (linear shapes, Newton) and a
+    Mooney-Rivlin cantilever on quadratic B-splines in every direction
+    (Newton); each with a random initial velocity so that the first system
+    already carries stress."""
+    rng = np.random.default_rng(20261210)
+    s = scenes.cantilever(grid=(10, 4, 8), cells=(6, 2, 4), cell_lo=(0, 1, 2), iprop=1, idimc=(2, 1, 2),
+                          scheme=scenes.FLIP, seed=131)
+    s.vel[:] = rng.normal(0.0, 0.05, size=s.vel.shape)
+    implicit_case("implicit_beam_quadratic", s, nr_flag=True, nsteps=3)
+    s = scenes.cantilever(grid=(10, 8, 8), cells=(6, 4, 4), cell_lo=(0, 2, 2), iprop=2, seed=132)
+    s.vel[:] = rng.normal(0.0, 0.05, size=s.vel.shape)
+    implicit_case("implicit_stvk", s, nr_flag=True, nsteps=3)
+    # Mooney-Rivlin: c1, c2 and the bulk modulus of E = 1e7, nu = 0.3 (c1 + c2 = mu / 2)
+    s = scenes.cantilever(grid=(8, 6, 6), cells=(5, 3, 3), cell_lo=(0, 1, 1), iprop=3, idimc=(2, 2, 2), seed=133)
+    s.mat_prop[:] = [[1.5e6, 0.42e6, 8.33e6]]
+    s.vel[:] = rng.normal(0.0, 0.05, size=s.vel.shape)
+    implicit_case("implicit_mooney_rivlin", s, nr_flag=True, nsteps=3)
 
 
 def affine_cases():
@@ -225,6 +249,9 @@ def main():
     if "--fluid" in sys.argv[1:]:
         fluid_case()
         return
+    if "--implicit2" in sys.argv[1:]:
+        implicit_extra_cases()
+        return
     if "--fbar" in sys.argv[1:]:
         fbar_cases()
         return
@@ -255,6 +282,7 @@ def main():
     io_cases()
     fbar_cases()
     fluid_case()
+    implicit_extra_cases()
 
 
 if __name__ == "__main__":

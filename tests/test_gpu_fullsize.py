@@ -30,7 +30,10 @@ pytestmark = pytest.mark.gpu
 
 FIELDS = ("x", "v", "F", "sigma", "vol")
 # FP32 bounds after 1000 steps of the 64,000-particle block, relative L2 against the FP64 oracle
-FP32_BOUNDS_BLOCK = {"x": 1e-6, "v": 1e-4, "F": 1e-5, "sigma": 1e-3, "vol": 1e-5}
+# (measured on a GB300: PIC x 7.0e-6, v 2.4e-5, F 4.3e-8, sigma 4.6e-5, vol 5.9e-8;
+#  FLIP x 4.3e-6, v 1.3e-4, F 1.4e-7, sigma 9.5e-5, vol 1.2e-7; the position error is
+#  the rounding of FP32 coordinates near 0.1 m under increments of dt v ~ 1e-7 m)
+FP32_BOUNDS_BLOCK = {"x": 2e-5, "v": 5e-4, "F": 1e-6, "sigma": 5e-4, "vol": 1e-6}
 # FP32 bounds after 1000 steps of the 4,096,000-particle spinning block (subsample), against the reference
 FP32_BOUNDS_SPIN = {"x": 1e-5, "v": 1e-4, "sigma": 1e-2}
 

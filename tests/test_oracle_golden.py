@@ -15,7 +15,7 @@ TOL = 1.0e-12
 EXPLICIT = ["explicit_pic", "explicit_flip", "explicit_quadratic", "explicit_neohookean", "explicit_stvk",
             "explicit_mooney_rivlin", "explicit_tpic", "explicit_apic", "explicit_tpic_quadratic",
             "explicit_apic_quadratic", "explicit_fbar_linear", "explicit_fbar_neohookean"]
-IMPLICIT = ["implicit_linear", "implicit_neohookean"]
+IMPLICIT = ["implicit_linear", "implicit_neohookean", "implicit_beam_quadratic", "implicit_stvk", "implicit_mooney_rivlin"]
 
 
 @pytest.mark.parametrize("name", EXPLICIT)
