@@ -2818,8 +2818,9 @@ static StepArgs<R> make_args(mpm_ctx *c) {
 }
 
 static bool use_cell_kernels(const mpm_ctx *c) {
-    return c->cell_scatter && !c->affine && c->precision == 32 && c->g.order[0] == 1 && c->g.order[1] == 1 &&
-           c->g.order[2] == 1;
+    // the per-cell kernels carry the explicit fields only (no particle acceleration of the implicit solid)
+    return c->cell_scatter && !c->affine && c->precision == 32 && c->nreal != 27 && c->g.order[0] == 1 &&
+           c->g.order[1] == 1 && c->g.order[2] == 1;
 }
 
 static int num_sms() {

@@ -18,18 +18,29 @@
 //   Node2Particle            var_trans_solid_implicit.cpp:106-167,
 //                            nonlinear_time_integration.cpp:73-96    -> k_imp_g2p, k_imp_shift
 //
-// Matrix storage: for control point n and stencil slot s (the 27 neighbours
-// n + (dx, dy, dz), dx,dy,dz in {-1,0,1}, s = (dx+1) + 3 (dy+1) + 9 (dz+1)),
-// the 3x3 block entry q = s * 9 + 3 a + b lives at A[aidx(q, n)], tiled by
-// 32 control points and by pairs of entries:
-// ((n / 32) * 122 + q / 2) * 64 + (n % 32) * 2 + q % 2.  A thread reads
-// entry pairs as 16-byte loads and a warp reading its 32 nodes' 243 values
-// walks one contiguous 62 KB range (coalesced and DRAM-page friendly); no
-// column indices (the grid is structured).
+// Matrix storage: for control point n and stencil slot s (the neighbours
+// n + (dx, dy, dz) with |dx| <= rx, |dy| <= ry, |dz| <= rz, where the radius
+// of an axis is its shape order: 1 for linear shape functions, 2 for the
+// quadratic B-spline, so 27, 75 or 125 slots; s = (dx+rx) + sx ((dy+ry) +
+// sy (dz+rz)), sx = 2 rx + 1), the 3x3 block entry q = s * 9 + 3 a + b lives
+// at A[aidx(q, n, qp)], tiled by 32 control points and by pairs of entries:
+// ((n / 32) * qp + q / 2) * 64 + (n % 32) * 2 + q % 2, qp = ceil(9 ns / 2).
+// A thread reads entry pairs as one vector load and a warp reading its 32
+// nodes' values walks one contiguous range (coalesced and DRAM-page
+// friendly); no column indices (the grid is structured).
+//
+// Precision: a context of precision 64 computes and stores everything in
+// FP64 (the parity mode).  Precision 32 keeps the particles (F as H = F - I),
+// the assembly arithmetic and the matrix in FP32 and the matvec of the
+// Krylov iterations in FP32 arithmetic; the Krylov vectors, their inner
+// products and norms, the true residual b - A x (the FP32-stored matrix
+// applied in FP64 arithmetic), the Newton check and the nodal kinematics
+// stay FP64.
 #include <cmath>
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "mpm_device.cuh"
@@ -42,13 +53,15 @@ mpm_status run_p2g(mpm_ctx *c, double facl);
 struct ImpState {
     int nr_flag = 0;
     double alpha_f = 1, alpha_m = 1, gamma = 0.5, beta = 0.25, nb[6] = {0};
-    double *A = nullptr;                   // 243 values per node, tiled by 32 nodes (aidx)
+    int prec = 64;                         // 64: FP64 operator; 32: FP32 particles, assembly and matrix
+    int qp = 122;                          // entry pairs per node of the stencil matrix (aidx)
+    void *A = nullptr;                     // 9 ns values per node (FP64 or FP32), tiled by 32 nodes (aidx)
     double *adiag = nullptr, *b = nullptr;  // 3 * nodec
     double *x = nullptr, *r = nullptr, *p = nullptr, *Ap = nullptr, *xs = nullptr;
     double *ndispl = nullptr, *nvel = nullptr, *naccel = nullptr, *naccel_k = nullptr;
     double *nmass = nullptr, *nvof = nullptr, *nei = nullptr;
-    double *stress_k = nullptr;            // 6 * num, Newton stress of the step
-    double *geup = nullptr;                // 3 * num
+    void *stress_k = nullptr;              // 6 * num, Newton stress of the step (particle precision)
+    void *geup = nullptr;                  // 3 * num (particle precision)
     double *part = nullptr;                // reduction partials
     double *scal = nullptr;                // device scalars
     double *h_scal = nullptr;              // pinned mirror
@@ -91,6 +104,9 @@ struct ImpArgs {
     int nr_flag;
     int shifting;
     int scheme;
+    int rad[3];   // stencil radius per axis (the shape order)
+    int ns;       // stencil slots (2 rad + 1 per axis)
+    int qp;       // entry pairs per node (aidx)
     int64_t num;
     const unsigned char *bcflag;
     const double *bcval;
@@ -99,10 +115,10 @@ struct ImpArgs {
     const double *matprop;
 };
 
-__host__ __device__ __forceinline__ size_t aidx(int q, int n) {
-    return (((size_t)(n >> 5) * 122 + (size_t)(q >> 1)) << 6) + (size_t)((n & 31) << 1) + (size_t)(q & 1);
+__host__ __device__ __forceinline__ size_t aidx(int q, int n, int qp) {
+    return (((size_t)(n >> 5) * qp + (size_t)(q >> 1)) << 6) + (size_t)((n & 31) << 1) + (size_t)(q & 1);
 }
-static size_t a_size(int nodec) { return (size_t)((nodec + 31) / 32) * 32 * 244; }
+static size_t a_size(int nodec, int qp) { return (size_t)((nodec + 31) / 32) * 64 * (size_t)qp; }
 
 static ImpArgs imp_args(mpm_ctx *c) {
     ImpArgs a;
@@ -127,6 +143,12 @@ static ImpArgs imp_args(mpm_ctx *c) {
     a.nr_flag = s->nr_flag;
     a.shifting = c->shifting;
     a.scheme = c->scheme;
+    a.ns = 1;
+    for (int d = 0; d < 3; d++) {
+        a.rad[d] = c->g.order[d];
+        a.ns *= 2 * a.rad[d] + 1;
+    }
+    a.qp = (9 * a.ns + 1) / 2;
     a.num = c->num;
     a.bcflag = c->d_bcflag;
     a.bcval = (const double *)c->d_bcval;
@@ -136,15 +158,18 @@ static ImpArgs imp_args(mpm_ctx *c) {
     return a;
 }
 
+// Particle fields of an implicit context (precision R; FP32 stores H = F - I in F)
+template <typename R>
 struct PView {
-    double *x[3], *v[3], *F[9], *s[6], *m, *vol0, *vol, *acc[3];
+    R *x[3], *v[3], *F[9], *s[6], *m, *vol0, *vol, *acc[3];
     int *matid;
 };
 
-static PView pview(mpm_ctx *c) {
-    PView v;
+template <typename R>
+static PView<R> pview(mpm_ctx *c) {
+    PView<R> v;
     size_t n = c->pstride;
-    double *f = (double *)c->pbuf[c->cur];
+    R *f = (R *)c->pbuf[c->cur];
     for (int k = 0; k < 3; k++) v.x[k] = f + k * n;
     for (int k = 0; k < 3; k++) v.v[k] = f + (3 + k) * n;
     for (int k = 0; k < 9; k++) v.F[k] = f + (6 + k) * n;
@@ -163,29 +188,42 @@ __device__ __forceinline__ void node_ijk(int n, const int *nnc, int &i, int &j, 
     k = n / (nnc[0] * nnc[1]);
 }
 
-// Linear shape functions at x in element (cx, cy, cz): weights and gradients
-// of the 8 nodes in MakSf order (module/shape_function.cpp:28-110).
-__device__ __forceinline__ void shape8(const ImpArgs &a, const double *x, int &cx, int &cy, int &cz, double *N,
-                                       double (*dN)[3], int *nid, bool &oob) {
-    KGeom<double> g;
+template <typename R>
+__device__ __forceinline__ KGeom<R> kgeom(const ImpArgs &a) {
+    KGeom<R> g;
     for (int d = 0; d < 3; d++) {
-        g.xmin[d] = a.xmin[d];
-        g.dx[d] = a.dx[d];
-        g.inv_dx[d] = a.inv_dx[d];
+        g.xmin[d] = (R)a.xmin[d];
+        g.dx[d] = (R)a.dx[d];
+        g.inv_dx[d] = (R)a.inv_dx[d];
         g.nel[d] = a.nel[d];
         g.nnc[d] = a.nnc[d];
+        g.ntile[d] = 0;
     }
-    cx = cell_of(x[0], g, 0, oob);
-    cy = cell_of(x[1], g, 1, oob);
-    cz = cell_of(x[2], g, 2, oob);
-    Axis<double, 1> ax, ay, az;
-    axis_linear<double>(x[0], g.xmin[0], g.dx[0], g.inv_dx[0], cx, ax);
-    axis_linear<double>(x[1], g.xmin[1], g.dx[1], g.inv_dx[1], cy, ay);
-    axis_linear<double>(x[2], g.xmin[2], g.dx[2], g.inv_dx[2], cz, az);
+    g.nodec = a.nodec;
+    return g;
+}
+
+// Shape functions at x (MakSf, module/shape_function.cpp:8-119) for shape
+// orders OX, OY, OZ: weights, gradients and control-point ids of the
+// (OX+1)(OY+1)(OZ+1) nodes in MakSf order (x fastest), and each node's
+// offset inside the element's node box (for the stencil slot).
+template <typename R, int OX, int OY, int OZ>
+__device__ __forceinline__ void shape_nodes(const ImpArgs &a, const KGeom<R> &g, const R *x, R *N, R (*dN)[3],
+                                            int *nid, bool &oob) {
+    const int cx = cell_of(x[0], g, 0, oob), cy = cell_of(x[1], g, 1, oob), cz = cell_of(x[2], g, 2, oob);
+    Axis<R, OX> ax;
+    Axis<R, OY> ay;
+    Axis<R, OZ> az;
+    axis_eval<R, OX>(x[0], g, 0, cx, ax);
+    axis_eval<R, OY>(x[1], g, 1, cy, ay);
+    axis_eval<R, OZ>(x[2], g, 2, cz, az);
     int id = 0;
-    for (int k = 0; k < 2; k++)
-        for (int j = 0; j < 2; j++)
-            for (int i = 0; i < 2; i++) {
+#pragma unroll
+    for (int k = 0; k <= OZ; k++)
+#pragma unroll
+        for (int j = 0; j <= OY; j++)
+#pragma unroll
+            for (int i = 0; i <= OX; i++) {
                 N[id] = ax.w[i] * ay.w[j] * az.w[k];
                 dN[id][0] = ax.dw[i] * ay.w[j] * az.w[k];
                 dN[id][1] = ax.w[i] * ay.dw[j] * az.w[k];
@@ -238,72 +276,209 @@ __global__ void k_imp_predict(ImpArgs a, double *ndispl, const double *nvel, con
 }
 
 // ------------------------------------------------------------- assembly
+// Material tangent of one particle in a factored form that the pair loop
+// contracts with the scaled gradient a of the row node and the gradient b of
+// the column node (K_ij = sum_kl a_k C_ikjl b_l of ComputeTangentModulus,
+// solve_solid_implicit.cpp:34-63, written out for each model's C):
+//   isotropic (models -1, 0, 1; C = lambda' I(x)I + 2 mu' I4sym):
+//       K = lambda' a b^T + mu' b a^T + mu' (a.b) I
+//   general (models 2, 3):
+//       K = (G a) b^T + a (G' b)^T + alpha (a.b) I + gam b a^T
+//           + eps (B a)(B b)^T + beta (a.B b) B + delta (B b)(B a)^T
+// plus, with NR_flag, the geometric term ((sigma a).b) I.
+template <typename R>
+struct Tangent {
+    bool general;
+    R lam, mu;                    // isotropic
+    R B[3][3], G[3][3], Gp[3][3];  // general
+    R alpha, gam, eps, beta, delta;
+};
+
+// St.Venant-Kirchhoff (MatStVk's stif_mat, constitutive_model.cpp:160-183):
+// C = lambda' b(x)b + mu' (b_ik b_jl + b_il b_jk), lambda' = lambda / J, mu' = mu / J, b = F F^T.
+template <typename R>
+__device__ __forceinline__ void tangent_stvk(Tangent<R> &t, const R F[3][3], R J, R E, R nu) {
+    const R rd = (R)1 / (((R)1 + nu) * ((R)1 - (R)2 * nu));
+    const R ij = (R)1 / J;
+    t.general = true;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            t.B[i][j] = F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2];
+            t.G[i][j] = (R)0;
+            t.Gp[i][j] = (R)0;
+        }
+    t.alpha = t.gam = (R)0;
+    t.eps = nu * E * rd * ij;
+    t.beta = t.delta = (R)0.5 * E * ((R)1 - (R)2 * nu) * rd * ij;
+}
+
+// Mooney-Rivlin (MatMooneyRivlin's stif_mat, constitutive_model.cpp:235-283)
+// with B the isochoric b, I1, I2 its invariants, hp = bulk ln J / J, s the
+// Cauchy stress, A = I1 B - B^2:
+//   G  = (bulk / J - t1 / 3 + c4) I - 2/3 dev(s) - c3 A,  G' = -2/3 dev(s) - c3 A,
+//   alpha = gam = t1 / 2 - hp,  eps = c2',  beta = delta = -c2' / 2,
+// t1 = 4 (c1 I1 + 2 c2 I2) / (3 J), c2' = 4 c2 / J, c3 = 4 c2 / (3 J), c4 = 8 c2 I2 / (9 J).
+template <typename R>
+__device__ __forceinline__ void tangent_mooney_rivlin(Tangent<R> &t, const R F[3][3], R J, R lnJ, const R *s, R c1,
+                                                      R c2, R bulk) {
+    const R ij = (R)1 / J;
+    const R k2 = exp((R)(-2.0 / 3.0) * lnJ);   // J^(-2/3)
+    R B2[3][3];
+    t.general = true;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) t.B[i][j] = k2 * (F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2]);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) B2[i][j] = t.B[i][0] * t.B[0][j] + t.B[i][1] * t.B[1][j] + t.B[i][2] * t.B[2][j];
+    const R i1 = t.B[0][0] + t.B[1][1] + t.B[2][2];
+    const R i2 = (R)0.5 * (i1 * i1 - (B2[0][0] + B2[1][1] + B2[2][2]));
+    const R hp = bulk * lnJ * ij;
+    const R t1 = (R)4 * (c1 * i1 + (R)2 * c2 * i2) * ij / (R)3;
+    const R c2p = (R)4 * c2 * ij, c3 = c2p / (R)3, c4 = (R)8 * c2 * i2 * ij / (R)9;
+    const R sg[3][3] = {{s[0], s[5], s[4]}, {s[5], s[1], s[3]}, {s[4], s[3], s[2]}};
+    const R tr3 = (s[0] + s[1] + s[2]) / (R)3;
+    const R g0 = bulk * ij - t1 / (R)3 + c4;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const R dev = sg[i][j] - (i == j ? tr3 : (R)0);
+            const R Aij = i1 * t.B[i][j] - B2[i][j];
+            t.Gp[i][j] = (R)(-2.0 / 3.0) * dev - c3 * Aij;
+            t.G[i][j] = t.Gp[i][j] + (i == j ? g0 : (R)0);
+        }
+    t.alpha = t.gam = (R)0.5 * t1 - hp;
+    t.eps = c2p;
+    t.beta = t.delta = (R)(-0.5) * c2p;
+}
+
 // One thread per particle (AssembleSystem, solve_solid_implicit.cpp:123-189):
 // UpdateDefGrad with alpha_f, the stress of the Newton iterate, the gradient
-// correction dN <- dN dF^-1, then 8x8 tangent blocks + lumped mass and the
-// internal/external force into the RHS, with FP64 atomics.
-__global__ void __launch_bounds__(128) k_imp_assemble(ImpArgs a, PView P, const double *ndispl, double *stress_k,
-                                                      double *A, double *b) {
+// correction dN <- dN dF^-1, then the tangent blocks of each unordered node
+// pair once (K_ba = K_ab^T: every C here has the major symmetry) + lumped
+// mass, and the internal/external force into the RHS, with atomics.  R is
+// the particle precision and the precision of the arithmetic and of A; the
+// RHS is summed in FP64.
+template <typename R, int OX, int OY, int OZ>
+__global__ void __launch_bounds__(128) k_imp_assemble(ImpArgs a, PView<R> P, const double *ndispl, R *stress_k,
+                                                      R *A, double *b) {
+    constexpr int NX = OX + 1, NY = OY + 1, NZ = OZ + 1, NE = NX * NY * NZ;
+    constexpr int SX = 2 * OX + 1, SY = 2 * OY + 1, NS = SX * SY * (2 * OZ + 1);
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= a.num) return;
     const size_t N = (size_t)a.nodec, NP = (size_t)a.num;
-    double x[3] = {P.x[0][p], P.x[1][p], P.x[2][p]};
-    int cx, cy, cz, nid[8];
-    double Nw[8], dN[8][3];
+    const KGeom<R> g = kgeom<R>(a);
+    const R x[3] = {P.x[0][p], P.x[1][p], P.x[2][p]};
+    int nid[NE];
+    R Nw[NE], dN[NE][3];
     bool oob = false;
-    shape8(a, x, cx, cy, cz, Nw, dN, nid, oob);
-    // ComputeDeltaDefGrad with alpha_f (material_point.cpp:127-151)
-    double d[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-    for (int q = 0; q < 8; q++)
+    shape_nodes<R, OX, OY, OZ>(a, g, x, Nw, dN, nid, oob);
+    // ComputeDeltaDefGrad with alpha_f (material_point.cpp:127-151): d = I + Dm
+    R Dm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int q = 0; q < NE; q++)
         for (int r = 0; r < 3; r++) {
-            const double u = ndispl[r * N + nid[q]];
-            for (int c = 0; c < 3; c++) d[r][c] += dN[q][c] * u;
+            const R u = (R)ndispl[r * N + nid[q]];
+            for (int c = 0; c < 3; c++) Dm[r][c] += dN[q][c] * u;
         }
-    for (int r = 0; r < 3; r++) {
-        for (int c = 0; c < 3; c++) d[r][c] *= a.af;
-        d[r][r] += 1.0;
+    const R af = (R)a.af;
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) Dm[r][c] *= af;
+    R d[3][3];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) d[r][c] = Dm[r][c] + (r == c ? (R)1 : (R)0);
+    // UpdateDefGrad: Fn = d F.  FP32 stores H = F - I and forms
+    // Hn = Dm + H + Dm H, J - 1 = det(I + Hn) - 1 without the rounding of numbers near 1.
+    R Fn[3][3], Hn[3][3], J, jm1;
+    if constexpr (sizeof(R) == 8) {
+        R F[3][3];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) F[r][c] = P.F[3 * r + c][p];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) {
+                R sum = 0.0;
+                for (int k = 0; k < 3; k++) sum += d[r][k] * F[k][c];
+                Fn[r][c] = sum;
+            }
+        J = det3(Fn);
+        jm1 = J - (R)1;
+    } else {
+        R H[3][3];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) H[r][c] = P.F[3 * r + c][p];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) {
+                R sum = Dm[r][c] + H[r][c];
+                for (int k = 0; k < 3; k++) sum += Dm[r][k] * H[k][c];
+                Hn[r][c] = sum;
+            }
+        jm1 = det_ipm1(Hn);
+        J = (R)1 + jm1;
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) Fn[r][c] = Hn[r][c] + (r == c ? (R)1 : (R)0);
     }
-    double F[3][3], Fn[3][3];
-    for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++) F[r][c] = P.F[3 * r + c][p];
-    for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++) {
-            double s = 0.0;
-            for (int k = 0; k < 3; k++) s += d[r][k] * F[k][c];
-            Fn[r][c] = s;
-        }
-    const double J = det3(Fn);
-    const double vol = J * P.vol0[p];
-    // UpdateConstitutiveModel on the Newton stress (constitutive_model.cpp:16-120)
-    double sk[6];
+    const R vol = J * P.vol0[p];
+    // UpdateConstitutiveModel on the Newton stress (constitutive_model.cpp:16-305)
+    R sk[6];
     for (int k = 0; k < 6; k++) sk[k] = stress_k[k * NP + p];
     const int mid = P.matid[p];
     const int model = a.iprop[mid];
-    const double E = a.matprop[3 * mid], nu = a.matprop[3 * mid + 1];
-    double lam = 0.0, mu = 0.0;
+    const R E = (R)a.matprop[3 * mid], nu = (R)a.matprop[3 * mid + 1], m3 = (R)a.matprop[3 * mid + 2];
+    Tangent<R> t;
+    t.general = false;
+    t.lam = t.mu = (R)0;
     if (model == 0) {
-        double Dm[3][3];
+        // the strain increment: FP64 takes d - I as the reference does, FP32 the exact Dm
+        R De[3][3];
         for (int r = 0; r < 3; r++)
-            for (int c = 0; c < 3; c++) Dm[r][c] = (r == c) ? d[r][c] - 1.0 : d[r][c];
-        lin_elast_update(sk, Dm, E, nu);
-        lam = E * nu / ((1.0 - 2.0 * nu) * (1.0 + nu));
-        mu = E / (2.0 * (1.0 + nu));
+            for (int c = 0; c < 3; c++)
+                De[r][c] = sizeof(R) == 8 ? (r == c ? d[r][c] - (R)1 : d[r][c]) : Dm[r][c];
+        lin_elast_update(sk, De, E, nu);
+        t.lam = E * nu / (((R)1 - (R)2 * nu) * ((R)1 + nu));
+        t.mu = E / ((R)2 * ((R)1 + nu));
     } else if (model == 1) {
-        const double lnj = neo_hookean_stress(sk, Fn, J, E, nu);
-        const double rd = 1.0 / ((1.0 + nu) * (1.0 - 2.0 * nu));
-        const double lmd = nu * E * rd;
-        const double mu0 = 0.5 * E * (1.0 - 2.0 * nu) * rd;
-        const double ij = 1.0 / J;
-        lam = lmd * ij;
-        mu = (mu0 - lmd * lnj) * ij;
+        R lnj;
+        if constexpr (sizeof(R) == 8) {
+            lnj = neo_hookean_stress(sk, Fn, J, E, nu);
+        } else {
+            neo_hookean_stress_h(sk, Hn, jm1, E, nu);
+            lnj = log1pf(jm1);
+        }
+        const R rd = (R)1 / (((R)1 + nu) * ((R)1 - (R)2 * nu));
+        const R lmd = nu * E * rd;
+        const R mu0 = (R)0.5 * E * ((R)1 - (R)2 * nu) * rd;
+        const R ij = (R)1 / J;
+        t.lam = lmd * ij;
+        t.mu = (mu0 - lmd * lnj) * ij;
+    } else if (model == 2) {
+        if constexpr (sizeof(R) == 8) {
+            stvk_stress(sk, Fn, J, E, nu);
+        } else {
+            stvk_stress_h(sk, Hn, jm1, E, nu);
+        }
+        tangent_stvk(t, Fn, J, E, nu);
+    } else if (model == 3) {   // mat_prop = {c1, c2, bulk}
+        R lnj;
+        if constexpr (sizeof(R) == 8) {
+            mooney_rivlin_stress(sk, Fn, J, E, nu, m3);
+            lnj = log(J);
+        } else {
+            mooney_rivlin_stress_h(sk, Hn, jm1, E, nu, m3);
+            lnj = log1pf(jm1);
+        }
+        tangent_mooney_rivlin(t, Fn, J, lnj, sk, E, nu, m3);
     } else {
-        for (int k = 0; k < 6; k++) sk[k] = 0.0;
+        for (int k = 0; k < 6; k++) sk[k] = (R)0;
     }
     for (int k = 0; k < 6; k++) stress_k[k * NP + p] = sk[k];
-    // ImplicitDsfCorr: dN <- dN dF^-1 (material_point.cpp:153-172)
-    double di[3][3];
+    // ImplicitDsfCorr: dN <- dN d^-1 (material_point.cpp:153-172)
+    R di[3][3];
     {
-        const double det = 1.0 / det3(d);
+        const R det = (R)1 / det3(d);
         di[0][0] = (d[1][1] * d[2][2] - d[1][2] * d[2][1]) * det;
         di[0][1] = (d[0][2] * d[2][1] - d[0][1] * d[2][2]) * det;
         di[0][2] = (d[0][1] * d[1][2] - d[0][2] * d[1][1]) * det;
@@ -314,92 +489,129 @@ __global__ void __launch_bounds__(128) k_imp_assemble(ImpArgs a, PView P, const 
         di[2][1] = (d[0][1] * d[2][0] - d[0][0] * d[2][1]) * det;
         di[2][2] = (d[0][0] * d[1][1] - d[0][1] * d[1][0]) * det;
     }
-    for (int q = 0; q < 8; q++) {
-        double t[3];
-        for (int c = 0; c < 3; c++) t[c] = dN[q][0] * di[0][c] + dN[q][1] * di[1][c] + dN[q][2] * di[2][c];
-        for (int c = 0; c < 3; c++) dN[q][c] = t[c];
+    for (int q = 0; q < NE; q++) {
+        R tq[3];
+        for (int c = 0; c < 3; c++) tq[c] = dN[q][0] * di[0][c] + dN[q][1] * di[1][c] + dN[q][2] * di[2][c];
+        for (int c = 0; c < 3; c++) dN[q][c] = tq[c];
     }
-    const double sg[3][3] = {{sk[0], sk[5], sk[4]}, {sk[5], sk[1], sk[3]}, {sk[4], sk[3], sk[2]}};
-    const double m = P.m[p];
-    const double fx = a.grav[0] * a.facl, fy = a.grav[1] * a.facl, fz = a.grav[2] * a.facl;
-    const double afv = a.af * vol;
-    // Tangent blocks with the factors of the particle folded into three
-    // vectors per node (L = af vol lambda' dN_a, M = af vol mu' dN_a,
-    // S = af vol sigma dN_a):  K_ab = L_a db^T + db M_a^T + I (M_a + S_a).db,
-    // and K_ba = K_ab^T, so each unordered pair is computed once.
-    for (int qa = 0; qa < 8; qa++) {
+    const R sg[3][3] = {{sk[0], sk[5], sk[4]}, {sk[5], sk[1], sk[3]}, {sk[4], sk[3], sk[2]}};
+    const R m = P.m[p];
+    const R fx = (R)(a.grav[0] * a.facl), fy = (R)(a.grav[1] * a.facl), fz = (R)(a.grav[2] * a.facl);
+    const R afv = af * vol;
+    const R am = (R)a.am, nb3 = (R)a.nb[3];
+    for (int qa = 0; qa < NE; qa++) {
         const int na = nid[qa];
-        const double emd = a.nb[3] * Nw[qa] * m;   // ComputeNRLumpedMat (material_point.h:144)
-        double L[3], M[3], T[3];
+        const int ia = qa % NX, ja = (qa / NX) % NY, ka = qa / (NX * NY);
+        const R emd = nb3 * Nw[qa] * m;   // ComputeNRLumpedMat (material_point.h:144)
+        R ah[3], Sa[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) ah[k] = afv * dN[qa][k];
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            Sa[k] = a.nr_flag ? sg[k][0] * ah[0] + sg[k][1] * ah[1] + sg[k][2] * ah[2] : (R)0;
+        // isotropic: L = lambda' a, M = mu' a, T = M + sigma a;  general: G a, B a
+        R L[3], M[3], T[3], Ga[3], Ba[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            L[k] = afv * lam * dN[qa][k];
-            M[k] = afv * mu * dN[qa][k];
-            const double sk_ = a.nr_flag ? afv * (sg[k][0] * dN[qa][0] + sg[k][1] * dN[qa][1] + sg[k][2] * dN[qa][2]) : 0.0;
-            T[k] = M[k] + sk_;
+            L[k] = t.lam * ah[k];
+            M[k] = t.mu * ah[k];
+            T[k] = M[k] + Sa[k];
+        }
+        if (t.general) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                Ga[k] = t.G[k][0] * ah[0] + t.G[k][1] * ah[1] + t.G[k][2] * ah[2];
+                Ba[k] = t.B[k][0] * ah[0] + t.B[k][1] * ah[1] + t.B[k][2] * ah[2];
+            }
         }
 #pragma unroll 1
-        for (int qb = qa; qb < 8; qb++) {
+        for (int qb = qa; qb < NE; qb++) {
             const int nbn = nid[qb];
-            const int dxo = (qb & 1) - (qa & 1), dyo = ((qb >> 1) & 1) - ((qa >> 1) & 1), dzo = (qb >> 2) - (qa >> 2);
-            const int s = (dxo + 1) + 3 * (dyo + 1) + 9 * (dzo + 1);
-            const double db0 = dN[qb][0], db1 = dN[qb][1], db2 = dN[qb][2];
-            const double db[3] = {db0, db1, db2};
-            const double dg = T[0] * db0 + T[1] * db1 + T[2] * db2;
-            double K[3][3];
+            const int dxo = qb % NX - ia, dyo = (qb / NX) % NY - ja, dzo = qb / (NX * NY) - ka;
+            const int sl = (dxo + OX) + SX * ((dyo + OY) + SY * (dzo + OZ));
+            const R db[3] = {dN[qb][0], dN[qb][1], dN[qb][2]};
+            R K[3][3];
+            if (!t.general) {
+                const R dg = T[0] * db[0] + T[1] * db[1] + T[2] * db[2];
 #pragma unroll
-            for (int i = 0; i < 3; i++)
+                for (int i = 0; i < 3; i++)
 #pragma unroll
-                for (int j = 0; j < 3; j++) K[i][j] = L[i] * db[j] + M[j] * db[i] + (i == j ? dg : 0.0);
+                    for (int j = 0; j < 3; j++) K[i][j] = L[i] * db[j] + M[j] * db[i] + (i == j ? dg : (R)0);
+            } else {
+                R Bb[3], Gb[3];
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    Bb[k] = t.B[k][0] * db[0] + t.B[k][1] * db[1] + t.B[k][2] * db[2];
+                    Gb[k] = t.Gp[k][0] * db[0] + t.Gp[k][1] * db[1] + t.Gp[k][2] * db[2];
+                }
+                const R ab = ah[0] * db[0] + ah[1] * db[1] + ah[2] * db[2];
+                const R aBb = ah[0] * Bb[0] + ah[1] * Bb[1] + ah[2] * Bb[2];
+                const R sab = Sa[0] * db[0] + Sa[1] * db[1] + Sa[2] * db[2];
+                const R dg = t.alpha * ab + sab;
+                const R bsc = t.beta * aBb;
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++)
+                        K[i][j] = Ga[i] * db[j] + ah[i] * Gb[j] + t.gam * db[i] * ah[j] + t.eps * Ba[i] * Bb[j] +
+                                  t.delta * Bb[i] * Ba[j] + bsc * t.B[i][j] + (i == j ? dg : (R)0);
+            }
             if (qa == qb) {
 #pragma unroll
-                for (int i = 0; i < 3; i++) K[i][i] += a.am * emd;
+                for (int i = 0; i < 3; i++) K[i][i] += am * emd;
             }
 #pragma unroll
             for (int i = 0; i < 3; i++)
 #pragma unroll
                 for (int j = 0; j < 3; j++) {
-                    atomicAdd(&A[aidx(s * 9 + 3 * i + j, na)], K[i][j]);
-                    if (qb != qa) atomicAdd(&A[aidx((26 - s) * 9 + 3 * j + i, nbn)], K[i][j]);
+                    atomicAdd(&A[aidx(sl * 9 + 3 * i + j, na, a.qp)], K[i][j]);
+                    if (qb != qa) atomicAdd(&A[aidx((NS - 1 - sl) * 9 + 3 * j + i, nbn, a.qp)], K[i][j]);
                 }
         }
-        const double f0 = -vol * (sk[0] * dN[qa][0] + sk[5] * dN[qa][1] + sk[4] * dN[qa][2]) + Nw[qa] * (m * fx);
-        const double f1 = -vol * (sk[5] * dN[qa][0] + sk[1] * dN[qa][1] + sk[3] * dN[qa][2]) + Nw[qa] * (m * fy);
-        const double f2 = -vol * (sk[4] * dN[qa][0] + sk[3] * dN[qa][1] + sk[2] * dN[qa][2]) + Nw[qa] * (m * fz);
-        atomicAdd(&b[na], f0);
-        atomicAdd(&b[N + na], f1);
-        atomicAdd(&b[2 * N + na], f2);
+        const R f0 = -vol * (sk[0] * dN[qa][0] + sk[5] * dN[qa][1] + sk[4] * dN[qa][2]) + Nw[qa] * (m * fx);
+        const R f1 = -vol * (sk[5] * dN[qa][0] + sk[1] * dN[qa][1] + sk[3] * dN[qa][2]) + Nw[qa] * (m * fy);
+        const R f2 = -vol * (sk[4] * dN[qa][0] + sk[3] * dN[qa][1] + sk[2] * dN[qa][2]) + Nw[qa] * (m * fz);
+        atomicAdd(&b[na], (double)f0);
+        atomicAdd(&b[N + na], (double)f1);
+        atomicAdd(&b[2 * N + na], (double)f2);
     }
 }
 
 // AddInertialForceToRHS (material_point.h:151-161) and the diagonal of the
 // scaling D^-1/2 (crsmat.cpp:87-146, FEM_flag false)
-__global__ void k_imp_rhs_diag(ImpArgs a, const double *A, const double *nmass, const double *naccel_k,
+template <typename R>
+__global__ void k_imp_rhs_diag(ImpArgs a, const R *A, const double *nmass, const double *naccel_k,
                                const double *naccel, double *b, double *adiag) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= a.nodec) return;
     const size_t N = (size_t)a.nodec;
+    const int dslot = (a.ns - 1) / 2;
     for (int c = 0; c < 3; c++) {
         const double aam = a.am * naccel_k[c * N + n] + (1.0 - a.am) * naccel[c * N + n];
         b[c * N + n] -= nmass[n] * aam;
-        const double dg = fabs(A[aidx(13 * 9 + 4 * c, n)]);
+        const double dg = fabs((double)A[aidx(dslot * 9 + 4 * c, n, a.qp)]);
         adiag[c * N + n] = dg < a.mtol ? 0.0 : 1.0 / sqrt(dg);
     }
 }
 
 // ApplyDiagonalScaling (crsmat.cpp:152-172)
-__global__ void k_imp_scale(ImpArgs a, double *A, const double *adiag) {
+template <typename R>
+__global__ void k_imp_scale(ImpArgs a, R *A, const double *adiag) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= a.nodec) return;
     const size_t N = (size_t)a.nodec;
     int i, j, k;
     node_ijk(n, a.nnc, i, j, k);
-    for (int s = 0; s < 27; s++) {
-        const int ii = i + s % 3 - 1, jj = j + (s / 3) % 3 - 1, kk = k + s / 9 - 1;
+    const int sx = 2 * a.rad[0] + 1, sy = 2 * a.rad[1] + 1;
+    for (int s = 0; s < a.ns; s++) {
+        const int ii = i + s % sx - a.rad[0], jj = j + (s / sx) % sy - a.rad[1], kk = k + s / (sx * sy) - a.rad[2];
         if (ii < 0 || jj < 0 || kk < 0 || ii >= a.nnc[0] || jj >= a.nnc[1] || kk >= a.nnc[2]) continue;
         const size_t col = ii + (size_t)a.nnc[0] * (jj + (size_t)a.nnc[1] * kk);
         for (int r = 0; r < 3; r++)
-            for (int c = 0; c < 3; c++) A[aidx(s * 9 + 3 * r + c, n)] *= adiag[r * N + n] * adiag[c * N + col];
+            for (int c = 0; c < 3; c++) {
+                R &v = A[aidx(s * 9 + 3 * r + c, n, a.qp)];
+                v = (R)((double)v * (adiag[r * N + n] * adiag[c * N + col]));
+            }
     }
 }
 
@@ -481,10 +693,16 @@ __global__ void k_finish(const double *part, int nblk, double *out, int slot) {
     if (threadIdx.x == 0) out[slot] = t;
 }
 
-// y = A x with BC rows zeroed (MatVecMult + BCResidualSet), optional dot(x, y)
-__global__ void __launch_bounds__(256) k_imp_matvec(ImpArgs a, const double *A, const double *x, double *y,
+// y = A x with BC rows zeroed (MatVecMult + BCResidualSet), optional dot(x, y).
+// TA: storage of A; TC: arithmetic (FP32 in the Krylov iterations of the
+// FP32 operator, FP64 for its true residual and in the FP64 mode); x and y
+// are FP64.  RX, RY, RZ: the stencil radius per axis.
+template <typename TA, typename TC, int RX, int RY, int RZ>
+__global__ void __launch_bounds__(256) k_imp_matvec(ImpArgs a, const TA *A, const double *x, double *y,
                                                     double *part, unsigned *cnt = nullptr, double *scal = nullptr,
                                                     int slot = 0) {
+    using TA2 = typename std::conditional<sizeof(TA) == 8, double2, float2>::type;
+    constexpr int SX = 2 * RX + 1, SY = 2 * RY + 1, NS = SX * SY * (2 * RZ + 1);
     __shared__ double sh[32];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     double dot = 0.0;
@@ -492,42 +710,42 @@ __global__ void __launch_bounds__(256) k_imp_matvec(ImpArgs a, const double *A, 
         const size_t N = (size_t)a.nodec;
         int i, j, k;
         node_ijk(n, a.nnc, i, j, k);
-        double acc[3] = {0.0, 0.0, 0.0};
+        TC acc[3] = {(TC)0, (TC)0, (TC)0};
 #pragma unroll
-        for (int s = 0; s < 27; s++) {
-            const int ii = i + s % 3 - 1, jj = j + (s / 3) % 3 - 1, kk = k + s / 9 - 1;
+        for (int s = 0; s < NS; s++) {
+            const int ii = i + s % SX - RX, jj = j + (s / SX) % SY - RY, kk = k + s / (SX * SY) - RZ;
             if (ii < 0 || jj < 0 || kk < 0 || ii >= a.nnc[0] || jj >= a.nnc[1] || kk >= a.nnc[2]) continue;
             const size_t col = ii + (size_t)a.nnc[0] * (jj + (size_t)a.nnc[1] * kk);
-            const double x0 = x[col], x1 = x[N + col], x2 = x[2 * N + col];
+            const TC x0 = (TC)x[col], x1 = (TC)x[N + col], x2 = (TC)x[2 * N + col];
             // the block's 9 entries: 4 aligned pairs and 1 single (which end depends on the parity of 9 s)
-            double e[9];
+            TC e[9];
             if ((s & 1) == 0) {
 #pragma unroll
                 for (int t = 0; t < 4; t++) {
-                    const double2 v = __ldg(reinterpret_cast<const double2 *>(A + aidx(s * 9 + 2 * t, n)));
-                    e[2 * t] = v.x;
-                    e[2 * t + 1] = v.y;
+                    const TA2 v = __ldg(reinterpret_cast<const TA2 *>(A + aidx(s * 9 + 2 * t, n, a.qp)));
+                    e[2 * t] = (TC)v.x;
+                    e[2 * t + 1] = (TC)v.y;
                 }
-                e[8] = __ldg(A + aidx(s * 9 + 8, n));
+                e[8] = (TC)__ldg(A + aidx(s * 9 + 8, n, a.qp));
             } else {
-                e[0] = __ldg(A + aidx(s * 9, n));
+                e[0] = (TC)__ldg(A + aidx(s * 9, n, a.qp));
 #pragma unroll
                 for (int t = 0; t < 4; t++) {
-                    const double2 v = __ldg(reinterpret_cast<const double2 *>(A + aidx(s * 9 + 1 + 2 * t, n)));
-                    e[1 + 2 * t] = v.x;
-                    e[2 + 2 * t] = v.y;
+                    const TA2 v = __ldg(reinterpret_cast<const TA2 *>(A + aidx(s * 9 + 1 + 2 * t, n, a.qp)));
+                    e[1 + 2 * t] = (TC)v.x;
+                    e[2 + 2 * t] = (TC)v.y;
                 }
             }
-            // chained FMAs: the FP64 pipe is this kernel's limit, and a
+            // chained FMAs: in FP64 the FP64 pipe is this kernel's limit, and a
             // separate product and add per entry would cost a third more
 #pragma unroll
             for (int r = 0; r < 3; r++) acc[r] = fma(e[3 * r + 2], x2, fma(e[3 * r + 1], x1, fma(e[3 * r], x0, acc[r])));
         }
         const unsigned char bf = a.bcflag[n];
         for (int c = 0; c < 3; c++) {
-            if (bf & (1 << c)) acc[c] = 0.0;
-            y[c * N + n] = acc[c];
-            dot += x[c * N + n] * acc[c];
+            const double v = (bf & (1 << c)) ? 0.0 : (double)acc[c];
+            y[c * N + n] = v;
+            dot += x[c * N + n] * v;
         }
     }
     if (part && cnt) {   // dot(x, y) reduced by the last block into scal[slot]
@@ -694,105 +912,138 @@ __global__ void k_imp_nei(ImpArgs a, const double *nvof, double *nei, double *pa
 // Node2Particle (var_trans_solid_implicit.cpp:202-255) with the nodal kinematics
 // already committed: F, J, vol, stress, displacement/acceleration/velocity
 // gathers and the shifting gradient; CommitParticleKinematics without the shift.
-__global__ void __launch_bounds__(128) k_imp_g2p(ImpArgs a, PView P, const double *ndispl, const double *nvel,
-                                                 const double *naccel, const double *nei, double *geup,
-                                                 double *part, DevCtl *ctl, int parity) {
+template <typename R, int OX, int OY, int OZ>
+__global__ void __launch_bounds__(128) k_imp_g2p(ImpArgs a, PView<R> P, const double *ndispl, const double *nvel,
+                                                 const double *naccel, const double *nei, R *geup, double *part,
+                                                 DevCtl *ctl, int parity) {
+    constexpr int NE = (OX + 1) * (OY + 1) * (OZ + 1);
     __shared__ double sh[32];
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     double gd = 0.0;
     if (p < a.num) {
         const size_t N = (size_t)a.nodec, NP = (size_t)a.num;
-        double x[3] = {P.x[0][p], P.x[1][p], P.x[2][p]};
-        int cx, cy, cz, nid[8];
-        double Nw[8], dN[8][3];
+        const KGeom<R> g = kgeom<R>(a);
+        const R x[3] = {P.x[0][p], P.x[1][p], P.x[2][p]};
+        int nid[NE];
+        R Nw[NE], dN[NE][3];
         bool oob = false;
-        shape8(a, x, cx, cy, cz, Nw, dN, nid, oob);
-        double d[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-        for (int q = 0; q < 8; q++)
+        shape_nodes<R, OX, OY, OZ>(a, g, x, Nw, dN, nid, oob);
+        R Dm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int q = 0; q < NE; q++)
             for (int r = 0; r < 3; r++) {
-                const double u = ndispl[r * N + nid[q]];
-                for (int c = 0; c < 3; c++) d[r][c] += dN[q][c] * 1.0 * u;
+                const R u = (R)ndispl[r * N + nid[q]];
+                for (int c = 0; c < 3; c++) Dm[r][c] += dN[q][c] * (R)1 * u;
             }
-        for (int r = 0; r < 3; r++) d[r][r] += 1.0;
-        double F[3][3], Fn[3][3];
+        R d[3][3];
         for (int r = 0; r < 3; r++)
-            for (int c = 0; c < 3; c++) F[r][c] = P.F[3 * r + c][p];
-        for (int r = 0; r < 3; r++)
-            for (int c = 0; c < 3; c++) {
-                double s = 0.0;
-                for (int k = 0; k < 3; k++) s += d[r][k] * F[k][c];
-                Fn[r][c] = s;
-            }
-        const double J = det3(Fn);
-        const double vol = J * P.vol0[p];
-        for (int r = 0; r < 3; r++)
-            for (int c = 0; c < 3; c++) P.F[3 * r + c][p] = Fn[r][c];
+            for (int c = 0; c < 3; c++) d[r][c] = Dm[r][c] + (r == c ? (R)1 : (R)0);
+        R Fn[3][3], Hn[3][3], J, jm1;
+        if constexpr (sizeof(R) == 8) {
+            R F[3][3];
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) F[r][c] = P.F[3 * r + c][p];
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) {
+                    R sum = 0.0;
+                    for (int k = 0; k < 3; k++) sum += d[r][k] * F[k][c];
+                    Fn[r][c] = sum;
+                }
+            J = det3(Fn);
+            jm1 = J - (R)1;
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) P.F[3 * r + c][p] = Fn[r][c];
+        } else {
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) {
+                    R sum = Dm[r][c] + P.F[3 * r + c][p];
+                    for (int k = 0; k < 3; k++) sum += Dm[r][k] * P.F[3 * k + c][p];
+                    Hn[r][c] = sum;
+                }
+            jm1 = det_ipm1(Hn);
+            J = (R)1 + jm1;
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) {
+                    Fn[r][c] = Hn[r][c] + (r == c ? (R)1 : (R)0);
+                    P.F[3 * r + c][p] = Hn[r][c];
+                }
+        }
+        const R vol = J * P.vol0[p];
         P.vol[p] = vol;
-        double sk[6];
+        R sk[6];
         for (int k = 0; k < 6; k++) sk[k] = P.s[k][p];
         const int mid = P.matid[p];
         const int model = a.iprop[mid];
-        const double E = a.matprop[3 * mid], nu = a.matprop[3 * mid + 1];
+        const R E = (R)a.matprop[3 * mid], nu = (R)a.matprop[3 * mid + 1], m3 = (R)a.matprop[3 * mid + 2];
         if (model == 0) {
-            double Dm[3][3];
+            R De[3][3];
             for (int r = 0; r < 3; r++)
-                for (int c = 0; c < 3; c++) Dm[r][c] = (r == c) ? d[r][c] - 1.0 : d[r][c];
-            lin_elast_update(sk, Dm, E, nu);
+                for (int c = 0; c < 3; c++)
+                    De[r][c] = sizeof(R) == 8 ? (r == c ? d[r][c] - (R)1 : d[r][c]) : Dm[r][c];
+            lin_elast_update(sk, De, E, nu);
         } else if (model == 1) {
-            neo_hookean_stress(sk, Fn, J, E, nu);
+            if constexpr (sizeof(R) == 8) neo_hookean_stress(sk, Fn, J, E, nu);
+            else neo_hookean_stress_h(sk, Hn, jm1, E, nu);
+        } else if (model == 2) {
+            if constexpr (sizeof(R) == 8) stvk_stress(sk, Fn, J, E, nu);
+            else stvk_stress_h(sk, Hn, jm1, E, nu);
+        } else if (model == 3) {
+            if constexpr (sizeof(R) == 8) mooney_rivlin_stress(sk, Fn, J, E, nu, m3);
+            else mooney_rivlin_stress_h(sk, Hn, jm1, E, nu, m3);
         } else {
-            for (int k = 0; k < 6; k++) sk[k] = 0.0;
+            for (int k = 0; k < 6; k++) sk[k] = (R)0;
         }
         for (int k = 0; k < 6; k++) P.s[k][p] = sk[k];
         const bool flip = (a.scheme == MPM_FLIP);
         double disp[3] = {0, 0, 0}, acc[3] = {0, 0, 0}, vel[3] = {0, 0, 0};
-        const double aold[3] = {P.acc[0][p], P.acc[1][p], P.acc[2][p]};
+        const double aold[3] = {(double)P.acc[0][p], (double)P.acc[1][p], (double)P.acc[2][p]};
         if (model != -1) {
-            for (int q = 0; q < 8; q++)
+            for (int q = 0; q < NE; q++)
                 for (int c = 0; c < 3; c++) {
-                    disp[c] += Nw[q] * ndispl[c * N + nid[q]];
-                    acc[c] += Nw[q] * naccel[c * N + nid[q]];
-                    vel[c] += Nw[q] * nvel[c * N + nid[q]];
+                    disp[c] += (double)Nw[q] * ndispl[c * N + nid[q]];
+                    acc[c] += (double)Nw[q] * naccel[c * N + nid[q]];
+                    vel[c] += (double)Nw[q] * nvel[c * N + nid[q]];
                 }
         }
         // shifting gradient at the old position with the new volume (material_point.cpp:192-216)
-        double g[3] = {0, 0, 0};
-        for (int q = 0; q < 8; q++)
-            for (int c = 0; c < 3; c++) g[c] += dN[q][c] * nei[nid[q]];
+        R gv[3] = {0, 0, 0};
+        for (int q = 0; q < NE; q++)
+            for (int c = 0; c < 3; c++) gv[c] += dN[q][c] * (R)nei[nid[q]];
         for (int c = 0; c < 3; c++) {
-            g[c] *= 2.0 * vol;
-            geup[c * NP + p] = g[c];
-            gd += g[c] * g[c];
+            gv[c] *= (R)2 * vol;
+            geup[c * NP + p] = gv[c];
+            gd += (double)gv[c] * (double)gv[c];
         }
         // CommitParticleKinematics (nonlinear_time_integration.cpp:83-96), shift added by k_imp_shift
         float amax = 0.0f, vmax = 0.0f;
         for (int c = 0; c < 3; c++) {
-            double vc = flip ? P.v[c][p] + a.dt * ((1.0 - a.gamma) * aold[c] + a.gamma * acc[c]) : vel[c];
-            P.v[c][p] = vc;
-            P.acc[c][p] = acc[c];
-            P.x[c][p] = x[c] + disp[c];
+            const double vc = flip ? (double)P.v[c][p] + a.dt * ((1.0 - a.gamma) * aold[c] + a.gamma * acc[c]) : vel[c];
+            P.v[c][p] = (R)vc;
+            P.acc[c][p] = (R)acc[c];
+            P.x[c][p] = (R)((double)x[c] + disp[c]);
             amax = fmaxf(amax, (float)fabs(acc[c]));
             vmax = fmaxf(vmax, (float)fabs(vc));
         }
-        const float rs = (float)fmax(fabs(sk[0]) + fabs(sk[5]) + fabs(sk[4]),
-                                     fmax(fabs(sk[5]) + fabs(sk[1]) + fabs(sk[3]), fabs(sk[4]) + fabs(sk[3]) + fabs(sk[2])));
+        const float rs = (float)fmax(fabs((double)sk[0]) + fabs((double)sk[5]) + fabs((double)sk[4]),
+                                     fmax(fabs((double)sk[5]) + fabs((double)sk[1]) + fabs((double)sk[3]),
+                                          fabs((double)sk[4]) + fabs((double)sk[3]) + fabs((double)sk[2])));
         atomic_max_pos(&ctl->nxt[parity ^ 1][B_AMAX], amax * 1.000001f);
         atomic_max_pos(&ctl->nxt[parity ^ 1][B_VMAX], vmax * 1.000001f);
-        atomic_max_pos(&ctl->nxt[parity ^ 1][B_VOLMAX], (float)fabs(vol) * 1.000001f);
-        atomic_max_pos(&ctl->nxt[parity ^ 1][B_VOLSMAX], (float)fabs(vol) * rs * 1.000001f);
+        atomic_max_pos(&ctl->nxt[parity ^ 1][B_VOLMAX], (float)fabs((double)vol) * 1.000001f);
+        atomic_max_pos(&ctl->nxt[parity ^ 1][B_VOLSMAX], (float)fabs((double)vol) * rs * 1.000001f);
     }
     const double t = block_sum(gd, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
 // x += -b0 geup, b0 = eu / gd unless gd < mtol (material_point.cpp:219-225)
-__global__ void k_imp_shift(ImpArgs a, PView P, const double *geup, const double *scal) {
+template <typename R>
+__global__ void k_imp_shift(ImpArgs a, PView<R> P, const R *geup, const double *scal) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const double gd = scal[S_GD];
     const double b0 = block_div(scal[S_EU], gd, gd < a.mtol);
     if (p >= a.num || !a.shifting || b0 == 0.0) return;
     const size_t NP = (size_t)a.num;
-    for (int c = 0; c < 3; c++) P.x[c][p] += -b0 * geup[c * NP + p];
+    for (int c = 0; c < 3; c++) P.x[c][p] = (R)((double)P.x[c][p] + -b0 * (double)geup[c * NP + p]);
 }
 
 // ------------------------------------------------ flexible CG (Notay's FCG(1))
@@ -1085,10 +1336,10 @@ namespace mpm {
 void implicit_free(mpm_ctx *c) {
     ImpState *s = c->imp;
     if (!s) return;
-    double *bufs[] = {s->A, s->adiag, s->b, s->x, s->r, s->p, s->Ap, s->xs, s->ndispl, s->nvel, s->naccel,
+    void *bufs[] = {s->A, s->adiag, s->b, s->x, s->r, s->p, s->Ap, s->xs, s->ndispl, s->nvel, s->naccel,
                       s->naccel_k, s->nmass, s->nvof, s->nei, s->stress_k, s->geup, s->part, s->scal,
                       s->z, s->bs, s->xstar, s->ev, s->gp, s->gq, s->gqq, s->gbeta};
-    for (double *b : bufs)
+    for (void *b : bufs)
         if (b) cudaFree(b);
     if (s->cnt) cudaFree(s->cnt);
     if (s->gqf) cudaFree(s->gqf);
@@ -1107,21 +1358,27 @@ static mpm_status ensure_particle_scratch(mpm_ctx *c) {
     if (s->geup) cudaFree(s->geup);
     s->stress_k = s->geup = nullptr;
     size_t n = (size_t)(c->num > 0 ? c->num : 1);
-    CKI(cudaMalloc((void **)&s->stress_k, sizeof(double) * 6 * n));
-    CKI(cudaMalloc((void **)&s->geup, sizeof(double) * 3 * n));
+    CKI(cudaMalloc((void **)&s->stress_k, c->rsize * 6 * n));
+    CKI(cudaMalloc((void **)&s->geup, c->rsize * 3 * n));
     s->num_alloc = c->num;
     return MPM_OK;
 }
 
 mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
     if (!c) return MPM_ERR_BAD_ARG;
-    if (c->nreal != 27 || c->precision != 64) return MPM_ERR_UNSUPPORTED;
-    if (c->g.order[0] != 1 || c->g.order[1] != 1 || c->g.order[2] != 1) return MPM_ERR_UNSUPPORTED;
+    if (c->nreal != 27) return MPM_ERR_UNSUPPORTED;
+    {
+        // the shape orders mpm_gpu_create takes: linear, quadratic, or quadratic in x and z
+        const int *o = c->g.order;
+        const bool ok = (o[0] == 1 && o[1] == 1 && o[2] == 1) || (o[0] == 2 && o[1] == 2 && o[2] == 2) ||
+                        (o[0] == 2 && o[1] == 1 && o[2] == 2);
+        if (!ok) return MPM_ERR_UNSUPPORTED;
+    }
     {
         std::vector<int> ip(c->nmat);
         CKI(cudaMemcpy(ip.data(), c->d_iprop, sizeof(int) * c->nmat, cudaMemcpyDeviceToHost));
         for (int m : ip)
-            if (m > 1) return MPM_ERR_UNSUPPORTED;   // no tangent for the fluid model
+            if (m > 3) return MPM_ERR_UNSUPPORTED;   // no tangent for the fluid model
     }
     implicit_free(c);
     ImpState *s = new ImpState();
@@ -1133,6 +1390,8 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
         if (v == 1 || v == 2 || v == 4 || v == 8) s->gm = v;   // divides the 8 iterations of a graph launch
     }
     s->nr_flag = nr_flag ? 1 : 0;
+    s->prec = c->precision;
+    s->qp = imp_args(c).qp;
     // GeneralizedAlphaParaSet + NewmarkBetaParaSet (nonlinear_time_integration.cpp:10-56), second order
     double t = 1.0 + spec_rad;
     s->alpha_f = 1.0 / t;
@@ -1148,7 +1407,7 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
     s->nb[4] = 1.0 / (b * dt);
     s->nb[5] = 1.0 / (2.0 * b) - 1.0;
     const size_t N = (size_t)c->g.nodec;
-    CKI(cudaMalloc((void **)&s->A, sizeof(double) * a_size((int)N)));
+    CKI(cudaMalloc((void **)&s->A, (s->prec == 64 ? sizeof(double) : sizeof(float)) * a_size((int)N, s->qp)));
     double **vec3[] = {&s->adiag, &s->b,    &s->x,       &s->r, &s->p,  &s->Ap,    &s->xs, &s->ndispl,
                        &s->nvel,  &s->naccel, &s->naccel_k, &s->z, &s->bs, &s->xstar, &s->ev};
     for (double **v : vec3) CKI(cudaMalloc((void **)v, sizeof(double) * 3 * N));
@@ -1175,6 +1434,78 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
 }
 
 static int nb_nodes(mpm_ctx *c) { return (c->g.nodec + 255) / 256; }
+
+// y = A x on the context's stream (k_imp_matvec for the context's matrix
+// precision and stencil); hi: FP64 arithmetic whatever the storage (the
+// true residual and the Newton check of the FP32 operator).
+static void launch_matvec(mpm_ctx *c, const ImpArgs &a, int nb, const double *x, double *y, double *part,
+                          unsigned *cnt = nullptr, double *scal = nullptr, int slot = 0, bool hi = false) {
+    ImpState *s = c->imp;
+    const int *o = c->g.order;
+    auto go = [&](auto ta, auto tc) {
+        using TA = decltype(ta);
+        using TC = decltype(tc);
+        const TA *A = (const TA *)s->A;
+        if (o[0] == 1 && o[1] == 1 && o[2] == 1)
+            k_imp_matvec<TA, TC, 1, 1, 1><<<nb, 256, 0, c->stream>>>(a, A, x, y, part, cnt, scal, slot);
+        else if (o[1] == 2)
+            k_imp_matvec<TA, TC, 2, 2, 2><<<nb, 256, 0, c->stream>>>(a, A, x, y, part, cnt, scal, slot);
+        else
+            k_imp_matvec<TA, TC, 2, 1, 2><<<nb, 256, 0, c->stream>>>(a, A, x, y, part, cnt, scal, slot);
+    };
+    if (s->prec == 64) go(double(), double());
+    else if (hi) go(float(), double());
+    else go(float(), float());
+}
+
+// AssembleSystem: k_imp_assemble (per particle), k_imp_rhs_diag, k_imp_scale
+template <typename R>
+static void launch_assemble(mpm_ctx *c, const ImpArgs &a) {
+    ImpState *s = c->imp;
+    const PView<R> P = pview<R>(c);
+    R *A = (R *)s->A, *sk = (R *)s->stress_k;
+    const int pb = (int)((c->num + 127) / 128);
+    const int *o = c->g.order;
+    if (o[0] == 1 && o[1] == 1 && o[2] == 1)
+        k_imp_assemble<R, 1, 1, 1><<<pb, 128, 0, c->stream>>>(a, P, s->ndispl, sk, A, s->b);
+    else if (o[1] == 2)
+        k_imp_assemble<R, 2, 2, 2><<<pb, 128, 0, c->stream>>>(a, P, s->ndispl, sk, A, s->b);
+    else
+        k_imp_assemble<R, 2, 1, 2><<<pb, 128, 0, c->stream>>>(a, P, s->ndispl, sk, A, s->b);
+    k_imp_rhs_diag<R><<<nb_nodes(c), 256, 0, c->stream>>>(a, A, s->nmass, s->naccel_k, s->naccel, s->b, s->adiag);
+    k_imp_scale<R><<<nb_nodes(c), 256, 0, c->stream>>>(a, A, s->adiag);
+}
+
+// Node2Particle's particle pass (k_imp_g2p) and the shift (k_imp_shift)
+template <typename R>
+static void launch_g2p(mpm_ctx *c, const ImpArgs &a, int parity, int pb) {
+    ImpState *s = c->imp;
+    const PView<R> P = pview<R>(c);
+    R *geup = (R *)s->geup;
+    const int *o = c->g.order;
+    if (o[0] == 1 && o[1] == 1 && o[2] == 1)
+        k_imp_g2p<R, 1, 1, 1><<<pb, 128, 0, c->stream>>>(a, P, s->ndispl, s->nvel, s->naccel, s->nei, geup, s->part,
+                                                          c->d_ctl, parity);
+    else if (o[1] == 2)
+        k_imp_g2p<R, 2, 2, 2><<<pb, 128, 0, c->stream>>>(a, P, s->ndispl, s->nvel, s->naccel, s->nei, geup, s->part,
+                                                          c->d_ctl, parity);
+    else
+        k_imp_g2p<R, 2, 1, 2><<<pb, 128, 0, c->stream>>>(a, P, s->ndispl, s->nvel, s->naccel, s->nei, geup, s->part,
+                                                          c->d_ctl, parity);
+    k_finish<<<1, 256, 0, c->stream>>>(s->part, pb, s->scal, S_GD);
+    k_imp_shift<R><<<pb, 128, 0, c->stream>>>(a, P, geup, s->scal);
+}
+
+// stress_k <- the particles' stress (InitializeNRStress)
+static mpm_status copy_stress_k(mpm_ctx *c) {
+    ImpState *s = c->imp;
+    const size_t rs = c->rsize, n = (size_t)c->num;
+    const char *f = (const char *)c->pbuf[c->cur];
+    for (int k = 0; k < 6; k++)
+        CKI(cudaMemcpyAsync((char *)s->stress_k + k * n * rs, f + (15 + k) * c->pstride * rs, rs * n,
+                            cudaMemcpyDeviceToDevice, c->stream));
+    return MPM_OK;
+}
 
 // P2G of the implicit solid: AccelP2G mode of the scatter + k_imp_grid
 static mpm_status imp_p2g(mpm_ctx *c, double facl) {
@@ -1233,7 +1564,7 @@ static void cg_iteration(mpm_ctx *c, const ImpArgs &a, int nb, int it) {
     ImpState *s = c->imp;
     const int cur = (it & 1) ? S_RR1 : S_RR0;
     timer_begin(c, K_MATVEC);
-    k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->p, s->Ap, s->part, s->cnt + 3, s->scal, S_PAP);
+    launch_matvec(c, a, nb, s->p, s->Ap, s->part, s->cnt + 3, s->scal, S_PAP);
     timer_end(c, K_MATVEC);
     timer_begin(c, K_KRYLOV);
     k_cg_update<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->xs, s->r, s->p, s->Ap, s->part, s->cnt + 4);
@@ -1247,7 +1578,9 @@ static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
     ImpArgs a = imp_args(c);
     const int nb = nb_nodes(c);
     k_cg_scale_in<<<nb, 256, 0, c->stream>>>(a, s->x, s->b, s->adiag, s->xs, s->r);
-    k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->xs, s->Ap, nullptr);
+    if (s->prec == 32)   // the scaled RHS, for the true residual of the FP32 operator
+        CKI(cudaMemcpyAsync(s->bs, s->r, sizeof(double) * 3 * c->g.nodec, cudaMemcpyDeviceToDevice, c->stream));
+    launch_matvec(c, a, nb, s->xs, s->Ap, nullptr, nullptr, nullptr, 0, true);
     k_cg_init<<<nb, 256, 0, c->stream>>>(a, s->Ap, s->r, s->p, s->part);
     k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RR0);
     c->launches += 4;
@@ -1283,9 +1616,29 @@ static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
                 return MPM_ERR_NONFINITE;
             }
             if (s->debug) fprintf(stderr, "mpm_gb300 cg: it %d |r|/|r0| %.3e\n", it, sqrt(rr / rr0));
-            if (rr < eps * rr0) done = true;
-            else if (rr < FINE_FACTOR * eps * rr0) fine = true;
-            s->last_rel = sqrt(rr / rr0);
+            if (rr < eps * rr0 && s->prec == 32) {
+                // FP32 operator: the recursive residual carries the rounding of
+                // the FP32 matvecs, so convergence is judged on the true
+                // residual bs - A x (FP64 arithmetic); if it is not below the
+                // tolerance, CG restarts from it (r, and p = r)
+                const int cur = (it & 1) ? S_RR1 : S_RR0;
+                launch_matvec(c, a, nb, s->xs, s->z, nullptr, nullptr, nullptr, 0, true);
+                k_true_residual<<<nb, 256, 0, c->stream>>>(a, s->bs, s->z, s->r, s->part);
+                k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, cur);
+                CKI(cudaMemcpyAsync(s->p, s->r, sizeof(double) * 3 * c->g.nodec, cudaMemcpyDeviceToDevice,
+                                    c->stream));
+                c->launches += 3;
+                CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream));
+                CKI(cudaStreamSynchronize(c->stream));
+                const double rrt = s->h_scal[cur];
+                if (s->debug) fprintf(stderr, "mpm_gb300 cg: it %d true |r|/|r0| %.3e\n", it, sqrt(rrt / rr0));
+                if (rrt < eps * rr0) done = true;
+                s->last_rel = sqrt(rrt / rr0);
+            } else {
+                if (rr < eps * rr0) done = true;
+                else if (rr < FINE_FACTOR * eps * rr0) fine = true;
+                s->last_rel = sqrt(rr / rr0);
+            }
         }
     }
     k_cg_scale_out<<<(3 * c->g.nodec + 255) / 256, 256, 0, c->stream>>>(a, s->xs, s->adiag, s->x);
@@ -1307,7 +1660,7 @@ static mpm_status gcr_iter(mpm_ctx *c, const ImpArgs &a, int nb, int u, int sl) 
     timer_end(c, K_PRECOND);
     if (st != MPM_OK) return st;
     timer_begin(c, K_MATVEC);
-    k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->gp + (size_t)sl * st3, s->gq + (size_t)sl * st3, nullptr);
+    launch_matvec(c, a, nb, s->gp + (size_t)sl * st3, s->gq + (size_t)sl * st3, nullptr);
     timer_end(c, K_MATVEC);
     timer_begin(c, K_KRYLOV);
     if (u > 0)
@@ -1334,7 +1687,7 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
     const size_t N = (size_t)c->g.nodec;
     k_cg_scale_in<<<nb, 256, 0, c->stream>>>(a, s->x, s->b, s->adiag, s->xs, s->r);
     CKI(cudaMemcpyAsync(s->bs, s->r, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, c->stream));
-    k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->xs, s->Ap, nullptr);
+    launch_matvec(c, a, nb, s->xs, s->Ap, nullptr, nullptr, nullptr, 0, true);
     k_true_residual<<<nb, 256, 0, c->stream>>>(a, s->bs, s->Ap, s->r, s->part);
     k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RR0);
     k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
@@ -1376,7 +1729,7 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
         k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_PR);
         timer_end(c, K_KRYLOV);
         timer_begin(c, K_MATVEC);
-        k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->p, s->Ap, s->part);
+        launch_matvec(c, a, nb, s->p, s->Ap, s->part);
         timer_end(c, K_MATVEC);
         timer_begin(c, K_KRYLOV);
         k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_PAP);
@@ -1435,7 +1788,7 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
                 }
                 if (s->debug) fprintf(stderr, "mpm_gb300 gcr: it %d |r|/|r0| %.3e\n", it, sqrt(rr / rr0));
                 if (rr < eps * rr0) {
-                    k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->xs, s->z, nullptr);
+                    launch_matvec(c, a, nb, s->xs, s->z, nullptr, nullptr, nullptr, 0, true);
                     k_true_residual<<<nb, 256, 0, c->stream>>>(a, s->bs, s->z, s->r, s->part);
                     k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
                     c->launches += 3;
@@ -1510,7 +1863,7 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
                         use_nn ? "network" : "jacobi");
             if (rr < eps * rr0) {
                 // confirm on the true residual
-                k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->xs, s->z, nullptr);
+                launch_matvec(c, a, nb, s->xs, s->z, nullptr, nullptr, nullptr, 0, true);
                 k_true_residual<<<nb, 256, 0, c->stream>>>(a, s->bs, s->z, s->r, s->part);
                 k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
                 c->launches += 3;
@@ -1547,14 +1900,12 @@ static mpm_status imp_assemble(mpm_ctx *c) {
     ImpState *s = c->imp;
     ImpArgs a = imp_args(c);
     const size_t N = (size_t)c->g.nodec;
-    CKI(cudaMemsetAsync(s->A, 0, sizeof(double) * a_size((int)N), c->stream));
+    CKI(cudaMemsetAsync(s->A, 0, (s->prec == 64 ? sizeof(double) : sizeof(float)) * a_size((int)N, s->qp),
+                        c->stream));
     CKI(cudaMemsetAsync(s->b, 0, sizeof(double) * 3 * N, c->stream));
-    PView P = pview(c);
-    const int pb = (int)((c->num + 127) / 128);
     timer_begin(c, K_ASSEMBLE);
-    k_imp_assemble<<<pb, 128, 0, c->stream>>>(a, P, s->ndispl, s->stress_k, s->A, s->b);
-    k_imp_rhs_diag<<<nb_nodes(c), 256, 0, c->stream>>>(a, s->A, s->nmass, s->naccel_k, s->naccel, s->b, s->adiag);
-    k_imp_scale<<<nb_nodes(c), 256, 0, c->stream>>>(a, s->A, s->adiag);
+    if (s->prec == 64) launch_assemble<double>(c, a);
+    else launch_assemble<float>(c, a);
     timer_end(c, K_ASSEMBLE);
     c->launches += 3;
     return check_launch(c);
@@ -1566,7 +1917,7 @@ static mpm_status imp_residuals(mpm_ctx *c, double *ref, double *absr) {
     ImpArgs a = imp_args(c);
     const int nb = nb_nodes(c);
     k_imp_prepare_residual<<<nb, 256, 0, c->stream>>>(a, s->x, s->adiag, s->b, s->xs);
-    k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->xs, s->Ap, nullptr);
+    launch_matvec(c, a, nb, s->xs, s->Ap, nullptr, nullptr, nullptr, 0, true);
     k_imp_residual<<<nb, 256, 0, c->stream>>>(a, s->Ap, s->adiag, s->b, s->part);
     k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RES);
     k_finish<<<1, 256, 0, c->stream>>>(s->part + nb, nb, s->scal, S_IDOF);
@@ -1589,10 +1940,7 @@ static mpm_status imp_newton(mpm_ctx *c, double eps, int kmax, int *krylov, int 
     ImpState *s = c->imp;
     ImpArgs a = imp_args(c);
     const size_t N = (size_t)c->g.nodec;
-    PView P = pview(c);
-    for (int k = 0; k < 6; k++)
-        CKI(cudaMemcpyAsync(s->stress_k + k * (size_t)c->num, P.s[k], sizeof(double) * c->num,
-                            cudaMemcpyDeviceToDevice, c->stream));
+    if (copy_stress_k(c) != MPM_OK) return MPM_ERR_CUDA;
     CKI(cudaMemsetAsync(s->ndispl, 0, sizeof(double) * 3 * N, c->stream));
     CKI(cudaMemsetAsync(s->x, 0, sizeof(double) * 3 * N, c->stream));
     const int iter_max = s->nr_flag ? 1000 : 0;
@@ -1639,12 +1987,9 @@ static mpm_status imp_g2p(mpm_ctx *c) {
     k_imp_nei<<<nb, 256, 0, c->stream>>>(a, s->nvof, s->nei, s->part);
     k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_EU);
     k_imp_reset_next<<<1, 1, 0, c->stream>>>(c->d_ctl, parity);
-    PView P = pview(c);
     const int pb = (int)((c->num + 127) / 128);
-    k_imp_g2p<<<pb, 128, 0, c->stream>>>(a, P, s->ndispl, s->nvel, s->naccel, s->nei, s->geup, s->part, c->d_ctl,
-                                         parity);
-    k_finish<<<1, 256, 0, c->stream>>>(s->part, pb, s->scal, S_GD);
-    k_imp_shift<<<pb, 128, 0, c->stream>>>(a, P, s->geup, s->scal);
+    if (s->prec == 64) launch_g2p<double>(c, a, parity, pb);
+    else launch_g2p<float>(c, a, parity, pb);
     c->launches += 7;
     return check_launch(c);
 }
@@ -1693,10 +2038,7 @@ mpm_status mpm_gpu_implicit_assemble(mpm_ctx *c, double facl) {
     if (st != MPM_OK) return st;
     ImpState *s = c->imp;
     ImpArgs a = imp_args(c);
-    PView P = pview(c);
-    for (int k = 0; k < 6; k++)
-        CKI(cudaMemcpyAsync(s->stress_k + k * (size_t)c->num, P.s[k], sizeof(double) * c->num,
-                            cudaMemcpyDeviceToDevice, c->stream));
+    if (copy_stress_k(c) != MPM_OK) return MPM_ERR_CUDA;
     CKI(cudaMemsetAsync(s->ndispl, 0, sizeof(double) * 3 * c->g.nodec, c->stream));
     CKI(cudaMemsetAsync(s->x, 0, sizeof(double) * 3 * c->g.nodec, c->stream));
     k_imp_predict<<<nb_nodes(c), 256, 0, c->stream>>>(a, s->ndispl, s->nvel, s->naccel, s->naccel_k, nullptr, 1);
@@ -1713,10 +2055,18 @@ mpm_status mpm_gpu_implicit_get_system(mpm_ctx *c, double *stencil, double *adia
     const size_t N = (size_t)c->g.nodec;
     CKI(cudaStreamSynchronize(c->stream));
     if (stencil) {
-        std::vector<double> t(a_size((int)N));
-        CKI(cudaMemcpy(t.data(), s->A, sizeof(double) * t.size(), cudaMemcpyDeviceToHost));
-        for (int q = 0; q < 243; q++)
-            for (size_t n = 0; n < N; n++) stencil[(size_t)q * N + n] = t[aidx(q, (int)n)];
+        const int nq = 9 * imp_args(c).ns;
+        if (s->prec == 64) {
+            std::vector<double> t(a_size((int)N, s->qp));
+            CKI(cudaMemcpy(t.data(), s->A, sizeof(double) * t.size(), cudaMemcpyDeviceToHost));
+            for (int q = 0; q < nq; q++)
+                for (size_t n = 0; n < N; n++) stencil[(size_t)q * N + n] = t[aidx(q, (int)n, s->qp)];
+        } else {
+            std::vector<float> t(a_size((int)N, s->qp));
+            CKI(cudaMemcpy(t.data(), s->A, sizeof(float) * t.size(), cudaMemcpyDeviceToHost));
+            for (int q = 0; q < nq; q++)
+                for (size_t n = 0; n < N; n++) stencil[(size_t)q * N + n] = (double)t[aidx(q, (int)n, s->qp)];
+        }
     }
     if (adiag) CKI(cudaMemcpy(adiag, s->adiag, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost));
     if (b_rhs) CKI(cudaMemcpy(b_rhs, s->b, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost));
@@ -1730,7 +2080,7 @@ mpm_status mpm_gpu_implicit_matvec(mpm_ctx *c, const double *x, double *y) {
     CKI(cudaMemcpyAsync(s->xs, x, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, c->stream));
     ImpArgs a = imp_args(c);
     timer_begin(c, K_MATVEC);
-    k_imp_matvec<<<nb_nodes(c), 256, 0, c->stream>>>(a, s->A, s->xs, s->Ap, nullptr);
+    launch_matvec(c, a, nb_nodes(c), s->xs, s->Ap, nullptr, nullptr, nullptr, 0, true);
     timer_end(c, K_MATVEC);
     c->launches++;
     CKI(cudaMemcpyAsync(y, s->Ap, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, c->stream));
@@ -1783,7 +2133,7 @@ static mpm_status cg_scaled(mpm_ctx *c, double eps, int kmax, mpm_nn *net, int s
             if (st != MPM_OK) return st;
             pairs++;
         }
-        k_imp_matvec<<<nb, 256, 0, c->stream>>>(a, s->A, s->p, s->Ap, s->part, s->cnt + 3, s->scal, S_PAP);
+        launch_matvec(c, a, nb, s->p, s->Ap, s->part, s->cnt + 3, s->scal, S_PAP);
         k_cg_update<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->xs, s->r, s->p, s->Ap, s->part, s->cnt + 4);
         k_cg_dir<<<nb, 256, 0, c->stream>>>(a, s->scal, cur, s->r, s->p);
         it++;

@@ -332,10 +332,16 @@ class GpuSolid:
 
 
 class GpuImplicitSolid(GpuSolid):
-    """The implicit solid (FP64) on the GPU; operator names of implicitmpm::SolidMaterialPoint."""
+    """The implicit solid on the GPU; operator names of implicitmpm::SolidMaterialPoint.
 
-    def __init__(self, scene, nr_flag=False, spec_rad=1.0, shifting=True, stream=None):
-        super().__init__(scene, precision=64, shifting=shifting, stream=stream, implicit=True)
+    precision 64 (default): the FP64 operator (parity mode); 32: FP32
+    particles, assembly, matrix and Krylov matvecs, with FP64 inner products,
+    norms, true residual and Newton check."""
+
+    def __init__(self, scene, nr_flag=False, spec_rad=1.0, shifting=True, stream=None, precision=64):
+        super().__init__(scene, precision=precision, shifting=shifting, stream=stream, implicit=True)
+        self.radius = tuple(int(o) for o in scene.idimc)
+        self.nslots = int(np.prod([2 * r + 1 for r in self.radius]))
         _chk(self.lib.mpm_gpu_implicit_setup(self.ctx, int(nr_flag), float(spec_rad)), "mpm_gpu_implicit_setup")
 
     def implicit_steps(self, n, facl=1.0, eps=1.0e-8, kmax=10000, full=False):
@@ -368,12 +374,13 @@ class GpuImplicitSolid(GpuSolid):
         _chk(self.lib.mpm_gpu_implicit_assemble(self.ctx, facl), "mpm_gpu_implicit_assemble")
 
     def system(self):
+        """(stencil [ns][9][nodec], D^-1/2, RHS) of the last assembled system."""
         n = self.nodec
-        A = np.zeros(27 * 9 * n)
+        A = np.zeros(self.nslots * 9 * n)
         d = np.zeros(3 * n)
         b = np.zeros(3 * n)
         _chk(self.lib.mpm_gpu_implicit_get_system(self.ctx, _ptr(A), _ptr(d), _ptr(b)), "mpm_gpu_implicit_get_system")
-        return A.reshape(27, 9, n), d, b
+        return A.reshape(self.nslots, 9, n), d, b
 
     def matvec(self, x):
         x = _d(x)
@@ -391,12 +398,16 @@ class GpuImplicitSolid(GpuSolid):
         return x, it.value
 
 
-def stencil_to_csr(stencil, xynodec, matrow, matcolid):
-    """Reorder [27][E][nodec] stencil values (E = 9 for the solid's 3x3
-    blocks, 16 for the fluid's 4x4 blocks) into the reference's CSR
-    block-major layout amat[e][j] for the graph (matrow, matcolid) of
-    CrsMat::BuildCrsMat."""
+def stencil_to_csr(stencil, xynodec, matrow, matcolid, radius=(1, 1, 1)):
+    """Reorder [ns][E][nodec] stencil values (E = 9 for the solid's 3x3
+    blocks, 16 for the fluid's 4x4 blocks; ns = prod(2 r + 1) slots for the
+    stencil radius r per axis, the shape order: 27 for linear shape
+    functions, 125 for quadratic B-splines, 75 for idimc 2 1 2) into the
+    reference's CSR block-major layout amat[e][j] for the graph (matrow,
+    matcolid) of CrsMat::BuildCrsMat."""
     nx, ny, nz = xynodec
+    rx, ry, rz = radius
+    sx, sy = 2 * rx + 1, 2 * ry + 1
     nodec = nx * ny * nz
     ne = stencil.shape[1]
     amat = np.zeros((ne, len(matcolid)))
@@ -404,7 +415,7 @@ def stencil_to_csr(stencil, xynodec, matrow, matcolid):
     cols = np.asarray(matcolid)
     ri, rj, rk = rows % nx, (rows // nx) % ny, rows // (nx * ny)
     ci, cj, ck = cols % nx, (cols // nx) % ny, cols // (nx * ny)
-    slot = (ci - ri + 1) + 3 * (cj - rj + 1) + 9 * (ck - rk + 1)
+    slot = (ci - ri + rx) + sx * (cj - rj + ry) + sx * sy * (ck - rk + rz)
     for e in range(ne):
         amat[e] = stencil[slot, e, rows]
     return amat

@@ -15,6 +15,18 @@ reference's own FP64 path without running it:
              shifting on, 1000 steps of dt = 2e-6 s: about an hour on one core.
              Writes tests/golden/fullsize_spinning_block.npz.
 
+--cantilever the 1,728,000-particle Neo-Hookean cantilever (60^3 cells on a
+             64^3 grid, dx = 1e-2 m, 8 particles per cell, E = 1e7 Pa,
+             nu = 0.3, x = 0 face clamped, dt = 1e-3 s), Newton with the
+             implicit solid's own convergence test, 3 steps, each linear
+             system solved to ||r||^2 < 1e-20 ||r0||^2 (far below the
+             reference's default, so that the result does not depend on the
+             Krylov method).  Runs the oracle's C restatement
+             (oracle/mpm_oracle.c, which matches the reference's implicit
+             solid bit for bit at equal tolerance, tests/test_oracle_golden.py)
+             because the reference's GPBiCGSafe stops at its fixed 1e-8.
+             Writes tests/golden/fullsize_cantilever.npz.
+
 The fixture holds the sorted ids of 32,768 particles drawn without
 replacement (seed 4242), their initial coordinates (a test checks that it
 regenerated the same scene), their coordinates, velocities and Voigt stress
@@ -75,12 +87,37 @@ def spinning(nsteps=1000, chunk=50):
     print("wrote", path)
 
 
+def cantilever(nsteps=3, eps=1.0e-20):
+    from oracle import port
+
+    s = scenes.cantilever(iprop=1)
+    ids = sample_ids(s.num)
+    o = port.PortSolid(s, implicit=True, nr_flag=True)
+    t0 = time.time()
+    kt = nt = 0
+    for k in range(nsteps):
+        a, b = o.implicit_steps(1, eps=eps)
+        kt += a
+        nt += b
+        print(f"step {k + 1}/{nsteps}  {time.time() - t0:.0f} s  krylov {a}  newton {b}", flush=True)
+    p = o.particles()
+    out = {"ids": ids, "x0": s.coord[ids], "x": p["x"][ids], "v": p["v"][ids], "sigma": p["sigma"][ids],
+           "F": p["F"][ids], "nsteps": np.array(nsteps), "num": np.array(s.num), "eps": np.array(eps),
+           "krylov": np.array(kt), "newton": np.array(nt), "seconds": np.array(time.time() - t0)}
+    path = os.path.join(OUT, "fullsize_cantilever.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path)
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--spinning", action="store_true")
+    ap.add_argument("--cantilever", action="store_true")
     ap.add_argument("--steps", type=int, default=1000)
     a = ap.parse_args()
-    if not ref.available():
-        raise SystemExit("oracle/_ref/libmpmref.so missing: run oracle/build_ref.sh <reference checkout> first")
+    if a.cantilever:
+        cantilever()
     if a.spinning:
+        if not ref.available():
+            raise SystemExit("oracle/_ref/libmpmref.so missing: run oracle/build_ref.sh <reference checkout> first")
         spinning(a.steps)
