@@ -263,10 +263,11 @@ def run_reference(args):
 def run_implicit(args, torch, stream):
     """The implicit solid: 1,728,000-particle Neo-Hookean cantilever on a 64^3 grid,
     E = 1e7 Pa, nu = 0.3, dt = 1e-3 s, Newton + Krylov solved to a relative
-    residual of 1e-8 (eps = 1e-16 on squared norms), FP64.  Two solids from the
-    same initial state: Jacobi-PCG, and flexible CG with the learned
-    preconditioner (committed parameters trained by mpm_gb300.train_precond,
-    else a short on-the-spot training run, stated in the record)."""
+    residual of 1e-8 (eps = 1e-16 on squared norms).  For the FP32 operator (the
+    record's top level) and the FP64 one ("fp64"), two solids each from the same
+    initial state: Jacobi-PCG, and flexible GCR with the learned preconditioner
+    (committed parameters trained by mpm_gb300.train_precond, else a short
+    on-the-spot training run, stated in the record)."""
     from mpm_gb300 import capi, scenes, train_precond
 
     s = scenes.cantilever(iprop=1)
@@ -297,48 +298,13 @@ def run_implicit(args, torch, stream):
         ev1.synchronize()
         return max(ev0.elapsed_time(ev1), (time.perf_counter() - t0) * 1e3) / reps, its[-1]
 
-    gpu = capi.GpuImplicitSolid(s, nr_flag=True, stream=stream.cuda_stream)
-    jac_ms, jac = timed(gpu)
-    jac_solve_ms, jac_solve_it = timed_solve(gpu)
-    gpu.close()
-    out = {"metric": "implicit step time", "value": jac_ms, "unit": "ms/step", "higher_is_better": False,
-           "steps": args.implicit_steps, "particles": s.num, "grid": list(s.xyelem), "dtype": "f64",
-           "solver": "Newton + Jacobi (symmetric diagonal scaling) CG to ||r||/||r0|| <= 1e-8",
-           "krylov_iters_per_step": jac["krylov_iters"] / args.implicit_steps,
-           "newton_iters_per_step": jac["newton_iters"] / args.implicit_steps}
     params = train_precond.load_weights()
     training = "committed parameters (" + os.path.basename(train_precond.WEIGHTS) + ")"
     if params is None:
         params, rec = train_precond.train(pairs=args.train_pairs, epochs=2, out=None, log=lambda *_: None)
         training = (f"trained in this run: {rec['pairs']} pairs, {rec['epochs']} epochs, "
                     f"{rec['harvest_s'] + rec['train_s']:.0f} s")
-    net = capi.PrecondNet(s.xynodec)
-    net.set_params(params)
-    gpu = capi.GpuImplicitSolid(s, nr_flag=True, stream=stream.cuda_stream)
-    gpu.set_precond(net)
-    nn_ms, nn = timed(gpu)
-    nn_solve_ms, nn_solve_it = timed_solve(gpu)
-    # one application of the network: CUDA-event kernel timers over one more
-    # solve (timers run the solve without graphs; the per-class time is the
-    # network's kernels, from the input scaling to the output layer)
-    gpu.enable_kernel_timing(True)
-    gpu.solve(eps=1.0e-16, download=False)
-    kt = gpu.kernel_times()
-    gpu.enable_kernel_timing(False)
-    gpu.sync()
-    nn_app_ms = kt["precond_nn"][0] / max(kt["precond_nn"][1], 1) if "precond_nn" in kt else None
-    gpu.close()
-    net.close()
-    out["learned"] = {"value": nn_ms, "unit": "ms/step",
-                      "solver": "Newton + flexible GCR(8) with the learned right preconditioner (linear BF16 "
-                                "tcgen05 conv encoder-decoder, z = r + N r) while each 8-iteration window halves "
-                                "the residual, then CG with Jacobi; true FP64 residual <= 1e-8",
-                      "krylov_iters_per_step": nn["krylov_iters"] / args.implicit_steps,
-                      "newton_iters_per_step": nn["newton_iters"] / args.implicit_steps,
-                      "fallbacks": nn["precond_fallbacks"], "network_applications": nn["nn_applications"],
-                      "training": training,
-                      "speedup_vs_jacobi": jac_ms / nn_ms if nn_ms > 0 else None}
-    # algorithmic FLOPs of one application: sum over the five 3x3x3
+    # algorithmic FLOPs of one network application: sum over the five 3x3x3
     # convolutions of output nodes x 2 x 27 x C_in x C_out (real channels)
     n0 = list(s.xynodec)
     n1 = [m // 2 + 1 for m in n0]
@@ -351,19 +317,72 @@ def run_implicit(args, torch, stream):
             tc_peak = json.load(f).get("bf16_tflops")
     except (OSError, ValueError):
         pass
-    if nn_app_ms:
-        ach = flops / (nn_app_ms * 1e-3) / 1e12
-        out["learned"]["network"] = {
-            "us_per_application": nn_app_ms * 1e3, "flops_per_application": flops,
-            "roofline": {"bound": "tensor", "achieved": ach, "peak": tc_peak, "unit": "TFLOP/s",
-                         "frac": ach / tc_peak if tc_peak else None,
-                         "note": "latency-bound: the five convolutions run on 65^3, 33^3 and 17^3 grids "
-                                 "out of L2; the tensor pipe is 7-13 % busy (ncu)"}}
-    out["solve"] = {"what": "one linear solve of the assembled system after the timed steps, from x = 0 to "
-                            "||r||/||r0|| <= 1e-8, solution left on the device",
-                    "jacobi_ms": jac_solve_ms, "jacobi_iters": jac_solve_it,
-                    "learned_ms": nn_solve_ms, "learned_iters": nn_solve_it,
-                    "speedup": jac_solve_ms / nn_solve_ms if nn_solve_ms > 0 else None}
+
+    def arms(prec):
+        """Jacobi-PCG and the learned solver from the same initial state, for the
+        FP32 operator (prec 32) or the FP64 one (prec 64)."""
+        gpu = capi.GpuImplicitSolid(s, nr_flag=True, stream=stream.cuda_stream, precision=prec)
+        jac_ms, jac = timed(gpu)
+        gpu.enable_kernel_timing(True)
+        gpu.implicit_steps(1, eps=1.0e-16)
+        kt_j = gpu.kernel_times()   # per-kernel-class time of one more step (timers run without graphs)
+        gpu.enable_kernel_timing(False)
+        jac_solve_ms, jac_solve_it = timed_solve(gpu)
+        gpu.close()
+        net = capi.PrecondNet(s.xynodec)
+        net.set_params(params)
+        gpu = capi.GpuImplicitSolid(s, nr_flag=True, stream=stream.cuda_stream, precision=prec)
+        gpu.set_precond(net)
+        nn_ms, nn = timed(gpu)
+        nn_solve_ms, nn_solve_it = timed_solve(gpu)
+        # one application of the network: CUDA-event kernel timers over one more
+        # solve (timers run the solve without graphs; the per-class time is the
+        # network's kernels, from the input scaling to the output layer)
+        gpu.enable_kernel_timing(True)
+        gpu.solve(eps=1.0e-16, download=False)
+        kt = gpu.kernel_times()
+        gpu.enable_kernel_timing(False)
+        gpu.sync()
+        nn_app_ms = kt["precond_nn"][0] / max(kt["precond_nn"][1], 1) if "precond_nn" in kt else None
+        gpu.close()
+        net.close()
+        out = {"metric": "implicit step time", "value": jac_ms, "unit": "ms/step", "higher_is_better": False,
+               "steps": args.implicit_steps, "particles": s.num, "grid": list(s.xyelem),
+               "dtype": "f32" if prec == 32 else "f64",
+               "operator": ("FP32 particles, assembly, matrix and Krylov matvecs; FP64 Krylov dots and norms, "
+                            "true residual (FP32 matrix in FP64 arithmetic) and Newton check") if prec == 32
+               else "FP64 throughout",
+               "solver": "Newton + Jacobi (symmetric diagonal scaling) CG to a true ||r||/||r0|| <= 1e-8",
+               "krylov_iters_per_step": jac["krylov_iters"] / args.implicit_steps,
+               "newton_iters_per_step": jac["newton_iters"] / args.implicit_steps,
+               "kernel_ms_one_jacobi_step": {k: round(v[0], 4) for k, v in kt_j.items()}}
+        out["learned"] = {"value": nn_ms, "unit": "ms/step",
+                          "solver": "Newton + flexible GCR(8) with the learned right preconditioner (linear BF16 "
+                                    "tcgen05 conv encoder-decoder, z = r + N r) while each 8-iteration window "
+                                    "halves the residual, then CG with Jacobi; true FP64 residual <= 1e-8",
+                          "krylov_iters_per_step": nn["krylov_iters"] / args.implicit_steps,
+                          "newton_iters_per_step": nn["newton_iters"] / args.implicit_steps,
+                          "fallbacks": nn["precond_fallbacks"], "network_applications": nn["nn_applications"],
+                          "training": training,
+                          "speedup_vs_jacobi": jac_ms / nn_ms if nn_ms > 0 else None,
+                          "target_speedup": 2.0}
+        if nn_app_ms:
+            ach = flops / (nn_app_ms * 1e-3) / 1e12
+            out["learned"]["network"] = {
+                "us_per_application": nn_app_ms * 1e3, "flops_per_application": flops,
+                "roofline": {"bound": "tensor", "achieved": ach, "peak": tc_peak, "unit": "TFLOP/s",
+                             "frac": ach / tc_peak if tc_peak else None,
+                             "note": "latency-bound: the five convolutions run on 65^3, 33^3 and 17^3 grids "
+                                     "out of L2; the tensor pipe is 7-13 % busy (ncu)"}}
+        out["solve"] = {"what": "one linear solve of the assembled system after the timed steps, from x = 0 to "
+                                "||r||/||r0|| <= 1e-8, solution left on the device",
+                        "jacobi_ms": jac_solve_ms, "jacobi_iters": jac_solve_it,
+                        "learned_ms": nn_solve_ms, "learned_iters": nn_solve_it,
+                        "speedup": jac_solve_ms / nn_solve_ms if nn_solve_ms > 0 else None}
+        return out
+
+    out = arms(32)
+    out["fp64"] = arms(64)
     return out
 
 

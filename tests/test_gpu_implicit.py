@@ -22,8 +22,10 @@ IMPLICIT = ["implicit_linear", "implicit_neohookean", "implicit_beam_quadratic",
             "implicit_mooney_rivlin"]
 TIGHT = 1.0e-24
 # FP32 operator against the FP64 oracle after the fixture's steps (relative L2),
-# each linear system solved to a true FP64 relative residual of 1e-8
-FP32_BOUNDS = {"x": 1e-6, "v": 2e-3, "F": 1e-5, "sigma": 2e-3, "vol": 1e-5}
+# each linear system solved to a true FP64 relative residual of 1e-8 (measured
+# on a GB300 over the five fixtures: x <= 5.7e-8, v <= 4.1e-6, F <= 1.2e-9,
+# sigma <= 2.7e-6, vol <= 4.5e-8)
+FP32_BOUNDS = {"x": 5e-7, "v": 5e-5, "F": 1e-8, "sigma": 3e-5, "vol": 5e-7}
 
 
 @pytest.mark.parametrize("name", IMPLICIT)
