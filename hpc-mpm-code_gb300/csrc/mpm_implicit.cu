@@ -1620,13 +1620,13 @@ static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
                 // FP32 operator: the recursive residual carries the rounding of
                 // the FP32 matvecs, so convergence is judged on the true
                 // residual bs - A x (FP64 arithmetic); if it is not below the
-                // tolerance, CG restarts from it (r, and p = r)
+                // tolerance, it replaces the recursive residual (and its norm,
+                // for the next beta) and CG goes on with the same direction
+                // (residual replacement, which keeps the Krylov progress)
                 const int cur = (it & 1) ? S_RR1 : S_RR0;
                 launch_matvec(c, a, nb, s->xs, s->z, nullptr, nullptr, nullptr, 0, true);
                 k_true_residual<<<nb, 256, 0, c->stream>>>(a, s->bs, s->z, s->r, s->part);
                 k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, cur);
-                CKI(cudaMemcpyAsync(s->p, s->r, sizeof(double) * 3 * c->g.nodec, cudaMemcpyDeviceToDevice,
-                                    c->stream));
                 c->launches += 3;
                 CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream));
                 CKI(cudaStreamSynchronize(c->stream));
@@ -1779,6 +1779,16 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
                 it++;
             }
             if (it % check == 0 || it == kmax || fine) {
+                if (s->prec == 32) {
+                    // FP32 operator: the recursive residual drifts from the true one
+                    // by the rounding of the FP32 matvecs, so at every check it is
+                    // replaced by the true residual bs - A x (FP64 arithmetic); the
+                    // kept directions and their images stay valid
+                    launch_matvec(c, a, nb, s->xs, s->z, nullptr, nullptr, nullptr, 0, true);
+                    k_true_residual<<<nb, 256, 0, c->stream>>>(a, s->bs, s->z, s->r, s->part);
+                    k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);
+                    c->launches += 3;
+                }
                 CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * S_NSCAL, cudaMemcpyDeviceToHost, c->stream));
                 CKI(cudaStreamSynchronize(c->stream));
                 double rr = s->h_scal[S_RRC];
@@ -1787,7 +1797,9 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
                     return MPM_ERR_NONFINITE;
                 }
                 if (s->debug) fprintf(stderr, "mpm_gb300 gcr: it %d |r|/|r0| %.3e\n", it, sqrt(rr / rr0));
-                if (rr < eps * rr0) {
+                if (rr < eps * rr0 && s->prec == 32) {
+                    done = true;   // rr is the true residual
+                } else if (rr < eps * rr0) {
                     launch_matvec(c, a, nb, s->xs, s->z, nullptr, nullptr, nullptr, 0, true);
                     k_true_residual<<<nb, 256, 0, c->stream>>>(a, s->bs, s->z, s->r, s->part);
                     k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, S_RRC);

@@ -15,7 +15,11 @@
 // functions only (idimc = 1, the order every fluid deck of the reference uses).
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
 
 #include "mpm_device.cuh"
 
@@ -206,19 +210,12 @@ __global__ void k_ns_inertia(NsArgs a, const double *__restrict__ nvel, const do
 
 }  // namespace
 
-extern "C" mpm_status mpm_gpu_ns_assemble(const mpm_grid_desc *grid, const mpm_ns_params *prm, int64_t n,
-                                          const double *x, const double *mass, const double *vol, const double *nvel,
-                                          const double *naccel, const double *ndispl, const double *npres,
-                                          const double *nmass, double *tau1, double *tau2, double *stencil,
-                                          double *b_rhs, int *status, void *stream) {
-    if (!grid || !prm || n < 0 || !status || !stencil || !b_rhs || !nvel || !naccel || !ndispl || !npres || !nmass)
-        return MPM_ERR_BAD_ARG;
-    if (n > 0 && (!x || !mass || !vol || !tau1 || !tau2)) return MPM_ERR_BAD_ARG;
-    NsArgs a;
+// NsArgs of a grid and the fluid constants; false for an unusable grid
+static bool ns_args(const mpm_grid_desc *grid, const mpm_ns_params *prm, int64_t n, NsArgs &a) {
     memset(&a, 0, sizeof(a));
     int64_t nodec = 1;
     for (int d = 0; d < 3; d++) {
-        if (grid->idimc[d] != 1 || grid->xyelem[d] < 1 || !(grid->dxy[d] > 0.0)) return MPM_ERR_BAD_ARG;
+        if (grid->idimc[d] != 1 || grid->xyelem[d] < 1 || !(grid->dxy[d] > 0.0)) return false;
         a.g.xmin[d] = grid->xymin[d];
         a.g.dx[d] = grid->dxy[d];
         a.g.inv_dx[d] = 1.0 / grid->dxy[d];
@@ -226,7 +223,7 @@ extern "C" mpm_status mpm_gpu_ns_assemble(const mpm_grid_desc *grid, const mpm_n
         a.g.nnc[d] = grid->xyelem[d] + 1;
         nodec *= a.g.nnc[d];
     }
-    if (nodec > (int64_t)INT32_MAX / 27 || !(prm->dt > 0.0) || !(prm->beta_nb > 0.0)) return MPM_ERR_BAD_ARG;
+    if (nodec > (int64_t)INT32_MAX / 27 || !(prm->dt > 0.0) || !(prm->beta_nb > 0.0)) return false;
     a.g.nodec = (int)nodec;
     a.rho = prm->rho;
     a.rmu = prm->rmu;
@@ -242,19 +239,572 @@ extern "C" mpm_status mpm_gpu_ns_assemble(const mpm_grid_desc *grid, const mpm_n
     a.mtol = prm->mtol;
     a.he0 = grid->dxy[0] * cbrt(6.0 / M_PI);
     a.n = n;
-    cudaStream_t st = (cudaStream_t)stream;
-    cudaError_t e = cudaMemsetAsync(stencil, 0, sizeof(double) * 27 * 16 * (size_t)nodec, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(b_rhs, 0, sizeof(double) * 4 * (size_t)nodec, st);
+    return true;
+}
+
+// The system of one Newton iteration into stencil / b_rhs (cleared first) on `st`.
+static cudaError_t ns_assemble_launch(const NsArgs &a, const double *x, const double *mass, const double *vol,
+                                      const double *nvel, const double *naccel, const double *ndispl,
+                                      const double *npres, const double *nmass, double *tau1, double *tau2,
+                                      double *stencil, double *b_rhs, int *status, cudaStream_t st) {
+    const size_t nodec = (size_t)a.g.nodec;
+    cudaError_t e = cudaMemsetAsync(stencil, 0, sizeof(double) * 27 * 16 * nodec, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b_rhs, 0, sizeof(double) * 4 * nodec, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(status, 0, sizeof(int), st);
-    if (e != cudaSuccess) return MPM_ERR_CUDA;
-    if (n > 0)
-        k_ns_assemble<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(a, x, mass, vol, nvel, naccel, ndispl, npres, tau1,
-                                                                    tau2, stencil, b_rhs, status);
+    if (e != cudaSuccess) return e;
+    if (a.n > 0)
+        k_ns_assemble<<<(unsigned)((a.n + 127) / 128), 128, 0, st>>>(a, x, mass, vol, nvel, naccel, ndispl, npres,
+                                                                      tau1, tau2, stencil, b_rhs, status);
     k_ns_inertia<<<(unsigned)((nodec + 255) / 256), 256, 0, st>>>(a, nvel, naccel, ndispl, nmass, b_rhs);
-    e = cudaGetLastError();
+    return cudaGetLastError();
+}
+
+extern "C" mpm_status mpm_gpu_ns_assemble(const mpm_grid_desc *grid, const mpm_ns_params *prm, int64_t n,
+                                          const double *x, const double *mass, const double *vol, const double *nvel,
+                                          const double *naccel, const double *ndispl, const double *npres,
+                                          const double *nmass, double *tau1, double *tau2, double *stencil,
+                                          double *b_rhs, int *status, void *stream) {
+    if (!grid || !prm || n < 0 || !status || !stencil || !b_rhs || !nvel || !naccel || !ndispl || !npres || !nmass)
+        return MPM_ERR_BAD_ARG;
+    if (n > 0 && (!x || !mass || !vol || !tau1 || !tau2)) return MPM_ERR_BAD_ARG;
+    NsArgs a;
+    if (!ns_args(grid, prm, n, a)) return MPM_ERR_BAD_ARG;
+    const cudaError_t e = ns_assemble_launch(a, x, mass, vol, nvel, naccel, ndispl, npres, nmass, tau1, tau2, stencil,
+                                             b_rhs, status, (cudaStream_t)stream);
     if (e != cudaSuccess) {
         fprintf(stderr, "mpm_gpu_ns_assemble: %s\n", cudaGetErrorString(e));
         return MPM_ERR_CUDA;
     }
     return MPM_OK;
+}
+
+// ===================================================================== SolveNS
+// The Newton loop of StabilizedMPM::SolveNS (solve_ns_mpm.cpp:28-62) with the
+// reference's native solver path (use_petsc off): per Newton iteration
+// BCNRSet, the system (k_ns_assemble / k_ns_inertia), BuildDiagonalPreconditioner
+// for 4 degrees of freedom (crsmat.cpp:87-184), GPBiCGSafe on the scaled system
+// (solver.cpp:19-141) restated with device-side reductions, UpdateNRIncrement
+// and CheckNRConvergence (solver.cpp:484-593).  Vectors are component-major
+// [u | v | w | p] of nodec each.
+namespace {
+
+enum NsScal {
+    NS_RTR = 0, NS_RSR, NS_RSR0, NS_BTB, NS_BETA, NS_ALPH, NS_ZETA, NS_ETA, NS_DONE, NS_ITER, NS_RES, NS_IDOF,
+    NS_NSCAL
+};
+
+struct NsVec {
+    double *rr, *rs, *pp, *Ap, *Ar, *Az, *Au, *uu, *zz, *xs, *Ax;
+};
+
+// Sums of V per-thread values over the grid: block partials in part[v * gridDim.x + b];
+// the last block to finish adds them in block order (run-to-run identical) and returns true.
+template <int V>
+__device__ bool ns_reduce(double (&v)[V], double *part, unsigned *cnt, double (&tot)[V]) {
+    __shared__ double sh[V][8];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < V; j++) {
+        double t = v[j];
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) sh[j][wid] = t;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < V) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[threadIdx.x][w];
+        part[threadIdx.x * gridDim.x + blockIdx.x] = t;
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    if ((int)threadIdx.x < V) {
+        double t = 0.0;
+        for (unsigned b = 0; b < gridDim.x; b++) t += __ldcg(part + threadIdx.x * gridDim.x + b);
+        sh[threadIdx.x][0] = t;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < V; j++) tot[j] = sh[j][0];
+    if (threadIdx.x == 0) *cnt = 0u;
+    return true;
+}
+
+// D^-1/2 of the four diagonal entries of every node (ExtractDiagonal + ComputeDiagonalInverseSqrt)
+__global__ void k_nsv_diag(int nodec, double mtol, const double *A, double *adiag) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nodec) return;
+    const size_t N = (size_t)nodec;
+    for (int m = 0; m < 4; m++) {
+        const double d = fabs(A[(size_t)(13 * 16 + 5 * m) * N + n]);
+        adiag[m * N + n] = d < mtol ? 0.0 : 1.0 / sqrt(d);
+    }
+}
+
+// ApplyDiagonalScaling: A_ij <- D_i A_ij D_j
+__global__ void k_nsv_scale_mat(KGeom<double> g, double *A, const double *adiag) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= g.nodec) return;
+    const size_t N = (size_t)g.nodec;
+    const int i = n % g.nnc[0], j = (n / g.nnc[0]) % g.nnc[1], k = n / (g.nnc[0] * g.nnc[1]);
+    for (int s = 0; s < 27; s++) {
+        const int ii = i + s % 3 - 1, jj = j + (s / 3) % 3 - 1, kk = k + s / 9 - 1;
+        if (ii < 0 || jj < 0 || kk < 0 || ii >= g.nnc[0] || jj >= g.nnc[1] || kk >= g.nnc[2]) continue;
+        const size_t col = ii + (size_t)g.nnc[0] * (jj + (size_t)g.nnc[1] * kk);
+        for (int r = 0; r < 4; r++)
+            for (int c = 0; c < 4; c++) A[(size_t)(s * 16 + 4 * r + c) * N + n] *= adiag[r * N + n] * adiag[c * N + col];
+    }
+}
+
+// y = A x with the BC rows zeroed (MatVecMult + BCResidualSet)
+__global__ void __launch_bounds__(256) k_nsv_matvec(KGeom<double> g, const double *__restrict__ A,
+                                                    const unsigned char *__restrict__ bcf, const double *x, double *y,
+                                                    const double *done) {
+    if (done && *done != 0.0) return;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= g.nodec) return;
+    const size_t N = (size_t)g.nodec;
+    const int i = n % g.nnc[0], j = (n / g.nnc[0]) % g.nnc[1], k = n / (g.nnc[0] * g.nnc[1]);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int s = 0; s < 27; s++) {
+        const int ii = i + s % 3 - 1, jj = j + (s / 3) % 3 - 1, kk = k + s / 9 - 1;
+        if (ii < 0 || jj < 0 || kk < 0 || ii >= g.nnc[0] || jj >= g.nnc[1] || kk >= g.nnc[2]) continue;
+        const size_t col = ii + (size_t)g.nnc[0] * (jj + (size_t)g.nnc[1] * kk);
+        const double xc[4] = {x[col], x[N + col], x[2 * N + col], x[3 * N + col]};
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) acc[r] = fma(__ldg(A + (size_t)(s * 16 + 4 * r + c) * N + n), xc[c], acc[r]);
+    }
+    const unsigned char f = bcf[n];
+#pragma unroll
+    for (int r = 0; r < 4; r++) y[r * N + n] = (f >> r) & 1 ? 0.0 : acc[r];
+}
+
+// ScaleSolution + BCResidualSet: xs = x / D, rr = b D (zero where D < mtol and on BC rows)
+__global__ void k_nsv_scale_in(int nodec, double mtol, const unsigned char *bcf, const double *x, const double *b,
+                               const double *adiag, double *xs, double *rr) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nodec) return;
+    const size_t N = (size_t)nodec;
+    const unsigned char f = bcf[n];
+    for (int m = 0; m < 4; m++) {
+        const size_t i = m * N + n;
+        const double d = adiag[i];
+        xs[i] = d < mtol ? 0.0 : x[i] / d;
+        rr[i] = (d < mtol || ((f >> m) & 1)) ? 0.0 : b[i] * d;
+    }
+}
+
+// rr = rr - Ax, rs = rr, the other GPBiCGSafe vectors zero; rtr (= rsr = btb), beta = 0
+__global__ void __launch_bounds__(256) k_nsv_init(int nodec, NsVec v, double *part, unsigned *cnt, double *scal) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    double d[1] = {0.0};
+    if (n < nodec) {
+        const size_t N = (size_t)nodec;
+        for (int m = 0; m < 4; m++) {
+            const size_t i = m * N + n;
+            const double r = v.rr[i] - v.Ax[i];
+            v.rr[i] = r;
+            v.rs[i] = r;
+            v.pp[i] = v.Ap[i] = v.Au[i] = v.Az[i] = v.uu[i] = v.zz[i] = 0.0;
+            d[0] += r * r;
+        }
+    }
+    double t[1];
+    if (!ns_reduce<1>(d, part, cnt, t)) return;
+    if (threadIdx.x == 0) {
+        scal[NS_RTR] = scal[NS_RSR] = scal[NS_BTB] = t[0];
+        scal[NS_BETA] = 0.0;
+        scal[NS_ITER] = 0.0;
+        scal[NS_DONE] = 0.0;
+    }
+}
+
+// pp = rr + beta (pp - uu), Ap = Ar + beta (Ap - Au); the six dots; then alpha, zeta, eta
+__global__ void __launch_bounds__(256) k_gpb_1(int nodec, NsVec v, double *part, unsigned *cnt, double *scal) {
+    if (scal[NS_DONE] != 0.0) return;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const double beta = scal[NS_BETA];
+    double d[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (n < nodec) {
+        const size_t N = (size_t)nodec;
+        for (int m = 0; m < 4; m++) {
+            const size_t i = m * N + n;
+            const double p = v.rr[i] + beta * (v.pp[i] - v.uu[i]);
+            const double ap = v.Ar[i] + beta * (v.Ap[i] - v.Au[i]);
+            v.pp[i] = p;
+            v.Ap[i] = ap;
+            const double az = v.Az[i], ar = v.Ar[i], r = v.rr[i];
+            d[0] += v.rs[i] * ap;
+            d[1] += az * az;
+            d[2] += ar * r;
+            d[3] += az * r;
+            d[4] += ar * az;
+            d[5] += ar * ar;
+        }
+    }
+    double t[6];
+    if (!ns_reduce<6>(d, part, cnt, t)) return;
+    if (threadIdx.x == 0) {
+        const double rAp = t[0], AzAz = t[1], Arrr = t[2], Azrr = t[3], ArAz = t[4], ArAr = t[5];
+        scal[NS_RSR0] = scal[NS_RSR];
+        scal[NS_ALPH] = scal[NS_RSR] / rAp;
+        if (scal[NS_ITER] == 0.0) {
+            scal[NS_ZETA] = Arrr / ArAr;
+            scal[NS_ETA] = 0.0;
+        } else {
+            const double den = ArAr * AzAz - ArAz * ArAz;
+            scal[NS_ZETA] = (AzAz * Arrr - Azrr * ArAz) / den;
+            scal[NS_ETA] = (ArAr * Azrr - ArAz * Arrr) / den;
+        }
+    }
+}
+
+// uu = zeta Ap + eta (Az + beta uu)
+__global__ void k_gpb_2(int nodec, NsVec v, const double *scal) {
+    if (scal[NS_DONE] != 0.0) return;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nodec) return;
+    const double zeta = scal[NS_ZETA], eta = scal[NS_ETA], beta = scal[NS_BETA];
+    const size_t N = (size_t)nodec;
+    for (int m = 0; m < 4; m++) {
+        const size_t i = m * N + n;
+        v.uu[i] = zeta * v.Ap[i] + eta * (v.Az[i] + beta * v.uu[i]);
+    }
+}
+
+// tt = rr - alpha Ap; zz = zeta rr + eta zz - alpha uu; Az = zeta Ar + eta Az - alpha Au;
+// x += alpha pp + zz; rr = tt - Az; then rsr, rtr, the stopping test rtr < eps btb and beta
+__global__ void __launch_bounds__(256) k_gpb_3(int nodec, NsVec v, double eps, double *part, unsigned *cnt,
+                                               double *scal) {
+    if (scal[NS_DONE] != 0.0) return;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const double alph = scal[NS_ALPH], zeta = scal[NS_ZETA], eta = scal[NS_ETA];
+    double d[2] = {0.0, 0.0};
+    if (n < nodec) {
+        const size_t N = (size_t)nodec;
+        for (int m = 0; m < 4; m++) {
+            const size_t i = m * N + n;
+            const double r = v.rr[i];
+            const double tt = r - alph * v.Ap[i];
+            const double zz = zeta * r + eta * v.zz[i] - alph * v.uu[i];
+            const double az = zeta * v.Ar[i] + eta * v.Az[i] - alph * v.Au[i];
+            v.zz[i] = zz;
+            v.Az[i] = az;
+            v.xs[i] += alph * v.pp[i] + zz;
+            const double rn = tt - az;
+            v.rr[i] = rn;
+            d[0] += v.rs[i] * rn;
+            d[1] += rn * rn;
+        }
+    }
+    double t[2];
+    if (!ns_reduce<2>(d, part, cnt, t)) return;
+    if (threadIdx.x == 0) {
+        scal[NS_RSR] = t[0];
+        scal[NS_RTR] = t[1];
+        scal[NS_ITER] += 1.0;
+        if (t[1] < eps * scal[NS_BTB]) scal[NS_DONE] = 1.0;
+        else scal[NS_BETA] = (alph / zeta) * (t[0] / scal[NS_RSR0]);
+    }
+}
+
+// RestorSolution: x = xs D (zero where D <= mtol)
+__global__ void k_nsv_restore(int nodec, double mtol, const double *xs, const double *adiag, double *x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 4 * nodec) return;
+    x[i] = adiag[i] > mtol ? xs[i] * adiag[i] : 0.0;
+}
+
+// x_pre = x / D for the physical residual (ComputeRefResidual)
+__global__ void k_nsv_prep(int nodec, double mtol, const double *x, const double *adiag, double *xp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 4 * nodec) return;
+    xp[i] = adiag[i] > mtol ? x[i] / adiag[i] : 0.0;
+}
+
+// r = b - (A x_pre) / D with b's BC rows zeroed: r.r and the active row count
+__global__ void __launch_bounds__(256) k_nsv_resid(int nodec, double mtol, const unsigned char *bcf, const double *b,
+                                                   const double *Ax, const double *adiag, double *part, unsigned *cnt,
+                                                   double *scal) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    double d[2] = {0.0, 0.0};
+    if (n < nodec) {
+        const size_t N = (size_t)nodec;
+        const unsigned char f = bcf[n];
+        for (int m = 0; m < 4; m++) {
+            const size_t i = m * N + n;
+            const double bi = ((f >> m) & 1) ? 0.0 : b[i];
+            const double ax = adiag[i] > mtol ? Ax[i] / adiag[i] : 0.0;
+            const double r = bi - ax;
+            d[0] += r * r;
+            d[1] += adiag[i] > mtol ? 1.0 : 0.0;
+        }
+    }
+    double t[2];
+    if (!ns_reduce<2>(d, part, cnt, t)) return;
+    if (threadIdx.x == 0) {
+        scal[NS_RES] = t[0];
+        scal[NS_IDOF] = t[1];
+    }
+}
+
+// BCNRSet: ndispl = fbc dt facl on the u/v/w lists, npres = fbc facl on the p list
+__global__ void k_nsv_bcnr(int nodec, const unsigned char *bcf, const double *bcv, double dt_facl, double facl,
+                           double *ndispl, double *npres) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nodec) return;
+    const size_t N = (size_t)nodec;
+    const unsigned char f = bcf[n];
+    for (int m = 0; m < 3; m++)
+        if ((f >> m) & 1) ndispl[m * N + n] = bcv[m * N + n] * dt_facl;
+    if ((f >> 3) & 1) npres[n] = bcv[3 * N + n] * facl;
+}
+
+// UpdateNRIncrement: ndispl += x[0..3N), npres += x[3N..4N)
+__global__ void k_nsv_update(int nodec, const double *x, double *ndispl, double *npres) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 4 * nodec) return;
+    if (i < 3 * nodec) ndispl[i] += x[i];
+    else npres[i - 3 * nodec] += x[i];
+}
+
+}  // namespace
+
+struct mpm_ns {
+    mpm_grid_desc grid;
+    mpm_ns_params prm;
+    NsArgs a;
+    cudaStream_t stream = nullptr;
+    int nodec = 0;
+    double *A = nullptr, *b = nullptr, *adiag = nullptr, *x = nullptr, *bcv = nullptr, *part = nullptr;
+    double *scal = nullptr, *h_scal = nullptr;
+    unsigned char *bcf = nullptr;
+    unsigned *cnt = nullptr;
+    int *status = nullptr;
+    NsVec v{};
+    std::vector<int> bc_nodes[4];
+    std::vector<double> bc_vals[4];
+};
+
+#define CKN(call)                                                                                                      \
+    do {                                                                                                               \
+        cudaError_t _e = (call);                                                                                       \
+        if (_e != cudaSuccess) {                                                                                       \
+            fprintf(stderr, "mpm_gb300: %s failed: %s\n", #call, cudaGetErrorString(_e));                              \
+            return _e == cudaErrorMemoryAllocation ? MPM_ERR_OOM : MPM_ERR_CUDA;                                       \
+        }                                                                                                              \
+    } while (0)
+
+extern "C" void mpm_ns_destroy(mpm_ns *s) {
+    if (!s) return;
+    void *bufs[] = {s->A,    s->b,      s->adiag, s->x,    s->bcv,  s->part, s->scal, s->bcf,
+                    s->cnt,  s->status, s->v.rr,  s->v.rs, s->v.pp, s->v.Ap, s->v.Ar, s->v.Az,
+                    s->v.Au, s->v.uu,   s->v.zz,  s->v.xs, s->v.Ax};
+    for (void *p : bufs)
+        if (p) cudaFree(p);
+    if (s->h_scal) cudaFreeHost(s->h_scal);
+    delete s;
+}
+
+extern "C" mpm_status mpm_ns_create(const mpm_grid_desc *grid, const mpm_ns_params *prm, mpm_ns **out) {
+    if (!grid || !prm || !out) return MPM_ERR_BAD_ARG;
+    *out = nullptr;
+    NsArgs a;
+    if (!ns_args(grid, prm, 0, a)) return MPM_ERR_BAD_ARG;
+    mpm_ns *s = new (std::nothrow) mpm_ns();
+    if (!s) return MPM_ERR_OOM;
+    s->grid = *grid;
+    s->prm = *prm;
+    s->a = a;
+    s->nodec = a.g.nodec;
+    const size_t N = (size_t)a.g.nodec;
+    const int nb = (int)((N + 255) / 256);
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](void **p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    };
+    alloc((void **)&s->A, sizeof(double) * 27 * 16 * N);
+    alloc((void **)&s->b, sizeof(double) * 4 * N);
+    alloc((void **)&s->adiag, sizeof(double) * 4 * N);
+    alloc((void **)&s->x, sizeof(double) * 4 * N);
+    alloc((void **)&s->bcv, sizeof(double) * 4 * N);
+    alloc((void **)&s->part, sizeof(double) * 8 * (size_t)nb);
+    alloc((void **)&s->scal, sizeof(double) * NS_NSCAL);
+    alloc((void **)&s->bcf, N);
+    alloc((void **)&s->cnt, sizeof(unsigned) * 4);
+    alloc((void **)&s->status, sizeof(int));
+    double **vecs[] = {&s->v.rr, &s->v.rs, &s->v.pp, &s->v.Ap, &s->v.Ar, &s->v.Az,
+                       &s->v.Au, &s->v.uu, &s->v.zz, &s->v.xs, &s->v.Ax};
+    for (double **p : vecs) alloc((void **)p, sizeof(double) * 4 * N);
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&s->h_scal, sizeof(double) * NS_NSCAL);
+    if (e == cudaSuccess) e = cudaMemset(s->cnt, 0, sizeof(unsigned) * 4);
+    if (e == cudaSuccess) e = cudaMemset(s->bcf, 0, N);
+    if (e == cudaSuccess) e = cudaMemset(s->bcv, 0, sizeof(double) * 4 * N);
+    if (e == cudaSuccess) e = cudaMemset(s->scal, 0, sizeof(double) * NS_NSCAL);
+    if (e != cudaSuccess) {
+        mpm_ns_destroy(s);
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? MPM_ERR_OOM : MPM_ERR_CUDA;
+    }
+    *out = s;
+    return MPM_OK;
+}
+
+extern "C" mpm_status mpm_ns_set_stream(mpm_ns *s, void *stream) {
+    if (!s) return MPM_ERR_BAD_ARG;
+    s->stream = (cudaStream_t)stream;
+    return MPM_OK;
+}
+
+extern "C" mpm_status mpm_ns_set_bc(mpm_ns *s, int comp, int n, const int *nodes, const double *vals) {
+    if (!s || comp < 0 || comp > 3 || n < 0 || (n > 0 && (!nodes || !vals))) return MPM_ERR_BAD_ARG;
+    for (int i = 0; i < n; i++)
+        if (nodes[i] < 0 || nodes[i] >= s->nodec) return MPM_ERR_BAD_ARG;
+    s->bc_nodes[comp].assign(nodes, nodes + n);
+    s->bc_vals[comp].assign(vals, vals + n);
+    const size_t N = (size_t)s->nodec;
+    std::vector<unsigned char> flag(N, 0);
+    std::vector<double> val(4 * N, 0.0);
+    for (int k = 0; k < 4; k++)
+        for (size_t i = 0; i < s->bc_nodes[k].size(); i++) {   // later entries win, as the BC loops
+            const int nd = s->bc_nodes[k][i];
+            flag[nd] |= (unsigned char)(1 << k);
+            val[k * N + nd] = s->bc_vals[k][i];
+        }
+    CKN(cudaStreamSynchronize(s->stream));
+    CKN(cudaMemcpy(s->bcf, flag.data(), N, cudaMemcpyHostToDevice));
+    CKN(cudaMemcpy(s->bcv, val.data(), sizeof(double) * 4 * N, cudaMemcpyHostToDevice));
+    return MPM_OK;
+}
+
+// ||b - A x|| and sqrt(rtr / idof) of the scaled system in s (ComputeRefResidual /
+// ComputeAbsResidual); x is physical.  Synchronises the stream.
+static mpm_status ns_residual(mpm_ns *s, const double *x, double *ref, double *absr) {
+    const int nodec = s->nodec, nb = (nodec + 255) / 256, nb4 = (4 * nodec + 255) / 256;
+    k_nsv_prep<<<nb4, 256, 0, s->stream>>>(nodec, s->a.mtol, x, s->adiag, s->v.Ax);
+    k_nsv_matvec<<<nb, 256, 0, s->stream>>>(s->a.g, s->A, s->bcf, s->v.Ax, s->v.Ar, nullptr);
+    k_nsv_resid<<<nb, 256, 0, s->stream>>>(nodec, s->a.mtol, s->bcf, s->b, s->v.Ar, s->adiag, s->part, s->cnt,
+                                           s->scal);
+    CKN(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * NS_NSCAL, cudaMemcpyDeviceToHost, s->stream));
+    CKN(cudaStreamSynchronize(s->stream));
+    const double rtr = s->h_scal[NS_RES], idof = s->h_scal[NS_IDOF];
+    *ref = sqrt(rtr);
+    if (absr) *absr = idof <= 1.0e-30 ? 0.0 : sqrt(rtr / idof);
+    return MPM_OK;
+}
+
+// One GPBiCGSafe call (solver.cpp:19-141) on the scaled system from the current
+// physical s->x, stopped at rtr < eps btb as the reference does, or at kmax
+// iterations.  Iterations are launched in blocks of 8; once the device-side
+// test has stopped the solve the remaining launches of a block return at once.
+static mpm_status ns_gpbicgsafe(mpm_ns *s, double eps, int kmax, int *iters) {
+    const int nodec = s->nodec, nb = (nodec + 255) / 256, nb4 = (4 * nodec + 255) / 256;
+    cudaStream_t st = s->stream;
+    const double *done = s->scal + NS_DONE;
+    k_nsv_scale_in<<<nb, 256, 0, st>>>(nodec, s->a.mtol, s->bcf, s->x, s->b, s->adiag, s->v.xs, s->v.rr);
+    k_nsv_matvec<<<nb, 256, 0, st>>>(s->a.g, s->A, s->bcf, s->v.xs, s->v.Ax, nullptr);
+    k_nsv_init<<<nb, 256, 0, st>>>(nodec, s->v, s->part, s->cnt, s->scal);
+    int it = 0;
+    bool finished = false;
+    while (!finished && it < kmax) {
+        const int blk = kmax - it < 8 ? kmax - it : 8;
+        for (int k = 0; k < blk; k++) {
+            k_nsv_matvec<<<nb, 256, 0, st>>>(s->a.g, s->A, s->bcf, s->v.rr, s->v.Ar, done);
+            k_gpb_1<<<nb, 256, 0, st>>>(nodec, s->v, s->part, s->cnt + 1, s->scal);
+            k_gpb_2<<<nb, 256, 0, st>>>(nodec, s->v, s->scal);
+            k_nsv_matvec<<<nb, 256, 0, st>>>(s->a.g, s->A, s->bcf, s->v.uu, s->v.Au, done);
+            k_gpb_3<<<nb, 256, 0, st>>>(nodec, s->v, eps, s->part, s->cnt + 2, s->scal);
+        }
+        CKN(cudaGetLastError());
+        CKN(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * NS_NSCAL, cudaMemcpyDeviceToHost, st));
+        CKN(cudaStreamSynchronize(st));
+        it = (int)s->h_scal[NS_ITER];
+        if (s->h_scal[NS_RTR] != s->h_scal[NS_RTR]) return MPM_ERR_NONFINITE;
+        finished = s->h_scal[NS_DONE] != 0.0;
+    }
+    k_nsv_restore<<<nb4, 256, 0, st>>>(nodec, s->a.mtol, s->v.xs, s->adiag, s->x);
+    CKN(cudaGetLastError());
+    *iters = it;
+    return finished ? MPM_OK : MPM_ERR_KRYLOV_MAXIT;
+}
+
+extern "C" mpm_status mpm_ns_solve(mpm_ns *s, int64_t n, const double *x, const double *mass, const double *vol,
+                                   const double *nvel, const double *naccel, const double *nmass, double *ndispl,
+                                   double *npres, double *tau1, double *tau2, double rtol, int kmax,
+                                   mpm_ns_stats *stats) {
+    if (!s || n < 0 || !nvel || !naccel || !nmass || !ndispl || !npres || !(rtol > 0.0) || kmax < 1)
+        return MPM_ERR_BAD_ARG;
+    if (n > 0 && (!x || !mass || !vol || !tau1 || !tau2)) return MPM_ERR_BAD_ARG;
+    const int nodec = s->nodec, nb = (nodec + 255) / 256, nb4 = (4 * nodec + 255) / 256;
+    const size_t N = (size_t)nodec;
+    cudaStream_t st = s->stream;
+    NsArgs a = s->a;
+    a.n = n;
+    // SolveNS: ndispl, npres and the solver's iterate start at zero
+    CKN(cudaMemsetAsync(ndispl, 0, sizeof(double) * 3 * N, st));
+    CKN(cudaMemsetAsync(npres, 0, sizeof(double) * N, st));
+    CKN(cudaMemsetAsync(s->x, 0, sizeof(double) * 4 * N, st));
+    const int iter_max = 100;
+    double r0r = 0.0, rkr = 0.0, rabs = 0.0;
+    int NR_it, ktot = 0;
+    mpm_status rc = MPM_OK;
+    for (NR_it = 0; NR_it <= iter_max; NR_it++) {
+        k_nsv_bcnr<<<nb, 256, 0, st>>>(nodec, s->bcf, s->bcv, s->prm.dt * s->prm.facl, s->prm.facl, ndispl, npres);
+        CKN(cudaGetLastError());
+        CKN(ns_assemble_launch(a, x, mass, vol, nvel, naccel, ndispl, npres, nmass, tau1, tau2, s->A, s->b,
+                               s->status, st));
+        k_nsv_diag<<<nb, 256, 0, st>>>(nodec, a.mtol, s->A, s->adiag);
+        k_nsv_scale_mat<<<nb, 256, 0, st>>>(a.g, s->A, s->adiag);
+        CKN(cudaGetLastError());
+        int bad = 0;
+        CKN(cudaMemcpyAsync(&bad, s->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CKN(cudaStreamSynchronize(st));
+        if (bad) {
+            rc = MPM_ERR_PARTICLE_OUT_OF_BOX;
+            break;
+        }
+        // the linear solve: GPBiCGSafe at the reference's own test (eps 1e-8 on
+        // squared norms), called again from where it stopped until the physical
+        // residual is below rtol ||b|| (||b|| with the BC rows zeroed: the
+        // residual of x = 0)
+        CKN(cudaMemsetAsync(s->v.xs, 0, sizeof(double) * 4 * N, st));
+        double bnorm;
+        mpm_status q = ns_residual(s, s->v.xs, &bnorm, nullptr);
+        if (q != MPM_OK) return q;
+        for (int call = 0; call < 20; call++) {
+            double r;
+            q = ns_residual(s, s->x, &r, nullptr);
+            if (q != MPM_OK) return q;
+            if (r <= rtol * bnorm) break;
+            int k = 0;
+            rc = ns_gpbicgsafe(s, 1.0e-8, kmax, &k);
+            ktot += k;
+            if (rc != MPM_OK) break;
+        }
+        if (rc != MPM_OK) break;
+        k_nsv_update<<<nb4, 256, 0, st>>>(nodec, s->x, ndispl, npres);
+        CKN(cudaGetLastError());
+        // CheckNRConvergence: the residual of the solved linear system
+        q = ns_residual(s, s->x, &rkr, &rabs);
+        if (q != MPM_OK) return q;
+        if (NR_it == 0) r0r = rkr;
+        const double rref = r0r > 1.0e-30 ? rkr / r0r : 0.0;
+        if (rref < 1.0e-6 || r0r < 1.0e-6 || rabs < 1.0e-8) break;
+    }
+    if (rc == MPM_OK && NR_it > iter_max) rc = MPM_ERR_NEWTON_MAXIT;
+    if (stats) {
+        stats->newton_iters = NR_it > iter_max ? iter_max + 1 : NR_it + 1;
+        stats->krylov_iters = ktot;
+        stats->r0r = r0r;
+        stats->last_residual = rkr;
+        stats->last_abs_residual = rabs;
+    }
+    return rc;
 }

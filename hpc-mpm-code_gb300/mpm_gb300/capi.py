@@ -79,7 +79,8 @@ EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_s
            "mpm_gpu_get_tuning", "mpm_nn_num_params", "mpm_nn_create", "mpm_nn_destroy", "mpm_nn_set_stream",
            "mpm_nn_init_params", "mpm_nn_set_linear", "mpm_nn_set_additive", "mpm_nn_set_symmetric", "mpm_nn_set_params", "mpm_nn_get_params", "mpm_nn_forward", "mpm_nn_backward",
            "mpm_nn_num_pairs", "mpm_nn_train", "mpm_gpu_implicit_set_precond", "mpm_gpu_implicit_harvest", "mpm_gpu_implicit_apply_precond",
-           "mpm_gpu_set_graph", "mpm_gpu_set_tuning", "mpm_gpu_selftest_wait"]
+           "mpm_gpu_set_graph", "mpm_gpu_set_tuning", "mpm_gpu_selftest_wait", "mpm_ns_create", "mpm_ns_destroy",
+           "mpm_ns_set_stream", "mpm_ns_set_bc", "mpm_ns_solve"]
 
 
 def load(path: str | None = None):
@@ -533,3 +534,78 @@ def ns_assemble(xyelem, xymin, dxy, rho, rmu, dt, beta, gamma, gravity, facl, mt
     if int(status.item()) != 0:
         raise RuntimeError("mpm_gpu_ns_assemble: a particle lies outside the grid")
     return tau1, tau2, st.view(27, 16, nodec), b
+
+
+class NsStats(C.Structure):
+    _fields_ = [("newton_iters", C.c_int), ("krylov_iters", C.c_int), ("r0r", C.c_double),
+                ("last_residual", C.c_double), ("last_abs_residual", C.c_double)]
+
+
+class NsSolver:
+    """StabilizedMPM::SolveNS (module/fluid/MPM/solve_ns_mpm.cpp:28-62) on the GPU:
+    mpm_ns_create / mpm_ns_set_bc / mpm_ns_solve.  bcs: four (nodes, values)
+    pairs for u, v, w, p (ubc, vbc, wbc, pbc)."""
+
+    def __init__(self, xyelem, xymin, dxy, rho, rmu, dt, beta, gamma, gravity, facl, mtol, bcs=None,
+                 stream=None):
+        import torch
+
+        self.lib = lib = load()
+        lib.mpm_ns_create.argtypes = [C.POINTER(GridDesc), C.POINTER(NsParams), C.POINTER(C.c_void_p)]
+        lib.mpm_ns_destroy.argtypes = [C.c_void_p]
+        lib.mpm_ns_destroy.restype = None
+        lib.mpm_ns_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+        lib.mpm_ns_set_bc.argtypes = [C.c_void_p, C.c_int, C.c_int, _ip, _dp]
+        lib.mpm_ns_solve.argtypes = [C.c_void_p, C.c_int64] + [C.c_void_p] * 10 + [C.c_double, C.c_int,
+                                                                                    C.POINTER(NsStats)]
+        g = GridDesc()
+        for d in range(3):
+            g.xyelem[d] = int(xyelem[d])
+            g.xymin[d] = float(xymin[d])
+            g.dxy[d] = float(dxy[d])
+            g.idimc[d] = 1
+            g.npxye[d] = 2
+        p = NsParams(rho, rmu, dt, beta, gamma, (C.c_double * 3)(*[float(v) for v in gravity]), facl, mtol)
+        h = C.c_void_p()
+        _chk(lib.mpm_ns_create(C.byref(g), C.byref(p), C.byref(h)), "mpm_ns_create")
+        self.ns = h
+        self.nodec = int(np.prod(np.asarray(xyelem) + 1))
+        self.stream = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        _chk(lib.mpm_ns_set_stream(self.ns, C.c_void_p(self.stream)), "mpm_ns_set_stream")
+        for comp, (nodes, vals) in enumerate(bcs or []):
+            self.set_bc(comp, nodes, vals)
+
+    def set_bc(self, comp, nodes, vals):
+        nodes = np.ascontiguousarray(nodes, dtype=np.int32)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        _chk(self.lib.mpm_ns_set_bc(self.ns, comp, len(nodes), _ptr(nodes, _ip), _ptr(vals)), "mpm_ns_set_bc")
+
+    def solve(self, x, mass, vol, nvel, naccel, nmass, rtol=1.0e-10, kmax=10000):
+        """FP64 CUDA tensors as ns_assemble (x (3, n) or (3*n,)); returns
+        (ndispl, npres, tau1, tau2) as CUDA tensors and the stats dict."""
+        import torch
+
+        for t in (x, mass, vol, nvel, naccel, nmass):
+            if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+                raise ValueError("NsSolver.solve: inputs must be contiguous FP64 CUDA tensors")
+        dev = mass.device
+        n = int(mass.numel())
+        f = lambda k: torch.empty(k, dtype=torch.float64, device=dev)
+        nd, npres, t1, t2 = f(3 * self.nodec), f(self.nodec), f(max(n, 1)), f(max(n, 1))
+        st = NsStats()
+        rc = self.lib.mpm_ns_solve(self.ns, n, x.data_ptr(), mass.data_ptr(), vol.data_ptr(), nvel.data_ptr(),
+                                   naccel.data_ptr(), nmass.data_ptr(), nd.data_ptr(), npres.data_ptr(),
+                                   t1.data_ptr(), t2.data_ptr(), float(rtol), int(kmax), C.byref(st))
+        _chk(rc, "mpm_ns_solve")
+        return (nd, npres, t1[:n], t2[:n]), {k: getattr(st, k) for k, _ in NsStats._fields_}
+
+    def close(self):
+        if getattr(self, "ns", None):
+            self.lib.mpm_ns_destroy(self.ns)
+            self.ns = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

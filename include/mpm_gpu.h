@@ -67,8 +67,8 @@ typedef struct {
  * the model numbers of ConstitutiveModel::UpdateStress
  * (module/solid/constitutive_model.cpp:287-305): -1 rigid, 0 linear elastic,
  * 1 Neo-Hookean, 2 St.Venant-Kirchhoff ({E, nu, -}), 3 Mooney-Rivlin
- * ({c1, c2, bulk modulus}).  Implicit contexts take -1, 0 and 1 (the models
- * with a GPU tangent); explicit contexts all of them and
+ * ({c1, c2, bulk modulus}).  Implicit contexts take -1 to 3 (each with its
+ * tangent of ComputeTangentModulus); explicit contexts all of them and
  * iprop 4 (no counterpart in the reference): a weakly compressible Newtonian
  * fluid with the Tait equation of state, mat_prop = {c0 (speed of sound),
  * gamma, mu (dynamic viscosity)}; the rest density is each particle's
@@ -228,13 +228,19 @@ mpm_status mpm_gpu_set_tuning(mpm_ctx *ctx, int p2g_minb, int musl_minb, int upd
 mpm_status mpm_gpu_kernel_times(mpm_ctx *ctx, int *count, const char **names, double *ms, int64_t *launches);
 
 /* ---- the implicit solid (module/solid/implicit/, module/solver/) ----------------
- * A context created with cfg->implicit = 1 and precision 64 (linear shape
- * functions).  mpm_gpu_implicit_setup replaces the solid set-up of the FSI
- * driver: GeneralizedAlphaParaSet + NewmarkBetaParaSet
+ * A context created with cfg->implicit = 1, linear or quadratic B-spline
+ * shape functions (idimc 1 1 1, 2 2 2 or 2 1 2) and precision 64 (the FP64
+ * operator, the parity mode) or 32 (the FP32 operator: FP32 particles,
+ * assembly, matrix and Krylov matvecs; FP64 Krylov inner products and norms,
+ * true residual b - A x with the FP32 matrix applied in FP64 arithmetic, and
+ * Newton check; the FP32 solves replace their recursive residual by the true
+ * one at their checks).  mpm_gpu_implicit_setup replaces the solid set-up of
+ * the FSI driver: GeneralizedAlphaParaSet + NewmarkBetaParaSet
  * (module/nonlinear_time_integration.cpp:10-56, spec_rad = 1 gives
  * alpha_f = alpha_m = 0.5, Newmark beta = 1/4, gamma = 1/2) and
- * CrsMat::BuildCrsMat (module/solver/crsmat.cpp:21-81; here a 27-point block
- * stencil).  nr_flag as MaterialPoint::NR_flag (module/material_point.h:134). */
+ * CrsMat::BuildCrsMat (module/solver/crsmat.cpp:21-81; here a block stencil of
+ * 27 slots for linear shapes, 125 for quadratic ones, 75 for idimc 2 1 2).
+ * nr_flag as MaterialPoint::NR_flag (module/material_point.h:134). */
 typedef struct {
     int newton_iters;          /* linear solves (Newton iterations) over the call */
     int krylov_iters;          /* CG iterations over the call */
@@ -253,7 +259,8 @@ mpm_status mpm_gpu_implicit_step(mpm_ctx *ctx, int nsteps, double facl, double e
                                  mpm_solve_stats *stats);
 /* Test hooks.  assemble: Particle2Node + the first Newton system of a step
  * (ndispl = 0), scaled as BuildDiagonalPreconditioner leaves it.
- * get_system: stencil values [27][9][nodec] (slot s = (dx+1)+3(dy+1)+9(dz+1),
+ * get_system: stencil values [ns][9][nodec] (ns slots, slot s = (dx+r0) +
+ * (2 r0 + 1)((dy+r1) + (2 r1 + 1)(dz+r2)) for the radius r = idimc per axis,
  * entry 3a+b), D^-1/2 and the RHS (3*nodec each).  matvec: y = A x with BC
  * rows zeroed, CrsMat::MatVecMult (module/solver/solver.cpp:405-433), host
  * arrays of 3*nodec.  solve: the assembled system from x = 0, physical x
@@ -373,6 +380,47 @@ mpm_status mpm_gpu_ns_assemble(const mpm_grid_desc *grid, const mpm_ns_params *p
                                const double *mass, const double *vol, const double *nvel, const double *naccel,
                                const double *ndispl, const double *npres, const double *nmass, double *tau1,
                                double *tau2, double *stencil, double *b_rhs, int *status, void *stream);
+
+/* ---- stabilized incompressible fluid: the Newton loop of one time step ------
+ * Replaces StabilizedMPM::SolveNS (module/fluid/MPM/solve_ns_mpm.cpp:28-62)
+ * on the reference's native solver path: MakNSStabCoeff once, then per Newton
+ * iteration BCNRSet (module/fluid/MPM/stabilized_mpm.h:56-63), the system of
+ * mpm_gpu_ns_assemble, BuildDiagonalPreconditioner for 4 degrees of freedom
+ * (module/solver/crsmat.cpp:87-184), GPBiCGSafe on the scaled system
+ * (module/solver/solver.cpp:19-141, the same method in FP64 with its stopping
+ * test ||r||^2 < 1e-8 ||r0||^2), UpdateNRIncrement (solve_ns_mpm.cpp:21-26)
+ * and CheckNRConvergence (module/solver/solver.cpp:565-593).  The one
+ * difference: the linear solve is GPBiCGSafe called again from where it
+ * stopped until the physical residual ||b - A x|| is below rtol ||b||, so that
+ * the result does not depend on where a Krylov method happens to stop (with a
+ * tight solve the reference's Newton test, which measures the residual of the
+ * solved linear system, ends the loop after the first iteration).
+ * A context holds the 27-point stencil of 4x4 blocks, the solver's vectors
+ * and the boundary conditions (comp 0..3 = u, v, w, p: ubc, vbc, wbc with
+ * BCSetDt on the displacement, pbc with BCSetVal on the pressure; BC rows are
+ * zeroed in the matvec and the right-hand side, BCResidualSet). */
+typedef struct mpm_ns mpm_ns;
+typedef struct {
+    int newton_iters;          /* Newton iterations of the call */
+    int krylov_iters;          /* GPBiCGSafe iterations over all linear solves */
+    double r0r;                /* CheckNRConvergence's reference residual (first iteration) */
+    double last_residual;      /* ||b - A x|| of the last linear system */
+    double last_abs_residual;  /* its sqrt(r.r / active rows) */
+} mpm_ns_stats;
+mpm_status mpm_ns_create(const mpm_grid_desc *grid, const mpm_ns_params *prm, mpm_ns **out);
+void mpm_ns_destroy(mpm_ns *ns);
+mpm_status mpm_ns_set_stream(mpm_ns *ns, void *stream);
+mpm_status mpm_ns_set_bc(mpm_ns *ns, int comp, int n, const int *nodes, const double *vals);
+/* Caller-owned device arrays as mpm_gpu_ns_assemble: particles x (three blocks
+ * of n), mass, vol; the nodal state of the time step nvel, naccel (3*nodec,
+ * component-major) and nmass (nodec).  Writes ndispl (3*nodec) and npres
+ * (nodec), both starting from zero as SolveNS sets them, and tau1 / tau2.
+ * kmax bounds each GPBiCGSafe call (MPM_ERR_KRYLOV_MAXIT); at most 100 Newton
+ * iterations (MPM_ERR_NEWTON_MAXIT); a particle outside the grid returns
+ * MPM_ERR_PARTICLE_OUT_OF_BOX.  Synchronises the context's stream. */
+mpm_status mpm_ns_solve(mpm_ns *ns, int64_t n, const double *x, const double *mass, const double *vol,
+                        const double *nvel, const double *naccel, const double *nmass, double *ndispl,
+                        double *npres, double *tau1, double *tau2, double rtol, int kmax, mpm_ns_stats *stats);
 
 /* ---- allocation-free P2G -----------------------------------------------------
  * No counterpart in the reference: an extra entry point for callers that

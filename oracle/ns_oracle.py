@@ -136,3 +136,85 @@ def ns_assemble(xyelem, xymin, dxy, rho, rmu, dt, beta, gamma, gravity, facl, mt
         np.add.at(bvec, r * N + nid.ravel(), -rhs[..., r].ravel())
     bvec[:3 * N] -= (np.asarray(nmass)[None, :] * acc_k).ravel()   # AddInertialForceToRHS
     return tau1, tau2, stencil.reshape(27, 16, N), bvec
+
+
+def stencil_matrix(stencil, nnc):
+    """The [27][16][nodec] stencil as a scipy CSR matrix of 4 nodec rows
+    (row m nodec + i, column c nodec + j for entry k = 4 m + c of the block
+    between row node i and its neighbour j in slot s)."""
+    import scipy.sparse as sp
+
+    nx, ny, nz = (int(v) for v in nnc)
+    N = nx * ny * nz
+    st = np.asarray(stencil).reshape(27, 16, N)
+    n = np.arange(N)
+    i, j, k = n % nx, (n // nx) % ny, n // (nx * ny)
+    rows, cols, vals = [], [], []
+    for s in range(27):
+        ii, jj, kk = i + s % 3 - 1, j + (s // 3) % 3 - 1, k + s // 9 - 1
+        ok = (ii >= 0) & (jj >= 0) & (kk >= 0) & (ii < nx) & (jj < ny) & (kk < nz)
+        col = ii + nx * (jj + ny * kk)
+        for e in range(16):
+            m, c = divmod(e, 4)
+            v = st[s, e]
+            sel = ok & (v != 0.0)
+            rows.append(m * N + n[sel])
+            cols.append(c * N + col[sel])
+            vals.append(v[sel])
+    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(4 * N, 4 * N))
+
+
+def ns_solve(xyelem, xymin, dxy, rho, rmu, dt, beta, gamma, gravity, facl, mtol, x, mass, vol, nvel, naccel,
+             nmass, bcs, max_newton=100):
+    """SolveNS (module/fluid/MPM/solve_ns_mpm.cpp:28-62) with each linear
+    system solved exactly (sparse direct solve): BCNRSet
+    (stabilized_mpm.h:56-63: u, v, w lists set the displacement to value dt
+    facl, the p list the pressure to value facl), ns_assemble, the solve on
+    the rows with a diagonal above mtol that carry no BC (the scaled Krylov
+    solve of the reference leaves the increment of every other row at zero),
+    UpdateNRIncrement and CheckNRConvergence (solver.cpp:484-593) on the
+    physical residual with the BC rows of b zeroed.  bcs: four
+    (nodes, values) pairs for u, v, w, p.  Returns ndispl (3 nodec),
+    npres (nodec), the Newton iterations and each iteration's residual."""
+    import scipy.sparse.linalg as spl
+
+    nnc = np.asarray(xyelem) + 1
+    N = int(np.prod(nnc))
+    ndispl = np.zeros(3 * N)
+    npres = np.zeros(N)
+    bc = np.zeros(4 * N, dtype=bool)
+    for comp, (nodes, _) in enumerate(bcs):
+        bc[comp * N + np.asarray(nodes, dtype=np.int64)] = True
+    r0r = 0.0
+    hist = []
+    for it in range(max_newton):
+        for comp in range(3):
+            nodes, vals = bcs[comp]
+            ndispl[comp * N + np.asarray(nodes, dtype=np.int64)] = np.asarray(vals) * dt * facl
+        nodes, vals = bcs[3]
+        npres[np.asarray(nodes, dtype=np.int64)] = np.asarray(vals) * facl
+        _, _, st, b = ns_assemble(xyelem, xymin, dxy, rho, rmu, dt, beta, gamma, gravity, facl, mtol, x, mass, vol,
+                                  nvel, naccel, ndispl, npres, nmass)
+        A = stencil_matrix(st, nnc)
+        dg = np.abs(A.diagonal())
+        active = dg >= mtol
+        bb = np.where(bc, 0.0, b)
+        free = active & ~bc
+        xl = np.zeros(4 * N)
+        idx = np.nonzero(free)[0]
+        xl[idx] = spl.spsolve(A[idx][:, idx].tocsc(), bb[idx])
+        ndispl += xl[:3 * N]
+        npres += xl[3 * N:]
+        Ax = A @ xl
+        Ax[bc] = 0.0
+        r = bb - np.where(dg > mtol, Ax, 0.0)
+        rkr = float(np.sqrt(r @ r))
+        idof = float(np.count_nonzero(dg > mtol))
+        rabs = 0.0 if idof <= 1e-30 else float(np.sqrt((r @ r) / idof))
+        hist.append(rkr)
+        if it == 0:
+            r0r = rkr
+        rref = rkr / r0r if r0r > 1e-30 else 0.0
+        if rref < 1e-6 or r0r < 1e-6 or rabs < 1e-8:
+            break
+    return ndispl, npres, it + 1, np.array(hist)

@@ -196,3 +196,31 @@ class RefFluid:
         self.lib.ref_ns_get_matrix(matrow, matcolid, amat, b)
         return dict(tau1=tau1, tau2=tau2, matrow=matrow, matcolid=matcolid, amat=amat.reshape(16, self.nmat),
                     b_rhs=b)
+
+    def solve(self, nvel, naccel, nmass, facl, bcs, rtol=1.0e-10, max_newton=50):
+        """SolveNS: the Newton loop of one time step on the nodal state, each
+        linear system solved to ||b - A x|| <= rtol ||b||.  bcs: four
+        (nodes, values) pairs for u, v, w, p.  Returns ndispl, npres, Newton
+        iterations and Krylov iterations; self.rkr_hist holds the residual of
+        each Newton iteration."""
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        lib = self.lib
+        lib.ref_ns_solve.restype = C.c_int
+        lib.ref_ns_solve.argtypes = [_dp, _dp, _dp, C.c_double, _ip] + [_ip, _dp] * 4 + [
+            C.c_double, C.c_int, _dp, _dp, C.POINTER(C.c_int), _dp]
+        nodes = [i32(n) if len(n) else np.zeros(1, dtype=np.int32) for n, _ in bcs]
+        vals = [f64(v) if len(v) else np.zeros(1) for _, v in bcs]
+        counts = i32([len(n) for n, _ in bcs])
+        nd = np.zeros(3 * self.nodec)
+        npr = np.zeros(self.nodec)
+        kry = C.c_int(0)
+        args = []
+        for k in range(4):
+            args += [nodes[k], vals[k]]
+        hist = np.zeros(max_newton)
+        it = lib.ref_ns_solve(f64(nvel), f64(naccel), f64(nmass), float(facl), counts, *args, float(rtol),
+                              int(max_newton), nd, npr, C.byref(kry), hist)
+        assert it > 0
+        self.rkr_hist = hist[:it]
+        return nd, npr, it, kry.value

@@ -767,6 +767,70 @@ int ref_ns_get_matrix(int *matrow, int *matcolid, double *amat, double *b_rhs) {
     return M.nmat;
 }
 
+/* SolveNS (solve_ns_mpm.cpp:28-62) on the given nodal state, restated as a
+ * loop over the reference's own members: MakNSStabCoeff once, then per
+ * Newton iteration BCNRSet, PredictNewmarkBetaVelAndAccel, AssembleNSSystem
+ * (with BuildDiagonalPreconditioner: use_petsc off), the native GPBiCGSafe,
+ * UpdateNRIncrement and CheckNRConvergence.  The one change is the linear
+ * solve's stopping point: GPBiCGSafe stops at a relative residual of 1e-4
+ * (squared 1e-8, solver.cpp:64) and is called again from where it stopped
+ * until the physical residual ||b - A x|| (ComputeRefResidual) is below
+ * rtol ||b||, so that the result does not depend on the Krylov method.
+ * BC lists: n_c nodes and values per component u, v, w, p.  At most
+ * max_newton iterations; rkr_hist (may be NULL) receives the residual of
+ * each iteration's linear system after the update (as CheckNRConvergence
+ * measures it).  Returns the Newton iterations; ndispl (3 nodec) and npres
+ * (nodec) receive the state. */
+int ref_ns_solve(const double *nvel, const double *naccel, const double *nmass, double facl_in, const int *nbc_n,
+                 const int *nbc_u, const double *fbc_u, const int *nbc_v, const double *fbc_v, const int *nbc_w,
+                 const double *fbc_w, const int *nbc_p, const double *fbc_p, double rtol, int max_newton,
+                 double *ndispl, double *npres, int *krylov_out, double *rkr_hist) {
+    if (!g_ns) return -1;
+    auto &w = *g_ns;
+    facl = facl_in;
+    w.nvel.assign(nvel, nvel + (size_t)nodec * 3);
+    w.naccel.assign(naccel, naccel + (size_t)nodec * 3);
+    w.nmass.assign(nmass, nmass + (size_t)nodec);
+    BoundaryCondition *bcs[4] = {&w.ubc, &w.vbc, &w.wbc, &w.pbc};
+    const int *nb[4] = {nbc_u, nbc_v, nbc_w, nbc_p};
+    const double *fb[4] = {fbc_u, fbc_v, fbc_w, fbc_p};
+    for (int k = 0; k < 4; k++) {
+        bcs[k]->ibc = nbc_n[k];
+        bcs[k]->nbc.assign(nb[k], nb[k] + nbc_n[k]);
+        bcs[k]->fbc.assign(fb[k], fb[k] + nbc_n[k]);
+    }
+    w.NS_.use_petsc = false;
+    std::vector<double> nvel_k(nodec * 3), naccel_k(nodec * 3);
+    constexpr int iter_max = 10000;
+    w.MakNSStabCoeff();
+    VectorAssign(nodec * 3, w.ndispl);
+    VectorAssign(nodec, w.npres);
+    VectorAssign(nodec * 4, w.NS_.x_lhs);
+    double r0r = 0.0;
+    int NR_it, ktot = 0;
+    for (NR_it = 0; NR_it <= iter_max && NR_it < max_newton; NR_it++) {
+        w.BCNRSet();
+        w.PredictNewmarkBetaVelAndAccel(nvel_k, naccel_k);
+        w.AssembleNSSystem(nvel_k, naccel_k);
+        double bb = 0.0;
+        w.BCResidualSet(w.NS_.b_rhs);
+        for (double v : w.NS_.b_rhs) bb += v * v;
+        const double bnorm = std::sqrt(bb);
+        for (int call = 0; call < 20; call++) {
+            if (w.NS_.ComputeRefResidual() <= rtol * bnorm) break;
+            ktot += GPBiCGSafe(w.NS_);
+        }
+        w.UpdateNRIncrement();
+        if (rkr_hist) rkr_hist[NR_it] = w.NS_.ComputeRefResidual();
+        if (w.NS_.CheckNRConvergence(NR_it, iter_max, 0, r0r)) break;
+    }
+    std::memcpy(ndispl, w.ndispl.data(), sizeof(double) * 3 * (size_t)nodec);
+    std::memcpy(npres, w.npres.data(), sizeof(double) * (size_t)nodec);
+    if (krylov_out) *krylov_out = ktot;
+    w.NS_.use_petsc = true;
+    return NR_it + 1;
+}
+
 int ref_nodec(void) { return nodec; }
 int ref_num(void) {
     MaterialPoint *mp = active();

@@ -13,6 +13,7 @@ committed and this script is re-run only when a case is added:
     python tests/golden/make_golden.py --fbar             # only the F-bar cases
     python tests/golden/make_golden.py --fluid            # only the stabilized fluid assembly
     python tests/golden/make_golden.py --implicit2        # only the quadratic / StVK / Mooney-Rivlin implicit cases
+    python tests/golden/make_golden.py --fluid-newton     # only the stabilized fluid Newton loop
 """
 from __future__ import annotations
 
@@ -234,6 +235,68 @@ def fluid_case(name="ns_assemble"):
     np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **c, **out)
 
 
+def ns_box_inputs(xyelem=(6, 5, 4), dx=0.01, ppd=2, seed=3, amp=0.05):
+    """A fluid box filled with particles (every cell, ppd^3 per cell with
+    +-0.1 spacing jitter, rho = 1000), the nodal mass of their linear P2G, a
+    smooth velocity field that vanishes on the walls, zero acceleration;
+    no-slip walls (u = v = w = 0) on the sides and bottom, p = 0 on the top
+    face.  Newmark beta = 1/4, gamma = 1/2, dt = 2e-3 s, gravity -9.8 m/s^2."""
+    rng = np.random.default_rng(seed)
+    xyelem = np.array(xyelem)
+    nnc = xyelem + 1
+    N = int(np.prod(nnc))
+    pts = []
+    for k in range(xyelem[2]):
+        for j in range(xyelem[1]):
+            for i in range(xyelem[0]):
+                for c in range(ppd ** 3):
+                    a, b, d = c % ppd, (c // ppd) % ppd, c // ppd ** 2
+                    off = (np.array([a, b, d]) + 0.5) / ppd + rng.uniform(-0.1, 0.1, 3) / ppd
+                    pts.append((np.array([i, j, k]) + off) * dx)
+    x = np.array(pts)
+    n = len(x)
+    vol = np.full(n, dx ** 3 / ppd ** 3)
+    mass = 1000.0 * vol
+    cell = np.floor(x / dx).astype(int)
+    nmass = np.zeros(N)
+    for q in range(8):
+        i, j, k = q & 1, (q >> 1) & 1, q >> 2
+        w = np.ones(n)
+        for d, o in enumerate((i, j, k)):
+            w *= 1.0 - np.abs(x[:, d] - dx * (cell[:, d] + o)) / dx
+        nid = (cell[:, 0] + i) + nnc[0] * ((cell[:, 1] + j) + nnc[1] * (cell[:, 2] + k))
+        np.add.at(nmass, nid, w * mass)
+    ix = np.arange(N) % nnc[0]
+    iy = (np.arange(N) // nnc[0]) % nnc[1]
+    iz = np.arange(N) // (nnc[0] * nnc[1])
+    X, Y, Z = ix / xyelem[0], iy / xyelem[1], iz / xyelem[2]
+    nvel = np.zeros((3, N))
+    s3 = np.sin(np.pi * X) * np.sin(np.pi * Y) * np.sin(np.pi * Z)
+    nvel[0] = amp * s3 * np.cos(np.pi * Y)
+    nvel[1] = -amp * s3 * np.cos(np.pi * X)
+    nvel[2] = 0.3 * amp * np.sin(np.pi * X) * np.sin(np.pi * Y) * np.sin(2 * np.pi * Z)
+    wall = np.nonzero((ix == 0) | (ix == xyelem[0]) | (iy == 0) | (iy == xyelem[1]) | (iz == 0))[0]
+    top = np.nonzero(iz == xyelem[2])[0]
+    return dict(xyelem=xyelem, xymin=np.zeros(3), dxy=np.full(3, dx), x=x, mass=mass, vol=vol, nvel=nvel.ravel(),
+                naccel=np.zeros(3 * N), nmass=nmass, rho=1000.0, rmu=1.0e-3, dt=2.0e-3, beta=0.25, gamma=0.5,
+                gravity=np.array([0.0, 0.0, -9.8]), facl=1.0, mtol=1.0e-12, bc_wall=wall.astype(np.int32),
+                bc_top=top.astype(np.int32))
+
+
+def fluid_newton_case(name="ns_solve"):
+    """SolveNS on the filled box: the reference's Newton loop with GPBiCGSafe
+    post-iterated to ||b - A x|| <= 1e-10 ||b|| (ref_harness.cpp, ref_ns_solve)."""
+    c = ns_box_inputs()
+    r = ref.RefFluid(c["xyelem"], c["xymin"], c["dxy"], c["dt"], c["mtol"], c["gravity"], c["x"], c["mass"],
+                     c["vol"], c["rho"], c["rmu"], c["beta"], c["gamma"])
+    wall, top = c["bc_wall"], c["bc_top"]
+    bcs = [(wall, np.zeros(len(wall)))] * 3 + [(top, np.zeros(len(top)))]
+    nd, npres, newton, krylov = r.solve(c["nvel"], c["naccel"], c["nmass"], c["facl"], bcs, rtol=1.0e-10)
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **c, ndispl=nd, npres=npres, newton=np.array(newton),
+                        krylov=np.array(krylov), rtol=np.array(1.0e-10))
+    print("wrote", name, len(c["mass"]), "particles,", newton, "Newton iterations,", krylov, "Krylov iterations")
+
+
 def main():
     if not ref.available():
         raise SystemExit("oracle/_ref/libmpmref.so missing: run oracle/build_ref.sh <reference checkout> first")
@@ -248,6 +311,9 @@ def main():
         return
     if "--fluid" in sys.argv[1:]:
         fluid_case()
+        return
+    if "--fluid-newton" in sys.argv[1:]:
+        fluid_newton_case()
         return
     if "--implicit2" in sys.argv[1:]:
         implicit_extra_cases()
@@ -283,6 +349,7 @@ def main():
     fbar_cases()
     fluid_case()
     implicit_extra_cases()
+    fluid_newton_case()
 
 
 if __name__ == "__main__":

@@ -15,7 +15,7 @@ def declared_symbols():
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
         text = open(h).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-        syms.update(re.findall(r"\b(mpm_gpu_\w+)\s*\(", text))
+        syms.update(re.findall(r"\b(mpm_(?:gpu|ns|nn)_\w+)\s*\(", text))
     return syms
 
 

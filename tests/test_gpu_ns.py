@@ -124,3 +124,42 @@ def test_gpu_ns_full_size_symmetry_and_timing():
             scale = float(a.abs().max()) + 1e-300
             worst = max(worst, float((a - bt).abs().max()) / scale)
     assert worst < 1e-12, worst
+
+
+def _newton_gpu(c, bcs, rtol=1.0e-10):
+    torch = pytest.importorskip("torch")
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda:0")
+    s = capi.NsSolver(c["xyelem"], c["xymin"], c["dxy"], *(c[k] for k in KEYS), bcs=bcs)
+    (nd, npres, _, _), st = s.solve(t(c["x"].T.copy()), t(c["mass"]), t(c["vol"]), t(c["nvel"]), t(c["naccel"]),
+                                    t(c["nmass"]), rtol=rtol)
+    s.close()
+    return nd.cpu().numpy(), npres.cpu().numpy(), st
+
+
+def _box_bcs(c):
+    return [(c["bc_wall"], np.zeros(len(c["bc_wall"])))] * 3 + [(c["bc_top"], np.zeros(len(c["bc_top"])))]
+
+
+def test_gpu_ns_newton_matches_reference_fixture():
+    """SolveNS on the GPU (mpm_ns_solve: Newton + GPBiCGSafe on the scaled
+    4-DOF system) against the reference's own Newton loop, both solved to
+    ||b - A x|| <= 1e-10 ||b||: displacement and pressure within 1e-9."""
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ns_solve.npz")))
+    nd, npres, st = _newton_gpu(g, _box_bcs(g))
+    print(f"\nSolveNS vs reference: ndispl {rel(nd, g['ndispl']):.2e}, npres {rel(npres, g['npres']):.2e}; {st}")
+    assert st["newton_iters"] == int(g["newton"])
+    assert rel(nd, g["ndispl"]) < 1e-9 and rel(npres, g["npres"]) < 1e-9
+    assert st["last_residual"] < 1e-6   # CheckNRConvergence's residual of the solved system
+
+
+def test_gpu_ns_newton_matches_oracle_larger_box():
+    """A larger, ragged box against the numpy SolveNS with exact solves."""
+    c = make_golden.ns_box_inputs(xyelem=(11, 8, 7), seed=7, amp=0.2)
+    bcs = _box_bcs(c)
+    want_d, want_p, it, _ = ns_oracle.ns_solve(c["xyelem"], c["xymin"], c["dxy"], *(c[k] for k in KEYS), c["x"],
+                                               c["mass"], c["vol"], c["nvel"], c["naccel"], c["nmass"], bcs)
+    nd, npres, st = _newton_gpu(c, bcs)
+    print(f"\nSolveNS vs oracle ({len(c['mass'])} particles): ndispl {rel(nd, want_d):.2e}, "
+          f"npres {rel(npres, want_p):.2e}; {st}")
+    assert st["newton_iters"] == it
+    assert rel(nd, want_d) < 1e-9 and rel(npres, want_p) < 1e-9

@@ -66,3 +66,19 @@ def test_ns_velocity_blocks_are_symmetric():
                 assert np.allclose(st[s, 4 * r + c, rows], st[26 - s, 4 * c + r, cols], rtol=1e-12, atol=1e-9)
         assert np.allclose(st[s, 15, rows], st[26 - s, 15, cols], rtol=1e-12, atol=1e-15)
     assert N == st.shape[2]
+
+
+def test_ns_newton_oracle_matches_reference_fixture():
+    """The numpy SolveNS (exact linear solves) against the reference's own
+    Newton loop with GPBiCGSafe post-iterated to ||b - A x|| <= 1e-10 ||b||
+    (fixture tests/golden/ns_solve.npz, made by make_golden.py --fluid-newton):
+    the same Newton iteration count and the displacement and pressure within
+    the reference's solve tolerance."""
+    g = dict(np.load(os.path.join(os.path.dirname(GOLDEN), "ns_solve.npz")))
+    bcs = [(g["bc_wall"], np.zeros(len(g["bc_wall"])))] * 3 + [(g["bc_top"], np.zeros(len(g["bc_top"])))]
+    nd, npres, it, hist = ns_oracle.ns_solve(g["xyelem"], g["xymin"], g["dxy"], float(g["rho"]), float(g["rmu"]),
+                                             float(g["dt"]), float(g["beta"]), float(g["gamma"]), g["gravity"],
+                                             float(g["facl"]), float(g["mtol"]), g["x"], g["mass"], g["vol"],
+                                             g["nvel"], g["naccel"], g["nmass"], bcs)
+    assert it == int(g["newton"])
+    assert rel(nd, g["ndispl"]) < 1e-10 and rel(npres, g["npres"]) < 1e-10
