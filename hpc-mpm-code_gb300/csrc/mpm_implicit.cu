@@ -1620,13 +1620,16 @@ static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
                 // FP32 operator: the recursive residual carries the rounding of
                 // the FP32 matvecs, so convergence is judged on the true
                 // residual bs - A x (FP64 arithmetic); if it is not below the
-                // tolerance, it replaces the recursive residual (and its norm,
-                // for the next beta) and CG goes on with the same direction
-                // (residual replacement, which keeps the Krylov progress)
+                // tolerance, CG restarts from it (r, and p = r).  Keeping the
+                // old direction instead diverged: at this point the recursive
+                // residual, and with it p, has fallen far below the true
+                // residual, so alpha = r.r / p.Ap overshoots.
                 const int cur = (it & 1) ? S_RR1 : S_RR0;
                 launch_matvec(c, a, nb, s->xs, s->z, nullptr, nullptr, nullptr, 0, true);
                 k_true_residual<<<nb, 256, 0, c->stream>>>(a, s->bs, s->z, s->r, s->part);
                 k_finish<<<1, 256, 0, c->stream>>>(s->part, nb, s->scal, cur);
+                CKI(cudaMemcpyAsync(s->p, s->r, sizeof(double) * 3 * c->g.nodec, cudaMemcpyDeviceToDevice,
+                                    c->stream));
                 c->launches += 3;
                 CKI(cudaMemcpyAsync(s->h_scal, s->scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->stream));
                 CKI(cudaStreamSynchronize(c->stream));
