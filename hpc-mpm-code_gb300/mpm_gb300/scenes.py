@@ -228,6 +228,33 @@ def dam_break(grid=(256, 128, 128), dx=4.0e-3, cells=(128, 128, 96), npc=2, jitt
     return scene
 
 
+def hydrostatic_column(cells=(8, 8, 20), dx=4.0e-3, head=4, npc=2, c0=30.0, gamma=7.0, mu=1.0e-3, rho=1000.0,
+                       g=9.81, dt=5.0e-6):
+    """A Tait-fluid column at rest in its hydrostatic state: it fills the box
+    laterally (slip walls on every face, `head` empty cell layers above it),
+    and each particle starts at the pressure p = rho g (H - z) of its depth,
+    with J = (1 + gamma p / (rho c0^2))^(-1/gamma) (the Tait equation of state
+    solved for J), F = J^(1/3) I, Cauchy stress -p I, mass rho V / J and
+    vol0 = V / J for the lattice volume V = dx^3 / npc^3 (so that the rest
+    density m / vol0 is rho and the current volume J vol0 is V).  Returns
+    (scene, F (n, 3, 3), stress (n, 6), vol (n), H)."""
+    s = dam_break(grid=(cells[0], cells[1], cells[2] + head), dx=dx, cells=cells, npc=npc, c0=c0, gamma=gamma,
+                  mu=mu, rho=rho, dt=dt, gravity=(0.0, 0.0, -g), name="hydrostatic_column")
+    H = cells[2] * dx
+    p = rho * g * (H - s.coord[:, 2])
+    J = (1.0 + gamma * p / (rho * c0 * c0)) ** (-1.0 / gamma)
+    V = dx ** 3 / npc ** 3
+    s.mass[:] = rho * V / J
+    s.vol0[:] = V / J
+    F = np.zeros((s.num, 3, 3))
+    for i in range(3):
+        F[:, i, i] = J ** (1.0 / 3.0)
+    stress = np.zeros((s.num, 6))
+    stress[:, :3] = -p[:, None]
+    vol = s.vol0 * np.linalg.det(F)
+    return s, F, stress, vol, H
+
+
 @dataclass
 class Batch:
     """Independent scenes packed into one grid (see ``pack_scenes``)."""

@@ -161,6 +161,23 @@ int mo_load(mo_ctx *c, int num, const double *coord, const double *vel, const do
     return 0;
 }
 
+/* A loaded state other than the undeformed one (as the GPU path's load +
+ * upload): F (9 per particle), stress (6) and vol, any may be NULL; jac
+ * follows F. */
+int mo_set_state(mo_ctx *c, const double *F, const double *stress, const double *vol) {
+    for (size_t p = 0; p < (size_t)c->num; p++) {
+        if (F) {
+            memcpy(c->F + 9 * p, F + 9 * p, sizeof(double) * 9);
+            const double *f = F + 9 * p;
+            c->jac[p] = f[0] * (f[4] * f[8] - f[5] * f[7]) + f[1] * (f[5] * f[6] - f[3] * f[8]) +
+                        f[2] * (f[3] * f[7] - f[4] * f[6]);
+        }
+        if (stress) memcpy(c->stress + 6 * p, stress + 6 * p, sizeof(double) * 6);
+        if (vol) c->vol[p] = vol[p];
+    }
+    return 0;
+}
+
 int mo_set_bc(mo_ctx *c, int comp, int n, const int *nodes, const double *vals) {
     if (comp < 0 || comp > 2) return -1;
     free(c->bc_nodes[comp]);

@@ -25,6 +25,7 @@ void mo_destroy(mo_ctx *c);
 int mo_nodec(const mo_ctx *c);
 int mo_load(mo_ctx *c, int num, const double *coord, const double *vel, const double *mass, const double *vol0,
             const int *matid, int scheme, int shifting);
+int mo_set_state(mo_ctx *c, const double *F, const double *stress, const double *vol);
 int mo_set_bc(mo_ctx *c, int comp, int n, const int *nodes, const double *vals);
 int mo_explicit_p2g(mo_ctx *c, double facl);
 int mo_explicit_steps(mo_ctx *c, int nsteps, double facl);

@@ -37,6 +37,7 @@ def _lib():
     lib.mo_nodec.argtypes = [C.c_void_p]
     lib.mo_load.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _ip, C.c_int, C.c_int]
     lib.mo_set_bc.argtypes = [C.c_void_p, C.c_int, C.c_int, _ip, _dp]
+    lib.mo_set_state.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.mo_explicit_p2g.argtypes = [C.c_void_p, C.c_double]
     lib.mo_explicit_steps.argtypes = [C.c_void_p, C.c_int, C.c_double]
     lib.mo_get_nodal.argtypes = [C.c_void_p, C.c_int, _dp]
@@ -85,6 +86,12 @@ class PortSolid:
         if getattr(self, "ctx", None):
             self.lib.mo_destroy(self.ctx)
             self.ctx = None
+
+    def set_state(self, F=None, stress=None, vol=None):
+        """Overwrite F (n, 3, 3), the Voigt stress (n, 6) and vol (n) of the loaded particles."""
+        keep = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (F, stress, vol)]
+        ptr = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)
+        self.lib.mo_set_state(self.ctx, *(ptr(a) for a in keep))
 
     def steps(self, n, facl=1.0):
         self.lib.mo_explicit_steps(self.ctx, n, facl)

@@ -48,3 +48,59 @@ def test_fluid_fp32_within_tolerance():
     tol = {"x": 1e-6, "v": 1e-3, "sigma": 2e-3, "vol": 1e-5}
     for k, t in tol.items():
         assert rel_l2(p[k], q[k]) <= t, (k, rel_l2(p[k], q[k]))
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_tait_column_stays_hydrostatic(precision):
+    """Known answer without the oracle: a Tait-fluid column started in its
+    hydrostatic state (the equation of state solved for the J of the
+    pressure rho g (H - z) at each particle's depth, scenes.hydrostatic_column)
+    stays at rest.  After 2000 steps (10 ms, about one acoustic period
+    4 H / c0) every particle's pressure is within 0.2 % of rho g H of
+    rho g (H - z) and no particle moves faster than 1e-4 m/s."""
+    s, F, stress, vol, H = scenes.hydrostatic_column()
+    g = capi.GpuSolid(s, precision=precision)
+    g.load(s.coord, s.vel, s.mass, s.vol0, F=F.reshape(-1, 9), stress=stress, matid=s.matid)
+    g.upload_state(vol=np.ascontiguousarray(vol))
+    g.steps(2000)
+    q = g.particles()
+    g.sync()
+    g.close()
+    pr = -q["sigma"][:, :3].mean(axis=1)
+    ph = 1000.0 * 9.81 * (H - s.coord[:, 2])
+    err = np.abs(pr - ph).max() / (1000.0 * 9.81 * H)
+    vmax = np.abs(q["v"]).max()
+    print(f"\nhydrostatic column FP{precision}: max |p - rho g (H - z)| / (rho g H) = {err:.2e}, max |v| = {vmax:.2e}")
+    assert err <= 2e-3 and vmax <= 1e-4
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_dam_break_front_speed(precision):
+    """Known answer without the oracle: a quasi-two-dimensional dam break (a
+    25 x 25-cell water column, a = H = 0.1 m, two cells thick between slip
+    walls, FLIP, dt = 2e-5 s).  In the dimensionless variables of the dam
+    break experiments, T = t sqrt(2 g / a) and Z = front / a, the front leaves
+    the early acceleration phase by T ~ 2; from then on it must move slower
+    than the inviscid shallow-water front 2 sqrt(g H) of Ritter's dam-break
+    solution and faster than 1.2 sqrt(g H), and at T ~ 2 it must lie between
+    Z = 2.0 and Z = 2.8.  (On the oracle this case gives Z = 2.44 at T = 1.96
+    and a mean front speed of 1.79 sqrt(g H) for T in [1.96, 2.80].)"""
+    dx, a_cells = 4.0e-3, 25
+    s = scenes.dam_break(grid=(100, 2, 40), dx=dx, cells=(a_cells, 2, a_cells), npc=2, dt=2.0e-5,
+                         scheme=scenes.FLIP)
+    a = a_cells * dx
+    g = 9.81
+    gpu = capi.GpuSolid(s, precision=precision)
+    fronts = []
+    for n in (7000, 10000):
+        gpu.steps(n - (7000 if fronts else 0))
+        fronts.append(np.percentile(gpu.particles()["x"][:, 0], 99.9))
+    gpu.sync()
+    gpu.close()
+    t = np.array([7000, 10000]) * 2.0e-5
+    T = t * np.sqrt(2.0 * g / a)
+    Z = np.array(fronts) / a
+    speed = (fronts[1] - fronts[0]) / (t[1] - t[0]) / np.sqrt(g * a)
+    print(f"\ndam break FP{precision}: T {T.round(2)} Z {Z.round(3)}, front speed {speed:.2f} sqrt(g H)")
+    assert 2.0 <= Z[0] <= 2.8
+    assert 1.2 <= speed <= 2.0

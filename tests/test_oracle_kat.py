@@ -77,3 +77,35 @@ def test_oracle_affine_transfers_keep_angular_momentum():
     assert np.linalg.norm(At - Aa) <= 1.0e-10 * np.linalg.norm(At)
     assert np.linalg.norm(out[scenes.TPIC][4]["v"] - out[scenes.APIC][4]["v"]) <= 1.0e-10 * np.linalg.norm(
         out[scenes.TPIC][4]["v"])
+
+
+def test_tait_column_stays_hydrostatic():
+    """A Tait-fluid column started in its hydrostatic state (pressure
+    rho g (H - z) from the equation of state solved for J) stays at rest:
+    after 1000 steps (5 ms, half an acoustic period 4 H / c0) every particle's
+    pressure is within 0.1 % of rho g H of its hydrostatic value and no
+    particle moves faster than 1e-4 m/s."""
+    s, F, stress, vol, H = scenes.hydrostatic_column()
+    o = port.PortSolid(s)
+    o.set_state(F=F.reshape(-1, 9), stress=stress, vol=vol)
+    o.steps(1000)
+    q = o.particles()
+    pr = -q["sigma"][:, :3].mean(axis=1)
+    ph = 1000.0 * 9.81 * (H - s.coord[:, 2])
+    assert np.abs(pr - ph).max() <= 1e-3 * 1000.0 * 9.81 * H
+    assert np.abs(q["v"]).max() <= 1e-4
+
+
+def test_dam_break_front_speed_oracle():
+    """The dam-break known answer of tests/test_gpu_fluid.py on the oracle,
+    over a shorter run: by T = t sqrt(2 g / a) = 1.4 the front has moved
+    between 0.5 a and 1.0 a (Z in [1.5, 2.0]), slower than Ritter's
+    inviscid front (Z = 1 + 2 sqrt(g H) t / a = 2.98)."""
+    dx, a_cells = 4.0e-3, 25
+    s = scenes.dam_break(grid=(100, 2, 40), dx=dx, cells=(a_cells, 2, a_cells), npc=2, dt=2.0e-5,
+                         scheme=scenes.FLIP)
+    o = port.PortSolid(s)
+    o.steps(5000)
+    a = a_cells * dx
+    Z = np.percentile(o.particles()["x"][:, 0], 99.9) / a
+    assert 1.5 <= Z <= 2.0, Z
