@@ -1,8 +1,9 @@
 """Focused runs of one workload each, for profiling with ncu.
 
     python -m mpm_gb300.cases explicit [--cells 64] [--steps 20]
-    python -m mpm_gb300.cases implicit [--steps 1]       # Jacobi-PCG Newton steps, 1.728M-particle cantilever
-    python -m mpm_gb300.cases precond  [--steps 1]       # the same with the learned preconditioner
+    python -m mpm_gb300.cases implicit [--steps 1] [--precision 32]  # Jacobi-PCG Newton steps, 1.728M-particle cantilever
+    python -m mpm_gb300.cases precond  [--steps 1] [--precision 32]  # the same with the learned preconditioner
+    python -m mpm_gb300.cases ns       [--reps 3]        # stabilized-fluid Newton solves (SolveNS), filled box
     python -m mpm_gb300.cases network  [--reps 10]       # network forward passes on the 65^3 grid
     python -m mpm_gb300.cases batched  [--steps 20]      # 256 packed scenes
     python -m mpm_gb300.cases fluid    [--steps 20]      # 12.6M-particle Tait dam break
@@ -29,7 +30,7 @@ def _stream():
     return torch.cuda.Stream()
 
 
-def run(case, steps, cells, reps):
+def run(case, steps, cells, reps, precision=64):
     st = _stream()
     if case in ("explicit", "apic", "fbar"):
         s = scenes.spinning_block(cells=(cells, cells, cells),
@@ -42,7 +43,7 @@ def run(case, steps, cells, reps):
         g.sync()
     elif case in ("implicit", "precond"):
         s = scenes.cantilever(iprop=1)
-        g = capi.GpuImplicitSolid(s, nr_flag=True, stream=st.cuda_stream)
+        g = capi.GpuImplicitSolid(s, nr_flag=True, stream=st.cuda_stream, precision=precision)
         if case == "precond":
             from . import train_precond
 
@@ -60,6 +61,23 @@ def run(case, steps, cells, reps):
         x = np.random.default_rng(0).normal(size=(1, 65 ** 3, 6)).astype(np.float32)
         for _ in range(reps):
             net.forward(x)
+    elif case == "ns":
+        import os
+        import torch
+
+        sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))),
+                                        "tests", "golden"))
+        import make_golden
+
+        c = make_golden.ns_box_inputs(xyelem=(24, 20, 16), seed=9, amp=0.2)
+        bcs = [(c["bc_wall"], np.zeros(len(c["bc_wall"])))] * 3 + [(c["bc_top"], np.zeros(len(c["bc_top"])))]
+        t = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda:0")
+        ns = capi.NsSolver(c["xyelem"], c["xymin"], c["dxy"], c["rho"], c["rmu"], c["dt"], c["beta"], c["gamma"],
+                           c["gravity"], c["facl"], c["mtol"], bcs=bcs, stream=st.cuda_stream)
+        args = [t(c["x"].T.copy()), t(c["mass"]), t(c["vol"]), t(c["nvel"]), t(c["naccel"]), t(c["nmass"])]
+        for _ in range(reps):
+            ns.solve(*args)
+        ns.close()
     elif case == "batched":
         b = scenes.pack_scenes(scenes.batch_scenes())
         g = capi.GpuSolid(b.scene, precision=32, shifting=False, stream=st.cuda_stream)
@@ -81,8 +99,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--cells", type=int, default=64)
     ap.add_argument("--reps", type=int, default=10)
+    ap.add_argument("--precision", type=int, default=64, choices=[32, 64])
     a = ap.parse_args()
-    run(a.case, a.steps, a.cells, a.reps)
+    run(a.case, a.steps, a.cells, a.reps, a.precision)
 
 
 if __name__ == "__main__":
