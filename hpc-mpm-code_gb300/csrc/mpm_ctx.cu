@@ -400,6 +400,7 @@ mpm_status mpm_gpu_set_bc(mpm_ctx *c, int comp, int n, const int *nodes, const d
         for (size_t i = 0; i < 3 * N; i++) vf[i] = (float)val[i];
         CK(cudaMemcpy(c->d_bcval, vf.data(), sizeof(float) * 3 * N, cudaMemcpyHostToDevice));
     }
+    if (c->imp) return implicit_bc_changed(c);
     return MPM_OK;
 }
 

@@ -60,6 +60,7 @@ struct ImpState {
     double *x = nullptr, *r = nullptr, *p = nullptr, *Ap = nullptr, *xs = nullptr;
     double *ndispl = nullptr, *nvel = nullptr, *naccel = nullptr, *naccel_k = nullptr;
     double *nmass = nullptr, *nvof = nullptr, *nei = nullptr;
+    double *bcval64 = nullptr;             // 3 * nodec prescribed BC values in FP64 (implicit_bc_changed)
     void *stress_k = nullptr;              // 6 * num, Newton stress of the step (particle precision)
     void *geup = nullptr;                  // 3 * num (particle precision)
     double *part = nullptr;                // reduction partials
@@ -151,7 +152,9 @@ static ImpArgs imp_args(mpm_ctx *c) {
     a.qp = (9 * a.ns + 1) / 2;
     a.num = c->num;
     a.bcflag = c->d_bcflag;
-    a.bcval = (const double *)c->d_bcval;
+    // prescribed values in FP64 whatever the context's precision (an FP32
+    // context keeps its own copy in FP32, d_bcval)
+    a.bcval = s->bcval64;
     a.nvol = c->d_nvol;
     a.iprop = c->d_iprop;
     a.matprop = c->d_matprop;
@@ -1336,7 +1339,7 @@ namespace mpm {
 void implicit_free(mpm_ctx *c) {
     ImpState *s = c->imp;
     if (!s) return;
-    void *bufs[] = {s->A, s->adiag, s->b, s->x, s->r, s->p, s->Ap, s->xs, s->ndispl, s->nvel, s->naccel,
+    void *bufs[] = {s->A, s->bcval64, s->adiag, s->b, s->x, s->r, s->p, s->Ap, s->xs, s->ndispl, s->nvel, s->naccel,
                       s->naccel_k, s->nmass, s->nvof, s->nei, s->stress_k, s->geup, s->part, s->scal,
                       s->z, s->bs, s->xstar, s->ev, s->gp, s->gq, s->gqq, s->gbeta};
     for (void *b : bufs)
@@ -1348,6 +1351,22 @@ void implicit_free(mpm_ctx *c) {
         if (g) cudaGraphExecDestroy(g);
     delete s;
     c->imp = nullptr;
+}
+}  // namespace mpm
+
+namespace mpm {
+// The FP64 copy of the BC values the implicit kernels read, from the host
+// lists of mpm_gpu_set_bc (later entries win, as there).
+mpm_status implicit_bc_changed(mpm_ctx *c) {
+    ImpState *s = c->imp;
+    if (!s || !s->bcval64) return MPM_OK;
+    const size_t N = (size_t)c->g.nodec;
+    std::vector<double> val(3 * N, 0.0);
+    for (int k = 0; k < 3; k++)
+        for (size_t i = 0; i < c->bc_nodes[k].size(); i++) val[k * N + c->bc_nodes[k][i]] = c->bc_vals[k][i];
+    CKI(cudaStreamSynchronize(c->stream));
+    CKI(cudaMemcpy(s->bcval64, val.data(), sizeof(double) * 3 * N, cudaMemcpyHostToDevice));
+    return MPM_OK;
 }
 }  // namespace mpm
 
@@ -1408,6 +1427,11 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
     s->nb[5] = 1.0 / (2.0 * b) - 1.0;
     const size_t N = (size_t)c->g.nodec;
     CKI(cudaMalloc((void **)&s->A, (s->prec == 64 ? sizeof(double) : sizeof(float)) * a_size((int)N, s->qp)));
+    CKI(cudaMalloc((void **)&s->bcval64, sizeof(double) * 3 * N));
+    {
+        const mpm_status q = implicit_bc_changed(c);
+        if (q != MPM_OK) return q;
+    }
     double **vec3[] = {&s->adiag, &s->b,    &s->x,       &s->r, &s->p,  &s->Ap,    &s->xs, &s->ndispl,
                        &s->nvel,  &s->naccel, &s->naccel_k, &s->z, &s->bs, &s->xstar, &s->ev};
     for (double **v : vec3) CKI(cudaMalloc((void **)v, sizeof(double) * 3 * N));

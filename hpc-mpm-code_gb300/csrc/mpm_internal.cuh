@@ -222,6 +222,7 @@ namespace mpm {
 mpm_status sort_particles(mpm_ctx *c);
 // mpm_implicit.cu
 void implicit_free(mpm_ctx *c);
+mpm_status implicit_bc_changed(mpm_ctx *c);   // after mpm_gpu_set_bc on an implicit context
 // mpm_explicit.cu
 mpm_status run_p2g(mpm_ctx *c, double facl);
 mpm_status run_grid1(mpm_ctx *c, int mode);
