@@ -610,11 +610,17 @@ __global__ void k_imp_scale(ImpArgs a, R *A, const double *adiag) {
         const int ii = i + s % sx - a.rad[0], jj = j + (s / sx) % sy - a.rad[1], kk = k + s / (sx * sy) - a.rad[2];
         if (ii < 0 || jj < 0 || kk < 0 || ii >= a.nnc[0] || jj >= a.nnc[1] || kk >= a.nnc[2]) continue;
         const size_t col = ii + (size_t)a.nnc[0] * (jj + (size_t)a.nnc[1] * kk);
-        for (int r = 0; r < 3; r++)
-            for (int c = 0; c < 3; c++) {
-                R &v = A[aidx(s * 9 + 3 * r + c, n, a.qp)];
-                v = (R)((double)v * (adiag[r * N + n] * adiag[c * N + col]));
-            }
+        if constexpr (sizeof(R) == 8) {
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) A[aidx(s * 9 + 3 * r + c, n, a.qp)] *= adiag[r * N + n] * adiag[c * N + col];
+        } else {
+            // the FP32 matrix is scaled in FP32 (one FP64 operation per entry
+            // would make this pass FP64-pipe bound)
+            const float dr[3] = {(float)adiag[n], (float)adiag[N + n], (float)adiag[2 * N + n]};
+            const float dc[3] = {(float)adiag[col], (float)adiag[N + col], (float)adiag[2 * N + col]};
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) A[aidx(s * 9 + 3 * r + c, n, a.qp)] *= dr[r] * dc[c];
+        }
     }
 }
 
@@ -997,14 +1003,16 @@ __global__ void __launch_bounds__(128) k_imp_g2p(ImpArgs a, PView<R> P, const do
         }
         for (int k = 0; k < 6; k++) P.s[k][p] = sk[k];
         const bool flip = (a.scheme == MPM_FLIP);
-        double disp[3] = {0, 0, 0}, acc[3] = {0, 0, 0}, vel[3] = {0, 0, 0};
-        const double aold[3] = {(double)P.acc[0][p], (double)P.acc[1][p], (double)P.acc[2][p]};
+        // gathers in the particle precision (FP64 arithmetic for FP32
+        // particles would make this pass FP64-pipe bound)
+        R disp[3] = {0, 0, 0}, acc[3] = {0, 0, 0}, vel[3] = {0, 0, 0};
+        const R aold[3] = {P.acc[0][p], P.acc[1][p], P.acc[2][p]};
         if (model != -1) {
             for (int q = 0; q < NE; q++)
                 for (int c = 0; c < 3; c++) {
-                    disp[c] += (double)Nw[q] * ndispl[c * N + nid[q]];
-                    acc[c] += (double)Nw[q] * naccel[c * N + nid[q]];
-                    vel[c] += (double)Nw[q] * nvel[c * N + nid[q]];
+                    disp[c] += Nw[q] * (R)ndispl[c * N + nid[q]];
+                    acc[c] += Nw[q] * (R)naccel[c * N + nid[q]];
+                    vel[c] += Nw[q] * (R)nvel[c * N + nid[q]];
                 }
         }
         // shifting gradient at the old position with the new volume (material_point.cpp:192-216)
@@ -1018,11 +1026,12 @@ __global__ void __launch_bounds__(128) k_imp_g2p(ImpArgs a, PView<R> P, const do
         }
         // CommitParticleKinematics (nonlinear_time_integration.cpp:83-96), shift added by k_imp_shift
         float amax = 0.0f, vmax = 0.0f;
+        const R dtr = (R)a.dt, gam = (R)a.gamma;
         for (int c = 0; c < 3; c++) {
-            const double vc = flip ? (double)P.v[c][p] + a.dt * ((1.0 - a.gamma) * aold[c] + a.gamma * acc[c]) : vel[c];
-            P.v[c][p] = (R)vc;
-            P.acc[c][p] = (R)acc[c];
-            P.x[c][p] = (R)((double)x[c] + disp[c]);
+            const R vc = flip ? P.v[c][p] + dtr * (((R)1 - gam) * aold[c] + gam * acc[c]) : vel[c];
+            P.v[c][p] = vc;
+            P.acc[c][p] = acc[c];
+            P.x[c][p] = x[c] + disp[c];
             amax = fmaxf(amax, (float)fabs(acc[c]));
             vmax = fmaxf(vmax, (float)fabs(vc));
         }

@@ -124,4 +124,5 @@ def test_cantilever_1_7m_3_steps_vs_oracle(precision):
     if precision == 64:
         assert max(errs.values()) <= 1e-9, errs
     else:
-        assert errs["x"] <= 1e-6 and errs["v"] <= 1e-3 and errs["sigma"] <= 1e-3 and errs["F"] <= 1e-5, errs
+        # measured on a GB300: x 4.3e-8, v 8.7e-6, sigma 1.3e-5, F 7.4e-10
+        assert errs["x"] <= 5e-7 and errs["v"] <= 1e-4 and errs["sigma"] <= 1e-4 and errs["F"] <= 1e-8, errs
