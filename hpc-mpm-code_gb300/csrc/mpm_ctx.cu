@@ -194,6 +194,7 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
         return st;
     }
     cudaMemcpy(c->d_iprop, mat->iprop, sizeof(int) * c->nmat, cudaMemcpyHostToDevice);
+    for (int k = 0; k < c->nmat; k++) c->sigma_in = c->sigma_in || mat->iprop[k] == 0;
     cudaMemcpy(c->d_matprop, mat->mat_prop, sizeof(double) * 3 * c->nmat, cudaMemcpyHostToDevice);
     cudaMemset(c->d_acc, 0, sizeof(unsigned long long) * NACC * N);
     cudaMemset(c->d_acc2, 0, sizeof(unsigned long long) * 3 * N);
@@ -495,11 +496,7 @@ static mpm_status capture_block(mpm_ctx *c, int G, double facl) {
     c->graph_launches = c->launches - l0;
     c->graph_facl = facl;
     c->graph_stream = c->stream;
-    c->graph_tune[0] = c->tune.p2g_minb;
-    c->graph_tune[1] = c->tune.musl_minb;
-    c->graph_tune[2] = c->tune.update_ctas_per_sm;
-    c->graph_tune[3] = c->tune.p2g_staged;
-    c->graph_tune[4] = c->tune.musl_staged;
+    c->graph_tune = c->tune;
     c->graph_cur = c->cur;
     c->graph_pbuf[0] = c->pbuf[0];
     c->graph_pbuf[1] = c->pbuf[1];
@@ -523,9 +520,7 @@ mpm_status mpm_gpu_step_explicit(mpm_ctx *c, int nsteps, double facl) {
         done++;
     }
     if (c->graph_exec && (c->graph_facl != facl || c->graph_stream != c->stream ||
-                          c->graph_tune[0] != c->tune.p2g_minb || c->graph_tune[1] != c->tune.musl_minb ||
-                          c->graph_tune[2] != c->tune.update_ctas_per_sm || c->graph_tune[3] != c->tune.p2g_staged ||
-                          c->graph_tune[4] != c->tune.musl_staged ||
+                          !mpm::same_launches(c->graph_tune, c->tune) ||
                           c->graph_cur != c->cur ||
                           c->graph_pbuf[0] != c->pbuf[0] || c->graph_pbuf[1] != c->pbuf[1]))
         drop_graph(c);
@@ -1041,13 +1036,14 @@ mpm_status mpm_gpu_autotune(mpm_ctx *c, int steps_per_trial, double facl) {
 
 mpm_status mpm_gpu_set_tuning(mpm_ctx *c, int p2g_minb, int musl_minb, int update_ctas_per_sm) {
     if (!c) return MPM_ERR_BAD_ARG;
-    if ((p2g_minb < 0 || p2g_minb == 1 || p2g_minb > 7) || (musl_minb < 0 || musl_minb == 1 || musl_minb > 5) ||
+    if ((p2g_minb < 0 || p2g_minb == 1 || p2g_minb > 9) || (musl_minb < 0 || musl_minb == 1 || musl_minb > 7) ||
         update_ctas_per_sm < 0 || update_ctas_per_sm > 8)
         return MPM_ERR_BAD_ARG;
     c->tune.p2g_staged = p2g_minb == 0;
-    c->tune.p2g_moments = p2g_minb == 4 ? 1 : p2g_minb == 5 ? 2 : p2g_minb == 6 ? 3 : p2g_minb == 7 ? 4 : 0;
+    c->tune.p2g_moments = p2g_minb >= 4 ? p2g_minb - 3 : 0;
     if (p2g_minb == 2 || p2g_minb == 3) c->tune.p2g_minb = p2g_minb;
     c->tune.musl_staged = musl_minb == 0 ? 1 : musl_minb == 4 ? 2 : 0;
+    c->tune.musl_moments = musl_minb == 6 ? 1 : musl_minb == 7 ? 2 : 0;
     if (musl_minb == 2 || musl_minb == 3 || musl_minb == 5) c->tune.musl_minb = musl_minb;
     c->tune.update_ctas_per_sm = update_ctas_per_sm;
     return MPM_OK;
@@ -1057,7 +1053,8 @@ mpm_status mpm_gpu_get_tuning(mpm_ctx *c, int *p2g_minb, int *musl_minb, int *up
     if (!c) return MPM_ERR_BAD_ARG;
     if (p2g_minb)
         *p2g_minb = c->tune.p2g_moments ? 3 + c->tune.p2g_moments : c->tune.p2g_staged ? 0 : c->tune.p2g_minb;
-    if (musl_minb) *musl_minb = c->tune.musl_staged == 2 ? 4 : c->tune.musl_staged ? 0 : c->tune.musl_minb;
+    if (musl_minb)
+        *musl_minb = c->tune.musl_moments ? 5 + c->tune.musl_moments : c->tune.musl_staged == 2 ? 4 : c->tune.musl_staged ? 0 : c->tune.musl_minb;
     if (update_ctas_per_sm) *update_ctas_per_sm = c->tune.update_ctas_per_sm;
     return MPM_OK;
 }

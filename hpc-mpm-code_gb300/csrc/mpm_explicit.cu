@@ -69,6 +69,8 @@ struct StepArgs {
     int gnorm;                  // FP32 gathers divide by their weight sum
     int implicit;               // implicit solid: the force fields carry sum N m a (AccelP2G)
     int fbar;                   // F-bar projection: k_grid2 leaves the nodal volume sums to k_fbar_grid
+    int sigma_in;               // some material's stress update reads the previous stress (model 0)
+    int single_mat;             // one material: every particle's matid is 0
     double nump;                // particle count as a bound factor
     double mmax;                // max particle mass
     double gshape;              // bound on |dN/dx|
@@ -281,6 +283,32 @@ __device__ __forceinline__ void p2g_particle(const StepArgs<float> &a, const Sca
         }
 }
 
+// Node n of a brick's (BRX+1)(BRY+1)(BRZ+1) node box: its grid indices
+// (false outside the grid) and, for corner c = i + 2 (j + 2 k), the brick-local
+// index of the cell (nx - i, ny - j, nz - k) or -1 where that cell is not in
+// the brick.
+constexpr int BOX_NODES = (BRX + 1) * (BRY + 1) * (BRZ + 1);
+__device__ __forceinline__ bool box_node_cells(const KGeom<float> &g, int n, int ox, int oy, int oz, int &gx,
+                                               int &gy, int &gz, int *off) {
+    constexpr int NX = BRX + 1, NY = BRY + 1;
+    const int nx = n % NX, ny = (n / NX) % NY, nz = n / (NX * NY);
+    gx = ox + nx;
+    gy = oy + ny;
+    gz = oz + nz;
+    if (gx >= g.nnc[0] || gy >= g.nnc[1] || gz >= g.nnc[2]) return false;
+#pragma unroll
+    for (int k = 0; k < 2; k++)
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const int ex = nx - i, ey = ny - j, ez = nz - k;
+                off[i + 2 * (j + 2 * k)] = (ex >= 0 && ex < BRX && ey >= 0 && ey < BRY && ez >= 0 && ez < BRZ)
+                                               ? ex + BRX * (ey + BRY * ez) : -1;
+            }
+    return true;
+}
+
 // The end of a cell-P2G CTA: corners to shared memory, counters, and the
 // node pass: each node of the (BRX+1)(BRY+1)(BRZ+1) box adds the corners of
 // its adjacent cells in a fixed order and issues one int64 RED per field.
@@ -297,29 +325,26 @@ __device__ __forceinline__ void p2g_node_pass(const StepArgs<float> &a, const Sc
         if (tot >> 16) atomicAdd(&a.ctl->err_oob, (unsigned)(tot >> 16));
     }
     __syncthreads();
-    constexpr int NX = BRX + 1, NY = BRY + 1, NZ = BRZ + 1, NB = NX * NY * NZ;
-    for (int it = threadIdx.x; it < NB * NACC; it += CELL_THREADS) {
-        const int f = it / NB, n = it % NB;
-        const int nx = n % NX, ny = (n / NX) % NY, nz = n / (NX * NY);
-        const int gx = ox + nx, gy = oy + ny, gz = oz + nz;
-        if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
-        float sum = 0.0f;
-#pragma unroll
-        for (int k = 0; k < 2; k++)
-#pragma unroll
-            for (int j = 0; j < 2; j++)
-#pragma unroll
-                for (int i = 0; i < 2; i++) {
-                    const int ex = nx - i, ey = ny - j, ez = nz - k;
-                    if (ex >= 0 && ex < BRX && ey >= 0 && ey < BRY && ez >= 0 && ez < BRZ)
-                        sum += corner[f * 8 + i + 2 * (j + 2 * k)][ex + BRX * (ey + BRY * ez)];
-                }
+    // one thread per node of the box, all fields: the node's adjacent cells
+    // are found once and each field's corners are added in the fixed order
+    // (k, j, i) = (0, 0, 0) .. (1, 1, 1)
+    for (int n = threadIdx.x; n < BOX_NODES; n += CELL_THREADS) {
+        int gx, gy, gz, off[8];
+        if (!box_node_cells(a.g, n, ox, oy, oz, gx, gy, gz, off)) continue;
         // every node of a non-empty brick's box is marked active, so that the
         // grid passes also refresh nodes a particle touches with zero weight
-        if (f == 0) a.tileflag[tile_of_node(a.g, gx, gy, gz)] = 1;
-        if (sum != 0.0f) {
-            const Fix &F = f == 0 ? S.m : f == 1 ? S.v : f <= 4 ? S.p : S.f;
-            atomic_add_i64(&a.acc[(size_t)f * a.g.nodec + node_id(a.g, gx, gy, gz)], fx(sum, F));
+        a.tileflag[tile_of_node(a.g, gx, gy, gz)] = 1;
+        const size_t gn = node_id(a.g, gx, gy, gz);
+#pragma unroll
+        for (int f = 0; f < NACC; f++) {
+            float sum = 0.0f;
+#pragma unroll
+            for (int c = 0; c < 8; c++)
+                if (off[c] >= 0) sum += corner[f * 8 + c][off[c]];
+            if (sum != 0.0f) {
+                const Fix &F = f == 0 ? S.m : f == 1 ? S.v : f <= 4 ? S.p : S.f;
+                atomic_add_i64(&a.acc[(size_t)f * a.g.nodec + gn], fx(sum, F));
+            }
         }
     }
 }
@@ -372,6 +397,20 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell(StepArgs<float>
 // agree), each thread expands them into the four corners of its z-layer,
 // and the node pass is the one of k_p2g_cell.  Deterministic: every sum is
 // in a fixed order.
+// the cell-sum moments q x {1, u, v, w, uv, uw, vw, uvw} of a pair (already
+// added across the lanes) expanded into the four corners (i, j, h) of lane h
+__device__ __forceinline__ void moments_to_layer(const float *M, int h, float *out) {
+    const float sz = h ? 1.0f : -1.0f;
+    // the layer's bilinear coefficients over {1, u, v, uv}
+    const float L0 = M[0] * 0.125f + sz * M[3] * 0.25f, L1 = M[1] * 0.25f + sz * M[5] * 0.5f,
+                L2 = M[2] * 0.25f + sz * M[6] * 0.5f, L3 = M[4] * 0.5f + sz * M[7];
+    const float lo = L0 - L2, hi = L0 + L2, dlo = L1 - L3, dhi = L1 + L3;
+    out[0] = lo - dlo;   // (i, j) = (0, 0)
+    out[1] = lo + dlo;   // (1, 0)
+    out[2] = hi - dhi;   // (0, 1)
+    out[3] = hi + dhi;   // (1, 1)
+}
+
 __device__ __forceinline__ float cell_offset_u(float x, const KGeom<float> &g, int d, int c) {
     const float xy = g.xmin[d] + g.dx[d] * (float)c;   // as axis_linear forms x - x_i
     return (x - xy) * g.inv_dx[d] - 0.5f;
@@ -388,7 +427,22 @@ __device__ __noinline__ void p2g_miss(const StepArgs<float> &a, const Scales &S,
     p2g_particle<AFF>(a, S, cx, cy, cz, 1, x0, x1, x2, m, vol, vel, sg, fxg, fyg, fzg, dummy, misses, oobs, -1, A);
 }
 
-template <int MINB, bool LIST>
+// the inputs of one particle of the moment-form P2G
+struct P2gIn {
+    float x[3], m, vol, v[3], s[6];
+};
+__device__ __forceinline__ void p2g_fetch(const Particles<float> &P, int p, P2gIn &o) {
+#pragma unroll
+    for (int d = 0; d < 3; d++) o.x[d] = ld(P.x[d] + p);
+    o.m = ld(P.m + p);
+    o.vol = ld(P.vol + p);
+#pragma unroll
+    for (int d = 0; d < 3; d++) o.v[d] = ld(P.v[d] + p);
+#pragma unroll
+    for (int e = 0; e < 6; e++) o.s[e] = ld(P.s[e] + p);
+}
+
+template <int MINB, bool LIST, bool PF = false>
 __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_mom(StepArgs<float> a) {
     __shared__ float corner[NACC * 8][BRC];       // 32 KB
     __shared__ Scales S;
@@ -416,12 +470,20 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_mom(StepArgs<fl
 #pragma unroll
             for (int k = 0; k < 4; k++) Fm[f][k] = 0.0f;
         int misses = 0, oobs = 0;
+        P2gIn nx;
+        if (PF && p0 + h < p1) p2g_fetch(P, p0 + h, nx);
         for (int p = p0 + h; p < p1; p += 2) {
-            const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p);
-            const float m = ld(P.m + p), vol = ld(P.vol + p);
-            const float vel[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
-            const float sg[6] = {ld(P.s[0] + p), ld(P.s[1] + p), ld(P.s[2] + p),
-                                 ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
+            // PF: this particle's inputs were loaded one iteration ahead, and the
+            // next one's loads are issued before the work on this one
+            P2gIn in;
+            if (PF) {
+                in = nx;
+                if (p + 2 < p1) p2g_fetch(P, p + 2, nx);
+            } else {
+                p2g_fetch(P, p, in);
+            }
+            const float x0 = in.x[0], x1 = in.x[1], x2 = in.x[2], m = in.m, vol = in.vol;
+            const float *vel = in.v, *sg = in.s;
             bool oob = false;
             const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
             if (px != cx || py != cy || pz != cz) {
@@ -458,36 +520,31 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_mom(StepArgs<fl
         for (int f = 0; f < 9; f++)
 #pragma unroll
             for (int k = 0; k < 4; k++) Fm[f][k] += __shfl_xor_sync(pair, Fm[f][k], 1);
-        // corners (i, j, h) of this thread's z-layer
+        // corners (i, j, h) of this thread's z-layer: with the layer's sign
+        // sz folded in first, every field is K0 + sx K1 + sy K2 + sx sy K3
         float acc[NACC][4];
         const float sz = h ? 1.0f : -1.0f;
         const float gv[3] = {fxg, fyg, fzg};
 #pragma unroll
-        for (int j = 0; j < 2; j++)
+        for (int f = 0; f < 5; f++) moments_to_layer(M[f], h, acc[f]);
 #pragma unroll
-            for (int i = 0; i < 2; i++) {
-                const int c = i + 2 * j;
-                const float sx = i ? 1.0f : -1.0f, sy = j ? 1.0f : -1.0f;
+        for (int ax = 0; ax < 3; ax++) {
+            // internal force -sum_b dN/dx_b (vol sigma_ab): the derivative along
+            // b carries the sign of b's axis, the bilinear part the other two
+            const float *Fx = Fm[3 * ax], *Fy = Fm[3 * ax + 1], *Fz = Fm[3 * ax + 2];
+            const float ix = a.g.inv_dx[0], iy = a.g.inv_dx[1], iz = a.g.inv_dx[2] * sz;
+            // d/dx: sx (Fx0/4 + sz Fx2/2 + sy (Fx1/2 + sz Fx3)); Fx's bilinear axes are (y, z)
+            const float ax0 = ix * (Fx[0] * 0.25f + sz * Fx[2] * 0.5f), bx0 = ix * (Fx[1] * 0.5f + sz * Fx[3]);
+            // d/dy: sy (Fy0/4 + sz Fy2/2 + sx (Fy1/2 + sz Fy3)); Fy's bilinear axes are (x, z)
+            const float ay1 = iy * (Fy[0] * 0.25f + sz * Fy[2] * 0.5f), by1 = iy * (Fy[1] * 0.5f + sz * Fy[3]);
+            // d/dz: sz (Fz0/4 + sx Fz1/2 + sy Fz2/2 + sx sy Fz3); Fz's bilinear axes are (x, y)
+            const float K0 = iz * Fz[0] * 0.25f, K1 = ax0 + iz * Fz[1] * 0.5f, K2 = ay1 + iz * Fz[2] * 0.5f,
+                        K3 = bx0 + by1 + iz * Fz[3];
+            const float lo = K0 - K2, hi = K0 + K2, dlo = K1 - K3, dhi = K1 + K3;
+            const float T[4] = {lo - dlo, lo + dlo, hi - dhi, hi + dhi};
 #pragma unroll
-                for (int f = 0; f < 5; f++)
-                    acc[f][c] = M[f][0] * 0.125f + (sx * M[f][1] + sy * M[f][2] + sz * M[f][3]) * 0.25f +
-                                (sx * sy * M[f][4] + sx * sz * M[f][5] + sy * sz * M[f][6]) * 0.5f +
-                                sx * sy * sz * M[f][7];
-                // the signs of the two bilinear axes of each derivative direction b
-                const float sb[3] = {sx, sy, sz};
-                const float sc[3] = {sy, sx, sx}, sd[3] = {sz, sz, sy};
-#pragma unroll
-                for (int ax = 0; ax < 3; ax++) {
-                    float fi = 0.0f;
-#pragma unroll
-                    for (int bb = 0; bb < 3; bb++) {
-                        const float *F = Fm[3 * ax + bb];
-                        fi += a.g.inv_dx[bb] * sb[bb] *
-                              (F[0] * 0.25f + (sc[bb] * F[1] + sd[bb] * F[2]) * 0.5f + sc[bb] * sd[bb] * F[3]);
-                    }
-                    acc[5 + ax][c] = -fi + acc[0][c] * gv[ax];
-                }
-            }
+            for (int c = 0; c < 4; c++) acc[5 + ax][c] = fmaf(acc[0][c], gv[ax], -T[c]);
+        }
         p2g_node_pass(a, S, corner, sh_red, lc, h, ox, oy, oz, acc, misses, oobs);
         __syncthreads();   // shared memory is reused by the next brick
     }
@@ -873,24 +930,18 @@ __device__ __forceinline__ void musl_node_pass(const StepArgs<float> &a, const S
         if (vm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VMAX], vm * 1.000001f);
     }
     __syncthreads();
-    constexpr int NX = BRX + 1, NY = BRY + 1, NZ = BRZ + 1, NB = NX * NY * NZ;
-    for (int it = threadIdx.x; it < NB * 3; it += CELL_THREADS) {
-        const int d = it / NB, n = it % NB;
-        const int nx = n % NX, ny = (n / NX) % NY, nz = n / (NX * NY);
-        const int gx = ox + nx, gy = oy + ny, gz = oz + nz;
-        if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
-        float sum = 0.0f;
+    for (int n = threadIdx.x; n < BOX_NODES; n += CELL_THREADS) {
+        int gx, gy, gz, off[8];
+        if (!box_node_cells(a.g, n, ox, oy, oz, gx, gy, gz, off)) continue;
+        const size_t gn = node_id(a.g, gx, gy, gz);
 #pragma unroll
-        for (int k = 0; k < 2; k++)
+        for (int d = 0; d < 3; d++) {
+            float sum = 0.0f;
 #pragma unroll
-            for (int j = 0; j < 2; j++)
-#pragma unroll
-                for (int i = 0; i < 2; i++) {
-                    const int ex = nx - i, ey = ny - j, ez = nz - k;
-                    if (ex >= 0 && ex < BRX && ey >= 0 && ey < BRY && ez >= 0 && ez < BRZ)
-                        sum += corner[d * 8 + i + 2 * (j + 2 * k)][ex + BRX * (ey + BRY * ez)];
-                }
-        if (sum != 0.0f) atomic_add_i64(&a.acc2[d * N + node_id(a.g, gx, gy, gz)], fx(sum, S.q));
+            for (int c = 0; c < 8; c++)
+                if (off[c] >= 0) sum += corner[d * 8 + c][off[c]];
+            if (sum != 0.0f) atomic_add_i64(&a.acc2[d * N + gn], fx(sum, S.q));
+        }
     }
 }
 
@@ -931,6 +982,170 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell(StepArgs<f
             }
             musl_particle(a, S, C, cx, cy, cz, h, p, ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p), ld(P.m + p),
                           ld(P.vol + p), vold, acc, gacc, vmax);
+        }
+        musl_node_pass(a, S, corner, sh_l, sh_f, lc, h, ox, oy, oz, acc, gacc, vmax);
+        __syncthreads();   // shared memory is reused by the next brick
+    }
+}
+
+// Gather + MUSL in moment form.  Inside one cell the linear interpolant of a
+// nodal field is a trilinear polynomial in the particle's offset (u, v, w)
+// from the cell centre (u in [-1/2, 1/2], as in k_p2g_cell_mom).  Each lane of
+// a cell's pair forms the eight monomial coefficients over
+// {1, u, v, w, uv, uw, vw, uvw} of the gather field (three components) and of
+// the shifting field once per cell, by a sum / difference stage per axis
+// ((f0 + f1) / 2, f1 - f0); the lanes exchange their z-layer halves for the z
+// stage, in the same operand order, so both hold the same coefficients.  A
+// constant field gives (f, 0, ..., 0) exactly, so the gathered velocity needs
+// no division by the weight sum.  Per particle the gather is 7 FMAs per
+// component, the shifting gradient 3 per axis, and the MUSL momentum m v is
+// summed against the monomials (24 FMAs) and expanded into corners once per
+// cell.  The two lanes take alternate particles.  Deterministic: every sum is
+// in a fixed order.  Same sums as the corner form up to FP32 rounding.
+__device__ __forceinline__ void lin_stage(float f0, float f1, float &a, float &b) {
+    a = (f0 + f1) * 0.5f;
+    b = f1 - f0;
+}
+
+// f: this lane's z-layer corners f[i + 2 j]; c: coefficients over
+// {1, u, v, w, uv, uw, vw, uvw}, the same in both lanes of the pair
+__device__ __forceinline__ void trilinear_coeffs(const float *f, int h, unsigned pair, float *c) {
+    float a0, b0, a1, b1, L[4];
+    lin_stage(f[0], f[1], a0, b0);    // x stage, j = 0
+    lin_stage(f[2], f[3], a1, b1);    // x stage, j = 1
+    lin_stage(a0, a1, L[0], L[2]);    // y stage: {1, v} of the layer
+    lin_stage(b0, b1, L[1], L[3]);    //          {u, uv}
+    float lo[4], hi[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float o = __shfl_xor_sync(pair, L[k], 1);
+        lo[k] = h ? o : L[k];
+        hi[k] = h ? L[k] : o;
+    }
+    lin_stage(lo[0], hi[0], c[0], c[3]);   // 1, w
+    lin_stage(lo[1], hi[1], c[1], c[5]);   // u, uw
+    lin_stage(lo[2], hi[2], c[2], c[6]);   // v, vw
+    lin_stage(lo[3], hi[3], c[4], c[7]);   // uv, uvw
+}
+
+__device__ __forceinline__ float trilinear_eval(const float *c, float u, float v, float w, float uv, float uw,
+                                                float vw, float uvw) {
+    float r = fmaf(c[1], u, c[0]);
+    r = fmaf(c[2], v, r);
+    r = fmaf(c[3], w, r);
+    r = fmaf(c[4], uv, r);
+    r = fmaf(c[5], uw, r);
+    r = fmaf(c[6], vw, r);
+    return fmaf(c[7], uvw, r);
+}
+
+// the inputs of one particle of the moment-form gather (v: FLIP only)
+struct MuslIn {
+    float x[3], m, vol, v[3];
+};
+__device__ __forceinline__ void musl_fetch(const Particles<float> &P, int p, bool flip, MuslIn &o) {
+    o.x[0] = ld(P.x[0] + p);
+    o.x[1] = ld(P.x[1] + p);
+    o.x[2] = ld(P.x[2] + p);
+    o.m = ld(P.m + p);
+    o.vol = ld(P.vol + p);
+    o.v[0] = flip ? ld(P.v[0] + p) : 0.0f;
+    o.v[1] = flip ? ld(P.v[1] + p) : 0.0f;
+    o.v[2] = flip ? ld(P.v[2] + p) : 0.0f;
+}
+
+template <int MINB, bool LIST>
+__global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_mom(StepArgs<float> a) {
+    __shared__ float corner[3 * 8][BRC];
+    __shared__ Scales S;
+    __shared__ long long sh_l[32];
+    __shared__ float sh_f[32];
+    load_scales_musl(a, S);
+    const int nbl = LIST ? *a.nblist : 1;
+    const bool flip = (a.scheme == MPM_FLIP);
+    const unsigned pair = 3u << ((threadIdx.x & 31) & ~1u);
+    for (int li = LIST ? (int)blockIdx.x : 0; li < nbl; li += LIST ? (int)gridDim.x : 1) {
+        const int b = LIST ? a.blist[li] : (int)blockIdx.x;
+        const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
+        const int *cs = a.cstart + (size_t)b * (BRC + 1);
+        if (cs[0] == cs[BRC]) continue;   // empty brick (uniform across the CTA)
+        int ox, oy, oz;
+        brick_origin(b, a.nbrick, ox, oy, oz);
+        const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
+        const int p0 = cs[lc], p1 = cs[lc + 1];
+        const Particles<float> &P = a.P;
+        // the first particle's loads are in flight with the cell's nodal values
+        MuslIn nx;
+        if (p0 + h < p1) musl_fetch(P, p0 + h, flip, nx);
+        float Gc[3][8], Ec[8];
+        {
+            MuslCell C;
+            musl_load_cell(a, cx, cy, cz, h, p1 > p0, C);
+#pragma unroll
+            for (int d = 0; d < 3; d++) trilinear_coeffs(C.G[d], h, pair, Gc[d]);
+            trilinear_coeffs(C.E, h, pair, Ec);
+        }
+        if (flip) {
+            // FLIP gathers the nodal acceleration: v += dt sum N a
+#pragma unroll
+            for (int d = 0; d < 3; d++)
+#pragma unroll
+                for (int k = 0; k < 8; k++) Gc[d][k] *= a.dt;
+        }
+#pragma unroll
+        for (int k = 1; k < 8; k++) {
+            // the shifting gradient is 2 vol grad(nei); d/dx = inv_dx d/du
+            Ec[k] *= 2.0f;
+        }
+        float M[3][8];
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+#pragma unroll
+            for (int k = 0; k < 8; k++) M[d][k] = 0.0f;
+        long long gacc = 0;
+        float vmax = 0.0f;
+        for (int p = p0 + h; p < p1; p += 2) {
+            // this particle's inputs, and the next one's loads issued before the work on this one
+            const float x0 = nx.x[0], x1 = nx.x[1], x2 = nx.x[2], m = nx.m, vol = nx.vol;
+            float vel[3] = {nx.v[0], nx.v[1], nx.v[2]};
+            if (p + 2 < p1) musl_fetch(P, p + 2, flip, nx);
+            bool oob = false;
+            const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
+            if (px != cx || py != cy || pz != cz) {
+                // a particle that left its sorted cell: the deferred pass (k_musl_misses)
+                a.miss[atomicAdd(&a.ctl->n_miss_musl, 1u)] = p;
+                continue;
+            }
+            const float u = cell_offset_u(x0, a.g, 0, px), v = cell_offset_u(x1, a.g, 1, py),
+                        w = cell_offset_u(x2, a.g, 2, pz);
+            const float uv = u * v, uw = u * w, vw = v * w, uvw = uv * w;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                const float g = trilinear_eval(Gc[d], u, v, w, uv, uw, vw, uvw);
+                vel[d] = flip ? vel[d] + g : g;
+            }
+            P.v[0][p] = vel[0];
+            P.v[1][p] = vel[1];
+            P.v[2][p] = vel[2];
+            vmax = fmaxf(vmax, fmaxf(fabsf(vel[0]), fmaxf(fabsf(vel[1]), fabsf(vel[2]))));
+            const float g0 = fmaf(Ec[7], vw, fmaf(Ec[5], w, fmaf(Ec[4], v, Ec[1]))) * a.g.inv_dx[0] * vol;
+            const float g1 = fmaf(Ec[7], uw, fmaf(Ec[6], w, fmaf(Ec[4], u, Ec[2]))) * a.g.inv_dx[1] * vol;
+            const float g2 = fmaf(Ec[7], uv, fmaf(Ec[6], v, fmaf(Ec[5], u, Ec[3]))) * a.g.inv_dx[2] * vol;
+            gacc += fx(g0 * g0 + g1 * g1 + g2 * g2, S.gd);
+            const float mono[8] = {1.0f, u, v, w, uv, uw, vw, uvw};
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                const float q = m * vel[d];
+#pragma unroll
+                for (int k = 0; k < 8; k++) M[d][k] = fmaf(q, mono[k], M[d][k]);
+            }
+        }
+        float acc[3][4];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+#pragma unroll
+            for (int k = 0; k < 8; k++) M[d][k] += __shfl_xor_sync(pair, M[d][k], 1);
+            moments_to_layer(M[d], h, acc[d]);
         }
         musl_node_pass(a, S, corner, sh_l, sh_f, lc, h, ox, oy, oz, acc, gacc, vmax);
         __syncthreads();   // shared memory is reused by the next brick
@@ -2668,17 +2883,25 @@ __global__ void __launch_bounds__(UCH, 3) k_g2p_update_tma(StepArgs<float> a, in
         fence_mbar_init();
     }
     __syncthreads();
+    // fields a step does not read are not copied: the previous stress unless
+    // a material updates it incrementally, the current volume unless the
+    // shifting is on (b0 != 0), the material ids of a one-material scene
+    const float rb0 = (float)a.ctl->b0;
+    const bool need_s = a.sigma_in != 0, need_vol = rb0 != 0.0f, need_mid = a.single_mat == 0;
+    auto wanted = [&](int f) { return (f < 12 || f >= 18 || need_s) && (f != 19 || need_vol); };
     auto issue = [&](int chunk, int stage) {
         const int p0 = chunk * UCH;
         const int cnt = min(UCH, (int)a.num - p0);
         const unsigned bytes = (unsigned)((cnt + 3) & ~3) * 4u;   // whole 16-byte units (arrays are padded)
         float *dst = (float *)(smem + stage * USTAGE);
+        unsigned nf = need_mid ? 1u : 0u;
+        for (int f = 0; f < UNF; f++) nf += wanted(f) ? 1u : 0u;
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_expect_tx(&bar[stage], bytes * (UNF + 1));
-        for (int f = 0; f < UNF; f++) bulk_g2s(dst + f * UCH, src[f] + p0, bytes, &bar[stage]);
-        bulk_g2s(dst + UNF * UCH, P.matid + p0, bytes, &bar[stage]);
+        mbar_expect_tx(&bar[stage], bytes * nf);
+        for (int f = 0; f < UNF; f++)
+            if (wanted(f)) bulk_g2s(dst + f * UCH, src[f] + p0, bytes, &bar[stage]);
+        if (need_mid) bulk_g2s(dst + UNF * UCH, P.matid + p0, bytes, &bar[stage]);
     };
-    const float rb0 = (float)a.ctl->b0;
     float volmax = 0.0f, vsmax = 0.0f;
     int bad = 0;
     bool failed = false;
@@ -2705,10 +2928,10 @@ __global__ void __launch_bounds__(UCH, 3) k_g2p_update_tma(StepArgs<float> a, in
                 for (int c = 0; c < 3; c++) H[r][c] = sf[(3 + 3 * r + c) * UCH + t];
             float s6[6];
 #pragma unroll
-            for (int k = 0; k < 6; k++) s6[k] = sf[(12 + k) * UCH + t];
+            for (int k = 0; k < 6; k++) s6[k] = need_s ? sf[(12 + k) * UCH + t] : 0.0f;
             GlobalNodes gnodes{a.nvel2, a.nei, N, a.g};
-            update_particle(a, P, p, x, H, s6, sf[18 * UCH + t], sf[19 * UCH + t], smid[t], rb0, gnodes, volmax,
-                            vsmax, bad);
+            update_particle(a, P, p, x, H, s6, sf[18 * UCH + t], need_vol ? sf[19 * UCH + t] : 0.0f,
+                            need_mid ? smid[t] : 0, rb0, gnodes, volmax, vsmax, bad);
         }
         __syncthreads();   // the stage is refilled only after every thread has read it
     }
@@ -2803,6 +3026,8 @@ static StepArgs<R> make_args(mpm_ctx *c) {
     a.shifting = c->shifting;
     a.all_tiles = c->write_nodal_dl ? 1 : 0;
     a.gnorm = c->gather_norm;
+    a.sigma_in = c->sigma_in ? 1 : 0;
+    a.single_mat = c->nmat == 1 ? 1 : 0;
     a.implicit = c->nreal == 27 ? 1 : 0;
     a.nump = (double)c->num;
     a.mmax = c->mmax;
@@ -2857,6 +3082,10 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                     k_p2g_cell_mom<1, false><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
                 } else if (c->tune.p2g_moments == 4) {
                     k_p2g_cell_mom<3, true><<<list_grid(c, 3), CELL_THREADS, 0, c->stream>>>(a);
+                } else if (c->tune.p2g_moments == 5) {
+                    k_p2g_cell_mom<2, true, true><<<list_grid(c, 2), CELL_THREADS, 0, c->stream>>>(a);
+                } else if (c->tune.p2g_moments == 6) {
+                    k_p2g_cell_mom<1, true, true><<<list_grid(c, 1), CELL_THREADS, 0, c->stream>>>(a);
                 } else if (c->tune.p2g_moments) {
                     if (c->tune.brick_list)
                         k_p2g_cell_mom<2, true><<<list_grid(c, 2), CELL_THREADS, 0, c->stream>>>(a);
@@ -2905,7 +3134,11 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
         timer_begin(c, K_G2P_MUSL);
         if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
             if (use_cell_kernels(c)) {
-                if (c->tune.musl_staged == 2) {
+                if (c->tune.musl_moments == 2) {
+                    k_g2p_musl_mom<2, true><<<list_grid(c, 2), CELL_THREADS, 0, c->stream>>>(a);
+                } else if (c->tune.musl_moments) {
+                    k_g2p_musl_mom<3, true><<<list_grid(c, 3), CELL_THREADS, 0, c->stream>>>(a);
+                } else if (c->tune.musl_staged == 2) {
                     k_musl_brick<<<c->g.nbricks, BCH, 0, c->stream>>>(a);
                 } else if (c->tune.musl_staged) {
                     static bool attr = false;

@@ -108,8 +108,10 @@ struct WorkItem {
 };
 
 
-// Launch variants that give bitwise identical results; chosen by
-// mpm_gpu_autotune from measured times (defaults otherwise).
+// Launch variants.  The ones mpm_gpu_autotune chooses between from measured
+// times (staged or direct, resident CTAs per SM) give bitwise identical
+// results; the moment forms (the defaults) differ from the corner forms by
+// FP32 rounding only and are not switched by the autotuner.
 struct Tune {
     int p2g_moments = 1;            // FP32 P2G in moment form (k_p2g_cell_mom); 0: corner sums
     int brick_list = 1;             // moment P2G and gather + MUSL walk the list of bricks holding particles
@@ -117,9 +119,17 @@ struct Tune {
     int p2g_minb = 2;               // resident CTAs the direct per-cell P2G is compiled for (2 or 3)
     int musl_staged = 0;            // gather + MUSL reads the brick's particles from staged shared memory
     int musl_minb = 3;              // resident CTAs the direct gather + MUSL kernel is compiled for
+    int musl_moments = 2;           // FP32 gather + MUSL in moment form (k_g2p_musl_mom, 1: 3 / 2: 2 resident CTAs per SM); 0: corner form
     int update_ctas_per_sm = 3;     // persistent CTAs per SM of the staged particle update (0: per-brick update)
     bool done = false;
 };
+
+// two tunings that launch the same kernels (a captured graph stays valid)
+inline bool same_launches(const Tune &x, const Tune &y) {
+    return x.p2g_moments == y.p2g_moments && x.brick_list == y.brick_list && x.p2g_staged == y.p2g_staged &&
+           x.p2g_minb == y.p2g_minb && x.musl_staged == y.musl_staged && x.musl_minb == y.musl_minb &&
+           x.musl_moments == y.musl_moments && x.update_ctas_per_sm == y.update_ctas_per_sm;
+}
 
 struct KernelTimer {
     bool on = false;
@@ -140,6 +150,7 @@ struct mpm_ctx {
     double dt = 0, mtol = 0, gravity[3] = {0, 0, 0};
     double facl = 1.0;
     int nmat = 0;
+    bool sigma_in = false;   // a material updates its stress incrementally (model 0 reads sigma)
     int npxye[3] = {1, 1, 1};
     cudaStream_t stream = nullptr;
     // host I/O pipeline of mpm_gpu_steps_host: copy streams and per-field events
@@ -207,7 +218,7 @@ struct mpm_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     double graph_facl = 0.0;
     cudaStream_t graph_stream = nullptr;
-    int graph_tune[5] = {0, 0, 0, 0, 0};
+    mpm::Tune graph_tune;
     int graph_cur = 0;
     void *graph_pbuf[2] = {nullptr, nullptr};
     int64_t graph_launches = 0;
