@@ -210,16 +210,23 @@ mpm_status mpm_gpu_enable_kernel_timing(mpm_ctx *ctx, int on);
  * direct per-cell P2G and the resident CTAs per SM of the per-cell scatter and
  * gather kernels, persistent CTAs per SM of the staged particle update) by
  * running 3 x steps_per_trial explicit steps.
- * All variants compute bitwise the same results, so the trial steps are
- * ordinary steps of the simulation.  The re-sort period is not tuned: it
- * changes FP32 rounding. */
+ * The variants it switches between compute bitwise the same results, so the
+ * trial steps are ordinary steps of the simulation; with the moment-form
+ * P2G and gather (the defaults) selected, only the update variant changes.
+ * Neither the form (moment or corner) nor the re-sort period is tuned: both
+ * change FP32 rounding. */
 mpm_status mpm_gpu_autotune(mpm_ctx *ctx, int steps_per_trial, double facl);
 /* p2g_minb / musl_minb: 0 = the shared-memory staged kernel, 2 or 3 = the
  * direct per-cell kernel compiled for that many resident CTAs per SM;
  * p2g_minb 4 (default) / 5 / 7 = the moment-form P2G over the active-brick
- * list for 2 / 1 / 3 resident CTAs per SM, 6 = chunked bricks; musl_minb 4 =
- * one CTA per brick, 5 = the gather over the brick list for 4 resident CTAs
- * per SM (3 is the default); update_ctas_per_sm: 1..8 persistent CTAs per SM
+ * list for 2 / 1 / 3 resident CTAs per SM, 6 = chunked bricks, 8 / 9 = the
+ * moment-form P2G loading each particle one iteration ahead, for 2 / 1
+ * resident CTAs per SM; musl_minb 4 = one CTA per brick, 5 = the corner-form
+ * gather over the brick list for 4 resident CTAs per SM, 7 (default) / 6 =
+ * the moment-form gather for 2 / 3 resident CTAs per SM.  The moment forms
+ * differ from the corner forms by FP32 rounding; the corner-form variants
+ * (p2g_minb 0, 2, 3; musl_minb 0, 2, 3, 5) are bitwise identical to one
+ * another, as are the update variants; update_ctas_per_sm: 1..8 persistent CTAs per SM
  * of the bulk-copy staged particle update (3, the default, is what its 80
  * registers let reside), 0 = the update with one CTA per brick and the
  * brick's nodal values in shared memory. */
