@@ -229,13 +229,14 @@ __device__ __forceinline__ void p2g_particle(const StepArgs<float> &a, const Sca
                                              int &misses, int &oobs, int defer_p = -1, const float *A = nullptr) {
     bool oob = false;
     const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
-    oobs += oob && h == 0;
     Axis<float, 1> ax, ay, az;
     axis_eval<float, 1>(x0, a.g, 0, px, ax);
     axis_eval<float, 1>(x1, a.g, 1, py, ay);
     axis_eval<float, 1>(x2, a.g, 2, pz, az);
     const float mfx = m * fxg, mfy = m * fyg, mfz = m * fzg;
     const bool mine = (px == cx) && (py == cy) && (pz == cz);
+    // counted once, by the pass that scatters the particle (a deferred one by k_p2g_misses)
+    oobs += oob && h == 0 && (mine || defer_p < 0);
     const float wz = h ? az.w[1] : az.w[0], dwz = h ? az.dw[1] : az.dw[0];
     if (!mine) {
         // a particle that left its sorted cell scatters on its own, in the
@@ -312,6 +313,19 @@ __device__ __forceinline__ bool box_node_cells(const KGeom<float> &g, int n, int
 // The end of a cell-P2G CTA: corners to shared memory, counters, and the
 // node pass: each node of the (BRX+1)(BRY+1)(BRZ+1) box adds the corners of
 // its adjacent cells in a fixed order and issues one int64 RED per field.
+// The counters of the cell-P2G kernels: particles that left their sorted cell
+// and particles outside the grid.
+__device__ __forceinline__ void p2g_counters(const StepArgs<float> &a, int *sh_red, int misses, int oobs) {
+    int tot = block_reduce(misses + (oobs << 16), OpAddI(), sh_red);
+    if (threadIdx.x == 0 && tot) {
+        if (tot & 0xffff) atomicAdd(&a.ctl->tile_misses, (unsigned)(tot & 0xffff));
+        if (tot >> 16) atomicAdd(&a.ctl->err_oob, (unsigned)(tot >> 16));
+    }
+}
+
+// COUNT: reduce the counters here (false: the caller reduces them once, at
+// the end of a persistent CTA)
+template <bool COUNT = true>
 __device__ __forceinline__ void p2g_node_pass(const StepArgs<float> &a, const Scales &S, float (*corner)[BRC],
                                               int *sh_red, int lc, int h, int ox, int oy, int oz,
                                               const float (*acc)[4], int misses, int oobs) {
@@ -319,11 +333,7 @@ __device__ __forceinline__ void p2g_node_pass(const StepArgs<float> &a, const Sc
     for (int f = 0; f < NACC; f++)
 #pragma unroll
         for (int c = 0; c < 4; c++) corner[f * 8 + c + 4 * h][lc] = acc[f][c];
-    int tot = block_reduce(misses + (oobs << 16), OpAddI(), sh_red);
-    if (threadIdx.x == 0 && tot) {
-        if (tot & 0xffff) atomicAdd(&a.ctl->tile_misses, (unsigned)(tot & 0xffff));
-        if (tot >> 16) atomicAdd(&a.ctl->err_oob, (unsigned)(tot >> 16));
-    }
+    if (COUNT) p2g_counters(a, sh_red, misses, oobs);
     __syncthreads();
     // one thread per node of the box, all fields: the node's adjacent cells
     // are found once and each field's corners are added in the fixed order
@@ -415,6 +425,11 @@ __device__ __forceinline__ float cell_offset_u(float x, const KGeom<float> &g, i
     const float xy = g.xmin[d] + g.dx[d] * (float)c;   // as axis_linear forms x - x_i
     return (x - xy) * g.inv_dx[d] - 0.5f;
 }
+// the point lies in the cell whose centre the offsets are taken from (false
+// for a non-finite offset)
+__device__ __forceinline__ bool in_cell(float u, float v, float w) {
+    return u >= -0.5f && u < 0.5f && v >= -0.5f && v < 0.5f && w >= -0.5f && w < 0.5f;
+}
 
 // both z-layers of a particle that left its sorted cell, by fixed-point atomics
 template <bool AFF = false>
@@ -448,6 +463,7 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_mom(StepArgs<fl
     __shared__ Scales S;
     __shared__ int sh_red[32];
     load_scales(a, S);
+    int misses = 0, oobs = 0;   // over all of this CTA's bricks
     const int nbl = LIST ? *a.nblist : 1;
     for (int li = LIST ? (int)blockIdx.x : 0; li < nbl; li += LIST ? (int)gridDim.x : 1) {
         const int b = LIST ? a.blist[li] : (int)blockIdx.x;
@@ -469,7 +485,6 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_mom(StepArgs<fl
         for (int f = 0; f < 9; f++)
 #pragma unroll
             for (int k = 0; k < 4; k++) Fm[f][k] = 0.0f;
-        int misses = 0, oobs = 0;
         P2gIn nx;
         if (PF && p0 + h < p1) p2g_fetch(P, p0 + h, nx);
         for (int p = p0 + h; p < p1; p += 2) {
@@ -484,17 +499,16 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_mom(StepArgs<fl
             }
             const float x0 = in.x[0], x1 = in.x[1], x2 = in.x[2], m = in.m, vol = in.vol;
             const float *vel = in.v, *sg = in.s;
-            bool oob = false;
-            const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
-            if (px != cx || py != cy || pz != cz) {
-                // a particle that left its sorted cell scatters in the deferred pass
+            // offsets from the sorted cell's centre; a particle outside that
+            // cell (or outside the grid, or not finite) scatters in the
+            // deferred pass, which also counts the ones outside the grid
+            const float u = cell_offset_u(x0, a.g, 0, cx), v = cell_offset_u(x1, a.g, 1, cy),
+                        w = cell_offset_u(x2, a.g, 2, cz);
+            if (!in_cell(u, v, w)) {
                 misses++;
                 a.miss[atomicAdd(&a.ctl->n_miss_p2g, 1u)] = p;
                 continue;
             }
-            oobs += oob;
-            const float u = cell_offset_u(x0, a.g, 0, px), v = cell_offset_u(x1, a.g, 1, py),
-                        w = cell_offset_u(x2, a.g, 2, pz);
             const float uv = u * v, uw = u * w, vw = v * w;
             const float mono[8] = {1.0f, u, v, w, uv, uw, vw, uv * w};
             const float q[5] = {m, vol, m * vel[0], m * vel[1], m * vel[2]};
@@ -545,9 +559,10 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_mom(StepArgs<fl
 #pragma unroll
             for (int c = 0; c < 4; c++) acc[5 + ax][c] = fmaf(acc[0][c], gv[ax], -T[c]);
         }
-        p2g_node_pass(a, S, corner, sh_red, lc, h, ox, oy, oz, acc, misses, oobs);
+        p2g_node_pass<false>(a, S, corner, sh_red, lc, h, ox, oy, oz, acc, misses, oobs);
         __syncthreads();   // shared memory is reused by the next brick
     }
+    p2g_counters(a, sh_red, misses, oobs);
 }
 
 // P2G, one CTA of 128 threads per brick, in two phases per chunk of 128 of
@@ -915,6 +930,18 @@ __device__ __forceinline__ void musl_particle(const StepArgs<float> &a, const Sc
         }
 }
 
+// the counters of the gather + MUSL kernels: sum |geup|^2 and max |v|
+__device__ __forceinline__ void musl_counters(const StepArgs<float> &a, long long *sh_l, float *sh_f, long long gacc,
+                                              float vmax) {
+    long long gsum = block_reduce(gacc, OpAddL(), sh_l);
+    float vm = block_reduce(vmax, OpMaxF(), sh_f);
+    if (threadIdx.x == 0) {
+        if (gsum) atomicAdd(&a.ctl->geup_acc, (unsigned long long)gsum);
+        if (vm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VMAX], vm * 1.000001f);
+    }
+}
+
+template <bool COUNT = true>
 __device__ __forceinline__ void musl_node_pass(const StepArgs<float> &a, const Scales &S, float (*corner)[BRC],
                                                long long *sh_l, float *sh_f, int lc, int h, int ox, int oy, int oz,
                                                const float (*acc)[4], long long gacc, float vmax) {
@@ -923,12 +950,7 @@ __device__ __forceinline__ void musl_node_pass(const StepArgs<float> &a, const S
     for (int d = 0; d < 3; d++)
 #pragma unroll
         for (int c = 0; c < 4; c++) corner[d * 8 + c + 4 * h][lc] = acc[d][c];
-    long long gsum = block_reduce(gacc, OpAddL(), sh_l);
-    float vm = block_reduce(vmax, OpMaxF(), sh_f);
-    if (threadIdx.x == 0) {
-        if (gsum) atomicAdd(&a.ctl->geup_acc, (unsigned long long)gsum);
-        if (vm > 0.0f) atomic_max_pos(&a.ctl->nxt[a.parity ^ 1][B_VMAX], vm * 1.000001f);
-    }
+    if (COUNT) musl_counters(a, sh_l, sh_f, gacc, vmax);
     __syncthreads();
     for (int n = threadIdx.x; n < BOX_NODES; n += CELL_THREADS) {
         int gx, gy, gz, off[8];
@@ -1064,6 +1086,8 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_mom(StepArgs<fl
     const int nbl = LIST ? *a.nblist : 1;
     const bool flip = (a.scheme == MPM_FLIP);
     const unsigned pair = 3u << ((threadIdx.x & 31) & ~1u);
+    long long gacc = 0;   // over all of this CTA's bricks
+    float vmax = 0.0f;
     for (int li = LIST ? (int)blockIdx.x : 0; li < nbl; li += LIST ? (int)gridDim.x : 1) {
         const int b = LIST ? a.blist[li] : (int)blockIdx.x;
         const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
@@ -1102,22 +1126,18 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_mom(StepArgs<fl
         for (int d = 0; d < 3; d++)
 #pragma unroll
             for (int k = 0; k < 8; k++) M[d][k] = 0.0f;
-        long long gacc = 0;
-        float vmax = 0.0f;
         for (int p = p0 + h; p < p1; p += 2) {
             // this particle's inputs, and the next one's loads issued before the work on this one
             const float x0 = nx.x[0], x1 = nx.x[1], x2 = nx.x[2], m = nx.m, vol = nx.vol;
             float vel[3] = {nx.v[0], nx.v[1], nx.v[2]};
             if (p + 2 < p1) musl_fetch(P, p + 2, flip, nx);
-            bool oob = false;
-            const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
-            if (px != cx || py != cy || pz != cz) {
-                // a particle that left its sorted cell: the deferred pass (k_musl_misses)
+            const float u = cell_offset_u(x0, a.g, 0, cx), v = cell_offset_u(x1, a.g, 1, cy),
+                        w = cell_offset_u(x2, a.g, 2, cz);
+            if (!in_cell(u, v, w)) {
+                // a particle outside its sorted cell: the deferred pass (k_musl_misses)
                 a.miss[atomicAdd(&a.ctl->n_miss_musl, 1u)] = p;
                 continue;
             }
-            const float u = cell_offset_u(x0, a.g, 0, px), v = cell_offset_u(x1, a.g, 1, py),
-                        w = cell_offset_u(x2, a.g, 2, pz);
             const float uv = u * v, uw = u * w, vw = v * w, uvw = uv * w;
 #pragma unroll
             for (int d = 0; d < 3; d++) {
@@ -1147,9 +1167,10 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_mom(StepArgs<fl
             for (int k = 0; k < 8; k++) M[d][k] += __shfl_xor_sync(pair, M[d][k], 1);
             moments_to_layer(M[d], h, acc[d]);
         }
-        musl_node_pass(a, S, corner, sh_l, sh_f, lc, h, ox, oy, oz, acc, gacc, vmax);
+        musl_node_pass<false>(a, S, corner, sh_l, sh_f, lc, h, ox, oy, oz, acc, gacc, vmax);
         __syncthreads();   // shared memory is reused by the next brick
     }
+    musl_counters(a, sh_l, sh_f, gacc, vmax);
 }
 
 // Gather + MUSL, one CTA of 128 threads per brick, two phases per chunk of
@@ -1434,6 +1455,7 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell_staged(Ste
 template <bool AFF = false>
 __global__ void __launch_bounds__(256) k_p2g_misses(StepArgs<float> a) {
     __shared__ Scales S;
+    __shared__ int sh_red[32];
     load_scales(a, S);
     const unsigned n = a.ctl->n_miss_p2g;
     const float fxg = a.grav[0] * a.facl, fyg = a.grav[1] * a.facl, fzg = a.grav[2] * a.facl;
@@ -1452,6 +1474,10 @@ __global__ void __launch_bounds__(256) k_p2g_misses(StepArgs<float> a) {
         p2g_miss<AFF>(a, S, -1, -1, -1, ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p), ld(P.m + p), ld(P.vol + p),
                       vel, sg, fxg, fyg, fzg, misses, oobs, A);
     }
+    // the particles outside the grid (every one of them is deferred by the
+    // moment-form P2G)
+    const int tot = block_reduce(oobs, OpAddI(), sh_red);
+    if (threadIdx.x == 0 && tot) atomicAdd(&a.ctl->err_oob, (unsigned)tot);
 }
 
 __global__ void __launch_bounds__(256) k_musl_misses(StepArgs<float> a) {
@@ -2067,8 +2093,12 @@ __global__ void __launch_bounds__(256) k_affine_musl(StepArgs<R> a) {
 }
 
 // ------------------------------------------------------------ grid pass 1
+constexpr int GRID_THREADS = 256;                            // threads of a grid-pass CTA
+constexpr int GRID_NPT = TILE * TILE * TILE / GRID_THREADS;  // nodes of a tile per thread
+static_assert(GRID_NPT * GRID_THREADS == TILE * TILE * TILE, "a grid-pass CTA covers its tile exactly");
+
 template <typename R, bool LIST>
-__global__ void __launch_bounds__(256) k_grid1(StepArgs<R> a) {
+__global__ void __launch_bounds__(GRID_THREADS) k_grid1(StepArgs<R> a) {
     __shared__ double sh_d[32];
     __shared__ float sh_f[32];
     __shared__ bool s_last;
@@ -2084,23 +2114,43 @@ __global__ void __launch_bounds__(256) k_grid1(StepArgs<R> a) {
         int tx, ty, tz;
         tile_coords(t, a.g.ntile, tx, ty, tz);
         const size_t N = (size_t)a.g.nodec;
-        for (int li = threadIdx.x; li < TILE * TILE * TILE; li += blockDim.x) {
-            const int gx = tx * TILE + (li % TILE), gy = ty * TILE + (li / TILE) % TILE, gz = tz * TILE + li / (TILE * TILE);
-            if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
-            const size_t n = node_id(a.g, gx, gy, gz);
-            const R mass = unfx((long long)a.acc[n], S.m, (R)0);
-            R vof = unfx((long long)a.acc[N + n], S.v, (R)0);
-            R nv[3], na[3];
+        // the tile's nodes, GRID_NPT per thread: every load of them is issued
+        // before any of them is used
+        long long q[GRID_NPT][NACC];
+        unsigned char bfl[GRID_NPT];
+        double nvl[GRID_NPT];
+        size_t nid[GRID_NPT];
+        bool in[GRID_NPT];
 #pragma unroll
+        for (int k = 0; k < GRID_NPT; k++) {
+            const int li = threadIdx.x + k * GRID_THREADS;
+            const int gx = tx * TILE + (li % TILE), gy = ty * TILE + (li / TILE) % TILE, gz = tz * TILE + li / (TILE * TILE);
+            in[k] = gx < a.g.nnc[0] && gy < a.g.nnc[1] && gz < a.g.nnc[2];
+            nid[k] = in[k] ? node_id(a.g, gx, gy, gz) : 0;
+            if (in[k]) {
+#pragma unroll
+                for (int f = 0; f < NACC; f++) q[k][f] = (long long)a.acc[f * N + nid[k]];
+                bfl[k] = a.bcflag[nid[k]];
+                nvl[k] = a.nvol[nid[k]];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < GRID_NPT; k++) {
+            if (!in[k]) continue;
+            const size_t n = nid[k];
+            const R mass = unfx(q[k][0], S.m, (R)0);
+            R vof = unfx(q[k][1], S.v, (R)0);
+            R nv[3], na[3];
             const R im = (mass > a.mtol) ? recip<R>(mass) : (R)0;   // one reciprocal per node
+#pragma unroll
             for (int c = 0; c < 3; c++) {
-                const R pc = unfx((long long)a.acc[(2 + c) * N + n], S.p, (R)0);
-                const R fc = unfx((long long)a.acc[(5 + c) * N + n], S.f, (R)0);
+                const R pc = unfx(q[k][2 + c], S.p, (R)0);
+                const R fc = unfx(q[k][5 + c], S.f, (R)0);
                 nv[c] = pc * im;
                 na[c] = fc * im;
             }
             if (vof < a.mtol) vof = (R)0;
-            const unsigned char bf = a.bcflag[n];
+            const unsigned char bf = bfl[k];
             if (bf) {
 #pragma unroll
                 for (int c = 0; c < 3; c++)
@@ -2122,7 +2172,7 @@ __global__ void __launch_bounds__(256) k_grid1(StepArgs<R> a) {
                 a.G[c * N + n] = gv;
                 gmax = fmaxf(gmax, fabsf((float)gv));
             }
-            R e = vof - (R)a.nvol[n];
+            R e = vof - (R)nvl[k];
             e = e > (R)0 ? e : (R)0;
             a.nei[n] = e;
             eu += (float)e * (float)e;
@@ -2163,7 +2213,7 @@ __global__ void __launch_bounds__(256) k_grid1(StepArgs<R> a) {
 
 // ------------------------------------------------------------ grid pass 2
 template <typename R, bool LIST>
-__global__ void __launch_bounds__(256) k_grid2(StepArgs<R> a) {
+__global__ void __launch_bounds__(GRID_THREADS) k_grid2(StepArgs<R> a) {
     __shared__ Scales S;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         // b0 of DeltaCorrectionParticleShifting (material_point.cpp:219)
@@ -2178,19 +2228,36 @@ __global__ void __launch_bounds__(256) k_grid2(StepArgs<R> a) {
     int tx, ty, tz;
     tile_coords(t, a.g.ntile, tx, ty, tz);
     const size_t N = (size_t)a.g.nodec;
-    for (int li = threadIdx.x; li < TILE * TILE * TILE; li += blockDim.x) {
-        const int gx = tx * TILE + (li % TILE), gy = ty * TILE + (li / TILE) % TILE, gz = tz * TILE + li / (TILE * TILE);
-        if (gx >= a.g.nnc[0] || gy >= a.g.nnc[1] || gz >= a.g.nnc[2]) continue;
-        const size_t n = node_id(a.g, gx, gy, gz);
-        const R mass = unfx((long long)a.acc[n], S.m, (R)0);
-        R nv[3];
+    long long q[GRID_NPT][4];
+    unsigned char bfl[GRID_NPT];
+    size_t nid[GRID_NPT];
+    bool in[GRID_NPT];
 #pragma unroll
+    for (int k = 0; k < GRID_NPT; k++) {
+        const int li = threadIdx.x + k * GRID_THREADS;
+        const int gx = tx * TILE + (li % TILE), gy = ty * TILE + (li / TILE) % TILE, gz = tz * TILE + li / (TILE * TILE);
+        in[k] = gx < a.g.nnc[0] && gy < a.g.nnc[1] && gz < a.g.nnc[2];
+        nid[k] = in[k] ? node_id(a.g, gx, gy, gz) : 0;
+        if (in[k]) {
+            q[k][0] = (long long)a.acc[nid[k]];
+#pragma unroll
+            for (int c = 0; c < 3; c++) q[k][1 + c] = (long long)a.acc2[c * N + nid[k]];
+            bfl[k] = a.bcflag[nid[k]];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < GRID_NPT; k++) {
+        if (!in[k]) continue;
+        const size_t n = nid[k];
+        const R mass = unfx(q[k][0], S.m, (R)0);
+        R nv[3];
         const R im = (mass > a.mtol) ? recip<R>(mass) : (R)0;
+#pragma unroll
         for (int c = 0; c < 3; c++) {
-            const R pc = unfx((long long)a.acc2[c * N + n], S.q, (R)0);
+            const R pc = unfx(q[k][1 + c], S.q, (R)0);
             nv[c] = pc * im;
         }
-        const unsigned char bf = a.bcflag[n];
+        const unsigned char bf = bfl[k];
         if (bf) {
 #pragma unroll
             for (int c = 0; c < 3; c++)
@@ -3259,21 +3326,23 @@ template <typename R>
 static mpm_status grid_kernel(mpm_ctx *c, int which) {
     StepArgs<R> a = make_args<R>(c);
     const bool list = !a.all_tiles;
-    const int lgrid = std::min(c->g.ntiles, 6 * num_sms());   // 40 registers: 6 CTAs of 256 reside per SM
+    // persistent grids of as many CTAs as reside per SM: 4 for the first pass
+    // (64 registers with its batched loads), 6 for the second (40)
+    const int lgrid1 = std::min(c->g.ntiles, 4 * num_sms()), lgrid = std::min(c->g.ntiles, 6 * num_sms());
     if (which == 0) {
         timer_begin(c, K_GRID1);
         if (list) {
             k_tile_list<<<1, 1024, 0, c->stream>>>(c->d_tileflag, c->g.ntiles, c->d_tlist, c->d_ntlist);
-            k_grid1<R, true><<<lgrid, 256, 0, c->stream>>>(a);
+            k_grid1<R, true><<<lgrid1, GRID_THREADS, 0, c->stream>>>(a);
             c->launches++;
         } else {
-            k_grid1<R, false><<<c->g.ntiles, 256, 0, c->stream>>>(a);
+            k_grid1<R, false><<<c->g.ntiles, GRID_THREADS, 0, c->stream>>>(a);
         }
         timer_end(c, K_GRID1);
     } else {
         timer_begin(c, K_GRID2);
-        if (list) k_grid2<R, true><<<lgrid, 256, 0, c->stream>>>(a);
-        else k_grid2<R, false><<<c->g.ntiles, 256, 0, c->stream>>>(a);
+        if (list) k_grid2<R, true><<<lgrid, GRID_THREADS, 0, c->stream>>>(a);
+        else k_grid2<R, false><<<c->g.ntiles, GRID_THREADS, 0, c->stream>>>(a);
         timer_end(c, K_GRID2);
     }
     c->launches++;
