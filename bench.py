@@ -17,6 +17,9 @@ dt = 2e-6 s.  Seeded synthetic data; the reference publishes no dataset.
              and the state is downloaded (mpm_gpu_download_particles).
 * roofline   the whole explicit step against the measured HBM copy
              bandwidth, with the algorithmic bytes N_p*176 + N_n*56 per step.
+* accuracy   the FP32 path's x, v and sigma after the workload's 1000 steps
+             against the reference's own FP64 run of the same seeded
+             workload (a committed 32,768-particle subsample), relative L2.
 * cpu_baseline / --impl reference: the CPU restatement of the reference's
              algorithm (oracle/mpm_oracle.c, pinned bit-exact to the
              reference's own compiled code) on a bounded sample.
@@ -53,6 +56,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
+                    help="skip the 1000-step FP32 run checked against the reference's full-size fixture")
     ap.add_argument("--batched-steps", type=int, default=100,
                     help="steps of the 256-scene batched workload (0 skips)")
     ap.add_argument("--fluid-steps", type=int, default=100,
@@ -492,6 +497,28 @@ def run_fbar(args, torch, stream, hbm_peak):
                          "note": "N_p*(176 + 40) + N_n*56: the solid formula plus def_grad_bar and J-bar"}}
 
 
+def fullsize_accuracy(capi, stream, path):
+    """Relative L2 errors of x, v and sigma of the FP32 path after the
+    workload's full step count, on the fixture's particle subsample, against
+    the reference's FP64 run."""
+    g = np.load(path)
+    s = workload(80)
+    ids = g["ids"]
+    if s.num != int(g["num"]) or not np.array_equal(s.coord[ids], g["x0"]):
+        return {"error": "the fixture was made from a different scene"}
+    gpu = capi.GpuSolid(s, precision=32, stream=stream.cuda_stream)
+    nsteps = int(g["nsteps"])
+    gpu.steps(nsteps)
+    p = gpu.particles()
+    gpu.sync()
+    gpu.close()
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    out = {"vs": "the reference's FP64 run of the same workload (tests/golden/fullsize_spinning_block.npz)",
+           "metric": "relative L2 over the subsample", "steps": nsteps, "sample": int(ids.size)}
+    out.update({k: rel(p[k][ids], g[k]) for k in ("x", "v", "sigma")})
+    return out
+
+
 def run_gb300(args):
     import torch
 
@@ -582,6 +609,17 @@ def run_gb300(args):
                    "arrays in pinned memory, the copies pipelined piece by piece on two copy streams"}
     gpu.sync()
 
+    # accuracy of the FP32 path after the workload's 1000 steps against the
+    # reference's own FP64 run of the same seeded workload, stored as a fixture
+    # (a subsample of the particles; tests/golden/make_fullsize.py)
+    accuracy = None
+    fx_path = os.path.join(ROOT, "tests", "golden", "fullsize_spinning_block.npz")
+    if args.cells == 80 and rank == 0 and args.accuracy and os.path.exists(fx_path):
+        try:
+            accuracy = fullsize_accuracy(capi, stream, fx_path)
+        except Exception as exc:   # reported, never required
+            accuracy = {"error": str(exc)}
+
     implicit = None
     if args.implicit_steps > 0:
         try:
@@ -628,7 +666,7 @@ def run_gb300(args):
                            "l2": "inputs larger than L2: 393 MB particle state per step, no flush"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(),
                 "gpu_launches": int(launches), "kernels": kernels, "implicit": implicit,
-                "batched": batched, "fluid": fluid, "apic": apic, "fbar": fbar}
+                "batched": batched, "fluid": fluid, "apic": apic, "fbar": fbar, "accuracy": accuracy}
         print(json.dumps(line), flush=True)
     gpu.close()
     if world > 1:
