@@ -574,9 +574,12 @@ def run_gb300(args):
 
     alg = algorithmic_bytes(s.num, s.nodec)
     achieved = alg / (ms_step * 1e-3) / 1e9
+    # DRAM bytes per step of this workload from the full-size ncu capture
+    # summarised in profiles/ (dram__bytes_read.sum + dram__bytes_write.sum of
+    # every kernel of the step, the re-sort over its period)
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "explicit_step_traffic.json")
-    if os.path.exists(tpath):
+    tpath = os.path.join(ROOT, "profiles", "explicit_step_traffic_spinning_block_4M.json")
+    if args.cells == 80 and os.path.exists(tpath):
         with open(tpath) as f:
             traffic = json.load(f).get("dram_bytes_per_step")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
