@@ -3417,9 +3417,13 @@ __global__ void k_nodal_volume(Geom g, int npx, int npy, int npz, double *nvol) 
     nvol[n] = wsum[0] * wsum[1] * wsum[2] * volp;
 }
 
+void launch_nodal_volume(const Geom &g, const int *npxye, double *nvol, cudaStream_t st) {
+    const int nb = (g.nodec + 255) / 256;
+    k_nodal_volume<<<nb, 256, 0, st>>>(g, npxye[0], npxye[1], npxye[2], nvol);
+}
+
 mpm_status compute_nodal_volume(mpm_ctx *c) {
-    int nb = (c->g.nodec + 255) / 256;
-    k_nodal_volume<<<nb, 256, 0, c->stream>>>(c->g, c->npxye[0], c->npxye[1], c->npxye[2], c->d_nvol);
+    launch_nodal_volume(c->g, c->npxye, c->d_nvol, c->stream);
     c->launches++;
     return MPM_OK;
 }

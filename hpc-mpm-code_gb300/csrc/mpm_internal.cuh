@@ -239,6 +239,8 @@ mpm_status run_p2g(mpm_ctx *c, double facl);
 mpm_status run_grid1(mpm_ctx *c, int mode);
 mpm_status run_g2p(mpm_ctx *c);
 mpm_status compute_nodal_volume(mpm_ctx *c);
+// MakNodalVol (module/mesh.cpp:160-202) of grid g into nvol (nodec) on st
+void launch_nodal_volume(const Geom &g, const int *npxye, double *nvol, cudaStream_t st);
 // timing helpers (mpm_ctx.cu)
 void timer_begin(mpm_ctx *c, int cls);
 void timer_end(mpm_ctx *c, int cls);

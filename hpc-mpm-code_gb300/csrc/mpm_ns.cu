@@ -290,7 +290,7 @@ namespace {
 
 enum NsScal {
     NS_RTR = 0, NS_RSR, NS_RSR0, NS_BTB, NS_BETA, NS_ALPH, NS_ZETA, NS_ETA, NS_DONE, NS_ITER, NS_RES, NS_IDOF,
-    NS_NSCAL
+    NS_EU, NS_GD, NS_NSCAL
 };
 
 struct NsVec {
@@ -575,6 +575,231 @@ __global__ void k_nsv_update(int nodec, const double *x, double *ndispl, double 
     else npres[i - 3 * nodec] += x[i];
 }
 
+// ================================================================ time step
+// Particle2Node and Node2Particle of StabilizedMPM
+// (module/fluid/MPM/var_trans_fluid.cpp:17-135) around the Newton loop, one
+// thread per particle or node.  The P2G sums are int64 fixed point (scales
+// 2^e from the step's bounds: exact, order-independent sums), the shifting
+// sums reduce in block order: a step is run-to-run identical.
+enum NsBound { NB_M = 0, NB_VOL, NB_MV, NB_MA, NB_N };
+enum NsStatusBit { NS_OUTSIDE = 1, NS_NONFINITE = 2 };
+
+struct NsStepArgs {
+    KGeom<double> g;
+    int64_t n;
+    double mtol, facl, dt, gamma, nb[6];
+    int flip;
+};
+
+__device__ __forceinline__ void ns_max(unsigned *slot, double v) {
+    float f = (float)v * 1.000001f;   // bounds only: rounded up to a float
+    if (!(f >= 0.0f)) f = INFINITY;
+    atomicMax(slot, __float_as_uint(f));
+}
+
+// bounds of the P2G contributions (max m, vol, m |v|, m |a|); particles outside
+// the grid or with non-finite inputs are reported and skipped by the scatter
+__global__ void k_nsp_bounds(NsStepArgs a, const double *__restrict__ x, const double *__restrict__ vel,
+                             const double *__restrict__ acc, const double *__restrict__ mass,
+                             const double *__restrict__ vol, unsigned *bnd, int *status) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.n) return;
+    const int64_t n = a.n;
+    const double m = mass[p], V = vol[p];
+    double vm = 0.0, am = 0.0, sum = m + V;
+    bool oob = false;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        vm = fmax(vm, fabs(vel[c * n + p]));
+        am = fmax(am, fabs(acc[c * n + p]));
+        sum += x[c * n + p] + vel[c * n + p] + acc[c * n + p];
+        (void)cell_of(x[c * n + p], a.g, c, oob);
+    }
+    if (!isfinite(sum)) {
+        atomicOr(status, NS_NONFINITE);
+        return;
+    }
+    if (oob) {
+        atomicOr(status, NS_OUTSIDE);
+        return;
+    }
+    ns_max(bnd + NB_M, fabs(m));
+    ns_max(bnd + NB_VOL, fabs(V));
+    ns_max(bnd + NB_MV, fabs(m) * vm);
+    ns_max(bnd + NB_MA, fabs(m) * am);
+}
+
+__device__ __forceinline__ void ns_scales(const NsStepArgs &a, const unsigned *bnd, Fix *F) {
+    const double nump = (double)a.n;
+#pragma unroll
+    for (int k = 0; k < NB_N; k++) F[k] = make_fix(nump * (double)__uint_as_float(bnd[k]));
+}
+
+// StandardVarP2G (mass, vol), VelP2G, AccelP2G (material_point.h:223-247,
+// module/map_and_interpolate.cpp:12-49) for PIC / FLIP: 8 int64 sums per node
+__global__ void __launch_bounds__(128) k_nsp_scatter(NsStepArgs a, const double *__restrict__ x,
+                                                     const double *__restrict__ vel, const double *__restrict__ acc,
+                                                     const double *__restrict__ mass, const double *__restrict__ vol,
+                                                     const unsigned *bnd, unsigned long long *sums) {
+    __shared__ Fix F[NB_N];
+    if (threadIdx.x == 0) ns_scales(a, bnd, F);
+    __syncthreads();
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.n) return;
+    const int64_t n = a.n;
+    const size_t N = (size_t)a.g.nodec;
+    const double xp[3] = {x[p], x[n + p], x[2 * n + p]};
+    const double m = mass[p], V = vol[p];
+    const double v[3] = {vel[p], vel[n + p], vel[2 * n + p]}, ac[3] = {acc[p], acc[n + p], acc[2 * n + p]};
+    bool oob = false;
+    double sum = m + V;
+    for (int c = 0; c < 3; c++) sum += xp[c] + v[c] + ac[c];
+    const int cx = cell_of(xp[0], a.g, 0, oob), cy = cell_of(xp[1], a.g, 1, oob), cz = cell_of(xp[2], a.g, 2, oob);
+    if (oob || !isfinite(sum)) return;   // reported by k_nsp_bounds
+    double Nw[8], dN[8][3];
+    int nid[8];
+    shape8(a.g, xp, cx, cy, cz, Nw, dN, nid);
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const double nm = Nw[q] * m;
+        long long o[8];
+        o[0] = fx(nm, F[NB_M]);
+        o[1] = fx(Nw[q] * V, F[NB_VOL]);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            o[2 + c] = fx(nm * v[c], F[NB_MV]);
+            o[5 + c] = fx(nm * ac[c], F[NB_MA]);
+        }
+#pragma unroll
+        for (int f = 0; f < 8; f++)
+            if (o[f]) atomic_add_i64(sums + (size_t)f * N + nid[q], o[f]);
+    }
+}
+
+// nmass, nvof, nvel = nmome / nmass, naccel = nforce / nmass (nmass > mtol), then
+// BCSetVal (value facl) on nvel and BCSetZero on naccel for the u, v, w lists
+// (var_trans_fluid.cpp:52-78)
+__global__ void k_nsp_grid(NsStepArgs a, const unsigned long long *__restrict__ sums, const unsigned *bnd,
+                           const unsigned char *__restrict__ bcf, const double *__restrict__ bcv, double *nmass,
+                           double *nvof, double *nvel, double *naccel) {
+    __shared__ Fix F[NB_N];
+    if (threadIdx.x == 0) ns_scales(a, bnd, F);
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.g.nodec) return;
+    const size_t N = (size_t)a.g.nodec;
+    const double m = unfx((long long)sums[i], F[NB_M], 0.0);
+    nmass[i] = m;
+    nvof[i] = unfx((long long)sums[N + i], F[NB_VOL], 0.0);
+    const unsigned char f = bcf[i];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        double v = 0.0, ac = 0.0;
+        if (m > a.mtol) {
+            v = unfx((long long)sums[(2 + c) * N + i], F[NB_MV], 0.0) / m;
+            ac = unfx((long long)sums[(5 + c) * N + i], F[NB_MA], 0.0) / m;
+        }
+        if ((f >> c) & 1) {
+            v = bcv[c * N + i] * a.facl;
+            ac = 0.0;
+        }
+        nvel[c * N + i] = v;
+        naccel[c * N + i] = ac;
+    }
+}
+
+// PredictNewmarkBetaVelAndAccel + CommitNodalKinematics
+// (nonlinear_time_integration.cpp:58-77) and the shifting's nei = max(0, nvof -
+// nvol) with sum nei^2 (material_point.cpp:175-185) into scal[slot]
+__global__ void __launch_bounds__(256) k_nsn_commit(NsStepArgs a, const double *__restrict__ ndispl,
+                                                    const double *__restrict__ nvof, const double *__restrict__ nvol,
+                                                    double *nvel, double *naccel, double *nei, double *part,
+                                                    unsigned *cnt, double *scal, int slot) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double d[1] = {0.0};
+    if (i < a.g.nodec) {
+        const size_t N = (size_t)a.g.nodec;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const size_t k = c * N + i;
+            const double u = ndispl[k], v = nvel[k], w = naccel[k];
+            nvel[k] = a.nb[0] * u - a.nb[1] * v - a.nb[2] * w;
+            naccel[k] = a.nb[3] * u - a.nb[4] * v - a.nb[5] * w;
+        }
+        const double e = fmax(0.0, -nvol[i] + nvof[i]);
+        nei[i] = e;
+        d[0] = e * e;
+    }
+    double t[1];
+    if (ns_reduce<1>(d, part, cnt, t) && threadIdx.x == 0) scal[slot] = t[0];
+}
+
+// Node2Particle's gathers (var_trans_fluid.cpp:104-124): pressure, displacement,
+// acceleration and (PIC) velocity; FLIP's velocity update and the
+// displacement of CommitParticleKinematics (nonlinear_time_integration.cpp:79-96);
+// the shifting gradient geup = 2 vol sum dN nei at the step's start position
+// (material_point.cpp:187-213) and sum |geup|^2 into scal[slot]
+__global__ void __launch_bounds__(256) k_nsp_g2p(NsStepArgs a, double *x, double *vel, double *acc, double *pres,
+                                                 const double *__restrict__ vol, const double *__restrict__ nvel,
+                                                 const double *__restrict__ naccel, const double *__restrict__ ndispl,
+                                                 const double *__restrict__ npres, const double *__restrict__ nei,
+                                                 double *geup, double *part, unsigned *cnt, double *scal, int slot) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double d[1] = {0.0};
+    if (p < a.n) {
+        const int64_t n = a.n;
+        const size_t N = (size_t)a.g.nodec;
+        const double xp[3] = {x[p], x[n + p], x[2 * n + p]};
+        bool oob = false;
+        const int cx = cell_of(xp[0], a.g, 0, oob), cy = cell_of(xp[1], a.g, 1, oob),
+                  cz = cell_of(xp[2], a.g, 2, oob);
+        double Nw[8], dN[8][3];
+        int nid[8];
+        shape8(a.g, xp, cx, cy, cz, Nw, dN, nid);
+        double pr = 0.0, du[3] = {0.0, 0.0, 0.0}, an[3] = {0.0, 0.0, 0.0}, vn[3] = {0.0, 0.0, 0.0};
+        double gu[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const int k = nid[q];
+            const double w = Nw[q], e = nei[k];
+            pr += w * npres[k];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                du[c] += w * ndispl[c * N + k];
+                an[c] += w * naccel[c * N + k];
+                vn[c] += w * nvel[c * N + k];
+                gu[c] += dN[q][c] * e;
+            }
+        }
+        const double tv = 2.0 * vol[p];
+        pres[p] = pr;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const double aold = acc[c * n + p];
+            vel[c * n + p] = a.flip ? vel[c * n + p] + a.dt * ((1.0 - a.gamma) * aold + a.gamma * an[c]) : vn[c];
+            acc[c * n + p] = an[c];
+            x[c * n + p] = xp[c] + du[c];
+            const double g = gu[c] * tv;
+            geup[c * n + p] = g;
+            d[0] += g * g;
+        }
+    }
+    double t[1];
+    if (ns_reduce<1>(d, part, cnt, t) && threadIdx.x == 0) scal[slot] = t[0];
+}
+
+// x += -b0 geup, b0 = eu / gd unless gd < mtol (material_point.cpp:215-225)
+__global__ void k_nsp_shift(NsStepArgs a, const double *__restrict__ geup, const double *__restrict__ scal, int eu,
+                            int gd, double *x) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.n) return;
+    const double g = scal[gd];
+    const double b0 = g < a.mtol ? 0.0 : scal[eu] / g;
+    if (b0 == 0.0) return;
+#pragma unroll
+    for (int c = 0; c < 3; c++) x[c * a.n + p] += -b0 * geup[c * a.n + p];
+}
+
 }  // namespace
 
 struct mpm_ns {
@@ -591,6 +816,13 @@ struct mpm_ns {
     NsVec v{};
     std::vector<int> bc_nodes[4];
     std::vector<double> bc_vals[4];
+    // time step (mpm_ns_step): nodal state, P2G sums and bounds, particle scratch
+    double *nmass = nullptr, *nvof = nullptr, *nvel = nullptr, *naccel = nullptr, *ndispl = nullptr;
+    double *npres = nullptr, *nvol = nullptr, *nei = nullptr;
+    unsigned long long *sums = nullptr;
+    unsigned *bnd = nullptr;
+    double *tau1 = nullptr, *tau2 = nullptr, *geup = nullptr, *ppart = nullptr;
+    int64_t pcap = 0;
 };
 
 #define CKN(call)                                                                                                      \
@@ -604,9 +836,11 @@ struct mpm_ns {
 
 extern "C" void mpm_ns_destroy(mpm_ns *s) {
     if (!s) return;
-    void *bufs[] = {s->A,    s->b,      s->adiag, s->x,    s->bcv,  s->part, s->scal, s->bcf,
-                    s->cnt,  s->status, s->v.rr,  s->v.rs, s->v.pp, s->v.Ap, s->v.Ar, s->v.Az,
-                    s->v.Au, s->v.uu,   s->v.zz,  s->v.xs, s->v.Ax};
+    void *bufs[] = {s->A,     s->b,      s->adiag,  s->x,      s->bcv,    s->part, s->scal,  s->bcf,
+                    s->cnt,   s->status, s->v.rr,   s->v.rs,   s->v.pp,   s->v.Ap, s->v.Ar,  s->v.Az,
+                    s->v.Au,  s->v.uu,   s->v.zz,   s->v.xs,   s->v.Ax,   s->nmass, s->nvof, s->nvel,
+                    s->naccel, s->ndispl, s->npres, s->nvol,   s->nei,    s->sums, s->bnd,   s->tau1,
+                    s->tau2,  s->geup,   s->ppart};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (s->h_scal) cudaFreeHost(s->h_scal);
@@ -807,4 +1041,157 @@ extern "C" mpm_status mpm_ns_solve(mpm_ns *s, int64_t n, const double *x, const 
         stats->last_abs_residual = rabs;
     }
     return rc;
+}
+
+// =============================================================== time step
+// The nodal state, P2G sums and nodal volume of mpm_ns_step, allocated on the
+// first step; the particle scratch (tau1, tau2, geup, reduction partials)
+// grows with the particle count.
+static mpm_status ns_step_buffers(mpm_ns *s, int64_t n) {
+    const size_t N = (size_t)s->nodec;
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](void **p, size_t bytes) {
+        if (e == cudaSuccess && !*p) e = cudaMalloc(p, bytes);
+    };
+    const bool first = s->nvol == nullptr;
+    alloc((void **)&s->nmass, sizeof(double) * N);
+    alloc((void **)&s->nvof, sizeof(double) * N);
+    alloc((void **)&s->nvel, sizeof(double) * 3 * N);
+    alloc((void **)&s->naccel, sizeof(double) * 3 * N);
+    alloc((void **)&s->ndispl, sizeof(double) * 3 * N);
+    alloc((void **)&s->npres, sizeof(double) * N);
+    alloc((void **)&s->nei, sizeof(double) * N);
+    alloc((void **)&s->sums, sizeof(unsigned long long) * 8 * N);
+    alloc((void **)&s->bnd, sizeof(unsigned) * NB_N);
+    alloc((void **)&s->nvol, sizeof(double) * N);
+    if (e == cudaSuccess && first) {
+        Geom g{};
+        for (int d = 0; d < 3; d++) {
+            g.nel[d] = s->grid.xyelem[d];
+            g.nnc[d] = s->grid.xyelem[d] + 1;
+            g.order[d] = 1;
+            g.xmin[d] = s->grid.xymin[d];
+            g.dx[d] = s->grid.dxy[d];
+        }
+        g.nodec = s->nodec;
+        g.nelem = s->grid.xyelem[0] * s->grid.xyelem[1] * s->grid.xyelem[2];
+        launch_nodal_volume(g, s->grid.npxye, s->nvol, s->stream);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && n > s->pcap) {
+        for (double **p : {&s->tau1, &s->tau2, &s->geup, &s->ppart}) {
+            if (*p) cudaFree(*p);
+            *p = nullptr;
+        }
+        const int64_t cap = n + n / 4 + 256;
+        alloc((void **)&s->tau1, sizeof(double) * cap);
+        alloc((void **)&s->tau2, sizeof(double) * cap);
+        alloc((void **)&s->geup, sizeof(double) * 3 * cap);
+        alloc((void **)&s->ppart, sizeof(double) * ((cap + 255) / 256 + 1));
+        s->pcap = e == cudaSuccess ? cap : 0;
+    }
+    if (e != cudaSuccess) {
+        fprintf(stderr, "mpm_ns_step: %s\n", cudaGetErrorString(e));
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? MPM_ERR_OOM : MPM_ERR_CUDA;
+    }
+    return MPM_OK;
+}
+
+static NsStepArgs ns_step_args(const mpm_ns *s, int64_t n, int scheme, double facl) {
+    NsStepArgs a;
+    memset(&a, 0, sizeof(a));
+    a.g = s->a.g;
+    a.n = n;
+    a.mtol = s->prm.mtol;
+    a.facl = facl;
+    a.dt = s->prm.dt;
+    a.gamma = s->prm.gamma_nb;
+    for (int k = 0; k < 6; k++) a.nb[k] = s->a.nb[k];
+    a.flip = scheme == MPM_FLIP;
+    return a;
+}
+
+static mpm_status ns_step_check(mpm_ns *s, int64_t n, const double *x, const double *vel, const double *accel,
+                                const double *mass, const double *vol, int scheme, double facl) {
+    if (!s || n < 0 || n > ((int64_t)1 << 31) - 256 || !(facl == facl)) return MPM_ERR_BAD_ARG;
+    if (scheme != MPM_PIC && scheme != MPM_FLIP) return MPM_ERR_UNSUPPORTED;
+    if (n > 0 && (!x || !vel || !accel || !mass || !vol)) return MPM_ERR_BAD_ARG;
+    mpm_status rc = ns_step_buffers(s, n);
+    if (rc != MPM_OK) return rc;
+    // the step's load factor: BCSetVal, BCNRSet and the body force read it
+    s->prm.facl = facl;
+    for (int d = 0; d < 3; d++) s->a.f[d] = s->prm.gravity[d] * facl;
+    return MPM_OK;
+}
+
+// Particle2Node (var_trans_fluid.cpp:17-80) into the context's nodal state.
+// Synchronises the stream.
+static mpm_status ns_p2g(mpm_ns *s, const NsStepArgs &a, const double *x, const double *vel, const double *accel,
+                         const double *mass, const double *vol) {
+    const size_t N = (size_t)s->nodec;
+    cudaStream_t st = s->stream;
+    CKN(cudaMemsetAsync(s->sums, 0, sizeof(unsigned long long) * 8 * N, st));
+    CKN(cudaMemsetAsync(s->bnd, 0, sizeof(unsigned) * NB_N, st));
+    CKN(cudaMemsetAsync(s->status, 0, sizeof(int), st));
+    const unsigned npb = (unsigned)((a.n + 127) / 128);
+    if (a.n > 0) {
+        k_nsp_bounds<<<npb, 128, 0, st>>>(a, x, vel, accel, mass, vol, s->bnd, s->status);
+        k_nsp_scatter<<<npb, 128, 0, st>>>(a, x, vel, accel, mass, vol, s->bnd, s->sums);
+    }
+    k_nsp_grid<<<(s->nodec + 255) / 256, 256, 0, st>>>(a, s->sums, s->bnd, s->bcf, s->bcv, s->nmass, s->nvof,
+                                                       s->nvel, s->naccel);
+    CKN(cudaGetLastError());
+    int bad = 0;
+    CKN(cudaMemcpyAsync(&bad, s->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CKN(cudaStreamSynchronize(st));
+    if (bad & NS_NONFINITE) return MPM_ERR_NONFINITE;
+    if (bad & NS_OUTSIDE) return MPM_ERR_PARTICLE_OUT_OF_BOX;
+    return MPM_OK;
+}
+
+extern "C" mpm_status mpm_ns_p2g(mpm_ns *s, int64_t n, const double *x, const double *vel, const double *accel,
+                                 const double *mass, const double *vol, int scheme, double facl) {
+    mpm_status rc = ns_step_check(s, n, x, vel, accel, mass, vol, scheme, facl);
+    if (rc != MPM_OK) return rc;
+    return ns_p2g(s, ns_step_args(s, n, scheme, facl), x, vel, accel, mass, vol);
+}
+
+extern "C" mpm_status mpm_ns_step(mpm_ns *s, int64_t n, double *x, double *vel, double *accel, double *pres,
+                                  const double *mass, const double *vol, int scheme, double facl, double rtol,
+                                  int kmax, mpm_ns_stats *stats) {
+    mpm_status rc = ns_step_check(s, n, x, vel, accel, mass, vol, scheme, facl);
+    if (rc != MPM_OK) return rc;
+    if (!(rtol > 0.0) || kmax < 1 || (n > 0 && !pres)) return MPM_ERR_BAD_ARG;
+    const NsStepArgs a = ns_step_args(s, n, scheme, facl);
+    cudaStream_t st = s->stream;
+    rc = ns_p2g(s, a, x, vel, accel, mass, vol);
+    if (rc != MPM_OK) return rc;
+    // ---- SolveNS (solve_ns_mpm.cpp:28-62)
+    rc = mpm_ns_solve(s, n, x, mass, vol, s->nvel, s->naccel, s->nmass, s->ndispl, s->npres, s->tau1, s->tau2, rtol,
+                      kmax, stats);
+    if (rc != MPM_OK) return rc;
+    // ---- Node2Particle (var_trans_fluid.cpp:82-135)
+    k_nsn_commit<<<(s->nodec + 255) / 256, 256, 0, st>>>(a, s->ndispl, s->nvof, s->nvol, s->nvel, s->naccel, s->nei,
+                                                         s->part, s->cnt + 3, s->scal, NS_EU);
+    if (n > 0) {
+        const unsigned npb = (unsigned)((n + 255) / 256);
+        k_nsp_g2p<<<npb, 256, 0, st>>>(a, x, vel, accel, pres, vol, s->nvel, s->naccel, s->ndispl, s->npres, s->nei,
+                                       s->geup, s->ppart, s->cnt + 3, s->scal, NS_GD);
+        k_nsp_shift<<<npb, 256, 0, st>>>(a, s->geup, s->scal, NS_EU, NS_GD, x);
+    }
+    CKN(cudaGetLastError());
+    CKN(cudaStreamSynchronize(st));
+    return MPM_OK;
+}
+
+extern "C" mpm_status mpm_ns_get_nodal(mpm_ns *s, int field, double *host) {
+    if (!s || !host || field < 0 || field > 6) return MPM_ERR_BAD_ARG;
+    if (!s->nvol) return MPM_ERR_BAD_ARG;   // no time step yet
+    const size_t N = (size_t)s->nodec;
+    const double *src[7] = {s->nmass, s->nvof, s->nvel, s->naccel, s->ndispl, s->npres, s->nvol};
+    const size_t len[7] = {N, N, 3 * N, 3 * N, 3 * N, N, N};
+    CKN(cudaStreamSynchronize(s->stream));
+    CKN(cudaMemcpy(host, src[field], sizeof(double) * len[field], cudaMemcpyDeviceToHost));
+    return MPM_OK;
 }

@@ -80,7 +80,7 @@ EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_s
            "mpm_nn_init_params", "mpm_nn_set_linear", "mpm_nn_set_additive", "mpm_nn_set_symmetric", "mpm_nn_set_params", "mpm_nn_get_params", "mpm_nn_forward", "mpm_nn_backward",
            "mpm_nn_num_pairs", "mpm_nn_train", "mpm_gpu_implicit_set_precond", "mpm_gpu_implicit_harvest", "mpm_gpu_implicit_apply_precond",
            "mpm_gpu_set_graph", "mpm_gpu_set_tuning", "mpm_gpu_selftest_wait", "mpm_ns_create", "mpm_ns_destroy",
-           "mpm_ns_set_stream", "mpm_ns_set_bc", "mpm_ns_solve"]
+           "mpm_ns_set_stream", "mpm_ns_set_bc", "mpm_ns_solve", "mpm_ns_p2g", "mpm_ns_step", "mpm_ns_get_nodal"]
 
 
 def load(path: str | None = None):
@@ -542,12 +542,14 @@ class NsStats(C.Structure):
 
 
 class NsSolver:
-    """StabilizedMPM::SolveNS (module/fluid/MPM/solve_ns_mpm.cpp:28-62) on the GPU:
-    mpm_ns_create / mpm_ns_set_bc / mpm_ns_solve.  bcs: four (nodes, values)
-    pairs for u, v, w, p (ubc, vbc, wbc, pbc)."""
+    """The stabilized fluid MPM of module/fluid/MPM/ on the GPU: SolveNS
+    (solve_ns_mpm.cpp:28-62, mpm_ns_solve), Particle2Node (mpm_ns_p2g) and whole
+    time steps Particle2Node + SolveNS + Node2Particle (var_trans_fluid.cpp,
+    mpm_ns_step), through mpm_ns_create / mpm_ns_set_bc.  bcs: four
+    (nodes, values) pairs for u, v, w, p (ubc, vbc, wbc, pbc)."""
 
     def __init__(self, xyelem, xymin, dxy, rho, rmu, dt, beta, gamma, gravity, facl, mtol, bcs=None,
-                 stream=None):
+                 stream=None, npxye=(2, 2, 2)):
         import torch
 
         self.lib = lib = load()
@@ -564,7 +566,7 @@ class NsSolver:
             g.xymin[d] = float(xymin[d])
             g.dxy[d] = float(dxy[d])
             g.idimc[d] = 1
-            g.npxye[d] = 2
+            g.npxye[d] = int(npxye[d])
         p = NsParams(rho, rmu, dt, beta, gamma, (C.c_double * 3)(*[float(v) for v in gravity]), facl, mtol)
         h = C.c_void_p()
         _chk(lib.mpm_ns_create(C.byref(g), C.byref(p), C.byref(h)), "mpm_ns_create")
@@ -598,6 +600,52 @@ class NsSolver:
                                    t1.data_ptr(), t2.data_ptr(), float(rtol), int(kmax), C.byref(st))
         _chk(rc, "mpm_ns_solve")
         return (nd, npres, t1[:n], t2[:n]), {k: getattr(st, k) for k, _ in NsStats._fields_}
+
+    def _step_args(self, x, vel, accel, mass, vol):
+        import torch
+
+        for t in (x, vel, accel, mass, vol):
+            if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+                raise ValueError("NsSolver: particle arrays must be contiguous FP64 CUDA tensors")
+        n = int(mass.numel())
+        for t in (x, vel, accel):
+            if t.numel() != 3 * n:
+                raise ValueError("NsSolver: x, vel, accel hold three blocks of n values")
+        return n
+
+    def p2g(self, x, vel, accel, mass, vol, scheme=0, facl=1.0):
+        """StabilizedMPM::Particle2Node (mpm_ns_p2g) into the context's nodal
+        state; x, vel, accel (3, n) FP64 CUDA tensors, mass, vol (n)."""
+        lib = self.lib
+        lib.mpm_ns_p2g.argtypes = [C.c_void_p, C.c_int64] + [C.c_void_p] * 5 + [C.c_int, C.c_double]
+        n = self._step_args(x, vel, accel, mass, vol)
+        _chk(lib.mpm_ns_p2g(self.ns, n, x.data_ptr(), vel.data_ptr(), accel.data_ptr(), mass.data_ptr(),
+                            vol.data_ptr(), int(scheme), float(facl)), "mpm_ns_p2g")
+
+    def step(self, x, vel, accel, pres, mass, vol, scheme=0, facl=1.0, rtol=1.0e-10, kmax=10000):
+        """One fluid time step (mpm_ns_step: Particle2Node, SolveNS,
+        Node2Particle) updating x, vel, accel (3, n) and pres (n) in place;
+        returns the stats dict of its Newton loop."""
+        lib = self.lib
+        lib.mpm_ns_step.argtypes = [C.c_void_p, C.c_int64] + [C.c_void_p] * 6 + [C.c_int, C.c_double, C.c_double,
+                                                                                  C.c_int, C.POINTER(NsStats)]
+        n = self._step_args(x, vel, accel, mass, vol)
+        st = NsStats()
+        _chk(lib.mpm_ns_step(self.ns, n, x.data_ptr(), vel.data_ptr(), accel.data_ptr(), pres.data_ptr(),
+                             mass.data_ptr(), vol.data_ptr(), int(scheme), float(facl), float(rtol), int(kmax),
+                             C.byref(st)), "mpm_ns_step")
+        return {k: getattr(st, k) for k, _ in NsStats._fields_}
+
+    NODAL = {"nmass": (0, 1), "nvof": (1, 1), "nvel": (2, 3), "naccel": (3, 3), "ndispl": (4, 3), "npres": (5, 1),
+             "nvol": (6, 1)}
+
+    def nodal(self, name):
+        """The context's nodal field after p2g / step (mpm_ns_get_nodal) as a host array."""
+        field, comps = self.NODAL[name]
+        out = np.zeros(comps * self.nodec)
+        self.lib.mpm_ns_get_nodal.argtypes = [C.c_void_p, C.c_int, _dp]
+        _chk(self.lib.mpm_ns_get_nodal(self.ns, field, _ptr(out)), "mpm_ns_get_nodal")
+        return out
 
     def close(self):
         if getattr(self, "ns", None):

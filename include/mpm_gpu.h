@@ -429,6 +429,43 @@ mpm_status mpm_ns_solve(mpm_ns *ns, int64_t n, const double *x, const double *ma
                         const double *nvel, const double *naccel, const double *nmass, double *ndispl,
                         double *npres, double *tau1, double *tau2, double rtol, int kmax, mpm_ns_stats *stats);
 
+/* ---- stabilized incompressible fluid: whole time steps --------------------
+ * The particle side of the fluid loop of work/src_fluid/MPM/main.cpp:45-68 on
+ * caller-owned device arrays (FP64, structure of arrays): x, vel, accel as
+ * three blocks of n, pres, mass, vol (n); linear shape functions; scheme
+ * MPM_PIC or MPM_FLIP (TPIC / APIC: MPM_ERR_UNSUPPORTED).  facl is the load
+ * factor of the step (the reference's global facl: BCSetVal, BCNRSet and the
+ * body force read it) and stays the context's load factor afterwards.
+ * mpm_ns_p2g replaces StabilizedMPM::Particle2Node
+ * (module/fluid/MPM/var_trans_fluid.cpp:17-80): nmass, nvof, nvel = sum N m v /
+ * nmass, naccel = sum N m a / nmass (where nmass > mtol), BCSetVal (value
+ * facl) on nvel and BCSetZero on naccel for the u, v, w lists; the sums are
+ * int64 fixed point, so they do not depend on the particle order.  It writes
+ * the context's own nodal state (mpm_ns_get_nodal reads it).
+ * mpm_ns_step is one time step: Particle2Node as above, SolveNS as
+ * mpm_ns_solve (linear systems to ||b - A x|| <= rtol ||b||), then
+ * Node2Particle (var_trans_fluid.cpp:82-135): the Newmark predictor committed
+ * to the nodes (module/nonlinear_time_integration.cpp:58-77), the pressure,
+ * displacement, acceleration and (PIC) velocity gathers, FLIP's velocity
+ * update and the displacement of CommitParticleKinematics
+ * (nonlinear_time_integration.cpp:79-96), and DeltaCorrectionParticleShifting
+ * (module/material_point.cpp:174-228) with the nodal volume of MakNodalVol
+ * (module/mesh.cpp:160-202, the grid's npxye).  Updates x, vel, accel, pres in
+ * place.  MeshPointLinklist has no counterpart: each particle finds its cell.
+ * A particle outside the grid returns MPM_ERR_PARTICLE_OUT_OF_BOX, a
+ * non-finite input MPM_ERR_NONFINITE (both before anything is written).
+ * Synchronises the context's stream. */
+mpm_status mpm_ns_p2g(mpm_ns *ns, int64_t n, const double *x, const double *vel, const double *accel,
+                      const double *mass, const double *vol, int scheme, double facl);
+mpm_status mpm_ns_step(mpm_ns *ns, int64_t n, double *x, double *vel, double *accel, double *pres,
+                       const double *mass, const double *vol, int scheme, double facl, double rtol, int kmax,
+                       mpm_ns_stats *stats);
+/* The context's nodal state after mpm_ns_p2g / mpm_ns_step, to a host array:
+ * field 0 nmass, 1 nvof, 2 nvel, 3 naccel, 4 ndispl, 5 npres, 6 nvol
+ * (3*nodec component-major for 2-4, nodec otherwise).  After a step, nvel and
+ * naccel hold the committed Newmark values of Node2Particle. */
+mpm_status mpm_ns_get_nodal(mpm_ns *ns, int field, double *host);
+
 /* ---- allocation-free P2G -----------------------------------------------------
  * No counterpart in the reference: an extra entry point for callers that
  * cannot let a library allocate device memory (a host program that owns

@@ -218,3 +218,114 @@ def ns_solve(xyelem, xymin, dxy, rho, rmu, dt, beta, gamma, gravity, facl, mtol,
         if rref < 1e-6 or r0r < 1e-6 or rabs < 1e-8:
             break
     return ndispl, npres, it + 1, np.array(hist)
+
+
+# ---------------------------------------------------------------- time step
+def nodal_volume(xyelem, xymin, dxy, npxye):
+    """MakNodalVol (module/mesh.cpp:160-202) for linear shape functions: every
+    element's npxye Gaussian points (GaussianDistribution, mesh.cpp:12-52) add
+    N volp to their nodes; the sum factorises over the axes."""
+    xyelem = np.asarray(xyelem)
+    nnc = xyelem + 1
+    offs = {1: [0.0], 2: [-0.25, 0.25], 3: [-1.0 / 3.0, 0.0, 1.0 / 3.0], 4: [-0.375, -0.125, 0.125, 0.375],
+            5: [-0.4, -0.2, 0.0, 0.2, 0.4], 6: [-5 / 12, -3 / 12, -1 / 12, 1 / 12, 3 / 12, 5 / 12]}
+    w = []
+    for d in range(3):
+        s = np.zeros(nnc[d])
+        for e in range(xyelem[d]):
+            xe = xymin[d] + dxy[d] * (e + 0.5)
+            for o in offs.get(int(npxye[d]), [0.0] * int(npxye[d])):
+                xp = xe + o * dxy[d]
+                for k in range(2):
+                    s[e + k] += 1.0 - abs(xp - (xymin[d] + dxy[d] * (e + k))) / dxy[d]
+        w.append(s)
+    volp = float(np.prod(dxy)) / float(np.prod(npxye))
+    return (w[0][None, None, :] * w[1][None, :, None] * w[2][:, None, None]).ravel() * volp
+
+
+def _cells(x, xyelem, xymin, dxy):
+    """The element of each point (the last element holds the upper wall, as MeshPointLinklist)."""
+    c = np.floor((x - np.asarray(xymin)) / np.asarray(dxy)).astype(np.int64)
+    return np.minimum(np.maximum(c, 0), np.asarray(xyelem) - 1)
+
+
+def ns_p2g(xyelem, xymin, dxy, mtol, facl, x, mass, vol, vel, accel, bcs):
+    """StabilizedMPM::Particle2Node (module/fluid/MPM/var_trans_fluid.cpp:17-80)
+    for PIC / FLIP: nmass, nvof, nmome = sum N m v, nforce = sum N m a
+    (StandardVarP2G, VelP2G, AccelP2G), nvel = nmome / nmass and
+    naccel = nforce / nmass where nmass > mtol, then BCSetVal (value facl) on
+    nvel and BCSetZero on naccel for the u, v, w lists.  Returns nmass, nvof,
+    nvel, naccel (component-major)."""
+    nnc = np.asarray(xyelem) + 1
+    N = int(np.prod(nnc))
+    W, _, nid = _shape(x, xymin, dxy, _cells(x, xyelem, xymin, dxy), nnc)
+    nmass = np.zeros(N)
+    nvof = np.zeros(N)
+    nmome = np.zeros(3 * N)
+    nforce = np.zeros(3 * N)
+    np.add.at(nmass, nid, W * mass[:, None])
+    np.add.at(nvof, nid, W * vol[:, None])
+    for c in range(3):
+        np.add.at(nmome, c * N + nid, W * (mass * vel[:, c])[:, None])
+        np.add.at(nforce, c * N + nid, W * (mass * accel[:, c])[:, None])
+    ok = nmass > mtol
+    nvel = np.zeros(3 * N)
+    naccel = np.zeros(3 * N)
+    for c in range(3):
+        nvel[c * N:(c + 1) * N][ok] = nmome[c * N:(c + 1) * N][ok] / nmass[ok]
+        naccel[c * N:(c + 1) * N][ok] = nforce[c * N:(c + 1) * N][ok] / nmass[ok]
+    for c in range(3):
+        nodes, vals = bcs[c]
+        nodes = np.asarray(nodes, dtype=np.int64)
+        nvel[c * N + nodes] = np.asarray(vals) * facl
+        naccel[c * N + nodes] = 0.0
+    return nmass, nvof, nvel, naccel
+
+
+def ns_g2p(xyelem, xymin, dxy, dt, beta, gamma, mtol, scheme, x, vol, vel, accel, nvel, naccel, ndispl, npres, nvof,
+           nvol):
+    """StabilizedMPM::Node2Particle (var_trans_fluid.cpp:82-135) for PIC (0) and
+    FLIP (1): PredictNewmarkBetaVelAndAccel + CommitNodalKinematics
+    (module/nonlinear_time_integration.cpp:58-77), the pressure, displacement,
+    acceleration and (PIC) velocity gathers, DeltaCorrectionParticleShifting
+    (module/material_point.cpp:174-228, at the positions of the step's start)
+    and CommitParticleKinematics (nonlinear_time_integration.cpp:79-96).
+    Returns x, vel, accel (n, 3) and pres (n)."""
+    nnc = np.asarray(xyelem) + 1
+    N = int(np.prod(nnc))
+    nb = newmark(dt, beta, gamma)
+    nvel_k = nb[0] * ndispl - nb[1] * nvel - nb[2] * naccel
+    naccel_k = nb[3] * ndispl - nb[4] * nvel - nb[5] * naccel
+    W, D, nid = _shape(x, xymin, dxy, _cells(x, xyelem, xymin, dxy), nnc)
+    pres = (W * npres[nid]).sum(axis=1)
+    disp = np.stack([(W * ndispl[c * N + nid]).sum(axis=1) for c in range(3)], axis=1)
+    acc = np.stack([(W * naccel_k[c * N + nid]).sum(axis=1) for c in range(3)], axis=1)
+    if scheme == 1:
+        v = vel + dt * ((1.0 - gamma) * accel + gamma * acc)
+    else:
+        v = np.stack([(W * nvel_k[c * N + nid]).sum(axis=1) for c in range(3)], axis=1)
+    nei = np.maximum(0.0, -nvol + nvof)
+    eu = float((nei * nei).sum())
+    geup = (D * nei[nid][:, :, None]).sum(axis=1) * (2.0 * vol)[:, None]
+    gd = float((geup * geup).sum())
+    b0 = 0.0 if gd < mtol else eu / gd
+    return x + disp - b0 * geup, v, acc, pres
+
+
+def ns_step(xyelem, xymin, dxy, npxye, rho, rmu, dt, beta, gamma, gravity, facl, mtol, scheme, x, mass, vol, vel,
+            accel, bcs, nsteps=1):
+    """nsteps time steps of work/src_fluid/MPM/main.cpp:45-68 (Particle2Node,
+    SolveNS with exact linear solves, Node2Particle).  Returns the nodal
+    fields of the first Particle2Node and the particle state (x, v, a, pres)."""
+    nvol = nodal_volume(xyelem, xymin, dxy, npxye)
+    first = None
+    pres = np.zeros(len(mass))
+    for _ in range(nsteps):
+        nmass, nvof, nvel, naccel = ns_p2g(xyelem, xymin, dxy, mtol, facl, x, mass, vol, vel, accel, bcs)
+        if first is None:
+            first = dict(nmass=nmass, nvof=nvof, nvel=nvel, naccel=naccel)
+        nd, npres, _, _ = ns_solve(xyelem, xymin, dxy, rho, rmu, dt, beta, gamma, gravity, facl, mtol, x, mass, vol,
+                                   nvel, naccel, nmass, bcs)
+        x, vel, accel, pres = ns_g2p(xyelem, xymin, dxy, dt, beta, gamma, mtol, scheme, x, vol, vel, accel, nvel,
+                                     naccel, nd, npres, nvof, nvol)
+    return first, dict(x=x, v=vel, a=accel, pres=pres)

@@ -224,3 +224,36 @@ class RefFluid:
         assert it > 0
         self.rkr_hist = hist[:it]
         return nd, npr, it, kry.value
+
+    def run(self, vel, accel, scheme, facl, bcs, nsteps, rtol=1.0e-10):
+        """nsteps time steps of the fluid loop (work/src_fluid/MPM/main.cpp:45-68):
+        MeshPointLinklist, Particle2Node, SolveNS (each linear system solved to
+        ||b - A x|| <= rtol ||b||), Node2Particle, from particle velocities and
+        accelerations (n, 3); scheme 0 PIC, 1 FLIP.  Returns the nodal fields of
+        the first Particle2Node (nmass, nvof, nvel, naccel), the particle state
+        after the last step (x, v, a as (n, 3), pres), and the Newton and Krylov
+        iteration counts."""
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        lib = self.lib
+        lib.ref_ns_run.restype = C.c_int
+        lib.ref_ns_run.argtypes = [_dp, _dp, C.c_int, C.c_double, _ip] + [_ip, _dp] * 4 + [
+            C.c_double, C.c_int, _dp, _dp, _dp, _dp, _dp, C.POINTER(C.c_int)]
+        nodes = [i32(n) if len(n) else np.zeros(1, dtype=np.int32) for n, _ in bcs]
+        vals = [f64(v) if len(v) else np.zeros(1) for _, v in bcs]
+        counts = i32([len(n) for n, _ in bcs])
+        args = []
+        for k in range(4):
+            args += [nodes[k], vals[k]]
+        N = self.nodec
+        nodal = np.zeros(8 * N)
+        x = np.zeros((self.num, 3))
+        v = np.zeros((self.num, 3))
+        a = np.zeros((self.num, 3))
+        pres = np.zeros(self.num)
+        kry = C.c_int(0)
+        it = lib.ref_ns_run(f64(vel), f64(accel), int(scheme), float(facl), counts, *args, float(rtol), int(nsteps),
+                            nodal, x, v, a, pres, C.byref(kry))
+        assert it > 0
+        out = dict(nmass=nodal[:N], nvof=nodal[N:2 * N], nvel=nodal[2 * N:5 * N], naccel=nodal[5 * N:])
+        return out, dict(x=x, v=v, a=a, pres=pres), it, kry.value

@@ -767,6 +767,59 @@ int ref_ns_get_matrix(int *matrow, int *matcolid, double *amat, double *b_rhs) {
     return M.nmat;
 }
 
+}  // extern "C"
+
+namespace {
+
+void ns_set_bcs(stabilizedmpm::StabilizedMPM &w, const int *nbc_n, const int *nbc_u, const double *fbc_u,
+                const int *nbc_v, const double *fbc_v, const int *nbc_w, const double *fbc_w, const int *nbc_p,
+                const double *fbc_p) {
+    BoundaryCondition *bcs[4] = {&w.ubc, &w.vbc, &w.wbc, &w.pbc};
+    const int *nb[4] = {nbc_u, nbc_v, nbc_w, nbc_p};
+    const double *fb[4] = {fbc_u, fbc_v, fbc_w, fbc_p};
+    for (int k = 0; k < 4; k++) {
+        bcs[k]->ibc = nbc_n[k];
+        bcs[k]->nbc.assign(nb[k], nb[k] + nbc_n[k]);
+        bcs[k]->fbc.assign(fb[k], fb[k] + nbc_n[k]);
+    }
+}
+
+/* The Newton loop of SolveNS on w's nodal state (nvel, naccel, nmass and the
+ * BC lists already set); see ref_ns_solve.  Returns the Newton iterations. */
+int ns_newton(stabilizedmpm::StabilizedMPM &w, double rtol, int max_newton, int *ktot, double *rkr_hist) {
+    w.NS_.use_petsc = false;
+    std::vector<double> nvel_k(nodec * 3), naccel_k(nodec * 3);
+    constexpr int iter_max = 10000;
+    w.MakNSStabCoeff();
+    VectorAssign(nodec * 3, w.ndispl);
+    VectorAssign(nodec, w.npres);
+    VectorAssign(nodec * 4, w.NS_.x_lhs);
+    double r0r = 0.0;
+    int NR_it;
+    for (NR_it = 0; NR_it <= iter_max && NR_it < max_newton; NR_it++) {
+        w.BCNRSet();
+        w.PredictNewmarkBetaVelAndAccel(nvel_k, naccel_k);
+        w.AssembleNSSystem(nvel_k, naccel_k);
+        double bb = 0.0;
+        w.BCResidualSet(w.NS_.b_rhs);
+        for (double v : w.NS_.b_rhs) bb += v * v;
+        const double bnorm = std::sqrt(bb);
+        for (int call = 0; call < 20; call++) {
+            if (w.NS_.ComputeRefResidual() <= rtol * bnorm) break;
+            *ktot += GPBiCGSafe(w.NS_);
+        }
+        w.UpdateNRIncrement();
+        if (rkr_hist) rkr_hist[NR_it] = w.NS_.ComputeRefResidual();
+        if (w.NS_.CheckNRConvergence(NR_it, iter_max, 0, r0r)) break;
+    }
+    w.NS_.use_petsc = true;
+    return NR_it + 1;
+}
+
+}  // namespace
+
+extern "C" {
+
 /* SolveNS (solve_ns_mpm.cpp:28-62) on the given nodal state, restated as a
  * loop over the reference's own members: MakNSStabCoeff once, then per
  * Newton iteration BCNRSet, PredictNewmarkBetaVelAndAccel, AssembleNSSystem
@@ -791,44 +844,66 @@ int ref_ns_solve(const double *nvel, const double *naccel, const double *nmass, 
     w.nvel.assign(nvel, nvel + (size_t)nodec * 3);
     w.naccel.assign(naccel, naccel + (size_t)nodec * 3);
     w.nmass.assign(nmass, nmass + (size_t)nodec);
-    BoundaryCondition *bcs[4] = {&w.ubc, &w.vbc, &w.wbc, &w.pbc};
-    const int *nb[4] = {nbc_u, nbc_v, nbc_w, nbc_p};
-    const double *fb[4] = {fbc_u, fbc_v, fbc_w, fbc_p};
-    for (int k = 0; k < 4; k++) {
-        bcs[k]->ibc = nbc_n[k];
-        bcs[k]->nbc.assign(nb[k], nb[k] + nbc_n[k]);
-        bcs[k]->fbc.assign(fb[k], fb[k] + nbc_n[k]);
-    }
-    w.NS_.use_petsc = false;
-    std::vector<double> nvel_k(nodec * 3), naccel_k(nodec * 3);
-    constexpr int iter_max = 10000;
-    w.MakNSStabCoeff();
-    VectorAssign(nodec * 3, w.ndispl);
-    VectorAssign(nodec, w.npres);
-    VectorAssign(nodec * 4, w.NS_.x_lhs);
-    double r0r = 0.0;
-    int NR_it, ktot = 0;
-    for (NR_it = 0; NR_it <= iter_max && NR_it < max_newton; NR_it++) {
-        w.BCNRSet();
-        w.PredictNewmarkBetaVelAndAccel(nvel_k, naccel_k);
-        w.AssembleNSSystem(nvel_k, naccel_k);
-        double bb = 0.0;
-        w.BCResidualSet(w.NS_.b_rhs);
-        for (double v : w.NS_.b_rhs) bb += v * v;
-        const double bnorm = std::sqrt(bb);
-        for (int call = 0; call < 20; call++) {
-            if (w.NS_.ComputeRefResidual() <= rtol * bnorm) break;
-            ktot += GPBiCGSafe(w.NS_);
-        }
-        w.UpdateNRIncrement();
-        if (rkr_hist) rkr_hist[NR_it] = w.NS_.ComputeRefResidual();
-        if (w.NS_.CheckNRConvergence(NR_it, iter_max, 0, r0r)) break;
-    }
+    ns_set_bcs(w, nbc_n, nbc_u, fbc_u, nbc_v, fbc_v, nbc_w, fbc_w, nbc_p, fbc_p);
+    int ktot = 0;
+    const int it = ns_newton(w, rtol, max_newton, &ktot, rkr_hist);
     std::memcpy(ndispl, w.ndispl.data(), sizeof(double) * 3 * (size_t)nodec);
     std::memcpy(npres, w.npres.data(), sizeof(double) * (size_t)nodec);
     if (krylov_out) *krylov_out = ktot;
-    w.NS_.use_petsc = true;
-    return NR_it + 1;
+    return it;
+}
+
+/* nsteps time steps of work/src_fluid/MPM/main.cpp:45-68 on the particles
+ * given to ref_ns_init: MeshPointLinklist, the reference's own
+ * Particle2Node (module/fluid/MPM/var_trans_fluid.cpp:17-80), SolveNS as in
+ * ref_ns_solve (ns_newton) and the reference's own Node2Particle
+ * (var_trans_fluid.cpp:82-135: Newmark predictor, CommitNodalKinematics,
+ * pressure / displacement / acceleration / velocity gathers,
+ * DeltaCorrectionParticleShifting, CommitParticleKinematics).  vel and accel
+ * are num x 3; scheme 0 PIC, 1 FLIP.  nodal1 (may be NULL) receives
+ * Particle2Node's nmass, nvof, nvel (3), naccel (3) of the first step (8
+ * nodec, component-major); the particle state after the last step goes to
+ * coord_out, vel_out, accel_out (num x 3) and pres_out (num).  Returns the
+ * Newton iterations of all steps. */
+int ref_ns_run(const double *vel, const double *accel, int scheme, double facl_in, const int *nbc_n,
+               const int *nbc_u, const double *fbc_u, const int *nbc_v, const double *fbc_v, const int *nbc_w,
+               const double *fbc_w, const int *nbc_p, const double *fbc_p, double rtol, int nsteps,
+               double *nodal1, double *coord_out, double *vel_out, double *accel_out, double *pres_out,
+               int *krylov_out) {
+    if (!g_ns) return -1;
+    auto &w = *g_ns;
+    facl = facl_in;
+    w.solswitch = scheme == 1 ? MapScheme::FLIP : MapScheme::PIC;
+    for (int p = 0; p < w.num; p++)
+        for (int i = 0; i < 3; i++) {
+            w.vel[p][i] = vel[3 * p + i];
+            w.accel[p][i] = accel[3 * p + i];
+        }
+    ns_set_bcs(w, nbc_n, nbc_u, fbc_u, nbc_v, fbc_v, nbc_w, fbc_w, nbc_p, fbc_p);
+    int ntot = 0, ktot = 0;
+    for (int st = 0; st < nsteps; st++) {
+        w.MeshPointLinklist();
+        w.Particle2Node();
+        if (st == 0 && nodal1) {
+            const size_t N = (size_t)nodec;
+            std::memcpy(nodal1, w.nmass.data(), sizeof(double) * N);
+            std::memcpy(nodal1 + N, w.nvof.data(), sizeof(double) * N);
+            std::memcpy(nodal1 + 2 * N, w.nvel.data(), sizeof(double) * 3 * N);
+            std::memcpy(nodal1 + 5 * N, w.naccel.data(), sizeof(double) * 3 * N);
+        }
+        ntot += ns_newton(w, rtol, 100, &ktot, nullptr);
+        w.Node2Particle();
+    }
+    for (int p = 0; p < w.num; p++) {
+        for (int i = 0; i < 3; i++) {
+            coord_out[3 * p + i] = w.coord[p][i];
+            vel_out[3 * p + i] = w.vel[p][i];
+            accel_out[3 * p + i] = w.accel[p][i];
+        }
+        pres_out[p] = w.pres[p];
+    }
+    if (krylov_out) *krylov_out = ktot;
+    return ntot;
 }
 
 int ref_nodec(void) { return nodec; }

@@ -14,6 +14,7 @@ committed and this script is re-run only when a case is added:
     python tests/golden/make_golden.py --fluid            # only the stabilized fluid assembly
     python tests/golden/make_golden.py --implicit2        # only the quadratic / StVK / Mooney-Rivlin implicit cases
     python tests/golden/make_golden.py --fluid-newton     # only the stabilized fluid Newton loop
+    python tests/golden/make_golden.py --fluid-step       # only whole stabilized fluid time steps
 """
 from __future__ import annotations
 
@@ -297,6 +298,42 @@ def fluid_newton_case(name="ns_solve"):
     print("wrote", name, len(c["mass"]), "particles,", newton, "Newton iterations,", krylov, "Krylov iterations")
 
 
+def ns_particle_kinematics(x, dx, xyelem, amp=0.05, seed=5):
+    """Particle velocities from the smooth field of ns_box_inputs evaluated at
+    the particles, and small seeded accelerations (the FLIP update reads them)."""
+    rng = np.random.default_rng(seed)
+    X, Y, Z = (x[:, d] / (dx * xyelem[d]) for d in range(3))
+    s3 = np.sin(np.pi * X) * np.sin(np.pi * Y) * np.sin(np.pi * Z)
+    v = np.stack([amp * s3 * np.cos(np.pi * Y), -amp * s3 * np.cos(np.pi * X),
+                  0.3 * amp * np.sin(np.pi * X) * np.sin(np.pi * Y) * np.sin(2 * np.pi * Z)], axis=1)
+    a = rng.normal(0.0, 0.1, x.shape)
+    return v, a
+
+
+def fluid_step_case(name="ns_step", nsteps=3):
+    """Whole time steps of the reference's fluid loop (MeshPointLinklist,
+    Particle2Node, SolveNS with the linear systems solved to 1e-10 as in
+    --fluid-newton, Node2Particle) on the filled box of ns_box_inputs, PIC and
+    FLIP: the nodal fields of the first Particle2Node and the particle state
+    (x, v, a, pres) after one step and after nsteps."""
+    c = ns_box_inputs()
+    wall, top = c["bc_wall"], c["bc_top"]
+    bcs = [(wall, np.zeros(len(wall)))] * 3 + [(top, np.zeros(len(top)))]
+    vel, acc = ns_particle_kinematics(c["x"], c["dxy"][0], c["xyelem"])
+    out = dict(c, vel=vel, accel=acc, nsteps=np.array(nsteps))
+    for scheme, tag in ((0, "pic"), (1, "flip")):
+        for k in (1, nsteps):
+            r = ref.RefFluid(c["xyelem"], c["xymin"], c["dxy"], c["dt"], c["mtol"], c["gravity"], c["x"],
+                             c["mass"], c["vol"], c["rho"], c["rmu"], c["beta"], c["gamma"])
+            nodal, part, newton, krylov = r.run(vel, acc, scheme, c["facl"], bcs, k, rtol=1.0e-10)
+            if k == 1:
+                out.update({f"{tag}_p2g_{f}": v for f, v in nodal.items()})
+            out.update({f"{tag}_s{k}_{f}": v for f, v in part.items()})
+            out[f"{tag}_s{k}_newton"] = np.array(newton)
+            print(name, tag, k, "steps:", newton, "Newton,", krylov, "Krylov iterations")
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+
+
 def main():
     if not ref.available():
         raise SystemExit("oracle/_ref/libmpmref.so missing: run oracle/build_ref.sh <reference checkout> first")
@@ -314,6 +351,9 @@ def main():
         return
     if "--fluid-newton" in sys.argv[1:]:
         fluid_newton_case()
+        return
+    if "--fluid-step" in sys.argv[1:]:
+        fluid_step_case()
         return
     if "--implicit2" in sys.argv[1:]:
         implicit_extra_cases()
@@ -350,6 +390,7 @@ def main():
     fluid_case()
     implicit_extra_cases()
     fluid_newton_case()
+    fluid_step_case()
 
 
 if __name__ == "__main__":

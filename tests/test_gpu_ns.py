@@ -163,3 +163,94 @@ def test_gpu_ns_newton_matches_oracle_larger_box():
           f"npres {rel(npres, want_p):.2e}; {st}")
     assert st["newton_iters"] == it
     assert rel(nd, want_d) < 1e-9 and rel(npres, want_p) < 1e-9
+
+
+# ------------------------------------------------------------ whole time steps
+def _fluid_gpu(c, bcs, vel, accel, scheme, nsteps, p2g_only=False, x=None):
+    """The GPU fluid loop (mpm_ns_p2g / mpm_ns_step) on FP64 CUDA arrays;
+    returns the nodal fields of the first Particle2Node, the particle state
+    after nsteps and the last step's stats."""
+    torch = pytest.importorskip("torch")
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda:0")
+    s = capi.NsSolver(c["xyelem"], c["xymin"], c["dxy"], *(c[k] for k in KEYS), bcs=bcs)
+    X = t((c["x"] if x is None else x).T.copy())
+    V, A = t(vel.T.copy()), t(accel.T.copy())
+    P = t(np.zeros(len(c["mass"])))
+    m, vol = t(c["mass"]), t(c["vol"])
+    s.p2g(X, V, A, m, vol, scheme, c["facl"])
+    first = {k: s.nodal(k) for k in ("nmass", "nvof", "nvel", "naccel")}
+    st = None
+    if not p2g_only:
+        for _ in range(nsteps):
+            st = s.step(X, V, A, P, m, vol, scheme, c["facl"], rtol=1.0e-10)
+    s.close()
+    h = lambda a: a.cpu().numpy().T.copy()
+    return first, dict(x=h(X), v=h(V), a=h(A), pres=P.cpu().numpy()), st
+
+
+def test_gpu_ns_step_matches_reference_fixture():
+    """Whole fluid time steps on the GPU against the reference's own loop
+    (MeshPointLinklist, Particle2Node, SolveNS, Node2Particle of
+    module/fluid/MPM/; fixture tests/golden/ns_step.npz from make_golden.py
+    --fluid-step), PIC and FLIP: Particle2Node's nodal fields to 1e-12 (the
+    fixed-point sums), the particle displacement, velocity, acceleration and
+    pressure after 1 and 3 steps to 1e-9 relative L2 (both sides solve each
+    linear system to 1e-10)."""
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ns_step.npz")))
+    bcs = _box_bcs(g)
+    for scheme, tag in ((0, "pic"), (1, "flip")):
+        for k in (1, int(g["nsteps"])):
+            first, part, st = _fluid_gpu(g, bcs, g["vel"], g["accel"], scheme, k)
+            if k == 1:
+                for f, v in first.items():
+                    assert rel(v, g[f"{tag}_p2g_{f}"]) < TOL, (tag, f, rel(v, g[f"{tag}_p2g_{f}"]))
+            want = {f: g[f"{tag}_s{k}_{f}"] for f in ("x", "v", "a", "pres")}
+            errs = {"dx": rel(part["x"] - g["x"], want["x"] - g["x"])}
+            errs.update({f: rel(part[f], want[f]) for f in ("v", "a", "pres")})
+            print(f"\nfluid step vs reference, {tag}, {k} steps: " + ", ".join(f"{f} {e:.2e}" for f, e in errs.items()))
+            assert max(errs.values()) < 1e-9, (tag, k, errs)
+
+
+def test_gpu_ns_step_matches_oracle_larger_box_and_is_reproducible():
+    """A larger, ragged box (4,928 particles, faster flow) for 2 FLIP steps
+    against the numpy oracle with exact solves, and a second run of the same
+    steps bitwise identical (fixed-point P2G sums, block-ordered reductions).
+    Tolerances: 1e-8 on the displacement and velocity; 1e-7 on the
+    acceleration and pressure, which the Newmark update a = u / (beta dt^2) -
+    ... and the pressure block take from the solve with its residual error
+    (||b - A x|| <= 1e-10 ||b||) amplified (measured 1.8e-8 and 8.8e-9)."""
+    c = make_golden.ns_box_inputs(xyelem=(11, 8, 7), seed=7, amp=0.2)
+    bcs = _box_bcs(c)
+    vel, acc = make_golden.ns_particle_kinematics(c["x"], c["dxy"][0], c["xyelem"], amp=0.2, seed=9)
+    _, want = ns_oracle.ns_step(c["xyelem"], c["xymin"], c["dxy"], (2, 2, 2), *(c[k] for k in KEYS), 1, c["x"],
+                                c["mass"], c["vol"], vel, acc, bcs, nsteps=2)
+    _, got, st = _fluid_gpu(c, bcs, vel, acc, 1, 2)
+    _, again, _ = _fluid_gpu(c, bcs, vel, acc, 1, 2)
+    errs = {"dx": rel(got["x"] - c["x"], want["x"] - c["x"])}
+    errs.update({f: rel(got[f], want[f]) for f in ("v", "a", "pres")})
+    print(f"\nfluid step vs oracle ({len(c['mass'])} particles, 2 FLIP steps): "
+          + ", ".join(f"{f} {e:.2e}" for f, e in errs.items()) + f"; {st}")
+    assert errs["dx"] < 1e-8 and errs["v"] < 1e-8, errs
+    assert errs["a"] < 1e-7 and errs["pres"] < 1e-7, errs
+    for f in got:
+        assert np.array_equal(got[f], again[f]), f
+
+
+def test_gpu_ns_step_reports_particle_outside_grid():
+    """A particle beyond the grid's upper x wall: mpm_ns_step returns
+    MPM_ERR_PARTICLE_OUT_OF_BOX before writing anything (the reference stops
+    on a particle that leaves the domain, module/mpi_data.cpp:31-34)."""
+    torch = pytest.importorskip("torch")
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ns_step.npz")))
+    x = g["x"].copy()
+    x[5, 0] = g["dxy"][0] * (g["xyelem"][0] + 0.3)
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda:0")
+    s = capi.NsSolver(g["xyelem"], g["xymin"], g["dxy"], *(g[k] for k in KEYS), bcs=_box_bcs(g))
+    X, V, A = t(x.T.copy()), t(g["vel"].T.copy()), t(g["accel"].T.copy())
+    P = t(np.zeros(len(g["mass"])))
+    before = X.clone()
+    with pytest.raises(capi.MpmError) as err:
+        s.step(X, V, A, P, t(g["mass"]), t(g["vol"]), 0, 1.0)
+    assert err.value.code == 4   # MPM_ERR_PARTICLE_OUT_OF_BOX
+    assert torch.equal(X, before)
+    s.close()

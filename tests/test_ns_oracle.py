@@ -82,3 +82,33 @@ def test_ns_newton_oracle_matches_reference_fixture():
                                              g["nvel"], g["naccel"], g["nmass"], bcs)
     assert it == int(g["newton"])
     assert rel(nd, g["ndispl"]) < 1e-10 and rel(npres, g["npres"]) < 1e-10
+
+
+def ns_step_fixture():
+    g = dict(np.load(os.path.join(os.path.dirname(GOLDEN), "ns_step.npz")))
+    bcs = [(g["bc_wall"], np.zeros(len(g["bc_wall"])))] * 3 + [(g["bc_top"], np.zeros(len(g["bc_top"])))]
+    return g, bcs
+
+
+def test_ns_step_oracle_matches_reference_fixture():
+    """Whole fluid time steps (Particle2Node, SolveNS, Node2Particle of
+    module/fluid/MPM/var_trans_fluid.cpp and solve_ns_mpm.cpp) of the numpy
+    oracle against the reference's own loop (fixture tests/golden/ns_step.npz,
+    made by make_golden.py --fluid-step; linear systems solved to 1e-10 there,
+    exactly here), PIC and FLIP, after 1 and 3 steps: the first Particle2Node's
+    nodal fields to 1e-14, the particle displacement, velocity, acceleration
+    and pressure to 1e-9 relative L2 (the reference's solve tolerance)."""
+    g, bcs = ns_step_fixture()
+    for scheme, tag in ((0, "pic"), (1, "flip")):
+        for k in (1, int(g["nsteps"])):
+            first, part = ns_oracle.ns_step(g["xyelem"], g["xymin"], g["dxy"], (2, 2, 2), float(g["rho"]),
+                                            float(g["rmu"]), float(g["dt"]), float(g["beta"]), float(g["gamma"]),
+                                            g["gravity"], float(g["facl"]), float(g["mtol"]), scheme, g["x"],
+                                            g["mass"], g["vol"], g["vel"], g["accel"], bcs, nsteps=k)
+            if k == 1:
+                for f, v in first.items():
+                    assert rel(v, g[f"{tag}_p2g_{f}"]) < 1e-14, (tag, f)
+            want = {f: g[f"{tag}_s{k}_{f}"] for f in ("x", "v", "a", "pres")}
+            assert rel(part["x"] - g["x"], want["x"] - g["x"]) < 1e-9, (tag, k)
+            for f in ("v", "a", "pres"):
+                assert rel(part[f], want[f]) < 1e-9, (tag, k, f)
