@@ -448,7 +448,7 @@ def run_fluid(args, torch, stream, hbm_peak):
             "dtype": "f32",
             "roofline": {"bound": "hbm", "achieved": alg / (ms_step * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                          "frac": alg / (ms_step * 1e-3) / 1e9 / hbm_peak, "algorithmic_bytes_per_step": alg,
-                         "note": "fluid formula N_p*64 + N_n*56; the generic solid kernels also move F and stress"}}
+                         "note": "fluid formula N_p*64 + N_n*56; the fluid keeps J - 1 in place of the 9-field deformation gradient, and the stress (6 fields) that the P2G reads"}}
 
 
 def run_apic(args, torch, stream, hbm_peak):

@@ -121,6 +121,7 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     mpm_ctx *c = new (std::nothrow) mpm_ctx();
     if (!c) return MPM_ERR_OOM;
     if (const char *gn = getenv("MPM_GB300_GATHER_NORM")) c->gather_norm = atoi(gn) != 0;
+    if (const char *al = getenv("MPM_GB300_ALTERNATE")) c->alternate = atoi(al) != 0;
     if (const char *ic = getenv("MPM_GB300_IO_CHUNKS"))
         c->io_chunks = std::max(1, std::min(mpm_ctx::IO_MAX_CHUNKS, atoi(ic)));
     Geom &g = c->g;
@@ -195,6 +196,12 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     }
     cudaMemcpy(c->d_iprop, mat->iprop, sizeof(int) * c->nmat, cudaMemcpyHostToDevice);
     for (int k = 0; k < c->nmat; k++) c->sigma_in = c->sigma_in || mat->iprop[k] == 0;
+    {   // a Tait fluid needs only J of its deformation gradient (the FP32 linear explicit path)
+        bool all_tait = true;
+        for (int k = 0; k < c->nmat; k++) all_tait = all_tait && mat->iprop[k] == 4;
+        c->fluid_j = all_tait && c->precision == 32 && !cfg->implicit && !c->affine && !c->fbar &&
+                     g.order[0] == 1 && g.order[1] == 1 && g.order[2] == 1;
+    }
     cudaMemcpy(c->d_matprop, mat->mat_prop, sizeof(double) * 3 * c->nmat, cudaMemcpyHostToDevice);
     cudaMemset(c->d_acc, 0, sizeof(unsigned long long) * NACC * N);
     cudaMemset(c->d_acc2, 0, sizeof(unsigned long long) * 3 * N);
@@ -288,6 +295,12 @@ static mpm_status upload_particles(mpm_ctx *c, int64_t n, const double *coord, c
             const double eye = (k % 4) == 0 ? 1.0 : 0.0;
             const double Fk = F ? F[9 * p + k] : eye;
             f[(6 + k) * S + p] = sizeof(R) == 4 ? (R)(Fk - eye) : (R)Fk;
+        }
+        if (c->fluid_j) {   // J - 1 in field 6, the rest unused
+            double H[9];
+            for (int k = 0; k < 9; k++) H[k] = F ? F[9 * p + k] - ((k % 4) == 0 ? 1.0 : 0.0) : 0.0;
+            f[6 * S + p] = (R)det_ipm1_d(H);
+            for (int k = 1; k < 9; k++) f[(6 + k) * S + p] = (R)0;
         }
         double s[6];
         for (int k = 0; k < 6; k++) {
@@ -623,7 +636,7 @@ constexpr int ST_X = 0, ST_V = 3, ST_F = 6, ST_S = 15, ST_VOL = 21, ST_W = 22;
 
 template <typename R>
 __global__ void k_state_gather(const R *__restrict__ f, size_t N, size_t S, int nreal, double *__restrict__ st,
-                               unsigned mask) {
+                               unsigned mask, int fluidj = 0) {
     const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= N) return;
     const int *pid = (const int *)(f + nreal * S) + S;
@@ -632,9 +645,13 @@ __global__ void k_state_gather(const R *__restrict__ f, size_t N, size_t S, int 
         for (int k = 0; k < 3; k++) st[ST_X * N + 3 * p + k] = (double)f[k * S + j];
     if (mask & 2)
         for (int k = 0; k < 3; k++) st[ST_V * N + 3 * p + k] = (double)f[(3 + k) * S + j];
-    if (mask & 4)
+    if ((mask & 4) && fluidj) {   // only J is kept: F = J^(1/3) I
+        const double c3 = cbrt(1.0 + (double)f[6 * S + j]);
+        for (int k = 0; k < 9; k++) st[ST_F * N + 9 * p + k] = (k % 4) == 0 ? c3 : 0.0;
+    } else if (mask & 4) {
         for (int k = 0; k < 9; k++)
             st[ST_F * N + 9 * p + k] = (double)f[(6 + k) * S + j] + (sizeof(R) == 4 && (k % 4) == 0 ? 1.0 : 0.0);
+    }
     if (mask & 8)
         for (int k = 0; k < 6; k++) st[ST_S * N + 6 * p + k] = (double)f[(15 + k) * S + j];
     if (mask & 16) st[ST_VOL * N + p] = (double)f[23 * S + j];
@@ -643,8 +660,7 @@ __global__ void k_state_gather(const R *__restrict__ f, size_t N, size_t S, int 
 // Also raises the fixed-point bounds of the next P2G to cover the new state.
 template <typename R>
 __global__ void k_state_scatter(R *__restrict__ f, size_t N, size_t S, int nreal, const double *__restrict__ st,
-                                unsigned mask, DevCtl *ctl,
-                                int parity) {
+                                unsigned mask, DevCtl *ctl, int parity, int fluidj = 0) {
     const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= N) return;
     {
@@ -682,9 +698,14 @@ __global__ void k_state_scatter(R *__restrict__ f, size_t N, size_t S, int nreal
         for (int k = 0; k < 3; k++) f[k * S + j] = (R)st[ST_X * N + 3 * p + k];
     if (mask & 2)
         for (int k = 0; k < 3; k++) f[(3 + k) * S + j] = (R)st[ST_V * N + 3 * p + k];
-    if (mask & 4)
+    if ((mask & 4) && fluidj) {   // only J - 1 is kept
+        double H[9];
+        for (int k = 0; k < 9; k++) H[k] = st[ST_F * N + 9 * p + k] - ((k % 4) == 0 ? 1.0 : 0.0);
+        f[6 * S + j] = (R)det_ipm1_d(H);
+    } else if (mask & 4) {
         for (int k = 0; k < 9; k++)
             f[(6 + k) * S + j] = (R)(st[ST_F * N + 9 * p + k] - (sizeof(R) == 4 && (k % 4) == 0 ? 1.0 : 0.0));
+    }
     if (mask & 8)
         for (int k = 0; k < 6; k++) f[(15 + k) * S + j] = (R)st[ST_S * N + 6 * p + k];
     if (mask & 16) f[23 * S + j] = (R)st[ST_VOL * N + p];
@@ -750,7 +771,7 @@ mpm_status mpm_gpu_download_particles(mpm_ctx *c, double *coord, double *vel, do
     unsigned mask = (coord ? 1u : 0u) | (vel ? 2u : 0u) | (F ? 4u : 0u) | (stress ? 8u : 0u) | (vol ? 16u : 0u);
     const int nb = (int)((N + 255) / 256);
     if (c->precision == 64) k_state_gather<double><<<nb, 256, 0, c->stream>>>((const double *)c->pbuf[c->cur], N, c->pstride, c->nreal, c->d_stage, mask);
-    else k_state_gather<float><<<nb, 256, 0, c->stream>>>((const float *)c->pbuf[c->cur], N, c->pstride, c->nreal, c->d_stage, mask);
+    else k_state_gather<float><<<nb, 256, 0, c->stream>>>((const float *)c->pbuf[c->cur], N, c->pstride, c->nreal, c->d_stage, mask, c->fluid_j);
     c->launches++;
     if (check_launch(c) != MPM_OK) return MPM_ERR_CUDA;
     const double *st = c->d_stage;
@@ -851,7 +872,7 @@ mpm_status mpm_gpu_upload_particles(mpm_ctx *c, const double *coord, const doubl
     if (c->precision == 64)
         k_state_scatter<double><<<nb, 256, 0, c->stream>>>((double *)c->pbuf[c->cur], N, c->pstride, c->nreal, st, mask, c->d_ctl, par);
     else
-        k_state_scatter<float><<<nb, 256, 0, c->stream>>>((float *)c->pbuf[c->cur], N, c->pstride, c->nreal, st, mask, c->d_ctl, par);
+        k_state_scatter<float><<<nb, 256, 0, c->stream>>>((float *)c->pbuf[c->cur], N, c->pstride, c->nreal, st, mask, c->d_ctl, par, c->fluid_j);
     c->launches++;
     return check_launch(c);
 }
@@ -917,7 +938,7 @@ mpm_status mpm_gpu_steps_host(mpm_ctx *c, int nsteps, double facl, double *coord
                                                                 mask, c->d_ctl, par);
         else
             k_state_scatter<float><<<nb, 256, 0, c->stream>>>((float *)c->pbuf[c->cur], N, c->pstride, c->nreal, st,
-                                                               mask, c->d_ctl, par);
+                                                               mask, c->d_ctl, par, c->fluid_j);
         c->launches++;
         if ((s = check_launch(c)) != MPM_OK) return s;
         if ((s = mpm_gpu_step_explicit(c, 1, facl)) != MPM_OK) return s;
@@ -926,7 +947,7 @@ mpm_status mpm_gpu_steps_host(mpm_ctx *c, int nsteps, double facl, double *coord
                                                                c->nreal, st, mask);
         else
             k_state_gather<float><<<nb, 256, 0, c->stream>>>((const float *)c->pbuf[c->cur], N, c->pstride,
-                                                              c->nreal, st, mask);
+                                                              c->nreal, st, mask, c->fluid_j);
         c->launches++;
         if ((s = check_launch(c)) != MPM_OK) return s;
         CK(cudaEventRecord(c->io_ev[EV_GATHER], c->stream));

@@ -457,6 +457,15 @@ __device__ __forceinline__ void tait_stress(R *s, const R inc[3][3], R jm1, R rh
     s[5] = mu * (inc[0][1] + inc[1][0]) * inv_dt;
 }
 
+// det(I + H) - 1 in FP64 for a row-major H[9] (host and device)
+__host__ __device__ inline double det_ipm1_d(const double *H) {
+    const double tr = H[0] + H[4] + H[8];
+    const double m2 = H[0] * H[4] + H[0] * H[8] + H[4] * H[8] - H[1] * H[3] - H[2] * H[6] - H[5] * H[7];
+    const double d = H[0] * (H[4] * H[8] - H[5] * H[7]) + H[1] * (H[5] * H[6] - H[3] * H[8]) +
+                     H[2] * (H[3] * H[7] - H[4] * H[6]);
+    return tr + m2 + d;
+}
+
 // det(I + H) - 1 without forming I + H
 __device__ __forceinline__ float det_ipm1(const float H[3][3]) {
     const float tr = H[0][0] + H[1][1] + H[2][2];

@@ -71,6 +71,10 @@ struct StepArgs {
     int fbar;                   // F-bar projection: k_grid2 leaves the nodal volume sums to k_fbar_grid
     int sigma_in;               // some material's stress update reads the previous stress (model 0)
     int single_mat;             // one material: every particle's matid is 0
+    int fluidj;                 // Tait fluid only: F field 0 holds J - 1, fields 1-8 unused (FP32)
+    // traversal directions of the particle kernels: each starts where the
+    // previous particle pass ended, so its first bricks are still in L2
+    int rev_p2g, rev_g2p, rev_upd;
     double nump;                // particle count as a bound factor
     double mmax;                // max particle mass
     double gshape;              // bound on |dN/dx|
@@ -466,7 +470,7 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_mom(StepArgs<fl
     int misses = 0, oobs = 0;   // over all of this CTA's bricks
     const int nbl = LIST ? *a.nblist : 1;
     for (int li = LIST ? (int)blockIdx.x : 0; li < nbl; li += LIST ? (int)gridDim.x : 1) {
-        const int b = LIST ? a.blist[li] : (int)blockIdx.x;
+        const int b = LIST ? a.blist[a.rev_p2g ? nbl - 1 - li : li] : (int)blockIdx.x;
         const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
         const int *cs = a.cstart + (size_t)b * (BRC + 1);
         if (cs[0] == cs[BRC]) continue;   // empty brick (uniform across the CTA)
@@ -976,7 +980,7 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell(StepArgs<f
     load_scales_musl(a, S);
     const int nbl = LIST ? *a.nblist : 1;
     for (int li = LIST ? (int)blockIdx.x : 0; li < nbl; li += LIST ? (int)gridDim.x : 1) {
-        const int b = LIST ? a.blist[li] : (int)blockIdx.x;
+        const int b = LIST ? a.blist[a.rev_g2p ? nbl - 1 - li : li] : (int)blockIdx.x;
         const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
         const int *cs = a.cstart + (size_t)b * (BRC + 1);
         if (cs[0] == cs[BRC]) continue;   // empty brick (uniform across the CTA)
@@ -1089,7 +1093,7 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_mom(StepArgs<fl
     long long gacc = 0;   // over all of this CTA's bricks
     float vmax = 0.0f;
     for (int li = LIST ? (int)blockIdx.x : 0; li < nbl; li += LIST ? (int)gridDim.x : 1) {
-        const int b = LIST ? a.blist[li] : (int)blockIdx.x;
+        const int b = LIST ? a.blist[a.rev_g2p ? nbl - 1 - li : li] : (int)blockIdx.x;
         const int lc = threadIdx.x >> 1, h = threadIdx.x & 1;
         const int *cs = a.cstart + (size_t)b * (BRC + 1);
         if (cs[0] == cs[BRC]) continue;   // empty brick (uniform across the CTA)
@@ -2775,7 +2779,9 @@ struct BoxNodes {
 // Second G2P pass of one FP32 particle on linear shape functions
 // (var_trans_solid_explicit.cpp:150-185, 247-296): F from the MUSL nodal
 // velocities, position with shifting, volume and stress, written back.
-template <typename Nodes>
+// FLUIDJ: a Tait-fluid context, where field F[0] holds J - 1 (a separate
+// instantiation, so that the solid kernels carry no fluid branch).
+template <typename Nodes, bool FLUIDJ = false>
 __device__ __forceinline__ void update_particle(const StepArgs<float> &a, const Particles<float> &P, int p,
                                                 const float *x, const float (*H)[3], const float *s_in, float vol0,
                                                 float volc, int mid, float rb0, const Nodes &nodes, float &volmax,
@@ -2819,6 +2825,36 @@ __device__ __forceinline__ void update_particle(const StepArgs<float> &a, const 
 #pragma unroll
         for (int c = 0; c < 3; c++) xn[c] += -rb0 * (gu[c] * tv);
     }
+    float s[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) s[k] = s_in[k];
+    const int model = a.iprop[mid];
+    const float E = (float)a.matprop[3 * mid], nu = (float)a.matprop[3 * mid + 1];
+    if constexpr (FLUIDJ) {
+        // Tait fluid: only J is tracked, J_new - 1 = (1 + (J - 1)) det(I + D) - 1
+        const float dj = det_ipm1(D);
+        const float jm1 = H[0][0] + dj + H[0][0] * dj;
+        const float J = 1.0f + jm1;
+        const float volp = J * vol0;
+        tait_stress<float>(s, D, jm1, P.m[p] * rcp_approx(vol0), E, nu, (float)a.matprop[3 * mid + 2],
+                           rcp_approx(a.dt));
+        const bool fin = isfinite(xn[0]) && isfinite(xn[1]) && isfinite(xn[2]) && isfinite(J) && isfinite(s[0]) &&
+                         isfinite(s[1]) && isfinite(s[2]) && isfinite(s[3]) && isfinite(s[4]) && isfinite(s[5]);
+        bad += !fin;
+#pragma unroll
+        for (int c = 0; c < 3; c++) P.x[c][p] = xn[c];
+        P.F[0][p] = jm1;
+#pragma unroll
+        for (int k = 0; k < 6; k++) P.s[k][p] = s[k];
+        P.vol[p] = volp;
+        const float rs0 = fabsf(s[0]) + fabsf(s[5]) + fabsf(s[4]);
+        const float rs1 = fabsf(s[5]) + fabsf(s[1]) + fabsf(s[3]);
+        const float rs2 = fabsf(s[4]) + fabsf(s[3]) + fabsf(s[2]);
+        const float vf = fabsf(volp);
+        volmax = fmaxf(volmax, vf);
+        vsmax = fmaxf(vsmax, vf * fmaxf(rs0, fmaxf(rs1, rs2)));
+        return;
+    }
     // H <- H + D + D H (the FP32 path stores H = F - I)
     float Hn[3][3];
 #pragma unroll
@@ -2833,11 +2869,6 @@ __device__ __forceinline__ void update_particle(const StepArgs<float> &a, const 
     const float jm1 = det_ipm1(Hn);
     const float J = 1.0f + jm1;
     const float volp = J * vol0;
-    float s[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) s[k] = s_in[k];
-    const int model = a.iprop[mid];
-    const float E = (float)a.matprop[3 * mid], nu = (float)a.matprop[3 * mid + 1];
     if (model == 0) lin_elast_update(s, D, E, nu);
     else if (model == 1) neo_hookean_stress_h(s, Hn, jm1, E, nu);
     else if (model == 2) stvk_stress_h(s, Hn, jm1, E, nu);
@@ -2906,18 +2937,22 @@ __global__ void __launch_bounds__(256) k_g2p_update_brick(StepArgs<float> a) {
 #pragma unroll
         for (int r = 0; r < 3; r++)
 #pragma unroll
-            for (int c = 0; c < 3; c++) H[r][c] = ld(P.F[3 * r + c] + p);
+            for (int c = 0; c < 3; c++) H[r][c] = (a.fluidj && (r | c)) ? 0.0f : ld(P.F[3 * r + c] + p);
         float s6[6];
 #pragma unroll
         for (int k = 0; k < 6; k++) s6[k] = ld(P.s[k] + p);
         bool oob = false;
         const int cx = cell_of(x[0], a.g, 0, oob), cy = cell_of(x[1], a.g, 1, oob), cz = cell_of(x[2], a.g, 2, oob);
         if (nodes.inside(cx, cy, cz))
-            update_particle(a, P, p, x, H, s6, ld(P.vol0 + p), ld(P.vol + p), P.matid[p], rb0, nodes, volmax, vsmax,
-                            bad);
+            a.fluidj ? update_particle<BoxNodes, true>(a, P, p, x, H, s6, ld(P.vol0 + p), ld(P.vol + p), P.matid[p],
+                                                       rb0, nodes, volmax, vsmax, bad)
+                     : update_particle<BoxNodes>(a, P, p, x, H, s6, ld(P.vol0 + p), ld(P.vol + p), P.matid[p], rb0,
+                                                 nodes, volmax, vsmax, bad);
         else
-            update_particle(a, P, p, x, H, s6, ld(P.vol0 + p), ld(P.vol + p), P.matid[p], rb0, nodes.gl, volmax,
-                            vsmax, bad);
+            a.fluidj ? update_particle<GlobalNodes, true>(a, P, p, x, H, s6, ld(P.vol0 + p), ld(P.vol + p),
+                                                          P.matid[p], rb0, nodes.gl, volmax, vsmax, bad)
+                     : update_particle<GlobalNodes>(a, P, p, x, H, s6, ld(P.vol0 + p), ld(P.vol + p), P.matid[p],
+                                                    rb0, nodes.gl, volmax, vsmax, bad);
     }
     const float vm = block_reduce(volmax, OpMaxF(), sh_f);
     const float sm = block_reduce(vsmax, OpMaxF(), sh_f);
@@ -2935,6 +2970,7 @@ constexpr size_t USTAGE = (size_t)UNF * UCH * 4 + UCH * 4;   // bytes per stage
 constexpr unsigned UWAIT = 1u << 22;              // bounded mbarrier wait (try_wait iterations)
 
 // At most 80 registers, so that three CTAs (24 warps) are resident per SM.
+template <bool FLUIDJ>
 __global__ void __launch_bounds__(UCH, 3) k_g2p_update_tma(StepArgs<float> a, int nchunks) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) unsigned long long bar[2];
@@ -2955,9 +2991,15 @@ __global__ void __launch_bounds__(UCH, 3) k_g2p_update_tma(StepArgs<float> a, in
     // shifting is on (b0 != 0), the material ids of a one-material scene
     const float rb0 = (float)a.ctl->b0;
     const bool need_s = a.sigma_in != 0, need_vol = rb0 != 0.0f, need_mid = a.single_mat == 0;
-    auto wanted = [&](int f) { return (f < 12 || f >= 18 || need_s) && (f != 19 || need_vol); };
+    // a Tait-fluid context reads J - 1 (field 3) and none of the other eight F fields
+    constexpr bool fluidj = FLUIDJ;
+    auto wanted = [&](int f) {
+        return (f < 12 || f >= 18 || need_s) && (f != 19 || need_vol) && !(fluidj && f >= 4 && f < 12);
+    };
+    // chunk k of the walk is particle chunk nchunks - 1 - k when the walk is reversed
+    auto phys = [&](int k) { return a.rev_upd ? nchunks - 1 - k : k; };
     auto issue = [&](int chunk, int stage) {
-        const int p0 = chunk * UCH;
+        const int p0 = phys(chunk) * UCH;
         const int cnt = min(UCH, (int)a.num - p0);
         const unsigned bytes = (unsigned)((cnt + 3) & ~3) * 4u;   // whole 16-byte units (arrays are padded)
         float *dst = (float *)(smem + stage * USTAGE);
@@ -2985,19 +3027,19 @@ __global__ void __launch_bounds__(UCH, 3) k_g2p_update_tma(StepArgs<float> a, in
         const float *sf = (const float *)(smem + stage * USTAGE);
         const int *smid = (const int *)(sf + UNF * UCH);
         const int t = threadIdx.x;
-        const int p = chunk * UCH + t;
+        const int p = phys(chunk) * UCH + t;
         if (p < a.num) {
             float x[3] = {sf[0 * UCH + t], sf[1 * UCH + t], sf[2 * UCH + t]};
             float H[3][3];
 #pragma unroll
             for (int r = 0; r < 3; r++)
 #pragma unroll
-                for (int c = 0; c < 3; c++) H[r][c] = sf[(3 + 3 * r + c) * UCH + t];
+                for (int c = 0; c < 3; c++) H[r][c] = (fluidj && (r | c)) ? 0.0f : sf[(3 + 3 * r + c) * UCH + t];
             float s6[6];
 #pragma unroll
             for (int k = 0; k < 6; k++) s6[k] = need_s ? sf[(12 + k) * UCH + t] : 0.0f;
             GlobalNodes gnodes{a.nvel2, a.nei, N, a.g};
-            update_particle(a, P, p, x, H, s6, sf[18 * UCH + t], need_vol ? sf[19 * UCH + t] : 0.0f,
+            update_particle<GlobalNodes, FLUIDJ>(a, P, p, x, H, s6, sf[18 * UCH + t], need_vol ? sf[19 * UCH + t] : 0.0f,
                             need_mid ? smid[t] : 0, rb0, gnodes, volmax, vsmax, bad);
         }
         __syncthreads();   // the stage is refilled only after every thread has read it
@@ -3095,6 +3137,11 @@ static StepArgs<R> make_args(mpm_ctx *c) {
     a.gnorm = c->gather_norm;
     a.sigma_in = c->sigma_in ? 1 : 0;
     a.single_mat = c->nmat == 1 ? 1 : 0;
+    a.fluidj = c->fluid_j ? 1 : 0;
+    if (c->alternate) {
+        a.rev_p2g = a.rev_upd = a.parity;
+        a.rev_g2p = a.parity ^ 1;
+    }
     a.implicit = c->nreal == 27 ? 1 : 0;
     a.nump = (double)c->num;
     a.mmax = c->mmax;
@@ -3287,7 +3334,9 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                 const int nchunks = (int)((c->num + UCH - 1) / UCH);
                 static bool attr = false;
                 if (!attr) {
-                    cudaFuncSetAttribute(k_g2p_update_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                    cudaFuncSetAttribute(k_g2p_update_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(2 * USTAGE));
+                    cudaFuncSetAttribute(k_g2p_update_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(2 * USTAGE));
                     attr = true;
                 }
@@ -3295,7 +3344,8 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                 cudaGetDevice(&dev);
                 cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
                 const int grid = std::min(nchunks, nsm * c->tune.update_ctas_per_sm);
-                k_g2p_update_tma<<<grid, UCH, 2 * USTAGE, c->stream>>>(a, nchunks);
+                if (c->fluid_j) k_g2p_update_tma<true><<<grid, UCH, 2 * USTAGE, c->stream>>>(a, nchunks);
+                else k_g2p_update_tma<false><<<grid, UCH, 2 * USTAGE, c->stream>>>(a, nchunks);
                 staged = true;
             }
         }

@@ -169,6 +169,8 @@ struct mpm_ctx {
                                            // 33 with the affine matrix (TPIC / APIC)
     bool affine = false;                   // TPIC or APIC: fields [24, 33) hold the affine matrix
     bool fbar = false;                     // F-bar: 11 fields from off_fbar (Fbar 9, Jbar, trial J)
+    bool fluid_j = false;                  // FP32, every material a Tait fluid: field 6 holds J - 1 and the other
+                                           // eight deformation-gradient fields are neither read nor written
     int off_fbar = 0;
     size_t pstride = 64;                   // elements between particle field arrays: num rounded up to 64
     void *pbuf[2] = {nullptr, nullptr};   // two SoA copies
@@ -209,6 +211,7 @@ struct mpm_ctx {
     bool write_nodal_dl = false;
     int cell_scatter = 1;   // FP32 linear: per-cell register scatter (else staging-box atomics)
     int tma_update = 1;     // FP32 linear: particle update with bulk-copy staged input
+    int alternate = 1;      // particle kernels walk bricks / chunks in alternating directions (MPM_GB300_ALTERNATE=0: forward)
     mpm_status latched = MPM_OK;
     mpm::KernelTimer timer;
     mpm::Tune tune;

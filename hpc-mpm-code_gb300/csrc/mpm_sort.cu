@@ -14,7 +14,7 @@
 //   k_scatter     particles grouped by brick (order within a brick arbitrary)
 //   k_cell_sort   per brick: cell histogram and starts, then each particle's
 //                 rank inside its cell by load index
-//   k_permute     all particle fields moved into the sorted order
+//   k_permute     the particle fields moved into the sorted order
 #include "mpm_device.cuh"
 
 namespace mpm {
@@ -167,19 +167,22 @@ __global__ void __launch_bounds__(BRC) k_cell_sort(const int *bstart, const int 
 // so that a thread keeps eight gathers in flight.
 template <typename R>
 __global__ void k_permute(const R *__restrict__ src, R *__restrict__ dst, const int *__restrict__ perm, int n,
-                          int nreal, size_t N) {
+                          int nreal, size_t N, int skip_lo, int skip_hi) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const size_t i = (size_t)perm[j];
-    int f = 0;
-    for (; f + 8 <= nreal; f += 8) {
+    // fields [skip_lo, skip_hi) are not moved (no kernel of the context reads them)
+    const int nmove = nreal - (skip_hi - skip_lo);
+    auto field = [&](int k) { return k < skip_lo ? k : k + (skip_hi - skip_lo); };
+    int q = 0;
+    for (; q + 8 <= nmove; q += 8) {
         R v[8];
 #pragma unroll
-        for (int k = 0; k < 8; k++) v[k] = __ldg(src + (size_t)(f + k) * N + i);
+        for (int k = 0; k < 8; k++) v[k] = __ldg(src + (size_t)field(q + k) * N + i);
 #pragma unroll
-        for (int k = 0; k < 8; k++) dst[(size_t)(f + k) * N + j] = v[k];
+        for (int k = 0; k < 8; k++) dst[(size_t)field(q + k) * N + j] = v[k];
     }
-    for (; f < nreal; f++) dst[(size_t)f * N + j] = __ldg(src + (size_t)f * N + i);
+    for (; q < nmove; q++) dst[(size_t)field(q) * N + j] = __ldg(src + (size_t)field(q) * N + i);
     const int *si = (const int *)(src + (size_t)nreal * N);
     int *di = (int *)(dst + (size_t)nreal * N);
     const int a0 = __ldg(si + i), a1 = __ldg(si + N + i);
@@ -220,7 +223,9 @@ static mpm_status sort_impl(mpm_ctx *c) {
                                                       c->d_cstart);
     timer_end(c, K_SCATTER);
     timer_begin(c, K_PERMUTE);
-    k_permute<R><<<nb, 256, 0, c->stream>>>(src, dst, c->d_perm, n, c->nreal, N);
+    // a Tait-fluid context keeps J - 1 in the first F field and never reads the other eight
+    const int skip_lo = c->fluid_j ? 7 : 0, skip_hi = c->fluid_j ? 15 : 0;
+    k_permute<R><<<nb, 256, 0, c->stream>>>(src, dst, c->d_perm, n, c->nreal, N, skip_lo, skip_hi);
     timer_end(c, K_PERMUTE);
     c->launches += 5;
     c->cur ^= 1;

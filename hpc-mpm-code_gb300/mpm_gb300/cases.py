@@ -4,6 +4,7 @@
     python -m mpm_gb300.cases implicit [--steps 1] [--precision 32]  # Jacobi-PCG Newton steps, 1.728M-particle cantilever
     python -m mpm_gb300.cases precond  [--steps 1] [--precision 32]  # the same with the learned preconditioner
     python -m mpm_gb300.cases ns       [--reps 3]        # stabilized-fluid Newton solves (SolveNS), filled box
+    python -m mpm_gb300.cases ns_assemble [--cells 56] [--reps 3]  # stabilized-fluid systems, cells^3 block at 8 per cell
     python -m mpm_gb300.cases network  [--reps 10]       # network forward passes on the 65^3 grid
     python -m mpm_gb300.cases batched  [--steps 20]      # 256 packed scenes
     python -m mpm_gb300.cases fluid    [--steps 20]      # 12.6M-particle Tait dam break
@@ -78,6 +79,27 @@ def run(case, steps, cells, reps, precision=64):
         for _ in range(reps):
             ns.solve(*args)
         ns.close()
+    elif case == "ns_assemble":
+        import torch
+
+        ne = cells + 20
+        dx = 1.0 / ne
+        rng = np.random.default_rng(9)
+        lo = 10
+        cl = np.stack(np.meshgrid(*[np.arange(lo, lo + cells)] * 3, indexing="ij"), -1).reshape(-1, 3)
+        sub = np.array([(i, j, k) for k in range(2) for j in range(2) for i in range(2)])
+        x = ((cl[:, None, :] + (sub[None] + 0.5) / 2.0).reshape(-1, 3) +
+             rng.uniform(-0.2, 0.2, (len(cl) * 8, 3)) / 2) * dx
+        n, N = len(x), (ne + 1) ** 3
+        t = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda:0")
+        vol = np.full(n, dx ** 3 / 8)
+        args = [t(x.T.copy()), t(1000.0 * vol), t(vol), t(rng.normal(0, 0.5, 3 * N)), t(rng.normal(0, 2, 3 * N)),
+                t(rng.normal(0, 1e-3 * dx, 3 * N)), t(rng.normal(0, 50, N)), t(rng.uniform(0, 0.2, N))]
+        with torch.cuda.stream(st):
+            for _ in range(reps):
+                capi.ns_assemble((ne,) * 3, (0.0,) * 3, (dx,) * 3, 1000.0, 0.05, 1e-3, 0.25, 0.5, (0.0, 0.0, -9.8),
+                                 1.0, 1e-12, *args, stream=st.cuda_stream)
+        torch.cuda.synchronize()
     elif case == "batched":
         b = scenes.pack_scenes(scenes.batch_scenes())
         g = capi.GpuSolid(b.scene, precision=32, shifting=False, stream=st.cuda_stream)
