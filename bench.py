@@ -362,7 +362,7 @@ def run_implicit(args, torch, stream):
                "newton_iters_per_step": jac["newton_iters"] / args.implicit_steps,
                "kernel_ms_one_jacobi_step": {k: round(v[0], 4) for k, v in kt_j.items()}}
         out["learned"] = {"value": nn_ms, "unit": "ms/step",
-                          "solver": "Newton + flexible GCR(8) with the learned right preconditioner (linear BF16 "
+                          "solver": "Newton + flexible GCR(4) with the learned right preconditioner (linear BF16 "
                                     "tcgen05 conv encoder-decoder, z = r + N r) while each 8-iteration window "
                                     "halves the residual, then CG with Jacobi; true FP64 residual <= 1e-8",
                           "krylov_iters_per_step": nn["krylov_iters"] / args.implicit_steps,

@@ -122,6 +122,7 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     if (!c) return MPM_ERR_OOM;
     if (const char *gn = getenv("MPM_GB300_GATHER_NORM")) c->gather_norm = atoi(gn) != 0;
     if (const char *al = getenv("MPM_GB300_ALTERNATE")) c->alternate = atoi(al) != 0;
+    if (const char *pd = getenv("MPM_GB300_PDL")) c->pdl = atoi(pd) != 0;
     if (const char *ic = getenv("MPM_GB300_IO_CHUNKS"))
         c->io_chunks = std::max(1, std::min(mpm_ctx::IO_MAX_CHUNKS, atoi(ic)));
     Geom &g = c->g;

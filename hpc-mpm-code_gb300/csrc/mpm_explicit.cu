@@ -463,6 +463,7 @@ __device__ __forceinline__ void p2g_fetch(const Particles<float> &P, int p, P2gI
 
 template <int MINB, bool LIST, bool PF = false>
 __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_mom(StepArgs<float> a) {
+    pdl_wait();
     __shared__ float corner[NACC * 8][BRC];       // 32 KB
     __shared__ Scales S;
     __shared__ int sh_red[32];
@@ -1082,6 +1083,7 @@ __device__ __forceinline__ void musl_fetch(const Particles<float> &P, int p, boo
 
 template <int MINB, bool LIST>
 __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_mom(StepArgs<float> a) {
+    pdl_wait();
     __shared__ float corner[3 * 8][BRC];
     __shared__ Scales S;
     __shared__ long long sh_l[32];
@@ -1458,6 +1460,7 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell_staged(Ste
 // independent, so the results do not depend on the queue order).
 template <bool AFF = false>
 __global__ void __launch_bounds__(256) k_p2g_misses(StepArgs<float> a) {
+    pdl_wait();
     __shared__ Scales S;
     __shared__ int sh_red[32];
     load_scales(a, S);
@@ -1485,6 +1488,7 @@ __global__ void __launch_bounds__(256) k_p2g_misses(StepArgs<float> a) {
 }
 
 __global__ void __launch_bounds__(256) k_musl_misses(StepArgs<float> a) {
+    pdl_wait();
     __shared__ Scales S;
     __shared__ long long sh_l[32];
     __shared__ float sh_f[32];
@@ -1558,6 +1562,7 @@ __global__ void __launch_bounds__(256) k_musl_misses(StepArgs<float> a) {
 // downloads) and resets the per-step device counters.
 template <typename R>
 __global__ void k_step_reset(StepArgs<R> a) {
+    pdl_wait();
     Scales s;
     compute_scales(a, s);
     DevCtl *ctl = a.ctl;
@@ -2103,6 +2108,7 @@ static_assert(GRID_NPT * GRID_THREADS == TILE * TILE * TILE, "a grid-pass CTA co
 
 template <typename R, bool LIST>
 __global__ void __launch_bounds__(GRID_THREADS) k_grid1(StepArgs<R> a) {
+    pdl_wait();
     __shared__ double sh_d[32];
     __shared__ float sh_f[32];
     __shared__ bool s_last;
@@ -2218,6 +2224,7 @@ __global__ void __launch_bounds__(GRID_THREADS) k_grid1(StepArgs<R> a) {
 // ------------------------------------------------------------ grid pass 2
 template <typename R, bool LIST>
 __global__ void __launch_bounds__(GRID_THREADS) k_grid2(StepArgs<R> a) {
+    pdl_wait();
     __shared__ Scales S;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         // b0 of DeltaCorrectionParticleShifting (material_point.cpp:219)
@@ -2485,6 +2492,7 @@ __global__ void __launch_bounds__(256) k_fbar_grid(StepArgs<R> a) {
 
 // Compaction of the active-tile flags into a list in tile order (one CTA).
 __global__ void __launch_bounds__(1024) k_tile_list(const unsigned char *flag, int ntiles, int *list, int *nlist) {
+    pdl_wait();
     __shared__ int s_cnt[1024];
     const int T = blockDim.x;
     const int per = (ntiles + T - 1) / T;
@@ -2972,6 +2980,7 @@ constexpr unsigned UWAIT = 1u << 22;              // bounded mbarrier wait (try_
 // At most 80 registers, so that three CTAs (24 warps) are resident per SM.
 template <bool FLUIDJ>
 __global__ void __launch_bounds__(UCH, 3) k_g2p_update_tma(StepArgs<float> a, int nchunks) {
+    pdl_wait();
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) unsigned long long bar[2];
     __shared__ float sh_f[32];
@@ -3173,6 +3182,29 @@ static int num_sms() {
     return n;
 }
 
+// A launch of kernel k on st; with pdl, with programmatic stream
+// serialization, so that its CTAs are scheduled while its predecessor drains
+// (the kernel's pdl_wait orders its memory accesses after the predecessor).
+template <typename... P, typename... A>
+static void launch(bool pdl, void (*k)(P...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
+                   A... args) {
+    if (!pdl) {
+        k<<<grid, block, smem, st>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // persistent grid over the active-brick list: never more CTAs than bricks
 static int list_grid(const mpm_ctx *c, int per_sm) {
     return std::min(c->g.nbricks, per_sm * num_sms());
@@ -3185,7 +3217,7 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
     constexpr int BOX = (BRX + OX) * (BRY + OY) * (BRZ + OZ);
     if (c->num == 0) return MPM_OK;
     if (which == 0) {
-        k_step_reset<R><<<1, 1, 0, c->stream>>>(a);
+        launch(c->pdl != 0, k_step_reset<R>, 1, 1, 0, c->stream, a);
         c->launches++;
         timer_begin(c, K_P2G);
         if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
@@ -3202,7 +3234,7 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                     k_p2g_cell_mom<1, true, true><<<list_grid(c, 1), CELL_THREADS, 0, c->stream>>>(a);
                 } else if (c->tune.p2g_moments) {
                     if (c->tune.brick_list)
-                        k_p2g_cell_mom<2, true><<<list_grid(c, 2), CELL_THREADS, 0, c->stream>>>(a);
+                        launch(c->pdl != 0, k_p2g_cell_mom<2, true>, list_grid(c, 2), CELL_THREADS, 0, c->stream, a);
                     else
                         k_p2g_cell_mom<2, false><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
                 } else if (c->tune.p2g_staged) {
@@ -3218,7 +3250,7 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                 } else {
                     k_p2g_cell<2><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
                 }
-                k_p2g_misses<<<2 * num_sms(), 256, 0, c->stream>>>(a);
+                launch(c->pdl != 0, k_p2g_misses<false>, 2 * num_sms(), 256, 0, c->stream, a);
                 timer_end(c, K_P2G);
                 c->launches += 2;
                 return check_launch(c);
@@ -3249,7 +3281,7 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
         if constexpr (sizeof(R) == 4 && OX == 1 && OY == 1 && OZ == 1) {
             if (use_cell_kernels(c)) {
                 if (c->tune.musl_moments == 2) {
-                    k_g2p_musl_mom<2, true><<<list_grid(c, 2), CELL_THREADS, 0, c->stream>>>(a);
+                    launch(c->pdl != 0, k_g2p_musl_mom<2, true>, list_grid(c, 2), CELL_THREADS, 0, c->stream, a);
                 } else if (c->tune.musl_moments) {
                     k_g2p_musl_mom<3, true><<<list_grid(c, 3), CELL_THREADS, 0, c->stream>>>(a);
                 } else if (c->tune.musl_staged == 2) {
@@ -3271,7 +3303,7 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                 } else {
                     k_g2p_musl_cell<3, false><<<c->g.nbricks, CELL_THREADS, 0, c->stream>>>(a);
                 }
-                k_musl_misses<<<2 * num_sms(), 256, 0, c->stream>>>(a);
+                launch(c->pdl != 0, k_musl_misses, 2 * num_sms(), 256, 0, c->stream, a);
                 timer_end(c, K_G2P_MUSL);
                 c->launches += 2;
                 return check_launch(c);
@@ -3344,8 +3376,8 @@ static mpm_status launch_particle_kernel(mpm_ctx *c, int which) {
                 cudaGetDevice(&dev);
                 cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
                 const int grid = std::min(nchunks, nsm * c->tune.update_ctas_per_sm);
-                if (c->fluid_j) k_g2p_update_tma<true><<<grid, UCH, 2 * USTAGE, c->stream>>>(a, nchunks);
-                else k_g2p_update_tma<false><<<grid, UCH, 2 * USTAGE, c->stream>>>(a, nchunks);
+                if (c->fluid_j) launch(c->pdl != 0, k_g2p_update_tma<true>, grid, UCH, 2 * USTAGE, c->stream, a, nchunks);
+                else launch(c->pdl != 0, k_g2p_update_tma<false>, grid, UCH, 2 * USTAGE, c->stream, a, nchunks);
                 staged = true;
             }
         }
@@ -3382,8 +3414,9 @@ static mpm_status grid_kernel(mpm_ctx *c, int which) {
     if (which == 0) {
         timer_begin(c, K_GRID1);
         if (list) {
-            k_tile_list<<<1, 1024, 0, c->stream>>>(c->d_tileflag, c->g.ntiles, c->d_tlist, c->d_ntlist);
-            k_grid1<R, true><<<lgrid1, GRID_THREADS, 0, c->stream>>>(a);
+            launch(c->pdl != 0, k_tile_list, 1, 1024, 0, c->stream, (const unsigned char *)c->d_tileflag, c->g.ntiles,
+                   c->d_tlist, c->d_ntlist);
+            launch(c->pdl != 0, k_grid1<R, true>, lgrid1, GRID_THREADS, 0, c->stream, a);
             c->launches++;
         } else {
             k_grid1<R, false><<<c->g.ntiles, GRID_THREADS, 0, c->stream>>>(a);
@@ -3391,7 +3424,7 @@ static mpm_status grid_kernel(mpm_ctx *c, int which) {
         timer_end(c, K_GRID1);
     } else {
         timer_begin(c, K_GRID2);
-        if (list) k_grid2<R, true><<<lgrid, GRID_THREADS, 0, c->stream>>>(a);
+        if (list) launch(c->pdl != 0, k_grid2<R, true>, lgrid, GRID_THREADS, 0, c->stream, a);
         else k_grid2<R, false><<<c->g.ntiles, GRID_THREADS, 0, c->stream>>>(a);
         timer_end(c, K_GRID2);
     }

@@ -211,6 +211,7 @@ struct mpm_ctx {
     bool write_nodal_dl = false;
     int cell_scatter = 1;   // FP32 linear: per-cell register scatter (else staging-box atomics)
     int tma_update = 1;     // FP32 linear: particle update with bulk-copy staged input
+    int pdl = 1;            // step kernels launched with programmatic dependent launch (MPM_GB300_PDL=0: off)
     int alternate = 1;      // particle kernels walk bricks / chunks in alternating directions (MPM_GB300_ALTERNATE=0: forward)
     mpm_status latched = MPM_OK;
     mpm::KernelTimer timer;

@@ -154,23 +154,36 @@ __global__ void __launch_bounds__(128) k_ns_assemble(NsArgs a, const double *__r
         const double ai[3] = {dN[qa][0], dN[qa][1], dN[qa][2]};
         const double Ni = Nw[qa];
         const double emd = a.nb[3] * Ni * m;   // ComputeNRLumpedMat
+        // the row node's factors of the 16 entries, formed once per row node:
+        //   K_rc = nb0 vmu (a_c b_r + (a.b) d_rc) + nb0 vt2 a_r b_c,  K_r3 = -V a_r N_j,
+        //   K_3c = nb0 V N_i b_c + mt1 a_c N_j,  K_33 = V t1 (a.b)
+        double A1[3], A2[3], Pu[3], Q[3], T[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            A1[c] = a.nb[0] * vmu * ai[c];
+            A2[c] = a.nb[0] * vt2 * ai[c];
+            Pu[c] = -V * ai[c];
+            Q[c] = mt1 * ai[c];
+            T[c] = V * t1 * ai[c];
+        }
+        const double c1 = a.nb[0] * V * Ni;
 #pragma unroll 1
         for (int qb = 0; qb < 8; qb++) {
             const double bj[3] = {dN[qb][0], dN[qb][1], dN[qb][2]};
             const double Nj = Nw[qb];
             const int s = ((qb & 1) - (qa & 1) + 1) + 3 * (((qb >> 1) & 1) - ((qa >> 1) & 1) + 1) +
                           9 * ((qb >> 2) - (qa >> 2) + 1);
-            const double ab = ai[0] * bj[0] + ai[1] * bj[1] + ai[2] * bj[2];
+            const double ab1 = fma(A1[0], bj[0], fma(A1[1], bj[1], A1[2] * bj[2]));   // nb0 vmu (a.b)
             double K[16];
 #pragma unroll
             for (int r = 0; r < 3; r++) {
 #pragma unroll
-                for (int c = 0; c < 3; c++)
-                    K[4 * r + c] = a.nb[0] * (vmu * (ai[c] * bj[r] + (r == c ? ab : 0.0)) + vt2 * ai[r] * bj[c]);
-                K[4 * r + 3] = -V * ai[r] * Nj;
-                K[12 + r] = a.nb[0] * V * Ni * bj[r] + mt1 * ai[r] * Nj;
+                for (int c = 0; c < 3; c++) K[4 * r + c] = fma(A1[c], bj[r], A2[r] * bj[c]);
+                K[5 * r] += ab1;
+                K[4 * r + 3] = Pu[r] * Nj;
+                K[12 + r] = fma(c1, bj[r], Q[r] * Nj);
             }
-            K[15] = V * t1 * ab;
+            K[15] = fma(T[0], bj[0], fma(T[1], bj[1], T[2] * bj[2]));
             if (qa == qb) {
                 K[0] += emd;
                 K[5] += emd;

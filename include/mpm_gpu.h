@@ -284,7 +284,7 @@ mpm_status mpm_gpu_implicit_solve(mpm_ctx *ctx, double eps, int kmax, double *x,
  * encoder-decoder over the control-point grid (3 input and 3 output
  * channels, 16/32/64 hidden channels, BF16 weights and activations, FP32
  * accumulation on tcgen05 tensor cores) serves as the right preconditioner
- * of a flexible Krylov solver (GCR over the last 8 directions; flexible CG
+ * of a flexible Krylov solver (GCR over the last 4 directions; flexible CG
  * when MPM_GB300_FCG_ONLY is set).  Convergence is always judged on
  * the true FP64 residual, and a solve falls back to the Jacobi preconditioner
  * when the network stops reducing the residual, so the accuracy of the

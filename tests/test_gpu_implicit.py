@@ -72,8 +72,10 @@ def test_implicit_steps_match_oracle(name):
     o.implicit_steps(int(g["nsteps"]), eps=TIGHT)
     p, q = gpu.particles(), o.particles()
     gpu.sync()
-    for k in ("x", "v", "F", "sigma", "vol"):
-        assert rel_l2(p[k], q[k]) <= 1e-9, (k, rel_l2(p[k], q[k]))
+    errs = {k: rel_l2(p[k], q[k]) for k in ("x", "v", "F", "sigma", "vol")}
+    print(f"\n{name} FP64 implicit steps vs oracle: " + ", ".join(f"{k} {e:.1e}" for k, e in errs.items()))
+    for k, e in errs.items():
+        assert e <= 1e-10, (k, e)   # measured <= 4.3e-12 (both sides solve every system to ||r||^2 < 1e-24 ||r0||^2)
     # one linear solve per step at least; with NR_flag the reference's check
     # (solver.cpp:565-593) measures the residual of the solved linear system,
     # which a tight solve makes small at the first iteration
