@@ -77,6 +77,7 @@ struct ImpState {
     double *gp = nullptr, *gq = nullptr;    // flexible GCR: GM directions and their images (GM * 3 * nodec)
     double *gqq = nullptr, *gbeta = nullptr;  // |A p|^2 of each kept direction, projection coefficients
     float *gqf = nullptr;                   // FP32 copies of the kept images (GM * 3 * nodec), for the dots
+    float *gp32 = nullptr, *gq32 = nullptr;  // FP32 operator: the directions and images in FP32 (GM * 3 * nodec)
     unsigned *cnt = nullptr;                // block counters of the single-launch reductions (zero between launches)
     int fallbacks = 0;                      // solves that switched from the network to Jacobi
     int nn_applications = 0;
@@ -704,10 +705,11 @@ __global__ void k_finish(const double *part, int nblk, double *out, int slot) {
 
 // y = A x with BC rows zeroed (MatVecMult + BCResidualSet), optional dot(x, y).
 // TA: storage of A; TC: arithmetic (FP32 in the Krylov iterations of the
-// FP32 operator, FP64 for its true residual and in the FP64 mode); x and y
-// are FP64.  RX, RY, RZ: the stencil radius per axis.
-template <typename TA, typename TC, int RX, int RY, int RZ>
-__global__ void __launch_bounds__(256) k_imp_matvec(ImpArgs a, const TA *A, const double *x, double *y,
+// FP32 operator, FP64 for its true residual and in the FP64 mode); TV: the
+// vectors x and y (FP64, or FP32 for the flexible GCR directions of the FP32
+// operator).  RX, RY, RZ: the stencil radius per axis.
+template <typename TA, typename TC, int RX, int RY, int RZ, typename TV = double>
+__global__ void __launch_bounds__(256) k_imp_matvec(ImpArgs a, const TA *A, const TV *x, TV *y,
                                                     double *part, unsigned *cnt = nullptr, double *scal = nullptr,
                                                     int slot = 0) {
     using TA2 = typename std::conditional<sizeof(TA) == 8, double2, float2>::type;
@@ -753,8 +755,8 @@ __global__ void __launch_bounds__(256) k_imp_matvec(ImpArgs a, const TA *A, cons
         const unsigned char bf = a.bcflag[n];
         for (int c = 0; c < 3; c++) {
             const double v = (bf & (1 << c)) ? 0.0 : (double)acc[c];
-            y[c * N + n] = v;
-            dot += x[c * N + n] * v;
+            y[c * N + n] = (TV)v;
+            dot += (double)x[c * N + n] * v;
         }
     }
     if (part && cnt) {   // dot(x, y) reduced by the last block into scal[slot]
@@ -1210,7 +1212,8 @@ __device__ __forceinline__ int gcr_prev(int slot, int j, int w) { return (slot -
 // orthogonality of the kept images is at FP32 level.  So the dots run in
 // FP32 on FP32 copies of the kept images (the FP64 pipe is this part's
 // scarce resource), and the block partials are summed in FP64.
-__global__ void __launch_bounds__(256) k_gcr_dots(ImpArgs a, const double *Q, const float *Qf, int slot, int used,
+template <typename T>
+__global__ void __launch_bounds__(256) k_gcr_dots(ImpArgs a, const T *Q, const float *Qf, int slot, int used,
                                                   int w, double *part, unsigned *cnt, const double *qq,
                                                   double *beta) {
     __shared__ double sh[32];
@@ -1222,7 +1225,7 @@ __global__ void __launch_bounds__(256) k_gcr_dots(ImpArgs a, const double *Q, co
 #pragma unroll
     for (int j = 0; j < GM; j++) d[j] = 0.0f;
     if (n < a.nodec) {
-        const double *q = Q + (size_t)slot * st;
+        const T *q = Q + (size_t)slot * st;
         const float q0 = (float)q[n], q1 = (float)q[N + n], q2 = (float)q[2 * N + n];
 #pragma unroll
         for (int j = 0; j < GM; j++)
@@ -1256,9 +1259,12 @@ __global__ void __launch_bounds__(256) k_gcr_dots(ImpArgs a, const double *Q, co
     if (threadIdx.x == 0) *cnt = 0u;
 }
 
-// p -= sum beta_j P_j, q -= sum beta_j Q_j (FP64; an FP32 copy of q is kept
-// for the dots); then (last block) q.r and q.q
-__global__ void __launch_bounds__(256) k_gcr_axpy(ImpArgs a, double *P, double *Q, float *Qf, int slot, int used,
+// p -= sum beta_j P_j, q -= sum beta_j Q_j in the precision T of the
+// directions (FP64: an FP32 copy of q is kept for the dots; FP32: the images
+// themselves are what the dots read, Qf is null); then (last block) q.r and
+// q.q in FP64
+template <typename T>
+__global__ void __launch_bounds__(256) k_gcr_axpy(ImpArgs a, T *P, T *Q, float *Qf, int slot, int used,
                                                   int w, const double *beta, const double *r, double *part,
                                                   unsigned *cnt, double *scal) {
     __shared__ double sh[32];
@@ -1266,13 +1272,13 @@ __global__ void __launch_bounds__(256) k_gcr_axpy(ImpArgs a, double *P, double *
     const size_t N = (size_t)a.nodec, st = 3 * N;
     double v[2] = {0.0, 0.0};
     if (n < a.nodec) {
-        double *p = P + (size_t)slot * st, *q = Q + (size_t)slot * st;
-        double bj[GM];
+        T *p = P + (size_t)slot * st, *q = Q + (size_t)slot * st;
+        T bj[GM];
 #pragma unroll
-        for (int j = 0; j < GM; j++) bj[j] = j < used ? beta[j] : 0.0;
+        for (int j = 0; j < GM; j++) bj[j] = j < used ? (T)beta[j] : (T)0;
         for (int c = 0; c < 3; c++) {
             const size_t i = c * N + n;
-            double pv = p[i], qv = q[i];
+            T pv = p[i], qv = q[i];
 #pragma unroll
             for (int j = 0; j < GM; j++)
                 if (j < used) {
@@ -1282,9 +1288,9 @@ __global__ void __launch_bounds__(256) k_gcr_axpy(ImpArgs a, double *P, double *
                 }
             p[i] = pv;
             q[i] = qv;
-            Qf[(size_t)slot * st + i] = (float)qv;   // the copy k_gcr_dots reads
-            v[0] += qv * r[i];
-            v[1] += qv * qv;
+            if (Qf) Qf[(size_t)slot * st + i] = (float)qv;   // the copy k_gcr_dots reads
+            v[0] += (double)qv * r[i];
+            v[1] += (double)qv * (double)qv;
         }
     }
     if (!partials_last<2>(v, 2, part, cnt)) return;
@@ -1299,8 +1305,9 @@ __global__ void __launch_bounds__(256) k_gcr_axpy(ImpArgs a, double *P, double *
 
 // alpha = q.r / q.q; x += alpha p; r -= alpha q; keeps q.q of the slot; then
 // (last block) r.r
-__global__ void __launch_bounds__(256) k_gcr_update(ImpArgs a, double *scal, double *x, double *r, const double *P,
-                                                    const double *Q, int slot, double *qq, double *part,
+template <typename T>
+__global__ void __launch_bounds__(256) k_gcr_update(ImpArgs a, double *scal, double *x, double *r, const T *P,
+                                                    const T *Q, int slot, double *qq, double *part,
                                                     unsigned *cnt) {
     __shared__ double sh[32];
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1310,11 +1317,11 @@ __global__ void __launch_bounds__(256) k_gcr_update(ImpArgs a, double *scal, dou
     if (blockIdx.x == 0 && threadIdx.x == 0) qq[slot] = dqq;
     double v[1] = {0.0};
     if (n < a.nodec) {
-        const double *p = P + (size_t)slot * st, *q = Q + (size_t)slot * st;
+        const T *p = P + (size_t)slot * st, *q = Q + (size_t)slot * st;
         for (int c = 0; c < 3; c++) {
             const size_t i = c * N + n;
-            x[i] += alpha * p[i];
-            const double w = r[i] - alpha * q[i];
+            x[i] += alpha * (double)p[i];
+            const double w = r[i] - alpha * (double)q[i];
             r[i] = w;
             v[0] += w * w;
         }
@@ -1355,6 +1362,8 @@ void implicit_free(mpm_ctx *c) {
         if (b) cudaFree(b);
     if (s->cnt) cudaFree(s->cnt);
     if (s->gqf) cudaFree(s->gqf);
+    if (s->gp32) cudaFree(s->gp32);
+    if (s->gq32) cudaFree(s->gq32);
     if (s->h_scal) cudaFreeHost(s->h_scal);
     for (cudaGraphExec_t g : {s->g_cg, s->g_fcg_nn, s->g_fcg_jac, s->g_gcr})
         if (g) cudaGraphExecDestroy(g);
@@ -1449,6 +1458,10 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
     CKI(cudaMalloc((void **)&s->gqq, sizeof(double) * GM));
     CKI(cudaMalloc((void **)&s->gbeta, sizeof(double) * GM));
     CKI(cudaMalloc((void **)&s->gqf, sizeof(float) * GM * 3 * N));
+    if (s->prec == 32) {
+        CKI(cudaMalloc((void **)&s->gp32, sizeof(float) * GM * 3 * N));
+        CKI(cudaMalloc((void **)&s->gq32, sizeof(float) * GM * 3 * N));
+    }
     CKI(cudaMalloc((void **)&s->cnt, sizeof(unsigned) * 8));
     CKI(cudaMemset(s->cnt, 0, sizeof(unsigned) * 8));
     CKI(cudaMalloc((void **)&s->nmass, sizeof(double) * N));
@@ -1489,6 +1502,19 @@ static void launch_matvec(mpm_ctx *c, const ImpArgs &a, int nb, const double *x,
     if (s->prec == 64) go(double(), double());
     else if (hi) go(float(), double());
     else go(float(), float());
+}
+
+// y = A x with FP32 vectors and FP32 arithmetic (FP32 operator only): the
+// matvec of the flexible GCR directions.
+static void launch_matvec_f32(mpm_ctx *c, const ImpArgs &a, int nb, const float *x, float *y) {
+    const int *o = c->g.order;
+    const float *A = (const float *)c->imp->A;
+    if (o[0] == 1 && o[1] == 1 && o[2] == 1)
+        k_imp_matvec<float, float, 1, 1, 1, float><<<nb, 256, 0, c->stream>>>(a, A, x, y, nullptr);
+    else if (o[1] == 2)
+        k_imp_matvec<float, float, 2, 2, 2, float><<<nb, 256, 0, c->stream>>>(a, A, x, y, nullptr);
+    else
+        k_imp_matvec<float, float, 2, 1, 2, float><<<nb, 256, 0, c->stream>>>(a, A, x, y, nullptr);
 }
 
 // AssembleSystem: k_imp_assemble (per particle), k_imp_rhs_diag, k_imp_scale
@@ -1690,6 +1716,30 @@ static mpm_status imp_cg(mpm_ctx *c, double eps, int kmax, int *iters) {
 static mpm_status gcr_iter(mpm_ctx *c, const ImpArgs &a, int nb, int u, int sl) {
     ImpState *s = c->imp;
     const size_t st3 = 3 * (size_t)c->g.nodec;
+    if (s->gp32 && mpm_nn_fp32_output(s->net)) {
+        // FP32 operator: directions and images in FP32 (the FP32 matvec computes
+        // them in FP32 anyway; x, r and the true residual stay FP64)
+        float *p = s->gp32 + (size_t)sl * st3, *q = s->gq32 + (size_t)sl * st3;
+        timer_begin(c, K_PRECOND);
+        mpm_status st = mpm_nn_apply_precond_f32(s->net, c->stream, s->r, s->scal + S_RRC, s->adiag, a.bcflag, a.mtol,
+                                                 p);
+        timer_end(c, K_PRECOND);
+        if (st != MPM_OK) return st;
+        timer_begin(c, K_MATVEC);
+        launch_matvec_f32(c, a, nb, p, q);
+        timer_end(c, K_MATVEC);
+        timer_begin(c, K_KRYLOV);
+        if (u > 0)
+            k_gcr_dots<float><<<nb, 256, 0, c->stream>>>(a, s->gq32, s->gq32, sl, u, s->gm, s->part, s->cnt, s->gqq,
+                                                         s->gbeta);
+        k_gcr_axpy<float><<<nb, 256, 0, c->stream>>>(a, s->gp32, s->gq32, nullptr, sl, u, s->gm, s->gbeta, s->r,
+                                                     s->part, s->cnt + 1, s->scal);
+        k_gcr_update<float><<<nb, 256, 0, c->stream>>>(a, s->scal, s->xs, s->r, s->gp32, s->gq32, sl, s->gqq,
+                                                       s->part, s->cnt + 2);
+        timer_end(c, K_KRYLOV);
+        c->launches += 9 + 3 + (u > 0 ? 1 : 0);
+        return MPM_OK;
+    }
     timer_begin(c, K_PRECOND);
     mpm_status st = mpm_nn_apply_precond(s->net, c->stream, s->r, s->scal + S_RRC, s->adiag, a.bcflag, a.mtol,
                                          s->gp + (size_t)sl * st3);
@@ -1700,11 +1750,12 @@ static mpm_status gcr_iter(mpm_ctx *c, const ImpArgs &a, int nb, int u, int sl) 
     timer_end(c, K_MATVEC);
     timer_begin(c, K_KRYLOV);
     if (u > 0)
-        k_gcr_dots<<<nb, 256, 0, c->stream>>>(a, s->gq, s->gqf, sl, u, s->gm, s->part, s->cnt, s->gqq, s->gbeta);
-    k_gcr_axpy<<<nb, 256, 0, c->stream>>>(a, s->gp, s->gq, s->gqf, sl, u, s->gm, s->gbeta, s->r, s->part, s->cnt + 1,
-                                          s->scal);
-    k_gcr_update<<<nb, 256, 0, c->stream>>>(a, s->scal, s->xs, s->r, s->gp, s->gq, sl, s->gqq, s->part,
-                                            s->cnt + 2);
+        k_gcr_dots<double><<<nb, 256, 0, c->stream>>>(a, s->gq, s->gqf, sl, u, s->gm, s->part, s->cnt, s->gqq,
+                                                      s->gbeta);
+    k_gcr_axpy<double><<<nb, 256, 0, c->stream>>>(a, s->gp, s->gq, s->gqf, sl, u, s->gm, s->gbeta, s->r, s->part,
+                                                  s->cnt + 1, s->scal);
+    k_gcr_update<double><<<nb, 256, 0, c->stream>>>(a, s->scal, s->xs, s->r, s->gp, s->gq, sl, s->gqq, s->part,
+                                                    s->cnt + 2);
     timer_end(c, K_KRYLOV);
     c->launches += 9 + 3 + (u > 0 ? 1 : 0);
     return MPM_OK;

@@ -860,8 +860,9 @@ __global__ void k_output_precond(const bf16 *d0, const float *w5, const float *b
 // Linear network: the last prolongation, skip addition and output layer in
 // one pass, z = r + s * W5^T (e0 + up(c1)), without storing d0; zero on
 // inactive and boundary rows.
+template <typename TZ>
 __global__ void k_output_up(const bf16 *c1, const bf16 *e0, const float *w5, const double *rr, Lvl lf, Lvl lc,
-                            const double *adiag, const unsigned char *bcflag, double mtol, const double *r, double *z) {
+                            const double *adiag, const unsigned char *bcflag, double mtol, const double *r, TZ *z) {
     __shared__ float sw5[48];
     const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (threadIdx.x < 48) sw5[threadIdx.x] = w5[threadIdx.x];
@@ -897,7 +898,7 @@ __global__ void k_output_up(const bf16 *c1, const bf16 *e0, const float *w5, con
         for (int k = 0; k < 16; k++) o += f[k] * sw5[k * 3 + c];
         const int64_t i = c * nodec + n;
         const bool off = (bf & (1 << c)) || !(adiag[i] >= mtol);
-        z[i] = off ? 0.0 : (r ? r[i] : 0.0) + s * (double)o;
+        z[i] = (TZ)(off ? 0.0 : (r ? r[i] : 0.0) + s * (double)o);
     }
 }
 
@@ -1727,8 +1728,9 @@ mpm_status mpm_nn_apply_precond(mpm_nn *net, cudaStream_t st, const double *r, c
     k_input_r<<<blocks(nodec), 256, 0, st>>>(r, rr, net->feat, nodec, net->linear, net->x0);
     if (net->linear && !net->symmetric) {
         CKN(forward(net, st, 1, false));
-        k_output_up<<<blocks(nodec), 256, 0, st>>>(net->c1, net->e0, net->p + w5_offset(), rr, net->L[0], net->L[1],
-                                                   adiag, bcflag, mtol, net->additive ? r : nullptr, z);
+        k_output_up<double><<<blocks(nodec), 256, 0, st>>>(net->c1, net->e0, net->p + w5_offset(), rr, net->L[0],
+                                                           net->L[1], adiag, bcflag, mtol,
+                                                           net->additive ? r : nullptr, z);
         CKN(cudaGetLastError());
         return MPM_OK;
     }
@@ -1744,6 +1746,20 @@ mpm_status mpm_nn_apply_precond(mpm_nn *net, cudaStream_t st, const double *r, c
     k_output_precond<<<blocks(nodec), 256, 0, st>>>(net->d0, net->p + w5_offset(),
                                                    net->linear ? nullptr : net->p + b5_offset(), rr, nodec,
                                                    adiag, bcflag, mtol, net->additive ? r : nullptr, z);
+    CKN(cudaGetLastError());
+    return MPM_OK;
+}
+
+int mpm_nn_fp32_output(const mpm_nn *net) { return net && net->linear && !net->symmetric; }
+
+mpm_status mpm_nn_apply_precond_f32(mpm_nn *net, cudaStream_t st, const double *r, const double *rr,
+                                    const double *adiag, const unsigned char *bcflag, double mtol, float *z) {
+    if (!mpm_nn_fp32_output(net)) return MPM_ERR_UNSUPPORTED;
+    const int64_t nodec = net->L[0].v;
+    k_input_r<<<blocks(nodec), 256, 0, st>>>(r, rr, net->feat, nodec, net->linear, net->x0);
+    CKN(forward(net, st, 1, false));
+    k_output_up<float><<<blocks(nodec), 256, 0, st>>>(net->c1, net->e0, net->p + w5_offset(), rr, net->L[0],
+                                                      net->L[1], adiag, bcflag, mtol, net->additive ? r : nullptr, z);
     CKN(cudaGetLastError());
     return MPM_OK;
 }

@@ -55,6 +55,11 @@ int64_t b5_offset();
 // zeroed on inactive (adiag < mtol) and boundary-condition rows.
 mpm_status mpm_nn_apply_precond(mpm_nn *net, cudaStream_t st, const double *r, const double *rr, const double *adiag,
                                 const unsigned char *bcflag, double mtol, double *z);
+// The same with z in FP32, for the network's default mode (linear, not
+// symmetrised: true from mpm_nn_fp32_output); MPM_ERR_UNSUPPORTED otherwise.
+mpm_status mpm_nn_apply_precond_f32(mpm_nn *net, cudaStream_t st, const double *r, const double *rr,
+                                    const double *adiag, const unsigned char *bcflag, double mtol, float *z);
+int mpm_nn_fp32_output(const mpm_nn *net);
 // Feature channels of the system about to be solved (phi, FP64 component-major).
 mpm_status mpm_nn_set_feature(mpm_nn *net, cudaStream_t st, const double *phi);
 // Harvest: the features of a new system; the pairs appended next belong to it.

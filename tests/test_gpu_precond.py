@@ -93,22 +93,25 @@ def test_symmetric_preconditioner_is_symmetric():
     assert abs(lhs - rhs) <= 3e-2 * max(abs(lhs), abs(rhs)), (lhs, rhs)
 
 
-def test_committed_network_on_the_full_cantilever():
+@pytest.mark.parametrize("precision", [64, 32])
+def test_committed_network_on_the_full_cantilever(precision):
     """The committed parameters (weights/precond_cantilever64.f32, trained by
     mpm_gb300.train_precond) on the 1,728,000-particle cantilever they were
     trained for: the system after one implicit step is solved to
     ||r|| / ||r0|| <= 1e-8 on the true FP64 residual by both solvers; the
-    learned solver needs at most 36 % of Jacobi-PCG's iterations (measured 34
-    against 100 with the default GCR window of 4 directions, 32 with 8) and
-    the two solutions agree to 1e-5; a following implicit step with the
-    network falls back to Jacobi nowhere."""
+    learned solver needs at most 36 % of Jacobi-PCG's iterations (FP64
+    operator: measured 34 against 100 with the default GCR window of 4
+    directions, 32 with 8) and the two solutions agree to 1e-5; a following
+    implicit step with the network falls back to Jacobi nowhere.  With the
+    FP32 operator the learned GCR keeps its directions and their images in
+    FP32 (x, r and the true residual stay FP64)."""
     from mpm_gb300 import train_precond
 
     params = train_precond.load_weights()
     if params is None:
         pytest.skip("no committed preconditioner parameters")
     s = scenes.cantilever(iprop=1)
-    gpu = capi.GpuImplicitSolid(s, nr_flag=True)
+    gpu = capi.GpuImplicitSolid(s, nr_flag=True, precision=precision)
     gpu.implicit_steps(1, eps=EPS)
     gpu.assemble()
     xj, itj = gpu.solve(eps=EPS)
@@ -119,7 +122,8 @@ def test_committed_network_on_the_full_cantilever():
     st = gpu.implicit_steps(1, eps=EPS, full=True)   # a whole step with the network: its statistics
     gpu.set_precond(None)
     gpu.sync()
-    print(f"\nfull cantilever: Jacobi-PCG {itj} iterations, learned GCR {itn} iterations; next step {st}")
+    print(f"\nfull cantilever, FP{precision} operator: Jacobi-PCG {itj} iterations, learned GCR {itn} iterations; "
+          f"solutions {rel_l2(xn, xj):.1e} apart; next step {st}")
     assert rel_l2(xn, xj) <= 1e-5
     assert itn <= 0.36 * itj, (itn, itj)
     assert st["precond_fallbacks"] == 0 and st["nn_applications"] > 0, st
