@@ -7,7 +7,7 @@
     python -m mpm_gb300.cases ns_assemble [--cells 56] [--reps 3]  # stabilized-fluid systems, cells^3 block at 8 per cell
     python -m mpm_gb300.cases network  [--reps 10]       # network forward passes on the 65^3 grid
     python -m mpm_gb300.cases batched  [--steps 20]      # 256 packed scenes
-    python -m mpm_gb300.cases fluid    [--steps 20]      # 12.6M-particle Tait dam break
+    python -m mpm_gb300.cases fluid    [--steps 20] [--cells 128]  # Tait dam break, a cells x cells x 3/4 cells column (128: 12.6M particles)
     python -m mpm_gb300.cases apic     [--cells 64] [--steps 20]   # the explicit block with APIC transfers
     python -m mpm_gb300.cases fbar     [--cells 64] [--steps 20]   # the explicit block with the F-bar projection
 
@@ -107,7 +107,9 @@ def run(case, steps, cells, reps, precision=64):
         g.steps(steps)
         g.sync()
     elif case == "fluid":
-        g = capi.GpuSolid(scenes.dam_break(), precision=32, stream=st.cuda_stream)
+        scene = scenes.dam_break() if cells >= 128 else scenes.dam_break(
+            grid=(2 * cells, cells, cells), cells=(cells, cells, 3 * cells // 4))
+        g = capi.GpuSolid(scene, precision=32, stream=st.cuda_stream)
         g.steps(3)
         g.steps(steps)
         g.sync()
@@ -119,11 +121,13 @@ def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("case")
     ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--cells", type=int, default=64)
+    ap.add_argument("--cells", type=int, default=None,
+                    help="block edge in cells (explicit / apic / fbar: 64; fluid: 128, the full dam break)")
     ap.add_argument("--reps", type=int, default=10)
     ap.add_argument("--precision", type=int, default=64, choices=[32, 64])
     a = ap.parse_args()
-    run(a.case, a.steps, a.cells, a.reps, a.precision)
+    cells = a.cells if a.cells is not None else (128 if a.case == "fluid" else 64)
+    run(a.case, a.steps, cells, a.reps, a.precision)
 
 
 if __name__ == "__main__":
