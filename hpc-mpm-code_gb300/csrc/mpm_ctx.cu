@@ -183,6 +183,7 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     alloc((void **)&c->d_tcount, sizeof(int) * g.nbricks);
     alloc((void **)&c->d_tstart, sizeof(int) * (g.nbricks + 1));
     alloc((void **)&c->d_tcursor, sizeof(int) * g.nbricks);
+    alloc((void **)&c->d_scanpart, sizeof(int) * 3 * ((size_t)(g.nbricks + SCAN_SEG - 1) / SCAN_SEG + 1));
     alloc((void **)&c->d_cstart, sizeof(int) * (size_t)g.nbricks * (BRC + 1));
     alloc((void **)&c->d_nwork, sizeof(int));
     alloc((void **)&c->d_blist, sizeof(int) * g.nbricks);
@@ -256,6 +257,7 @@ void mpm_gpu_destroy(mpm_ctx *c) {
     free_dev(c->d_tcount);
     free_dev(c->d_tstart);
     free_dev(c->d_tcursor);
+    free_dev(c->d_scanpart);
     free_dev(c->d_cstart);
     free_dev(c->d_nwork);
     free_dev(c->d_blist);

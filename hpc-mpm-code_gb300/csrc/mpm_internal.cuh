@@ -31,6 +31,7 @@ constexpr int TILE = 8;              // node tile edge for the grid passes and a
 constexpr int BRX = 4, BRY = 4, BRZ = 8;   // particle brick: cells per brick edge
 constexpr int BRC = BRX * BRY * BRZ;       // cells per brick (one CTA thread per cell)
 constexpr int CHUNK = 1024;          // max particles per work item
+constexpr int SCAN_SEG = 4096;       // bricks per segment of the brick-count scan (mpm_sort.cu)
 constexpr int NACC = 8;              // P2G fields: mass, vof, mome xyz, force xyz
 constexpr int NKCLASS = 14;          // kernel classes for timing
 
@@ -190,6 +191,7 @@ struct mpm_ctx {
     int *d_key = nullptr, *d_perm = nullptr, *d_tcount = nullptr, *d_tstart = nullptr, *d_tcursor = nullptr;
     int *d_tmp = nullptr, *d_perm2 = nullptr;   // per-brick cell sort
     int *d_cstart = nullptr;                    // nbricks * (BRC + 1) cell start offsets
+    int *d_scanpart = nullptr;                  // per-segment sums of the brick-count scan (3 per segment + totals)
     double *d_stage = nullptr;                  // FP64 AoS staging for host <-> device particle state
     mpm::WorkItem *d_work = nullptr;
     int *d_nwork = nullptr;

@@ -10,7 +10,9 @@
 // order too), which makes the reordering deterministic.
 //
 //   k_bin         brick key + brick histogram
-//   k_scan        brick starts, work-item list (chunks of <= CHUNK particles)
+//   k_scan_up / k_scan_mid / k_scan_down
+//                 brick starts, work-item list (chunks of <= CHUNK particles),
+//                 list of non-empty bricks: a three-launch scan over segments
 //   k_scatter     particles grouped by brick (order within a brick arbitrary)
 //   k_cell_sort   per brick: cell histogram and starts, then each particle's
 //                 rank inside its cell by load index
@@ -42,62 +44,149 @@ __global__ void k_bin(KGeom<R> g, int nbx, int nby, const R *x0, const R *x1, co
     if ((threadIdx.x & 31) == 0 && bad) atomicAdd(oob_count, __popc(bad));
 }
 
-// One CTA: exclusive scan of the brick counts, the work list of <= CHUNK
-// particle chunks per brick, and the reset of the counters for the next sort.
-__global__ void __launch_bounds__(1024) k_scan(int nb, int *bcount, int *bstart, int *bcursor, WorkItem *work,
-                                               int *nwork, int cap, int *blist, int *nblist) {
-    __shared__ int s_cnt[1024];
-    __shared__ int s_chk[1024];
-    __shared__ int s_act[1024];
-    const int T = blockDim.x;
-    const int per = (nb + T - 1) / T;
-    const int lo = threadIdx.x * per, hi = min(lo + per, nb);
-    int csum = 0, ksum = 0, asum = 0;
-    for (int t = lo; t < hi; t++) {
-        int c = bcount[t];
-        csum += c;
-        ksum += (c + CHUNK - 1) / CHUNK;
-        asum += c > 0;
-    }
-    s_cnt[threadIdx.x] = csum;
-    s_chk[threadIdx.x] = ksum;
-    s_act[threadIdx.x] = asum;
-    __syncthreads();
-    for (int off = 1; off < T; off <<= 1) {
-        int a = threadIdx.x >= off ? s_cnt[threadIdx.x - off] : 0;
-        int b = threadIdx.x >= off ? s_chk[threadIdx.x - off] : 0;
-        int d = threadIdx.x >= off ? s_act[threadIdx.x - off] : 0;
-        __syncthreads();
-        s_cnt[threadIdx.x] += a;
-        s_chk[threadIdx.x] += b;
-        s_act[threadIdx.x] += d;
-        __syncthreads();
-    }
-    int pbase = s_cnt[threadIdx.x] - csum;
-    int wbase = s_chk[threadIdx.x] - ksum;
-    int abase = s_act[threadIdx.x] - asum;
-    for (int t = lo; t < hi; t++) {
-        int c = bcount[t];
-        if (c > 0) blist[abase++] = t;
-        bstart[t] = pbase;
-        bcursor[t] = 0;
-        bcount[t] = 0;
-        for (int b = 0; b < c; b += CHUNK) {
-            if (wbase < cap) {
-                WorkItem w;
-                w.tile = t;
-                w.begin = pbase + b;
-                w.end = pbase + min(c, b + CHUNK);
-                work[wbase] = w;
-            }
-            wbase++;
+// Exclusive scan of the brick counts in three launches over segments of
+// SCAN_SEG bricks: (1) each CTA sums its segment's particles, work items
+// (chunks of <= CHUNK particles) and non-empty bricks; (2) one CTA scans the
+// segment sums; (3) each CTA scans its segment again in brick order from its
+// segment's offsets and writes the brick starts, the work list, the list of
+// non-empty bricks, and resets the counters for the next sort.  Every load
+// and store of the brick arrays is coalesced.
+constexpr int SCAN_T = 1024;                 // threads per CTA
+constexpr int SCAN_ITEMS = SCAN_SEG / SCAN_T;  // bricks per thread and segment
+static_assert(SCAN_ITEMS * SCAN_T == SCAN_SEG, "scan segment");
+
+struct Tri {
+    int c, k, a;   // particles, work items, non-empty bricks
+};
+__device__ __forceinline__ Tri tri_of(int c) { return Tri{c, (c + CHUNK - 1) / CHUNK, c > 0 ? 1 : 0}; }
+
+// inclusive block-wide scan of (c, k, a) over SCAN_T threads; the block total in *tot
+__device__ __forceinline__ Tri block_scan(Tri v, Tri *sh, Tri *tot) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int c = __shfl_up_sync(0xffffffffu, v.c, o), k = __shfl_up_sync(0xffffffffu, v.k, o),
+                  a = __shfl_up_sync(0xffffffffu, v.a, o);
+        if (lane >= o) {
+            v.c += c;
+            v.k += k;
+            v.a += a;
         }
-        pbase += c;
     }
-    if (threadIdx.x == T - 1) {
-        *nwork = min(s_chk[T - 1], cap);
-        *nblist = s_act[T - 1];
-        bstart[nb] = s_cnt[T - 1];
+    if (lane == 31) sh[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        Tri w = lane < (SCAN_T >> 5) ? sh[lane] : Tri{0, 0, 0};
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int c = __shfl_up_sync(0xffffffffu, w.c, o), k = __shfl_up_sync(0xffffffffu, w.k, o),
+                      a = __shfl_up_sync(0xffffffffu, w.a, o);
+            if (lane >= o) {
+                w.c += c;
+                w.k += k;
+                w.a += a;
+            }
+        }
+        if (lane < (SCAN_T >> 5)) sh[lane] = w;   // inclusive warp offsets
+    }
+    __syncthreads();
+    if (wid > 0) {
+        const Tri b = sh[wid - 1];
+        v.c += b.c;
+        v.k += b.k;
+        v.a += b.a;
+    }
+    *tot = sh[(SCAN_T >> 5) - 1];
+    __syncthreads();   // sh is reused by the next call
+    return v;
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_scan_up(int nb, const int *__restrict__ bcount, int *part) {
+    __shared__ Tri sh[32];
+    const int base = blockIdx.x * SCAN_SEG;
+    Tri v{0, 0, 0};
+#pragma unroll
+    for (int r = 0; r < SCAN_ITEMS; r++) {
+        const int t = base + r * SCAN_T + threadIdx.x;
+        if (t < nb) {
+            const Tri q = tri_of(bcount[t]);
+            v.c += q.c;
+            v.k += q.k;
+            v.a += q.a;
+        }
+    }
+    Tri tot;
+    block_scan(v, sh, &tot);
+    if (threadIdx.x == 0) {
+        part[3 * blockIdx.x] = tot.c;
+        part[3 * blockIdx.x + 1] = tot.k;
+        part[3 * blockIdx.x + 2] = tot.a;
+    }
+}
+
+// exclusive scan of the nseg segment sums in place; the totals after them
+__global__ void __launch_bounds__(SCAN_T) k_scan_mid(int nseg, int *part) {
+    __shared__ Tri sh[32];
+    Tri carry{0, 0, 0};
+    for (int s0 = 0; s0 < nseg; s0 += SCAN_T) {
+        const int i = s0 + threadIdx.x;
+        const Tri v = i < nseg ? Tri{part[3 * i], part[3 * i + 1], part[3 * i + 2]} : Tri{0, 0, 0};
+        Tri tot;
+        const Tri inc = block_scan(v, sh, &tot);
+        if (i < nseg) {
+            part[3 * i] = carry.c + inc.c - v.c;
+            part[3 * i + 1] = carry.k + inc.k - v.k;
+            part[3 * i + 2] = carry.a + inc.a - v.a;
+        }
+        carry.c += tot.c;
+        carry.k += tot.k;
+        carry.a += tot.a;
+    }
+    if (threadIdx.x == 0) {
+        part[3 * nseg] = carry.c;
+        part[3 * nseg + 1] = carry.k;
+        part[3 * nseg + 2] = carry.a;
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_scan_down(int nb, int nseg, int *bcount, int *bstart, int *bcursor,
+                                                      WorkItem *work, int *nwork, int cap, int *blist, int *nblist,
+                                                      const int *part) {
+    __shared__ Tri sh[32];
+    const int base = blockIdx.x * SCAN_SEG;
+    Tri carry{part[3 * blockIdx.x], part[3 * blockIdx.x + 1], part[3 * blockIdx.x + 2]};
+    for (int r = 0; r < SCAN_ITEMS; r++) {
+        const int t = base + r * SCAN_T + threadIdx.x;
+        const int c = t < nb ? bcount[t] : 0;
+        const Tri v = tri_of(c);
+        Tri tot;
+        const Tri inc = block_scan(v, sh, &tot);
+        if (t < nb) {
+            const int pbase = carry.c + inc.c - v.c;
+            int wbase = carry.k + inc.k - v.k;
+            if (c > 0) blist[carry.a + inc.a - v.a] = t;
+            bstart[t] = pbase;
+            bcursor[t] = 0;
+            bcount[t] = 0;
+            for (int b = 0; b < c; b += CHUNK) {
+                if (wbase < cap) {
+                    WorkItem w;
+                    w.tile = t;
+                    w.begin = pbase + b;
+                    w.end = pbase + min(c, b + CHUNK);
+                    work[wbase] = w;
+                }
+                wbase++;
+            }
+        }
+        carry.c += tot.c;
+        carry.k += tot.k;
+        carry.a += tot.a;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *nwork = min(part[3 * nseg + 1], cap);
+        *nblist = part[3 * nseg + 2];
+        bstart[nb] = part[3 * nseg];
     }
 }
 
@@ -127,21 +216,35 @@ __global__ void __launch_bounds__(BRC) k_cell_sort(const int *bstart, const int 
     const int b = blockIdx.x;
     const int lo = bstart[b], hi = bstart[b + 1];
     const int lc = threadIdx.x;
+    int *cs = cstart + (size_t)b * (BRC + 1);
+    if (lo == hi) {   // an empty brick (uniform across the CTA): every cell starts at lo
+        cs[lc] = lo;
+        if (lc == 0) cs[BRC] = hi;
+        return;
+    }
     s_cnt[lc] = 0;
     s_cur[lc] = 0;
     __syncthreads();
     for (int j = lo + lc; j < hi; j += BRC) atomicAdd(&s_cnt[key[tmp[j]] % BRC], 1);
     __syncthreads();
-    if (lc == 0) {
-        int acc = 0;
-        for (int c = 0; c < BRC; c++) {
-            s_start[c] = acc;
-            acc += s_cnt[c];
+    {   // exclusive scan of the BRC cell counts: warp scans, then the warp offsets
+        static_assert(BRC % 32 == 0 && BRC / 32 <= 32, "cell scan layout");
+        const int lane = lc & 31, wid = lc >> 5;
+        int v = s_cnt[lc];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += u;
         }
-        s_start[BRC] = acc;
+        __shared__ int s_w[BRC / 32];
+        if (lane == 31) s_w[wid] = v;
+        __syncthreads();
+        int off = 0;
+        for (int w = 0; w < wid; w++) off += s_w[w];
+        s_start[lc + 1] = off + v;
+        if (lc == 0) s_start[0] = 0;
     }
     __syncthreads();
-    int *cs = cstart + (size_t)b * (BRC + 1);
     cs[lc] = lo + s_start[lc];
     if (lc == 0) cs[BRC] = hi;
     for (int j = lo + lc; j < hi; j += BRC) {
@@ -214,8 +317,15 @@ static mpm_status sort_impl(mpm_ctx *c) {
                                         c->d_tcount, &c->d_ctl->err_oob);
     timer_end(c, K_BIN);
     timer_begin(c, K_SCAN);
-    k_scan<<<1, 1024, 0, c->stream>>>(c->g.nbricks, c->d_tcount, c->d_tstart, c->d_tcursor, c->d_work, c->d_nwork,
-                                      c->nwork_cap, c->d_blist, c->d_nblist);
+    {
+        const int nseg = (c->g.nbricks + SCAN_SEG - 1) / SCAN_SEG;
+        k_scan_up<<<nseg, SCAN_T, 0, c->stream>>>(c->g.nbricks, c->d_tcount, c->d_scanpart);
+        k_scan_mid<<<1, SCAN_T, 0, c->stream>>>(nseg, c->d_scanpart);
+        k_scan_down<<<nseg, SCAN_T, 0, c->stream>>>(c->g.nbricks, nseg, c->d_tcount, c->d_tstart, c->d_tcursor,
+                                                    c->d_work, c->d_nwork, c->nwork_cap, c->d_blist, c->d_nblist,
+                                                    c->d_scanpart);
+        c->launches += 2;
+    }
     timer_end(c, K_SCAN);
     timer_begin(c, K_SCATTER);
     k_scatter<<<nb, 256, 0, c->stream>>>(c->d_key, n, c->d_tstart, c->d_tcursor, c->d_tmp);
