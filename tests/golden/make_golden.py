@@ -310,6 +310,40 @@ def ns_particle_kinematics(x, dx, xyelem, amp=0.05, seed=5):
     return v, a
 
 
+def fluid_lid_case(name="ns_step_lid", nsteps=2):
+    """Whole time steps of the reference's fluid loop with non-zero boundary
+    values and a load factor below one: the filled box of ns_box_inputs as a
+    lid-driven cavity (no-slip sides and bottom, the top face moving at
+    u = 0.04 m/s, the pressure fixed to 5 Pa at one top corner node),
+    facl = 0.6, FLIP; the particle state after nsteps and the nodal fields of
+    the first Particle2Node."""
+    c = ns_box_inputs()
+    c["facl"] = 0.6
+    xyelem = np.asarray(c["xyelem"])
+    nnc = xyelem + 1
+    N = int(np.prod(nnc))
+    iz = np.arange(N) // (nnc[0] * nnc[1])
+    top = np.nonzero(iz == xyelem[2])[0]
+    wall = np.setdiff1d(c["bc_wall"], top)
+    u_nodes = np.concatenate([wall, top]).astype(np.int32)
+    u_vals = np.concatenate([np.zeros(len(wall)), np.full(len(top), 0.04)])
+    vw_nodes = u_nodes
+    corner = np.array([top[-1]], dtype=np.int32)
+    bcs = [(u_nodes, u_vals), (vw_nodes, np.zeros(len(vw_nodes))), (vw_nodes, np.zeros(len(vw_nodes))),
+           (corner, np.array([5.0]))]
+    vel, acc = ns_particle_kinematics(c["x"], c["dxy"][0], c["xyelem"], seed=8)
+    r = ref.RefFluid(c["xyelem"], c["xymin"], c["dxy"], c["dt"], c["mtol"], c["gravity"], c["x"], c["mass"], c["vol"],
+                     c["rho"], c["rmu"], c["beta"], c["gamma"])
+    nodal, part, newton, krylov = r.run(vel, acc, 1, c["facl"], bcs, nsteps, rtol=1.0e-10)
+    out = {k: v for k, v in c.items() if k not in ("bc_wall", "bc_top")}
+    out.update(vel=vel, accel=acc, nsteps=np.array(nsteps), bc_u_nodes=u_nodes, bc_u_vals=u_vals,
+               bc_vw_nodes=vw_nodes, bc_p_nodes=corner, bc_p_vals=np.array([5.0]))
+    out.update({f"p2g_{f}": v for f, v in nodal.items()})
+    out.update({f"s_{f}": v for f, v in part.items()})
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
+    print(name, nsteps, "steps:", newton, "Newton,", krylov, "Krylov iterations")
+
+
 def fluid_step_case(name="ns_step", nsteps=3):
     """Whole time steps of the reference's fluid loop (MeshPointLinklist,
     Particle2Node, SolveNS with the linear systems solved to 1e-10 as in
@@ -354,6 +388,7 @@ def main():
         return
     if "--fluid-step" in sys.argv[1:]:
         fluid_step_case()
+        fluid_lid_case()
         return
     if "--implicit2" in sys.argv[1:]:
         implicit_extra_cases()
@@ -391,6 +426,7 @@ def main():
     implicit_extra_cases()
     fluid_newton_case()
     fluid_step_case()
+    fluid_lid_case()
 
 
 if __name__ == "__main__":

@@ -236,6 +236,23 @@ def test_gpu_ns_step_matches_oracle_larger_box_and_is_reproducible():
         assert np.array_equal(got[f], again[f]), f
 
 
+def test_gpu_ns_step_with_boundary_values_matches_reference():
+    """Non-zero boundary values and a load factor of 0.6 (the lid-driven
+    cavity of tests/golden/ns_step_lid.npz, 2 FLIP steps of the reference's
+    own fluid loop): Particle2Node's nodal fields to 1e-12, the particle state
+    to 1e-9."""
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ns_step_lid.npz")))
+    vw = (g["bc_vw_nodes"], np.zeros(len(g["bc_vw_nodes"])))
+    bcs = [(g["bc_u_nodes"], g["bc_u_vals"]), vw, vw, (g["bc_p_nodes"], g["bc_p_vals"])]
+    first, part, st = _fluid_gpu(g, bcs, g["vel"], g["accel"], 1, int(g["nsteps"]))
+    for f, v in first.items():
+        assert rel(v, g[f"p2g_{f}"]) < TOL, (f, rel(v, g[f"p2g_{f}"]))
+    errs = {"dx": rel(part["x"] - g["x"], g["s_x"] - g["x"])}
+    errs.update({f: rel(part[f], g[f"s_{f}"]) for f in ("v", "a", "pres")})
+    print("\nlid-driven fluid steps vs reference: " + ", ".join(f"{f} {e:.2e}" for f, e in errs.items()))
+    assert max(errs.values()) < 1e-9, errs
+
+
 def test_gpu_ns_step_reports_particle_outside_grid():
     """A particle beyond the grid's upper x wall: mpm_ns_step returns
     MPM_ERR_PARTICLE_OUT_OF_BOX before writing anything (the reference stops

@@ -112,3 +112,29 @@ def test_ns_step_oracle_matches_reference_fixture():
             assert rel(part["x"] - g["x"], want["x"] - g["x"]) < 1e-9, (tag, k)
             for f in ("v", "a", "pres"):
                 assert rel(part[f], want[f]) < 1e-9, (tag, k, f)
+
+
+def ns_lid_fixture():
+    g = dict(np.load(os.path.join(os.path.dirname(GOLDEN), "ns_step_lid.npz")))
+    vw = (g["bc_vw_nodes"], np.zeros(len(g["bc_vw_nodes"])))
+    bcs = [(g["bc_u_nodes"], g["bc_u_vals"]), vw, vw, (g["bc_p_nodes"], g["bc_p_vals"])]
+    return g, bcs
+
+
+def test_ns_step_oracle_with_boundary_values_matches_reference():
+    """The fluid loop with non-zero boundary values and a load factor of 0.6
+    (a lid-driven cavity: the top face at u = 0.04 m/s, 5 Pa at one node;
+    fixture tests/golden/ns_step_lid.npz from make_golden.py --fluid-step):
+    BCSetVal and BCNRSet scale the values by facl (and dt) as the reference
+    does; nodal fields of the first Particle2Node to 1e-14, the particle state
+    after 2 FLIP steps to 1e-9."""
+    g, bcs = ns_lid_fixture()
+    first, part = ns_oracle.ns_step(g["xyelem"], g["xymin"], g["dxy"], (2, 2, 2), float(g["rho"]), float(g["rmu"]),
+                                    float(g["dt"]), float(g["beta"]), float(g["gamma"]), g["gravity"],
+                                    float(g["facl"]), float(g["mtol"]), 1, g["x"], g["mass"], g["vol"], g["vel"],
+                                    g["accel"], bcs, nsteps=int(g["nsteps"]))
+    for f, v in first.items():
+        assert rel(v, g[f"p2g_{f}"]) < 1e-14, f
+    assert rel(part["x"] - g["x"], g["s_x"] - g["x"]) < 1e-9
+    for f in ("v", "a", "pres"):
+        assert rel(part[f], g[f"s_{f}"]) < 1e-9, f
