@@ -836,6 +836,7 @@ struct mpm_ns {
     unsigned *bnd = nullptr;
     double *tau1 = nullptr, *tau2 = nullptr, *geup = nullptr, *ppart = nullptr;
     int64_t pcap = 0;
+    bool nvol_ready = false;   // MakNodalVol has run into nvol
 };
 
 #define CKN(call)                                                                                                      \
@@ -1066,7 +1067,6 @@ static mpm_status ns_step_buffers(mpm_ns *s, int64_t n) {
     auto alloc = [&](void **p, size_t bytes) {
         if (e == cudaSuccess && !*p) e = cudaMalloc(p, bytes);
     };
-    const bool first = s->nvol == nullptr;
     alloc((void **)&s->nmass, sizeof(double) * N);
     alloc((void **)&s->nvof, sizeof(double) * N);
     alloc((void **)&s->nvel, sizeof(double) * 3 * N);
@@ -1077,7 +1077,7 @@ static mpm_status ns_step_buffers(mpm_ns *s, int64_t n) {
     alloc((void **)&s->sums, sizeof(unsigned long long) * 8 * N);
     alloc((void **)&s->bnd, sizeof(unsigned) * NB_N);
     alloc((void **)&s->nvol, sizeof(double) * N);
-    if (e == cudaSuccess && first) {
+    if (e == cudaSuccess && !s->nvol_ready) {
         Geom g{};
         for (int d = 0; d < 3; d++) {
             g.nel[d] = s->grid.xyelem[d];
@@ -1090,6 +1090,7 @@ static mpm_status ns_step_buffers(mpm_ns *s, int64_t n) {
         g.nelem = s->grid.xyelem[0] * s->grid.xyelem[1] * s->grid.xyelem[2];
         launch_nodal_volume(g, s->grid.npxye, s->nvol, s->stream);
         e = cudaGetLastError();
+        s->nvol_ready = e == cudaSuccess;
     }
     if (e == cudaSuccess && n > s->pcap) {
         for (double **p : {&s->tau1, &s->tau2, &s->geup, &s->ppart}) {

@@ -144,7 +144,10 @@ mpm_status mpm_gpu_download_nodal(mpm_ctx *ctx, int field, double *host);
 /* Particles in the order they were loaded; any pointer may be NULL.  The
  * state of the particle vectors (coord, vel, def_grad, stress, vol) that the
  * reference's drivers read after Node2Particle (module/material_point.h:186-198).
- * Host buffers in pinned memory transfer at full link speed. */
+ * Host buffers in pinned memory transfer at full link speed.  A precision-32
+ * context whose materials are all Tait fluids (iprop 4) keeps only J = det F
+ * of the deformation gradient: F comes back as J^(1/3) I, and an uploaded F
+ * contributes its determinant. */
 mpm_status mpm_gpu_download_particles(mpm_ctx *ctx, double *coord, double *vel, double *F, double *stress,
                                       double *vol);
 /* TPIC / APIC contexts: the affine velocity matrix of each particle, 9
