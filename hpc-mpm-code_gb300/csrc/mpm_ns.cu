@@ -148,50 +148,63 @@ __global__ void __launch_bounds__(128) k_ns_assemble(NsArgs a, const double *__r
     const double V = vol[p], m = mass[p];
     const double divv = gv[0][0] + gv[1][1] + gv[2][2];
     const double vmu = V * a.rmu, vt2 = V * t2, mt1 = a.nb[3] * m * t1;
+    // the velocity block of the pair (a, b) is the transpose of that of (b, a)
+    // and K_33 is symmetric, so each unordered pair is formed once:
+    //   K_rc = nb0 vmu (a_c b_r + (a.b) d_rc) + nb0 vt2 a_r b_c,  K_r3 = -V a_r N_j,
+    //   K_3c = nb0 V N_i b_c + mt1 a_c N_j,  K_33 = V t1 (a.b)
+    // (a the row node's corrected gradient, b the column node's)
+    const double kv = a.nb[0] * vmu, kt = a.nb[0] * vt2, kc = a.nb[0] * V, vt1 = V * t1;
 #pragma unroll 1
     for (int qa = 0; qa < 8; qa++) {
         const int na = nid[qa];
         const double ai[3] = {dN[qa][0], dN[qa][1], dN[qa][2]};
         const double Ni = Nw[qa];
         const double emd = a.nb[3] * Ni * m;   // ComputeNRLumpedMat
-        // the row node's factors of the 16 entries, formed once per row node:
-        //   K_rc = nb0 vmu (a_c b_r + (a.b) d_rc) + nb0 vt2 a_r b_c,  K_r3 = -V a_r N_j,
-        //   K_3c = nb0 V N_i b_c + mt1 a_c N_j,  K_33 = V t1 (a.b)
-        double A1[3], A2[3], Pu[3], Q[3], T[3];
+        double A1[3], A2[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            A1[c] = a.nb[0] * vmu * ai[c];
-            A2[c] = a.nb[0] * vt2 * ai[c];
-            Pu[c] = -V * ai[c];
-            Q[c] = mt1 * ai[c];
-            T[c] = V * t1 * ai[c];
+            A1[c] = kv * ai[c];
+            A2[c] = kt * ai[c];
         }
-        const double c1 = a.nb[0] * V * Ni;
+        const double c1a = kc * Ni, mNi = mt1 * Ni, vNi = -V * Ni;
 #pragma unroll 1
-        for (int qb = 0; qb < 8; qb++) {
+        for (int qb = qa; qb < 8; qb++) {
             const double bj[3] = {dN[qb][0], dN[qb][1], dN[qb][2]};
             const double Nj = Nw[qb];
             const int s = ((qb & 1) - (qa & 1) + 1) + 3 * (((qb >> 1) & 1) - ((qa >> 1) & 1) + 1) +
                           9 * ((qb >> 2) - (qa >> 2) + 1);
-            const double ab1 = fma(A1[0], bj[0], fma(A1[1], bj[1], A1[2] * bj[2]));   // nb0 vmu (a.b)
-            double K[16];
+            const double ab = fma(ai[0], bj[0], fma(ai[1], bj[1], ai[2] * bj[2]));
+            const double ab1 = kv * ab, k33 = vt1 * ab;
+            double Vb[3][3];   // velocity block of row a, column b
 #pragma unroll
-            for (int r = 0; r < 3; r++) {
+            for (int r = 0; r < 3; r++)
 #pragma unroll
-                for (int c = 0; c < 3; c++) K[4 * r + c] = fma(A1[c], bj[r], A2[r] * bj[c]);
-                K[5 * r] += ab1;
-                K[4 * r + 3] = Pu[r] * Nj;
-                K[12 + r] = fma(c1, bj[r], Q[r] * Nj);
+                for (int c = 0; c < 3; c++) Vb[r][c] = fma(A1[c], bj[r], A2[r] * bj[c]) + (r == c ? ab1 : 0.0);
+            const double Pj = -V * Nj, mNj = mt1 * Nj;
+            {   // row a, column b
+                double *row = A + (size_t)s * 16 * N + na;
+#pragma unroll
+                for (int r = 0; r < 3; r++) {
+#pragma unroll
+                    for (int c = 0; c < 3; c++)
+                        atomicAdd(row + (size_t)(4 * r + c) * N, Vb[r][c] + (qa == qb && r == c ? emd : 0.0));
+                    atomicAdd(row + (size_t)(4 * r + 3) * N, Pj * ai[r]);
+                    atomicAdd(row + (size_t)(12 + r) * N, fma(c1a, bj[r], mNj * ai[r]));
+                }
+                atomicAdd(row + (size_t)15 * N, k33);
             }
-            K[15] = fma(T[0], bj[0], fma(T[1], bj[1], T[2] * bj[2]));
-            if (qa == qb) {
-                K[0] += emd;
-                K[5] += emd;
-                K[10] += emd;
-            }
-            double *row = A + (size_t)s * 16 * N + na;
+            if (qb != qa) {   // row b, column a: the transposed velocity block
+                double *row = A + (size_t)(26 - s) * 16 * N + nid[qb];
+                const double c1b = kc * Nj;
 #pragma unroll
-            for (int k = 0; k < 16; k++) atomicAdd(row + (size_t)k * N, K[k]);
+                for (int r = 0; r < 3; r++) {
+#pragma unroll
+                    for (int c = 0; c < 3; c++) atomicAdd(row + (size_t)(4 * r + c) * N, Vb[c][r]);
+                    atomicAdd(row + (size_t)(4 * r + 3) * N, vNi * bj[r]);
+                    atomicAdd(row + (size_t)(12 + r) * N, fma(c1b, ai[r], mNi * bj[r]));
+                }
+                atomicAdd(row + (size_t)15 * N, k33);
+            }
         }
         double rg[4];
 #pragma unroll
