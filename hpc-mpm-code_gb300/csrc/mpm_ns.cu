@@ -850,6 +850,11 @@ struct mpm_ns {
     double *tau1 = nullptr, *tau2 = nullptr, *geup = nullptr, *ppart = nullptr;
     int64_t pcap = 0;
     bool nvol_ready = false;   // MakNodalVol has run into nvol
+    // particles held by the context (mpm_ns_load_particles): 12 SoA arrays of np
+    double *pbuf = nullptr;
+    int64_t np = 0;
+    bool p2g_done = false;     // Particle2Node ran since the last Node2Particle
+    int p2g_scheme = MPM_PIC;
 };
 
 #define CKN(call)                                                                                                      \
@@ -867,7 +872,7 @@ extern "C" void mpm_ns_destroy(mpm_ns *s) {
                     s->cnt,   s->status, s->v.rr,   s->v.rs,   s->v.pp,   s->v.Ap, s->v.Ar,  s->v.Az,
                     s->v.Au,  s->v.uu,   s->v.zz,   s->v.xs,   s->v.Ax,   s->nmass, s->nvof, s->nvel,
                     s->naccel, s->ndispl, s->npres, s->nvol,   s->nei,    s->sums, s->bnd,   s->tau1,
-                    s->tau2,  s->geup,   s->ppart};
+                    s->tau2,  s->geup,   s->ppart,  s->pbuf};
     for (void *p : bufs)
         if (p) cudaFree(p);
     if (s->h_scal) cudaFreeHost(s->h_scal);
@@ -1184,25 +1189,15 @@ extern "C" mpm_status mpm_ns_p2g(mpm_ns *s, int64_t n, const double *x, const do
     return ns_p2g(s, ns_step_args(s, n, scheme, facl), x, vel, accel, mass, vol);
 }
 
-extern "C" mpm_status mpm_ns_step(mpm_ns *s, int64_t n, double *x, double *vel, double *accel, double *pres,
-                                  const double *mass, const double *vol, int scheme, double facl, double rtol,
-                                  int kmax, mpm_ns_stats *stats) {
-    mpm_status rc = ns_step_check(s, n, x, vel, accel, mass, vol, scheme, facl);
-    if (rc != MPM_OK) return rc;
-    if (!(rtol > 0.0) || kmax < 1 || (n > 0 && !pres)) return MPM_ERR_BAD_ARG;
-    const NsStepArgs a = ns_step_args(s, n, scheme, facl);
+// Node2Particle (var_trans_fluid.cpp:82-135) from the context's nodal state
+// after the solve.  Synchronises the stream.
+static mpm_status ns_g2p(mpm_ns *s, const NsStepArgs &a, double *x, double *vel, double *accel, double *pres,
+                         const double *vol) {
     cudaStream_t st = s->stream;
-    rc = ns_p2g(s, a, x, vel, accel, mass, vol);
-    if (rc != MPM_OK) return rc;
-    // ---- SolveNS (solve_ns_mpm.cpp:28-62)
-    rc = mpm_ns_solve(s, n, x, mass, vol, s->nvel, s->naccel, s->nmass, s->ndispl, s->npres, s->tau1, s->tau2, rtol,
-                      kmax, stats);
-    if (rc != MPM_OK) return rc;
-    // ---- Node2Particle (var_trans_fluid.cpp:82-135)
     k_nsn_commit<<<(s->nodec + 255) / 256, 256, 0, st>>>(a, s->ndispl, s->nvof, s->nvol, s->nvel, s->naccel, s->nei,
                                                          s->part, s->cnt + 3, s->scal, NS_EU);
-    if (n > 0) {
-        const unsigned npb = (unsigned)((n + 255) / 256);
+    if (a.n > 0) {
+        const unsigned npb = (unsigned)((a.n + 255) / 256);
         k_nsp_g2p<<<npb, 256, 0, st>>>(a, x, vel, accel, pres, vol, s->nvel, s->naccel, s->ndispl, s->npres, s->nei,
                                        s->geup, s->ppart, s->cnt + 3, s->scal, NS_GD);
         k_nsp_shift<<<npb, 256, 0, st>>>(a, s->geup, s->scal, NS_EU, NS_GD, x);
@@ -1210,6 +1205,111 @@ extern "C" mpm_status mpm_ns_step(mpm_ns *s, int64_t n, double *x, double *vel, 
     CKN(cudaGetLastError());
     CKN(cudaStreamSynchronize(st));
     return MPM_OK;
+}
+
+extern "C" mpm_status mpm_ns_step(mpm_ns *s, int64_t n, double *x, double *vel, double *accel, double *pres,
+                                  const double *mass, const double *vol, int scheme, double facl, double rtol,
+                                  int kmax, mpm_ns_stats *stats) {
+    mpm_status rc = ns_step_check(s, n, x, vel, accel, mass, vol, scheme, facl);
+    if (rc != MPM_OK) return rc;
+    if (!(rtol > 0.0) || kmax < 1 || (n > 0 && !pres)) return MPM_ERR_BAD_ARG;
+    const NsStepArgs a = ns_step_args(s, n, scheme, facl);
+    rc = ns_p2g(s, a, x, vel, accel, mass, vol);
+    if (rc != MPM_OK) return rc;
+    // ---- SolveNS (solve_ns_mpm.cpp:28-62)
+    rc = mpm_ns_solve(s, n, x, mass, vol, s->nvel, s->naccel, s->nmass, s->ndispl, s->npres, s->tau1, s->tau2, rtol,
+                      kmax, stats);
+    if (rc != MPM_OK) return rc;
+    return ns_g2p(s, a, x, vel, accel, pres, vol);
+}
+
+// ------------------------------------------------- particles held by the context
+// The three member calls of a StabilizedMPM time step on particles the
+// context holds (uploaded once from the reference's AoS host vectors).
+extern "C" mpm_status mpm_ns_load_particles(mpm_ns *s, int64_t n, const double *coord, const double *vel,
+                                            const double *accel, const double *mass, const double *vol) {
+    if (!s || n < 0 || n > ((int64_t)1 << 31) - 256) return MPM_ERR_BAD_ARG;
+    if (n > 0 && (!coord || !mass || !vol)) return MPM_ERR_BAD_ARG;
+    CKN(cudaStreamSynchronize(s->stream));
+    if (s->pbuf) cudaFree(s->pbuf);
+    s->pbuf = nullptr;
+    s->np = 0;
+    s->p2g_done = false;
+    const size_t N = (size_t)(n > 0 ? n : 1);
+    // SoA: x 3, vel 3, accel 3, pres, mass, vol
+    CKN(cudaMalloc((void **)&s->pbuf, sizeof(double) * 12 * N));
+    std::vector<double> h(12 * N, 0.0);
+    for (int64_t p = 0; p < n; p++) {
+        for (int d = 0; d < 3; d++) {
+            h[d * N + p] = coord[3 * p + d];
+            h[(3 + d) * N + p] = vel ? vel[3 * p + d] : 0.0;
+            h[(6 + d) * N + p] = accel ? accel[3 * p + d] : 0.0;
+        }
+        h[10 * N + p] = mass[p];
+        h[11 * N + p] = vol[p];
+    }
+    CKN(cudaMemcpy(s->pbuf, h.data(), sizeof(double) * 12 * N, cudaMemcpyHostToDevice));
+    s->np = n;
+    return MPM_OK;
+}
+
+extern "C" mpm_status mpm_ns_download_particles(mpm_ns *s, double *coord, double *vel, double *accel, double *pres) {
+    if (!s || (s->np > 0 && !s->pbuf)) return MPM_ERR_BAD_ARG;
+    const int64_t n = s->np;
+    if (n == 0) return MPM_OK;
+    const size_t N = (size_t)n;
+    std::vector<double> h(12 * N);
+    CKN(cudaStreamSynchronize(s->stream));
+    CKN(cudaMemcpy(h.data(), s->pbuf, sizeof(double) * 12 * N, cudaMemcpyDeviceToHost));
+    for (int64_t p = 0; p < n; p++) {
+        for (int d = 0; d < 3; d++) {
+            if (coord) coord[3 * p + d] = h[d * N + p];
+            if (vel) vel[3 * p + d] = h[(3 + d) * N + p];
+            if (accel) accel[3 * p + d] = h[(6 + d) * N + p];
+        }
+        if (pres) pres[p] = h[9 * N + p];
+    }
+    return MPM_OK;
+}
+
+// the resident arrays: x, vel, accel (3 blocks each), pres, mass, vol
+static void ns_resident(mpm_ns *s, double *&x, double *&vel, double *&accel, double *&pres, double *&mass,
+                        double *&vol) {
+    const size_t N = (size_t)(s->np > 0 ? s->np : 1);
+    x = s->pbuf;
+    vel = s->pbuf + 3 * N;
+    accel = s->pbuf + 6 * N;
+    pres = s->pbuf + 9 * N;
+    mass = s->pbuf + 10 * N;
+    vol = s->pbuf + 11 * N;
+}
+
+extern "C" mpm_status mpm_ns_particle2node(mpm_ns *s, int scheme, double facl) {
+    if (!s || !s->pbuf) return MPM_ERR_STATE;
+    double *x, *vel, *accel, *pres, *mass, *vol;
+    ns_resident(s, x, vel, accel, pres, mass, vol);
+    mpm_status rc = ns_step_check(s, s->np, x, vel, accel, mass, vol, scheme, facl);
+    if (rc != MPM_OK) return rc;
+    rc = ns_p2g(s, ns_step_args(s, s->np, scheme, facl), x, vel, accel, mass, vol);
+    s->p2g_done = rc == MPM_OK;
+    s->p2g_scheme = scheme;
+    return rc;
+}
+
+extern "C" mpm_status mpm_ns_solve_ns(mpm_ns *s, double rtol, int kmax, mpm_ns_stats *stats) {
+    if (!s || !s->pbuf || !s->p2g_done) return MPM_ERR_STATE;
+    double *x, *vel, *accel, *pres, *mass, *vol;
+    ns_resident(s, x, vel, accel, pres, mass, vol);
+    return mpm_ns_solve(s, s->np, x, mass, vol, s->nvel, s->naccel, s->nmass, s->ndispl, s->npres, s->tau1, s->tau2,
+                        rtol, kmax, stats);
+}
+
+extern "C" mpm_status mpm_ns_node2particle(mpm_ns *s) {
+    if (!s || !s->pbuf || !s->p2g_done) return MPM_ERR_STATE;
+    double *x, *vel, *accel, *pres, *mass, *vol;
+    ns_resident(s, x, vel, accel, pres, mass, vol);
+    s->p2g_done = false;   // the next time step starts with Particle2Node
+    return ns_g2p(s, ns_step_args(s, s->np, s->p2g_scheme, s->prm.facl), x, vel, accel, pres, vol);
 }
 
 extern "C" mpm_status mpm_ns_get_nodal(mpm_ns *s, int field, double *host) {

@@ -22,14 +22,11 @@
 #include <string>
 #include <vector>
 
+#include "gpu_reference_common.h"
 #include "mpm_gpu.h"
 #include "solid/solid_material_point.h"
 
 namespace mpmgpu_ref {
-
-inline void Check(mpm_status s, const char *where) {
-    if (s != MPM_OK) throw std::runtime_error(std::string(where) + ": " + mpm_gpu_status_string(s));
-}
 
 // The material table of dataset.h (iprop is a vector of doubles there,
 // mat_prop holds npropmax values per material) as the C ABI takes it: the
@@ -44,19 +41,6 @@ inline void MaterialTable(std::vector<int> &ip, std::vector<double> &mp) {
         const size_t np = std::min<size_t>(3, mat_prop[k].size());
         for (size_t j = 0; j < np; ++j) mp[3 * k + j] = mat_prop[k][j];
     }
-}
-
-// The grid globals of mesh.h / dataset.h (set by InputParaGriddata and datain_para).
-inline mpm_grid_desc GridDesc() {
-    mpm_grid_desc g{};
-    for (int d = 0; d < 3; ++d) {
-        g.xyelem[d] = xyelem[d];
-        g.xymin[d] = xymin[d];
-        g.dxy[d] = dxy[d];
-        g.idimc[d] = idimc[d];
-        g.npxye[d] = npxye[d];
-    }
-    return g;
 }
 
 inline mpm_config Config(MapScheme scheme, int precision) {

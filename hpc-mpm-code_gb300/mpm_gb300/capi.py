@@ -80,7 +80,9 @@ EXPORTS = ["mpm_gpu_create", "mpm_gpu_destroy", "mpm_gpu_set_stream", "mpm_gpu_s
            "mpm_nn_init_params", "mpm_nn_set_linear", "mpm_nn_set_additive", "mpm_nn_set_symmetric", "mpm_nn_set_params", "mpm_nn_get_params", "mpm_nn_forward", "mpm_nn_backward",
            "mpm_nn_num_pairs", "mpm_nn_train", "mpm_gpu_implicit_set_precond", "mpm_gpu_implicit_harvest", "mpm_gpu_implicit_apply_precond",
            "mpm_gpu_set_graph", "mpm_gpu_set_tuning", "mpm_gpu_selftest_wait", "mpm_ns_create", "mpm_ns_destroy",
-           "mpm_ns_set_stream", "mpm_ns_set_bc", "mpm_ns_solve", "mpm_ns_p2g", "mpm_ns_step", "mpm_ns_get_nodal"]
+           "mpm_ns_set_stream", "mpm_ns_set_bc", "mpm_ns_solve", "mpm_ns_p2g", "mpm_ns_step", "mpm_ns_get_nodal",
+           "mpm_ns_load_particles", "mpm_ns_particle2node", "mpm_ns_solve_ns", "mpm_ns_node2particle",
+           "mpm_ns_download_particles"]
 
 
 def load(path: str | None = None):
@@ -635,6 +637,39 @@ class NsSolver:
                              mass.data_ptr(), vol.data_ptr(), int(scheme), float(facl), float(rtol), int(kmax),
                              C.byref(st)), "mpm_ns_step")
         return {k: getattr(st, k) for k, _ in NsStats._fields_}
+
+    # --- the reference's three member calls on particles the context holds
+    def load_particles(self, coord, vel, accel, mass, vol):
+        """mpm_ns_load_particles from host arrays (coord, vel, accel (n, 3); mass, vol (n))."""
+        self.lib.mpm_ns_load_particles.argtypes = [C.c_void_p, C.c_int64, _dp, _dp, _dp, _dp, _dp]
+        f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        self._host = [f(coord), f(vel), f(accel), f(mass), f(vol)]
+        _chk(self.lib.mpm_ns_load_particles(self.ns, len(self._host[3]), *[_ptr(a) for a in self._host]),
+             "mpm_ns_load_particles")
+        self.np = len(self._host[3])
+
+    def particle2node(self, scheme=0, facl=1.0):
+        self.lib.mpm_ns_particle2node.argtypes = [C.c_void_p, C.c_int, C.c_double]
+        _chk(self.lib.mpm_ns_particle2node(self.ns, int(scheme), float(facl)), "mpm_ns_particle2node")
+
+    def solve_ns(self, rtol=1.0e-10, kmax=10000):
+        self.lib.mpm_ns_solve_ns.argtypes = [C.c_void_p, C.c_double, C.c_int, C.POINTER(NsStats)]
+        st = NsStats()
+        _chk(self.lib.mpm_ns_solve_ns(self.ns, float(rtol), int(kmax), C.byref(st)), "mpm_ns_solve_ns")
+        return {k: getattr(st, k) for k, _ in NsStats._fields_}
+
+    def node2particle(self):
+        self.lib.mpm_ns_node2particle.argtypes = [C.c_void_p]
+        _chk(self.lib.mpm_ns_node2particle(self.ns), "mpm_ns_node2particle")
+
+    def download_particles(self):
+        """x, v, a (n, 3) and pres (n) of the particles the context holds."""
+        self.lib.mpm_ns_download_particles.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+        n = self.np
+        x, v, a, p = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n)
+        _chk(self.lib.mpm_ns_download_particles(self.ns, _ptr(x), _ptr(v), _ptr(a), _ptr(p)),
+             "mpm_ns_download_particles")
+        return dict(x=x, v=v, a=a, pres=p)
 
     NODAL = {"nmass": (0, 1), "nvof": (1, 1), "nvel": (2, 3), "naccel": (3, 3), "ndispl": (4, 3), "npres": (5, 1),
              "nvol": (6, 1)}

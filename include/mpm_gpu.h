@@ -463,6 +463,28 @@ mpm_status mpm_ns_p2g(mpm_ns *ns, int64_t n, const double *x, const double *vel,
 mpm_status mpm_ns_step(mpm_ns *ns, int64_t n, double *x, double *vel, double *accel, double *pres,
                        const double *mass, const double *vol, int scheme, double facl, double rtol, int kmax,
                        mpm_ns_stats *stats);
+/* The same time step as the reference's three member calls, on particles the
+ * context holds: mpm_ns_load_particles copies the reference's host vectors
+ * (coord, vel, accel as n x 3, mass and vol of n; vel and accel may be NULL
+ * for zero) to the device once; then per time step
+ *   mpm_ns_particle2node  replaces StabilizedMPM::Particle2Node
+ *                         (module/fluid/MPM/var_trans_fluid.cpp:17-80),
+ *   mpm_ns_solve_ns       replaces StabilizedMPM::SolveNS
+ *                         (module/fluid/MPM/solve_ns_mpm.cpp:28-62) on the
+ *                         nodal state Particle2Node left (as mpm_ns_solve),
+ *   mpm_ns_node2particle  replaces StabilizedMPM::Node2Particle
+ *                         (var_trans_fluid.cpp:82-135),
+ * each with the semantics of mpm_ns_step (scheme and facl are those of the
+ * step's Particle2Node).  mpm_ns_download_particles copies coord, vel, accel
+ * (n x 3) and pres (n) back (any pointer may be NULL), where the reference
+ * writes output or restarts.  solve_ns and node2particle before a
+ * particle2node return MPM_ERR_STATE.  All synchronise the context's stream. */
+mpm_status mpm_ns_load_particles(mpm_ns *ns, int64_t n, const double *coord, const double *vel,
+                                 const double *accel, const double *mass, const double *vol);
+mpm_status mpm_ns_particle2node(mpm_ns *ns, int scheme, double facl);
+mpm_status mpm_ns_solve_ns(mpm_ns *ns, double rtol, int kmax, mpm_ns_stats *stats);
+mpm_status mpm_ns_node2particle(mpm_ns *ns);
+mpm_status mpm_ns_download_particles(mpm_ns *ns, double *coord, double *vel, double *accel, double *pres);
 /* The context's nodal state after mpm_ns_p2g / mpm_ns_step, to a host array:
  * field 0 nmass, 1 nvof, 2 nvel, 3 naccel, 4 ndispl, 5 npres, 6 nvol
  * (3*nodec component-major for 2-4, nodec otherwise).  After a step, nvel and

@@ -253,6 +253,33 @@ def test_gpu_ns_step_with_boundary_values_matches_reference():
     assert max(errs.values()) < 1e-9, errs
 
 
+def test_gpu_ns_member_calls_on_held_particles_match_the_step():
+    """The reference's three member calls on particles the context holds
+    (mpm_ns_load_particles, then per step mpm_ns_particle2node,
+    mpm_ns_solve_ns, mpm_ns_node2particle; mpm_ns_download_particles) give
+    bitwise the particle state of mpm_ns_step on caller arrays, which the
+    fixture test pins to the reference; a call out of order is refused."""
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ns_step.npz")))
+    bcs = _box_bcs(g)
+    _, want, _ = _fluid_gpu(g, bcs, g["vel"], g["accel"], 1, 3)
+    pytest.importorskip("torch")
+    s = capi.NsSolver(g["xyelem"], g["xymin"], g["dxy"], *(g[k] for k in KEYS), bcs=bcs)
+    s.load_particles(g["x"], g["vel"], g["accel"], g["mass"], g["vol"])
+    with pytest.raises(capi.MpmError) as err:
+        s.node2particle()
+    assert err.value.code == 8   # MPM_ERR_STATE: Node2Particle before Particle2Node
+    for _ in range(3):
+        s.particle2node(1, g["facl"])
+        st = s.solve_ns(rtol=1.0e-10)
+        s.node2particle()
+    got = s.download_particles()
+    s.close()
+    assert st["newton_iters"] >= 1
+    for f in ("x", "v", "a", "pres"):
+        assert np.array_equal(got[f], want[f]), f
+    assert rel(got["x"] - g["x"], g["flip_s3_x"] - g["x"]) < 1e-9
+
+
 def test_gpu_ns_step_reports_particle_outside_grid():
     """A particle beyond the grid's upper x wall: mpm_ns_step returns
     MPM_ERR_PARTICLE_OUT_OF_BOX before writing anything (the reference stops
