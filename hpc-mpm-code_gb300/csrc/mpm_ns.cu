@@ -1210,9 +1210,9 @@ static mpm_status ns_g2p(mpm_ns *s, const NsStepArgs &a, double *x, double *vel,
 extern "C" mpm_status mpm_ns_step(mpm_ns *s, int64_t n, double *x, double *vel, double *accel, double *pres,
                                   const double *mass, const double *vol, int scheme, double facl, double rtol,
                                   int kmax, mpm_ns_stats *stats) {
+    if (!(rtol > 0.0) || kmax < 1 || (n > 0 && !pres)) return MPM_ERR_BAD_ARG;
     mpm_status rc = ns_step_check(s, n, x, vel, accel, mass, vol, scheme, facl);
     if (rc != MPM_OK) return rc;
-    if (!(rtol > 0.0) || kmax < 1 || (n > 0 && !pres)) return MPM_ERR_BAD_ARG;
     const NsStepArgs a = ns_step_args(s, n, scheme, facl);
     rc = ns_p2g(s, a, x, vel, accel, mass, vol);
     if (rc != MPM_OK) return rc;
