@@ -78,6 +78,7 @@ struct ImpState {
     double *gqq = nullptr, *gbeta = nullptr;  // |A p|^2 of each kept direction, projection coefficients
     float *gqf = nullptr;                   // FP32 copies of the kept images (GM * 3 * nodec), for the dots
     float *gp32 = nullptr, *gq32 = nullptr;  // FP32 operator: the directions and images in FP32 (GM * 3 * nodec)
+    float *dfx = nullptr;                   // FP32 operator: x split into high and low FP32 parts (2 * 3 * nodec)
     unsigned *cnt = nullptr;                // block counters of the single-launch reductions (zero between launches)
     int fallbacks = 0;                      // solves that switched from the network to Jacobi
     int nn_applications = 0;
@@ -773,6 +774,78 @@ __global__ void __launch_bounds__(256) k_imp_matvec(ImpArgs a, const TA *A, cons
     }
 }
 
+// x = xh + xl with FP32 parts (xl the rounding error of xh): 48 bits of x
+__global__ void k_split_df(const double *__restrict__ x, float *__restrict__ xh, float *__restrict__ xl, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = x[i];
+    const float h = (float)v;
+    xh[i] = h;
+    xl[i] = (float)(v - (double)h);
+}
+
+// y = A x for the FP32-stored stencil of the FP32 operator, in double-float
+// arithmetic instead of FP64 (the true residual and the Newton check): each
+// product e x = e (xh + xl) is e xh exactly (an FMA gives its rounding error)
+// plus e xl, and the row sums are carried as an unevaluated FP32 pair
+// (Knuth's two-sum for the high part).  About 44 bits of the sum, on the FP32
+// pipe (GB300 executes 2 FP64 FMAs per SM and clock, against 128 FP32 lanes).
+template <int RX, int RY, int RZ>
+__global__ void __launch_bounds__(256) k_imp_matvec_df(ImpArgs a, const float *A, const float *__restrict__ xh,
+                                                       const float *__restrict__ xl, double *y) {
+    constexpr int SX = 2 * RX + 1, SY = 2 * RY + 1, NS = SX * SY * (2 * RZ + 1);
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= a.nodec) return;
+    const size_t N = (size_t)a.nodec;
+    int i, j, k;
+    node_ijk(n, a.nnc, i, j, k);
+    float sh[3] = {0.0f, 0.0f, 0.0f}, sl[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+        const int ii = i + s % SX - RX, jj = j + (s / SX) % SY - RY, kk = k + s / (SX * SY) - RZ;
+        if (ii < 0 || jj < 0 || kk < 0 || ii >= a.nnc[0] || jj >= a.nnc[1] || kk >= a.nnc[2]) continue;
+        const size_t col = ii + (size_t)a.nnc[0] * (jj + (size_t)a.nnc[1] * kk);
+        const float h[3] = {__ldg(xh + col), __ldg(xh + N + col), __ldg(xh + 2 * N + col)};
+        const float l[3] = {__ldg(xl + col), __ldg(xl + N + col), __ldg(xl + 2 * N + col)};
+        float e[9];
+        if ((s & 1) == 0) {
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const float2 v = __ldg(reinterpret_cast<const float2 *>(A + aidx(s * 9 + 2 * t, n, a.qp)));
+                e[2 * t] = v.x;
+                e[2 * t + 1] = v.y;
+            }
+            e[8] = __ldg(A + aidx(s * 9 + 8, n, a.qp));
+        } else {
+            e[0] = __ldg(A + aidx(s * 9, n, a.qp));
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                const float2 v = __ldg(reinterpret_cast<const float2 *>(A + aidx(s * 9 + 1 + 2 * t, n, a.qp)));
+                e[1 + 2 * t] = v.x;
+                e[2 + 2 * t] = v.y;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                // round-to-nearest intrinsics: the compiler may not fuse or
+                // reorder them, which the error-free transformations rely on
+                const float ev = e[3 * r + c];
+                const float p = __fmul_rn(ev, h[c]);
+                const float pe = fmaf(ev, h[c], -p);   // e xh - p, exactly
+                const float sum = __fadd_rn(sh[r], p);   // two-sum of sh and p
+                const float bp = __fsub_rn(sum, sh[r]);
+                const float err = __fadd_rn(__fsub_rn(sh[r], __fsub_rn(sum, bp)), __fsub_rn(p, bp));
+                sh[r] = sum;
+                sl[r] += err + fmaf(ev, l[c], pe);
+            }
+    }
+    const unsigned char bf = a.bcflag[n];
+#pragma unroll
+    for (int c = 0; c < 3; c++) y[c * N + n] = (bf & (1 << c)) ? 0.0 : (double)sh[c] + (double)sl[c];
+}
+
 // ScaleSolution + BCResidualSet: xs = x / D, r = b D (crsmat.cpp:190-209)
 __global__ void k_cg_scale_in(ImpArgs a, const double *x, const double *b, const double *adiag, double *xs,
                               double *rr) {
@@ -1363,6 +1436,7 @@ void implicit_free(mpm_ctx *c) {
     if (s->cnt) cudaFree(s->cnt);
     if (s->gqf) cudaFree(s->gqf);
     if (s->gp32) cudaFree(s->gp32);
+    if (s->dfx) cudaFree(s->dfx);
     if (s->gq32) cudaFree(s->gq32);
     if (s->h_scal) cudaFreeHost(s->h_scal);
     for (cudaGraphExec_t g : {s->g_cg, s->g_fcg_nn, s->g_fcg_jac, s->g_gcr})
@@ -1461,6 +1535,7 @@ mpm_status mpm_gpu_implicit_setup(mpm_ctx *c, int nr_flag, double spec_rad) {
     if (s->prec == 32) {
         CKI(cudaMalloc((void **)&s->gp32, sizeof(float) * GM * 3 * N));
         CKI(cudaMalloc((void **)&s->gq32, sizeof(float) * GM * 3 * N));
+        if (!getenv("MPM_GB300_TRUE_RESIDUAL_FP64")) CKI(cudaMalloc((void **)&s->dfx, sizeof(float) * 2 * 3 * N));
     }
     CKI(cudaMalloc((void **)&s->cnt, sizeof(unsigned) * 8));
     CKI(cudaMemset(s->cnt, 0, sizeof(unsigned) * 8));
@@ -1499,9 +1574,24 @@ static void launch_matvec(mpm_ctx *c, const ImpArgs &a, int nb, const double *x,
         else
             k_imp_matvec<TA, TC, 2, 1, 2><<<nb, 256, 0, c->stream>>>(a, A, x, y, part, cnt, scal, slot);
     };
-    if (s->prec == 64) go(double(), double());
-    else if (hi) go(float(), double());
-    else go(float(), float());
+    if (s->prec == 64) {
+        go(double(), double());
+    } else if (hi && !part && s->dfx) {
+        // FP32 operator, true residual / Newton check: double-float arithmetic
+        const int n3 = 3 * c->g.nodec;
+        k_split_df<<<(n3 + 255) / 256, 256, 0, c->stream>>>(x, s->dfx, s->dfx + n3, n3);
+        const float *A = (const float *)s->A;
+        if (o[0] == 1 && o[1] == 1 && o[2] == 1)
+            k_imp_matvec_df<1, 1, 1><<<nb, 256, 0, c->stream>>>(a, A, s->dfx, s->dfx + n3, y);
+        else if (o[1] == 2)
+            k_imp_matvec_df<2, 2, 2><<<nb, 256, 0, c->stream>>>(a, A, s->dfx, s->dfx + n3, y);
+        else
+            k_imp_matvec_df<2, 1, 2><<<nb, 256, 0, c->stream>>>(a, A, s->dfx, s->dfx + n3, y);
+    } else if (hi) {
+        go(float(), double());
+    } else {
+        go(float(), float());
+    }
 }
 
 // y = A x with FP32 vectors and FP32 arithmetic (FP32 operator only): the
