@@ -171,6 +171,7 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
     };
     alloc((void **)&c->d_iprop, sizeof(int) * c->nmat);
     alloc((void **)&c->d_matprop, sizeof(double) * 3 * c->nmat);
+    alloc((void **)&c->d_matpropf, sizeof(float) * 3 * c->nmat);
     alloc((void **)&c->d_acc, sizeof(unsigned long long) * NACC * N);
     alloc((void **)&c->d_acc2, sizeof(unsigned long long) * 3 * N);
     if (c->fbar) alloc((void **)&c->d_facc, sizeof(unsigned long long) * N);
@@ -205,6 +206,11 @@ mpm_status mpm_gpu_create(const mpm_grid_desc *grid, const mpm_material_desc *ma
                      g.order[0] == 1 && g.order[1] == 1 && g.order[2] == 1;
     }
     cudaMemcpy(c->d_matprop, mat->mat_prop, sizeof(double) * 3 * c->nmat, cudaMemcpyHostToDevice);
+    {   // the FP32 kernels read the table without FP64 loads and conversions per particle
+        std::vector<float> mf(3 * (size_t)c->nmat);
+        for (size_t k = 0; k < mf.size(); k++) mf[k] = (float)mat->mat_prop[k];
+        cudaMemcpy(c->d_matpropf, mf.data(), sizeof(float) * mf.size(), cudaMemcpyHostToDevice);
+    }
     cudaMemset(c->d_acc, 0, sizeof(unsigned long long) * NACC * N);
     cudaMemset(c->d_acc2, 0, sizeof(unsigned long long) * 3 * N);
     if (c->d_facc) cudaMemset(c->d_facc, 0, sizeof(unsigned long long) * N);
@@ -245,6 +251,7 @@ void mpm_gpu_destroy(mpm_ctx *c) {
     free_particles(c);
     free_dev(c->d_iprop);
     free_dev(c->d_matprop);
+    free_dev(c->d_matpropf);
     free_dev(c->d_acc);
     free_dev(c->d_acc2);
     free_dev(c->d_facc);

@@ -62,6 +62,7 @@ struct StepArgs {
     DevCtl *ctl;
     const int *iprop;
     const double *matprop;
+    const float *matpropf;      // the same table in FP32 (the FP32 particle kernels)
     R dt, facl, mtol, grav[3];
     int parity;
     int scheme;
@@ -2763,7 +2764,12 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
         for (int k = 0; k < 6; k++) s[k] = ld(P.s[k] + p);
         const int mid = P.matid[p];
         const int model = a.iprop[mid];
-        const R E = (R)a.matprop[3 * mid], nu = (R)a.matprop[3 * mid + 1];
+        // FP32 reads the FP32 copy of the table (no FP64 loads and conversions per particle)
+        auto mprop = [&](int k) -> R {
+            if constexpr (sizeof(R) == 4) return a.matpropf[3 * mid + k];
+            else return (R)a.matprop[3 * mid + k];
+        };
+        const R E = mprop(0), nu = mprop(1);
         if (model == 0) {
             lin_elast_update(s, Dm, E, nu);
         } else if (model == 1) {
@@ -2778,13 +2784,13 @@ __global__ void __launch_bounds__(256) k_g2p_update(StepArgs<R> a) {
             if constexpr (sizeof(R) == 8) stvk_stress(s, Fs, J, E, nu);
             else stvk_stress_h(s, Fs, det_ipm1(Fn), E, nu);
         } else if (model == 3) {   // mat_prop = {c1, c2, bulk}
-            if constexpr (sizeof(R) == 8) mooney_rivlin_stress(s, Fs, J, E, nu, (R)a.matprop[3 * mid + 2]);
-            else mooney_rivlin_stress_h(s, Fs, det_ipm1(Fn), E, nu, (R)a.matprop[3 * mid + 2]);
+            if constexpr (sizeof(R) == 8) mooney_rivlin_stress(s, Fs, J, E, nu, mprop(2));
+            else mooney_rivlin_stress_h(s, Fs, det_ipm1(Fn), E, nu, mprop(2));
         } else if (model == 4) {
             R jm1;
             if constexpr (sizeof(R) == 8) jm1 = J - (R)1;
             else jm1 = det_ipm1(Fn);
-            tait_stress<R>(s, Dm, jm1, ld(P.m + p) * recip<R>(ld(P.vol0 + p)), E, nu, (R)a.matprop[3 * mid + 2],
+            tait_stress<R>(s, Dm, jm1, ld(P.m + p) * recip<R>(ld(P.vol0 + p)), E, nu, mprop(2),
                            recip<R>(a.dt));
         } else if (model == -1) {
 #pragma unroll
@@ -2934,14 +2940,14 @@ __device__ __forceinline__ void update_particle(const StepArgs<float> &a, const 
 #pragma unroll
     for (int k = 0; k < 6; k++) s[k] = s_in[k];
     const int model = a.iprop[mid];
-    const float E = (float)a.matprop[3 * mid], nu = (float)a.matprop[3 * mid + 1];
+    const float E = a.matpropf[3 * mid], nu = a.matpropf[3 * mid + 1];
     if constexpr (FLUIDJ) {
         // Tait fluid: only J is tracked, J_new - 1 = (1 + (J - 1)) det(I + D) - 1
         const float dj = det_ipm1(D);
         const float jm1 = H[0][0] + dj + H[0][0] * dj;
         const float J = 1.0f + jm1;
         const float volp = J * vol0;
-        tait_stress<float>(s, D, jm1, P.m[p] * rcp_approx(vol0), E, nu, (float)a.matprop[3 * mid + 2],
+        tait_stress<float>(s, D, jm1, P.m[p] * rcp_approx(vol0), E, nu, a.matpropf[3 * mid + 2],
                            rcp_approx(a.dt));
         const bool fin = isfinite(xn[0]) && isfinite(xn[1]) && isfinite(xn[2]) && isfinite(J) && isfinite(s[0]) &&
                          isfinite(s[1]) && isfinite(s[2]) && isfinite(s[3]) && isfinite(s[4]) && isfinite(s[5]);
@@ -2977,9 +2983,9 @@ __device__ __forceinline__ void update_particle(const StepArgs<float> &a, const 
     if (model == 0) lin_elast_update(s, D, E, nu);
     else if (model == 1) neo_hookean_stress_h(s, Hn, jm1, E, nu);
     else if (model == 2) stvk_stress_h(s, Hn, jm1, E, nu);
-    else if (model == 3) mooney_rivlin_stress_h(s, Hn, jm1, E, nu, (float)a.matprop[3 * mid + 2]);
+    else if (model == 3) mooney_rivlin_stress_h(s, Hn, jm1, E, nu, a.matpropf[3 * mid + 2]);
     else if (model == 4)
-        tait_stress<float>(s, D, jm1, P.m[p] * rcp_approx(vol0), E, nu, (float)a.matprop[3 * mid + 2],
+        tait_stress<float>(s, D, jm1, P.m[p] * rcp_approx(vol0), E, nu, a.matpropf[3 * mid + 2],
                            rcp_approx(a.dt));
     else if (model == -1)
 #pragma unroll
@@ -3233,6 +3239,7 @@ static StepArgs<R> make_args(mpm_ctx *c) {
     a.ctl = c->d_ctl;
     a.iprop = c->d_iprop;
     a.matprop = c->d_matprop;
+    a.matpropf = c->d_matpropf;
     a.dt = (R)c->dt;
     a.facl = (R)c->facl;
     a.mtol = (R)c->mtol;

@@ -163,6 +163,7 @@ struct mpm_ctx {
     // materials on device
     int *d_iprop = nullptr;
     double *d_matprop = nullptr;
+    float *d_matpropf = nullptr;   // FP32 copy of the material table for the FP32 particle kernels
     // particles
     int64_t num = 0;
     size_t rsize = 4;
