@@ -354,9 +354,6 @@ __device__ __forceinline__ bool box_node_cells(const KGeom<float> &g, int n, int
     return true;
 }
 
-// The end of a cell-P2G CTA: corners to shared memory, counters, and the
-// node pass: each node of the (BRX+1)(BRY+1)(BRZ+1) box adds the corners of
-// its adjacent cells in a fixed order and issues one int64 RED per field.
 // The counters of the cell-P2G kernels: particles that left their sorted cell
 // and particles outside the grid.
 __device__ __forceinline__ void p2g_counters(const StepArgs<float> &a, int *sh_red, int misses, int oobs) {
@@ -367,21 +364,12 @@ __device__ __forceinline__ void p2g_counters(const StepArgs<float> &a, int *sh_r
     }
 }
 
-// COUNT: reduce the counters here (false: the caller reduces them once, at
-// the end of a persistent CTA)
-template <bool COUNT = true>
-__device__ __forceinline__ void p2g_node_pass(const StepArgs<float> &a, const Scales &S, float (*corner)[BRC],
-                                              int *sh_red, int lc, int h, int ox, int oy, int oz,
-                                              const float (*acc)[4], int misses, int oobs) {
-#pragma unroll
-    for (int f = 0; f < NACC; f++)
-#pragma unroll
-        for (int c = 0; c < 4; c++) corner[f * 8 + c + 4 * h][lc] = acc[f][c];
-    if (COUNT) p2g_counters(a, sh_red, misses, oobs);
-    __syncthreads();
-    // one thread per node of the box, all fields: the node's adjacent cells
-    // are found once and each field's corners are added in the fixed order
-    // (k, j, i) = (0, 0, 0) .. (1, 1, 1)
+// The node pass over the brick's corner sums in shared memory (corner
+// f * 8 + c of cell lc in corner[f * 8 + c][lc]): one thread per node of the
+// box, all fields; the node's adjacent cells are found once and each field's
+// corners are added in the fixed order (k, j, i) = (0, 0, 0) .. (1, 1, 1).
+__device__ __forceinline__ void p2g_box_nodes(const StepArgs<float> &a, const Scales &S, const float (*corner)[BRC],
+                                              int ox, int oy, int oz) {
     for (int n = threadIdx.x; n < BOX_NODES; n += CELL_THREADS) {
         int gx, gy, gz, off[8];
         if (!box_node_cells(a.g, n, ox, oy, oz, gx, gy, gz, off)) continue;
@@ -401,6 +389,22 @@ __device__ __forceinline__ void p2g_node_pass(const StepArgs<float> &a, const Sc
             }
         }
     }
+}
+
+// The end of a cell-P2G brick: this thread's corners of z-layer h to shared
+// memory, then the node pass.  COUNT: reduce the counters here (false: the
+// caller reduces them once, at the end of a persistent CTA).
+template <bool COUNT = true>
+__device__ __forceinline__ void p2g_node_pass(const StepArgs<float> &a, const Scales &S, float (*corner)[BRC],
+                                              int *sh_red, int lc, int h, int ox, int oy, int oz,
+                                              const float (*acc)[4], int misses, int oobs) {
+#pragma unroll
+    for (int f = 0; f < NACC; f++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) corner[f * 8 + c + 4 * h][lc] = acc[f][c];
+    if (COUNT) p2g_counters(a, sh_red, misses, oobs);
+    __syncthreads();
+    p2g_box_nodes(a, S, corner, ox, oy, oz);
 }
 
 template <int MINB, bool AFF = false>
@@ -463,6 +467,33 @@ __device__ __forceinline__ void moments_to_layer(const float *M, int h, float *o
     out[1] = lo + dlo;   // (1, 0)
     out[2] = hi - dhi;   // (0, 1)
     out[3] = hi + dhi;   // (1, 1)
+}
+
+// The internal force sum_b dN/dx_b (vol sigma_ab) at the four corners
+// (i, j, h) of z-layer h, from the stress moments Fm[3 a + b] of vol sigma_ab
+// against the bilinear monomials of the two axes other than b: the derivative
+// along b carries the sign of b's axis, the bilinear part the other two.
+// With the layer's sign sz folded in first, every component is
+// K0 + sx K1 + sy K2 + sx sy K3; T[a][i + 2 j].
+__device__ __forceinline__ void stress_to_layer(const float (*Fm)[4], int h, const KGeom<float> &g, float (*T)[4]) {
+    const float sz = h ? 1.0f : -1.0f;
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+        const float *Fx = Fm[3 * ax], *Fy = Fm[3 * ax + 1], *Fz = Fm[3 * ax + 2];
+        const float ix = g.inv_dx[0], iy = g.inv_dx[1], iz = g.inv_dx[2] * sz;
+        // d/dx: sx (Fx0/4 + sz Fx2/2 + sy (Fx1/2 + sz Fx3)); Fx's bilinear axes are (y, z)
+        const float ax0 = ix * (Fx[0] * 0.25f + sz * Fx[2] * 0.5f), bx0 = ix * (Fx[1] * 0.5f + sz * Fx[3]);
+        // d/dy: sy (Fy0/4 + sz Fy2/2 + sx (Fy1/2 + sz Fy3)); Fy's bilinear axes are (x, z)
+        const float ay1 = iy * (Fy[0] * 0.25f + sz * Fy[2] * 0.5f), by1 = iy * (Fy[1] * 0.5f + sz * Fy[3]);
+        // d/dz: sz (Fz0/4 + sx Fz1/2 + sy Fz2/2 + sx sy Fz3); Fz's bilinear axes are (x, y)
+        const float K0 = iz * Fz[0] * 0.25f, K1 = ax0 + iz * Fz[1] * 0.5f, K2 = ay1 + iz * Fz[2] * 0.5f,
+                    K3 = bx0 + by1 + iz * Fz[3];
+        const float lo = K0 - K2, hi = K0 + K2, dlo = K1 - K3, dhi = K1 + K3;
+        T[ax][0] = lo - dlo;
+        T[ax][1] = lo + dlo;
+        T[ax][2] = hi - dhi;
+        T[ax][3] = hi + dhi;
+    }
 }
 
 __device__ __forceinline__ float cell_offset_u(float x, const KGeom<float> &g, int d, int c) {
@@ -579,31 +610,16 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_p2g_cell_mom(StepArgs<fl
         for (int f = 0; f < 9; f++)
 #pragma unroll
             for (int k = 0; k < 4; k++) Fm[f][k] += __shfl_xor_sync(pair, Fm[f][k], 1);
-        // corners (i, j, h) of this thread's z-layer: with the layer's sign
-        // sz folded in first, every field is K0 + sx K1 + sy K2 + sx sy K3
-        float acc[NACC][4];
-        const float sz = h ? 1.0f : -1.0f;
+        // corners (i, j, h) of this thread's z-layer
+        float acc[NACC][4], T[3][4];
         const float gv[3] = {fxg, fyg, fzg};
 #pragma unroll
         for (int f = 0; f < 5; f++) moments_to_layer(M[f], h, acc[f]);
+        stress_to_layer(Fm, h, a.g, T);
 #pragma unroll
-        for (int ax = 0; ax < 3; ax++) {
-            // internal force -sum_b dN/dx_b (vol sigma_ab): the derivative along
-            // b carries the sign of b's axis, the bilinear part the other two
-            const float *Fx = Fm[3 * ax], *Fy = Fm[3 * ax + 1], *Fz = Fm[3 * ax + 2];
-            const float ix = a.g.inv_dx[0], iy = a.g.inv_dx[1], iz = a.g.inv_dx[2] * sz;
-            // d/dx: sx (Fx0/4 + sz Fx2/2 + sy (Fx1/2 + sz Fx3)); Fx's bilinear axes are (y, z)
-            const float ax0 = ix * (Fx[0] * 0.25f + sz * Fx[2] * 0.5f), bx0 = ix * (Fx[1] * 0.5f + sz * Fx[3]);
-            // d/dy: sy (Fy0/4 + sz Fy2/2 + sx (Fy1/2 + sz Fy3)); Fy's bilinear axes are (x, z)
-            const float ay1 = iy * (Fy[0] * 0.25f + sz * Fy[2] * 0.5f), by1 = iy * (Fy[1] * 0.5f + sz * Fy[3]);
-            // d/dz: sz (Fz0/4 + sx Fz1/2 + sy Fz2/2 + sx sy Fz3); Fz's bilinear axes are (x, y)
-            const float K0 = iz * Fz[0] * 0.25f, K1 = ax0 + iz * Fz[1] * 0.5f, K2 = ay1 + iz * Fz[2] * 0.5f,
-                        K3 = bx0 + by1 + iz * Fz[3];
-            const float lo = K0 - K2, hi = K0 + K2, dlo = K1 - K3, dhi = K1 + K3;
-            const float T[4] = {lo - dlo, lo + dlo, hi - dhi, hi + dhi};
+        for (int ax = 0; ax < 3; ax++)
 #pragma unroll
-            for (int c = 0; c < 4; c++) acc[5 + ax][c] = fmaf(acc[0][c], gv[ax], -T[c]);
-        }
+            for (int c = 0; c < 4; c++) acc[5 + ax][c] = fmaf(acc[0][c], gv[ax], -T[ax][c]);
         p2g_node_pass<false>(a, S, corner, sh_red, lc, h, ox, oy, oz, acc, misses, oobs);
         __syncthreads();   // shared memory is reused by the next brick
     }
@@ -986,17 +1002,12 @@ __device__ __forceinline__ void musl_counters(const StepArgs<float> &a, long lon
     }
 }
 
-template <bool COUNT = true>
-__device__ __forceinline__ void musl_node_pass(const StepArgs<float> &a, const Scales &S, float (*corner)[BRC],
-                                               long long *sh_l, float *sh_f, int lc, int h, int ox, int oy, int oz,
-                                               const float (*acc)[4], long long gacc, float vmax) {
+// The re-projection's node pass over the brick's corner sums of m v in
+// shared memory (component d, corner c of cell lc in corner[d * 8 + c][lc]),
+// in the fixed corner order of p2g_box_nodes.
+__device__ __forceinline__ void musl_box_nodes(const StepArgs<float> &a, const Scales &S, const float (*corner)[BRC],
+                                               int ox, int oy, int oz) {
     const size_t N = (size_t)a.g.nodec;
-#pragma unroll
-    for (int d = 0; d < 3; d++)
-#pragma unroll
-        for (int c = 0; c < 4; c++) corner[d * 8 + c + 4 * h][lc] = acc[d][c];
-    if (COUNT) musl_counters(a, sh_l, sh_f, gacc, vmax);
-    __syncthreads();
     for (int n = threadIdx.x; n < BOX_NODES; n += CELL_THREADS) {
         int gx, gy, gz, off[8];
         if (!box_node_cells(a.g, n, ox, oy, oz, gx, gy, gz, off)) continue;
@@ -1010,6 +1021,21 @@ __device__ __forceinline__ void musl_node_pass(const StepArgs<float> &a, const S
             if (sum != 0.0f) atomic_add_i64(&a.acc2[d * N + gn], fx(sum, S.q));
         }
     }
+}
+
+// The end of a gather + MUSL brick: this thread's corners of z-layer h to
+// shared memory, then the node pass.  COUNT as in p2g_node_pass.
+template <bool COUNT = true>
+__device__ __forceinline__ void musl_node_pass(const StepArgs<float> &a, const Scales &S, float (*corner)[BRC],
+                                               long long *sh_l, float *sh_f, int lc, int h, int ox, int oy, int oz,
+                                               const float (*acc)[4], long long gacc, float vmax) {
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) corner[d * 8 + c + 4 * h][lc] = acc[d][c];
+    if (COUNT) musl_counters(a, sh_l, sh_f, gacc, vmax);
+    __syncthreads();
+    musl_box_nodes(a, S, corner, ox, oy, oz);
 }
 
 template <int MINB, bool LIST>

@@ -324,7 +324,7 @@ static mpm_status sort_impl(mpm_ctx *c) {
         k_scan_down<<<nseg, SCAN_T, 0, c->stream>>>(c->g.nbricks, nseg, c->d_tcount, c->d_tstart, c->d_tcursor,
                                                     c->d_work, c->d_nwork, c->nwork_cap, c->d_blist, c->d_nblist,
                                                     c->d_scanpart);
-        c->launches += 2;
+        c->launches += 3;
     }
     timer_end(c, K_SCAN);
     timer_begin(c, K_SCATTER);
