@@ -506,17 +506,6 @@ __device__ __forceinline__ bool in_cell(float u, float v, float w) {
     return u >= -0.5f && u < 0.5f && v >= -0.5f && v < 0.5f && w >= -0.5f && w < 0.5f;
 }
 
-// both z-layers of a particle that left its sorted cell, by fixed-point atomics
-template <bool AFF = false>
-__device__ __noinline__ void p2g_miss(const StepArgs<float> &a, const Scales &S, int cx, int cy, int cz, float x0,
-                                      float x1, float x2, float m, float vol, const float *vel, const float *sg,
-                                      float fxg, float fyg, float fzg, int &misses, int &oobs,
-                                      const float *A = nullptr) {
-    float dummy[NACC][4];
-    p2g_particle<AFF>(a, S, cx, cy, cz, 0, x0, x1, x2, m, vol, vel, sg, fxg, fyg, fzg, dummy, misses, oobs, -1, A);
-    p2g_particle<AFF>(a, S, cx, cy, cz, 1, x0, x1, x2, m, vol, vel, sg, fxg, fyg, fzg, dummy, misses, oobs, -1, A);
-}
-
 // the inputs of one particle of the moment-form P2G
 struct P2gIn {
     float x[3], m, vol, v[3], s[6];
@@ -1522,8 +1511,9 @@ __global__ void __launch_bounds__(CELL_THREADS, MINB) k_g2p_musl_cell_staged(Ste
 }
 
 // Deferred passes for the particles that left their sorted cell since the
-// last re-sort: one thread per queued particle, fixed-point atomics (order
-// independent, so the results do not depend on the queue order).
+// last re-sort: fixed-point atomics (order independent, so the results do
+// not depend on the queue order); the P2G with eight threads per queued
+// particle, the gather + MUSL with one.
 template <bool AFF = false>
 __global__ void __launch_bounds__(256) k_p2g_misses(StepArgs<float> a) {
     pdl_wait();
@@ -1533,19 +1523,47 @@ __global__ void __launch_bounds__(256) k_p2g_misses(StepArgs<float> a) {
     const unsigned n = a.ctl->n_miss_p2g;
     const float fxg = a.grav[0] * a.facl, fyg = a.grav[1] * a.facl, fzg = a.grav[2] * a.facl;
     const Particles<float> &P = a.P;
-    int misses = 0, oobs = 0;
-    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int p = a.miss[i];
+    int oobs = 0;
+    // eight threads per deferred particle, one per corner (i, j, h): the
+    // corner's terms are those of p2g_particle's scatter path, and the int64
+    // sums make the result independent of which thread adds them
+    for (size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x; g < 8 * (size_t)n;
+         g += (size_t)gridDim.x * blockDim.x) {
+        const int p = a.miss[g >> 3];
+        const int ci = g & 1, cj = (g >> 1) & 1, h = (g >> 2) & 1;
+        const float x0 = ld(P.x[0] + p), x1 = ld(P.x[1] + p), x2 = ld(P.x[2] + p), m = ld(P.m + p),
+                    vol = ld(P.vol + p);
         const float vel[3] = {ld(P.v[0] + p), ld(P.v[1] + p), ld(P.v[2] + p)};
         const float sg[6] = {ld(P.s[0] + p), ld(P.s[1] + p), ld(P.s[2] + p),
                              ld(P.s[3] + p), ld(P.s[4] + p), ld(P.s[5] + p)};
-        float A[AFF ? 9 : 1];
+        bool oob = false;
+        const int px = cell_of(x0, a.g, 0, oob), py = cell_of(x1, a.g, 1, oob), pz = cell_of(x2, a.g, 2, oob);
+        oobs += oob && (g & 7) == 0;
+        Axis<float, 1> ax, ay, az;
+        axis_eval<float, 1>(x0, a.g, 0, px, ax);
+        axis_eval<float, 1>(x1, a.g, 1, py, ay);
+        axis_eval<float, 1>(x2, a.g, 2, pz, az);
+        const float mfx = m * fxg, mfy = m * fyg, mfz = m * fzg;
+        const float wz = h ? az.w[1] : az.w[0], dwz = h ? az.dw[1] : az.dw[0];
+        const float wxy = ax.w[ci] * ay.w[cj];
+        float vn[3] = {vel[0], vel[1], vel[2]};
         if constexpr (AFF) {
+            float A[9];
 #pragma unroll
             for (int e = 0; e < 9; e++) A[e] = ld(P.C[e] + p);
+            affine_velocity(vel, A, cp_coord<float, 1>(a.g, 0, px + ci) - x0, cp_coord<float, 1>(a.g, 1, py + cj) - x1,
+                            cp_coord<float, 1>(a.g, 2, pz + h) - x2, vn);
         }
-        p2g_miss<AFF>(a, S, -1, -1, -1, ld(P.x[0] + p), ld(P.x[1] + p), ld(P.x[2] + p), ld(P.m + p), ld(P.vol + p),
-                      vel, sg, fxg, fyg, fzg, misses, oobs, A);
+        float q[NACC];
+        p2g_terms(wxy * wz, ax.dw[ci] * ay.w[cj] * wz, ax.w[ci] * ay.dw[cj] * wz, wxy * dwz, m, vol, vn, sg, mfx, mfy,
+                  mfz, q);
+        long long o[NACC];
+        fx_terms(q, S, o);
+        const size_t gn = node_id(a.g, px + ci, py + cj, pz + h);
+#pragma unroll
+        for (int f = 0; f < NACC; f++)
+            if (o[f]) atomic_add_i64(&a.acc[(size_t)f * a.g.nodec + gn], o[f]);
+        a.tileflag[tile_of_node(a.g, px + ci, py + cj, pz + h)] = 1;
     }
     // the particles outside the grid (every one of them is deferred by the
     // moment-form P2G)
