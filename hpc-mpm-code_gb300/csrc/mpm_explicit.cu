@@ -644,7 +644,6 @@ __global__ void __launch_bounds__(BCH) k_p2g_brick(StepArgs<float> a) {
     const Particles<float> &P = a.P;
     // this thread's cell (phase 2)
     const int lc = tid;
-    const int cx = ox + (lc % BRX), cy = oy + (lc / BRX) % BRY, cz = oz + lc / (BRX * BRY);
     const int p0 = scs[lc], p1 = scs[lc + 1];
     float M[NMOM];
 #pragma unroll

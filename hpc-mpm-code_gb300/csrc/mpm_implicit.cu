@@ -1929,7 +1929,6 @@ static mpm_status imp_fcg(mpm_ctx *c, double eps, int kmax, int *iters) {
     // symmetry of the (learned, non-symmetric) preconditioner.  It runs while
     // every window of `check` iterations at least halves the residual norm.
     if (use_nn && s->gcr) {
-        const size_t st3 = 3 * N;
         int used = 0, slot = 0;
         double rr_win = rr0;
         bool fine = false;   // close to the tolerance: one iteration at a time, checked after each
